@@ -1,0 +1,256 @@
+#!/usr/bin/env python3
+"""Benchmark of the explicit central-difference hot path (DOF-steps/s).
+
+A "step" is one time step of the whole model: element forces, the ordered
+node gather, the diagonal solve and the state update.  The default workload
+is the 3D configuration (lin3DHexa8 128 x 128 x 64, h = 2 m, log-normal Vs
+field, double-couple body force) in the FP64 plain form; the PML layers of
+that configuration are not built yet and the box has fixed/roller faces
+instead (stated in the JSON config).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload config2|config1]
+
+value   : free DOF x steps / device time of the K steps (CUDA events on the
+          library's stream, inputs resident in HBM, working set > L2).
+e2e     : the same metric through the C ABI with host buffers: model arrays
+          copied in by svl_cd_create and the full displacement field copied
+          back to a host buffer after every step (svl_cd_run with history).
+roofline: algorithmic bytes of one step (37 B per free DOF for H8, 40 for
+          Q4) over the measured step time, against MEASURED_PEAKS.json.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+ALGO_BYTES_PER_DOF = {2: 40.0, 3: 37.0}
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle sampling during the timed region."""
+
+    def __init__(self, gpu_index=0):
+        self.proc = None
+        self.path = None
+        self.gpu = gpu_index
+
+    def __enter__(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu),
+                 "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.path or not os.path.exists(self.path):
+            return None
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for n, v in zip(names, r[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+def build_workload(name):
+    from svl_gb300 import workloads
+    if name == "config1":
+        m, L, dt = workloads.config1()
+        desc = "lin2DQuad4 200x100 plane-strain box, CD, FP64 plain"
+    elif name == "config2":
+        m, L, dt = workloads.config2()
+        desc = "lin3DHexa8 128x128x64 box (h=2 m, log-normal Vs), CD, FP64 plain; PML layers not built (fixed bottom, roller sides)"
+    else:
+        raise SystemExit("unknown workload %s" % name)
+    return m, L, dt, desc
+
+
+def cpu_baseline(m, L, dt, steps_cap, budget_s=20.0):
+    """Oracle (CPU port of the reference path), fast mode, all host threads."""
+    from oracle import oracle as O
+    nthreads = O.num_threads()
+    t = {}
+    n = max(1, steps_cap)
+    O.cd_run(m, L, dt, 1, mode=1, history=False, timing=t)   # warm-up / sizing step
+    per = max(t["seconds"], 1e-6)
+    n = int(max(1, min(steps_cap, budget_s / per)))
+    O.cd_run(m, L, dt, n, mode=1, history=False, timing=t)
+    val = m.nfree * n / t["seconds"]
+    return {"value": val, "unit": "DOF-steps/s", "cores": nthreads, "kind": "port",
+            "sample": "%d time steps of the same model on the CPU oracle (OpenMP element loop, ordered scatter)" % n}
+
+
+def dist_info():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=400)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="config2", choices=["config1", "config2"])
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    ws, rank, local = dist_info()
+    warm = max(3, args.warmup)
+
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        m, L, dt, desc = build_workload(args.workload)
+        cb = cpu_baseline(m, L, dt, steps_cap=min(args.steps, 20))
+        line = {"metric": "DOF-steps/s", "value": cb["value"], "unit": "DOF-steps/s", "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": warm, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)", "impl": "reference",
+                "config": {"workload": desc, "free_dof": m.nfree, "elements": m.nelem},
+                "cpu_baseline": cb,
+                "e2e": {"value": cb["value"], "unit": "DOF-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return 0
+
+    import ctypes as C
+    from svl_gb300 import CentralDifference
+    from svl_gb300 import _capi as capi
+
+    pg = None
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", init_method="env://")
+        pg = dist
+    capi.check(capi.lib().svl_set_device(local))
+
+    m, L, dt, desc = build_workload(args.workload)
+    nd = m.ndim
+    cd = CentralDifference(m, L, dt)
+    cd.Initialize()
+    cd.run(1, warm)                      # warm-up (graph capture happens here)
+    # per-kernel device times for the roofline (individual launches + events)
+    prof = cd.profile(1 + warm, 20)
+    cd.Initialize()
+    if pg:
+        pg.barrier()
+    with ClockSampler(local) as clk:
+        ms = cd.run_timed(1, args.steps)
+    if pg:
+        import torch
+        t = torch.tensor([ms], device="cuda")
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        ms = float(t.item())
+        pg.barrier()
+    launches = cd.launches()
+    clocks = clk.summary()
+    ms_step = ms / args.steps
+    value = ws * m.nfree * args.steps / (ms / 1e3)
+    U = cd.GetDisplacements()
+    finite = bool(np.isfinite(U).all())
+    cd.close()
+
+    peak, peak_kind = measured_peaks()
+    step_ms_prof = float(prof.sum() / 20.0)
+    algo_bytes = ALGO_BYTES_PER_DOF[nd] * m.nfree
+    achieved = algo_bytes / (ms_step / 1e3) / 1e9
+    kernel_names = ["k_element", "k_node", "k_residual", "k_free", "k_update"]
+    shares = {kernel_names[i]: round(float(prof[i] / max(prof.sum(), 1e-12)), 4) for i in range(5) if prof[i] > 0}
+
+    e2e = None
+    if not args.no_e2e:
+        ne2e = min(args.steps, 100)
+        hist = np.empty((ne2e, m.ntotal))
+        t0 = time.perf_counter()
+        cd2 = CentralDifference(m, L, dt)        # host arrays -> device
+        cd2.Initialize()
+        cd2.run(1, ne2e, history=True)          # full U to the host every step
+        cd2.close()
+        t1 = time.perf_counter()
+        md_bytes = (m.coords.nbytes + m.totaldof.nbytes + m.freedof.nbytes + m.conn.nbytes +
+                    m.elem_mat.nbytes + m.mat_param.nbytes + m.mat_type.nbytes)
+        e2e = {"value": ws * m.nfree * ne2e / (t1 - t0), "unit": "DOF-steps/s",
+               "h2d_bytes_per_step": int(md_bytes / ne2e), "d2h_bytes_per_step": int(m.ntotal * 8),
+               "steps": ne2e, "includes": "svl_cd_create from host arrays + run with full-field history to host"}
+        del hist
+
+    cb = None
+    if rank == 0 and not args.no_cpu:
+        cb = cpu_baseline(m, L, dt, steps_cap=10)
+
+    if rank == 0:
+        line = {
+            "metric": "DOF-steps/s", "value": value, "unit": "DOF-steps/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": warm, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+            "config": {"workload": desc, "free_dof": m.nfree, "elements": m.nelem, "dt": dt,
+                       "precision": "fp64 plain", "parallelism": "replicas" if ws > 1 else "single GPU",
+                       "l2": "no flush; working set > L2 (element force block %d MB + state %d MB)" % (
+                           m.nelem * (24 if nd == 3 else 8) * 8 // 2 ** 20, m.ntotal * 7 * 8 // 2 ** 20)},
+            "roofline": {"bound": "hbm", "kernel": "one CD step (k_element + k_node)", "achieved": achieved,
+                         "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
+                         "traffic": None, "algorithmic_bytes_per_step": algo_bytes,
+                         "kernel_share": shares, "profiled_step_ms": step_ms_prof},
+            "cpu_baseline": cb, "e2e": e2e, "gpu_launches": int(launches), "clocks": clocks,
+            "finite": finite,
+        }
+        print(json.dumps(line))
+    if pg:
+        pg.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

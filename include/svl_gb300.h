@@ -1,0 +1,224 @@
+/*
+ * svl_gb300.h -- C ABI of the GB300-native SeismoVLAB time-stepping hot path.
+ *
+ * Everything here is plain C: pointers, sizes and status codes, no C++ or torch
+ * types.  One opaque handle per integrator; each handle owns its device
+ * buffers and one CUDA stream and is not thread-safe (independent handles may
+ * be driven from different host threads).  Host arrays passed to *_create are
+ * copied; the caller keeps ownership.
+ *
+ * Error convention.  Every entry point returns an int status: SVL_OK (0) on
+ * success, a positive SVL_ERR_* code otherwise, with a message available from
+ * svl_last_error().  The reference returns `bool stop` (true = failure) from
+ * LinearSystem::SolveSystem (RP/11-Solvers/01-Direct/EigenSolver.cpp:52-58),
+ * Integrator::ComputeNewStep (RP/10-Integrators/02-CentralDifference/
+ * CentralDifference.cpp:132-135) and Analysis::Analyze
+ * (RP/08-Analysis/02-Dynamic/DynamicAnalysis.cpp:41-44); the C++ adapters in
+ * svl_gb300/host map status != 0 to stop == true.
+ *
+ * Paths in citations are relative to the SeismoVLAB/SVL tree: RP/ is
+ * 02-Run_Process/, PP/ is 01-Pre_Process/.
+ */
+#ifndef SVL_GB300_H
+#define SVL_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define SVL_OK               0
+#define SVL_ERR_INVALID      1  /* bad argument / inconsistent model           */
+#define SVL_ERR_CUDA         2  /* CUDA runtime error                          */
+#define SVL_ERR_NONFINITE    3  /* NaN/Inf detected in the state               */
+#define SVL_ERR_MAXITER      4  /* iterative solve hit its iteration cap       */
+#define SVL_ERR_BREAKDOWN    5  /* PCG breakdown (p.Ap <= 0)                   */
+#define SVL_ERR_UNSUPPORTED  6  /* valid model the GPU path does not cover     */
+#define SVL_ERR_NOMEM        7  /* device allocation failed                    */
+#define SVL_ERR_NODEVICE     8  /* no CUDA device / extension not usable       */
+
+/* ---- element and material kinds --------------------------------------- */
+/* Element classes (RP/04-Elements/06-Quadrilateral/lin2DQuad4.cpp,
+ * RP/04-Elements/10-Hexahedron/lin3DHexa8.cpp). */
+#define SVL_ELEM_LIN2DQUAD4   1
+#define SVL_ELEM_LIN3DHEXA8   2
+
+/* Material classes and the layout of their 8-double parameter rows.
+ *   ELASTIC2DPLANESTRAIN (RP/02-Materials/01-Linear/Elastic2DPlaneStrain.cpp:5-27)
+ *   ELASTIC3DLINEAR      (RP/02-Materials/01-Linear/Elastic3DLinear.cpp:5-29)
+ *       param = {E, nu, rho, 0, 0, 0, 0, 0}
+ *   PLASTICPLANESTRAINJ2 (RP/02-Materials/02-NonLinear/PlasticPlaneStrainJ2.cpp:6-52)
+ *   PLASTIC3DJ2          (RP/02-Materials/02-NonLinear/Plastic3DJ2.cpp:6-52)
+ *       param = {K, G, rho, H, beta, SigmaY, 0, 0}                         */
+#define SVL_MAT_ELASTIC2DPLANESTRAIN  1
+#define SVL_MAT_ELASTIC3DLINEAR       2
+#define SVL_MAT_PLASTICPLANESTRAINJ2  3
+#define SVL_MAT_PLASTIC3DJ2           4
+#define SVL_MAT_NPARAM                8
+
+/* ---- pre-processed model ---------------------------------------------- */
+/* The content of one SVL partition file (PP/Core/SeismoVLAB.py:79-103, parsed
+ * by RP/12-Utilities/Driver.hpp:1981-2045), already converted to arrays.
+ * Nodes are listed in ascending node-tag order and elements in ascending
+ * element-tag order: that order is the reference's std::map iteration order
+ * and therefore its assembly (summation) order.                           */
+typedef struct svl_model_desc {
+    int32_t ndim;              /* 2 or 3                                       */
+    int32_t nnode;
+    int32_t ndof;              /* dofs per node (2 for Q4, 3 for H8)            */
+    const double*  coords;     /* [nnode][ndim]                                */
+    const int32_t* totaldof;   /* [nnode][ndof] total-dof numbers               */
+    const int32_t* freedof;    /* [nnode][ndof] >=0 free, -1 restrained, <-1 constrained */
+    int32_t ntotal;            /* number of total dofs                          */
+    int32_t nfree;             /* number of free dofs                           */
+    /* Constraints (RP/01-Node/Constraint.cpp; T rows built as in
+     * RP/06-Mesh/Mesh.cpp:328-383): slave total dof <- sum factor * master free dof. */
+    int32_t nconstraint;
+    const int32_t* con_slave;  /* [nconstraint] total dof of the slave          */
+    const int32_t* con_ptr;    /* [nconstraint+1] CSR into con_master/factor    */
+    const int32_t* con_master; /* free dofs of the masters                      */
+    const double*  con_factor; /* combination factors                           */
+    /* Elements: one class per model.                                          */
+    int32_t elem_type;         /* SVL_ELEM_*                                    */
+    int32_t nelem;
+    const int32_t* conn;       /* [nelem][nen] node positions (0-based into node arrays) */
+    const int32_t* elem_mat;   /* [nelem] index into the material table        */
+    const double*  elem_thickness; /* [nelem] (Q4 only) or NULL for 1.0         */
+    int32_t nmat;
+    const int32_t* mat_type;   /* [nmat] SVL_MAT_*                              */
+    const double*  mat_param;  /* [nmat][SVL_MAT_NPARAM]                        */
+    int32_t lumped;            /* 1: row-sum lumped mass (massform LUMPED)      */
+    const double*  node_mass;  /* [ntotal] extra nodal masses, or NULL          */
+} svl_model_desc;
+
+/* ---- loads -------------------------------------------------------------- */
+/* Time series are the reference's "TimeSeries" functions (Driver.hpp:1514-1527).
+ * A force entry adds coef * series[s][k] to total dof `force_dof` at step k
+ * (series[s][k] = 0 past the end; the reference indexes without a check,
+ * RP/05-Loads/Load.cpp:69-71).  Point loads (Assembler.cpp:334-350) become one
+ * entry per loaded dof with coef = combination factor * direction; element body
+ * loads (Assembler.cpp:439-459) become one entry per element dof with coef =
+ * factor * (rho * integral of H^T dir), see svl_element_body_force.
+ * Support motions (Assembler.cpp:493-532, Node.cpp:228-247): dof `sm_dof`
+ * follows factor * series[s][k] (series[s][0] past the end).                */
+typedef struct svl_load_desc {
+    int32_t nseries;
+    const int32_t* series_ptr;  /* [nseries+1] offsets into series_val          */
+    const double*  series_val;
+    int32_t nforce;
+    const int32_t* force_dof;
+    const int32_t* force_series;
+    const double*  force_coef;
+    int32_t nsupport;
+    const int32_t* sm_dof;
+    const int32_t* sm_series;
+    const double*  sm_factor;
+} svl_load_desc;
+
+/* ---- library info ------------------------------------------------------- */
+const char* svl_version(void);
+const char* svl_last_error(void);
+int svl_device_info(int* device_count, int* sm_count, int* cc_major, int* cc_minor);
+/* Selects the CUDA device for handles created afterwards on this host thread
+ * (one process per GPU: pass the local rank).  No counterpart in the
+ * reference, whose ranks are MPI processes without a device. */
+int svl_set_device(int device);
+
+/* ---- structured mesh generator + PlainScheme numbering ------------------ */
+/* Mirrors PP/Method/Builder.py makeDomainArea (244-418) / makeDomainVolume
+ * (57-242): nodes numbered x-fastest, Q4 conn (i,j),(i+1,j),(i+1,j+1),(i,j+1),
+ * H8 conn as Builder.py:167-183, then PP/Core/Numberer.py PlainScheme
+ * (185-233) for total/free dof numbers.
+ * fix_mask[f] restrains dof bits on face f (0:xmin 1:xmax 2:ymin 3:ymax
+ * 4:zmin 5:zmax; bit d = dof d).  Faces are applied in that order.  With
+ * periodic_x != 0 every unrestrained dof of a node on xmax is tied by an
+ * EQUAL constraint (factor 1) to the node on xmin at the same y(,z); the
+ * constraints are numbered in ascending slave-node order, dof-minor.      */
+typedef struct svl_grid_spec {
+    int32_t ndim;
+    int32_t ne[3];
+    double  h[3];
+    double  origin[3];
+    int32_t fix_mask[6];
+    int32_t periodic_x;
+} svl_grid_spec;
+
+int svl_grid_sizes(const svl_grid_spec* spec, int32_t* nnode, int32_t* nelem,
+                   int32_t* ntotal, int32_t* nfree, int32_t* nconstraint);
+/* Output arrays sized from svl_grid_sizes (nen = 4 for 2D, 8 for 3D; each
+ * constraint has exactly one master, so con_master/con_factor have
+ * nconstraint entries and con_ptr nconstraint+1). */
+int svl_grid_build(const svl_grid_spec* spec, double* coords, int32_t* totaldof,
+                   int32_t* freedof, int32_t* conn, int32_t* con_slave,
+                   int32_t* con_ptr, int32_t* con_master, double* con_factor);
+
+/* Nodal load vector of a unit-amplitude element body load, rho * int(H^T q)
+ * over the element (lin2DQuad4.cpp:528-560 / lin3DHexa8 ComputeBodyForces).
+ * fe has nen*ndim entries. */
+int svl_element_body_force(const svl_model_desc* model, int32_t elem,
+                           const double* q, double* fe);
+
+/* Row-sum lumped mass on total dofs, assembled in element-tag order with the
+ * mass tolerance filter (Assembler.cpp:48-67, 623-697). */
+int svl_lumped_mass(const svl_model_desc* model, double mtol, double* mass_total);
+
+/* ---- explicit central difference (CentralDifference + Linear) ---------- */
+/* Replaces, for lumped mass without damping:
+ *   CentralDifference::Initialize / ComputeEffectiveForce /
+ *   ComputeEffectiveStiffness / ComputeSupportMotionVector / ComputeNewStep
+ *     (RP/10-Integrators/02-CentralDifference/CentralDifference.cpp:36-71,
+ *      124-151, 190-231),
+ *   Linear::ComputeNewIncrement (RP/09-Algorithms/01-Linear/Linear.cpp:22-56),
+ *   EigenSolver::SolveSystem on the diagonal K = M/dt^2 (EigenSolver.cpp:19-59),
+ *   Algorithm::UpdateStatesIncrements (RP/09-Algorithms/Algorithm.cpp:18-56),
+ *   Assembler::ComputeInternalForceVector / ComputeExternalForceVector /
+ *     ComputeSupportMotionIncrement (RP/07-Assembler/Assembler.cpp:240-269,
+ *     291-532),
+ *   and the element/material calls under them.                              */
+#define SVL_PREC_FP64   0   /* everything in FP64 (the plain form)             */
+#define SVL_PREC_MIXED  1   /* FP32/TF32 element forces, FP64 state update      */
+
+typedef struct svl_cd_opts {
+    double  dt;
+    double  ftol;        /* force assembly tolerance (JSON integrator ftol, 1e-12) */
+    double  mtol;        /* mass assembly tolerance  (JSON integrator mtol, 1e-12) */
+    int32_t precision;   /* SVL_PREC_*                                          */
+    int32_t check_every; /* NaN/Inf scan every n steps (0 = never)               */
+} svl_cd_opts;
+
+typedef struct svl_cd svl_cd;
+
+int  svl_cd_create(const svl_model_desc* model, const svl_load_desc* loads,
+                   const svl_cd_opts* opts, svl_cd** out);
+/* Initial conditions on total dofs (host arrays, NULL = zero); sets
+ * Up = U - dt V + dt^2/2 A (CentralDifference.cpp:61). */
+int  svl_cd_set_initial(svl_cd* cd, const double* U0, const double* V0, const double* A0);
+/* Advances steps k_first .. k_first+nsteps-1 (the reference's loop index k,
+ * DynamicAnalysis.cpp:36).  If U_hist is not NULL it receives the total
+ * displacement after every step, [nsteps][ntotal], copied to the host. */
+int  svl_cd_run(svl_cd* cd, int32_t k_first, int32_t nsteps, double* U_hist);
+/* which: 0 = U, 1 = V, 2 = A (total dofs, host copy). */
+int  svl_cd_get(svl_cd* cd, int32_t which, double* out);
+/* Device pointer of U / V / A (valid until the next svl_cd_run). */
+int  svl_cd_device_ptr(svl_cd* cd, int32_t which, const double** dptr);
+/* Number of kernel launches the last svl_cd_run issued. */
+int  svl_cd_launch_count(svl_cd* cd, int64_t* launches);
+/* svl_cd_run without history, bracketed by CUDA events recorded on the
+ * handle's own stream; *ms = elapsed device time of the nsteps.  No
+ * counterpart in the reference (measurement hook). */
+int  svl_cd_run_timed(svl_cd* cd, int32_t k_first, int32_t nsteps, float* ms);
+/* Runs nsteps launching every kernel individually with CUDA events between
+ * them; ms_kernel[i] receives the summed device time of kernel kind i
+ * (0 = element forces, 1 = node gather/update, 2 = residual, 3 = free-dof
+ * solve, 4 = update; unused kinds stay 0).  No counterpart in the reference. */
+int  svl_cd_profile(svl_cd* cd, int32_t k_first, int32_t nsteps, double* ms_kernel);
+int  svl_cd_sync(svl_cd* cd);
+void svl_cd_destroy(svl_cd* cd);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SVL_GB300_H */

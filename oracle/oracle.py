@@ -1,0 +1,133 @@
+"""ctypes binding of the CPU oracle (oracle/svl_oracle.cpp).
+
+TEST INFRASTRUCTURE: imported only by tests/, __graft_entry__.smoke() and
+bench.py's CPU-baseline arm, as the checker -- never by the svl_gb300 product.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+ORACLE_LIB = Path(__file__).resolve().parent / "_build" / "libsvl_oracle.so"
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not ORACLE_LIB.exists():
+            raise RuntimeError("oracle library missing (%s); run __graft_entry__.build()" % ORACLE_LIB)
+        L = C.CDLL(str(ORACLE_LIB))
+        vp = C.c_void_p
+        f64p = C.POINTER(C.c_double)
+        L.oracle_cd_run.argtypes = [vp, vp, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int, C.c_int,
+                                    f64p, f64p, f64p, f64p, f64p, f64p, f64p, f64p]
+        L.oracle_newmark_run.argtypes = [vp, vp, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double,
+                                         C.c_int, C.c_double, f64p, C.POINTER(C.c_long)]
+        L.oracle_element_fint.argtypes = [vp, f64p, f64p]
+        L.oracle_element_matrices.argtypes = [vp, C.c_int, f64p, f64p, f64p]
+        L.oracle_body_force.argtypes = [vp, C.c_int, f64p, f64p]
+        L.oracle_lumped_mass.argtypes = [vp, C.c_double, f64p]
+        L.oracle_j2_path.argtypes = [C.c_int, f64p, C.c_int, f64p, f64p]
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    if a is None:
+        return C.cast(None, C.POINTER(C.c_double))
+    return np.ascontiguousarray(a, dtype=np.float64).ctypes.data_as(C.POINTER(C.c_double))
+
+
+def cd_run(model, loads, dt, nsteps, k_first=1, ftol=1e-12, mtol=1e-12, mode=0, history=True,
+           U0=None, V0=None, A0=None, timing=None):
+    """Central difference on the CPU; returns (hist [nsteps, ntotal] or None, U, V, A).
+    If `timing` is a dict, timing['seconds'] receives the step-loop wall time."""
+    md = model.desc()
+    ld = loads.desc() if loads is not None else None
+    nt = model.ntotal
+    hist = np.zeros((nsteps, nt)) if history else None
+    U, V, A = np.zeros(nt), np.zeros(nt), np.zeros(nt)
+    keep = [None if a is None else np.ascontiguousarray(a, dtype=np.float64) for a in (U0, V0, A0)]
+    secs = np.zeros(1)
+    st = lib().oracle_cd_run(C.addressof(md), C.addressof(ld) if ld is not None else None, dt, ftol, mtol,
+                             k_first, nsteps, mode, _p(keep[0]), _p(keep[1]), _p(keep[2]),
+                             _p(hist) if hist is not None else _p(None),
+                             U.ctypes.data_as(C.POINTER(C.c_double)), V.ctypes.data_as(C.POINTER(C.c_double)),
+                             A.ctypes.data_as(C.POINTER(C.c_double)), secs.ctypes.data_as(C.POINTER(C.c_double)))
+    if st != 0:
+        raise RuntimeError("oracle_cd_run failed with status %d" % st)
+    if timing is not None:
+        timing["seconds"] = float(secs[0])
+    return hist, U, V, A
+
+
+def newmark_run(model, loads, dt, nsteps, k_first=1, algo=0, maxit=50, cnvgtol=1e-6, solver=0, pcg_tol=1e-12):
+    md = model.desc()
+    ld = loads.desc() if loads is not None else None
+    hist = np.zeros((nsteps, model.ntotal))
+    it = C.c_long(0)
+    st = lib().oracle_newmark_run(C.addressof(md), C.addressof(ld) if ld is not None else None, dt, k_first,
+                                  nsteps, algo, maxit, cnvgtol, solver, pcg_tol,
+                                  hist.ctypes.data_as(C.POINTER(C.c_double)), C.byref(it))
+    if st != 0:
+        raise RuntimeError("oracle_newmark_run failed with status %d" % st)
+    return hist, it.value
+
+
+def element_fint(model, U):
+    nc = model.conn.shape[1] * model.ndim
+    out = np.zeros((model.nelem, nc))
+    md = model.desc()
+    Ua = np.ascontiguousarray(U, dtype=np.float64)
+    st = lib().oracle_element_fint(C.addressof(md), Ua.ctypes.data_as(C.POINTER(C.c_double)),
+                                   out.ctypes.data_as(C.POINTER(C.c_double)))
+    assert st == 0
+    return out
+
+
+def element_matrices(model, e):
+    nc = model.conn.shape[1] * model.ndim
+    K, Ml, Mc = np.zeros((nc, nc)), np.zeros((nc, nc)), np.zeros((nc, nc))
+    md = model.desc()
+    st = lib().oracle_element_matrices(C.addressof(md), e, K.ctypes.data_as(C.POINTER(C.c_double)),
+                                       Ml.ctypes.data_as(C.POINTER(C.c_double)),
+                                       Mc.ctypes.data_as(C.POINTER(C.c_double)))
+    assert st == 0
+    return K, Ml, Mc
+
+
+def body_force(model, e, q):
+    nc = model.conn.shape[1] * model.ndim
+    fe = np.zeros(nc)
+    md = model.desc()
+    qa = np.ascontiguousarray(q, dtype=np.float64)
+    st = lib().oracle_body_force(C.addressof(md), e, qa.ctypes.data_as(C.POINTER(C.c_double)),
+                                 fe.ctypes.data_as(C.POINTER(C.c_double)))
+    assert st == 0
+    return fe
+
+
+def lumped_mass(model, mtol=1e-12):
+    M = np.zeros(model.ntotal)
+    md = model.desc()
+    st = lib().oracle_lumped_mass(C.addressof(md), mtol, M.ctypes.data_as(C.POINTER(C.c_double)))
+    assert st == 0
+    return M
+
+
+def j2_path(mat_type, param, strains):
+    strains = np.ascontiguousarray(strains, dtype=np.float64)
+    out = np.zeros_like(strains)
+    p = np.ascontiguousarray(param, dtype=np.float64)
+    st = lib().oracle_j2_path(mat_type, p.ctypes.data_as(C.POINTER(C.c_double)), strains.shape[0],
+                              strains.ctypes.data_as(C.POINTER(C.c_double)), out.ctypes.data_as(C.POINTER(C.c_double)))
+    assert st == 0
+    return out
+
+
+def num_threads():
+    lib().oracle_num_threads.restype = C.c_int
+    return lib().oracle_num_threads()

@@ -1,0 +1,1061 @@
+/*
+ * svl_oracle.cpp -- CPU FP64 restatement of SeismoVLAB's time-stepping hot
+ * path.  TEST INFRASTRUCTURE ONLY: this file is the checker the GPU path is
+ * compared against (tests/, __graft_entry__.smoke(), bench.py's CPU baseline
+ * arm).  Nothing in the svl_gb300 product links or calls it.
+ *
+ * It follows the reference's structure on purpose ("reference-faithful"):
+ * Jacobian, its inverse and the strain-displacement matrix are recomputed at
+ * every Gauss point on every call; element contributions are summed in
+ * element-tag order with the assembler's tolerance filters; the central
+ * difference update is the diagonal solve of (M/dt^2) with Eigen's
+ * (1/d)*b convention.  A second, "fast" internal-force routine (precomputed
+ * Gauss-point geometry, OpenMP over elements, same summation order) exists
+ * only to time a multi-core CPU baseline.
+ *
+ * Parity status: pinned against the reference's own artefacts where they
+ * exist -- the pre-processor's numbering (tests/golden/, generated by running
+ * PP/ on small models) and the OpenSees histories shipped with the
+ * validation cases F02/F03/J02 (03-Validations/01-Debugging) -- but not
+ * against the SVL binary, which cannot be built without Eigen/PETSc/MUMPS.
+ *
+ * Citations are relative to the SVL tree: RP/ = 02-Run_Process/.
+ * Compile with -ffp-contract=off so x86 and Arm hosts round identically.
+ */
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+#include <string>
+#include <algorithm>
+#include <chrono>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#include "../include/svl_gb300.h"
+
+namespace {
+
+/* Gauss points: RP/04-Elements/11-Integration/GaussQuadrature.cpp:303-316
+ * (quad, r fastest) and the hexa table below it (r, then s, then t); the
+ * abscissa is the 15-digit truncated 1/sqrt(3) with unit weights. */
+const double kGauss = 0.577350269189626;
+
+struct Model {
+    int ndim, nnode, ndof, ntotal, nfree, nelem, nen, ngp, nstr, etype;
+    std::vector<double> X;            // [nnode][ndim]
+    std::vector<int> tdof, fdof;      // [nnode][ndof]
+    std::vector<int> conn, emat;
+    std::vector<double> thick;
+    std::vector<int> mtype;
+    std::vector<double> mpar;
+    std::vector<double> nodemass;     // [ntotal] or empty
+    int nconstraint;
+    std::vector<int> cslave, cptr, cmaster;
+    std::vector<double> cfactor;
+    int lumped;
+};
+
+struct Loads {
+    std::vector<int> sptr; std::vector<double> sval;
+    std::vector<int> fdof, fser; std::vector<double> fcoef;
+    std::vector<int> smdof, smser; std::vector<double> smfac;
+    double series(int s, int k) const {            // Load::GetLoadVector (Load.cpp:69-71)
+        int n = sptr[s + 1] - sptr[s];
+        return (k >= 0 && k < n) ? sval[sptr[s] + k] : 0.0;
+    }
+    double support(int s, int k) const {           // Node::GetSupportMotion (Node.cpp:228-247)
+        int n = sptr[s + 1] - sptr[s];
+        if (n <= 0) return 0.0;
+        return (k < n) ? sval[sptr[s] + k] : sval[sptr[s]];
+    }
+};
+
+bool load_model(const svl_model_desc* d, Model& m) {
+    if (!d) return false;
+    m.ndim = d->ndim; m.nnode = d->nnode; m.ndof = d->ndof;
+    m.ntotal = d->ntotal; m.nfree = d->nfree; m.nelem = d->nelem; m.etype = d->elem_type;
+    if (m.etype == SVL_ELEM_LIN2DQUAD4) { m.nen = 4; m.ngp = 4; m.nstr = 3; if (m.ndim != 2) return false; }
+    else if (m.etype == SVL_ELEM_LIN3DHEXA8) { m.nen = 8; m.ngp = 8; m.nstr = 6; if (m.ndim != 3) return false; }
+    else return false;
+    if (m.ndof != m.ndim) return false;
+    m.X.assign(d->coords, d->coords + (size_t)m.nnode * m.ndim);
+    m.tdof.assign(d->totaldof, d->totaldof + (size_t)m.nnode * m.ndof);
+    m.fdof.assign(d->freedof, d->freedof + (size_t)m.nnode * m.ndof);
+    m.conn.assign(d->conn, d->conn + (size_t)m.nelem * m.nen);
+    m.emat.assign(d->elem_mat, d->elem_mat + m.nelem);
+    m.thick.assign(m.nelem, 1.0);
+    if (d->elem_thickness) m.thick.assign(d->elem_thickness, d->elem_thickness + m.nelem);
+    m.mtype.assign(d->mat_type, d->mat_type + d->nmat);
+    m.mpar.assign(d->mat_param, d->mat_param + (size_t)d->nmat * SVL_MAT_NPARAM);
+    if (d->node_mass) m.nodemass.assign(d->node_mass, d->node_mass + m.ntotal);
+    m.nconstraint = d->nconstraint;
+    if (m.nconstraint > 0) {
+        m.cslave.assign(d->con_slave, d->con_slave + m.nconstraint);
+        m.cptr.assign(d->con_ptr, d->con_ptr + m.nconstraint + 1);
+        m.cmaster.assign(d->con_master, d->con_master + m.cptr.back());
+        m.cfactor.assign(d->con_factor, d->con_factor + m.cptr.back());
+    }
+    m.lumped = d->lumped;
+    return true;
+}
+
+void load_loads(const svl_load_desc* l, Loads& L) {
+    L.sptr.assign(1, 0);
+    if (!l) return;
+    if (l->nseries > 0) {
+        L.sptr.assign(l->series_ptr, l->series_ptr + l->nseries + 1);
+        L.sval.assign(l->series_val, l->series_val + L.sptr.back());
+    }
+    if (l->nforce > 0) {
+        L.fdof.assign(l->force_dof, l->force_dof + l->nforce);
+        L.fser.assign(l->force_series, l->force_series + l->nforce);
+        L.fcoef.assign(l->force_coef, l->force_coef + l->nforce);
+    }
+    if (l->nsupport > 0) {
+        L.smdof.assign(l->sm_dof, l->sm_dof + l->nsupport);
+        L.smser.assign(l->sm_series, l->sm_series + l->nsupport);
+        L.smfac.assign(l->sm_factor, l->sm_factor + l->nsupport);
+    }
+}
+
+/* ---------------- materials (per Gauss point) ---------------------------- */
+
+struct MatState {                  // committed + trial state of one Gauss point
+    double strain[6], stress[6], ep[6], back[6], alpha;
+    double ep_n[6], back_n[6], alpha_n, strain_n[6], stress_n[6];
+    double tangent[36], tangent_n[36];
+};
+
+// 6x6 helpers of the J2 models (PlasticPlaneStrainJ2.cpp:282-350).
+void j2_identity_tensor(double D[36]) {          // 1 (x) 1 on the normal block
+    for (int i = 0; i < 36; ++i) D[i] = 0.0;
+    for (int i = 0; i < 3; ++i) for (int j = 0; j < 3; ++j) D[i * 6 + j] = 1.0;
+}
+void j2_identity_operator(double I[36]) {        // symmetric identity, 1/2 on shear
+    for (int i = 0; i < 36; ++i) I[i] = 0.0;
+    for (int i = 0; i < 3; ++i) I[i * 6 + i] = 1.0;
+    for (int i = 3; i < 6; ++i) I[i * 6 + i] = 0.5;
+}
+double j2_norm(const double T[6]) {
+    return std::sqrt(T[0] * T[0] + T[1] * T[1] + T[2] * T[2] + 2.0 * (T[3] * T[3] + T[4] * T[4] + T[5] * T[5]));
+}
+
+void j2_elastic_tangent(double K, double G, double C[36]) {
+    double D[36], I[36];
+    j2_identity_tensor(D); j2_identity_operator(I);
+    for (int i = 0; i < 36; ++i) C[i] = K * D[i] + 2.0 * G * (I[i] - 1.0 / 3.0 * D[i]);
+}
+
+void mat_init(MatState& s, int type, const double* p) {
+    std::memset(&s, 0, sizeof(s));
+    if (type == SVL_MAT_PLASTICPLANESTRAINJ2 || type == SVL_MAT_PLASTIC3DJ2) {
+        j2_elastic_tangent(p[0], p[1], s.tangent);
+        std::memcpy(s.tangent_n, s.tangent, sizeof(s.tangent));
+    }
+}
+
+/* J2 radial return on the 6-vector tensor strain E (shear = 1/2 gamma):
+ * PlasticPlaneStrainJ2::UpdateState (PlasticPlaneStrainJ2.cpp:227-279) and
+ * Plastic3DJ2::UpdateState (Plastic3DJ2.cpp:206-255) share this arithmetic.
+ * Like the reference, the update starts from the current (not the last
+ * committed) plastic strain, back stress and hardening variable. */
+void j2_update(MatState& s, const double* p, const double E[6]) {
+    const double K = p[0], G = p[1], H = p[3], beta = p[4], SY = p[5];
+    const double one[6] = {1, 1, 1, 0, 0, 0};
+    double D[36], I[36], Id[36];
+    j2_identity_tensor(D); j2_identity_operator(I);
+    for (int i = 0; i < 36; ++i) Id[i] = I[i] - 1.0 / 3.0 * D[i];
+    for (int i = 0; i < 6; ++i) s.strain[i] = E[i];
+    double tr = E[0] + E[1] + E[2];
+    double dev[6], trial[6], rel[6];
+    for (int i = 0; i < 6; ++i) dev[i] = E[i] - 1.0 / 3.0 * tr * one[i];
+    for (int i = 0; i < 6; ++i) trial[i] = 2.0 * G * (dev[i] - s.ep[i]);
+    for (int i = 0; i < 6; ++i) rel[i] = trial[i] - s.back[i];
+    double nrm = j2_norm(rel);
+    double f = nrm - std::sqrt(2.0 / 3.0) * (SY + s.alpha * beta * H);
+    if (f <= 0) {
+        for (int i = 0; i < 36; ++i) s.tangent[i] = K * D[i] + 2.0 * G * Id[i];
+        for (int i = 0; i < 6; ++i) s.stress[i] = K * tr * one[i] + trial[i];
+    } else {
+        double n[6];
+        for (int i = 0; i < 6; ++i) n[i] = rel[i] / nrm;
+        double dg = f / (2.0 * G + 2.0 / 3.0 * H);
+        s.alpha += std::sqrt(2.0 / 3.0) * dg;
+        for (int i = 0; i < 6; ++i) s.back[i] += 2.0 / 3.0 * (1.0 - beta) * H * dg * n[i];
+        for (int i = 0; i < 6; ++i) s.ep[i] += dg * n[i];
+        for (int i = 0; i < 6; ++i) s.stress[i] = K * tr * one[i] + trial[i] - 2.0 * G * dg * n[i];
+        double c1 = 1.0 / (1.0 + H / G / 3.0), c2 = 4.0 * G * G * dg / nrm;
+        for (int i = 0; i < 6; ++i)
+            for (int j = 0; j < 6; ++j) {
+                double nn = n[i] * n[j];
+                s.tangent[i * 6 + j] = K * D[i * 6 + j] + 2.0 * G * (Id[i * 6 + j] - c1 * nn) - c2 * (Id[i * 6 + j] - nn);
+            }
+    }
+}
+
+/* Material::UpdateState(strain, 1) for the engineering strain vector of the
+ * element (3 entries in 2D: xx, yy, gamma_xy; 6 in 3D). */
+void mat_update(MatState& s, int type, const double* p, const double* eps) {
+    if (type == SVL_MAT_ELASTIC2DPLANESTRAIN) {
+        for (int i = 0; i < 3; ++i) s.strain[i] = eps[i];
+    } else if (type == SVL_MAT_ELASTIC3DLINEAR) {
+        for (int i = 0; i < 6; ++i) s.strain[i] = eps[i];
+    } else if (type == SVL_MAT_PLASTICPLANESTRAINJ2) {
+        // plane strain mapped to [0, exx, eyy, 0, gxy/2, 0] (PlasticPlaneStrainJ2.cpp:236)
+        double E[6] = {0.0, eps[0], eps[1], 0.0, 0.5 * eps[2], 0.0};
+        j2_update(s, p, E);
+    } else {
+        // (Plastic3DJ2.cpp:215)
+        double E[6] = {eps[0], eps[1], eps[2], 0.5 * eps[3], 0.5 * eps[4], 0.5 * eps[5]};
+        j2_update(s, p, E);
+    }
+}
+
+void elastic_coeffs(const double* p, double& c1, double& c2, double& c3) {
+    const double E = p[0], nu = p[1];
+    c1 = E * (1.0 - nu) / (1.0 - 2.0 * nu) / (1.0 + nu);
+    c2 = E * nu / (1.0 - 2.0 * nu) / (1.0 + nu);
+    c3 = E / (2.0 * (1.0 + nu));
+}
+
+// Material::GetStress (Elastic2DPlaneStrain.cpp:96-99, Elastic3DLinear.cpp:97,
+// PlasticPlaneStrainJ2.cpp:123-128 returns indices 1,2,4).
+void mat_stress(const MatState& s, int type, const double* p, double* sig) {
+    if (type == SVL_MAT_ELASTIC2DPLANESTRAIN) {
+        double c1, c2, c3; elastic_coeffs(p, c1, c2, c3);
+        sig[0] = c1 * s.strain[0] + c2 * s.strain[1];
+        sig[1] = c2 * s.strain[0] + c1 * s.strain[1];
+        sig[2] = c3 * s.strain[2];
+    } else if (type == SVL_MAT_ELASTIC3DLINEAR) {
+        double c1, c2, c3; elastic_coeffs(p, c1, c2, c3);
+        const double* e = s.strain;
+        sig[0] = c1 * e[0] + c2 * e[1] + c2 * e[2];
+        sig[1] = c2 * e[0] + c1 * e[1] + c2 * e[2];
+        sig[2] = c2 * e[0] + c2 * e[1] + c1 * e[2];
+        sig[3] = c3 * e[3]; sig[4] = c3 * e[4]; sig[5] = c3 * e[5];
+    } else if (type == SVL_MAT_PLASTICPLANESTRAINJ2) {
+        sig[0] = s.stress[1]; sig[1] = s.stress[2]; sig[2] = s.stress[4];
+    } else {
+        for (int i = 0; i < 6; ++i) sig[i] = s.stress[i];
+    }
+}
+
+// Material::GetTangentStiffness (nstr x nstr, row-major).
+void mat_tangent(const MatState& s, int type, const double* p, double* C) {
+    if (type == SVL_MAT_ELASTIC2DPLANESTRAIN) {
+        double c1, c2, c3; elastic_coeffs(p, c1, c2, c3);
+        double T[9] = {c1, c2, 0, c2, c1, 0, 0, 0, c3};
+        std::memcpy(C, T, sizeof(T));
+    } else if (type == SVL_MAT_ELASTIC3DLINEAR) {
+        double c1, c2, c3; elastic_coeffs(p, c1, c2, c3);
+        for (int i = 0; i < 36; ++i) C[i] = 0.0;
+        for (int i = 0; i < 3; ++i) for (int j = 0; j < 3; ++j) C[i * 6 + j] = (i == j) ? c1 : c2;
+        for (int i = 3; i < 6; ++i) C[i * 6 + i] = c3;
+    } else if (type == SVL_MAT_PLASTICPLANESTRAINJ2) {
+        // (PlasticPlaneStrainJ2.cpp:151-159) rows/cols 1,2,4 of the 6x6 tangent
+        const int ix[3] = {1, 2, 4};
+        for (int i = 0; i < 3; ++i) for (int j = 0; j < 3; ++j) C[i * 3 + j] = s.tangent[ix[i] * 6 + ix[j]];
+    } else {
+        std::memcpy(C, s.tangent, sizeof(double) * 36);
+    }
+}
+
+void mat_commit(MatState& s) {
+    std::memcpy(s.ep_n, s.ep, sizeof(s.ep)); std::memcpy(s.back_n, s.back, sizeof(s.back));
+    s.alpha_n = s.alpha;
+    std::memcpy(s.strain_n, s.strain, sizeof(s.strain)); std::memcpy(s.stress_n, s.stress, sizeof(s.stress));
+    std::memcpy(s.tangent_n, s.tangent, sizeof(s.tangent));
+}
+
+double mat_density(int type, const double* p) { (void)type; return p[2]; }
+
+/* ---------------- element kinematics ------------------------------------- */
+
+void gauss_point(int nd, int q, double xi[3]) {
+    xi[0] = (q & 1) ? kGauss : -kGauss;
+    xi[1] = (q & 2) ? kGauss : -kGauss;
+    xi[2] = (q & 4) ? kGauss : -kGauss;
+    if (nd == 2) xi[2] = 0.0;
+}
+
+// Natural derivatives dN_a/dr_i of the bilinear / trilinear shape functions,
+// node order of lin2DQuad4.cpp:648-667 and lin3DHexa8.cpp:756-807.
+void shape_derivs(int nd, const double* xi, double dN[8][3], double N[8]) {
+    if (nd == 2) {
+        const double sr[4] = {-1, 1, 1, -1}, ss[4] = {-1, -1, 1, 1};
+        for (int a = 0; a < 4; ++a) {
+            N[a] = 0.25 * (1.0 + sr[a] * xi[0]) * (1.0 + ss[a] * xi[1]);
+            dN[a][0] = 0.25 * sr[a] * (1.0 + ss[a] * xi[1]);
+            dN[a][1] = 0.25 * ss[a] * (1.0 + sr[a] * xi[0]);
+            dN[a][2] = 0.0;
+        }
+    } else {
+        const double sr[8] = {-1, 1, 1, -1, -1, 1, 1, -1};
+        const double ss[8] = {-1, -1, 1, 1, -1, -1, 1, 1};
+        const double st[8] = {-1, -1, -1, -1, 1, 1, 1, 1};
+        for (int a = 0; a < 8; ++a) {
+            double fr = 1.0 + sr[a] * xi[0], fs = 1.0 + ss[a] * xi[1], ft = 1.0 + st[a] * xi[2];
+            N[a] = 0.125 * fr * fs * ft;
+            dN[a][0] = 0.125 * sr[a] * fs * ft;
+            dN[a][1] = 0.125 * ss[a] * fr * ft;
+            dN[a][2] = 0.125 * st[a] * fr * fs;
+        }
+    }
+}
+
+/* Jacobian J_ij = d x_j / d r_i, its determinant and the physical shape
+ * derivatives dN_a/dx_j = sum_i Jinv_ji dN_a/dr_i (the B coefficients of
+ * lin2DQuad4.cpp:688-710 / lin3DHexa8.cpp:811-853). */
+double element_gp(const Model& m, int e, int q, double dNx[8][3], double N[8]) {
+    const int nd = m.ndim, nen = m.nen;
+    double xi[3], dN[8][3];
+    gauss_point(nd, q, xi);
+    shape_derivs(nd, xi, dN, N);
+    double J[3][3] = {{0}};
+    for (int a = 0; a < nen; ++a) {
+        const double* x = &m.X[(size_t)m.conn[(size_t)e * nen + a] * nd];
+        for (int i = 0; i < nd; ++i) for (int j = 0; j < nd; ++j) J[i][j] += dN[a][i] * x[j];
+    }
+    double det, Ji[3][3];
+    if (nd == 2) {
+        det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+        Ji[0][0] = J[1][1] / det; Ji[0][1] = -J[0][1] / det;
+        Ji[1][0] = -J[1][0] / det; Ji[1][1] = J[0][0] / det;
+    } else {
+        double c00 = J[1][1] * J[2][2] - J[1][2] * J[2][1];
+        double c01 = J[1][2] * J[2][0] - J[1][0] * J[2][2];
+        double c02 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+        det = J[0][0] * c00 + J[0][1] * c01 + J[0][2] * c02;
+        Ji[0][0] = c00 / det;
+        Ji[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) / det;
+        Ji[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) / det;
+        Ji[1][0] = c01 / det;
+        Ji[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) / det;
+        Ji[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) / det;
+        Ji[2][0] = c02 / det;
+        Ji[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) / det;
+        Ji[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) / det;
+    }
+    for (int a = 0; a < nen; ++a)
+        for (int j = 0; j < nd; ++j) {
+            double v = 0.0;
+            for (int i = 0; i < nd; ++i) v += Ji[j][i] * dN[a][i];
+            dNx[a][j] = v;
+        }
+    return det;
+}
+
+// Engineering strain B u at one Gauss point.
+void strain_of(int nd, int nen, const double dNx[8][3], const double* ue, double* eps) {
+    if (nd == 2) {
+        double exx = 0, eyy = 0, gxy = 0;
+        for (int a = 0; a < nen; ++a) {
+            exx += dNx[a][0] * ue[2 * a];
+            eyy += dNx[a][1] * ue[2 * a + 1];
+            gxy += dNx[a][1] * ue[2 * a] + dNx[a][0] * ue[2 * a + 1];
+        }
+        eps[0] = exx; eps[1] = eyy; eps[2] = gxy;
+    } else {
+        double e[6] = {0, 0, 0, 0, 0, 0};
+        for (int a = 0; a < nen; ++a) {
+            const double* u = ue + 3 * a;
+            e[0] += dNx[a][0] * u[0];
+            e[1] += dNx[a][1] * u[1];
+            e[2] += dNx[a][2] * u[2];
+            e[3] += dNx[a][1] * u[0] + dNx[a][0] * u[1];
+            e[4] += dNx[a][2] * u[1] + dNx[a][1] * u[2];
+            e[5] += dNx[a][2] * u[0] + dNx[a][0] * u[2];
+        }
+        for (int i = 0; i < 6; ++i) eps[i] = e[i];
+    }
+}
+
+// fe += c * B^T sig.
+void add_BTsig(int nd, int nen, const double dNx[8][3], const double* sig, double c, double* fe) {
+    if (nd == 2) {
+        for (int a = 0; a < nen; ++a) {
+            fe[2 * a]     += c * (dNx[a][0] * sig[0] + dNx[a][1] * sig[2]);
+            fe[2 * a + 1] += c * (dNx[a][1] * sig[1] + dNx[a][0] * sig[2]);
+        }
+    } else {
+        for (int a = 0; a < nen; ++a) {
+            const double bx = dNx[a][0], by = dNx[a][1], bz = dNx[a][2];
+            fe[3 * a]     += c * (bx * sig[0] + by * sig[3] + bz * sig[5]);
+            fe[3 * a + 1] += c * (by * sig[1] + bx * sig[3] + bz * sig[4]);
+            fe[3 * a + 2] += c * (bz * sig[2] + by * sig[4] + bx * sig[5]);
+        }
+    }
+}
+
+// B as an nstr x (nen*nd) dense matrix (for stiffness assembly).
+void B_matrix(int nd, int nen, const double dNx[8][3], double* B) {
+    const int nc = nen * nd;
+    if (nd == 2) {
+        for (int i = 0; i < 3 * nc; ++i) B[i] = 0.0;
+        for (int a = 0; a < nen; ++a) {
+            B[0 * nc + 2 * a] = dNx[a][0];
+            B[1 * nc + 2 * a + 1] = dNx[a][1];
+            B[2 * nc + 2 * a] = dNx[a][1]; B[2 * nc + 2 * a + 1] = dNx[a][0];
+        }
+    } else {
+        for (int i = 0; i < 6 * nc; ++i) B[i] = 0.0;
+        for (int a = 0; a < nen; ++a) {
+            const double bx = dNx[a][0], by = dNx[a][1], bz = dNx[a][2];
+            B[0 * nc + 3 * a] = bx; B[1 * nc + 3 * a + 1] = by; B[2 * nc + 3 * a + 2] = bz;
+            B[3 * nc + 3 * a] = by; B[3 * nc + 3 * a + 1] = bx;
+            B[4 * nc + 3 * a + 1] = bz; B[4 * nc + 3 * a + 2] = by;
+            B[5 * nc + 3 * a] = bz; B[5 * nc + 3 * a + 2] = bx;
+        }
+    }
+}
+
+/* ---------------- the simulated mesh ------------------------------------- */
+
+struct Sim {
+    Model m; Loads L;
+    std::vector<MatState> gp;          // [nelem][ngp]
+    std::vector<int> edofs;            // [nelem][nen*ndof] total dofs
+    // T (total <- free) as row lists: for every total dof the (free, factor) pairs.
+    std::vector<int> Tptr, Tcol; std::vector<double> Tval;
+    std::vector<int> smflag;
+    double ftol = 1e-12, mtol = 1e-12, ktol = 1e-12;
+
+    bool init(const svl_model_desc* d, const svl_load_desc* l) {
+        if (!load_model(d, m)) return false;
+        load_loads(l, L);
+        const int nc = m.nen * m.ndof;
+        edofs.resize((size_t)m.nelem * nc);
+        for (int e = 0; e < m.nelem; ++e)
+            for (int a = 0; a < m.nen; ++a)
+                for (int j = 0; j < m.ndof; ++j)
+                    edofs[(size_t)e * nc + a * m.ndof + j] = m.tdof[(size_t)m.conn[(size_t)e * m.nen + a] * m.ndof + j];
+        gp.resize((size_t)m.nelem * m.ngp);
+        for (int e = 0; e < m.nelem; ++e)
+            for (int q = 0; q < m.ngp; ++q)
+                mat_init(gp[(size_t)e * m.ngp + q], m.mtype[m.emat[e]], &m.mpar[(size_t)m.emat[e] * SVL_MAT_NPARAM]);
+        build_T();
+        smflag.assign(m.ntotal, 0);
+        for (int d0 : L.smdof) smflag[d0] = 1;
+        return true;
+    }
+
+    // Mesh::GetTotalToFreeMatrix (Mesh.cpp:328-383): identity rows for free
+    // dofs, factor rows for constrained dofs, zero rows for restrained ones.
+    void build_T() {
+        std::vector<std::vector<std::pair<int, double>>> rows(m.ntotal);
+        for (int n = 0; n < m.nnode; ++n)
+            for (int j = 0; j < m.ndof; ++j) {
+                int f = m.fdof[(size_t)n * m.ndof + j], t = m.tdof[(size_t)n * m.ndof + j];
+                if (f > -1) rows[t].push_back({f, 1.0});
+            }
+        for (int c = 0; c < m.nconstraint; ++c)
+            for (int i = m.cptr[c]; i < m.cptr[c + 1]; ++i)
+                rows[m.cslave[c]].push_back({m.cmaster[i], m.cfactor[i]});
+        Tptr.assign(m.ntotal + 1, 0);
+        for (int t = 0; t < m.ntotal; ++t) {
+            std::sort(rows[t].begin(), rows[t].end());
+            // setFromTriplets sums duplicates
+            std::vector<std::pair<int, double>> r;
+            for (auto& p : rows[t]) { if (!r.empty() && r.back().first == p.first) r.back().second += p.second; else r.push_back(p); }
+            for (auto& p : r) { Tcol.push_back(p.first); Tval.push_back(p.second); }
+            Tptr[t + 1] = (int)Tcol.size();
+        }
+    }
+    // x_total = T x_free
+    void T_apply(const std::vector<double>& xf, std::vector<double>& xt) const {
+        xt.assign(m.ntotal, 0.0);
+        for (int t = 0; t < m.ntotal; ++t) {
+            double s = 0.0;
+            for (int i = Tptr[t]; i < Tptr[t + 1]; ++i) s += Tval[i] * xf[Tcol[i]];
+            xt[t] = s;
+        }
+    }
+    // y_free = T^T y_total, summed in ascending total-dof order.
+    void TT_apply(const std::vector<double>& yt, std::vector<double>& yf) const {
+        yf.assign(m.nfree, 0.0);
+        for (int t = 0; t < m.ntotal; ++t)
+            for (int i = Tptr[t]; i < Tptr[t + 1]; ++i) yf[Tcol[i]] += Tval[i] * yt[t];
+    }
+
+    const double* mp(int e) const { return &m.mpar[(size_t)m.emat[e] * SVL_MAT_NPARAM]; }
+    int mt(int e) const { return m.mtype[m.emat[e]]; }
+
+    // Element::ComputeInternalForces (lin2DQuad4.cpp:383-412, lin3DHexa8.cpp:383-412).
+    void element_fint(int e, double* fe) const {
+        const int nc = m.nen * m.ndof;
+        for (int i = 0; i < nc; ++i) fe[i] = 0.0;
+        for (int q = 0; q < m.ngp; ++q) {
+            double dNx[8][3], N[8];
+            double det = element_gp(m, e, q, dNx, N);
+            double sig[6];
+            mat_stress(gp[(size_t)e * m.ngp + q], mt(e), mp(e), sig);
+            double c = (m.ndim == 2) ? 1.0 * m.thick[e] * std::fabs(det) : 1.0 * std::fabs(det);
+            add_BTsig(m.ndim, m.nen, dNx, sig, c, fe);
+        }
+    }
+    // Element::UpdateState with strain B (U + dU) (lin2DQuad4.cpp:87-107, 618-633).
+    void element_update(int e, const std::vector<double>& Ustrain) {
+        const int nc = m.nen * m.ndof;
+        double ue[24];
+        for (int i = 0; i < nc; ++i) ue[i] = Ustrain[edofs[(size_t)e * nc + i]];
+        for (int q = 0; q < m.ngp; ++q) {
+            double dNx[8][3], N[8];
+            element_gp(m, e, q, dNx, N);
+            double eps[6];
+            strain_of(m.ndim, m.nen, dNx, ue, eps);
+            mat_update(gp[(size_t)e * m.ngp + q], mt(e), mp(e), eps);
+        }
+    }
+    void commit_all() { for (auto& s : gp) mat_commit(s); }
+
+    // Element::ComputeStiffnessMatrix with the current tangent.
+    void element_K(int e, double* Ke) const {
+        const int nc = m.nen * m.ndof, ns = m.nstr;
+        for (int i = 0; i < nc * nc; ++i) Ke[i] = 0.0;
+        for (int q = 0; q < m.ngp; ++q) {
+            double dNx[8][3], N[8];
+            double det = element_gp(m, e, q, dNx, N);
+            double B[6 * 24], C[36], CB[6 * 24];
+            B_matrix(m.ndim, m.nen, dNx, B);
+            mat_tangent(gp[(size_t)e * m.ngp + q], mt(e), mp(e), C);
+            double c = (m.ndim == 2) ? 1.0 * m.thick[e] * std::fabs(det) : 1.0 * std::fabs(det);
+            for (int i = 0; i < ns; ++i)
+                for (int j = 0; j < nc; ++j) {
+                    double v = 0.0;
+                    for (int k = 0; k < ns; ++k) v += C[i * ns + k] * B[k * nc + j];
+                    CB[i * nc + j] = v;
+                }
+            for (int i = 0; i < nc; ++i)
+                for (int j = 0; j < nc; ++j) {
+                    double v = 0.0;
+                    for (int k = 0; k < ns; ++k) v += B[k * nc + i] * CB[k * nc + j];
+                    Ke[i * nc + j] += c * v;
+                }
+        }
+    }
+    // Element::ComputeMassMatrix with row-sum lumping (lin2DQuad4.cpp:243-285).
+    void element_M(int e, double* Me, bool lump) const {
+        const int nc = m.nen * m.ndof, nd = m.ndim;
+        for (int i = 0; i < nc * nc; ++i) Me[i] = 0.0;
+        const double rho = mat_density(mt(e), mp(e));
+        for (int q = 0; q < m.ngp; ++q) {
+            double dNx[8][3], N[8];
+            double det = element_gp(m, e, q, dNx, N);
+            double c = (nd == 2) ? 1.0 * rho * m.thick[e] * std::fabs(det) : 1.0 * rho * std::fabs(det);
+            for (int a = 0; a < m.nen; ++a)
+                for (int b = 0; b < m.nen; ++b)
+                    for (int j = 0; j < nd; ++j) Me[(a * nd + j) * nc + (b * nd + j)] += c * (N[a] * N[b]);
+        }
+        if (lump)
+            for (int i = 0; i < nc; ++i)
+                for (int j = 0; j < nc; ++j)
+                    if (i != j) { Me[i * nc + i] += Me[i * nc + j]; Me[i * nc + j] = 0.0; }
+    }
+    // Element body force rho int(H^T q) (lin2DQuad4.cpp:528-560).
+    void element_body(int e, const double* qv, double* fe) const {
+        const int nc = m.nen * m.ndof, nd = m.ndim;
+        for (int i = 0; i < nc; ++i) fe[i] = 0.0;
+        const double rho = mat_density(mt(e), mp(e));
+        for (int q = 0; q < m.ngp; ++q) {
+            double dNx[8][3], N[8];
+            double det = element_gp(m, e, q, dNx, N);
+            double c = (nd == 2) ? 1.0 * rho * m.thick[e] * std::fabs(det) : 1.0 * rho * std::fabs(det);
+            for (int a = 0; a < m.nen; ++a)
+                for (int j = 0; j < nd; ++j) fe[a * nd + j] += c * (N[a] * qv[j]);
+        }
+    }
+
+    // Assembler::ComputeInternalForceVector (Assembler.cpp:240-269).
+    void assemble_fint(std::vector<double>& F) const {
+        F.assign(m.ntotal, 0.0);
+        const int nc = m.nen * m.ndof;
+        double fe[24];
+        for (int e = 0; e < m.nelem; ++e) {
+            element_fint(e, fe);
+            for (int j = 0; j < nc; ++j)
+                if (std::fabs(fe[j]) > ftol) F[edofs[(size_t)e * nc + j]] += fe[j];
+        }
+    }
+    // Diagonal of the assembled lumped mass (Assembler.cpp:48-67, 623-697).
+    void assemble_mass_diag(std::vector<double>& M) const {
+        std::vector<double> Me_e(m.ntotal, 0.0), Mn(m.ntotal, 0.0);
+        const int nc = m.nen * m.ndof;
+        std::vector<double> Me((size_t)nc * nc);
+        for (int e = 0; e < m.nelem; ++e) {
+            element_M(e, Me.data(), true);
+            for (int j = 0; j < nc; ++j)
+                for (int i = 0; i < nc; ++i) {
+                    double v = Me[(size_t)i * nc + j];
+                    if (std::fabs(v) > mtol && i == j) Me_e[edofs[(size_t)e * nc + i]] += v;
+                }
+        }
+        if (!m.nodemass.empty())
+            for (int t = 0; t < m.ntotal; ++t) if (std::fabs(m.nodemass[t]) > mtol) Mn[t] = m.nodemass[t];
+        M.resize(m.ntotal);
+        for (int t = 0; t < m.ntotal; ++t) M[t] = Me_e[t] + Mn[t];
+    }
+    // Assembler::ComputeExternalForceVector (Assembler.cpp:291-489), in the
+    // pre-resolved (dof, series, coef) form.
+    void fext(int k, std::vector<double>& F) const {
+        F.assign(m.ntotal, 0.0);
+        for (size_t i = 0; i < L.fdof.size(); ++i) F[L.fdof[i]] += L.fcoef[i] * L.series(L.fser[i], k);
+    }
+    // Assembler::ComputeSupportMotionIncrement (Assembler.cpp:493-532).
+    void support_increment(int k, std::vector<double>& SM) const {
+        SM.assign(m.ntotal, 0.0);
+        for (size_t i = 0; i < L.smdof.size(); ++i) {
+            double g = L.support(L.smser[i], k);
+            if (k > 0) g -= L.support(L.smser[i], k - 1);
+            SM[L.smdof[i]] += L.smfac[i] * g;
+        }
+    }
+};
+
+/* ---------------- central difference (CentralDifference.cpp) ------------- */
+
+struct CD {
+    Sim s; double dt;
+    std::vector<double> U, V, A, Up, Md, Kd, Kff_inv, Us;
+    bool fast = false;
+    std::vector<double> geo;   // fast mode: [nelem][ngp][nen*ndim + 1]
+    std::vector<double> fe_all;  // fast mode: element force blocks
+
+    bool init(const svl_model_desc* d, const svl_load_desc* l, double dt_, double ftol, double mtol) {
+        if (!s.init(d, l)) return false;
+        if (!s.m.lumped) return false;
+        dt = dt_; s.ftol = ftol; s.mtol = mtol;
+        const int nt = s.m.ntotal;
+        U.assign(nt, 0); V.assign(nt, 0); A.assign(nt, 0); Up.assign(nt, 0); Us.assign(nt, 0);
+        s.assemble_mass_diag(Md);
+        // K = 1/dt/dt*M + 1/2/dt*C with C = 0 (CentralDifference.cpp:70)
+        Kd.resize(nt);
+        for (int t = 0; t < nt; ++t) Kd[t] = 1.0 / dt / dt * Md[t];
+        // Keff = T^T K T (diagonal when every slave has one master)
+        std::vector<double> kf(s.m.nfree, 0.0);
+        for (int t = 0; t < nt; ++t)
+            for (int i = s.Tptr[t]; i < s.Tptr[t + 1]; ++i) kf[s.Tcol[i]] += s.Tval[i] * Kd[t] * s.Tval[i];
+        Kff_inv.resize(s.m.nfree);
+        for (int f = 0; f < s.m.nfree; ++f) Kff_inv[f] = 1.0 / kf[f];
+        return true;
+    }
+    void set_initial(const double* U0, const double* V0, const double* A0) {
+        for (int t = 0; t < s.m.ntotal; ++t) {
+            U[t] = U0 ? U0[t] : 0.0; V[t] = V0 ? V0[t] : 0.0; A[t] = A0 ? A0[t] : 0.0;
+            Up[t] = U[t] - dt * V[t] + dt * dt / 2.0 * A[t];
+        }
+    }
+    void enable_fast() {
+        const Model& m = s.m;
+        const int per = m.nen * m.ndim + 1;
+        geo.resize((size_t)m.nelem * m.ngp * per);
+        for (int e = 0; e < m.nelem; ++e)
+            for (int q = 0; q < m.ngp; ++q) {
+                double dNx[8][3], N[8];
+                double det = element_gp(m, e, q, dNx, N);
+                double* g = &geo[((size_t)e * m.ngp + q) * per];
+                for (int a = 0; a < m.nen; ++a) for (int j = 0; j < m.ndim; ++j) g[a * m.ndim + j] = dNx[a][j];
+                g[per - 1] = (m.ndim == 2) ? 1.0 * m.thick[e] * std::fabs(det) : 1.0 * std::fabs(det);
+            }
+        fast = true;
+    }
+    // Fast internal force: precomputed geometry, elements in parallel, then a
+    // serial element-order scatter so the sums match the faithful routine.
+    void fint_fast(std::vector<double>& F) {
+        const Model& m = s.m;
+        const int nc = m.nen * m.ndof, per = m.nen * m.ndim + 1;
+        fe_all.resize((size_t)m.nelem * nc);
+        #pragma omp parallel for schedule(static)
+        for (int e = 0; e < m.nelem; ++e) {
+            double* fe = &fe_all[(size_t)e * nc];
+            for (int i = 0; i < nc; ++i) fe[i] = 0.0;
+            for (int q = 0; q < m.ngp; ++q) {
+                const double* g = &geo[((size_t)e * m.ngp + q) * per];
+                double dNx[8][3];
+                for (int a = 0; a < m.nen; ++a) for (int j = 0; j < m.ndim; ++j) dNx[a][j] = g[a * m.ndim + j];
+                double sig[6];
+                mat_stress(s.gp[(size_t)e * m.ngp + q], s.mt(e), s.mp(e), sig);
+                add_BTsig(m.ndim, m.nen, dNx, sig, g[per - 1], fe);
+            }
+        }
+        F.assign(m.ntotal, 0.0);
+        for (int e = 0; e < m.nelem; ++e)
+            for (int j = 0; j < nc; ++j) {
+                double v = fe_all[(size_t)e * nc + j];
+                if (std::fabs(v) > s.ftol) F[s.edofs[(size_t)e * nc + j]] += v;
+            }
+    }
+    void update_fast(const std::vector<double>& Ustr) {
+        const Model& m = s.m;
+        const int nc = m.nen * m.ndof, per = m.nen * m.ndim + 1;
+        #pragma omp parallel for schedule(static)
+        for (int e = 0; e < m.nelem; ++e) {
+            double ue[24];
+            for (int i = 0; i < nc; ++i) ue[i] = Ustr[s.edofs[(size_t)e * nc + i]];
+            for (int q = 0; q < m.ngp; ++q) {
+                const double* g = &geo[((size_t)e * m.ngp + q) * per];
+                double dNx[8][3];
+                for (int a = 0; a < m.nen; ++a) for (int j = 0; j < m.ndim; ++j) dNx[a][j] = g[a * m.ndim + j];
+                double eps[6];
+                strain_of(m.ndim, m.nen, dNx, ue, eps);
+                mat_update(s.gp[(size_t)e * m.ngp + q], s.mt(e), s.mp(e), eps);
+            }
+        }
+    }
+
+    // One CentralDifference::ComputeNewStep(k) with Linear + diagonal solve,
+    // followed by the CommitState of DynamicAnalysis::UpdateDomain.
+    void step(int k) {
+        const int nt = s.m.ntotal;
+        std::vector<double> Fint, Fext, R(nt), Feff, SM, du, dUt;
+        if (fast) fint_fast(Fint); else s.assemble_fint(Fint);
+        s.fext(k, Fext);
+        // Fext + Fbar - Fint + (1/dt/dt*M - 1/2/dt*C)*(U - Up)   (CentralDifference.cpp:217)
+        for (int t = 0; t < nt; ++t) R[t] = (Fext[t] + 0.0 - Fint[t]) + (1.0 / dt / dt * Md[t]) * (U[t] - Up[t]);
+        s.TT_apply(R, Feff);
+        // support motion: Feff -= T^T (K SM)   (CentralDifference.cpp:190-202)
+        s.support_increment(k, SM);
+        {
+            std::vector<double> KSM(nt), lg;
+            for (int t = 0; t < nt; ++t) KSM[t] = Kd[t] * SM[t];
+            s.TT_apply(KSM, lg);
+            for (int f = 0; f < s.m.nfree; ++f) Feff[f] -= lg[f];
+        }
+        // diagonal LDL^T solve: x = (1/d) * b
+        du.resize(s.m.nfree);
+        for (int f = 0; f < s.m.nfree; ++f) du[f] = Kff_inv[f] * Feff[f];
+        // Algorithm::UpdateStatesIncrements: strain from U + T du (no support motion)
+        s.T_apply(du, dUt);
+        for (int t = 0; t < nt; ++t) Us[t] = U[t] + dUt[t];
+        if (fast) update_fast(Us); else for (int e = 0; e < s.m.nelem; ++e) s.element_update(e, Us);
+        // CentralDifference::ComputeNewStep (CentralDifference.cpp:138-148)
+        for (int t = 0; t < nt; ++t) {
+            double dU = dUt[t] + SM[t];
+            V[t] = 1.0 / 2.0 / dt * (U[t] + dU - Up[t]);
+            A[t] = 1.0 / dt / dt * (dU - U[t] + Up[t]);
+            Up[t] = U[t];
+            U[t] += dU;
+        }
+        s.commit_all();
+    }
+};
+
+/* ---------------- sparse matrices and solvers (Newmark) ------------------ */
+
+struct CSR { int n = 0; std::vector<int> ptr, col; std::vector<double> val; };
+
+// Triplets summed in insertion order per entry (setFromTriplets), free dofs only.
+struct Trip { int r, c; double v; };
+void csr_from_triplets(int n, std::vector<Trip>& tr, CSR& A) {
+    std::stable_sort(tr.begin(), tr.end(), [](const Trip& a, const Trip& b) { return a.r < b.r || (a.r == b.r && a.c < b.c); });
+    A.n = n; A.ptr.assign(n + 1, 0); A.col.clear(); A.val.clear();
+    for (size_t i = 0; i < tr.size();) {
+        size_t j = i; double v = 0.0;
+        while (j < tr.size() && tr[j].r == tr[i].r && tr[j].c == tr[i].c) { v += tr[j].v; ++j; }
+        A.col.push_back(tr[i].c); A.val.push_back(v); A.ptr[tr[i].r + 1]++;
+        i = j;
+    }
+    for (int r = 0; r < n; ++r) A.ptr[r + 1] += A.ptr[r];
+}
+
+void csr_mv(const CSR& A, const std::vector<double>& x, std::vector<double>& y) {
+    y.assign(A.n, 0.0);
+    for (int r = 0; r < A.n; ++r) { double s = 0; for (int i = A.ptr[r]; i < A.ptr[r + 1]; ++i) s += A.val[i] * x[A.col[i]]; y[r] = s; }
+}
+
+// Dense LDL^T (small systems only; stands in for SimplicialLDLT).
+bool dense_ldlt_solve(const CSR& A, const std::vector<double>& b, std::vector<double>& x) {
+    const int n = A.n;
+    std::vector<double> M((size_t)n * n, 0.0);
+    for (int r = 0; r < n; ++r) for (int i = A.ptr[r]; i < A.ptr[r + 1]; ++i) M[(size_t)r * n + A.col[i]] = A.val[i];
+    std::vector<double> D(n);
+    for (int j = 0; j < n; ++j) {
+        double d = M[(size_t)j * n + j];
+        for (int k = 0; k < j; ++k) d -= M[(size_t)j * n + k] * M[(size_t)j * n + k] * D[k];
+        if (d == 0.0 || !std::isfinite(d)) return false;
+        D[j] = d;
+        for (int i = j + 1; i < n; ++i) {
+            double v = M[(size_t)i * n + j];
+            for (int k = 0; k < j; ++k) v -= M[(size_t)i * n + k] * M[(size_t)j * n + k] * D[k];
+            M[(size_t)i * n + j] = v / d;
+        }
+    }
+    x = b;
+    for (int i = 0; i < n; ++i) for (int k = 0; k < i; ++k) x[i] -= M[(size_t)i * n + k] * x[k];
+    for (int i = 0; i < n; ++i) x[i] = x[i] / D[i];
+    for (int i = n - 1; i >= 0; --i) for (int k = i + 1; k < n; ++k) x[i] -= M[(size_t)k * n + i] * x[k];
+    return true;
+}
+
+// Jacobi-preconditioned CG to a true relative residual tolerance.
+int pcg_solve(const CSR& A, const std::vector<double>& b, std::vector<double>& x, double rtol, int maxit, int* iters) {
+    const int n = A.n;
+    std::vector<double> dinv(n, 1.0), r(n), z(n), p(n), q;
+    for (int i = 0; i < n; ++i) for (int k = A.ptr[i]; k < A.ptr[i + 1]; ++k) if (A.col[k] == i) dinv[i] = 1.0 / A.val[k];
+    x.assign(n, 0.0);
+    double bn = 0; for (double v : b) bn += v * v; bn = std::sqrt(bn);
+    if (bn == 0.0) { if (iters) *iters = 0; return 0; }
+    r = b;
+    for (int i = 0; i < n; ++i) z[i] = dinv[i] * r[i];
+    p = z;
+    double rz = 0; for (int i = 0; i < n; ++i) rz += r[i] * z[i];
+    for (int it = 1; it <= maxit; ++it) {
+        csr_mv(A, p, q);
+        double pq = 0; for (int i = 0; i < n; ++i) pq += p[i] * q[i];
+        if (!(pq > 0)) { if (iters) *iters = it; return SVL_ERR_BREAKDOWN; }
+        double al = rz / pq;
+        for (int i = 0; i < n; ++i) { x[i] += al * p[i]; r[i] -= al * q[i]; }
+        double rn = 0; for (double v : r) rn += v * v;
+        if (std::sqrt(rn) <= rtol * bn) {
+            // confirm with the true residual
+            std::vector<double> Ax; csr_mv(A, x, Ax);
+            double tr = 0; for (int i = 0; i < n; ++i) { double d = b[i] - Ax[i]; tr += d * d; }
+            if (std::sqrt(tr) <= rtol * bn) { if (iters) *iters = it; return 0; }
+            for (int i = 0; i < n; ++i) r[i] = b[i] - Ax[i];
+        }
+        for (int i = 0; i < n; ++i) z[i] = dinv[i] * r[i];
+        double rz2 = 0; for (int i = 0; i < n; ++i) rz2 += r[i] * z[i];
+        double be = rz2 / rz; rz = rz2;
+        for (int i = 0; i < n; ++i) p[i] = z[i] + be * p[i];
+    }
+    if (iters) *iters = maxit;
+    return SVL_ERR_MAXITER;
+}
+
+/* ---------------- Newmark (NewmarkBeta.cpp, beta=1/4, gamma=1/2) -------- */
+
+struct Newmark {
+    Sim s; double dt;
+    std::vector<double> U, V, A, Mfull_diag;
+    CSR Mt;                      // total-dof mass (lumped or consistent)
+    int solver = 0;              // 0 dense LDL^T, 1 Jacobi-PCG
+    double pcg_tol = 1e-12; int pcg_maxit = 100000; long pcg_iters = 0;
+
+    bool init(const svl_model_desc* d, const svl_load_desc* l, double dt_) {
+        if (!s.init(d, l)) return false;
+        dt = dt_;
+        const int nt = s.m.ntotal;
+        U.assign(nt, 0); V.assign(nt, 0); A.assign(nt, 0);
+        // total mass matrix triplets in element order with the mass filter
+        std::vector<Trip> tr;
+        const int nc = s.m.nen * s.m.ndof;
+        std::vector<double> Me((size_t)nc * nc);
+        for (int e = 0; e < s.m.nelem; ++e) {
+            s.element_M(e, Me.data(), s.m.lumped != 0);
+            for (int j = 0; j < nc; ++j)
+                for (int i = 0; i < nc; ++i) {
+                    double v = Me[(size_t)i * nc + j];
+                    if (std::fabs(v) > s.mtol) tr.push_back({s.edofs[(size_t)e * nc + i], s.edofs[(size_t)e * nc + j], v});
+                }
+        }
+        if (!s.m.nodemass.empty())
+            for (int t = 0; t < nt; ++t) if (std::fabs(s.m.nodemass[t]) > s.mtol) tr.push_back({t, t, s.m.nodemass[t]});
+        csr_from_triplets(nt, tr, Mt);
+        return true;
+    }
+    // T^T K T as free-dof CSR
+    void reduce(const std::vector<Trip>& totalTr, CSR& Kff) const {
+        std::vector<Trip> tr;
+        for (const Trip& t : totalTr)
+            for (int i = s.Tptr[t.r]; i < s.Tptr[t.r + 1]; ++i)
+                for (int j = s.Tptr[t.c]; j < s.Tptr[t.c + 1]; ++j)
+                    tr.push_back({s.Tcol[i], s.Tcol[j], s.Tval[i] * t.v * s.Tval[j]});
+        csr_from_triplets(s.m.nfree, tr, Kff);
+    }
+    // Effective stiffness K + 4/dt^2 M (NewmarkBeta.cpp:224-235), C = 0.
+    void keff(CSR& Kff) const {
+        std::vector<Trip> tr;
+        const int nc = s.m.nen * s.m.ndof;
+        std::vector<double> Ke((size_t)nc * nc);
+        for (int e = 0; e < s.m.nelem; ++e) {
+            s.element_K(e, Ke.data());
+            for (int j = 0; j < nc; ++j)
+                for (int i = 0; i < nc; ++i) {
+                    double v = Ke[(size_t)i * nc + j];
+                    if (std::fabs(v) > s.ktol) tr.push_back({s.edofs[(size_t)e * nc + i], s.edofs[(size_t)e * nc + j], v});
+                }
+        }
+        for (int r = 0; r < Mt.n; ++r)
+            for (int i = Mt.ptr[r]; i < Mt.ptr[r + 1]; ++i) tr.push_back({r, Mt.col[i], 4.0 / dt / dt * Mt.val[i]});
+        reduce(tr, Kff);
+    }
+    bool solve(const CSR& K, const std::vector<double>& b, std::vector<double>& x) {
+        if (solver == 0) return dense_ldlt_solve(K, b, x);
+        int it = 0;
+        int st = pcg_solve(K, b, x, pcg_tol, pcg_maxit, &it);
+        pcg_iters += it;
+        return st == 0;
+    }
+    // One NewmarkBeta::ComputeNewStep with Linear (algo 0) or Newton (algo 1).
+    int step(int k, int algo, int maxit, double cnvgtol) {
+        const int nt = s.m.ntotal, nf = s.m.nfree;
+        std::vector<double> dUf(nf, 0.0), du, dUt, Fint, Fext, SM, F(nt), Feff, MV, Us(nt);
+        double norm0 = 0.0;
+        int it = 0;
+        for (;;) {
+            s.T_apply(dUf, dUt);
+            s.assemble_fint(Fint);
+            s.fext(k, Fext);
+            std::vector<double> w(nt);
+            for (int t = 0; t < nt; ++t) w[t] = 4.0 / dt * V[t] + A[t] - 4.0 / dt / dt * dUt[t];
+            csr_mv(Mt, w, MV);
+            // Fext + Fbar - Fint + M*(4/dt V + A - 4/dt^2 dU) (NewmarkBeta.cpp:215)
+            for (int t = 0; t < nt; ++t) F[t] = (Fext[t] + 0.0 - Fint[t]) + MV[t];
+            s.TT_apply(F, Feff);
+            CSR K; keff(K);
+            // support motion term: Feff -= T^T (K_total SM).  K_total SM needs
+            // the total stiffness; restrained rows only couple through K.
+            s.support_increment(k, SM);
+            bool anySM = false; for (double v : SM) if (v != 0.0) { anySM = true; break; }
+            if (anySM) {
+                std::vector<Trip> tr; const int nc = s.m.nen * s.m.ndof;
+                std::vector<double> Ke((size_t)nc * nc);
+                for (int e = 0; e < s.m.nelem; ++e) {
+                    s.element_K(e, Ke.data());
+                    for (int j = 0; j < nc; ++j) for (int i = 0; i < nc; ++i) {
+                        double v = Ke[(size_t)i * nc + j];
+                        if (std::fabs(v) > s.ktol) tr.push_back({s.edofs[(size_t)e * nc + i], s.edofs[(size_t)e * nc + j], v});
+                    }
+                }
+                for (int r = 0; r < Mt.n; ++r) for (int i = Mt.ptr[r]; i < Mt.ptr[r + 1]; ++i) tr.push_back({r, Mt.col[i], 4.0 / dt / dt * Mt.val[i]});
+                CSR Kt; csr_from_triplets(nt, tr, Kt);
+                std::vector<double> KS, lg; csr_mv(Kt, SM, KS); s.TT_apply(KS, lg);
+                for (int f = 0; f < nf; ++f) Feff[f] -= lg[f];
+            }
+            if (!solve(K, Feff, du)) return SVL_ERR_BREAKDOWN;
+            for (int f = 0; f < nf; ++f) dUf[f] += du[f];
+            // convergence (Algorithm.cpp:122-188), test 5 = relative increment
+            double res = 0.0;
+            if (algo == 1) {
+                double dn = 0, Dn = 0;
+                for (int f = 0; f < nf; ++f) { dn += du[f] * du[f]; Dn += dUf[f] * dUf[f]; }
+                dn = std::sqrt(dn); Dn = std::sqrt(Dn);
+                if (it == 0) { norm0 = Dn; res = dn; } else res = dn / norm0;
+            }
+            s.T_apply(dUf, dUt);
+            for (int t = 0; t < nt; ++t) Us[t] = U[t] + dUt[t];
+            for (int e = 0; e < s.m.nelem; ++e) s.element_update(e, Us);
+            ++it;
+            if (algo == 0 || !(res > cnvgtol) || it >= maxit) {
+                // NewmarkBeta::ComputeNewStep (NewmarkBeta.cpp:130-139)
+                for (int t = 0; t < nt; ++t) {
+                    double d = dUt[t];
+                    U[t] += (d + SM[t]);
+                    A[t] = 4.0 / dt / dt * d - 4.0 / dt * V[t] - A[t];
+                    V[t] = 2.0 / dt * d - V[t];
+                }
+                s.commit_all();
+                return 0;
+            }
+        }
+    }
+};
+
+}  // namespace
+
+/* ---------------- C ABI of the oracle ------------------------------------ */
+extern "C" {
+
+/* Central difference run.  hist_U: [nsteps][ntotal] or NULL; V/A out: [ntotal]
+ * or NULL.  mode 0 = reference-faithful single thread, 1 = fast (OpenMP). */
+int oracle_cd_run(const svl_model_desc* model, const svl_load_desc* loads, double dt,
+                  double ftol, double mtol, int k_first, int nsteps, int mode,
+                  const double* U0, const double* V0, const double* A0,
+                  double* hist_U, double* U_out, double* V_out, double* A_out, double* step_seconds) {
+    CD cd;
+    if (!cd.init(model, loads, dt, ftol, mtol)) return SVL_ERR_INVALID;
+    cd.set_initial(U0, V0, A0);
+    if (mode == 1) cd.enable_fast();
+    const int nt = cd.s.m.ntotal;
+    const auto t0 = std::chrono::steady_clock::now();
+    for (int i = 0; i < nsteps; ++i) {
+        cd.step(k_first + i);
+        if (hist_U) std::memcpy(hist_U + (size_t)i * nt, cd.U.data(), sizeof(double) * nt);
+    }
+    if (step_seconds) step_seconds[0] = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    if (U_out) std::memcpy(U_out, cd.U.data(), sizeof(double) * nt);
+    if (V_out) std::memcpy(V_out, cd.V.data(), sizeof(double) * nt);
+    if (A_out) std::memcpy(A_out, cd.A.data(), sizeof(double) * nt);
+    return 0;
+}
+
+/* Newmark (average acceleration) run with Linear (algo 0) or Newton (algo 1)
+ * iterations and a dense LDL^T (solver 0) or Jacobi-PCG (solver 1) solve. */
+int oracle_newmark_run(const svl_model_desc* model, const svl_load_desc* loads, double dt,
+                       int k_first, int nsteps, int algo, int maxit, double cnvgtol,
+                       int solver, double pcg_tol, double* hist_U, long* pcg_iters) {
+    Newmark nm;
+    if (!nm.init(model, loads, dt)) return SVL_ERR_INVALID;
+    nm.solver = solver; nm.pcg_tol = pcg_tol;
+    const int nt = nm.s.m.ntotal;
+    for (int i = 0; i < nsteps; ++i) {
+        int st = nm.step(k_first + i, algo, maxit, cnvgtol);
+        if (st) return st;
+        if (hist_U) std::memcpy(hist_U + (size_t)i * nt, nm.U.data(), sizeof(double) * nt);
+    }
+    if (pcg_iters) *pcg_iters = nm.pcg_iters;
+    return 0;
+}
+
+/* Element-level probes used by the tests. */
+int oracle_element_fint(const svl_model_desc* model, const double* U_total, double* fe_all) {
+    Sim s;
+    if (!s.init(model, nullptr)) return SVL_ERR_INVALID;
+    std::vector<double> U(U_total, U_total + s.m.ntotal);
+    for (int e = 0; e < s.m.nelem; ++e) s.element_update(e, U);
+    const int nc = s.m.nen * s.m.ndof;
+    for (int e = 0; e < s.m.nelem; ++e) s.element_fint(e, fe_all + (size_t)e * nc);
+    return 0;
+}
+
+int oracle_element_matrices(const svl_model_desc* model, int e, double* Ke, double* Me_lumped, double* Me_consistent) {
+    Sim s;
+    if (!s.init(model, nullptr)) return SVL_ERR_INVALID;
+    if (Ke) s.element_K(e, Ke);
+    if (Me_lumped) s.element_M(e, Me_lumped, true);
+    if (Me_consistent) s.element_M(e, Me_consistent, false);
+    return 0;
+}
+
+int oracle_body_force(const svl_model_desc* model, int e, const double* q, double* fe) {
+    Sim s;
+    if (!s.init(model, nullptr)) return SVL_ERR_INVALID;
+    s.element_body(e, q, fe);
+    return 0;
+}
+
+int oracle_lumped_mass(const svl_model_desc* model, double mtol, double* M) {
+    Sim s;
+    if (!s.init(model, nullptr)) return SVL_ERR_INVALID;
+    s.mtol = mtol;
+    std::vector<double> Md;
+    s.assemble_mass_diag(Md);
+    std::memcpy(M, Md.data(), sizeof(double) * Md.size());
+    return 0;
+}
+
+/* Single Gauss-point J2 driver: applies `n` strain increments (engineering
+ * strain rows of size 3 or 6) with a commit after each, returning the stress
+ * after each increment. */
+int oracle_j2_path(int mat_type, const double* param, int n, const double* strains, double* stresses) {
+    MatState s; mat_init(s, mat_type, param);
+    const int ns = (mat_type == SVL_MAT_PLASTICPLANESTRAINJ2 || mat_type == SVL_MAT_ELASTIC2DPLANESTRAIN) ? 3 : 6;
+    for (int i = 0; i < n; ++i) {
+        mat_update(s, mat_type, param, strains + (size_t)i * ns);
+        mat_stress(s, mat_type, param, stresses + (size_t)i * ns);
+        mat_commit(s);
+    }
+    return 0;
+}
+
+int oracle_num_threads(void) {
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+}  // extern "C"

@@ -1,0 +1,12 @@
+"""svl_gb300: GB300-native (sm_103a) time-stepping hot path of SeismoVLAB.
+
+The product is the C-ABI library svl_gb300/lib/libsvl_gb300.so (CUDA kernels
+and C++ host code, declared in include/svl_gb300.h).  This package is its
+Python binding: model/load containers, the structured-grid generator, and a
+mirror of the reference's Integrator interface.
+"""
+from ._capi import SvlError, lib  # noqa: F401
+from .integrators import CentralDifference  # noqa: F401
+from .model import Loads, Model, elastic_params, j2_params, ricker  # noqa: F401
+
+__all__ = ["CentralDifference", "Loads", "Model", "SvlError", "lib", "ricker", "elastic_params", "j2_params"]

@@ -1,0 +1,145 @@
+"""ctypes view of include/svl_gb300.h.
+
+This is the Python-side binding of the C ABI (the same binding a reference
+maintainer would add with ctypes).  The library must have been built in-tree
+(`__graft_entry__.build()`); loading fails loudly otherwise -- there is no CPU
+fallback in the product path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+LIB_PATH = Path(__file__).resolve().parent / "lib" / "libsvl_gb300.so"
+
+SVL_OK = 0
+SVL_ERR_INVALID = 1
+SVL_ERR_CUDA = 2
+SVL_ERR_NONFINITE = 3
+SVL_ERR_MAXITER = 4
+SVL_ERR_BREAKDOWN = 5
+SVL_ERR_UNSUPPORTED = 6
+SVL_ERR_NOMEM = 7
+SVL_ERR_NODEVICE = 8
+
+SVL_ELEM_LIN2DQUAD4 = 1
+SVL_ELEM_LIN3DHEXA8 = 2
+
+SVL_MAT_ELASTIC2DPLANESTRAIN = 1
+SVL_MAT_ELASTIC3DLINEAR = 2
+SVL_MAT_PLASTICPLANESTRAINJ2 = 3
+SVL_MAT_PLASTIC3DJ2 = 4
+SVL_MAT_NPARAM = 8
+
+SVL_PREC_FP64 = 0
+SVL_PREC_MIXED = 1
+
+i32p = C.POINTER(C.c_int32)
+f64p = C.POINTER(C.c_double)
+
+
+class ModelDesc(C.Structure):
+    _fields_ = [
+        ("ndim", C.c_int32), ("nnode", C.c_int32), ("ndof", C.c_int32),
+        ("coords", f64p), ("totaldof", i32p), ("freedof", i32p),
+        ("ntotal", C.c_int32), ("nfree", C.c_int32),
+        ("nconstraint", C.c_int32), ("con_slave", i32p), ("con_ptr", i32p),
+        ("con_master", i32p), ("con_factor", f64p),
+        ("elem_type", C.c_int32), ("nelem", C.c_int32), ("conn", i32p),
+        ("elem_mat", i32p), ("elem_thickness", f64p),
+        ("nmat", C.c_int32), ("mat_type", i32p), ("mat_param", f64p),
+        ("lumped", C.c_int32), ("node_mass", f64p),
+    ]
+
+
+class LoadDesc(C.Structure):
+    _fields_ = [
+        ("nseries", C.c_int32), ("series_ptr", i32p), ("series_val", f64p),
+        ("nforce", C.c_int32), ("force_dof", i32p), ("force_series", i32p), ("force_coef", f64p),
+        ("nsupport", C.c_int32), ("sm_dof", i32p), ("sm_series", i32p), ("sm_factor", f64p),
+    ]
+
+
+class GridSpec(C.Structure):
+    _fields_ = [
+        ("ndim", C.c_int32), ("ne", C.c_int32 * 3), ("h", C.c_double * 3),
+        ("origin", C.c_double * 3), ("fix_mask", C.c_int32 * 6), ("periodic_x", C.c_int32),
+    ]
+
+
+class CdOpts(C.Structure):
+    _fields_ = [("dt", C.c_double), ("ftol", C.c_double), ("mtol", C.c_double),
+                ("precision", C.c_int32), ("check_every", C.c_int32)]
+
+
+def ptr(a, ctype):
+    """Pointer to a contiguous numpy array (None -> NULL)."""
+    if a is None:
+        return C.cast(None, C.POINTER(ctype))
+    assert a.flags["C_CONTIGUOUS"], "array must be C-contiguous"
+    return a.ctypes.data_as(C.POINTER(ctype))
+
+
+_lib = None
+
+
+class SvlError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("svl status %d: %s" % (code, msg))
+        self.code = code
+
+
+def lib():
+    """Load libsvl_gb300.so (raises if it was not built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        raise RuntimeError("libsvl_gb300.so is missing (%s); run __graft_entry__.build()" % LIB_PATH)
+    L = C.CDLL(str(LIB_PATH))
+    L.svl_version.restype = C.c_char_p
+    L.svl_last_error.restype = C.c_char_p
+    L.svl_device_info.argtypes = [C.POINTER(C.c_int)] * 4
+    L.svl_set_device.argtypes = [C.c_int]
+    L.svl_grid_sizes.argtypes = [C.POINTER(GridSpec)] + [C.POINTER(C.c_int32)] * 5
+    L.svl_grid_build.argtypes = [C.POINTER(GridSpec), f64p, i32p, i32p, i32p, i32p, i32p, i32p, f64p]
+    L.svl_element_body_force.argtypes = [C.POINTER(ModelDesc), C.c_int32, f64p, f64p]
+    L.svl_lumped_mass.argtypes = [C.POINTER(ModelDesc), C.c_double, f64p]
+    L.svl_cd_create.argtypes = [C.POINTER(ModelDesc), C.POINTER(LoadDesc), C.POINTER(CdOpts), C.POINTER(C.c_void_p)]
+    L.svl_cd_set_initial.argtypes = [C.c_void_p, f64p, f64p, f64p]
+    L.svl_cd_run.argtypes = [C.c_void_p, C.c_int32, C.c_int32, f64p]
+    L.svl_cd_get.argtypes = [C.c_void_p, C.c_int32, f64p]
+    L.svl_cd_device_ptr.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_void_p)]
+    L.svl_cd_launch_count.argtypes = [C.c_void_p, C.POINTER(C.c_int64)]
+    L.svl_cd_sync.argtypes = [C.c_void_p]
+    L.svl_cd_run_timed.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(C.c_float)]
+    L.svl_cd_profile.argtypes = [C.c_void_p, C.c_int32, C.c_int32, f64p]
+    L.svl_cd_destroy.argtypes = [C.c_void_p]
+    L.svl_cd_destroy.restype = None
+    _lib = L
+    return L
+
+
+def check(code):
+    if code != SVL_OK:
+        raise SvlError(code, lib().svl_last_error().decode())
+    return code
+
+
+def exported_symbols():
+    """Names declared in include/svl_gb300.h (for the export test)."""
+    import re
+    hdr = Path(__file__).resolve().parent.parent / "include" / "svl_gb300.h"
+    names = re.findall(r"^\s*(?:const\s+)?[A-Za-z_][A-Za-z0-9_]*\s*\**\s*(svl_[a-z0-9_]+)\s*\(",
+                       hdr.read_text(), flags=re.M)
+    return sorted(set(names))
+
+
+def as_f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def as_i32(a):
+    return np.ascontiguousarray(a, dtype=np.int32)

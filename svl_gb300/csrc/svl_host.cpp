@@ -1,0 +1,396 @@
+// Host-side pieces of the C ABI: model validation, element geometry,
+// lumped mass, the T operator, the structured-grid generator with the
+// pre-processor's PlainScheme numbering, and element body loads.
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <utility>
+
+#include "svl_internal.hpp"
+
+namespace svl {
+
+static thread_local char g_err[1024] = "";
+
+void set_error(const char* fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    std::vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+}
+
+bool HostModel::has_j2() const {
+    for (int t : mtype)
+        if (t == SVL_MAT_PLASTICPLANESTRAINJ2 || t == SVL_MAT_PLASTIC3DJ2) return true;
+    return false;
+}
+
+bool model_from_desc(const svl_model_desc* d, HostModel& m) {
+    if (!d) { set_error("model descriptor is NULL"); return false; }
+    m.ndim = d->ndim; m.nnode = d->nnode; m.ndof = d->ndof;
+    m.ntotal = d->ntotal; m.nfree = d->nfree; m.etype = d->elem_type;
+    m.nelem = d->nelem; m.nmat = d->nmat;
+    if (m.etype == SVL_ELEM_LIN2DQUAD4) { m.nen = 4; m.ngp = 4; m.nstr = 3; }
+    else if (m.etype == SVL_ELEM_LIN3DHEXA8) { m.nen = 8; m.ngp = 8; m.nstr = 6; }
+    else { set_error("unsupported element type %d", m.etype); return false; }
+    if ((m.etype == SVL_ELEM_LIN2DQUAD4 && m.ndim != 2) || (m.etype == SVL_ELEM_LIN3DHEXA8 && m.ndim != 3)) {
+        set_error("element type %d does not match ndim %d", m.etype, m.ndim); return false;
+    }
+    if (m.ndof != m.ndim) { set_error("ndof (%d) must equal ndim (%d) for solid elements", m.ndof, m.ndim); return false; }
+    if (m.nnode <= 0 || m.nelem <= 0 || m.ntotal <= 0 || m.nfree < 0 || m.nmat <= 0) {
+        set_error("empty model (nnode=%d nelem=%d ntotal=%d nfree=%d nmat=%d)", m.nnode, m.nelem, m.ntotal, m.nfree, m.nmat);
+        return false;
+    }
+    if (!d->coords || !d->totaldof || !d->freedof || !d->conn || !d->elem_mat || !d->mat_type || !d->mat_param) {
+        set_error("model descriptor has a NULL array"); return false;
+    }
+    m.X.assign(d->coords, d->coords + (size_t)m.nnode * m.ndim);
+    m.tdof.assign(d->totaldof, d->totaldof + (size_t)m.nnode * m.ndof);
+    m.fdof.assign(d->freedof, d->freedof + (size_t)m.nnode * m.ndof);
+    m.conn.assign(d->conn, d->conn + (size_t)m.nelem * m.nen);
+    m.emat.assign(d->elem_mat, d->elem_mat + m.nelem);
+    m.thick.assign(m.nelem, 1.0);
+    if (d->elem_thickness) m.thick.assign(d->elem_thickness, d->elem_thickness + m.nelem);
+    m.mtype.assign(d->mat_type, d->mat_type + m.nmat);
+    m.mpar.assign(d->mat_param, d->mat_param + (size_t)m.nmat * SVL_MAT_NPARAM);
+    m.nodemass.clear();
+    if (d->node_mass) m.nodemass.assign(d->node_mass, d->node_mass + m.ntotal);
+    m.lumped = d->lumped;
+    m.nconstraint = d->nconstraint;
+    m.cslave.clear(); m.cptr.assign(1, 0); m.cmaster.clear(); m.cfactor.clear();
+    if (m.nconstraint > 0) {
+        if (!d->con_slave || !d->con_ptr || !d->con_master || !d->con_factor) { set_error("constraint arrays are NULL"); return false; }
+        m.cslave.assign(d->con_slave, d->con_slave + m.nconstraint);
+        m.cptr.assign(d->con_ptr, d->con_ptr + m.nconstraint + 1);
+        if (m.cptr[0] != 0) { set_error("con_ptr[0] must be 0"); return false; }
+        for (int c = 0; c < m.nconstraint; ++c)
+            if (m.cptr[c + 1] < m.cptr[c]) { set_error("con_ptr is not monotone"); return false; }
+        m.cmaster.assign(d->con_master, d->con_master + m.cptr.back());
+        m.cfactor.assign(d->con_factor, d->con_factor + m.cptr.back());
+        for (int c = 0; c < m.nconstraint; ++c)
+            if (m.cslave[c] < 0 || m.cslave[c] >= m.ntotal) { set_error("constraint %d slave dof out of range", c); return false; }
+        for (int32_t f : m.cmaster)
+            if (f < 0 || f >= m.nfree) { set_error("constraint master dof %d out of range", f); return false; }
+    }
+    // index checks: every later device access is bounded by these
+    for (int32_t n : m.conn) if (n < 0 || n >= m.nnode) { set_error("connectivity node %d out of range", n); return false; }
+    for (int32_t k : m.emat) if (k < 0 || k >= m.nmat) { set_error("element material %d out of range", k); return false; }
+    for (int32_t t : m.tdof) if (t < 0 || t >= m.ntotal) { set_error("total dof %d out of range", t); return false; }
+    {
+        std::vector<char> seen(m.ntotal, 0);
+        for (int32_t t : m.tdof) { if (seen[t]) { set_error("total dof %d appears twice", t); return false; } seen[t] = 1; }
+        std::vector<char> fseen(m.nfree, 0);
+        for (int32_t f : m.fdof) {
+            if (f >= m.nfree) { set_error("free dof %d out of range", f); return false; }
+            if (f >= 0) { if (fseen[f]) { set_error("free dof %d appears twice", f); return false; } fseen[f] = 1; }
+        }
+    }
+    for (int k = 0; k < m.nmat; ++k) {
+        int t = m.mtype[k];
+        bool two = (t == SVL_MAT_ELASTIC2DPLANESTRAIN || t == SVL_MAT_PLASTICPLANESTRAINJ2);
+        bool three = (t == SVL_MAT_ELASTIC3DLINEAR || t == SVL_MAT_PLASTIC3DJ2);
+        if (!(two || three)) { set_error("unsupported material type %d", t); return false; }
+        if ((m.ndim == 2) != two) { set_error("material %d (type %d) does not match ndim %d", k, t, m.ndim); return false; }
+    }
+    return true;
+}
+
+static void natural_derivs(int nd, const double* xi, double dN[8][3], double N[8]) {
+    if (nd == 2) {
+        static const double sr[4] = {-1, 1, 1, -1}, ss[4] = {-1, -1, 1, 1};
+        for (int a = 0; a < 4; ++a) {
+            N[a] = 0.25 * (1.0 + sr[a] * xi[0]) * (1.0 + ss[a] * xi[1]);
+            dN[a][0] = 0.25 * sr[a] * (1.0 + ss[a] * xi[1]);
+            dN[a][1] = 0.25 * ss[a] * (1.0 + sr[a] * xi[0]);
+            dN[a][2] = 0.0;
+        }
+    } else {
+        static const double sr[8] = {-1, 1, 1, -1, -1, 1, 1, -1};
+        static const double ss[8] = {-1, -1, 1, 1, -1, -1, 1, 1};
+        static const double st[8] = {-1, -1, -1, -1, 1, 1, 1, 1};
+        for (int a = 0; a < 8; ++a) {
+            const double fr = 1.0 + sr[a] * xi[0], fs = 1.0 + ss[a] * xi[1], ft = 1.0 + st[a] * xi[2];
+            N[a] = 0.125 * fr * fs * ft;
+            dN[a][0] = 0.125 * sr[a] * fs * ft;
+            dN[a][1] = 0.125 * ss[a] * fr * ft;
+            dN[a][2] = 0.125 * st[a] * fr * fs;
+        }
+    }
+}
+
+double gp_geometry(const HostModel& m, int e, int q, double dNx[8][3], double N[8]) {
+    const int nd = m.ndim, nen = m.nen;
+    double xi[3] = {(q & 1) ? kGaussAbscissa : -kGaussAbscissa,
+                    (q & 2) ? kGaussAbscissa : -kGaussAbscissa,
+                    (q & 4) ? kGaussAbscissa : -kGaussAbscissa};
+    if (nd == 2) xi[2] = 0.0;
+    double dN[8][3];
+    natural_derivs(nd, xi, dN, N);
+    // J_ij = d x_j / d r_i
+    double J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    for (int a = 0; a < nen; ++a) {
+        const double* x = &m.X[(size_t)m.conn[(size_t)e * nen + a] * nd];
+        for (int i = 0; i < nd; ++i)
+            for (int j = 0; j < nd; ++j) J[i][j] += dN[a][i] * x[j];
+    }
+    double det, Ji[3][3];
+    if (nd == 2) {
+        det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+        Ji[0][0] = J[1][1] / det; Ji[0][1] = -J[0][1] / det;
+        Ji[1][0] = -J[1][0] / det; Ji[1][1] = J[0][0] / det;
+    } else {
+        const double c00 = J[1][1] * J[2][2] - J[1][2] * J[2][1];
+        const double c01 = J[1][2] * J[2][0] - J[1][0] * J[2][2];
+        const double c02 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+        det = J[0][0] * c00 + J[0][1] * c01 + J[0][2] * c02;
+        Ji[0][0] = c00 / det;
+        Ji[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) / det;
+        Ji[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) / det;
+        Ji[1][0] = c01 / det;
+        Ji[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) / det;
+        Ji[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) / det;
+        Ji[2][0] = c02 / det;
+        Ji[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) / det;
+        Ji[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) / det;
+    }
+    for (int a = 0; a < nen; ++a)
+        for (int j = 0; j < nd; ++j) {
+            double v = 0.0;
+            for (int i = 0; i < nd; ++i) v += Ji[j][i] * dN[a][i];
+            dNx[a][j] = v;
+        }
+    if (nd == 2)
+        for (int a = 0; a < nen; ++a) dNx[a][2] = 0.0;
+    return det;
+}
+
+void lumped_mass_diag(const HostModel& m, double mtol, std::vector<double>& M) {
+    const int nd = m.ndim, nen = m.nen, nc = nen * m.ndof;
+    std::vector<double> Me_e(m.ntotal, 0.0);
+    std::vector<double> Me((size_t)nc * nc);
+    for (int e = 0; e < m.nelem; ++e) {
+        std::fill(Me.begin(), Me.end(), 0.0);
+        const double rho = m.param(e)[2];
+        for (int q = 0; q < m.ngp; ++q) {
+            double dNx[8][3], N[8];
+            const double det = gp_geometry(m, e, q, dNx, N);
+            const double c = nd == 2 ? 1.0 * rho * m.thick[e] * std::fabs(det) : 1.0 * rho * std::fabs(det);
+            for (int a = 0; a < nen; ++a)
+                for (int b = 0; b < nen; ++b)
+                    for (int j = 0; j < nd; ++j) Me[(size_t)(a * nd + j) * nc + (b * nd + j)] += c * (N[a] * N[b]);
+        }
+        // row-sum lumping (lin2DQuad4.cpp:272-282)
+        for (int i = 0; i < nc; ++i)
+            for (int j = 0; j < nc; ++j)
+                if (i != j) { Me[(size_t)i * nc + i] += Me[(size_t)i * nc + j]; Me[(size_t)i * nc + j] = 0.0; }
+        for (int a = 0; a < nen; ++a)
+            for (int j = 0; j < nd; ++j) {
+                const int i = a * nd + j;
+                const double v = Me[(size_t)i * nc + i];
+                if (std::fabs(v) > mtol) Me_e[m.tdof[(size_t)m.conn[(size_t)e * nen + a] * m.ndof + j]] += v;
+            }
+    }
+    M.assign(m.ntotal, 0.0);
+    for (int t = 0; t < m.ntotal; ++t) {
+        double mn = 0.0;
+        if (!m.nodemass.empty() && std::fabs(m.nodemass[t]) > mtol) mn = m.nodemass[t];
+        M[t] = Me_e[t] + mn;
+    }
+}
+
+void build_total_to_free(const HostModel& m, std::vector<int32_t>& ptr,
+                         std::vector<int32_t>& col, std::vector<double>& val) {
+    std::vector<std::vector<std::pair<int32_t, double>>> rows(m.ntotal);
+    for (int n = 0; n < m.nnode; ++n)
+        for (int j = 0; j < m.ndof; ++j) {
+            const int32_t f = m.fdof[(size_t)n * m.ndof + j];
+            if (f > -1) rows[m.tdof[(size_t)n * m.ndof + j]].push_back({f, 1.0});
+        }
+    for (int c = 0; c < m.nconstraint; ++c)
+        for (int i = m.cptr[c]; i < m.cptr[c + 1]; ++i) rows[m.cslave[c]].push_back({m.cmaster[i], m.cfactor[i]});
+    ptr.assign(m.ntotal + 1, 0);
+    col.clear(); val.clear();
+    for (int t = 0; t < m.ntotal; ++t) {
+        std::sort(rows[t].begin(), rows[t].end(),
+                  [](const std::pair<int32_t, double>& a, const std::pair<int32_t, double>& b) { return a.first < b.first; });
+        for (size_t i = 0; i < rows[t].size(); ++i) {
+            if (!col.empty() && (int)col.size() > ptr[t] && col.back() == rows[t][i].first) val.back() += rows[t][i].second;
+            else { col.push_back(rows[t][i].first); val.push_back(rows[t][i].second); }
+        }
+        ptr[t + 1] = (int32_t)col.size();
+    }
+}
+
+}  // namespace svl
+
+using namespace svl;
+
+extern "C" {
+
+const char* svl_version(void) { return "svl_gb300 0.1.0 (sm_103a)"; }
+const char* svl_last_error(void) { return g_err; }
+
+/* ---- structured grid ---------------------------------------------------- */
+
+static bool grid_check(const svl_grid_spec* s) {
+    if (!s) { set_error("grid spec is NULL"); return false; }
+    if (s->ndim != 2 && s->ndim != 3) { set_error("grid ndim must be 2 or 3"); return false; }
+    for (int i = 0; i < s->ndim; ++i)
+        if (s->ne[i] <= 0) { set_error("grid ne[%d] must be positive", i); return false; }
+    double nn = 1.0;
+    for (int i = 0; i < s->ndim; ++i) nn *= (s->ne[i] + 1.0);
+    if (nn * s->ndim > 2.0e9) { set_error("grid too large for 32-bit dof numbers"); return false; }
+    return true;
+}
+
+int svl_grid_sizes(const svl_grid_spec* s, int32_t* nnode, int32_t* nelem, int32_t* ntotal, int32_t* nfree, int32_t* ncon) {
+    if (!grid_check(s)) return SVL_ERR_INVALID;
+    const int nd = s->ndim;
+    const int nx = s->ne[0], ny = s->ne[1], nz = nd == 3 ? s->ne[2] : 0;
+    const int64_t nn = (int64_t)(nx + 1) * (ny + 1) * (nd == 3 ? nz + 1 : 1);
+    const int64_t ne = (int64_t)nx * ny * (nd == 3 ? nz : 1);
+    // count restrained / constrained dofs by building the masks
+    int64_t nr = 0, nc = 0;
+    for (int64_t n = 0; n < nn; ++n) {
+        const int i = (int)(n % (nx + 1));
+        const int j = (int)((n / (nx + 1)) % (ny + 1));
+        const int k = nd == 3 ? (int)(n / ((int64_t)(nx + 1) * (ny + 1))) : 0;
+        int mask = 0;
+        if (i == 0) mask |= s->fix_mask[0];
+        if (i == nx) mask |= s->fix_mask[1];
+        if (j == 0) mask |= s->fix_mask[2];
+        if (j == ny) mask |= s->fix_mask[3];
+        if (nd == 3 && k == 0) mask |= s->fix_mask[4];
+        if (nd == 3 && k == nz) mask |= s->fix_mask[5];
+        for (int d = 0; d < nd; ++d) {
+            if (mask & (1 << d)) ++nr;
+            else if (s->periodic_x && i == nx) ++nc;
+        }
+    }
+    if (nnode) *nnode = (int32_t)nn;
+    if (nelem) *nelem = (int32_t)ne;
+    if (ntotal) *ntotal = (int32_t)(nn * nd);
+    if (nfree) *nfree = (int32_t)(nn * nd - nr - nc);
+    if (ncon) *ncon = (int32_t)nc;
+    return SVL_OK;
+}
+
+int svl_grid_build(const svl_grid_spec* s, double* coords, int32_t* totaldof, int32_t* freedof,
+                   int32_t* conn, int32_t* con_slave, int32_t* con_ptr, int32_t* con_master, double* con_factor) {
+    if (!grid_check(s)) return SVL_ERR_INVALID;
+    if (!coords || !totaldof || !freedof || !conn) { set_error("grid output array is NULL"); return SVL_ERR_INVALID; }
+    const int nd = s->ndim;
+    const int nx = s->ne[0], ny = s->ne[1], nz = nd == 3 ? s->ne[2] : 0;
+    const int64_t nn = (int64_t)(nx + 1) * (ny + 1) * (nd == 3 ? nz + 1 : 1);
+    const double hx = s->h[0], hy = s->h[1], hz = nd == 3 ? s->h[2] : 0.0;
+    // Builder.py: coords = P0 + i*DX + j*DY + k*DZ, node tags x-fastest
+    for (int64_t n = 0; n < nn; ++n) {
+        const int i = (int)(n % (nx + 1));
+        const int j = (int)((n / (nx + 1)) % (ny + 1));
+        const int k = nd == 3 ? (int)(n / ((int64_t)(nx + 1) * (ny + 1))) : 0;
+        coords[n * nd + 0] = s->origin[0] + i * hx;
+        coords[n * nd + 1] = s->origin[1] + j * hy;
+        if (nd == 3) coords[n * nd + 2] = s->origin[2] + k * hz;
+    }
+    // Restraints mark freedof = -1, periodic x-max dofs get constraint tags
+    // -2, -3, ... in ascending node order (dof-minor); PlainScheme then
+    // numbers total dofs consecutively and free dofs over the unmarked ones
+    // (Numberer.py:185-233).
+    int32_t ncount = 0, tcount = 0, fcount = 0;
+    std::vector<int64_t> slave_nodes; std::vector<int> slave_dofs;
+    for (int64_t n = 0; n < nn; ++n) {
+        const int i = (int)(n % (nx + 1));
+        const int j = (int)((n / (nx + 1)) % (ny + 1));
+        const int k = nd == 3 ? (int)(n / ((int64_t)(nx + 1) * (ny + 1))) : 0;
+        int mask = 0;
+        if (i == 0) mask |= s->fix_mask[0];
+        if (i == nx) mask |= s->fix_mask[1];
+        if (j == 0) mask |= s->fix_mask[2];
+        if (j == ny) mask |= s->fix_mask[3];
+        if (nd == 3 && k == 0) mask |= s->fix_mask[4];
+        if (nd == 3 && k == nz) mask |= s->fix_mask[5];
+        for (int d = 0; d < nd; ++d) {
+            totaldof[n * nd + d] = tcount++;
+            if (mask & (1 << d)) freedof[n * nd + d] = -1;
+            else if (s->periodic_x && i == nx) {
+                freedof[n * nd + d] = -2 - ncount;
+                slave_nodes.push_back(n); slave_dofs.push_back(d);
+                ++ncount;
+            } else freedof[n * nd + d] = fcount++;
+        }
+    }
+    if (ncount > 0) {
+        if (!con_slave || !con_ptr || !con_master || !con_factor) { set_error("constraint output arrays are NULL"); return SVL_ERR_INVALID; }
+        con_ptr[0] = 0;
+        for (int c = 0; c < ncount; ++c) {
+            const int64_t n = slave_nodes[c];
+            const int d = slave_dofs[c];
+            const int64_t master = n - nx;   // same row, i = 0
+            con_slave[c] = totaldof[n * nd + d];
+            con_master[c] = freedof[master * nd + d];
+            con_factor[c] = 1.0;
+            con_ptr[c + 1] = c + 1;
+            if (con_master[c] < 0) { set_error("periodic master dof of node %lld is not free", (long long)master); return SVL_ERR_INVALID; }
+        }
+    }
+    // connectivity (Builder.py:167-183 for Hexa8; Quad4 analogous)
+    int64_t e = 0;
+    if (nd == 2) {
+        for (int j = 0; j < ny; ++j)
+            for (int i = 0; i < nx; ++i, ++e) {
+                const int32_t n1 = j * (nx + 1) + i;
+                conn[e * 4 + 0] = n1;
+                conn[e * 4 + 1] = n1 + 1;
+                conn[e * 4 + 2] = n1 + 1 + (nx + 1);
+                conn[e * 4 + 3] = n1 + (nx + 1);
+            }
+    } else {
+        const int64_t layer = (int64_t)(nx + 1) * (ny + 1);
+        for (int k = 0; k < nz; ++k)
+            for (int j = 0; j < ny; ++j)
+                for (int i = 0; i < nx; ++i, ++e) {
+                    const int64_t n1 = layer * k + (int64_t)j * (nx + 1) + i;
+                    conn[e * 8 + 0] = (int32_t)n1;
+                    conn[e * 8 + 1] = (int32_t)(n1 + 1);
+                    conn[e * 8 + 2] = (int32_t)(n1 + 1 + (nx + 1));
+                    conn[e * 8 + 3] = (int32_t)(n1 + (nx + 1));
+                    conn[e * 8 + 4] = (int32_t)(n1 + layer);
+                    conn[e * 8 + 5] = (int32_t)(n1 + layer + 1);
+                    conn[e * 8 + 6] = (int32_t)(n1 + layer + 1 + (nx + 1));
+                    conn[e * 8 + 7] = (int32_t)(n1 + layer + (nx + 1));
+                }
+    }
+    return SVL_OK;
+}
+
+int svl_element_body_force(const svl_model_desc* d, int32_t elem, const double* q, double* fe) {
+    HostModel m;
+    if (!model_from_desc(d, m)) return SVL_ERR_INVALID;
+    if (elem < 0 || elem >= m.nelem || !q || !fe) { set_error("bad element index or NULL array"); return SVL_ERR_INVALID; }
+    const int nd = m.ndim, nen = m.nen;
+    for (int i = 0; i < nen * nd; ++i) fe[i] = 0.0;
+    const double rho = m.param(elem)[2];
+    for (int g = 0; g < m.ngp; ++g) {
+        double dNx[8][3], N[8];
+        const double det = gp_geometry(m, elem, g, dNx, N);
+        const double c = nd == 2 ? 1.0 * rho * m.thick[elem] * std::fabs(det) : 1.0 * rho * std::fabs(det);
+        for (int a = 0; a < nen; ++a)
+            for (int j = 0; j < nd; ++j) fe[a * nd + j] += c * (N[a] * q[j]);
+    }
+    return SVL_OK;
+}
+
+int svl_lumped_mass(const svl_model_desc* d, double mtol, double* mass_total) {
+    HostModel m;
+    if (!model_from_desc(d, m)) return SVL_ERR_INVALID;
+    if (!mass_total) { set_error("output is NULL"); return SVL_ERR_INVALID; }
+    std::vector<double> M;
+    lumped_mass_diag(m, mtol, M);
+    std::memcpy(mass_total, M.data(), sizeof(double) * M.size());
+    return SVL_OK;
+}
+
+}  // extern "C"

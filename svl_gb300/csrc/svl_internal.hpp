@@ -1,0 +1,57 @@
+// Internal host-side model representation shared by the C-ABI translation
+// units.  Not installed; the public interface is include/svl_gb300.h.
+#pragma once
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/svl_gb300.h"
+
+namespace svl {
+
+void set_error(const char* fmt, ...);
+
+// Gauss abscissa of the 2x2 / 2x2x2 rules, truncated to 15 digits exactly as
+// RP/04-Elements/11-Integration/GaussQuadrature.cpp:303-316 tabulates it.
+constexpr double kGaussAbscissa = 0.577350269189626;
+
+struct HostModel {
+    int ndim = 0, nnode = 0, ndof = 0, ntotal = 0, nfree = 0;
+    int etype = 0, nelem = 0, nen = 0, ngp = 0, nstr = 0, nmat = 0;
+    std::vector<double> X;
+    std::vector<int32_t> tdof, fdof, conn, emat;
+    std::vector<double> thick;
+    std::vector<int32_t> mtype;
+    std::vector<double> mpar;
+    std::vector<double> nodemass;
+    int nconstraint = 0;
+    std::vector<int32_t> cslave, cptr, cmaster;
+    std::vector<double> cfactor;
+    int lumped = 1;
+
+    bool has_j2() const;
+    const double* param(int e) const { return &mpar[(size_t)emat[e] * SVL_MAT_NPARAM]; }
+    int mat_type(int e) const { return mtype[emat[e]]; }
+};
+
+// Validates a descriptor and copies it; returns false with svl_last_error set.
+bool model_from_desc(const svl_model_desc* d, HostModel& m);
+
+// Physical shape-function derivatives dN_a/dx_j, shape values N_a and the
+// Jacobian determinant at Gauss point q of element e.  Same kinematics as
+// lin2DQuad4.cpp:648-710 and lin3DHexa8.cpp:756-853.
+double gp_geometry(const HostModel& m, int e, int q, double dNx[8][3], double N[8]);
+
+// Integration factor w * t * |detJ| (2D) or w * |detJ| (3D), w = 1.
+inline double gp_factor(const HostModel& m, int e, double det) {
+    return m.ndim == 2 ? 1.0 * m.thick[e] * (det < 0 ? -det : det) : 1.0 * (det < 0 ? -det : det);
+}
+
+// Diagonal of the assembled row-sum-lumped mass on total dofs.
+void lumped_mass_diag(const HostModel& m, double mtol, std::vector<double>& M);
+
+// T (total <- free) rows as CSR over total dofs, sorted columns, duplicates summed.
+void build_total_to_free(const HostModel& m, std::vector<int32_t>& ptr,
+                         std::vector<int32_t>& col, std::vector<double>& val);
+
+}  // namespace svl

@@ -1,0 +1,92 @@
+"""Python mirror of the reference's Integrator interface over the C ABI.
+
+`CentralDifference` stands in for RP/10-Integrators/02-CentralDifference
+(CentralDifference.hpp) driven by the Linear algorithm with the diagonal
+EigenSolver solve: Initialize / ComputeNewStep(k) -> stop flag /
+GetDisplacements / GetVelocities / GetAccelerations keep the reference's
+names and meaning; `run` advances many steps in one call (device-resident).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _capi as capi
+from ._capi import check, lib, ptr
+from .model import Loads, Model
+
+
+class CentralDifference:
+    def __init__(self, model: Model, loads: Loads | None, dt: float, ftol: float = 1e-12,
+                 mtol: float = 1e-12, check_every: int = 0):
+        self.model = model
+        self.dt = float(dt)
+        self._md = model.desc()
+        self._ld = (loads or Loads()).desc()
+        opts = capi.CdOpts(dt=self.dt, ftol=ftol, mtol=mtol, precision=capi.SVL_PREC_FP64,
+                           check_every=check_every)
+        h = C.c_void_p()
+        check(lib().svl_cd_create(C.byref(self._md), C.byref(self._ld), C.byref(opts), C.byref(h)))
+        self._h = h
+        self.ntotal = model.ntotal
+
+    # -- reference-style interface --------------------------------------
+    def Initialize(self, U0=None, V0=None, A0=None):
+        arrs = [None if a is None else capi.as_f64(a) for a in (U0, V0, A0)]
+        check(lib().svl_cd_set_initial(self._h, *(ptr(a, C.c_double) for a in arrs)))
+
+    def ComputeNewStep(self, k: int) -> bool:
+        """One step k; returns True on failure (the reference's `stop`)."""
+        return lib().svl_cd_run(self._h, int(k), 1, ptr(None, C.c_double)) != capi.SVL_OK
+
+    def GetDisplacements(self) -> np.ndarray:
+        return self._get(0)
+
+    def GetVelocities(self) -> np.ndarray:
+        return self._get(1)
+
+    def GetAccelerations(self) -> np.ndarray:
+        return self._get(2)
+
+    # -- batch interface -------------------------------------------------
+    def run(self, k_first: int, nsteps: int, history: bool = False):
+        hist = np.zeros((nsteps, self.ntotal)) if history else None
+        check(lib().svl_cd_run(self._h, int(k_first), int(nsteps), ptr(hist, C.c_double)))
+        return hist
+
+    def run_timed(self, k_first: int, nsteps: int) -> float:
+        """Device time (ms) of nsteps, CUDA events on the handle's stream."""
+        ms = C.c_float()
+        check(lib().svl_cd_run_timed(self._h, int(k_first), int(nsteps), C.byref(ms)))
+        return float(ms.value)
+
+    def profile(self, k_first: int, nsteps: int) -> np.ndarray:
+        """Per-kernel-kind device time (ms) summed over nsteps."""
+        out = np.zeros(5)
+        check(lib().svl_cd_profile(self._h, int(k_first), int(nsteps), ptr(out, C.c_double)))
+        return out
+
+    def launches(self) -> int:
+        n = C.c_int64()
+        check(lib().svl_cd_launch_count(self._h, C.byref(n)))
+        return int(n.value)
+
+    def sync(self):
+        check(lib().svl_cd_sync(self._h))
+
+    def _get(self, which):
+        out = np.zeros(self.ntotal)
+        check(lib().svl_cd_get(self._h, which, ptr(out, C.c_double)))
+        return out
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().svl_cd_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

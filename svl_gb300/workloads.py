@@ -1,0 +1,83 @@
+"""Seeded synthetic models with the shapes and value distributions of the
+benchmark configurations (no reference data is used):
+
+* config1: 200 x 100 lin2DQuad4 plane-strain box, h = 1 m, rho = 2000,
+  Vs = 200, nu = 0.25, fixed bottom, x-roller sides, vertical Ricker
+  (f0 = 5 Hz) point load at the top-centre node, dt = 0.5 h / Vp.
+* config2: 128 x 128 x 64 lin3DHexa8 box, h = 2 m, Vs log-normal (mean 400,
+  COV 0.2, exponential correlation 20 m), nu = 0.3, rho = 2100,
+  double-couple-like body force (four element groups) with a Ricker
+  f0 = 3 Hz, dt = 0.5 h / max Vp.  Boundary: fixed bottom, rollers on the
+  sides (the PML layers of the configuration are not built yet).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from . import _capi as capi
+from .model import Loads, Model, ricker
+
+
+def lognormal_field(shape, h, mean, cov, corr_len, seed):
+    """Log-normal field with exponential correlation, by spectral synthesis
+    of a Gaussian field on the element grid (periodic embedding on a grid
+    padded by one correlation length)."""
+    rng = np.random.default_rng(seed)
+    pad = [int(s + np.ceil(corr_len / h)) for s in shape]
+    white = rng.standard_normal(pad)
+    ks = np.meshgrid(*[np.fft.fftfreq(n, d=h) * 2 * np.pi for n in pad], indexing="ij")
+    k2 = sum(k * k for k in ks)
+    d = len(shape)
+    # spectral density of exp(-r/l) in d dimensions ~ (1 + k^2 l^2)^(-(d+1)/2)
+    psd = (1.0 + k2 * corr_len ** 2) ** (-(d + 1) / 2.0)
+    g = np.real(np.fft.ifftn(np.fft.fftn(white) * np.sqrt(psd)))
+    g = g[tuple(slice(0, s) for s in shape)]
+    g = (g - g.mean()) / g.std()
+    sigma = np.sqrt(np.log(1.0 + cov ** 2))
+    mu = np.log(mean) - 0.5 * sigma ** 2
+    return np.exp(mu + sigma * g)
+
+
+def config1(nx=200, ny=100, nt=2001, amp=1.0e6):
+    h, rho, vs, nu = 1.0, 2000.0, 200.0, 0.25
+    G = rho * vs ** 2
+    E = 2 * G * (1 + nu)
+    m = Model.grid(2, (nx, ny), (h, h), fix_mask=(1, 1, 3, 0, 0, 0),
+                   mat_type=np.array([capi.SVL_MAT_ELASTIC2DPLANESTRAIN], np.int32),
+                   mat_param=np.array([[E, nu, rho, 0, 0, 0, 0, 0]]))
+    lam = E * nu / ((1 + nu) * (1 - 2 * nu))
+    vp = np.sqrt((lam + 2 * G) / rho)
+    dt = 0.5 * h / vp
+    L = Loads()
+    s = L.add_series(ricker(nt, dt, 5.0, amp=amp))
+    L.add_point_load(m, ny * (nx + 1) + nx // 2, (0.0, -1.0), s)
+    return m, L, dt
+
+
+def config2(nx=128, ny=128, nz=64, nt=4001, seed=0, amp=1.0e3):
+    h, rho, nu = 2.0, 2100.0, 0.3
+    vs = lognormal_field((nx, ny, nz), h, 400.0, 0.2, 20.0, seed)
+    # element order: x fastest, then y, then z (Builder.py:167-183)
+    vs_e = np.transpose(vs, (2, 1, 0)).reshape(-1)
+    ne = nx * ny * nz
+    G = rho * vs_e ** 2
+    E = 2 * G * (1 + nu)
+    mp = np.zeros((ne, 8))
+    mp[:, 0], mp[:, 1], mp[:, 2] = E, nu, rho
+    m = Model.grid(3, (nx, ny, nz), (h, h, h), fix_mask=(1, 1, 2, 2, 7, 0),
+                   mat_type=np.full(ne, capi.SVL_MAT_ELASTIC3DLINEAR, np.int32), mat_param=mp,
+                   elem_mat=np.arange(ne, dtype=np.int32))
+    vp_max = np.sqrt(E.max() * (1 - nu) / ((1 + nu) * (1 - 2 * nu)) / rho)
+    dt = 0.5 * h / vp_max
+    L = Loads()
+    s = L.add_series(ricker(nt, dt, 3.0, amp=1.0))
+    cx, cy, cz = nx // 2, ny // 2, nz // 2
+
+    def eid(i, j, k):
+        return (k * ny + j) * nx + i
+    # double couple: +x on the element above, -x below; +y right, -y left
+    L.add_body_load(m, [eid(cx, cy + 1, cz)], (amp, 0.0, 0.0), s)
+    L.add_body_load(m, [eid(cx, cy - 1, cz)], (-amp, 0.0, 0.0), s)
+    L.add_body_load(m, [eid(cx + 1, cy, cz)], (0.0, amp, 0.0), s)
+    L.add_body_load(m, [eid(cx - 1, cy, cz)], (0.0, -amp, 0.0), s)
+    return m, L, dt

@@ -1,0 +1,203 @@
+"""The oracle pinned against the reference's own artefacts.
+
+* OpenSees histories shipped with the reference's validation cases F02
+  (lin2DQuad4 + Elastic2DPlaneStrain, Newmark), F03 (PlasticPlaneStrainJ2,
+  Newton) and J02 (lin3DHexa8 + Elastic3DLinear): the oracle's Newmark run
+  reproduces them.  The reference reports only an RMS error with no
+  threshold; the tolerances here are calibrated on the oracle and leave
+  headroom over the 6-significant-digit rounding of the .out files.
+* Internal consistency: lumped mass, body loads, element symmetry, the
+  faithful and fast central-difference modes, and the J2 return mapping.
+
+The zips are read at test time from the reference tree when it is present.
+"""
+import io
+import zipfile
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from svl_gb300 import _capi as capi
+from svl_gb300.model import Loads, Model
+from tests.helpers import h8_box, q4_box, q4_j2_columns, rel_l2
+
+REF = Path("/root/reference/03-Validations/01-Debugging")
+
+
+def _zip_text(case, member):
+    z = REF / (case + ".zip")
+    if not z.exists():
+        pytest.skip("reference validation case %s not available" % case)
+    with zipfile.ZipFile(z) as f:
+        return f.read(case + "/" + member).decode()
+
+
+def _loadtxt(case, member, skip=0):
+    return np.loadtxt(io.StringIO(_zip_text(case, member)), skiprows=skip)
+
+
+def _one_quad(j2=False):
+    if not j2:  # F02: nodes 1..4 at (0,0) (2,0) (0,2) (2,2), conn [1,2,4,3]
+        coords = np.array([[0, 0], [2, 0], [0, 2], [2, 2]], float)
+        fdof = np.array([[-1, -1], [0, -1], [1, 2], [3, 4]], np.int32)
+        conn = np.array([[0, 1, 3, 2]], np.int32)
+        mt = np.array([capi.SVL_MAT_ELASTIC2DPLANESTRAIN], np.int32)
+        mp = np.array([[2.08e8, 0.3, 2000.0, 0, 0, 0, 0, 0]])
+    else:       # F03: conn [1,2,3,4], rho = 0, J2
+        coords = np.array([[0, 0], [2, 0], [2, 2], [0, 2]], float)
+        fdof = np.array([[-1, -1], [0, -1], [1, -1], [2, -1]], np.int32)
+        conn = np.array([[0, 1, 2, 3]], np.int32)
+        mt = np.array([capi.SVL_MAT_PLASTICPLANESTRAINJ2], np.int32)
+        mp = np.array([[1.333333e8, 8.0e7, 0.0, 8.0e7, 1.0, 4.0e7, 0, 0]])
+    return Model(ndim=2, coords=coords, totaldof=np.arange(8, dtype=np.int32).reshape(4, 2), freedof=fdof,
+                 conn=conn, elem_type=capi.SVL_ELEM_LIN2DQUAD4, elem_mat=np.zeros(1, np.int32), mat_type=mt,
+                 mat_param=mp)
+
+
+def _rel_rms(a, b):
+    return float(np.sqrt(np.mean((a - b) ** 2)) / np.sqrt(np.mean(b ** 2)))
+
+
+def test_f02_quad_elastic_newmark_matches_opensees():
+    case = "F02-DY_Lin_2DPointLoad_ElasticPStrain_Quad4"
+    vals = _loadtxt(case, "StressLoad.txt")[1:]
+    ref = _loadtxt(case, "OpenSees/displacement.out")
+    m = _one_quad()
+    L = Loads()
+    s = L.add_series(vals)
+    L.add_point_load(m, 3, (0.01, -0.02), s)
+    h, _ = O.newmark_run(m, L, 0.025, 200)
+    assert _rel_rms(h[:, 6], ref[:, 1]) < 1e-5
+    assert _rel_rms(h[:, 7], ref[:, 2]) < 1e-5
+
+
+def test_f03_quad_j2_newton_matches_opensees():
+    case = "F03-DY_Lin_2DPointLoad_J2PStrain_Quad4"
+    vals = _loadtxt(case, "ricker.in")[1:]
+    ref = _loadtxt(case, "OpenSees/displacement.out")
+    m = _one_quad(j2=True)
+    L = Loads()
+    s = L.add_series(vals)
+    L.add_point_load(m, 2, (8.0e7, 0.0), s)
+    h, _ = O.newmark_run(m, L, 0.001, ref.shape[0], algo=1, maxit=100, cnvgtol=1e-6)
+    # OpenSees' J2Plasticity differs in formulation details; the reference
+    # itself only reports this RMS.  Early elastic steps agree to print precision.
+    assert _rel_rms(h[:, 4], ref[:, 1]) < 5e-3
+    assert np.allclose(h[:5, 4], ref[:5, 1], rtol=1e-4)
+
+
+def test_j02_hexa_elastic_newmark_matches_opensees():
+    case = "J02-DY_Lin_3DPointLoad_Elastic_Hexa8"
+    vals = _loadtxt(case, "StressLoad.txt")[1:]
+    ref = _loadtxt(case, "OpenSees/displacement.out")
+    coords = np.array([[0, 0, 0], [2, 0, 0], [2, 2, 0], [0, 2, 0], [0, 0, 2], [2, 0, 2], [2, 2, 2], [0, 2, 2]], float)
+    restr = {0: [0, 1, 2], 1: [2], 2: [2], 3: [2]}
+    fdof = np.zeros((8, 3), np.int32)
+    c = 0
+    for n in range(8):
+        for d in range(3):
+            if d in restr.get(n, []):
+                fdof[n, d] = -1
+            else:
+                fdof[n, d] = c
+                c += 1
+    m = Model(ndim=3, coords=coords, totaldof=np.arange(24, dtype=np.int32).reshape(8, 3), freedof=fdof,
+              conn=np.arange(8, dtype=np.int32)[None, :], elem_type=capi.SVL_ELEM_LIN3DHEXA8,
+              elem_mat=np.zeros(1, np.int32), mat_type=np.array([capi.SVL_MAT_ELASTIC3DLINEAR], np.int32),
+              mat_param=np.array([[2.08e8, 0.3, 2000.0, 0, 0, 0, 0, 0]]), lumped=False)  # J02 keeps the default massform (Consistent)
+    L = Loads()
+    s = L.add_series(vals)
+    L.add_point_load(m, 5, (0.01, 0.0, 0.0), s)
+    L.add_point_load(m, 7, (0.0, 0.01, 0.0), s)
+    L.add_point_load(m, 6, (0.0, 0.0, -0.05), s)
+    h, _ = O.newmark_run(m, L, 0.025, 200)
+    # the OpenSees model is the same cube with y and z exchanged
+    assert _rel_rms(h[:, 18], ref[:, 1]) < 1e-5
+    assert _rel_rms(h[:, 20], ref[:, 2]) < 1e-5
+    assert _rel_rms(h[:, 19], ref[:, 3]) < 1e-5
+
+
+def test_central_difference_converges_to_newmark_on_f02():
+    """The reference ships no CD golden for a solid element; with a small
+    step the oracle's CD history approaches its OpenSees-pinned Newmark one."""
+    m = _one_quad()
+    case = "F02-DY_Lin_2DPointLoad_ElasticPStrain_Quad4"
+    vals = _loadtxt(case, "StressLoad.txt")[1:]
+    sub = 50
+    t = np.arange(len(vals)) * 0.025
+    tf = np.arange((len(vals) - 1) * sub + 1) * (0.025 / sub)
+    L = Loads()
+    s = L.add_series(np.interp(tf, t, vals))
+    L.add_point_load(m, 3, (0.01, -0.02), s)
+    h, _, _, _ = O.cd_run(m, L, 0.025 / sub, 100 * sub)
+    Ln = Loads()
+    sn = Ln.add_series(vals)
+    Ln.add_point_load(m, 3, (0.01, -0.02), sn)
+    hn, _ = O.newmark_run(m, Ln, 0.025, 100)
+    assert _rel_rms(h[sub - 1::sub, 6], hn[:, 6]) < 2e-2
+
+
+def test_lumped_mass_and_body_force_agree_with_library():
+    m, _, _ = h8_box(3, 3, 2)
+    assert np.array_equal(O.lumped_mass(m), m.lumped_mass())
+    for e in (0, 5, 17):
+        q = np.array([1.0, -2.0, 0.5])
+        assert np.array_equal(O.body_force(m, e, q), m.body_force(e, q))
+    # total mass = rho * volume (all dofs, x-direction)
+    M = O.lumped_mass(m, mtol=0.0)
+    vol = 3 * 3 * 2 * 8.0
+    assert abs(M[m.totaldof[:, 0]].sum() - 2100.0 * vol) < 1e-6 * 2100.0 * vol
+
+
+def test_element_stiffness_symmetric_and_rigid_modes():
+    for m in (q4_box(3, 2)[0], h8_box(2, 2, 2)[0]):
+        K, Ml, Mc = O.element_matrices(m, 0)
+        assert np.allclose(K, K.T, rtol=0, atol=1e-6 * np.abs(K).max())
+        nd = m.ndim
+        nen = m.conn.shape[1]
+        for d in range(nd):  # translations are zero-energy modes
+            r = np.zeros(nen * nd)
+            r[d::nd] = 1.0
+            assert np.abs(K @ r).max() < 1e-6 * np.abs(K).max()
+        assert np.allclose(Ml.sum(), Mc.sum())
+
+
+def test_cd_fast_mode_equals_faithful_mode():
+    m, L, dt = q4_box(12, 6, nt=120)
+    h0, *_ = O.cd_run(m, L, dt, 120, mode=0)
+    h1, *_ = O.cd_run(m, L, dt, 120, mode=1)
+    assert np.array_equal(h0, h1)
+    m, L, dt = q4_j2_columns(2, 3, (5, 7), nt=80)
+    h0, *_ = O.cd_run(m, L, dt, 80, mode=0)
+    h1, *_ = O.cd_run(m, L, dt, 80, mode=1)
+    assert np.array_equal(h0, h1)
+
+
+def test_j2_return_mapping_properties():
+    K, G, H, SY = 1.0e8, 6.0e7, 1.2e6, 5.0e4
+    p = np.array([K, G, 2000.0, H, 1.0, SY, 0, 0])
+    n = 60
+    g = np.linspace(0, 6e-3, n)
+    strains = np.stack([np.zeros(n), np.zeros(n), g], axis=1)        # simple shear path (3D plane strain)
+    sig = O.j2_path(capi.SVL_MAT_PLASTICPLANESTRAINJ2, p, strains)
+    tau = sig[:, 2]
+    # elastic branch: tau = G gamma
+    first = g < SY / np.sqrt(3) / G * 0.9
+    assert np.allclose(tau[first], G * g[first], rtol=1e-12)
+    # plastic branch: tau bounded by the hardened yield stress, monotone
+    assert np.all(np.diff(tau) >= -1e-9)
+    assert tau[-1] < SY / np.sqrt(3) * 1.2
+    # elastic material is linear
+    pe = np.array([2.0e8, 0.25, 2000.0, 0, 0, 0, 0, 0])
+    se = O.j2_path(capi.SVL_MAT_ELASTIC2DPLANESTRAIN, pe, strains)
+    assert np.allclose(se[:, 2], 2.0e8 / 2.5 * g)
+
+
+def test_cd_linearity_in_load_amplitude():
+    m, L, dt = q4_box(10, 5, nt=100)
+    h1, *_ = O.cd_run(m, L, dt, 100)
+    L.force_coef = [2.0 * c for c in L.force_coef]
+    h2, *_ = O.cd_run(m, L, dt, 100)
+    assert rel_l2(h2, 2 * h1) < 1e-12
