@@ -1,0 +1,73 @@
+// C++ mirror of the reference's Integrator interface over the C ABI.
+//
+// A maintainer of the C++ reference would swap
+//   std::make_shared<CentralDifference>(mesh, dt, mtol, ktol, ftol)
+// (RP/12-Utilities/Driver.hpp:1818-1820) for svl::gpu::CentralDifference built
+// from the same partition arrays.  Method names and meanings follow
+// RP/10-Integrators/Integrator.hpp:53-144: ComputeNewStep returns `stop`
+// (true = failure), state getters return total-dof vectors.
+#pragma once
+
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/svl_gb300.h"
+
+namespace svl {
+namespace gpu {
+
+class Error : public std::runtime_error {
+public:
+    Error(int code, const std::string& what) : std::runtime_error(what), code(code) {}
+    int code;
+};
+
+inline void check(int st) {
+    if (st != SVL_OK) throw Error(st, svl_last_error());
+}
+
+class CentralDifference {
+public:
+    // CentralDifference(mesh, dt, mtol, ktol, ftol) (CentralDifference.cpp:6-27)
+    CentralDifference(const svl_model_desc& model, const svl_load_desc& loads, double dt,
+                      double mtol = 1e-12, double ftol = 1e-12)
+        : ntotal_(model.ntotal) {
+        svl_cd_opts o{};
+        o.dt = dt;
+        o.mtol = mtol;
+        o.ftol = ftol;
+        o.precision = SVL_PREC_FP64;
+        o.check_every = 1;
+        check(svl_cd_create(&model, &loads, &o, &h_));
+    }
+    ~CentralDifference() { svl_cd_destroy(h_); }
+    CentralDifference(const CentralDifference&) = delete;
+    CentralDifference& operator=(const CentralDifference&) = delete;
+
+    // Initialize(mesh): initial conditions from the nodes (CentralDifference.cpp:36-71)
+    void Initialize(const double* U0 = nullptr, const double* V0 = nullptr, const double* A0 = nullptr) {
+        check(svl_cd_set_initial(h_, U0, V0, A0));
+    }
+    // ComputeNewStep(mesh, k) -> stop (CentralDifference.cpp:124-151)
+    bool ComputeNewStep(unsigned int k) { return svl_cd_run(h_, (int32_t)k, 1, nullptr) != SVL_OK; }
+    // Many steps in one call, optional displacement history [n][ntotal].
+    bool ComputeNewSteps(unsigned int k_first, unsigned int n, double* U_hist = nullptr) {
+        return svl_cd_run(h_, (int32_t)k_first, (int32_t)n, U_hist) != SVL_OK;
+    }
+    std::vector<double> GetDisplacements() const { return get(0); }
+    std::vector<double> GetVelocities() const { return get(1); }
+    std::vector<double> GetAccelerations() const { return get(2); }
+
+private:
+    std::vector<double> get(int which) const {
+        std::vector<double> v(ntotal_);
+        check(svl_cd_get(h_, which, v.data()));
+        return v;
+    }
+    svl_cd* h_ = nullptr;
+    int ntotal_ = 0;
+};
+
+}  // namespace gpu
+}  // namespace svl
