@@ -218,6 +218,42 @@ int  svl_cd_profile(svl_cd* cd, int32_t k_first, int32_t nsteps, double* ms_kern
 int  svl_cd_sync(svl_cd* cd);
 void svl_cd_destroy(svl_cd* cd);
 
+/* ---- stepping without device allocation -------------------------------- */
+/* No counterpart in the reference: SVL allocates all of its (host) memory
+ * freely.  Some callers of this library cannot let it call cudaMalloc or
+ * cudaFree once their time loop runs: applications that hand out all device
+ * memory from their own pool (a framework's caching allocator, or a solver
+ * that reserved the remaining HBM for itself) and forbid third-party code
+ * from allocating, because those calls synchronise the whole device and can
+ * fail or fragment the pool in the middle of a simulation.  svl_cd_run may
+ * allocate on first use (it instantiates a CUDA graph, and a device history
+ * buffer when a history is requested); svl_cd_run_noalloc never allocates.
+ *
+ * It advances the handle's state exactly like svl_cd_run(cd, k_first,
+ * nsteps, NULL) -- same kernels, same results -- but the per-step element
+ * force block lives in one library-wide static device array of
+ * SVL_NOALLOC_SCRATCH_BYTES instead of the handle's own buffer, and the
+ * kernels are launched directly (no graph).  Every GPU that loads the
+ * library holds that array until the process exits.
+ *
+ * Limit: nelem * nen * ndof * 8 bytes must fit in SVL_NOALLOC_SCRATCH_BYTES
+ * (8 MiB: at most 43690 lin3DHexa8 or 131072 lin2DQuad4 elements); larger
+ * models are rejected with SVL_ERR_UNSUPPORTED.
+ * Output: if d_U_out is not NULL it must be a device buffer of ntotal
+ * doubles owned by the caller; it receives U after the last step.
+ * The call is asynchronous on the handle's stream (svl_cd_sync waits) and
+ * does not scan for NaN/Inf.
+ * Set-up: the first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress, with that device made current for the lookup);
+ * make that first call before any stream capture.
+ * Sharing: all calls in the process share the one array and it keeps the
+ * last call's contents.  Each step overwrites every entry it later reads,
+ * so nothing has to start at zero, but calls that overlap on the GPU
+ * (different streams, handles or host threads) race on the array and must
+ * be serialised by the caller. */
+#define SVL_NOALLOC_SCRATCH_BYTES (8u << 20)
+int  svl_cd_run_noalloc(svl_cd* cd, int32_t k_first, int32_t nsteps, double* d_U_out);
+
 #ifdef __cplusplus
 }
 #endif

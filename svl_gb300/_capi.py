@@ -33,6 +33,8 @@ SVL_MAT_PLASTICPLANESTRAINJ2 = 3
 SVL_MAT_PLASTIC3DJ2 = 4
 SVL_MAT_NPARAM = 8
 
+SVL_NOALLOC_SCRATCH_BYTES = 8 << 20
+
 SVL_PREC_FP64 = 0
 SVL_PREC_MIXED = 1
 
@@ -116,6 +118,7 @@ def lib():
     L.svl_cd_sync.argtypes = [C.c_void_p]
     L.svl_cd_run_timed.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(C.c_float)]
     L.svl_cd_profile.argtypes = [C.c_void_p, C.c_int32, C.c_int32, f64p]
+    L.svl_cd_run_noalloc.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p]
     L.svl_cd_destroy.argtypes = [C.c_void_p]
     L.svl_cd_destroy.restype = None
     _lib = L

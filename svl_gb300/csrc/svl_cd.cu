@@ -31,6 +31,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <vector>
 
 #include "svl_internal.hpp"
@@ -805,3 +806,95 @@ int svl_cd_sync(svl_cd* cd) {
 void svl_cd_destroy(svl_cd* cd) { delete cd; }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Stepping without device allocation (svl_cd_run_noalloc).
+//
+// For callers that must not let the library allocate device memory while
+// their time loop runs (they own all device memory through their own pool,
+// and cudaMalloc/cudaFree would synchronise the device and may fail or
+// fragment that pool).  The element force block, the only per-step scratch
+// of the CD kernels, lives in this file-scope static array instead of the
+// handle's buffer; every GPU that loads the library holds it until exit.
+
+static __device__ __align__(256) double g_noalloc_scratch[SVL_NOALLOC_SCRATCH_BYTES / sizeof(double)];
+
+namespace {
+
+constexpr int kNoallocMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+double* g_noalloc_addr[kNoallocMaxDevices] = {};
+
+// Once per device, with that device current: the device address of the
+// static array (the host-side symbol is only a stand-in, never a device
+// pointer).
+int noalloc_scratch(int dev, double** out) {
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (dev < 0 || dev >= kNoallocMaxDevices) { set_error("device %d out of range for the no-alloc scratch", dev); return SVL_ERR_INVALID; }
+    if (!g_noalloc_addr[dev]) {
+        int prev = 0;
+        CUDA_TRY(cudaGetDevice(&prev));
+        if (prev != dev) CUDA_TRY(cudaSetDevice(dev));
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (prev != dev) cudaSetDevice(prev);
+        if (e != cudaSuccess || !p) {
+            set_error("cudaGetSymbolAddress of the no-alloc scratch failed on device %d: %s", dev, cudaGetErrorString(e));
+            return SVL_ERR_CUDA;
+        }
+        g_noalloc_addr[dev] = static_cast<double*>(p);
+    }
+    *out = g_noalloc_addr[dev];
+    return SVL_OK;
+}
+
+__global__ void k_set_step(int* step, int value) { step[0] = value; }
+
+// The launches of one step, as in svl_cd_run, on a view whose element force
+// block points at the static scratch.
+int noalloc_launch_step(svl_cd* cd, const DevView& d) {
+    const HostModel& m = cd->m;
+    const int eb = 128, nb = 256;
+    const int eg = (m.nelem + eb - 1) / eb, ng = (m.nnode + nb - 1) / nb, fg = (m.nfree + nb - 1) / nb;
+    if (m.ndim == 2) k_element<2, 4><<<eg, eb, 0, cd->stream>>>(d, d.Us, m.ngp, 1);
+    else k_element<3, 8><<<eg, eb, 0, cd->stream>>>(d, d.Us, m.ngp, 1);
+    if (cd->identity_T) {
+        if (m.ndim == 2) k_node<2><<<ng, nb, 0, cd->stream>>>(d);
+        else k_node<3><<<ng, nb, 0, cd->stream>>>(d);
+    } else {
+        if (m.ndim == 2) k_residual<2><<<ng, nb, 0, cd->stream>>>(d);
+        else k_residual<3><<<ng, nb, 0, cd->stream>>>(d);
+        if (m.nfree > 0) k_free<<<fg, nb, 0, cd->stream>>>(d);
+        if (m.ndim == 2) k_update<2><<<ng, nb, 0, cd->stream>>>(d);
+        else k_update<3><<<ng, nb, 0, cd->stream>>>(d);
+    }
+    CUDA_TRY(cudaGetLastError());
+    return SVL_OK;
+}
+
+}  // namespace
+
+extern "C" int svl_cd_run_noalloc(svl_cd* cd, int32_t k_first, int32_t nsteps, double* d_U_out) {
+    if (!cd) { set_error("NULL handle"); return SVL_ERR_INVALID; }
+    if (nsteps < 0) { set_error("nsteps must be >= 0"); return SVL_ERR_INVALID; }
+    const HostModel& m = cd->m;
+    const size_t need = (size_t)m.nelem * m.nen * m.ndof * sizeof(double);
+    if (need > (size_t)SVL_NOALLOC_SCRATCH_BYTES) {
+        set_error("svl_cd_run_noalloc: the element force block needs %zu bytes but the no-alloc scratch holds "
+                  "at most %u bytes (%d elements of %d dofs); use svl_cd_run for this model",
+                  need, (unsigned)SVL_NOALLOC_SCRATCH_BYTES, m.nelem, m.nen * m.ndof);
+        return SVL_ERR_UNSUPPORTED;
+    }
+    cudaPointerAttributes attr{};
+    CUDA_TRY(cudaPointerGetAttributes(&attr, cd->d.U));
+    double* scratch = nullptr;
+    TRY(noalloc_scratch(attr.device, &scratch));
+    DevView d = cd->d;
+    d.fe = scratch;
+    k_set_step<<<1, 1, 0, cd->stream>>>(d.step, k_first - 1);
+    CUDA_TRY(cudaGetLastError());
+    for (int s = 0; s < nsteps; ++s) TRY(noalloc_launch_step(cd, d));
+    if (d_U_out)
+        CUDA_TRY(cudaMemcpyAsync(d_U_out, d.U, sizeof(double) * m.ntotal, cudaMemcpyDeviceToDevice, cd->stream));
+    return SVL_OK;
+}
