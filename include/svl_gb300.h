@@ -218,6 +218,36 @@ int  svl_cd_profile(svl_cd* cd, int32_t k_first, int32_t nsteps, double* ms_kern
 int  svl_cd_sync(svl_cd* cd);
 void svl_cd_destroy(svl_cd* cd);
 
+/* ---- structured grids: mixed-precision batched central difference ------ */
+/* The same step as svl_cd_run for `ninst` instances of one uniform
+ * lin3DHexa8 grid (svl_grid_build layout, Elastic3DLinear materials, lumped
+ * mass, point/body loads, restraints; no constraints or support motion),
+ * advanced together by one fused kernel per step.  The element force is the
+ * tensor-core contraction F_e = lambda_e (K_lambda u_e) + mu_e (K_mu u_e):
+ * the 48 x 24 stacked reference matrix times the 24 x elements displacement
+ * block, TF32 hi/lo split operands (three products) with FP32 accumulation
+ * in TMEM; the displacement update stays in FP64.  Reference summation order
+ * at every node is kept; the assembler's force tolerance filter is not
+ * applied on this path.  `models` and `loads` are arrays of ninst
+ * descriptors (one per instance, same grid).  precision must be
+ * SVL_PREC_MIXED.  Replaces the same reference functions as svl_cd_create /
+ * svl_cd_run for models of that shape. */
+typedef struct svl_cdx svl_cdx;
+int  svl_cdx_create(const svl_grid_spec* grid, int32_t ninst, const svl_model_desc* models,
+                    const svl_load_desc* loads, const svl_cd_opts* opts, svl_cdx** out);
+/* Initial conditions of instance `inst` (total dofs, NULL = zero). */
+int  svl_cdx_set_initial(svl_cdx* cdx, int32_t inst, const double* U0, const double* V0, const double* A0);
+/* Steps k_first .. k_first+nsteps-1 of every instance; U_hist (host, or
+ * NULL) receives [nsteps][ninst][ntotal] displacements. */
+int  svl_cdx_run(svl_cdx* cdx, int32_t k_first, int32_t nsteps, double* U_hist);
+/* svl_cdx_run without history bracketed by CUDA events on the handle's
+ * stream (measurement hook, no counterpart in the reference). */
+int  svl_cdx_run_timed(svl_cdx* cdx, int32_t k_first, int32_t nsteps, float* ms);
+/* which: 0 = U, 1 = V, 2 = A of instance `inst` after the last step. */
+int  svl_cdx_get(svl_cdx* cdx, int32_t inst, int32_t which, double* out);
+int  svl_cdx_launch_count(svl_cdx* cdx, int64_t* launches);
+void svl_cdx_destroy(svl_cdx* cdx);
+
 /* ---- stepping without device allocation -------------------------------- */
 /* No counterpart in the reference: SVL allocates all of its (host) memory
  * freely.  Some callers of this library cannot let it call cudaMalloc or

@@ -118,6 +118,15 @@ def lib():
     L.svl_cd_sync.argtypes = [C.c_void_p]
     L.svl_cd_run_timed.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(C.c_float)]
     L.svl_cd_profile.argtypes = [C.c_void_p, C.c_int32, C.c_int32, f64p]
+    L.svl_cdx_create.argtypes = [C.POINTER(GridSpec), C.c_int32, C.POINTER(ModelDesc), C.POINTER(LoadDesc),
+                                 C.POINTER(CdOpts), C.POINTER(C.c_void_p)]
+    L.svl_cdx_set_initial.argtypes = [C.c_void_p, C.c_int32, f64p, f64p, f64p]
+    L.svl_cdx_run.argtypes = [C.c_void_p, C.c_int32, C.c_int32, f64p]
+    L.svl_cdx_run_timed.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(C.c_float)]
+    L.svl_cdx_get.argtypes = [C.c_void_p, C.c_int32, C.c_int32, f64p]
+    L.svl_cdx_launch_count.argtypes = [C.c_void_p, C.POINTER(C.c_int64)]
+    L.svl_cdx_destroy.argtypes = [C.c_void_p]
+    L.svl_cdx_destroy.restype = None
     L.svl_cd_run_noalloc.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p]
     L.svl_cd_destroy.argtypes = [C.c_void_p]
     L.svl_cd_destroy.restype = None

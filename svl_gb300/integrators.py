@@ -90,3 +90,72 @@ class CentralDifference:
             self.close()
         except Exception:
             pass
+
+
+class StructuredCentralDifference:
+    """Mixed-precision batched central difference for `ninst` instances of one
+    uniform lin3DHexa8 grid (svl_cdx_*): tensor-core element forces (TF32
+    hi/lo, FP32 accumulation), FP64 displacement update.  Same step as
+    CentralDifference; `instances` is a list of (Model, Loads) built on the
+    grid given by `ne`, `h`, `origin`."""
+
+    def __init__(self, ne, h, instances, dt: float, origin=(0.0, 0.0, 0.0), mtol: float = 1e-12):
+        self.dt = float(dt)
+        self.ninst = len(instances)
+        spec = capi.GridSpec()
+        spec.ndim = 3
+        for i in range(3):
+            spec.ne[i] = int(ne[i])
+            spec.h[i] = float(h[i])
+            spec.origin[i] = float(origin[i])
+        self._spec = spec
+        md = (capi.ModelDesc * self.ninst)()
+        ld = (capi.LoadDesc * self.ninst)()
+        self._keep = []
+        for i, (m, L) in enumerate(instances):
+            md[i] = m.desc()
+            self._keep.append(m)
+            L = L or Loads()
+            ld[i] = L.desc()
+            self._keep.append(L)
+        self._md, self._ld = md, ld
+        opts = capi.CdOpts(dt=self.dt, ftol=0.0, mtol=mtol, precision=capi.SVL_PREC_MIXED, check_every=0)
+        hnd = C.c_void_p()
+        check(lib().svl_cdx_create(C.byref(spec), self.ninst, md, ld, C.byref(opts), C.byref(hnd)))
+        self._h = hnd
+        self.ntotal = instances[0][0].ntotal
+
+    def Initialize(self, inst: int = 0, U0=None, V0=None, A0=None):
+        arrs = [None if a is None else capi.as_f64(a) for a in (U0, V0, A0)]
+        check(lib().svl_cdx_set_initial(self._h, int(inst), *(ptr(a, C.c_double) for a in arrs)))
+
+    def run(self, k_first: int, nsteps: int, history: bool = False):
+        hist = np.zeros((nsteps, self.ninst, self.ntotal)) if history else None
+        check(lib().svl_cdx_run(self._h, int(k_first), int(nsteps), ptr(hist, C.c_double)))
+        return hist
+
+    def run_timed(self, k_first: int, nsteps: int) -> float:
+        ms = C.c_float()
+        check(lib().svl_cdx_run_timed(self._h, int(k_first), int(nsteps), C.byref(ms)))
+        return float(ms.value)
+
+    def get(self, inst: int, which: int = 0) -> np.ndarray:
+        out = np.zeros(self.ntotal)
+        check(lib().svl_cdx_get(self._h, int(inst), int(which), ptr(out, C.c_double)))
+        return out
+
+    def launches(self) -> int:
+        n = C.c_int64()
+        check(lib().svl_cdx_launch_count(self._h, C.byref(n)))
+        return int(n.value)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().svl_cdx_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
