@@ -1,21 +1,24 @@
 #!/usr/bin/env python3
 """Benchmark of the explicit central-difference hot path (DOF-steps/s).
 
-A "step" is one time step of the whole model: element forces, the ordered
-node gather, the diagonal solve and the state update.  The default workload
-is the 3D configuration (lin3DHexa8 128 x 128 x 64, h = 2 m, log-normal Vs
-field, double-couple body force) in the FP64 plain form; the PML layers of
-that configuration are not built yet and the box has fixed/roller faces
-instead (stated in the JSON config).
+A "step" is one time step of the whole batch: element forces, the ordered
+node gather, the diagonal solve and the state update.  Default workload: the
+3D configuration (lin3DHexa8 128 x 128 x 64, h = 2 m, log-normal Vs field,
+double-couple body force), as a batch of 4 seeded realisations advanced by
+the mixed-precision path (tensor-core element forces, FP64 update); the FP64
+plain path is timed on one realisation beside it, and the mixed result's
+error against it is reported.  The PML layers of that configuration are not
+built yet; the box has fixed/roller faces instead (stated in the config).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload config2|config1]
+                    [--precision mixed|fp64] [--instances B] [--workload config2|config1]
 
-value   : free DOF x steps / device time of the K steps (CUDA events on the
-          library's stream, inputs resident in HBM, working set > L2).
+value   : free DOF x instances x steps / device time of the K steps (CUDA
+          events on the library's stream, inputs resident in HBM, working
+          set > L2: 4 instances hold ~300 MB of state).
 e2e     : the same metric through the C ABI with host buffers: model arrays
-          copied in by svl_cd_create and the full displacement field copied
-          back to a host buffer after every step (svl_cd_run with history).
+          copied in by the create call and every instance's full displacement
+          field copied back to a host buffer after every step.
 roofline: algorithmic bytes of one step (37 B per free DOF for H8, 40 for
           Q4) over the measured step time, against MEASURED_PEAKS.json.
 """
@@ -101,14 +104,15 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(rows)}
 
 
-def build_workload(name):
+def build_workload(name, seed=0):
     from svl_gb300 import workloads
     if name == "config1":
         m, L, dt = workloads.config1()
-        desc = "lin2DQuad4 200x100 plane-strain box, CD, FP64 plain"
+        desc = "lin2DQuad4 200x100 plane-strain box, CD"
     elif name == "config2":
-        m, L, dt = workloads.config2()
-        desc = "lin3DHexa8 128x128x64 box (h=2 m, log-normal Vs), CD, FP64 plain; PML layers not built (fixed bottom, roller sides)"
+        m, L, dt = workloads.config2(seed=seed)
+        desc = ("lin3DHexa8 128x128x64 box (h=2 m, log-normal Vs, COV 0.2, corr 20 m), CD; "
+                "PML layers not built (fixed bottom, roller sides)")
     else:
         raise SystemExit("unknown workload %s" % name)
     return m, L, dt, desc
@@ -143,11 +147,17 @@ def main():
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="config2", choices=["config1", "config2"])
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--instances", type=int, default=4)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-fp64-compare", action="store_true")
     args = ap.parse_args()
     ws, rank, local = dist_info()
     warm = max(3, args.warmup)
+    if args.workload == "config1":
+        args.precision = "fp64"
+    nb = args.instances if args.precision == "mixed" else 1
 
     if args.impl == "reference":
         if rank != 0:
@@ -163,8 +173,7 @@ def main():
         print(json.dumps(line))
         return 0
 
-    import ctypes as C
-    from svl_gb300 import CentralDifference
+    from svl_gb300 import CentralDifference, StructuredCentralDifference
     from svl_gb300 import _capi as capi
 
     pg = None
@@ -176,14 +185,33 @@ def main():
         pg = dist
     capi.check(capi.lib().svl_set_device(local))
 
-    m, L, dt, desc = build_workload(args.workload)
+    insts = [build_workload(args.workload, seed=b) for b in range(nb)]
+    m, L, dt0, desc = insts[0]
+    dt = min(x[2] for x in insts)
     nd = m.ndim
-    cd = CentralDifference(m, L, dt)
-    cd.Initialize()
-    cd.run(1, warm)                      # warm-up (graph capture happens here)
-    # per-kernel device times for the roofline (individual launches + events)
-    prof = cd.profile(1 + warm, 20)
-    cd.Initialize()
+    nfree_total = sum(x[0].nfree for x in insts)
+    grid = m.grid_shape
+
+    def make_handle():
+        if args.precision == "mixed":
+            h = StructuredCentralDifference(grid, (2.0, 2.0, 2.0), [(x[0], x[1]) for x in insts], dt)
+            for b in range(nb):
+                h.Initialize(b)
+        else:
+            h = CentralDifference(m, L, dt)
+            h.Initialize()
+        return h
+
+    cd = make_handle()
+    cd.run(1, warm)                                   # warm-up
+    prof = None
+    if args.precision == "fp64":
+        prof = cd.profile(1 + warm, 20)
+    if args.precision == "mixed":
+        for b in range(nb):
+            cd.Initialize(b)
+    else:
+        cd.Initialize()
     if pg:
         pg.barrier()
     with ClockSampler(local) as clk:
@@ -197,33 +225,49 @@ def main():
     launches = cd.launches()
     clocks = clk.summary()
     ms_step = ms / args.steps
-    value = ws * m.nfree * args.steps / (ms / 1e3)
-    U = cd.GetDisplacements()
-    finite = bool(np.isfinite(U).all())
+    value = ws * nfree_total * args.steps / (ms / 1e3)
+    U_last = cd.get(0, 0) if args.precision == "mixed" else cd.GetDisplacements()
+    finite = bool(np.isfinite(U_last).all())
     cd.close()
 
+    # FP64 plain path on instance 0, same steps: speed and the mixed result's error
+    fp64 = None
+    if args.precision == "mixed" and not args.no_fp64_compare:
+        ref = CentralDifference(m, L, dt)
+        ref.Initialize()
+        ms64 = ref.run_timed(1, args.steps)
+        U64 = ref.GetDisplacements()
+        ref.close()
+        err = float(np.linalg.norm(U_last - U64) / max(np.linalg.norm(U64), 1e-300))
+        v64 = m.nfree * args.steps / (ms64 / 1e3)
+        fp64 = {"value": ws * v64, "unit": "DOF-steps/s", "ms_per_step": ms64 / args.steps,
+                "speedup_mixed_over_fp64": value / (ws * v64),
+                "mixed_rel_l2_final_u_vs_fp64": err, "steps": args.steps, "instance": 0}
+
     peak, peak_kind = measured_peaks()
-    step_ms_prof = float(prof.sum() / 20.0)
-    algo_bytes = ALGO_BYTES_PER_DOF[nd] * m.nfree
+    algo_bytes = ALGO_BYTES_PER_DOF[nd] * nfree_total
     achieved = algo_bytes / (ms_step / 1e3) / 1e9
-    kernel_names = ["k_element", "k_node", "k_residual", "k_free", "k_update"]
-    shares = {kernel_names[i]: round(float(prof[i] / max(prof.sum(), 1e-12)), 4) for i in range(5) if prof[i] > 0}
+    if args.precision == "fp64":
+        kernel_names = ["k_element", "k_node", "k_residual", "k_free", "k_update"]
+        shares = {kernel_names[i]: round(float(prof[i] / max(prof.sum(), 1e-12)), 4) for i in range(5) if prof[i] > 0}
+        kname = "one FP64 CD step (k_element + k_node)"
+    else:
+        shares = None
+        kname = "k_cdx_step (fused mixed-precision step, all instances) + k_cdx_loads"
 
     e2e = None
     if not args.no_e2e:
-        ne2e = min(args.steps, 100)
-        hist = np.empty((ne2e, m.ntotal))
+        ne2e = min(args.steps, 20 if args.precision == "mixed" else 50)
         t0 = time.perf_counter()
-        cd2 = CentralDifference(m, L, dt)        # host arrays -> device
-        cd2.Initialize()
-        cd2.run(1, ne2e, history=True)          # full U to the host every step
+        cd2 = make_handle()                             # host arrays -> device
+        hist = cd2.run(1, ne2e, history=True)          # every instance's full U to the host each step
         cd2.close()
         t1 = time.perf_counter()
-        md_bytes = (m.coords.nbytes + m.totaldof.nbytes + m.freedof.nbytes + m.conn.nbytes +
-                    m.elem_mat.nbytes + m.mat_param.nbytes + m.mat_type.nbytes)
-        e2e = {"value": ws * m.nfree * ne2e / (t1 - t0), "unit": "DOF-steps/s",
-               "h2d_bytes_per_step": int(md_bytes / ne2e), "d2h_bytes_per_step": int(m.ntotal * 8),
-               "steps": ne2e, "includes": "svl_cd_create from host arrays + run with full-field history to host"}
+        md_bytes = nb * (m.coords.nbytes + m.totaldof.nbytes + m.freedof.nbytes + m.conn.nbytes +
+                         m.elem_mat.nbytes + m.mat_param.nbytes + m.mat_type.nbytes)
+        e2e = {"value": ws * nfree_total * ne2e / (t1 - t0), "unit": "DOF-steps/s",
+               "h2d_bytes_per_step": int(md_bytes / ne2e), "d2h_bytes_per_step": int(nb * m.ntotal * 8),
+               "steps": ne2e, "includes": "handle creation from host arrays + run with every instance's full-field history to host"}
         del hist
 
     cb = None
@@ -231,18 +275,23 @@ def main():
         cb = cpu_baseline(m, L, dt, steps_cap=10)
 
     if rank == 0:
+        ws_mb = (nb * m.ntotal * 8 * (2 if args.precision == "mixed" else 7) + nb * m.ntotal * 4
+                 + (m.nelem * 24 * 8 if args.precision == "fp64" else nb * m.nelem * 8)) // 2 ** 20
         line = {
             "metric": "DOF-steps/s", "value": value, "unit": "DOF-steps/s", "n_gpus": ws, "steps": args.steps,
             "warmup": warm, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
-            "config": {"workload": desc, "free_dof": m.nfree, "elements": m.nelem, "dt": dt,
-                       "precision": "fp64 plain", "parallelism": "replicas" if ws > 1 else "single GPU",
-                       "l2": "no flush; working set > L2 (element force block %d MB + state %d MB)" % (
-                           m.nelem * (24 if nd == 3 else 8) * 8 // 2 ** 20, m.ntotal * 7 * 8 // 2 ** 20)},
-            "roofline": {"bound": "hbm", "kernel": "one CD step (k_element + k_node)", "achieved": achieved,
-                         "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
-                         "traffic": None, "algorithmic_bytes_per_step": algo_bytes,
-                         "kernel_share": shares, "profiled_step_ms": step_ms_prof},
+            "vs_baseline": None, "dtype": "tf32x3+f64" if args.precision == "mixed" else "f64",
+            "data": "synthetic (seeded)",
+            "config": {"workload": desc, "instances": nb, "free_dof_per_instance": m.nfree,
+                       "elements_per_instance": m.nelem, "dt": dt,
+                       "precision": ("mixed: TF32 hi/lo tensor-core element forces, FP32 accumulate, FP64 update"
+                                     if args.precision == "mixed" else "fp64 plain"),
+                       "parallelism": "replicas" if ws > 1 else "single GPU",
+                       "l2": "no flush; working set ~%d MB > 129 MB L2" % ws_mb},
+            "roofline": {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
+                         "algorithmic_bytes_per_step": algo_bytes, "kernel_share": shares},
+            "fp64_plain": fp64,
             "cpu_baseline": cb, "e2e": e2e, "gpu_launches": int(launches), "clocks": clocks,
             "finite": finite,
         }

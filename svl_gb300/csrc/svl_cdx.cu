@@ -11,12 +11,19 @@
 //      TMEM), then F_e = lambda_e D[:, 0:24] + mu_e D[:, 24:48];
 //   3. gathers the eight element contributions of every owned node in the
 //      reference's element-tag order (no atomics) and updates
-//      u_{n+1} = 2 u_n - u_{n-1} + (dt^2/m)(f_ext - f_int) in FP64
+//      u_{n+1} = u_n + (u_n - u_{n-1}) + (dt^2/m)(f_ext - f_int)
 //      (CentralDifference.cpp:138-148 with the diagonal solve, for lumped
 //      mass without damping).
+// The displacement state is kept as a compensated pair of FP32 numbers
+// (u = hi + lo, about 48 significant bits) updated with error-free TwoSum
+// transformations, so the hot loop issues no FP64 instruction: on GB300 the
+// FP64 pipe (about 1.2 TFLOP/s) cannot keep up with even an FP64 axpy over
+// the state at HBM speed.  Host-side reads and writes convert to and from FP64.
 // Element-local dof order and node order follow lin3DHexa8.cpp:756-853.
 // A small k_cdx_loads kernel adds (dt^2/m) f_ext for the loaded dofs.
+#include <cuda.h>
 #include <cuda_runtime.h>
+#include <cudaTypedefs.h>
 
 #include <algorithm>
 #include <cmath>
@@ -40,14 +47,29 @@ namespace {
     } while (0)
 #define TRY(x) do { int st_ = (x); if (st_ != SVL_OK) return st_; } while (0)
 
-// Node tile owned by one CTA and derived sizes.
-constexpr int TX = 8, TY = 8, TZ = 4;
+constexpr int align_up(int x, int a) { return (x + a - 1) / a * a; }
+
+// Node tile owned by one CTA per pass and derived sizes.
+constexpr int TX = 8, TY = 8, TZ = 8;
 constexpr int HX = TX + 2, HY = TY + 2, HZ = TZ + 2;          // halo nodes
 constexpr int EX = TX + 1, EY = TY + 1, EZ = TZ + 1;          // elements touching the tile
-constexpr int NEL = EX * EY * EZ;                             // 405
-constexpr int NMT = (NEL + 127) / 128;                        // MMA tiles of 128 elements
-constexpr int NTHREADS = 256;
+constexpr int NEL = EX * EY * EZ;                             // 729
+constexpr int NMT = (NEL + 127) / 128;                        // 6 MMA tiles of 128 elements
+constexpr int NTHREADS = 512;                                 // 16 warps
+constexpr int NBUILD = 256;                                   // warps 0-7 build operands
+constexpr int ISSUE_WARP = 8;                                 // warp 8 issues the MMAs
+constexpr int UPD_WARP0 = 9;                                  // warps 9-15 gather and update
+constexpr int NUPD = NTHREADS - UPD_WARP0 * 32;               // 224 threads
+constexpr int EPI_WARP0 = 12;                                 // warps 12-15 also drain TMEM
+constexpr int NEPI = 128;
 constexpr int FSTRIDE = 25;                                   // padded row of element forces
+constexpr int RAWX = 40;                                      // TMA box: floats per halo row
+constexpr int RAW_SHIFT = 3;                                  // halo row starts 3 nodes left of x0-1
+constexpr int RAW_BYTES = RAWX * HY * HZ * 4;                 // 16000 B
+constexpr int LMX = 16;                                       // TMA box: lambda/mu floats per row
+constexpr int LM_SHIFT = 3;                                   // element row starts 3 left of x0-1
+constexpr int LM_BYTES = LMX * EY * EZ * 4;                   // 5184 B each
+constexpr int TILE_TX_BYTES = RAW_BYTES + 2 * LM_BYTES;       // bytes per tile by TMA
 
 // Canonical no-swizzle K-major operand layout: 8-row x 16-byte core matrices;
 // element (r, k) at (r/8)*SBO + (k/4)*LBO + (r%8)*16 + (k%4)*4 bytes.
@@ -55,33 +77,40 @@ constexpr int KDIM = 24;                                      // element dofs
 constexpr int LBO = 128;                                      // next core matrix along K
 constexpr int SBO = (KDIM / 4) * 128;                         // next 8 rows: 768 B
 constexpr int A_BYTES = (128 / 8) * SBO;                      // 12288 B per operand
-constexpr int B_BYTES = (48 / 8) * SBO;                       // 4608 B per operand
+constexpr int B_ROWS = 96;                                    // [K_stack hi (48 rows); K_stack lo (48 rows)]
+constexpr int B_BYTES = (B_ROWS / 8) * SBO;                   // 9216 B
 
-// Shared memory carve-up (bytes, 1024-aligned operands first).
-constexpr int OFF_AHI = 0;
-constexpr int OFF_ALO = OFF_AHI + A_BYTES;
-constexpr int OFF_BHI = OFF_ALO + A_BYTES;
-constexpr int OFF_BLO = OFF_BHI + 5120;                        // B_BYTES rounded to 1 KB
-constexpr int OFF_U = OFF_BLO + 5120;
-constexpr int OFF_LAM = OFF_U + HX * HY * HZ * 3 * 8;
-constexpr int OFF_MU = OFF_LAM + NEL * 4;
-constexpr int OFF_F = OFF_MU + NEL * 4;
-constexpr int align_up(int x, int a) { return (x + a - 1) / a * a; }
-constexpr int OFF_BAR = align_up(OFF_F + NEL * FSTRIDE * 4, 16);   // mbarrier: 8-byte aligned
-constexpr int OFF_TMEM = OFF_BAR + 16;
+constexpr int OFF_B = 0;
+constexpr int OFF_A = align_up(OFF_B + B_BYTES, 1024);       // [2 buffers][hi, lo]
+constexpr int A_STRIDE = 2 * A_BYTES;
+constexpr int OFF_TT = OFF_A + 2 * A_STRIDE;                   // [2 buffers] TMA tile: halo, lambda, mu
+constexpr int TT_LAM = align_up(RAW_BYTES, 128);                 // TMA tensor destinations: 128-byte aligned
+constexpr int TT_MU = align_up(TT_LAM + LM_BYTES, 128);
+constexpr int TT_STRIDE = align_up(TT_MU + LM_BYTES, 1024);
+constexpr int OFF_F = OFF_TT + 2 * TT_STRIDE;
+constexpr int OFF_BAR = align_up(OFF_F + NEL * FSTRIDE * 4, 16);
+constexpr int NBAR = 10;                                      // tma[2] a_full[2] a_empty[2] d_full[2] d_empty[2]
+constexpr int OFF_TMEM = OFF_BAR + NBAR * 8;
 constexpr int SMEM_BYTES = OFF_TMEM + 16;
-static_assert(OFF_BAR % 8 == 0 && OFF_TMEM % 4 == 0, "barrier / TMEM slot alignment");
-static_assert(OFF_AHI % 1024 == 0 && OFF_ALO % 1024 == 0 && OFF_BHI % 1024 == 0 && OFF_BLO % 1024 == 0,
-              "MMA operands start on 1 KB boundaries");
-static_assert(OFF_U % 8 == 0 && OFF_LAM % 4 == 0 && OFF_MU % 4 == 0 && OFF_F % 4 == 0, "staging alignment");
+static_assert(OFF_A % 1024 == 0 && A_STRIDE % 1024 == 0, "MMA operands on 1 KB boundaries");
+static_assert(OFF_TT % 1024 == 0 && TT_STRIDE % 1024 == 0 && TT_LAM % 128 == 0 && TT_MU % 128 == 0, "TMA destinations");
+static_assert(OFF_F % 16 == 0 && OFF_BAR % 8 == 0 && OFF_TMEM % 4 == 0, "alignment");
+static_assert(SMEM_BYTES <= 227 * 1024, "shared memory budget");
+static_assert(TX * TY * TZ <= 3 * NUPD, "three owned nodes per update thread at most");
 
-constexpr uint32_t TMEM_COLS = 64;
-constexpr long kWaitLimit = 2000000;    // bounded mbarrier wait (well under a second)
+constexpr uint32_t TMEM_COLS = 512;     // two buffers of [hi chain: 96 cols | lo chain: 48 cols]
+constexpr uint32_t ACC_COLS = 256;
+constexpr uint32_t LO_COLS = 128;       // offset of the lo chain inside a buffer
+constexpr long kWaitLimit = 4000000;    // bounded mbarrier wait
 
-// Instruction descriptor for tcgen05.mma.kind::tf32: D = F32 (bits 4-5),
+// Instruction descriptors for tcgen05.mma.kind::tf32: D = F32 (bits 4-5),
 // A = B = TF32 (bits 7-9, 10-12), both K-major, N >> 3 (bits 17-22),
 // M >> 4 (bits 24-28).
-constexpr uint32_t kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((48u >> 3) << 17) | ((128u >> 4) << 24);
+constexpr uint32_t idesc_tf32(uint32_t m, uint32_t n) {
+    return (1u << 4) | (2u << 7) | (2u << 10) | ((n >> 3) << 17) | ((m >> 4) << 24);
+}
+constexpr uint32_t kIdescN96 = idesc_tf32(128, 96);
+constexpr uint32_t kIdescN48 = idesc_tf32(128, 48);
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
     return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -99,16 +128,24 @@ __device__ __forceinline__ float to_tf32(float x) {
     return __uint_as_float(r);
 }
 
-__device__ __forceinline__ void mma_tf32(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+__device__ __forceinline__ void mma_tf32(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t accumulate) {
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
         "setp.ne.b32 p, %4, 0;\n\t"
         "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n"
-        :: "r"(tmem_d), "l"(adesc), "l"(bdesc), "r"(kIdesc), "r"(accumulate));
+        :: "r"(tmem_d), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
 }
 
 __device__ __forceinline__ void mma_commit(uint32_t bar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" :: "r"(bar) : "memory");
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" :: "r"(bar) : "memory");
 }
 
 __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
@@ -124,201 +161,357 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
     return false;
 }
 
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
-    uint32_t r[16];
+// TMA: 4D tiled load, completion counted on `bar` (expect_tx set by the caller).
+__device__ __forceinline__ void tma_load4(const CUtensorMap* tmap, uint32_t dst, uint32_t bar, int x, int y, int z, int w) {
     asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-        : "r"(taddr));
+        "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], [%6];"
+        :: "r"(dst), "l"(reinterpret_cast<uint64_t>(tmap)), "r"(x), "r"(y), "r"(z), "r"(w), "r"(bar) : "memory");
+}
+
+template <int N>
+__device__ __forceinline__ void tmem_ld(uint32_t taddr, float* v);
+template <>
+__device__ __forceinline__ void tmem_ld<8>(uint32_t taddr, float* v) {
+    uint32_t r[8];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+                 : "r"(taddr));
 #pragma unroll
-    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+    for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
 }
 
 struct CdxView {
     int nx, ny, nz, ninst;
-    long long nn, ne;                // nodes / elements per instance
-    const double* __restrict__ ucur; // [inst][node][3]
-    double* uprev;                   // read u_{n-1}, write u_{n+1} (same node, same thread)
-    const float* __restrict__ lam;   // [inst][element]
-    const float* __restrict__ mu;
-    const float* __restrict__ cdof;  // [inst][node][3]  dt^2/m, 0 on restrained dofs
-    const float* __restrict__ bop;   // [2][B_BYTES/4] hi, lo operand images
-    int* step;
+    int pitch;                           // floats per padded x-row of the state arrays
+    int ntx, nty, ntz, ntiles;
+    const float* __restrict__ ul_cur;    // u_n low part   [inst][z][y][pitch]
+    float* uh_prev;                      // read u_{n-1}, write u_{n+1} (same dof, same thread)
+    float* ul_prev;
+    const float* __restrict__ cdof;      // [inst][z][y][pitch]  dt^2/m, 0 on restrained dofs
+    const float* __restrict__ bop;       // [B_ROWS x 24] hi then lo operand image
+    // external loads grouped by tile, then by dof
+    const int* __restrict__ tl_ptr;      // [ntiles+1] into the unique-dof arrays
+    const long long* __restrict__ ld_dof;// padded index of the dof
+    const int* __restrict__ ld_ptr;      // [nld+1] into ser/coef
+    const int* __restrict__ ld_ser;
+    const double* __restrict__ ld_coef;
+    const int* __restrict__ s_ptr;
+    const double* __restrict__ s_val;
+    int k;                               // step index
     int* status;
 };
 
-__global__ void __launch_bounds__(NTHREADS, 2) k_cdx_step(CdxView v) {
+// Error-free transformations on FP32 (Knuth TwoSum, Dekker FastTwoSum).
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+__device__ __forceinline__ void fast_two_sum(float a, float b, float& s, float& e) {
+    s = __fadd_rn(a, b);
+    e = __fsub_rn(b, __fsub_rn(s, a));
+}
+// (ah + al) + (bh + bl) as a normalised pair.
+__device__ __forceinline__ void df_add(float ah, float al, float bh, float bl, float& rh, float& rl) {
+    float s, e;
+    two_sum(ah, bh, s, e);
+    e = __fadd_rn(e, __fadd_rn(al, bl));
+    fast_two_sum(s, e, rh, rl);
+}
+
+// AND of `v` over the warps 9-15 group, on named barrier 2 (also a memory barrier for the group).
+__device__ __forceinline__ bool group_and(bool v) {
+    uint32_t r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\t"
+        "setp.ne.u32 p, %1, 0;\n\t"
+        "bar.red.and.pred q, 2, %2, p;\n\t"
+        "selp.u32 %0, 1, 0, q;\n\t}\n"
+        : "=r"(r) : "r"((uint32_t)v), "r"(NUPD) : "memory");
+    return r != 0;
+}
+
+struct TileOrigin { int inst, x0, y0, z0; };
+__device__ __forceinline__ TileOrigin tile_origin(const CdxView& v, int tile) {
+    TileOrigin o;
+    int r = tile;
+    const int tx = r % v.ntx; r /= v.ntx;
+    const int ty = r % v.nty; r /= v.nty;
+    const int tz = r % v.ntz;
+    o.inst = r / v.ntz;
+    o.x0 = tx * TX; o.y0 = ty * TY; o.z0 = tz * TZ;
+    return o;
+}
+
+__global__ void __launch_bounds__(NTHREADS, 1)
+k_cdx_step(const __grid_constant__ CUtensorMap tmap_u, const __grid_constant__ CUtensorMap tmap_lam,
+           const __grid_constant__ CUtensorMap tmap_mu, CdxView v) {
     extern __shared__ __align__(1024) unsigned char smem[];
     const int tid = threadIdx.x;
     const int warp = tid >> 5, lane = tid & 31;
-    const int ntz = (v.nz + 1 + TZ - 1) / TZ;
-    const int inst = blockIdx.z / ntz;
-    const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY, z0 = (blockIdx.z % ntz) * TZ;
     const int nxn = v.nx + 1, nyn = v.ny + 1, nzn = v.nz + 1;
-    if (tid == 0 && blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0) v.step[0] += 1;
-
-    double* sU = reinterpret_cast<double*>(smem + OFF_U);
-    float* sLam = reinterpret_cast<float*>(smem + OFF_LAM);
-    float* sMu = reinterpret_cast<float*>(smem + OFF_MU);
     float* sF = reinterpret_cast<float*>(smem + OFF_F);
-    float* sAhi = reinterpret_cast<float*>(smem + OFF_AHI);
-    float* sAlo = reinterpret_cast<float*>(smem + OFF_ALO);
-    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + OFF_BAR);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + OFF_BAR);
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + OFF_TMEM);
+    const uint32_t b_tma[2] = {smem_u32(bars + 0), smem_u32(bars + 1)};
+    const uint32_t b_afull[2] = {smem_u32(bars + 2), smem_u32(bars + 3)};
+    const uint32_t b_aempty[2] = {smem_u32(bars + 4), smem_u32(bars + 5)};
+    const uint32_t b_dfull[2] = {smem_u32(bars + 6), smem_u32(bars + 7)};
+    const uint32_t b_dempty[2] = {smem_u32(bars + 8), smem_u32(bars + 9)};
+    // TMA destinations and MMA operands assume a 1 KB aligned dynamic window
+    if (smem_u32(smem) & 1023u) {
+        if (tid == 0) atomicOr(v.status, 2);
+        return;
+    }
 
-    // -- TMEM allocation (warp 0) and the MMA barrier ------------------------
+    // -- once per CTA: TMEM, barriers, B operand ----------------------------
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
                      :: "r"(smem_u32(tmem_slot)), "r"(TMEM_COLS) : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
     if (tid == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(bar)) : "memory");
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(b_tma[b], 1);
+            mbar_init(b_afull[b], NBUILD);
+            mbar_init(b_aempty[b], 1);
+            mbar_init(b_dfull[b], 1);
+            mbar_init(b_dempty[b], NEPI);
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-
-    // -- stage B operands, displacement halo and lambda/mu ------------------
     {
         const float4* src = reinterpret_cast<const float4*>(v.bop);
-        float4* dhi = reinterpret_cast<float4*>(smem + OFF_BHI);
-        float4* dlo = reinterpret_cast<float4*>(smem + OFF_BLO);
-        for (int i = tid; i < B_BYTES / 16; i += NTHREADS) {
-            dhi[i] = src[i];
-            dlo[i] = src[B_BYTES / 16 + i];
-        }
+        float4* dst = reinterpret_cast<float4*>(smem + OFF_B);
+        for (int i = tid; i < B_BYTES / 16; i += NTHREADS) dst[i] = src[i];
     }
-    const double* ug = v.ucur + (size_t)inst * v.nn * 3;
-    for (int i = tid; i < HX * HY * HZ * 3; i += NTHREADS) {
-        const int c = i % 3, hn = i / 3;
-        const int hx = hn % HX, hy = (hn / HX) % HY, hz = hn / (HX * HY);
-        const int gx = x0 - 1 + hx, gy = y0 - 1 + hy, gz = z0 - 1 + hz;
-        double val = 0.0;
-        if (gx >= 0 && gx < nxn && gy >= 0 && gy < nyn && gz >= 0 && gz < nzn)
-            val = ug[(((size_t)gz * nyn + gy) * nxn + gx) * 3 + c];
-        sU[i] = val;
-    }
-    for (int le = tid; le < NEL; le += NTHREADS) {
-        const int lx = le % EX, ly = (le / EX) % EY, lz = le / (EX * EY);
-        const int ex = x0 - 1 + lx, ey = y0 - 1 + ly, ez = z0 - 1 + lz;
-        float l = 0.f, m = 0.f;
-        if (ex >= 0 && ex < v.nx && ey >= 0 && ey < v.ny && ez >= 0 && ez < v.nz) {
-            const size_t g = (size_t)inst * v.ne + ((size_t)ez * v.ny + ey) * v.nx + ex;
-            l = v.lam[g];
-            m = v.mu[g];
-        }
-        sLam[le] = l;
-        sMu[le] = m;
-    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = *tmem_slot;
-    const uint32_t bar_a = smem_u32(bar);
+
+    auto issue_tile = [&](int tile, int buf) {
+        const TileOrigin o = tile_origin(v, tile);
+        const uint32_t dst = smem_u32(smem + OFF_TT + buf * TT_STRIDE);
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" :: "r"(b_tma[buf]), "r"(TILE_TX_BYTES) : "memory");
+        tma_load4(&tmap_u, dst, b_tma[buf], (o.x0 - 1 - RAW_SHIFT) * 3, o.y0 - 1, o.z0 - 1, o.inst);
+        tma_load4(&tmap_lam, dst + TT_LAM, b_tma[buf], o.x0 - 1 - LM_SHIFT, o.y0 - 1, o.z0 - 1, o.inst);
+        tma_load4(&tmap_mu, dst + TT_MU, b_tma[buf], o.x0 - 1 - LM_SHIFT, o.y0 - 1, o.z0 - 1, o.inst);
+    };
+    const int ntile_cta = v.ntiles > (int)blockIdx.x ? (v.ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
     bool ok = true;
 
-    // -- element forces, one 128-element MMA tile at a time ----------------
-    for (int t = 0; t < NMT; ++t) {
-        {   // build A rows: thread pair per element, 4 nodes (12 dofs) each
-            const int m = tid >> 1, half = tid & 1;
-            const int le = t * 128 + m;
-            float hi[12], lo[12];
-            if (le < NEL) {
-                const int lx = le % EX, ly = (le / EX) % EY, lz = le / (EX * EY);
+    if (warp < NBUILD / 32) {
+        // ===== builders: A operand rows (element x 24 dofs), TF32 hi / lo =====
+        uint32_t ph_tma[2] = {0, 0}, ph_aempty[2] = {1, 1};
+        const int h = tid >> 7, m = tid & 127;
+        for (int it = 0, mt = 0; it < ntile_cta && ok; ++it) {
+            const int buf = it & 1;
+            ok = mbar_wait(b_tma[buf], ph_tma[buf]);
+            ph_tma[buf] ^= 1;
+            const float* raw = reinterpret_cast<const float*>(smem + OFF_TT + buf * TT_STRIDE);
+            for (int t = 0; t < NMT && ok; ++t, ++mt) {
+                const int b = mt & 1;
+                ok = mbar_wait(b_aempty[b], ph_aempty[b]);
+                ph_aempty[b] ^= 1;
+                if (!ok) break;
+                const int le = t * 128 + m;
+                float hv[12], lv[12];
+                if (le < NEL) {
+                    const int lx = le % EX, ly = (le / EX) % EY, lz = le / (EX * EY);
+                    // nodes n1..n4 (h = 0) or n5..n8 (h = 1) of the element, in the raw halo rows
+                    const int r0 = (lz + h) * HY + ly;
+                    const float* p0 = raw + r0 * RAWX + (RAW_SHIFT + lx) * 3;
+                    const float* p1 = p0 + RAWX;
+                    const float u[12] = {p0[0], p0[1], p0[2], p0[3], p0[4], p0[5],
+                                         p1[3], p1[4], p1[5], p1[0], p1[1], p1[2]};
 #pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    const int a = half * 4 + q;
-                    // lin3DHexa8 node offsets: n1..n8
-                    const int dx = (a == 1 || a == 2 || a == 5 || a == 6) ? 1 : 0;
-                    const int dy = (a == 2 || a == 3 || a == 6 || a == 7) ? 1 : 0;
-                    const int dz = (a >= 4) ? 1 : 0;
-                    const int hn = ((lz + dz) * HY + (ly + dy)) * HX + (lx + dx);
+                    for (int i = 0; i < 12; ++i) {
+                        hv[i] = to_tf32(u[i]);
+                        lv[i] = to_tf32(__fsub_rn(u[i], hv[i]));
+                    }
+                } else {
 #pragma unroll
-                    for (int c = 0; c < 3; ++c) {
-                        const double u = sU[hn * 3 + c];
-                        const float h = to_tf32(__double2float_rn(u));
-                        hi[q * 3 + c] = h;
-                        lo[q * 3 + c] = to_tf32(__double2float_rn(u - (double)h));
+                    for (int i = 0; i < 12; ++i) { hv[i] = 0.f; lv[i] = 0.f; }
+                }
+                unsigned char* Ab = smem + OFF_A + b * A_STRIDE;
+                const int off = (m >> 3) * SBO + (3 * h) * LBO + (m & 7) * 16;
+#pragma unroll
+                for (int g = 0; g < 3; ++g) {
+                    *reinterpret_cast<float4*>(Ab + off + g * LBO) = make_float4(hv[4 * g], hv[4 * g + 1], hv[4 * g + 2], hv[4 * g + 3]);
+                    *reinterpret_cast<float4*>(Ab + A_BYTES + off + g * LBO) = make_float4(lv[4 * g], lv[4 * g + 1], lv[4 * g + 2], lv[4 * g + 3]);
+                }
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                mbar_arrive(b_afull[b]);
+            }
+        }
+    } else if (warp == ISSUE_WARP) {
+        // ===== MMA issuer: two independent accumulator chains per M-tile =====
+        if (lane == 0) {
+            uint32_t ph_afull[2] = {0, 0}, ph_dempty[2] = {1, 1};
+            const uint32_t bB = smem_u32(smem + OFF_B);
+            const int total = ntile_cta * NMT;
+            for (int mt = 0; mt < total && ok; ++mt) {
+                const int b = mt & 1;
+                ok = mbar_wait(b_afull[b], ph_afull[b]) && mbar_wait(b_dempty[b], ph_dempty[b]);
+                ph_afull[b] ^= 1;
+                ph_dempty[b] ^= 1;
+                if (!ok) break;
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint32_t a_hi = smem_u32(smem + OFF_A + b * A_STRIDE), a_lo = a_hi + A_BYTES;
+                const uint32_t d = tmem + (uint32_t)b * ACC_COLS;
+#pragma unroll
+                for (int ks = 0; ks < KDIM / 8; ++ks) {       // three K=8 steps (2 core matrices each)
+                    const uint32_t koff = ks * 2 * LBO;
+                    // [d, d+96): A_hi . [K hi; K lo]     [d+128, d+176): A_lo . K hi
+                    mma_tf32(d, make_desc(a_hi + koff), make_desc(bB + koff), kIdescN96, ks > 0);
+                    mma_tf32(d + LO_COLS, make_desc(a_lo + koff), make_desc(bB + koff), kIdescN48, ks > 0);
+                }
+                mma_commit(b_dfull[b]);
+                mma_commit(b_aempty[b]);
+            }
+        }
+    } else {
+        // ===== warps 9-15: TMA, TMEM drain (12-15), ordered gather, update ======
+        const int gt = tid - UPD_WARP0 * 32;                  // 0..223
+        uint32_t ph_tma[2] = {0, 0}, ph_dfull[2] = {0, 0};
+        bool pending[2] = {false, false};
+        if (gt == 0) {
+            for (int it = 0; it < 2 && it < ntile_cta; ++it) issue_tile(blockIdx.x + it * gridDim.x, it);
+        }
+        for (int it = 0; it < 2 && it < ntile_cta; ++it) pending[it] = true;
+        for (int it = 0, mt = 0; it < ntile_cta && ok; ++it) {
+            const int tile = blockIdx.x + it * gridDim.x;
+            const int buf = it & 1;
+            const TileOrigin o = tile_origin(v, tile);
+            const unsigned char* tt = smem + OFF_TT + buf * TT_STRIDE;
+            const float* raw = reinterpret_cast<const float*>(tt);
+            const float* tlam = reinterpret_cast<const float*>(tt + TT_LAM);
+            const float* tmu = reinterpret_cast<const float*>(tt + TT_MU);
+            ok = mbar_wait(b_tma[buf], ph_tma[buf]);
+            ph_tma[buf] ^= 1;
+            pending[buf] = false;
+            if (warp >= EPI_WARP0) {
+                const int q = warp - EPI_WARP0;                   // TMEM lane quarter
+                for (int t = 0; t < NMT && ok; ++t, ++mt) {
+                    const int b = mt & 1;
+                    ok = mbar_wait(b_dfull[b], ph_dfull[b]);
+                    ph_dfull[b] ^= 1;
+                    if (!ok) break;
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                    const uint32_t row = tmem + (uint32_t)b * ACC_COLS + ((uint32_t)(q * 32) << 16);
+                    const int le = t * 128 + q * 32 + lane;
+                    const int lx = le % EX, lr = min(le, NEL - 1) / EX;          // lr = lz*EY + ly
+                    const float l = tlam[lr * LMX + LM_SHIFT + lx], mu = tmu[lr * LMX + LM_SHIFT + lx];
+                    float f[24];
+                    // hi chain: cols 0-23 K_lambda.u, 24-47 K_mu.u (K hi), 48-95 the same with K lo;
+                    // lo chain: cols 128-151 K_lambda.u_lo, 152-175 K_mu.u_lo (K hi)
+#pragma unroll
+                    for (int g = 0; g < 3; ++g) {
+                        float a[8], c[8], e[8];
+                        tmem_ld<8>(row + 8 * g, a);
+                        tmem_ld<8>(row + 48 + 8 * g, c);
+                        tmem_ld<8>(row + LO_COLS + 8 * g, e);
+                        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+                        for (int i = 0; i < 8; ++i) f[8 * g + i] = l * (a[i] + c[i] + e[i]);
+                    }
+#pragma unroll
+                    for (int g = 0; g < 3; ++g) {
+                        float a[8], c[8], e[8];
+                        tmem_ld<8>(row + 24 + 8 * g, a);
+                        tmem_ld<8>(row + 72 + 8 * g, c);
+                        tmem_ld<8>(row + LO_COLS + 24 + 8 * g, e);
+                        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+                        for (int i = 0; i < 8; ++i) f[8 * g + i] += mu * (a[i] + c[i] + e[i]);
+                    }
+                    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+                    mbar_arrive(b_dempty[b]);
+                    if (le < NEL) {
+#pragma unroll
+                        for (int j = 0; j < 24; ++j) sF[le * FSTRIDE + j] = f[j];
                     }
                 }
             } else {
-#pragma unroll
-                for (int i = 0; i < 12; ++i) { hi[i] = 0.f; lo[i] = 0.f; }
+                mt += NMT;
             }
-#pragma unroll
-            for (int i = 0; i < 12; ++i) {
-                const int k = half * 12 + i;
-                const int off = (m >> 3) * (SBO / 4) + (k >> 2) * (LBO / 4) + (m & 7) * 4 + (k & 3);
-                sAhi[off] = hi[i];
-                sAlo[off] = lo[i];
-            }
-        }
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        __syncthreads();
-        if (tid == 0) {
-            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const uint32_t a_hi = smem_u32(smem + OFF_AHI), a_lo = smem_u32(smem + OFF_ALO);
-            const uint32_t b_hi = smem_u32(smem + OFF_BHI), b_lo = smem_u32(smem + OFF_BLO);
-            uint32_t acc = 0;
-#pragma unroll
-            for (int ks = 0; ks < KDIM / 8; ++ks) {           // three K=8 steps (2 core matrices each)
-                const uint32_t koff = ks * 2 * LBO;
-                mma_tf32(tmem, make_desc(a_hi + koff), make_desc(b_hi + koff), acc); acc = 1;
-                mma_tf32(tmem, make_desc(a_hi + koff), make_desc(b_lo + koff), 1);
-                mma_tf32(tmem, make_desc(a_lo + koff), make_desc(b_hi + koff), 1);
-            }
-            mma_commit(bar_a);
-        }
-        __syncwarp();
-        ok = mbar_wait(bar_a, (uint32_t)(t & 1));
-        ok = __syncthreads_and(ok) != 0;          // keep the .sync.aligned loads warp-uniform
-        if (!ok && tid == 0) atomicOr(v.status, 1);
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        if (warp < 4 && ok) {
-            float d[48];
-            const uint32_t row = tmem + ((uint32_t)(warp * 32) << 16);
-            tmem_ld16(row + 0, d);
-            tmem_ld16(row + 16, d + 16);
-            tmem_ld16(row + 32, d + 32);
-            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-            const int le = t * 128 + warp * 32 + lane;
-            if (le < NEL) {
-                const float l = sLam[le], m = sMu[le];
-#pragma unroll
-                for (int j = 0; j < 24; ++j) sF[le * FSTRIDE + j] = l * d[j] + m * d[24 + j];
-            }
-        }
-        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-        __syncthreads();
-        if (!ok) break;
-    }
+            // all element forces of this tile are in sF (group barrier; ok made uniform)
+            ok = group_and(ok);
+            if (!ok) break;
 
-    // -- ordered gather and FP64 update of the owned nodes ------------------
-    if (ok) {
-        const int ox = tid % TX, oy = (tid / TX) % TY, oz = tid / (TX * TY);   // 256 = TX*TY*TZ
-        const int gx = x0 + ox, gy = y0 + oy, gz = z0 + oz;
-        if (gx < nxn && gy < nyn && gz < nzn) {
-            // (element offset, local node) in ascending element-tag order
-            const int sel[8][4] = {{0, 0, 0, 6}, {1, 0, 0, 7}, {0, 1, 0, 5}, {1, 1, 0, 4},
-                                   {0, 0, 1, 2}, {1, 0, 1, 3}, {0, 1, 1, 1}, {1, 1, 1, 0}};
-            float f[3] = {0.f, 0.f, 0.f};
+            // -- ordered gather and compensated update of the owned nodes ------
+            const int nxn_ = nxn, nyn_ = nyn, nzn_ = nzn;
+            for (int nd = gt; nd < TX * TY * TZ; nd += NUPD) {
+                const int ox = nd & 7, oy = (nd >> 3) & 7, oz = nd >> 6;
+                const int gx = o.x0 + ox, gy = o.y0 + oy, gz = o.z0 + oz;
+                if (gx >= nxn_ || gy >= nyn_ || gz >= nzn_) continue;
+                const size_t gbase = ((((size_t)o.inst * nzn_ + gz) * nyn_ + gy) * v.pitch) + (size_t)gx * 3;
+                float al[3], bh[3], bl[3], cc[3];
 #pragma unroll
-            for (int s = 0; s < 8; ++s) {
-                const int le = ((oz + sel[s][2]) * EY + (oy + sel[s][1])) * EX + (ox + sel[s][0]);
-                const float* fe = sF + le * FSTRIDE + sel[s][3] * 3;
-                f[0] += fe[0]; f[1] += fe[1]; f[2] += fe[2];
-            }
-            const size_t node = ((size_t)gz * nyn + gy) * nxn + gx;
-            const size_t base = ((size_t)inst * v.nn + node) * 3;
-            const int hn = ((oz + 1) * HY + (oy + 1)) * HX + (ox + 1);
+                for (int c = 0; c < 3; ++c) {
+                    al[c] = v.ul_cur[gbase + c];
+                    bh[c] = v.uh_prev[gbase + c];
+                    bl[c] = v.ul_prev[gbase + c];
+                    cc[c] = v.cdof[gbase + c];
+                }
+                // (element offset, local node) in ascending element-tag order
+                const int sel[8][4] = {{0, 0, 0, 6}, {1, 0, 0, 7}, {0, 1, 0, 5}, {1, 1, 0, 4},
+                                       {0, 0, 1, 2}, {1, 0, 1, 3}, {0, 1, 1, 1}, {1, 1, 1, 0}};
+                float f[3] = {0.f, 0.f, 0.f};
 #pragma unroll
-            for (int c = 0; c < 3; ++c) {
-                const double u = sU[hn * 3 + c];
-                const double up = v.uprev[base + c];
-                const double cc = (double)v.cdof[base + c];
-                v.uprev[base + c] = (u + (u - up)) - cc * (double)f[c];
+                for (int s2 = 0; s2 < 8; ++s2) {
+                    const int le = ((oz + sel[s2][2]) * EY + (oy + sel[s2][1])) * EX + (ox + sel[s2][0]);
+                    const float* fe = sF + le * FSTRIDE + sel[s2][3] * 3;
+                    f[0] += fe[0]; f[1] += fe[1]; f[2] += fe[2];
+                }
+                const float* ah = raw + ((oz + 1) * HY + (oy + 1)) * RAWX + (RAW_SHIFT + ox + 1) * 3;
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    const float inc = -cc[c] * f[c];
+                    float dh, dl2, Dh, Dl, nh, nl;
+                    df_add(ah[c], al[c], -bh[c], -bl[c], dh, dl2);   // u_n - u_{n-1}
+                    df_add(dh, dl2, inc, 0.f, Dh, Dl);               // + (dt^2/m)(-f_int)
+                    df_add(ah[c], al[c], Dh, Dl, nh, nl);            // u_{n+1}
+                    v.uh_prev[gbase + c] = nh;
+                    v.ul_prev[gbase + c] = nl;
+                }
             }
+            asm volatile("bar.sync 2, %0;" :: "r"(NUPD) : "memory");   // sF and the halo are free again
+            // -- external loads on this tile's dofs: (dt^2/m) f_ext(k) -------
+            const int tl0 = v.tl_ptr[tile], tl1 = v.tl_ptr[tile + 1];
+            if (tl1 > tl0) {
+                for (int j2 = tl0 + gt; j2 < tl1; j2 += NUPD) {
+                    double fx = 0.0;
+                    for (int e = v.ld_ptr[j2]; e < v.ld_ptr[j2 + 1]; ++e) {
+                        const int sidx = v.ld_ser[e];
+                        const int b0 = v.s_ptr[sidx], n = v.s_ptr[sidx + 1] - b0;
+                        fx += v.ld_coef[e] * ((v.k >= 0 && v.k < n) ? v.s_val[b0 + v.k] : 0.0);
+                    }
+                    const long long d = v.ld_dof[j2];
+                    const double inc = (double)v.cdof[d] * fx;
+                    const float ih = (float)inc, il = (float)(inc - (double)ih);
+                    float nh, nl;
+                    df_add(v.uh_prev[d], v.ul_prev[d], ih, il, nh, nl);
+                    v.uh_prev[d] = nh;
+                    v.ul_prev[d] = nl;
+                }
+            }
+            // this tile's buffer is free: bring in the tile after next
+            if (gt == 0 && it + 2 < ntile_cta) {
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                issue_tile(blockIdx.x + (it + 2) * gridDim.x, buf);
+            }
+            if (it + 2 < ntile_cta) pending[buf] = true;
+        }
+        if (!ok) {
+            if (gt == 0) atomicOr(v.status, 1);
+            for (int b = 0; b < 2; ++b)            // never leave with a TMA copy in flight
+                if (pending[b]) mbar_wait(b_tma[b], ph_tma[b]);
         }
     }
+    if (!ok) atomicOr(v.status, 1);
 
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
@@ -328,30 +521,15 @@ __global__ void __launch_bounds__(NTHREADS, 2) k_cdx_step(CdxView v) {
     }
 }
 
-// u_{n+1} += (dt^2/m) f_ext(k) on the loaded dofs (one thread per dof,
-// entries of a dof summed in input order).
-__global__ void k_cdx_loads(double* unext, const float* __restrict__ cdof, int nld, const long long* __restrict__ ld_dof,
-                            const int* __restrict__ ld_ptr, const int* __restrict__ ld_ser, const double* __restrict__ ld_coef,
-                            const int* __restrict__ s_ptr, const double* __restrict__ s_val, const int* step) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nld) return;
-    const int k = step[0];
-    double f = 0.0;
-    for (int j = ld_ptr[i]; j < ld_ptr[i + 1]; ++j) {
-        const int s = ld_ser[j];
-        const int b = s_ptr[s], n = s_ptr[s + 1] - b;
-        f += ld_coef[j] * ((k >= 0 && k < n) ? s_val[b + k] : 0.0);
-    }
-    const long long d = ld_dof[i];
-    unext[d] += (double)cdof[d] * f;
-}
-
-// V and A of the last step from u_{n+1}, u_n, u_{n-1} (CentralDifference.cpp:141-144).
-__global__ void k_cdx_va(const double* unext, const double* ucur, const double* uprev_copy, double* V, double* A,
-                         long long n, double inv_2dt, double inv_dt2) {
+// V and A of the last step from u_{n+1}, u_n, u_{n-1} (CentralDifference.cpp:141-144),
+// evaluated in FP64 from the compensated pairs (once per run).
+__global__ void k_cdx_va(const float* nh, const float* nl, const float* ch, const float* cl, const float* ph,
+                         const float* pl, double* V, double* A, long long n, double inv_2dt, double inv_dt2) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const double un = unext[i], u = ucur[i], up = uprev_copy[i];
+    const double un = (double)nh[i] + (double)nl[i];
+    const double u = (double)ch[i] + (double)cl[i];
+    const double up = (double)ph[i] + (double)pl[i];
     const double dU = un - u;
     V[i] = inv_2dt * (u + dU - up);
     A[i] = inv_dt2 * (dU - u + up);
@@ -372,20 +550,28 @@ float host_tf32(double x) {
 struct svl_cdx {
     int nx = 0, ny = 0, nz = 0, ninst = 0;
     long long nn = 0, ne = 0, ntotal = 0;
+    int pitch = 0;                       // floats per padded x-row (multiple of 4)
+    long long nstate = 0;                // padded state length (all instances)
+    int ntx = 0, nty = 0, ntz = 0, ntiles = 0, grid = 0;
     double dt = 0;
     cudaStream_t stream = nullptr;
     std::vector<void*> allocs;
-    double* u[2] = {nullptr, nullptr};
-    double* uprev_copy = nullptr;
+    float* uh[2] = {nullptr, nullptr};   // compensated displacement pairs (hi, lo), padded rows
+    float* ul[2] = {nullptr, nullptr};
+    float* ph_copy = nullptr;            // u_{n-1} kept for V/A of the last step
+    float* pl_copy = nullptr;
     double* V = nullptr;
     double* A = nullptr;
     float *lam = nullptr, *mu = nullptr, *cdof = nullptr, *bop = nullptr;
-    int *step = nullptr, *status = nullptr;
+    int* status = nullptr;
+    int *tl_ptr = nullptr, *ld_ptr = nullptr, *ld_ser = nullptr, *s_ptr = nullptr;
     long long* ld_dof = nullptr;
-    int *ld_ptr = nullptr, *ld_ser = nullptr, *s_ptr = nullptr;
     double *ld_coef = nullptr, *s_val = nullptr;
-    int nld = 0;
-    int cur = 0;                     // index of u_n in u[]
+    int pe = 0;                          // floats per padded element row of lambda/mu
+    CUtensorMap tmap[2];                 // halo maps of uh[0], uh[1]
+    CUtensorMap tmap_lam, tmap_mu;
+    std::vector<long long> pad_index;    // total dof (node*3+c) -> padded position, one instance
+    int cur = 0;                         // index of u_n in uh/ul
     int64_t launches = 0, launches_last = 0;
     bool va_valid = false;
 
@@ -411,6 +597,31 @@ struct svl_cdx {
         if (stream) cudaStreamDestroy(stream);
     }
 };
+
+// 4D tiled map {pitch, ny, nz, ninst} floats with box {bx, by, bz, 1};
+// out-of-range elements read as zero.
+static int make_map(float* base, int pitch, int ny, int nz, int ninst, int bx, int by, int bz, CUtensorMap* map) {
+    static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+    if (!encode) {
+        cudaDriverEntryPointQueryResult q;
+        void* fn = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess || !fn) {
+            set_error("cuTensorMapEncodeTiled is not available from the driver");
+            return SVL_ERR_CUDA;
+        }
+        encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+    }
+    const cuuint64_t dims[4] = {(cuuint64_t)pitch, (cuuint64_t)ny, (cuuint64_t)nz, (cuuint64_t)ninst};
+    const cuuint64_t strides[3] = {(cuuint64_t)pitch * 4, (cuuint64_t)pitch * 4 * ny, (cuuint64_t)pitch * 4 * ny * nz};
+    const cuuint32_t box[4] = {(cuuint32_t)bx, (cuuint32_t)by, (cuuint32_t)bz, 1};
+    const cuuint32_t estr[4] = {1, 1, 1, 1};
+    const CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, base, dims, strides, box, estr,
+                              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                              CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) { set_error("cuTensorMapEncodeTiled failed (%d)", (int)r); return SVL_ERR_CUDA; }
+    return SVL_OK;
+}
 
 static int cdx_check_instance(const svl_grid_spec* g, const HostModel& m, int inst) {
     const int nx = g->ne[0], ny = g->ne[1], nz = g->ne[2];
@@ -444,6 +655,25 @@ static int cdx_check_instance(const svl_grid_spec* g, const HostModel& m, int in
     return SVL_OK;
 }
 
+static void split_pair(double x, float& hi, float& lo) {
+    hi = (float)x;
+    lo = (float)(x - (double)hi);
+}
+
+// Device pair (hi, lo) of instance `inst` -> FP64 total-dof vector.
+static int fetch_pair(svl_cdx* h, const float* dh, const float* dl, int inst, double* out) {
+    const size_t per = h->nstate / h->ninst;
+    std::vector<float> hi(per), lo(per);
+    CUDA_TRY(cudaMemcpyAsync(hi.data(), dh + (size_t)inst * per, per * 4, cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(cudaMemcpyAsync(lo.data(), dl + (size_t)inst * per, per * 4, cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    for (long long t = 0; t < h->ntotal; ++t) {
+        const long long p = h->pad_index[t];
+        out[t] = (double)hi[p] + (double)lo[p];
+    }
+    return SVL_OK;
+}
+
 extern "C" {
 
 int svl_cdx_create(const svl_grid_spec* g, int32_t ninst, const svl_model_desc* models, const svl_load_desc* loads,
@@ -459,13 +689,28 @@ int svl_cdx_create(const svl_grid_spec* g, int32_t ninst, const svl_model_desc* 
     svl_cdx* h = new svl_cdx();
     auto fail = [&](int st) { delete h; return st; };
     h->nx = g->ne[0]; h->ny = g->ne[1]; h->nz = g->ne[2]; h->ninst = ninst;
-    h->nn = (long long)(h->nx + 1) * (h->ny + 1) * (h->nz + 1);
+    const int nxn = h->nx + 1, nyn = h->ny + 1, nzn = h->nz + 1;
+    h->nn = (long long)nxn * nyn * nzn;
     h->ne = (long long)h->nx * h->ny * h->nz;
     h->ntotal = h->nn * 3;
+    h->pitch = (nxn * 3 + 3) / 4 * 4;
+    const long long per = (long long)h->pitch * nyn * nzn;
+    h->nstate = per * ninst;
+    h->ntx = (nxn + TX - 1) / TX; h->nty = (nyn + TY - 1) / TY; h->ntz = (nzn + TZ - 1) / TZ;
+    const long long ntiles = (long long)h->ntx * h->nty * h->ntz * ninst;
+    if (ntiles > INT32_MAX || h->nstate > ((long long)1 << 40)) { set_error("grid too large"); return fail(SVL_ERR_INVALID); }
+    h->ntiles = (int)ntiles;
     h->dt = opts->dt;
     if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) { set_error("cudaStreamCreate failed"); return fail(SVL_ERR_CUDA); }
+    h->pad_index.resize(h->ntotal);
+    for (long long n = 0; n < h->nn; ++n) {
+        const long long x = n % nxn, y = (n / nxn) % nyn, z = n / ((long long)nxn * nyn);
+        for (int c = 0; c < 3; ++c) h->pad_index[n * 3 + c] = (z * nyn + y) * h->pitch + x * 3 + c;
+    }
 
-    std::vector<float> lam((size_t)ninst * h->ne), mu((size_t)ninst * h->ne), cdof((size_t)ninst * h->ntotal);
+    h->pe = (h->nx + 8 + 3) / 4 * 4;                  // row padding keeps TMA strides 16-byte multiples
+    const size_t lm_per = (size_t)h->pe * h->ny * h->nz;
+    std::vector<float> lam(lm_per * ninst, 0.f), mu(lm_per * ninst, 0.f), cdof((size_t)h->nstate, 0.f);
     std::vector<double> Klam(24 * 24, 0.0), Kmu(24 * 24, 0.0);
     const double dt2 = opts->dt * opts->dt;
     std::vector<long long> fdof;
@@ -478,13 +723,13 @@ int svl_cdx_create(const svl_grid_spec* g, int32_t ninst, const svl_model_desc* 
         if (!model_from_desc(&models[b], m)) return fail(SVL_ERR_INVALID);
         int st = cdx_check_instance(g, m, b);
         if (st) return fail(st);
-        // every element must have the geometry of element 0 (uniform grid)
         if (b == 0) {
+            // reference matrices of the (uniform) element: K = lambda K_lambda + mu K_mu
             for (int q = 0; q < 8; ++q) {
                 double dNx[8][3], N[8];
                 const double w = gp_factor(m, 0, gp_geometry(m, 0, q, dNx, N));
                 double div[24], B[6][24];
-                for (int i = 0; i < 24; ++i) { div[i] = 0; for (int s = 0; s < 6; ++s) B[s][i] = 0; }
+                for (int i2 = 0; i2 < 24; ++i2) { div[i2] = 0; for (int r = 0; r < 6; ++r) B[r][i2] = 0; }
                 for (int a = 0; a < 8; ++a) {
                     const double bx = dNx[a][0], by = dNx[a][1], bz = dNx[a][2];
                     div[3 * a] = bx; div[3 * a + 1] = by; div[3 * a + 2] = bz;
@@ -495,12 +740,12 @@ int svl_cdx_create(const svl_grid_spec* g, int32_t ninst, const svl_model_desc* 
                 }
                 // C = lambda m m^T + mu diag(2,2,2,1,1,1)
                 static const double D[6] = {2, 2, 2, 1, 1, 1};
-                for (int i = 0; i < 24; ++i)
-                    for (int j = 0; j < 24; ++j) {
-                        Klam[i * 24 + j] += w * div[i] * div[j];
-                        double s = 0;
-                        for (int r = 0; r < 6; ++r) s += B[r][i] * D[r] * B[r][j];
-                        Kmu[i * 24 + j] += w * s;
+                for (int r1 = 0; r1 < 24; ++r1)
+                    for (int c1 = 0; c1 < 24; ++c1) {
+                        Klam[r1 * 24 + c1] += w * div[r1] * div[c1];
+                        double acc = 0;
+                        for (int r = 0; r < 6; ++r) acc += B[r][r1] * D[r] * B[r][c1];
+                        Kmu[r1 * 24 + c1] += w * acc;
                     }
             }
         }
@@ -512,77 +757,104 @@ int svl_cdx_create(const svl_grid_spec* g, int32_t ninst, const svl_model_desc* 
                     if (std::fabs(w0 - w1) > 1e-12 * std::fabs(w0)) { set_error("instance %d: grid is not uniform", b); return fail(SVL_ERR_UNSUPPORTED); }
                 }
             }
-            const double* p = m.param(e);
-            const double E = p[0], nu = p[1];
-            lam[(size_t)b * h->ne + e] = (float)(E * nu / (1.0 - 2.0 * nu) / (1.0 + nu));
-            mu[(size_t)b * h->ne + e] = (float)(E / (2.0 * (1.0 + nu)));
+            const double* pr = m.param(e);
+            const double E = pr[0], nu = pr[1];
+            const int ex = e % h->nx, ey = (e / h->nx) % h->ny, ez = e / (h->nx * h->ny);
+            const size_t li = (size_t)b * lm_per + ((size_t)ez * h->ny + ey) * h->pe + ex;
+            lam[li] = (float)(E * nu / (1.0 - 2.0 * nu) / (1.0 + nu));
+            mu[li] = (float)(E / (2.0 * (1.0 + nu)));
         }
         std::vector<double> M;
         lumped_mass_diag(m, opts->mtol, M);
         for (long long t = 0; t < h->ntotal; ++t) {
             const bool fixed = m.fdof[t] < 0;
             if (!fixed && !(M[t] > 0)) { set_error("instance %d: free dof %lld has no mass", b, t); return fail(SVL_ERR_INVALID); }
-            cdof[(size_t)b * h->ntotal + t] = fixed ? 0.0f : (float)(dt2 / M[t]);
+            cdof[(size_t)b * per + h->pad_index[t]] = fixed ? 0.0f : (float)(dt2 / M[t]);
         }
         if (loads) {
             const svl_load_desc& L = loads[b];
             if (L.nsupport > 0) { set_error("instance %d: support motion is not supported on the structured path", b); return fail(SVL_ERR_UNSUPPORTED); }
             const int soff = (int)s_ptr.size() - 1;
-            for (int s = 0; s < L.nseries; ++s) {
-                const int n = L.series_ptr[s + 1] - L.series_ptr[s];
+            for (int sidx = 0; sidx < L.nseries; ++sidx) {
+                const int n = L.series_ptr[sidx + 1] - L.series_ptr[sidx];
                 if (n < 0) { set_error("bad series_ptr"); return fail(SVL_ERR_INVALID); }
-                s_val.insert(s_val.end(), L.series_val + L.series_ptr[s], L.series_val + L.series_ptr[s + 1]);
+                s_val.insert(s_val.end(), L.series_val + L.series_ptr[sidx], L.series_val + L.series_ptr[sidx + 1]);
                 s_ptr.push_back((int)s_val.size());
             }
-            for (int i = 0; i < L.nforce; ++i) {
-                if (L.force_dof[i] < 0 || L.force_dof[i] >= h->ntotal || L.force_series[i] < 0 || L.force_series[i] >= L.nseries) {
-                    set_error("instance %d: load entry %d out of range", b, i); return fail(SVL_ERR_INVALID);
+            for (int i2 = 0; i2 < L.nforce; ++i2) {
+                if (L.force_dof[i2] < 0 || L.force_dof[i2] >= h->ntotal || L.force_series[i2] < 0 || L.force_series[i2] >= L.nseries) {
+                    set_error("instance %d: load entry %d out of range", b, i2); return fail(SVL_ERR_INVALID);
                 }
-                fdof.push_back((long long)b * h->ntotal + L.force_dof[i]);
-                fser.push_back(soff + L.force_series[i]);
-                fcoef.push_back(L.force_coef[i]);
+                fdof.push_back((long long)b * h->ntotal + L.force_dof[i2]);
+                fser.push_back(soff + L.force_series[i2]);
+                fcoef.push_back(L.force_coef[i2]);
             }
         }
     }
-    // B operand images: rows 0-23 K_lambda, 24-47 K_mu, canonical K-major layout
-    std::vector<float> bop(2 * (B_BYTES / 4), 0.f);
+    // B operand image, canonical K-major layout, 96 rows:
+    // [K_lambda hi; K_mu hi; K_lambda lo; K_mu lo] (24 rows each)
+    std::vector<float> bop(B_BYTES / 4, 0.f);
     for (int n = 0; n < 48; ++n)
         for (int k = 0; k < 24; ++k) {
             const double val = n < 24 ? Klam[n * 24 + k] : Kmu[(n - 24) * 24 + k];
             const float hi = host_tf32(val);
             const float lo = host_tf32(val - (double)hi);
-            const int off = (n >> 3) * (SBO / 4) + (k >> 2) * (LBO / 4) + (n & 7) * 4 + (k & 3);
-            bop[off] = hi;
-            bop[B_BYTES / 4 + off] = lo;
+            const int nl = n + 48;
+            bop[(n >> 3) * (SBO / 4) + (k >> 2) * (LBO / 4) + (n & 7) * 4 + (k & 3)] = hi;
+            bop[(nl >> 3) * (SBO / 4) + (k >> 2) * (LBO / 4) + (nl & 7) * 4 + (k & 3)] = lo;
         }
-    // loads grouped by dof, input order kept within a dof
+    // loads: unique dofs (entries kept in input order), grouped by the tile owning the node
     std::vector<int> order(fdof.size());
-    for (size_t i = 0; i < order.size(); ++i) order[i] = (int)i;
-    std::stable_sort(order.begin(), order.end(), [&](int a, int b2) { return fdof[a] < fdof[b2]; });
+    for (size_t i2 = 0; i2 < order.size(); ++i2) order[i2] = (int)i2;
+    auto tile_of = [&](long long gdof) {
+        const long long b = gdof / h->ntotal, t = gdof % h->ntotal, n = t / 3;
+        const long long x = n % nxn, y = (n / nxn) % nyn, z = n / ((long long)nxn * nyn);
+        return (((b * h->ntz + z / TZ) * h->nty + y / TY) * h->ntx + x / TX);
+    };
+    std::stable_sort(order.begin(), order.end(), [&](int a, int c) {
+        const long long ta = tile_of(fdof[a]), tc = tile_of(fdof[c]);
+        return ta < tc || (ta == tc && fdof[a] < fdof[c]);
+    });
+    std::vector<int> tl_ptr(h->ntiles + 1, 0), ld_ptr(1, 0), ld_ser;
     std::vector<long long> ld_dof;
-    std::vector<int> ld_ptr(1, 0), ld_ser;
     std::vector<double> ld_coef;
-    for (size_t i = 0; i < order.size(); ++i) {
-        const int j = order[i];
-        if (ld_dof.empty() || ld_dof.back() != fdof[j]) { if (!ld_dof.empty()) ld_ptr.push_back((int)ld_ser.size()); ld_dof.push_back(fdof[j]); }
-        ld_ser.push_back(fser[j]);
-        ld_coef.push_back(fcoef[j]);
+    long long last = -1;
+    for (int j2 : order) {
+        if (fdof[j2] != last) {
+            if (last >= 0) ld_ptr.push_back((int)ld_ser.size());
+            const long long b = fdof[j2] / h->ntotal, t = fdof[j2] % h->ntotal;
+            ld_dof.push_back(b * per + h->pad_index[t]);
+            tl_ptr[tile_of(fdof[j2]) + 1]++;
+            last = fdof[j2];
+        }
+        ld_ser.push_back(fser[j2]);
+        ld_coef.push_back(fcoef[j2]);
     }
-    if (!ld_dof.empty()) ld_ptr.push_back((int)ld_ser.size());
-    h->nld = (int)ld_dof.size();
+    if (last >= 0) ld_ptr.push_back((int)ld_ser.size());
+    for (int t = 0; t < h->ntiles; ++t) tl_ptr[t + 1] += tl_ptr[t];
 
     int st;
-    const size_t nt = (size_t)ninst * h->ntotal;
-    if ((st = h->alloc(nt, &h->u[0])) || (st = h->alloc(nt, &h->u[1])) || (st = h->alloc(nt, &h->uprev_copy)) ||
-        (st = h->alloc(nt, &h->V)) || (st = h->alloc(nt, &h->A)) || (st = h->upload(lam, &h->lam)) ||
+    const size_t ns = (size_t)h->nstate;
+    if ((st = h->alloc(ns, &h->uh[0])) || (st = h->alloc(ns, &h->uh[1])) || (st = h->alloc(ns, &h->ul[0])) ||
+        (st = h->alloc(ns, &h->ul[1])) || (st = h->alloc(ns, &h->ph_copy)) || (st = h->alloc(ns, &h->pl_copy)) ||
+        (st = h->alloc(ns, &h->V)) || (st = h->alloc(ns, &h->A)) || (st = h->upload(lam, &h->lam)) ||
         (st = h->upload(mu, &h->mu)) || (st = h->upload(cdof, &h->cdof)) || (st = h->upload(bop, &h->bop)) ||
-        (st = h->alloc(2, &h->step)) || (st = h->alloc(1, &h->status)) || (st = h->upload(ld_dof, &h->ld_dof)) ||
+        (st = h->alloc(1, &h->status)) || (st = h->upload(tl_ptr, &h->tl_ptr)) || (st = h->upload(ld_dof, &h->ld_dof)) ||
         (st = h->upload(ld_ptr, &h->ld_ptr)) || (st = h->upload(ld_ser, &h->ld_ser)) || (st = h->upload(ld_coef, &h->ld_coef)) ||
         (st = h->upload(s_ptr, &h->s_ptr)) || (st = h->upload(s_val, &h->s_val)))
+        return fail(st);
+    if ((st = make_map(h->uh[0], h->pitch, nyn, nzn, ninst, RAWX, HY, HZ, &h->tmap[0])) ||
+        (st = make_map(h->uh[1], h->pitch, nyn, nzn, ninst, RAWX, HY, HZ, &h->tmap[1])) ||
+        (st = make_map(h->lam, h->pe, h->ny, h->nz, ninst, LMX, EY, EZ, &h->tmap_lam)) ||
+        (st = make_map(h->mu, h->pe, h->ny, h->nz, ninst, LMX, EY, EZ, &h->tmap_mu)))
         return fail(st);
     if (cudaFuncSetAttribute(k_cdx_step, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES) != cudaSuccess) {
         set_error("cannot set %d bytes of dynamic shared memory", SMEM_BYTES); return fail(SVL_ERR_CUDA);
     }
+    int dev = 0, sms = 0;
+    CUDA_TRY(cudaGetDevice(&dev));
+    CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    h->grid = std::min(h->ntiles, sms);      // persistent: one CTA per SM
     if (cudaStreamSynchronize(h->stream) != cudaSuccess) { set_error("upload failed"); return fail(SVL_ERR_CUDA); }
     *out = h;
     return SVL_OK;
@@ -590,40 +862,46 @@ int svl_cdx_create(const svl_grid_spec* g, int32_t ninst, const svl_model_desc* 
 
 int svl_cdx_set_initial(svl_cdx* h, int32_t inst, const double* U0, const double* V0, const double* A0) {
     if (!h || inst < 0 || inst >= h->ninst) { set_error("bad handle or instance"); return SVL_ERR_INVALID; }
-    const size_t n = (size_t)h->ntotal;
-    std::vector<double> U(n, 0.0), Up(n);
-    if (U0) std::memcpy(U.data(), U0, n * 8);
-    for (size_t i = 0; i < n; ++i) {
-        const double v = V0 ? V0[i] : 0.0, a = A0 ? A0[i] : 0.0;
-        Up[i] = U[i] - h->dt * v + h->dt * h->dt / 2.0 * a;
+    const size_t per = (size_t)(h->nstate / h->ninst);
+    std::vector<float> hi(per, 0.f), lo(per, 0.f), phi(per, 0.f), plo(per, 0.f);
+    for (long long t = 0; t < h->ntotal; ++t) {
+        const double u = U0 ? U0[t] : 0.0, vv = V0 ? V0[t] : 0.0, a = A0 ? A0[t] : 0.0;
+        const double up = u - h->dt * vv + h->dt * h->dt / 2.0 * a;
+        const long long p = h->pad_index[t];
+        split_pair(u, hi[p], lo[p]);
+        split_pair(up, phi[p], plo[p]);
     }
-    CUDA_TRY(cudaMemcpyAsync(h->u[h->cur] + inst * n, U.data(), n * 8, cudaMemcpyHostToDevice, h->stream));
-    CUDA_TRY(cudaMemcpyAsync(h->u[1 - h->cur] + inst * n, Up.data(), n * 8, cudaMemcpyHostToDevice, h->stream));
+    const size_t off = (size_t)inst * per;
+    CUDA_TRY(cudaMemcpyAsync(h->uh[h->cur] + off, hi.data(), per * 4, cudaMemcpyHostToDevice, h->stream));
+    CUDA_TRY(cudaMemcpyAsync(h->ul[h->cur] + off, lo.data(), per * 4, cudaMemcpyHostToDevice, h->stream));
+    CUDA_TRY(cudaMemcpyAsync(h->uh[1 - h->cur] + off, phi.data(), per * 4, cudaMemcpyHostToDevice, h->stream));
+    CUDA_TRY(cudaMemcpyAsync(h->ul[1 - h->cur] + off, plo.data(), per * 4, cudaMemcpyHostToDevice, h->stream));
     CUDA_TRY(cudaStreamSynchronize(h->stream));
     h->va_valid = false;
     return SVL_OK;
 }
 
-static int cdx_step(svl_cdx* h, bool want_va) {
+static int cdx_step(svl_cdx* h, int k, bool want_va) {
     CdxView v;
     v.nx = h->nx; v.ny = h->ny; v.nz = h->nz; v.ninst = h->ninst;
-    v.nn = h->nn; v.ne = h->ne;
-    v.ucur = h->u[h->cur];
-    v.uprev = h->u[1 - h->cur];
-    v.lam = h->lam; v.mu = h->mu; v.cdof = h->cdof; v.bop = h->bop;
-    v.step = h->step; v.status = h->status;
-    const size_t nt = (size_t)h->ninst * h->ntotal;
-    if (want_va) CUDA_TRY(cudaMemcpyAsync(h->uprev_copy, v.uprev, nt * 8, cudaMemcpyDeviceToDevice, h->stream));
-    const dim3 grid((h->nx + 1 + TX - 1) / TX, (h->ny + 1 + TY - 1) / TY, ((h->nz + 1 + TZ - 1) / TZ) * h->ninst);
-    k_cdx_step<<<grid, NTHREADS, SMEM_BYTES, h->stream>>>(v);
-    ++h->launches;
-    if (h->nld > 0) {
-        k_cdx_loads<<<(h->nld + 127) / 128, 128, 0, h->stream>>>(v.uprev, h->cdof, h->nld, h->ld_dof, h->ld_ptr, h->ld_ser,
-                                                               h->ld_coef, h->s_ptr, h->s_val, h->step);
-        ++h->launches;
-    }
+    v.pitch = h->pitch; v.ntx = h->ntx; v.nty = h->nty; v.ntz = h->ntz; v.ntiles = h->ntiles;
+    v.ul_cur = h->ul[h->cur];
+    v.uh_prev = h->uh[1 - h->cur]; v.ul_prev = h->ul[1 - h->cur];
+    v.cdof = h->cdof; v.bop = h->bop;
+    v.tl_ptr = h->tl_ptr; v.ld_dof = h->ld_dof; v.ld_ptr = h->ld_ptr; v.ld_ser = h->ld_ser; v.ld_coef = h->ld_coef;
+    v.s_ptr = h->s_ptr; v.s_val = h->s_val;
+    v.k = k;
+    v.status = h->status;
+    const size_t ns = (size_t)h->nstate;
     if (want_va) {
-        k_cdx_va<<<(unsigned)((nt + 255) / 256), 256, 0, h->stream>>>(v.uprev, v.ucur, h->uprev_copy, h->V, h->A, (long long)nt,
+        CUDA_TRY(cudaMemcpyAsync(h->ph_copy, v.uh_prev, ns * 4, cudaMemcpyDeviceToDevice, h->stream));
+        CUDA_TRY(cudaMemcpyAsync(h->pl_copy, v.ul_prev, ns * 4, cudaMemcpyDeviceToDevice, h->stream));
+    }
+    k_cdx_step<<<h->grid, NTHREADS, SMEM_BYTES, h->stream>>>(h->tmap[h->cur], h->tmap_lam, h->tmap_mu, v);
+    ++h->launches;
+    if (want_va) {
+        k_cdx_va<<<(unsigned)((ns + 255) / 256), 256, 0, h->stream>>>(v.uh_prev, v.ul_prev, h->uh[h->cur], v.ul_cur, h->ph_copy,
+                                                                   h->pl_copy, h->V, h->A, (long long)ns,
                                                                    1.0 / 2.0 / h->dt, 1.0 / h->dt / h->dt);
         ++h->launches;
     }
@@ -632,23 +910,26 @@ static int cdx_step(svl_cdx* h, bool want_va) {
     return SVL_OK;
 }
 
-int svl_cdx_run(svl_cdx* h, int32_t k_first, int32_t nsteps, double* U_hist) {
-    if (!h || nsteps < 0) { set_error("bad argument"); return SVL_ERR_INVALID; }
-    const int64_t l0 = h->launches;
-    const int kstart = k_first - 1;
-    CUDA_TRY(cudaMemcpyAsync(h->step, &kstart, sizeof(int), cudaMemcpyHostToDevice, h->stream));
-    const size_t nt = (size_t)h->ninst * h->ntotal;
-    for (int s = 0; s < nsteps; ++s) {
-        TRY(cdx_step(h, s == nsteps - 1));
-        if (U_hist) CUDA_TRY(cudaMemcpyAsync(U_hist + (size_t)s * nt, h->u[h->cur], nt * 8, cudaMemcpyDeviceToHost, h->stream));
-    }
-    h->va_valid = nsteps > 0;
-    h->launches_last = h->launches - l0;
+static int cdx_status(svl_cdx* h) {
     int status = 0;
     CUDA_TRY(cudaMemcpyAsync(&status, h->status, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
     CUDA_TRY(cudaStreamSynchronize(h->stream));
-    if (status) { set_error("tensor-core step timed out waiting for an MMA (status %d)", status); return SVL_ERR_CUDA; }
+    if (status) { set_error("tensor-core step gave up waiting on a barrier (status %d)", status); return SVL_ERR_CUDA; }
     return SVL_OK;
+}
+
+int svl_cdx_run(svl_cdx* h, int32_t k_first, int32_t nsteps, double* U_hist) {
+    if (!h || nsteps < 0) { set_error("bad argument"); return SVL_ERR_INVALID; }
+    const int64_t l0 = h->launches;
+    for (int s = 0; s < nsteps; ++s) {
+        TRY(cdx_step(h, k_first + s, s == nsteps - 1));
+        if (U_hist)
+            for (int b = 0; b < h->ninst; ++b)
+                TRY(fetch_pair(h, h->uh[h->cur], h->ul[h->cur], b, U_hist + ((size_t)s * h->ninst + b) * h->ntotal));
+    }
+    h->va_valid = nsteps > 0;
+    h->launches_last = h->launches - l0;
+    return cdx_status(h);
 }
 
 int svl_cdx_run_timed(svl_cdx* h, int32_t k_first, int32_t nsteps, float* ms) {
@@ -656,11 +937,9 @@ int svl_cdx_run_timed(svl_cdx* h, int32_t k_first, int32_t nsteps, float* ms) {
     cudaEvent_t a, b;
     CUDA_TRY(cudaEventCreate(&a));
     CUDA_TRY(cudaEventCreate(&b));
-    const int kstart = k_first - 1;
-    CUDA_TRY(cudaMemcpyAsync(h->step, &kstart, sizeof(int), cudaMemcpyHostToDevice, h->stream));
     const int64_t l0 = h->launches;
     CUDA_TRY(cudaEventRecord(a, h->stream));
-    for (int s = 0; s < nsteps; ++s) TRY(cdx_step(h, false));
+    for (int s = 0; s < nsteps; ++s) TRY(cdx_step(h, k_first + s, false));
     CUDA_TRY(cudaEventRecord(b, h->stream));
     CUDA_TRY(cudaEventSynchronize(b));
     CUDA_TRY(cudaEventElapsedTime(ms, a, b));
@@ -668,19 +947,19 @@ int svl_cdx_run_timed(svl_cdx* h, int32_t k_first, int32_t nsteps, float* ms) {
     cudaEventDestroy(b);
     h->launches_last = h->launches - l0;
     h->va_valid = false;
-    int status = 0;
-    CUDA_TRY(cudaMemcpy(&status, h->status, sizeof(int), cudaMemcpyDeviceToHost));
-    if (status) { set_error("tensor-core step timed out waiting for an MMA (status %d)", status); return SVL_ERR_CUDA; }
-    return SVL_OK;
+    return cdx_status(h);
 }
 
 int svl_cdx_get(svl_cdx* h, int32_t inst, int32_t which, double* out) {
     if (!h || !out || inst < 0 || inst >= h->ninst) { set_error("bad argument"); return SVL_ERR_INVALID; }
-    const double* src = which == 0 ? h->u[h->cur] : which == 1 ? h->V : which == 2 ? h->A : nullptr;
-    if (!src) { set_error("which must be 0, 1 or 2"); return SVL_ERR_INVALID; }
-    if (which != 0 && !h->va_valid) { set_error("V/A are only available after svl_cdx_run"); return SVL_ERR_INVALID; }
-    CUDA_TRY(cudaMemcpyAsync(out, src + (size_t)inst * h->ntotal, h->ntotal * 8, cudaMemcpyDeviceToHost, h->stream));
+    if (which < 0 || which > 2) { set_error("which must be 0, 1 or 2"); return SVL_ERR_INVALID; }
+    if (which == 0) return fetch_pair(h, h->uh[h->cur], h->ul[h->cur], inst, out);
+    if (!h->va_valid) { set_error("V/A are only available after svl_cdx_run"); return SVL_ERR_INVALID; }
+    const size_t per = (size_t)(h->nstate / h->ninst);
+    std::vector<double> tmp(per);
+    CUDA_TRY(cudaMemcpyAsync(tmp.data(), (which == 1 ? h->V : h->A) + (size_t)inst * per, per * 8, cudaMemcpyDeviceToHost, h->stream));
     CUDA_TRY(cudaStreamSynchronize(h->stream));
+    for (long long t = 0; t < h->ntotal; ++t) out[t] = tmp[h->pad_index[t]];
     return SVL_OK;
 }
 
