@@ -62,14 +62,16 @@ constexpr int UPD_WARP0 = 9;                                  // warps 9-15 gath
 constexpr int NUPD = NTHREADS - UPD_WARP0 * 32;               // 224 threads
 constexpr int EPI_WARP0 = 12;                                 // warps 12-15 also drain TMEM
 constexpr int NEPI = 128;
-constexpr int FSTRIDE = 25;                                   // padded row of element forces
 constexpr int RAWX = 40;                                      // TMA box: floats per halo row
 constexpr int RAW_SHIFT = 3;                                  // halo row starts 3 nodes left of x0-1
 constexpr int RAW_BYTES = RAWX * HY * HZ * 4;                 // 16000 B
 constexpr int LMX = 16;                                       // TMA box: lambda/mu floats per row
 constexpr int LM_SHIFT = 3;                                   // element row starts 3 left of x0-1
 constexpr int LM_BYTES = LMX * EY * EZ * 4;                   // 5184 B each
-constexpr int TILE_TX_BYTES = RAW_BYTES + 2 * LM_BYTES;       // bytes per tile by TMA
+constexpr int OWN_BYTES = TX * 3 * TY * TZ * 4;               // 6144 B per owned-node array
+constexpr int HALO_TX_BYTES = RAW_BYTES + 2 * LM_BYTES;       // halo + lambda + mu per tile
+constexpr int OWN_TX_BYTES = 4 * OWN_BYTES;                   // owned-node state per tile
+constexpr int FSTRIDE = 25;                                   // padded row of element forces
 
 // Canonical no-swizzle K-major operand layout: 8-row x 16-byte core matrices;
 // element (r, k) at (r/8)*SBO + (k/4)*LBO + (r%8)*16 + (k%4)*4 bytes.
@@ -83,17 +85,20 @@ constexpr int B_BYTES = (B_ROWS / 8) * SBO;                   // 9216 B
 constexpr int OFF_B = 0;
 constexpr int OFF_A = align_up(OFF_B + B_BYTES, 1024);       // [2 buffers][hi, lo]
 constexpr int A_STRIDE = 2 * A_BYTES;
-constexpr int OFF_TT = OFF_A + 2 * A_STRIDE;                   // [2 buffers] TMA tile: halo, lambda, mu
-constexpr int TT_LAM = align_up(RAW_BYTES, 128);                 // TMA tensor destinations: 128-byte aligned
+constexpr int OFF_TT = OFF_A + 2 * A_STRIDE;                   // [2 buffers] halo of u_n (high part), lambda, mu
+constexpr int TT_LAM = align_up(RAW_BYTES, 128);
 constexpr int TT_MU = align_up(TT_LAM + LM_BYTES, 128);
 constexpr int TT_STRIDE = align_up(TT_MU + LM_BYTES, 1024);
-constexpr int OFF_F = OFF_TT + 2 * TT_STRIDE;
+constexpr int OFF_OWN = OFF_TT + 2 * TT_STRIDE;                  // owned: u_n low, u_{n-1} hi/lo, dt^2/m
+constexpr int OWN_ULC = 0, OWN_UHP = OWN_BYTES, OWN_ULP = 2 * OWN_BYTES, OWN_CD = 3 * OWN_BYTES;
+constexpr int OFF_F = align_up(OFF_OWN + 4 * OWN_BYTES, 128);    // element forces
 constexpr int OFF_BAR = align_up(OFF_F + NEL * FSTRIDE * 4, 16);
-constexpr int NBAR = 10;                                      // tma[2] a_full[2] a_empty[2] d_full[2] d_empty[2]
+constexpr int NBAR = 11;                                      // tma[2] a_full[2] a_empty[2] d_full[2] d_empty[2] own
 constexpr int OFF_TMEM = OFF_BAR + NBAR * 8;
 constexpr int SMEM_BYTES = OFF_TMEM + 16;
 static_assert(OFF_A % 1024 == 0 && A_STRIDE % 1024 == 0, "MMA operands on 1 KB boundaries");
-static_assert(OFF_TT % 1024 == 0 && TT_STRIDE % 1024 == 0 && TT_LAM % 128 == 0 && TT_MU % 128 == 0, "TMA destinations");
+static_assert(OFF_TT % 1024 == 0 && TT_STRIDE % 1024 == 0 && TT_LAM % 128 == 0 && TT_MU % 128 == 0 &&
+              OFF_OWN % 128 == 0 && OWN_BYTES % 128 == 0, "TMA destinations");
 static_assert(OFF_F % 16 == 0 && OFF_BAR % 8 == 0 && OFF_TMEM % 4 == 0, "alignment");
 static_assert(SMEM_BYTES <= 227 * 1024, "shared memory budget");
 static_assert(TX * TY * TZ <= 3 * NUPD, "three owned nodes per update thread at most");
@@ -184,8 +189,7 @@ struct CdxView {
     int nx, ny, nz, ninst;
     int pitch;                           // floats per padded x-row of the state arrays
     int ntx, nty, ntz, ntiles;
-    const float* __restrict__ ul_cur;    // u_n low part   [inst][z][y][pitch]
-    float* uh_prev;                      // read u_{n-1}, write u_{n+1} (same dof, same thread)
+    float* uh_prev;                      // u_{n-1} (read through TMA), u_{n+1} written here
     float* ul_prev;
     const float* __restrict__ cdof;      // [inst][z][y][pitch]  dt^2/m, 0 on restrained dofs
     const float* __restrict__ bop;       // [B_ROWS x 24] hi then lo operand image
@@ -245,19 +249,27 @@ __device__ __forceinline__ TileOrigin tile_origin(const CdxView& v, int tile) {
 
 __global__ void __launch_bounds__(NTHREADS, 1)
 k_cdx_step(const __grid_constant__ CUtensorMap tmap_u, const __grid_constant__ CUtensorMap tmap_lam,
-           const __grid_constant__ CUtensorMap tmap_mu, CdxView v) {
+           const __grid_constant__ CUtensorMap tmap_mu, const __grid_constant__ CUtensorMap tmap_ulc,
+           const __grid_constant__ CUtensorMap tmap_uhp, const __grid_constant__ CUtensorMap tmap_ulp,
+           const __grid_constant__ CUtensorMap tmap_cd, CdxView v) {
     extern __shared__ __align__(1024) unsigned char smem[];
     const int tid = threadIdx.x;
     const int warp = tid >> 5, lane = tid & 31;
     const int nxn = v.nx + 1, nyn = v.ny + 1, nzn = v.nz + 1;
-    float* sF = reinterpret_cast<float*>(smem + OFF_F);
+    float* sF = reinterpret_cast<float*>(smem + OFF_F);     // element forces of the tile
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem + OFF_BAR);
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + OFF_TMEM);
-    const uint32_t b_tma[2] = {smem_u32(bars + 0), smem_u32(bars + 1)};
-    const uint32_t b_afull[2] = {smem_u32(bars + 2), smem_u32(bars + 3)};
-    const uint32_t b_aempty[2] = {smem_u32(bars + 4), smem_u32(bars + 5)};
-    const uint32_t b_dfull[2] = {smem_u32(bars + 6), smem_u32(bars + 7)};
-    const uint32_t b_dempty[2] = {smem_u32(bars + 8), smem_u32(bars + 9)};
+    // barrier addresses are computed (no small arrays indexed at run time: those live in local memory)
+    const uint32_t bar0 = smem_u32(bars);
+#define B_TMA(b) (bar0 + 8u * (uint32_t)(b))
+#define B_AFULL(b) (bar0 + 16u + 8u * (uint32_t)(b))
+#define B_AEMPTY(b) (bar0 + 32u + 8u * (uint32_t)(b))
+#define B_DFULL(b) (bar0 + 48u + 8u * (uint32_t)(b))
+#define B_DEMPTY(b) (bar0 + 64u + 8u * (uint32_t)(b))
+    const uint32_t b_own = bar0 + 80u;
+// phase bits of two-slot barriers packed in one word
+#define PH(w, b) (((w) >> (b)) & 1u)
+#define FLIP(w, b) ((w) ^= (1u << (b)))
     // TMA destinations and MMA operands assume a 1 KB aligned dynamic window
     if (smem_u32(smem) & 1023u) {
         if (tid == 0) atomicOr(v.status, 2);
@@ -272,12 +284,13 @@ k_cdx_step(const __grid_constant__ CUtensorMap tmap_u, const __grid_constant__ C
     }
     if (tid == 0) {
         for (int b = 0; b < 2; ++b) {
-            mbar_init(b_tma[b], 1);
-            mbar_init(b_afull[b], NBUILD);
-            mbar_init(b_aempty[b], 1);
-            mbar_init(b_dfull[b], 1);
-            mbar_init(b_dempty[b], NEPI);
+            mbar_init(B_TMA(b), 1);
+            mbar_init(B_AFULL(b), NBUILD);
+            mbar_init(B_AEMPTY(b), 1);
+            mbar_init(B_DFULL(b), 1);
+            mbar_init(B_DEMPTY(b), NEPI);
         }
+        mbar_init(b_own, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     {
@@ -294,27 +307,36 @@ k_cdx_step(const __grid_constant__ CUtensorMap tmap_u, const __grid_constant__ C
     auto issue_tile = [&](int tile, int buf) {
         const TileOrigin o = tile_origin(v, tile);
         const uint32_t dst = smem_u32(smem + OFF_TT + buf * TT_STRIDE);
-        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" :: "r"(b_tma[buf]), "r"(TILE_TX_BYTES) : "memory");
-        tma_load4(&tmap_u, dst, b_tma[buf], (o.x0 - 1 - RAW_SHIFT) * 3, o.y0 - 1, o.z0 - 1, o.inst);
-        tma_load4(&tmap_lam, dst + TT_LAM, b_tma[buf], o.x0 - 1 - LM_SHIFT, o.y0 - 1, o.z0 - 1, o.inst);
-        tma_load4(&tmap_mu, dst + TT_MU, b_tma[buf], o.x0 - 1 - LM_SHIFT, o.y0 - 1, o.z0 - 1, o.inst);
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" :: "r"(B_TMA(buf)), "r"(HALO_TX_BYTES) : "memory");
+        tma_load4(&tmap_u, dst, B_TMA(buf), (o.x0 - 1 - RAW_SHIFT) * 3, o.y0 - 1, o.z0 - 1, o.inst);
+        tma_load4(&tmap_lam, dst + TT_LAM, B_TMA(buf), o.x0 - 1 - LM_SHIFT, o.y0 - 1, o.z0 - 1, o.inst);
+        tma_load4(&tmap_mu, dst + TT_MU, B_TMA(buf), o.x0 - 1 - LM_SHIFT, o.y0 - 1, o.z0 - 1, o.inst);
+    };
+    auto issue_owned = [&](int tile) {
+        const TileOrigin o = tile_origin(v, tile);
+        const uint32_t dst = smem_u32(smem + OFF_OWN);
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" :: "r"(b_own), "r"(OWN_TX_BYTES) : "memory");
+        tma_load4(&tmap_ulc, dst + OWN_ULC, b_own, o.x0 * 3, o.y0, o.z0, o.inst);
+        tma_load4(&tmap_uhp, dst + OWN_UHP, b_own, o.x0 * 3, o.y0, o.z0, o.inst);
+        tma_load4(&tmap_ulp, dst + OWN_ULP, b_own, o.x0 * 3, o.y0, o.z0, o.inst);
+        tma_load4(&tmap_cd, dst + OWN_CD, b_own, o.x0 * 3, o.y0, o.z0, o.inst);
     };
     const int ntile_cta = v.ntiles > (int)blockIdx.x ? (v.ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
     bool ok = true;
 
     if (warp < NBUILD / 32) {
         // ===== builders: A operand rows (element x 24 dofs), TF32 hi / lo =====
-        uint32_t ph_tma[2] = {0, 0}, ph_aempty[2] = {1, 1};
+        uint32_t ph_tma = 0u, ph_aempty = 3u;
         const int h = tid >> 7, m = tid & 127;
         for (int it = 0, mt = 0; it < ntile_cta && ok; ++it) {
             const int buf = it & 1;
-            ok = mbar_wait(b_tma[buf], ph_tma[buf]);
-            ph_tma[buf] ^= 1;
+            ok = mbar_wait(B_TMA(buf), PH(ph_tma, buf));
+            FLIP(ph_tma, buf);
             const float* raw = reinterpret_cast<const float*>(smem + OFF_TT + buf * TT_STRIDE);
             for (int t = 0; t < NMT && ok; ++t, ++mt) {
                 const int b = mt & 1;
-                ok = mbar_wait(b_aempty[b], ph_aempty[b]);
-                ph_aempty[b] ^= 1;
+                ok = mbar_wait(B_AEMPTY(b), PH(ph_aempty, b));
+                FLIP(ph_aempty, b);
                 if (!ok) break;
                 const int le = t * 128 + m;
                 float hv[12], lv[12];
@@ -343,20 +365,20 @@ k_cdx_step(const __grid_constant__ CUtensorMap tmap_u, const __grid_constant__ C
                     *reinterpret_cast<float4*>(Ab + A_BYTES + off + g * LBO) = make_float4(lv[4 * g], lv[4 * g + 1], lv[4 * g + 2], lv[4 * g + 3]);
                 }
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                mbar_arrive(b_afull[b]);
+                mbar_arrive(B_AFULL(b));
             }
         }
     } else if (warp == ISSUE_WARP) {
         // ===== MMA issuer: two independent accumulator chains per M-tile =====
         if (lane == 0) {
-            uint32_t ph_afull[2] = {0, 0}, ph_dempty[2] = {1, 1};
+            uint32_t ph_afull = 0u, ph_dempty = 3u;
             const uint32_t bB = smem_u32(smem + OFF_B);
             const int total = ntile_cta * NMT;
             for (int mt = 0; mt < total && ok; ++mt) {
                 const int b = mt & 1;
-                ok = mbar_wait(b_afull[b], ph_afull[b]) && mbar_wait(b_dempty[b], ph_dempty[b]);
-                ph_afull[b] ^= 1;
-                ph_dempty[b] ^= 1;
+                ok = mbar_wait(B_AFULL(b), PH(ph_afull, b)) && mbar_wait(B_DEMPTY(b), PH(ph_dempty, b));
+                FLIP(ph_afull, b);
+                FLIP(ph_dempty, b);
                 if (!ok) break;
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                 const uint32_t a_hi = smem_u32(smem + OFF_A + b * A_STRIDE), a_lo = a_hi + A_BYTES;
@@ -368,36 +390,39 @@ k_cdx_step(const __grid_constant__ CUtensorMap tmap_u, const __grid_constant__ C
                     mma_tf32(d, make_desc(a_hi + koff), make_desc(bB + koff), kIdescN96, ks > 0);
                     mma_tf32(d + LO_COLS, make_desc(a_lo + koff), make_desc(bB + koff), kIdescN48, ks > 0);
                 }
-                mma_commit(b_dfull[b]);
-                mma_commit(b_aempty[b]);
+                mma_commit(B_DFULL(b));
+                mma_commit(B_AEMPTY(b));
             }
         }
     } else {
         // ===== warps 9-15: TMA, TMEM drain (12-15), ordered gather, update ======
         const int gt = tid - UPD_WARP0 * 32;                  // 0..223
-        uint32_t ph_tma[2] = {0, 0}, ph_dfull[2] = {0, 0};
-        bool pending[2] = {false, false};
+        uint32_t ph_tma = 0u, ph_dfull = 0u, ph_own = 0;
+        uint32_t pending = 0u;
+        bool pending_own = ntile_cta > 0;
         if (gt == 0) {
             for (int it = 0; it < 2 && it < ntile_cta; ++it) issue_tile(blockIdx.x + it * gridDim.x, it);
+            if (ntile_cta > 0) issue_owned(blockIdx.x);
         }
-        for (int it = 0; it < 2 && it < ntile_cta; ++it) pending[it] = true;
+        for (int it = 0; it < 2 && it < ntile_cta; ++it) pending |= 1u << it;
         for (int it = 0, mt = 0; it < ntile_cta && ok; ++it) {
             const int tile = blockIdx.x + it * gridDim.x;
             const int buf = it & 1;
             const TileOrigin o = tile_origin(v, tile);
+            const int tl0 = v.tl_ptr[tile], tl1 = v.tl_ptr[tile + 1];     // used at the end of the tile
             const unsigned char* tt = smem + OFF_TT + buf * TT_STRIDE;
             const float* raw = reinterpret_cast<const float*>(tt);
             const float* tlam = reinterpret_cast<const float*>(tt + TT_LAM);
             const float* tmu = reinterpret_cast<const float*>(tt + TT_MU);
-            ok = mbar_wait(b_tma[buf], ph_tma[buf]);
-            ph_tma[buf] ^= 1;
-            pending[buf] = false;
+            ok = mbar_wait(B_TMA(buf), PH(ph_tma, buf));
+            FLIP(ph_tma, buf);
+            pending &= ~(1u << buf);
             if (warp >= EPI_WARP0) {
                 const int q = warp - EPI_WARP0;                   // TMEM lane quarter
-                for (int t = 0; t < NMT && ok; ++t, ++mt) {
+                for (int t = 0; t < NMT; ++t, ++mt) {
                     const int b = mt & 1;
-                    ok = mbar_wait(b_dfull[b], ph_dfull[b]);
-                    ph_dfull[b] ^= 1;
+                    ok = ok && mbar_wait(B_DFULL(b), PH(ph_dfull, b));
+                    FLIP(ph_dfull, b);
                     if (!ok) break;
                     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                     const uint32_t row = tmem + (uint32_t)b * ACC_COLS + ((uint32_t)(q * 32) << 16);
@@ -415,7 +440,7 @@ k_cdx_step(const __grid_constant__ CUtensorMap tmap_u, const __grid_constant__ C
                         tmem_ld<8>(row + LO_COLS + 8 * g, e);
                         asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-                        for (int i = 0; i < 8; ++i) f[8 * g + i] = l * (a[i] + c[i] + e[i]);
+                        for (int i2 = 0; i2 < 8; ++i2) f[8 * g + i2] = l * (a[i2] + c[i2] + e[i2]);
                     }
 #pragma unroll
                     for (int g = 0; g < 3; ++g) {
@@ -425,37 +450,35 @@ k_cdx_step(const __grid_constant__ CUtensorMap tmap_u, const __grid_constant__ C
                         tmem_ld<8>(row + LO_COLS + 24 + 8 * g, e);
                         asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-                        for (int i = 0; i < 8; ++i) f[8 * g + i] += mu * (a[i] + c[i] + e[i]);
+                        for (int i2 = 0; i2 < 8; ++i2) f[8 * g + i2] += mu * (a[i2] + c[i2] + e[i2]);
                     }
                     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-                    mbar_arrive(b_dempty[b]);
+                    mbar_arrive(B_DEMPTY(b));
                     if (le < NEL) {
 #pragma unroll
-                        for (int j = 0; j < 24; ++j) sF[le * FSTRIDE + j] = f[j];
+                        for (int jj = 0; jj < 24; ++jj) sF[le * FSTRIDE + jj] = f[jj];
                     }
                 }
             } else {
                 mt += NMT;
             }
-            // all element forces of this tile are in sF (group barrier; ok made uniform)
+            // all element forces of this tile are in sF (group barrier; ok made uniform);
+            // the owned-node state of this tile has landed
+            ok = ok && mbar_wait(b_own, ph_own);
+            ph_own ^= 1;
+            pending_own = false;
             ok = group_and(ok);
             if (!ok) break;
 
-            // -- ordered gather and compensated update of the owned nodes ------
-            const int nxn_ = nxn, nyn_ = nyn, nzn_ = nzn;
+            // -- ordered gather and compensated update of the owned nodes -----
+            const float* tulc = reinterpret_cast<const float*>(smem + OFF_OWN + OWN_ULC);
+            const float* tuhp = reinterpret_cast<const float*>(smem + OFF_OWN + OWN_UHP);
+            const float* tulp = reinterpret_cast<const float*>(smem + OFF_OWN + OWN_ULP);
+            const float* tcd = reinterpret_cast<const float*>(smem + OFF_OWN + OWN_CD);
             for (int nd = gt; nd < TX * TY * TZ; nd += NUPD) {
                 const int ox = nd & 7, oy = (nd >> 3) & 7, oz = nd >> 6;
                 const int gx = o.x0 + ox, gy = o.y0 + oy, gz = o.z0 + oz;
-                if (gx >= nxn_ || gy >= nyn_ || gz >= nzn_) continue;
-                const size_t gbase = ((((size_t)o.inst * nzn_ + gz) * nyn_ + gy) * v.pitch) + (size_t)gx * 3;
-                float al[3], bh[3], bl[3], cc[3];
-#pragma unroll
-                for (int c = 0; c < 3; ++c) {
-                    al[c] = v.ul_cur[gbase + c];
-                    bh[c] = v.uh_prev[gbase + c];
-                    bl[c] = v.ul_prev[gbase + c];
-                    cc[c] = v.cdof[gbase + c];
-                }
+                if (gx >= nxn || gy >= nyn || gz >= nzn) continue;
                 // (element offset, local node) in ascending element-tag order
                 const int sel[8][4] = {{0, 0, 0, 6}, {1, 0, 0, 7}, {0, 1, 0, 5}, {1, 1, 0, 4},
                                        {0, 0, 1, 2}, {1, 0, 1, 3}, {0, 1, 1, 1}, {1, 1, 1, 0}};
@@ -466,21 +489,27 @@ k_cdx_step(const __grid_constant__ CUtensorMap tmap_u, const __grid_constant__ C
                     const float* fe = sF + le * FSTRIDE + sel[s2][3] * 3;
                     f[0] += fe[0]; f[1] += fe[1]; f[2] += fe[2];
                 }
+                const size_t gbase = ((((size_t)o.inst * nzn + gz) * nyn + gy) * v.pitch) + (size_t)gx * 3;
+                const int ob = (oz * TY + oy) * (TX * 3) + ox * 3;
                 const float* ah = raw + ((oz + 1) * HY + (oy + 1)) * RAWX + (RAW_SHIFT + ox + 1) * 3;
 #pragma unroll
                 for (int c = 0; c < 3; ++c) {
-                    const float inc = -cc[c] * f[c];
+                    const float inc = -tcd[ob + c] * f[c];
                     float dh, dl2, Dh, Dl, nh, nl;
-                    df_add(ah[c], al[c], -bh[c], -bl[c], dh, dl2);   // u_n - u_{n-1}
-                    df_add(dh, dl2, inc, 0.f, Dh, Dl);               // + (dt^2/m)(-f_int)
-                    df_add(ah[c], al[c], Dh, Dl, nh, nl);            // u_{n+1}
+                    df_add(ah[c], tulc[ob + c], -tuhp[ob + c], -tulp[ob + c], dh, dl2);   // u_n - u_{n-1}
+                    df_add(dh, dl2, inc, 0.f, Dh, Dl);                                    // + (dt^2/m)(-f_int)
+                    df_add(ah[c], tulc[ob + c], Dh, Dl, nh, nl);                          // u_{n+1}
                     v.uh_prev[gbase + c] = nh;
                     v.ul_prev[gbase + c] = nl;
                 }
             }
-            asm volatile("bar.sync 2, %0;" :: "r"(NUPD) : "memory");   // sF and the halo are free again
+            asm volatile("bar.sync 2, %0;" :: "r"(NUPD) : "memory");   // element forces and the tile buffers are free
+            if (gt == 0 && it + 1 < ntile_cta) {
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                issue_owned(blockIdx.x + (it + 1) * gridDim.x);
+            }
+            if (it + 1 < ntile_cta) pending_own = true;
             // -- external loads on this tile's dofs: (dt^2/m) f_ext(k) -------
-            const int tl0 = v.tl_ptr[tile], tl1 = v.tl_ptr[tile + 1];
             if (tl1 > tl0) {
                 for (int j2 = tl0 + gt; j2 < tl1; j2 += NUPD) {
                     double fx = 0.0;
@@ -503,12 +532,13 @@ k_cdx_step(const __grid_constant__ CUtensorMap tmap_u, const __grid_constant__ C
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                 issue_tile(blockIdx.x + (it + 2) * gridDim.x, buf);
             }
-            if (it + 2 < ntile_cta) pending[buf] = true;
+            if (it + 2 < ntile_cta) pending |= 1u << buf;
         }
         if (!ok) {
             if (gt == 0) atomicOr(v.status, 1);
             for (int b = 0; b < 2; ++b)            // never leave with a TMA copy in flight
-                if (pending[b]) mbar_wait(b_tma[b], ph_tma[b]);
+                if ((pending >> b) & 1u) mbar_wait(B_TMA(b), PH(ph_tma, b));
+            if (pending_own) mbar_wait(b_own, ph_own);
         }
     }
     if (!ok) atomicOr(v.status, 1);
@@ -569,6 +599,8 @@ struct svl_cdx {
     double *ld_coef = nullptr, *s_val = nullptr;
     int pe = 0;                          // floats per padded element row of lambda/mu
     CUtensorMap tmap[2];                 // halo maps of uh[0], uh[1]
+    CUtensorMap own_uh[2], own_ul[2];    // owned-node maps of uh[*], ul[*]
+    CUtensorMap own_cd;                  // owned-node map of dt^2/m
     CUtensorMap tmap_lam, tmap_mu;
     std::vector<long long> pad_index;    // total dof (node*3+c) -> padded position, one instance
     int cur = 0;                         // index of u_n in uh/ul
@@ -846,7 +878,12 @@ int svl_cdx_create(const svl_grid_spec* g, int32_t ninst, const svl_model_desc* 
     if ((st = make_map(h->uh[0], h->pitch, nyn, nzn, ninst, RAWX, HY, HZ, &h->tmap[0])) ||
         (st = make_map(h->uh[1], h->pitch, nyn, nzn, ninst, RAWX, HY, HZ, &h->tmap[1])) ||
         (st = make_map(h->lam, h->pe, h->ny, h->nz, ninst, LMX, EY, EZ, &h->tmap_lam)) ||
-        (st = make_map(h->mu, h->pe, h->ny, h->nz, ninst, LMX, EY, EZ, &h->tmap_mu)))
+        (st = make_map(h->mu, h->pe, h->ny, h->nz, ninst, LMX, EY, EZ, &h->tmap_mu)) ||
+        (st = make_map(h->uh[0], h->pitch, nyn, nzn, ninst, TX * 3, TY, TZ, &h->own_uh[0])) ||
+        (st = make_map(h->uh[1], h->pitch, nyn, nzn, ninst, TX * 3, TY, TZ, &h->own_uh[1])) ||
+        (st = make_map(h->ul[0], h->pitch, nyn, nzn, ninst, TX * 3, TY, TZ, &h->own_ul[0])) ||
+        (st = make_map(h->ul[1], h->pitch, nyn, nzn, ninst, TX * 3, TY, TZ, &h->own_ul[1])) ||
+        (st = make_map(h->cdof, h->pitch, nyn, nzn, ninst, TX * 3, TY, TZ, &h->own_cd)))
         return fail(st);
     if (cudaFuncSetAttribute(k_cdx_step, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES) != cudaSuccess) {
         set_error("cannot set %d bytes of dynamic shared memory", SMEM_BYTES); return fail(SVL_ERR_CUDA);
@@ -885,7 +922,6 @@ static int cdx_step(svl_cdx* h, int k, bool want_va) {
     CdxView v;
     v.nx = h->nx; v.ny = h->ny; v.nz = h->nz; v.ninst = h->ninst;
     v.pitch = h->pitch; v.ntx = h->ntx; v.nty = h->nty; v.ntz = h->ntz; v.ntiles = h->ntiles;
-    v.ul_cur = h->ul[h->cur];
     v.uh_prev = h->uh[1 - h->cur]; v.ul_prev = h->ul[1 - h->cur];
     v.cdof = h->cdof; v.bop = h->bop;
     v.tl_ptr = h->tl_ptr; v.ld_dof = h->ld_dof; v.ld_ptr = h->ld_ptr; v.ld_ser = h->ld_ser; v.ld_coef = h->ld_coef;
@@ -897,10 +933,11 @@ static int cdx_step(svl_cdx* h, int k, bool want_va) {
         CUDA_TRY(cudaMemcpyAsync(h->ph_copy, v.uh_prev, ns * 4, cudaMemcpyDeviceToDevice, h->stream));
         CUDA_TRY(cudaMemcpyAsync(h->pl_copy, v.ul_prev, ns * 4, cudaMemcpyDeviceToDevice, h->stream));
     }
-    k_cdx_step<<<h->grid, NTHREADS, SMEM_BYTES, h->stream>>>(h->tmap[h->cur], h->tmap_lam, h->tmap_mu, v);
+    k_cdx_step<<<h->grid, NTHREADS, SMEM_BYTES, h->stream>>>(h->tmap[h->cur], h->tmap_lam, h->tmap_mu, h->own_ul[h->cur],
+                                                             h->own_uh[1 - h->cur], h->own_ul[1 - h->cur], h->own_cd, v);
     ++h->launches;
     if (want_va) {
-        k_cdx_va<<<(unsigned)((ns + 255) / 256), 256, 0, h->stream>>>(v.uh_prev, v.ul_prev, h->uh[h->cur], v.ul_cur, h->ph_copy,
+        k_cdx_va<<<(unsigned)((ns + 255) / 256), 256, 0, h->stream>>>(v.uh_prev, v.ul_prev, h->uh[h->cur], h->ul[h->cur], h->ph_copy,
                                                                    h->pl_copy, h->V, h->A, (long long)ns,
                                                                    1.0 / 2.0 / h->dt, 1.0 / h->dt / h->dt);
         ++h->launches;
