@@ -133,6 +133,27 @@ def cpu_baseline(m, L, dt, steps_cap, budget_s=20.0):
             "sample": "%d time steps of the same model on the CPU oracle (OpenMP element loop, ordered scatter)" % n}
 
 
+def implicit_pcg(steps, warm=2, tol=1e-8):
+    """Newmark (average acceleration) + Linear on the 64^3 layered H8 model:
+    mean wall time per step of the effective-stiffness solve to a true
+    relative residual of `tol` (Jacobi-PCG, FP64, matrix-free)."""
+    from svl_gb300 import NewmarkBeta, workloads
+    m, L, dt = workloads.config4(nt=warm + steps + 2)
+    nm = NewmarkBeta(m, L, dt, pcg_tol=tol)
+    nm.Initialize()
+    nm.run(1, warm)
+    it0, _, _ = nm.stats()
+    ms = nm.run_timed(1 + warm, steps)
+    it1, _, res = nm.stats()
+    launches = nm.launches()
+    nm.close()
+    return {"workload": "lin3DHexa8 64x64x64 (h=1 m), layered G (100x contrast) x 10% log-normal, "
+                        "Newmark beta=1/4 gamma=1/2, dt=10x explicit limit, fixed bottom, roller sides",
+            "free_dof": m.nfree, "steps": steps, "ms_per_step": ms / steps, "precond": "jacobi",
+            "pcg_iters_per_step": (it1 - it0) / steps, "rel_residual_last": res, "tol": tol,
+            "residual": "true |b - K_eff x| / |b|, FP64", "gpu_launches": int(launches)}
+
+
 def dist_info():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -152,6 +173,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64-compare", action="store_true")
+    ap.add_argument("--implicit-steps", type=int, default=10,
+                    help="Newmark steps of the 64^3 implicit workload timed beside the headline (0 = skip)")
     args = ap.parse_args()
     ws, rank, local = dist_info()
     warm = max(3, args.warmup)
@@ -273,6 +296,7 @@ def main():
     cb = None
     if rank == 0 and not args.no_cpu:
         cb = cpu_baseline(m, L, dt, steps_cap=10)
+    implicit = implicit_pcg(args.implicit_steps) if (rank == 0 and args.implicit_steps > 0) else None
 
     if rank == 0:
         ws_mb = (nb * m.ntotal * 8 * (2 if args.precision == "mixed" else 7) + nb * m.ntotal * 4
@@ -291,7 +315,7 @@ def main():
             "roofline": {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
                          "algorithmic_bytes_per_step": algo_bytes, "kernel_share": shares},
-            "fp64_plain": fp64,
+            "fp64_plain": fp64, "implicit_pcg_time_to_1e-8": implicit,
             "cpu_baseline": cb, "e2e": e2e, "gpu_launches": int(launches), "clocks": clocks,
             "finite": finite,
         }

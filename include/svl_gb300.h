@@ -248,6 +248,53 @@ int  svl_cdx_get(svl_cdx* cdx, int32_t inst, int32_t which, double* out);
 int  svl_cdx_launch_count(svl_cdx* cdx, int64_t* launches);
 void svl_cdx_destroy(svl_cdx* cdx);
 
+/* ---- implicit Newmark (average acceleration), Linear algorithm --------- */
+/* NewmarkBeta with beta = 1/4, gamma = 1/2 (ExtendedNewmarkBeta with G = 0)
+ * and the Linear algorithm: one solve of the effective stiffness per step.
+ * Replaces
+ *   NewmarkBeta::Initialize / ComputeNewStep / ComputeEffectiveForce /
+ *     ComputeEffectiveStiffness (RP/10-Integrators/03-Newmark/
+ *     NewmarkBeta.cpp:35-66, 117-141, 198-235),
+ *   Linear::ComputeNewIncrement (RP/09-Algorithms/01-Linear/Linear.cpp:22-56),
+ *   and the effective-stiffness solve of EigenSolver::SolveSystem /
+ *     PetscSolver KSP CG (RP/11-Solvers/01-Direct/EigenSolver.cpp:19-59,
+ *     RP/11-Solvers/02-Iterative/PetscSolver.cc:53-150).
+ * The effective stiffness T^T (K + 4/dt^2 M) T is never assembled: the
+ * Jacobi-preconditioned conjugate gradient applies it element by element
+ * (the stiffness action of every element, summed per node in ascending
+ * element order, plus the lumped mass), in FP64, and stops on the TRUE
+ * relative residual |Feff - Keff du| / |Feff| <= pcg_tol.  Dot products are
+ * reduced in a fixed order: runs are bitwise reproducible.
+ * Covered: elastic materials, lumped mass, no constraints, no support
+ * motion; other models return SVL_ERR_UNSUPPORTED. */
+#define SVL_PRECOND_JACOBI 0
+typedef struct svl_nm_opts {
+    double  dt;
+    double  ftol;        /* force assembly tolerance (as svl_cd_opts)             */
+    double  mtol;        /* mass assembly tolerance                               */
+    double  pcg_tol;     /* relative true-residual tolerance of each solve        */
+    int32_t pcg_maxit;   /* iteration cap per solve (SVL_ERR_MAXITER past it)     */
+    int32_t precond;     /* SVL_PRECOND_JACOBI                                    */
+} svl_nm_opts;
+
+typedef struct svl_nm svl_nm;
+int  svl_nm_create(const svl_model_desc* model, const svl_load_desc* loads,
+                   const svl_nm_opts* opts, svl_nm** out);
+/* Initial conditions on total dofs (host arrays, NULL = zero). */
+int  svl_nm_set_initial(svl_nm* nm, const double* U0, const double* V0, const double* A0);
+/* Steps k_first .. k_first+nsteps-1; U_hist as in svl_cd_run. */
+int  svl_nm_run(svl_nm* nm, int32_t k_first, int32_t nsteps, double* U_hist);
+/* svl_nm_run without history bracketed by CUDA events on the handle's
+ * stream; *ms = elapsed time (measurement hook, no counterpart). */
+int  svl_nm_run_timed(svl_nm* nm, int32_t k_first, int32_t nsteps, float* ms);
+int  svl_nm_get(svl_nm* nm, int32_t which, double* out);
+/* Conjugate-gradient iterations summed over all solves, of the last solve,
+ * and the last solve's true relative residual. */
+int  svl_nm_stats(svl_nm* nm, int64_t* iters_total, int64_t* iters_last, double* rel_residual_last);
+int  svl_nm_launch_count(svl_nm* nm, int64_t* launches);
+int  svl_nm_sync(svl_nm* nm);
+void svl_nm_destroy(svl_nm* nm);
+
 /* ---- stepping without device allocation -------------------------------- */
 /* No counterpart in the reference: SVL allocates all of its (host) memory
  * freely.  Some callers of this library cannot let it call cudaMalloc or

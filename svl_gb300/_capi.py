@@ -38,6 +38,8 @@ SVL_NOALLOC_SCRATCH_BYTES = 8 << 20
 SVL_PREC_FP64 = 0
 SVL_PREC_MIXED = 1
 
+SVL_PRECOND_JACOBI = 0
+
 i32p = C.POINTER(C.c_int32)
 f64p = C.POINTER(C.c_double)
 
@@ -74,6 +76,11 @@ class GridSpec(C.Structure):
 class CdOpts(C.Structure):
     _fields_ = [("dt", C.c_double), ("ftol", C.c_double), ("mtol", C.c_double),
                 ("precision", C.c_int32), ("check_every", C.c_int32)]
+
+
+class NmOpts(C.Structure):
+    _fields_ = [("dt", C.c_double), ("ftol", C.c_double), ("mtol", C.c_double), ("pcg_tol", C.c_double),
+                ("pcg_maxit", C.c_int32), ("precond", C.c_int32)]
 
 
 def ptr(a, ctype):
@@ -130,6 +137,16 @@ def lib():
     L.svl_cd_run_noalloc.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p]
     L.svl_cd_destroy.argtypes = [C.c_void_p]
     L.svl_cd_destroy.restype = None
+    L.svl_nm_create.argtypes = [C.POINTER(ModelDesc), C.POINTER(LoadDesc), C.POINTER(NmOpts), C.POINTER(C.c_void_p)]
+    L.svl_nm_set_initial.argtypes = [C.c_void_p, f64p, f64p, f64p]
+    L.svl_nm_run.argtypes = [C.c_void_p, C.c_int32, C.c_int32, f64p]
+    L.svl_nm_run_timed.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(C.c_float)]
+    L.svl_nm_get.argtypes = [C.c_void_p, C.c_int32, f64p]
+    L.svl_nm_stats.argtypes = [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_double)]
+    L.svl_nm_launch_count.argtypes = [C.c_void_p, C.POINTER(C.c_int64)]
+    L.svl_nm_sync.argtypes = [C.c_void_p]
+    L.svl_nm_destroy.argtypes = [C.c_void_p]
+    L.svl_nm_destroy.restype = None
     _lib = L
     return L
 

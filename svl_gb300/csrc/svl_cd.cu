@@ -898,3 +898,402 @@ extern "C" int svl_cd_run_noalloc(svl_cd* cd, int32_t k_first, int32_t nsteps, d
         CUDA_TRY(cudaMemcpyAsync(d_U_out, d.U, sizeof(double) * m.ntotal, cudaMemcpyDeviceToDevice, cd->stream));
     return SVL_OK;
 }
+
+// ===========================================================================
+// Implicit Newmark (average acceleration, beta = 1/4, gamma = 1/2) with the
+// Linear algorithm and a matrix-free Jacobi-preconditioned conjugate-gradient
+// solve of the effective stiffness (FP64).
+//
+// Per step (RP/10-Integrators/03-Newmark/NewmarkBeta.cpp:117-141, 198-235;
+// ExtendedNewmarkBeta with G = 0):
+//   Feff = T^T [Fext - Fint + M (4/dt V + A)]
+//   Keff = T^T (K + 4/dt^2 M) T          (applied matrix-free: element
+//                                          stiffness action + lumped mass)
+//   solve Keff du = Feff                    (EigenSolver / PetscSolver.cc:53-150 KSPCG)
+//   dU = T du;  U += dU;  A = 4/dt^2 dU - 4/dt V - A;  V = 2/dt dU - V
+// The solve stops on the true relative residual |Feff - Keff du| / |Feff|.
+// Dot products are reduced in a fixed order (block partials, then one block),
+// so runs are bitwise reproducible.
+
+namespace {
+
+constexpr int kDotBlocks = 304;         // 2 x 152 SMs, fixed so the reduction order is fixed
+constexpr int kDotThreads = 256;
+
+// partial[blockIdx] = sum over a fixed strided subset of a[i]*b[i]
+__global__ void __launch_bounds__(kDotThreads) k_dot_partial(const double* __restrict__ a, const double* __restrict__ b,
+                                                             int n, double* __restrict__ partial) {
+    __shared__ double sh[kDotThreads / 32];
+    double s = 0.0;
+    for (int i = blockIdx.x * kDotThreads + threadIdx.x; i < n; i += kDotBlocks * kDotThreads) s += a[i] * b[i];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double t = threadIdx.x < kDotThreads / 32 ? sh[threadIdx.x] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+        if (threadIdx.x == 0) partial[blockIdx.x] = t;
+    }
+}
+
+// out[slot] = sum of the kDotBlocks partials (one block, fixed order)
+__global__ void k_dot_final(const double* __restrict__ partial, double* out, int slot) {
+    __shared__ double sh[kDotThreads / 32];
+    double s = 0.0;
+    for (int i = threadIdx.x; i < kDotBlocks; i += kDotThreads) s += partial[i];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double t = threadIdx.x < kDotThreads / 32 ? sh[threadIdx.x] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+        if (threadIdx.x == 0) out[slot] = t;
+    }
+}
+
+// Scalars of the PCG, in device memory: 0 rz, 1 pq, 2 rr, 3 bb, 4 rz_new
+enum { S_RZ = 0, S_PQ = 1, S_RR = 2, S_BB = 3, S_RZN = 4, S_NSCAL = 8 };
+
+// Effective force per node (identity T): b_f = (Fext - Fint) + M (4/dt V + A)
+template <int ND>
+__global__ void __launch_bounds__(256) k_nm_rhs(DevView d, double* __restrict__ b, double c_v) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= d.nnode) return;
+    const int k = d.step[0];
+#pragma unroll
+    for (int c = 0; c < ND; ++c) {
+        const int t = d.ntdof[n * ND + c];
+        const int f = d.tfree[t];
+        if (f < 0) continue;
+        const double fint = gather_fint<ND>(d, n, c);
+        const double fext = fext_at(d, t, k);
+        b[f] = ((fext + 0.0) - fint) + d.Md[t] * (c_v * d.V[t] + d.A[t]);
+    }
+}
+
+// q = Keff p: scatter p to total dofs (free part), element stiffness action done by
+// k_element on that vector, then q_f = sum_e (K_e p_e) + 4/dt^2 M p (identity T).
+__global__ void k_nm_expand(DevView d, const double* __restrict__ pf, double* __restrict__ pt) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= d.ntotal) return;
+    const int f = d.tfree[t];
+    pt[t] = f >= 0 ? pf[f] : 0.0;
+}
+
+template <int ND>
+__global__ void __launch_bounds__(256) k_nm_apply(DevView d, const double* __restrict__ pt, double* __restrict__ q, double c_m) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= d.nnode) return;
+#pragma unroll
+    for (int c = 0; c < ND; ++c) {
+        const int t = d.ntdof[n * ND + c];
+        const int f = d.tfree[t];
+        if (f < 0) continue;
+        q[f] = gather_fint<ND>(d, n, c) + c_m * d.Md[t] * pt[t];
+    }
+}
+
+// x += alpha p; r -= alpha q; z = Dinv r   (alpha = rz / pq)
+__global__ void k_pcg_xr(const double* __restrict__ sc, const double* __restrict__ p, const double* __restrict__ q,
+                         const double* __restrict__ dinv, double* x, double* r, double* z, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double alpha = sc[S_RZ] / sc[S_PQ];
+    x[i] += alpha * p[i];
+    const double ri = r[i] - alpha * q[i];
+    r[i] = ri;
+    z[i] = dinv[i] * ri;
+}
+
+// p = z + beta p (beta = rz_new / rz), then rz = rz_new
+__global__ void k_pcg_p(double* sc, const double* __restrict__ z, double* p, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const double beta = sc[S_RZN] / sc[S_RZ];
+    if (i < n) p[i] = z[i] + beta * p[i];
+}
+__global__ void k_pcg_roll(double* sc) { sc[S_RZ] = sc[S_RZN]; }
+
+// r = b - q; z = Dinv r; p = z   (start / residual replacement)
+__global__ void k_pcg_reset(const double* __restrict__ b, const double* __restrict__ q, const double* __restrict__ dinv,
+                            double* r, double* z, double* p, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double ri = b[i] - q[i];
+    r[i] = ri;
+    const double zi = dinv[i] * ri;
+    z[i] = zi;
+    p[i] = zi;
+}
+
+// state update after the solve (NewmarkBeta.cpp:130-139), identity T, no support motion
+template <int ND>
+__global__ void __launch_bounds__(256) k_nm_update(DevView d, const double* __restrict__ du, double c_a, double c_av,
+                                                   double c_vv, int* flag) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= d.nnode) return;
+    bool bad = false;
+#pragma unroll
+    for (int c = 0; c < ND; ++c) {
+        const int t = d.ntdof[n * ND + c];
+        const int f = d.tfree[t];
+        const double dU = f >= 0 ? du[f] : 0.0;
+        const double u = d.U[t] + dU;
+        d.U[t] = u;
+        d.Us[t] = u;
+        d.A[t] = c_a * dU - c_av * d.V[t] - d.A[t];
+        d.V[t] = c_vv * dU - d.V[t];
+        bad |= !isfinite(u);
+    }
+    if (bad) atomicOr(flag, 1);
+}
+
+__global__ void k_step_inc(int* step) { step[0] += 1; }
+
+}  // namespace
+
+struct svl_nm {
+    svl_cd* cd = nullptr;          // model tables, state vectors, stream (shared layout)
+    svl_nm_opts opts{};
+    int nf = 0;
+    double *b = nullptr, *x = nullptr, *r = nullptr, *z = nullptr, *p = nullptr, *q = nullptr, *pt = nullptr;
+    double *dinv = nullptr, *partial = nullptr, *sc = nullptr;
+    int64_t iters_total = 0, iters_last = 0;
+    double res_last = 0.0;
+    ~svl_nm() { delete cd; }
+};
+
+static int nm_dot(svl_nm* nm, const double* a, const double* b, int slot) {
+    k_dot_partial<<<kDotBlocks, kDotThreads, 0, nm->cd->stream>>>(a, b, nm->nf, nm->partial);
+    k_dot_final<<<1, kDotThreads, 0, nm->cd->stream>>>(nm->partial, nm->sc, slot);
+    nm->cd->launches += 2;
+    return SVL_OK;
+}
+
+// q = Keff v (free dofs)
+static int nm_apply(svl_nm* nm, const double* v, double* q) {
+    svl_cd* cd = nm->cd;
+    const HostModel& m = cd->m;
+    DevView d = cd->d;
+    d.ftol = -1.0;                  // the operator action is not filtered
+    const int tb = 256;
+    k_nm_expand<<<(m.ntotal + tb - 1) / tb, tb, 0, cd->stream>>>(d, v, nm->pt);
+    const int eg = (m.nelem + 127) / 128;
+    if (m.ndim == 2) k_element<2, 4><<<eg, 128, 0, cd->stream>>>(d, nm->pt, m.ngp, 0);
+    else k_element<3, 8><<<eg, 128, 0, cd->stream>>>(d, nm->pt, m.ngp, 0);
+    const double c_m = 4.0 / nm->opts.dt / nm->opts.dt;
+    if (m.ndim == 2) k_nm_apply<2><<<(m.nnode + tb - 1) / tb, tb, 0, cd->stream>>>(d, nm->pt, q, c_m);
+    else k_nm_apply<3><<<(m.nnode + tb - 1) / tb, tb, 0, cd->stream>>>(d, nm->pt, q, c_m);
+    cd->launches += 3;
+    CUDA_TRY(cudaGetLastError());
+    return SVL_OK;
+}
+
+static int nm_solve(svl_nm* nm) {
+    svl_cd* cd = nm->cd;
+    const int n = nm->nf, tb = 256, g = (n + tb - 1) / tb;
+    double hs[S_NSCAL];
+    CUDA_TRY(cudaMemsetAsync(nm->x, 0, sizeof(double) * n, cd->stream));
+    nm_dot(nm, nm->b, nm->b, S_BB);
+    CUDA_TRY(cudaMemsetAsync(nm->q, 0, sizeof(double) * n, cd->stream));
+    k_pcg_reset<<<g, tb, 0, cd->stream>>>(nm->b, nm->q, nm->dinv, nm->r, nm->z, nm->p, n);
+    nm_dot(nm, nm->r, nm->z, S_RZ);
+    CUDA_TRY(cudaMemcpyAsync(hs, nm->sc, sizeof(hs), cudaMemcpyDeviceToHost, cd->stream));
+    CUDA_TRY(cudaStreamSynchronize(cd->stream));
+    const double bb = hs[S_BB];
+    nm->iters_last = 0;
+    nm->res_last = 0.0;
+    if (bb == 0.0) return SVL_OK;
+    const double tol2 = nm->opts.pcg_tol * nm->opts.pcg_tol * bb;
+    const int check = 4;
+    for (int it = 1; it <= nm->opts.pcg_maxit; ++it) {
+        TRY(nm_apply(nm, nm->p, nm->q));
+        nm_dot(nm, nm->p, nm->q, S_PQ);
+        k_pcg_xr<<<g, tb, 0, cd->stream>>>(nm->sc, nm->p, nm->q, nm->dinv, nm->x, nm->r, nm->z, n);
+        nm_dot(nm, nm->r, nm->z, S_RZN);
+        nm_dot(nm, nm->r, nm->r, S_RR);
+        k_pcg_p<<<g, tb, 0, cd->stream>>>(nm->sc, nm->z, nm->p, n);
+        k_pcg_roll<<<1, 1, 0, cd->stream>>>(nm->sc);
+        cd->launches += 3;
+        nm->iters_last = it;
+        if (it % check == 0 || it == nm->opts.pcg_maxit) {
+            CUDA_TRY(cudaMemcpyAsync(hs, nm->sc, sizeof(hs), cudaMemcpyDeviceToHost, cd->stream));
+            CUDA_TRY(cudaStreamSynchronize(cd->stream));
+            if (!(hs[S_PQ] > 0.0)) { set_error("PCG breakdown: p.Kp = %g at iteration %d", hs[S_PQ], it); return SVL_ERR_BREAKDOWN; }
+            if (!std::isfinite(hs[S_RR])) { set_error("PCG residual is not finite"); return SVL_ERR_NONFINITE; }
+            if (hs[S_RR] <= tol2) {
+                // confirm with the true residual, replace the recursive one if it drifted
+                TRY(nm_apply(nm, nm->x, nm->q));
+                k_pcg_reset<<<g, tb, 0, cd->stream>>>(nm->b, nm->q, nm->dinv, nm->r, nm->z, nm->p, n);
+                nm_dot(nm, nm->r, nm->r, S_RR);
+                nm_dot(nm, nm->r, nm->z, S_RZ);
+                cd->launches += 1;
+                CUDA_TRY(cudaMemcpyAsync(hs, nm->sc, sizeof(hs), cudaMemcpyDeviceToHost, cd->stream));
+                CUDA_TRY(cudaStreamSynchronize(cd->stream));
+                nm->res_last = std::sqrt(hs[S_RR] / bb);
+                if (hs[S_RR] <= tol2) { nm->iters_total += it; return SVL_OK; }
+            }
+        }
+    }
+    nm->iters_total += nm->iters_last;
+    CUDA_TRY(cudaMemcpyAsync(hs, nm->sc, sizeof(hs), cudaMemcpyDeviceToHost, cd->stream));
+    CUDA_TRY(cudaStreamSynchronize(cd->stream));
+    nm->res_last = std::sqrt(hs[S_RR] / bb);
+    set_error("PCG did not reach %g in %d iterations (relative residual %g)", nm->opts.pcg_tol, nm->opts.pcg_maxit, nm->res_last);
+    return SVL_ERR_MAXITER;
+}
+
+extern "C" {
+
+int svl_nm_create(const svl_model_desc* model, const svl_load_desc* loads, const svl_nm_opts* opts, svl_nm** out) {
+    if (!out || !opts) { set_error("NULL argument"); return SVL_ERR_INVALID; }
+    *out = nullptr;
+    if (!(opts->dt > 0.0) || !(opts->pcg_tol > 0.0) || opts->pcg_maxit <= 0) { set_error("bad Newmark options"); return SVL_ERR_INVALID; }
+    svl_cd_opts co{};
+    co.dt = opts->dt; co.ftol = opts->ftol; co.mtol = opts->mtol; co.precision = SVL_PREC_FP64; co.check_every = 0;
+    svl_cd* cd = nullptr;
+    int st = svl_cd_create(model, loads, &co, &cd);
+    if (st) return st;
+    svl_nm* nm = new svl_nm();
+    nm->cd = cd;
+    nm->opts = *opts;
+    auto fail = [&](int s2) { delete nm; return s2; };
+    const HostModel& m = cd->m;
+    if (!cd->identity_T) { set_error("the implicit path does not take constraints yet"); return fail(SVL_ERR_UNSUPPORTED); }
+    if (cd->has_sm) { set_error("the implicit path does not take support motion yet"); return fail(SVL_ERR_UNSUPPORTED); }
+    if (m.has_j2()) { set_error("the implicit Linear path is elastic; J2 needs Newton iterations"); return fail(SVL_ERR_UNSUPPORTED); }
+    nm->nf = m.nfree;
+    // Jacobi diagonal: diag(K) + 4/dt^2 M on free dofs (identity T)
+    std::vector<double> Kd(m.ntotal, 0.0);
+    const int nc = m.nen * m.ndof;
+    for (int e = 0; e < m.nelem; ++e) {
+        const double* pr = m.param(e);
+        const double E = pr[0], nu = pr[1];
+        const double c1 = E * (1.0 - nu) / (1.0 - 2.0 * nu) / (1.0 + nu), c2 = E * nu / (1.0 - 2.0 * nu) / (1.0 + nu),
+                     c3 = E / (2.0 * (1.0 + nu));
+        std::vector<double> kd(nc, 0.0);
+        for (int q = 0; q < m.ngp; ++q) {
+            double dNx[8][3], N[8];
+            const double w = gp_factor(m, e, gp_geometry(m, e, q, dNx, N));
+            for (int a = 0; a < m.nen; ++a) {
+                const double bx = dNx[a][0], by = dNx[a][1], bz = dNx[a][2];
+                if (m.ndim == 2) {
+                    kd[2 * a] += w * (c1 * bx * bx + c3 * by * by);
+                    kd[2 * a + 1] += w * (c1 * by * by + c3 * bx * bx);
+                } else {
+                    kd[3 * a] += w * (c1 * bx * bx + c3 * (by * by + bz * bz));
+                    kd[3 * a + 1] += w * (c1 * by * by + c3 * (bx * bx + bz * bz));
+                    kd[3 * a + 2] += w * (c1 * bz * bz + c3 * (bx * bx + by * by));
+                }
+            }
+        }
+        (void)c2;
+        for (int a = 0; a < m.nen; ++a)
+            for (int c = 0; c < m.ndof; ++c) Kd[m.tdof[(size_t)m.conn[(size_t)e * m.nen + a] * m.ndof + c]] += kd[a * m.ndof + c];
+    }
+    std::vector<double> M;
+    lumped_mass_diag(m, opts->mtol, M);
+    std::vector<double> dinv(std::max(m.nfree, 1), 1.0);
+    const double c_m = 4.0 / opts->dt / opts->dt;
+    for (int n = 0; n < m.nnode; ++n)
+        for (int c = 0; c < m.ndof; ++c) {
+            const int t = m.tdof[(size_t)n * m.ndof + c], f = m.fdof[(size_t)n * m.ndof + c];
+            if (f >= 0) dinv[f] = 1.0 / (Kd[t] + c_m * M[t]);
+        }
+    double** vecs[] = {&nm->b, &nm->x, &nm->r, &nm->z, &nm->p, &nm->q};
+    for (double** pv : vecs) if ((st = cd->zeros((size_t)std::max(m.nfree, 1), pv))) return fail(st);
+    if ((st = cd->zeros((size_t)m.ntotal, &nm->pt)) || (st = cd->zeros(kDotBlocks, &nm->partial)) ||
+        (st = cd->zeros(S_NSCAL, &nm->sc)))
+        return fail(st);
+    const double* dd = nullptr;
+    if ((st = cd->upload(dinv, &dd))) return fail(st);
+    nm->dinv = const_cast<double*>(dd);
+    if (cudaStreamSynchronize(cd->stream) != cudaSuccess) { set_error("upload failed"); return fail(SVL_ERR_CUDA); }
+    *out = nm;
+    return SVL_OK;
+}
+
+int svl_nm_set_initial(svl_nm* nm, const double* U0, const double* V0, const double* A0) {
+    if (!nm) { set_error("NULL handle"); return SVL_ERR_INVALID; }
+    TRY(svl_cd_set_initial(nm->cd, U0, V0, A0));
+    // strain displacement = U0 for an elastic start from given displacements
+    if (U0) CUDA_TRY(cudaMemcpy(nm->cd->d.Us, nm->cd->d.U, sizeof(double) * nm->cd->m.ntotal, cudaMemcpyDeviceToDevice));
+    return SVL_OK;
+}
+
+int svl_nm_run(svl_nm* nm, int32_t k_first, int32_t nsteps, double* U_hist) {
+    if (!nm || nsteps < 0) { set_error("bad argument"); return SVL_ERR_INVALID; }
+    svl_cd* cd = nm->cd;
+    const HostModel& m = cd->m;
+    const int64_t l0 = cd->launches;
+    const double dt = nm->opts.dt;
+    int kstart = k_first - 1;
+    CUDA_TRY(cudaMemcpyAsync(cd->d.step, &kstart, sizeof(int), cudaMemcpyHostToDevice, cd->stream));
+    const int tb = 256, ng = (m.nnode + tb - 1) / tb, eg = (m.nelem + 127) / 128;
+    for (int s = 0; s < nsteps; ++s) {
+        k_step_inc<<<1, 1, 0, cd->stream>>>(cd->d.step);
+        // internal force from the committed state (filtered like the assembler)
+        if (m.ndim == 2) k_element<2, 4><<<eg, 128, 0, cd->stream>>>(cd->d, cd->d.Us, m.ngp, 0);
+        else k_element<3, 8><<<eg, 128, 0, cd->stream>>>(cd->d, cd->d.Us, m.ngp, 0);
+        if (m.ndim == 2) k_nm_rhs<2><<<ng, tb, 0, cd->stream>>>(cd->d, nm->b, 4.0 / dt);
+        else k_nm_rhs<3><<<ng, tb, 0, cd->stream>>>(cd->d, nm->b, 4.0 / dt);
+        cd->launches += 3;
+        CUDA_TRY(cudaGetLastError());
+        TRY(nm_solve(nm));
+        if (m.ndim == 2) k_nm_update<2><<<ng, tb, 0, cd->stream>>>(cd->d, nm->x, 4.0 / dt / dt, 4.0 / dt, 2.0 / dt, cd->d.flag);
+        else k_nm_update<3><<<ng, tb, 0, cd->stream>>>(cd->d, nm->x, 4.0 / dt / dt, 4.0 / dt, 2.0 / dt, cd->d.flag);
+        cd->launches += 1;
+        CUDA_TRY(cudaGetLastError());
+        if (U_hist) CUDA_TRY(cudaMemcpyAsync(U_hist + (size_t)s * m.ntotal, cd->d.U, sizeof(double) * m.ntotal, cudaMemcpyDeviceToHost, cd->stream));
+    }
+    cd->launches_last = cd->launches - l0;
+    int flag = 0;
+    CUDA_TRY(cudaMemcpyAsync(&flag, cd->d.flag, sizeof(int), cudaMemcpyDeviceToHost, cd->stream));
+    CUDA_TRY(cudaStreamSynchronize(cd->stream));
+    if (flag) { set_error("non-finite displacement detected"); return SVL_ERR_NONFINITE; }
+    return SVL_OK;
+}
+
+int svl_nm_run_timed(svl_nm* nm, int32_t k_first, int32_t nsteps, float* ms) {
+    if (!nm || !ms) { set_error("NULL argument"); return SVL_ERR_INVALID; }
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    CUDA_TRY(cudaEventCreate(&e0));
+    if (cudaEventCreate(&e1) != cudaSuccess) { cudaEventDestroy(e0); set_error("cudaEventCreate failed"); return SVL_ERR_CUDA; }
+    int st = SVL_OK;
+    if (cudaEventRecord(e0, nm->cd->stream) != cudaSuccess) st = SVL_ERR_CUDA;
+    if (!st) st = svl_nm_run(nm, k_first, nsteps, nullptr);
+    if (!st && cudaEventRecord(e1, nm->cd->stream) != cudaSuccess) st = SVL_ERR_CUDA;
+    if (!st && cudaEventSynchronize(e1) != cudaSuccess) st = SVL_ERR_CUDA;
+    if (!st && cudaEventElapsedTime(ms, e0, e1) != cudaSuccess) st = SVL_ERR_CUDA;
+    if (st == SVL_ERR_CUDA) set_error("event timing failed");
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return st;
+}
+
+int svl_nm_get(svl_nm* nm, int32_t which, double* out) {
+    if (!nm) { set_error("NULL handle"); return SVL_ERR_INVALID; }
+    return svl_cd_get(nm->cd, which, out);
+}
+
+int svl_nm_stats(svl_nm* nm, int64_t* iters_total, int64_t* iters_last, double* rel_residual_last) {
+    if (!nm) { set_error("NULL handle"); return SVL_ERR_INVALID; }
+    if (iters_total) *iters_total = nm->iters_total;
+    if (iters_last) *iters_last = nm->iters_last;
+    if (rel_residual_last) *rel_residual_last = nm->res_last;
+    return SVL_OK;
+}
+
+int svl_nm_launch_count(svl_nm* nm, int64_t* launches) {
+    if (!nm || !launches) { set_error("NULL argument"); return SVL_ERR_INVALID; }
+    *launches = nm->cd->launches_last;
+    return SVL_OK;
+}
+
+int svl_nm_sync(svl_nm* nm) {
+    if (!nm) { set_error("NULL handle"); return SVL_ERR_INVALID; }
+    return svl_cd_sync(nm->cd);
+}
+
+void svl_nm_destroy(svl_nm* nm) { delete nm; }
+
+}  // extern "C"

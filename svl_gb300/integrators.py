@@ -159,3 +159,80 @@ class StructuredCentralDifference:
             self.close()
         except Exception:
             pass
+
+
+class NewmarkBeta:
+    """Implicit Newmark, average acceleration (beta = 1/4, gamma = 1/2), with
+    the Linear algorithm: one effective-stiffness solve per step by a
+    matrix-free Jacobi-preconditioned conjugate gradient in FP64 that stops
+    on the true relative residual (svl_nm_*).  Mirrors NewmarkBeta
+    (RP/10-Integrators/03-Newmark/NewmarkBeta.cpp) driven by Linear
+    (RP/09-Algorithms/01-Linear/Linear.cpp) over an iterative LinearSystem
+    (RP/11-Solvers/02-Iterative/PetscSolver.cc, KSPCG, rtol `pcg_tol`)."""
+
+    def __init__(self, model: Model, loads: Loads | None, dt: float, pcg_tol: float = 1e-8,
+                 pcg_maxit: int = 20000, ftol: float = 1e-12, mtol: float = 1e-12):
+        self.model = model
+        self.dt = float(dt)
+        self._md = model.desc()
+        self._ld = (loads or Loads()).desc()
+        opts = capi.NmOpts(dt=self.dt, ftol=ftol, mtol=mtol, pcg_tol=float(pcg_tol), pcg_maxit=int(pcg_maxit),
+                           precond=capi.SVL_PRECOND_JACOBI)
+        h = C.c_void_p()
+        check(lib().svl_nm_create(C.byref(self._md), C.byref(self._ld), C.byref(opts), C.byref(h)))
+        self._h = h
+        self.ntotal = model.ntotal
+
+    def Initialize(self, U0=None, V0=None, A0=None):
+        arrs = [None if a is None else capi.as_f64(a) for a in (U0, V0, A0)]
+        check(lib().svl_nm_set_initial(self._h, *(ptr(a, C.c_double) for a in arrs)))
+
+    def ComputeNewStep(self, k: int) -> bool:
+        """One step k; returns True on failure (the reference's `stop`)."""
+        return lib().svl_nm_run(self._h, int(k), 1, ptr(None, C.c_double)) != capi.SVL_OK
+
+    def GetDisplacements(self) -> np.ndarray:
+        return self._get(0)
+
+    def GetVelocities(self) -> np.ndarray:
+        return self._get(1)
+
+    def GetAccelerations(self) -> np.ndarray:
+        return self._get(2)
+
+    def run(self, k_first: int, nsteps: int, history: bool = False):
+        hist = np.zeros((nsteps, self.ntotal)) if history else None
+        check(lib().svl_nm_run(self._h, int(k_first), int(nsteps), ptr(hist, C.c_double)))
+        return hist
+
+    def run_timed(self, k_first: int, nsteps: int) -> float:
+        ms = C.c_float()
+        check(lib().svl_nm_run_timed(self._h, int(k_first), int(nsteps), C.byref(ms)))
+        return float(ms.value)
+
+    def stats(self):
+        """(CG iterations over all solves, of the last solve, last true relative residual)."""
+        a, b, r = C.c_int64(), C.c_int64(), C.c_double()
+        check(lib().svl_nm_stats(self._h, C.byref(a), C.byref(b), C.byref(r)))
+        return int(a.value), int(b.value), float(r.value)
+
+    def launches(self) -> int:
+        n = C.c_int64()
+        check(lib().svl_nm_launch_count(self._h, C.byref(n)))
+        return int(n.value)
+
+    def _get(self, which):
+        out = np.zeros(self.ntotal)
+        check(lib().svl_nm_get(self._h, which, ptr(out, C.c_double)))
+        return out
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().svl_nm_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

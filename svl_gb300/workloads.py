@@ -9,6 +9,11 @@ benchmark configurations (no reference data is used):
   double-couple-like body force (four element groups) with a Ricker
   f0 = 3 Hz, dt = 0.5 h / max Vp.  Boundary: fixed bottom, rollers on the
   sides (the PML layers of the configuration are not built yet).
+* config4: 64 x 64 x 64 lin3DHexa8 box, h = 1 m, seeded piecewise-layered
+  shear modulus (layer contrast up to 100x) times 10% log-normal noise per
+  element, nu = 0.3, rho = 2000, Newmark average acceleration at
+  dt = 10 x the explicit limit h / max Vp, the same double-couple Ricker
+  source (f0 = 3 Hz); fixed bottom, rollers on the sides.
 """
 from __future__ import annotations
 
@@ -76,6 +81,47 @@ def config2(nx=128, ny=128, nz=64, nt=4001, seed=0, amp=1.0e3):
     def eid(i, j, k):
         return (k * ny + j) * nx + i
     # double couple: +x on the element above, -x below; +y right, -y left
+    L.add_body_load(m, [eid(cx, cy + 1, cz)], (amp, 0.0, 0.0), s)
+    L.add_body_load(m, [eid(cx, cy - 1, cz)], (-amp, 0.0, 0.0), s)
+    L.add_body_load(m, [eid(cx + 1, cy, cz)], (0.0, amp, 0.0), s)
+    L.add_body_load(m, [eid(cx - 1, cy, cz)], (0.0, -amp, 0.0), s)
+    return m, L, dt
+
+
+def layered_stiffness(nz, n_layers, contrast, seed):
+    """Per-element-layer shear modulus factor: n_layers seeded layers of
+    random thickness, log-uniform factors in [1, contrast] (the softest and
+    stiffest layers pinned to 1 and `contrast`)."""
+    rng = np.random.default_rng(seed)
+    cuts = np.sort(rng.choice(np.arange(1, nz), size=n_layers - 1, replace=False))
+    f = np.exp(rng.uniform(0.0, np.log(contrast), n_layers))
+    f[np.argmin(f)], f[np.argmax(f)] = 1.0, contrast
+    layer = np.searchsorted(cuts, np.arange(nz), side="right")
+    return f[layer]
+
+
+def config4(nx=64, ny=64, nz=64, nt=501, seed=0, amp=1.0e3, contrast=100.0, n_layers=6):
+    h, rho, nu, vs_soft = 1.0, 2000.0, 0.3, 100.0
+    rng = np.random.default_rng(seed + 1)
+    ne = nx * ny * nz
+    fz = layered_stiffness(nz, n_layers, contrast, seed)          # [nz]
+    noise = np.exp(0.1 * rng.standard_normal(ne) - 0.5 * 0.1 ** 2)
+    k = np.arange(ne) // (nx * ny)                                   # element layer (x fastest)
+    G = rho * vs_soft ** 2 * fz[k] * noise
+    E = 2 * G * (1 + nu)
+    mp = np.zeros((ne, 8))
+    mp[:, 0], mp[:, 1], mp[:, 2] = E, nu, rho
+    m = Model.grid(3, (nx, ny, nz), (h, h, h), fix_mask=(1, 1, 2, 2, 7, 0),
+                   mat_type=np.full(ne, capi.SVL_MAT_ELASTIC3DLINEAR, np.int32), mat_param=mp,
+                   elem_mat=np.arange(ne, dtype=np.int32))
+    vp_max = np.sqrt(E.max() * (1 - nu) / ((1 + nu) * (1 - 2 * nu)) / rho)
+    dt = 10.0 * h / vp_max
+    L = Loads()
+    s = L.add_series(ricker(nt, dt, 3.0, amp=1.0))
+    cx, cy, cz = nx // 2, ny // 2, nz // 2
+
+    def eid(i, j, kk):
+        return (kk * ny + j) * nx + i
     L.add_body_load(m, [eid(cx, cy + 1, cz)], (amp, 0.0, 0.0), s)
     L.add_body_load(m, [eid(cx, cy - 1, cz)], (-amp, 0.0, 0.0), s)
     L.add_body_load(m, [eid(cx + 1, cy, cz)], (0.0, amp, 0.0), s)
