@@ -133,25 +133,45 @@ def cpu_baseline(m, L, dt, steps_cap, budget_s=20.0):
             "sample": "%d time steps of the same model on the CPU oracle (OpenMP element loop, ordered scatter)" % n}
 
 
-def implicit_pcg(steps, warm=2, tol=1e-8):
+def implicit_pcg(steps, warm=20, tol=1e-8):
     """Newmark (average acceleration) + Linear on the 64^3 layered H8 model:
     mean wall time per step of the effective-stiffness solve to a true
-    relative residual of `tol` (Jacobi-PCG, FP64, matrix-free)."""
+    relative residual of `tol`, Jacobi-PCG against the learned preconditioner
+    (flexible CG, Jacobi fallback), both FP64 matrix-free.  The learned handle
+    runs the same `warm` Jacobi steps first, then trains (timed separately)."""
     from svl_gb300 import NewmarkBeta, workloads
     m, L, dt = workloads.config4(nt=warm + steps + 2)
-    nm = NewmarkBeta(m, L, dt, pcg_tol=tol)
-    nm.Initialize()
-    nm.run(1, warm)
-    it0, _, _ = nm.stats()
-    ms = nm.run_timed(1 + warm, steps)
-    it1, _, res = nm.stats()
-    launches = nm.launches()
-    nm.close()
+    jac = NewmarkBeta(m, L, dt, pcg_tol=tol)
+    lrn = NewmarkBeta(m, L, dt, pcg_tol=tol)
+    for h in (jac, lrn):
+        h.Initialize()
+        h.run(1, warm)
+    t0 = time.perf_counter()
+    loss = lrn.train_preconditioner(1 + warm, **NN_TRAIN)
+    train_s = time.perf_counter() - t0
+    out = {}
+    for name, h in (("jacobi", jac), ("learned", lrn)):
+        it0 = h.stats()[0]
+        ms = h.run_timed(1 + warm, steps)
+        it1, _, res = h.stats()
+        out[name] = {"ms_per_step": ms / steps, "pcg_iters_per_step": (it1 - it0) / steps, "rel_residual_last": res,
+                     "gpu_launches": int(h.launches())}
+    solves, fallbacks, jref = lrn.precond_stats()
+    Uj, Ul = jac.GetDisplacements(), lrn.GetDisplacements()
+    jac.close()
+    lrn.close()
+    out["learned"].update({"train_seconds": train_s, "train_loss": loss, "fallbacks": fallbacks, "solves": solves,
+                           "train": dict(NN_TRAIN)})
     return {"workload": "lin3DHexa8 64x64x64 (h=1 m), layered G (100x contrast) x 10% log-normal, "
                         "Newmark beta=1/4 gamma=1/2, dt=10x explicit limit, fixed bottom, roller sides",
-            "free_dof": m.nfree, "steps": steps, "ms_per_step": ms / steps, "precond": "jacobi",
-            "pcg_iters_per_step": (it1 - it0) / steps, "rel_residual_last": res, "tol": tol,
-            "residual": "true |b - K_eff x| / |b|, FP64", "gpu_launches": int(launches)}
+            "free_dof": m.nfree, "steps": steps, "tol": tol, "residual": "true |b - K_eff x| / |b|, FP64",
+            "jacobi": out["jacobi"], "learned": out["learned"],
+            "speedup_learned_over_jacobi": out["jacobi"]["ms_per_step"] / out["learned"]["ms_per_step"],
+            "iteration_ratio": out["jacobi"]["pcg_iters_per_step"] / max(out["learned"]["pcg_iters_per_step"], 1e-9),
+            "rel_l2_final_u_learned_vs_jacobi": float(np.linalg.norm(Ul - Uj) / max(np.linalg.norm(Uj), 1e-300))}
+
+
+NN_TRAIN = {"solve_steps": 0, "n_synthetic": 400, "iters": 2000, "batch": 4, "lr": 2e-3, "seed": 1}
 
 
 def dist_info():

@@ -267,14 +267,15 @@ void svl_cdx_destroy(svl_cdx* cdx);
  * reduced in a fixed order: runs are bitwise reproducible.
  * Covered: elastic materials, lumped mass, no constraints, no support
  * motion; other models return SVL_ERR_UNSUPPORTED. */
-#define SVL_PRECOND_JACOBI 0
+#define SVL_PRECOND_JACOBI  0
+#define SVL_PRECOND_LEARNED 1   /* see svl_nm_train_preconditioner                */
 typedef struct svl_nm_opts {
     double  dt;
     double  ftol;        /* force assembly tolerance (as svl_cd_opts)             */
     double  mtol;        /* mass assembly tolerance                               */
     double  pcg_tol;     /* relative true-residual tolerance of each solve        */
     int32_t pcg_maxit;   /* iteration cap per solve (SVL_ERR_MAXITER past it)     */
-    int32_t precond;     /* SVL_PRECOND_JACOBI                                    */
+    int32_t precond;     /* SVL_PRECOND_JACOBI or SVL_PRECOND_LEARNED             */
 } svl_nm_opts;
 
 typedef struct svl_nm svl_nm;
@@ -294,6 +295,52 @@ int  svl_nm_stats(svl_nm* nm, int64_t* iters_total, int64_t* iters_last, double*
 int  svl_nm_launch_count(svl_nm* nm, int64_t* launches);
 int  svl_nm_sync(svl_nm* nm);
 void svl_nm_destroy(svl_nm* nm);
+
+/* ---- learned preconditioner (no counterpart in the reference) ----------- */
+/* For hexahedral models whose nodes form a lattice (svl_grid_build meshes and
+ * any other mesh with one node per point of an nx x ny x nz lattice), the
+ * solve can be preconditioned by a small 3D convolutional network on that
+ * lattice: z = D^-1/2 (r_hat + net(r_hat, rho r_hat)), r_hat = D^-1/2 r,
+ * D = diag(K_eff), rho = (4/dt^2 m) / D; four 3x3x3 convolutions
+ * 6 -> 16 -> 16 -> 16 -> 3 with ReLU between them, FP32.  The solve is then a
+ * flexible conjugate gradient (each direction K_eff-orthogonalised against
+ * the previous one).  Jacobi-PCG is both the fallback and the judge: a solve
+ * that has used as many iterations as the last plain Jacobi-PCG solve without
+ * reaching pcg_tol continues with Jacobi-PCG from where it stands, and every
+ * solve ends on the true FP64 residual.  The network is trained on the GPU
+ * by the library's own forward and backward kernels (Adam, fixed-order
+ * reductions). */
+typedef struct svl_nn_train_opts {
+    int32_t  solve_steps;  /* Newmark steps advanced with Jacobi-PCG whose CG
+                              iterates give (r_k, e_k = x* - x_k) pairs        */
+    int32_t  record_every; /* record every n-th CG iterate (at most 12 a solve) */
+    int32_t  n_synthetic;  /* pairs (e, r = K_eff e), e random with 0..5
+                              smoothing sweeps of the scaled operator          */
+    int32_t  iters;        /* Adam iterations                                  */
+    int32_t  batch;        /* pairs per iteration                              */
+    float    lr;           /* Adam step (decays to 1/4 at 60 %, 1/20 at 85 %) */
+    uint64_t seed;
+} svl_nn_train_opts;
+/* Runs the solve_steps steps k_first.. (they advance the state), generates
+ * the synthetic pairs, trains, and switches the handle to
+ * SVL_PRECOND_LEARNED.  *loss = mean relative squared error of the trained
+ * preconditioner on its pairs over the last tenth of the iterations. */
+int  svl_nm_train_preconditioner(svl_nm* nm, int32_t k_first, const svl_nn_train_opts* opts, float* loss);
+int  svl_nm_set_preconditioner(svl_nm* nm, int32_t precond);
+/* Number of network weights; get (w_out) and/or set (w_in) them.  Layout:
+ * layer by layer, [cout][cin][27] with tap t = 9 (dz+1) + 3 (dy+1) + (dx+1). */
+int  svl_nn_num_weights(void);
+int  svl_nm_preconditioner_weights(svl_nm* nm, float* w_out, const float* w_in);
+/* Solves that used the learned preconditioner, how many of them fell back to
+ * Jacobi-PCG, and the iteration count of the last plain Jacobi-PCG solve. */
+int  svl_nm_precond_stats(svl_nm* nm, int64_t* learned_solves, int64_t* fallbacks, int64_t* jacobi_ref_iters);
+/* Node lattice dims (nx, ny, nz), zeros if the model is not a lattice. */
+int  svl_nm_lattice(svl_nm* nm, int32_t* dims);
+/* Test hook: loss sum and weight gradient of one sample on the device.  x, t:
+ * host grids [3][nz][ny][nx] of r_hat and e_hat; grad: svl_nn_num_weights(). */
+int  svl_nm_nn_loss_grad(svl_nm* nm, const float* x, const float* t, float* loss, float* grad);
+/* Test hook: the rho feature grid and the free-dof mask grid, [3][nz][ny][nx]. */
+int  svl_nm_nn_grids(svl_nm* nm, float* rho, float* mask);
 
 /* ---- stepping without device allocation -------------------------------- */
 /* No counterpart in the reference: SVL allocates all of its (host) memory

@@ -39,6 +39,7 @@ SVL_PREC_FP64 = 0
 SVL_PREC_MIXED = 1
 
 SVL_PRECOND_JACOBI = 0
+SVL_PRECOND_LEARNED = 1
 
 i32p = C.POINTER(C.c_int32)
 f64p = C.POINTER(C.c_double)
@@ -81,6 +82,11 @@ class CdOpts(C.Structure):
 class NmOpts(C.Structure):
     _fields_ = [("dt", C.c_double), ("ftol", C.c_double), ("mtol", C.c_double), ("pcg_tol", C.c_double),
                 ("pcg_maxit", C.c_int32), ("precond", C.c_int32)]
+
+
+class NnTrainOpts(C.Structure):
+    _fields_ = [("solve_steps", C.c_int32), ("record_every", C.c_int32), ("n_synthetic", C.c_int32),
+                ("iters", C.c_int32), ("batch", C.c_int32), ("lr", C.c_float), ("seed", C.c_uint64)]
 
 
 def ptr(a, ctype):
@@ -145,6 +151,14 @@ def lib():
     L.svl_nm_stats.argtypes = [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_double)]
     L.svl_nm_launch_count.argtypes = [C.c_void_p, C.POINTER(C.c_int64)]
     L.svl_nm_sync.argtypes = [C.c_void_p]
+    f32p = C.POINTER(C.c_float)
+    L.svl_nm_train_preconditioner.argtypes = [C.c_void_p, C.c_int32, C.POINTER(NnTrainOpts), f32p]
+    L.svl_nm_set_preconditioner.argtypes = [C.c_void_p, C.c_int32]
+    L.svl_nm_preconditioner_weights.argtypes = [C.c_void_p, f32p, f32p]
+    L.svl_nm_precond_stats.argtypes = [C.c_void_p] + [C.POINTER(C.c_int64)] * 3
+    L.svl_nm_lattice.argtypes = [C.c_void_p, i32p]
+    L.svl_nm_nn_loss_grad.argtypes = [C.c_void_p, f32p, f32p, f32p, f32p]
+    L.svl_nm_nn_grids.argtypes = [C.c_void_p, f32p, f32p]
     L.svl_nm_destroy.argtypes = [C.c_void_p]
     L.svl_nm_destroy.restype = None
     _lib = L

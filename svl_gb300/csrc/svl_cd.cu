@@ -35,6 +35,7 @@
 #include <vector>
 
 #include "svl_internal.hpp"
+#include "svl_nnpc.hpp"
 
 using namespace svl;
 
@@ -1049,7 +1050,92 @@ __global__ void __launch_bounds__(256) k_nm_update(DevView d, const double* __re
 
 __global__ void k_step_inc(int* step) { step[0] += 1; }
 
+// two dot products in one pass: partial[0..B) = a1.b1, partial[B..2B) = a2.b2
+__global__ void __launch_bounds__(kDotThreads) k_dot2_partial(const double* __restrict__ a1, const double* __restrict__ b1,
+                                                              const double* __restrict__ a2, const double* __restrict__ b2,
+                                                              int n, double* __restrict__ partial) {
+    __shared__ double sh[2][kDotThreads / 32];
+    double s1 = 0.0, s2 = 0.0;
+    for (int i = blockIdx.x * kDotThreads + threadIdx.x; i < n; i += kDotBlocks * kDotThreads) {
+        s1 += a1[i] * b1[i];
+        s2 += a2[i] * b2[i];
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+        s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+    }
+    if ((threadIdx.x & 31) == 0) { sh[0][threadIdx.x >> 5] = s1; sh[1][threadIdx.x >> 5] = s2; }
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double t1 = threadIdx.x < kDotThreads / 32 ? sh[0][threadIdx.x] : 0.0;
+        double t2 = threadIdx.x < kDotThreads / 32 ? sh[1][threadIdx.x] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) {
+            t1 += __shfl_xor_sync(0xffffffffu, t1, o);
+            t2 += __shfl_xor_sync(0xffffffffu, t2, o);
+        }
+        if (threadIdx.x == 0) { partial[blockIdx.x] = t1; partial[kDotBlocks + blockIdx.x] = t2; }
+    }
+}
+
+// flexible CG scalars (slots of the same array as the PCG ones)
+enum { S_RP = 5, S_ZQ = 6 };
+
+// x += alpha p; r -= alpha q   (alpha = r.p / p.q)
+__global__ void k_fcg_xr(const double* __restrict__ sc, const double* __restrict__ p, const double* __restrict__ q,
+                         double* x, double* r, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double alpha = sc[S_RP] / sc[S_PQ];
+    x[i] += alpha * p[i];
+    r[i] -= alpha * q[i];
+}
+
+// p = z - (z.q / p.q) p   (A-orthogonal to the previous direction)
+__global__ void k_fcg_p(const double* __restrict__ sc, const double* __restrict__ z, double* p, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double beta = -sc[S_ZQ] / sc[S_PQ];
+    p[i] = z[i] + beta * p[i];
+}
+
+__global__ void k_vmul(const double* __restrict__ a, const double* __restrict__ b, double* __restrict__ out, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = a[i] * b[i];
+}
+
+// e -= w * sdinv .* q   (one Richardson sweep with the scaled operator)
+__global__ void k_smooth(double* e, const double* __restrict__ q, const double* __restrict__ sdinv, double w, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) e[i] -= w * sdinv[i] * q[i];
+}
+
+// e_hat = D^1/2 (x* - x_k)
+__global__ void k_ehat(const double* __restrict__ xs, const double* __restrict__ xk, const double* __restrict__ sdinv,
+                       double* __restrict__ out, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = (xs[i] - xk[i]) / sdinv[i];
+}
+
+__device__ __forceinline__ uint64_t mix64(uint64_t z) {
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+// standard normal samples (counter-based hash + Box-Muller)
+__global__ void k_randn(double* e, int n, uint64_t seed) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint64_t h1 = mix64(seed + 2ull * (uint64_t)i + 0x9E3779B97F4A7C15ull);
+    const uint64_t h2 = mix64(h1 ^ 0xD6E8FEB86659FD93ull);
+    const double u1 = ((double)(h1 >> 11) + 0.5) * (1.0 / 9007199254740992.0);
+    const double u2 = (double)(h2 >> 11) * (1.0 / 9007199254740992.0);
+    e[i] = sqrt(-2.0 * log(u1)) * cospi(2.0 * u2);
+}
+
 }  // namespace
+
+constexpr int kRecMax = 12;        // recorded CG iterates per solve
 
 struct svl_nm {
     svl_cd* cd = nullptr;          // model tables, state vectors, stream (shared layout)
@@ -1059,13 +1145,43 @@ struct svl_nm {
     double *dinv = nullptr, *partial = nullptr, *sc = nullptr;
     int64_t iters_total = 0, iters_last = 0;
     double res_last = 0.0;
-    ~svl_nm() { delete cd; }
+    // node-lattice models: learned preconditioner
+    bool lattice = false;
+    int lnx = 0, lny = 0, lnz = 0;
+    std::vector<int32_t> gmap;
+    std::vector<double> sdinv_h, rho_h;
+    double* sdinv = nullptr;
+    double *e1 = nullptr, *e2 = nullptr;
+    svl::NnPrecond* nn = nullptr;
+    int precond = SVL_PRECOND_JACOBI;
+    int64_t jac_ref = 0, fallbacks = 0, learned_solves = 0;
+    // CG iterates recorded for training pairs
+    int rec_every = 0, rec_n = 0;
+    std::vector<double*> rec_x, rec_r;
+    ~svl_nm() {
+        if (nn) svl::nn_destroy(nn);
+        delete cd;
+    }
 };
 
 static int nm_dot(svl_nm* nm, const double* a, const double* b, int slot) {
     k_dot_partial<<<kDotBlocks, kDotThreads, 0, nm->cd->stream>>>(a, b, nm->nf, nm->partial);
     k_dot_final<<<1, kDotThreads, 0, nm->cd->stream>>>(nm->partial, nm->sc, slot);
     nm->cd->launches += 2;
+    return SVL_OK;
+}
+
+static int nm_dot2(svl_nm* nm, const double* a1, const double* b1, int slot1, const double* a2, const double* b2, int slot2) {
+    k_dot2_partial<<<kDotBlocks, kDotThreads, 0, nm->cd->stream>>>(a1, b1, a2, b2, nm->nf, nm->partial);
+    k_dot_final<<<1, kDotThreads, 0, nm->cd->stream>>>(nm->partial, nm->sc, slot1);
+    k_dot_final<<<1, kDotThreads, 0, nm->cd->stream>>>(nm->partial + kDotBlocks, nm->sc, slot2);
+    nm->cd->launches += 3;
+    return SVL_OK;
+}
+
+static int nm_scalars(svl_nm* nm, double* hs) {
+    CUDA_TRY(cudaMemcpyAsync(hs, nm->sc, sizeof(double) * S_NSCAL, cudaMemcpyDeviceToHost, nm->cd->stream));
+    CUDA_TRY(cudaStreamSynchronize(nm->cd->stream));
     return SVL_OK;
 }
 
@@ -1088,59 +1204,191 @@ static int nm_apply(svl_nm* nm, const double* v, double* q) {
     return SVL_OK;
 }
 
-static int nm_solve(svl_nm* nm) {
+static int nm_record(svl_nm* nm, int it) {
+    if (nm->rec_every <= 0 || it % nm->rec_every != 0 || nm->rec_n >= (int)nm->rec_x.size()) return SVL_OK;
+    const size_t bytes = sizeof(double) * nm->nf;
+    CUDA_TRY(cudaMemcpyAsync(nm->rec_x[nm->rec_n], nm->x, bytes, cudaMemcpyDeviceToDevice, nm->cd->stream));
+    CUDA_TRY(cudaMemcpyAsync(nm->rec_r[nm->rec_n], nm->r, bytes, cudaMemcpyDeviceToDevice, nm->cd->stream));
+    nm->rec_n++;
+    return SVL_OK;
+}
+
+// Jacobi-PCG from x = 0 (warm = false) or from the current x.
+static int nm_solve_jacobi(svl_nm* nm, bool warm, int64_t maxit) {
     svl_cd* cd = nm->cd;
     const int n = nm->nf, tb = 256, g = (n + tb - 1) / tb;
     double hs[S_NSCAL];
-    CUDA_TRY(cudaMemsetAsync(nm->x, 0, sizeof(double) * n, cd->stream));
+    if (warm) {
+        TRY(nm_apply(nm, nm->x, nm->q));
+    } else {
+        CUDA_TRY(cudaMemsetAsync(nm->x, 0, sizeof(double) * n, cd->stream));
+        CUDA_TRY(cudaMemsetAsync(nm->q, 0, sizeof(double) * n, cd->stream));
+    }
     nm_dot(nm, nm->b, nm->b, S_BB);
-    CUDA_TRY(cudaMemsetAsync(nm->q, 0, sizeof(double) * n, cd->stream));
     k_pcg_reset<<<g, tb, 0, cd->stream>>>(nm->b, nm->q, nm->dinv, nm->r, nm->z, nm->p, n);
     nm_dot(nm, nm->r, nm->z, S_RZ);
-    CUDA_TRY(cudaMemcpyAsync(hs, nm->sc, sizeof(hs), cudaMemcpyDeviceToHost, cd->stream));
-    CUDA_TRY(cudaStreamSynchronize(cd->stream));
+    nm_dot(nm, nm->r, nm->r, S_RR);
+    TRY(nm_scalars(nm, hs));
     const double bb = hs[S_BB];
-    nm->iters_last = 0;
-    nm->res_last = 0.0;
-    if (bb == 0.0) return SVL_OK;
+    if (bb == 0.0) { nm->res_last = 0.0; return SVL_OK; }
     const double tol2 = nm->opts.pcg_tol * nm->opts.pcg_tol * bb;
+    if (warm && hs[S_RR] <= tol2) { nm->res_last = std::sqrt(hs[S_RR] / bb); return SVL_OK; }
     const int check = 4;
-    for (int it = 1; it <= nm->opts.pcg_maxit; ++it) {
+    for (int64_t it = 1; it <= maxit; ++it) {
         TRY(nm_apply(nm, nm->p, nm->q));
         nm_dot(nm, nm->p, nm->q, S_PQ);
         k_pcg_xr<<<g, tb, 0, cd->stream>>>(nm->sc, nm->p, nm->q, nm->dinv, nm->x, nm->r, nm->z, n);
-        nm_dot(nm, nm->r, nm->z, S_RZN);
-        nm_dot(nm, nm->r, nm->r, S_RR);
+        nm_dot2(nm, nm->r, nm->z, S_RZN, nm->r, nm->r, S_RR);
         k_pcg_p<<<g, tb, 0, cd->stream>>>(nm->sc, nm->z, nm->p, n);
         k_pcg_roll<<<1, 1, 0, cd->stream>>>(nm->sc);
         cd->launches += 3;
-        nm->iters_last = it;
-        if (it % check == 0 || it == nm->opts.pcg_maxit) {
-            CUDA_TRY(cudaMemcpyAsync(hs, nm->sc, sizeof(hs), cudaMemcpyDeviceToHost, cd->stream));
-            CUDA_TRY(cudaStreamSynchronize(cd->stream));
-            if (!(hs[S_PQ] > 0.0)) { set_error("PCG breakdown: p.Kp = %g at iteration %d", hs[S_PQ], it); return SVL_ERR_BREAKDOWN; }
+        nm->iters_last++;
+        nm->iters_total++;
+        TRY(nm_record(nm, (int)it));
+        if (it % check == 0 || it == maxit) {
+            TRY(nm_scalars(nm, hs));
+            if (!(hs[S_PQ] > 0.0)) { set_error("PCG breakdown: p.Kp = %g at iteration %lld", hs[S_PQ], (long long)it); return SVL_ERR_BREAKDOWN; }
             if (!std::isfinite(hs[S_RR])) { set_error("PCG residual is not finite"); return SVL_ERR_NONFINITE; }
             if (hs[S_RR] <= tol2) {
-                // confirm with the true residual, replace the recursive one if it drifted
+                // confirm with the true residual; restart from it if the recursive one drifted
                 TRY(nm_apply(nm, nm->x, nm->q));
                 k_pcg_reset<<<g, tb, 0, cd->stream>>>(nm->b, nm->q, nm->dinv, nm->r, nm->z, nm->p, n);
-                nm_dot(nm, nm->r, nm->r, S_RR);
-                nm_dot(nm, nm->r, nm->z, S_RZ);
+                nm_dot2(nm, nm->r, nm->r, S_RR, nm->r, nm->z, S_RZ);
                 cd->launches += 1;
-                CUDA_TRY(cudaMemcpyAsync(hs, nm->sc, sizeof(hs), cudaMemcpyDeviceToHost, cd->stream));
-                CUDA_TRY(cudaStreamSynchronize(cd->stream));
+                TRY(nm_scalars(nm, hs));
                 nm->res_last = std::sqrt(hs[S_RR] / bb);
-                if (hs[S_RR] <= tol2) { nm->iters_total += it; return SVL_OK; }
+                if (hs[S_RR] <= tol2) {
+                    if (!warm) nm->jac_ref = it;
+                    return SVL_OK;
+                }
             }
         }
     }
-    nm->iters_total += nm->iters_last;
-    CUDA_TRY(cudaMemcpyAsync(hs, nm->sc, sizeof(hs), cudaMemcpyDeviceToHost, cd->stream));
-    CUDA_TRY(cudaStreamSynchronize(cd->stream));
+    TRY(nm_scalars(nm, hs));
     nm->res_last = std::sqrt(hs[S_RR] / bb);
-    set_error("PCG did not reach %g in %d iterations (relative residual %g)", nm->opts.pcg_tol, nm->opts.pcg_maxit, nm->res_last);
+    set_error("PCG did not reach %g in %lld iterations (relative residual %g)", nm->opts.pcg_tol, (long long)maxit, nm->res_last);
     return SVL_ERR_MAXITER;
 }
+
+// Flexible CG with the learned preconditioner; falls back to Jacobi-PCG
+// (continuing from the current iterate) once it has used as many iterations
+// as the last plain Jacobi solve needed.
+static int nm_solve_learned(svl_nm* nm) {
+    svl_cd* cd = nm->cd;
+    const int n = nm->nf, tb = 256, g = (n + tb - 1) / tb;
+    double hs[S_NSCAL];
+    const size_t bytes = sizeof(double) * n;
+    CUDA_TRY(cudaMemsetAsync(nm->x, 0, bytes, cd->stream));
+    CUDA_TRY(cudaMemcpyAsync(nm->r, nm->b, bytes, cudaMemcpyDeviceToDevice, cd->stream));
+    nm_dot(nm, nm->b, nm->b, S_BB);
+    TRY(svl::nn_apply(nm->nn, nm->r, nm->z));
+    CUDA_TRY(cudaMemcpyAsync(nm->p, nm->z, bytes, cudaMemcpyDeviceToDevice, cd->stream));
+    cd->launches += 7;
+    TRY(nm_scalars(nm, hs));
+    const double bb = hs[S_BB];
+    nm->learned_solves++;
+    if (bb == 0.0) { nm->res_last = 0.0; return SVL_OK; }
+    const double tol2 = nm->opts.pcg_tol * nm->opts.pcg_tol * bb;
+    const int64_t budget = std::min<int64_t>(nm->opts.pcg_maxit, nm->jac_ref > 0 ? nm->jac_ref : nm->opts.pcg_maxit);
+    const int check = 4;
+    bool cold = false;
+    for (int64_t it = 1; it <= budget; ++it) {
+        TRY(nm_apply(nm, nm->p, nm->q));
+        nm_dot2(nm, nm->p, nm->q, S_PQ, nm->r, nm->p, S_RP);
+        k_fcg_xr<<<g, tb, 0, cd->stream>>>(nm->sc, nm->p, nm->q, nm->x, nm->r, n);
+        TRY(svl::nn_apply(nm->nn, nm->r, nm->z));
+        nm_dot2(nm, nm->z, nm->q, S_ZQ, nm->r, nm->r, S_RR);
+        k_fcg_p<<<g, tb, 0, cd->stream>>>(nm->sc, nm->z, nm->p, n);
+        cd->launches += 2 + 7;
+        nm->iters_last++;
+        nm->iters_total++;
+        if (it % check == 0 || it == budget) {
+            TRY(nm_scalars(nm, hs));
+            if (!(hs[S_PQ] > 0.0) || !std::isfinite(hs[S_RR]) || !std::isfinite(hs[S_PQ])) {
+                cold = !std::isfinite(hs[S_RR]) || !std::isfinite(hs[S_PQ]);    // the iterate may be spoiled
+                break;
+            }
+            if (hs[S_RR] <= tol2) {
+                TRY(nm_apply(nm, nm->x, nm->q));
+                k_pcg_reset<<<g, tb, 0, cd->stream>>>(nm->b, nm->q, nm->dinv, nm->r, nm->z, nm->p, n);
+                nm_dot(nm, nm->r, nm->r, S_RR);
+                cd->launches += 1;
+                TRY(nm_scalars(nm, hs));
+                nm->res_last = std::sqrt(hs[S_RR] / bb);
+                if (hs[S_RR] <= tol2) return SVL_OK;
+                // drifted: restart the flexible iteration from the true residual
+                TRY(svl::nn_apply(nm->nn, nm->r, nm->z));
+                CUDA_TRY(cudaMemcpyAsync(nm->p, nm->z, bytes, cudaMemcpyDeviceToDevice, cd->stream));
+            }
+        }
+    }
+    nm->fallbacks++;
+    return nm_solve_jacobi(nm, !cold, std::max<int64_t>(1, nm->opts.pcg_maxit - nm->iters_last));
+}
+
+static int nm_solve(svl_nm* nm) {
+    nm->iters_last = 0;
+    nm->res_last = 0.0;
+    if (nm->precond == SVL_PRECOND_LEARNED && nm->nn && nm->rec_every == 0) return nm_solve_learned(nm);
+    return nm_solve_jacobi(nm, false, nm->opts.pcg_maxit);
+}
+
+// training pairs from the CG iterates recorded during the last solve: e_hat =
+// D^1/2 (x* - x_k), r_hat = D^-1/2 r_k, normalised by |e_hat|
+static int nm_pairs_from_iterates(svl_nm* nm) {
+    svl_cd* cd = nm->cd;
+    const int n = nm->nf, tb = 256, g = (n + tb - 1) / tb;
+    double hs[S_NSCAL];
+    for (int j = 0; j < nm->rec_n; ++j) {
+        k_ehat<<<g, tb, 0, cd->stream>>>(nm->x, nm->rec_x[j], nm->sdinv, nm->e1, n);
+        k_vmul<<<g, tb, 0, cd->stream>>>(nm->rec_r[j], nm->sdinv, nm->e2, n);
+        nm_dot(nm, nm->e1, nm->e1, S_RP);
+        TRY(nm_scalars(nm, hs));
+        if (hs[S_RP] > 0.0 && std::isfinite(hs[S_RP])) TRY(svl::nn_record_pair(nm->nn, nm->e2, nm->e1, 1.0 / std::sqrt(hs[S_RP])));
+    }
+    nm->rec_n = 0;
+    return SVL_OK;
+}
+
+// Node lattice of a 3D hexahedral model: distinct x, y, z coordinate values
+// whose product is the node count, each node on its own lattice point.
+static bool detect_lattice(const HostModel& m, int dims[3], std::vector<int32_t>& cell) {
+    if (m.ndim != 3 || m.nen != 8 || m.nnode == 0) return false;
+    int nd[3];
+    std::vector<std::vector<double>> vals(3);
+    for (int a = 0; a < 3; ++a) {
+        std::vector<double> v(m.nnode);
+        double lo = 1e300, hi = -1e300;
+        for (int n = 0; n < m.nnode; ++n) { v[n] = m.X[(size_t)n * 3 + a]; lo = std::min(lo, v[n]); hi = std::max(hi, v[n]); }
+        std::sort(v.begin(), v.end());
+        const double tol = 1e-9 * std::max(1.0, hi - lo);
+        std::vector<double> u;
+        for (double x : v) if (u.empty() || x - u.back() > tol) u.push_back(x);
+        vals[a] = u;
+        nd[a] = (int)u.size();
+    }
+    if ((int64_t)nd[0] * nd[1] * nd[2] != m.nnode) return false;
+    cell.assign(m.nnode, -1);
+    std::vector<char> used((size_t)m.nnode, 0);
+    for (int n = 0; n < m.nnode; ++n) {
+        int ijk[3];
+        for (int a = 0; a < 3; ++a) {
+            const auto& u = vals[a];
+            const double x = m.X[(size_t)n * 3 + a];
+            size_t k = std::lower_bound(u.begin(), u.end(), x) - u.begin();
+            if (k == u.size() || (k > 0 && std::fabs(u[k - 1] - x) < std::fabs(u[k] - x))) k = k == 0 ? 0 : k - 1;
+            ijk[a] = (int)k;
+        }
+        const int c = ijk[0] + nd[0] * (ijk[1] + nd[1] * ijk[2]);
+        if (used[c]) return false;
+        used[c] = 1;
+        cell[n] = c;
+    }
+    dims[0] = nd[0]; dims[1] = nd[1]; dims[2] = nd[2];
+    return true;
+}
+
+static int nm_step(svl_nm* nm, double* U_hist_row);
 
 extern "C" {
 
@@ -1148,6 +1396,7 @@ int svl_nm_create(const svl_model_desc* model, const svl_load_desc* loads, const
     if (!out || !opts) { set_error("NULL argument"); return SVL_ERR_INVALID; }
     *out = nullptr;
     if (!(opts->dt > 0.0) || !(opts->pcg_tol > 0.0) || opts->pcg_maxit <= 0) { set_error("bad Newmark options"); return SVL_ERR_INVALID; }
+    if (opts->precond != SVL_PRECOND_JACOBI && opts->precond != SVL_PRECOND_LEARNED) { set_error("unknown preconditioner %d", opts->precond); return SVL_ERR_INVALID; }
     svl_cd_opts co{};
     co.dt = opts->dt; co.ftol = opts->ftol; co.mtol = opts->mtol; co.precision = SVL_PREC_FP64; co.check_every = 0;
     svl_cd* cd = nullptr;
@@ -1168,8 +1417,7 @@ int svl_nm_create(const svl_model_desc* model, const svl_load_desc* loads, const
     for (int e = 0; e < m.nelem; ++e) {
         const double* pr = m.param(e);
         const double E = pr[0], nu = pr[1];
-        const double c1 = E * (1.0 - nu) / (1.0 - 2.0 * nu) / (1.0 + nu), c2 = E * nu / (1.0 - 2.0 * nu) / (1.0 + nu),
-                     c3 = E / (2.0 * (1.0 + nu));
+        const double c1 = E * (1.0 - nu) / (1.0 - 2.0 * nu) / (1.0 + nu), c3 = E / (2.0 * (1.0 + nu));
         std::vector<double> kd(nc, 0.0);
         for (int q = 0; q < m.ngp; ++q) {
             double dNx[8][3], N[8];
@@ -1186,7 +1434,6 @@ int svl_nm_create(const svl_model_desc* model, const svl_load_desc* loads, const
                 }
             }
         }
-        (void)c2;
         for (int a = 0; a < m.nen; ++a)
             for (int c = 0; c < m.ndof; ++c) Kd[m.tdof[(size_t)m.conn[(size_t)e * m.nen + a] * m.ndof + c]] += kd[a * m.ndof + c];
     }
@@ -1201,12 +1448,43 @@ int svl_nm_create(const svl_model_desc* model, const svl_load_desc* loads, const
         }
     double** vecs[] = {&nm->b, &nm->x, &nm->r, &nm->z, &nm->p, &nm->q};
     for (double** pv : vecs) if ((st = cd->zeros((size_t)std::max(m.nfree, 1), pv))) return fail(st);
-    if ((st = cd->zeros((size_t)m.ntotal, &nm->pt)) || (st = cd->zeros(kDotBlocks, &nm->partial)) ||
+    if ((st = cd->zeros((size_t)m.ntotal, &nm->pt)) || (st = cd->zeros(2 * kDotBlocks, &nm->partial)) ||
         (st = cd->zeros(S_NSCAL, &nm->sc)))
         return fail(st);
     const double* dd = nullptr;
     if ((st = cd->upload(dinv, &dd))) return fail(st);
     nm->dinv = const_cast<double*>(dd);
+    // lattice models: the maps and scalings of the learned preconditioner
+    int dims[3];
+    std::vector<int32_t> cell;
+    if (m.nfree > 0 && detect_lattice(m, dims, cell)) {
+        nm->lattice = true;
+        nm->lnx = dims[0]; nm->lny = dims[1]; nm->lnz = dims[2];
+        const int64_t V = (int64_t)dims[0] * dims[1] * dims[2];
+        nm->gmap.assign(m.nfree, 0);
+        nm->sdinv_h.assign(m.nfree, 0.0);
+        nm->rho_h.assign(m.nfree, 0.0);
+        for (int n = 0; n < m.nnode; ++n)
+            for (int c = 0; c < 3; ++c) {
+                const int t = m.tdof[(size_t)n * 3 + c], f = m.fdof[(size_t)n * 3 + c];
+                if (f < 0) continue;
+                nm->gmap[f] = (int32_t)(c * V + cell[n]);
+                nm->sdinv_h[f] = std::sqrt(dinv[f]);
+                nm->rho_h[f] = c_m * M[t] * dinv[f];
+            }
+        const double* sd = nullptr;
+        if ((st = cd->upload(nm->sdinv_h, &sd)) || (st = cd->zeros((size_t)m.nfree, &nm->e1)) ||
+            (st = cd->zeros((size_t)m.nfree, &nm->e2)))
+            return fail(st);
+        nm->sdinv = const_cast<double*>(sd);
+        if (opts->precond == SVL_PRECOND_LEARNED) {
+            if ((st = svl::nn_create(nm->lnx, nm->lny, nm->lnz, nm->gmap, nm->sdinv_h, nm->rho_h, cd->stream, &nm->nn))) return fail(st);
+            nm->precond = SVL_PRECOND_LEARNED;
+        }
+    } else if (opts->precond == SVL_PRECOND_LEARNED) {
+        set_error("the learned preconditioner needs a hexahedral model whose nodes form a lattice");
+        return fail(SVL_ERR_UNSUPPORTED);
+    }
     if (cudaStreamSynchronize(cd->stream) != cudaSuccess) { set_error("upload failed"); return fail(SVL_ERR_CUDA); }
     *out = nm;
     return SVL_OK;
@@ -1220,31 +1498,42 @@ int svl_nm_set_initial(svl_nm* nm, const double* U0, const double* V0, const dou
     return SVL_OK;
 }
 
+}  // extern "C"
+
+// one step: effective force, solve, state update (d.step already advanced)
+static int nm_step(svl_nm* nm, double* U_hist_row) {
+    svl_cd* cd = nm->cd;
+    const HostModel& m = cd->m;
+    const double dt = nm->opts.dt;
+    const int tb = 256, ng = (m.nnode + tb - 1) / tb, eg = (m.nelem + 127) / 128;
+    k_step_inc<<<1, 1, 0, cd->stream>>>(cd->d.step);
+    // internal force from the committed state (filtered like the assembler)
+    if (m.ndim == 2) k_element<2, 4><<<eg, 128, 0, cd->stream>>>(cd->d, cd->d.Us, m.ngp, 0);
+    else k_element<3, 8><<<eg, 128, 0, cd->stream>>>(cd->d, cd->d.Us, m.ngp, 0);
+    if (m.ndim == 2) k_nm_rhs<2><<<ng, tb, 0, cd->stream>>>(cd->d, nm->b, 4.0 / dt);
+    else k_nm_rhs<3><<<ng, tb, 0, cd->stream>>>(cd->d, nm->b, 4.0 / dt);
+    cd->launches += 3;
+    CUDA_TRY(cudaGetLastError());
+    TRY(nm_solve(nm));
+    if (nm->rec_n > 0) TRY(nm_pairs_from_iterates(nm));
+    if (m.ndim == 2) k_nm_update<2><<<ng, tb, 0, cd->stream>>>(cd->d, nm->x, 4.0 / dt / dt, 4.0 / dt, 2.0 / dt, cd->d.flag);
+    else k_nm_update<3><<<ng, tb, 0, cd->stream>>>(cd->d, nm->x, 4.0 / dt / dt, 4.0 / dt, 2.0 / dt, cd->d.flag);
+    cd->launches += 1;
+    CUDA_TRY(cudaGetLastError());
+    if (U_hist_row) CUDA_TRY(cudaMemcpyAsync(U_hist_row, cd->d.U, sizeof(double) * m.ntotal, cudaMemcpyDeviceToHost, cd->stream));
+    return SVL_OK;
+}
+
+extern "C" {
+
 int svl_nm_run(svl_nm* nm, int32_t k_first, int32_t nsteps, double* U_hist) {
     if (!nm || nsteps < 0) { set_error("bad argument"); return SVL_ERR_INVALID; }
     svl_cd* cd = nm->cd;
     const HostModel& m = cd->m;
     const int64_t l0 = cd->launches;
-    const double dt = nm->opts.dt;
     int kstart = k_first - 1;
     CUDA_TRY(cudaMemcpyAsync(cd->d.step, &kstart, sizeof(int), cudaMemcpyHostToDevice, cd->stream));
-    const int tb = 256, ng = (m.nnode + tb - 1) / tb, eg = (m.nelem + 127) / 128;
-    for (int s = 0; s < nsteps; ++s) {
-        k_step_inc<<<1, 1, 0, cd->stream>>>(cd->d.step);
-        // internal force from the committed state (filtered like the assembler)
-        if (m.ndim == 2) k_element<2, 4><<<eg, 128, 0, cd->stream>>>(cd->d, cd->d.Us, m.ngp, 0);
-        else k_element<3, 8><<<eg, 128, 0, cd->stream>>>(cd->d, cd->d.Us, m.ngp, 0);
-        if (m.ndim == 2) k_nm_rhs<2><<<ng, tb, 0, cd->stream>>>(cd->d, nm->b, 4.0 / dt);
-        else k_nm_rhs<3><<<ng, tb, 0, cd->stream>>>(cd->d, nm->b, 4.0 / dt);
-        cd->launches += 3;
-        CUDA_TRY(cudaGetLastError());
-        TRY(nm_solve(nm));
-        if (m.ndim == 2) k_nm_update<2><<<ng, tb, 0, cd->stream>>>(cd->d, nm->x, 4.0 / dt / dt, 4.0 / dt, 2.0 / dt, cd->d.flag);
-        else k_nm_update<3><<<ng, tb, 0, cd->stream>>>(cd->d, nm->x, 4.0 / dt / dt, 4.0 / dt, 2.0 / dt, cd->d.flag);
-        cd->launches += 1;
-        CUDA_TRY(cudaGetLastError());
-        if (U_hist) CUDA_TRY(cudaMemcpyAsync(U_hist + (size_t)s * m.ntotal, cd->d.U, sizeof(double) * m.ntotal, cudaMemcpyDeviceToHost, cd->stream));
-    }
+    for (int s = 0; s < nsteps; ++s) TRY(nm_step(nm, U_hist ? U_hist + (size_t)s * m.ntotal : nullptr));
     cd->launches_last = cd->launches - l0;
     int flag = 0;
     CUDA_TRY(cudaMemcpyAsync(&flag, cd->d.flag, sizeof(int), cudaMemcpyDeviceToHost, cd->stream));
@@ -1268,6 +1557,109 @@ int svl_nm_run_timed(svl_nm* nm, int32_t k_first, int32_t nsteps, float* ms) {
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     return st;
+}
+
+int svl_nm_train_preconditioner(svl_nm* nm, int32_t k_first, const svl_nn_train_opts* o, float* loss) {
+    if (!nm || !o) { set_error("NULL argument"); return SVL_ERR_INVALID; }
+    if (!nm->lattice) { set_error("the learned preconditioner needs a hexahedral model whose nodes form a lattice"); return SVL_ERR_UNSUPPORTED; }
+    if (o->solve_steps < 0 || o->n_synthetic < 0 || o->iters <= 0 || o->batch <= 0 || !(o->lr > 0.f) ||
+        (o->solve_steps > 0 && o->record_every <= 0)) {
+        set_error("bad training options");
+        return SVL_ERR_INVALID;
+    }
+    svl_cd* cd = nm->cd;
+    if (!nm->nn) TRY(svl::nn_create(nm->lnx, nm->lny, nm->lnz, nm->gmap, nm->sdinv_h, nm->rho_h, cd->stream, &nm->nn));
+    // 1. Newmark steps with Jacobi-PCG, recording CG iterates
+    if (o->solve_steps > 0) {
+        while ((int)nm->rec_x.size() < kRecMax) {
+            double *xa = nullptr, *ra = nullptr;
+            TRY(cd->zeros((size_t)nm->nf, &xa));
+            TRY(cd->zeros((size_t)nm->nf, &ra));
+            nm->rec_x.push_back(xa);
+            nm->rec_r.push_back(ra);
+        }
+        nm->rec_every = o->record_every;
+        nm->rec_n = 0;
+        const int st = svl_nm_run(nm, k_first, o->solve_steps, nullptr);
+        nm->rec_every = 0;
+        nm->rec_n = 0;
+        if (st) return st;
+    }
+    // 2. synthetic pairs: e random with 0..5 smoothing sweeps, r_hat = A_hat e
+    const int n = nm->nf, tb = 256, g = (n + tb - 1) / tb;
+    double hs[S_NSCAL];
+    for (int i = 0; i < o->n_synthetic; ++i) {
+        k_randn<<<g, tb, 0, cd->stream>>>(nm->e1, n, o->seed * 0x9E3779B97F4A7C15ull + (uint64_t)i * 0x100000001B3ull);
+        for (int sweep = 0; sweep < i % 6; ++sweep) {
+            k_vmul<<<g, tb, 0, cd->stream>>>(nm->e1, nm->sdinv, nm->e2, n);
+            TRY(nm_apply(nm, nm->e2, nm->q));
+            k_smooth<<<g, tb, 0, cd->stream>>>(nm->e1, nm->q, nm->sdinv, 0.5, n);
+        }
+        k_vmul<<<g, tb, 0, cd->stream>>>(nm->e1, nm->sdinv, nm->e2, n);
+        TRY(nm_apply(nm, nm->e2, nm->q));
+        k_vmul<<<g, tb, 0, cd->stream>>>(nm->q, nm->sdinv, nm->e2, n);
+        nm_dot(nm, nm->e1, nm->e1, S_RP);
+        TRY(nm_scalars(nm, hs));
+        TRY(svl::nn_record_pair(nm->nn, nm->e2, nm->e1, 1.0 / std::sqrt(hs[S_RP])));
+    }
+    CUDA_TRY(cudaGetLastError());
+    // 3. Adam
+    float l = 0.f;
+    TRY(svl::nn_train(nm->nn, o->iters, o->batch, o->lr, o->seed, &l));
+    if (loss) *loss = l;
+    nm->precond = SVL_PRECOND_LEARNED;
+    return SVL_OK;
+}
+
+int svl_nm_set_preconditioner(svl_nm* nm, int32_t precond) {
+    if (!nm) { set_error("NULL handle"); return SVL_ERR_INVALID; }
+    if (precond == SVL_PRECOND_JACOBI) { nm->precond = precond; return SVL_OK; }
+    if (precond != SVL_PRECOND_LEARNED) { set_error("unknown preconditioner %d", precond); return SVL_ERR_INVALID; }
+    if (!nm->lattice) { set_error("the learned preconditioner needs a hexahedral model whose nodes form a lattice"); return SVL_ERR_UNSUPPORTED; }
+    if (!nm->nn) TRY(svl::nn_create(nm->lnx, nm->lny, nm->lnz, nm->gmap, nm->sdinv_h, nm->rho_h, nm->cd->stream, &nm->nn));
+    nm->precond = precond;
+    return SVL_OK;
+}
+
+int svl_nn_num_weights(void) { return svl::kNnWeights; }
+
+int svl_nm_preconditioner_weights(svl_nm* nm, float* w_out, const float* w_in) {
+    if (!nm) { set_error("NULL handle"); return SVL_ERR_INVALID; }
+    if (!nm->lattice) { set_error("no learned preconditioner on this model"); return SVL_ERR_UNSUPPORTED; }
+    if (!nm->nn) TRY(svl::nn_create(nm->lnx, nm->lny, nm->lnz, nm->gmap, nm->sdinv_h, nm->rho_h, nm->cd->stream, &nm->nn));
+    if (w_in) TRY(svl::nn_set_weights(nm->nn, w_in));
+    if (w_out) TRY(svl::nn_get_weights(nm->nn, w_out));
+    return SVL_OK;
+}
+
+int svl_nm_precond_stats(svl_nm* nm, int64_t* learned_solves, int64_t* fallbacks, int64_t* jacobi_ref_iters) {
+    if (!nm) { set_error("NULL handle"); return SVL_ERR_INVALID; }
+    if (learned_solves) *learned_solves = nm->learned_solves;
+    if (fallbacks) *fallbacks = nm->fallbacks;
+    if (jacobi_ref_iters) *jacobi_ref_iters = nm->jac_ref;
+    return SVL_OK;
+}
+
+int svl_nm_lattice(svl_nm* nm, int32_t* dims) {
+    if (!nm || !dims) { set_error("NULL argument"); return SVL_ERR_INVALID; }
+    dims[0] = nm->lattice ? nm->lnx : 0;
+    dims[1] = nm->lattice ? nm->lny : 0;
+    dims[2] = nm->lattice ? nm->lnz : 0;
+    return SVL_OK;
+}
+
+int svl_nm_nn_loss_grad(svl_nm* nm, const float* x, const float* t, float* loss, float* grad) {
+    if (!nm || !x || !t || !loss || !grad) { set_error("NULL argument"); return SVL_ERR_INVALID; }
+    if (!nm->lattice) { set_error("no learned preconditioner on this model"); return SVL_ERR_UNSUPPORTED; }
+    if (!nm->nn) TRY(svl::nn_create(nm->lnx, nm->lny, nm->lnz, nm->gmap, nm->sdinv_h, nm->rho_h, nm->cd->stream, &nm->nn));
+    return svl::nn_loss_grad_host(nm->nn, x, t, loss, grad);
+}
+
+int svl_nm_nn_grids(svl_nm* nm, float* rho, float* mask) {
+    if (!nm) { set_error("NULL handle"); return SVL_ERR_INVALID; }
+    if (!nm->lattice) { set_error("no learned preconditioner on this model"); return SVL_ERR_UNSUPPORTED; }
+    if (!nm->nn) TRY(svl::nn_create(nm->lnx, nm->lny, nm->lnz, nm->gmap, nm->sdinv_h, nm->rho_h, nm->cd->stream, &nm->nn));
+    return svl::nn_get_grids(nm->nn, rho, mask);
 }
 
 int svl_nm_get(svl_nm* nm, int32_t which, double* out) {

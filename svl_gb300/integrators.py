@@ -171,13 +171,13 @@ class NewmarkBeta:
     (RP/11-Solvers/02-Iterative/PetscSolver.cc, KSPCG, rtol `pcg_tol`)."""
 
     def __init__(self, model: Model, loads: Loads | None, dt: float, pcg_tol: float = 1e-8,
-                 pcg_maxit: int = 20000, ftol: float = 1e-12, mtol: float = 1e-12):
+                 pcg_maxit: int = 20000, ftol: float = 1e-12, mtol: float = 1e-12, precond: int = 0):
         self.model = model
         self.dt = float(dt)
         self._md = model.desc()
         self._ld = (loads or Loads()).desc()
         opts = capi.NmOpts(dt=self.dt, ftol=ftol, mtol=mtol, pcg_tol=float(pcg_tol), pcg_maxit=int(pcg_maxit),
-                           precond=capi.SVL_PRECOND_JACOBI)
+                           precond=int(precond))
         h = C.c_void_p()
         check(lib().svl_nm_create(C.byref(self._md), C.byref(self._ld), C.byref(opts), C.byref(h)))
         self._h = h
@@ -209,6 +209,57 @@ class NewmarkBeta:
         ms = C.c_float()
         check(lib().svl_nm_run_timed(self._h, int(k_first), int(nsteps), C.byref(ms)))
         return float(ms.value)
+
+    # -- learned preconditioner (lattice models) ---------------------------
+    def train_preconditioner(self, k_first: int, solve_steps: int = 20, record_every: int = 4,
+                             n_synthetic: int = 300, iters: int = 1500, batch: int = 4, lr: float = 2e-3,
+                             seed: int = 0) -> float:
+        """Advance solve_steps steps with Jacobi-PCG recording CG iterates, add
+        synthetic pairs, train the network, switch to the learned preconditioner.
+        Returns the final training loss (mean relative squared error)."""
+        o = capi.NnTrainOpts(solve_steps=solve_steps, record_every=record_every, n_synthetic=n_synthetic,
+                             iters=iters, batch=batch, lr=lr, seed=seed)
+        loss = C.c_float()
+        check(lib().svl_nm_train_preconditioner(self._h, int(k_first), C.byref(o), C.byref(loss)))
+        return float(loss.value)
+
+    def set_preconditioner(self, precond: int):
+        check(lib().svl_nm_set_preconditioner(self._h, int(precond)))
+
+    def nn_weights(self, new=None) -> np.ndarray:
+        n = lib().svl_nn_num_weights()
+        out = np.zeros(n, np.float32)
+        w_in = None if new is None else np.ascontiguousarray(new, dtype=np.float32)
+        check(lib().svl_nm_preconditioner_weights(self._h, ptr(out, C.c_float), ptr(w_in, C.c_float)))
+        return out
+
+    def precond_stats(self):
+        """(solves with the learned preconditioner, fallbacks to Jacobi, last Jacobi iteration count)."""
+        a, b, c = C.c_int64(), C.c_int64(), C.c_int64()
+        check(lib().svl_nm_precond_stats(self._h, C.byref(a), C.byref(b), C.byref(c)))
+        return int(a.value), int(b.value), int(c.value)
+
+    def lattice(self):
+        d = np.zeros(3, np.int32)
+        check(lib().svl_nm_lattice(self._h, ptr(d, C.c_int32)))
+        return tuple(int(v) for v in d)
+
+    def nn_loss_grad(self, x, t):
+        """Device loss and weight gradient of one sample (grids [3][nz][ny][nx])."""
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        t = np.ascontiguousarray(t, dtype=np.float32)
+        loss = np.zeros(1, np.float32)
+        grad = np.zeros(lib().svl_nn_num_weights(), np.float32)
+        check(lib().svl_nm_nn_loss_grad(self._h, ptr(x, C.c_float), ptr(t, C.c_float), ptr(loss, C.c_float),
+                                        ptr(grad, C.c_float)))
+        return float(loss[0]), grad
+
+    def nn_grids(self):
+        nx, ny, nz = self.lattice()
+        rho = np.zeros((3, nz, ny, nx), np.float32)
+        mask = np.zeros((3, nz, ny, nx), np.float32)
+        check(lib().svl_nm_nn_grids(self._h, ptr(rho, C.c_float), ptr(mask, C.c_float)))
+        return rho, mask
 
     def stats(self):
         """(CG iterations over all solves, of the last solve, last true relative residual)."""
