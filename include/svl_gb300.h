@@ -339,6 +339,14 @@ int  svl_nm_lattice(svl_nm* nm, int32_t* dims);
 /* Test hook: loss sum and weight gradient of one sample on the device.  x, t:
  * host grids [3][nz][ny][nx] of r_hat and e_hat; grad: svl_nn_num_weights(). */
 int  svl_nm_nn_loss_grad(svl_nm* nm, const float* x, const float* t, float* loss, float* grad);
+/* Network output y for a host r_hat grid x (both [3][nz][ny][nx]) through the
+ * FP32 CUDA-core kernels (path 0) or the BF16 tensor-core kernels (path 1).
+ * Test hook. */
+int  svl_nm_nn_forward(svl_nm* nm, const float* x, float* y, int32_t path);
+/* Inference path of the learned preconditioner inside the solve: 1 = BF16
+ * tensor cores (tcgen05, the default), 0 = FP32 CUDA cores (the training
+ * kernels). */
+int  svl_nm_nn_set_path(svl_nm* nm, int32_t path);
 /* Test hook: the rho feature grid and the free-dof mask grid, [3][nz][ny][nx]. */
 int  svl_nm_nn_grids(svl_nm* nm, float* rho, float* mask);
 

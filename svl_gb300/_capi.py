@@ -159,6 +159,8 @@ def lib():
     L.svl_nm_lattice.argtypes = [C.c_void_p, i32p]
     L.svl_nm_nn_loss_grad.argtypes = [C.c_void_p, f32p, f32p, f32p, f32p]
     L.svl_nm_nn_grids.argtypes = [C.c_void_p, f32p, f32p]
+    L.svl_nm_nn_forward.argtypes = [C.c_void_p, f32p, f32p, C.c_int32]
+    L.svl_nm_nn_set_path.argtypes = [C.c_void_p, C.c_int32]
     L.svl_nm_destroy.argtypes = [C.c_void_p]
     L.svl_nm_destroy.restype = None
     _lib = L

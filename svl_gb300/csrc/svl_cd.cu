@@ -1315,7 +1315,7 @@ static int nm_solve_learned(svl_nm* nm) {
                 cd->launches += 1;
                 TRY(nm_scalars(nm, hs));
                 nm->res_last = std::sqrt(hs[S_RR] / bb);
-                if (hs[S_RR] <= tol2) return SVL_OK;
+                if (hs[S_RR] <= tol2) return svl::nn_status(nm->nn);
                 // drifted: restart the flexible iteration from the true residual
                 TRY(svl::nn_apply(nm->nn, nm->r, nm->z));
                 CUDA_TRY(cudaMemcpyAsync(nm->p, nm->z, bytes, cudaMemcpyDeviceToDevice, cd->stream));
@@ -1494,7 +1494,8 @@ int svl_nm_set_initial(svl_nm* nm, const double* U0, const double* V0, const dou
     if (!nm) { set_error("NULL handle"); return SVL_ERR_INVALID; }
     TRY(svl_cd_set_initial(nm->cd, U0, V0, A0));
     // strain displacement = U0 for an elastic start from given displacements
-    if (U0) CUDA_TRY(cudaMemcpy(nm->cd->d.Us, nm->cd->d.U, sizeof(double) * nm->cd->m.ntotal, cudaMemcpyDeviceToDevice));
+    if (U0) CUDA_TRY(cudaMemcpyAsync(nm->cd->d.Us, nm->cd->d.U, sizeof(double) * nm->cd->m.ntotal, cudaMemcpyDeviceToDevice, nm->cd->stream));
+    CUDA_TRY(cudaStreamSynchronize(nm->cd->stream));
     return SVL_OK;
 }
 
@@ -1653,6 +1654,22 @@ int svl_nm_nn_loss_grad(svl_nm* nm, const float* x, const float* t, float* loss,
     if (!nm->lattice) { set_error("no learned preconditioner on this model"); return SVL_ERR_UNSUPPORTED; }
     if (!nm->nn) TRY(svl::nn_create(nm->lnx, nm->lny, nm->lnz, nm->gmap, nm->sdinv_h, nm->rho_h, nm->cd->stream, &nm->nn));
     return svl::nn_loss_grad_host(nm->nn, x, t, loss, grad);
+}
+
+int svl_nm_nn_forward(svl_nm* nm, const float* x, float* y, int32_t path) {
+    if (!nm || !x || !y) { set_error("NULL argument"); return SVL_ERR_INVALID; }
+    if (!nm->lattice) { set_error("no learned preconditioner on this model"); return SVL_ERR_UNSUPPORTED; }
+    if (!nm->nn) TRY(svl::nn_create(nm->lnx, nm->lny, nm->lnz, nm->gmap, nm->sdinv_h, nm->rho_h, nm->cd->stream, &nm->nn));
+    return svl::nn_forward_host(nm->nn, x, y, path);
+}
+
+int svl_nm_nn_set_path(svl_nm* nm, int32_t path) {
+    if (!nm) { set_error("NULL handle"); return SVL_ERR_INVALID; }
+    if (path != 0 && path != 1) { set_error("path must be 0 (CUDA cores) or 1 (tensor cores)"); return SVL_ERR_INVALID; }
+    if (!nm->lattice) { set_error("no learned preconditioner on this model"); return SVL_ERR_UNSUPPORTED; }
+    if (!nm->nn) TRY(svl::nn_create(nm->lnx, nm->lny, nm->lnz, nm->gmap, nm->sdinv_h, nm->rho_h, nm->cd->stream, &nm->nn));
+    svl::nn_set_path(nm->nn, path);
+    return SVL_OK;
 }
 
 int svl_nm_nn_grids(svl_nm* nm, float* rho, float* mask) {

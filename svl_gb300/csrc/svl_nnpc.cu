@@ -9,6 +9,8 @@
 #include <cstring>
 #include <vector>
 
+#include <cuda_bf16.h>
+
 #include "svl_internal.hpp"
 #include "svl_nnpc.hpp"
 
@@ -212,6 +214,205 @@ __global__ void k_adam(float* __restrict__ W, const float* __restrict__ G, float
     W[i] -= lr_t * mi / (sqrtf(vi) + eps);
 }
 
+
+// ---------------------------------------------------------------------------
+// Tensor-core inference path (tcgen05.mma.kind::f16, BF16 operands, FP32
+// accumulation in TMEM).  Activations are channel-last BF16 grids [V][16].
+// One CTA computes a tile of 8 (x) x 16 (y) x TCZ (z) voxels: the haloed
+// block (10 x 18 x (TCZ+2) voxels) is staged in shared memory in the
+// no-swizzle K-major canonical layout, channel group g (8 channels = 16 B)
+// at g * TC_LBO, voxel (x, y, z) at z * TC_SZ + y * TC_SY + x * 16.  The
+// A operand of z-plane p and tap (dx, dy, dz) is then that block read from
+// (p + 1 + dz, 1 + dy, 1 + dx) with row stride TC_SY between 8-row groups:
+// each tap is one descriptor offset, no data movement.  27 MMAs of
+// M128 x N16 x K16 accumulate one plane in 16 TMEM columns.
+constexpr int TCX = 8, TCY = 16, TCZ = 8;
+constexpr int TC_HX = TCX + 2, TC_HY = TCY + 2, TC_HZ = TCZ + 2;
+constexpr int TC_SY = TC_HX * 16;                 // 160 B
+constexpr int TC_SZ = TC_HY * TC_SY;              // 2880 B
+constexpr int TC_LBO = TC_HZ * TC_SZ;             // 28800 B: second channel group
+constexpr int TC_A_BYTES = 2 * TC_LBO;
+constexpr int TC_TAP_BYTES = 512;                 // 16 x 16 BF16 B operand per tap
+constexpr int TC_B_BYTES = kNnTaps * TC_TAP_BYTES;
+constexpr int TC_OFF_B = TC_A_BYTES;
+constexpr int TC_OFF_BAR = TC_OFF_B + TC_B_BYTES;
+constexpr int TC_SMEM = TC_OFF_BAR + 16;
+constexpr int TC_THREADS = 128;
+constexpr uint32_t TC_TMEM_COLS = 128;            // TCZ planes x 16 columns
+constexpr long kTcWaitLimit = 4000000;
+static_assert(TC_SY % 16 == 0 && TC_SZ % 16 == 0 && TC_LBO % 16 == 0, "descriptor strides");
+static_assert(TC_OFF_B % 128 == 0 && TC_OFF_BAR % 8 == 0, "alignment");
+static_assert((TC_LBO >> 4) < (1 << 14) && (TC_SY >> 4) < (1 << 14), "descriptor fields");
+static_assert(TCZ * 16 <= (int)TC_TMEM_COLS, "TMEM columns");
+static_assert(TC_SMEM <= 227 * 1024, "shared memory");
+
+// D = F32 (bits 4-5), A = B = BF16 (bits 7-9, 10-12), K-major, N >> 3, M >> 4
+constexpr uint32_t kIdescBf16 = (1u << 4) | (1u << 7) | (1u << 10) | ((16u >> 3) << 17) | ((128u >> 4) << 24);
+
+__device__ __forceinline__ uint32_t tc_smem_u32(const void* p) { return static_cast<uint32_t>(__cvta_generic_to_shared(p)); }
+
+__device__ __forceinline__ uint64_t tc_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)(lbo >> 4) << 16) | ((uint64_t)(sbo >> 4) << 32) | (1ull << 46);
+}
+
+// W fp32 [cout][cin][27] -> per-tap B operand images (N = 16 out rows, K = 16 in
+// channels, K-major core matrices: (n/8)*256 + (k/8)*128 + (n%8)*16 + (k%8)*2).
+__global__ void k_wprep(const float* __restrict__ W, __nv_bfloat16* __restrict__ out, int cin, int cout) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;      // over 27 * 16 * 16
+    if (i >= kNnTaps * 256) return;
+    const int t = i / 256, n = (i / 16) % 16, k = i % 16;
+    const float w = (n < cout && k < cin) ? W[(n * cin + k) * kNnTaps + t] : 0.f;
+    const int off = t * 256 + (n / 8) * 128 + (k / 8) * 64 + (n % 8) * 8 + (k % 8);   // in bf16 units
+    out[off] = __float2bfloat16_rn(w);
+}
+
+// One tile of one layer.  mode 0: relu, BF16 channel-last output; mode 1:
+// linear, FP32 channel-major output of the first 3 channels.
+template <int MODE>
+__global__ void __launch_bounds__(TC_THREADS) k_conv_tc(const __nv_bfloat16* __restrict__ in,
+                                                         const __nv_bfloat16* __restrict__ wimg,
+                                                         __nv_bfloat16* __restrict__ out_bf, float* __restrict__ out_f,
+                                                         Dims d, int ntx, int nty, int* __restrict__ status) {
+    extern __shared__ __align__(128) unsigned char tsm[];
+    const int tid = threadIdx.x, warp = tid >> 5;
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(tsm + TC_OFF_BAR + 8);
+    const uint32_t bar = tc_smem_u32(tsm + TC_OFF_BAR);
+    if (tc_smem_u32(tsm) & 127u) {                        // descriptors assume a 128 B aligned window
+        if (tid == 0) atomicOr(status, 4);
+        return;
+    }
+    const int tile = blockIdx.x;
+    const int x0 = (tile % ntx) * TCX, y0 = ((tile / ntx) % nty) * TCY, z0 = (tile / (ntx * nty)) * TCZ;
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                     :: "r"(tc_smem_u32(tmem_slot)), "r"(TC_TMEM_COLS) : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(bar), "r"(1) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    // B operand images (27 taps)
+    {
+        const uint4* src = reinterpret_cast<const uint4*>(wimg);
+        uint4* dst = reinterpret_cast<uint4*>(tsm + TC_OFF_B);
+        for (int i = tid; i < TC_B_BYTES / 16; i += TC_THREADS) dst[i] = src[i];
+    }
+    // haloed activation block, zero outside the lattice
+    const size_t plane = (size_t)d.nx * d.ny;
+    for (int i = tid; i < 2 * TC_HX * TC_HY * TC_HZ; i += TC_THREADS) {
+        const int g = i & 1, c = i >> 1;
+        const int hx = c % TC_HX, hy = (c / TC_HX) % TC_HY, hz = c / (TC_HX * TC_HY);
+        const int x = x0 + hx - 1, y = y0 + hy - 1, z = z0 + hz - 1;
+        uint4 val = make_uint4(0u, 0u, 0u, 0u);
+        if (x >= 0 && x < d.nx && y >= 0 && y < d.ny && z >= 0 && z < d.nz)
+            val = *reinterpret_cast<const uint4*>(in + ((size_t)z * plane + (size_t)y * d.nx + x) * 16 + g * 8);
+        *reinterpret_cast<uint4*>(tsm + g * TC_LBO + hz * TC_SZ + hy * TC_SY + hx * 16) = val;
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tmem_slot;
+    const uint32_t abase = tc_smem_u32(tsm), bbase = tc_smem_u32(tsm + TC_OFF_B);
+    const int nplanes = min(TCZ, d.nz - z0);
+    if (tid == 0) {
+        for (int p = 0; p < nplanes; ++p) {
+            for (int t = 0; t < kNnTaps; ++t) {
+                const int dx = t % 3 - 1, dy = (t / 3) % 3 - 1, dz = t / 9 - 1;
+                const uint32_t aaddr = abase + (p + 1 + dz) * TC_SZ + (1 + dy) * TC_SY + (1 + dx) * 16;
+                const uint64_t adesc = tc_desc(aaddr, TC_LBO, TC_SY);
+                const uint64_t bdesc = tc_desc(bbase + t * TC_TAP_BYTES, 128, 256);
+                const uint32_t acc = t > 0 ? 1u : 0u;
+                asm volatile(
+                    "{\n\t.reg .pred q;\n\t"
+                    "setp.ne.b32 q, %4, 0;\n\t"
+                    "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, q;\n\t}\n"
+                    :: "r"(tmem + (uint32_t)(p * 16)), "l"(adesc), "l"(bdesc), "r"(kIdescBf16), "r"(acc));
+            }
+        }
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" :: "r"(bar) : "memory");
+    }
+    // wait for the accumulators (bounded)
+    bool ok = false;
+    for (long it = 0; it < kTcWaitLimit && !ok; ++it) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred q;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 q, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, q;\n\t}\n"
+            : "=r"(done) : "r"(bar), "r"(0u) : "memory");
+        ok = done != 0;
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (!ok) {
+        if (tid == 0) atomicOr(status, 1);
+    } else {
+        const int m = tid;                                  // TMEM lane = tile row
+        const int x = x0 + (m & 7), y = y0 + (m >> 3);
+        for (int p = 0; p < nplanes; ++p) {
+            uint32_t r[16];
+            const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(p * 16);
+            asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+                         : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                           "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+                         : "r"(taddr));
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            const int z = z0 + p;
+            if (x < d.nx && y < d.ny) {
+                const size_t v = (size_t)z * plane + (size_t)y * d.nx + x;
+                if (MODE == 0) {
+                    __align__(16) __nv_bfloat162 h[8];
+#pragma unroll
+                    for (int j = 0; j < 8; ++j)
+                        h[j] = __floats2bfloat162_rn(fmaxf(__uint_as_float(r[2 * j]), 0.f), fmaxf(__uint_as_float(r[2 * j + 1]), 0.f));
+                    uint4* dst = reinterpret_cast<uint4*>(out_bf + v * 16);
+                    dst[0] = *reinterpret_cast<uint4*>(&h[0]);
+                    dst[1] = *reinterpret_cast<uint4*>(&h[4]);
+                } else {
+#pragma unroll
+                    for (int c = 0; c < kNnOut; ++c) out_f[(size_t)c * d.V + v] = __uint_as_float(r[c]);
+                }
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "r"(TC_TMEM_COLS) : "memory");
+    }
+}
+
+// features, channel-last BF16 [V][16]: channels 0-2 r_hat, 3-5 rho r_hat, rest 0 (grid pre-zeroed)
+__global__ void k_feat_free_tc(const double* __restrict__ r, const double* __restrict__ sdinv,
+                               const float* __restrict__ rho_grid, const int32_t* __restrict__ gmap,
+                               __nv_bfloat16* __restrict__ f, int nf, int V) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nf) return;
+    const int g = gmap[i], c = g / V, node = g - c * V;
+    const float v = (float)(r[i] * sdinv[i]);
+    f[(size_t)node * 16 + c] = __float2bfloat16_rn(v);
+    f[(size_t)node * 16 + 3 + c] = __float2bfloat16_rn(rho_grid[g] * v);
+}
+
+__global__ void k_feat_grid_tc(const float* __restrict__ x, const float* __restrict__ rho, __nv_bfloat16* __restrict__ f, int V) {
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= V) return;
+    __align__(16) __nv_bfloat16 h[16];
+#pragma unroll
+    for (int c = 0; c < 16; ++c) h[c] = __float2bfloat16_rn(0.f);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const float a = x[(size_t)c * V + v];
+        h[c] = __float2bfloat16_rn(a);
+        h[3 + c] = __float2bfloat16_rn(rho[(size_t)c * V + v] * a);
+    }
+    uint4* dst = reinterpret_cast<uint4*>(f + (size_t)v * 16);
+    dst[0] = *reinterpret_cast<uint4*>(&h[0]);
+    dst[1] = *reinterpret_cast<uint4*>(&h[8]);
+}
+
 inline int nblocks(size_t n, int t = kThreads) { return (int)((n + t - 1) / t); }
 
 // layer table: (cin, cout, offset into the weight vector)
@@ -245,6 +446,12 @@ struct NnPrecond {
     float* lsum = nullptr;     // loss accumulator(s)
     std::vector<float*> X, Y;  // training pairs [3][V] each
     int nblk_wg = 0;
+    // tensor-core inference
+    int use_tc = 1;
+    bool tc_ready = false;
+    __nv_bfloat16 *wimg = nullptr, *featc = nullptr, *actA = nullptr, *actB = nullptr;
+    int* status = nullptr;
+    int ntx = 0, nty = 0, ntz = 0;
 
     template <typename T>
     int alloc(size_t n, T** p) {
@@ -269,6 +476,28 @@ struct NnPrecond {
         k_conv<kNnHid, kNnHid, true><<<g, kThreads, 0, stream>>>(a0, W + kLayers[1].off, a1, d, nullptr);
         k_conv<kNnHid, kNnHid, true><<<g, kThreads, 0, stream>>>(a1, W + kLayers[2].off, a2, d, nullptr);
         k_conv<kNnHid, kNnOut, false><<<g, kThreads, 0, stream>>>(a2, W + kLayers[3].off, y, d, nullptr);
+        NN_TRY(cudaGetLastError());
+        return SVL_OK;
+    }
+
+    int prepare_tc() {
+        for (int l = 0; l < 4; ++l)
+            k_wprep<<<nblocks(kNnTaps * 256), kThreads, 0, stream>>>(W + kLayers[l].off, wimg + (size_t)l * kNnTaps * 256,
+                                                                     kLayers[l].cin, kLayers[l].cout);
+        NN_TRY(cudaGetLastError());
+        tc_ready = true;
+        return SVL_OK;
+    }
+
+    // tensor-core forward of the BF16 features in `featc`; output y (FP32 [3][V])
+    int forward_tc() {
+        if (!tc_ready) if (int st = prepare_tc()) return st;
+        const int nt = ntx * nty * ntz;
+        const size_t lw = (size_t)kNnTaps * 256;
+        k_conv_tc<0><<<nt, TC_THREADS, TC_SMEM, stream>>>(featc, wimg, actA, nullptr, d, ntx, nty, status);
+        k_conv_tc<0><<<nt, TC_THREADS, TC_SMEM, stream>>>(actA, wimg + lw, actB, nullptr, d, ntx, nty, status);
+        k_conv_tc<0><<<nt, TC_THREADS, TC_SMEM, stream>>>(actB, wimg + 2 * lw, actA, nullptr, d, ntx, nty, status);
+        k_conv_tc<1><<<nt, TC_THREADS, TC_SMEM, stream>>>(actA, wimg + 3 * lw, nullptr, y, d, ntx, nty, status);
         NN_TRY(cudaGetLastError());
         return SVL_OK;
     }
@@ -333,6 +562,21 @@ int nn_create(int nx, int ny, int nz, const std::vector<int32_t>& gmap, const st
         (st = nn->alloc(1 << 16, &nn->lsum)))
         return fail(st);
     nn->nblk_wg = (int)((V + kWgChunk - 1) / kWgChunk);
+    nn->ntx = (nx + TCX - 1) / TCX;
+    nn->nty = (ny + TCY - 1) / TCY;
+    nn->ntz = (nz + TCZ - 1) / TCZ;
+    if ((st = nn->alloc((size_t)4 * kNnTaps * 256, &nn->wimg)) || (st = nn->alloc(16 * V, &nn->featc)) ||
+        (st = nn->alloc(16 * V, &nn->actA)) || (st = nn->alloc(16 * V, &nn->actB)) || (st = nn->alloc(4, &nn->status)))
+        return fail(st);
+    NN_TRY(cudaMemsetAsync(nn->status, 0, sizeof(int), stream));
+    {
+        static bool attr_set = false;
+        if (!attr_set) {
+            NN_TRY(cudaFuncSetAttribute(k_conv_tc<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM));
+            NN_TRY(cudaFuncSetAttribute(k_conv_tc<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM));
+            attr_set = true;
+        }
+    }
     if ((st = nn->alloc((size_t)nn->nblk_wg * kNnTaps * kNnHid * kNnHid, &nn->partial))) return fail(st);
     // host-side grids: rho and mask on the lattice
     std::vector<float> rg(3 * V, 0.f), mg(3 * V, 0.f);
@@ -366,9 +610,15 @@ void nn_destroy(NnPrecond* nn) { delete nn; }
 
 int nn_apply(NnPrecond* nn, const double* r, double* z) {
     const int n3 = 3 * nn->d.V;
-    NN_TRY(cudaMemsetAsync(nn->feat, 0, sizeof(float) * kNnIn * (size_t)nn->d.V, nn->stream));
-    k_feat_free<<<nblocks(nn->nf), kThreads, 0, nn->stream>>>(r, nn->sdinv, nn->rho, nn->gmap, nn->feat, nn->nf, n3);
-    if (int st = nn->forward()) return st;
+    if (nn->use_tc) {
+        NN_TRY(cudaMemsetAsync(nn->featc, 0, sizeof(__nv_bfloat16) * 16 * (size_t)nn->d.V, nn->stream));
+        k_feat_free_tc<<<nblocks(nn->nf), kThreads, 0, nn->stream>>>(r, nn->sdinv, nn->rho, nn->gmap, nn->featc, nn->nf, nn->d.V);
+        if (int st = nn->forward_tc()) return st;
+    } else {
+        NN_TRY(cudaMemsetAsync(nn->feat, 0, sizeof(float) * kNnIn * (size_t)nn->d.V, nn->stream));
+        k_feat_free<<<nblocks(nn->nf), kThreads, 0, nn->stream>>>(r, nn->sdinv, nn->rho, nn->gmap, nn->feat, nn->nf, n3);
+        if (int st = nn->forward()) return st;
+    }
     k_out_free<<<nblocks(nn->nf), kThreads, 0, nn->stream>>>(nn->y, r, nn->sdinv, nn->gmap, z, nn->nf);
     NN_TRY(cudaGetLastError());
     return SVL_OK;
@@ -413,6 +663,7 @@ int nn_train(NnPrecond* nn, int iters, int batch, float lr, uint64_t seed, float
         k_adam<<<nblocks(kNnWeights), kThreads, 0, nn->stream>>>(nn->W, nn->G, nn->am, nn->av, kNnWeights, lr_t, b1, b2, eps);
         NN_TRY(cudaGetLastError());
     }
+    nn->tc_ready = false;
     std::vector<float> lh(iters);
     NN_TRY(cudaMemcpyAsync(lh.data(), nn->lsum, sizeof(float) * iters, cudaMemcpyDeviceToHost, nn->stream));
     NN_TRY(cudaStreamSynchronize(nn->stream));
@@ -425,6 +676,7 @@ int nn_train(NnPrecond* nn, int iters, int batch, float lr, uint64_t seed, float
 }
 
 int nn_set_weights(NnPrecond* nn, const float* w) {
+    nn->tc_ready = false;
     NN_TRY(cudaMemcpyAsync(nn->W, w, sizeof(float) * kNnWeights, cudaMemcpyHostToDevice, nn->stream));
     NN_TRY(cudaStreamSynchronize(nn->stream));
     return SVL_OK;
@@ -451,6 +703,36 @@ int nn_loss_grad_host(NnPrecond* nn, const float* x, const float* t, float* loss
     NN_TRY(cudaStreamSynchronize(nn->stream));
     return SVL_OK;
 }
+
+int nn_forward_host(NnPrecond* nn, const float* x, float* y, int path) {
+    const size_t n3 = 3 * (size_t)nn->d.V;
+    float* X = nullptr;
+    if (int st = nn->alloc(n3, &X)) return st;
+    NN_TRY(cudaMemcpyAsync(X, x, n3 * 4, cudaMemcpyHostToDevice, nn->stream));
+    if (path == 1) {
+        k_feat_grid_tc<<<nblocks(nn->d.V), kThreads, 0, nn->stream>>>(X, nn->rho, nn->featc, nn->d.V);
+        if (int st = nn->forward_tc()) return st;
+    } else {
+        k_feat_grid<<<nblocks(n3), kThreads, 0, nn->stream>>>(X, nn->rho, nn->feat, (int)n3);
+        if (int st = nn->forward()) return st;
+    }
+    NN_TRY(cudaMemcpyAsync(y, nn->y, n3 * 4, cudaMemcpyDeviceToHost, nn->stream));
+    NN_TRY(cudaStreamSynchronize(nn->stream));
+    return nn_status(nn);
+}
+
+int nn_status(NnPrecond* nn) {
+    int h = 0;
+    NN_TRY(cudaMemcpyAsync(&h, nn->status, sizeof(int), cudaMemcpyDeviceToHost, nn->stream));
+    NN_TRY(cudaStreamSynchronize(nn->stream));
+    if (h) {
+        set_error("tensor-core convolution reported status %d (1 = accumulator wait gave up, 4 = misaligned shared memory)", h);
+        return SVL_ERR_CUDA;
+    }
+    return SVL_OK;
+}
+
+void nn_set_path(NnPrecond* nn, int path) { nn->use_tc = path == 1; }
 
 int nn_get_grids(NnPrecond* nn, float* rho, float* mask) {
     const size_t n3 = 3 * (size_t)nn->d.V;

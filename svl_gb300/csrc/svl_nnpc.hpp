@@ -47,5 +47,12 @@ int nn_get_weights(NnPrecond* nn, float* w);
 int nn_loss_grad_host(NnPrecond* nn, const float* x, const float* t, float* loss, float* grad);
 // Host copies of the rho and free-dof mask grids ([3][V] each).  Test hook.
 int nn_get_grids(NnPrecond* nn, float* rho, float* mask);
+// Network output y ([3][V]) for a host r_hat grid x ([3][V]); path 0 = FP32 CUDA
+// cores, 1 = BF16 tensor cores.  Test hook.
+int nn_forward_host(NnPrecond* nn, const float* x, float* y, int path);
+// Inference path used by nn_apply (0 = FP32 CUDA cores, 1 = tensor cores, the default).
+void nn_set_path(NnPrecond* nn, int path);
+// SVL_OK, or an error if a tensor-core launch reported a bounded wait that gave up.
+int nn_status(NnPrecond* nn);
 
 }  // namespace svl

@@ -254,6 +254,17 @@ class NewmarkBeta:
                                         ptr(grad, C.c_float)))
         return float(loss[0]), grad
 
+    def nn_forward(self, x, path: int = 1):
+        """Network output y for an r_hat grid x ([3][nz][ny][nx]); path 0 = FP32
+        CUDA cores, 1 = BF16 tensor cores."""
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        y = np.zeros_like(x)
+        check(lib().svl_nm_nn_forward(self._h, ptr(x, C.c_float), ptr(y, C.c_float), int(path)))
+        return y
+
+    def nn_set_path(self, path: int):
+        check(lib().svl_nm_nn_set_path(self._h, int(path)))
+
     def nn_grids(self):
         nx, ny, nz = self.lattice()
         rho = np.zeros((3, nz, ny, nx), np.float32)

@@ -30,6 +30,24 @@ def test_device_gradient_matches_oracle(gpu):
     assert rel_l2(g, go) <= 1e-4
 
 
+def test_tensor_core_forward_matches_fp32_and_oracle(gpu):
+    # 10 x 18 x 11 node lattice: ragged 8 x 16 x 8 tiles on every axis
+    m, L, dt = h8_box(9, 17, 10, seed=4, nt=10)
+    nm = NewmarkBeta(m, L, 10 * dt)
+    rho, mask = nm.nn_grids()
+    rng = np.random.default_rng(5)
+    w = (rng.standard_normal(N.num_weights()) * 0.2).astype(np.float32)
+    nm.nn_weights(w)
+    x = (rng.standard_normal(mask.shape) * mask).astype(np.float32)
+    y32 = nm.nn_forward(x, path=0)
+    ytc = nm.nn_forward(x, path=1)
+    nm.close()
+    yo = N.forward(w.astype(np.float64), x.astype(np.float64), rho.astype(np.float64))[4]
+    assert np.abs(yo).max() > 0
+    assert rel_l2(y32, yo) <= 1e-5
+    assert rel_l2(ytc, yo) <= 3e-2        # BF16 operands, FP32 accumulation
+
+
 def test_trained_preconditioner_cuts_iterations(gpu):
     m, L, dt = workloads.config4(16, 16, 16, nt=80)
     a = NewmarkBeta(m, L, dt, pcg_tol=1e-8, precond=capi.SVL_PRECOND_JACOBI)
@@ -54,6 +72,27 @@ def test_trained_preconditioner_cuts_iterations(gpu):
     assert res <= 1e-8
     assert it_a < 0.6 * it_b, (it_a, it_b)
     assert rel_l2(ha, hb) <= 1e-5
+
+
+def test_cuda_core_and_tensor_core_paths_both_converge(gpu):
+    m, L, dt = workloads.config4(12, 12, 12, nt=40)
+    a = NewmarkBeta(m, L, dt, pcg_tol=1e-8)
+    a.Initialize()
+    a.run(1, 5)
+    a.train_preconditioner(6, solve_steps=0, n_synthetic=100, iters=300, batch=4, seed=3)
+    U0 = [a.GetDisplacements(), a.GetVelocities(), a.GetAccelerations()]
+    its = []
+    res = []
+    for path in (0, 1):
+        a.Initialize(*U0)
+        a.nn_set_path(path)
+        i0 = a.stats()[0]
+        a.run(6, 5)
+        its.append(a.stats()[0] - i0)
+        res.append(a.stats()[2])
+    a.close()
+    assert max(res) <= 1e-8
+    assert abs(its[1] - its[0]) <= 0.25 * its[0] + 2, its
 
 
 def test_training_from_solve_iterates_runs(gpu):
