@@ -9,7 +9,9 @@
 #include <cstring>
 #include <vector>
 
+#include <cuda.h>
 #include <cuda_bf16.h>
+#include <cudaTypedefs.h>
 
 #include "svl_internal.hpp"
 #include "svl_nnpc.hpp"
@@ -219,35 +221,39 @@ __global__ void k_adam(float* __restrict__ W, const float* __restrict__ G, float
 // Tensor-core inference path (tcgen05.mma.kind::f16, BF16 operands, FP32
 // accumulation in TMEM).  Activations are channel-last BF16 grids [V][16].
 // One CTA computes a tile of 8 (x) x 16 (y) x TCZ (z) voxels: the haloed
-// block (10 x 18 x (TCZ+2) voxels) is staged in shared memory in the
+// block (10 x 18 x (TCZ+2) voxels) is staged by TMA in shared memory in the
 // no-swizzle K-major canonical layout, channel group g (8 channels = 16 B)
 // at g * TC_LBO, voxel (x, y, z) at z * TC_SZ + y * TC_SY + x * 16.  The
-// A operand of z-plane p and tap (dx, dy, dz) is then that block read from
-// (p + 1 + dz, 1 + dy, 1 + dx) with row stride TC_SY between 8-row groups:
-// each tap is one descriptor offset, no data movement.  27 MMAs of
-// M128 x N16 x K16 accumulate one plane in 16 TMEM columns.
-constexpr int TCX = 8, TCY = 16, TCZ = 8;
+// A operand of halo plane h shifted by (dx, dy) is that block read from
+// (h, 1 + dy, 1 + dx) with row stride TC_SY between 8-row groups: a shift is
+// a descriptor offset, no data movement.  The three z taps are folded into
+// N: for each (dx, dy) and halo plane h one M128 x N48 x K16 MMA multiplies
+// A(h) by [W(dz=+1) | W(dz=0) | W(dz=-1)] into TMEM columns 16 h .. 16 h + 47,
+// which hold the accumulators of output planes h-2, h-1, h (plane p lives at
+// columns 16 (p + 2)).  9 (TCZ + 2) MMAs per tile instead of 27 TCZ.
+constexpr int TCX = 8, TCY = 16, TCZ = 12;
 constexpr int TC_HX = TCX + 2, TC_HY = TCY + 2, TC_HZ = TCZ + 2;
 constexpr int TC_SY = TC_HX * 16;                 // 160 B
 constexpr int TC_SZ = TC_HY * TC_SY;              // 2880 B
-constexpr int TC_LBO = TC_HZ * TC_SZ;             // 28800 B: second channel group
+constexpr int TC_LBO = TC_HZ * TC_SZ;             // second channel group
 constexpr int TC_A_BYTES = 2 * TC_LBO;
-constexpr int TC_TAP_BYTES = 512;                 // 16 x 16 BF16 B operand per tap
-constexpr int TC_B_BYTES = kNnTaps * TC_TAP_BYTES;
+constexpr int TC_PAIRS = 9;                       // (dx, dy)
+constexpr int TC_PAIR_BYTES = 48 * 16 * 2;        // N48 x K16 BF16 B operand
+constexpr int TC_B_BYTES = TC_PAIRS * TC_PAIR_BYTES;
 constexpr int TC_OFF_B = TC_A_BYTES;
 constexpr int TC_OFF_BAR = TC_OFF_B + TC_B_BYTES;
-constexpr int TC_SMEM = TC_OFF_BAR + 16;
+constexpr int TC_SMEM = TC_OFF_BAR + 32;
 constexpr int TC_THREADS = 128;
-constexpr uint32_t TC_TMEM_COLS = 128;            // TCZ planes x 16 columns
+constexpr uint32_t TC_TMEM_COLS = 256;            // (TCZ + 4) planes x 16 columns, rounded up
 constexpr long kTcWaitLimit = 4000000;
-static_assert(TC_SY % 16 == 0 && TC_SZ % 16 == 0 && TC_LBO % 16 == 0, "descriptor strides");
+static_assert(TC_SY % 16 == 0 && TC_SZ % 16 == 0 && TC_LBO % 128 == 0, "descriptor strides / TMA destinations");
 static_assert(TC_OFF_B % 128 == 0 && TC_OFF_BAR % 8 == 0, "alignment");
 static_assert((TC_LBO >> 4) < (1 << 14) && (TC_SY >> 4) < (1 << 14), "descriptor fields");
-static_assert(TCZ * 16 <= (int)TC_TMEM_COLS, "TMEM columns");
+static_assert((TCZ + 4) * 16 <= (int)TC_TMEM_COLS, "TMEM columns");
 static_assert(TC_SMEM <= 227 * 1024, "shared memory");
 
 // D = F32 (bits 4-5), A = B = BF16 (bits 7-9, 10-12), K-major, N >> 3, M >> 4
-constexpr uint32_t kIdescBf16 = (1u << 4) | (1u << 7) | (1u << 10) | ((16u >> 3) << 17) | ((128u >> 4) << 24);
+constexpr uint32_t kIdescBf16N48 = (1u << 4) | (1u << 7) | (1u << 10) | ((48u >> 3) << 17) | ((128u >> 4) << 24);
 
 __device__ __forceinline__ uint32_t tc_smem_u32(const void* p) { return static_cast<uint32_t>(__cvta_generic_to_shared(p)); }
 
@@ -255,28 +261,30 @@ __device__ __forceinline__ uint64_t tc_desc(uint32_t saddr, uint32_t lbo, uint32
     return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)(lbo >> 4) << 16) | ((uint64_t)(sbo >> 4) << 32) | (1ull << 46);
 }
 
-// W fp32 [cout][cin][27] -> per-tap B operand images (N = 16 out rows, K = 16 in
-// channels, K-major core matrices: (n/8)*256 + (k/8)*128 + (n%8)*16 + (k%8)*2).
+// W fp32 [cout][cin][27] -> per-(dx, dy) B operand images: rows n = 16 blk + co
+// with blk 0, 1, 2 <-> dz = +1, 0, -1; K = 16 input channels; K-major core
+// matrices: (n/8)*256 + (k/8)*128 + (n%8)*16 + (k%8)*2 bytes.
 __global__ void k_wprep(const float* __restrict__ W, __nv_bfloat16* __restrict__ out, int cin, int cout) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;      // over 27 * 16 * 16
-    if (i >= kNnTaps * 256) return;
-    const int t = i / 256, n = (i / 16) % 16, k = i % 16;
-    const float w = (n < cout && k < cin) ? W[(n * cin + k) * kNnTaps + t] : 0.f;
-    const int off = t * 256 + (n / 8) * 128 + (k / 8) * 64 + (n % 8) * 8 + (k % 8);   // in bf16 units
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;      // over 9 * 48 * 16
+    if (i >= TC_PAIRS * 48 * 16) return;
+    const int j = i / (48 * 16), n = (i / 16) % 48, k = i % 16;
+    const int blk = n / 16, co = n % 16, dz = 1 - blk;
+    const int t = (dz + 1) * 9 + j;                           // j = (dy+1)*3 + (dx+1)
+    const float w = (co < cout && k < cin) ? W[(co * cin + k) * kNnTaps + t] : 0.f;
+    const int off = j * (48 * 16) + (n / 8) * 128 + (k / 8) * 64 + (n % 8) * 8 + (k % 8);   // in bf16 units
     out[off] = __float2bfloat16_rn(w);
 }
 
-// One tile of one layer.  mode 0: relu, BF16 channel-last output; mode 1:
-// linear, FP32 channel-major output of the first 3 channels.
 template <int MODE>
-__global__ void __launch_bounds__(TC_THREADS) k_conv_tc(const __nv_bfloat16* __restrict__ in,
+__global__ void __launch_bounds__(TC_THREADS) k_conv_tc(const __grid_constant__ CUtensorMap tmap_in,
                                                          const __nv_bfloat16* __restrict__ wimg,
                                                          __nv_bfloat16* __restrict__ out_bf, float* __restrict__ out_f,
                                                          Dims d, int ntx, int nty, int* __restrict__ status) {
     extern __shared__ __align__(128) unsigned char tsm[];
     const int tid = threadIdx.x, warp = tid >> 5;
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(tsm + TC_OFF_BAR + 8);
-    const uint32_t bar = tc_smem_u32(tsm + TC_OFF_BAR);
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(tsm + TC_OFF_BAR + 16);
+    const uint32_t bar = tc_smem_u32(tsm + TC_OFF_BAR);            // MMA completion
+    const uint32_t bar_tma = tc_smem_u32(tsm + TC_OFF_BAR + 8);    // halo arrival
     if (tc_smem_u32(tsm) & 127u) {                        // descriptors assume a 128 B aligned window
         if (tid == 0) atomicOr(status, 4);
         return;
@@ -290,7 +298,16 @@ __global__ void __launch_bounds__(TC_THREADS) k_conv_tc(const __nv_bfloat16* __r
     }
     if (tid == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(bar), "r"(1) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(bar_tma), "r"(1) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        // haloed block, one 8-channel group per copy; zero fill outside the lattice
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" :: "r"(bar_tma), "r"(TC_A_BYTES) : "memory");
+#pragma unroll
+        for (int g = 0; g < 2; ++g)
+            asm volatile(
+                "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], [%6];"
+                :: "r"(tc_smem_u32(tsm + g * TC_LBO)), "l"(reinterpret_cast<uint64_t>(&tmap_in)), "r"(g * 8),
+                   "r"(x0 - 1), "r"(y0 - 1), "r"(z0 - 1), "r"(bar_tma) : "memory");
     }
     // B operand images (27 taps)
     {
@@ -298,16 +315,23 @@ __global__ void __launch_bounds__(TC_THREADS) k_conv_tc(const __nv_bfloat16* __r
         uint4* dst = reinterpret_cast<uint4*>(tsm + TC_OFF_B);
         for (int i = tid; i < TC_B_BYTES / 16; i += TC_THREADS) dst[i] = src[i];
     }
-    // haloed activation block, zero outside the lattice
     const size_t plane = (size_t)d.nx * d.ny;
-    for (int i = tid; i < 2 * TC_HX * TC_HY * TC_HZ; i += TC_THREADS) {
-        const int g = i & 1, c = i >> 1;
-        const int hx = c % TC_HX, hy = (c / TC_HX) % TC_HY, hz = c / (TC_HX * TC_HY);
-        const int x = x0 + hx - 1, y = y0 + hy - 1, z = z0 + hz - 1;
-        uint4 val = make_uint4(0u, 0u, 0u, 0u);
-        if (x >= 0 && x < d.nx && y >= 0 && y < d.ny && z >= 0 && z < d.nz)
-            val = *reinterpret_cast<const uint4*>(in + ((size_t)z * plane + (size_t)y * d.nx + x) * 16 + g * 8);
-        *reinterpret_cast<uint4*>(tsm + g * TC_LBO + hz * TC_SZ + hy * TC_SY + hx * 16) = val;
+    __syncthreads();                                     // barriers initialised before anyone polls
+    bool ok = false;
+    for (long it = 0; it < kTcWaitLimit && !ok; ++it) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred q;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 q, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, q;\n\t}\n"
+            : "=r"(done) : "r"(bar_tma), "r"(0u) : "memory");
+        ok = done != 0;
+    }
+    ok = __syncthreads_and(ok);
+    if (!ok) {                                          // halo never arrived: report, release TMEM, stop
+        if (tid == 0) atomicOr(status, 2);
+        if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(*tmem_slot), "r"(TC_TMEM_COLS) : "memory");
+        return;
     }
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -316,25 +340,39 @@ __global__ void __launch_bounds__(TC_THREADS) k_conv_tc(const __nv_bfloat16* __r
     const uint32_t tmem = *tmem_slot;
     const uint32_t abase = tc_smem_u32(tsm), bbase = tc_smem_u32(tsm + TC_OFF_B);
     const int nplanes = min(TCZ, d.nz - z0);
+    // zero the accumulators (every MMA accumulates)
+    {
+        const uint32_t zr = 0u;
+        for (int c = 0; c < (TCZ + 4) * 16; c += 16)
+            asm volatile("tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1};"
+                         :: "r"(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c), "r"(zr) : "memory");
+        asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     if (tid == 0) {
-        for (int p = 0; p < nplanes; ++p) {
-            for (int t = 0; t < kNnTaps; ++t) {
-                const int dx = t % 3 - 1, dy = (t / 3) % 3 - 1, dz = t / 9 - 1;
-                const uint32_t aaddr = abase + (p + 1 + dz) * TC_SZ + (1 + dy) * TC_SY + (1 + dx) * 16;
-                const uint64_t adesc = tc_desc(aaddr, TC_LBO, TC_SY);
-                const uint64_t bdesc = tc_desc(bbase + t * TC_TAP_BYTES, 128, 256);
-                const uint32_t acc = t > 0 ? 1u : 0u;
-                asm volatile(
-                    "{\n\t.reg .pred q;\n\t"
-                    "setp.ne.b32 q, %4, 0;\n\t"
-                    "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, q;\n\t}\n"
-                    :: "r"(tmem + (uint32_t)(p * 16)), "l"(adesc), "l"(bdesc), "r"(kIdescBf16), "r"(acc));
+        // halo planes h = 0 .. nplanes + 1 in residue classes mod 3, so that
+        // consecutive MMAs write disjoint column ranges
+        for (int j = 0; j < TC_PAIRS; ++j) {
+            const int dx = j % 3 - 1, dy = j / 3 - 1;
+            const uint64_t bdesc = tc_desc(bbase + j * TC_PAIR_BYTES, 128, 256);
+            for (int r3 = 0; r3 < 3; ++r3) {
+                for (int h = r3; h <= nplanes + 1; h += 3) {
+                    const uint32_t aaddr = abase + h * TC_SZ + (1 + dy) * TC_SY + (1 + dx) * 16;
+                    const uint64_t adesc = tc_desc(aaddr, TC_LBO, TC_SY);
+                    asm volatile(
+                        "{\n\t.reg .pred q;\n\t"
+                        "setp.ne.b32 q, %4, 0;\n\t"
+                        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, q;\n\t}\n"
+                        :: "r"(tmem + (uint32_t)(h * 16)), "l"(adesc), "l"(bdesc), "r"(kIdescBf16N48), "r"(1u));
+                }
             }
         }
         asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" :: "r"(bar) : "memory");
     }
     // wait for the accumulators (bounded)
-    bool ok = false;
+    ok = false;
     for (long it = 0; it < kTcWaitLimit && !ok; ++it) {
         uint32_t done;
         asm volatile(
@@ -352,7 +390,7 @@ __global__ void __launch_bounds__(TC_THREADS) k_conv_tc(const __nv_bfloat16* __r
         const int x = x0 + (m & 7), y = y0 + (m >> 3);
         for (int p = 0; p < nplanes; ++p) {
             uint32_t r[16];
-            const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(p * 16);
+            const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)((p + 2) * 16);
             asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
                          : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
                            "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
@@ -396,6 +434,27 @@ __global__ void k_feat_free_tc(const double* __restrict__ r, const double* __res
     f[(size_t)node * 16 + 3 + c] = __float2bfloat16_rn(rho_grid[g] * v);
 }
 
+// features, channel-last BF16 [V][16], one thread per voxel (no pre-zeroing)
+__global__ void k_feat_voxel_tc(const double* __restrict__ r, const double* __restrict__ sdinv,
+                                const float* __restrict__ rho_grid, const int32_t* __restrict__ inv,
+                                __nv_bfloat16* __restrict__ f, int V) {
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= V) return;
+    __align__(16) __nv_bfloat16 h[16];
+#pragma unroll
+    for (int c = 0; c < 16; ++c) h[c] = __float2bfloat16_rn(0.f);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const int i = inv[(size_t)c * V + v];
+        const float a = i >= 0 ? (float)(r[i] * sdinv[i]) : 0.f;
+        h[c] = __float2bfloat16_rn(a);
+        h[3 + c] = __float2bfloat16_rn(rho_grid[(size_t)c * V + v] * a);
+    }
+    uint4* dst = reinterpret_cast<uint4*>(f + (size_t)v * 16);
+    dst[0] = *reinterpret_cast<uint4*>(&h[0]);
+    dst[1] = *reinterpret_cast<uint4*>(&h[8]);
+}
+
 __global__ void k_feat_grid_tc(const float* __restrict__ x, const float* __restrict__ rho, __nv_bfloat16* __restrict__ f, int V) {
     const int v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= V) return;
@@ -412,6 +471,32 @@ __global__ void k_feat_grid_tc(const float* __restrict__ x, const float* __restr
     dst[0] = *reinterpret_cast<uint4*>(&h[0]);
     dst[1] = *reinterpret_cast<uint4*>(&h[8]);
 }
+
+// TMA map of a channel-last BF16 grid [nz][ny][nx][16]: box = one 8-channel
+// group of the haloed tile (8 x 10 x 18 x TC_HZ), zero fill outside.
+int make_grid_map(const __nv_bfloat16* base, const Dims& d, CUtensorMap* map) {
+    static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+    if (!encode) {
+        cudaDriverEntryPointQueryResult q;
+        void* fn = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess || !fn) {
+            set_error("cuTensorMapEncodeTiled is not available from the driver");
+            return SVL_ERR_CUDA;
+        }
+        encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+    }
+    const cuuint64_t dims[4] = {16, (cuuint64_t)d.nx, (cuuint64_t)d.ny, (cuuint64_t)d.nz};
+    const cuuint64_t strides[3] = {32, (cuuint64_t)d.nx * 32, (cuuint64_t)d.nx * d.ny * 32};
+    const cuuint32_t box[4] = {8, TC_HX, TC_HY, TC_HZ};
+    const cuuint32_t estr[4] = {1, 1, 1, 1};
+    const CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<__nv_bfloat16*>(base), dims, strides, box,
+                              estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                              CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) { set_error("cuTensorMapEncodeTiled failed (%d)", (int)r); return SVL_ERR_CUDA; }
+    return SVL_OK;
+}
+static_assert(TC_HX * TC_HY * TC_HZ * 8 * 2 == TC_LBO, "one TMA box fills one channel-group block");
 
 inline int nblocks(size_t n, int t = kThreads) { return (int)((n + t - 1) / t); }
 
@@ -452,6 +537,8 @@ struct NnPrecond {
     __nv_bfloat16 *wimg = nullptr, *featc = nullptr, *actA = nullptr, *actB = nullptr;
     int* status = nullptr;
     int ntx = 0, nty = 0, ntz = 0;
+    CUtensorMap map_feat{}, map_A{}, map_B{};
+    int32_t* inv = nullptr;    // [3][V] free dof or -1
 
     template <typename T>
     int alloc(size_t n, T** p) {
@@ -482,22 +569,23 @@ struct NnPrecond {
 
     int prepare_tc() {
         for (int l = 0; l < 4; ++l)
-            k_wprep<<<nblocks(kNnTaps * 256), kThreads, 0, stream>>>(W + kLayers[l].off, wimg + (size_t)l * kNnTaps * 256,
-                                                                     kLayers[l].cin, kLayers[l].cout);
+            k_wprep<<<nblocks(TC_PAIRS * 48 * 16), kThreads, 0, stream>>>(W + kLayers[l].off, wimg + (size_t)l * TC_PAIRS * 48 * 16,
+                                                                          kLayers[l].cin, kLayers[l].cout);
         NN_TRY(cudaGetLastError());
         tc_ready = true;
         return SVL_OK;
     }
 
     // tensor-core forward of the BF16 features in `featc`; output y (FP32 [3][V])
+    // tensor-core forward of the BF16 features in `featc`; output y (FP32 [3][V])
     int forward_tc() {
         if (!tc_ready) if (int st = prepare_tc()) return st;
         const int nt = ntx * nty * ntz;
-        const size_t lw = (size_t)kNnTaps * 256;
-        k_conv_tc<0><<<nt, TC_THREADS, TC_SMEM, stream>>>(featc, wimg, actA, nullptr, d, ntx, nty, status);
-        k_conv_tc<0><<<nt, TC_THREADS, TC_SMEM, stream>>>(actA, wimg + lw, actB, nullptr, d, ntx, nty, status);
-        k_conv_tc<0><<<nt, TC_THREADS, TC_SMEM, stream>>>(actB, wimg + 2 * lw, actA, nullptr, d, ntx, nty, status);
-        k_conv_tc<1><<<nt, TC_THREADS, TC_SMEM, stream>>>(actA, wimg + 3 * lw, nullptr, y, d, ntx, nty, status);
+        const size_t lw = (size_t)TC_PAIRS * 48 * 16;
+        k_conv_tc<0><<<nt, TC_THREADS, TC_SMEM, stream>>>(map_feat, wimg, actA, nullptr, d, ntx, nty, status);
+        k_conv_tc<0><<<nt, TC_THREADS, TC_SMEM, stream>>>(map_A, wimg + lw, actB, nullptr, d, ntx, nty, status);
+        k_conv_tc<0><<<nt, TC_THREADS, TC_SMEM, stream>>>(map_B, wimg + 2 * lw, actA, nullptr, d, ntx, nty, status);
+        k_conv_tc<1><<<nt, TC_THREADS, TC_SMEM, stream>>>(map_A, wimg + 3 * lw, nullptr, y, d, ntx, nty, status);
         NN_TRY(cudaGetLastError());
         return SVL_OK;
     }
@@ -565,10 +653,20 @@ int nn_create(int nx, int ny, int nz, const std::vector<int32_t>& gmap, const st
     nn->ntx = (nx + TCX - 1) / TCX;
     nn->nty = (ny + TCY - 1) / TCY;
     nn->ntz = (nz + TCZ - 1) / TCZ;
-    if ((st = nn->alloc((size_t)4 * kNnTaps * 256, &nn->wimg)) || (st = nn->alloc(16 * V, &nn->featc)) ||
+    if ((st = nn->alloc((size_t)4 * TC_PAIRS * 48 * 16, &nn->wimg)) || (st = nn->alloc(16 * V, &nn->featc)) ||
         (st = nn->alloc(16 * V, &nn->actA)) || (st = nn->alloc(16 * V, &nn->actB)) || (st = nn->alloc(4, &nn->status)))
         return fail(st);
     NN_TRY(cudaMemsetAsync(nn->status, 0, sizeof(int), stream));
+    {
+        std::vector<int32_t> inv(3 * V, -1);
+        for (size_t f = 0; f < gmap.size(); ++f) inv[gmap[f]] = (int32_t)f;
+        if ((st = nn->alloc(3 * V, &nn->inv))) return fail(st);
+        NN_TRY(cudaMemcpyAsync(nn->inv, inv.data(), inv.size() * 4, cudaMemcpyHostToDevice, stream));
+        NN_TRY(cudaStreamSynchronize(stream));
+    }
+    if ((st = make_grid_map(nn->featc, nn->d, &nn->map_feat)) || (st = make_grid_map(nn->actA, nn->d, &nn->map_A)) ||
+        (st = make_grid_map(nn->actB, nn->d, &nn->map_B)))
+        return fail(st);
     {
         static bool attr_set = false;
         if (!attr_set) {
@@ -611,8 +709,7 @@ void nn_destroy(NnPrecond* nn) { delete nn; }
 int nn_apply(NnPrecond* nn, const double* r, double* z) {
     const int n3 = 3 * nn->d.V;
     if (nn->use_tc) {
-        NN_TRY(cudaMemsetAsync(nn->featc, 0, sizeof(__nv_bfloat16) * 16 * (size_t)nn->d.V, nn->stream));
-        k_feat_free_tc<<<nblocks(nn->nf), kThreads, 0, nn->stream>>>(r, nn->sdinv, nn->rho, nn->gmap, nn->featc, nn->nf, nn->d.V);
+        k_feat_voxel_tc<<<nblocks(nn->d.V), kThreads, 0, nn->stream>>>(r, nn->sdinv, nn->rho, nn->inv, nn->featc, nn->d.V);
         if (int st = nn->forward_tc()) return st;
     } else {
         NN_TRY(cudaMemsetAsync(nn->feat, 0, sizeof(float) * kNnIn * (size_t)nn->d.V, nn->stream));
