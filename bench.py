@@ -171,7 +171,7 @@ def implicit_pcg(steps, warm=20, tol=1e-8):
             "rel_l2_final_u_learned_vs_jacobi": float(np.linalg.norm(Ul - Uj) / max(np.linalg.norm(Uj), 1e-300))}
 
 
-NN_TRAIN = {"solve_steps": 0, "n_synthetic": 400, "iters": 2000, "batch": 4, "lr": 2e-3, "seed": 1}
+NN_TRAIN = {"solve_steps": 0, "n_synthetic": 300, "iters": 1500, "batch": 8, "lr": 2e-3, "seed": 1, "max_sweeps": 5}
 
 
 def dist_info():

@@ -320,6 +320,9 @@ typedef struct svl_nn_train_opts {
     int32_t  batch;        /* pairs per iteration                              */
     float    lr;           /* Adam step (decays to 1/4 at 60 %, 1/20 at 85 %) */
     uint64_t seed;
+    int32_t  max_sweeps;   /* synthetic pair i gets i % (max_sweeps + 1)
+                              smoothing sweeps (0 = the default, 5)           */
+    int32_t  reserved;
 } svl_nn_train_opts;
 /* Runs the solve_steps steps k_first.. (they advance the state), generates
  * the synthetic pairs, trains, and switches the handle to

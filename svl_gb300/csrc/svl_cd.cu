@@ -1155,6 +1155,7 @@ struct svl_nm {
     svl::NnPrecond* nn = nullptr;
     int precond = SVL_PRECOND_JACOBI;
     int64_t jac_ref = 0, fallbacks = 0, learned_solves = 0;
+    int64_t train_trial_iters = 0;          // trial-solve iterations of the kept weights
     // CG iterates recorded for training pairs
     int rec_every = 0, rec_n = 0;
     std::vector<double*> rec_x, rec_r;
@@ -1273,7 +1274,7 @@ static int nm_solve_jacobi(svl_nm* nm, bool warm, int64_t maxit) {
 // Flexible CG with the learned preconditioner; falls back to Jacobi-PCG
 // (continuing from the current iterate) once it has used as many iterations
 // as the last plain Jacobi solve needed.
-static int nm_solve_learned(svl_nm* nm) {
+static int nm_solve_learned(svl_nm* nm, bool allow_fallback = true) {
     svl_cd* cd = nm->cd;
     const int n = nm->nf, tb = 256, g = (n + tb - 1) / tb;
     double hs[S_NSCAL];
@@ -1322,6 +1323,7 @@ static int nm_solve_learned(svl_nm* nm) {
             }
         }
     }
+    if (!allow_fallback) { set_error("learned preconditioner did not converge within the Jacobi budget"); return SVL_ERR_MAXITER; }
     nm->fallbacks++;
     return nm_solve_jacobi(nm, !cold, std::max<int64_t>(1, nm->opts.pcg_maxit - nm->iters_last));
 }
@@ -1501,6 +1503,58 @@ int svl_nm_set_initial(svl_nm* nm, const double* U0, const double* V0, const dou
 
 }  // extern "C"
 
+// Effective force of step k into nm->b (state untouched).
+static int nm_rhs(svl_nm* nm, int k) {
+    svl_cd* cd = nm->cd;
+    const HostModel& m = cd->m;
+    const double dt = nm->opts.dt;
+    const int tb = 256, ng = (m.nnode + tb - 1) / tb, eg = (m.nelem + 127) / 128;
+    const int km1 = k - 1;
+    CUDA_TRY(cudaMemcpyAsync(cd->d.step, &km1, sizeof(int), cudaMemcpyHostToDevice, cd->stream));
+    k_step_inc<<<1, 1, 0, cd->stream>>>(cd->d.step);
+    if (m.ndim == 2) k_element<2, 4><<<eg, 128, 0, cd->stream>>>(cd->d, cd->d.Us, m.ngp, 0);
+    else k_element<3, 8><<<eg, 128, 0, cd->stream>>>(cd->d, cd->d.Us, m.ngp, 0);
+    if (m.ndim == 2) k_nm_rhs<2><<<ng, tb, 0, cd->stream>>>(cd->d, nm->b, 4.0 / dt);
+    else k_nm_rhs<3><<<ng, tb, 0, cd->stream>>>(cd->d, nm->b, 4.0 / dt);
+    CUDA_TRY(cudaGetLastError());
+    return SVL_OK;
+}
+
+// Right-hand side for scoring the network: the effective force of step k, or
+// K_eff applied to a smooth random field when that force is zero.
+static int nm_trial_rhs(svl_nm* nm, int k) {
+    TRY(nm_rhs(nm, k));
+    double hs[S_NSCAL];
+    nm_dot(nm, nm->b, nm->b, S_RP);
+    TRY(nm_scalars(nm, hs));
+    if (hs[S_RP] > 0.0) return SVL_OK;
+    svl_cd* cd = nm->cd;
+    const int n = nm->nf, tb = 256, g = (n + tb - 1) / tb;
+    k_randn<<<g, tb, 0, cd->stream>>>(nm->e1, n, 0x5EEDull + (uint64_t)k);
+    for (int sweep = 0; sweep < 3; ++sweep) {
+        k_vmul<<<g, tb, 0, cd->stream>>>(nm->e1, nm->sdinv, nm->e2, n);
+        TRY(nm_apply(nm, nm->e2, nm->q));
+        k_smooth<<<g, tb, 0, cd->stream>>>(nm->e1, nm->q, nm->sdinv, 0.5, n);
+    }
+    k_vmul<<<g, tb, 0, cd->stream>>>(nm->e1, nm->sdinv, nm->e2, n);
+    return nm_apply(nm, nm->e2, nm->b);
+}
+
+// Flexible-CG iterations the current network needs on the effective force of
+// step k (a large number if it does not converge within the Jacobi budget);
+// counters and state are left as they were.
+static int64_t nm_trial(svl_nm* nm, int k) {
+    const int64_t it_tot = nm->iters_total, it_last = nm->iters_last, ls = nm->learned_solves, fb = nm->fallbacks;
+    const double res = nm->res_last;
+    int64_t score = INT64_MAX / 4;
+    if (nm_trial_rhs(nm, k) == SVL_OK) {
+        nm->iters_last = 0;
+        if (nm_solve_learned(nm, false) == SVL_OK) score = nm->iters_last;
+    }
+    nm->iters_total = it_tot; nm->iters_last = it_last; nm->learned_solves = ls; nm->fallbacks = fb; nm->res_last = res;
+    return score;
+}
+
 // one step: effective force, solve, state update (d.step already advanced)
 static int nm_step(svl_nm* nm, double* U_hist_row) {
     svl_cd* cd = nm->cd;
@@ -1586,12 +1640,14 @@ int svl_nm_train_preconditioner(svl_nm* nm, int32_t k_first, const svl_nn_train_
         nm->rec_n = 0;
         if (st) return st;
     }
+    const int k_trial = k_first + o->solve_steps;       // the next step to be run
     // 2. synthetic pairs: e random with 0..5 smoothing sweeps, r_hat = A_hat e
     const int n = nm->nf, tb = 256, g = (n + tb - 1) / tb;
+    const int max_sweeps = o->max_sweeps > 0 ? o->max_sweeps : 5;
     double hs[S_NSCAL];
     for (int i = 0; i < o->n_synthetic; ++i) {
         k_randn<<<g, tb, 0, cd->stream>>>(nm->e1, n, o->seed * 0x9E3779B97F4A7C15ull + (uint64_t)i * 0x100000001B3ull);
-        for (int sweep = 0; sweep < i % 6; ++sweep) {
+        for (int sweep = 0; sweep < i % (max_sweeps + 1); ++sweep) {
             k_vmul<<<g, tb, 0, cd->stream>>>(nm->e1, nm->sdinv, nm->e2, n);
             TRY(nm_apply(nm, nm->e2, nm->q));
             k_smooth<<<g, tb, 0, cd->stream>>>(nm->e1, nm->q, nm->sdinv, 0.5, n);
@@ -1604,10 +1660,34 @@ int svl_nm_train_preconditioner(svl_nm* nm, int32_t k_first, const svl_nn_train_
         TRY(svl::nn_record_pair(nm->nn, nm->e2, nm->e1, 1.0 / std::sqrt(hs[S_RP])));
     }
     CUDA_TRY(cudaGetLastError());
-    // 3. Adam
-    float l = 0.f;
-    TRY(svl::nn_train(nm->nn, o->iters, o->batch, o->lr, o->seed, &l));
-    if (loss) *loss = l;
+    // 3. Adam in segments; after each, a trial flexible-CG solve on the
+    //    effective force of the next step scores the network, and the
+    //    best-scoring weights are kept (training loss alone does not track
+    //    the iteration count).
+    if (nm->jac_ref <= 0) {                 // the trial budget is a plain Jacobi solve
+        TRY(nm_trial_rhs(nm, k_trial));
+        nm->iters_last = 0;
+        const int64_t it_tot = nm->iters_total;
+        TRY(nm_solve_jacobi(nm, false, nm->opts.pcg_maxit));
+        nm->iters_total = it_tot;
+    }
+    const int nseg = std::max(1, std::min(o->iters / 250, 16));
+    std::vector<float> best_w(svl::kNnWeights);
+    int64_t best = INT64_MAX;
+    float l = 0.f, best_loss = 0.f;
+    for (int sgm = 0; sgm < nseg; ++sgm) {
+        const int i0 = (int)((int64_t)o->iters * sgm / nseg), i1 = (int)((int64_t)o->iters * (sgm + 1) / nseg);
+        TRY(svl::nn_train_segment(nm->nn, i0, i1, o->iters, o->batch, o->lr, o->seed, &l));
+        const int64_t score = nm_trial(nm, k_trial);
+        if (score <= best) {
+            best = score;
+            best_loss = l;
+            TRY(svl::nn_get_weights(nm->nn, best_w.data()));
+        }
+    }
+    TRY(svl::nn_set_weights(nm->nn, best_w.data()));
+    nm->train_trial_iters = best;
+    if (loss) *loss = best_loss;
     nm->precond = SVL_PRECOND_LEARNED;
     return SVL_OK;
 }

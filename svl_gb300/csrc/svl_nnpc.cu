@@ -737,20 +737,26 @@ int nn_record_pair(NnPrecond* nn, const double* rhat, const double* ehat, double
 
 int nn_num_pairs(const NnPrecond* nn) { return (int)nn->X.size(); }
 
-int nn_train(NnPrecond* nn, int iters, int batch, float lr, uint64_t seed, float* loss) {
+int nn_train_segment(NnPrecond* nn, int it_begin, int it_end, int iters, int batch, float lr, uint64_t seed, float* loss) {
     const int np = (int)nn->X.size();
-    if (np == 0 || iters <= 0 || batch <= 0) { set_error("nothing to train on"); return SVL_ERR_INVALID; }
+    if (np == 0 || iters <= 0 || batch <= 0 || it_begin < 0 || it_end > iters || it_begin >= it_end) {
+        set_error("nothing to train on");
+        return SVL_ERR_INVALID;
+    }
     if (iters > (1 << 16)) { set_error("at most 65536 training iterations"); return SVL_ERR_INVALID; }
-    NN_TRY(cudaMemsetAsync(nn->am, 0, sizeof(float) * kNnWeights, nn->stream));
-    NN_TRY(cudaMemsetAsync(nn->av, 0, sizeof(float) * kNnWeights, nn->stream));
-    NN_TRY(cudaMemsetAsync(nn->lsum, 0, sizeof(float) * iters, nn->stream));
+    if (it_begin == 0) {
+        NN_TRY(cudaMemsetAsync(nn->am, 0, sizeof(float) * kNnWeights, nn->stream));
+        NN_TRY(cudaMemsetAsync(nn->av, 0, sizeof(float) * kNnWeights, nn->stream));
+    }
+    NN_TRY(cudaMemsetAsync(nn->lsum + it_begin, 0, sizeof(float) * (it_end - it_begin), nn->stream));
     const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
-    uint64_t s = seed ^ 0xD1B54A32D192ED03ull;
-    for (int it = 0; it < iters; ++it) {
+    for (int it = it_begin; it < it_end; ++it) {
         NN_TRY(cudaMemsetAsync(nn->G, 0, sizeof(float) * kNnWeights, nn->stream));
         for (int b = 0; b < batch; ++b) {
-            s = s * 6364136223846793005ull + 1442695040888963407ull;
-            const int p = (int)((s >> 33) % (uint64_t)np);
+            // pair index from a counter-based hash of (seed, iteration, slot)
+            uint64_t h = seed ^ (0x9E3779B97F4A7C15ull * (uint64_t)(it * 131 + b + 1));
+            h ^= h >> 31; h *= 0xBF58476D1CE4E5B9ull; h ^= h >> 29;
+            const int p = (int)(h % (uint64_t)np);
             if (int st = nn->sample(nn->X[p], nn->Y[p], 1.f / batch, nn->lsum + it)) return st;
         }
         const float frac = (float)it / iters;
@@ -761,15 +767,20 @@ int nn_train(NnPrecond* nn, int iters, int batch, float lr, uint64_t seed, float
         NN_TRY(cudaGetLastError());
     }
     nn->tc_ready = false;
-    std::vector<float> lh(iters);
-    NN_TRY(cudaMemcpyAsync(lh.data(), nn->lsum, sizeof(float) * iters, cudaMemcpyDeviceToHost, nn->stream));
+    const int n = it_end - it_begin;
+    std::vector<float> lh(n);
+    NN_TRY(cudaMemcpyAsync(lh.data(), nn->lsum + it_begin, sizeof(float) * n, cudaMemcpyDeviceToHost, nn->stream));
     NN_TRY(cudaStreamSynchronize(nn->stream));
-    const int tail = std::max(1, iters / 10);
+    const int tail = std::max(1, n / 10);
     double acc = 0.0;
-    for (int i = iters - tail; i < iters; ++i) acc += lh[i];
+    for (int i = n - tail; i < n; ++i) acc += lh[i];
     if (loss) *loss = (float)(acc / tail / batch);
     if (!std::isfinite(acc)) { set_error("training diverged"); return SVL_ERR_NONFINITE; }
     return SVL_OK;
+}
+
+int nn_train(NnPrecond* nn, int iters, int batch, float lr, uint64_t seed, float* loss) {
+    return nn_train_segment(nn, 0, iters, iters, batch, lr, seed, loss);
 }
 
 int nn_set_weights(NnPrecond* nn, const float* w) {

@@ -39,6 +39,9 @@ int nn_num_pairs(const NnPrecond* nn);
 // Adam on the recorded pairs; *loss = mean relative squared error over the
 // last tenth of the iterations.
 int nn_train(NnPrecond* nn, int iters, int batch, float lr, uint64_t seed, float* loss);
+// Iterations [it_begin, it_end) of an `iters`-long Adam run (learning-rate
+// schedule over the whole run; moments reset when it_begin == 0).
+int nn_train_segment(NnPrecond* nn, int it_begin, int it_end, int iters, int batch, float lr, uint64_t seed, float* loss);
 int nn_set_weights(NnPrecond* nn, const float* w);
 int nn_get_weights(NnPrecond* nn, float* w);
 // Device forward + loss + backward of one sample given as host grids
