@@ -69,5 +69,62 @@ private:
     int ntotal_ = 0;
 };
 
+// NewmarkBeta(mesh, dt, mtol, ktol, ftol) with the Linear algorithm and an
+// iterative LinearSystem (RP/10-Integrators/03-Newmark/NewmarkBeta.cpp:6-141,
+// RP/11-Solvers/02-Iterative/PetscSolver.cc:16-150): the effective-stiffness
+// solve is matrix-free Jacobi-PCG on the GPU to a true relative residual of
+// `tol`, optionally with the learned preconditioner (TrainPreconditioner).
+class NewmarkBeta {
+public:
+    NewmarkBeta(const svl_model_desc& model, const svl_load_desc& loads, double dt, double tol = 1e-8,
+                double mtol = 1e-12, double ftol = 1e-12, int maxit = 20000)
+        : ntotal_(model.ntotal) {
+        svl_nm_opts o{};
+        o.dt = dt;
+        o.ftol = ftol;
+        o.mtol = mtol;
+        o.pcg_tol = tol;
+        o.pcg_maxit = maxit;
+        o.precond = SVL_PRECOND_JACOBI;
+        check(svl_nm_create(&model, &loads, &o, &h_));
+    }
+    ~NewmarkBeta() { svl_nm_destroy(h_); }
+    NewmarkBeta(const NewmarkBeta&) = delete;
+    NewmarkBeta& operator=(const NewmarkBeta&) = delete;
+
+    void Initialize(const double* U0 = nullptr, const double* V0 = nullptr, const double* A0 = nullptr) {
+        check(svl_nm_set_initial(h_, U0, V0, A0));
+    }
+    // ComputeNewStep(mesh, k) -> stop (NewmarkBeta.cpp:117-141)
+    bool ComputeNewStep(unsigned int k) { return svl_nm_run(h_, (int32_t)k, 1, nullptr) != SVL_OK; }
+    bool ComputeNewSteps(unsigned int k_first, unsigned int n, double* U_hist = nullptr) {
+        return svl_nm_run(h_, (int32_t)k_first, (int32_t)n, U_hist) != SVL_OK;
+    }
+    // Trains the learned preconditioner on synthetic pairs of this model's
+    // effective stiffness and switches to it (lattice meshes only).
+    float TrainPreconditioner(unsigned int k_next) {
+        svl_nn_train_opts t{};
+        t.n_synthetic = 300;
+        t.iters = 1500;
+        t.batch = 8;
+        t.lr = 2e-3f;
+        float loss = 0.f;
+        check(svl_nm_train_preconditioner(h_, (int32_t)k_next, &t, &loss));
+        return loss;
+    }
+    std::vector<double> GetDisplacements() const { return get(0); }
+    std::vector<double> GetVelocities() const { return get(1); }
+    std::vector<double> GetAccelerations() const { return get(2); }
+
+private:
+    std::vector<double> get(int which) const {
+        std::vector<double> v(ntotal_);
+        check(svl_nm_get(h_, which, v.data()));
+        return v;
+    }
+    svl_nm* h_ = nullptr;
+    int ntotal_ = 0;
+};
+
 }  // namespace gpu
 }  // namespace svl

@@ -36,7 +36,13 @@ int main() {
             if (cd.ComputeNewStep(k)) { std::printf("stop at %u\n", k); return 2; }
         double mx = 0;
         for (double u : cd.GetDisplacements()) mx = std::fmax(mx, std::fabs(u));
-        std::printf("max|U| %.6e\n", mx);
+        svl::gpu::NewmarkBeta nm(md, ld, 4.0 * dt);
+        nm.Initialize();
+        for (unsigned k = 1; k <= 20; ++k)
+            if (nm.ComputeNewStep(k)) { std::printf("newmark stop at %u\n", k); return 3; }
+        double mn = 0;
+        for (double u : nm.GetDisplacements()) mn = std::fmax(mn, std::fabs(u));
+        std::printf("max|U| %.6e newmark %.6e\n", mx, mn);
     } catch (const svl::gpu::Error& e) {
         if (e.code == SVL_ERR_NODEVICE) { std::printf("nodevice\n"); return 0; }
         std::printf("error %d %s\n", e.code, e.what());
