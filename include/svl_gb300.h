@@ -353,6 +353,27 @@ int  svl_nm_nn_set_path(svl_nm* nm, int32_t path);
 /* Test hook: the rho feature grid and the free-dof mask grid, [3][nz][ny][nx]. */
 int  svl_nm_nn_grids(svl_nm* nm, float* rho, float* mask);
 
+/* ---- PML elements ---------------------------------------------------------- */
+/* Element action of PML2DQuad4 (5 dofs per node: ux uy s11 s22 s12) and
+ * PML3DHexa8 (9 dofs per node: ux uy uz s11 s22 s33 s12 s23 s13) for a batch
+ * of elements, on the GPU:
+ *   y_e = coef[0] M_e u0_e + coef[1] C_e u1_e + coef[2] K_e u2_e + coef[3] G_e u3_e
+ * with M, C, K, G the element mass, damping, stiffness and PML-history
+ * matrices of PML2DQuad4.cpp:233-470 / PML3DHexa8.cpp:214-712 (G is empty
+ * in 2D), applied at the Gauss points without forming them.  coef[2] = 1,
+ * others 0 gives ComputeInternalForces (K u, :474-494 / :716-742).
+ *   X      [nelem][nen][ndim] node coordinates in the element's node order
+ *   mat    [nelem][3] E, nu, rho (Elastic2DPlaneStrain / Elastic3DLinear)
+ *   thick  [nelem] thickness (2D) or NULL for 1
+ *   par    [nelem][3 + 2 ndim] m, L, R, x0[ndim], n[ndim] (the element's
+ *          PML parameters in the order of the reference constructors)
+ *   u      [4][nelem][nc] input vectors (a block may hold anything when its
+ *          coefficient is 0), y [nelem][nc] output; host arrays.
+ * No counterpart in the reference beyond the element functions named. */
+int  svl_pml_element_action(int32_t ndim, int32_t nelem, const double* X, const double* mat,
+                            const double* thick, const double* par, const double* coef,
+                            const double* u, double* y);
+
 /* ---- stepping without device allocation -------------------------------- */
 /* No counterpart in the reference: SVL allocates all of its (host) memory
  * freely.  Some callers of this library cannot let it call cudaMalloc or

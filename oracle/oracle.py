@@ -31,6 +31,8 @@ def lib():
         L.oracle_body_force.argtypes = [vp, C.c_int, f64p, f64p]
         L.oracle_lumped_mass.argtypes = [vp, C.c_double, f64p]
         L.oracle_j2_path.argtypes = [C.c_int, f64p, C.c_int, f64p, f64p]
+        L.oracle_pml_matrices.argtypes = [C.c_int, f64p, C.c_double, C.c_double, C.c_double, C.c_double, f64p,
+                                          f64p, f64p, f64p, f64p]
         _lib = L
     return _lib
 
@@ -131,3 +133,16 @@ def j2_path(mat_type, param, strains):
 def num_threads():
     lib().oracle_num_threads.restype = C.c_int
     return lib().oracle_num_threads()
+
+
+def pml_matrices(ndim, X, E, nu, rho, par, t=1.0):
+    """(M, C, K, G) of one PML2DQuad4 / PML3DHexa8 element."""
+    nc = 20 if ndim == 2 else 72
+    out = [np.zeros((nc, nc)) for _ in range(4)]
+    Xa = np.ascontiguousarray(X, dtype=np.float64)
+    pa = np.ascontiguousarray(par, dtype=np.float64)
+    f64 = C.POINTER(C.c_double)
+    st = lib().oracle_pml_matrices(int(ndim), Xa.ctypes.data_as(f64), float(E), float(nu), float(rho), float(t),
+                                   pa.ctypes.data_as(f64), *[o.ctypes.data_as(f64) for o in out])
+    assert st == 0
+    return out

@@ -953,6 +953,156 @@ struct Newmark {
     }
 };
 
+/* ---------------- PML elements (PML2DQuad4, PML3DHexa8) ------------------ */
+
+/* Stretching factors at a point (PML2DQuad4.cpp:655-693,
+ * PML3DHexa8.cpp:952-996): a_i = 1 + a0 ((x_i - x0_i) n_i / L)^m,
+ * b_i = b0 (...)^m, a0 = (m+1) (L/10) / (2L) ln(1/R), b0 = (m+1) Vp / (2L) ln(1/R). */
+void pml_stretch(int nd, const double* x, const double* par, double rho, double mu, double lambda, double* a, double* b) {
+    const double m = par[0], L = par[1], R = par[2];
+    const double* x0 = par + 3;
+    const double* n = par + 3 + nd;
+    const double Vp = std::sqrt((lambda + 2.0 * mu) / rho);
+    const double bpml = L / 10.0;
+    const double a0 = (m + 1.0) * bpml / 2.0 / L * std::log(1.0 / R);
+    const double b0 = (m + 1.0) * Vp / 2.0 / L * std::log(1.0 / R);
+    for (int i = 0; i < nd; ++i) {
+        const double r = std::pow((x[i] - x0[i]) * n[i] / L, m);
+        a[i] = 1.0 + a0 * r;
+        b[i] = b0 * r;
+    }
+}
+
+/* Element matrices of PML2DQuad4 (5 dofs/node: ux uy s11 s22 s12;
+ * PML2DQuad4.cpp:233-470) and PML3DHexa8 (9 dofs/node: ux uy uz s11 s22 s33
+ * s12 s23 s13; PML3DHexa8.cpp:214-712), row-major nc x nc.  Each matrix is a
+ * scalar s times the displacement block rho N N and the stress-compliance
+ * block, plus (not for M) the displacement-stress coupling dN_j N_k q_d for
+ * derivative direction d:
+ *   3D  M: s = ax ay az,                          q = 0
+ *       C: s = ax ay bz + ax by az + bx ay az,    q = (ay az, ax az, ax ay)
+ *       K: s = ax by bz + bx by az + bx ay bz,    q = (ay bz + az by, ax bz + az bx, ax by + ay bx)
+ *       G: s = bx by bz,                          q = (by bz, bx bz, bx by)
+ *   2D  M: s = ax ay, C: s = ax by + ay bx, q = (ay, ax); K: s = bx by, q = (by, bx); G empty.
+ * Same Gauss points and accumulation order as the lin elements; mu =
+ * E / 2 / (1 + nu) and lambda = E nu / (1 + nu) / (1 - 2 nu) as in the
+ * reference.  par: m, L, R, x0[nd], n[nd]. */
+void pml_matrices(int nd, const double* X, double E, double nu, double rho, double t, const double* par,
+                  double* Mo, double* Co, double* Ko, double* Go) {
+    const int nen = nd == 2 ? 4 : 8, nn = nd == 2 ? 5 : 9, nc = nen * nn, ngp = nen;
+    double* out[4] = {Mo, Co, Ko, Go};
+    for (double* o : out) if (o) std::fill(o, o + (size_t)nc * nc, 0.0);
+    const double mu = E / 2.0 / (1 + nu);
+    const double lambda = E * nu / (1.0 + nu) / (1.0 - 2.0 * nu);
+    for (int q = 0; q < ngp; ++q) {
+        double xi[3], dN[8][3], N[8];
+        gauss_point(nd, q, xi);
+        shape_derivs(nd, xi, dN, N);
+        double J[3][3] = {{0}}, xg[3] = {0, 0, 0};
+        for (int a = 0; a < nen; ++a)
+            for (int i = 0; i < nd; ++i) {
+                xg[i] += N[a] * X[a * nd + i];
+                for (int j = 0; j < nd; ++j) J[i][j] += dN[a][i] * X[a * nd + j];
+            }
+        double det, Ji[3][3];
+        if (nd == 2) {
+            det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+            Ji[0][0] = J[1][1] / det; Ji[0][1] = -J[0][1] / det;
+            Ji[1][0] = -J[1][0] / det; Ji[1][1] = J[0][0] / det;
+        } else {
+            const double c00 = J[1][1] * J[2][2] - J[1][2] * J[2][1];
+            const double c01 = J[1][2] * J[2][0] - J[1][0] * J[2][2];
+            const double c02 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+            det = J[0][0] * c00 + J[0][1] * c01 + J[0][2] * c02;
+            Ji[0][0] = c00 / det;
+            Ji[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) / det;
+            Ji[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) / det;
+            Ji[1][0] = c01 / det;
+            Ji[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) / det;
+            Ji[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) / det;
+            Ji[2][0] = c02 / det;
+            Ji[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) / det;
+            Ji[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) / det;
+        }
+        double dx[8][3];
+        for (int a = 0; a < nen; ++a)
+            for (int j = 0; j < nd; ++j) {
+                double v = 0.0;
+                for (int i = 0; i < nd; ++i) v += Ji[j][i] * dN[a][i];
+                dx[a][j] = v;
+            }
+        const double D = std::fabs(det);
+        const double f = nd == 2 ? t * 1.0 * D : 1.0 * D;
+        double a[3] = {1, 1, 1}, b[3] = {0, 0, 0};
+        pml_stretch(nd, xg, par, rho, mu, lambda, a, b);
+        double sc[4], qd[4][3];
+        if (nd == 2) {
+            sc[0] = a[0] * a[1];                 qd[0][0] = 0.0;  qd[0][1] = 0.0;
+            sc[1] = a[0] * b[1] + a[1] * b[0];   qd[1][0] = a[1]; qd[1][1] = a[0];
+            sc[2] = b[0] * b[1];                 qd[2][0] = b[1]; qd[2][1] = b[0];
+            sc[3] = 0.0;                         qd[3][0] = 0.0;  qd[3][1] = 0.0;
+        } else {
+            sc[0] = a[0] * a[1] * a[2];
+            sc[1] = a[0] * a[1] * b[2] + a[0] * b[1] * a[2] + b[0] * a[1] * a[2];
+            sc[2] = a[0] * b[1] * b[2] + b[0] * b[1] * a[2] + b[0] * a[1] * b[2];
+            sc[3] = b[0] * b[1] * b[2];
+            qd[0][0] = qd[0][1] = qd[0][2] = 0.0;
+            qd[1][0] = a[1] * a[2]; qd[1][1] = a[0] * a[2]; qd[1][2] = a[0] * a[1];
+            qd[2][0] = a[1] * b[2] + a[2] * b[1]; qd[2][1] = a[0] * b[2] + a[2] * b[0]; qd[2][2] = a[0] * b[1] + a[1] * b[0];
+            qd[3][0] = b[1] * b[2]; qd[3][1] = b[0] * b[2]; qd[3][2] = b[0] * b[1];
+        }
+        for (int mi = 0; mi < 4; ++mi) {
+            double* Mx = out[mi];
+            if (!Mx || (nd == 2 && mi == 3)) continue;
+            const double s = sc[mi];
+            auto at = [&](int r, int c) -> double& { return Mx[(size_t)r * nc + c]; };
+            for (int j = 0; j < nen; ++j)
+                for (int k = 0; k < nen; ++k) {
+                    const double NN = N[j] * N[k] * f;
+                    if (nd == 2) {
+                        const int r = 5 * j, c = 5 * k;
+                        at(r, c) += rho * s * NN;
+                        at(r + 1, c + 1) += rho * s * NN;
+                        at(r + 2, c + 2) += -s * (lambda + 2.0 * mu) / 4.0 / mu / (lambda + mu) * NN;
+                        at(r + 3, c + 3) += -s * (lambda + 2.0 * mu) / 4.0 / mu / (lambda + mu) * NN;
+                        at(r + 4, c + 4) += -s / mu * NN;
+                        at(r + 2, c + 3) += s * lambda / 4.0 / mu / (lambda + mu) * NN;
+                        at(r + 3, c + 2) += s * lambda / 4.0 / mu / (lambda + mu) * NN;
+                        if (mi == 0) continue;
+                        const double qx = qd[mi][0], qy = qd[mi][1];
+                        at(r, c + 2) += qx * dx[j][0] * N[k] * f;
+                        at(r + 2, c) += qx * dx[k][0] * N[j] * f;
+                        at(r, c + 4) += qy * dx[j][1] * N[k] * f;
+                        at(r + 4, c) += qy * dx[k][1] * N[j] * f;
+                        at(r + 1, c + 3) += qy * dx[j][1] * N[k] * f;
+                        at(r + 3, c + 1) += qy * dx[k][1] * N[j] * f;
+                        at(r + 1, c + 4) += qx * dx[j][0] * N[k] * f;
+                        at(r + 4, c + 1) += qx * dx[k][0] * N[j] * f;
+                    } else {
+                        const int r = 9 * j, c = 9 * k;
+                        const double kap = s * (lambda + mu) / mu / (3.0 * lambda + 2.0 * mu);
+                        const double lam = s * lambda / 2.0 / mu / (3.0 * lambda + 2.0 * mu);
+                        for (int d = 0; d < 3; ++d) at(r + d, c + d) += rho * s * NN;
+                        for (int d = 3; d < 6; ++d) at(r + d, c + d) += -kap * NN;
+                        for (int d = 6; d < 9; ++d) at(r + d, c + d) += -s / mu * NN;
+                        at(r + 3, c + 4) += lam * NN; at(r + 3, c + 5) += lam * NN; at(r + 4, c + 5) += lam * NN;
+                        at(r + 4, c + 3) += lam * NN; at(r + 5, c + 3) += lam * NN; at(r + 5, c + 4) += lam * NN;
+                        if (mi == 0) continue;
+                        const double qx = qd[mi][0], qy = qd[mi][1], qz = qd[mi][2];
+                        // displacement rows x stress columns and the transposes
+                        const struct { int u, sg, dir; } cp[9] = {{0, 3, 0}, {0, 6, 1}, {0, 8, 2}, {1, 4, 1}, {1, 6, 0},
+                                                                  {1, 7, 2}, {2, 5, 2}, {2, 8, 0}, {2, 7, 1}};
+                        for (const auto& e : cp) {
+                            const double qv = e.dir == 0 ? qx : (e.dir == 1 ? qy : qz);
+                            at(r + e.u, c + e.sg) += dx[j][e.dir] * N[k] * qv * f;
+                            at(r + e.sg, c + e.u) += dx[k][e.dir] * N[j] * qv * f;
+                        }
+                    }
+                }
+        }
+    }
+}
+
 }  // namespace
 
 /* ---------------- C ABI of the oracle ------------------------------------ */
@@ -1033,6 +1183,14 @@ int oracle_lumped_mass(const svl_model_desc* model, double mtol, double* M) {
     std::vector<double> Md;
     s.assemble_mass_diag(Md);
     std::memcpy(M, Md.data(), sizeof(double) * Md.size());
+    return 0;
+}
+
+/* PML element matrices (row-major nc x nc; any output may be NULL). */
+int oracle_pml_matrices(int ndim, const double* X, double E, double nu, double rho, double t, const double* par,
+                        double* M, double* C, double* K, double* G) {
+    if (ndim != 2 && ndim != 3) return SVL_ERR_INVALID;
+    pml_matrices(ndim, X, E, nu, rho, t, par, M, C, K, G);
     return 0;
 }
 

@@ -162,6 +162,7 @@ def lib():
     L.svl_nm_nn_grids.argtypes = [C.c_void_p, f32p, f32p]
     L.svl_nm_nn_forward.argtypes = [C.c_void_p, f32p, f32p, C.c_int32]
     L.svl_nm_nn_set_path.argtypes = [C.c_void_p, C.c_int32]
+    L.svl_pml_element_action.argtypes = [C.c_int32, C.c_int32, f64p, f64p, f64p, f64p, f64p, f64p, f64p]
     L.svl_nm_destroy.argtypes = [C.c_void_p]
     L.svl_nm_destroy.restype = None
     _lib = L
