@@ -11,7 +11,7 @@ error against it is reported.  The PML layers of that configuration are not
 built yet; the box has fixed/roller faces instead (stated in the config).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--precision mixed|fp64] [--instances B] [--workload config2|config1]
+                    [--precision mixed|fp64] [--instances B] [--workload config2|config1|config3]
 
 value   : free DOF x instances x steps / device time of the K steps (CUDA
           events on the library's stream, inputs resident in HBM, working
@@ -40,6 +40,8 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 ALGO_BYTES_PER_DOF = {2: 40.0, 3: 37.0}
+# plane-strain J2 state read + written per element and step: 2 x 9 doubles x 4 Gauss points
+J2_STATE_BYTES_PER_ELEMENT = 576.0
 
 
 def measured_peaks():
@@ -106,6 +108,12 @@ class ClockSampler:
 
 def build_workload(name, seed=0):
     from svl_gb300 import workloads
+    if name == "config3":
+        m, L, dt, info = workloads.config3(seed=seed, nt=4001)
+        desc = ("ensemble of %d plane-strain J2 soil columns (lin2DQuad4, 10 wide, %d-%d elements high, h=0.5 m), "
+                "periodic sides, base support motion, CD; dt=%.3g (stable step)" %
+                (info["columns"], info["heights"][0], info["heights"][1], dt))
+        return m, L, dt, desc
     if name == "config1":
         m, L, dt = workloads.config1()
         desc = "lin2DQuad4 200x100 plane-strain box, CD"
@@ -171,6 +179,22 @@ def implicit_pcg(steps, warm=20, tol=1e-8):
             "rel_l2_final_u_learned_vs_jacobi": float(np.linalg.norm(Ul - Uj) / max(np.linalg.norm(Uj), 1e-300))}
 
 
+def implicit_profile():
+    from svl_gb300 import NewmarkBeta, workloads
+    from svl_gb300 import _capi as capi
+    m, L, dt = workloads.config4(nt=10)
+    nm = NewmarkBeta(m, L, dt, pcg_tol=1e-8)
+    nm.Initialize()
+    nm.run(1, 2)
+    w = (np.random.default_rng(0).standard_normal(capi.lib().svl_nn_num_weights()) * 0.02).astype(np.float32)
+    nm.nn_weights(w)
+    nm.set_preconditioner(capi.SVL_PRECOND_LEARNED)
+    nm.run(3, 1)
+    print(json.dumps({"implicit_profile": True, "pcg_iters_total": nm.stats()[0], "precond_stats": nm.precond_stats()}))
+    nm.close()
+    return 0
+
+
 NN_TRAIN = {"solve_steps": 0, "n_synthetic": 300, "iters": 1500, "batch": 8, "lr": 2e-3, "seed": 1, "max_sweeps": 5}
 
 
@@ -187,18 +211,26 @@ def main():
     ap.add_argument("--steps", type=int, default=400)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="config2", choices=["config1", "config2"])
+    ap.add_argument("--workload", default="config2", choices=["config1", "config2", "config3"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--instances", type=int, default=4)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64-compare", action="store_true")
-    ap.add_argument("--implicit-steps", type=int, default=10,
-                    help="Newmark steps of the 64^3 implicit workload timed beside the headline (0 = skip)")
+    ap.add_argument("--implicit-steps", type=int, default=None,
+                    help="Newmark steps of the 64^3 implicit workload timed beside the headline "
+                         "(default 10 with the default workload, else 0)")
+    ap.add_argument("--implicit-profile", action="store_true",
+                    help="profiling aid: 2 Jacobi-PCG steps and 1 flexible-CG step with a fixed untrained "
+                         "network on the 64^3 implicit workload, then exit (for an ncu launch list)")
     args = ap.parse_args()
+    if args.implicit_profile:
+        return implicit_profile()
+    if args.implicit_steps is None:
+        args.implicit_steps = 10 if args.workload == "config2" else 0
     ws, rank, local = dist_info()
     warm = max(3, args.warmup)
-    if args.workload == "config1":
+    if args.workload in ("config1", "config3"):
         args.precision = "fp64"
     nb = args.instances if args.precision == "mixed" else 1
 
@@ -228,7 +260,9 @@ def main():
         pg = dist
     capi.check(capi.lib().svl_set_device(local))
 
-    insts = [build_workload(args.workload, seed=b) for b in range(nb)]
+    # ensembles shard across ranks: every rank advances its own 256 columns (weak scaling)
+    seed0 = rank * 1000 if args.workload == "config3" else 0
+    insts = [build_workload(args.workload, seed=seed0 + b) for b in range(nb)]
     m, L, dt0, desc = insts[0]
     dt = min(x[2] for x in insts)
     nd = m.ndim
@@ -289,11 +323,13 @@ def main():
 
     peak, peak_kind = measured_peaks()
     algo_bytes = ALGO_BYTES_PER_DOF[nd] * nfree_total
+    if args.workload == "config3":
+        algo_bytes += J2_STATE_BYTES_PER_ELEMENT * m.nelem
     achieved = algo_bytes / (ms_step / 1e3) / 1e9
     if args.precision == "fp64":
         kernel_names = ["k_element", "k_node", "k_residual", "k_free", "k_update"]
         shares = {kernel_names[i]: round(float(prof[i] / max(prof.sum(), 1e-12)), 4) for i in range(5) if prof[i] > 0}
-        kname = "one FP64 CD step (k_element + k_node)"
+        kname = "one FP64 CD step (all its kernels)"
     else:
         shares = None
         kname = "k_cdx_step (fused mixed-precision step, all instances) + k_cdx_loads"

@@ -9,6 +9,15 @@ benchmark configurations (no reference data is used):
   double-couple-like body force (four element groups) with a Ricker
   f0 = 3 Hz, dt = 0.5 h / max Vp.  Boundary: fixed bottom, rollers on the
   sides (the PML layers of the configuration are not built yet).
+* config3: an ensemble of 2D plane-strain soil columns, 10 lin2DQuad4
+  elements wide, heights uniform in [50, 400] elements of 0.5 m (seeded),
+  PlasticPlaneStrainJ2 (G = rho Vs^2 with Vs uniform in [150, 500] m/s,
+  su uniform in [30, 120] kPa, Sy = sqrt(3) su, H = 0.02 G, beta = 1,
+  rho = 2000, nu = 0.3), periodic side nodes (EQUAL constraints), fixed base
+  driven by a horizontal support motion: band-limited (0.1-20 Hz) white-noise
+  acceleration scaled to a PGA uniform in [0.1, 0.5] g, integrated twice in
+  the frequency domain.  dt = min(5e-4, 0.5 h / max Vp): 5e-4 s exceeds the
+  explicit limit of the stiffest columns, so the stable step is used.
 * config4: 64 x 64 x 64 lin3DHexa8 box, h = 1 m, seeded piecewise-layered
   shear modulus (layer contrast up to 100x) times 10% log-normal noise per
   element, nu = 0.3, rho = 2000, Newmark average acceleration at
@@ -127,3 +136,55 @@ def config4(nx=64, ny=64, nz=64, nt=501, seed=0, amp=1.0e3, contrast=100.0, n_la
     L.add_body_load(m, [eid(cx + 1, cy, cz)], (0.0, amp, 0.0), s)
     L.add_body_load(m, [eid(cx - 1, cy, cz)], (0.0, -amp, 0.0), s)
     return m, L, dt
+
+
+def base_motion(nt, dt, f_lo, f_hi, pga, rng):
+    """Displacement whose second derivative is band-limited white noise with
+    peak |acceleration| = pga (spectral double integration, no drift)."""
+    n = int(2 ** np.ceil(np.log2(max(nt, 2))))
+    w = rng.standard_normal(n)
+    W = np.fft.rfft(w)
+    f = np.fft.rfftfreq(n, dt)
+    band = (f >= f_lo) & (f <= f_hi)
+    W[~band] = 0.0
+    acc = np.fft.irfft(W, n)[:nt]
+    acc *= pga / max(np.abs(acc).max(), 1e-300)
+    Wa = np.fft.rfft(np.concatenate([acc, np.zeros(n - nt)]))
+    om = 2 * np.pi * f
+    D = np.zeros_like(Wa)
+    D[band] = -Wa[band] / om[band] ** 2
+    return np.fft.irfft(D, n)[:nt]
+
+
+def config3(ncol=256, seed=0, nt=None, width=10, h=0.5, duration=20.0, hmin=50, hmax=400):
+    """Returns (model, loads, dt, info) of the whole ensemble as one model
+    (columns concatenated; instances never interact)."""
+    from .model import j2_params
+    rng = np.random.default_rng(seed)
+    rho, nu = 2000.0, 0.3
+    heights = rng.integers(hmin, hmax + 1, ncol)
+    vs = rng.uniform(150.0, 500.0, ncol)
+    su = rng.uniform(30e3, 120e3, ncol)
+    pga = rng.uniform(0.1, 0.5, ncol) * 9.81
+    vp = vs * np.sqrt(2 * (1 - nu) / (1 - 2 * nu))
+    dt = min(5e-4, 0.5 * h / vp.max())
+    if nt is None:
+        nt = int(round(duration / dt)) + 1
+    models = []
+    for c in range(ncol):
+        G = rho * vs[c] ** 2
+        K = 2 * G * (1 + nu) / (3 * (1 - 2 * nu))
+        m = Model.grid(2, (width, int(heights[c])), (h, h), fix_mask=(0, 0, 3, 0, 0, 0), periodic_x=True,
+                       mat_type=np.array([capi.SVL_MAT_PLASTICPLANESTRAINJ2], np.int32),
+                       mat_param=j2_params(K, G, rho, 0.02 * G, 1.0, np.sqrt(3.0) * su[c])[None, :])
+        models.append(m)
+    loads = []
+    for c, m in enumerate(models):
+        L = Loads()
+        s = L.add_series(base_motion(nt, dt, 0.1, 20.0, pga[c], rng))
+        for i in range(width + 1):
+            L.add_support_motion(m, i, 0, s)
+        loads.append(L)
+    info = {"columns": ncol, "elements": int(sum(x.nelem for x in models)), "dt": dt, "nt": nt,
+            "heights": [int(heights.min()), int(heights.max())]}
+    return Model.concat(models), Loads.concat(loads, models), dt, info
