@@ -118,6 +118,13 @@ typedef struct svl_load_desc {
     const double*  sm_factor;
 } svl_load_desc;
 
+/* ---- page-locked host memory ---------------------------------------------- */
+/* History buffers handed to the *_run calls are copied into with DMA; when
+ * they are page-locked the copies run at full link speed and overlap the
+ * stepping.  Returns NULL on failure.  No counterpart in the reference. */
+void* svl_host_alloc(size_t bytes);
+void  svl_host_free(void* p);
+
 /* ---- library info ------------------------------------------------------- */
 const char* svl_version(void);
 const char* svl_last_error(void);

@@ -61,7 +61,7 @@ def build_library(force: bool = False, verbose: bool = False) -> Path:
                 if verbose and out.strip():
                     print(out)
     if force or jobs or _stale(LIB, objs):
-        _run([NVCC, "-shared", *GENCODE, "-o", str(LIB), *map(str, objs), "-lcudart"])
+        _run([NVCC, "-shared", *GENCODE, "-o", str(LIB), *map(str, objs), "-lcudart", "-Xlinker", "-lpthread"])
     return LIB
 
 

@@ -144,6 +144,10 @@ def lib():
     L.svl_cd_run_noalloc.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p]
     L.svl_cd_destroy.argtypes = [C.c_void_p]
     L.svl_cd_destroy.restype = None
+    L.svl_host_alloc.argtypes = [C.c_size_t]
+    L.svl_host_alloc.restype = C.c_void_p
+    L.svl_host_free.argtypes = [C.c_void_p]
+    L.svl_host_free.restype = None
     L.svl_nm_create.argtypes = [C.POINTER(ModelDesc), C.POINTER(LoadDesc), C.POINTER(NmOpts), C.POINTER(C.c_void_p)]
     L.svl_nm_set_initial.argtypes = [C.c_void_p, f64p, f64p, f64p]
     L.svl_nm_run.argtypes = [C.c_void_p, C.c_int32, C.c_int32, f64p]
@@ -190,3 +194,27 @@ def as_f64(a):
 
 def as_i32(a):
     return np.ascontiguousarray(a, dtype=np.int32)
+
+
+class _Pinned:
+    def __init__(self, nbytes):
+        self.p = lib().svl_host_alloc(nbytes)
+        if not self.p:
+            raise SvlError(SVL_ERR_NOMEM, lib().svl_last_error().decode())
+
+    def __del__(self):
+        try:
+            lib().svl_host_free(self.p)
+        except Exception:
+            pass
+
+
+def pinned_empty(shape, dtype=np.float64):
+    """numpy array in page-locked host memory (svl_host_alloc); the memory is
+    released when the array and its views are gone."""
+    dtype = np.dtype(dtype)
+    n = int(np.prod(shape)) * dtype.itemsize
+    owner = _Pinned(max(n, 1))
+    buf = (C.c_char * max(n, 1)).from_address(owner.p)
+    buf._owner = owner
+    return np.frombuffer(buf, dtype=dtype, count=int(np.prod(shape))).reshape(shape)

@@ -349,8 +349,10 @@ struct svl_cd {
     int graph_steps = 0;
     int64_t launches = 0;
     int64_t launches_last = 0;
-    double* hist_dev = nullptr;
+    double* hist2[2] = {nullptr, nullptr};  // history chunks (run with a host history)
     int hist_cap = 0;
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t filled[2] = {nullptr, nullptr}, drained[2] = {nullptr, nullptr};
 
     template <typename T>
     int upload(const std::vector<T>& h, const T** out) {
@@ -376,7 +378,13 @@ struct svl_cd {
         if (graph) cudaGraphExecDestroy(graph);
         if (stream) cudaStreamSynchronize(stream);
         for (void* p : allocs) cudaFree(p);
-        if (hist_dev) cudaFree(hist_dev);
+        if (copy_stream) cudaStreamSynchronize(copy_stream);
+        for (int i = 0; i < 2; ++i) {
+            if (hist2[i]) cudaFree(hist2[i]);
+            if (filled[i]) cudaEventDestroy(filled[i]);
+            if (drained[i]) cudaEventDestroy(drained[i]);
+        }
+        if (copy_stream) cudaStreamDestroy(copy_stream);
         if (stream) cudaStreamDestroy(stream);
     }
 };
@@ -675,29 +683,53 @@ int svl_cd_run(svl_cd* cd, int32_t k_first, int32_t nsteps, double* U_hist) {
     const int64_t l0 = cd->launches;
     int kstart = k_first - 1;
     CUDA_TRY(cudaMemcpyAsync(cd->d.step, &kstart, sizeof(int), cudaMemcpyHostToDevice, cd->stream));
-    if (U_hist) {
-        // chunked device history, copied out as each chunk completes
+    if (U_hist && nsteps > 0) {
+        // two device history chunks: the copy of chunk c (copy stream)
+        // overlaps the stepping of chunk c + 1
         const int chunk = (int)std::max<int64_t>(1, std::min<int64_t>(nsteps, (int64_t)(256ll << 20) / ((int64_t)nt * 8)));
         if (cd->hist_cap < chunk) {
             CUDA_TRY(cudaStreamSynchronize(cd->stream));
-            if (cd->hist_dev) cudaFree(cd->hist_dev);
-            cd->hist_dev = nullptr;
+            if (cd->copy_stream) CUDA_TRY(cudaStreamSynchronize(cd->copy_stream));
+            for (int i = 0; i < 2; ++i) {
+                if (cd->hist2[i]) cudaFree(cd->hist2[i]);
+                cd->hist2[i] = nullptr;
+            }
             cd->hist_cap = 0;
-            if (cudaMalloc(&cd->hist_dev, (size_t)chunk * nt * sizeof(double)) != cudaSuccess) {
-                set_error("history buffer allocation failed"); return SVL_ERR_NOMEM;
+            for (int i = 0; i < 2; ++i)
+                if (cudaMalloc(&cd->hist2[i], (size_t)chunk * nt * sizeof(double)) != cudaSuccess) {
+                    set_error("history buffer allocation failed"); return SVL_ERR_NOMEM;
+                }
+            if (!cd->copy_stream) {
+                CUDA_TRY(cudaStreamCreateWithFlags(&cd->copy_stream, cudaStreamNonBlocking));
+                for (int i = 0; i < 2; ++i) {
+                    CUDA_TRY(cudaEventCreateWithFlags(&cd->filled[i], cudaEventDisableTiming));
+                    CUDA_TRY(cudaEventCreateWithFlags(&cd->drained[i], cudaEventDisableTiming));
+                    CUDA_TRY(cudaEventRecord(cd->drained[i], cd->copy_stream));
+                }
             }
             cd->hist_cap = chunk;
         }
-        for (int s0 = 0; s0 < nsteps; s0 += chunk) {
+        auto fill = [&](int s0, int slot) -> int {
             const int n = std::min(chunk, nsteps - s0);
+            CUDA_TRY(cudaStreamWaitEvent(cd->stream, cd->drained[slot], 0));
             for (int i = 0; i < n; ++i) {
                 TRY(cd_launch_step(cd));
-                CUDA_TRY(cudaMemcpyAsync(cd->hist_dev + (size_t)i * nt, cd->d.U, sizeof(double) * nt, cudaMemcpyDeviceToDevice, cd->stream));
+                CUDA_TRY(cudaMemcpyAsync(cd->hist2[slot] + (size_t)i * nt, cd->d.U, sizeof(double) * nt, cudaMemcpyDeviceToDevice, cd->stream));
             }
-            CUDA_TRY(cudaMemcpyAsync(U_hist + (size_t)s0 * nt, cd->hist_dev, sizeof(double) * nt * n, cudaMemcpyDeviceToHost, cd->stream));
-            CUDA_TRY(cudaStreamSynchronize(cd->stream));
+            CUDA_TRY(cudaEventRecord(cd->filled[slot], cd->stream));
+            return SVL_OK;
+        };
+        const int nch = (nsteps + chunk - 1) / chunk;
+        TRY(fill(0, 0));
+        for (int c = 0; c < nch; ++c) {
+            const int s0 = c * chunk, n = std::min(chunk, nsteps - s0), slot = c & 1;
+            if (c + 1 < nch) TRY(fill(s0 + chunk, slot ^ 1));
+            CUDA_TRY(cudaStreamWaitEvent(cd->copy_stream, cd->filled[slot], 0));
+            CUDA_TRY(cudaMemcpyAsync(U_hist + (size_t)s0 * nt, cd->hist2[slot], sizeof(double) * nt * n, cudaMemcpyDeviceToHost, cd->copy_stream));
+            CUDA_TRY(cudaEventRecord(cd->drained[slot], cd->copy_stream));
         }
-    } else {
+        CUDA_TRY(cudaStreamSynchronize(cd->copy_stream));
+    } else if (!U_hist) {
         // G steps per CUDA graph replay
         const int G = 16;
         if (!cd->graph && nsteps >= G) {
@@ -1757,6 +1789,19 @@ int svl_nm_nn_grids(svl_nm* nm, float* rho, float* mask) {
     if (!nm->lattice) { set_error("no learned preconditioner on this model"); return SVL_ERR_UNSUPPORTED; }
     if (!nm->nn) TRY(svl::nn_create(nm->lnx, nm->lny, nm->lnz, nm->gmap, nm->sdinv_h, nm->rho_h, nm->cd->stream, &nm->nn));
     return svl::nn_get_grids(nm->nn, rho, mask);
+}
+
+void* svl_host_alloc(size_t bytes) {
+    void* p = nullptr;
+    if (cudaHostAlloc(&p, std::max<size_t>(bytes, 1), cudaHostAllocDefault) != cudaSuccess) {
+        set_error("cudaHostAlloc of %zu bytes failed", bytes);
+        return nullptr;
+    }
+    return p;
+}
+
+void svl_host_free(void* p) {
+    if (p) cudaFreeHost(p);
 }
 
 int svl_nm_get(svl_nm* nm, int32_t which, double* out) {

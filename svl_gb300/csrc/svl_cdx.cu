@@ -565,6 +565,20 @@ __global__ void k_cdx_va(const float* nh, const float* nl, const float* ch, cons
     A[i] = inv_dt2 * (dU - u + up);
 }
 
+// FP64 total-dof displacement of every instance from the padded compensated
+// pairs: out[b][t] = hi + lo at the padded position of total dof t = node*3 + c.
+__global__ void k_cdx_hist(const float* __restrict__ uh, const float* __restrict__ ul, double* __restrict__ out,
+                           long long ntotal, int nxn, int nyn, int pitch, long long per, int ninst) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ntotal * ninst) return;
+    const long long b = i / ntotal, t = i - b * ntotal;
+    const long long n = t / 3;
+    const int c = (int)(t - n * 3);
+    const long long x = n % nxn, y = (n / nxn) % nyn, z = n / ((long long)nxn * nyn);
+    const long long p = b * per + (z * nyn + y) * pitch + x * 3 + c;
+    out[i] = (double)uh[p] + (double)ul[p];
+}
+
 float host_tf32(double x) {
     float f = (float)x;
     uint32_t b;
@@ -606,6 +620,11 @@ struct svl_cdx {
     int cur = 0;                         // index of u_n in uh/ul
     int64_t launches = 0, launches_last = 0;
     bool va_valid = false;
+    // history: two device chunks, filled on `stream`, drained on `copy_stream`
+    double* hist[2] = {nullptr, nullptr};
+    int hist_cap = 0;                    // steps per chunk
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t filled[2] = {nullptr, nullptr}, drained[2] = {nullptr, nullptr};
 
     template <typename T>
     int alloc(size_t n, T** out) {
@@ -625,7 +644,14 @@ struct svl_cdx {
     }
     ~svl_cdx() {
         if (stream) cudaStreamSynchronize(stream);
+        if (copy_stream) cudaStreamSynchronize(copy_stream);
         for (void* p : allocs) cudaFree(p);
+        for (int i = 0; i < 2; ++i) {
+            if (hist[i]) cudaFree(hist[i]);
+            if (filled[i]) cudaEventDestroy(filled[i]);
+            if (drained[i]) cudaEventDestroy(drained[i]);
+        }
+        if (copy_stream) cudaStreamDestroy(copy_stream);
         if (stream) cudaStreamDestroy(stream);
     }
 };
@@ -955,14 +981,71 @@ static int cdx_status(svl_cdx* h) {
     return SVL_OK;
 }
 
+// Enqueues steps [s0, s0 + n) of a run on the compute stream, writing each
+// step's FP64 fields into history chunk `slot`.
+static int cdx_fill_chunk(svl_cdx* h, int k_first, int s0, int n, int nsteps, int slot) {
+    const long long per_step = h->ntotal * h->ninst;
+    CUDA_TRY(cudaStreamWaitEvent(h->stream, h->drained[slot], 0));       // the chunk's previous copy is done
+    for (int i = 0; i < n; ++i) {
+        const int s = s0 + i;
+        TRY(cdx_step(h, k_first + s, s == nsteps - 1));
+        k_cdx_hist<<<(unsigned)((per_step + 255) / 256), 256, 0, h->stream>>>(
+            h->uh[h->cur], h->ul[h->cur], h->hist[slot] + (size_t)i * per_step, h->ntotal, h->nx + 1, h->ny + 1, h->pitch,
+            h->nstate / h->ninst, h->ninst);
+        ++h->launches;
+    }
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaEventRecord(h->filled[slot], h->stream));
+    return SVL_OK;
+}
+
 int svl_cdx_run(svl_cdx* h, int32_t k_first, int32_t nsteps, double* U_hist) {
     if (!h || nsteps < 0) { set_error("bad argument"); return SVL_ERR_INVALID; }
     const int64_t l0 = h->launches;
-    for (int s = 0; s < nsteps; ++s) {
-        TRY(cdx_step(h, k_first + s, s == nsteps - 1));
-        if (U_hist)
-            for (int b = 0; b < h->ninst; ++b)
-                TRY(fetch_pair(h, h->uh[h->cur], h->ul[h->cur], b, U_hist + ((size_t)s * h->ninst + b) * h->ntotal));
+    if (!U_hist) {
+        for (int s = 0; s < nsteps; ++s) TRY(cdx_step(h, k_first + s, s == nsteps - 1));
+    } else if (nsteps > 0) {
+        // device-side FP64 conversion into two chunk buffers; the copy of chunk
+        // c (on copy_stream) overlaps the computation of chunk c + 1
+        const long long per_step = h->ntotal * h->ninst;
+        const int chunk = (int)std::max<long long>(1, std::min<long long>(nsteps, (256ll << 20) / (per_step * 8)));
+        if (h->hist_cap < chunk) {
+            CUDA_TRY(cudaStreamSynchronize(h->stream));
+            if (h->copy_stream) CUDA_TRY(cudaStreamSynchronize(h->copy_stream));
+            for (int i = 0; i < 2; ++i) {
+                if (h->hist[i]) cudaFree(h->hist[i]);
+                h->hist[i] = nullptr;
+            }
+            h->hist_cap = 0;
+            for (int i = 0; i < 2; ++i)
+                if (cudaMalloc(&h->hist[i], (size_t)chunk * per_step * sizeof(double)) != cudaSuccess) {
+                    set_error("history buffer allocation failed");
+                    return SVL_ERR_NOMEM;
+                }
+            if (!h->copy_stream) {
+                CUDA_TRY(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
+                for (int i = 0; i < 2; ++i) {
+                    CUDA_TRY(cudaEventCreateWithFlags(&h->filled[i], cudaEventDisableTiming));
+                    CUDA_TRY(cudaEventCreateWithFlags(&h->drained[i], cudaEventDisableTiming));
+                    CUDA_TRY(cudaEventRecord(h->drained[i], h->copy_stream));
+                }
+            }
+            h->hist_cap = chunk;
+        }
+        const int nch = (nsteps + chunk - 1) / chunk;
+        TRY(cdx_fill_chunk(h, k_first, 0, std::min(chunk, nsteps), nsteps, 0));
+        for (int c = 0; c < nch; ++c) {
+            const int s0 = c * chunk, n = std::min(chunk, nsteps - s0), slot = c & 1;
+            if (c + 1 < nch) {
+                const int s1 = s0 + chunk;
+                TRY(cdx_fill_chunk(h, k_first, s1, std::min(chunk, nsteps - s1), nsteps, slot ^ 1));
+            }
+            CUDA_TRY(cudaStreamWaitEvent(h->copy_stream, h->filled[slot], 0));
+            CUDA_TRY(cudaMemcpyAsync(U_hist + (size_t)s0 * per_step, h->hist[slot], (size_t)n * per_step * sizeof(double),
+                                     cudaMemcpyDeviceToHost, h->copy_stream));
+            CUDA_TRY(cudaEventRecord(h->drained[slot], h->copy_stream));
+        }
+        CUDA_TRY(cudaStreamSynchronize(h->copy_stream));
     }
     h->va_valid = nsteps > 0;
     h->launches_last = h->launches - l0;

@@ -9,6 +9,9 @@
 #include <map>
 #include <utility>
 
+#include <functional>
+#include <thread>
+
 #include "svl_internal.hpp"
 
 namespace svl {
@@ -167,32 +170,52 @@ double gp_geometry(const HostModel& m, int e, int q, double dNx[8][3], double N[
     return det;
 }
 
+void parallel_for(int64_t n, const std::function<void(int64_t, int64_t)>& body) {
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    const int64_t nt = std::min<int64_t>(hw, std::max<int64_t>(1, n / 4096));
+    if (nt <= 1) { body(0, n); return; }
+    std::vector<std::thread> th;
+    for (int64_t i = 0; i < nt; ++i) th.emplace_back(body, n * i / nt, n * (i + 1) / nt);
+    for (auto& t : th) t.join();
+}
+
 void lumped_mass_diag(const HostModel& m, double mtol, std::vector<double>& M) {
     const int nd = m.ndim, nen = m.nen, nc = nen * m.ndof;
-    std::vector<double> Me_e(m.ntotal, 0.0);
-    std::vector<double> Me((size_t)nc * nc);
-    for (int e = 0; e < m.nelem; ++e) {
-        std::fill(Me.begin(), Me.end(), 0.0);
-        const double rho = m.param(e)[2];
-        for (int q = 0; q < m.ngp; ++q) {
-            double dNx[8][3], N[8];
-            const double det = gp_geometry(m, e, q, dNx, N);
-            const double c = nd == 2 ? 1.0 * rho * m.thick[e] * std::fabs(det) : 1.0 * rho * std::fabs(det);
-            for (int a = 0; a < nen; ++a)
+    // element diagonals in parallel, assembled afterwards in element order
+    std::vector<double> diag((size_t)m.nelem * nen * nd);
+    // The consistent mass of a displacement element is block diagonal in the
+    // components, Me[(a,j)][(b,j)] = sum_q c_q N_a N_b for every j, so the
+    // row-sum lumping (lin2DQuad4.cpp:272-282: the diagonal plus the row's
+    // other entries in ascending column order; the zero entries change
+    // nothing) is m_aa + sum_{b != a, ascending} m_ab, the same for every
+    // component -- the same operations in the same order as on the full matrix.
+    (void)nc;
+    parallel_for(m.nelem, [&](int64_t e0, int64_t e1) {
+        for (int64_t e = e0; e < e1; ++e) {
+            double mab[8][8] = {};
+            const double rho = m.param((int)e)[2];
+            for (int q = 0; q < m.ngp; ++q) {
+                double dNx[8][3], N[8];
+                const double det = gp_geometry(m, (int)e, q, dNx, N);
+                const double c = nd == 2 ? 1.0 * rho * m.thick[e] * std::fabs(det) : 1.0 * rho * std::fabs(det);
+                for (int a = 0; a < nen; ++a)
+                    for (int b = 0; b < nen; ++b) mab[a][b] += c * (N[a] * N[b]);
+            }
+            for (int a = 0; a < nen; ++a) {
+                double d = mab[a][a];
                 for (int b = 0; b < nen; ++b)
-                    for (int j = 0; j < nd; ++j) Me[(size_t)(a * nd + j) * nc + (b * nd + j)] += c * (N[a] * N[b]);
+                    if (b != a) d += mab[a][b];
+                for (int j = 0; j < nd; ++j) diag[((size_t)e * nen + a) * nd + j] = d;
+            }
         }
-        // row-sum lumping (lin2DQuad4.cpp:272-282)
-        for (int i = 0; i < nc; ++i)
-            for (int j = 0; j < nc; ++j)
-                if (i != j) { Me[(size_t)i * nc + i] += Me[(size_t)i * nc + j]; Me[(size_t)i * nc + j] = 0.0; }
+    });
+    std::vector<double> Me_e(m.ntotal, 0.0);
+    for (int e = 0; e < m.nelem; ++e)
         for (int a = 0; a < nen; ++a)
             for (int j = 0; j < nd; ++j) {
-                const int i = a * nd + j;
-                const double v = Me[(size_t)i * nc + i];
+                const double v = diag[((size_t)e * nen + a) * nd + j];
                 if (std::fabs(v) > mtol) Me_e[m.tdof[(size_t)m.conn[(size_t)e * nen + a] * m.ndof + j]] += v;
             }
-    }
     M.assign(m.ntotal, 0.0);
     for (int t = 0; t < m.ntotal; ++t) {
         double mn = 0.0;

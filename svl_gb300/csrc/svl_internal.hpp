@@ -2,6 +2,7 @@
 // units.  Not installed; the public interface is include/svl_gb300.h.
 #pragma once
 #include <cstdint>
+#include <functional>
 #include <string>
 #include <vector>
 
@@ -46,6 +47,9 @@ double gp_geometry(const HostModel& m, int e, int q, double dNx[8][3], double N[
 inline double gp_factor(const HostModel& m, int e, double det) {
     return m.ndim == 2 ? 1.0 * m.thick[e] * (det < 0 ? -det : det) : 1.0 * (det < 0 ? -det : det);
 }
+
+// body(begin, end) over [0, n) split across the host's hardware threads.
+void parallel_for(int64_t n, const std::function<void(int64_t, int64_t)>& body);
 
 // Diagonal of the assembled row-sum-lumped mass on total dofs.
 void lumped_mass_diag(const HostModel& m, double mtol, std::vector<double>& M);

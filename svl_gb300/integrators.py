@@ -50,8 +50,13 @@ class CentralDifference:
         return self._get(2)
 
     # -- batch interface -------------------------------------------------
-    def run(self, k_first: int, nsteps: int, history: bool = False):
-        hist = np.zeros((nsteps, self.ntotal)) if history else None
+    def run(self, k_first: int, nsteps: int, history: bool = False, out=None):
+        """Steps k_first .. k_first+nsteps-1; with history=True (or a
+        C-contiguous float64 `out` of shape [nsteps, ntotal], e.g. from
+        svl_gb300.pinned_empty) returns the displacement after every step."""
+        hist = out if out is not None else (np.zeros((nsteps, self.ntotal)) if history else None)
+        if hist is not None:
+            assert hist.shape == (nsteps, self.ntotal) and hist.dtype == np.float64 and hist.flags["C_CONTIGUOUS"]
         check(lib().svl_cd_run(self._h, int(k_first), int(nsteps), ptr(hist, C.c_double)))
         return hist
 
@@ -129,8 +134,12 @@ class StructuredCentralDifference:
         arrs = [None if a is None else capi.as_f64(a) for a in (U0, V0, A0)]
         check(lib().svl_cdx_set_initial(self._h, int(inst), *(ptr(a, C.c_double) for a in arrs)))
 
-    def run(self, k_first: int, nsteps: int, history: bool = False):
-        hist = np.zeros((nsteps, self.ninst, self.ntotal)) if history else None
+    def run(self, k_first: int, nsteps: int, history: bool = False, out=None):
+        """Steps of every instance; history (or `out`, float64 [nsteps, ninst,
+        ntotal], e.g. from svl_gb300.pinned_empty) receives all displacements."""
+        hist = out if out is not None else (np.zeros((nsteps, self.ninst, self.ntotal)) if history else None)
+        if hist is not None:
+            assert hist.shape == (nsteps, self.ninst, self.ntotal) and hist.dtype == np.float64 and hist.flags["C_CONTIGUOUS"]
         check(lib().svl_cdx_run(self._h, int(k_first), int(nsteps), ptr(hist, C.c_double)))
         return hist
 
