@@ -1,0 +1,276 @@
+"""Reader for SeismoVLAB partition files and writer for its node recorders.
+
+A partition file is what the SVL pre-processor writes for one process
+(`<run dir>/Partition/<name>.<combo>.<rank>.json`, PP/Core/SeismoVLAB.py
+createPartitions) and what the run-process parses (RP/12-Utilities/Driver.hpp
+UpdateMesh / UpdateMaterials / UpdateLoads / UpdateSupportMotion /
+UpdateConstraints, 392-1700, and the simulation block 1760-1840).  This module
+maps it onto the library's model and load descriptors so an unmodified
+pre-processed model runs on the GPU integrators, and writes node recorder
+output in the run-process's text format (RP/12-Utilities/Recorder.cpp:73-106
+header, 239-268 rows).
+
+Covered: lin2DQuad4 / lin3DHexa8 elements; Elastic2DPlaneStrain,
+Elastic3DLinear, PlasticPlaneStrainJ2, Plastic3DJ2 materials; restraints;
+EQUAL-type constraints; nodal masses; point loads and element body loads
+(constant or time series); support motions (constant or time series); node
+recorders of displacement, velocity or acceleration; CentralDifference and
+NewmarkBeta integrators.  Anything else raises PartitionError naming it.
+"""
+from __future__ import annotations
+
+import json
+from dataclasses import dataclass, field
+from pathlib import Path
+from typing import List, Optional
+
+import numpy as np
+
+from . import _capi as capi
+from .model import Loads, Model
+
+_ELEM = {"LIN2DQUAD4": (2, 4, capi.SVL_ELEM_LIN2DQUAD4), "LIN3DHEXA8": (3, 8, capi.SVL_ELEM_LIN3DHEXA8)}
+_MAT = {
+    "ELASTIC2DPLANESTRAIN": (capi.SVL_MAT_ELASTIC2DPLANESTRAIN, ("E", "nu", "rho")),
+    "ELASTIC3DLINEAR": (capi.SVL_MAT_ELASTIC3DLINEAR, ("E", "nu", "rho")),
+    "PLASTICPLANESTRAINJ2": (capi.SVL_MAT_PLASTICPLANESTRAINJ2, ("K", "G", "rho", "h", "beta", "Sy")),
+    "PLASTIC3DJ2": (capi.SVL_MAT_PLASTIC3DJ2, ("K", "G", "rho", "h", "beta", "Sy")),
+}
+
+
+class PartitionError(ValueError):
+    """The partition file uses something this path does not cover."""
+
+
+def read_series(path: Path) -> np.ndarray:
+    """Time-series file: first token the number of values, then the values
+    (Driver.hpp:1514-1527)."""
+    tok = path.read_text().split()
+    n = int(float(tok[0]))
+    vals = np.array([float(t) for t in tok[1:1 + n]], dtype=np.float64)
+    if vals.size != n:
+        raise PartitionError("%s: expected %d values, found %d" % (path, n, vals.size))
+    return vals
+
+
+@dataclass
+class Recorder:
+    name: str
+    file: str
+    response: str
+    ids: List[int]
+    precision: int
+    nsamp: int = 1
+
+
+@dataclass
+class Partition:
+    model: Model
+    loads: Loads
+    integrator: str
+    dt: float
+    nt: int
+    ftol: float
+    mtol: float
+    ktol: float
+    algorithm: dict
+    solver: dict
+    combo_folder: str
+    node_tags: np.ndarray
+    elem_tags: np.ndarray
+    recorders: List[Recorder] = field(default_factory=list)
+    root: Optional[Path] = None
+
+    def make_integrator(self, pcg_tol: Optional[float] = None):
+        """The GPU integrator the simulation block asks for (CentralDifference or
+        NewmarkBeta with the Linear algorithm); an iterative solver's `tol` is the
+        PCG tolerance, a direct solver gets 1e-12."""
+        from .integrators import CentralDifference, NewmarkBeta
+        if self.integrator == "CENTRALDIFFERENCE":
+            return CentralDifference(self.model, self.loads, self.dt, ftol=self.ftol, mtol=self.mtol)
+        if self.integrator in ("NEWMARKBETA", "EXTENDEDNEWMARKBETA"):
+            if self.algorithm.get("name", "LINEAR").upper() != "LINEAR":
+                raise PartitionError("algorithm %s is not covered (Linear only)" % self.algorithm.get("name"))
+            tol = pcg_tol if pcg_tol is not None else (float(self.solver.get("tol", 1e-12))
+                                                       if self.solver.get("name", "").upper() == "PETSC" else 1e-12)
+            return NewmarkBeta(self.model, self.loads, self.dt, pcg_tol=tol, ftol=self.ftol, mtol=self.mtol)
+        raise PartitionError("integrator %s is not covered" % self.integrator)
+
+    def run(self, write_recorders: bool = True, solution_dir: Optional[Path] = None):
+        """The run-process's dynamic loop (DynamicAnalysis.cpp:25-64): steps
+        k = 1 .. nt-1 and every node recorder written after each step.  Returns
+        the displacement history [nt-1][ntotal]."""
+        h = self.make_integrator()
+        h.Initialize()
+        nsteps = self.nt - 1
+        need_va = any(r.response in ("VEL", "ACCEL") for r in self.recorders)
+        if need_va:
+            U = np.zeros((nsteps, self.model.ntotal))
+            V = np.zeros_like(U)
+            A = np.zeros_like(U)
+            for s in range(nsteps):
+                if h.ComputeNewStep(s + 1):
+                    raise RuntimeError("A PROBLEM WAS ENCOUNTERED at step %d: %s"
+                                       % (s + 1, capi.lib().svl_last_error().decode()))
+                U[s], V[s], A[s] = h.GetDisplacements(), h.GetVelocities(), h.GetAccelerations()
+        else:
+            U = h.run(1, nsteps, history=True)
+            V = A = None
+        h.close()
+        if write_recorders and self.recorders:
+            out = Path(solution_dir) if solution_dir else (self.root / "Solution" / self.combo_folder)
+            out.mkdir(parents=True, exist_ok=True)
+            for r in self.recorders:
+                hist = {"DISP": U, "VEL": V, "ACCEL": A}[r.response]
+                write_node_recorder(out / r.file, self, r, hist)
+        return U
+
+
+def write_node_recorder(path: Path, part: Partition, rec: Recorder, hist: np.ndarray):
+    """Node recorder in the run-process's format: `n_nodes n_dofs ntotal nt`,
+    one `tag ndof totaldofs...` line per node, then one line per step with every
+    recorded dof in scientific notation with `precision` digits, each value
+    followed by a space (Recorder.cpp:73-106, 239-268)."""
+    m = part.model
+    pos = {int(t): i for i, t in enumerate(part.node_tags)}
+    idx = [pos[t] for t in rec.ids]
+    ndof = m.totaldof.shape[1]
+    fmt = "%." + str(int(rec.precision)) + "e "
+    cols = np.concatenate([m.totaldof[i] for i in idx]) if idx else np.zeros(0, np.int64)
+    with open(path, "w") as f:
+        f.write("%d %d %d %d\n" % (len(idx), ndof * len(idx), m.ntotal, part.nt))
+        for t, i in zip(rec.ids, idx):
+            f.write("%d %d %s\n" % (t, ndof, " ".join(str(int(d)) for d in m.totaldof[i])))
+        for row in hist[:, cols]:
+            f.write("".join(fmt % v for v in row) + "\n")
+
+
+def load_partition(path, run_dir=None) -> Partition:
+    """Parses one partition file.  Time-series files are looked up relative to
+    `run_dir` (default: the directory that holds the Partition folder, the
+    run-process's working directory)."""
+    path = Path(path)
+    d = json.loads(path.read_text())
+    root = Path(run_dir) if run_dir else (path.parent.parent if path.parent.name == "Partition" else path.parent)
+    g = d["Global"]
+    ndim = int(g["ndim"])
+    # nodes in ascending tag order (the run-process's std::map order)
+    ntags = sorted(int(t) for t in d["Nodes"])
+    nodes = [d["Nodes"][str(t)] for t in ntags]
+    ndofs = {int(n["ndof"]) for n in nodes}
+    if len(ndofs) != 1 or ndofs.pop() != ndim:
+        raise PartitionError("nodes with %s dofs: only %d-dof displacement nodes are covered" % (sorted({int(n['ndof']) for n in nodes}), ndim))
+    coords = np.array([n["coords"] for n in nodes], dtype=np.float64).reshape(len(nodes), ndim)
+    totaldof = np.array([n["totaldof"] for n in nodes], dtype=np.int32).reshape(len(nodes), ndim)
+    freedof = np.array([n["freedof"] for n in nodes], dtype=np.int32).reshape(len(nodes), ndim)
+    npos = {t: i for i, t in enumerate(ntags)}
+    # materials
+    mtags = sorted(int(t) for t in d.get("Materials", {}))
+    mpos = {t: i for i, t in enumerate(mtags)}
+    mat_type = np.zeros(len(mtags), np.int32)
+    mat_param = np.zeros((len(mtags), capi.SVL_MAT_NPARAM))
+    for i, t in enumerate(mtags):
+        mat = d["Materials"][str(t)]
+        name = mat["name"].upper()
+        if name not in _MAT:
+            raise PartitionError("material %s (tag %d) is not covered" % (mat["name"], t))
+        mat_type[i], keys = _MAT[name]
+        mat_param[i, :len(keys)] = [float(mat["attributes"][k]) for k in keys]
+    # elements in ascending tag order
+    etags = sorted(int(t) for t in d["Elements"])
+    els = [d["Elements"][str(t)] for t in etags]
+    names = {e["name"].upper() for e in els}
+    if len(names) != 1 or next(iter(names)) not in _ELEM:
+        raise PartitionError("element classes %s: one of %s per model is covered" % (sorted(names), sorted(_ELEM)))
+    edim, nen, etype = _ELEM[next(iter(names))]
+    if edim != ndim:
+        raise PartitionError("element dimension does not match Global.ndim")
+    conn = np.array([[npos[int(c)] for c in e["conn"]] for e in els], dtype=np.int32).reshape(len(els), nen)
+    elem_mat = np.array([mpos[int(e["attributes"]["material"])] for e in els], dtype=np.int32)
+    thick = np.array([float(e["attributes"].get("th", 1.0)) for e in els]) if ndim == 2 else None
+    # dampings: only the undamped case
+    for t, dm in d.get("Dampings", {}).items():
+        if dm["name"].upper() != "FREE":
+            raise PartitionError("damping %s (tag %s) is not covered" % (dm["name"], t))
+    # nodal masses
+    node_mass = None
+    if d.get("Masses"):
+        node_mass = np.zeros(int(g["ntotal"]))
+        for t, ms in d["Masses"].items():
+            i = npos[int(t)]
+            for k, v in enumerate(ms["mass"]):
+                node_mass[totaldof[i, k]] += float(v)
+    # constraints: slave total dof <- sum factor * master free dof
+    con = None
+    if d.get("Constraints"):
+        ctags = sorted((int(t) for t in d["Constraints"]), reverse=True)
+        cs, cp, cm, cf = [], [0], [], []
+        for t in ctags:
+            c = d["Constraints"][str(t)]
+            cs.append(int(c["stag"]))
+            cm += [int(x) for x in c["mtag"]]
+            cf += [float(x) for x in c["factor"]]
+            cp.append(len(cm))
+        con = (np.array(cs, np.int32), np.array(cp, np.int32), np.array(cm, np.int32), np.array(cf))
+    model = Model(ndim=ndim, coords=coords, totaldof=totaldof, freedof=freedof, conn=conn, elem_type=etype,
+                  elem_mat=elem_mat, mat_type=mat_type, mat_param=mat_param,
+                  lumped=str(g.get("massform", "CONSISTENT")).upper() == "LUMPED",
+                  thickness=thick, node_mass=node_mass)
+    if con is not None:
+        model.con_slave, model.con_ptr, model.con_master, model.con_factor = con
+    if model.ntotal != int(g["ntotal"]) or model.nfree != int(g["nfree"]):
+        raise PartitionError("Global ntotal/nfree do not match the nodes")
+    # simulation block
+    sim = d["Simulations"]
+    at = sim["attributes"]
+    integ = at["integrator"]
+    nt = int(at["analysis"]["nt"])
+    if at["analysis"]["name"].upper() != "DYNAMIC":
+        raise PartitionError("analysis %s is not covered" % at["analysis"]["name"])
+    combo = d["Combinations"][str(sim["combo"])]
+    loads = Loads()
+    epos = {t: i for i, t in enumerate(etags)}
+    for ltag, fac in zip(combo["attributes"]["load"], combo["attributes"]["factor"]):
+        ld = d["Loads"][str(ltag)]
+        la = ld["attributes"]
+        kind, fun = la["type"].upper(), la["name"].upper()
+        if fun == "TIMESERIES":
+            series = read_series(root / la["file"])
+        elif fun == "CONSTANT":
+            series = np.full(nt, float(la["mag"]))          # GetLoadVector() of a constant load: every step
+        else:
+            raise PartitionError("load function %s is not covered" % la["name"])
+        s = loads.add_series(series)
+        direction = [float(x) for x in la["dir"]]
+        if ld["name"].upper() == "POINTLOAD" and kind == "CONCENTRATED":
+            for ntag in la["list"]:
+                loads.add_point_load(model, npos[int(ntag)], direction, s, factor=float(fac))
+        elif ld["name"].upper() == "ELEMENTLOAD" and kind == "BODY":
+            loads.add_body_load(model, [epos[int(e)] for e in la["list"]], direction, s, factor=float(fac))
+        else:
+            raise PartitionError("load %s/%s (tag %s) is not covered" % (ld["name"], la["type"], ltag))
+    for ntag, sp in d.get("Supports", {}).items():
+        i = npos[int(ntag)]
+        for n, dof in enumerate(sp["dof"]):
+            if sp["type"].upper() == "TIMESERIES":
+                series = read_series(root / sp["file"][n])
+            elif sp["type"].upper() == "CONSTANT":
+                series = np.array([float(sp["value"][n])])
+            else:
+                raise PartitionError("support motion %s is not covered" % sp["type"])
+            loads.add_support_motion(model, i, int(dof), loads.add_series(series))
+    recs = []
+    for rtag in sorted(d.get("Recorders", {}), key=int):
+        r = d["Recorders"][rtag]
+        if r["name"].upper() != "NODE":
+            raise PartitionError("recorder %s is not covered (NODE only)" % r["name"])
+        resp = r["resp"].upper()
+        if resp not in ("DISP", "VEL", "ACCEL"):
+            raise PartitionError("node recorder response %s is not covered" % r["resp"])
+        recs.append(Recorder(name="NODE", file=r["file"], response=resp, ids=[int(x) for x in r["list"]],
+                             precision=int(r.get("ndps", 8)), nsamp=int(r.get("nsamp", 1))))
+    return Partition(model=model, loads=loads, integrator=integ["name"].upper(), dt=float(integ["dt"]), nt=nt,
+                     ftol=float(integ.get("ftol", 1e-12)), mtol=float(integ.get("mtol", 1e-12)),
+                     ktol=float(integ.get("ktol", 1e-12)), algorithm=at.get("algorithm", {}),
+                     solver=at.get("solver", {}), combo_folder=combo["attributes"].get("folder", combo["name"]),
+                     node_tags=np.array(ntags), elem_tags=np.array(etags), recorders=recs, root=root)

@@ -1,0 +1,196 @@
+"""Generate complete SVL partition files (and their time-series files) by
+running the SeismoVLAB pre-processor itself (PP/Core/SeismoVLAB.py
+CreateRunAnalysisFiles) on small models that exercise every field the
+partition reader maps: materials (elastic and J2), restraints, EQUAL
+constraints, point and element body loads (constant and time series),
+support motions, node recorders, the integrator/solver settings.
+
+Run from the repository root where the reference tree is available:
+    python tests/golden/make_partition_fixtures.py /path/to/SVL
+The reference imports matplotlib, which is not installed here; a stub module
+is written to a scratch folder for the subprocesses.  Outputs:
+tests/golden/partition_<case>/ with the partition JSON under Partition/ and
+the time-series files next to it (the run directory layout of the reference).
+"""
+from __future__ import annotations
+
+import json
+import os
+import shutil
+import subprocess
+import sys
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+
+COMMON = r'''
+import json, sys, math
+import numpy as np
+from Core import SeismoVLAB as SVL
+case = sys.argv[1]
+SVL.Options["file"] = "Fixture"
+SVL.Options["nparts"] = 1
+def ricker(nt, dt, f0, amp):
+    t0 = 1.2 / f0
+    out = []
+    for k in range(nt):
+        b = (math.pi * f0 * (k * dt - t0)) ** 2
+        out.append(amp * (1 - 2 * b) * math.exp(-b))
+    return out
+def write_series(name, vals):
+    with open(name, "w") as f:
+        f.write("%d\n" % len(vals))
+        for v in vals:
+            f.write("%.17g\n" % v)
+'''
+
+CASES = {
+    # Q4 elastic box, point load time series + constant point load, CD, node recorder
+    "q4_cd": COMMON + r'''
+SVL.Options["dimension"] = 2
+SVL.Options["massform"] = "lumped"
+nx, ny, dt, nt = 6, 4, 1.0e-3, 41
+SVL.addMaterial(tag=1, name="Elastic2DPlaneStrain", attributes={"E": 2.0e8, "nu": 0.25, "rho": 2000.0})
+SVL.addMaterial(tag=2, name="Elastic2DPlaneStrain", attributes={"E": 3.0e8, "nu": 0.30, "rho": 2100.0})
+mesh = SVL.makeDomainArea(options={"ne": [nx, ny], "ndof": 2, "class": "LIN2DQUAD4", "elems": "QUAD4",
+    "P0": [0.0, 0.0], "P1": [nx * 1.0, 0.0], "P2": [0.0, ny * 1.0],
+    "attributes": {"material": 1, "th": 1.0, "rule": "Gauss", "np": 4}})
+for tag in sorted(mesh["Nodes"]):
+    n = mesh["Nodes"][tag]
+    SVL.addNode(tag=tag, ndof=n["ndof"], coords=list(map(float, n["coords"])))
+for tag in sorted(mesh["Elements"]):
+    el = mesh["Elements"][tag]
+    at = dict(el["attributes"])
+    if tag % 3 == 0:
+        at["material"] = 2
+    SVL.addElement(tag=tag, conn=list(el["conn"]), name=el["name"], attributes=at)
+for tag in sorted(mesh["Nodes"]):
+    t = tag - 1; i = t % (nx + 1); j = t // (nx + 1)
+    if j == 0:
+        SVL.addRestrain(tag=tag, dof=[1, 2])
+    elif i == 0 or i == nx:
+        SVL.addRestrain(tag=tag, dof=1)
+write_series("ricker.txt", ricker(nt, dt, 25.0, 1.0e5))
+top = ny * (nx + 1) + nx // 2 + 1
+SVL.addFunction(tag=1, name="TimeSeries", attributes={"file": "ricker.txt", "dir": [0.0, -1.0]})
+SVL.addFunction(tag=2, name="Constant", attributes={"mag": 2.5e3, "dir": [1.0, 0.0]})
+SVL.addLoad(tag=1, name="PointLoad", attributes={"type": "Concentrated", "fun": 1, "list": [top]})
+SVL.addLoad(tag=2, name="PointLoad", attributes={"type": "Concentrated", "fun": 2, "list": [top - 1]})
+SVL.addCombinationCase(tag=1, name="Fixture", attributes={"load": [1, 2], "factor": [1.0, 0.5]})
+SVL.addRecorder(tag=1, attributes={"name": "NODE", "file": "Disp.out", "ndps": 8, "resp": "disp", "list": [top, top - 1]})
+SVL.addAnalysis(tag=1, attributes={"name": "Dynamic", "nt": nt})
+SVL.addAlgorithm(tag=1, attributes={"name": "Linear", "nstep": 1})
+SVL.addIntegrator(tag=1, attributes={"name": "CentralDifference", "dt": dt})
+SVL.addSolver(tag=1, attributes={"name": "Eigen", "update": "OFF"})
+SVL.addSimulation(tag=1, combo=1, attributes={"analysis": 1, "algorithm": 1, "integrator": 1, "solver": 1})
+SVL.CreateRunAnalysisFiles()
+''',
+    # H8 elastic box, element body load time series, Newmark + PETSc CG
+    "h8_newmark_body": COMMON + r'''
+SVL.Options["dimension"] = 3
+SVL.Options["massform"] = "lumped"
+nx, ny, nz, dt, nt = 3, 3, 2, 2.0e-3, 31
+SVL.addMaterial(tag=1, name="Elastic3DLinear", attributes={"E": 2.0e8, "nu": 0.3, "rho": 2000.0})
+mesh = SVL.makeDomainVolume(options={"ne": [nx, ny, nz], "ndof": 3, "class": "LIN3DHEXA8", "elems": "HEXA8",
+    "P0": [0.0, 0.0, 0.0], "P1": [nx * 2.0, 0.0, 0.0], "P2": [0.0, ny * 2.0, 0.0], "P3": [0.0, 0.0, nz * 2.0],
+    "attributes": {"material": 1, "rule": "Gauss", "np": 8}})
+for tag in sorted(mesh["Nodes"]):
+    n = mesh["Nodes"][tag]
+    SVL.addNode(tag=tag, ndof=n["ndof"], coords=list(map(float, n["coords"])))
+for tag in sorted(mesh["Elements"]):
+    el = mesh["Elements"][tag]
+    SVL.addElement(tag=tag, conn=list(el["conn"]), name=el["name"], attributes=dict(el["attributes"]))
+for tag in sorted(mesh["Nodes"]):
+    t = tag - 1; k = t // ((nx + 1) * (ny + 1))
+    if k == 0:
+        SVL.addRestrain(tag=tag, dof=[1, 2, 3])
+write_series("body.txt", ricker(nt, dt, 20.0, 1.0))
+SVL.addFunction(tag=1, name="TimeSeries", attributes={"file": "body.txt", "dir": [1.0, 0.0, 0.0]})
+SVL.addLoad(tag=1, name="ElementLoad", attributes={"type": "Body", "fun": 1, "list": [8, 11]})
+SVL.addCombinationCase(tag=1, name="Fixture", attributes={"load": [1], "factor": [2.0e3]})
+SVL.addRecorder(tag=1, attributes={"name": "NODE", "file": "Disp.out", "ndps": 10, "resp": "disp", "list": [40, 48]})
+SVL.addAnalysis(tag=1, attributes={"name": "Dynamic", "nt": nt})
+SVL.addAlgorithm(tag=1, attributes={"name": "Linear", "nstep": 1})
+SVL.addIntegrator(tag=1, attributes={"name": "NewmarkBeta", "dt": dt})
+SVL.addSolver(tag=1, attributes={"name": "Petsc", "option": "KSPCG", "tol": 1.0e-10})
+SVL.addSimulation(tag=1, combo=1, attributes={"analysis": 1, "algorithm": 1, "integrator": 1, "solver": 1})
+SVL.CreateRunAnalysisFiles()
+''',
+    # J2 soil column: periodic sides (EQUAL constraints), base support motion, CD
+    "q4_j2_column": COMMON + r'''
+SVL.Options["dimension"] = 2
+SVL.Options["massform"] = "lumped"
+nx, ny, h, dt, nt = 2, 6, 0.5, 2.0e-4, 61
+G = 2000.0 * 200.0 ** 2; K = 2 * G * 1.3 / (3 * 0.4)
+SVL.addMaterial(tag=1, name="PlasticPlaneStrainJ2", attributes={"K": K, "G": G, "rho": 2000.0, "h": 0.02 * G,
+                                                                 "beta": 1.0, "Sy": math.sqrt(3.0) * 40.0e3})
+mesh = SVL.makeDomainArea(options={"ne": [nx, ny], "ndof": 2, "class": "LIN2DQUAD4", "elems": "QUAD4",
+    "P0": [0.0, 0.0], "P1": [nx * h, 0.0], "P2": [0.0, ny * h],
+    "attributes": {"material": 1, "th": 1.0, "rule": "Gauss", "np": 4}})
+for tag in sorted(mesh["Nodes"]):
+    n = mesh["Nodes"][tag]
+    SVL.addNode(tag=tag, ndof=n["ndof"], coords=list(map(float, n["coords"])))
+for tag in sorted(mesh["Elements"]):
+    el = mesh["Elements"][tag]
+    SVL.addElement(tag=tag, conn=list(el["conn"]), name=el["name"], attributes=dict(el["attributes"]))
+base = [t for t in sorted(mesh["Nodes"]) if (t - 1) // (nx + 1) == 0]
+for tag in base:
+    SVL.addRestrain(tag=tag, dof=[1, 2])
+ctag = -2
+for tag in sorted(mesh["Nodes"]):
+    i = (tag - 1) % (nx + 1)
+    if i != nx or tag in base:
+        continue
+    for d in range(2):
+        SVL.addConstraint(tag=ctag, name="Equal", attributes={"stag": tag, "sdof": d + 1, "mtag": [tag - nx], "mdof": [d + 1]})
+        ctag -= 1
+motion = [0.02 * math.sin(2 * math.pi * 8.0 * k * dt) * (1 - math.exp(-k / 10.0)) for k in range(nt)]
+write_series("base.txt", motion)
+for tag in base:
+    SVL.addSupportMotion(tag=tag, attributes={"type": "TimeSeries", "file": "base.txt", "dof": 1})
+SVL.addFunction(tag=1, name="Constant", attributes={"mag": 0.0, "dir": [0.0, -1.0]})
+SVL.addLoad(tag=1, name="PointLoad", attributes={"type": "Concentrated", "fun": 1, "list": [max(mesh["Nodes"])]})
+SVL.addCombinationCase(tag=1, name="Fixture", attributes={"load": [1], "factor": [1.0]})
+SVL.addRecorder(tag=1, attributes={"name": "NODE", "file": "Top.out", "ndps": 8, "resp": "disp", "list": [max(mesh["Nodes"])]})
+SVL.addAnalysis(tag=1, attributes={"name": "Dynamic", "nt": nt})
+SVL.addAlgorithm(tag=1, attributes={"name": "Linear", "nstep": 1})
+SVL.addIntegrator(tag=1, attributes={"name": "CentralDifference", "dt": dt})
+SVL.addSolver(tag=1, attributes={"name": "Eigen", "update": "OFF"})
+SVL.addSimulation(tag=1, combo=1, attributes={"analysis": 1, "algorithm": 1, "integrator": 1, "solver": 1})
+SVL.CreateRunAnalysisFiles()
+''',
+}
+
+
+def main(ref_root: str):
+    pp = Path(ref_root) / "01-Pre_Process"
+    scratch = HERE / ".pp_scratch"
+    if scratch.exists():
+        shutil.rmtree(scratch)
+    stub = scratch / "stub" / "matplotlib"
+    stub.mkdir(parents=True)
+    (stub / "__init__.py").write_text("def use(*a, **k):\n    pass\n")
+    for mod in ("pyplot.py", "pylab.py"):
+        (stub / mod).write_text("def __getattr__(name):\n    return lambda *a, **k: None\n")
+    env = dict(os.environ, PYTHONPATH=os.pathsep.join([str(scratch / "stub"), str(pp)]))
+    for name, script in CASES.items():
+        work = scratch / name
+        work.mkdir(parents=True)
+        r = subprocess.run([sys.executable, "-c", script, name], cwd=work, env=env, capture_output=True, text=True,
+                           timeout=300)
+        if r.returncode != 0:
+            raise SystemExit("pre-processor failed for %s:\n%s\n%s" % (name, r.stdout, r.stderr))
+        out = HERE / ("partition_%s" % name)
+        if out.exists():
+            shutil.rmtree(out)
+        (out / "Partition").mkdir(parents=True)
+        for p in (work / "Partition").glob("*.json"):
+            shutil.copy(p, out / "Partition" / p.name)
+        for p in work.glob("*.txt"):
+            shutil.copy(p, out / p.name)
+        print("wrote", out.name, sorted(x.name for x in out.rglob("*") if x.is_file()))
+    shutil.rmtree(scratch)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

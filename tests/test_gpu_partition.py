@@ -1,0 +1,51 @@
+"""Pre-processed SVL models (partition files written by the SeismoVLAB
+pre-processor, tests/golden/partition_*) run end to end on the GPU through
+the partition reader, against the oracle, with the node recorders written in
+the run-process's format."""
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from svl_gb300.partition import load_partition
+from tests.helpers import rel_l2
+
+pytestmark = pytest.mark.gpu
+GOLD = Path(__file__).resolve().parent / "golden"
+
+
+def _part(case):
+    return load_partition(GOLD / ("partition_%s" % case) / "Partition" / "Fixture.1.0.json")
+
+
+def _read_recorder(path):
+    lines = path.read_text().splitlines()
+    nn, ndofs, ntotal, nt = map(int, lines[0].split())
+    head = [list(map(int, ln.split())) for ln in lines[1:1 + nn]]
+    rows = np.array([[float(v) for v in ln.split()] for ln in lines[1 + nn:]])
+    return (nn, ndofs, ntotal, nt), head, rows
+
+
+@pytest.mark.parametrize("case", ["q4_cd", "q4_j2_column"])
+def test_cd_partitions_match_oracle_and_record(gpu, case, tmp_path):
+    p = _part(case)
+    U = p.run(solution_dir=tmp_path)
+    ho, *_ = O.cd_run(p.model, p.loads, p.dt, p.nt - 1, mode=1)
+    assert np.abs(ho).max() > 0
+    assert rel_l2(U, ho) <= 1e-12
+    r = p.recorders[0]
+    (nn, ndofs, ntotal, nt), head, rows = _read_recorder(tmp_path / r.file)
+    assert (nn, ntotal, nt) == (len(r.ids), p.model.ntotal, p.nt) and rows.shape[0] == p.nt - 1
+    cols = [d for h in head for d in h[2:]]
+    assert [h[0] for h in head] == r.ids
+    assert np.allclose(rows, U[:, cols], rtol=10.0 ** -r.precision, atol=0)
+
+
+def test_newmark_partition_matches_oracle(gpu, tmp_path):
+    p = _part("h8_newmark_body")
+    U = p.run(solution_dir=tmp_path)
+    ho, _ = O.newmark_run(p.model, p.loads, p.dt, p.nt - 1, solver=0)
+    assert np.abs(ho).max() > 0
+    assert rel_l2(U, ho) <= 1e-8            # the file's PETSc tolerance is 1e-10
+    assert (tmp_path / p.recorders[0].file).exists()

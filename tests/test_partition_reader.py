@@ -1,0 +1,88 @@
+"""The partition-file reader against files written by the SeismoVLAB
+pre-processor itself (tests/golden/partition_*, made by
+tests/golden/make_partition_fixtures.py): numbering, materials, loads,
+constraints, support motions, recorders, and a short oracle run of each."""
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from svl_gb300 import _capi as capi
+from svl_gb300.partition import PartitionError, load_partition, read_series
+
+GOLD = Path(__file__).resolve().parent / "golden"
+
+
+def _part(case):
+    return GOLD / ("partition_%s" % case) / "Partition" / "Fixture.1.0.json"
+
+
+@pytest.mark.parametrize("case", ["q4_cd", "h8_newmark_body", "q4_j2_column"])
+def test_numbering_and_connectivity_follow_the_file(case):
+    p = load_partition(_part(case))
+    d = json.loads(_part(case).read_text())
+    tags = sorted(int(t) for t in d["Nodes"])
+    assert list(p.node_tags) == tags
+    assert np.array_equal(p.model.totaldof, np.array([d["Nodes"][str(t)]["totaldof"] for t in tags]))
+    assert np.array_equal(p.model.freedof, np.array([d["Nodes"][str(t)]["freedof"] for t in tags]))
+    for i, et in enumerate(sorted(int(t) for t in d["Elements"])):
+        assert [tags[j] for j in p.model.conn[i]] == d["Elements"][str(et)]["conn"]
+    assert p.model.ntotal == d["Global"]["ntotal"] and p.model.nfree == d["Global"]["nfree"]
+
+
+def test_q4_loads_materials_and_recorder():
+    p = load_partition(_part("q4_cd"))
+    assert p.integrator == "CENTRALDIFFERENCE" and p.dt == 1e-3 and p.nt == 41
+    assert set(p.model.mat_type) == {capi.SVL_MAT_ELASTIC2DPLANESTRAIN}
+    assert np.allclose(p.model.mat_param[1, :3], [3.0e8, 0.3, 2100.0])
+    ricker = read_series(GOLD / "partition_q4_cd" / "ricker.txt")
+    assert np.array_equal(p.loads.series[0], ricker)
+    assert np.array_equal(p.loads.series[1], np.full(41, 2500.0))   # constant load: every step
+    # point loads: the time series on dof y of node 32 (factor 1), the constant on x of node 31 (factor 0.5)
+    ty = int(p.model.totaldof[list(p.node_tags).index(32), 1])
+    tx = int(p.model.totaldof[list(p.node_tags).index(31), 0])
+    assert list(zip(p.loads.force_dof, p.loads.force_series, p.loads.force_coef)) == [(ty, 0, -1.0), (tx, 1, 0.5)]
+    r = p.recorders[0]
+    assert r.response == "DISP" and r.ids == [31, 32] and r.precision == 8 and r.file == "Disp.0.out"
+
+
+def test_h8_body_load_and_solver_settings():
+    p = load_partition(_part("h8_newmark_body"))
+    assert p.integrator == "NEWMARKBETA" and p.solver["name"] == "PETSC" and p.solver["tol"] == 1e-10
+    # body load entries sum to factor * rho * volume * series for each loaded element
+    coef = np.array(p.loads.force_coef)
+    assert np.isclose(coef.sum(), 2.0e3 * 2000.0 * 8.0 * 2)
+    assert all(s == 0 for s in p.loads.force_series)
+
+
+def test_j2_column_constraints_and_support_motion():
+    p = load_partition(_part("q4_j2_column"))
+    m = p.model
+    assert set(m.mat_type) == {capi.SVL_MAT_PLASTICPLANESTRAINJ2}
+    d = json.loads(_part("q4_j2_column").read_text())
+    assert m.nconstraint == len(d["Constraints"])
+    for t, c in d["Constraints"].items():
+        i = list(m.con_slave).index(c["stag"])
+        assert list(m.con_master[m.con_ptr[i]:m.con_ptr[i + 1]]) == c["mtag"]
+    base = read_series(GOLD / "partition_q4_j2_column" / "base.txt")
+    assert len(p.loads.sm_dof) == 3 and all(np.array_equal(p.loads.series[s], base) for s in p.loads.sm_series)
+
+
+@pytest.mark.parametrize("case", ["q4_cd", "q4_j2_column"])
+def test_oracle_runs_the_parsed_model(case):
+    p = load_partition(_part(case))
+    h, *_ = O.cd_run(p.model, p.loads, p.dt, p.nt - 1, mode=1)
+    assert np.all(np.isfinite(h)) and np.abs(h).max() > 0
+
+
+def test_uncovered_content_is_named(tmp_path):
+    d = json.loads(_part("q4_cd").read_text())
+    d["Dampings"]["1"]["name"] = "RAYLEIGH"
+    (tmp_path / "Partition").mkdir()
+    f = tmp_path / "Partition" / "x.json"
+    f.write_text(json.dumps(d))
+    (tmp_path / "ricker.txt").write_text((GOLD / "partition_q4_cd" / "ricker.txt").read_text())
+    with pytest.raises(PartitionError, match="RAYLEIGH"):
+        load_partition(f)
