@@ -272,8 +272,16 @@ void svl_cdx_destroy(svl_cdx* cdx);
  * element order, plus the lumped mass), in FP64, and stops on the TRUE
  * relative residual |Feff - Keff du| / |Feff| <= pcg_tol.  Dot products are
  * reduced in a fixed order: runs are bitwise reproducible.
- * Covered: elastic materials, lumped mass, no constraints, no support
- * motion; other models return SVL_ERR_UNSUPPORTED. */
+ * With SVL_ALGO_NEWTON the step iterates NewtonRaphson::ComputeNewIncrement:
+ * effective force from the current element states, a PCG solve with the
+ * consistent tangent (J2 elements: the tangent of their last return mapping,
+ * as Material::GetTangentStiffness returns it), the states updated from
+ * U + dU, until the chosen convergence test passes or `maxit` iterations.
+ * Covered: elastic materials (both algorithms), J2 materials (Newton),
+ * lumped mass, no constraints, no support motion; other models return
+ * SVL_ERR_UNSUPPORTED. */
+#define SVL_ALGO_LINEAR     0   /* Linear.cpp:22-56: one solve per step           */
+#define SVL_ALGO_NEWTON     1   /* NewtonRaphson.cpp:24-75: tangent iterations    */
 #define SVL_PRECOND_JACOBI  0
 #define SVL_PRECOND_LEARNED 1   /* see svl_nm_train_preconditioner                */
 typedef struct svl_nm_opts {
@@ -283,6 +291,14 @@ typedef struct svl_nm_opts {
     double  pcg_tol;     /* relative true-residual tolerance of each solve        */
     int32_t pcg_maxit;   /* iteration cap per solve (SVL_ERR_MAXITER past it)     */
     int32_t precond;     /* SVL_PRECOND_JACOBI or SVL_PRECOND_LEARNED             */
+    int32_t algorithm;   /* SVL_ALGO_LINEAR or SVL_ALGO_NEWTON                    */
+    int32_t maxit;       /* Newton: iterations per step (the algorithm's nstep)   */
+    double  cnvgtol;     /* Newton: convergence tolerance (cnvgtol; 0 = always
+                            `maxit` iterations)                                   */
+    int32_t cnvgtest;    /* Newton: 4 relative unbalanced force (the reference's
+                            default), 5 relative displacement increment
+                            (Algorithm.cpp:122-188)                               */
+    int32_t reserved;
 } svl_nm_opts;
 
 typedef struct svl_nm svl_nm;
@@ -299,6 +315,9 @@ int  svl_nm_get(svl_nm* nm, int32_t which, double* out);
 /* Conjugate-gradient iterations summed over all solves, of the last solve,
  * and the last solve's true relative residual. */
 int  svl_nm_stats(svl_nm* nm, int64_t* iters_total, int64_t* iters_last, double* rel_residual_last);
+/* Newton iterations over all steps, of the last step, and the last step's
+ * final convergence-test value. */
+int  svl_nm_newton_stats(svl_nm* nm, int64_t* iters_total, int64_t* iters_last, double* residual_last);
 int  svl_nm_launch_count(svl_nm* nm, int64_t* launches);
 int  svl_nm_sync(svl_nm* nm);
 void svl_nm_destroy(svl_nm* nm);

@@ -25,7 +25,7 @@ def lib():
         L.oracle_cd_run.argtypes = [vp, vp, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int, C.c_int,
                                     f64p, f64p, f64p, f64p, f64p, f64p, f64p, f64p]
         L.oracle_newmark_run.argtypes = [vp, vp, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double,
-                                         C.c_int, C.c_double, f64p, C.POINTER(C.c_long)]
+                                         C.c_int, C.c_double, f64p, C.POINTER(C.c_long), C.POINTER(C.c_int)]
         L.oracle_element_fint.argtypes = [vp, f64p, f64p]
         L.oracle_element_matrices.argtypes = [vp, C.c_int, f64p, f64p, f64p]
         L.oracle_body_force.argtypes = [vp, C.c_int, f64p, f64p]
@@ -66,14 +66,19 @@ def cd_run(model, loads, dt, nsteps, k_first=1, ftol=1e-12, mtol=1e-12, mode=0, 
     return hist, U, V, A
 
 
-def newmark_run(model, loads, dt, nsteps, k_first=1, algo=0, maxit=50, cnvgtol=1e-6, solver=0, pcg_tol=1e-12):
+def newmark_run(model, loads, dt, nsteps, k_first=1, algo=0, maxit=50, cnvgtol=1e-6, solver=0, pcg_tol=1e-12,
+                step_iters=None):
+    """algo 0 Linear, 1 Newton with test 5, 2 Newton with test 4; solver 0
+    dense LDL^T, 1 Jacobi-PCG.  step_iters (int32 [nsteps]) receives the
+    Newton iterations of every step."""
     md = model.desc()
     ld = loads.desc() if loads is not None else None
     hist = np.zeros((nsteps, model.ntotal))
     it = C.c_long(0)
+    si = None if step_iters is None else step_iters.ctypes.data_as(C.POINTER(C.c_int))
     st = lib().oracle_newmark_run(C.addressof(md), C.addressof(ld) if ld is not None else None, dt, k_first,
                                   nsteps, algo, maxit, cnvgtol, solver, pcg_tol,
-                                  hist.ctypes.data_as(C.POINTER(C.c_double)), C.byref(it))
+                                  hist.ctypes.data_as(C.POINTER(C.c_double)), C.byref(it), si)
     if st != 0:
         raise RuntimeError("oracle_newmark_run failed with status %d" % st)
     return hist, it.value

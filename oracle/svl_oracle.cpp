@@ -926,13 +926,20 @@ struct Newmark {
             }
             if (!solve(K, Feff, du)) return SVL_ERR_BREAKDOWN;
             for (int f = 0; f < nf; ++f) dUf[f] += du[f];
-            // convergence (Algorithm.cpp:122-188), test 5 = relative increment
+            // convergence (Algorithm.cpp:122-188): algo 1 = test 5 (relative
+            // displacement increment), algo 2 = test 4 (relative unbalanced
+            // force, the norm of the effective force this iteration solved for)
             double res = 0.0;
             if (algo == 1) {
                 double dn = 0, Dn = 0;
                 for (int f = 0; f < nf; ++f) { dn += du[f] * du[f]; Dn += dUf[f] * dUf[f]; }
                 dn = std::sqrt(dn); Dn = std::sqrt(Dn);
                 if (it == 0) { norm0 = Dn; res = dn; } else res = dn / norm0;
+            } else if (algo == 2) {
+                double fn = 0;
+                for (int f = 0; f < nf; ++f) fn += Feff[f] * Feff[f];
+                fn = std::sqrt(fn);
+                if (it == 0) { norm0 = fn; res = fn; } else res = fn / norm0;
             }
             s.T_apply(dUf, dUt);
             for (int t = 0; t < nt; ++t) Us[t] = U[t] + dUt[t];
@@ -947,10 +954,12 @@ struct Newmark {
                     V[t] = 2.0 / dt * d - V[t];
                 }
                 s.commit_all();
+                last_iters = it;
                 return 0;
             }
         }
     }
+    int last_iters = 0;
 };
 
 /* ---------------- PML elements (PML2DQuad4, PML3DHexa8) ------------------ */
@@ -1135,7 +1144,7 @@ int oracle_cd_run(const svl_model_desc* model, const svl_load_desc* loads, doubl
  * iterations and a dense LDL^T (solver 0) or Jacobi-PCG (solver 1) solve. */
 int oracle_newmark_run(const svl_model_desc* model, const svl_load_desc* loads, double dt,
                        int k_first, int nsteps, int algo, int maxit, double cnvgtol,
-                       int solver, double pcg_tol, double* hist_U, long* pcg_iters) {
+                       int solver, double pcg_tol, double* hist_U, long* pcg_iters, int* step_iters) {
     Newmark nm;
     if (!nm.init(model, loads, dt)) return SVL_ERR_INVALID;
     nm.solver = solver; nm.pcg_tol = pcg_tol;
@@ -1143,6 +1152,7 @@ int oracle_newmark_run(const svl_model_desc* model, const svl_load_desc* loads, 
     for (int i = 0; i < nsteps; ++i) {
         int st = nm.step(k_first + i, algo, maxit, cnvgtol);
         if (st) return st;
+        if (step_iters) step_iters[i] = nm.last_iters;
         if (hist_U) std::memcpy(hist_U + (size_t)i * nt, nm.U.data(), sizeof(double) * nt);
     }
     if (pcg_iters) *pcg_iters = nm.pcg_iters;

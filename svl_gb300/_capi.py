@@ -79,9 +79,14 @@ class CdOpts(C.Structure):
                 ("precision", C.c_int32), ("check_every", C.c_int32)]
 
 
+SVL_ALGO_LINEAR = 0
+SVL_ALGO_NEWTON = 1
+
+
 class NmOpts(C.Structure):
     _fields_ = [("dt", C.c_double), ("ftol", C.c_double), ("mtol", C.c_double), ("pcg_tol", C.c_double),
-                ("pcg_maxit", C.c_int32), ("precond", C.c_int32)]
+                ("pcg_maxit", C.c_int32), ("precond", C.c_int32), ("algorithm", C.c_int32), ("maxit", C.c_int32),
+                ("cnvgtol", C.c_double), ("cnvgtest", C.c_int32), ("reserved", C.c_int32)]
 
 
 class NnTrainOpts(C.Structure):
@@ -155,6 +160,7 @@ def lib():
     L.svl_nm_get.argtypes = [C.c_void_p, C.c_int32, f64p]
     L.svl_nm_stats.argtypes = [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_double)]
     L.svl_nm_launch_count.argtypes = [C.c_void_p, C.POINTER(C.c_int64)]
+    L.svl_nm_newton_stats.argtypes = [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_double)]
     L.svl_nm_sync.argtypes = [C.c_void_p]
     f32p = C.POINTER(C.c_float)
     L.svl_nm_train_preconditioner.argtypes = [C.c_void_p, C.c_int32, C.POINTER(NnTrainOpts), f32p]

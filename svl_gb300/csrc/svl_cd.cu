@@ -63,6 +63,8 @@ struct DevView {
     const int32_t* ekind;    // [E]             kMatElastic / kMatJ2
     const double* ecoef;     // [5][E]          c1,c2,c3 | K,G,H,beta,SY
     double* gstate;          // [13][ngp][E]    J2 state
+    double* ctan;            // [nt][ngp][E]    J2 consistent tangent of the last update, or null
+                             //                 (nt = 9: rows/cols 1,2,4 in 2D; 36 in 3D)
     double* fe;              // [nen*ndof][E]
     // nodes / dofs
     const int32_t* ntdof;    // [nnode][ndof]
@@ -111,8 +113,38 @@ __device__ __forceinline__ double sm_at(const DevView& d, int t, int k) {
 
 // J2 radial return on the tensor strain E[6] (shear = gamma/2), in place on
 // the Gauss-point state (PlasticPlaneStrainJ2.cpp:227-279, Plastic3DJ2.cpp:206-255).
+// Consistent tangent of the return mapping (PlasticPlaneStrainJ2.cpp:276,
+// Plastic3DJ2.cpp): K 1(x)1 + 2G Id for an elastic step, else
+// K 1(x)1 + 2G (Id - c1 n(x)n) - c2 (Id - n(x)n), c1 = 1/(1 + H/(3G)),
+// c2 = 4 G^2 dg / |xi|; Id = I - 1(x)1/3 with I = diag(1,1,1,1/2,1/2,1/2).
+// Stored entry by entry in [entry][ngp][E] order: 2D keeps rows/cols 1,2,4.
+template <int ND>
+__device__ __forceinline__ void j2_store_tangent(double* ct, size_t stride, double K, double G, bool plastic,
+                                                 const double n[6], double c1, double c2) {
+    constexpr int NS = ND == 2 ? 3 : 6;
+    const int ix[6] = {ND == 2 ? 1 : 0, ND == 2 ? 2 : 1, ND == 2 ? 4 : 2, 3, 4, 5};
+#pragma unroll
+    for (int a = 0; a < NS; ++a)
+#pragma unroll
+        for (int b = 0; b < NS; ++b) {
+            const int i = ix[a], j = ix[b];
+            const double D = (i < 3 && j < 3) ? 1.0 : 0.0;
+            const double I = (i == j) ? (i < 3 ? 1.0 : 0.5) : 0.0;
+            const double Id = I - 1.0 / 3.0 * D;
+            double v;
+            if (!plastic) v = K * D + 2.0 * G * Id;
+            else {
+                const double nn = n[i] * n[j];
+                v = K * D + 2.0 * G * (Id - c1 * nn) - c2 * (Id - nn);
+            }
+            ct[(size_t)(a * NS + b) * stride] = v;
+        }
+}
+
+template <int ND = 3>
 __device__ __forceinline__ void j2_return(const double E[6], double st[kJ2State], double K, double G,
-                                          double H, double beta, double SY, double sig6[6]) {
+                                          double H, double beta, double SY, double sig6[6],
+                                          double* ct = nullptr, size_t ct_stride = 0) {
     const double tr = E[0] + E[1] + E[2];
     double trial[6], rel[6];
 #pragma unroll
@@ -127,16 +159,23 @@ __device__ __forceinline__ void j2_return(const double E[6], double st[kJ2State]
     if (f <= 0) {
 #pragma unroll
         for (int i = 0; i < 6; ++i) sig6[i] = (i < 3 ? K * tr : 0.0) + trial[i];
+        if (ct) {
+            const double z[6] = {0, 0, 0, 0, 0, 0};
+            j2_store_tangent<ND>(ct, ct_stride, K, G, false, z, 0.0, 0.0);
+        }
     } else {
         const double dg = f / (2.0 * G + 2.0 / 3.0 * H);
         st[12] += sqrt(2.0 / 3.0) * dg;
+        double nv[6];
 #pragma unroll
         for (int i = 0; i < 6; ++i) {
             const double n = rel[i] / nrm;
+            nv[i] = n;
             st[6 + i] += 2.0 / 3.0 * (1.0 - beta) * H * dg * n;
             st[i] += dg * n;
             sig6[i] = (i < 3 ? K * tr : 0.0) + trial[i] - 2.0 * G * dg * n;
         }
+        if (ct) j2_store_tangent<ND>(ct, ct_stride, K, G, true, nv, 1.0 / (1.0 + H / G / 3.0), 4.0 * G * G * dg / nrm);
     }
 }
 
@@ -182,7 +221,8 @@ __global__ void __launch_bounds__(128) k_element(DevView d, const double* __rest
                 for (int i = 0; i < kJ2State; ++i) st[i] = gs[(size_t)i * ngp * E];
                 const double Ev[6] = {0.0, exx, eyy, 0.0, 0.5 * gxy, 0.0};
                 double s6[6];
-                j2_return(Ev, st, c1, c2, c3, d.ecoef[3 * (size_t)E + e], d.ecoef[4 * (size_t)E + e], s6);
+                j2_return<2>(Ev, st, c1, c2, c3, d.ecoef[3 * (size_t)E + e], d.ecoef[4 * (size_t)E + e], s6,
+                             d.ctan ? d.ctan + (size_t)q * E + e : nullptr, (size_t)ngp * E);
 #pragma unroll
                 for (int i = 0; i < kJ2State; ++i) gs[(size_t)i * ngp * E] = st[i];
                 sig[0] = s6[1]; sig[1] = s6[2]; sig[2] = s6[4];
@@ -215,7 +255,8 @@ __global__ void __launch_bounds__(128) k_element(DevView d, const double* __rest
 #pragma unroll
                 for (int i = 0; i < kJ2State; ++i) st[i] = gs[(size_t)i * ngp * E];
                 const double Ev[6] = {ev[0], ev[1], ev[2], 0.5 * ev[3], 0.5 * ev[4], 0.5 * ev[5]};
-                j2_return(Ev, st, c1, c2, c3, d.ecoef[3 * (size_t)E + e], d.ecoef[4 * (size_t)E + e], sig);
+                j2_return<3>(Ev, st, c1, c2, c3, d.ecoef[3 * (size_t)E + e], d.ecoef[4 * (size_t)E + e], sig,
+                             d.ctan ? d.ctan + (size_t)q * E + e : nullptr, (size_t)ngp * E);
 #pragma unroll
                 for (int i = 0; i < kJ2State; ++i) gs[(size_t)i * ngp * E] = st[i];
             }
@@ -233,6 +274,92 @@ __global__ void __launch_bounds__(128) k_element(DevView d, const double* __rest
         const double v = fe[j];
         d.fe[(size_t)j * E + e] = (fabs(v) > d.ftol) ? v : 0.0;
     }
+}
+
+// Tangent stiffness action q_e = sum_q w B^T C_t B p_e (element stiffness of
+// lin2DQuad4.cpp:289-318 / lin3DHexa8.cpp:289-318 with Material::GetTangentStiffness):
+// elastic elements from c1, c2, c3; J2 elements from the tangent stored at
+// their last update (2D: rows/cols 1,2,4 of the 6x6 tensor-strain tangent
+// applied to the engineering strain, as the reference assembles it).  Writes
+// the unfiltered element vectors into d.fe (an operator scratch block).
+template <int ND, int NEN>
+__global__ void __launch_bounds__(128) k_element_tan(DevView d, const double* __restrict__ P, int ngp) {
+    constexpr int NC = ND * NEN;
+    constexpr int PER = NEN * ND + 1;
+    constexpr int NS = ND == 2 ? 3 : 6;
+    const int E = d.nelem;
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= E) return;
+    double ue[NC], fe[NC];
+#pragma unroll
+    for (int j = 0; j < NC; ++j) { ue[j] = P[d.edof[(size_t)j * E + e]]; fe[j] = 0.0; }
+    const int kind = d.ekind[e];
+    const double* g0 = d.geo + (size_t)d.egeo[e] * ngp * PER;
+    const double c1 = d.ecoef[e], c2 = d.ecoef[(size_t)E + e], c3 = d.ecoef[2 * (size_t)E + e];
+    for (int q = 0; q < ngp; ++q) {
+        const double* g = g0 + q * PER;
+        double b[NEN][3];
+#pragma unroll
+        for (int a = 0; a < NEN; ++a)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) b[a][j] = (j < ND) ? __ldg(g + a * ND + j) : 0.0;
+        const double w = __ldg(g + PER - 1);
+        double ev[NS], sig[NS];
+#pragma unroll
+        for (int i = 0; i < NS; ++i) ev[i] = 0.0;
+#pragma unroll
+        for (int a = 0; a < NEN; ++a) {
+            if (ND == 2) {
+                ev[0] += b[a][0] * ue[2 * a];
+                ev[1] += b[a][1] * ue[2 * a + 1];
+                ev[2] += b[a][1] * ue[2 * a] + b[a][0] * ue[2 * a + 1];
+            } else {
+                const double ux = ue[3 * a], uy = ue[3 * a + 1], uz = ue[3 * a + 2];
+                ev[0] += b[a][0] * ux;
+                ev[1] += b[a][1] * uy;
+                ev[2] += b[a][2] * uz;
+                ev[3 % NS] += b[a][1] * ux + b[a][0] * uy;
+                ev[4 % NS] += b[a][2] * uy + b[a][1] * uz;
+                ev[5 % NS] += b[a][2] * ux + b[a][0] * uz;
+            }
+        }
+        if (kind == kMatElastic) {
+            if (ND == 2) {
+                sig[0] = c1 * ev[0] + c2 * ev[1];
+                sig[1] = c2 * ev[0] + c1 * ev[1];
+                sig[2] = c3 * ev[2];
+            } else {
+                sig[0] = c1 * ev[0] + c2 * ev[1] + c2 * ev[2];
+                sig[1] = c2 * ev[0] + c1 * ev[1] + c2 * ev[2];
+                sig[2] = c2 * ev[0] + c2 * ev[1] + c1 * ev[2];
+                sig[3 % NS] = c3 * ev[3 % NS]; sig[4 % NS] = c3 * ev[4 % NS]; sig[5 % NS] = c3 * ev[5 % NS];
+            }
+        } else {
+            const double* ct = d.ctan + (size_t)q * E + e;
+            const size_t st = (size_t)ngp * E;
+#pragma unroll
+            for (int a = 0; a < NS; ++a) {
+                double v = 0.0;
+#pragma unroll
+                for (int bb = 0; bb < NS; ++bb) v += ct[(size_t)(a * NS + bb) * st] * ev[bb];
+                sig[a] = v;
+            }
+        }
+#pragma unroll
+        for (int a = 0; a < NEN; ++a) {
+            if (ND == 2) {
+                fe[2 * a] += w * (b[a][0] * sig[0] + b[a][1] * sig[2]);
+                fe[2 * a + 1] += w * (b[a][1] * sig[1] + b[a][0] * sig[2]);
+            } else {
+                const double bx = b[a][0], by = b[a][1], bz = b[a][2];
+                fe[3 * a] += w * (bx * sig[0] + by * sig[3 % NS] + bz * sig[5 % NS]);
+                fe[3 * a + 1] += w * (by * sig[1] + bx * sig[3 % NS] + bz * sig[4 % NS]);
+                fe[3 * a + 2] += w * (bz * sig[2] + by * sig[4 % NS] + bx * sig[5 % NS]);
+            }
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < NC; ++j) d.fe[(size_t)j * E + e] = fe[j];
 }
 
 template <int ND>
@@ -989,7 +1116,8 @@ enum { S_RZ = 0, S_PQ = 1, S_RR = 2, S_BB = 3, S_RZN = 4, S_NSCAL = 8 };
 
 // Effective force per node (identity T): b_f = (Fext - Fint) + M (4/dt V + A)
 template <int ND>
-__global__ void __launch_bounds__(256) k_nm_rhs(DevView d, double* __restrict__ b, double c_v) {
+__global__ void __launch_bounds__(256) k_nm_rhs(DevView d, double* __restrict__ b, double c_v,
+                                                const double* __restrict__ dUf, double c_m) {
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= d.nnode) return;
     const int k = d.step[0];
@@ -1000,8 +1128,23 @@ __global__ void __launch_bounds__(256) k_nm_rhs(DevView d, double* __restrict__ 
         if (f < 0) continue;
         const double fint = gather_fint<ND>(d, n, c);
         const double fext = fext_at(d, t, k);
-        b[f] = ((fext + 0.0) - fint) + d.Md[t] * (c_v * d.V[t] + d.A[t]);
+        // Fext - Fint + M (4/dt V + A - 4/dt^2 dU)   (NewmarkBeta.cpp:215, C = 0)
+        const double w = dUf ? (c_v * d.V[t] + d.A[t]) - c_m * dUf[f] : c_v * d.V[t] + d.A[t];
+        b[f] = ((fext + 0.0) - fint) + d.Md[t] * w;
     }
+}
+
+// Us = U + dU on total dofs (identity T) for the state update of a Newton iteration
+__global__ void k_nm_us(DevView d, const double* __restrict__ dUf) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= d.ntotal) return;
+    const int f = d.tfree[t];
+    d.Us[t] = d.U[t] + (f >= 0 ? dUf[f] : 0.0);
+}
+
+__global__ void k_axpy1(double* __restrict__ y, const double* __restrict__ x, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) y[i] += x[i];
 }
 
 // q = Keff p: scatter p to total dofs (free part), element stiffness action done by
@@ -1188,6 +1331,12 @@ struct svl_nm {
     int precond = SVL_PRECOND_JACOBI;
     int64_t jac_ref = 0, fallbacks = 0, learned_solves = 0;
     int64_t train_trial_iters = 0;          // trial-solve iterations of the kept weights
+    // Newton: operator scratch block, accumulated increment, iteration counts
+    double* fe_op = nullptr;                // [nc][E] element vectors of the operator action
+    double* dUf = nullptr;                  // [nfree] displacement increment of the step
+    bool newton = false, tangent = false;   // tangent: J2 elements present (stored tangents)
+    int64_t newton_iters_total = 0, newton_iters_last = 0;
+    double newton_res_last = 0.0;
     // CG iterates recorded for training pairs
     int rec_every = 0, rec_n = 0;
     std::vector<double*> rec_x, rec_r;
@@ -1224,11 +1373,17 @@ static int nm_apply(svl_nm* nm, const double* v, double* q) {
     const HostModel& m = cd->m;
     DevView d = cd->d;
     d.ftol = -1.0;                  // the operator action is not filtered
+    d.fe = nm->fe_op;               // and keeps the state's element forces intact
     const int tb = 256;
     k_nm_expand<<<(m.ntotal + tb - 1) / tb, tb, 0, cd->stream>>>(d, v, nm->pt);
     const int eg = (m.nelem + 127) / 128;
-    if (m.ndim == 2) k_element<2, 4><<<eg, 128, 0, cd->stream>>>(d, nm->pt, m.ngp, 0);
-    else k_element<3, 8><<<eg, 128, 0, cd->stream>>>(d, nm->pt, m.ngp, 0);
+    if (nm->tangent) {
+        if (m.ndim == 2) k_element_tan<2, 4><<<eg, 128, 0, cd->stream>>>(d, nm->pt, m.ngp);
+        else k_element_tan<3, 8><<<eg, 128, 0, cd->stream>>>(d, nm->pt, m.ngp);
+    } else {
+        if (m.ndim == 2) k_element<2, 4><<<eg, 128, 0, cd->stream>>>(d, nm->pt, m.ngp, 0);
+        else k_element<3, 8><<<eg, 128, 0, cd->stream>>>(d, nm->pt, m.ngp, 0);
+    }
     const double c_m = 4.0 / nm->opts.dt / nm->opts.dt;
     if (m.ndim == 2) k_nm_apply<2><<<(m.nnode + tb - 1) / tb, tb, 0, cd->stream>>>(d, nm->pt, q, c_m);
     else k_nm_apply<3><<<(m.nnode + tb - 1) / tb, tb, 0, cd->stream>>>(d, nm->pt, q, c_m);
@@ -1443,15 +1598,30 @@ int svl_nm_create(const svl_model_desc* model, const svl_load_desc* loads, const
     const HostModel& m = cd->m;
     if (!cd->identity_T) { set_error("the implicit path does not take constraints yet"); return fail(SVL_ERR_UNSUPPORTED); }
     if (cd->has_sm) { set_error("the implicit path does not take support motion yet"); return fail(SVL_ERR_UNSUPPORTED); }
-    if (m.has_j2()) { set_error("the implicit Linear path is elastic; J2 needs Newton iterations"); return fail(SVL_ERR_UNSUPPORTED); }
+    if (opts->algorithm != SVL_ALGO_LINEAR && opts->algorithm != SVL_ALGO_NEWTON) { set_error("unknown algorithm %d", opts->algorithm); return fail(SVL_ERR_INVALID); }
+    nm->newton = opts->algorithm == SVL_ALGO_NEWTON;
+    if (nm->newton && (opts->maxit <= 0 || !(opts->cnvgtol >= 0.0) || (opts->cnvgtest != 4 && opts->cnvgtest != 5))) {
+        set_error("Newton needs maxit > 0, cnvgtol >= 0 (0: always maxit iterations) and cnvgtest 4 or 5");
+        return fail(SVL_ERR_INVALID);
+    }
+    if (m.has_j2() && !nm->newton) { set_error("the implicit Linear path is elastic; J2 needs Newton iterations"); return fail(SVL_ERR_UNSUPPORTED); }
+    nm->tangent = nm->newton && m.has_j2();
     nm->nf = m.nfree;
     // Jacobi diagonal: diag(K) + 4/dt^2 M on free dofs (identity T)
     std::vector<double> Kd(m.ntotal, 0.0);
     const int nc = m.nen * m.ndof;
     for (int e = 0; e < m.nelem; ++e) {
         const double* pr = m.param(e);
-        const double E = pr[0], nu = pr[1];
-        const double c1 = E * (1.0 - nu) / (1.0 - 2.0 * nu) / (1.0 + nu), c3 = E / (2.0 * (1.0 + nu));
+        const int mt = m.mat_type(e);
+        double c1, c3;
+        if (mt == SVL_MAT_ELASTIC2DPLANESTRAIN || mt == SVL_MAT_ELASTIC3DLINEAR) {
+            const double E = pr[0], nu = pr[1];
+            c1 = E * (1.0 - nu) / (1.0 - 2.0 * nu) / (1.0 + nu);
+            c3 = E / (2.0 * (1.0 + nu));
+        } else {                    // J2: the elastic moduli K, G
+            c1 = pr[0] + 4.0 / 3.0 * pr[1];
+            c3 = pr[1];
+        }
         std::vector<double> kd(nc, 0.0);
         for (int q = 0; q < m.ngp; ++q) {
             double dNx[8][3], N[8];
@@ -1488,6 +1658,13 @@ int svl_nm_create(const svl_model_desc* model, const svl_load_desc* loads, const
     const double* dd = nullptr;
     if ((st = cd->upload(dinv, &dd))) return fail(st);
     nm->dinv = const_cast<double*>(dd);
+    if ((st = cd->zeros((size_t)nc * m.nelem, &nm->fe_op)) || (st = cd->zeros((size_t)std::max(m.nfree, 1), &nm->dUf)))
+        return fail(st);
+    if (nm->tangent) {
+        double* ct = nullptr;
+        if ((st = cd->zeros((size_t)(m.ndim == 2 ? 9 : 36) * m.ngp * m.nelem, &ct))) return fail(st);
+        cd->d.ctan = ct;
+    }
     // lattice models: the maps and scalings of the learned preconditioner
     int dims[3];
     std::vector<int32_t> cell;
@@ -1529,6 +1706,15 @@ int svl_nm_set_initial(svl_nm* nm, const double* U0, const double* V0, const dou
     TRY(svl_cd_set_initial(nm->cd, U0, V0, A0));
     // strain displacement = U0 for an elastic start from given displacements
     if (U0) CUDA_TRY(cudaMemcpyAsync(nm->cd->d.Us, nm->cd->d.U, sizeof(double) * nm->cd->m.ntotal, cudaMemcpyDeviceToDevice, nm->cd->stream));
+    if (nm->newton) {
+        // element states, forces and tangents of the initial displacement
+        svl_cd* cd = nm->cd;
+        const HostModel& m = cd->m;
+        const int eg = (m.nelem + 127) / 128;
+        if (m.ndim == 2) k_element<2, 4><<<eg, 128, 0, cd->stream>>>(cd->d, cd->d.Us, m.ngp, 0);
+        else k_element<3, 8><<<eg, 128, 0, cd->stream>>>(cd->d, cd->d.Us, m.ngp, 0);
+        CUDA_TRY(cudaGetLastError());
+    }
     CUDA_TRY(cudaStreamSynchronize(nm->cd->stream));
     return SVL_OK;
 }
@@ -1546,8 +1732,8 @@ static int nm_rhs(svl_nm* nm, int k) {
     k_step_inc<<<1, 1, 0, cd->stream>>>(cd->d.step);
     if (m.ndim == 2) k_element<2, 4><<<eg, 128, 0, cd->stream>>>(cd->d, cd->d.Us, m.ngp, 0);
     else k_element<3, 8><<<eg, 128, 0, cd->stream>>>(cd->d, cd->d.Us, m.ngp, 0);
-    if (m.ndim == 2) k_nm_rhs<2><<<ng, tb, 0, cd->stream>>>(cd->d, nm->b, 4.0 / dt);
-    else k_nm_rhs<3><<<ng, tb, 0, cd->stream>>>(cd->d, nm->b, 4.0 / dt);
+    if (m.ndim == 2) k_nm_rhs<2><<<ng, tb, 0, cd->stream>>>(cd->d, nm->b, 4.0 / dt, nullptr, 0.0);
+    else k_nm_rhs<3><<<ng, tb, 0, cd->stream>>>(cd->d, nm->b, 4.0 / dt, nullptr, 0.0);
     CUDA_TRY(cudaGetLastError());
     return SVL_OK;
 }
@@ -1587,8 +1773,63 @@ static int64_t nm_trial(svl_nm* nm, int k) {
     return score;
 }
 
+// One NewtonRaphson step (NewtonRaphson.cpp:24-75 with NewmarkBeta's effective
+// force and stiffness): iterate Feff(current states, dU) -> tangent solve ->
+// dU += du -> convergence test -> state update from U + dU.
+static int nm_step_newton(svl_nm* nm, double* U_hist_row) {
+    svl_cd* cd = nm->cd;
+    const HostModel& m = cd->m;
+    const double dt = nm->opts.dt;
+    const int tb = 256, ng = (m.nnode + tb - 1) / tb, eg = (m.nelem + 127) / 128, n = nm->nf;
+    const int gf = (n + tb - 1) / tb, gt = (m.ntotal + tb - 1) / tb;
+    double hs[S_NSCAL];
+    k_step_inc<<<1, 1, 0, cd->stream>>>(cd->d.step);
+    CUDA_TRY(cudaMemsetAsync(nm->dUf, 0, sizeof(double) * std::max(n, 1), cd->stream));
+    double norm0 = 0.0, res = 0.0;
+    int it = 0;
+    for (;;) {
+        if (m.ndim == 2) k_nm_rhs<2><<<ng, tb, 0, cd->stream>>>(cd->d, nm->b, 4.0 / dt, nm->dUf, 4.0 / dt / dt);
+        else k_nm_rhs<3><<<ng, tb, 0, cd->stream>>>(cd->d, nm->b, 4.0 / dt, nm->dUf, 4.0 / dt / dt);
+        CUDA_TRY(cudaGetLastError());
+        double fn = 0.0;
+        if (nm->opts.cnvgtest == 4) {
+            nm_dot(nm, nm->b, nm->b, S_RP);
+            TRY(nm_scalars(nm, hs));
+            fn = std::sqrt(hs[S_RP]);
+        }
+        TRY(nm_solve(nm));                                  // x = du
+        k_axpy1<<<gf, tb, 0, cd->stream>>>(nm->dUf, nm->x, n);
+        if (nm->opts.cnvgtest == 5) {
+            nm_dot2(nm, nm->x, nm->x, S_RP, nm->dUf, nm->dUf, S_ZQ);
+            TRY(nm_scalars(nm, hs));
+            const double dn = std::sqrt(hs[S_RP]), Dn = std::sqrt(hs[S_ZQ]);
+            if (it == 0) { norm0 = Dn; res = dn; } else res = dn / norm0;
+        } else {
+            if (it == 0) { norm0 = fn; res = fn; } else res = fn / norm0;
+        }
+        // UpdateStatesIncrements: element states from U + dU (Algorithm.cpp:18-56)
+        k_nm_us<<<gt, tb, 0, cd->stream>>>(cd->d, nm->dUf);
+        if (m.ndim == 2) k_element<2, 4><<<eg, 128, 0, cd->stream>>>(cd->d, cd->d.Us, m.ngp, 0);
+        else k_element<3, 8><<<eg, 128, 0, cd->stream>>>(cd->d, cd->d.Us, m.ngp, 0);
+        cd->launches += 4;
+        CUDA_TRY(cudaGetLastError());
+        ++it;
+        if (!(res > nm->opts.cnvgtol) || it >= nm->opts.maxit) break;
+    }
+    nm->newton_iters_last = it;
+    nm->newton_iters_total += it;
+    nm->newton_res_last = res;
+    if (m.ndim == 2) k_nm_update<2><<<ng, tb, 0, cd->stream>>>(cd->d, nm->dUf, 4.0 / dt / dt, 4.0 / dt, 2.0 / dt, cd->d.flag);
+    else k_nm_update<3><<<ng, tb, 0, cd->stream>>>(cd->d, nm->dUf, 4.0 / dt / dt, 4.0 / dt, 2.0 / dt, cd->d.flag);
+    cd->launches += 1;
+    CUDA_TRY(cudaGetLastError());
+    if (U_hist_row) CUDA_TRY(cudaMemcpyAsync(U_hist_row, cd->d.U, sizeof(double) * m.ntotal, cudaMemcpyDeviceToHost, cd->stream));
+    return SVL_OK;
+}
+
 // one step: effective force, solve, state update (d.step already advanced)
 static int nm_step(svl_nm* nm, double* U_hist_row) {
+    if (nm->newton) return nm_step_newton(nm, U_hist_row);
     svl_cd* cd = nm->cd;
     const HostModel& m = cd->m;
     const double dt = nm->opts.dt;
@@ -1597,8 +1838,8 @@ static int nm_step(svl_nm* nm, double* U_hist_row) {
     // internal force from the committed state (filtered like the assembler)
     if (m.ndim == 2) k_element<2, 4><<<eg, 128, 0, cd->stream>>>(cd->d, cd->d.Us, m.ngp, 0);
     else k_element<3, 8><<<eg, 128, 0, cd->stream>>>(cd->d, cd->d.Us, m.ngp, 0);
-    if (m.ndim == 2) k_nm_rhs<2><<<ng, tb, 0, cd->stream>>>(cd->d, nm->b, 4.0 / dt);
-    else k_nm_rhs<3><<<ng, tb, 0, cd->stream>>>(cd->d, nm->b, 4.0 / dt);
+    if (m.ndim == 2) k_nm_rhs<2><<<ng, tb, 0, cd->stream>>>(cd->d, nm->b, 4.0 / dt, nullptr, 0.0);
+    else k_nm_rhs<3><<<ng, tb, 0, cd->stream>>>(cd->d, nm->b, 4.0 / dt, nullptr, 0.0);
     cd->launches += 3;
     CUDA_TRY(cudaGetLastError());
     TRY(nm_solve(nm));
@@ -1814,6 +2055,14 @@ int svl_nm_stats(svl_nm* nm, int64_t* iters_total, int64_t* iters_last, double* 
     if (iters_total) *iters_total = nm->iters_total;
     if (iters_last) *iters_last = nm->iters_last;
     if (rel_residual_last) *rel_residual_last = nm->res_last;
+    return SVL_OK;
+}
+
+int svl_nm_newton_stats(svl_nm* nm, int64_t* iters_total, int64_t* iters_last, double* residual_last) {
+    if (!nm) { set_error("NULL handle"); return SVL_ERR_INVALID; }
+    if (iters_total) *iters_total = nm->newton_iters_total;
+    if (iters_last) *iters_last = nm->newton_iters_last;
+    if (residual_last) *residual_last = nm->newton_res_last;
     return SVL_OK;
 }
 

@@ -180,13 +180,19 @@ class NewmarkBeta:
     (RP/11-Solvers/02-Iterative/PetscSolver.cc, KSPCG, rtol `pcg_tol`)."""
 
     def __init__(self, model: Model, loads: Loads | None, dt: float, pcg_tol: float = 1e-8,
-                 pcg_maxit: int = 20000, ftol: float = 1e-12, mtol: float = 1e-12, precond: int = 0):
+                 pcg_maxit: int = 20000, ftol: float = 1e-12, mtol: float = 1e-12, precond: int = 0,
+                 algorithm: str = "linear", maxit: int = 50, cnvgtol: float = 1e-6, cnvgtest: int = 4):
+        """algorithm "linear" (Linear.cpp) or "newton" (NewtonRaphson.cpp, with
+        `maxit` iterations, tolerance `cnvgtol` and convergence test `cnvgtest`:
+        4 relative unbalanced force, 5 relative displacement increment)."""
         self.model = model
         self.dt = float(dt)
         self._md = model.desc()
         self._ld = (loads or Loads()).desc()
+        algo = {"linear": capi.SVL_ALGO_LINEAR, "newton": capi.SVL_ALGO_NEWTON}[algorithm.lower()]
         opts = capi.NmOpts(dt=self.dt, ftol=ftol, mtol=mtol, pcg_tol=float(pcg_tol), pcg_maxit=int(pcg_maxit),
-                           precond=int(precond))
+                           precond=int(precond), algorithm=algo, maxit=int(maxit), cnvgtol=float(cnvgtol),
+                           cnvgtest=int(cnvgtest))
         h = C.c_void_p()
         check(lib().svl_nm_create(C.byref(self._md), C.byref(self._ld), C.byref(opts), C.byref(h)))
         self._h = h
@@ -288,6 +294,12 @@ class NewmarkBeta:
         """(CG iterations over all solves, of the last solve, last true relative residual)."""
         a, b, r = C.c_int64(), C.c_int64(), C.c_double()
         check(lib().svl_nm_stats(self._h, C.byref(a), C.byref(b), C.byref(r)))
+        return int(a.value), int(b.value), float(r.value)
+
+    def newton_stats(self):
+        """(Newton iterations over all steps, of the last step, last convergence-test value)."""
+        a, b, r = C.c_int64(), C.c_int64(), C.c_double()
+        check(lib().svl_nm_newton_stats(self._h, C.byref(a), C.byref(b), C.byref(r)))
         return int(a.value), int(b.value), float(r.value)
 
     def launches(self) -> int:

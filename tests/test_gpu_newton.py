@@ -1,0 +1,96 @@
+"""GPU Newmark with Newton-Raphson iterations on J2 models (svl_nm_* with
+SVL_ALGO_NEWTON): consistent-tangent PCG solves and state updates from
+U + dU, against the oracle's Newton (dense LDL^T).
+
+The reference's Newton path restarts each J2 return mapping from the
+current (not the committed) internal variables, so once iterates converge
+onto the yield surface the elastic/plastic branch of a Gauss point is
+decided by rounding, and the history is chaotic in the last digits: in the
+oracle itself a 1e-12 relative perturbation of the load, or a PCG solve in
+place of the dense one, moves the history by ~1e-3 after plastic onset.
+Parity is therefore checked bit-tight (1e-9) with a fixed, small number of
+Newton iterations (cnvgtol = 0), where the oracle's dense and PCG runs
+agree to 1e-14, and loosely (5e-3, and 1e-9 before yielding) with the
+convergence tests 4 and 5."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from svl_gb300 import Loads, Model, NewmarkBeta, SvlError, j2_params, ricker
+from svl_gb300 import _capi as capi
+from tests.helpers import h8_box, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+def j2_box(ndim, ne, h=0.5, vs=200.0, su=15e3, amp=4e5, nt=60):
+    rho, nu = 2000.0, 0.3
+    G = rho * vs ** 2
+    K = 2 * G * (1 + nu) / (3 * (1 - 2 * nu))
+    mt = capi.SVL_MAT_PLASTICPLANESTRAINJ2 if ndim == 2 else capi.SVL_MAT_PLASTIC3DJ2
+    fix = (0, 0, 3, 0, 0, 0) if ndim == 2 else (0, 0, 0, 0, 7, 0)
+    m = Model.grid(ndim, ne, (h,) * ndim, fix_mask=fix, mat_type=np.array([mt], np.int32),
+                   mat_param=j2_params(K, G, rho, 0.02 * G, 0.5, np.sqrt(3.0) * su)[None, :])
+    vp = np.sqrt((K + 4 * G / 3) / rho)
+    dt = 2.0 * h / vp
+    L = Loads()
+    s = L.add_series(ricker(nt + 1, dt, 8.0, amp=amp))
+    top = m.nnode - 1 - ne[0] // 2
+    L.add_point_load(m, top, (1.0, -0.5) if ndim == 2 else (1.0, 0.5, -0.5), s)
+    return m, L, dt
+
+
+@pytest.mark.parametrize("ndim,ne,amp,nt", [(2, (8, 6), 4e5, 60), (3, (4, 3, 3), 2e6, 30)], ids=["quad", "hexa"])
+def test_newton_fixed_iterations_match_oracle(gpu, ndim, ne, amp, nt):
+    m, L, dt = j2_box(ndim, ne, amp=amp, nt=nt)
+    nm = NewmarkBeta(m, L, dt, pcg_tol=1e-13, algorithm="newton", maxit=3, cnvgtol=0.0, cnvgtest=4)
+    nm.Initialize()
+    hist = nm.run(1, nt, history=True)
+    its, last, _ = nm.newton_stats()
+    nm.close()
+    ho, _ = O.newmark_run(m, L, dt, nt, algo=2, maxit=3, cnvgtol=0.0, solver=0)
+    hl, _ = O.newmark_run(m, L, dt, nt, algo=0, solver=0)
+    assert its == 3 * nt and last == 3
+    assert rel_l2(ho, hl) > 1e-2                     # the load drives the model plastic
+    assert rel_l2(hist, ho) <= 1e-9
+
+
+@pytest.mark.parametrize("test", [4, 5])
+def test_newton_convergence_tests_track_oracle(gpu, test):
+    m, L, dt = j2_box(2, (8, 6))
+    nt = 60
+    nm = NewmarkBeta(m, L, dt, pcg_tol=1e-13, algorithm="newton", maxit=40, cnvgtol=1e-9, cnvgtest=test)
+    nm.Initialize()
+    hist = nm.run(1, nt, history=True)
+    its, _, res = nm.newton_stats()
+    nm.close()
+    si = np.zeros(nt, np.int32)
+    ho, _ = O.newmark_run(m, L, dt, nt, algo=2 if test == 4 else 1, maxit=40, cnvgtol=1e-9, solver=0, step_iters=si)
+    assert res <= 1e-9
+    onset = int(np.argmax(si > si[0]))               # first step that needs more iterations (yielding)
+    assert onset > 5
+    assert rel_l2(hist[:onset], ho[:onset]) <= 1e-12
+    # after yielding the reference algorithm amplifies rounding (see the module
+    # docstring): same iteration effort, histories within the oracle's own spread
+    assert abs(its - int(si.sum())) <= 0.1 * si.sum()
+    assert rel_l2(hist, ho) <= 5e-3
+
+
+def test_newton_on_elastic_model_matches_linear(gpu):
+    m, L, dt = h8_box(5, 4, 4, seed=7, nt=30)
+    a = NewmarkBeta(m, L, 8 * dt, pcg_tol=1e-12, algorithm="newton", maxit=10, cnvgtol=1e-10, cnvgtest=5)
+    b = NewmarkBeta(m, L, 8 * dt, pcg_tol=1e-12)
+    a.Initialize()
+    b.Initialize()
+    ha = a.run(1, 20, history=True)
+    hb = b.run(1, 20, history=True)
+    a.close()
+    b.close()
+    assert rel_l2(ha, hb) <= 1e-9
+
+
+def test_linear_path_rejects_j2(gpu):
+    m, L, dt = j2_box(2, (4, 3))
+    with pytest.raises(SvlError) as ei:
+        NewmarkBeta(m, L, dt)
+    assert ei.value.code == capi.SVL_ERR_UNSUPPORTED
