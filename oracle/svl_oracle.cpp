@@ -907,7 +907,9 @@ struct Newmark {
             CSR K; keff(K);
             // support motion term: Feff -= T^T (K_total SM).  K_total SM needs
             // the total stiffness; restrained rows only couple through K.
-            s.support_increment(k, SM);
+            // NewmarkBeta takes the increment of step k-1 (NewmarkBeta.cpp:186),
+            // unlike CentralDifference (CentralDifference.cpp:196).
+            s.support_increment(k - 1, SM);
             bool anySM = false; for (double v : SM) if (v != 0.0) { anySM = true; break; }
             if (anySM) {
                 std::vector<Trip> tr; const int nc = s.m.nen * s.m.ndof;

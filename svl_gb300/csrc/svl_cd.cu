@@ -1142,6 +1142,94 @@ __global__ void k_nm_us(DevView d, const double* __restrict__ dUf) {
     d.Us[t] = d.U[t] + (f >= 0 ? dUf[f] : 0.0);
 }
 
+// --- implicit path with a general T (constraints) and support motion -----
+// pt = T pf (rows of T over total dofs)
+__global__ void k_nmg_expand(DevView d, const double* __restrict__ pf, double* __restrict__ pt) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= d.ntotal) return;
+    double v = 0.0;
+    for (int i = d.T_ptr[t]; i < d.T_ptr[t + 1]; ++i) v += d.T_val[i] * pf[d.T_col[i]];
+    pt[t] = v;
+}
+
+// ft = sum_e K_e p_e + c_m M p on total dofs (ordered gather of d.fe)
+template <int ND>
+__global__ void __launch_bounds__(256) k_nmg_total(DevView d, const double* __restrict__ pt, double* __restrict__ ft,
+                                                   double c_m) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= d.nnode) return;
+#pragma unroll
+    for (int c = 0; c < ND; ++c) {
+        const int t = d.ntdof[n * ND + c];
+        ft[t] = gather_fint<ND>(d, n, c) + c_m * d.Md[t] * pt[t];
+    }
+}
+
+// q = T^T ft (optionally minus T^T lg)
+__global__ void k_nmg_reduce(DevView d, const double* __restrict__ ft, const double* __restrict__ lg,
+                             double* __restrict__ q) {
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= d.nfree) return;
+    double v = 0.0, w = 0.0;
+    for (int i = d.TT_ptr[f]; i < d.TT_ptr[f + 1]; ++i) {
+        v += d.TT_val[i] * ft[d.TT_row[i]];
+        if (lg) w += d.TT_val[i] * lg[d.TT_row[i]];
+    }
+    q[f] = lg ? v - w : v;
+}
+
+// total-dof effective force Fext - Fint + M (4/dt V + A - 4/dt^2 dU_t)
+template <int ND>
+__global__ void __launch_bounds__(256) k_nmg_rhs(DevView d, double* __restrict__ ft, const double* __restrict__ dUt,
+                                                 double c_v, double c_m) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= d.nnode) return;
+    const int k = d.step[0];
+#pragma unroll
+    for (int c = 0; c < ND; ++c) {
+        const int t = d.ntdof[n * ND + c];
+        const double fint = gather_fint<ND>(d, n, c);
+        const double fext = fext_at(d, t, k);
+        const double w = (c_v * d.V[t] + d.A[t]) - c_m * dUt[t];
+        ft[t] = ((fext + 0.0) - fint) + d.Md[t] * w;
+    }
+}
+
+// support-motion increment of step k - 1 (NewmarkBeta.cpp:186) on total dofs
+__global__ void k_nmg_sm(DevView d, double* __restrict__ sm) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= d.ntotal) return;
+    sm[t] = sm_at(d, t, d.step[0] - 1);
+}
+
+// Us = U + dU_t;  at the end of the step U += dU_t + SM, A and V from dU_t
+template <int ND>
+__global__ void __launch_bounds__(256) k_nmg_update(DevView d, const double* __restrict__ dUt,
+                                                    const double* __restrict__ sm, double c_a, double c_av,
+                                                    double c_vv, int* flag) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= d.nnode) return;
+    bool bad = false;
+#pragma unroll
+    for (int c = 0; c < ND; ++c) {
+        const int t = d.ntdof[n * ND + c];
+        const double dU = dUt[t];
+        const double u0 = d.U[t];
+        const double u = u0 + (dU + sm[t]);
+        d.U[t] = u;
+        d.Us[t] = u0 + dU;          // states follow U + T du, without the support motion
+        d.A[t] = c_a * dU - c_av * d.V[t] - d.A[t];
+        d.V[t] = c_vv * dU - d.V[t];
+        bad |= !isfinite(u);
+    }
+    if (bad) atomicOr(flag, 1);
+}
+
+__global__ void k_nmg_us(DevView d, const double* __restrict__ dUt) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < d.ntotal) d.Us[t] = d.U[t] + dUt[t];
+}
+
 __global__ void k_axpy1(double* __restrict__ y, const double* __restrict__ x, int n) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) y[i] += x[i];
@@ -1333,6 +1421,8 @@ struct svl_nm {
     int64_t train_trial_iters = 0;          // trial-solve iterations of the kept weights
     // Newton: operator scratch block, accumulated increment, iteration counts
     double* fe_op = nullptr;                // [nc][E] element vectors of the operator action
+    bool general = false;                   // constraints (T not identity) or support motion
+    double *ft = nullptr, *dUt = nullptr, *smv = nullptr, *lg = nullptr, *pt2 = nullptr;   // total-dof scratch
     double* dUf = nullptr;                  // [nfree] displacement increment of the step
     bool newton = false, tangent = false;   // tangent: J2 elements present (stored tangents)
     int64_t newton_iters_total = 0, newton_iters_last = 0;
@@ -1367,14 +1457,45 @@ static int nm_scalars(svl_nm* nm, double* hs) {
     return SVL_OK;
 }
 
+// out = (K + 4/dt^2 M) pt on total dofs (K: element stiffness or tangent action)
+static int nm_op_total(svl_nm* nm, const double* pt, double* out) {
+    svl_cd* cd = nm->cd;
+    const HostModel& m = cd->m;
+    DevView d = cd->d;
+    d.ftol = -1.0;
+    d.fe = nm->fe_op;
+    const int tb = 256, eg = (m.nelem + 127) / 128, ng = (m.nnode + tb - 1) / tb;
+    if (nm->tangent) {
+        if (m.ndim == 2) k_element_tan<2, 4><<<eg, 128, 0, cd->stream>>>(d, pt, m.ngp);
+        else k_element_tan<3, 8><<<eg, 128, 0, cd->stream>>>(d, pt, m.ngp);
+    } else {
+        if (m.ndim == 2) k_element<2, 4><<<eg, 128, 0, cd->stream>>>(d, pt, m.ngp, 0);
+        else k_element<3, 8><<<eg, 128, 0, cd->stream>>>(d, pt, m.ngp, 0);
+    }
+    const double c_m = 4.0 / nm->opts.dt / nm->opts.dt;
+    if (m.ndim == 2) k_nmg_total<2><<<ng, tb, 0, cd->stream>>>(d, pt, out, c_m);
+    else k_nmg_total<3><<<ng, tb, 0, cd->stream>>>(d, pt, out, c_m);
+    cd->launches += 2;
+    CUDA_TRY(cudaGetLastError());
+    return SVL_OK;
+}
+
 // q = Keff v (free dofs)
 static int nm_apply(svl_nm* nm, const double* v, double* q) {
     svl_cd* cd = nm->cd;
     const HostModel& m = cd->m;
+    const int tb = 256;
+    if (nm->general) {                      // q = T^T (K + c_m M) T v
+        k_nmg_expand<<<(m.ntotal + tb - 1) / tb, tb, 0, cd->stream>>>(cd->d, v, nm->pt);
+        TRY(nm_op_total(nm, nm->pt, nm->ft));
+        k_nmg_reduce<<<(nm->nf + tb - 1) / tb, tb, 0, cd->stream>>>(cd->d, nm->ft, nullptr, q);
+        cd->launches += 2;
+        CUDA_TRY(cudaGetLastError());
+        return SVL_OK;
+    }
     DevView d = cd->d;
     d.ftol = -1.0;                  // the operator action is not filtered
     d.fe = nm->fe_op;               // and keeps the state's element forces intact
-    const int tb = 256;
     k_nm_expand<<<(m.ntotal + tb - 1) / tb, tb, 0, cd->stream>>>(d, v, nm->pt);
     const int eg = (m.nelem + 127) / 128;
     if (nm->tangent) {
@@ -1596,8 +1717,7 @@ int svl_nm_create(const svl_model_desc* model, const svl_load_desc* loads, const
     nm->opts = *opts;
     auto fail = [&](int s2) { delete nm; return s2; };
     const HostModel& m = cd->m;
-    if (!cd->identity_T) { set_error("the implicit path does not take constraints yet"); return fail(SVL_ERR_UNSUPPORTED); }
-    if (cd->has_sm) { set_error("the implicit path does not take support motion yet"); return fail(SVL_ERR_UNSUPPORTED); }
+    nm->general = !cd->identity_T || cd->has_sm;
     if (opts->algorithm != SVL_ALGO_LINEAR && opts->algorithm != SVL_ALGO_NEWTON) { set_error("unknown algorithm %d", opts->algorithm); return fail(SVL_ERR_INVALID); }
     nm->newton = opts->algorithm == SVL_ALGO_NEWTON;
     if (nm->newton && (opts->maxit <= 0 || !(opts->cnvgtol >= 0.0) || (opts->cnvgtest != 4 && opts->cnvgtest != 5))) {
@@ -1645,11 +1765,21 @@ int svl_nm_create(const svl_model_desc* model, const svl_load_desc* loads, const
     lumped_mass_diag(m, opts->mtol, M);
     std::vector<double> dinv(std::max(m.nfree, 1), 1.0);
     const double c_m = 4.0 / opts->dt / opts->dt;
-    for (int n = 0; n < m.nnode; ++n)
-        for (int c = 0; c < m.ndof; ++c) {
-            const int t = m.tdof[(size_t)n * m.ndof + c], f = m.fdof[(size_t)n * m.ndof + c];
-            if (f >= 0) dinv[f] = 1.0 / (Kd[t] + c_m * M[t]);
-        }
+    if (!cd->identity_T) {
+        // diagonal of T^T diag(K + c_m M) T (the Jacobi preconditioner only)
+        std::vector<int32_t> Tp, Tc;
+        std::vector<double> Tv, dg(std::max(m.nfree, 1), 0.0);
+        build_total_to_free(m, Tp, Tc, Tv);
+        for (int t = 0; t < m.ntotal; ++t)
+            for (int i = Tp[t]; i < Tp[t + 1]; ++i) dg[Tc[i]] += Tv[i] * Tv[i] * (Kd[t] + c_m * M[t]);
+        for (int f = 0; f < m.nfree; ++f) dinv[f] = dg[f] > 0.0 ? 1.0 / dg[f] : 1.0;
+    } else {
+        for (int n = 0; n < m.nnode; ++n)
+            for (int c = 0; c < m.ndof; ++c) {
+                const int t = m.tdof[(size_t)n * m.ndof + c], f = m.fdof[(size_t)n * m.ndof + c];
+                if (f >= 0) dinv[f] = 1.0 / (Kd[t] + c_m * M[t]);
+            }
+    }
     double** vecs[] = {&nm->b, &nm->x, &nm->r, &nm->z, &nm->p, &nm->q};
     for (double** pv : vecs) if ((st = cd->zeros((size_t)std::max(m.nfree, 1), pv))) return fail(st);
     if ((st = cd->zeros((size_t)m.ntotal, &nm->pt)) || (st = cd->zeros(2 * kDotBlocks, &nm->partial)) ||
@@ -1660,6 +1790,10 @@ int svl_nm_create(const svl_model_desc* model, const svl_load_desc* loads, const
     nm->dinv = const_cast<double*>(dd);
     if ((st = cd->zeros((size_t)nc * m.nelem, &nm->fe_op)) || (st = cd->zeros((size_t)std::max(m.nfree, 1), &nm->dUf)))
         return fail(st);
+    if (nm->general) {
+        double** tv[] = {&nm->ft, &nm->dUt, &nm->smv, &nm->lg, &nm->pt2};
+        for (double** pv : tv) if ((st = cd->zeros((size_t)m.ntotal, pv))) return fail(st);
+    }
     if (nm->tangent) {
         double* ct = nullptr;
         if ((st = cd->zeros((size_t)(m.ndim == 2 ? 9 : 36) * m.ngp * m.nelem, &ct))) return fail(st);
@@ -1668,7 +1802,7 @@ int svl_nm_create(const svl_model_desc* model, const svl_load_desc* loads, const
     // lattice models: the maps and scalings of the learned preconditioner
     int dims[3];
     std::vector<int32_t> cell;
-    if (m.nfree > 0 && detect_lattice(m, dims, cell)) {
+    if (m.nfree > 0 && cd->identity_T && detect_lattice(m, dims, cell)) {
         nm->lattice = true;
         nm->lnx = dims[0]; nm->lny = dims[1]; nm->lnz = dims[2];
         const int64_t V = (int64_t)dims[0] * dims[1] * dims[2];
@@ -1693,7 +1827,7 @@ int svl_nm_create(const svl_model_desc* model, const svl_load_desc* loads, const
             nm->precond = SVL_PRECOND_LEARNED;
         }
     } else if (opts->precond == SVL_PRECOND_LEARNED) {
-        set_error("the learned preconditioner needs a hexahedral model whose nodes form a lattice");
+        set_error("the learned preconditioner needs a hexahedral model without constraints whose nodes form a lattice");
         return fail(SVL_ERR_UNSUPPORTED);
     }
     if (cudaStreamSynchronize(cd->stream) != cudaSuccess) { set_error("upload failed"); return fail(SVL_ERR_CUDA); }
@@ -1773,6 +1907,52 @@ static int64_t nm_trial(svl_nm* nm, int k) {
     return score;
 }
 
+// b = T^T (Fext - Fint + M(4/dt V + A - 4/dt^2 T dU)) - T^T (Keff SM), general T;
+// dUt (total) must hold T dUf, smv the step's support-motion increment.
+static int nmg_rhs(svl_nm* nm) {
+    svl_cd* cd = nm->cd;
+    const HostModel& m = cd->m;
+    const double dt = nm->opts.dt;
+    const int tb = 256, ng = (m.nnode + tb - 1) / tb;
+    if (m.ndim == 2) k_nmg_rhs<2><<<ng, tb, 0, cd->stream>>>(cd->d, nm->ft, nm->dUt, 4.0 / dt, 4.0 / dt / dt);
+    else k_nmg_rhs<3><<<ng, tb, 0, cd->stream>>>(cd->d, nm->ft, nm->dUt, 4.0 / dt, 4.0 / dt / dt);
+    cd->launches += 1;
+    const double* lg = nullptr;
+    if (cd->has_sm) {
+        // Keff SM (NewmarkBeta::ComputeSupportMotionVector, NewmarkBeta.cpp:180-194)
+        TRY(nm_op_total(nm, nm->smv, nm->lg));
+        lg = nm->lg;
+    }
+    k_nmg_reduce<<<(nm->nf + tb - 1) / tb, tb, 0, cd->stream>>>(cd->d, nm->ft, lg, nm->b);
+    cd->launches += 1;
+    CUDA_TRY(cudaGetLastError());
+    return SVL_OK;
+}
+
+// Linear step with a general T and/or support motion.
+static int nmg_step_linear(svl_nm* nm, double* U_hist_row) {
+    svl_cd* cd = nm->cd;
+    const HostModel& m = cd->m;
+    const double dt = nm->opts.dt;
+    const int tb = 256, ng = (m.nnode + tb - 1) / tb, eg = (m.nelem + 127) / 128, gt = (m.ntotal + tb - 1) / tb;
+    k_step_inc<<<1, 1, 0, cd->stream>>>(cd->d.step);
+    if (m.ndim == 2) k_element<2, 4><<<eg, 128, 0, cd->stream>>>(cd->d, cd->d.Us, m.ngp, 0);
+    else k_element<3, 8><<<eg, 128, 0, cd->stream>>>(cd->d, cd->d.Us, m.ngp, 0);
+    k_nmg_sm<<<gt, tb, 0, cd->stream>>>(cd->d, nm->smv);
+    CUDA_TRY(cudaMemsetAsync(nm->dUt, 0, sizeof(double) * m.ntotal, cd->stream));
+    cd->launches += 3;
+    TRY(nmg_rhs(nm));
+    TRY(nm_solve(nm));
+    if (nm->rec_n > 0) TRY(nm_pairs_from_iterates(nm));
+    k_nmg_expand<<<gt, tb, 0, cd->stream>>>(cd->d, nm->x, nm->dUt);
+    if (m.ndim == 2) k_nmg_update<2><<<ng, tb, 0, cd->stream>>>(cd->d, nm->dUt, nm->smv, 4.0 / dt / dt, 4.0 / dt, 2.0 / dt, cd->d.flag);
+    else k_nmg_update<3><<<ng, tb, 0, cd->stream>>>(cd->d, nm->dUt, nm->smv, 4.0 / dt / dt, 4.0 / dt, 2.0 / dt, cd->d.flag);
+    cd->launches += 2;
+    CUDA_TRY(cudaGetLastError());
+    if (U_hist_row) CUDA_TRY(cudaMemcpyAsync(U_hist_row, cd->d.U, sizeof(double) * m.ntotal, cudaMemcpyDeviceToHost, cd->stream));
+    return SVL_OK;
+}
+
 // One NewtonRaphson step (NewtonRaphson.cpp:24-75 with NewmarkBeta's effective
 // force and stiffness): iterate Feff(current states, dU) -> tangent solve ->
 // dU += du -> convergence test -> state update from U + dU.
@@ -1785,11 +1965,19 @@ static int nm_step_newton(svl_nm* nm, double* U_hist_row) {
     double hs[S_NSCAL];
     k_step_inc<<<1, 1, 0, cd->stream>>>(cd->d.step);
     CUDA_TRY(cudaMemsetAsync(nm->dUf, 0, sizeof(double) * std::max(n, 1), cd->stream));
+    if (nm->general) {
+        k_nmg_sm<<<gt, tb, 0, cd->stream>>>(cd->d, nm->smv);
+        CUDA_TRY(cudaMemsetAsync(nm->dUt, 0, sizeof(double) * m.ntotal, cd->stream));
+    }
     double norm0 = 0.0, res = 0.0;
     int it = 0;
     for (;;) {
-        if (m.ndim == 2) k_nm_rhs<2><<<ng, tb, 0, cd->stream>>>(cd->d, nm->b, 4.0 / dt, nm->dUf, 4.0 / dt / dt);
-        else k_nm_rhs<3><<<ng, tb, 0, cd->stream>>>(cd->d, nm->b, 4.0 / dt, nm->dUf, 4.0 / dt / dt);
+        if (nm->general) {
+            TRY(nmg_rhs(nm));               // K SM with the current tangent, every iteration
+        } else {
+            if (m.ndim == 2) k_nm_rhs<2><<<ng, tb, 0, cd->stream>>>(cd->d, nm->b, 4.0 / dt, nm->dUf, 4.0 / dt / dt);
+            else k_nm_rhs<3><<<ng, tb, 0, cd->stream>>>(cd->d, nm->b, 4.0 / dt, nm->dUf, 4.0 / dt / dt);
+        }
         CUDA_TRY(cudaGetLastError());
         double fn = 0.0;
         if (nm->opts.cnvgtest == 4) {
@@ -1807,8 +1995,13 @@ static int nm_step_newton(svl_nm* nm, double* U_hist_row) {
         } else {
             if (it == 0) { norm0 = fn; res = fn; } else res = fn / norm0;
         }
-        // UpdateStatesIncrements: element states from U + dU (Algorithm.cpp:18-56)
-        k_nm_us<<<gt, tb, 0, cd->stream>>>(cd->d, nm->dUf);
+        // UpdateStatesIncrements: element states from U + T dU (Algorithm.cpp:18-56)
+        if (nm->general) {
+            k_nmg_expand<<<gt, tb, 0, cd->stream>>>(cd->d, nm->dUf, nm->dUt);
+            k_nmg_us<<<gt, tb, 0, cd->stream>>>(cd->d, nm->dUt);
+        } else {
+            k_nm_us<<<gt, tb, 0, cd->stream>>>(cd->d, nm->dUf);
+        }
         if (m.ndim == 2) k_element<2, 4><<<eg, 128, 0, cd->stream>>>(cd->d, cd->d.Us, m.ngp, 0);
         else k_element<3, 8><<<eg, 128, 0, cd->stream>>>(cd->d, cd->d.Us, m.ngp, 0);
         cd->launches += 4;
@@ -1819,8 +2012,13 @@ static int nm_step_newton(svl_nm* nm, double* U_hist_row) {
     nm->newton_iters_last = it;
     nm->newton_iters_total += it;
     nm->newton_res_last = res;
-    if (m.ndim == 2) k_nm_update<2><<<ng, tb, 0, cd->stream>>>(cd->d, nm->dUf, 4.0 / dt / dt, 4.0 / dt, 2.0 / dt, cd->d.flag);
-    else k_nm_update<3><<<ng, tb, 0, cd->stream>>>(cd->d, nm->dUf, 4.0 / dt / dt, 4.0 / dt, 2.0 / dt, cd->d.flag);
+    if (nm->general) {
+        if (m.ndim == 2) k_nmg_update<2><<<ng, tb, 0, cd->stream>>>(cd->d, nm->dUt, nm->smv, 4.0 / dt / dt, 4.0 / dt, 2.0 / dt, cd->d.flag);
+        else k_nmg_update<3><<<ng, tb, 0, cd->stream>>>(cd->d, nm->dUt, nm->smv, 4.0 / dt / dt, 4.0 / dt, 2.0 / dt, cd->d.flag);
+    } else {
+        if (m.ndim == 2) k_nm_update<2><<<ng, tb, 0, cd->stream>>>(cd->d, nm->dUf, 4.0 / dt / dt, 4.0 / dt, 2.0 / dt, cd->d.flag);
+        else k_nm_update<3><<<ng, tb, 0, cd->stream>>>(cd->d, nm->dUf, 4.0 / dt / dt, 4.0 / dt, 2.0 / dt, cd->d.flag);
+    }
     cd->launches += 1;
     CUDA_TRY(cudaGetLastError());
     if (U_hist_row) CUDA_TRY(cudaMemcpyAsync(U_hist_row, cd->d.U, sizeof(double) * m.ntotal, cudaMemcpyDeviceToHost, cd->stream));
@@ -1830,6 +2028,7 @@ static int nm_step_newton(svl_nm* nm, double* U_hist_row) {
 // one step: effective force, solve, state update (d.step already advanced)
 static int nm_step(svl_nm* nm, double* U_hist_row) {
     if (nm->newton) return nm_step_newton(nm, U_hist_row);
+    if (nm->general) return nmg_step_linear(nm, U_hist_row);
     svl_cd* cd = nm->cd;
     const HostModel& m = cd->m;
     const double dt = nm->opts.dt;

@@ -94,3 +94,42 @@ def test_linear_path_rejects_j2(gpu):
     with pytest.raises(SvlError) as ei:
         NewmarkBeta(m, L, dt)
     assert ei.value.code == capi.SVL_ERR_UNSUPPORTED
+
+
+def _columns(elastic):
+    from tests.helpers import q4_j2_columns
+    m, L, dt = q4_j2_columns(ncol=2, width=3, heights=(6, 8), nt=80, pga=6.0)
+    if elastic:
+        G, K, rho = m.mat_param[:, 1], m.mat_param[:, 0], m.mat_param[:, 2]
+        E = 9 * K * G / (3 * K + G)
+        nu = (3 * K - 2 * G) / (2 * (3 * K + G))
+        mp = np.zeros_like(m.mat_param)
+        mp[:, 0], mp[:, 1], mp[:, 2] = E, nu, rho
+        m.mat_param = mp
+        m.mat_type = np.full_like(m.mat_type, capi.SVL_MAT_ELASTIC2DPLANESTRAIN)
+    return m, L, dt
+
+
+def test_linear_newmark_with_constraints_and_support_motion(gpu):
+    m, L, dt = _columns(elastic=True)
+    assert m.nconstraint > 0 and len(L.sm_dof) > 0
+    nt = 60
+    nm = NewmarkBeta(m, L, 4 * dt, pcg_tol=1e-13)
+    nm.Initialize()
+    hist = nm.run(1, nt, history=True)
+    nm.close()
+    ho, _ = O.newmark_run(m, L, 4 * dt, nt, solver=0)
+    assert np.abs(ho).max() > 0
+    assert rel_l2(hist, ho) <= 1e-9
+
+
+def test_newton_j2_columns_with_constraints_and_support_motion(gpu):
+    m, L, dt = _columns(elastic=False)
+    nt = 60
+    nm = NewmarkBeta(m, L, 4 * dt, pcg_tol=1e-13, algorithm="newton", maxit=3, cnvgtol=0.0, cnvgtest=4)
+    nm.Initialize()
+    hist = nm.run(1, nt, history=True)
+    nm.close()
+    ho, _ = O.newmark_run(m, L, 4 * dt, nt, algo=2, maxit=3, cnvgtol=0.0, solver=0)
+    assert np.abs(ho).max() > 0
+    assert rel_l2(hist, ho) <= 1e-9
