@@ -92,6 +92,10 @@ typedef struct svl_model_desc {
     const double*  mat_param;  /* [nmat][SVL_MAT_NPARAM]                        */
     int32_t lumped;            /* 1: row-sum lumped mass (massform LUMPED)      */
     const double*  node_mass;  /* [ntotal] extra nodal masses, or NULL          */
+    /* Rayleigh damping of each element (Dampings "Rayleigh", Driver.hpp:1375-1400):
+     * C_e = am M_e + ak K0_e with K0 the initial stiffness (lin2DQuad4.cpp:322-372,
+     * lin3DHexa8.cpp).  [nelem][2] = {am, ak}, or NULL for undamped elements. */
+    const double*  elem_rayleigh;
 } svl_model_desc;
 
 /* ---- loads -------------------------------------------------------------- */

@@ -52,6 +52,7 @@ struct Model {
     std::vector<int> mtype;
     std::vector<double> mpar;
     std::vector<double> nodemass;     // [ntotal] or empty
+    std::vector<double> ray;          // [nelem][2] Rayleigh (am, ak) or empty
     int nconstraint;
     std::vector<int> cslave, cptr, cmaster;
     std::vector<double> cfactor;
@@ -91,6 +92,7 @@ bool load_model(const svl_model_desc* d, Model& m) {
     m.mtype.assign(d->mat_type, d->mat_type + d->nmat);
     m.mpar.assign(d->mat_param, d->mat_param + (size_t)d->nmat * SVL_MAT_NPARAM);
     if (d->node_mass) m.nodemass.assign(d->node_mass, d->node_mass + m.ntotal);
+    if (d->elem_rayleigh) m.ray.assign(d->elem_rayleigh, d->elem_rayleigh + (size_t)2 * m.nelem);
     m.nconstraint = d->nconstraint;
     if (m.nconstraint > 0) {
         m.cslave.assign(d->con_slave, d->con_slave + m.nconstraint);
@@ -536,6 +538,45 @@ struct Sim {
                 }
         }
     }
+    // Element::ComputeInitialStiffnessMatrix (lin2DQuad4.cpp:714-739): B^T C0 B
+    // with the material's initial tangent (J2: K 1(x)1 + 2G Id, PlasticPlaneStrainJ2.cpp:163-180).
+    void element_K0(int e, double* Ke) const {
+        const int nc = m.nen * m.ndof, ns = m.nstr;
+        for (int i = 0; i < nc * nc; ++i) Ke[i] = 0.0;
+        const int type = mt(e);
+        const double* p = mp(e);
+        double C[36];
+        if (type == SVL_MAT_PLASTICPLANESTRAINJ2 || type == SVL_MAT_PLASTIC3DJ2) {
+            double C6[36];
+            j2_elastic_tangent(p[0], p[1], C6);
+            if (type == SVL_MAT_PLASTICPLANESTRAINJ2) {
+                const int ix[3] = {1, 2, 4};
+                for (int i = 0; i < 3; ++i) for (int j = 0; j < 3; ++j) C[i * 3 + j] = C6[ix[i] * 6 + ix[j]];
+            } else std::memcpy(C, C6, sizeof(C6));
+        } else {
+            MatState z; mat_init(z, type, p);
+            mat_tangent(z, type, p, C);
+        }
+        for (int q = 0; q < m.ngp; ++q) {
+            double dNx[8][3], N[8];
+            double det = element_gp(m, e, q, dNx, N);
+            double B[6 * 24], CB[6 * 24];
+            B_matrix(m.ndim, m.nen, dNx, B);
+            double c = (m.ndim == 2) ? 1.0 * m.thick[e] * std::fabs(det) : 1.0 * std::fabs(det);
+            for (int i = 0; i < ns; ++i)
+                for (int j = 0; j < nc; ++j) {
+                    double v = 0.0;
+                    for (int k = 0; k < ns; ++k) v += C[i * ns + k] * B[k * nc + j];
+                    CB[i * nc + j] = v;
+                }
+            for (int i = 0; i < nc; ++i)
+                for (int j = 0; j < nc; ++j) {
+                    double v = 0.0;
+                    for (int k = 0; k < ns; ++k) v += B[k * nc + i] * CB[k * nc + j];
+                    Ke[i * nc + j] += c * v;
+                }
+        }
+    }
     // Element::ComputeMassMatrix with row-sum lumping (lin2DQuad4.cpp:243-285).
     void element_M(int e, double* Me, bool lump) const {
         const int nc = m.nen * m.ndof, nd = m.ndim;
@@ -619,6 +660,7 @@ struct Sim {
 struct CD {
     Sim s; double dt;
     std::vector<double> U, V, A, Up, Md, Kd, Kff_inv, Us;
+    std::vector<double> Cd;    // Rayleigh damping diagonal (mass-proportional), empty when undamped
     bool fast = false;
     std::vector<double> geo;   // fast mode: [nelem][ngp][nen*ndim + 1]
     std::vector<double> fe_all;  // fast mode: element force blocks
@@ -630,9 +672,27 @@ struct CD {
         const int nt = s.m.ntotal;
         U.assign(nt, 0); V.assign(nt, 0); A.assign(nt, 0); Up.assign(nt, 0); Us.assign(nt, 0);
         s.assemble_mass_diag(Md);
-        // K = 1/dt/dt*M + 1/2/dt*C with C = 0 (CentralDifference.cpp:70)
+        // C = sum_e am_e M_e + ak_e K0_e (lin2DQuad4.cpp:355-366); with a lumped
+        // mass it is diagonal only when every ak_e is zero, which the diagonal
+        // solve below needs
+        if (!s.m.ray.empty()) {
+            const int nc = s.m.nen * s.m.ndof;
+            std::vector<double> Me((size_t)nc * nc);
+            Cd.assign(nt, 0.0);
+            for (int e = 0; e < s.m.nelem; ++e) {
+                const double am = s.m.ray[2 * e], ak = s.m.ray[2 * e + 1];
+                if (ak != 0.0) return false;
+                if (am == 0.0) continue;
+                s.element_M(e, Me.data(), true);
+                for (int i = 0; i < nc; ++i) {
+                    const double v = am * Me[(size_t)i * nc + i];
+                    if (std::fabs(v) > s.ktol) Cd[s.edofs[(size_t)e * nc + i]] += v;
+                }
+            }
+        }
+        // K = 1/dt/dt*M + 1/2/dt*C (CentralDifference.cpp:70)
         Kd.resize(nt);
-        for (int t = 0; t < nt; ++t) Kd[t] = 1.0 / dt / dt * Md[t];
+        for (int t = 0; t < nt; ++t) Kd[t] = Cd.empty() ? 1.0 / dt / dt * Md[t] : 1.0 / dt / dt * Md[t] + 1.0 / 2.0 / dt * Cd[t];
         // Keff = T^T K T (diagonal when every slave has one master)
         std::vector<double> kf(s.m.nfree, 0.0);
         for (int t = 0; t < nt; ++t)
@@ -713,7 +773,10 @@ struct CD {
         if (fast) fint_fast(Fint); else s.assemble_fint(Fint);
         s.fext(k, Fext);
         // Fext + Fbar - Fint + (1/dt/dt*M - 1/2/dt*C)*(U - Up)   (CentralDifference.cpp:217)
-        for (int t = 0; t < nt; ++t) R[t] = (Fext[t] + 0.0 - Fint[t]) + (1.0 / dt / dt * Md[t]) * (U[t] - Up[t]);
+        for (int t = 0; t < nt; ++t) {
+            const double c = Cd.empty() ? 1.0 / dt / dt * Md[t] : 1.0 / dt / dt * Md[t] - 1.0 / 2.0 / dt * Cd[t];
+            R[t] = (Fext[t] + 0.0 - Fint[t]) + c * (U[t] - Up[t]);
+        }
         s.TT_apply(R, Feff);
         // support motion: Feff -= T^T (K SM)   (CentralDifference.cpp:190-202)
         s.support_increment(k, SM);
@@ -830,6 +893,7 @@ struct Newmark {
     Sim s; double dt;
     std::vector<double> U, V, A, Mfull_diag;
     CSR Mt;                      // total-dof mass (lumped or consistent)
+    CSR Ct;                      // total-dof Rayleigh damping (empty when undamped)
     int solver = 0;              // 0 dense LDL^T, 1 Jacobi-PCG
     double pcg_tol = 1e-12; int pcg_maxit = 100000; long pcg_iters = 0;
 
@@ -853,6 +917,24 @@ struct Newmark {
         if (!s.m.nodemass.empty())
             for (int t = 0; t < nt; ++t) if (std::fabs(s.m.nodemass[t]) > s.mtol) tr.push_back({t, t, s.m.nodemass[t]});
         csr_from_triplets(nt, tr, Mt);
+        // Rayleigh C_e = am M_e + ak K0_e (lin2DQuad4.cpp:355-366), assembled with
+        // the stiffness tolerance (Assembler.cpp:117-158)
+        if (!s.m.ray.empty()) {
+            std::vector<Trip> ct;
+            std::vector<double> K0((size_t)nc * nc);
+            for (int e = 0; e < s.m.nelem; ++e) {
+                const double am = s.m.ray[2 * e], ak = s.m.ray[2 * e + 1];
+                if (am == 0.0 && ak == 0.0) continue;
+                s.element_M(e, Me.data(), s.m.lumped != 0);
+                s.element_K0(e, K0.data());
+                for (int j = 0; j < nc; ++j)
+                    for (int i = 0; i < nc; ++i) {
+                        const double v = am * Me[(size_t)i * nc + j] + ak * K0[(size_t)i * nc + j];
+                        if (std::fabs(v) > s.ktol) ct.push_back({s.edofs[(size_t)e * nc + i], s.edofs[(size_t)e * nc + j], v});
+                    }
+            }
+            csr_from_triplets(nt, ct, Ct);
+        }
         return true;
     }
     // T^T K T as free-dof CSR
@@ -879,6 +961,8 @@ struct Newmark {
         }
         for (int r = 0; r < Mt.n; ++r)
             for (int i = Mt.ptr[r]; i < Mt.ptr[r + 1]; ++i) tr.push_back({r, Mt.col[i], 4.0 / dt / dt * Mt.val[i]});
+        for (int r = 0; r < Ct.n; ++r)
+            for (int i = Ct.ptr[r]; i < Ct.ptr[r + 1]; ++i) tr.push_back({r, Ct.col[i], 2.0 / dt * Ct.val[i]});
         reduce(tr, Kff);
     }
     bool solve(const CSR& K, const std::vector<double>& b, std::vector<double>& x) {
@@ -901,8 +985,14 @@ struct Newmark {
             std::vector<double> w(nt);
             for (int t = 0; t < nt; ++t) w[t] = 4.0 / dt * V[t] + A[t] - 4.0 / dt / dt * dUt[t];
             csr_mv(Mt, w, MV);
-            // Fext + Fbar - Fint + M*(4/dt V + A - 4/dt^2 dU) (NewmarkBeta.cpp:215)
+            // Fext + Fbar - Fint + M*(4/dt V + A - 4/dt^2 dU) + C*(V - 2/dt dU) (NewmarkBeta.cpp:215)
             for (int t = 0; t < nt; ++t) F[t] = (Fext[t] + 0.0 - Fint[t]) + MV[t];
+            if (Ct.n) {
+                std::vector<double> w2(nt), CV;
+                for (int t = 0; t < nt; ++t) w2[t] = V[t] - 2.0 / dt * dUt[t];
+                csr_mv(Ct, w2, CV);
+                for (int t = 0; t < nt; ++t) F[t] += CV[t];
+            }
             s.TT_apply(F, Feff);
             CSR K; keff(K);
             // support motion term: Feff -= T^T (K_total SM).  K_total SM needs
@@ -922,6 +1012,7 @@ struct Newmark {
                     }
                 }
                 for (int r = 0; r < Mt.n; ++r) for (int i = Mt.ptr[r]; i < Mt.ptr[r + 1]; ++i) tr.push_back({r, Mt.col[i], 4.0 / dt / dt * Mt.val[i]});
+                for (int r = 0; r < Ct.n; ++r) for (int i = Ct.ptr[r]; i < Ct.ptr[r + 1]; ++i) tr.push_back({r, Ct.col[i], 2.0 / dt * Ct.val[i]});
                 CSR Kt; csr_from_triplets(nt, tr, Kt);
                 std::vector<double> KS, lg; csr_mv(Kt, SM, KS); s.TT_apply(KS, lg);
                 for (int f = 0; f < nf; ++f) Feff[f] -= lg[f];

@@ -55,7 +55,7 @@ class ModelDesc(C.Structure):
         ("elem_type", C.c_int32), ("nelem", C.c_int32), ("conn", i32p),
         ("elem_mat", i32p), ("elem_thickness", f64p),
         ("nmat", C.c_int32), ("mat_type", i32p), ("mat_param", f64p),
-        ("lumped", C.c_int32), ("node_mass", f64p),
+        ("lumped", C.c_int32), ("node_mass", f64p), ("elem_rayleigh", f64p),
     ]
 
 

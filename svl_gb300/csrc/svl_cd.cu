@@ -74,6 +74,9 @@ struct DevView {
     const double* Md;        // [ntotal]
     const double* kinv;      // [nfree]  1 / (T^T K T)_ff
     const double* Kd;        // [ntotal] 1/dt^2 M
+    // Rayleigh damping C = sum_e (am_e M_e + ak_e K0_e) (lin2DQuad4.cpp:355-366)
+    const double* Cd;        // [ntotal] sum_e am_e M_e (lumped), or null
+    const double* dk0;       // [3][E]   ak_e * (c1, c2, c3) of the initial elastic tangent, or null
     double *U, *V, *A, *Up, *Us, *R, *du;
     // T and T^T as CSR (constraint path)
     const int32_t *T_ptr, *T_col; const double* T_val;
@@ -282,8 +285,11 @@ __global__ void __launch_bounds__(128) k_element(DevView d, const double* __rest
 // their last update (2D: rows/cols 1,2,4 of the 6x6 tensor-strain tangent
 // applied to the engineering strain, as the reference assembles it).  Writes
 // the unfiltered element vectors into d.fe (an operator scratch block).
+// With damping tables, adds cc * ak_e K0_e p_e (the stiffness-proportional
+// part of C); with_tan = 0 leaves the tangent out (damping action only).
 template <int ND, int NEN>
-__global__ void __launch_bounds__(128) k_element_tan(DevView d, const double* __restrict__ P, int ngp) {
+__global__ void __launch_bounds__(128) k_element_tan(DevView d, const double* __restrict__ P, int ngp, int with_tan,
+                                                     double cc) {
     constexpr int NC = ND * NEN;
     constexpr int PER = NEN * ND + 1;
     constexpr int NS = ND == 2 ? 3 : 6;
@@ -323,7 +329,9 @@ __global__ void __launch_bounds__(128) k_element_tan(DevView d, const double* __
                 ev[5 % NS] += b[a][2] * ux + b[a][0] * uz;
             }
         }
-        if (kind == kMatElastic) {
+#pragma unroll
+        for (int i = 0; i < NS; ++i) sig[i] = 0.0;
+        if (with_tan && kind == kMatElastic) {
             if (ND == 2) {
                 sig[0] = c1 * ev[0] + c2 * ev[1];
                 sig[1] = c2 * ev[0] + c1 * ev[1];
@@ -334,7 +342,7 @@ __global__ void __launch_bounds__(128) k_element_tan(DevView d, const double* __
                 sig[2] = c2 * ev[0] + c2 * ev[1] + c1 * ev[2];
                 sig[3 % NS] = c3 * ev[3 % NS]; sig[4 % NS] = c3 * ev[4 % NS]; sig[5 % NS] = c3 * ev[5 % NS];
             }
-        } else {
+        } else if (with_tan) {
             const double* ct = d.ctan + (size_t)q * E + e;
             const size_t st = (size_t)ngp * E;
 #pragma unroll
@@ -343,6 +351,19 @@ __global__ void __launch_bounds__(128) k_element_tan(DevView d, const double* __
 #pragma unroll
                 for (int bb = 0; bb < NS; ++bb) v += ct[(size_t)(a * NS + bb) * st] * ev[bb];
                 sig[a] = v;
+            }
+        }
+        if (d.dk0) {
+            const double k1 = cc * d.dk0[e], k2 = cc * d.dk0[(size_t)E + e], k3 = cc * d.dk0[2 * (size_t)E + e];
+            if (ND == 2) {
+                sig[0] += k1 * ev[0] + k2 * ev[1];
+                sig[1] += k2 * ev[0] + k1 * ev[1];
+                sig[2] += k3 * ev[2];
+            } else {
+                sig[0] += k1 * ev[0] + k2 * ev[1] + k2 * ev[2];
+                sig[1] += k2 * ev[0] + k1 * ev[1] + k2 * ev[2];
+                sig[2] += k2 * ev[0] + k2 * ev[1] + k1 * ev[2];
+                sig[3 % NS] += k3 * ev[3 % NS]; sig[4 % NS] += k3 * ev[4 % NS]; sig[5 % NS] += k3 * ev[5 % NS];
             }
         }
 #pragma unroll
@@ -387,7 +408,9 @@ __global__ void __launch_bounds__(256) k_node(DevView d) {
         const double fint = gather_fint<ND>(d, n, c);
         const double fext = fext_at(d, t, k);
         const double u = d.U[t], up = d.Up[t];
-        const double R = ((fext + 0.0) - fint) + (d.inv_dt2 * d.Md[t]) * (u - up);
+        // Fext - Fint + (1/dt^2 M - 1/2/dt C)(U - Up)   (CentralDifference.cpp:217)
+        const double mc = d.Cd ? d.inv_dt2 * d.Md[t] - d.inv_2dt * d.Cd[t] : d.inv_dt2 * d.Md[t];
+        const double R = ((fext + 0.0) - fint) + mc * (u - up);
         const double sm = sm_at(d, t, k);
         const int f = d.tfree[t];
         double dut = 0.0;
@@ -415,7 +438,8 @@ __global__ void __launch_bounds__(256) k_residual(DevView d) {
         const int t = d.ntdof[n * ND + c];
         const double fint = gather_fint<ND>(d, n, c);
         const double fext = fext_at(d, t, k);
-        d.R[t] = ((fext + 0.0) - fint) + (d.inv_dt2 * d.Md[t]) * (d.U[t] - d.Up[t]);
+        const double mc = d.Cd ? d.inv_dt2 * d.Md[t] - d.inv_2dt * d.Cd[t] : d.inv_dt2 * d.Md[t];
+        d.R[t] = ((fext + 0.0) - fint) + mc * (d.U[t] - d.Up[t]);
     }
 }
 
@@ -585,8 +609,32 @@ static int cd_setup(svl_cd* cd, const svl_load_desc* L) {
     lumped_mass_diag(m, cd->opts.mtol, Md);
     const double dt = cd->opts.dt;
     const double inv_dt2 = 1.0 / dt / dt;
+    // Rayleigh damping: the mass-proportional diagonal sum_e am_e M_e and the
+    // per-element ak_e-scaled initial elastic coefficients
+    std::vector<double> Cdm, dk0;
+    if (!m.ray.empty()) {
+        rayleigh_mass_diag(m, Cdm);
+        bool any_ak = false;
+        for (int e = 0; e < E; ++e) any_ak |= m.ray[2 * (size_t)e + 1] != 0.0;
+        if (any_ak) {
+            dk0.assign((size_t)3 * E, 0.0);
+            for (int e = 0; e < E; ++e) {
+                const double ak = m.ray[2 * (size_t)e + 1];
+                double c1 = ecoef[e], c2 = ecoef[(size_t)E + e], c3 = ecoef[2 * (size_t)E + e];
+                if (ekind[e] == kMatJ2) {
+                    // K 1(x)1 + 2G (I - 1/3 1(x)1), shear entries 1/2 (PlasticPlaneStrainJ2.cpp:163-180)
+                    const double K = ecoef[e], G = ecoef[(size_t)E + e];
+                    c1 = K * 1.0 + 2.0 * G * (1.0 - 1.0 / 3.0);
+                    c2 = K * 1.0 + 2.0 * G * (0.0 - 1.0 / 3.0);
+                    c3 = 2.0 * G * 0.5;
+                }
+                dk0[e] = ak * c1; dk0[(size_t)E + e] = ak * c2; dk0[2 * (size_t)E + e] = ak * c3;
+            }
+        }
+    }
+    // K = 1/dt/dt M + 1/2/dt C (CentralDifference.cpp:70); C diagonal here
     std::vector<double> Kd(m.ntotal);
-    for (int t = 0; t < m.ntotal; ++t) Kd[t] = inv_dt2 * Md[t];
+    for (int t = 0; t < m.ntotal; ++t) Kd[t] = Cdm.empty() ? inv_dt2 * Md[t] : inv_dt2 * Md[t] + 1.0 / 2.0 / dt * Cdm[t];
     std::vector<int32_t> T_ptr, T_col;
     std::vector<double> T_val;
     build_total_to_free(m, T_ptr, T_col, T_val);
@@ -666,6 +714,8 @@ static int cd_setup(svl_cd* cd, const svl_load_desc* L) {
     TRY(cd->upload(Md, &d.Md));
     TRY(cd->upload(kinv, &d.kinv));
     TRY(cd->upload(Kd, &d.Kd));
+    if (!Cdm.empty()) TRY(cd->upload(Cdm, &d.Cd));
+    if (!dk0.empty()) TRY(cd->upload(dk0, &d.dk0));
     TRY(cd->zeros(m.ntotal, &d.U)); TRY(cd->zeros(m.ntotal, &d.V)); TRY(cd->zeros(m.ntotal, &d.A));
     TRY(cd->zeros(m.ntotal, &d.Up)); TRY(cd->zeros(m.ntotal, &d.Us)); TRY(cd->zeros(m.ntotal, &d.R));
     TRY(cd->zeros(m.nfree, &d.du));
@@ -758,7 +808,18 @@ int svl_set_device(int device) {
     return SVL_OK;
 }
 
+static int cd_create(const svl_model_desc* model, const svl_load_desc* loads, const svl_cd_opts* opts, svl_cd** out,
+                     bool implicit);
+
 int svl_cd_create(const svl_model_desc* model, const svl_load_desc* loads, const svl_cd_opts* opts, svl_cd** out) {
+    return cd_create(model, loads, opts, out, false);
+}
+
+}  // extern "C"
+
+// implicit: the model serves the Newmark path, whose solve takes any damping
+static int cd_create(const svl_model_desc* model, const svl_load_desc* loads, const svl_cd_opts* opts, svl_cd** out,
+                     bool implicit) {
     if (!out || !opts) { set_error("NULL argument"); return SVL_ERR_INVALID; }
     *out = nullptr;
     if (!(opts->dt > 0.0)) { set_error("dt must be positive"); return SVL_ERR_INVALID; }
@@ -772,6 +833,14 @@ int svl_cd_create(const svl_model_desc* model, const svl_load_desc* loads, const
     cd->opts = *opts;
     if (!model_from_desc(model, cd->m)) { delete cd; return SVL_ERR_INVALID; }
     if (!cd->m.lumped) { delete cd; set_error("the explicit path needs a lumped mass (massform LUMPED)"); return SVL_ERR_UNSUPPORTED; }
+    if (!implicit)
+        for (size_t e = 0; e < cd->m.ray.size() / 2; ++e)
+            if (cd->m.ray[2 * e + 1] != 0.0) {
+                delete cd;
+                set_error("element %zu: stiffness-proportional Rayleigh damping (ak) makes the central-difference "
+                          "effective stiffness non-diagonal; use NewmarkBeta", e);
+                return SVL_ERR_UNSUPPORTED;
+            }
     if (cudaStreamCreateWithFlags(&cd->stream, cudaStreamNonBlocking) != cudaSuccess) {
         delete cd; set_error("cudaStreamCreate failed"); return SVL_ERR_CUDA;
     }
@@ -780,6 +849,8 @@ int svl_cd_create(const svl_model_desc* model, const svl_load_desc* loads, const
     *out = cd;
     return SVL_OK;
 }
+
+extern "C" {
 
 int svl_cd_set_initial(svl_cd* cd, const double* U0, const double* V0, const double* A0) {
     if (!cd) { set_error("NULL handle"); return SVL_ERR_INVALID; }
@@ -1152,16 +1223,38 @@ __global__ void k_nmg_expand(DevView d, const double* __restrict__ pf, double* _
     pt[t] = v;
 }
 
-// ft = sum_e K_e p_e + c_m M p on total dofs (ordered gather of d.fe)
+// ft = sum_e K_e p_e + c_m M p (+ c_c C_m p) on total dofs (ordered gather of d.fe)
 template <int ND>
 __global__ void __launch_bounds__(256) k_nmg_total(DevView d, const double* __restrict__ pt, double* __restrict__ ft,
-                                                   double c_m) {
+                                                   double c_m, double c_c) {
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= d.nnode) return;
 #pragma unroll
     for (int c = 0; c < ND; ++c) {
         const int t = d.ntdof[n * ND + c];
-        ft[t] = gather_fint<ND>(d, n, c) + c_m * d.Md[t] * pt[t];
+        double v = gather_fint<ND>(d, n, c) + c_m * d.Md[t] * pt[t];
+        if (d.Cd) v += c_c * d.Cd[t] * pt[t];
+        ft[t] = v;
+    }
+}
+
+// w = V - 2/dt dU_t: the vector the damping acts on in the effective force
+__global__ void k_nmg_wdamp(DevView d, const double* __restrict__ dUt, double c_u, double* __restrict__ w) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < d.ntotal) w[t] = d.V[t] - c_u * dUt[t];
+}
+
+// ft += C w: the element damping vectors in d.fe plus the mass-proportional diagonal
+template <int ND>
+__global__ void __launch_bounds__(256) k_nmg_damp(DevView d, const double* __restrict__ w, double* __restrict__ ft) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= d.nnode) return;
+#pragma unroll
+    for (int c = 0; c < ND; ++c) {
+        const int t = d.ntdof[n * ND + c];
+        double v = d.dk0 ? gather_fint<ND>(d, n, c) : 0.0;
+        if (d.Cd) v += d.Cd[t] * w[t];
+        ft[t] += v;
     }
 }
 
@@ -1421,7 +1514,8 @@ struct svl_nm {
     int64_t train_trial_iters = 0;          // trial-solve iterations of the kept weights
     // Newton: operator scratch block, accumulated increment, iteration counts
     double* fe_op = nullptr;                // [nc][E] element vectors of the operator action
-    bool general = false;                   // constraints (T not identity) or support motion
+    bool general = false;                   // constraints (T not identity), support motion or damping
+    bool damped = false;                    // Rayleigh damping present
     double *ft = nullptr, *dUt = nullptr, *smv = nullptr, *lg = nullptr, *pt2 = nullptr;   // total-dof scratch
     double* dUf = nullptr;                  // [nfree] displacement increment of the step
     bool newton = false, tangent = false;   // tangent: J2 elements present (stored tangents)
@@ -1465,16 +1559,17 @@ static int nm_op_total(svl_nm* nm, const double* pt, double* out) {
     d.ftol = -1.0;
     d.fe = nm->fe_op;
     const int tb = 256, eg = (m.nelem + 127) / 128, ng = (m.nnode + tb - 1) / tb;
-    if (nm->tangent) {
-        if (m.ndim == 2) k_element_tan<2, 4><<<eg, 128, 0, cd->stream>>>(d, pt, m.ngp);
-        else k_element_tan<3, 8><<<eg, 128, 0, cd->stream>>>(d, pt, m.ngp);
+    const double c_c = 2.0 / nm->opts.dt;     // K + 4/dt^2 M + 2/dt C (NewmarkBeta.cpp:231)
+    if (nm->tangent || d.dk0) {
+        if (m.ndim == 2) k_element_tan<2, 4><<<eg, 128, 0, cd->stream>>>(d, pt, m.ngp, 1, c_c);
+        else k_element_tan<3, 8><<<eg, 128, 0, cd->stream>>>(d, pt, m.ngp, 1, c_c);
     } else {
         if (m.ndim == 2) k_element<2, 4><<<eg, 128, 0, cd->stream>>>(d, pt, m.ngp, 0);
         else k_element<3, 8><<<eg, 128, 0, cd->stream>>>(d, pt, m.ngp, 0);
     }
     const double c_m = 4.0 / nm->opts.dt / nm->opts.dt;
-    if (m.ndim == 2) k_nmg_total<2><<<ng, tb, 0, cd->stream>>>(d, pt, out, c_m);
-    else k_nmg_total<3><<<ng, tb, 0, cd->stream>>>(d, pt, out, c_m);
+    if (m.ndim == 2) k_nmg_total<2><<<ng, tb, 0, cd->stream>>>(d, pt, out, c_m, c_c);
+    else k_nmg_total<3><<<ng, tb, 0, cd->stream>>>(d, pt, out, c_m, c_c);
     cd->launches += 2;
     CUDA_TRY(cudaGetLastError());
     return SVL_OK;
@@ -1499,8 +1594,8 @@ static int nm_apply(svl_nm* nm, const double* v, double* q) {
     k_nm_expand<<<(m.ntotal + tb - 1) / tb, tb, 0, cd->stream>>>(d, v, nm->pt);
     const int eg = (m.nelem + 127) / 128;
     if (nm->tangent) {
-        if (m.ndim == 2) k_element_tan<2, 4><<<eg, 128, 0, cd->stream>>>(d, nm->pt, m.ngp);
-        else k_element_tan<3, 8><<<eg, 128, 0, cd->stream>>>(d, nm->pt, m.ngp);
+        if (m.ndim == 2) k_element_tan<2, 4><<<eg, 128, 0, cd->stream>>>(d, nm->pt, m.ngp, 1, 0.0);
+        else k_element_tan<3, 8><<<eg, 128, 0, cd->stream>>>(d, nm->pt, m.ngp, 1, 0.0);
     } else {
         if (m.ndim == 2) k_element<2, 4><<<eg, 128, 0, cd->stream>>>(d, nm->pt, m.ngp, 0);
         else k_element<3, 8><<<eg, 128, 0, cd->stream>>>(d, nm->pt, m.ngp, 0);
@@ -1710,14 +1805,15 @@ int svl_nm_create(const svl_model_desc* model, const svl_load_desc* loads, const
     svl_cd_opts co{};
     co.dt = opts->dt; co.ftol = opts->ftol; co.mtol = opts->mtol; co.precision = SVL_PREC_FP64; co.check_every = 0;
     svl_cd* cd = nullptr;
-    int st = svl_cd_create(model, loads, &co, &cd);
+    int st = cd_create(model, loads, &co, &cd, true);
     if (st) return st;
     svl_nm* nm = new svl_nm();
     nm->cd = cd;
     nm->opts = *opts;
     auto fail = [&](int s2) { delete nm; return s2; };
     const HostModel& m = cd->m;
-    nm->general = !cd->identity_T || cd->has_sm;
+    nm->damped = !m.ray.empty();
+    nm->general = !cd->identity_T || cd->has_sm || nm->damped;
     if (opts->algorithm != SVL_ALGO_LINEAR && opts->algorithm != SVL_ALGO_NEWTON) { set_error("unknown algorithm %d", opts->algorithm); return fail(SVL_ERR_INVALID); }
     nm->newton = opts->algorithm == SVL_ALGO_NEWTON;
     if (nm->newton && (opts->maxit <= 0 || !(opts->cnvgtol >= 0.0) || (opts->cnvgtest != 4 && opts->cnvgtest != 5))) {
@@ -1727,7 +1823,8 @@ int svl_nm_create(const svl_model_desc* model, const svl_load_desc* loads, const
     if (m.has_j2() && !nm->newton) { set_error("the implicit Linear path is elastic; J2 needs Newton iterations"); return fail(SVL_ERR_UNSUPPORTED); }
     nm->tangent = nm->newton && m.has_j2();
     nm->nf = m.nfree;
-    // Jacobi diagonal: diag(K) + 4/dt^2 M on free dofs (identity T)
+    const double c_m = 4.0 / opts->dt / opts->dt, c_c = 2.0 / opts->dt;
+    // Jacobi diagonal: diag(K + 2/dt C) + 4/dt^2 M on free dofs (identity T)
     std::vector<double> Kd(m.ntotal, 0.0);
     const int nc = m.nen * m.ndof;
     for (int e = 0; e < m.nelem; ++e) {
@@ -1758,13 +1855,18 @@ int svl_nm_create(const svl_model_desc* model, const svl_load_desc* loads, const
                 }
             }
         }
+        const double ak = nm->damped ? m.ray[2 * (size_t)e + 1] : 0.0;
         for (int a = 0; a < m.nen; ++a)
-            for (int c = 0; c < m.ndof; ++c) Kd[m.tdof[(size_t)m.conn[(size_t)e * m.nen + a] * m.ndof + c]] += kd[a * m.ndof + c];
+            for (int c = 0; c < m.ndof; ++c) Kd[m.tdof[(size_t)m.conn[(size_t)e * m.nen + a] * m.ndof + c]] += (1.0 + c_c * ak) * kd[a * m.ndof + c];
     }
     std::vector<double> M;
     lumped_mass_diag(m, opts->mtol, M);
+    if (nm->damped) {                       // + 2/dt sum_e am_e M_e
+        std::vector<double> Cm;
+        rayleigh_mass_diag(m, Cm);
+        for (int t = 0; t < m.ntotal; ++t) Kd[t] += c_c * Cm[t];
+    }
     std::vector<double> dinv(std::max(m.nfree, 1), 1.0);
-    const double c_m = 4.0 / opts->dt / opts->dt;
     if (!cd->identity_T) {
         // diagonal of T^T diag(K + c_m M) T (the Jacobi preconditioner only)
         std::vector<int32_t> Tp, Tc;
@@ -1855,6 +1957,8 @@ int svl_nm_set_initial(svl_nm* nm, const double* U0, const double* V0, const dou
 
 }  // extern "C"
 
+static int nmg_rhs(svl_nm* nm);
+
 // Effective force of step k into nm->b (state untouched).
 static int nm_rhs(svl_nm* nm, int k) {
     svl_cd* cd = nm->cd;
@@ -1866,6 +1970,11 @@ static int nm_rhs(svl_nm* nm, int k) {
     k_step_inc<<<1, 1, 0, cd->stream>>>(cd->d.step);
     if (m.ndim == 2) k_element<2, 4><<<eg, 128, 0, cd->stream>>>(cd->d, cd->d.Us, m.ngp, 0);
     else k_element<3, 8><<<eg, 128, 0, cd->stream>>>(cd->d, cd->d.Us, m.ngp, 0);
+    if (nm->general) {
+        k_nmg_sm<<<(m.ntotal + tb - 1) / tb, tb, 0, cd->stream>>>(cd->d, nm->smv);
+        CUDA_TRY(cudaMemsetAsync(nm->dUt, 0, sizeof(double) * m.ntotal, cd->stream));
+        return nmg_rhs(nm);
+    }
     if (m.ndim == 2) k_nm_rhs<2><<<ng, tb, 0, cd->stream>>>(cd->d, nm->b, 4.0 / dt, nullptr, 0.0);
     else k_nm_rhs<3><<<ng, tb, 0, cd->stream>>>(cd->d, nm->b, 4.0 / dt, nullptr, 0.0);
     CUDA_TRY(cudaGetLastError());
@@ -1917,6 +2026,21 @@ static int nmg_rhs(svl_nm* nm) {
     if (m.ndim == 2) k_nmg_rhs<2><<<ng, tb, 0, cd->stream>>>(cd->d, nm->ft, nm->dUt, 4.0 / dt, 4.0 / dt / dt);
     else k_nmg_rhs<3><<<ng, tb, 0, cd->stream>>>(cd->d, nm->ft, nm->dUt, 4.0 / dt, 4.0 / dt / dt);
     cd->launches += 1;
+    if (nm->damped) {
+        // + C (V - 2/dt dU) (NewmarkBeta.cpp:215)
+        DevView d = cd->d;
+        d.fe = nm->fe_op;
+        const int eg = (m.nelem + 127) / 128;
+        k_nmg_wdamp<<<(m.ntotal + tb - 1) / tb, tb, 0, cd->stream>>>(d, nm->dUt, 2.0 / dt, nm->pt2);
+        if (d.dk0) {
+            if (m.ndim == 2) k_element_tan<2, 4><<<eg, 128, 0, cd->stream>>>(d, nm->pt2, m.ngp, 0, 1.0);
+            else k_element_tan<3, 8><<<eg, 128, 0, cd->stream>>>(d, nm->pt2, m.ngp, 0, 1.0);
+            cd->launches += 1;
+        }
+        if (m.ndim == 2) k_nmg_damp<2><<<ng, tb, 0, cd->stream>>>(d, nm->pt2, nm->ft);
+        else k_nmg_damp<3><<<ng, tb, 0, cd->stream>>>(d, nm->pt2, nm->ft);
+        cd->launches += 2;
+    }
     const double* lg = nullptr;
     if (cd->has_sm) {
         // Keff SM (NewmarkBeta::ComputeSupportMotionVector, NewmarkBeta.cpp:180-194)

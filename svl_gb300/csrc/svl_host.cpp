@@ -61,6 +61,15 @@ bool model_from_desc(const svl_model_desc* d, HostModel& m) {
     m.mpar.assign(d->mat_param, d->mat_param + (size_t)m.nmat * SVL_MAT_NPARAM);
     m.nodemass.clear();
     if (d->node_mass) m.nodemass.assign(d->node_mass, d->node_mass + m.ntotal);
+    if (d->elem_rayleigh) {
+        m.ray.assign(d->elem_rayleigh, d->elem_rayleigh + (size_t)2 * m.nelem);
+        bool any = false;
+        for (double v : m.ray) {
+            if (!std::isfinite(v)) { set_error("non-finite Rayleigh coefficient"); return false; }
+            any |= v != 0.0;
+        }
+        if (!any) m.ray.clear();
+    }
     m.lumped = d->lumped;
     m.nconstraint = d->nconstraint;
     m.cslave.clear(); m.cptr.assign(1, 0); m.cmaster.clear(); m.cfactor.clear();
@@ -179,10 +188,10 @@ void parallel_for(int64_t n, const std::function<void(int64_t, int64_t)>& body) 
     for (auto& t : th) t.join();
 }
 
-void lumped_mass_diag(const HostModel& m, double mtol, std::vector<double>& M) {
+// Row-sum lumped mass of every element node, diag[(e*nen + a)*nd + j].
+static void lumped_element_diag(const HostModel& m, std::vector<double>& diag) {
     const int nd = m.ndim, nen = m.nen, nc = nen * m.ndof;
-    // element diagonals in parallel, assembled afterwards in element order
-    std::vector<double> diag((size_t)m.nelem * nen * nd);
+    diag.assign((size_t)m.nelem * nen * nd, 0.0);
     // The consistent mass of a displacement element is block diagonal in the
     // components, Me[(a,j)][(b,j)] = sum_q c_q N_a N_b for every j, so the
     // row-sum lumping (lin2DQuad4.cpp:272-282: the diagonal plus the row's
@@ -209,6 +218,13 @@ void lumped_mass_diag(const HostModel& m, double mtol, std::vector<double>& M) {
             }
         }
     });
+}
+
+void lumped_mass_diag(const HostModel& m, double mtol, std::vector<double>& M) {
+    const int nd = m.ndim, nen = m.nen;
+    // element diagonals in parallel, assembled afterwards in element order
+    std::vector<double> diag;
+    lumped_element_diag(m, diag);
     std::vector<double> Me_e(m.ntotal, 0.0);
     for (int e = 0; e < m.nelem; ++e)
         for (int a = 0; a < nen; ++a)
@@ -221,6 +237,21 @@ void lumped_mass_diag(const HostModel& m, double mtol, std::vector<double>& M) {
         double mn = 0.0;
         if (!m.nodemass.empty() && std::fabs(m.nodemass[t]) > mtol) mn = m.nodemass[t];
         M[t] = Me_e[t] + mn;
+    }
+}
+
+void rayleigh_mass_diag(const HostModel& m, std::vector<double>& C) {
+    const int nd = m.ndim, nen = m.nen;
+    C.assign(m.ntotal, 0.0);
+    if (m.ray.empty()) return;
+    std::vector<double> diag;
+    lumped_element_diag(m, diag);
+    for (int e = 0; e < m.nelem; ++e) {
+        const double am = m.ray[2 * (size_t)e];
+        if (am == 0.0) continue;
+        for (int a = 0; a < nen; ++a)
+            for (int j = 0; j < nd; ++j)
+                C[m.tdof[(size_t)m.conn[(size_t)e * nen + a] * m.ndof + j]] += am * diag[((size_t)e * nen + a) * nd + j];
     }
 }
 

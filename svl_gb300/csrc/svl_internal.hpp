@@ -25,6 +25,7 @@ struct HostModel {
     std::vector<int32_t> mtype;
     std::vector<double> mpar;
     std::vector<double> nodemass;
+    std::vector<double> ray;          // [nelem][2] Rayleigh (am, ak), empty when undamped
     int nconstraint = 0;
     std::vector<int32_t> cslave, cptr, cmaster;
     std::vector<double> cfactor;
@@ -53,6 +54,9 @@ void parallel_for(int64_t n, const std::function<void(int64_t, int64_t)>& body);
 
 // Diagonal of the assembled row-sum-lumped mass on total dofs.
 void lumped_mass_diag(const HostModel& m, double mtol, std::vector<double>& M);
+// Mass-proportional Rayleigh damping on total dofs, sum_e am_e M_e with the
+// element row-sum lumped masses (lin2DQuad4.cpp:360-366 with a lumped mass)
+void rayleigh_mass_diag(const HostModel& m, std::vector<double>& C);
 
 // T (total <- free) rows as CSR over total dofs, sorted columns, duplicates summed.
 void build_total_to_free(const HostModel& m, std::vector<int32_t>& ptr,

@@ -37,6 +37,7 @@ class Model:
     con_factor: Optional[np.ndarray] = None
     lumped: bool = True
     node_mass: Optional[np.ndarray] = None
+    rayleigh: Optional[np.ndarray] = None  # [nelem, 2] (am, ak) or None
     grid_shape: Optional[tuple] = None   # (nx, ny[, nz]) when built by grid()
     _keep: list = field(default_factory=list, repr=False)
 
@@ -75,6 +76,7 @@ class Model:
             con_master=None if self.con_master is None else as_i32(self.con_master),
             con_factor=None if self.con_factor is None else as_f64(self.con_factor),
             node_mass=None if self.node_mass is None else as_f64(self.node_mass),
+            rayleigh=None if self.rayleigh is None else as_f64(self.rayleigh),
         )
         self._keep = list(arrs.values())
         d = capi.ModelDesc()
@@ -101,6 +103,7 @@ class Model:
         d.mat_param = ptr(arrs["mat_param"], C.c_double)
         d.lumped = 1 if self.lumped else 0
         d.node_mass = ptr(arrs["node_mass"], C.c_double)
+        d.elem_rayleigh = ptr(arrs["rayleigh"], C.c_double)
         return d
 
     # ------------------------------------------------------------------

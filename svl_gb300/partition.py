@@ -188,10 +188,23 @@ def load_partition(path, run_dir=None) -> Partition:
     conn = np.array([[npos[int(c)] for c in e["conn"]] for e in els], dtype=np.int32).reshape(len(els), nen)
     elem_mat = np.array([mpos[int(e["attributes"]["material"])] for e in els], dtype=np.int32)
     thick = np.array([float(e["attributes"].get("th", 1.0)) for e in els]) if ndim == 2 else None
-    # dampings: only the undamped case
-    for t, dm in d.get("Dampings", {}).items():
-        if dm["name"].upper() != "FREE":
-            raise PartitionError("damping %s (tag %s) is not covered" % (dm["name"], t))
+    # dampings in ascending tag order, each assigned to its element list
+    # (Driver.hpp:1365-1405); a later tag overrides an earlier one
+    epos = {t: i for i, t in enumerate(etags)}
+    ray = np.zeros((len(etags), 2))
+    for t in sorted(int(x) for x in d.get("Dampings", {})):
+        dm = d["Dampings"][str(t)]
+        name = dm["name"].upper()
+        at = dm.get("attributes", {})
+        if name == "FREE":
+            par = (0.0, 0.0)
+        elif name == "RAYLEIGH":
+            par = (float(at.get("am", 0.0)), float(at.get("ak", 0.0)))
+        else:
+            raise PartitionError("damping %s (tag %d) is not covered" % (dm["name"], t))
+        for e in at.get("list", []):
+            if int(e) in epos:
+                ray[epos[int(e)]] = par
     # nodal masses
     node_mass = None
     if d.get("Masses"):
@@ -215,7 +228,7 @@ def load_partition(path, run_dir=None) -> Partition:
     model = Model(ndim=ndim, coords=coords, totaldof=totaldof, freedof=freedof, conn=conn, elem_type=etype,
                   elem_mat=elem_mat, mat_type=mat_type, mat_param=mat_param,
                   lumped=str(g.get("massform", "CONSISTENT")).upper() == "LUMPED",
-                  thickness=thick, node_mass=node_mass)
+                  thickness=thick, node_mass=node_mass, rayleigh=ray if np.any(ray) else None)
     if con is not None:
         model.con_slave, model.con_ptr, model.con_master, model.con_factor = con
     if model.ntotal != int(g["ntotal"]) or model.nfree != int(g["nfree"]):
@@ -229,7 +242,6 @@ def load_partition(path, run_dir=None) -> Partition:
         raise PartitionError("analysis %s is not covered" % at["analysis"]["name"])
     combo = d["Combinations"][str(sim["combo"])]
     loads = Loads()
-    epos = {t: i for i, t in enumerate(etags)}
     for ltag, fac in zip(combo["attributes"]["load"], combo["attributes"]["factor"]):
         ld = d["Loads"][str(ltag)]
         la = ld["attributes"]

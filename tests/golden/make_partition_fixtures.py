@@ -3,7 +3,8 @@ running the SeismoVLAB pre-processor itself (PP/Core/SeismoVLAB.py
 CreateRunAnalysisFiles) on small models that exercise every field the
 partition reader maps: materials (elastic and J2), restraints, EQUAL
 constraints, point and element body loads (constant and time series),
-support motions, node recorders, the integrator/solver settings.
+support motions, Rayleigh dampings, node recorders, the integrator/solver
+settings.
 
 Run from the repository root where the reference tree is available:
     python tests/golden/make_partition_fixtures.py /path/to/SVL
@@ -156,6 +157,41 @@ SVL.addAnalysis(tag=1, attributes={"name": "Dynamic", "nt": nt})
 SVL.addAlgorithm(tag=1, attributes={"name": "Linear", "nstep": 1})
 SVL.addIntegrator(tag=1, attributes={"name": "CentralDifference", "dt": dt})
 SVL.addSolver(tag=1, attributes={"name": "Eigen", "update": "OFF"})
+SVL.addSimulation(tag=1, combo=1, attributes={"analysis": 1, "algorithm": 1, "integrator": 1, "solver": 1})
+SVL.CreateRunAnalysisFiles()
+''',
+    # Q4 box with two Rayleigh dampings over element groups, Newmark + PETSc CG
+    "q4_newmark_rayleigh": COMMON + r'''
+SVL.Options["dimension"] = 2
+SVL.Options["massform"] = "lumped"
+nx, ny, dt, nt = 6, 4, 2.0e-3, 31
+SVL.addMaterial(tag=1, name="Elastic2DPlaneStrain", attributes={"E": 2.0e8, "nu": 0.25, "rho": 2000.0})
+mesh = SVL.makeDomainArea(options={"ne": [nx, ny], "ndof": 2, "class": "LIN2DQUAD4", "elems": "QUAD4",
+    "P0": [0.0, 0.0], "P1": [nx * 1.0, 0.0], "P2": [0.0, ny * 1.0],
+    "attributes": {"material": 1, "th": 1.0, "rule": "Gauss", "np": 4}})
+for tag in sorted(mesh["Nodes"]):
+    n = mesh["Nodes"][tag]
+    SVL.addNode(tag=tag, ndof=n["ndof"], coords=list(map(float, n["coords"])))
+for tag in sorted(mesh["Elements"]):
+    el = mesh["Elements"][tag]
+    SVL.addElement(tag=tag, conn=list(el["conn"]), name=el["name"], attributes=dict(el["attributes"]))
+for tag in sorted(mesh["Nodes"]):
+    t = tag - 1; i = t % (nx + 1); j = t // (nx + 1)
+    if j == 0:
+        SVL.addRestrain(tag=tag, dof=[1, 2])
+etags = sorted(mesh["Elements"])
+SVL.addDamping(tag=1, name="Rayleigh", attributes={"am": 4.0, "list": [e for e in etags if e % 2 == 1]})
+SVL.addDamping(tag=2, name="Rayleigh", attributes={"am": 2.5, "ak": 1.5e-3, "list": [e for e in etags if e % 2 == 0]})
+write_series("ricker.txt", ricker(nt, dt, 20.0, 1.0e5))
+top = ny * (nx + 1) + nx // 2 + 1
+SVL.addFunction(tag=1, name="TimeSeries", attributes={"file": "ricker.txt", "dir": [1.0, -1.0]})
+SVL.addLoad(tag=1, name="PointLoad", attributes={"type": "Concentrated", "fun": 1, "list": [top]})
+SVL.addCombinationCase(tag=1, name="Fixture", attributes={"load": [1], "factor": [1.0]})
+SVL.addRecorder(tag=1, attributes={"name": "NODE", "file": "Disp.out", "ndps": 8, "resp": "disp", "list": [top]})
+SVL.addAnalysis(tag=1, attributes={"name": "Dynamic", "nt": nt})
+SVL.addAlgorithm(tag=1, attributes={"name": "Linear", "nstep": 1})
+SVL.addIntegrator(tag=1, attributes={"name": "NewmarkBeta", "dt": dt})
+SVL.addSolver(tag=1, attributes={"name": "Petsc", "option": "KSPCG", "tol": 1.0e-12})
 SVL.addSimulation(tag=1, combo=1, attributes={"analysis": 1, "algorithm": 1, "integrator": 1, "solver": 1})
 SVL.CreateRunAnalysisFiles()
 ''',

@@ -49,3 +49,12 @@ def test_newmark_partition_matches_oracle(gpu, tmp_path):
     assert np.abs(ho).max() > 0
     assert rel_l2(U, ho) <= 1e-8            # the file's PETSc tolerance is 1e-10
     assert (tmp_path / p.recorders[0].file).exists()
+
+
+def test_damped_newmark_partition_matches_oracle(gpu, tmp_path):
+    p = _part("q4_newmark_rayleigh")
+    assert np.any(p.model.rayleigh[:, 1] > 0)
+    U = p.run(solution_dir=tmp_path)
+    ho, _ = O.newmark_run(p.model, p.loads, p.dt, p.nt - 1, solver=0)
+    assert np.abs(ho).max() > 0
+    assert rel_l2(U, ho) <= 1e-9            # the file's PETSc tolerance is 1e-12

@@ -1,0 +1,88 @@
+"""Rayleigh damping on the GPU paths, against the oracle.
+
+NewmarkBeta takes C = sum_e (am_e M_e + ak_e K0_e) in its effective force
+C (V - 2/dt dU) and stiffness K + 4/dt^2 M + 2/dt C (NewmarkBeta.cpp:215,
+231): the mass part as a diagonal, the stiffness part as a second element
+action with the initial elastic moduli.  CentralDifference takes the
+mass-proportional part (its effective stiffness stays diagonal,
+CentralDifference.cpp:70, 217) and rejects ak != 0."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from svl_gb300 import CentralDifference, NewmarkBeta, SvlError
+from svl_gb300 import _capi as capi
+from tests.helpers import h8_box, q4_box, rel_l2
+from tests.test_gpu_newton import _columns, j2_box
+
+pytestmark = pytest.mark.gpu
+
+
+def _ray(m, am, ak, seed=0):
+    rng = np.random.default_rng(seed)
+    r = np.zeros((m.nelem, 2))
+    r[:, 0] = am * (0.5 + rng.random(m.nelem))
+    r[:, 1] = ak * (0.5 + rng.random(m.nelem))
+    return r
+
+
+@pytest.mark.parametrize("builder", ["q4", "h8"])
+def test_linear_newmark_rayleigh(gpu, builder):
+    if builder == "q4":
+        m, L, dt = q4_box(16, 8, nt=80)
+    else:
+        m, L, dt = h8_box(6, 5, 4, nt=80)
+    dt = 4 * dt
+    m.rayleigh = _ray(m, 3.0, 2.0e-3)
+    nm = NewmarkBeta(m, L, dt, pcg_tol=1e-13)
+    nm.Initialize()
+    hist = nm.run(1, 60, history=True)
+    nm.close()
+    ho, _ = O.newmark_run(m, L, dt, 60, solver=0)
+    m.rayleigh = None
+    hu, _ = O.newmark_run(m, L, dt, 60, solver=0)
+    assert rel_l2(ho, hu) > 1e-2
+    assert rel_l2(hist, ho) <= 1e-9
+
+
+def test_linear_newmark_rayleigh_constraints_support_motion(gpu):
+    m, L, dt = _columns(elastic=True)
+    m.rayleigh = _ray(m, 2.0, 1.0e-3, seed=3)
+    nm = NewmarkBeta(m, L, 4 * dt, pcg_tol=1e-13)
+    nm.Initialize()
+    hist = nm.run(1, 60, history=True)
+    nm.close()
+    ho, _ = O.newmark_run(m, L, 4 * dt, 60, solver=0)
+    assert np.abs(ho).max() > 0
+    assert rel_l2(hist, ho) <= 1e-9
+
+
+def test_newton_j2_rayleigh_fixed_iterations(gpu):
+    m, L, dt = j2_box(2, (8, 6), amp=4e5, nt=60)
+    m.rayleigh = _ray(m, 2.0, 5.0e-4, seed=5)
+    nm = NewmarkBeta(m, L, dt, pcg_tol=1e-13, algorithm="newton", maxit=3, cnvgtol=0.0, cnvgtest=4)
+    nm.Initialize()
+    hist = nm.run(1, 60, history=True)
+    nm.close()
+    ho, _ = O.newmark_run(m, L, dt, 60, algo=2, maxit=3, cnvgtol=0.0, solver=0)
+    assert rel_l2(hist, ho) <= 1e-9
+
+
+def test_central_difference_mass_proportional(gpu):
+    m, L, dt = q4_box(20, 10, nt=300)
+    m.rayleigh = _ray(m, 8.0, 0.0, seed=1)
+    cd = CentralDifference(m, L, dt)
+    cd.Initialize()
+    hist = cd.run(1, 300, history=True)
+    cd.close()
+    ho, *_ = O.cd_run(m, L, dt, 300)
+    assert np.abs(ho).max() > 0
+    assert rel_l2(hist, ho) <= 1e-12
+
+
+def test_central_difference_rejects_stiffness_proportional(gpu):
+    m, L, dt = q4_box(6, 4, nt=20)
+    m.rayleigh = _ray(m, 0.0, 1e-3)
+    with pytest.raises(SvlError) as ei:
+        CentralDifference(m, L, dt)
+    assert ei.value.code == capi.SVL_ERR_UNSUPPORTED

@@ -19,7 +19,7 @@ def _part(case):
     return GOLD / ("partition_%s" % case) / "Partition" / "Fixture.1.0.json"
 
 
-@pytest.mark.parametrize("case", ["q4_cd", "h8_newmark_body", "q4_j2_column"])
+@pytest.mark.parametrize("case", ["q4_cd", "h8_newmark_body", "q4_j2_column", "q4_newmark_rayleigh"])
 def test_numbering_and_connectivity_follow_the_file(case):
     p = load_partition(_part(case))
     d = json.loads(_part(case).read_text())
@@ -77,12 +77,30 @@ def test_oracle_runs_the_parsed_model(case):
     assert np.all(np.isfinite(h)) and np.abs(h).max() > 0
 
 
+def test_rayleigh_dampings_by_tag_order():
+    """The pre-processor adds a FREE damping over the elements missing from the
+    last damping's list (SeismoVLAB.py's damping check); assigned in ascending
+    tag order (Mesh::SetDamping), it overrides tag 1 on the odd elements."""
+    p = load_partition(_part("q4_newmark_rayleigh"))
+    d = json.loads(_part("q4_newmark_rayleigh").read_text())
+    assert d["Dampings"]["3"]["name"] == "FREE"
+    etags = sorted(int(t) for t in d["Elements"])
+    ray = p.model.rayleigh
+    for i, t in enumerate(etags):
+        assert tuple(ray[i]) == ((2.5, 1.5e-3) if t % 2 == 0 else (0.0, 0.0))
+    assert p.integrator == "NEWMARKBETA"
+    h, _ = O.newmark_run(p.model, p.loads, p.dt, p.nt - 1, solver=0)
+    p.model.rayleigh = None
+    h0, _ = O.newmark_run(p.model, p.loads, p.dt, p.nt - 1, solver=0)
+    assert np.all(np.isfinite(h)) and np.linalg.norm(h - h0) > 1e-3 * np.linalg.norm(h0)
+
+
 def test_uncovered_content_is_named(tmp_path):
     d = json.loads(_part("q4_cd").read_text())
-    d["Dampings"]["1"]["name"] = "RAYLEIGH"
+    d["Dampings"]["1"]["name"] = "CAUGHEY"
     (tmp_path / "Partition").mkdir()
     f = tmp_path / "Partition" / "x.json"
     f.write_text(json.dumps(d))
     (tmp_path / "ricker.txt").write_text((GOLD / "partition_q4_cd" / "ricker.txt").read_text())
-    with pytest.raises(PartitionError, match="RAYLEIGH"):
+    with pytest.raises(PartitionError, match="CAUGHEY"):
         load_partition(f)

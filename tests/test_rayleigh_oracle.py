@@ -1,0 +1,130 @@
+"""Rayleigh damping in the oracle, pinned against a dense textbook restatement.
+
+The oracle assembles C = sum_e (am_e M_e + ak_e K0_e) (lin2DQuad4.cpp:322-372,
+Driver.hpp:1375-1400) into the Newmark effective force and stiffness
+(NewmarkBeta.cpp:215, 231) and, for mass-proportional damping, into the
+central-difference diagonal (CentralDifference.cpp:70, 217).  The checks here
+integrate the same equations with dense numpy matrices built from the
+oracle's element matrices; the undamped runs fix the load-step convention.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from tests.helpers import h8_box, q4_box, rel_l2
+
+
+def _fext(L, ntotal, k):
+    f = np.zeros(ntotal)
+    for d, s, c in zip(L.force_dof, L.force_series, L.force_coef):
+        ser = L.series[s]
+        if 0 <= k < ser.size:
+            f[d] += c * ser[k]
+    return f
+
+
+def _assemble(m, ray):
+    nt = m.ntotal
+    K = np.zeros((nt, nt))
+    M = np.zeros((nt, nt))
+    Cm = np.zeros((nt, nt))
+    nd = m.ndim
+    for e in range(m.nelem):
+        Ke, Ml, _ = O.element_matrices(m, e)
+        dofs = m.totaldof[m.conn[e]].reshape(-1)
+        K[np.ix_(dofs, dofs)] += Ke
+        M[np.ix_(dofs, dofs)] += Ml
+        Cm[np.ix_(dofs, dofs)] += ray[e, 0] * Ml + ray[e, 1] * Ke
+    free = np.full(nt, -1)
+    fd = m.freedof.reshape(-1)
+    td = m.totaldof.reshape(-1)
+    free[td] = fd
+    idx = np.flatnonzero(free >= 0)
+    order = idx[np.argsort(free[idx])]
+    return K, M, Cm, order
+
+
+def _newmark_dense(m, L, dt, nsteps, ray):
+    K, M, C, fr = _assemble(m, ray)
+    nt = m.ntotal
+    U, V, A = np.zeros(nt), np.zeros(nt), np.zeros(nt)
+    Keff = (K + 4.0 / dt ** 2 * M + 2.0 / dt * C)[np.ix_(fr, fr)]
+    hist = np.zeros((nsteps, nt))
+    for i in range(nsteps):
+        k = 1 + i
+        F = _fext(L, nt, k) - K @ U + M @ (4.0 / dt * V + A) + C @ V
+        du = np.zeros(nt)
+        du[fr] = np.linalg.solve(Keff, F[fr])
+        An = 4.0 / dt ** 2 * du - 4.0 / dt * V - A
+        V = 2.0 / dt * du - V
+        A = An
+        U = U + du
+        hist[i] = U
+    return hist
+
+
+def _cd_dense(m, L, dt, nsteps, am):
+    _, M, _, fr = _assemble(m, np.zeros((m.nelem, 2)))
+    Md = np.diag(M).copy()
+    Cd = np.zeros(m.ntotal)
+    for e in range(m.nelem):
+        _, Ml, _ = O.element_matrices(m, e)
+        dofs = m.totaldof[m.conn[e]].reshape(-1)
+        Cd[dofs] += am[e] * np.diag(Ml)
+    K, *_ = _assemble(m, np.zeros((m.nelem, 2)))
+    nt = m.ntotal
+    U, Up = np.zeros(nt), np.zeros(nt)
+    hist = np.zeros((nsteps, nt))
+    for i in range(nsteps):
+        k = 1 + i
+        R = _fext(L, nt, k) - K @ U + (Md / dt ** 2 - Cd / (2 * dt)) * (U - Up)
+        du = np.zeros(nt)
+        du[fr] = R[fr] / (Md / dt ** 2 + Cd / (2 * dt))[fr]
+        Up = U
+        U = U + du
+        hist[i] = U
+    return hist
+
+
+def _ray(m, am, ak, seed=0):
+    rng = np.random.default_rng(seed)
+    r = np.zeros((m.nelem, 2))
+    r[:, 0] = am * (0.5 + rng.random(m.nelem))
+    r[:, 1] = ak * (0.5 + rng.random(m.nelem))
+    return r
+
+
+@pytest.mark.parametrize("builder", ["q4", "h8"])
+def test_newmark_rayleigh_matches_dense_restatement(builder):
+    if builder == "q4":
+        m, L, dt = q4_box(8, 5, nt=60)
+    else:
+        m, L, dt = h8_box(3, 3, 2, nt=60)
+    dt = 4 * dt
+    # undamped: fixes the load-index convention of the restatement
+    h0, _ = O.newmark_run(m, L, dt, 40)
+    assert rel_l2(_newmark_dense(m, L, dt, 40, np.zeros((m.nelem, 2))), h0) <= 1e-9
+    m.rayleigh = _ray(m, 3.0, 2.0e-3)
+    h1, _ = O.newmark_run(m, L, dt, 40)
+    hd = _newmark_dense(m, L, dt, 40, m.rayleigh)
+    assert rel_l2(hd, h1) <= 1e-9
+    assert rel_l2(h1, h0) > 1e-2                  # the damping changes the response
+    assert np.linalg.norm(h1[-10:]) < np.linalg.norm(h0[-10:])
+
+
+def test_central_difference_mass_proportional_damping():
+    m, L, dt = q4_box(10, 6, nt=200)
+    am = 8.0 * (0.5 + np.random.default_rng(1).random(m.nelem))
+    h0, *_ = O.cd_run(m, L, dt, 200)
+    m.rayleigh = np.stack([am, np.zeros(m.nelem)], axis=1)
+    h1, *_ = O.cd_run(m, L, dt, 200)
+    hd = _cd_dense(m, L, dt, 200, am)
+    assert rel_l2(hd, h1) <= 1e-10
+    assert rel_l2(h1, h0) > 1e-3
+
+
+def test_central_difference_rejects_stiffness_proportional_damping():
+    m, L, dt = q4_box(4, 3, nt=10)
+    m.rayleigh = np.tile([0.0, 1e-3], (m.nelem, 1))
+    with pytest.raises(RuntimeError):
+        O.cd_run(m, L, dt, 5)
