@@ -7,8 +7,10 @@
 //      shared memory;
 //   2. computes those elements' internal forces as a tcgen05 GEMM, 128
 //      elements per MMA tile:  D[128 x 48] = U_e[128 x 24] . [K_lambda; K_mu]^T,
-//      with TF32 hi/lo operands (hi.hi + hi.lo + lo.hi, FP32 accumulation in
-//      TMEM), then F_e = lambda_e D[:, 0:24] + mu_e D[:, 24:48];
+//      with TF32 hi/lo operands (lo.hi + hi.lo + hi.hi accumulated in one FP32
+//      TMEM accumulator; eight accumulator slots so the MMAs of the next tile
+//      run while the update of this one is in progress), then
+//      F_e = lambda_e D[:, 0:24] + mu_e D[:, 24:48];
 //   3. gathers the eight element contributions of every owned node in the
 //      reference's element-tag order (no atomics) and updates
 //      u_{n+1} = u_n + (u_n - u_{n-1}) + (dt^2/m)(f_ext - f_int)
@@ -93,7 +95,8 @@ constexpr int OFF_OWN = OFF_TT + 2 * TT_STRIDE;                  // owned: u_n l
 constexpr int OWN_ULC = 0, OWN_UHP = OWN_BYTES, OWN_ULP = 2 * OWN_BYTES, OWN_CD = 3 * OWN_BYTES;
 constexpr int OFF_F = align_up(OFF_OWN + 4 * OWN_BYTES, 128);    // element forces
 constexpr int OFF_BAR = align_up(OFF_F + NEL * FSTRIDE * 4, 16);
-constexpr int NBAR = 11;                                      // tma[2] a_full[2] a_empty[2] d_full[2] d_empty[2] own
+constexpr int NDB = 8;                                        // accumulator slots in TMEM (a tile's 6 M-tiles fit)
+constexpr int NBAR = 7 + 2 * NDB;                             // tma[2] a_full[2] a_empty[2] own d_full[NDB] d_empty[NDB]
 constexpr int OFF_TMEM = OFF_BAR + NBAR * 8;
 constexpr int SMEM_BYTES = OFF_TMEM + 16;
 static_assert(OFF_A % 1024 == 0 && A_STRIDE % 1024 == 0, "MMA operands on 1 KB boundaries");
@@ -103,9 +106,9 @@ static_assert(OFF_F % 16 == 0 && OFF_BAR % 8 == 0 && OFF_TMEM % 4 == 0, "alignme
 static_assert(SMEM_BYTES <= 227 * 1024, "shared memory budget");
 static_assert(TX * TY * TZ <= 3 * NUPD, "three owned nodes per update thread at most");
 
-constexpr uint32_t TMEM_COLS = 512;     // two buffers of [hi chain: 96 cols | lo chain: 48 cols]
-constexpr uint32_t ACC_COLS = 256;
-constexpr uint32_t LO_COLS = 128;       // offset of the lo chain inside a buffer
+constexpr uint32_t ACC_COLS = 64;       // 48 accumulator columns per slot
+constexpr uint32_t TMEM_COLS = NDB * ACC_COLS;
+constexpr uint32_t B_LO_OFF = (48 / 8) * SBO;   // K lo rows of the B image
 constexpr long kWaitLimit = 4000000;    // bounded mbarrier wait
 
 // Instruction descriptors for tcgen05.mma.kind::tf32: D = F32 (bits 4-5),
@@ -114,7 +117,6 @@ constexpr long kWaitLimit = 4000000;    // bounded mbarrier wait
 constexpr uint32_t idesc_tf32(uint32_t m, uint32_t n) {
     return (1u << 4) | (2u << 7) | (2u << 10) | ((n >> 3) << 17) | ((m >> 4) << 24);
 }
-constexpr uint32_t kIdescN96 = idesc_tf32(128, 96);
 constexpr uint32_t kIdescN48 = idesc_tf32(128, 48);
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -264,9 +266,9 @@ k_cdx_step(const __grid_constant__ CUtensorMap tmap_u, const __grid_constant__ C
 #define B_TMA(b) (bar0 + 8u * (uint32_t)(b))
 #define B_AFULL(b) (bar0 + 16u + 8u * (uint32_t)(b))
 #define B_AEMPTY(b) (bar0 + 32u + 8u * (uint32_t)(b))
-#define B_DFULL(b) (bar0 + 48u + 8u * (uint32_t)(b))
-#define B_DEMPTY(b) (bar0 + 64u + 8u * (uint32_t)(b))
-    const uint32_t b_own = bar0 + 80u;
+#define B_DFULL(b) (bar0 + 56u + 8u * (uint32_t)(b))
+#define B_DEMPTY(b) (bar0 + 56u + 8u * NDB + 8u * (uint32_t)(b))
+    const uint32_t b_own = bar0 + 48u;
 // phase bits of two-slot barriers packed in one word
 #define PH(w, b) (((w) >> (b)) & 1u)
 #define FLIP(w, b) ((w) ^= (1u << (b)))
@@ -287,6 +289,8 @@ k_cdx_step(const __grid_constant__ CUtensorMap tmap_u, const __grid_constant__ C
             mbar_init(B_TMA(b), 1);
             mbar_init(B_AFULL(b), NBUILD);
             mbar_init(B_AEMPTY(b), 1);
+        }
+        for (int b = 0; b < NDB; ++b) {
             mbar_init(B_DFULL(b), 1);
             mbar_init(B_DEMPTY(b), NEPI);
         }
@@ -369,28 +373,29 @@ k_cdx_step(const __grid_constant__ CUtensorMap tmap_u, const __grid_constant__ C
             }
         }
     } else if (warp == ISSUE_WARP) {
-        // ===== MMA issuer: two independent accumulator chains per M-tile =====
+        // ===== MMA issuer: D = A_lo K_hi + A_hi K_lo + A_hi K_hi in one accumulator =====
         if (lane == 0) {
-            uint32_t ph_afull = 0u, ph_dempty = 3u;
+            uint32_t ph_afull = 0u, ph_dempty = (1u << NDB) - 1u;
             const uint32_t bB = smem_u32(smem + OFF_B);
             const int total = ntile_cta * NMT;
             for (int mt = 0; mt < total && ok; ++mt) {
-                const int b = mt & 1;
-                ok = mbar_wait(B_AFULL(b), PH(ph_afull, b)) && mbar_wait(B_DEMPTY(b), PH(ph_dempty, b));
+                const int b = mt & 1, db = mt % NDB;
+                ok = mbar_wait(B_AFULL(b), PH(ph_afull, b)) && mbar_wait(B_DEMPTY(db), PH(ph_dempty, db));
                 FLIP(ph_afull, b);
-                FLIP(ph_dempty, b);
+                FLIP(ph_dempty, db);
                 if (!ok) break;
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                 const uint32_t a_hi = smem_u32(smem + OFF_A + b * A_STRIDE), a_lo = a_hi + A_BYTES;
-                const uint32_t d = tmem + (uint32_t)b * ACC_COLS;
+                const uint32_t d = tmem + (uint32_t)db * ACC_COLS;
 #pragma unroll
                 for (int ks = 0; ks < KDIM / 8; ++ks) {       // three K=8 steps (2 core matrices each)
                     const uint32_t koff = ks * 2 * LBO;
-                    // [d, d+96): A_hi . [K hi; K lo]     [d+128, d+176): A_lo . K hi
-                    mma_tf32(d, make_desc(a_hi + koff), make_desc(bB + koff), kIdescN96, ks > 0);
-                    mma_tf32(d + LO_COLS, make_desc(a_lo + koff), make_desc(bB + koff), kIdescN48, ks > 0);
+                    // the two small correction products first, then the main one
+                    mma_tf32(d, make_desc(a_lo + koff), make_desc(bB + koff), kIdescN48, ks > 0);
+                    mma_tf32(d, make_desc(a_hi + koff), make_desc(bB + B_LO_OFF + koff), kIdescN48, 1);
+                    mma_tf32(d, make_desc(a_hi + koff), make_desc(bB + koff), kIdescN48, 1);
                 }
-                mma_commit(B_DFULL(b));
+                mma_commit(B_DFULL(db));
                 mma_commit(B_AEMPTY(b));
             }
         }
@@ -420,7 +425,7 @@ k_cdx_step(const __grid_constant__ CUtensorMap tmap_u, const __grid_constant__ C
             if (warp >= EPI_WARP0) {
                 const int q = warp - EPI_WARP0;                   // TMEM lane quarter
                 for (int t = 0; t < NMT; ++t, ++mt) {
-                    const int b = mt & 1;
+                    const int b = mt % NDB;
                     ok = ok && mbar_wait(B_DFULL(b), PH(ph_dfull, b));
                     FLIP(ph_dfull, b);
                     if (!ok) break;
@@ -429,34 +434,16 @@ k_cdx_step(const __grid_constant__ CUtensorMap tmap_u, const __grid_constant__ C
                     const int le = t * 128 + q * 32 + lane;
                     const int lx = le % EX, lr = min(le, NEL - 1) / EX;          // lr = lz*EY + ly
                     const float l = tlam[lr * LMX + LM_SHIFT + lx], mu = tmu[lr * LMX + LM_SHIFT + lx];
-                    float f[24];
-                    // hi chain: cols 0-23 K_lambda.u, 24-47 K_mu.u (K hi), 48-95 the same with K lo;
-                    // lo chain: cols 128-151 K_lambda.u_lo, 152-175 K_mu.u_lo (K hi)
+                    // cols 0-23 K_lambda u, 24-47 K_mu u
+                    float dv[48];
 #pragma unroll
-                    for (int g = 0; g < 3; ++g) {
-                        float a[8], c[8], e[8];
-                        tmem_ld<8>(row + 8 * g, a);
-                        tmem_ld<8>(row + 48 + 8 * g, c);
-                        tmem_ld<8>(row + LO_COLS + 8 * g, e);
-                        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-                        for (int i2 = 0; i2 < 8; ++i2) f[8 * g + i2] = l * (a[i2] + c[i2] + e[i2]);
-                    }
-#pragma unroll
-                    for (int g = 0; g < 3; ++g) {
-                        float a[8], c[8], e[8];
-                        tmem_ld<8>(row + 24 + 8 * g, a);
-                        tmem_ld<8>(row + 72 + 8 * g, c);
-                        tmem_ld<8>(row + LO_COLS + 24 + 8 * g, e);
-                        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-                        for (int i2 = 0; i2 < 8; ++i2) f[8 * g + i2] += mu * (a[i2] + c[i2] + e[i2]);
-                    }
+                    for (int g = 0; g < 6; ++g) tmem_ld<8>(row + 8 * g, dv + 8 * g);
+                    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
                     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
                     mbar_arrive(B_DEMPTY(b));
                     if (le < NEL) {
 #pragma unroll
-                        for (int jj = 0; jj < 24; ++jj) sF[le * FSTRIDE + jj] = f[jj];
+                        for (int jj = 0; jj < 24; ++jj) sF[le * FSTRIDE + jj] = l * dv[jj] + mu * dv[24 + jj];
                     }
                 }
             } else {
