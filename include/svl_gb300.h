@@ -96,6 +96,15 @@ typedef struct svl_model_desc {
      * C_e = am M_e + ak K0_e with K0 the initial stiffness (lin2DQuad4.cpp:322-372,
      * lin3DHexa8.cpp).  [nelem][2] = {am, ak}, or NULL for undamped elements. */
     const double*  elem_rayleigh;
+    /* Perfectly matched layers (PML2DQuad4 / PML3DHexa8, Driver.hpp:1203-1220,
+     * 1288-1306).  The nodes of PML elements carry 5 (2D: ux uy s11 s22 s12) or
+     * 9 (3D: ux uy uz s11 s22 s33 s12 s23 s13) dofs; `ndof` is then the row
+     * stride of totaldof/freedof and node_ndof gives each node's count.  Solid
+     * elements use the first ndim dofs of their nodes (lin2DQuad4.cpp:130-147),
+     * PML elements all of them (PML2DQuad4.cpp:130-147).  Served by svl_xnm_*. */
+    const int32_t* node_ndof;       /* [nnode], or NULL: every node has ndof dofs   */
+    const int32_t* elem_pml;        /* [nelem] 1 for a PML element, or NULL         */
+    const double*  elem_pml_param;  /* [nelem][3 + 2 ndim]: n, L, R, x0[ndim], npml[ndim] */
 } svl_model_desc;
 
 /* ---- loads -------------------------------------------------------------- */

@@ -33,6 +33,8 @@ def lib():
         L.oracle_j2_path.argtypes = [C.c_int, f64p, C.c_int, f64p, f64p]
         L.oracle_pml_matrices.argtypes = [C.c_int, f64p, C.c_double, C.c_double, C.c_double, C.c_double, f64p,
                                           f64p, f64p, f64p, f64p]
+        L.oracle_xnewmark_run.argtypes = [vp, vp, C.c_double, C.c_int, C.c_int, f64p, f64p, f64p, f64p, f64p]
+        L.oracle_xnewmark_matrices.argtypes = [vp, f64p, f64p, f64p, f64p]
         _lib = L
     return _lib
 
@@ -150,4 +152,31 @@ def pml_matrices(ndim, X, E, nu, rho, par, t=1.0):
     st = lib().oracle_pml_matrices(int(ndim), Xa.ctypes.data_as(f64), float(E), float(nu), float(rho), float(t),
                                    pa.ctypes.data_as(f64), *[o.ctypes.data_as(f64) for o in out])
     assert st == 0
+    return out
+
+
+def xnewmark_run(model, loads, dt, nsteps, k_first=1):
+    """ExtendedNewmarkBeta + Linear with PML elements (dense LDL^T).  Returns
+    (history of U [nsteps, ntotal], final U, V, A, Ubar)."""
+    md = model.desc()
+    ld = loads.desc() if loads is not None else None
+    nt = model.ntotal
+    hist = np.zeros((nsteps, nt))
+    U, V, A, Ub = (np.zeros(nt) for _ in range(4))
+    f = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))  # noqa: E731
+    st = lib().oracle_xnewmark_run(C.addressof(md), C.addressof(ld) if ld is not None else None, dt, k_first,
+                                   nsteps, f(hist), f(U), f(V), f(A), f(Ub))
+    if st != 0:
+        raise RuntimeError("oracle_xnewmark_run failed with status %d" % st)
+    return hist, U, V, A, Ub
+
+
+def xnewmark_matrices(model):
+    """Dense total-dof K, M, C, G of an ExtendedNewmark model (small models)."""
+    nt = model.ntotal
+    out = [np.zeros((nt, nt)) for _ in range(4)]
+    md = model.desc()
+    st = lib().oracle_xnewmark_matrices(C.addressof(md), *(o.ctypes.data_as(C.POINTER(C.c_double)) for o in out))
+    if st != 0:
+        raise RuntimeError("oracle_xnewmark_matrices failed with status %d" % st)
     return out

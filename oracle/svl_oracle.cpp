@@ -46,7 +46,11 @@ const double kGauss = 0.577350269189626;
 struct Model {
     int ndim, nnode, ndof, ntotal, nfree, nelem, nen, ngp, nstr, etype;
     std::vector<double> X;            // [nnode][ndim]
-    std::vector<int> tdof, fdof;      // [nnode][ndof]
+    std::vector<int> tdof, fdof;      // [nnode][ndof] the first ndim dofs (ndof = ndim)
+    int dstride;                      // stride of the descriptor's dof rows
+    std::vector<int> nndof, tdof_all, fdof_all;   // every dof of a node (PML nodes 5 / 9)
+    std::vector<int> epml;            // [nelem] PML flag, empty without PML
+    std::vector<double> pml_par;      // [nelem][3 + 2 ndim]
     std::vector<int> conn, emat;
     std::vector<double> thick;
     std::vector<int> mtype;
@@ -81,10 +85,34 @@ bool load_model(const svl_model_desc* d, Model& m) {
     if (m.etype == SVL_ELEM_LIN2DQUAD4) { m.nen = 4; m.ngp = 4; m.nstr = 3; if (m.ndim != 2) return false; }
     else if (m.etype == SVL_ELEM_LIN3DHEXA8) { m.nen = 8; m.ngp = 8; m.nstr = 6; if (m.ndim != 3) return false; }
     else return false;
-    if (m.ndof != m.ndim) return false;
+    const int pnd = m.ndim == 2 ? 5 : 9;
+    m.dstride = d->ndof;
+    if (m.dstride != m.ndim && m.dstride != pnd) return false;
+    m.ndof = m.ndim;
     m.X.assign(d->coords, d->coords + (size_t)m.nnode * m.ndim);
-    m.tdof.assign(d->totaldof, d->totaldof + (size_t)m.nnode * m.ndof);
-    m.fdof.assign(d->freedof, d->freedof + (size_t)m.nnode * m.ndof);
+    m.nndof.assign(m.nnode, m.dstride);
+    if (d->node_ndof) m.nndof.assign(d->node_ndof, d->node_ndof + m.nnode);
+    m.tdof_all.assign((size_t)m.nnode * m.dstride, -1);
+    m.fdof_all.assign((size_t)m.nnode * m.dstride, -1);
+    m.tdof.assign((size_t)m.nnode * m.ndim, -1);
+    m.fdof.assign((size_t)m.nnode * m.ndim, -1);
+    for (int n = 0; n < m.nnode; ++n)
+        for (int j = 0; j < m.nndof[n]; ++j) {
+            const size_t i = (size_t)n * m.dstride + j;
+            m.tdof_all[i] = d->totaldof[i]; m.fdof_all[i] = d->freedof[i];
+            if (j < m.ndim) { m.tdof[(size_t)n * m.ndim + j] = d->totaldof[i]; m.fdof[(size_t)n * m.ndim + j] = d->freedof[i]; }
+        }
+    m.epml.clear(); m.pml_par.clear();
+    if (d->elem_pml) {
+        bool any = false;
+        for (int e = 0; e < m.nelem; ++e) any |= d->elem_pml[e] != 0;
+        if (any) {
+            if (!d->elem_pml_param) return false;
+            m.epml.assign(m.nelem, 0);
+            for (int e = 0; e < m.nelem; ++e) m.epml[e] = d->elem_pml[e] != 0;
+            m.pml_par.assign(d->elem_pml_param, d->elem_pml_param + (size_t)m.nelem * (3 + 2 * m.ndim));
+        }
+    }
     m.conn.assign(d->conn, d->conn + (size_t)m.nelem * m.nen);
     m.emat.assign(d->elem_mat, d->elem_mat + m.nelem);
     m.thick.assign(m.nelem, 1.0);
@@ -449,8 +477,8 @@ struct Sim {
     void build_T() {
         std::vector<std::vector<std::pair<int, double>>> rows(m.ntotal);
         for (int n = 0; n < m.nnode; ++n)
-            for (int j = 0; j < m.ndof; ++j) {
-                int f = m.fdof[(size_t)n * m.ndof + j], t = m.tdof[(size_t)n * m.ndof + j];
+            for (int j = 0; j < m.nndof[n]; ++j) {
+                int f = m.fdof_all[(size_t)n * m.dstride + j], t = m.tdof_all[(size_t)n * m.dstride + j];
                 if (f > -1) rows[t].push_back({f, 1.0});
             }
         for (int c = 0; c < m.nconstraint; ++c)
@@ -667,7 +695,7 @@ struct CD {
 
     bool init(const svl_model_desc* d, const svl_load_desc* l, double dt_, double ftol, double mtol) {
         if (!s.init(d, l)) return false;
-        if (!s.m.lumped) return false;
+        if (!s.m.lumped || !s.m.epml.empty()) return false;
         dt = dt_; s.ftol = ftol; s.mtol = mtol;
         const int nt = s.m.ntotal;
         U.assign(nt, 0); V.assign(nt, 0); A.assign(nt, 0); Up.assign(nt, 0); Us.assign(nt, 0);
@@ -899,6 +927,7 @@ struct Newmark {
 
     bool init(const svl_model_desc* d, const svl_load_desc* l, double dt_) {
         if (!s.init(d, l)) return false;
+        if (!s.m.epml.empty()) return false;       // PML: XNewmark
         dt = dt_;
         const int nt = s.m.ntotal;
         U.assign(nt, 0); V.assign(nt, 0); A.assign(nt, 0);
@@ -1207,6 +1236,176 @@ void pml_matrices(int nd, const double* X, double E, double nu, double rho, doub
 
 }  // namespace
 
+/* ---------------- ExtendedNewmarkBeta with PML (ExtendedNewmarkBeta.cpp) -- */
+
+/* ExtendedNewmarkBeta::ComputeNewStep with the Linear algorithm on a mesh of
+ * elastic solid elements (lin2DQuad4/lin3DHexa8, first ndim dofs of their
+ * nodes) and PML elements (PML2DQuad4/PML3DHexa8, every dof of their nodes):
+ *   M, C, K, G assembled once (ExtendedNewmarkBeta.cpp:64-70, Assembler.cpp
+ *   48-205) in element-tag order, M with the mass tolerance, C, K, G with the
+ *   stiffness tolerance; PML mass consistent (PML3DHexa8.cpp:214-284, the 2D
+ *   lumping is a TODO in PML2DQuad4.cpp:286-289); solid C Rayleigh, PML C its own;
+ *   Feff = Fext - Fint - G (Ubar + dt U + dt^2/6 V) + C V + M (4/dt V + A)  (:208-229)
+ *   Keff = K + 4/dt^2 M + 2/dt C + dt/3 G                                   (:233-245)
+ *   Feff -= T^T Keff SM(k)                                                  (:190-204)
+ *   dU = T du; Ubar += dt U + dt/3 (dU + SM) + dt^2/6 V; U += dU + SM;
+ *   A = 4/dt^2 dU - 4/dt V - A; V = 2/dt dU - V                             (:123-153)
+ * Fint: solid elements from their material state (strain of U + T du of the
+ * last step), PML elements K_e U_e with U the displacement after the last
+ * step (PML3DHexa8.cpp:716-742 with zero node increments after UpdateDomain). */
+struct XNewmark {
+    Sim s; double dt;
+    std::vector<double> U, V, A, Ubar;
+    CSR Kt, Mt, Ct, Gt;
+    std::vector<std::vector<int>> edof;      // per element: solid nen*ndim, PML nen*(5|9)
+    int solver = 0; double pcg_tol = 1e-12;
+
+    bool pml(int e) const { return !s.m.epml.empty() && s.m.epml[e]; }
+    void pml_elem(int e, double* Me, double* Ce, double* Ke, double* Ge) const {
+        const Model& m = s.m;
+        double X[8 * 3];
+        for (int a = 0; a < m.nen; ++a)
+            for (int i = 0; i < m.ndim; ++i) X[a * m.ndim + i] = m.X[(size_t)m.conn[(size_t)e * m.nen + a] * m.ndim + i];
+        const double* p = s.mp(e);
+        pml_matrices(m.ndim, X, p[0], p[1], p[2], m.ndim == 2 ? m.thick[e] : 1.0,
+                     &m.pml_par[(size_t)e * (3 + 2 * m.ndim)], Me, Ce, Ke, Ge);
+    }
+    bool init(const svl_model_desc* d, const svl_load_desc* l, double dt_) {
+        if (!s.init(d, l)) return false;
+        dt = dt_;
+        const Model& m = s.m;
+        for (int t : m.mtype)
+            if (t != SVL_MAT_ELASTIC2DPLANESTRAIN && t != SVL_MAT_ELASTIC3DLINEAR) return false;
+        const int nt = m.ntotal, pnd = m.ndim == 2 ? 5 : 9;
+        U.assign(nt, 0); V.assign(nt, 0); A.assign(nt, 0); Ubar.assign(nt, 0);
+        edof.resize(m.nelem);
+        for (int e = 0; e < m.nelem; ++e) {
+            const int k = pml(e) ? pnd : m.ndim;
+            for (int a = 0; a < m.nen; ++a) {
+                const int n = m.conn[(size_t)e * m.nen + a];
+                if (k > m.nndof[n]) return false;
+                for (int j = 0; j < k; ++j) edof[e].push_back(m.tdof_all[(size_t)n * m.dstride + j]);
+            }
+        }
+        std::vector<Trip> tk, tm, tc, tg;
+        const int ncmax = m.nen * pnd;
+        std::vector<double> Me((size_t)ncmax * ncmax), Ce(Me.size()), Ke(Me.size()), Ge(Me.size()), K0(Me.size());
+        auto push = [&](std::vector<Trip>& tr, int e, const double* A_, double tol) {
+            const int nc = (int)edof[e].size();
+            for (int j = 0; j < nc; ++j)
+                for (int i = 0; i < nc; ++i) {
+                    const double v = A_[(size_t)i * nc + j];
+                    if (std::fabs(v) > tol) tr.push_back({edof[e][i], edof[e][j], v});
+                }
+        };
+        for (int e = 0; e < m.nelem; ++e) {
+            const int nc = (int)edof[e].size();
+            if (pml(e)) {
+                pml_elem(e, Me.data(), Ce.data(), Ke.data(), Ge.data());
+                push(tm, e, Me.data(), s.mtol);
+                push(tc, e, Ce.data(), s.ktol);
+                push(tk, e, Ke.data(), s.ktol);
+                if (m.ndim == 3) push(tg, e, Ge.data(), s.ktol);     // PML2DQuad4 has no history matrix
+            } else {
+                s.element_M(e, Me.data(), m.lumped != 0);
+                s.element_K(e, Ke.data());
+                push(tm, e, Me.data(), s.mtol);
+                push(tk, e, Ke.data(), s.ktol);
+                if (!m.ray.empty()) {
+                    const double am = m.ray[2 * e], ak = m.ray[2 * e + 1];
+                    s.element_K0(e, K0.data());
+                    for (int i = 0; i < nc * nc; ++i) Ce[i] = am * Me[i] + ak * K0[i];
+                    push(tc, e, Ce.data(), s.ktol);
+                }
+            }
+        }
+        if (!m.nodemass.empty())
+            for (int t = 0; t < nt; ++t) if (std::fabs(m.nodemass[t]) > s.mtol) tm.push_back({t, t, m.nodemass[t]});
+        csr_from_triplets(nt, tk, Kt); csr_from_triplets(nt, tm, Mt);
+        csr_from_triplets(nt, tc, Ct); csr_from_triplets(nt, tg, Gt);
+        return true;
+    }
+    void set_initial(const double* U0, const double* V0, const double* A0, const double* Ub0) {
+        const int nt = s.m.ntotal;
+        for (int t = 0; t < nt; ++t) {
+            U[t] = U0 ? U0[t] : 0.0; V[t] = V0 ? V0[t] : 0.0; A[t] = A0 ? A0[t] : 0.0; Ubar[t] = Ub0 ? Ub0[t] : 0.0;
+        }
+        // solid element states from the initial displacement
+        for (int e = 0; e < s.m.nelem; ++e) if (!pml(e)) s.element_update(e, U);
+        s.commit_all();
+    }
+    // total effective stiffness K + 4/dt^2 M + 2/dt C + dt/3 G
+    void keff_total(CSR& Kt_eff) const {
+        std::vector<Trip> tr;
+        auto add = [&](const CSR& A_, double c) {
+            for (int r = 0; r < A_.n; ++r) for (int i = A_.ptr[r]; i < A_.ptr[r + 1]; ++i) tr.push_back({r, A_.col[i], c * A_.val[i]});
+        };
+        add(Kt, 1.0); add(Mt, 4.0 / dt / dt); add(Ct, 2.0 / dt); add(Gt, dt / 3.0);
+        csr_from_triplets(s.m.ntotal, tr, Kt_eff);
+    }
+    int step(int k) {
+        const Model& m = s.m;
+        const int nt = m.ntotal, nf = m.nfree;
+        // Fint in element order with the force filter
+        std::vector<double> Fint(nt, 0.0), Fext, w(nt), MW, CV, GW, F(nt), Feff, SM, du, dUt;
+        double fe[72], ue[72];
+        std::vector<double> Ke(72 * 72);
+        for (int e = 0; e < m.nelem; ++e) {
+            const int nc = (int)edof[e].size();
+            if (pml(e)) {
+                pml_elem(e, nullptr, nullptr, Ke.data(), nullptr);
+                for (int i = 0; i < nc; ++i) ue[i] = U[edof[e][i]];
+                for (int i = 0; i < nc; ++i) {
+                    double v = 0.0;
+                    for (int j = 0; j < nc; ++j) v += Ke[(size_t)i * nc + j] * ue[j];
+                    fe[i] = v;
+                }
+            } else {
+                s.element_fint(e, fe);
+            }
+            for (int j = 0; j < nc; ++j) if (std::fabs(fe[j]) > s.ftol) Fint[edof[e][j]] += fe[j];
+        }
+        s.fext(k, Fext);
+        for (int t = 0; t < nt; ++t) w[t] = 4.0 / dt * V[t] + A[t];
+        csr_mv(Mt, w, MW);
+        csr_mv(Ct, V, CV);
+        for (int t = 0; t < nt; ++t) w[t] = Ubar[t] + dt * U[t] + dt * dt / 6.0 * V[t];
+        csr_mv(Gt, w, GW);
+        for (int t = 0; t < nt; ++t) F[t] = (((Fext[t] + 0.0 - Fint[t]) - GW[t]) + CV[t]) + MW[t];
+        s.TT_apply(F, Feff);
+        CSR Ktot; keff_total(Ktot);
+        s.support_increment(k, SM);
+        bool anySM = false; for (double v : SM) if (v != 0.0) { anySM = true; break; }
+        if (anySM) {
+            std::vector<double> KS, lg; csr_mv(Ktot, SM, KS); s.TT_apply(KS, lg);
+            for (int f = 0; f < nf; ++f) Feff[f] -= lg[f];
+        }
+        // T^T Keff T
+        std::vector<Trip> tr;
+        for (int r = 0; r < Ktot.n; ++r)
+            for (int i = Ktot.ptr[r]; i < Ktot.ptr[r + 1]; ++i)
+                for (int a = s.Tptr[r]; a < s.Tptr[r + 1]; ++a)
+                    for (int b = s.Tptr[Ktot.col[i]]; b < s.Tptr[Ktot.col[i] + 1]; ++b)
+                        tr.push_back({s.Tcol[a], s.Tcol[b], s.Tval[a] * Ktot.val[i] * s.Tval[b]});
+        CSR Kff; csr_from_triplets(nf, tr, Kff);
+        if (solver == 0) { if (!dense_ldlt_solve(Kff, Feff, du)) return SVL_ERR_BREAKDOWN; }
+        else return SVL_ERR_INVALID;
+        s.T_apply(du, dUt);
+        std::vector<double> Us(nt);
+        for (int t = 0; t < nt; ++t) Us[t] = U[t] + dUt[t];
+        for (int e = 0; e < m.nelem; ++e) if (!pml(e)) s.element_update(e, Us);
+        for (int t = 0; t < nt; ++t) {
+            const double d = dUt[t], D = d + SM[t];
+            Ubar[t] = Ubar[t] + dt * U[t] + dt / 3.0 * D + dt * dt / 6.0 * V[t];
+            U[t] += D;
+            A[t] = 4.0 / dt / dt * d - 4.0 / dt * V[t] - A[t];
+            V[t] = 2.0 / dt * d - V[t];
+        }
+        s.commit_all();
+        return 0;
+    }
+};
+
 /* ---------------- C ABI of the oracle ------------------------------------ */
 extern "C" {
 
@@ -1249,6 +1448,42 @@ int oracle_newmark_run(const svl_model_desc* model, const svl_load_desc* loads, 
         if (hist_U) std::memcpy(hist_U + (size_t)i * nt, nm.U.data(), sizeof(double) * nt);
     }
     if (pcg_iters) *pcg_iters = nm.pcg_iters;
+    return 0;
+}
+
+/* ExtendedNewmarkBeta + Linear with PML elements (dense LDL^T solve). */
+int oracle_xnewmark_run(const svl_model_desc* model, const svl_load_desc* loads, double dt, int k_first, int nsteps,
+                        double* hist_U, double* U_out, double* V_out, double* A_out, double* Ubar_out) {
+    XNewmark x;
+    if (!x.init(model, loads, dt)) return SVL_ERR_INVALID;
+    x.set_initial(nullptr, nullptr, nullptr, nullptr);
+    const int nt = x.s.m.ntotal;
+    for (int i = 0; i < nsteps; ++i) {
+        int st = x.step(k_first + i);
+        if (st) return st;
+        if (hist_U) std::memcpy(hist_U + (size_t)i * nt, x.U.data(), sizeof(double) * nt);
+    }
+    if (U_out) std::memcpy(U_out, x.U.data(), sizeof(double) * nt);
+    if (V_out) std::memcpy(V_out, x.V.data(), sizeof(double) * nt);
+    if (A_out) std::memcpy(A_out, x.A.data(), sizeof(double) * nt);
+    if (Ubar_out) std::memcpy(Ubar_out, x.Ubar.data(), sizeof(double) * nt);
+    return 0;
+}
+
+/* Total-dof matrices K, M, C, G of the ExtendedNewmark model as dense arrays
+ * (small models; the tests check structure and the time stepping with them). */
+int oracle_xnewmark_matrices(const svl_model_desc* model, double* K, double* M, double* C, double* G) {
+    XNewmark x;
+    if (!x.init(model, nullptr, 1.0)) return SVL_ERR_INVALID;
+    const int nt = x.s.m.ntotal;
+    const CSR* src[4] = {&x.Kt, &x.Mt, &x.Ct, &x.Gt};
+    double* dst[4] = {K, M, C, G};
+    for (int q = 0; q < 4; ++q) {
+        if (!dst[q]) continue;
+        std::fill(dst[q], dst[q] + (size_t)nt * nt, 0.0);
+        for (int r = 0; r < nt; ++r)
+            for (int i = src[q]->ptr[r]; i < src[q]->ptr[r + 1]; ++i) dst[q][(size_t)r * nt + src[q]->col[i]] = src[q]->val[i];
+    }
     return 0;
 }
 

@@ -56,6 +56,7 @@ class ModelDesc(C.Structure):
         ("elem_mat", i32p), ("elem_thickness", f64p),
         ("nmat", C.c_int32), ("mat_type", i32p), ("mat_param", f64p),
         ("lumped", C.c_int32), ("node_mass", f64p), ("elem_rayleigh", f64p),
+        ("node_ndof", i32p), ("elem_pml", i32p), ("elem_pml_param", f64p),
     ]
 
 

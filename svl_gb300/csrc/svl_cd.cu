@@ -833,6 +833,11 @@ static int cd_create(const svl_model_desc* model, const svl_load_desc* loads, co
     cd->opts = *opts;
     if (!model_from_desc(model, cd->m)) { delete cd; return SVL_ERR_INVALID; }
     if (!cd->m.lumped) { delete cd; set_error("the explicit path needs a lumped mass (massform LUMPED)"); return SVL_ERR_UNSUPPORTED; }
+    if (cd->m.has_pml()) {
+        delete cd;
+        set_error("PML elements are served by svl_xnm_create (ExtendedNewmarkBeta)");
+        return SVL_ERR_UNSUPPORTED;
+    }
     if (!implicit)
         for (size_t e = 0; e < cd->m.ray.size() / 2; ++e)
             if (cd->m.ray[2 * e + 1] != 0.0) {

@@ -675,6 +675,7 @@ static int cdx_check_instance(const svl_grid_spec* g, const HostModel& m, int in
     if (m.nnode != nn || m.nelem != (long long)nx * ny * nz) { set_error("instance %d does not match the grid size", inst); return SVL_ERR_INVALID; }
     if (m.nconstraint) { set_error("instance %d: constraints are not supported on the structured path", inst); return SVL_ERR_UNSUPPORTED; }
     if (!m.lumped) { set_error("instance %d: the explicit path needs a lumped mass", inst); return SVL_ERR_UNSUPPORTED; }
+    if (m.has_pml()) { set_error("instance %d: PML elements are served by svl_xnm_create", inst); return SVL_ERR_UNSUPPORTED; }
     if (!m.ray.empty()) { set_error("instance %d: Rayleigh damping is served by the general path (svl_cd_create)", inst); return SVL_ERR_UNSUPPORTED; }
     for (int k = 0; k < m.nmat; ++k)
         if (m.mtype[k] != SVL_MAT_ELASTIC3DLINEAR) { set_error("instance %d: only Elastic3DLinear on the structured path", inst); return SVL_ERR_UNSUPPORTED; }

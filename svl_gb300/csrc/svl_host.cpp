@@ -42,7 +42,12 @@ bool model_from_desc(const svl_model_desc* d, HostModel& m) {
     if ((m.etype == SVL_ELEM_LIN2DQUAD4 && m.ndim != 2) || (m.etype == SVL_ELEM_LIN3DHEXA8 && m.ndim != 3)) {
         set_error("element type %d does not match ndim %d", m.etype, m.ndim); return false;
     }
-    if (m.ndof != m.ndim) { set_error("ndof (%d) must equal ndim (%d) for solid elements", m.ndof, m.ndim); return false; }
+    const int pnd = m.ndim == 2 ? 5 : 9;
+    m.dstride = d->ndof;
+    if (m.dstride != m.ndim && m.dstride != pnd) {
+        set_error("ndof (%d) must be ndim (%d), or %d with PML nodes", m.dstride, m.ndim, pnd); return false;
+    }
+    m.ndof = m.ndim;
     if (m.nnode <= 0 || m.nelem <= 0 || m.ntotal <= 0 || m.nfree < 0 || m.nmat <= 0) {
         set_error("empty model (nnode=%d nelem=%d ntotal=%d nfree=%d nmat=%d)", m.nnode, m.nelem, m.ntotal, m.nfree, m.nmat);
         return false;
@@ -51,9 +56,38 @@ bool model_from_desc(const svl_model_desc* d, HostModel& m) {
         set_error("model descriptor has a NULL array"); return false;
     }
     m.X.assign(d->coords, d->coords + (size_t)m.nnode * m.ndim);
-    m.tdof.assign(d->totaldof, d->totaldof + (size_t)m.nnode * m.ndof);
-    m.fdof.assign(d->freedof, d->freedof + (size_t)m.nnode * m.ndof);
+    m.nndof.assign(m.nnode, m.dstride);
+    if (d->node_ndof) {
+        for (int n = 0; n < m.nnode; ++n) {
+            const int k = d->node_ndof[n];
+            if (k != m.ndim && k != pnd) { set_error("node %d has %d dofs (%d or %d expected)", n, k, m.ndim, pnd); return false; }
+            if (k > m.dstride) { set_error("node %d has %d dofs, more than the stride %d", n, k, m.dstride); return false; }
+            m.nndof[n] = k;
+        }
+    }
+    m.tdof_all.assign((size_t)m.nnode * m.dstride, -1);
+    m.fdof_all.assign((size_t)m.nnode * m.dstride, -1);
+    m.tdof.resize((size_t)m.nnode * m.ndim);
+    m.fdof.resize((size_t)m.nnode * m.ndim);
+    for (int n = 0; n < m.nnode; ++n)
+        for (int j = 0; j < m.nndof[n]; ++j) {
+            const size_t i = (size_t)n * m.dstride + j;
+            m.tdof_all[i] = d->totaldof[i];
+            m.fdof_all[i] = d->freedof[i];
+            if (j < m.ndim) { m.tdof[(size_t)n * m.ndim + j] = d->totaldof[i]; m.fdof[(size_t)n * m.ndim + j] = d->freedof[i]; }
+        }
     m.conn.assign(d->conn, d->conn + (size_t)m.nelem * m.nen);
+    m.epml.clear(); m.pml_par.clear();
+    if (d->elem_pml) {
+        bool any = false;
+        for (int e = 0; e < m.nelem; ++e) any |= d->elem_pml[e] != 0;
+        if (any) {
+            if (!d->elem_pml_param) { set_error("PML elements without elem_pml_param"); return false; }
+            m.epml.assign(m.nelem, 0);
+            for (int e = 0; e < m.nelem; ++e) m.epml[e] = d->elem_pml[e] != 0;
+            m.pml_par.assign(d->elem_pml_param, d->elem_pml_param + (size_t)m.nelem * (3 + 2 * m.ndim));
+        }
+    }
     m.emat.assign(d->elem_mat, d->elem_mat + m.nelem);
     m.thick.assign(m.nelem, 1.0);
     if (d->elem_thickness) m.thick.assign(d->elem_thickness, d->elem_thickness + m.nelem);
@@ -90,15 +124,32 @@ bool model_from_desc(const svl_model_desc* d, HostModel& m) {
     // index checks: every later device access is bounded by these
     for (int32_t n : m.conn) if (n < 0 || n >= m.nnode) { set_error("connectivity node %d out of range", n); return false; }
     for (int32_t k : m.emat) if (k < 0 || k >= m.nmat) { set_error("element material %d out of range", k); return false; }
-    for (int32_t t : m.tdof) if (t < 0 || t >= m.ntotal) { set_error("total dof %d out of range", t); return false; }
     {
-        std::vector<char> seen(m.ntotal, 0);
-        for (int32_t t : m.tdof) { if (seen[t]) { set_error("total dof %d appears twice", t); return false; } seen[t] = 1; }
-        std::vector<char> fseen(m.nfree, 0);
-        for (int32_t f : m.fdof) {
-            if (f >= m.nfree) { set_error("free dof %d out of range", f); return false; }
-            if (f >= 0) { if (fseen[f]) { set_error("free dof %d appears twice", f); return false; } fseen[f] = 1; }
+        std::vector<char> seen(m.ntotal, 0), fseen(std::max(m.nfree, 1), 0);
+        for (int n = 0; n < m.nnode; ++n)
+            for (int j = 0; j < m.nndof[n]; ++j) {
+                const int32_t t = m.tdof_all[(size_t)n * m.dstride + j], f = m.fdof_all[(size_t)n * m.dstride + j];
+                if (t < 0 || t >= m.ntotal) { set_error("total dof %d out of range", t); return false; }
+                if (seen[t]) { set_error("total dof %d appears twice", t); return false; }
+                seen[t] = 1;
+                if (f >= m.nfree) { set_error("free dof %d out of range", f); return false; }
+                if (f >= 0) { if (fseen[f]) { set_error("free dof %d appears twice", f); return false; } fseen[f] = 1; }
+            }
+    }
+    if (m.has_pml()) {
+        // PML elements take every dof of their nodes; PML thresholds and stretching
+        for (int e = 0; e < m.nelem; ++e) {
+            if (!m.epml[e]) continue;
+            for (int a = 0; a < m.nen; ++a)
+                if (m.nndof[m.conn[(size_t)e * m.nen + a]] != pnd) { set_error("PML element %d has a node without %d dofs", e, pnd); return false; }
+            const double* p = &m.pml_par[(size_t)e * (3 + 2 * m.ndim)];
+            if (!(p[1] > 0.0) || !(p[2] > 0.0 && p[2] <= 1.0)) { set_error("PML element %d: L > 0 and 0 < R <= 1 needed", e); return false; }
+            const int mt = m.mtype[m.emat[e]];
+            if (mt != SVL_MAT_ELASTIC2DPLANESTRAIN && mt != SVL_MAT_ELASTIC3DLINEAR) { set_error("PML element %d needs an elastic material", e); return false; }
         }
+    } else {
+        for (int n = 0; n < m.nnode; ++n)
+            if (m.nndof[n] != m.ndim) { set_error("node %d has %d dofs but the model has no PML element", n, m.nndof[n]); return false; }
     }
     for (int k = 0; k < m.nmat; ++k) {
         int t = m.mtype[k];
@@ -259,9 +310,9 @@ void build_total_to_free(const HostModel& m, std::vector<int32_t>& ptr,
                          std::vector<int32_t>& col, std::vector<double>& val) {
     std::vector<std::vector<std::pair<int32_t, double>>> rows(m.ntotal);
     for (int n = 0; n < m.nnode; ++n)
-        for (int j = 0; j < m.ndof; ++j) {
-            const int32_t f = m.fdof[(size_t)n * m.ndof + j];
-            if (f > -1) rows[m.tdof[(size_t)n * m.ndof + j]].push_back({f, 1.0});
+        for (int j = 0; j < m.nndof[n]; ++j) {
+            const int32_t f = m.fdof_all[(size_t)n * m.dstride + j];
+            if (f > -1) rows[m.tdof_all[(size_t)n * m.dstride + j]].push_back({f, 1.0});
         }
     for (int c = 0; c < m.nconstraint; ++c)
         for (int i = m.cptr[c]; i < m.cptr[c + 1]; ++i) rows[m.cslave[c]].push_back({m.cmaster[i], m.cfactor[i]});

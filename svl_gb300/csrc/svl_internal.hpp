@@ -17,10 +17,15 @@ void set_error(const char* fmt, ...);
 constexpr double kGaussAbscissa = 0.577350269189626;
 
 struct HostModel {
-    int ndim = 0, nnode = 0, ndof = 0, ntotal = 0, nfree = 0;
+    int ndim = 0, nnode = 0, ndof = 0, ntotal = 0, nfree = 0;   // ndof = ndim (solid dofs per node)
     int etype = 0, nelem = 0, nen = 0, ngp = 0, nstr = 0, nmat = 0;
     std::vector<double> X;
-    std::vector<int32_t> tdof, fdof, conn, emat;
+    std::vector<int32_t> tdof, fdof, conn, emat;   // tdof/fdof: the first ndim dofs, [nnode][ndim]
+    // every dof of every node (PML nodes carry 5 / 9): [nnode][dstride], count nndof[n]
+    int dstride = 0;
+    std::vector<int32_t> nndof, tdof_all, fdof_all;
+    std::vector<int32_t> epml;        // [nelem] 1 for a PML element (empty: none)
+    std::vector<double> pml_par;      // [nelem][3 + 2 ndim] n, L, R, x0, npml
     std::vector<double> thick;
     std::vector<int32_t> mtype;
     std::vector<double> mpar;
@@ -32,6 +37,8 @@ struct HostModel {
     int lumped = 1;
 
     bool has_j2() const;
+    bool has_pml() const { return !epml.empty(); }
+    int pml_ndof() const { return ndim == 2 ? 5 : 9; }
     const double* param(int e) const { return &mpar[(size_t)emat[e] * SVL_MAT_NPARAM]; }
     int mat_type(int e) const { return mtype[emat[e]]; }
 };

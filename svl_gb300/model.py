@@ -38,6 +38,9 @@ class Model:
     lumped: bool = True
     node_mass: Optional[np.ndarray] = None
     rayleigh: Optional[np.ndarray] = None  # [nelem, 2] (am, ak) or None
+    node_ndof: Optional[np.ndarray] = None  # [nnode] dofs of each node (PML nodes 5 / 9), None: all ndof
+    elem_pml: Optional[np.ndarray] = None   # [nelem] 1 for PML2DQuad4 / PML3DHexa8 elements
+    pml_param: Optional[np.ndarray] = None  # [nelem, 3 + 2 ndim] n, L, R, x0, npml
     grid_shape: Optional[tuple] = None   # (nx, ny[, nz]) when built by grid()
     _keep: list = field(default_factory=list, repr=False)
 
@@ -53,13 +56,19 @@ class Model:
     def ndof(self):
         return int(self.totaldof.shape[1])
 
+    def dof_mask(self) -> np.ndarray:
+        """[nnode, ndof] True where the node has that dof."""
+        if self.node_ndof is None:
+            return np.ones(self.totaldof.shape, bool)
+        return np.arange(self.totaldof.shape[1])[None, :] < np.asarray(self.node_ndof)[:, None]
+
     @property
     def ntotal(self):
-        return int(self.totaldof.size)
+        return int(self.dof_mask().sum())
 
     @property
     def nfree(self):
-        return int((self.freedof >= 0).sum())
+        return int(((self.freedof >= 0) & self.dof_mask()).sum())
 
     @property
     def nconstraint(self):
@@ -77,6 +86,9 @@ class Model:
             con_factor=None if self.con_factor is None else as_f64(self.con_factor),
             node_mass=None if self.node_mass is None else as_f64(self.node_mass),
             rayleigh=None if self.rayleigh is None else as_f64(self.rayleigh),
+            node_ndof=None if self.node_ndof is None else as_i32(self.node_ndof),
+            elem_pml=None if self.elem_pml is None else as_i32(self.elem_pml),
+            pml_param=None if self.pml_param is None else as_f64(self.pml_param),
         )
         self._keep = list(arrs.values())
         d = capi.ModelDesc()
@@ -104,6 +116,9 @@ class Model:
         d.lumped = 1 if self.lumped else 0
         d.node_mass = ptr(arrs["node_mass"], C.c_double)
         d.elem_rayleigh = ptr(arrs["rayleigh"], C.c_double)
+        d.node_ndof = ptr(arrs["node_ndof"], C.c_int32)
+        d.elem_pml = ptr(arrs["elem_pml"], C.c_int32)
+        d.elem_pml_param = ptr(arrs["pml_param"], C.c_double)
         return d
 
     # ------------------------------------------------------------------

@@ -88,3 +88,67 @@ def q4_j2_columns(ncol=3, width=4, heights=(6, 9, 12), h=0.5, seed=1, nt=300, pg
             L.add_support_motion(m, i, 0, s)
         loads.append(L)
     return Model.concat(models), Loads.concat(loads, models), dt
+
+
+def pml_box(ndim=2, ni=(6, 4), npml=2, h=1.0, E=2.0e8, nu=0.25, rho=2000.0, nt=80, amp=1.0e6, f0=8.0,
+            dt_factor=2.0, R=1.0e-6, mexp=2.0, lumped=True):
+    """Elastic box with PML layers on the lateral sides and the bottom
+    (PML2DQuad4 / PML3DHexa8 with 5 / 9 dofs at their nodes), the outer PML
+    boundary fixed in displacement, a Ricker point load at the top centre.
+    Geometry and connectivity from the grid generator; dofs numbered node by
+    node with each node's own count (PlainScheme order)."""
+    pnd = 5 if ndim == 2 else 9
+    ne = [ni[0] + 2 * npml, ni[1] + npml] if ndim == 2 else [ni[0] + 2 * npml, ni[1] + 2 * npml, ni[2] + npml]
+    mt = capi.SVL_MAT_ELASTIC2DPLANESTRAIN if ndim == 2 else capi.SVL_MAT_ELASTIC3DLINEAR
+    g = Model.grid(ndim, ne, (h,) * ndim, mat_type=np.array([mt], np.int32),
+                   mat_param=elastic_params(ndim, E, nu, rho)[None, :])
+    nel = g.nelem
+    # element grid indices (generator order: x fastest)
+    idx = np.stack(np.unravel_index(np.arange(nel), ne[::-1])[::-1], axis=1)
+    vert = ndim - 1
+    lo = [npml * h] * ndim
+    hi = [(npml + ni[d]) * h for d in range(ndim)]
+    par = np.zeros((nel, 3 + 2 * ndim))
+    epml = np.zeros(nel, np.int32)
+    for e in range(nel):
+        n = np.zeros(ndim)
+        x0 = np.zeros(ndim)
+        for d in range(ndim):
+            i = idx[e, d]
+            if i < npml:
+                n[d], x0[d] = -1.0, lo[d]
+            elif d != vert and i >= ne[d] - npml:
+                n[d], x0[d] = 1.0, hi[d]
+        if np.any(n != 0):
+            epml[e] = 1
+            par[e] = np.concatenate([[mexp, npml * h, R], x0, n])
+    pnode = np.zeros(g.nnode, bool)
+    pnode[g.conn[epml == 1].ravel()] = True
+    ndof_n = np.where(pnode, pnd, ndim).astype(np.int32)
+    tdof = -np.ones((g.nnode, pnd), np.int32)
+    fdof = -np.ones((g.nnode, pnd), np.int32)
+    X = g.coords
+    outer = np.zeros(g.nnode, bool)
+    for d in range(ndim):
+        outer |= np.isclose(X[:, d], 0.0) if d == vert else (np.isclose(X[:, d], 0.0) | np.isclose(X[:, d], ne[d] * h))
+    t = f = 0
+    for nd_ in range(g.nnode):
+        for j in range(ndof_n[nd_]):
+            tdof[nd_, j] = t
+            t += 1
+            if not (outer[nd_] and j < ndim):
+                fdof[nd_, j] = f
+                f += 1
+    m = Model(ndim=ndim, coords=X, totaldof=tdof, freedof=fdof, conn=g.conn, elem_type=g.elem_type,
+              elem_mat=g.elem_mat, mat_type=g.mat_type, mat_param=g.mat_param, lumped=lumped,
+              node_ndof=ndof_n, elem_pml=epml, pml_param=par)
+    G = E / (2 * (1 + nu))
+    lam = E * nu / ((1 + nu) * (1 - 2 * nu))
+    vp = np.sqrt((lam + 2 * G) / rho)
+    dt = dt_factor * h / vp
+    L = Loads()
+    s = L.add_series(ricker(nt + 1, dt, f0, amp=amp))
+    top = np.flatnonzero(np.isclose(X[:, vert], ne[vert] * h))
+    c = top[np.argmin(np.sum((X[top, :vert] - np.array(hi[:vert]) / 2 - np.array(lo[:vert]) / 2) ** 2, axis=1))]
+    L.add_point_load(m, int(c), tuple([0.0] * vert + [-1.0]), s)
+    return m, L, dt
