@@ -335,6 +335,44 @@ int  svl_nm_launch_count(svl_nm* nm, int64_t* launches);
 int  svl_nm_sync(svl_nm* nm);
 void svl_nm_destroy(svl_nm* nm);
 
+/* ---- ExtendedNewmarkBeta with PML (svl_xnm_*) ---------------------------- */
+/* ExtendedNewmarkBeta (RP/10-Integrators/03-Newmark/ExtendedNewmarkBeta.cpp)
+ * with the Linear algorithm on a mesh of elastic lin2DQuad4/lin3DHexa8 solid
+ * elements (lumped mass, optional Rayleigh damping) and PML2DQuad4/PML3DHexa8
+ * elements (5 / 9 dofs per node, consistent mass):
+ *   Feff = Fext - Fint - G (Ubar + dt U + dt^2/6 V) + C V + M (4/dt V + A)  (:208-229)
+ *   Keff = K + 4/dt^2 M + 2/dt C + dt/3 G                                   (:233-245)
+ *   Feff -= T^T Keff SM(k)  (the increment of step k, :190-204)
+ *   Ubar += dt U + dt/3 (dU + SM) + dt^2/6 V; U += dU + SM;
+ *   A = 4/dt^2 dU - 4/dt V - A; V = 2/dt dU - V                             (:123-153)
+ * Fint of a solid element from the strain of U + T du of the last solve, of a
+ * PML element K_e U_e (PML3DHexa8.cpp:716-742).  With PML the effective
+ * matrix is symmetric indefinite, so the solve is MINRES with the
+ * D = |diag(Keff)| preconditioner, matrix-free on the GPU, stopped on the true
+ * residual in the norm MINRES minimises, ||b - Keff du||_{D^-1} <= tol ||b||_{D^-1}
+ * (displacement and stress rows differ by ~13 orders of magnitude).  The
+ * reference solves the same system with SimplicialLDLT / MUMPS / PETSc
+ * (EigenSolver.cpp:19-59). */
+typedef struct svl_xnm svl_xnm;
+typedef struct svl_xnm_opts {
+    double  dt;
+    double  ftol;        /* force assembly tolerance (1e-12)                       */
+    double  mtol;        /* mass assembly tolerance (1e-12)                        */
+    double  tol;         /* relative true-residual tolerance (D^-1 norm) of each solve */
+    int32_t maxit;       /* MINRES iteration cap per solve (SVL_ERR_MAXITER past it) */
+    int32_t reserved[3];
+} svl_xnm_opts;
+int  svl_xnm_create(const svl_model_desc* model, const svl_load_desc* loads, const svl_xnm_opts* opts,
+                    svl_xnm** out);
+/* U0, V0, A0, Ubar0: [ntotal] host arrays or NULL for zero. */
+int  svl_xnm_set_initial(svl_xnm* x, const double* U0, const double* V0, const double* A0, const double* Ubar0);
+/* Steps k_first .. k_first+nsteps-1; U_hist [nsteps][ntotal] host array or NULL. */
+int  svl_xnm_run(svl_xnm* x, int32_t k_first, int32_t nsteps, double* U_hist);
+/* which: 0 U, 1 V, 2 A, 3 Ubar (GetPMLHistoryVector); out [ntotal]. */
+int  svl_xnm_get(svl_xnm* x, int32_t which, double* out);
+int  svl_xnm_stats(svl_xnm* x, int64_t* iters_total, int64_t* iters_last, double* res_last);
+void svl_xnm_destroy(svl_xnm* x);
+
 /* ---- learned preconditioner (no counterpart in the reference) ----------- */
 /* For hexahedral models whose nodes form a lattice (svl_grid_build meshes and
  * any other mesh with one node per point of an nx x ny x nz lattice), the

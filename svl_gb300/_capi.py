@@ -90,6 +90,11 @@ class NmOpts(C.Structure):
                 ("cnvgtol", C.c_double), ("cnvgtest", C.c_int32), ("reserved", C.c_int32)]
 
 
+class XnmOpts(C.Structure):
+    _fields_ = [("dt", C.c_double), ("ftol", C.c_double), ("mtol", C.c_double), ("tol", C.c_double),
+                ("maxit", C.c_int32), ("reserved", C.c_int32 * 3)]
+
+
 class NnTrainOpts(C.Structure):
     _fields_ = [("solve_steps", C.c_int32), ("record_every", C.c_int32), ("n_synthetic", C.c_int32),
                 ("iters", C.c_int32), ("batch", C.c_int32), ("lr", C.c_float), ("seed", C.c_uint64),
@@ -154,6 +159,13 @@ def lib():
     L.svl_host_alloc.restype = C.c_void_p
     L.svl_host_free.argtypes = [C.c_void_p]
     L.svl_host_free.restype = None
+    L.svl_xnm_create.argtypes = [C.POINTER(ModelDesc), C.POINTER(LoadDesc), C.POINTER(XnmOpts), C.POINTER(C.c_void_p)]
+    L.svl_xnm_set_initial.argtypes = [C.c_void_p, f64p, f64p, f64p, f64p]
+    L.svl_xnm_run.argtypes = [C.c_void_p, C.c_int32, C.c_int32, f64p]
+    L.svl_xnm_get.argtypes = [C.c_void_p, C.c_int32, f64p]
+    L.svl_xnm_stats.argtypes = [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_double)]
+    L.svl_xnm_destroy.argtypes = [C.c_void_p]
+    L.svl_xnm_destroy.restype = None
     L.svl_nm_create.argtypes = [C.POINTER(ModelDesc), C.POINTER(LoadDesc), C.POINTER(NmOpts), C.POINTER(C.c_void_p)]
     L.svl_nm_set_initial.argtypes = [C.c_void_p, f64p, f64p, f64p]
     L.svl_nm_run.argtypes = [C.c_void_p, C.c_int32, C.c_int32, f64p]

@@ -665,38 +665,14 @@ static int cd_setup(svl_cd* cd, const svl_load_desc* L) {
             for (int i = T_ptr[t]; i < T_ptr[t + 1]; ++i) { const int p = fill[T_col[i]]++; TT_row[p] = t; TT_val[p] = T_val[i]; }
     }
     // --- loads ---------------------------------------------------------------
-    std::vector<int32_t> s_ptr(1, 0);
-    std::vector<double> s_val;
-    std::vector<int32_t> ld_ptr(m.ntotal + 1, 0), ld_ser, sm_ptr(m.ntotal + 1, 0), sm_ser;
-    std::vector<double> ld_coef, sm_fac;
-    if (L) {
-        if (L->nseries > 0) {
-            if (!L->series_ptr || !L->series_val) { set_error("series arrays are NULL"); return SVL_ERR_INVALID; }
-            s_ptr.assign(L->series_ptr, L->series_ptr + L->nseries + 1);
-            for (int s = 0; s < L->nseries; ++s)
-                if (s_ptr[s + 1] < s_ptr[s]) { set_error("series_ptr is not monotone"); return SVL_ERR_INVALID; }
-            s_val.assign(L->series_val, L->series_val + s_ptr.back());
-        }
-        auto csr = [&](int n, const int32_t* dof, const int32_t* ser, const double* val,
-                       std::vector<int32_t>& ptr, std::vector<int32_t>& oser, std::vector<double>& oval) -> int {
-            if (n <= 0) return SVL_OK;
-            if (!dof || !ser || !val) { set_error("load arrays are NULL"); return SVL_ERR_INVALID; }
-            std::vector<int> order(n);
-            for (int i = 0; i < n; ++i) {
-                if (dof[i] < 0 || dof[i] >= m.ntotal) { set_error("load dof %d out of range", dof[i]); return SVL_ERR_INVALID; }
-                if (ser[i] < 0 || ser[i] >= L->nseries) { set_error("load series %d out of range", ser[i]); return SVL_ERR_INVALID; }
-                order[i] = i;
-                ptr[dof[i] + 1]++;
-            }
-            std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return dof[a] < dof[b]; });
-            for (int t = 0; t < m.ntotal; ++t) ptr[t + 1] += ptr[t];
-            for (int i : order) { oser.push_back(ser[i]); oval.push_back(val[i]); }
-            return SVL_OK;
-        };
-        TRY(csr(L->nforce, L->force_dof, L->force_series, L->force_coef, ld_ptr, ld_ser, ld_coef));
-        TRY(csr(L->nsupport, L->sm_dof, L->sm_series, L->sm_factor, sm_ptr, sm_ser, sm_fac));
-        cd->has_sm = L->nsupport > 0;
-    }
+    LoadTables lt;
+    TRY(build_load_tables(m, L, lt));
+    cd->has_sm = lt.has_sm;
+    const std::vector<int32_t>& s_ptr = lt.s_ptr; const std::vector<double>& s_val = lt.s_val;
+    const std::vector<int32_t>& ld_ptr = lt.ld_ptr; const std::vector<int32_t>& ld_ser = lt.ld_ser;
+    const std::vector<double>& ld_coef = lt.ld_coef;
+    const std::vector<int32_t>& sm_ptr = lt.sm_ptr; const std::vector<int32_t>& sm_ser = lt.sm_ser;
+    const std::vector<double>& sm_fac = lt.sm_fac;
     // --- device upload -------------------------------------------------------
     DevView& d = cd->d;
     d.nelem = E; d.nnode = m.nnode; d.ntotal = m.ntotal; d.nfree = m.nfree;

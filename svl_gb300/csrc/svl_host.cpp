@@ -306,6 +306,43 @@ void rayleigh_mass_diag(const HostModel& m, std::vector<double>& C) {
     }
 }
 
+int build_load_tables(const HostModel& m, const svl_load_desc* L, LoadTables& o) {
+    o = LoadTables();
+    o.ld_ptr.assign(m.ntotal + 1, 0);
+    o.sm_ptr.assign(m.ntotal + 1, 0);
+    if (!L) return SVL_OK;
+    if (L->nseries > 0) {
+        if (!L->series_ptr || !L->series_val) { set_error("series arrays are NULL"); return SVL_ERR_INVALID; }
+        o.s_ptr.assign(L->series_ptr, L->series_ptr + L->nseries + 1);
+        if (o.s_ptr[0] != 0) { set_error("series_ptr[0] must be 0"); return SVL_ERR_INVALID; }
+        for (int s = 0; s < L->nseries; ++s)
+            if (o.s_ptr[s + 1] < o.s_ptr[s]) { set_error("series_ptr is not monotone"); return SVL_ERR_INVALID; }
+        o.s_val.assign(L->series_val, L->series_val + o.s_ptr.back());
+    }
+    auto csr = [&](int n, const int32_t* dof, const int32_t* ser, const double* val,
+                   std::vector<int32_t>& ptr, std::vector<int32_t>& oser, std::vector<double>& oval) -> int {
+        if (n <= 0) return SVL_OK;
+        if (!dof || !ser || !val) { set_error("load arrays are NULL"); return SVL_ERR_INVALID; }
+        std::vector<int> order(n);
+        for (int i = 0; i < n; ++i) {
+            if (dof[i] < 0 || dof[i] >= m.ntotal) { set_error("load dof %d out of range", dof[i]); return SVL_ERR_INVALID; }
+            if (ser[i] < 0 || ser[i] >= L->nseries) { set_error("load series %d out of range", ser[i]); return SVL_ERR_INVALID; }
+            order[i] = i;
+            ptr[dof[i] + 1]++;
+        }
+        std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return dof[a] < dof[b]; });
+        for (int t = 0; t < m.ntotal; ++t) ptr[t + 1] += ptr[t];
+        for (int i : order) { oser.push_back(ser[i]); oval.push_back(val[i]); }
+        return SVL_OK;
+    };
+    int st = csr(L->nforce, L->force_dof, L->force_series, L->force_coef, o.ld_ptr, o.ld_ser, o.ld_coef);
+    if (st) return st;
+    st = csr(L->nsupport, L->sm_dof, L->sm_series, L->sm_factor, o.sm_ptr, o.sm_ser, o.sm_fac);
+    if (st) return st;
+    o.has_sm = L->nsupport > 0;
+    return SVL_OK;
+}
+
 void build_total_to_free(const HostModel& m, std::vector<int32_t>& ptr,
                          std::vector<int32_t>& col, std::vector<double>& val) {
     std::vector<std::vector<std::pair<int32_t, double>>> rows(m.ntotal);

@@ -6,6 +6,8 @@
 #include <string>
 #include <vector>
 
+#include <cuda_runtime.h>
+
 #include "../../include/svl_gb300.h"
 
 namespace svl {
@@ -64,6 +66,36 @@ void lumped_mass_diag(const HostModel& m, double mtol, std::vector<double>& M);
 // Mass-proportional Rayleigh damping on total dofs, sum_e am_e M_e with the
 // element row-sum lumped masses (lin2DQuad4.cpp:360-366 with a lumped mass)
 void rayleigh_mass_diag(const HostModel& m, std::vector<double>& C);
+
+// Load descriptor as per-total-dof CSR tables: force entries (series, coef)
+// and support-motion entries (series, factor) grouped by dof in input order.
+struct LoadTables {
+    std::vector<int32_t> s_ptr{0};
+    std::vector<double> s_val;
+    std::vector<int32_t> ld_ptr, ld_ser, sm_ptr, sm_ser;
+    std::vector<double> ld_coef, sm_fac;
+    bool has_sm = false;
+};
+// Returns SVL_OK or an error code with svl_last_error set.
+int build_load_tables(const HostModel& m, const svl_load_desc* L, LoadTables& out);
+
+// PML element action y_e = coef_M M u_M + coef_C C u_C + coef_K K u_K + coef_G G u_G
+// (PML2DQuad4 / PML3DHexa8), one thread per element; see svl_pml.cu.
+struct PmlArgs {
+    int nelem;
+    const double* X;       // [nelem][nen][nd]
+    const double* mat;     // [nelem][3]  E, nu, rho
+    const double* thick;   // [nelem] (2D) or null
+    const double* par;     // [nelem][3 + 2 nd]  m, L, R, x0[nd], n[nd]
+    double coef[4];        // M, C, K, G
+    const double* u[4];    // [nelem][nc] each, or total-dof vectors when edof is set (null when the coefficient is 0)
+    const int32_t* edof;   // [nelem][nc] total dof of each element dof (gather mode), or null
+    double* y;             // [nelem][nc]
+    double ftol;           // >= 0: entries with |y| <= ftol are dropped (force filter)
+    double yscale;         // y is scaled by this after the filter
+    int accumulate;        // 1: y += result
+};
+int pml_action_launch(int ndim, const PmlArgs& A, cudaStream_t st);
 
 // T (total <- free) rows as CSR over total dofs, sorted columns, duplicates summed.
 void build_total_to_free(const HostModel& m, std::vector<int32_t>& ptr,

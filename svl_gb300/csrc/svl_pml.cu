@@ -35,16 +35,9 @@ namespace {
         }                                                                            \
     } while (0)
 
-struct PmlArgs {
-    int nelem;
-    const double* X;       // [nelem][nen][nd]
-    const double* mat;     // [nelem][3]  E, nu, rho
-    const double* thick;   // [nelem] (2D) or null
-    const double* par;     // [nelem][3 + 2 nd]  m, L, R, x0[nd], n[nd]
-    double coef[4];        // M, C, K, G
-    const double* u[4];    // [nelem][nc] each (null when the coefficient is 0)
-    double* y;             // [nelem][nc]
-};
+}  // namespace
+
+namespace svl {
 
 template <int ND>
 __global__ void __launch_bounds__(128) k_pml_action(PmlArgs A) {
@@ -141,7 +134,8 @@ __global__ void __launch_bounds__(128) k_pml_action(PmlArgs A) {
         for (int mi = 0; mi < 4; ++mi) {
             const double c = A.coef[mi];
             if (c == 0.0 || (ND == 2 && mi == 3)) continue;
-            const double* u = A.u[mi] + (size_t)e * NC;
+            const double* u = A.u[mi] + (A.edof ? 0 : (size_t)e * NC);
+            const int32_t* ed = A.edof ? A.edof + (size_t)e * NC : nullptr;
             double s, qx, qy, qz = 0.0;
             if (ND == 2) {
                 if (mi == 0) { s = as[0] * as[1]; qx = 0; qy = 0; }
@@ -168,13 +162,13 @@ __global__ void __launch_bounds__(128) k_pml_action(PmlArgs A) {
             for (int a = 0; a < NEN; ++a) {
 #pragma unroll
                 for (int d = 0; d < ND; ++d) {
-                    const double ua = u[a * NN + d];
+                    const double ua = ed ? u[ed[a * NN + d]] : u[a * NN + d];
                     U[d] += N[a] * ua;
 #pragma unroll
                     for (int j = 0; j < ND; ++j) Gd[d][j] += ua * dx[a][j];
                 }
 #pragma unroll
-                for (int i = 0; i < NS; ++i) S[i] += N[a] * u[a * NN + ND + i];
+                for (int i = 0; i < NS; ++i) S[i] += N[a] * (ed ? u[ed[a * NN + ND + i]] : u[a * NN + ND + i]);
             }
             const double cf = c * f;
 #pragma unroll
@@ -210,10 +204,24 @@ __global__ void __launch_bounds__(128) k_pml_action(PmlArgs A) {
     }
     double* out = A.y + (size_t)e * NC;
 #pragma unroll
-    for (int i = 0; i < NC; ++i) out[i] = y[i];
+    for (int i = 0; i < NC; ++i) {
+        double v = y[i];
+        if (A.ftol >= 0.0 && !(fabs(v) > A.ftol)) v = 0.0;
+        v *= A.yscale;
+        out[i] = A.accumulate ? out[i] + v : v;
+    }
 }
 
-}  // namespace
+int pml_action_launch(int ndim, const PmlArgs& A, cudaStream_t st) {
+    if (A.nelem <= 0) return SVL_OK;
+    const int tb = 128, gb = (A.nelem + tb - 1) / tb;
+    if (ndim == 2) k_pml_action<2><<<gb, tb, 0, st>>>(A);
+    else k_pml_action<3><<<gb, tb, 0, st>>>(A);
+    PML_TRY(cudaGetLastError());
+    return SVL_OK;
+}
+
+}  // namespace svl
 
 extern "C" int svl_pml_element_action(int32_t ndim, int32_t nelem, const double* X, const double* mat,
                                       const double* thick, const double* par, const double* coef,
@@ -240,6 +248,7 @@ extern "C" int svl_pml_element_action(int32_t ndim, int32_t nelem, const double*
     };
     PmlArgs A{};
     A.nelem = nelem;
+    A.ftol = -1.0; A.yscale = 1.0; A.accumulate = 0; A.edof = nullptr;
     A.X = dev(X, E * nen * ndim);
     A.mat = dev(mat, E * 3);
     A.thick = thick ? dev(thick, E) : nullptr;
@@ -249,12 +258,7 @@ extern "C" int svl_pml_element_action(int32_t ndim, int32_t nelem, const double*
         A.u[i] = coef[i] != 0.0 ? dev(u + (size_t)i * E * nc, E * nc) : nullptr;
     }
     A.y = dev(nullptr, E * nc);
-    if (!rc) {
-        const int tb = 128, gb = (int)((E + tb - 1) / tb);
-        if (ndim == 2) k_pml_action<2><<<gb, tb, 0, st>>>(A);
-        else k_pml_action<3><<<gb, tb, 0, st>>>(A);
-        if (cudaGetLastError() != cudaSuccess) rc = SVL_ERR_CUDA;
-    }
+    if (!rc) rc = pml_action_launch(ndim, A, st);
     if (!rc && cudaMemcpyAsync(y, A.y, E * nc * sizeof(double), cudaMemcpyDeviceToHost, st) != cudaSuccess) rc = SVL_ERR_CUDA;
     if (cudaStreamSynchronize(st) != cudaSuccess && !rc) rc = SVL_ERR_CUDA;
     for (void* p : bufs) cudaFree(p);

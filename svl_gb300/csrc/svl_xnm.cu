@@ -1,0 +1,824 @@
+// ExtendedNewmarkBeta with PML elements on the GPU (svl_xnm_*).
+//
+// The reference assembles M, C, K and G once (ExtendedNewmarkBeta.cpp:64-70),
+// re-assembles K and forms K + 4/dt^2 M + 2/dt C + dt/3 G every step
+// (:233-245) and factorises it.  Here nothing is assembled: every operator
+// application runs the element kernels on the vector and gathers the element
+// vectors per total dof in element-tag order (an inverse connectivity, no
+// atomics), so each total-dof sum has the reference's summation order.
+//   solid elements (lin2DQuad4 / lin3DHexa8, elastic, lumped mass):
+//     y_e = K_e (xK + cK2 ak_e xK2) + diag(m_e) (sM xM + cM2 am_e xM2)
+//     with C_e = am_e M_e + ak_e K_e (Rayleigh with the initial stiffness,
+//     which is K_e for an elastic material);
+//   PML elements: svl::pml_action_launch (svl_pml.cu) in gather mode.
+// With PML the effective matrix is symmetric indefinite (negative stress
+// blocks of M), so the solve is MINRES (Paige & Saunders 1975) with the SPD
+// preconditioner |diag(Keff)|^-1, restarted from its iterate until the true
+// residual meets the tolerance.  Reductions are two-stage with a fixed block
+// count, so results do not depend on scheduling.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "svl_internal.hpp"
+
+using namespace svl;
+
+namespace {
+
+#define XTRY(x) do { int st_ = (x); if (st_ != SVL_OK) return st_; } while (0)
+#define XCUDA(x)                                                                         \
+    do {                                                                                 \
+        cudaError_t err_ = (x);                                                          \
+        if (err_ != cudaSuccess) {                                                       \
+            set_error("%s failed: %s (%s:%d)", #x, cudaGetErrorString(err_), __FILE__, __LINE__); \
+            return SVL_ERR_CUDA;                                                         \
+        }                                                                                \
+    } while (0)
+
+constexpr int kBlocks = 304, kThreads = 256;     // fixed two-stage reduction shape
+
+struct XSolid {
+    int n, ngp;
+    const int32_t* edof;     // [n][NC]
+    const int32_t* egeo;     // [n] geometry class
+    const double* geo;       // [ngeo][ngp][NEN*ND + 1]  dN/dx and w t |J|
+    const double* coef;      // [n][3] c1 c2 c3
+    const double* ray;       // [n][2] am ak, or null
+    const double* mlump;     // [n][NEN] row-sum lumped mass per element node
+    const double *xK, *xK2, *xM, *xM2;   // total-dof inputs (null = 0)
+    double cK2, sM, cM2, ftol, yscale;
+    int accumulate;
+    double* y;               // [n][NC]
+};
+
+template <int ND, int NEN>
+__global__ void __launch_bounds__(128) k_xsolid(XSolid S) {
+    constexpr int NC = ND * NEN, PER = NEN * ND + 1;
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= S.n) return;
+    const int32_t* ed = S.edof + (size_t)e * NC;
+    const double am = S.ray ? S.ray[2 * e] : 0.0, ak = S.ray ? S.ray[2 * e + 1] : 0.0;
+    double uk[NC], y[NC];
+#pragma unroll
+    for (int j = 0; j < NC; ++j) {
+        const int t = ed[j];
+        double v = S.xK ? S.xK[t] : 0.0;
+        if (S.xK2 && S.cK2 != 0.0) v += S.cK2 * ak * S.xK2[t];
+        uk[j] = v;
+        y[j] = 0.0;
+    }
+    const double c1 = S.coef[3 * e], c2 = S.coef[3 * e + 1], c3 = S.coef[3 * e + 2];
+    const double* g0 = S.geo + (size_t)S.egeo[e] * S.ngp * PER;
+    for (int q = 0; q < S.ngp; ++q) {
+        const double* g = g0 + q * PER;
+        double b[NEN][3];
+#pragma unroll
+        for (int a = 0; a < NEN; ++a)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) b[a][j] = (j < ND) ? g[a * ND + j] : 0.0;
+        const double w = g[PER - 1];
+        if (ND == 2) {
+            double exx = 0, eyy = 0, gxy = 0;
+#pragma unroll
+            for (int a = 0; a < NEN; ++a) {
+                exx += b[a][0] * uk[2 * a];
+                eyy += b[a][1] * uk[2 * a + 1];
+                gxy += b[a][1] * uk[2 * a] + b[a][0] * uk[2 * a + 1];
+            }
+            const double s0 = c1 * exx + c2 * eyy, s1 = c2 * exx + c1 * eyy, s2 = c3 * gxy;
+#pragma unroll
+            for (int a = 0; a < NEN; ++a) {
+                y[2 * a] += w * (b[a][0] * s0 + b[a][1] * s2);
+                y[2 * a + 1] += w * (b[a][1] * s1 + b[a][0] * s2);
+            }
+        } else {
+            double ev[6] = {0, 0, 0, 0, 0, 0};
+#pragma unroll
+            for (int a = 0; a < NEN; ++a) {
+                const double ux = uk[3 * a], uy = uk[3 * a + 1], uz = uk[3 * a + 2];
+                ev[0] += b[a][0] * ux;
+                ev[1] += b[a][1] * uy;
+                ev[2] += b[a][2] * uz;
+                ev[3] += b[a][1] * ux + b[a][0] * uy;
+                ev[4] += b[a][2] * uy + b[a][1] * uz;
+                ev[5] += b[a][2] * ux + b[a][0] * uz;
+            }
+            double sg[6];
+            sg[0] = c1 * ev[0] + c2 * ev[1] + c2 * ev[2];
+            sg[1] = c2 * ev[0] + c1 * ev[1] + c2 * ev[2];
+            sg[2] = c2 * ev[0] + c2 * ev[1] + c1 * ev[2];
+            sg[3] = c3 * ev[3]; sg[4] = c3 * ev[4]; sg[5] = c3 * ev[5];
+#pragma unroll
+            for (int a = 0; a < NEN; ++a) {
+                const double bx = b[a][0], by = b[a][1], bz = b[a][2];
+                y[3 * a] += w * (bx * sg[0] + by * sg[3] + bz * sg[5]);
+                y[3 * a + 1] += w * (by * sg[1] + bx * sg[3] + bz * sg[4]);
+                y[3 * a + 2] += w * (bz * sg[2] + by * sg[4] + bx * sg[5]);
+            }
+        }
+    }
+    if (S.xM || S.xM2) {
+        const double* ml = S.mlump + (size_t)e * NEN;
+#pragma unroll
+        for (int j = 0; j < NC; ++j) {
+            const int t = ed[j];
+            double v = S.xM ? S.sM * S.xM[t] : 0.0;
+            if (S.xM2 && S.cM2 != 0.0) v += S.cM2 * am * S.xM2[t];
+            y[j] += ml[j / ND] * v;
+        }
+    }
+    double* out = S.y + (size_t)e * NC;
+#pragma unroll
+    for (int j = 0; j < NC; ++j) {
+        double v = y[j];
+        if (S.ftol >= 0.0 && !(fabs(v) > S.ftol)) v = 0.0;
+        v *= S.yscale;
+        out[j] = S.accumulate ? out[j] + v : v;
+    }
+}
+
+// y_t = sum of the element entries of dof t in element order (+ c_n m_t x_t) (+ Fext_t(k))
+struct XGather {
+    int ntotal;
+    const int64_t* inv_ptr;      // [ntotal+1]
+    const int64_t* inv_idx;      // into fe (solid block, then PML block)
+    const double* fe;
+    const double* nodemass;      // [ntotal] or null
+    double cn;
+    const double* xn;
+    // external force (RHS only)
+    int k, with_fext;
+    const int32_t *ld_ptr, *ld_ser; const double* ld_coef;
+    const int32_t* s_ptr; const double* s_val;
+    double* y;
+};
+
+__global__ void k_xgather(XGather G) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= G.ntotal) return;
+    double v = 0.0;
+    for (int64_t i = G.inv_ptr[t]; i < G.inv_ptr[t + 1]; ++i) v += G.fe[G.inv_idx[i]];
+    if (G.nodemass && G.xn) v += G.cn * G.nodemass[t] * G.xn[t];
+    if (G.with_fext) {
+        double f = 0.0;
+        for (int i = G.ld_ptr[t]; i < G.ld_ptr[t + 1]; ++i) {
+            const int s = G.ld_ser[i];
+            const int b = G.s_ptr[s], n = G.s_ptr[s + 1] - b;
+            f += G.ld_coef[i] * ((G.k >= 0 && G.k < n) ? G.s_val[b + G.k] : 0.0);
+        }
+        v += f;
+    }
+    G.y[t] = v;
+}
+
+// out_t = sum_f T_tf x_f
+__global__ void k_xexpand(int ntotal, const int32_t* __restrict__ Tp, const int32_t* __restrict__ Tc,
+                          const double* __restrict__ Tv, const double* __restrict__ x, double* __restrict__ out) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ntotal) return;
+    double v = 0.0;
+    for (int i = Tp[t]; i < Tp[t + 1]; ++i) v += Tv[i] * x[Tc[i]];
+    out[t] = v;
+}
+
+// out_f = sum_t T_tf y_t (- sum_t T_tf z_t)
+__global__ void k_xreduce(int nfree, const int32_t* __restrict__ TTp, const int32_t* __restrict__ TTr,
+                          const double* __restrict__ TTv, const double* __restrict__ y, const double* __restrict__ z,
+                          double* __restrict__ out) {
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= nfree) return;
+    double v = 0.0, w = 0.0;
+    for (int i = TTp[f]; i < TTp[f + 1]; ++i) {
+        v += TTv[i] * y[TTr[i]];
+        if (z) w += TTv[i] * z[TTr[i]];
+    }
+    out[f] = z ? v - w : v;
+}
+
+// support-motion increment of step k on total dofs (Assembler.cpp:493-532)
+__global__ void k_xsm(int ntotal, const int32_t* sm_ptr, const int32_t* sm_ser, const double* sm_fac,
+                      const int32_t* s_ptr, const double* s_val, int k, double* sm) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ntotal) return;
+    double v = 0.0;
+    for (int i = sm_ptr[t]; i < sm_ptr[t + 1]; ++i) {
+        const int s = sm_ser[i];
+        const int b = s_ptr[s], n = s_ptr[s + 1] - b;
+        double g = 0.0;
+        if (n > 0) {
+            g = k < n ? s_val[b + k] : s_val[b];
+            if (k > 0) g -= (k - 1 < n ? s_val[b + k - 1] : s_val[b]);
+        }
+        v += sm_fac[i] * g;
+    }
+    sm[t] = v;
+}
+
+// W = 4/dt V + A and Wg = Ubar + dt U + dt^2/6 V
+__global__ void k_xrhs_vec(int n, const double* U, const double* V, const double* A, const double* Ub, double dt,
+                           double* W, double* Wg) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    W[t] = 4.0 / dt * V[t] + A[t];
+    Wg[t] = Ub[t] + dt * U[t] + dt * dt / 6.0 * V[t];
+}
+
+// ExtendedNewmarkBeta::ComputeNewStep state update (dUt = T du, sm = SM(k))
+__global__ void k_xupdate(int n, double* U, double* V, double* A, double* Ub, double* Us, const double* dUt,
+                          const double* sm, double dt, int* bad) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const double d = dUt[t], D = d + (sm ? sm[t] : 0.0);
+    const double u = U[t], v = V[t];
+    Ub[t] = Ub[t] + dt * u + dt / 3.0 * D + dt * dt / 6.0 * v;
+    Us[t] = u + d;                       // solid strain displacement: U + T du
+    const double un = u + D;
+    U[t] = un;
+    A[t] = 4.0 / dt / dt * d - 4.0 / dt * v - A[t];
+    V[t] = 2.0 / dt * d - v;
+    if (!isfinite(un)) atomicOr(bad, 1);
+}
+
+__global__ void k_xdot_partial(const double* __restrict__ a, const double* __restrict__ b, int n, double* partial) {
+    __shared__ double sh[kThreads / 32];
+    double s = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) s += a[i] * b[i];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double v = threadIdx.x < kThreads / 32 ? sh[threadIdx.x] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (threadIdx.x == 0) partial[blockIdx.x] = v;
+    }
+}
+__global__ void k_xdot_final(const double* __restrict__ partial, double* out) {
+    __shared__ double sh[kThreads / 32];
+    double s = 0.0;
+    for (int i = threadIdx.x; i < kBlocks; i += kThreads) s += partial[i];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double v = threadIdx.x < kThreads / 32 ? sh[threadIdx.x] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (threadIdx.x == 0) *out = v;
+    }
+}
+
+__global__ void k_xaxpby(int n, double a, const double* x, double b, double* y) {   // y = a x + b y
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) y[i] = a * x[i] + b * y[i];
+}
+__global__ void k_xvmul(int n, const double* a, const double* b, double* out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = a[i] * b[i];
+}
+__global__ void k_xsub(int n, const double* a, const double* b, double* out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = a[i] - b[i];
+}
+// MINRES direction and iterate: w = (v - oldeps w1 - delta w2) / gamma; x += phi w
+__global__ void k_xmr_w(int n, const double* v, const double* w1, const double* w2, double* w, double* x,
+                        double oldeps, double delta, double inv_gamma, double phi) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double wi = (v[i] - oldeps * w1[i] - delta * w2[i]) * inv_gamma;
+    w[i] = wi;
+    x[i] += phi * wi;
+}
+// unit vector e_i in every element block (diagonal probes)
+__global__ void k_xunit(int nel, int nc, int i, double* u) {
+    const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= (int64_t)nel * nc) return;
+    u[j] = (j % nc) == i ? 1.0 : 0.0;
+}
+__global__ void k_xtake(int nel, int nc, int i, const double* y, double* d) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e < nel) d[(size_t)e * nc + i] = y[(size_t)e * nc + i];
+}
+
+}  // namespace
+
+struct svl_xnm {
+    HostModel m;
+    svl_xnm_opts opts{};
+    cudaStream_t stream = nullptr;
+    std::vector<void*> allocs;
+    int nsol = 0, npml = 0, ncs = 0, ncp = 0;
+    // solid elements
+    int32_t *s_edof = nullptr, *s_egeo = nullptr;
+    double *s_geo = nullptr, *s_coef = nullptr, *s_ray = nullptr, *s_mlump = nullptr;
+    // PML elements
+    double *p_X = nullptr, *p_mat = nullptr, *p_thick = nullptr, *p_par = nullptr;
+    int32_t* p_edof = nullptr;
+    // element vectors and their ordered gather
+    double* fe = nullptr;
+    int64_t *inv_ptr = nullptr, *inv_idx = nullptr;
+    double* nodemass = nullptr;
+    // T and T^T
+    int32_t *Tp = nullptr, *Tc = nullptr, *TTp = nullptr, *TTr = nullptr;
+    double *Tv = nullptr, *TTv = nullptr;
+    // loads
+    LoadTables lt;
+    int32_t *ld_ptr = nullptr, *ld_ser = nullptr, *s_ptr = nullptr, *sm_ptr = nullptr, *sm_ser = nullptr;
+    double *ld_coef = nullptr, *s_val = nullptr, *sm_fac = nullptr;
+    // state (total dofs) and scratch
+    double *U = nullptr, *V = nullptr, *A = nullptr, *Ub = nullptr, *Us = nullptr;
+    double *W = nullptr, *Wg = nullptr, *yt = nullptr, *ys = nullptr, *pt = nullptr, *sm = nullptr, *dUt = nullptr;
+    // free-dof vectors
+    double *b = nullptr, *x = nullptr, *r1 = nullptr, *r2 = nullptr, *yv = nullptr, *v = nullptr;
+    double *w = nullptr, *w1 = nullptr, *w2 = nullptr, *dinv = nullptr, *tmp = nullptr;
+    double *partial = nullptr, *scal = nullptr;
+    int* bad = nullptr;
+    int64_t iters_total = 0, iters_last = 0;
+    double res_last = 0.0;
+
+    ~svl_xnm() {
+        if (stream) cudaStreamSynchronize(stream);
+        for (void* p : allocs) cudaFree(p);
+        if (stream) cudaStreamDestroy(stream);
+    }
+    template <class T>
+    int alloc(size_t n, T** out) {
+        void* p = nullptr;
+        if (cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(T)) != cudaSuccess) {
+            set_error("cudaMalloc of %zu bytes failed", n * sizeof(T));
+            return SVL_ERR_NOMEM;
+        }
+        allocs.push_back(p);
+        XCUDA(cudaMemsetAsync(p, 0, std::max<size_t>(n, 1) * sizeof(T), stream));
+        *out = static_cast<T*>(p);
+        return SVL_OK;
+    }
+    template <class T>
+    int upload(const std::vector<T>& h, T** out) {
+        XTRY(alloc(h.size(), out));
+        if (!h.empty()) XCUDA(cudaMemcpyAsync(*out, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, stream));
+        return SVL_OK;
+    }
+};
+
+namespace {
+
+int grid_of(int n) { return (n + 255) / 256; }
+
+// y_total = sum over elements of the solid / PML kernels' vectors, gathered
+int x_gather(svl_xnm* X, double* y, double cn, const double* xn, int k, bool fext) {
+    XGather G{};
+    G.ntotal = X->m.ntotal; G.inv_ptr = X->inv_ptr; G.inv_idx = X->inv_idx; G.fe = X->fe;
+    G.nodemass = X->nodemass; G.cn = cn; G.xn = xn;
+    G.k = k; G.with_fext = fext ? 1 : 0;
+    G.ld_ptr = X->ld_ptr; G.ld_ser = X->ld_ser; G.ld_coef = X->ld_coef; G.s_ptr = X->s_ptr; G.s_val = X->s_val;
+    G.y = y;
+    k_xgather<<<grid_of(X->m.ntotal), 256, 0, X->stream>>>(G);
+    XCUDA(cudaGetLastError());
+    return SVL_OK;
+}
+
+XSolid solid_args(svl_xnm* X) {
+    XSolid S{};
+    S.n = X->nsol; S.ngp = X->m.ngp; S.edof = X->s_edof; S.egeo = X->s_egeo; S.geo = X->s_geo;
+    S.coef = X->s_coef; S.ray = X->s_ray; S.mlump = X->s_mlump; S.ftol = -1.0; S.yscale = 1.0;
+    S.y = X->fe;
+    return S;
+}
+PmlArgs pml_args(svl_xnm* X) {
+    PmlArgs P{};
+    P.nelem = X->npml; P.X = X->p_X; P.mat = X->p_mat; P.thick = X->p_thick; P.par = X->p_par;
+    P.edof = X->p_edof; P.y = X->fe + (size_t)X->nsol * X->ncs; P.ftol = -1.0; P.yscale = 1.0;
+    return P;
+}
+int launch_solid(svl_xnm* X, const XSolid& S) {
+    if (S.n <= 0) return SVL_OK;
+    const int g = (S.n + 127) / 128;
+    if (X->m.ndim == 2) k_xsolid<2, 4><<<g, 128, 0, X->stream>>>(S);
+    else k_xsolid<3, 8><<<g, 128, 0, X->stream>>>(S);
+    XCUDA(cudaGetLastError());
+    return SVL_OK;
+}
+
+// out_total = (K + 4/dt^2 M + 2/dt C + dt/3 G) p_total
+int x_op_total(svl_xnm* X, const double* p, double* out) {
+    const double dt = X->opts.dt, cm = 4.0 / dt / dt, cc = 2.0 / dt;
+    XSolid S = solid_args(X);
+    S.xK = p; S.xK2 = p; S.cK2 = cc; S.xM = p; S.sM = cm; S.xM2 = p; S.cM2 = cc;
+    XTRY(launch_solid(X, S));
+    PmlArgs P = pml_args(X);
+    P.coef[0] = cm; P.coef[1] = cc; P.coef[2] = 1.0; P.coef[3] = X->m.ndim == 3 ? dt / 3.0 : 0.0;
+    for (int i = 0; i < 4; ++i) P.u[i] = p;
+    XTRY(pml_action_launch(X->m.ndim, P, X->stream));
+    return x_gather(X, out, cm, p, 0, false);
+}
+
+// q_free = T^T Keff T v
+int x_apply(svl_xnm* X, const double* v, double* q) {
+    k_xexpand<<<grid_of(X->m.ntotal), 256, 0, X->stream>>>(X->m.ntotal, X->Tp, X->Tc, X->Tv, v, X->pt);
+    XTRY(x_op_total(X, X->pt, X->yt));
+    k_xreduce<<<grid_of(X->m.nfree), 256, 0, X->stream>>>(X->m.nfree, X->TTp, X->TTr, X->TTv, X->yt, nullptr, q);
+    XCUDA(cudaGetLastError());
+    return SVL_OK;
+}
+
+int x_dot(svl_xnm* X, const double* a, const double* b2, int slot) {
+    k_xdot_partial<<<kBlocks, kThreads, 0, X->stream>>>(a, b2, X->m.nfree, X->partial);
+    k_xdot_final<<<1, kThreads, 0, X->stream>>>(X->partial, X->scal + slot);
+    XCUDA(cudaGetLastError());
+    return SVL_OK;
+}
+int x_read(svl_xnm* X, int slot, double* out) {
+    XCUDA(cudaMemcpyAsync(out, X->scal + slot, sizeof(double), cudaMemcpyDeviceToHost, X->stream));
+    XCUDA(cudaStreamSynchronize(X->stream));
+    return SVL_OK;
+}
+
+// Preconditioned MINRES on T^T Keff T x = b from x = 0, restarted from its
+// iterate until the true residual meets ||b - A x||_{D^-1} <= tol ||b||_{D^-1}
+// with D = |diag(A)| (the norm MINRES minimises with this preconditioner; the
+// plain 2-norm mixes displacement rows ~1e9 and stress rows ~1e-4 in PML models).
+int x_solve(svl_xnm* X) {
+    const int n = X->m.nfree, g = grid_of(n);
+    X->iters_last = 0;
+    X->res_last = 0.0;
+    if (n == 0) return SVL_OK;
+    XCUDA(cudaMemsetAsync(X->x, 0, sizeof(double) * n, X->stream));
+    k_xvmul<<<g, 256, 0, X->stream>>>(n, X->dinv, X->b, X->yv);
+    XTRY(x_dot(X, X->b, X->yv, 0));
+    double bs2 = 0.0;
+    XTRY(x_read(X, 0, &bs2));
+    if (!std::isfinite(bs2)) { set_error("non-finite effective force"); return SVL_ERR_NONFINITE; }
+    if (bs2 == 0.0) return SVL_OK;
+    const double bs = std::sqrt(bs2), tol = X->opts.tol;
+    int64_t its = 0;
+    bool done = false;
+    for (int restart = 0; restart < 100 && !done; ++restart) {
+        // r1 = b - A x, y = D^-1 r1, beta1 = ||r1||_{D^-1}
+        if (restart == 0) {
+            XCUDA(cudaMemcpyAsync(X->r1, X->b, sizeof(double) * n, cudaMemcpyDeviceToDevice, X->stream));
+        } else {
+            XTRY(x_apply(X, X->x, X->tmp));
+            k_xsub<<<g, 256, 0, X->stream>>>(n, X->b, X->tmp, X->r1);
+        }
+        k_xvmul<<<g, 256, 0, X->stream>>>(n, X->dinv, X->r1, X->yv);
+        XCUDA(cudaMemcpyAsync(X->r2, X->r1, sizeof(double) * n, cudaMemcpyDeviceToDevice, X->stream));
+        XTRY(x_dot(X, X->r1, X->yv, 0));
+        double b1 = 0.0;
+        XTRY(x_read(X, 0, &b1));
+        if (!std::isfinite(b1)) { set_error("MINRES: non-finite residual"); return SVL_ERR_BREAKDOWN; }
+        const double beta1 = std::sqrt(b1);
+        X->res_last = beta1 / bs;
+        if (X->res_last <= tol) { done = true; break; }
+        if (its >= X->opts.maxit) break;
+        double beta = beta1, oldb = 0.0, dbar = 0.0, epsln = 0.0, phibar = beta1, cs = -1.0, sn = 0.0;
+        XCUDA(cudaMemsetAsync(X->w, 0, sizeof(double) * n, X->stream));
+        XCUDA(cudaMemsetAsync(X->w2, 0, sizeof(double) * n, X->stream));
+        const double inner = 0.5 * tol * bs;     // the recurrence estimates ||r||_{D^-1}
+        for (int it = 0; its < X->opts.maxit; ++it) {
+            ++its;
+            // v = y / beta; y = A v - (beta / oldb) r1 - (alfa / beta) r2
+            k_xaxpby<<<g, 256, 0, X->stream>>>(n, 1.0 / beta, X->yv, 0.0, X->v);
+            XTRY(x_apply(X, X->v, X->yv));
+            if (it > 0) k_xaxpby<<<g, 256, 0, X->stream>>>(n, -beta / oldb, X->r1, 1.0, X->yv);
+            XTRY(x_dot(X, X->v, X->yv, 1));
+            double alfa = 0.0;
+            XTRY(x_read(X, 1, &alfa));
+            k_xaxpby<<<g, 256, 0, X->stream>>>(n, -alfa / beta, X->r2, 1.0, X->yv);
+            std::swap(X->r1, X->r2);                 // r1 <- r2
+            std::swap(X->r2, X->yv);                 // r2 <- y; the old r1 buffer becomes y
+            k_xvmul<<<g, 256, 0, X->stream>>>(n, X->dinv, X->r2, X->yv);
+            oldb = beta;
+            XTRY(x_dot(X, X->r2, X->yv, 2));
+            double bb = 0.0;
+            XTRY(x_read(X, 2, &bb));
+            if (!std::isfinite(alfa) || !std::isfinite(bb) || bb < 0.0) {
+                set_error("MINRES breakdown (alpha %g, beta^2 %g)", alfa, bb);
+                return SVL_ERR_BREAKDOWN;
+            }
+            beta = std::sqrt(bb);
+            const double oldeps = epsln;
+            const double delta = cs * dbar + sn * alfa;
+            const double gbar = sn * dbar - cs * alfa;
+            epsln = sn * beta;
+            dbar = -cs * beta;
+            const double gamma = std::max(std::sqrt(gbar * gbar + beta * beta), 1e-300);
+            cs = gbar / gamma;
+            sn = beta / gamma;
+            const double phi = cs * phibar;
+            phibar = sn * phibar;
+            std::swap(X->w1, X->w2);                 // w1 <- w2, w2 <- w, w <- new
+            std::swap(X->w2, X->w);
+            k_xmr_w<<<g, 256, 0, X->stream>>>(n, X->v, X->w1, X->w2, X->w, X->x, oldeps, delta, 1.0 / gamma, phi);
+            XCUDA(cudaGetLastError());
+            if (phibar <= inner || beta == 0.0) break;
+        }
+    }
+    X->iters_last = its;
+    X->iters_total += its;
+    if (!done) {
+        set_error("MINRES did not reach %g in %lld iterations (scaled residual %g)", tol, (long long)its, X->res_last);
+        return SVL_ERR_MAXITER;
+    }
+    return SVL_OK;
+}
+
+// One ExtendedNewmarkBeta step k with the Linear algorithm.
+int x_step(svl_xnm* X, int k) {
+    const HostModel& m = X->m;
+    const int nt = m.ntotal, gt = grid_of(nt);
+    const double dt = X->opts.dt;
+    k_xrhs_vec<<<gt, 256, 0, X->stream>>>(nt, X->U, X->V, X->A, X->Ub, dt, X->W, X->Wg);
+    // solid: -Fint(Us) filtered, then + K (ak V) + M (W + am V)
+    XSolid S = solid_args(X);
+    S.xK = X->Us; S.ftol = X->opts.ftol; S.yscale = -1.0;
+    XTRY(launch_solid(X, S));
+    S = solid_args(X);
+    S.xK2 = X->V; S.cK2 = 1.0; S.xM = X->W; S.sM = 1.0; S.xM2 = X->V; S.cM2 = 1.0; S.accumulate = 1;
+    XTRY(launch_solid(X, S));
+    // PML: -Fint(U) filtered, then + M W + C V - G Wg
+    PmlArgs P = pml_args(X);
+    P.coef[2] = 1.0; P.u[2] = X->U; P.ftol = X->opts.ftol; P.yscale = -1.0;
+    XTRY(pml_action_launch(m.ndim, P, X->stream));
+    P = pml_args(X);
+    P.coef[0] = 1.0; P.u[0] = X->W; P.coef[1] = 1.0; P.u[1] = X->V;
+    if (m.ndim == 3) { P.coef[3] = -1.0; P.u[3] = X->Wg; }
+    P.accumulate = 1;
+    XTRY(pml_action_launch(m.ndim, P, X->stream));
+    XTRY(x_gather(X, X->yt, 1.0, X->W, k, true));
+    const double* sub = nullptr;
+    if (X->lt.has_sm) {
+        k_xsm<<<gt, 256, 0, X->stream>>>(nt, X->sm_ptr, X->sm_ser, X->sm_fac, X->s_ptr, X->s_val, k, X->sm);
+        XTRY(x_op_total(X, X->sm, X->ys));
+        sub = X->ys;
+    }
+    k_xreduce<<<grid_of(m.nfree), 256, 0, X->stream>>>(m.nfree, X->TTp, X->TTr, X->TTv, X->yt, sub, X->b);
+    XCUDA(cudaGetLastError());
+    XTRY(x_solve(X));
+    k_xexpand<<<gt, 256, 0, X->stream>>>(nt, X->Tp, X->Tc, X->Tv, X->x, X->dUt);
+    k_xupdate<<<gt, 256, 0, X->stream>>>(nt, X->U, X->V, X->A, X->Ub, X->Us, X->dUt, X->lt.has_sm ? X->sm : nullptr,
+                                         dt, X->bad);
+    XCUDA(cudaGetLastError());
+    return SVL_OK;
+}
+
+int x_setup(svl_xnm* X, const svl_load_desc* L) {
+    HostModel& m = X->m;
+    const int nd = m.ndim, nen = m.nen, pnd = m.pml_ndof();
+    const int npar = 3 + 2 * nd, per = nen * nd + 1;
+    X->ncs = nen * nd;
+    X->ncp = nen * pnd;
+    std::vector<int> sol, pml;
+    for (int e = 0; e < m.nelem; ++e) ((m.has_pml() && m.epml[e]) ? pml : sol).push_back(e);
+    X->nsol = (int)sol.size();
+    X->npml = (int)pml.size();
+    // flat element-vector index of (element, local dof), element-tag order per dof
+    std::vector<int64_t> base(m.nelem);
+    std::vector<int> ncount(m.nelem);
+    {
+        int is = 0, ip = 0;
+        for (int e = 0; e < m.nelem; ++e) {
+            if (m.has_pml() && m.epml[e]) { base[e] = (int64_t)X->nsol * X->ncs + (int64_t)ip * X->ncp; ncount[e] = X->ncp; ++ip; }
+            else { base[e] = (int64_t)is * X->ncs; ncount[e] = X->ncs; ++is; }
+        }
+    }
+    auto gdof = [&](int e, int i) {
+        const int k = ncount[e] == X->ncs ? nd : pnd;
+        const int n = m.conn[(size_t)e * nen + i / k];
+        return m.tdof_all[(size_t)n * m.dstride + i % k];
+    };
+    std::vector<int64_t> inv_ptr(m.ntotal + 1, 0), inv_idx;
+    for (int e = 0; e < m.nelem; ++e)
+        for (int i = 0; i < ncount[e]; ++i) inv_ptr[gdof(e, i) + 1]++;
+    for (int t = 0; t < m.ntotal; ++t) inv_ptr[t + 1] += inv_ptr[t];
+    inv_idx.resize(inv_ptr.back());
+    {
+        std::vector<int64_t> fill(inv_ptr.begin(), inv_ptr.end() - 1);
+        for (int e = 0; e < m.nelem; ++e)
+            for (int i = 0; i < ncount[e]; ++i) inv_idx[fill[gdof(e, i)]++] = base[e] + i;
+    }
+    // solid tables
+    std::vector<int32_t> s_edof((size_t)X->nsol * X->ncs), s_egeo(X->nsol);
+    std::vector<double> s_geo, s_coef((size_t)X->nsol * 3), s_ray, s_ml((size_t)X->nsol * nen);
+    std::vector<double> diag(m.ntotal, 0.0);
+    const double dt = X->opts.dt, cm = 4.0 / dt / dt, cc = 2.0 / dt;
+    {
+        std::map<std::vector<double>, int> seen;
+        std::vector<double> buf((size_t)m.ngp * per);
+        if (!m.ray.empty()) s_ray.assign((size_t)X->nsol * 2, 0.0);
+        for (int i = 0; i < X->nsol; ++i) {
+            const int e = sol[i];
+            for (int j = 0; j < X->ncs; ++j) s_edof[(size_t)i * X->ncs + j] = gdof(e, j);
+            double mab[8][8] = {};
+            const double* pr = m.param(e);
+            const double rho = pr[2];
+            for (int q = 0; q < m.ngp; ++q) {
+                double dNx[8][3], N[8];
+                const double det = gp_geometry(m, e, q, dNx, N);
+                for (int a = 0; a < nen; ++a)
+                    for (int j = 0; j < nd; ++j) buf[(size_t)q * per + a * nd + j] = dNx[a][j];
+                buf[(size_t)q * per + per - 1] = gp_factor(m, e, det);
+                const double c = nd == 2 ? 1.0 * rho * m.thick[e] * std::fabs(det) : 1.0 * rho * std::fabs(det);
+                for (int a = 0; a < nen; ++a)
+                    for (int b2 = 0; b2 < nen; ++b2) mab[a][b2] += c * (N[a] * N[b2]);
+            }
+            auto it = seen.find(buf);
+            if (it == seen.end()) {
+                it = seen.emplace(buf, (int)(s_geo.size() / ((size_t)m.ngp * per))).first;
+                s_geo.insert(s_geo.end(), buf.begin(), buf.end());
+            }
+            s_egeo[i] = it->second;
+            // row-sum lumping in the reference's order (lin2DQuad4.cpp:272-282)
+            for (int a = 0; a < nen; ++a) {
+                double d = mab[a][a];
+                for (int b2 = 0; b2 < nen; ++b2) if (b2 != a) d += mab[a][b2];
+                s_ml[(size_t)i * nen + a] = std::fabs(d) > X->opts.mtol ? d : 0.0;
+            }
+            const double E = pr[0], nu = pr[1];
+            const double c1 = E * (1.0 - nu) / (1.0 - 2.0 * nu) / (1.0 + nu);
+            const double c2 = E * nu / (1.0 - 2.0 * nu) / (1.0 + nu);
+            const double c3 = E / (2.0 * (1.0 + nu));
+            s_coef[3 * i] = c1; s_coef[3 * i + 1] = c2; s_coef[3 * i + 2] = c3;
+            const double am = m.ray.empty() ? 0.0 : m.ray[2 * (size_t)e], ak = m.ray.empty() ? 0.0 : m.ray[2 * (size_t)e + 1];
+            if (!s_ray.empty()) { s_ray[2 * i] = am; s_ray[2 * i + 1] = ak; }
+            // diagonal of the element's K + 4/dt^2 M + 2/dt C
+            for (int q = 0; q < m.ngp; ++q) {
+                const double* g = &buf[(size_t)q * per];
+                const double w = g[per - 1];
+                for (int a = 0; a < nen; ++a) {
+                    const double bx = g[a * nd], by = g[a * nd + 1], bz = nd == 3 ? g[a * nd + 2] : 0.0;
+                    double kd[3];
+                    if (nd == 2) { kd[0] = w * (c1 * bx * bx + c3 * by * by); kd[1] = w * (c1 * by * by + c3 * bx * bx); }
+                    else {
+                        kd[0] = w * (c1 * bx * bx + c3 * (by * by + bz * bz));
+                        kd[1] = w * (c1 * by * by + c3 * (bx * bx + bz * bz));
+                        kd[2] = w * (c1 * bz * bz + c3 * (bx * bx + by * by));
+                    }
+                    for (int j = 0; j < nd; ++j) diag[gdof(e, a * nd + j)] += (1.0 + cc * ak) * kd[j];
+                }
+            }
+            for (int a = 0; a < nen; ++a)
+                for (int j = 0; j < nd; ++j) diag[gdof(e, a * nd + j)] += (cm + cc * am) * s_ml[(size_t)i * nen + a];
+        }
+    }
+    // PML tables
+    std::vector<double> p_X((size_t)X->npml * nen * nd), p_mat((size_t)X->npml * 3), p_thick(X->npml, 1.0),
+        p_par((size_t)X->npml * npar);
+    std::vector<int32_t> p_edof((size_t)X->npml * X->ncp);
+    for (int i = 0; i < X->npml; ++i) {
+        const int e = pml[i];
+        for (int a = 0; a < nen; ++a)
+            for (int j = 0; j < nd; ++j) p_X[((size_t)i * nen + a) * nd + j] = m.X[(size_t)m.conn[(size_t)e * nen + a] * nd + j];
+        const double* pr = m.param(e);
+        p_mat[3 * i] = pr[0]; p_mat[3 * i + 1] = pr[1]; p_mat[3 * i + 2] = pr[2];
+        if (nd == 2) p_thick[i] = m.thick[e];
+        for (int j = 0; j < npar; ++j) p_par[(size_t)i * npar + j] = m.pml_par[(size_t)e * npar + j];
+        for (int j = 0; j < X->ncp; ++j) p_edof[(size_t)i * X->ncp + j] = gdof(e, j);
+    }
+    // T and T^T
+    std::vector<int32_t> Tp, Tc;
+    std::vector<double> Tv;
+    build_total_to_free(m, Tp, Tc, Tv);
+    std::vector<int32_t> TTp(m.nfree + 1, 0), TTr(Tc.size());
+    std::vector<double> TTv(Tc.size());
+    for (int32_t c : Tc) TTp[c + 1]++;
+    for (int f = 0; f < m.nfree; ++f) TTp[f + 1] += TTp[f];
+    {
+        std::vector<int32_t> fill(TTp.begin(), TTp.end() - 1);
+        for (int t = 0; t < m.ntotal; ++t)
+            for (int i = Tp[t]; i < Tp[t + 1]; ++i) { const int p = fill[Tc[i]]++; TTr[p] = t; TTv[p] = Tv[i]; }
+    }
+    XTRY(build_load_tables(m, L, X->lt));
+    // uploads
+    XTRY(X->upload(s_edof, &X->s_edof)); XTRY(X->upload(s_egeo, &X->s_egeo)); XTRY(X->upload(s_geo, &X->s_geo));
+    XTRY(X->upload(s_coef, &X->s_coef)); XTRY(X->upload(s_ml, &X->s_mlump));
+    if (!s_ray.empty()) XTRY(X->upload(s_ray, &X->s_ray));
+    XTRY(X->upload(p_X, &X->p_X)); XTRY(X->upload(p_mat, &X->p_mat)); XTRY(X->upload(p_thick, &X->p_thick));
+    XTRY(X->upload(p_par, &X->p_par)); XTRY(X->upload(p_edof, &X->p_edof));
+    XTRY(X->alloc((size_t)X->nsol * X->ncs + (size_t)X->npml * X->ncp, &X->fe));
+    XTRY(X->upload(inv_ptr, &X->inv_ptr)); XTRY(X->upload(inv_idx, &X->inv_idx));
+    if (!m.nodemass.empty()) {
+        std::vector<double> nm(m.ntotal, 0.0);
+        for (int t = 0; t < m.ntotal; ++t) if (std::fabs(m.nodemass[t]) > X->opts.mtol) nm[t] = m.nodemass[t];
+        for (int t = 0; t < m.ntotal; ++t) diag[t] += cm * nm[t];
+        XTRY(X->upload(nm, &X->nodemass));
+    }
+    XTRY(X->upload(Tp, &X->Tp)); XTRY(X->upload(Tc, &X->Tc)); XTRY(X->upload(Tv, &X->Tv));
+    XTRY(X->upload(TTp, &X->TTp)); XTRY(X->upload(TTr, &X->TTr)); XTRY(X->upload(TTv, &X->TTv));
+    XTRY(X->upload(X->lt.ld_ptr, &X->ld_ptr)); XTRY(X->upload(X->lt.ld_ser, &X->ld_ser)); XTRY(X->upload(X->lt.ld_coef, &X->ld_coef));
+    XTRY(X->upload(X->lt.s_ptr, &X->s_ptr)); XTRY(X->upload(X->lt.s_val, &X->s_val));
+    XTRY(X->upload(X->lt.sm_ptr, &X->sm_ptr)); XTRY(X->upload(X->lt.sm_ser, &X->sm_ser)); XTRY(X->upload(X->lt.sm_fac, &X->sm_fac));
+    double** tvec[] = {&X->U, &X->V, &X->A, &X->Ub, &X->Us, &X->W, &X->Wg, &X->yt, &X->ys, &X->pt, &X->sm, &X->dUt};
+    for (double** p : tvec) XTRY(X->alloc((size_t)m.ntotal, p));
+    double** fvec[] = {&X->b, &X->x, &X->r1, &X->r2, &X->yv, &X->v, &X->w, &X->w1, &X->w2, &X->tmp};
+    for (double** p : fvec) XTRY(X->alloc((size_t)std::max(m.nfree, 1), p));
+    XTRY(X->alloc(kBlocks, &X->partial));
+    XTRY(X->alloc(8, &X->scal));
+    XTRY(X->alloc(1, &X->bad));
+    // PML diagonal entries by unit probes of the element action (once)
+    if (X->npml > 0) {
+        double *ub = nullptr, *yb = nullptr, *db = nullptr;
+        const size_t ne = (size_t)X->npml * X->ncp;
+        XTRY(X->alloc(ne, &ub)); XTRY(X->alloc(ne, &yb)); XTRY(X->alloc(ne, &db));
+        PmlArgs P{};
+        P.nelem = X->npml; P.X = X->p_X; P.mat = X->p_mat; P.thick = X->p_thick; P.par = X->p_par;
+        P.edof = nullptr; P.y = yb; P.ftol = -1.0; P.yscale = 1.0;
+        P.coef[0] = cm; P.coef[1] = cc; P.coef[2] = 1.0; P.coef[3] = nd == 3 ? dt / 3.0 : 0.0;
+        for (int i = 0; i < 4; ++i) P.u[i] = ub;
+        const int gu = (int)((ne + 255) / 256), ge = grid_of(X->npml);
+        for (int i = 0; i < X->ncp; ++i) {
+            k_xunit<<<gu, 256, 0, X->stream>>>(X->npml, X->ncp, i, ub);
+            XTRY(pml_action_launch(nd, P, X->stream));
+            k_xtake<<<ge, 256, 0, X->stream>>>(X->npml, X->ncp, i, yb, db);
+        }
+        XCUDA(cudaGetLastError());
+        std::vector<double> dh(ne);
+        XCUDA(cudaMemcpyAsync(dh.data(), db, ne * sizeof(double), cudaMemcpyDeviceToHost, X->stream));
+        XCUDA(cudaStreamSynchronize(X->stream));
+        for (int i = 0; i < X->npml; ++i)
+            for (int j = 0; j < X->ncp; ++j) diag[p_edof[(size_t)i * X->ncp + j]] += dh[(size_t)i * X->ncp + j];
+    }
+    // Jacobi on the free dofs: |sum_t T_tf^2 diag_t|^-1
+    std::vector<double> dfree(std::max(m.nfree, 1), 0.0);
+    for (int t = 0; t < m.ntotal; ++t)
+        for (int i = Tp[t]; i < Tp[t + 1]; ++i) dfree[Tc[i]] += Tv[i] * Tv[i] * diag[t];
+    for (double& d : dfree) d = std::fabs(d) > 0.0 ? 1.0 / std::fabs(d) : 1.0;
+    XTRY(X->upload(dfree, &X->dinv));
+    XCUDA(cudaStreamSynchronize(X->stream));
+    return SVL_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int svl_xnm_create(const svl_model_desc* model, const svl_load_desc* loads, const svl_xnm_opts* opts, svl_xnm** out) {
+    if (!out || !opts) { set_error("NULL argument"); return SVL_ERR_INVALID; }
+    *out = nullptr;
+    if (!(opts->dt > 0.0) || !(opts->tol > 0.0) || opts->maxit <= 0) { set_error("bad ExtendedNewmark options"); return SVL_ERR_INVALID; }
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) { set_error("no CUDA device available"); return SVL_ERR_NODEVICE; }
+    svl_xnm* X = new svl_xnm();
+    X->opts = *opts;
+    auto fail = [&](int st) { delete X; return st; };
+    if (!model_from_desc(model, X->m)) return fail(SVL_ERR_INVALID);
+    if (X->m.has_j2()) { set_error("the ExtendedNewmark path covers elastic solid materials"); return fail(SVL_ERR_UNSUPPORTED); }
+    if (!X->m.lumped) { set_error("the ExtendedNewmark path needs a lumped mass for the solid elements"); return fail(SVL_ERR_UNSUPPORTED); }
+    if ((int64_t)X->m.nelem * X->m.nen * X->m.pml_ndof() > ((int64_t)1 << 40)) { set_error("model too large"); return fail(SVL_ERR_UNSUPPORTED); }
+    if (cudaStreamCreateWithFlags(&X->stream, cudaStreamNonBlocking) != cudaSuccess) { set_error("cudaStreamCreate failed"); return fail(SVL_ERR_CUDA); }
+    int st = x_setup(X, loads);
+    if (st) return fail(st);
+    *out = X;
+    return SVL_OK;
+}
+
+int svl_xnm_set_initial(svl_xnm* X, const double* U0, const double* V0, const double* A0, const double* Ubar0) {
+    if (!X) { set_error("NULL handle"); return SVL_ERR_INVALID; }
+    const size_t bytes = sizeof(double) * X->m.ntotal;
+    const double* src[4] = {U0, V0, A0, Ubar0};
+    double* dst[4] = {X->U, X->V, X->A, X->Ub};
+    for (int i = 0; i < 4; ++i) {
+        if (src[i]) XCUDA(cudaMemcpyAsync(dst[i], src[i], bytes, cudaMemcpyHostToDevice, X->stream));
+        else XCUDA(cudaMemsetAsync(dst[i], 0, bytes, X->stream));
+    }
+    XCUDA(cudaMemcpyAsync(X->Us, X->U, bytes, cudaMemcpyDeviceToDevice, X->stream));
+    XCUDA(cudaStreamSynchronize(X->stream));
+    return SVL_OK;
+}
+
+int svl_xnm_run(svl_xnm* X, int32_t k_first, int32_t nsteps, double* U_hist) {
+    if (!X || nsteps < 0) { set_error("bad argument"); return SVL_ERR_INVALID; }
+    const size_t nt = X->m.ntotal;
+    for (int i = 0; i < nsteps; ++i) {
+        XTRY(x_step(X, k_first + i));
+        if (U_hist) XCUDA(cudaMemcpyAsync(U_hist + (size_t)i * nt, X->U, sizeof(double) * nt, cudaMemcpyDeviceToHost, X->stream));
+    }
+    int bad = 0;
+    XCUDA(cudaMemcpyAsync(&bad, X->bad, sizeof(int), cudaMemcpyDeviceToHost, X->stream));
+    XCUDA(cudaStreamSynchronize(X->stream));
+    if (bad) { set_error("non-finite displacement"); return SVL_ERR_NONFINITE; }
+    return SVL_OK;
+}
+
+int svl_xnm_get(svl_xnm* X, int32_t which, double* out) {
+    if (!X || !out || which < 0 || which > 3) { set_error("bad argument"); return SVL_ERR_INVALID; }
+    const double* src[4] = {X->U, X->V, X->A, X->Ub};
+    XCUDA(cudaMemcpyAsync(out, src[which], sizeof(double) * X->m.ntotal, cudaMemcpyDeviceToHost, X->stream));
+    XCUDA(cudaStreamSynchronize(X->stream));
+    return SVL_OK;
+}
+
+int svl_xnm_stats(svl_xnm* X, int64_t* iters_total, int64_t* iters_last, double* res_last) {
+    if (!X) { set_error("NULL handle"); return SVL_ERR_INVALID; }
+    if (iters_total) *iters_total = X->iters_total;
+    if (iters_last) *iters_last = X->iters_last;
+    if (res_last) *res_last = X->res_last;
+    return SVL_OK;
+}
+
+void svl_xnm_destroy(svl_xnm* X) { delete X; }
+
+}  // extern "C"

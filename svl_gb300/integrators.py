@@ -170,6 +170,74 @@ class StructuredCentralDifference:
             pass
 
 
+class ExtendedNewmarkBeta:
+    """ExtendedNewmarkBeta (RP/10-Integrators/03-Newmark/ExtendedNewmarkBeta.cpp)
+    with the Linear algorithm for meshes with PML2DQuad4 / PML3DHexa8 layers
+    (svl_xnm_*): the PML history term G (Ubar + dt U + dt^2/6 V), Rayleigh and
+    PML damping, support motion of step k, and a matrix-free MINRES solve of
+    the symmetric indefinite effective matrix to the relative true residual
+    `tol` in the |diag|^-1 norm.  GetPMLHistoryVector returns Ubar."""
+
+    def __init__(self, model: Model, loads: Loads | None, dt: float, tol: float = 1e-10, maxit: int = 100000,
+                 ftol: float = 1e-12, mtol: float = 1e-12):
+        self.model = model
+        self.dt = float(dt)
+        self._md = model.desc()
+        self._ld = (loads or Loads()).desc()
+        opts = capi.XnmOpts(dt=self.dt, ftol=ftol, mtol=mtol, tol=float(tol), maxit=int(maxit))
+        h = C.c_void_p()
+        check(lib().svl_xnm_create(C.byref(self._md), C.byref(self._ld), C.byref(opts), C.byref(h)))
+        self._h = h
+        self.ntotal = model.ntotal
+
+    def Initialize(self, U0=None, V0=None, A0=None, Ubar0=None):
+        arrs = [None if a is None else capi.as_f64(a) for a in (U0, V0, A0, Ubar0)]
+        check(lib().svl_xnm_set_initial(self._h, *(ptr(a, C.c_double) for a in arrs)))
+
+    def ComputeNewStep(self, k: int) -> bool:
+        """One step k; returns True on failure (the reference's `stop`)."""
+        return lib().svl_xnm_run(self._h, int(k), 1, ptr(None, C.c_double)) != capi.SVL_OK
+
+    def _get(self, which):
+        out = np.zeros(self.ntotal)
+        check(lib().svl_xnm_get(self._h, int(which), ptr(out, C.c_double)))
+        return out
+
+    def GetDisplacements(self) -> np.ndarray:
+        return self._get(0)
+
+    def GetVelocities(self) -> np.ndarray:
+        return self._get(1)
+
+    def GetAccelerations(self) -> np.ndarray:
+        return self._get(2)
+
+    def GetPMLHistoryVector(self) -> np.ndarray:
+        return self._get(3)
+
+    def run(self, k_first: int, nsteps: int, history: bool = False):
+        hist = np.zeros((nsteps, self.ntotal)) if history else None
+        check(lib().svl_xnm_run(self._h, int(k_first), int(nsteps), ptr(hist, C.c_double)))
+        return hist
+
+    def stats(self):
+        """(MINRES iterations in total, in the last solve, last relative true residual)."""
+        a, b, r = C.c_int64(), C.c_int64(), C.c_double()
+        check(lib().svl_xnm_stats(self._h, C.byref(a), C.byref(b), C.byref(r)))
+        return a.value, b.value, r.value
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().svl_xnm_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class NewmarkBeta:
     """Implicit Newmark, average acceleration (beta = 1/4, gamma = 1/2), with
     the Linear algorithm: one effective-stiffness solve per step by a

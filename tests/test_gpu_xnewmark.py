@@ -1,0 +1,69 @@
+"""ExtendedNewmarkBeta with PML layers on the GPU (svl_xnm_*), against the
+oracle's ExtendedNewmarkBeta (dense LDL^T of the assembled K + 4/dt^2 M +
+2/dt C + dt/3 G): PML2DQuad4 and PML3DHexa8 boxes, the PML history vector,
+the reduction to NewmarkBeta without PML, constraints with support motion,
+and the paths that reject PML models."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from svl_gb300 import CentralDifference, ExtendedNewmarkBeta, NewmarkBeta, SvlError
+from svl_gb300 import _capi as capi
+from tests.helpers import h8_box, pml_box, q4_box, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("ndim,ni,npml,nt", [(2, (10, 6), 2, 120), (3, (3, 3, 2), 1, 40)], ids=["quad", "hexa"])
+def test_pml_box_matches_oracle(gpu, ndim, ni, npml, nt):
+    m, L, dt = pml_box(ndim, ni, npml=npml, nt=nt, f0=10.0, dt_factor=1.0)
+    x = ExtendedNewmarkBeta(m, L, dt, tol=1e-12)
+    x.Initialize()
+    hist = x.run(1, nt, history=True)
+    Ub = x.GetPMLHistoryVector()
+    V = x.GetVelocities()
+    its, last, res = x.stats()
+    x.close()
+    ho, Uo, Vo, Ao, Ubo = O.xnewmark_run(m, L, dt, nt)
+    assert np.abs(ho).max() > 0 and res <= 1e-12 and its > 0
+    # the effective matrix's condition number is ~1e13 (stress rows ~1e-4,
+    # displacement rows ~1e9): a solve is good to ~1e-10 at best
+    assert rel_l2(hist, ho) <= 1e-8
+    assert rel_l2(Ub, Ubo) <= 1e-8
+    assert rel_l2(V, Vo) <= 1e-7
+
+
+def test_without_pml_matches_newmark_with_rayleigh(gpu):
+    m, L, dt = h8_box(5, 4, 3, nt=40)
+    m.rayleigh = np.tile([1.5, 1.0e-3], (m.nelem, 1))
+    x = ExtendedNewmarkBeta(m, L, 4 * dt, tol=1e-13)
+    x.Initialize()
+    hist = x.run(1, 30, history=True)
+    x.close()
+    ho, _ = O.newmark_run(m, L, 4 * dt, 30, solver=0)
+    assert rel_l2(hist, ho) <= 1e-9
+
+
+def test_constraints_and_support_motion(gpu):
+    from tests.test_gpu_newton import _columns
+    m, L, dt = _columns(elastic=True)
+    x = ExtendedNewmarkBeta(m, L, 4 * dt, tol=1e-13)
+    x.Initialize()
+    hist = x.run(1, 50, history=True)
+    x.close()
+    ho, *_ = O.xnewmark_run(m, L, 4 * dt, 50)
+    assert np.abs(ho).max() > 0
+    assert rel_l2(hist, ho) <= 1e-9
+
+
+def test_other_paths_reject_pml_models(gpu):
+    m, L, dt = pml_box(2, (4, 3), npml=2, nt=10)
+    for make in (lambda: CentralDifference(m, L, dt), lambda: NewmarkBeta(m, L, dt)):
+        with pytest.raises(SvlError) as ei:
+            make()
+        assert ei.value.code == capi.SVL_ERR_UNSUPPORTED
+    m2, L2, dt2 = q4_box(4, 3, nt=10)
+    m2.mat_type = np.array([capi.SVL_MAT_PLASTICPLANESTRAINJ2], np.int32)
+    with pytest.raises(SvlError) as ei:
+        ExtendedNewmarkBeta(m2, L2, dt2)
+    assert ei.value.code == capi.SVL_ERR_UNSUPPORTED
