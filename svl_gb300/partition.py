@@ -10,12 +10,14 @@ pre-processed model runs on the GPU integrators, and writes node recorder
 output in the run-process's text format (RP/12-Utilities/Recorder.cpp:73-106
 header, 239-268 rows).
 
-Covered: lin2DQuad4 / lin3DHexa8 elements; Elastic2DPlaneStrain,
-Elastic3DLinear, PlasticPlaneStrainJ2, Plastic3DJ2 materials; restraints;
-EQUAL-type constraints; nodal masses; point loads and element body loads
-(constant or time series); support motions (constant or time series); node
-recorders of displacement, velocity or acceleration; CentralDifference and
-NewmarkBeta integrators.  Anything else raises PartitionError naming it.
+Covered: lin2DQuad4 / lin3DHexa8 elements with PML2DQuad4 / PML3DHexa8
+layers (5 / 9 dofs at their nodes); Elastic2DPlaneStrain, Elastic3DLinear,
+PlasticPlaneStrainJ2, Plastic3DJ2 materials; restraints; EQUAL-type
+constraints; nodal masses; Rayleigh dampings; point loads and element body
+loads (constant or time series); support motions (constant or time series);
+node recorders of displacement, velocity or acceleration; the integrators
+CentralDifference, Newmark and ExtendedNewmark under the names the run-process
+accepts (Driver.hpp:1808-1822).  Anything else raises PartitionError naming it.
 """
 from __future__ import annotations
 
@@ -30,6 +32,7 @@ from . import _capi as capi
 from .model import Loads, Model
 
 _ELEM = {"LIN2DQUAD4": (2, 4, capi.SVL_ELEM_LIN2DQUAD4), "LIN3DHEXA8": (3, 8, capi.SVL_ELEM_LIN3DHEXA8)}
+_PML = {"PML2DQUAD4": "LIN2DQUAD4", "PML3DHEXA8": "LIN3DHEXA8"}
 _MAT = {
     "ELASTIC2DPLANESTRAIN": (capi.SVL_MAT_ELASTIC2DPLANESTRAIN, ("E", "nu", "rho")),
     "ELASTIC3DLINEAR": (capi.SVL_MAT_ELASTIC3DLINEAR, ("E", "nu", "rho")),
@@ -82,19 +85,24 @@ class Partition:
     root: Optional[Path] = None
 
     def make_integrator(self, pcg_tol: Optional[float] = None):
-        """The GPU integrator the simulation block asks for (CentralDifference or
-        NewmarkBeta with the Linear algorithm); an iterative solver's `tol` is the
-        PCG tolerance, a direct solver gets 1e-12."""
-        from .integrators import CentralDifference, NewmarkBeta
+        """The GPU integrator the simulation block asks for: CENTRALDIFFERENCE,
+        NEWMARK (NewmarkBeta) or EXTENDEDNEWMARK (ExtendedNewmarkBeta, the one
+        that takes PML layers), with the Linear algorithm (Driver.hpp:1808-1822);
+        an iterative solver's `tol` is the solve tolerance, a direct solver
+        gets 1e-12."""
+        from .integrators import CentralDifference, ExtendedNewmarkBeta, NewmarkBeta
         if self.integrator == "CENTRALDIFFERENCE":
             return CentralDifference(self.model, self.loads, self.dt, ftol=self.ftol, mtol=self.mtol)
-        if self.integrator in ("NEWMARKBETA", "EXTENDEDNEWMARKBETA"):
+        if self.integrator in ("NEWMARK", "EXTENDEDNEWMARK"):
             if self.algorithm.get("name", "LINEAR").upper() != "LINEAR":
                 raise PartitionError("algorithm %s is not covered (Linear only)" % self.algorithm.get("name"))
             tol = pcg_tol if pcg_tol is not None else (float(self.solver.get("tol", 1e-12))
                                                        if self.solver.get("name", "").upper() == "PETSC" else 1e-12)
+            if self.integrator == "EXTENDEDNEWMARK":
+                return ExtendedNewmarkBeta(self.model, self.loads, self.dt, tol=tol, ftol=self.ftol, mtol=self.mtol)
             return NewmarkBeta(self.model, self.loads, self.dt, pcg_tol=tol, ftol=self.ftol, mtol=self.mtol)
-        raise PartitionError("integrator %s is not covered" % self.integrator)
+        raise PartitionError("integrator %s is not covered (the run-process names CENTRALDIFFERENCE, NEWMARK, "
+                             "EXTENDEDNEWMARK)" % self.integrator)
 
     def run(self, write_recorders: bool = True, solution_dir: Optional[Path] = None):
         """The run-process's dynamic loop (DynamicAnalysis.cpp:25-64): steps
@@ -134,13 +142,14 @@ def write_node_recorder(path: Path, part: Partition, rec: Recorder, hist: np.nda
     m = part.model
     pos = {int(t): i for i, t in enumerate(part.node_tags)}
     idx = [pos[t] for t in rec.ids]
-    ndof = m.totaldof.shape[1]
+    nnd = m.dof_mask().sum(axis=1)
     fmt = "%." + str(int(rec.precision)) + "e "
-    cols = np.concatenate([m.totaldof[i] for i in idx]) if idx else np.zeros(0, np.int64)
+    dofs = [m.totaldof[i, :nnd[i]] for i in idx]
+    cols = np.concatenate(dofs) if idx else np.zeros(0, np.int64)
     with open(path, "w") as f:
-        f.write("%d %d %d %d\n" % (len(idx), ndof * len(idx), m.ntotal, part.nt))
-        for t, i in zip(rec.ids, idx):
-            f.write("%d %d %s\n" % (t, ndof, " ".join(str(int(d)) for d in m.totaldof[i])))
+        f.write("%d %d %d %d\n" % (len(idx), cols.size, m.ntotal, part.nt))
+        for t, d in zip(rec.ids, dofs):
+            f.write("%d %d %s\n" % (t, d.size, " ".join(str(int(x)) for x in d)))
         for row in hist[:, cols]:
             f.write("".join(fmt % v for v in row) + "\n")
 
@@ -157,12 +166,18 @@ def load_partition(path, run_dir=None) -> Partition:
     # nodes in ascending tag order (the run-process's std::map order)
     ntags = sorted(int(t) for t in d["Nodes"])
     nodes = [d["Nodes"][str(t)] for t in ntags]
-    ndofs = {int(n["ndof"]) for n in nodes}
-    if len(ndofs) != 1 or ndofs.pop() != ndim:
-        raise PartitionError("nodes with %s dofs: only %d-dof displacement nodes are covered" % (sorted({int(n['ndof']) for n in nodes}), ndim))
+    pnd = 5 if ndim == 2 else 9
+    nnd = np.array([int(n["ndof"]) for n in nodes], dtype=np.int32)
+    if not np.all((nnd == ndim) | (nnd == pnd)):
+        raise PartitionError("nodes with %s dofs: %d-dof displacement nodes and %d-dof PML nodes are covered"
+                             % (sorted(set(nnd.tolist())), ndim, pnd))
+    stride = int(nnd.max())
     coords = np.array([n["coords"] for n in nodes], dtype=np.float64).reshape(len(nodes), ndim)
-    totaldof = np.array([n["totaldof"] for n in nodes], dtype=np.int32).reshape(len(nodes), ndim)
-    freedof = np.array([n["freedof"] for n in nodes], dtype=np.int32).reshape(len(nodes), ndim)
+    totaldof = -np.ones((len(nodes), stride), np.int32)
+    freedof = -np.ones((len(nodes), stride), np.int32)
+    for i, n in enumerate(nodes):
+        totaldof[i, :nnd[i]] = n["totaldof"]
+        freedof[i, :nnd[i]] = n["freedof"]
     npos = {t: i for i, t in enumerate(ntags)}
     # materials
     mtags = sorted(int(t) for t in d.get("Materials", {}))
@@ -180,11 +195,21 @@ def load_partition(path, run_dir=None) -> Partition:
     etags = sorted(int(t) for t in d["Elements"])
     els = [d["Elements"][str(t)] for t in etags]
     names = {e["name"].upper() for e in els}
-    if len(names) != 1 or next(iter(names)) not in _ELEM:
-        raise PartitionError("element classes %s: one of %s per model is covered" % (sorted(names), sorted(_ELEM)))
-    edim, nen, etype = _ELEM[next(iter(names))]
+    solid = {_PML.get(n, n) for n in names}
+    if len(solid) != 1 or next(iter(solid)) not in _ELEM:
+        raise PartitionError("element classes %s: one of %s per model (with its PML class) is covered"
+                             % (sorted(names), sorted(_ELEM)))
+    edim, nen, etype = _ELEM[next(iter(solid))]
     if edim != ndim:
         raise PartitionError("element dimension does not match Global.ndim")
+    # PML elements (Driver.hpp:1203-1220, 1288-1306): n, L, R, x0, npml
+    epml = np.array([1 if e["name"].upper() in _PML else 0 for e in els], dtype=np.int32)
+    pml_param = np.zeros((len(els), 3 + 2 * ndim))
+    for i, e in enumerate(els):
+        if epml[i]:
+            a = e["attributes"]
+            pml_param[i] = [float(a["n"]), float(a["L"]), float(a["R"])] + [float(v) for v in a["x0"][:ndim]] \
+                + [float(v) for v in a["npml"][:ndim]]
     conn = np.array([[npos[int(c)] for c in e["conn"]] for e in els], dtype=np.int32).reshape(len(els), nen)
     elem_mat = np.array([mpos[int(e["attributes"]["material"])] for e in els], dtype=np.int32)
     thick = np.array([float(e["attributes"].get("th", 1.0)) for e in els]) if ndim == 2 else None
@@ -228,7 +253,9 @@ def load_partition(path, run_dir=None) -> Partition:
     model = Model(ndim=ndim, coords=coords, totaldof=totaldof, freedof=freedof, conn=conn, elem_type=etype,
                   elem_mat=elem_mat, mat_type=mat_type, mat_param=mat_param,
                   lumped=str(g.get("massform", "CONSISTENT")).upper() == "LUMPED",
-                  thickness=thick, node_mass=node_mass, rayleigh=ray if np.any(ray) else None)
+                  thickness=thick, node_mass=node_mass, rayleigh=ray if np.any(ray) else None,
+                  node_ndof=nnd if stride != ndim else None, elem_pml=epml if epml.any() else None,
+                  pml_param=pml_param if epml.any() else None)
     if con is not None:
         model.con_slave, model.con_ptr, model.con_master, model.con_factor = con
     if model.ntotal != int(g["ntotal"]) or model.nfree != int(g["nfree"]):

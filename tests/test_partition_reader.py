@@ -19,14 +19,16 @@ def _part(case):
     return GOLD / ("partition_%s" % case) / "Partition" / "Fixture.1.0.json"
 
 
-@pytest.mark.parametrize("case", ["q4_cd", "h8_newmark_body", "q4_j2_column", "q4_newmark_rayleigh"])
+@pytest.mark.parametrize("case", ["q4_cd", "h8_newmark_body", "q4_j2_column", "q4_newmark_rayleigh", "q4_pml_extended"])
 def test_numbering_and_connectivity_follow_the_file(case):
     p = load_partition(_part(case))
     d = json.loads(_part(case).read_text())
     tags = sorted(int(t) for t in d["Nodes"])
     assert list(p.node_tags) == tags
-    assert np.array_equal(p.model.totaldof, np.array([d["Nodes"][str(t)]["totaldof"] for t in tags]))
-    assert np.array_equal(p.model.freedof, np.array([d["Nodes"][str(t)]["freedof"] for t in tags]))
+    nnd = p.model.dof_mask().sum(axis=1)
+    for i, t in enumerate(tags):
+        assert list(p.model.totaldof[i, :nnd[i]]) == d["Nodes"][str(t)]["totaldof"]
+        assert list(p.model.freedof[i, :nnd[i]]) == d["Nodes"][str(t)]["freedof"]
     for i, et in enumerate(sorted(int(t) for t in d["Elements"])):
         assert [tags[j] for j in p.model.conn[i]] == d["Elements"][str(et)]["conn"]
     assert p.model.ntotal == d["Global"]["ntotal"] and p.model.nfree == d["Global"]["nfree"]
@@ -50,7 +52,7 @@ def test_q4_loads_materials_and_recorder():
 
 def test_h8_body_load_and_solver_settings():
     p = load_partition(_part("h8_newmark_body"))
-    assert p.integrator == "NEWMARKBETA" and p.solver["name"] == "PETSC" and p.solver["tol"] == 1e-10
+    assert p.integrator == "NEWMARK" and p.solver["name"] == "PETSC" and p.solver["tol"] == 1e-10
     # body load entries sum to factor * rho * volume * series for each loaded element
     coef = np.array(p.loads.force_coef)
     assert np.isclose(coef.sum(), 2.0e3 * 2000.0 * 8.0 * 2)
@@ -88,11 +90,42 @@ def test_rayleigh_dampings_by_tag_order():
     ray = p.model.rayleigh
     for i, t in enumerate(etags):
         assert tuple(ray[i]) == ((2.5, 1.5e-3) if t % 2 == 0 else (0.0, 0.0))
-    assert p.integrator == "NEWMARKBETA"
+    assert p.integrator == "NEWMARK"
     h, _ = O.newmark_run(p.model, p.loads, p.dt, p.nt - 1, solver=0)
     p.model.rayleigh = None
     h0, _ = O.newmark_run(p.model, p.loads, p.dt, p.nt - 1, solver=0)
     assert np.all(np.isfinite(h)) and np.linalg.norm(h - h0) > 1e-3 * np.linalg.norm(h0)
+
+
+def test_pml_layers_and_extended_newmark():
+    """setPMLDomain + mergeDomain output: 5-dof PML nodes tied to the soil by
+    EQUAL constraints, PML2DQuad4 parameters per element, ExtendedNewmark."""
+    p = load_partition(_part("q4_pml_extended"))
+    d = json.loads(_part("q4_pml_extended").read_text())
+    m = p.model
+    assert p.integrator == "EXTENDEDNEWMARK" and m.nconstraint > 0
+    assert sorted(set(m.node_ndof.tolist())) == [2, 5]
+    etags = sorted(int(t) for t in d["Elements"])
+    for i, t in enumerate(etags):
+        e = d["Elements"][str(t)]
+        assert m.elem_pml[i] == (e["name"] == "PML2DQUAD4")
+        if m.elem_pml[i]:
+            a = e["attributes"]
+            assert list(m.pml_param[i]) == [a["n"], a["L"], a["R"]] + a["x0"] + a["npml"]
+    h, U, V, A, Ub = O.xnewmark_run(m, p.loads, p.dt, p.nt - 1)
+    assert np.all(np.isfinite(h)) and np.abs(h).max() > 0 and np.abs(Ub).max() > 0
+
+
+def test_integrator_names_are_the_run_process_ones(tmp_path):
+    d = json.loads(_part("h8_newmark_body").read_text())
+    d["Simulations"]["attributes"]["integrator"]["name"] = "NEWMARKBETA"
+    (tmp_path / "Partition").mkdir()
+    f = tmp_path / "Partition" / "x.json"
+    f.write_text(json.dumps(d))
+    (tmp_path / "body.txt").write_text((GOLD / "partition_h8_newmark_body" / "body.txt").read_text())
+    p = load_partition(f)
+    with pytest.raises(PartitionError, match="NEWMARKBETA"):
+        p.make_integrator()
 
 
 def test_uncovered_content_is_named(tmp_path):
