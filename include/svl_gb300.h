@@ -105,6 +105,14 @@ typedef struct svl_model_desc {
     const int32_t* node_ndof;       /* [nnode], or NULL: every node has ndof dofs   */
     const int32_t* elem_pml;        /* [nelem] 1 for a PML element, or NULL         */
     const double*  elem_pml_param;  /* [nelem][3 + 2 ndim]: n, L, R, x0[ndim], npml[ndim] */
+    /* Lysmer dashpots: ZeroLength1D elements with a Viscous1DLinear material
+     * (RP/04-Elements/01-Zero/ZeroLength1D.cpp:210-228, Driver.hpp:602-607,
+     * 1072-1078): C_e = eta a a^T with a = (-1, +1) on the direction `dir` of
+     * the element's two nodes; no mass, no stiffness and no internal force (the
+     * material's elastic stress is 0).  Listed in element-tag order.         */
+    int32_t ndashpot;
+    const int32_t* dashpot_dof;     /* [ndashpot][2] total dofs (node 1, node 2) */
+    const double*  dashpot_eta;     /* [ndashpot] damping coefficients          */
 } svl_model_desc;
 
 /* ---- loads -------------------------------------------------------------- */

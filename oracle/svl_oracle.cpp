@@ -51,6 +51,8 @@ struct Model {
     std::vector<int> nndof, tdof_all, fdof_all;   // every dof of a node (PML nodes 5 / 9)
     std::vector<int> epml;            // [nelem] PML flag, empty without PML
     std::vector<double> pml_par;      // [nelem][3 + 2 ndim]
+    std::vector<int> dp_dof;          // [ndashpot][2] Lysmer dashpots (ZeroLength1D + Viscous1DLinear)
+    std::vector<double> dp_eta;
     std::vector<int> conn, emat;
     std::vector<double> thick;
     std::vector<int> mtype;
@@ -121,6 +123,11 @@ bool load_model(const svl_model_desc* d, Model& m) {
     m.mpar.assign(d->mat_param, d->mat_param + (size_t)d->nmat * SVL_MAT_NPARAM);
     if (d->node_mass) m.nodemass.assign(d->node_mass, d->node_mass + m.ntotal);
     if (d->elem_rayleigh) m.ray.assign(d->elem_rayleigh, d->elem_rayleigh + (size_t)2 * m.nelem);
+    m.dp_dof.clear(); m.dp_eta.clear();
+    if (d->ndashpot > 0) {
+        m.dp_dof.assign(d->dashpot_dof, d->dashpot_dof + 2 * (size_t)d->ndashpot);
+        m.dp_eta.assign(d->dashpot_eta, d->dashpot_eta + d->ndashpot);
+    }
     m.nconstraint = d->nconstraint;
     if (m.nconstraint > 0) {
         m.cslave.assign(d->con_slave, d->con_slave + m.nconstraint);
@@ -688,7 +695,8 @@ struct Sim {
 struct CD {
     Sim s; double dt;
     std::vector<double> U, V, A, Up, Md, Kd, Kff_inv, Us;
-    std::vector<double> Cd;    // Rayleigh damping diagonal (mass-proportional), empty when undamped
+    std::vector<double> Cd;    // damping diagonal (mass-proportional Rayleigh, dashpots), empty when undamped
+    std::vector<int> dpa, dpb; std::vector<double> dpe;   // dashpot off-diagonal couplings C_ab = -eta
     bool fast = false;
     std::vector<double> geo;   // fast mode: [nelem][ngp][nen*ndim + 1]
     std::vector<double> fe_all;  // fast mode: element force blocks
@@ -717,6 +725,20 @@ struct CD {
                     if (std::fabs(v) > s.ktol) Cd[s.edofs[(size_t)e * nc + i]] += v;
                 }
             }
+        }
+        // dashpots: C_e = eta [1 -1; -1 1] (ZeroLength1D.cpp:210-228).  The
+        // diagonal solve holds when no dashpot couples two free (or constrained) dofs
+        for (size_t i = 0; i < s.m.dp_eta.size(); ++i) {
+            const int a = s.m.dp_dof[2 * i], b = s.m.dp_dof[2 * i + 1];
+            const double eta = s.m.dp_eta[i];
+            if (!(std::fabs(eta) > s.ktol)) continue;
+            const int na = s.Tptr[a + 1] - s.Tptr[a], nb = s.Tptr[b + 1] - s.Tptr[b];
+            if (na > 0 && nb > 0) return false;
+            if ((na > 0 && (na != 1 || s.Tval[s.Tptr[a]] != 1.0)) || (nb > 0 && (nb != 1 || s.Tval[s.Tptr[b]] != 1.0))) return false;
+            if (Cd.empty()) Cd.assign(nt, 0.0);
+            Cd[a] += eta; Cd[b] += eta;
+            dpa.push_back(a); dpb.push_back(b); dpe.push_back(eta);
+            dpa.push_back(b); dpb.push_back(a); dpe.push_back(eta);
         }
         // K = 1/dt/dt*M + 1/2/dt*C (CentralDifference.cpp:70)
         Kd.resize(nt);
@@ -805,12 +827,15 @@ struct CD {
             const double c = Cd.empty() ? 1.0 / dt / dt * Md[t] : 1.0 / dt / dt * Md[t] - 1.0 / 2.0 / dt * Cd[t];
             R[t] = (Fext[t] + 0.0 - Fint[t]) + c * (U[t] - Up[t]);
         }
+        for (size_t i = 0; i < dpa.size(); ++i)          // off-diagonal dashpot terms: -1/2/dt * (-eta)
+            R[dpa[i]] += 1.0 / 2.0 / dt * dpe[i] * (U[dpb[i]] - Up[dpb[i]]);
         s.TT_apply(R, Feff);
         // support motion: Feff -= T^T (K SM)   (CentralDifference.cpp:190-202)
         s.support_increment(k, SM);
         {
             std::vector<double> KSM(nt), lg;
             for (int t = 0; t < nt; ++t) KSM[t] = Kd[t] * SM[t];
+            for (size_t i = 0; i < dpa.size(); ++i) KSM[dpa[i]] -= 1.0 / 2.0 / dt * dpe[i] * SM[dpb[i]];
             s.TT_apply(KSM, lg);
             for (int f = 0; f < s.m.nfree; ++f) Feff[f] -= lg[f];
         }
@@ -962,9 +987,25 @@ struct Newmark {
                         if (std::fabs(v) > s.ktol) ct.push_back({s.edofs[(size_t)e * nc + i], s.edofs[(size_t)e * nc + j], v});
                     }
             }
+            push_dashpots(ct);
+            csr_from_triplets(nt, ct, Ct);
+        } else if (!s.m.dp_eta.empty()) {
+            std::vector<Trip> ct;
+            push_dashpots(ct);
             csr_from_triplets(nt, ct, Ct);
         }
         return true;
+    }
+    // ZeroLength1D damping eta a a^T, a = (-1, +1) on its two dofs, column by column
+    // with the stiffness tolerance (Assembler.cpp:117-158)
+    void push_dashpots(std::vector<Trip>& ct) const {
+        for (size_t i = 0; i < s.m.dp_eta.size(); ++i) {
+            const int a = s.m.dp_dof[2 * i], b = s.m.dp_dof[2 * i + 1];
+            const double eta = s.m.dp_eta[i];
+            if (!(std::fabs(eta) > s.ktol)) continue;
+            ct.push_back({a, a, eta}); ct.push_back({b, a, -eta});
+            ct.push_back({a, b, -eta}); ct.push_back({b, b, eta});
+        }
     }
     // T^T K T as free-dof CSR
     void reduce(const std::vector<Trip>& totalTr, CSR& Kff) const {
@@ -1318,6 +1359,12 @@ struct XNewmark {
                     push(tc, e, Ce.data(), s.ktol);
                 }
             }
+        }
+        for (size_t i = 0; i < m.dp_eta.size(); ++i) {       // ZeroLength1D dashpots
+            const int a = m.dp_dof[2 * i], b = m.dp_dof[2 * i + 1];
+            const double eta = m.dp_eta[i];
+            if (!(std::fabs(eta) > s.ktol)) continue;
+            tc.push_back({a, a, eta}); tc.push_back({b, a, -eta}); tc.push_back({a, b, -eta}); tc.push_back({b, b, eta});
         }
         if (!m.nodemass.empty())
             for (int t = 0; t < nt; ++t) if (std::fabs(m.nodemass[t]) > s.mtol) tm.push_back({t, t, m.nodemass[t]});

@@ -57,6 +57,7 @@ class ModelDesc(C.Structure):
         ("nmat", C.c_int32), ("mat_type", i32p), ("mat_param", f64p),
         ("lumped", C.c_int32), ("node_mass", f64p), ("elem_rayleigh", f64p),
         ("node_ndof", i32p), ("elem_pml", i32p), ("elem_pml_param", f64p),
+        ("ndashpot", C.c_int32), ("dashpot_dof", i32p), ("dashpot_eta", f64p),
     ]
 
 

@@ -77,6 +77,8 @@ struct DevView {
     // Rayleigh damping C = sum_e (am_e M_e + ak_e K0_e) (lin2DQuad4.cpp:355-366)
     const double* Cd;        // [ntotal] sum_e am_e M_e (lumped), or null
     const double* dk0;       // [3][E]   ak_e * (c1, c2, c3) of the initial elastic tangent, or null
+    // Lysmer dashpots on the implicit path: y_t += c sum eta (x_t - x_partner)
+    const int32_t* dp_ptr; const int32_t* dp_col; const double* dp_eta;
     double *U, *V, *A, *Up, *Us, *R, *du;
     // T and T^T as CSR (constraint path)
     const int32_t *T_ptr, *T_col; const double* T_val;
@@ -496,6 +498,7 @@ struct svl_cd {
     int ngeo = 0;
     bool identity_T = true;
     bool has_sm = false;
+    bool implicit = false;                 // tables for the Newmark path (dashpot couplings)
     cudaGraphExec_t graph = nullptr;
     int graph_steps = 0;
     int64_t launches = 0;
@@ -632,6 +635,37 @@ static int cd_setup(svl_cd* cd, const svl_load_desc* L) {
             }
         }
     }
+    // Lysmer dashpots (ZeroLength1D, C_e = eta [1 -1; -1 1]).  Explicit path:
+    // the solve stays diagonal when each dashpot ties a free dof to a restrained
+    // one that carries no support motion (its off-diagonal term then always
+    // multiplies zero); their diagonal joins C.  Implicit path: couplings per dof.
+    std::vector<int32_t> dp_ptr, dp_col;
+    std::vector<double> dp_eta;
+    if (!m.dp_eta.empty()) {
+        if (cd->implicit) {
+            dashpot_tables(m, dp_ptr, dp_col, dp_eta);
+        } else {
+            std::vector<signed char> kind(m.ntotal, 0), smd(m.ntotal, 0);     // 0 restrained, 1 free, 2 constrained
+            for (int n = 0; n < m.nnode; ++n)
+                for (int j = 0; j < m.nndof[n]; ++j)
+                    if (m.fdof_all[(size_t)n * m.dstride + j] >= 0) kind[m.tdof_all[(size_t)n * m.dstride + j]] = 1;
+            for (int c = 0; c < m.nconstraint; ++c) kind[m.cslave[c]] = 2;
+            if (L) for (int i = 0; i < L->nsupport; ++i)
+                if (L->sm_dof && L->sm_dof[i] >= 0 && L->sm_dof[i] < m.ntotal) smd[L->sm_dof[i]] = 1;
+            if (Cdm.empty()) Cdm.assign(m.ntotal, 0.0);
+            for (size_t i = 0; i < m.dp_eta.size(); ++i) {
+                const int a = m.dp_dof[2 * i], b = m.dp_dof[2 * i + 1];
+                if (kind[a] == 2 || kind[b] == 2 || (kind[a] == 1 && kind[b] == 1) ||
+                    (kind[a] == 0 && smd[a]) || (kind[b] == 0 && smd[b])) {
+                    set_error("dashpot %zu: the explicit path needs each dashpot between a free dof and a restrained "
+                              "dof without support motion (otherwise M/dt^2 + C/2dt is not diagonal)", i);
+                    return SVL_ERR_UNSUPPORTED;
+                }
+                Cdm[a] += m.dp_eta[i];
+                Cdm[b] += m.dp_eta[i];
+            }
+        }
+    }
     // K = 1/dt/dt M + 1/2/dt C (CentralDifference.cpp:70); C diagonal here
     std::vector<double> Kd(m.ntotal);
     for (int t = 0; t < m.ntotal; ++t) Kd[t] = Cdm.empty() ? inv_dt2 * Md[t] : inv_dt2 * Md[t] + 1.0 / 2.0 / dt * Cdm[t];
@@ -691,6 +725,9 @@ static int cd_setup(svl_cd* cd, const svl_load_desc* L) {
     TRY(cd->upload(kinv, &d.kinv));
     TRY(cd->upload(Kd, &d.Kd));
     if (!Cdm.empty()) TRY(cd->upload(Cdm, &d.Cd));
+    if (!dp_eta.empty()) {
+        TRY(cd->upload(dp_ptr, &d.dp_ptr)); TRY(cd->upload(dp_col, &d.dp_col)); TRY(cd->upload(dp_eta, &d.dp_eta));
+    }
     if (!dk0.empty()) TRY(cd->upload(dk0, &d.dk0));
     TRY(cd->zeros(m.ntotal, &d.U)); TRY(cd->zeros(m.ntotal, &d.V)); TRY(cd->zeros(m.ntotal, &d.A));
     TRY(cd->zeros(m.ntotal, &d.Up)); TRY(cd->zeros(m.ntotal, &d.Us)); TRY(cd->zeros(m.ntotal, &d.R));
@@ -825,6 +862,7 @@ static int cd_create(const svl_model_desc* model, const svl_load_desc* loads, co
     if (cudaStreamCreateWithFlags(&cd->stream, cudaStreamNonBlocking) != cudaSuccess) {
         delete cd; set_error("cudaStreamCreate failed"); return SVL_ERR_CUDA;
     }
+    cd->implicit = implicit;
     int st = cd_setup(cd, loads);
     if (st != SVL_OK) { delete cd; return st; }
     *out = cd;
@@ -1204,7 +1242,15 @@ __global__ void k_nmg_expand(DevView d, const double* __restrict__ pf, double* _
     pt[t] = v;
 }
 
-// ft = sum_e K_e p_e + c_m M p (+ c_c C_m p) on total dofs (ordered gather of d.fe)
+// sum over the dashpots at dof t of eta (x_t - x_partner)
+__device__ __forceinline__ double dashpot_sum(const DevView& d, int t, const double* __restrict__ x) {
+    double v = 0.0;
+    const double xt = x[t];
+    for (int i = d.dp_ptr[t]; i < d.dp_ptr[t + 1]; ++i) v += d.dp_eta[i] * (xt - x[d.dp_col[i]]);
+    return v;
+}
+
+// ft = sum_e K_e p_e + c_m M p (+ c_c C p) on total dofs (ordered gather of d.fe)
 template <int ND>
 __global__ void __launch_bounds__(256) k_nmg_total(DevView d, const double* __restrict__ pt, double* __restrict__ ft,
                                                    double c_m, double c_c) {
@@ -1215,6 +1261,7 @@ __global__ void __launch_bounds__(256) k_nmg_total(DevView d, const double* __re
         const int t = d.ntdof[n * ND + c];
         double v = gather_fint<ND>(d, n, c) + c_m * d.Md[t] * pt[t];
         if (d.Cd) v += c_c * d.Cd[t] * pt[t];
+        if (d.dp_ptr) v += c_c * dashpot_sum(d, t, pt);
         ft[t] = v;
     }
 }
@@ -1235,6 +1282,7 @@ __global__ void __launch_bounds__(256) k_nmg_damp(DevView d, const double* __res
         const int t = d.ntdof[n * ND + c];
         double v = d.dk0 ? gather_fint<ND>(d, n, c) : 0.0;
         if (d.Cd) v += d.Cd[t] * w[t];
+        if (d.dp_ptr) v += dashpot_sum(d, t, w);
         ft[t] += v;
     }
 }
@@ -1793,7 +1841,7 @@ int svl_nm_create(const svl_model_desc* model, const svl_load_desc* loads, const
     nm->opts = *opts;
     auto fail = [&](int s2) { delete nm; return s2; };
     const HostModel& m = cd->m;
-    nm->damped = !m.ray.empty();
+    nm->damped = !m.ray.empty() || !m.dp_eta.empty();
     nm->general = !cd->identity_T || cd->has_sm || nm->damped;
     if (opts->algorithm != SVL_ALGO_LINEAR && opts->algorithm != SVL_ALGO_NEWTON) { set_error("unknown algorithm %d", opts->algorithm); return fail(SVL_ERR_INVALID); }
     nm->newton = opts->algorithm == SVL_ALGO_NEWTON;
@@ -1842,10 +1890,14 @@ int svl_nm_create(const svl_model_desc* model, const svl_load_desc* loads, const
     }
     std::vector<double> M;
     lumped_mass_diag(m, opts->mtol, M);
-    if (nm->damped) {                       // + 2/dt sum_e am_e M_e
+    if (nm->damped) {                       // + 2/dt (sum_e am_e M_e + dashpot diagonal)
         std::vector<double> Cm;
         rayleigh_mass_diag(m, Cm);
         for (int t = 0; t < m.ntotal; ++t) Kd[t] += c_c * Cm[t];
+        for (size_t i = 0; i < m.dp_eta.size(); ++i) {
+            Kd[m.dp_dof[2 * i]] += c_c * m.dp_eta[i];
+            Kd[m.dp_dof[2 * i + 1]] += c_c * m.dp_eta[i];
+        }
     }
     std::vector<double> dinv(std::max(m.nfree, 1), 1.0);
     if (!cd->identity_T) {

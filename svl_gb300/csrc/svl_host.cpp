@@ -104,6 +104,14 @@ bool model_from_desc(const svl_model_desc* d, HostModel& m) {
         }
         if (!any) m.ray.clear();
     }
+    m.dp_dof.clear(); m.dp_eta.clear();
+    if (d->ndashpot > 0) {
+        if (!d->dashpot_dof || !d->dashpot_eta) { set_error("dashpot arrays are NULL"); return false; }
+        m.dp_dof.assign(d->dashpot_dof, d->dashpot_dof + 2 * (size_t)d->ndashpot);
+        m.dp_eta.assign(d->dashpot_eta, d->dashpot_eta + d->ndashpot);
+        for (int32_t t : m.dp_dof) if (t < 0 || t >= m.ntotal) { set_error("dashpot dof %d out of range", t); return false; }
+        for (double e : m.dp_eta) if (!(e >= 0.0) || !std::isfinite(e)) { set_error("dashpot coefficient must be finite and >= 0"); return false; }
+    } else if (d->ndashpot < 0) { set_error("ndashpot < 0"); return false; }
     m.lumped = d->lumped;
     m.nconstraint = d->nconstraint;
     m.cslave.clear(); m.cptr.assign(1, 0); m.cmaster.clear(); m.cfactor.clear();
@@ -288,6 +296,22 @@ void lumped_mass_diag(const HostModel& m, double mtol, std::vector<double>& M) {
         double mn = 0.0;
         if (!m.nodemass.empty() && std::fabs(m.nodemass[t]) > mtol) mn = m.nodemass[t];
         M[t] = Me_e[t] + mn;
+    }
+}
+
+void dashpot_tables(const HostModel& m, std::vector<int32_t>& ptr, std::vector<int32_t>& col,
+                    std::vector<double>& eta) {
+    ptr.assign(m.ntotal + 1, 0);
+    col.clear(); eta.clear();
+    const size_t n = m.dp_eta.size();
+    for (size_t i = 0; i < n; ++i) { ptr[m.dp_dof[2 * i] + 1]++; ptr[m.dp_dof[2 * i + 1] + 1]++; }
+    for (int t = 0; t < m.ntotal; ++t) ptr[t + 1] += ptr[t];
+    col.resize(ptr.back()); eta.resize(ptr.back());
+    std::vector<int32_t> fill(ptr.begin(), ptr.end() - 1);
+    for (size_t i = 0; i < n; ++i) {
+        const int32_t a = m.dp_dof[2 * i], b = m.dp_dof[2 * i + 1];
+        col[fill[a]] = b; eta[fill[a]++] = m.dp_eta[i];
+        col[fill[b]] = a; eta[fill[b]++] = m.dp_eta[i];
     }
 }
 

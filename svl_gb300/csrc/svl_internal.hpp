@@ -28,6 +28,8 @@ struct HostModel {
     std::vector<int32_t> nndof, tdof_all, fdof_all;
     std::vector<int32_t> epml;        // [nelem] 1 for a PML element (empty: none)
     std::vector<double> pml_par;      // [nelem][3 + 2 ndim] n, L, R, x0, npml
+    std::vector<int32_t> dp_dof;      // [ndashpot][2] total dofs of the Lysmer dashpots
+    std::vector<double> dp_eta;       // [ndashpot]
     std::vector<double> thick;
     std::vector<int32_t> mtype;
     std::vector<double> mpar;
@@ -63,6 +65,10 @@ void parallel_for(int64_t n, const std::function<void(int64_t, int64_t)>& body);
 
 // Diagonal of the assembled row-sum-lumped mass on total dofs.
 void lumped_mass_diag(const HostModel& m, double mtol, std::vector<double>& M);
+// Dashpot couplings per total dof, CSR: y_t += c * sum eta (x_t - x_partner)
+// for every dashpot that touches t (element order); empty without dashpots.
+void dashpot_tables(const HostModel& m, std::vector<int32_t>& ptr, std::vector<int32_t>& col,
+                    std::vector<double>& eta);
 // Mass-proportional Rayleigh damping on total dofs, sum_e am_e M_e with the
 // element row-sum lumped masses (lin2DQuad4.cpp:360-366 with a lumped mass)
 void rayleigh_mass_diag(const HostModel& m, std::vector<double>& C);

@@ -151,6 +151,10 @@ struct XGather {
     const double* nodemass;      // [ntotal] or null
     double cn;
     const double* xn;
+    // Lysmer dashpots: + cdp sum eta (x_t - x_partner)
+    const int32_t *dp_ptr, *dp_col; const double* dp_eta;
+    double cdp;
+    const double* xdp;
     // external force (RHS only)
     int k, with_fext;
     const int32_t *ld_ptr, *ld_ser; const double* ld_coef;
@@ -164,6 +168,12 @@ __global__ void k_xgather(XGather G) {
     double v = 0.0;
     for (int64_t i = G.inv_ptr[t]; i < G.inv_ptr[t + 1]; ++i) v += G.fe[G.inv_idx[i]];
     if (G.nodemass && G.xn) v += G.cn * G.nodemass[t] * G.xn[t];
+    if (G.dp_ptr && G.xdp) {
+        double c = 0.0;
+        const double xt = G.xdp[t];
+        for (int i = G.dp_ptr[t]; i < G.dp_ptr[t + 1]; ++i) c += G.dp_eta[i] * (xt - G.xdp[G.dp_col[i]]);
+        v += G.cdp * c;
+    }
     if (G.with_fext) {
         double f = 0.0;
         for (int i = G.ld_ptr[t]; i < G.ld_ptr[t + 1]; ++i) {
@@ -321,6 +331,8 @@ struct svl_xnm {
     double* fe = nullptr;
     int64_t *inv_ptr = nullptr, *inv_idx = nullptr;
     double* nodemass = nullptr;
+    int32_t *dp_ptr = nullptr, *dp_col = nullptr;
+    double* dp_eta = nullptr;
     // T and T^T
     int32_t *Tp = nullptr, *Tc = nullptr, *TTp = nullptr, *TTr = nullptr;
     double *Tv = nullptr, *TTv = nullptr;
@@ -369,10 +381,11 @@ namespace {
 int grid_of(int n) { return (n + 255) / 256; }
 
 // y_total = sum over elements of the solid / PML kernels' vectors, gathered
-int x_gather(svl_xnm* X, double* y, double cn, const double* xn, int k, bool fext) {
+int x_gather(svl_xnm* X, double* y, double cn, const double* xn, double cdp, const double* xdp, int k, bool fext) {
     XGather G{};
     G.ntotal = X->m.ntotal; G.inv_ptr = X->inv_ptr; G.inv_idx = X->inv_idx; G.fe = X->fe;
     G.nodemass = X->nodemass; G.cn = cn; G.xn = xn;
+    G.dp_ptr = X->dp_ptr; G.dp_col = X->dp_col; G.dp_eta = X->dp_eta; G.cdp = cdp; G.xdp = xdp;
     G.k = k; G.with_fext = fext ? 1 : 0;
     G.ld_ptr = X->ld_ptr; G.ld_ser = X->ld_ser; G.ld_coef = X->ld_coef; G.s_ptr = X->s_ptr; G.s_val = X->s_val;
     G.y = y;
@@ -413,7 +426,7 @@ int x_op_total(svl_xnm* X, const double* p, double* out) {
     P.coef[0] = cm; P.coef[1] = cc; P.coef[2] = 1.0; P.coef[3] = X->m.ndim == 3 ? dt / 3.0 : 0.0;
     for (int i = 0; i < 4; ++i) P.u[i] = p;
     XTRY(pml_action_launch(X->m.ndim, P, X->stream));
-    return x_gather(X, out, cm, p, 0, false);
+    return x_gather(X, out, cm, p, cc, p, 0, false);
 }
 
 // q_free = T^T Keff T v
@@ -548,7 +561,7 @@ int x_step(svl_xnm* X, int k) {
     if (m.ndim == 3) { P.coef[3] = -1.0; P.u[3] = X->Wg; }
     P.accumulate = 1;
     XTRY(pml_action_launch(m.ndim, P, X->stream));
-    XTRY(x_gather(X, X->yt, 1.0, X->W, k, true));
+    XTRY(x_gather(X, X->yt, 1.0, X->W, 1.0, X->V, k, true));
     const double* sub = nullptr;
     if (X->lt.has_sm) {
         k_xsm<<<gt, 256, 0, X->stream>>>(nt, X->sm_ptr, X->sm_ser, X->sm_fac, X->s_ptr, X->s_val, k, X->sm);
@@ -700,6 +713,16 @@ int x_setup(svl_xnm* X, const svl_load_desc* L) {
     XTRY(X->upload(p_par, &X->p_par)); XTRY(X->upload(p_edof, &X->p_edof));
     XTRY(X->alloc((size_t)X->nsol * X->ncs + (size_t)X->npml * X->ncp, &X->fe));
     XTRY(X->upload(inv_ptr, &X->inv_ptr)); XTRY(X->upload(inv_idx, &X->inv_idx));
+    if (!m.dp_eta.empty()) {                 // ZeroLength1D dashpots
+        std::vector<int32_t> dpp, dpc;
+        std::vector<double> dpe;
+        dashpot_tables(m, dpp, dpc, dpe);
+        for (size_t i = 0; i < m.dp_eta.size(); ++i) {
+            diag[m.dp_dof[2 * i]] += cc * m.dp_eta[i];
+            diag[m.dp_dof[2 * i + 1]] += cc * m.dp_eta[i];
+        }
+        XTRY(X->upload(dpp, &X->dp_ptr)); XTRY(X->upload(dpc, &X->dp_col)); XTRY(X->upload(dpe, &X->dp_eta));
+    }
     if (!m.nodemass.empty()) {
         std::vector<double> nm(m.ntotal, 0.0);
         for (int t = 0; t < m.ntotal; ++t) if (std::fabs(m.nodemass[t]) > X->opts.mtol) nm[t] = m.nodemass[t];

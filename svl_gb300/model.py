@@ -41,6 +41,8 @@ class Model:
     node_ndof: Optional[np.ndarray] = None  # [nnode] dofs of each node (PML nodes 5 / 9), None: all ndof
     elem_pml: Optional[np.ndarray] = None   # [nelem] 1 for PML2DQuad4 / PML3DHexa8 elements
     pml_param: Optional[np.ndarray] = None  # [nelem, 3 + 2 ndim] n, L, R, x0, npml
+    dashpot_dof: Optional[np.ndarray] = None  # [n, 2] total dofs of Lysmer dashpots (ZeroLength1D)
+    dashpot_eta: Optional[np.ndarray] = None  # [n] damping coefficients
     grid_shape: Optional[tuple] = None   # (nx, ny[, nz]) when built by grid()
     _keep: list = field(default_factory=list, repr=False)
 
@@ -89,6 +91,8 @@ class Model:
             node_ndof=None if self.node_ndof is None else as_i32(self.node_ndof),
             elem_pml=None if self.elem_pml is None else as_i32(self.elem_pml),
             pml_param=None if self.pml_param is None else as_f64(self.pml_param),
+            dashpot_dof=None if self.dashpot_dof is None else as_i32(self.dashpot_dof),
+            dashpot_eta=None if self.dashpot_eta is None else as_f64(self.dashpot_eta),
         )
         self._keep = list(arrs.values())
         d = capi.ModelDesc()
@@ -119,6 +123,9 @@ class Model:
         d.node_ndof = ptr(arrs["node_ndof"], C.c_int32)
         d.elem_pml = ptr(arrs["elem_pml"], C.c_int32)
         d.elem_pml_param = ptr(arrs["pml_param"], C.c_double)
+        d.ndashpot = 0 if self.dashpot_eta is None else int(np.asarray(self.dashpot_eta).size)
+        d.dashpot_dof = ptr(arrs["dashpot_dof"], C.c_int32)
+        d.dashpot_eta = ptr(arrs["dashpot_eta"], C.c_double)
         return d
 
     # ------------------------------------------------------------------

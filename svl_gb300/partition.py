@@ -13,7 +13,8 @@ header, 239-268 rows).
 Covered: lin2DQuad4 / lin3DHexa8 elements with PML2DQuad4 / PML3DHexa8
 layers (5 / 9 dofs at their nodes); Elastic2DPlaneStrain, Elastic3DLinear,
 PlasticPlaneStrainJ2, Plastic3DJ2 materials; restraints; EQUAL-type
-constraints; nodal masses; Rayleigh dampings; point loads and element body
+constraints; nodal masses; Rayleigh dampings; ZeroLength1D elements with a
+Viscous1DLinear material (Lysmer dashpots); point loads and element body
 loads (constant or time series); support motions (constant or time series);
 node recorders of displacement, velocity or acceleration; the integrators
 CentralDifference, Newmark and ExtendedNewmark under the names the run-process
@@ -179,8 +180,10 @@ def load_partition(path, run_dir=None) -> Partition:
         totaldof[i, :nnd[i]] = n["totaldof"]
         freedof[i, :nnd[i]] = n["freedof"]
     npos = {t: i for i, t in enumerate(ntags)}
-    # materials
-    mtags = sorted(int(t) for t in d.get("Materials", {}))
+    # materials (Viscous1DLinear, Driver.hpp:602-607, only as a ZeroLength1D dashpot)
+    viscous = {int(t): float(mt["attributes"].get("eta", 0.0)) for t, mt in d.get("Materials", {}).items()
+               if mt["name"].upper() == "VISCOUS1DLINEAR"}
+    mtags = sorted(int(t) for t in d.get("Materials", {}) if int(t) not in viscous)
     mpos = {t: i for i, t in enumerate(mtags)}
     mat_type = np.zeros(len(mtags), np.int32)
     mat_param = np.zeros((len(mtags), capi.SVL_MAT_NPARAM))
@@ -191,8 +194,23 @@ def load_partition(path, run_dir=None) -> Partition:
             raise PartitionError("material %s (tag %d) is not covered" % (mat["name"], t))
         mat_type[i], keys = _MAT[name]
         mat_param[i, :len(keys)] = [float(mat["attributes"][k]) for k in keys]
-    # elements in ascending tag order
-    etags = sorted(int(t) for t in d["Elements"])
+    # elements in ascending tag order; ZeroLength1D elements with a viscous
+    # material become dashpots on their direction `dir` (ZeroLength1D.cpp:210-228)
+    dash_dof, dash_eta = [], []
+    for t in sorted(int(x) for x in d["Elements"]):
+        e = d["Elements"][str(t)]
+        if e["name"].upper() != "ZEROLENGTH1D":
+            continue
+        mt = int(e["attributes"]["material"])
+        if mt not in viscous:
+            raise PartitionError("ZeroLength1D element %d: only a Viscous1DLinear material (a dashpot) is covered" % t)
+        j = int(e["attributes"]["dir"])
+        a, b = (npos[int(c)] for c in e["conn"])
+        if not (0 <= j < ndim):
+            raise PartitionError("ZeroLength1D element %d: dir %d out of range" % (t, j))
+        dash_dof.append((int(totaldof[a, j]), int(totaldof[b, j])))
+        dash_eta.append(viscous[mt])
+    etags = sorted(int(t) for t in d["Elements"] if d["Elements"][t]["name"].upper() != "ZEROLENGTH1D")
     els = [d["Elements"][str(t)] for t in etags]
     names = {e["name"].upper() for e in els}
     solid = {_PML.get(n, n) for n in names}
@@ -255,7 +273,9 @@ def load_partition(path, run_dir=None) -> Partition:
                   lumped=str(g.get("massform", "CONSISTENT")).upper() == "LUMPED",
                   thickness=thick, node_mass=node_mass, rayleigh=ray if np.any(ray) else None,
                   node_ndof=nnd if stride != ndim else None, elem_pml=epml if epml.any() else None,
-                  pml_param=pml_param if epml.any() else None)
+                  pml_param=pml_param if epml.any() else None,
+                  dashpot_dof=np.array(dash_dof, np.int32).reshape(-1, 2) if dash_dof else None,
+                  dashpot_eta=np.array(dash_eta) if dash_eta else None)
     if con is not None:
         model.con_slave, model.con_ptr, model.con_master, model.con_factor = con
     if model.ntotal != int(g["ntotal"]) or model.nfree != int(g["nfree"]):

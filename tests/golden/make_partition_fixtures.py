@@ -3,8 +3,8 @@ running the SeismoVLAB pre-processor itself (PP/Core/SeismoVLAB.py
 CreateRunAnalysisFiles) on small models that exercise every field the
 partition reader maps: materials (elastic and J2), restraints, EQUAL
 constraints, point and element body loads (constant and time series),
-support motions, Rayleigh dampings, PML layers, node recorders, the
-integrator/solver settings.
+support motions, Rayleigh dampings, PML layers, Lysmer dashpots, node
+recorders, the integrator/solver settings.
 
 Run from the repository root where the reference tree is available:
     python tests/golden/make_partition_fixtures.py /path/to/SVL
@@ -226,6 +226,50 @@ SVL.addRecorder(tag=1, attributes={"name": "NODE", "file": "Disp.out", "ndps": 8
 SVL.addAnalysis(tag=1, attributes={"name": "Dynamic", "nt": nt})
 SVL.addAlgorithm(tag=1, attributes={"name": "Linear", "nstep": 1})
 SVL.addIntegrator(tag=1, attributes={"name": "ExtendedNewmark", "dt": dt})
+SVL.addSolver(tag=1, attributes={"name": "Eigen", "update": "OFF"})
+SVL.addSimulation(tag=1, combo=1, attributes={"analysis": 1, "algorithm": 1, "integrator": 1, "solver": 1})
+SVL.CreateRunAnalysisFiles()
+''',
+    # Q4 soil column on Lysmer dashpots (ZeroLength1D + Viscous1DLinear to fixed
+    # anchor nodes at the base), periodic-free sides, CentralDifference
+    "q4_lysmer_cd": COMMON + r'''
+SVL.Options["dimension"] = 2
+SVL.Options["massform"] = "lumped"
+nx, ny, h, dt, nt = 4, 8, 0.5, 1.0e-4, 61
+rho, E, nu = 2000.0, 2.0e8, 0.25
+G = E / 2.0 / (1 + nu); lam = E * nu / (1 + nu) / (1 - 2 * nu)
+vp, vs = math.sqrt((lam + 2 * G) / rho), math.sqrt(G / rho)
+SVL.addMaterial(tag=1, name="Elastic2DPlaneStrain", attributes={"E": E, "nu": nu, "rho": rho})
+SVL.addMaterial(tag=2, name="Viscous1DLinear", attributes={"eta": rho * vp * h})
+SVL.addMaterial(tag=3, name="Viscous1DLinear", attributes={"eta": rho * vs * h})
+mesh = SVL.makeDomainArea(options={"ne": [nx, ny], "ndof": 2, "class": "LIN2DQUAD4", "elems": "QUAD4",
+    "P0": [0.0, 0.0], "P1": [nx * h, 0.0], "P2": [0.0, ny * h],
+    "attributes": {"material": 1, "th": 1.0, "rule": "Gauss", "np": 4}})
+for tag in sorted(mesh["Nodes"]):
+    n = mesh["Nodes"][tag]
+    SVL.addNode(tag=tag, ndof=n["ndof"], coords=list(map(float, n["coords"])))
+for tag in sorted(mesh["Elements"]):
+    el = mesh["Elements"][tag]
+    SVL.addElement(tag=tag, conn=list(el["conn"]), name=el["name"], attributes=dict(el["attributes"]))
+base = [t for t in sorted(mesh["Nodes"]) if abs(mesh["Nodes"][t]["coords"][1]) < 1e-9]
+ntag = max(mesh["Nodes"]) + 1
+etag = max(mesh["Elements"]) + 1
+for t in base:
+    SVL.addNode(tag=ntag, ndof=2, coords=list(map(float, mesh["Nodes"][t]["coords"])))
+    SVL.addRestrain(tag=ntag, dof=[1, 2])
+    SVL.addElement(tag=etag, conn=[ntag, t], name="ZeroLength1D", attributes={"material": 3, "dir": 1})
+    SVL.addElement(tag=etag + 1, conn=[ntag, t], name="ZeroLength1D", attributes={"material": 2, "dir": 2})
+    ntag += 1
+    etag += 2
+top = [t for t in sorted(mesh["Nodes"]) if abs(mesh["Nodes"][t]["coords"][1] - ny * h) < 1e-9]
+write_series("pulse.txt", ricker(nt, dt, 60.0, 2.0e4))
+SVL.addFunction(tag=1, name="TimeSeries", attributes={"file": "pulse.txt", "dir": [1.0, -0.5]})
+SVL.addLoad(tag=1, name="PointLoad", attributes={"type": "Concentrated", "fun": 1, "list": top})
+SVL.addCombinationCase(tag=1, name="Fixture", attributes={"load": [1], "factor": [1.0]})
+SVL.addRecorder(tag=1, attributes={"name": "NODE", "file": "Base.out", "ndps": 8, "resp": "disp", "list": base[:2]})
+SVL.addAnalysis(tag=1, attributes={"name": "Dynamic", "nt": nt})
+SVL.addAlgorithm(tag=1, attributes={"name": "Linear", "nstep": 1})
+SVL.addIntegrator(tag=1, attributes={"name": "CentralDifference", "dt": dt})
 SVL.addSolver(tag=1, attributes={"name": "Eigen", "update": "OFF"})
 SVL.addSimulation(tag=1, combo=1, attributes={"analysis": 1, "algorithm": 1, "integrator": 1, "solver": 1})
 SVL.CreateRunAnalysisFiles()

@@ -152,3 +152,39 @@ def pml_box(ndim=2, ni=(6, 4), npml=2, h=1.0, E=2.0e8, nu=0.25, rho=2000.0, nt=8
     c = top[np.argmin(np.sum((X[top, :vert] - np.array(hi[:vert]) / 2 - np.array(lo[:vert]) / 2) ** 2, axis=1))]
     L.add_point_load(m, int(c), tuple([0.0] * vert + [-1.0]), s)
     return m, L, dt
+
+
+def lysmer_box(nx=12, ny=6, h=1.0, E=2.0e8, nu=0.25, rho=2000.0, nt=200, amp=1.0e6, f0=8.0, dt_factor=0.5):
+    """Plane-strain box whose sides and bottom are free but held by Lysmer
+    dashpots (ZeroLength1D + Viscous1DLinear) to anchor nodes that are fixed:
+    normal dashpots rho Vp h and tangential rho Vs h per boundary node (half on
+    corner-adjacent edges is not attempted; the test needs only the operator)."""
+    m = Model.grid(2, (nx, ny), (h, h), mat_type=np.array([capi.SVL_MAT_ELASTIC2DPLANESTRAIN], np.int32),
+                   mat_param=elastic_params(2, E, nu, rho)[None, :])
+    G = E / (2 * (1 + nu))
+    lam = E * nu / ((1 + nu) * (1 - 2 * nu))
+    vp, vs = np.sqrt((lam + 2 * G) / rho), np.sqrt(G / rho)
+    X = m.coords
+    bnodes = [n for n in range(m.nnode) if np.isclose(X[n, 1], 0) or np.isclose(X[n, 0], 0) or np.isclose(X[n, 0], nx * h)]
+    nn0 = m.nnode
+    na = len(bnodes)
+    coords = np.vstack([X, X[bnodes]])
+    tdof = np.vstack([m.totaldof, (m.ntotal + np.arange(2 * na)).reshape(na, 2)]).astype(np.int32)
+    fdof = np.vstack([m.freedof, -np.ones((na, 2), np.int32)]).astype(np.int32)
+    dof, eta = [], []
+    for i, n in enumerate(bnodes):
+        a = nn0 + i
+        bottom = np.isclose(X[n, 1], 0)
+        for j in range(2):
+            normal = (j == 1) if bottom else (j == 0)
+            dof.append((int(m.totaldof[n, j]), int(tdof[a, j])))
+            eta.append(rho * (vp if normal else vs) * h)
+    m2 = Model(ndim=2, coords=coords, totaldof=tdof, freedof=fdof, conn=m.conn, elem_type=m.elem_type,
+               elem_mat=m.elem_mat, mat_type=m.mat_type, mat_param=m.mat_param, lumped=True,
+               dashpot_dof=np.array(dof, np.int32), dashpot_eta=np.array(eta))
+    dt = dt_factor * h / vp
+    L = Loads()
+    s = L.add_series(ricker(nt + 1, dt, f0, amp=amp))
+    top = ny * (nx + 1) + nx // 2
+    L.add_point_load(m2, top, (0.0, -1.0), s)
+    return m2, L, dt

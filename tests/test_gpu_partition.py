@@ -27,7 +27,7 @@ def _read_recorder(path):
     return (nn, ndofs, ntotal, nt), head, rows
 
 
-@pytest.mark.parametrize("case", ["q4_cd", "q4_j2_column"])
+@pytest.mark.parametrize("case", ["q4_cd", "q4_j2_column", "q4_lysmer_cd"])
 def test_cd_partitions_match_oracle_and_record(gpu, case, tmp_path):
     p = _part(case)
     U = p.run(solution_dir=tmp_path)

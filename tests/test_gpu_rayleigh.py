@@ -86,3 +86,56 @@ def test_central_difference_rejects_stiffness_proportional(gpu):
     with pytest.raises(SvlError) as ei:
         CentralDifference(m, L, dt)
     assert ei.value.code == capi.SVL_ERR_UNSUPPORTED
+
+
+def test_lysmer_dashpots_on_all_paths(gpu):
+    """ZeroLength1D dashpots to fixed anchors: explicit CD (diagonal), NewmarkBeta
+    and ExtendedNewmarkBeta, against the oracle."""
+    from svl_gb300 import ExtendedNewmarkBeta
+    from tests.helpers import lysmer_box
+    m, L, dt = lysmer_box(16, 8, nt=300)
+    cd = CentralDifference(m, L, dt)
+    cd.Initialize()
+    hc = cd.run(1, 300, history=True)
+    cd.close()
+    ho, *_ = O.cd_run(m, L, dt, 300)
+    assert np.abs(ho).max() > 0 and rel_l2(hc, ho) <= 1e-12
+    nm = NewmarkBeta(m, L, 4 * dt, pcg_tol=1e-13)
+    nm.Initialize()
+    hn = nm.run(1, 60, history=True)
+    nm.close()
+    hno, _ = O.newmark_run(m, L, 4 * dt, 60, solver=0)
+    assert rel_l2(hn, hno) <= 1e-9
+    x = ExtendedNewmarkBeta(m, L, 4 * dt, tol=1e-13)
+    x.Initialize()
+    hx = x.run(1, 60, history=True)
+    x.close()
+    assert rel_l2(hx, hno) <= 1e-9
+
+
+def test_newton_j2_with_lysmer_dashpots(gpu):
+    """The SPD alternative to a PML half-space under J2 layers: Newton with the
+    consistent tangent plus dashpot damping, fixed iteration count."""
+    from svl_gb300 import j2_params
+    from tests.helpers import lysmer_box
+    m, L, dt = lysmer_box(10, 6, nt=60, amp=4.0e5)
+    G = 2000.0 * 200.0 ** 2
+    K = 2 * G * 1.25 / (3 * 0.5)
+    m.mat_type = np.array([capi.SVL_MAT_PLASTICPLANESTRAINJ2], np.int32)
+    m.mat_param = j2_params(K, G, 2000.0, 0.02 * G, 0.5, np.sqrt(3.0) * 15e3)[None, :]
+    nm = NewmarkBeta(m, L, 2 * dt, pcg_tol=1e-13, algorithm="newton", maxit=3, cnvgtol=0.0, cnvgtest=4)
+    nm.Initialize()
+    hist = nm.run(1, 50, history=True)
+    nm.close()
+    ho, _ = O.newmark_run(m, L, 2 * dt, 50, algo=2, maxit=3, cnvgtol=0.0, solver=0)
+    assert np.abs(ho).max() > 0
+    assert rel_l2(hist, ho) <= 1e-9
+
+
+def test_central_difference_rejects_free_free_dashpot(gpu):
+    m, L, dt = q4_box(6, 4, nt=20)
+    m.dashpot_dof = np.array([[int(m.totaldof[20, 0]), int(m.totaldof[21, 0])]], np.int32)
+    m.dashpot_eta = np.array([1.0e5])
+    with pytest.raises(SvlError) as ei:
+        CentralDifference(m, L, dt)
+    assert ei.value.code == capi.SVL_ERR_UNSUPPORTED

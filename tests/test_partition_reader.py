@@ -19,7 +19,8 @@ def _part(case):
     return GOLD / ("partition_%s" % case) / "Partition" / "Fixture.1.0.json"
 
 
-@pytest.mark.parametrize("case", ["q4_cd", "h8_newmark_body", "q4_j2_column", "q4_newmark_rayleigh", "q4_pml_extended"])
+@pytest.mark.parametrize("case", ["q4_cd", "h8_newmark_body", "q4_j2_column", "q4_newmark_rayleigh", "q4_pml_extended",
+                                  "q4_lysmer_cd"])
 def test_numbering_and_connectivity_follow_the_file(case):
     p = load_partition(_part(case))
     d = json.loads(_part(case).read_text())
@@ -29,7 +30,8 @@ def test_numbering_and_connectivity_follow_the_file(case):
     for i, t in enumerate(tags):
         assert list(p.model.totaldof[i, :nnd[i]]) == d["Nodes"][str(t)]["totaldof"]
         assert list(p.model.freedof[i, :nnd[i]]) == d["Nodes"][str(t)]["freedof"]
-    for i, et in enumerate(sorted(int(t) for t in d["Elements"])):
+    solid = [t for t in sorted(int(x) for x in d["Elements"]) if d["Elements"][str(t)]["name"] != "ZEROLENGTH1D"]
+    for i, et in enumerate(solid):
         assert [tags[j] for j in p.model.conn[i]] == d["Elements"][str(et)]["conn"]
     assert p.model.ntotal == d["Global"]["ntotal"] and p.model.nfree == d["Global"]["nfree"]
 
@@ -114,6 +116,27 @@ def test_pml_layers_and_extended_newmark():
             assert list(m.pml_param[i]) == [a["n"], a["L"], a["R"]] + a["x0"] + a["npml"]
     h, U, V, A, Ub = O.xnewmark_run(m, p.loads, p.dt, p.nt - 1)
     assert np.all(np.isfinite(h)) and np.abs(h).max() > 0 and np.abs(Ub).max() > 0
+
+
+def test_zero_length_dashpots():
+    """ZeroLength1D + Viscous1DLinear elements become dashpots on the element's
+    direction (0-based in the file, Driver.hpp:1072-1078) between its two nodes."""
+    p = load_partition(_part("q4_lysmer_cd"))
+    d = json.loads(_part("q4_lysmer_cd").read_text())
+    tags = sorted(int(t) for t in d["Nodes"])
+    pos = {t: i for i, t in enumerate(tags)}
+    zl = [d["Elements"][str(t)] for t in sorted(int(x) for x in d["Elements"])
+          if d["Elements"][str(t)]["name"] == "ZEROLENGTH1D"]
+    assert len(zl) == p.model.dashpot_eta.size and p.model.nelem == len(d["Elements"]) - len(zl)
+    for e, (a, b), eta in zip(zl, p.model.dashpot_dof, p.model.dashpot_eta):
+        j = e["attributes"]["dir"]
+        n1, n2 = (pos[c] for c in e["conn"])
+        assert (a, b) == (p.model.totaldof[n1, j], p.model.totaldof[n2, j])
+        assert eta == d["Materials"][str(e["attributes"]["material"])]["attributes"]["eta"]
+    h, *_ = O.cd_run(p.model, p.loads, p.dt, p.nt - 1)
+    p.model.dashpot_dof = p.model.dashpot_eta = None
+    h0, *_ = O.cd_run(p.model, p.loads, p.dt, p.nt - 1)
+    assert np.all(np.isfinite(h)) and np.linalg.norm(h - h0) > 1e-6 * np.linalg.norm(h0)
 
 
 def test_integrator_names_are_the_run_process_ones(tmp_path):

@@ -128,3 +128,61 @@ def test_central_difference_rejects_stiffness_proportional_damping():
     m.rayleigh = np.tile([0.0, 1e-3], (m.nelem, 1))
     with pytest.raises(RuntimeError):
         O.cd_run(m, L, dt, 5)
+
+
+def _dashpot_matrix(m):
+    C = np.zeros((m.ntotal, m.ntotal))
+    for (a, b), e in zip(m.dashpot_dof, m.dashpot_eta):
+        C[a, a] += e; C[b, b] += e; C[a, b] -= e; C[b, a] -= e
+    return C
+
+
+def test_lysmer_dashpots_newmark_and_central_difference():
+    """ZeroLength1D dashpots (C_e = eta [1 -1; -1 1]) held to fixed anchors:
+    Newmark against the dense restatement, CD against its diagonal form."""
+    from tests.helpers import lysmer_box
+    m, L, dt = lysmer_box(10, 5, nt=200)
+    K, M, Cr, fr = _assemble(m, np.zeros((m.nelem, 2)))
+    C = _dashpot_matrix(m)
+    # Newmark
+    nt = m.ntotal
+    U, V, A = np.zeros(nt), np.zeros(nt), np.zeros(nt)
+    dtn = 4 * dt
+    Keff = (K + 4.0 / dtn ** 2 * M + 2.0 / dtn * C)[np.ix_(fr, fr)]
+    hd = np.zeros((60, nt))
+    for i in range(60):
+        F = _fext(L, nt, 1 + i) - K @ U + M @ (4.0 / dtn * V + A) + C @ V
+        du = np.zeros(nt)
+        du[fr] = np.linalg.solve(Keff, F[fr])
+        An = 4.0 / dtn ** 2 * du - 4.0 / dtn * V - A
+        V = 2.0 / dtn * du - V
+        A = An
+        U = U + du
+        hd[i] = U
+    h1, _ = O.newmark_run(m, L, dtn, 60)
+    assert rel_l2(h1, hd) <= 1e-9
+    m0 = dict(dashpot_dof=m.dashpot_dof, dashpot_eta=m.dashpot_eta)
+    m.dashpot_dof = m.dashpot_eta = None
+    h0, _ = O.newmark_run(m, L, dtn, 60)
+    assert rel_l2(h1, h0) > 1e-3
+    m.dashpot_dof, m.dashpot_eta = m0["dashpot_dof"], m0["dashpot_eta"]
+    # central difference: M/dt^2 + C/2dt is diagonal on the free dofs
+    Md = np.diag(M)
+    Cd = np.diag(C)
+    U, Up = np.zeros(nt), np.zeros(nt)
+    hc = np.zeros((200, nt))
+    for i in range(200):
+        R = _fext(L, nt, 1 + i) - K @ U + (Md / dt ** 2) * (U - Up) - C @ (U - Up) / (2 * dt)
+        du = np.zeros(nt)
+        du[fr] = R[fr] / (Md / dt ** 2 + Cd / (2 * dt))[fr]
+        Up = U
+        U = U + du
+        hc[i] = U
+    h2, *_ = O.cd_run(m, L, dt, 200)
+    assert np.abs(h2).max() > 0
+    assert rel_l2(h2, hc) <= 1e-10
+    # a dashpot between two free dofs makes the explicit solve non-diagonal
+    m.dashpot_dof = np.array([[int(m.totaldof[20, 0]), int(m.totaldof[21, 0])]], np.int32)
+    m.dashpot_eta = np.array([1.0e5])
+    with pytest.raises(RuntimeError):
+        O.cd_run(m, L, dt, 5)
