@@ -235,7 +235,7 @@ SVL.CreateRunAnalysisFiles()
     "q4_lysmer_cd": COMMON + r'''
 SVL.Options["dimension"] = 2
 SVL.Options["massform"] = "lumped"
-nx, ny, h, dt, nt = 4, 8, 0.5, 1.0e-4, 61
+nx, ny, h, dt, nt = 4, 8, 0.5, 2.0e-4, 301
 rho, E, nu = 2000.0, 2.0e8, 0.25
 G = E / 2.0 / (1 + nu); lam = E * nu / (1 + nu) / (1 - 2 * nu)
 vp, vs = math.sqrt((lam + 2 * G) / rho), math.sqrt(G / rho)
