@@ -1884,7 +1884,7 @@ int svl_nm_create(const svl_model_desc* model, const svl_load_desc* loads, const
                 }
             }
         }
-        const double ak = nm->damped ? m.ray[2 * (size_t)e + 1] : 0.0;
+        const double ak = m.ray.empty() ? 0.0 : m.ray[2 * (size_t)e + 1];
         for (int a = 0; a < m.nen; ++a)
             for (int c = 0; c < m.ndof; ++c) Kd[m.tdof[(size_t)m.conn[(size_t)e * m.nen + a] * m.ndof + c]] += (1.0 + c_c * ak) * kd[a * m.ndof + c];
     }
