@@ -37,6 +37,14 @@ from pathlib import Path
 import numpy as np
 
 ROOT = Path(__file__).resolve().parent
+
+# DRAM bytes (read + write) per free DOF of one k_cdx_step launch on the
+# lin3DHexa8 128x128x64 workload, from an ncu capture (dram__bytes_read.sum,
+# dram__bytes_write.sum) of the 2-instance case: 148.05 MB read + 20.07 MB
+# written per launch over 6 324 096 free DOF.  Part of the state written by one step is
+# still in L2 when the next step reads it, so this is below the 37 B/DOF of
+# algorithmic traffic.
+DRAM_BYTES_PER_DOF_STEP_MIXED_H8 = 26.585
 sys.path.insert(0, str(ROOT))
 
 ALGO_BYTES_PER_DOF = {2: 40.0, 3: 37.0}
@@ -383,12 +391,18 @@ def main():
             "data": "synthetic (seeded)",
             "config": {"workload": desc, "instances": nb, "free_dof_per_instance": m.nfree,
                        "elements_per_instance": m.nelem, "dt": dt,
-                       "precision": ("mixed: TF32 hi/lo tensor-core element forces, FP32 accumulate, FP64 update"
+                       "precision": ("mixed: TF32 hi/lo tensor-core element forces, FP32 accumulate, "
+                                     "compensated FP32-pair displacement state (~48 bits)"
                                      if args.precision == "mixed" else "fp64 plain"),
                        "parallelism": "replicas" if ws > 1 else "single GPU",
                        "l2": "no flush; working set ~%d MB > 129 MB L2" % ws_mb},
             "roofline": {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
+                         "frac": achieved / peak, "peak_source": peak_kind,
+                         "traffic": (DRAM_BYTES_PER_DOF_STEP_MIXED_H8 * nfree_total
+                                     if args.precision == "mixed" and args.workload == "config2" else None),
+                         "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum of k_cdx_step, "
+                                            "2-instance case (6.3 M DOF), scaled per free DOF to this launch"
+                                            if args.precision == "mixed" and args.workload == "config2" else None),
                          "algorithmic_bytes_per_step": algo_bytes, "kernel_share": shares},
             "fp64_plain": fp64, "implicit_pcg_time_to_1e-8": implicit,
             "cpu_baseline": cb, "e2e": e2e, "gpu_launches": int(launches), "clocks": clocks,
