@@ -137,6 +137,20 @@ typedef struct svl_load_desc {
     const int32_t* sm_dof;
     const int32_t* sm_series;
     const double*  sm_factor;
+    /* Domain-reduction loads (ELEMENTLOAD "GENERALWAVE", Driver.hpp:1669-1722;
+     * Assembler.cpp:460-478).  Every entry adds, at step k, factor times
+     * M~ A_o + C~ V_o + K~ U_o of its element (lin2DQuad4.cpp:564-614,
+     * lin3DHexa8.cpp:661-718): the element matrices with the blocks between two
+     * boundary dofs and between two exterior dofs set to zero, and U_o, V_o, A_o
+     * the free-field motion of the element's nodes at row k, negated at
+     * exterior nodes as the run-process does when it reads the files.        */
+    int32_t ndrm;
+    const int32_t* drm_elem;        /* [ndrm] element positions, in load-list order        */
+    const double*  drm_factor;      /* [ndrm] combination factor of the entry's load       */
+    int32_t drm_nt;                 /* rows of every node's motion                         */
+    const int32_t* drm_node_row;    /* [nnode] block of the node in drm_motion, -1 if none */
+    const int32_t* drm_node_ext;    /* [nnode] 1 exterior node, 0 boundary node            */
+    const double*  drm_motion;      /* [blocks][drm_nt][3 ndim] u[ndim] v[ndim] a[ndim]   */
 } svl_load_desc;
 
 /* ---- page-locked host memory ---------------------------------------------- */

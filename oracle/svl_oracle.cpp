@@ -69,6 +69,11 @@ struct Loads {
     std::vector<int> sptr; std::vector<double> sval;
     std::vector<int> fdof, fser; std::vector<double> fcoef;
     std::vector<int> smdof, smser; std::vector<double> smfac;
+    // domain reduction: entries (element, factor), node rows into the motion, exterior flags
+    std::vector<int> drm_elem; std::vector<double> drm_factor;
+    int drm_nt = 0;
+    std::vector<int> drm_row, drm_ext;
+    std::vector<double> drm_motion;
     double series(int s, int k) const {            // Load::GetLoadVector (Load.cpp:69-71)
         int n = sptr[s + 1] - sptr[s];
         return (k >= 0 && k < n) ? sval[sptr[s] + k] : 0.0;
@@ -139,9 +144,19 @@ bool load_model(const svl_model_desc* d, Model& m) {
     return true;
 }
 
-void load_loads(const svl_load_desc* l, Loads& L) {
+void load_loads(const svl_load_desc* l, Loads& L, int nnode, int ndim) {
     L.sptr.assign(1, 0);
     if (!l) return;
+    if (l->ndrm > 0) {
+        L.drm_elem.assign(l->drm_elem, l->drm_elem + l->ndrm);
+        L.drm_factor.assign(l->drm_factor, l->drm_factor + l->ndrm);
+        L.drm_nt = l->drm_nt;
+        L.drm_row.assign(l->drm_node_row, l->drm_node_row + nnode);
+        L.drm_ext.assign(l->drm_node_ext, l->drm_node_ext + nnode);
+        int nb = 0;
+        for (int r : L.drm_row) nb = std::max(nb, r + 1);
+        L.drm_motion.assign(l->drm_motion, l->drm_motion + (size_t)nb * l->drm_nt * 3 * ndim);
+    }
     if (l->nseries > 0) {
         L.sptr.assign(l->series_ptr, l->series_ptr + l->nseries + 1);
         L.sval.assign(l->series_val, l->series_val + L.sptr.back());
@@ -462,7 +477,7 @@ struct Sim {
 
     bool init(const svl_model_desc* d, const svl_load_desc* l) {
         if (!load_model(d, m)) return false;
-        load_loads(l, L);
+        load_loads(l, L, m.nnode, m.ndim);
         const int nc = m.nen * m.ndof;
         edofs.resize((size_t)m.nelem * nc);
         for (int e = 0; e < m.nelem; ++e)
@@ -678,6 +693,51 @@ struct Sim {
     void fext(int k, std::vector<double>& F) const {
         F.assign(m.ntotal, 0.0);
         for (size_t i = 0; i < L.fdof.size(); ++i) F[L.fdof[i]] += L.fcoef[i] * L.series(L.fser[i], k);
+        if (!L.drm_elem.empty()) drm_forces(k, F);
+    }
+    // lin2DQuad4::ComputeDomainReductionForces (lin2DQuad4.cpp:564-614,
+    // lin3DHexa8.cpp:661-718): M~ Ao + C~ Vo + K~ Uo with the entries between
+    // two dofs of equal boundary/exterior condition set to zero; motion rows past
+    // the end of the signals read as zero (the reference reads them unchecked).
+    void drm_forces(int k, std::vector<double>& F) const {
+        const int nc = m.nen * m.ndof, nd = m.ndim;
+        std::vector<double> Me((size_t)nc * nc), Ce((size_t)nc * nc, 0.0), Ke((size_t)nc * nc), K0((size_t)nc * nc);
+        std::vector<double> Uo(nc), Vo(nc), Ao(nc), fe(nc);
+        std::vector<int> cond(nc);
+        for (size_t i = 0; i < L.drm_elem.size(); ++i) {
+            const int e = L.drm_elem[i];
+            for (int a = 0; a < m.nen; ++a) {
+                const int n = m.conn[(size_t)e * m.nen + a];
+                const int r = L.drm_row[n];
+                const double sg = L.drm_ext[n] ? -1.0 : 1.0;
+                for (int c = 0; c < nd; ++c) {
+                    double u = 0, v = 0, acc = 0;
+                    if (r >= 0 && k >= 0 && k < L.drm_nt) {
+                        const double* row = &L.drm_motion[((size_t)r * L.drm_nt + k) * 3 * nd];
+                        u = row[c]; v = row[nd + c]; acc = row[2 * nd + c];
+                    }
+                    Uo[a * nd + c] = sg * u; Vo[a * nd + c] = sg * v; Ao[a * nd + c] = sg * acc;
+                    cond[a * nd + c] = L.drm_ext[n];
+                }
+            }
+            element_M(e, Me.data(), m.lumped != 0);
+            element_K(e, Ke.data());
+            std::fill(Ce.begin(), Ce.end(), 0.0);
+            if (!m.ray.empty()) {
+                element_K0(e, K0.data());
+                for (int j = 0; j < nc * nc; ++j) Ce[j] = m.ray[2 * e] * Me[j] + m.ray[2 * e + 1] * K0[j];
+            }
+            for (int r = 0; r < nc; ++r) {
+                double v = 0.0;
+                for (int c = 0; c < nc; ++c) {
+                    if (cond[r] == cond[c]) continue;
+                    const size_t ij = (size_t)r * nc + c;
+                    v += Me[ij] * Ao[c] + Ce[ij] * Vo[c] + Ke[ij] * Uo[c];
+                }
+                fe[r] = v;
+            }
+            for (int r = 0; r < nc; ++r) F[edofs[(size_t)e * nc + r]] += L.drm_factor[i] * fe[r];
+        }
     }
     // Assembler::ComputeSupportMotionIncrement (Assembler.cpp:493-532).
     void support_increment(int k, std::vector<double>& SM) const {

@@ -66,6 +66,8 @@ class LoadDesc(C.Structure):
         ("nseries", C.c_int32), ("series_ptr", i32p), ("series_val", f64p),
         ("nforce", C.c_int32), ("force_dof", i32p), ("force_series", i32p), ("force_coef", f64p),
         ("nsupport", C.c_int32), ("sm_dof", i32p), ("sm_series", i32p), ("sm_factor", f64p),
+        ("ndrm", C.c_int32), ("drm_elem", i32p), ("drm_factor", f64p), ("drm_nt", C.c_int32),
+        ("drm_node_row", i32p), ("drm_node_ext", i32p), ("drm_motion", f64p),
     ]
 
 

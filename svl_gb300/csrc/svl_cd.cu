@@ -79,6 +79,15 @@ struct DevView {
     const double* dk0;       // [3][E]   ak_e * (c1, c2, c3) of the initial elastic tangent, or null
     // Lysmer dashpots on the implicit path: y_t += c sum eta (x_t - x_partner)
     const int32_t* dp_ptr; const int32_t* dp_col; const double* dp_eta;
+    // domain-reduction entries: element, factor, ak of its Rayleigh damping;
+    // node rows into the free-field motion, exterior flags; element force
+    // blocks and their per-dof gather (entry order)
+    int ndrm, drm_nt;
+    const int32_t* drm_elem; const double* drm_factor; const double* drm_ak;
+    const int32_t* drm_node_of;              // [ndrm][nen] node positions of each entry's element
+    const int32_t* drm_row; const int32_t* drm_ext; const double* drm_motion;
+    double* drm_fe;
+    const int32_t* drm_ptr; const int32_t* drm_idx;
     double *U, *V, *A, *Up, *Us, *R, *du;
     // T and T^T as CSR (constraint path)
     const int32_t *T_ptr, *T_col; const double* T_val;
@@ -104,6 +113,8 @@ __device__ __forceinline__ double support_at(const DevView& d, int s, int k) {
 __device__ __forceinline__ double fext_at(const DevView& d, int t, int k) {
     double f = 0.0;
     for (int i = d.ld_ptr[t]; i < d.ld_ptr[t + 1]; ++i) f += d.ld_coef[i] * series_at(d, d.ld_ser[i], k);
+    if (d.drm_ptr)
+        for (int i = d.drm_ptr[t]; i < d.drm_ptr[t + 1]; ++i) f += d.drm_fe[d.drm_idx[i]];
     return f;
 }
 __device__ __forceinline__ double sm_at(const DevView& d, int t, int k) {
@@ -383,6 +394,100 @@ __global__ void __launch_bounds__(128) k_element_tan(DevView d, const double* __
     }
 #pragma unroll
     for (int j = 0; j < NC; ++j) d.fe[(size_t)j * E + e] = fe[j];
+}
+
+// Domain-reduction forces of step d.step[0] (lin2DQuad4.cpp:564-614,
+// lin3DHexa8.cpp:661-718) for elastic elements with a lumped mass: the
+// lumped mass is diagonal, so M~ (equal-condition blocks zeroed) vanishes and
+// C~ = ak K~; each entry computes factor * K~ (U_o + ak V_o) as
+// K (w on exterior nodes) on the boundary rows and K (w on boundary nodes) on
+// the exterior rows.  Rows past the end of the signals read as zero.
+template <int ND, int NEN>
+__global__ void __launch_bounds__(128) k_drm(DevView d, int ngp) {
+    constexpr int NC = ND * NEN, PER = NEN * ND + 1;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.ndrm) return;
+    const int E = d.nelem, e = d.drm_elem[i], k = d.step[0];
+    const double ak = d.drm_ak[i];
+    double wb[NC], we[NC], yb[NC], ye[NC];
+    int ext[NEN];
+#pragma unroll
+    for (int j = 0; j < NC; ++j) {
+        const int a = j / ND, c = j % ND;
+        const int node = d.drm_node_of[(size_t)i * NEN + a];
+        const int r = d.drm_row[node];
+        const bool x = d.drm_ext[node] != 0;
+        ext[a] = x;
+        double u = 0.0, v = 0.0;
+        if (k >= 0 && k < d.drm_nt) {
+            const double* row = d.drm_motion + ((size_t)r * d.drm_nt + k) * (3 * ND);
+            u = row[c];
+            v = row[ND + c];
+        }
+        const double w = (x ? -1.0 : 1.0) * (u + ak * v);
+        wb[j] = x ? 0.0 : w;
+        we[j] = x ? w : 0.0;
+        yb[j] = 0.0; ye[j] = 0.0;
+    }
+    const double c1 = d.ecoef[e], c2 = d.ecoef[(size_t)E + e], c3 = d.ecoef[2 * (size_t)E + e];
+    const double* g0 = d.geo + (size_t)d.egeo[e] * ngp * PER;
+    for (int q = 0; q < ngp; ++q) {
+        const double* g = g0 + q * PER;
+        double b[NEN][3];
+#pragma unroll
+        for (int a = 0; a < NEN; ++a)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) b[a][j] = (j < ND) ? __ldg(g + a * ND + j) : 0.0;
+        const double w = __ldg(g + PER - 1);
+#pragma unroll
+        for (int pass = 0; pass < 2; ++pass) {
+            const double* uu = pass == 0 ? wb : we;
+            double* yy = pass == 0 ? yb : ye;
+            if (ND == 2) {
+                double exx = 0, eyy = 0, gxy = 0;
+#pragma unroll
+                for (int a = 0; a < NEN; ++a) {
+                    exx += b[a][0] * uu[2 * a];
+                    eyy += b[a][1] * uu[2 * a + 1];
+                    gxy += b[a][1] * uu[2 * a] + b[a][0] * uu[2 * a + 1];
+                }
+                const double s0 = c1 * exx + c2 * eyy, s1 = c2 * exx + c1 * eyy, s2 = c3 * gxy;
+#pragma unroll
+                for (int a = 0; a < NEN; ++a) {
+                    yy[2 * a] += w * (b[a][0] * s0 + b[a][1] * s2);
+                    yy[2 * a + 1] += w * (b[a][1] * s1 + b[a][0] * s2);
+                }
+            } else {
+                double ev[6] = {0, 0, 0, 0, 0, 0};
+#pragma unroll
+                for (int a = 0; a < NEN; ++a) {
+                    const double ux = uu[3 * a], uy = uu[3 * a + 1], uz = uu[3 * a + 2];
+                    ev[0] += b[a][0] * ux;
+                    ev[1] += b[a][1] * uy;
+                    ev[2] += b[a][2] * uz;
+                    ev[3] += b[a][1] * ux + b[a][0] * uy;
+                    ev[4] += b[a][2] * uy + b[a][1] * uz;
+                    ev[5] += b[a][2] * ux + b[a][0] * uz;
+                }
+                double sg[6];
+                sg[0] = c1 * ev[0] + c2 * ev[1] + c2 * ev[2];
+                sg[1] = c2 * ev[0] + c1 * ev[1] + c2 * ev[2];
+                sg[2] = c2 * ev[0] + c2 * ev[1] + c1 * ev[2];
+                sg[3] = c3 * ev[3]; sg[4] = c3 * ev[4]; sg[5] = c3 * ev[5];
+#pragma unroll
+                for (int a = 0; a < NEN; ++a) {
+                    const double bx = b[a][0], by = b[a][1], bz = b[a][2];
+                    yy[3 * a] += w * (bx * sg[0] + by * sg[3] + bz * sg[5]);
+                    yy[3 * a + 1] += w * (by * sg[1] + bx * sg[3] + bz * sg[4]);
+                    yy[3 * a + 2] += w * (bz * sg[2] + by * sg[4] + bx * sg[5]);
+                }
+            }
+        }
+    }
+    const double fac = d.drm_factor[i];
+    double* out = d.drm_fe + (size_t)i * NC;
+#pragma unroll
+    for (int j = 0; j < NC; ++j) out[j] = fac * (ext[j / ND] ? yb[j] : ye[j]);
 }
 
 template <int ND>
@@ -707,6 +812,45 @@ static int cd_setup(svl_cd* cd, const svl_load_desc* L) {
     const std::vector<double>& ld_coef = lt.ld_coef;
     const std::vector<int32_t>& sm_ptr = lt.sm_ptr; const std::vector<int32_t>& sm_ser = lt.sm_ser;
     const std::vector<double>& sm_fac = lt.sm_fac;
+    // --- domain-reduction entries ----------------------------------------------
+    std::vector<int32_t> drm_elem, drm_node_of, drm_row, drm_ext, drm_ptr, drm_idx;
+    std::vector<double> drm_factor, drm_ak, drm_motion;
+    int drm_nt = 0;
+    if (L && L->ndrm > 0) {
+        if (!L->drm_elem || !L->drm_factor || !L->drm_node_row || !L->drm_node_ext || !L->drm_motion || L->drm_nt <= 0) {
+            set_error("domain-reduction arrays are NULL or drm_nt <= 0"); return SVL_ERR_INVALID;
+        }
+        drm_nt = L->drm_nt;
+        drm_row.assign(L->drm_node_row, L->drm_node_row + m.nnode);
+        drm_ext.assign(L->drm_node_ext, L->drm_node_ext + m.nnode);
+        int nblk = 0;
+        for (int r : drm_row) nblk = std::max(nblk, r + 1);
+        drm_motion.assign(L->drm_motion, L->drm_motion + (size_t)nblk * drm_nt * 3 * nd);
+        drm_ptr.assign(m.ntotal + 1, 0);
+        for (int i = 0; i < L->ndrm; ++i) {
+            const int e = L->drm_elem[i];
+            if (e < 0 || e >= E) { set_error("DRM entry %d: element %d out of range", i, e); return SVL_ERR_INVALID; }
+            if (ekind[e] != kMatElastic) { set_error("DRM element %d: elastic materials only", e); return SVL_ERR_UNSUPPORTED; }
+            drm_elem.push_back(e);
+            drm_factor.push_back(L->drm_factor[i]);
+            drm_ak.push_back(m.ray.empty() ? 0.0 : m.ray[2 * (size_t)e + 1]);
+            for (int a = 0; a < nen; ++a) {
+                const int n = m.conn[(size_t)e * nen + a];
+                if (drm_row[n] < 0) { set_error("DRM element %d: node %d has no free-field motion", e, n); return SVL_ERR_INVALID; }
+                drm_node_of.push_back(n);
+                for (int c = 0; c < nd; ++c) drm_ptr[m.tdof[(size_t)n * nd + c] + 1]++;
+            }
+        }
+        for (int t = 0; t < m.ntotal; ++t) drm_ptr[t + 1] += drm_ptr[t];
+        drm_idx.resize(drm_ptr.back());
+        std::vector<int32_t> fill(drm_ptr.begin(), drm_ptr.end() - 1);
+        for (int i = 0; i < L->ndrm; ++i) {
+            const int e = drm_elem[i];
+            for (int a = 0; a < nen; ++a)
+                for (int c = 0; c < nd; ++c)
+                    drm_idx[fill[m.tdof[(size_t)m.conn[(size_t)e * nen + a] * nd + c]]++] = i * nc + a * nd + c;
+        }
+    }
     // --- device upload -------------------------------------------------------
     DevView& d = cd->d;
     d.nelem = E; d.nnode = m.nnode; d.ntotal = m.ntotal; d.nfree = m.nfree;
@@ -727,6 +871,16 @@ static int cd_setup(svl_cd* cd, const svl_load_desc* L) {
     if (!Cdm.empty()) TRY(cd->upload(Cdm, &d.Cd));
     if (!dp_eta.empty()) {
         TRY(cd->upload(dp_ptr, &d.dp_ptr)); TRY(cd->upload(dp_col, &d.dp_col)); TRY(cd->upload(dp_eta, &d.dp_eta));
+    }
+    if (!drm_elem.empty()) {
+        d.ndrm = (int)drm_elem.size();
+        d.drm_nt = drm_nt;
+        TRY(cd->upload(drm_elem, &d.drm_elem)); TRY(cd->upload(drm_factor, &d.drm_factor));
+        TRY(cd->upload(drm_ak, &d.drm_ak)); TRY(cd->upload(drm_node_of, &d.drm_node_of));
+        TRY(cd->upload(drm_row, &d.drm_row)); TRY(cd->upload(drm_ext, &d.drm_ext));
+        TRY(cd->upload(drm_motion, &d.drm_motion));
+        TRY(cd->upload(drm_ptr, &d.drm_ptr)); TRY(cd->upload(drm_idx, &d.drm_idx));
+        TRY(cd->zeros((size_t)d.ndrm * nc, &d.drm_fe));
     }
     if (!dk0.empty()) TRY(cd->upload(dk0, &d.dk0));
     TRY(cd->zeros(m.ntotal, &d.U)); TRY(cd->zeros(m.ntotal, &d.V)); TRY(cd->zeros(m.ntotal, &d.A));
@@ -759,6 +913,12 @@ static int cd_launch_kind(svl_cd* cd, int kind) {
         // support-motion increment) feeds the material update.
         if (m.ndim == 2) k_element<2, 4><<<eg, eb, 0, cd->stream>>>(d, d.Us, m.ngp, 1);
         else k_element<3, 8><<<eg, eb, 0, cd->stream>>>(d, d.Us, m.ngp, 1);
+        if (d.ndrm > 0) {                   // domain-reduction forces of this step
+            const int gd = (d.ndrm + 127) / 128;
+            if (m.ndim == 2) k_drm<2, 4><<<gd, 128, 0, cd->stream>>>(d, m.ngp);
+            else k_drm<3, 8><<<gd, 128, 0, cd->stream>>>(d, m.ngp);
+            ++cd->launches;
+        }
         break;
     case 1:
         if (!cd->identity_T) return 1;
@@ -1990,6 +2150,18 @@ int svl_nm_set_initial(svl_nm* nm, const double* U0, const double* V0, const dou
 
 }  // extern "C"
 
+// domain-reduction forces of the step just begun (d.step already advanced)
+static int nm_drm(svl_nm* nm) {
+    svl_cd* cd = nm->cd;
+    if (cd->d.ndrm <= 0) return SVL_OK;
+    const int gd = (cd->d.ndrm + 127) / 128;
+    if (cd->m.ndim == 2) k_drm<2, 4><<<gd, 128, 0, cd->stream>>>(cd->d, cd->m.ngp);
+    else k_drm<3, 8><<<gd, 128, 0, cd->stream>>>(cd->d, cd->m.ngp);
+    cd->launches += 1;
+    CUDA_TRY(cudaGetLastError());
+    return SVL_OK;
+}
+
 static int nmg_rhs(svl_nm* nm);
 
 // Effective force of step k into nm->b (state untouched).
@@ -2001,6 +2173,7 @@ static int nm_rhs(svl_nm* nm, int k) {
     const int km1 = k - 1;
     CUDA_TRY(cudaMemcpyAsync(cd->d.step, &km1, sizeof(int), cudaMemcpyHostToDevice, cd->stream));
     k_step_inc<<<1, 1, 0, cd->stream>>>(cd->d.step);
+    TRY(nm_drm(nm));
     if (m.ndim == 2) k_element<2, 4><<<eg, 128, 0, cd->stream>>>(cd->d, cd->d.Us, m.ngp, 0);
     else k_element<3, 8><<<eg, 128, 0, cd->stream>>>(cd->d, cd->d.Us, m.ngp, 0);
     if (nm->general) {
@@ -2093,6 +2266,7 @@ static int nmg_step_linear(svl_nm* nm, double* U_hist_row) {
     const double dt = nm->opts.dt;
     const int tb = 256, ng = (m.nnode + tb - 1) / tb, eg = (m.nelem + 127) / 128, gt = (m.ntotal + tb - 1) / tb;
     k_step_inc<<<1, 1, 0, cd->stream>>>(cd->d.step);
+    TRY(nm_drm(nm));
     if (m.ndim == 2) k_element<2, 4><<<eg, 128, 0, cd->stream>>>(cd->d, cd->d.Us, m.ngp, 0);
     else k_element<3, 8><<<eg, 128, 0, cd->stream>>>(cd->d, cd->d.Us, m.ngp, 0);
     k_nmg_sm<<<gt, tb, 0, cd->stream>>>(cd->d, nm->smv);
@@ -2121,6 +2295,7 @@ static int nm_step_newton(svl_nm* nm, double* U_hist_row) {
     const int gf = (n + tb - 1) / tb, gt = (m.ntotal + tb - 1) / tb;
     double hs[S_NSCAL];
     k_step_inc<<<1, 1, 0, cd->stream>>>(cd->d.step);
+    TRY(nm_drm(nm));
     CUDA_TRY(cudaMemsetAsync(nm->dUf, 0, sizeof(double) * std::max(n, 1), cd->stream));
     if (nm->general) {
         k_nmg_sm<<<gt, tb, 0, cd->stream>>>(cd->d, nm->smv);
@@ -2191,6 +2366,7 @@ static int nm_step(svl_nm* nm, double* U_hist_row) {
     const double dt = nm->opts.dt;
     const int tb = 256, ng = (m.nnode + tb - 1) / tb, eg = (m.nelem + 127) / 128;
     k_step_inc<<<1, 1, 0, cd->stream>>>(cd->d.step);
+    TRY(nm_drm(nm));
     // internal force from the committed state (filtered like the assembler)
     if (m.ndim == 2) k_element<2, 4><<<eg, 128, 0, cd->stream>>>(cd->d, cd->d.Us, m.ngp, 0);
     else k_element<3, 8><<<eg, 128, 0, cd->stream>>>(cd->d, cd->d.Us, m.ngp, 0);

@@ -820,6 +820,7 @@ int svl_cdx_create(const svl_grid_spec* g, int32_t ninst, const svl_model_desc* 
         }
         if (loads) {
             const svl_load_desc& L = loads[b];
+            if (L.ndrm > 0) { set_error("instance %d: domain-reduction loads are served by svl_cd_create", b); return fail(SVL_ERR_UNSUPPORTED); }
             if (L.nsupport > 0) { set_error("instance %d: support motion is not supported on the structured path", b); return fail(SVL_ERR_UNSUPPORTED); }
             const int soff = (int)s_ptr.size() - 1;
             for (int sidx = 0; sidx < L.nseries; ++sidx) {

@@ -704,6 +704,7 @@ int x_setup(svl_xnm* X, const svl_load_desc* L) {
         for (int t = 0; t < m.ntotal; ++t)
             for (int i = Tp[t]; i < Tp[t + 1]; ++i) { const int p = fill[Tc[i]]++; TTr[p] = t; TTv[p] = Tv[i]; }
     }
+    if (L && L->ndrm > 0) { set_error("domain-reduction loads are served by svl_cd_create / svl_nm_create"); return SVL_ERR_UNSUPPORTED; }
     XTRY(build_load_tables(m, L, X->lt));
     // uploads
     XTRY(X->upload(s_edof, &X->s_edof)); XTRY(X->upload(s_egeo, &X->s_egeo)); XTRY(X->upload(s_geo, &X->s_geo));

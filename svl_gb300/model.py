@@ -244,7 +244,25 @@ class Loads:
     sm_dof: List[int] = field(default_factory=list)
     sm_series: List[int] = field(default_factory=list)
     sm_factor: List[float] = field(default_factory=list)
+    # domain-reduction (DRM) entries: element positions with their load factor,
+    # and per node the free-field motion [nt, 3 ndim] (u, v, a) and the exterior flag
+    drm_elem: List[int] = field(default_factory=list)
+    drm_factor: List[float] = field(default_factory=list)
+    drm_motion: dict = field(default_factory=dict)      # node position -> (ndarray [nt, 3 ndim], exterior flag)
+    _nnode: int = field(default=0, repr=False)
     _keep: list = field(default_factory=list, repr=False)
+
+    def add_drm(self, model: Model, elems: Sequence[int], motion: dict, factor: float = 1.0):
+        """ELEMENTLOAD "GENERALWAVE": the elements of the DRM layer and, for every
+        node of theirs, (free-field motion [nt, 3 ndim] as in the node file,
+        exterior flag).  Exterior motions are negated inside, as the
+        run-process does when it reads the files (Driver.hpp:1700-1719)."""
+        self._nnode = model.nnode
+        for e in elems:
+            self.drm_elem.append(int(e))
+            self.drm_factor.append(float(factor))
+        for n, (sig, ext) in motion.items():
+            self.drm_motion[int(n)] = (np.ascontiguousarray(sig, dtype=np.float64), 1 if ext else 0)
 
     def add_series(self, values) -> int:
         self.series.append(as_f64(values))
@@ -313,6 +331,29 @@ class Loads:
         d.sm_dof = ptr(arrs[5], C.c_int32)
         d.sm_series = ptr(arrs[6], C.c_int32)
         d.sm_factor = ptr(arrs[7], C.c_double)
+        d.ndrm = len(self.drm_elem)
+        if self.drm_elem:
+            nnode = self._nnode
+            rows = -np.ones(nnode, np.int32)
+            ext = np.zeros(nnode, np.int32)
+            nts = {sig.shape[0] for sig, _ in self.drm_motion.values()}
+            if len(nts) != 1:
+                raise ValueError("every DRM node needs the same number of rows")
+            nt = nts.pop()
+            blocks = []
+            for i, n in enumerate(sorted(self.drm_motion)):
+                sig, e = self.drm_motion[n]
+                rows[n] = i
+                ext[n] = e
+                blocks.append(sig)
+            extra = [as_i32(self.drm_elem), as_f64(self.drm_factor), rows, ext, as_f64(np.concatenate(blocks, axis=0))]
+            self._keep += extra
+            d.drm_elem = ptr(extra[0], C.c_int32)
+            d.drm_factor = ptr(extra[1], C.c_double)
+            d.drm_nt = int(nt)
+            d.drm_node_row = ptr(extra[2], C.c_int32)
+            d.drm_node_ext = ptr(extra[3], C.c_int32)
+            d.drm_motion = ptr(extra[4], C.c_double)
         return d
 
 

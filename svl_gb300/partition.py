@@ -14,7 +14,8 @@ Covered: lin2DQuad4 / lin3DHexa8 elements with PML2DQuad4 / PML3DHexa8
 layers (5 / 9 dofs at their nodes); Elastic2DPlaneStrain, Elastic3DLinear,
 PlasticPlaneStrainJ2, Plastic3DJ2 materials; restraints; EQUAL-type
 constraints; nodal masses; Rayleigh dampings; ZeroLength1D elements with a
-Viscous1DLinear material (Lysmer dashpots); point loads and element body
+Viscous1DLinear material (Lysmer dashpots); domain-reduction (DRM) element
+loads with per-node free-field files; point loads and element body
 loads (constant or time series); support motions (constant or time series);
 node recorders of displacement, velocity or acceleration; the integrators
 CentralDifference, Newmark and ExtendedNewmark under the names the run-process
@@ -55,6 +56,29 @@ def read_series(path: Path) -> np.ndarray:
     if vals.size != n:
         raise PartitionError("%s: expected %d values, found %d" % (path, n, vals.size))
     return vals
+
+
+def read_drm_motion(root: Path, pattern: str, elems: list, npos: dict, ndim: int) -> dict:
+    """Free-field motion of every node of the DRM elements: the file named by
+    `pattern` with "$" replaced by the node tag holds `nt nFields cond` and
+    then nt rows of u, v, a per direction; cond 1 marks an exterior node
+    (Driver.hpp:1689-1719)."""
+    out = {}
+    for e in elems:
+        for ntag in e["conn"]:
+            ntag = int(ntag)
+            if npos[ntag] in out:
+                continue
+            path = Path(pattern.replace("$", str(ntag)))
+            if not path.is_absolute():
+                path = root / path
+            tok = path.read_text().split()
+            nt, nf, cond = int(float(tok[0])), int(float(tok[1])), int(float(tok[2]))
+            if nf != 3 * ndim:
+                raise PartitionError("%s: %d fields per row, %d expected (u, v, a)" % (path, nf, 3 * ndim))
+            vals = np.array([float(x) for x in tok[3:3 + nt * nf]]).reshape(nt, nf)
+            out[npos[ntag]] = (vals, bool(cond))
+    return out
 
 
 @dataclass
@@ -293,6 +317,11 @@ def load_partition(path, run_dir=None) -> Partition:
         ld = d["Loads"][str(ltag)]
         la = ld["attributes"]
         kind, fun = la["type"].upper(), la["name"].upper()
+        if ld["name"].upper() == "ELEMENTLOAD" and kind == "GENERALWAVE":
+            loads.add_drm(model, [epos[int(e)] for e in la["list"]],
+                          read_drm_motion(root, la["file"], [e for e in (d["Elements"][str(t)] for t in la["list"])],
+                                          npos, ndim), factor=float(fac))
+            continue
         if fun == "TIMESERIES":
             series = read_series(root / la["file"])
         elif fun == "CONSTANT":

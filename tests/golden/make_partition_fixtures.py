@@ -3,8 +3,8 @@ running the SeismoVLAB pre-processor itself (PP/Core/SeismoVLAB.py
 CreateRunAnalysisFiles) on small models that exercise every field the
 partition reader maps: materials (elastic and J2), restraints, EQUAL
 constraints, point and element body loads (constant and time series),
-support motions, Rayleigh dampings, PML layers, Lysmer dashpots, node
-recorders, the integrator/solver settings.
+support motions, Rayleigh dampings, PML layers, Lysmer dashpots,
+domain-reduction loads, node recorders, the integrator/solver settings.
 
 Run from the repository root where the reference tree is available:
     python tests/golden/make_partition_fixtures.py /path/to/SVL
@@ -274,6 +274,65 @@ SVL.addSolver(tag=1, attributes={"name": "Eigen", "update": "OFF"})
 SVL.addSimulation(tag=1, combo=1, attributes={"analysis": 1, "algorithm": 1, "integrator": 1, "solver": 1})
 SVL.CreateRunAnalysisFiles()
 ''',
+    # Q4 box with a one-element domain-reduction ring; free-field motion of an
+    # SV pulse in per-node files (nt nFields cond), Newmark + Eigen
+    "q4_drm_newmark": COMMON + r'''
+import os
+SVL.Options["dimension"] = 2
+SVL.Options["massform"] = "lumped"
+nx, ny, h, dt, nt = 8, 6, 1.0, 1.0e-3, 41
+rho, E, nu = 2000.0, 2.0e8, 0.25
+G = E / 2.0 / (1 + nu)
+vs = math.sqrt(G / rho)
+SVL.addMaterial(tag=1, name="Elastic2DPlaneStrain", attributes={"E": E, "nu": nu, "rho": rho})
+mesh = SVL.makeDomainArea(options={"ne": [nx, ny], "ndof": 2, "class": "LIN2DQUAD4", "elems": "QUAD4",
+    "P0": [0.0, 0.0], "P1": [nx * h, 0.0], "P2": [0.0, ny * h],
+    "attributes": {"material": 1, "th": 1.0, "rule": "Gauss", "np": 4}})
+for tag in sorted(mesh["Nodes"]):
+    n = mesh["Nodes"][tag]
+    SVL.addNode(tag=tag, ndof=n["ndof"], coords=list(map(float, n["coords"])))
+for tag in sorted(mesh["Elements"]):
+    el = mesh["Elements"][tag]
+    SVL.addElement(tag=tag, conn=list(el["conn"]), name=el["name"], attributes=dict(el["attributes"]))
+for tag in sorted(mesh["Nodes"]):
+    x, y = mesh["Nodes"][tag]["coords"][:2]
+    if abs(y) < 1e-9:
+        SVL.addRestrain(tag=tag, dof=[1, 2])
+    elif abs(x) < 1e-9 or abs(x - nx * h) < 1e-9:
+        SVL.addRestrain(tag=tag, dof=1)
+inner = lambda p: p[0] >= h - 1e-9 and p[0] <= (nx - 1) * h + 1e-9 and p[1] >= h - 1e-9
+drm = []
+for tag in sorted(mesh["Elements"]):
+    ins = [inner(mesh["Nodes"][n]["coords"]) for n in mesh["Elements"][tag]["conn"]]
+    if any(ins) and not all(ins):
+        drm.append(tag)
+nodes = sorted({n for e in drm for n in mesh["Elements"][e]["conn"]})
+os.makedirs("drm", exist_ok=True)
+for n in nodes:
+    x, y = mesh["Nodes"][n]["coords"][:2]
+    rows = []
+    for k in range(nt):
+        def g(tau):
+            a = (math.pi * 20.0 * (tau - 0.06)) ** 2
+            return 1e-3 * (1 - 2 * a) * math.exp(-a)
+        t = k * dt - (ny * h - y) / vs
+        u = g(t); v = (g(t + dt) - g(t - dt)) / (2 * dt); a = (g(t + dt) - 2 * g(t) + g(t - dt)) / dt ** 2
+        rows.append("%.17g 0 %.17g 0 %.17g 0" % (u, v, a))
+    with open("drm/node%d.txt" % n, "w") as f:
+        f.write("%d 6 %d\n" % (nt, 0 if inner(mesh["Nodes"][n]["coords"]) else 1))
+        f.write("\n".join(rows) + "\n")
+SVL.addFunction(tag=1, name="TimeSeries", attributes={"file": "drm/node$.txt"})
+SVL.addLoad(tag=1, name="ElementLoad", attributes={"type": "GeneralWave", "fun": 1, "list": drm})
+SVL.addCombinationCase(tag=1, name="Fixture", attributes={"load": [1], "factor": [1.0]})
+top = [t for t in sorted(mesh["Nodes"]) if abs(mesh["Nodes"][t]["coords"][1] - ny * h) < 1e-9]
+SVL.addRecorder(tag=1, attributes={"name": "NODE", "file": "Top.out", "ndps": 8, "resp": "disp", "list": top[:3]})
+SVL.addAnalysis(tag=1, attributes={"name": "Dynamic", "nt": nt})
+SVL.addAlgorithm(tag=1, attributes={"name": "Linear", "nstep": 1})
+SVL.addIntegrator(tag=1, attributes={"name": "Newmark", "dt": dt})
+SVL.addSolver(tag=1, attributes={"name": "Eigen", "update": "OFF"})
+SVL.addSimulation(tag=1, combo=1, attributes={"analysis": 1, "algorithm": 1, "integrator": 1, "solver": 1})
+SVL.CreateRunAnalysisFiles()
+''',
 }
 
 
@@ -303,6 +362,8 @@ def main(ref_root: str):
             shutil.copy(p, out / "Partition" / p.name)
         for p in work.glob("*.txt"):
             shutil.copy(p, out / p.name)
+        if (work / "drm").is_dir():
+            shutil.copytree(work / "drm", out / "drm")
         print("wrote", out.name, sorted(x.name for x in out.rglob("*") if x.is_file()))
     shutil.rmtree(scratch)
 

@@ -188,3 +188,45 @@ def lysmer_box(nx=12, ny=6, h=1.0, E=2.0e8, nu=0.25, rho=2000.0, nt=200, amp=1.0
     top = ny * (nx + 1) + nx // 2
     L.add_point_load(m2, top, (0.0, -1.0), s)
     return m2, L, dt
+
+
+def drm_box(nx=12, ny=8, h=1.0, E=2.0e8, nu=0.25, rho=2000.0, nt=120, dt_factor=0.5, f0=6.0, seed=0):
+    """Plane-strain box with a one-element domain-reduction layer: the ring of
+    elements one element in from the sides and bottom; its inner nodes are the
+    boundary nodes, its outer nodes the exterior ones.  The free field is a
+    vertically travelling SV pulse u_x = g(t - y/Vs) (with v, a by finite
+    differences of the same expression), seeded amplitude."""
+    m = Model.grid(2, (nx, ny), (h, h), fix_mask=(1, 1, 3, 0, 0, 0),
+                   mat_type=np.array([capi.SVL_MAT_ELASTIC2DPLANESTRAIN], np.int32),
+                   mat_param=elastic_params(2, E, nu, rho)[None, :])
+    G = E / (2 * (1 + nu))
+    lam = E * nu / ((1 + nu) * (1 - 2 * nu))
+    vp, vs = np.sqrt((lam + 2 * G) / rho), np.sqrt(G / rho)
+    dt = dt_factor * h / vp
+    X = m.coords
+    xmin, xmax, ymin = h, (nx - 1) * h, h
+    inner = lambda p: (p[0] >= xmin - 1e-9) and (p[0] <= xmax + 1e-9) and (p[1] >= ymin - 1e-9)  # noqa: E731
+    elems = []
+    for e in range(m.nelem):
+        c = X[m.conn[e]]
+        ins = [inner(p) for p in c]
+        if any(ins) and not all(ins):
+            elems.append(e)
+    nodes = sorted(set(int(n) for e in elems for n in m.conn[e]))
+    amp = 1e-3 * (1.0 + np.random.default_rng(seed).random())
+    t = np.arange(nt + 2) * dt
+    def g(tau):
+        a = (np.pi * f0 * (tau - 1.2 / f0)) ** 2
+        return amp * (1 - 2 * a) * np.exp(-a)
+    motion = {}
+    for n in nodes:
+        y = X[n, 1]
+        u = g(t - (ny * h - y) / vs)
+        v = np.gradient(u, dt)
+        a = np.gradient(v, dt)
+        sig = np.zeros((nt + 2, 6))
+        sig[:, 0], sig[:, 2], sig[:, 4] = u, v, a
+        motion[n] = (sig, not inner(X[n]))
+    L = Loads()
+    L.add_drm(m, elems, motion, factor=1.0)
+    return m, L, dt, elems, motion

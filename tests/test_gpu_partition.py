@@ -68,3 +68,11 @@ def test_pml_partition_extended_newmark_matches_oracle(gpu, tmp_path):
     assert rel_l2(U, ho) <= 1e-8
     (nn, ndofs, ntotal, nt), head, rows = _read_recorder(tmp_path / p.recorders[0].file)
     assert ntotal == p.model.ntotal and rows.shape == (p.nt - 1, ndofs)
+
+
+def test_drm_partition_newmark_matches_oracle(gpu, tmp_path):
+    p = _part("q4_drm_newmark")
+    U = p.run(solution_dir=tmp_path)
+    ho, _ = O.newmark_run(p.model, p.loads, p.dt, p.nt - 1, solver=0)
+    assert np.abs(ho).max() > 0
+    assert rel_l2(U, ho) <= 1e-9

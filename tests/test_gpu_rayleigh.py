@@ -140,3 +140,23 @@ def test_central_difference_rejects_free_free_dashpot(gpu):
     with pytest.raises(SvlError) as ei:
         CentralDifference(m, L, dt)
     assert ei.value.code == capi.SVL_ERR_UNSUPPORTED
+
+
+def test_domain_reduction_central_difference_and_newmark(gpu):
+    """DRM forces (elastic, lumped mass: factor * K~ (U_o + ak V_o)) on the
+    explicit and implicit paths against the oracle's faithful element matrices."""
+    from tests.helpers import drm_box
+    m, L, dt, elems, motion = drm_box(16, 10, nt=200)
+    cd = CentralDifference(m, L, dt)
+    cd.Initialize()
+    hc = cd.run(1, 200, history=True)
+    cd.close()
+    ho, *_ = O.cd_run(m, L, dt, 200)
+    assert np.abs(ho).max() > 0 and rel_l2(hc, ho) <= 1e-12
+    m.rayleigh = np.tile([1.0, 4e-4], (m.nelem, 1))
+    nm = NewmarkBeta(m, L, 3 * dt, pcg_tol=1e-13)
+    nm.Initialize()
+    hn = nm.run(1, 60, history=True)
+    nm.close()
+    hno, _ = O.newmark_run(m, L, 3 * dt, 60, solver=0)
+    assert rel_l2(hn, hno) <= 1e-9

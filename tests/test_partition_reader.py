@@ -20,7 +20,7 @@ def _part(case):
 
 
 @pytest.mark.parametrize("case", ["q4_cd", "h8_newmark_body", "q4_j2_column", "q4_newmark_rayleigh", "q4_pml_extended",
-                                  "q4_lysmer_cd"])
+                                  "q4_lysmer_cd", "q4_drm_newmark"])
 def test_numbering_and_connectivity_follow_the_file(case):
     p = load_partition(_part(case))
     d = json.loads(_part(case).read_text())
@@ -137,6 +137,23 @@ def test_zero_length_dashpots():
     p.model.dashpot_dof = p.model.dashpot_eta = None
     h0, *_ = O.cd_run(p.model, p.loads, p.dt, p.nt - 1)
     assert np.all(np.isfinite(h)) and np.linalg.norm(h - h0) > 1e-6 * np.linalg.norm(h0)
+
+
+def test_domain_reduction_load():
+    """ELEMENTLOAD GENERALWAVE: DRM elements in load-list order, per-node files
+    (`$` -> node tag) with `nt nFields cond` headers (Driver.hpp:1669-1722)."""
+    p = load_partition(_part("q4_drm_newmark"))
+    d = json.loads(_part("q4_drm_newmark").read_text())
+    L = p.loads
+    etags = sorted(int(t) for t in d["Elements"])
+    assert [etags[e] for e in L.drm_elem] == d["Loads"]["1"]["attributes"]["list"]
+    ntags = sorted(int(t) for t in d["Nodes"])
+    for n, (sig, ext) in L.drm_motion.items():
+        f = (GOLD / "partition_q4_drm_newmark" / "drm" / ("node%d.txt" % ntags[n])).read_text().split()
+        assert int(f[0]) == sig.shape[0] and int(f[2]) == ext
+        assert float(f[3]) == sig[0, 0]
+    h, _ = O.newmark_run(p.model, L, p.dt, p.nt - 1, solver=0)
+    assert np.all(np.isfinite(h)) and np.abs(h).max() > 0
 
 
 def test_integrator_names_are_the_run_process_ones(tmp_path):
