@@ -142,6 +142,105 @@ __global__ void __launch_bounds__(128) k_xsolid(XSolid S) {
     }
 }
 
+// Domain-reduction forces (lin2DQuad4.cpp:564-614) of solid elastic elements
+// with a lumped mass: factor * K~ (U_o + ak V_o), K~ coupling only boundary and
+// exterior dofs (see k_drm in svl_cd.cu for the same reduction).
+struct XDrm {
+    int n, nt, k, ngp;
+    const int32_t* sidx;      // [n] solid-element index of each entry
+    const double* factor;     // [n]
+    const double* ak;         // [n]
+    const int32_t* node_of;   // [n][NEN]
+    const int32_t* row;       // [nnode]
+    const int32_t* ext;       // [nnode]
+    const double* motion;     // [blocks][nt][3 ND]
+    const int32_t* egeo; const double* geo; const double* coef;
+    double* fe;               // [n][NC]
+};
+
+template <int ND, int NEN>
+__global__ void __launch_bounds__(128) k_xdrm(XDrm D) {
+    constexpr int NC = ND * NEN, PER = NEN * ND + 1;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= D.n) return;
+    const int e = D.sidx[i], k = D.k;
+    double wb[NC], we[NC], yb[NC], ye[NC];
+    int ext[NEN];
+#pragma unroll
+    for (int j = 0; j < NC; ++j) {
+        const int a = j / ND, c = j % ND;
+        const int node = D.node_of[(size_t)i * NEN + a];
+        const bool x = D.ext[node] != 0;
+        ext[a] = x;
+        double u = 0.0, v = 0.0;
+        if (k >= 0 && k < D.nt) {
+            const double* rw = D.motion + ((size_t)D.row[node] * D.nt + k) * (3 * ND);
+            u = rw[c];
+            v = rw[ND + c];
+        }
+        const double w = (x ? -1.0 : 1.0) * (u + D.ak[i] * v);
+        wb[j] = x ? 0.0 : w;
+        we[j] = x ? w : 0.0;
+        yb[j] = 0.0; ye[j] = 0.0;
+    }
+    const double c1 = D.coef[3 * e], c2 = D.coef[3 * e + 1], c3 = D.coef[3 * e + 2];
+    const double* g0 = D.geo + (size_t)D.egeo[e] * D.ngp * PER;
+    for (int q = 0; q < D.ngp; ++q) {
+        const double* g = g0 + q * PER;
+        const double w = g[PER - 1];
+#pragma unroll
+        for (int pass = 0; pass < 2; ++pass) {
+            const double* uu = pass == 0 ? wb : we;
+            double* yy = pass == 0 ? yb : ye;
+            if (ND == 2) {
+                double exx = 0, eyy = 0, gxy = 0;
+#pragma unroll
+                for (int a = 0; a < NEN; ++a) {
+                    const double bx = g[a * ND], by = g[a * ND + 1];
+                    exx += bx * uu[2 * a];
+                    eyy += by * uu[2 * a + 1];
+                    gxy += by * uu[2 * a] + bx * uu[2 * a + 1];
+                }
+                const double s0 = c1 * exx + c2 * eyy, s1 = c2 * exx + c1 * eyy, s2 = c3 * gxy;
+#pragma unroll
+                for (int a = 0; a < NEN; ++a) {
+                    const double bx = g[a * ND], by = g[a * ND + 1];
+                    yy[2 * a] += w * (bx * s0 + by * s2);
+                    yy[2 * a + 1] += w * (by * s1 + bx * s2);
+                }
+            } else {
+                double ev[6] = {0, 0, 0, 0, 0, 0};
+#pragma unroll
+                for (int a = 0; a < NEN; ++a) {
+                    const double bx = g[a * ND], by = g[a * ND + 1], bz = g[a * ND + (ND - 1)];
+                    const double ux = uu[ND * a], uy = uu[ND * a + 1], uz = uu[ND * a + (ND - 1)];
+                    ev[0] += bx * ux;
+                    ev[1] += by * uy;
+                    ev[2] += bz * uz;
+                    ev[3] += by * ux + bx * uy;
+                    ev[4] += bz * uy + by * uz;
+                    ev[5] += bz * ux + bx * uz;
+                }
+                double sg[6];
+                sg[0] = c1 * ev[0] + c2 * ev[1] + c2 * ev[2];
+                sg[1] = c2 * ev[0] + c1 * ev[1] + c2 * ev[2];
+                sg[2] = c2 * ev[0] + c2 * ev[1] + c1 * ev[2];
+                sg[3] = c3 * ev[3]; sg[4] = c3 * ev[4]; sg[5] = c3 * ev[5];
+#pragma unroll
+                for (int a = 0; a < NEN; ++a) {
+                    const double bx = g[a * ND], by = g[a * ND + 1], bz = g[a * ND + (ND - 1)];
+                    yy[ND * a] += w * (bx * sg[0] + by * sg[3] + bz * sg[5]);
+                    yy[ND * a + 1] += w * (by * sg[1] + bx * sg[3] + bz * sg[4]);
+                    yy[ND * a + (ND - 1)] += w * (bz * sg[2] + by * sg[4] + bx * sg[5]);
+                }
+            }
+        }
+    }
+    double* out = D.fe + (size_t)i * NC;
+#pragma unroll
+    for (int j = 0; j < NC; ++j) out[j] = D.factor[i] * (ext[j / ND] ? yb[j] : ye[j]);
+}
+
 // y_t = sum of the element entries of dof t in element order (+ c_n m_t x_t) (+ Fext_t(k))
 struct XGather {
     int ntotal;
@@ -155,8 +254,9 @@ struct XGather {
     const int32_t *dp_ptr, *dp_col; const double* dp_eta;
     double cdp;
     const double* xdp;
-    // external force (RHS only)
+    // external force (RHS only), with the domain-reduction element forces
     int k, with_fext;
+    const int32_t *drm_ptr, *drm_idx; const double* drm_fe;
     const int32_t *ld_ptr, *ld_ser; const double* ld_coef;
     const int32_t* s_ptr; const double* s_val;
     double* y;
@@ -181,6 +281,8 @@ __global__ void k_xgather(XGather G) {
             const int b = G.s_ptr[s], n = G.s_ptr[s + 1] - b;
             f += G.ld_coef[i] * ((G.k >= 0 && G.k < n) ? G.s_val[b + G.k] : 0.0);
         }
+        if (G.drm_ptr)
+            for (int i = G.drm_ptr[t]; i < G.drm_ptr[t + 1]; ++i) f += G.drm_fe[G.drm_idx[i]];
         v += f;
     }
     G.y[t] = v;
@@ -333,6 +435,11 @@ struct svl_xnm {
     double* nodemass = nullptr;
     int32_t *dp_ptr = nullptr, *dp_col = nullptr;
     double* dp_eta = nullptr;
+    // domain reduction
+    int ndrm = 0, drm_nt = 0;
+    int32_t *drm_sidx = nullptr, *drm_node_of = nullptr, *drm_row = nullptr, *drm_ext = nullptr;
+    int32_t *drm_ptr = nullptr, *drm_idx = nullptr;
+    double *drm_factor = nullptr, *drm_ak = nullptr, *drm_motion = nullptr, *drm_fe = nullptr;
     // T and T^T
     int32_t *Tp = nullptr, *Tc = nullptr, *TTp = nullptr, *TTr = nullptr;
     double *Tv = nullptr, *TTv = nullptr;
@@ -388,6 +495,7 @@ int x_gather(svl_xnm* X, double* y, double cn, const double* xn, double cdp, con
     G.dp_ptr = X->dp_ptr; G.dp_col = X->dp_col; G.dp_eta = X->dp_eta; G.cdp = cdp; G.xdp = xdp;
     G.k = k; G.with_fext = fext ? 1 : 0;
     G.ld_ptr = X->ld_ptr; G.ld_ser = X->ld_ser; G.ld_coef = X->ld_coef; G.s_ptr = X->s_ptr; G.s_val = X->s_val;
+    if (fext && X->ndrm > 0) { G.drm_ptr = X->drm_ptr; G.drm_idx = X->drm_idx; G.drm_fe = X->drm_fe; }
     G.y = y;
     k_xgather<<<grid_of(X->m.ntotal), 256, 0, X->stream>>>(G);
     XCUDA(cudaGetLastError());
@@ -561,6 +669,17 @@ int x_step(svl_xnm* X, int k) {
     if (m.ndim == 3) { P.coef[3] = -1.0; P.u[3] = X->Wg; }
     P.accumulate = 1;
     XTRY(pml_action_launch(m.ndim, P, X->stream));
+    if (X->ndrm > 0) {
+        XDrm D{};
+        D.n = X->ndrm; D.nt = X->drm_nt; D.k = k; D.ngp = m.ngp;
+        D.sidx = X->drm_sidx; D.factor = X->drm_factor; D.ak = X->drm_ak; D.node_of = X->drm_node_of;
+        D.row = X->drm_row; D.ext = X->drm_ext; D.motion = X->drm_motion;
+        D.egeo = X->s_egeo; D.geo = X->s_geo; D.coef = X->s_coef; D.fe = X->drm_fe;
+        const int gd = (X->ndrm + 127) / 128;
+        if (m.ndim == 2) k_xdrm<2, 4><<<gd, 128, 0, X->stream>>>(D);
+        else k_xdrm<3, 8><<<gd, 128, 0, X->stream>>>(D);
+        XCUDA(cudaGetLastError());
+    }
     XTRY(x_gather(X, X->yt, 1.0, X->W, 1.0, X->V, k, true));
     const double* sub = nullptr;
     if (X->lt.has_sm) {
@@ -704,8 +823,44 @@ int x_setup(svl_xnm* X, const svl_load_desc* L) {
         for (int t = 0; t < m.ntotal; ++t)
             for (int i = Tp[t]; i < Tp[t + 1]; ++i) { const int p = fill[Tc[i]]++; TTr[p] = t; TTv[p] = Tv[i]; }
     }
-    if (L && L->ndrm > 0) { set_error("domain-reduction loads are served by svl_cd_create / svl_nm_create"); return SVL_ERR_UNSUPPORTED; }
     XTRY(build_load_tables(m, L, X->lt));
+    if (L && L->ndrm > 0) {
+        if (!L->drm_elem || !L->drm_factor || !L->drm_node_row || !L->drm_node_ext || !L->drm_motion || L->drm_nt <= 0) {
+            set_error("domain-reduction arrays are NULL or drm_nt <= 0"); return SVL_ERR_INVALID;
+        }
+        std::vector<int32_t> sidx_of(m.nelem, -1);
+        for (int i = 0; i < X->nsol; ++i) sidx_of[sol[i]] = i;
+        std::vector<int32_t> dsidx, dnode, drow(L->drm_node_row, L->drm_node_row + m.nnode),
+            dext(L->drm_node_ext, L->drm_node_ext + m.nnode), dptr(m.ntotal + 1, 0), didx;
+        std::vector<double> dfac, dak;
+        int nblk = 0;
+        for (int r : drow) nblk = std::max(nblk, r + 1);
+        std::vector<double> dmot(L->drm_motion, L->drm_motion + (size_t)nblk * L->drm_nt * 3 * nd);
+        for (int i = 0; i < L->ndrm; ++i) {
+            const int e = L->drm_elem[i];
+            if (e < 0 || e >= m.nelem || sidx_of[e] < 0) { set_error("DRM entry %d: element %d is not a solid element", i, e); return SVL_ERR_INVALID; }
+            dsidx.push_back(sidx_of[e]);
+            dfac.push_back(L->drm_factor[i]);
+            dak.push_back(m.ray.empty() ? 0.0 : m.ray[2 * (size_t)e + 1]);
+            for (int a = 0; a < nen; ++a) {
+                const int n = m.conn[(size_t)e * nen + a];
+                if (drow[n] < 0) { set_error("DRM element %d: node %d has no free-field motion", e, n); return SVL_ERR_INVALID; }
+                dnode.push_back(n);
+                for (int c = 0; c < nd; ++c) dptr[gdof(e, a * nd + c) + 1]++;
+            }
+        }
+        for (int t = 0; t < m.ntotal; ++t) dptr[t + 1] += dptr[t];
+        didx.resize(dptr.back());
+        std::vector<int32_t> fill(dptr.begin(), dptr.end() - 1);
+        for (int i = 0; i < L->ndrm; ++i)
+            for (int j = 0; j < X->ncs; ++j) didx[fill[gdof(L->drm_elem[i], j)]++] = i * X->ncs + j;
+        X->ndrm = L->ndrm;
+        X->drm_nt = L->drm_nt;
+        XTRY(X->upload(dsidx, &X->drm_sidx)); XTRY(X->upload(dfac, &X->drm_factor)); XTRY(X->upload(dak, &X->drm_ak));
+        XTRY(X->upload(dnode, &X->drm_node_of)); XTRY(X->upload(drow, &X->drm_row)); XTRY(X->upload(dext, &X->drm_ext));
+        XTRY(X->upload(dmot, &X->drm_motion)); XTRY(X->upload(dptr, &X->drm_ptr)); XTRY(X->upload(didx, &X->drm_idx));
+        XTRY(X->alloc((size_t)X->ndrm * X->ncs, &X->drm_fe));
+    }
     // uploads
     XTRY(X->upload(s_edof, &X->s_edof)); XTRY(X->upload(s_egeo, &X->s_egeo)); XTRY(X->upload(s_geo, &X->s_geo));
     XTRY(X->upload(s_coef, &X->s_coef)); XTRY(X->upload(s_ml, &X->s_mlump));

@@ -126,5 +126,51 @@ private:
     int ntotal_ = 0;
 };
 
+// ExtendedNewmarkBeta(mesh, dt, mtol, ktol, ftol) with the Linear algorithm
+// (RP/10-Integrators/03-Newmark/ExtendedNewmarkBeta.cpp:37-245) for meshes with
+// PML2DQuad4 / PML3DHexa8 layers: the effective-stiffness solve is
+// matrix-free MINRES on the GPU to a relative residual `tol` (|diag|^-1 norm).
+class ExtendedNewmarkBeta {
+public:
+    ExtendedNewmarkBeta(const svl_model_desc& model, const svl_load_desc& loads, double dt, double tol = 1e-10,
+                        double mtol = 1e-12, double ftol = 1e-12, int maxit = 100000)
+        : ntotal_(model.ntotal) {
+        svl_xnm_opts o{};
+        o.dt = dt;
+        o.ftol = ftol;
+        o.mtol = mtol;
+        o.tol = tol;
+        o.maxit = maxit;
+        check(svl_xnm_create(&model, &loads, &o, &h_));
+    }
+    ~ExtendedNewmarkBeta() { svl_xnm_destroy(h_); }
+    ExtendedNewmarkBeta(const ExtendedNewmarkBeta&) = delete;
+    ExtendedNewmarkBeta& operator=(const ExtendedNewmarkBeta&) = delete;
+
+    // Initialize(mesh): U, V, A and the PML history Ubar from the nodes (:37-71)
+    void Initialize(const double* U0 = nullptr, const double* V0 = nullptr, const double* A0 = nullptr,
+                    const double* Ubar0 = nullptr) {
+        check(svl_xnm_set_initial(h_, U0, V0, A0, Ubar0));
+    }
+    // ComputeNewStep(mesh, k) -> stop (:123-153)
+    bool ComputeNewStep(unsigned int k) { return svl_xnm_run(h_, (int32_t)k, 1, nullptr) != SVL_OK; }
+    bool ComputeNewSteps(unsigned int k_first, unsigned int n, double* U_hist = nullptr) {
+        return svl_xnm_run(h_, (int32_t)k_first, (int32_t)n, U_hist) != SVL_OK;
+    }
+    std::vector<double> GetDisplacements() const { return get(0); }
+    std::vector<double> GetVelocities() const { return get(1); }
+    std::vector<double> GetAccelerations() const { return get(2); }
+    std::vector<double> GetPMLHistoryVector() const { return get(3); }
+
+private:
+    std::vector<double> get(int which) const {
+        std::vector<double> v(ntotal_);
+        check(svl_xnm_get(h_, which, v.data()));
+        return v;
+    }
+    svl_xnm* h_ = nullptr;
+    int ntotal_ = 0;
+};
+
 }  // namespace gpu
 }  // namespace svl

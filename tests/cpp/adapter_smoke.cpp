@@ -42,7 +42,13 @@ int main() {
             if (nm.ComputeNewStep(k)) { std::printf("newmark stop at %u\n", k); return 3; }
         double mn = 0;
         for (double u : nm.GetDisplacements()) mn = std::fmax(mn, std::fabs(u));
-        std::printf("max|U| %.6e newmark %.6e\n", mx, mn);
+        svl::gpu::ExtendedNewmarkBeta xn(md, ld, 4.0 * dt, 1e-12);
+        xn.Initialize();
+        if (xn.ComputeNewSteps(1, 20)) { std::printf("extended newmark stop\n"); return 4; }
+        double mxn = 0, dmax = 0;
+        const std::vector<double> ux = xn.GetDisplacements(), un = nm.GetDisplacements();
+        for (size_t i = 0; i < ux.size(); ++i) { mxn = std::fmax(mxn, std::fabs(ux[i])); dmax = std::fmax(dmax, std::fabs(ux[i] - un[i])); }
+        std::printf("max|U| %.6e newmark %.6e extended %.6e (diff %.3e)\n", mx, mn, mxn, dmax);
     } catch (const svl::gpu::Error& e) {
         if (e.code == SVL_ERR_NODEVICE) { std::printf("nodevice\n"); return 0; }
         std::printf("error %d %s\n", e.code, e.what());

@@ -67,3 +67,39 @@ def test_other_paths_reject_pml_models(gpu):
     with pytest.raises(SvlError) as ei:
         ExtendedNewmarkBeta(m2, L2, dt2)
     assert ei.value.code == capi.SVL_ERR_UNSUPPORTED
+
+
+def test_domain_reduction_with_pml_layers(gpu):
+    """DRM ring inside the solid region of a PML box: ExtendedNewmarkBeta on the
+    GPU against the oracle (same faithful DRM forces, dense solve)."""
+    from svl_gb300.model import Loads
+    m, _, dt = pml_box(2, (12, 8), npml=2, nt=80, dt_factor=1.0)
+    X = m.coords
+    lo, hi, top = 3.0, 11.0, X[:, 1].max()
+    inner = lambda p: lo - 1e-9 <= p[0] <= hi + 1e-9 and p[1] >= lo - 1e-9  # noqa: E731
+    elems = []
+    for e in range(m.nelem):
+        if m.elem_pml[e]:
+            continue
+        ins = [inner(X[n]) for n in m.conn[e]]
+        if any(ins) and not all(ins):
+            elems.append(e)
+    assert elems
+    t = np.arange(90) * dt
+    motion = {}
+    for n in sorted({int(n) for e in elems for n in m.conn[e]}):
+        u = 1e-3 * np.sin(2 * np.pi * 8.0 * (t - (top - X[n, 1]) / 200.0)) * (t > (top - X[n, 1]) / 200.0)
+        sig = np.zeros((90, 6))
+        sig[:, 0] = u
+        sig[:, 2] = np.gradient(u, dt)
+        sig[:, 4] = np.gradient(sig[:, 2], dt)
+        motion[n] = (sig, not inner(X[n]))
+    L = Loads()
+    L.add_drm(m, elems, motion)
+    x = ExtendedNewmarkBeta(m, L, dt, tol=1e-12)
+    x.Initialize()
+    hist = x.run(1, 60, history=True)
+    x.close()
+    ho, *_ = O.xnewmark_run(m, L, dt, 60)
+    assert np.abs(ho).max() > 0
+    assert rel_l2(hist, ho) <= 1e-8
