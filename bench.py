@@ -189,6 +189,33 @@ def implicit_pcg(steps, warm=20, tol=1e-8):
             "rel_l2_final_u_learned_vs_jacobi": float(np.linalg.norm(Ul - Uj) / max(np.linalg.norm(Uj), 1e-300))}
 
 
+def nonlinear_newton(steps=8, warm=4, tol=1e-8, size=(64, 64, 32), n_j2=8):
+    """Newmark + NewtonRaphson (3 iterations per step, test 4 disabled by
+    cnvgtol = 0, as in the configuration) on the config-5 style model at a
+    reduced size: J2 top layers over an elastic base on Lysmer dashpots, base
+    plane wave as the Lysmer input force.  Jacobi-PCG per Newton iteration
+    to a true relative residual of `tol`; FP64 return mapping and tangents."""
+    from svl_gb300 import NewmarkBeta, workloads
+    m, L, dt = workloads.config5(*size, n_j2=n_j2, nt=warm + steps + 2)
+    nm = NewmarkBeta(m, L, dt, pcg_tol=tol, algorithm="newton", maxit=3, cnvgtol=0.0, cnvgtest=4)
+    nm.Initialize()
+    nm.run(1, warm)
+    it0 = nm.stats()[0]
+    n0 = nm.newton_stats()[0]
+    ms = nm.run_timed(1 + warm, steps)
+    it1, _, res = nm.stats()
+    n1 = nm.newton_stats()[0]
+    U = nm.GetDisplacements()
+    nm.close()
+    return {"workload": "lin3DHexa8 %dx%dx%d (h=2 m), top %d layers Plastic3DJ2 (su 40-150 kPa by depth), "
+                        "elastic base on Lysmer dashpots, band-limited base plane wave (PGA 0.3 g), "
+                        "Newmark-Newton 3 iterations per step" % (size + (n_j2,)),
+            "free_dof": m.nfree, "steps": steps, "ms_per_step": ms / steps,
+            "newton_iters_per_step": (n1 - n0) / steps, "pcg_iters_per_newton_iter": (it1 - it0) / max(n1 - n0, 1),
+            "pcg_tol": tol, "rel_residual_last": res, "finite": bool(np.all(np.isfinite(U))),
+            "dof_newton_iters_per_s": m.nfree * (n1 - n0) / (ms / 1e3)}
+
+
 def implicit_profile():
     from svl_gb300 import NewmarkBeta, workloads
     from svl_gb300 import _capi as capi
@@ -380,6 +407,7 @@ def main():
     if rank == 0 and not args.no_cpu:
         cb = cpu_baseline(m, L, dt, steps_cap=10)
     implicit = implicit_pcg(args.implicit_steps) if (rank == 0 and args.implicit_steps > 0) else None
+    newton = nonlinear_newton() if (rank == 0 and args.implicit_steps > 0 and args.workload == "config2") else None
 
     if rank == 0:
         ws_mb = (nb * m.ntotal * 8 * (2 if args.precision == "mixed" else 7) + nb * m.ntotal * 4
@@ -404,7 +432,7 @@ def main():
                                             "2-instance case (6.3 M DOF), scaled per free DOF to this launch"
                                             if args.precision == "mixed" and args.workload == "config2" else None),
                          "algorithmic_bytes_per_step": algo_bytes, "kernel_share": shares},
-            "fp64_plain": fp64, "implicit_pcg_time_to_1e-8": implicit,
+            "fp64_plain": fp64, "implicit_pcg_time_to_1e-8": implicit, "nonlinear_newton_j2": newton,
             "cpu_baseline": cb, "e2e": e2e, "gpu_launches": int(launches), "clocks": clocks,
             "finite": finite,
         }

@@ -23,6 +23,11 @@ benchmark configurations (no reference data is used):
   element, nu = 0.3, rho = 2000, Newmark average acceleration at
   dt = 10 x the explicit limit h / max Vp, the same double-couple Ricker
   source (f0 = 3 Hz); fixed bottom, rollers on the sides.
+* config5: lin3DHexa8 grid (h = 2 m) whose top layers are Plastic3DJ2 (su
+  40-150 kPa by depth) over an elastic base; the half-space below is
+  represented by Lysmer dashpots on the base nodes (the SPD alternative to a
+  PML half-space for PCG), the incident band-limited plane wave (0.1-10 Hz,
+  PGA 0.3 g) by the Lysmer input force; Newmark-Newton.
 """
 from __future__ import annotations
 
@@ -188,3 +193,65 @@ def config3(ncol=256, seed=0, nt=None, width=10, h=0.5, duration=20.0, hmin=50, 
     info = {"columns": ncol, "elements": int(sum(x.nelem for x in models)), "dt": dt, "nt": nt,
             "heights": [int(heights.min()), int(heights.max())]}
     return Model.concat(models), Loads.concat(loads, models), dt, info
+
+
+def config5(nx=128, ny=128, nz=64, n_j2=16, nt=301, seed=0, h=2.0, pga=0.3 * 9.81):
+    """Nonlinear implicit model: lin3DHexa8 grid, the top `n_j2` element
+    layers Plastic3DJ2 (su uniform in [40, 150] kPa by depth, seeded; H =
+    0.02 G, beta = 1), elastic below; Vs 300 m/s (J2 layers 200 m/s), nu = 0.3,
+    rho = 2000.  The half-space below is represented by Lysmer dashpots on the
+    base nodes (rho Vs A tangential, rho Vp A normal, A the node's base area)
+    tied to fixed anchor nodes, which keeps the effective stiffness SPD; the
+    incident plane wave (band-limited 0.1-10 Hz, PGA `pga`) enters as the
+    Lysmer input force 2 rho Vs A v_in(t) in x on the base nodes.  Sides:
+    rollers.  dt = 0.5 h / Vp of the elastic layers."""
+    from .model import j2_params
+    rng = np.random.default_rng(seed + 5)
+    rho, nu = 2000.0, 0.3
+    vs_el, vs_j2 = 300.0, 200.0
+    ne = nx * ny * nz
+    k = np.arange(ne) // (nx * ny)                     # element layer, 0 at the base
+    j2 = k >= nz - n_j2
+    mp = np.zeros((ne, 8))
+    mt = np.where(j2, capi.SVL_MAT_PLASTIC3DJ2, capi.SVL_MAT_ELASTIC3DLINEAR).astype(np.int32)
+    G_el, G_j2 = rho * vs_el ** 2, rho * vs_j2 ** 2
+    E_el = 2 * G_el * (1 + nu)
+    K_j2 = 2 * G_j2 * (1 + nu) / (3 * (1 - 2 * nu))
+    su_layer = np.sort(rng.uniform(40e3, 150e3, n_j2))[::-1]          # stiffer with depth
+    for e in np.flatnonzero(~j2):
+        mp[e, :3] = (E_el, nu, rho)
+    for e in np.flatnonzero(j2):
+        layer = nz - 1 - k[e]
+        mp[e] = j2_params(K_j2, G_j2, rho, 0.02 * G_j2, 1.0, np.sqrt(3.0) * su_layer[layer])
+    g = Model.grid(3, (nx, ny, nz), (h, h, h), fix_mask=(1, 1, 2, 2, 0, 0),
+                   mat_type=mt, mat_param=mp, elem_mat=np.arange(ne, dtype=np.int32))
+    vp = vs_el * np.sqrt(2 * (1 - nu) / (1 - 2 * nu))
+    dt = 0.5 * h / vp
+    X = g.coords
+    base = np.flatnonzero(np.isclose(X[:, 2], 0.0))
+    nb = base.size
+    nn0 = g.nnode
+    coords = np.vstack([X, X[base]])
+    tdof = np.vstack([g.totaldof, (g.ntotal + np.arange(3 * nb)).reshape(nb, 3)]).astype(np.int32)
+    fdof = np.vstack([g.freedof, -np.ones((nb, 3), np.int32)]).astype(np.int32)
+    ix = np.rint(X[base, 0] / h).astype(int)
+    iy = np.rint(X[base, 1] / h).astype(int)
+    area = h * h * np.where((ix == 0) | (ix == nx), 0.5, 1.0) * np.where((iy == 0) | (iy == ny), 0.5, 1.0)
+    dof, eta = [], []
+    for i, n in enumerate(base):
+        for j in range(3):
+            dof.append((int(g.totaldof[n, j]), int(tdof[nn0 + i, j])))
+            eta.append(rho * (vp if j == 2 else vs_el) * area[i])
+    m = Model(ndim=3, coords=coords, totaldof=tdof, freedof=fdof, conn=g.conn, elem_type=g.elem_type,
+              elem_mat=g.elem_mat, mat_type=g.mat_type, mat_param=g.mat_param, lumped=True,
+              dashpot_dof=np.array(dof, np.int32), dashpot_eta=np.array(eta))
+    disp = base_motion(nt + 2, dt, 0.1, 10.0, pga, rng)
+    v_in = np.gradient(disp, dt)
+    L = Loads()
+    s = L.add_series(v_in)
+    for i, n in enumerate(base):
+        if g.freedof[n, 0] >= 0:
+            L.force_dof.append(int(g.totaldof[n, 0]))
+            L.force_series.append(s)
+            L.force_coef.append(2.0 * rho * vs_el * area[i])
+    return m, L, dt
