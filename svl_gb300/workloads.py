@@ -245,7 +245,9 @@ def config5(nx=128, ny=128, nz=64, n_j2=16, nt=301, seed=0, h=2.0, pga=0.3 * 9.8
     m = Model(ndim=3, coords=coords, totaldof=tdof, freedof=fdof, conn=g.conn, elem_type=g.elem_type,
               elem_mat=g.elem_mat, mat_type=g.mat_type, mat_param=g.mat_param, lumped=True,
               dashpot_dof=np.array(dof, np.int32), dashpot_eta=np.array(eta))
-    disp = base_motion(nt + 2, dt, 0.1, 10.0, pga, rng)
+    # the record is synthesised over 20 s (frequency resolution for the 0.1-10 Hz
+    # band) and the first nt + 2 samples are used
+    disp = base_motion(max(nt + 2, int(20.0 / dt)), dt, 0.1, 10.0, pga, rng)[:nt + 2]
     v_in = np.gradient(disp, dt)
     L = Loads()
     s = L.add_series(v_in)
