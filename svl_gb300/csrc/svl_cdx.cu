@@ -53,7 +53,7 @@ constexpr int align_up(int x, int a) { return (x + a - 1) / a * a; }
 
 // Node tile owned by one CTA per pass and derived sizes.
 constexpr int TX = 8, TY = 8, TZ = 8;
-constexpr int HX = TX + 2, HY = TY + 2, HZ = TZ + 2;          // halo nodes
+constexpr int HY = TY + 2, HZ = TZ + 2;                       // halo nodes in y, z (x: RAWX floats)
 constexpr int EX = TX + 1, EY = TY + 1, EZ = TZ + 1;          // elements touching the tile
 constexpr int NEL = EX * EY * EZ;                             // 729
 constexpr int NMT = (NEL + 127) / 128;                        // 6 MMA tiles of 128 elements

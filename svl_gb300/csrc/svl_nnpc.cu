@@ -422,18 +422,6 @@ __global__ void __launch_bounds__(TC_THREADS) k_conv_tc(const __grid_constant__ 
     }
 }
 
-// features, channel-last BF16 [V][16]: channels 0-2 r_hat, 3-5 rho r_hat, rest 0 (grid pre-zeroed)
-__global__ void k_feat_free_tc(const double* __restrict__ r, const double* __restrict__ sdinv,
-                               const float* __restrict__ rho_grid, const int32_t* __restrict__ gmap,
-                               __nv_bfloat16* __restrict__ f, int nf, int V) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nf) return;
-    const int g = gmap[i], c = g / V, node = g - c * V;
-    const float v = (float)(r[i] * sdinv[i]);
-    f[(size_t)node * 16 + c] = __float2bfloat16_rn(v);
-    f[(size_t)node * 16 + 3 + c] = __float2bfloat16_rn(rho_grid[g] * v);
-}
-
 // features, channel-last BF16 [V][16], one thread per voxel (no pre-zeroing)
 __global__ void k_feat_voxel_tc(const double* __restrict__ r, const double* __restrict__ sdinv,
                                 const float* __restrict__ rho_grid, const int32_t* __restrict__ inv,
