@@ -2009,7 +2009,15 @@ int svl_nm_create(const svl_model_desc* model, const svl_load_desc* loads, const
         set_error("Newton needs maxit > 0, cnvgtol >= 0 (0: always maxit iterations) and cnvgtest 4 or 5");
         return fail(SVL_ERR_INVALID);
     }
-    if (m.has_j2() && !nm->newton) { set_error("the implicit Linear path is elastic; J2 needs Newton iterations"); return fail(SVL_ERR_UNSUPPORTED); }
+    if (m.has_j2() && !nm->newton) {
+        // Linear with a nonlinear material (Linear.cpp:22-56): effective force from
+        // the committed states, one solve with the tangent stiffness, one state
+        // update from U + dU -- exactly one Newton iteration
+        nm->newton = true;
+        nm->opts.maxit = 1;
+        nm->opts.cnvgtol = 0.0;
+        nm->opts.cnvgtest = 4;
+    }
     nm->tangent = nm->newton && m.has_j2();
     nm->nf = m.nfree;
     const double c_m = 4.0 / opts->dt / opts->dt, c_c = 2.0 / opts->dt;

@@ -89,11 +89,20 @@ def test_newton_on_elastic_model_matches_linear(gpu):
     assert rel_l2(ha, hb) <= 1e-9
 
 
-def test_linear_path_rejects_j2(gpu):
-    m, L, dt = j2_box(2, (4, 3))
-    with pytest.raises(SvlError) as ei:
-        NewmarkBeta(m, L, dt)
-    assert ei.value.code == capi.SVL_ERR_UNSUPPORTED
+def test_linear_algorithm_with_j2_matches_oracle(gpu):
+    """Linear with a J2 material (Linear.cpp:22-56): one tangent solve and one
+    state update per step, i.e. a single Newton iteration."""
+    m, L, dt = j2_box(2, (8, 6), amp=4e5, nt=60)
+    nm = NewmarkBeta(m, L, dt, pcg_tol=1e-13)
+    nm.Initialize()
+    hist = nm.run(1, 60, history=True)
+    its, last, _ = nm.newton_stats()
+    nm.close()
+    ho, _ = O.newmark_run(m, L, dt, 60, algo=0, solver=0)
+    hl, _ = O.newmark_run(m, L, dt, 60, algo=2, maxit=3, cnvgtol=0.0, solver=0)
+    assert its == 60 and last == 1
+    assert rel_l2(ho, hl) > 1e-6                     # one iteration differs from three once yielding
+    assert rel_l2(hist, ho) <= 1e-9
 
 
 def _columns(elastic):
