@@ -98,6 +98,10 @@ def test_nm_iteration_cap_is_reported(gpu):
 
 def test_nm_rejects_models_it_does_not_cover(gpu):
     m, L, dt = q4_j2_columns(ncol=2, heights=(4, 5), nt=10)
-    with pytest.raises(SvlError) as ei:        # periodic constraints + J2
+    with pytest.raises(SvlError) as ei:        # learned preconditioner off the node lattice
+        NewmarkBeta(m, L, dt, precond=capi.SVL_PRECOND_LEARNED)
+    assert ei.value.code == capi.SVL_ERR_UNSUPPORTED
+    m.lumped = False
+    with pytest.raises(SvlError) as ei:        # consistent mass
         NewmarkBeta(m, L, dt)
     assert ei.value.code == capi.SVL_ERR_UNSUPPORTED
