@@ -359,22 +359,32 @@ void svl_nm_destroy(svl_nm* nm);
 
 /* ---- ExtendedNewmarkBeta with PML (svl_xnm_*) ---------------------------- */
 /* ExtendedNewmarkBeta (RP/10-Integrators/03-Newmark/ExtendedNewmarkBeta.cpp)
- * with the Linear algorithm on a mesh of elastic lin2DQuad4/lin3DHexa8 solid
- * elements (lumped mass, optional Rayleigh damping) and PML2DQuad4/PML3DHexa8
+ * with the Linear or NewtonRaphson algorithm on a mesh of elastic or J2
+ * lin2DQuad4/lin3DHexa8 solid elements (lumped mass, optional Rayleigh
+ * damping with the initial stiffness) and elastic PML2DQuad4/PML3DHexa8
  * elements (5 / 9 dofs per node, consistent mass):
  *   Feff = Fext - Fint - G (Ubar + dt U + dt^2/6 V) + C V + M (4/dt V + A)  (:208-229)
  *   Keff = K + 4/dt^2 M + 2/dt C + dt/3 G                                   (:233-245)
  *   Feff -= T^T Keff SM(k)  (the increment of step k, :190-204)
  *   Ubar += dt U + dt/3 (dU + SM) + dt^2/6 V; U += dU + SM;
  *   A = 4/dt^2 dU - 4/dt V - A; V = 2/dt dU - V                             (:123-153)
- * Fint of a solid element from the strain of U + T du of the last solve, of a
- * PML element K_e U_e (PML3DHexa8.cpp:716-742).  With PML the effective
+ * Fint of a solid element from its state after the last solve (strain of
+ * U + T dU), of a PML element K_e U_e (PML3DHexa8.cpp:716-742).  Newton
+ * iterations (NewtonRaphson.cpp:24-75) repeat force, tangent solve and state
+ * update with the accumulated dU; the effective force has no increment terms
+ * (ExtendedNewmarkBeta.cpp:208-229), so only Fint follows the iterate.  With PML the effective
  * matrix is symmetric indefinite, so the solve is MINRES with the
  * D = |diag(Keff)| preconditioner, matrix-free on the GPU, stopped on the true
  * residual in the norm MINRES minimises, ||b - Keff du||_{D^-1} <= tol ||b||_{D^-1}
  * (displacement and stress rows differ by ~13 orders of magnitude).  The
  * reference solves the same system with SimplicialLDLT / MUMPS / PETSc
  * (EigenSolver.cpp:19-59). */
+#define SVL_XNM_EXTENDED_NEWMARK 0  /* ExtendedNewmarkBeta.cpp (the formulas above)  */
+#define SVL_XNM_NEWMARK          1  /* NewmarkBeta.cpp:117-235 on the same elements:
+                                       Feff = Fext - Fint + M (4/dt V + A - 4/dt^2 dU)
+                                              + C (V - 2/dt dU) - T^T Keff SM(k-1),
+                                       Keff = K + 4/dt^2 M + 2/dt C (G is not used;
+                                       the NEWMARK integrator of a PML model)     */
 typedef struct svl_xnm svl_xnm;
 typedef struct svl_xnm_opts {
     double  dt;
@@ -382,7 +392,13 @@ typedef struct svl_xnm_opts {
     double  mtol;        /* mass assembly tolerance (1e-12)                        */
     double  tol;         /* relative true-residual tolerance (D^-1 norm) of each solve */
     int32_t maxit;       /* MINRES iteration cap per solve (SVL_ERR_MAXITER past it) */
-    int32_t reserved[3];
+    int32_t algorithm;   /* SVL_ALGO_LINEAR or SVL_ALGO_NEWTON                    */
+    int32_t newton_maxit;/* Newton: iterations per step (the algorithm's nstep)   */
+    int32_t cnvgtest;    /* Newton: 4 relative unbalanced force, 5 relative
+                            displacement increment (Algorithm.cpp:122-188)        */
+    double  cnvgtol;     /* Newton: convergence tolerance (0 = always newton_maxit) */
+    int32_t integrator;  /* SVL_XNM_EXTENDED_NEWMARK or SVL_XNM_NEWMARK              */
+    int32_t reserved;
 } svl_xnm_opts;
 int  svl_xnm_create(const svl_model_desc* model, const svl_load_desc* loads, const svl_xnm_opts* opts,
                     svl_xnm** out);
@@ -393,6 +409,9 @@ int  svl_xnm_run(svl_xnm* x, int32_t k_first, int32_t nsteps, double* U_hist);
 /* which: 0 U, 1 V, 2 A, 3 Ubar (GetPMLHistoryVector); out [ntotal]. */
 int  svl_xnm_get(svl_xnm* x, int32_t which, double* out);
 int  svl_xnm_stats(svl_xnm* x, int64_t* iters_total, int64_t* iters_last, double* res_last);
+/* Newton iterations over all steps, of the last step, and the last step's
+ * final convergence-test value (1 iteration per step with Linear). */
+int  svl_xnm_newton_stats(svl_xnm* x, int64_t* iters_total, int64_t* iters_last, double* residual_last);
 void svl_xnm_destroy(svl_xnm* x);
 
 /* ---- learned preconditioner (no counterpart in the reference) ----------- */

@@ -33,7 +33,8 @@ def lib():
         L.oracle_j2_path.argtypes = [C.c_int, f64p, C.c_int, f64p, f64p]
         L.oracle_pml_matrices.argtypes = [C.c_int, f64p, C.c_double, C.c_double, C.c_double, C.c_double, f64p,
                                           f64p, f64p, f64p, f64p]
-        L.oracle_xnewmark_run.argtypes = [vp, vp, C.c_double, C.c_int, C.c_int, f64p, f64p, f64p, f64p, f64p]
+        L.oracle_xnewmark_run.argtypes = [vp, vp, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double,
+                                          C.c_int, f64p, f64p, f64p, f64p, f64p, C.POINTER(C.c_int)]
         L.oracle_xnewmark_matrices.argtypes = [vp, f64p, f64p, f64p, f64p]
         _lib = L
     return _lib
@@ -155,17 +156,22 @@ def pml_matrices(ndim, X, E, nu, rho, par, t=1.0):
     return out
 
 
-def xnewmark_run(model, loads, dt, nsteps, k_first=1):
-    """ExtendedNewmarkBeta + Linear with PML elements (dense LDL^T).  Returns
-    (history of U [nsteps, ntotal], final U, V, A, Ubar)."""
+def xnewmark_run(model, loads, dt, nsteps, k_first=1, algo=0, maxit=50, cnvgtol=1e-6, step_iters=None,
+                 newmark=False):
+    """ExtendedNewmarkBeta (or, newmark=True, NewmarkBeta) on models with PML
+    elements (dense LDL^T); algo 0 Linear, 1 Newton with test 5, 2 Newton
+    with test 4.  Returns (history of U [nsteps, ntotal], final U, V, A,
+    Ubar); step_iters (int32 [nsteps]) receives the iterations of every step."""
     md = model.desc()
     ld = loads.desc() if loads is not None else None
     nt = model.ntotal
     hist = np.zeros((nsteps, nt))
     U, V, A, Ub = (np.zeros(nt) for _ in range(4))
     f = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))  # noqa: E731
+    si = None if step_iters is None else step_iters.ctypes.data_as(C.POINTER(C.c_int))
     st = lib().oracle_xnewmark_run(C.addressof(md), C.addressof(ld) if ld is not None else None, dt, k_first,
-                                   nsteps, f(hist), f(U), f(V), f(A), f(Ub))
+                                   nsteps, algo, maxit, cnvgtol, int(bool(newmark)), f(hist), f(U), f(V), f(A),
+                                   f(Ub), si)
     if st != 0:
         raise RuntimeError("oracle_xnewmark_run failed with status %d" % st)
     return hist, U, V, A, Ub

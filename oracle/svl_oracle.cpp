@@ -81,7 +81,7 @@ struct Loads {
     double support(int s, int k) const {           // Node::GetSupportMotion (Node.cpp:228-247)
         int n = sptr[s + 1] - sptr[s];
         if (n <= 0) return 0.0;
-        return (k < n) ? sval[sptr[s] + k] : sval[sptr[s]];
+        return (k >= 0 && k < n) ? sval[sptr[s] + k] : sval[sptr[s]];   // k < 0: out of range (unsigned)
     }
 };
 
@@ -1339,9 +1339,10 @@ void pml_matrices(int nd, const double* X, double E, double nu, double rho, doub
 
 /* ---------------- ExtendedNewmarkBeta with PML (ExtendedNewmarkBeta.cpp) -- */
 
-/* ExtendedNewmarkBeta::ComputeNewStep with the Linear algorithm on a mesh of
- * elastic solid elements (lin2DQuad4/lin3DHexa8, first ndim dofs of their
- * nodes) and PML elements (PML2DQuad4/PML3DHexa8, every dof of their nodes):
+/* ExtendedNewmarkBeta::ComputeNewStep with the Linear or NewtonRaphson
+ * algorithm on a mesh of elastic or J2 solid elements (lin2DQuad4/lin3DHexa8,
+ * first ndim dofs of their nodes) and PML elements (PML2DQuad4/PML3DHexa8,
+ * every dof of their nodes):
  *   M, C, K, G assembled once (ExtendedNewmarkBeta.cpp:64-70, Assembler.cpp
  *   48-205) in element-tag order, M with the mass tolerance, C, K, G with the
  *   stiffness tolerance; PML mass consistent (PML3DHexa8.cpp:214-284, the 2D
@@ -1353,13 +1354,18 @@ void pml_matrices(int nd, const double* X, double E, double nu, double rho, doub
  *   A = 4/dt^2 dU - 4/dt V - A; V = 2/dt dU - V                             (:123-153)
  * Fint: solid elements from their material state (strain of U + T du of the
  * last step), PML elements K_e U_e with U the displacement after the last
- * step (PML3DHexa8.cpp:716-742 with zero node increments after UpdateDomain). */
+ * step (PML3DHexa8.cpp:716-742 with zero node increments after UpdateDomain).
+ * With J2 elements K is re-assembled with their current tangents at every
+ * iteration (Rayleigh C keeps the initial stiffness). */
 struct XNewmark {
     Sim s; double dt;
     std::vector<double> U, V, A, Ubar;
-    CSR Kt, Mt, Ct, Gt;
+    CSR Kt, Mt, Ct, Gt;                      // Kt: initial K (re-assembled per iteration with J2 tangents)
     std::vector<std::vector<int>> edof;      // per element: solid nen*ndim, PML nen*(5|9)
     int solver = 0; double pcg_tol = 1e-12;
+    bool nonlinear = false;                  // J2 solid elements present
+    bool newmark = false;                    // NewmarkBeta's force, stiffness and update
+    int last_iters = 0;
 
     bool pml(int e) const { return !s.m.epml.empty() && s.m.epml[e]; }
     void pml_elem(int e, double* Me, double* Ce, double* Ke, double* Ge) const {
@@ -1375,8 +1381,14 @@ struct XNewmark {
         if (!s.init(d, l)) return false;
         dt = dt_;
         const Model& m = s.m;
-        for (int t : m.mtype)
-            if (t != SVL_MAT_ELASTIC2DPLANESTRAIN && t != SVL_MAT_ELASTIC3DLINEAR) return false;
+        // PML elements take the elastic constants of their material; solid
+        // elements may be elastic or J2
+        for (int e = 0; e < m.nelem; ++e) {
+            const int t = s.mt(e);
+            const bool el = t == SVL_MAT_ELASTIC2DPLANESTRAIN || t == SVL_MAT_ELASTIC3DLINEAR;
+            if (!el && pml(e)) return false;
+            if (!el) nonlinear = true;
+        }
         const int nt = m.ntotal, pnd = m.ndim == 2 ? 5 : 9;
         U.assign(nt, 0); V.assign(nt, 0); A.assign(nt, 0); Ubar.assign(nt, 0);
         edof.resize(m.nelem);
@@ -1441,69 +1453,129 @@ struct XNewmark {
         for (int e = 0; e < s.m.nelem; ++e) if (!pml(e)) s.element_update(e, U);
         s.commit_all();
     }
+    // K with the solid elements' current tangents, in element order
+    void assemble_K(CSR& K) const {
+        const Model& m = s.m;
+        std::vector<Trip> tk;
+        std::vector<double> Ke(72 * 72);
+        for (int e = 0; e < m.nelem; ++e) {
+            const int nc = (int)edof[e].size();
+            if (pml(e)) pml_elem(e, nullptr, nullptr, Ke.data(), nullptr);
+            else s.element_K(e, Ke.data());
+            for (int j = 0; j < nc; ++j)
+                for (int i = 0; i < nc; ++i) {
+                    const double v = Ke[(size_t)i * nc + j];
+                    if (std::fabs(v) > s.ktol) tk.push_back({edof[e][i], edof[e][j], v});
+                }
+        }
+        csr_from_triplets(m.ntotal, tk, K);
+    }
     // total effective stiffness K + 4/dt^2 M + 2/dt C + dt/3 G
     void keff_total(CSR& Kt_eff) const {
         std::vector<Trip> tr;
         auto add = [&](const CSR& A_, double c) {
             for (int r = 0; r < A_.n; ++r) for (int i = A_.ptr[r]; i < A_.ptr[r + 1]; ++i) tr.push_back({r, A_.col[i], c * A_.val[i]});
         };
-        add(Kt, 1.0); add(Mt, 4.0 / dt / dt); add(Ct, 2.0 / dt); add(Gt, dt / 3.0);
+        add(Kt, 1.0); add(Mt, 4.0 / dt / dt); add(Ct, 2.0 / dt);
+        if (!newmark) add(Gt, dt / 3.0);
         csr_from_triplets(s.m.ntotal, tr, Kt_eff);
     }
-    int step(int k) {
+    // One ExtendedNewmarkBeta::ComputeNewStep with Linear (algo 0) or
+    // NewtonRaphson (algo 1: test 5, algo 2: test 4).  Every iteration
+    // re-evaluates ComputeEffectiveForce (:208-229, which has no increment
+    // terms: only Fint follows the iterate through the element states),
+    // ComputeEffectiveStiffness (:233-245, K with the current tangents) and
+    // the support-motion term (:190-204), solves, accumulates dU and updates
+    // the solid elements from U + T dU (NewtonRaphson.cpp:24-75,
+    // Algorithm.cpp:18-56).
+    int step(int k, int algo = 0, int maxit = 1, double cnvgtol = 0.0) {
         const Model& m = s.m;
         const int nt = m.ntotal, nf = m.nfree;
-        // Fint in element order with the force filter
-        std::vector<double> Fint(nt, 0.0), Fext, w(nt), MW, CV, GW, F(nt), Feff, SM, du, dUt;
+        std::vector<double> Fint(nt), Fext, w(nt), MW, CV, GW, F(nt), Feff, SM, du, dUt, dUf(nf, 0.0), Us(nt);
         double fe[72], ue[72];
         std::vector<double> Ke(72 * 72);
-        for (int e = 0; e < m.nelem; ++e) {
-            const int nc = (int)edof[e].size();
-            if (pml(e)) {
-                pml_elem(e, nullptr, nullptr, Ke.data(), nullptr);
-                for (int i = 0; i < nc; ++i) ue[i] = U[edof[e][i]];
-                for (int i = 0; i < nc; ++i) {
-                    double v = 0.0;
-                    for (int j = 0; j < nc; ++j) v += Ke[(size_t)i * nc + j] * ue[j];
-                    fe[i] = v;
-                }
-            } else {
-                s.element_fint(e, fe);
-            }
-            for (int j = 0; j < nc; ++j) if (std::fabs(fe[j]) > s.ftol) Fint[edof[e][j]] += fe[j];
-        }
-        s.fext(k, Fext);
-        for (int t = 0; t < nt; ++t) w[t] = 4.0 / dt * V[t] + A[t];
-        csr_mv(Mt, w, MW);
-        csr_mv(Ct, V, CV);
-        for (int t = 0; t < nt; ++t) w[t] = Ubar[t] + dt * U[t] + dt * dt / 6.0 * V[t];
-        csr_mv(Gt, w, GW);
-        for (int t = 0; t < nt; ++t) F[t] = (((Fext[t] + 0.0 - Fint[t]) - GW[t]) + CV[t]) + MW[t];
-        s.TT_apply(F, Feff);
-        CSR Ktot; keff_total(Ktot);
-        s.support_increment(k, SM);
+        double norm0 = 0.0, res = 0.0;
+        int it = 0;
+        s.support_increment(newmark ? k - 1 : k, SM);
         bool anySM = false; for (double v : SM) if (v != 0.0) { anySM = true; break; }
-        if (anySM) {
-            std::vector<double> KS, lg; csr_mv(Ktot, SM, KS); s.TT_apply(KS, lg);
-            for (int f = 0; f < nf; ++f) Feff[f] -= lg[f];
+        Us = U;                                  // node displacements + increments T dU
+        dUt.assign(nt, 0.0);
+        for (;;) {
+            // Fint in element order with the force filter; a PML element takes
+            // K_e (U + T dU) of its nodes (PML3DHexa8.cpp:716-742: the node
+            // increments are T dU of the iterate, Algorithm.cpp:18-56, zero
+            // after UpdateDomain)
+            std::fill(Fint.begin(), Fint.end(), 0.0);
+            for (int e = 0; e < m.nelem; ++e) {
+                const int nc = (int)edof[e].size();
+                if (pml(e)) {
+                    pml_elem(e, nullptr, nullptr, Ke.data(), nullptr);
+                    for (int i = 0; i < nc; ++i) ue[i] = Us[edof[e][i]];
+                    for (int i = 0; i < nc; ++i) {
+                        double v = 0.0;
+                        for (int j = 0; j < nc; ++j) v += Ke[(size_t)i * nc + j] * ue[j];
+                        fe[i] = v;
+                    }
+                } else {
+                    s.element_fint(e, fe);
+                }
+                for (int j = 0; j < nc; ++j) if (std::fabs(fe[j]) > s.ftol) Fint[edof[e][j]] += fe[j];
+            }
+            s.fext(k, Fext);
+            if (newmark) {
+                // Fext + Fbar - Fint + M (4/dt V + A - 4/dt^2 dU) + C (V - 2/dt dU) (NewmarkBeta.cpp:215)
+                for (int t = 0; t < nt; ++t) w[t] = 4.0 / dt * V[t] + A[t] - 4.0 / dt / dt * dUt[t];
+                csr_mv(Mt, w, MW);
+                for (int t = 0; t < nt; ++t) w[t] = V[t] - 2.0 / dt * dUt[t];
+                csr_mv(Ct, w, CV);
+                for (int t = 0; t < nt; ++t) F[t] = ((Fext[t] + 0.0 - Fint[t]) + MW[t]) + CV[t];
+            } else {
+                for (int t = 0; t < nt; ++t) w[t] = 4.0 / dt * V[t] + A[t];
+                csr_mv(Mt, w, MW);
+                csr_mv(Ct, V, CV);
+                for (int t = 0; t < nt; ++t) w[t] = Ubar[t] + dt * U[t] + dt * dt / 6.0 * V[t];
+                csr_mv(Gt, w, GW);
+                for (int t = 0; t < nt; ++t) F[t] = (((Fext[t] + 0.0 - Fint[t]) - GW[t]) + CV[t]) + MW[t];
+            }
+            s.TT_apply(F, Feff);
+            if (nonlinear) assemble_K(Kt);
+            CSR Ktot; keff_total(Ktot);
+            if (anySM) {
+                std::vector<double> KS, lg; csr_mv(Ktot, SM, KS); s.TT_apply(KS, lg);
+                for (int f = 0; f < nf; ++f) Feff[f] -= lg[f];
+            }
+            // T^T Keff T
+            std::vector<Trip> tr;
+            for (int r = 0; r < Ktot.n; ++r)
+                for (int i = Ktot.ptr[r]; i < Ktot.ptr[r + 1]; ++i)
+                    for (int a = s.Tptr[r]; a < s.Tptr[r + 1]; ++a)
+                        for (int b = s.Tptr[Ktot.col[i]]; b < s.Tptr[Ktot.col[i] + 1]; ++b)
+                            tr.push_back({s.Tcol[a], s.Tcol[b], s.Tval[a] * Ktot.val[i] * s.Tval[b]});
+            CSR Kff; csr_from_triplets(nf, tr, Kff);
+            if (solver == 0) { if (!dense_ldlt_solve(Kff, Feff, du)) return SVL_ERR_BREAKDOWN; }
+            else return SVL_ERR_INVALID;
+            for (int f = 0; f < nf; ++f) dUf[f] += du[f];
+            if (algo == 1) {
+                double dn = 0, Dn = 0;
+                for (int f = 0; f < nf; ++f) { dn += du[f] * du[f]; Dn += dUf[f] * dUf[f]; }
+                dn = std::sqrt(dn); Dn = std::sqrt(Dn);
+                if (it == 0) { norm0 = Dn; res = dn; } else res = dn / norm0;
+            } else if (algo == 2) {
+                double fn = 0;
+                for (int f = 0; f < nf; ++f) fn += Feff[f] * Feff[f];
+                fn = std::sqrt(fn);
+                if (it == 0) { norm0 = fn; res = fn; } else res = fn / norm0;
+            }
+            s.T_apply(dUf, dUt);
+            for (int t = 0; t < nt; ++t) Us[t] = U[t] + dUt[t];
+            for (int e = 0; e < m.nelem; ++e) if (!pml(e)) s.element_update(e, Us);
+            ++it;
+            if (algo == 0 || !(res > cnvgtol) || it >= maxit) break;
         }
-        // T^T Keff T
-        std::vector<Trip> tr;
-        for (int r = 0; r < Ktot.n; ++r)
-            for (int i = Ktot.ptr[r]; i < Ktot.ptr[r + 1]; ++i)
-                for (int a = s.Tptr[r]; a < s.Tptr[r + 1]; ++a)
-                    for (int b = s.Tptr[Ktot.col[i]]; b < s.Tptr[Ktot.col[i] + 1]; ++b)
-                        tr.push_back({s.Tcol[a], s.Tcol[b], s.Tval[a] * Ktot.val[i] * s.Tval[b]});
-        CSR Kff; csr_from_triplets(nf, tr, Kff);
-        if (solver == 0) { if (!dense_ldlt_solve(Kff, Feff, du)) return SVL_ERR_BREAKDOWN; }
-        else return SVL_ERR_INVALID;
-        s.T_apply(du, dUt);
-        std::vector<double> Us(nt);
-        for (int t = 0; t < nt; ++t) Us[t] = U[t] + dUt[t];
-        for (int e = 0; e < m.nelem; ++e) if (!pml(e)) s.element_update(e, Us);
+        last_iters = it;
         for (int t = 0; t < nt; ++t) {
             const double d = dUt[t], D = d + SM[t];
-            Ubar[t] = Ubar[t] + dt * U[t] + dt / 3.0 * D + dt * dt / 6.0 * V[t];
+            if (!newmark) Ubar[t] = Ubar[t] + dt * U[t] + dt / 3.0 * D + dt * dt / 6.0 * V[t];
             U[t] += D;
             A[t] = 4.0 / dt / dt * d - 4.0 / dt * V[t] - A[t];
             V[t] = 2.0 / dt * d - V[t];
@@ -1558,16 +1630,23 @@ int oracle_newmark_run(const svl_model_desc* model, const svl_load_desc* loads, 
     return 0;
 }
 
-/* ExtendedNewmarkBeta + Linear with PML elements (dense LDL^T solve). */
+/* ExtendedNewmarkBeta (newmark 0) or NewmarkBeta (newmark 1: the effective
+ * force with the increment terms, K + 4/dt^2 M + 2/dt C, the support-motion
+ * increment of step k - 1, no PML history; NewmarkBeta.cpp:117-235) on models
+ * with PML elements (dense LDL^T solve): algo 0 Linear, 1 Newton with test 5,
+ * 2 Newton with test 4; step_iters [nsteps] or NULL. */
 int oracle_xnewmark_run(const svl_model_desc* model, const svl_load_desc* loads, double dt, int k_first, int nsteps,
-                        double* hist_U, double* U_out, double* V_out, double* A_out, double* Ubar_out) {
+                        int algo, int maxit, double cnvgtol, int newmark,
+                        double* hist_U, double* U_out, double* V_out, double* A_out, double* Ubar_out, int* step_iters) {
     XNewmark x;
+    x.newmark = newmark != 0;
     if (!x.init(model, loads, dt)) return SVL_ERR_INVALID;
     x.set_initial(nullptr, nullptr, nullptr, nullptr);
     const int nt = x.s.m.ntotal;
     for (int i = 0; i < nsteps; ++i) {
-        int st = x.step(k_first + i);
+        int st = x.step(k_first + i, algo, algo == 0 ? 1 : maxit, cnvgtol);
         if (st) return st;
+        if (step_iters) step_iters[i] = x.last_iters;
         if (hist_U) std::memcpy(hist_U + (size_t)i * nt, x.U.data(), sizeof(double) * nt);
     }
     if (U_out) std::memcpy(U_out, x.U.data(), sizeof(double) * nt);

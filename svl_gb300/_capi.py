@@ -95,7 +95,13 @@ class NmOpts(C.Structure):
 
 class XnmOpts(C.Structure):
     _fields_ = [("dt", C.c_double), ("ftol", C.c_double), ("mtol", C.c_double), ("tol", C.c_double),
-                ("maxit", C.c_int32), ("reserved", C.c_int32 * 3)]
+                ("maxit", C.c_int32), ("algorithm", C.c_int32), ("newton_maxit", C.c_int32),
+                ("cnvgtest", C.c_int32), ("cnvgtol", C.c_double), ("integrator", C.c_int32),
+                ("reserved", C.c_int32)]
+
+
+SVL_XNM_EXTENDED_NEWMARK = 0
+SVL_XNM_NEWMARK = 1
 
 
 class NnTrainOpts(C.Structure):
@@ -167,6 +173,7 @@ def lib():
     L.svl_xnm_run.argtypes = [C.c_void_p, C.c_int32, C.c_int32, f64p]
     L.svl_xnm_get.argtypes = [C.c_void_p, C.c_int32, f64p]
     L.svl_xnm_stats.argtypes = [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_double)]
+    L.svl_xnm_newton_stats.argtypes = [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_double)]
     L.svl_xnm_destroy.argtypes = [C.c_void_p]
     L.svl_xnm_destroy.restype = None
     L.svl_nm_create.argtypes = [C.POINTER(ModelDesc), C.POINTER(LoadDesc), C.POINTER(NmOpts), C.POINTER(C.c_void_p)]

@@ -6,11 +6,15 @@
 // application runs the element kernels on the vector and gathers the element
 // vectors per total dof in element-tag order (an inverse connectivity, no
 // atomics), so each total-dof sum has the reference's summation order.
-//   solid elements (lin2DQuad4 / lin3DHexa8, elastic, lumped mass):
-//     y_e = K_e (xK + cK2 ak_e xK2) + diag(m_e) (sM xM + cM2 am_e xM2)
-//     with C_e = am_e M_e + ak_e K_e (Rayleigh with the initial stiffness,
-//     which is K_e for an elastic material);
+//   solid elements (lin2DQuad4 / lin3DHexa8, elastic or J2, lumped mass):
+//     y_e = K_e xK + ak_e K0_e (cK2 xK2) + diag(m_e) (sM xM + cM2 am_e xM2)
+//     with K_e the tangent (stored at each J2 return mapping) and
+//     C_e = am_e M_e + ak_e K0_e (Rayleigh with the initial stiffness);
 //   PML elements: svl::pml_action_launch (svl_pml.cu) in gather mode.
+// The solid element states and internal forces are updated by k_xstate from
+// U + T dU after every solve (Algorithm::UpdateStatesIncrements); the next
+// effective force reads the stored forces.  NewtonRaphson iterations repeat
+// force, tangent solve and state update with the accumulated dU.
 // With PML the effective matrix is symmetric indefinite (negative stress
 // blocks of M), so the solve is MINRES (Paige & Saunders 1975) with the SPD
 // preconditioner |diag(Keff)|^-1, restarted from its iterate until the true
@@ -25,6 +29,7 @@
 #include <cuda_runtime.h>
 
 #include "svl_internal.hpp"
+#include "svl_j2.cuh"
 
 using namespace svl;
 
@@ -47,7 +52,9 @@ struct XSolid {
     const int32_t* edof;     // [n][NC]
     const int32_t* egeo;     // [n] geometry class
     const double* geo;       // [ngeo][ngp][NEN*ND + 1]  dN/dx and w t |J|
-    const double* coef;      // [n][3] c1 c2 c3
+    const double* coef;      // [n][3] c1 c2 c3 of the initial elastic tangent
+    const int32_t* kind;     // [n] 1 for a J2 element, or null (all elastic)
+    const double* ctan;      // [NS*NS][ngp][n] J2 tangents of the last update
     const double* ray;       // [n][2] am ak, or null
     const double* mlump;     // [n][NEN] row-sum lumped mass per element node
     const double *xK, *xK2, *xM, *xM2;   // total-dof inputs (null = 0)
@@ -56,6 +63,193 @@ struct XSolid {
     double* y;               // [n][NC]
 };
 
+// Strain (engineering shear) of the element vector u at one Gauss point.
+template <int ND, int NEN>
+__device__ __forceinline__ void xstrain(const double (&b)[NEN][3], const double* u, double ev[6]) {
+#pragma unroll
+    for (int i = 0; i < 6; ++i) ev[i] = 0.0;
+#pragma unroll
+    for (int a = 0; a < NEN; ++a) {
+        if (ND == 2) {
+            ev[0] += b[a][0] * u[2 * a];
+            ev[1] += b[a][1] * u[2 * a + 1];
+            ev[2] += b[a][1] * u[2 * a] + b[a][0] * u[2 * a + 1];
+        } else {
+            const double ux = u[3 * a], uy = u[3 * a + 1], uz = u[3 * a + 2];
+            ev[0] += b[a][0] * ux;
+            ev[1] += b[a][1] * uy;
+            ev[2] += b[a][2] * uz;
+            ev[3] += b[a][1] * ux + b[a][0] * uy;
+            ev[4] += b[a][2] * uy + b[a][1] * uz;
+            ev[5] += b[a][2] * ux + b[a][0] * uz;
+        }
+    }
+}
+// y += w B^T sig (sig in the strain's order: 2D xx yy xy, 3D xx yy zz xy yz zx)
+template <int ND, int NEN>
+__device__ __forceinline__ void xbts(const double (&b)[NEN][3], double w, const double sig[6], double* y) {
+#pragma unroll
+    for (int a = 0; a < NEN; ++a) {
+        if (ND == 2) {
+            y[2 * a] += w * (b[a][0] * sig[0] + b[a][1] * sig[2]);
+            y[2 * a + 1] += w * (b[a][1] * sig[1] + b[a][0] * sig[2]);
+        } else {
+            const double bx = b[a][0], by = b[a][1], bz = b[a][2];
+            y[3 * a] += w * (bx * sig[0] + by * sig[3] + bz * sig[5]);
+            y[3 * a + 1] += w * (by * sig[1] + bx * sig[3] + bz * sig[4]);
+            y[3 * a + 2] += w * (bz * sig[2] + by * sig[4] + bx * sig[5]);
+        }
+    }
+}
+// sig = C0 ev with the elastic coefficients c1 c2 c3
+template <int ND>
+__device__ __forceinline__ void xelastic(double c1, double c2, double c3, const double ev[6], double sig[6]) {
+    if (ND == 2) {
+        sig[0] = c1 * ev[0] + c2 * ev[1];
+        sig[1] = c2 * ev[0] + c1 * ev[1];
+        sig[2] = c3 * ev[2];
+        sig[3] = sig[4] = sig[5] = 0.0;
+    } else {
+        sig[0] = c1 * ev[0] + c2 * ev[1] + c2 * ev[2];
+        sig[1] = c2 * ev[0] + c1 * ev[1] + c2 * ev[2];
+        sig[2] = c2 * ev[0] + c2 * ev[1] + c1 * ev[2];
+        sig[3] = c3 * ev[3]; sig[4] = c3 * ev[4]; sig[5] = c3 * ev[5];
+    }
+}
+
+// Operator action of one J2 element: the stored tangent on xK, the initial
+// elastic tangent on the stiffness-proportional damping input, lumped mass.
+template <int ND, int NEN>
+__device__ void xsolid_j2(const XSolid& S, int e, double ak, double am) {
+    constexpr int NC = ND * NEN, PER = NEN * ND + 1, NS = ND == 2 ? 3 : 6;
+    const int32_t* ed = S.edof + (size_t)e * NC;
+    double u1[NC], u2[NC], y[NC];
+#pragma unroll
+    for (int j = 0; j < NC; ++j) {
+        const int t = ed[j];
+        u1[j] = S.xK ? S.xK[t] : 0.0;
+        u2[j] = (S.xK2 && S.cK2 != 0.0) ? S.cK2 * ak * S.xK2[t] : 0.0;
+        y[j] = 0.0;
+    }
+    const double c1 = S.coef[3 * e], c2 = S.coef[3 * e + 1], c3 = S.coef[3 * e + 2];
+    const double* g0 = S.geo + (size_t)S.egeo[e] * S.ngp * PER;
+    const size_t cs = (size_t)S.ngp * S.n;
+    for (int q = 0; q < S.ngp; ++q) {
+        const double* g = g0 + q * PER;
+        double b[NEN][3];
+#pragma unroll
+        for (int a = 0; a < NEN; ++a)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) b[a][j] = (j < ND) ? g[a * ND + j] : 0.0;
+        const double w = g[PER - 1];
+        double e1[6], e2[6], sig[6];
+        xstrain<ND, NEN>(b, u1, e1);
+        xstrain<ND, NEN>(b, u2, e2);
+        xelastic<ND>(c1, c2, c3, e2, sig);
+        const double* ct = S.ctan + (size_t)q * S.n + e;
+#pragma unroll
+        for (int a = 0; a < NS; ++a) {
+            double v = 0.0;
+#pragma unroll
+            for (int bb = 0; bb < NS; ++bb) v += ct[(size_t)(a * NS + bb) * cs] * e1[bb];
+            sig[a] += v;
+        }
+        xbts<ND, NEN>(b, w, sig, y);
+    }
+    if (S.xM || S.xM2) {
+        const double* ml = S.mlump + (size_t)e * NEN;
+#pragma unroll
+        for (int j = 0; j < NC; ++j) {
+            const int t = ed[j];
+            double v = S.xM ? S.sM * S.xM[t] : 0.0;
+            if (S.xM2 && S.cM2 != 0.0) v += S.cM2 * am * S.xM2[t];
+            y[j] += ml[j / ND] * v;
+        }
+    }
+    double* out = S.y + (size_t)e * NC;
+#pragma unroll
+    for (int j = 0; j < NC; ++j) {
+        double v = y[j];
+        if (S.ftol >= 0.0 && !(fabs(v) > S.ftol)) v = 0.0;
+        v *= S.yscale;
+        out[j] = S.accumulate ? out[j] + v : v;
+    }
+}
+
+// Element::UpdateState from the strain displacement Us for every solid
+// element (elastic: sigma = C eps; J2: the return mapping in place on the
+// Gauss-point state, storing the consistent tangent), then the internal force
+// B^T sigma with the assembler's force tolerance (Assembler.cpp:262).
+struct XState {
+    int n, ngp;
+    const int32_t* edof; const int32_t* egeo; const double* geo; const double* coef;
+    const int32_t* kind;     // [n] or null
+    const double* j2p;       // [n][5] K G H beta SY
+    double* state;           // [13][ngp][n]
+    double* ctan;            // [NS*NS][ngp][n]
+    const double* Us;
+    double ftol;
+    double* fint;            // [n][NC]
+};
+
+template <int ND, int NEN>
+__global__ void __launch_bounds__(128) k_xstate(XState S) {
+    constexpr int NC = ND * NEN, PER = NEN * ND + 1;
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= S.n) return;
+    const int32_t* ed = S.edof + (size_t)e * NC;
+    double ue[NC], fe[NC];
+#pragma unroll
+    for (int j = 0; j < NC; ++j) { ue[j] = S.Us[ed[j]]; fe[j] = 0.0; }
+    const bool j2 = S.kind && S.kind[e];
+    const double c1 = S.coef[3 * e], c2 = S.coef[3 * e + 1], c3 = S.coef[3 * e + 2];
+    const double* g0 = S.geo + (size_t)S.egeo[e] * S.ngp * PER;
+    const size_t gs = (size_t)S.ngp * S.n;
+    for (int q = 0; q < S.ngp; ++q) {
+        const double* g = g0 + q * PER;
+        double b[NEN][3];
+#pragma unroll
+        for (int a = 0; a < NEN; ++a)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) b[a][j] = (j < ND) ? g[a * ND + j] : 0.0;
+        const double w = g[PER - 1];
+        double ev[6], sig[6];
+        xstrain<ND, NEN>(b, ue, ev);
+        if (!j2) {
+            xelastic<ND>(c1, c2, c3, ev, sig);
+        } else {
+            const double* p = S.j2p + (size_t)e * 5;
+            double st[kJ2State];
+            double* sp = S.state + (size_t)q * S.n + e;
+#pragma unroll
+            for (int i = 0; i < kJ2State; ++i) st[i] = sp[(size_t)i * gs];
+            double s6[6];
+            if (ND == 2) {
+                const double Ev[6] = {0.0, ev[0], ev[1], 0.0, 0.5 * ev[2], 0.0};
+                j2_return<2>(Ev, st, p[0], p[1], p[2], p[3], p[4], s6, S.ctan + (size_t)q * S.n + e, gs);
+                sig[0] = s6[1]; sig[1] = s6[2]; sig[2] = s6[4];
+                sig[3] = sig[4] = sig[5] = 0.0;
+            } else {
+                const double Ev[6] = {ev[0], ev[1], ev[2], 0.5 * ev[3], 0.5 * ev[4], 0.5 * ev[5]};
+                j2_return<3>(Ev, st, p[0], p[1], p[2], p[3], p[4], s6, S.ctan + (size_t)q * S.n + e, gs);
+#pragma unroll
+                for (int i = 0; i < 6; ++i) sig[i] = s6[i];
+            }
+#pragma unroll
+            for (int i = 0; i < kJ2State; ++i) sp[(size_t)i * gs] = st[i];
+        }
+        xbts<ND, NEN>(b, w, sig, fe);
+    }
+    double* out = S.fint + (size_t)e * NC;
+#pragma unroll
+    for (int j = 0; j < NC; ++j) out[j] = (fabs(fe[j]) > S.ftol) ? fe[j] : 0.0;
+}
+
+__global__ void k_xneg(size_t n, const double* __restrict__ a, double* __restrict__ out) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = -a[i];
+}
+
 template <int ND, int NEN>
 __global__ void __launch_bounds__(128) k_xsolid(XSolid S) {
     constexpr int NC = ND * NEN, PER = NEN * ND + 1;
@@ -63,6 +257,10 @@ __global__ void __launch_bounds__(128) k_xsolid(XSolid S) {
     if (e >= S.n) return;
     const int32_t* ed = S.edof + (size_t)e * NC;
     const double am = S.ray ? S.ray[2 * e] : 0.0, ak = S.ray ? S.ray[2 * e + 1] : 0.0;
+    if (S.kind && S.kind[e]) {
+        xsolid_j2<ND, NEN>(S, e, ak, am);
+        return;
+    }
     double uk[NC], y[NC];
 #pragma unroll
     for (int j = 0; j < NC; ++j) {
@@ -323,7 +521,7 @@ __global__ void k_xsm(int ntotal, const int32_t* sm_ptr, const int32_t* sm_ser, 
         const int b = s_ptr[s], n = s_ptr[s + 1] - b;
         double g = 0.0;
         if (n > 0) {
-            g = k < n ? s_val[b + k] : s_val[b];
+            g = (k >= 0 && k < n) ? s_val[b + k] : s_val[b];
             if (k > 0) g -= (k - 1 < n ? s_val[b + k - 1] : s_val[b]);
         }
         v += sm_fac[i] * g;
@@ -340,14 +538,24 @@ __global__ void k_xrhs_vec(int n, const double* U, const double* V, const double
     Wg[t] = Ub[t] + dt * U[t] + dt * dt / 6.0 * V[t];
 }
 
-// ExtendedNewmarkBeta::ComputeNewStep state update (dUt = T du, sm = SM(k))
+// NewmarkBeta: W = 4/dt V + A - 4/dt^2 dU and Vd = V - 2/dt dU (NewmarkBeta.cpp:215)
+__global__ void k_xrhs_nm(int n, const double* V, const double* A, const double* dUt, double dt, double* W,
+                          double* Vd) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    W[t] = 4.0 / dt * V[t] + A[t] - 4.0 / dt / dt * dUt[t];
+    Vd[t] = V[t] - 2.0 / dt * dUt[t];
+}
+
+// ExtendedNewmarkBeta::ComputeNewStep state update (dUt = T du, sm = SM(k));
+// NewmarkBeta's (no PML history) with pml_hist = 0
 __global__ void k_xupdate(int n, double* U, double* V, double* A, double* Ub, double* Us, const double* dUt,
-                          const double* sm, double dt, int* bad) {
+                          const double* sm, double dt, int pml_hist, int* bad) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n) return;
     const double d = dUt[t], D = d + (sm ? sm[t] : 0.0);
     const double u = U[t], v = V[t];
-    Ub[t] = Ub[t] + dt * u + dt / 3.0 * D + dt * dt / 6.0 * v;
+    if (pml_hist) Ub[t] = Ub[t] + dt * u + dt / 3.0 * D + dt * dt / 6.0 * v;
     Us[t] = u + d;                       // solid strain displacement: U + T du
     const double un = u + D;
     U[t] = un;
@@ -383,6 +591,10 @@ __global__ void k_xdot_final(const double* __restrict__ partial, double* out) {
     }
 }
 
+__global__ void k_xadd(int n, const double* a, const double* b, double* out) {       // out = a + b
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = a[i] + b[i];
+}
 __global__ void k_xaxpby(int n, double a, const double* x, double b, double* y) {   // y = a x + b y
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) y[i] = a * x[i] + b * y[i];
@@ -424,8 +636,10 @@ struct svl_xnm {
     std::vector<void*> allocs;
     int nsol = 0, npml = 0, ncs = 0, ncp = 0;
     // solid elements
-    int32_t *s_edof = nullptr, *s_egeo = nullptr;
+    int32_t *s_edof = nullptr, *s_egeo = nullptr, *s_kind = nullptr;
     double *s_geo = nullptr, *s_coef = nullptr, *s_ray = nullptr, *s_mlump = nullptr;
+    double *s_j2p = nullptr, *s_state = nullptr, *s_ctan = nullptr, *s_fint = nullptr;
+    bool has_j2 = false, newton = false;
     // PML elements
     double *p_X = nullptr, *p_mat = nullptr, *p_thick = nullptr, *p_par = nullptr;
     int32_t* p_edof = nullptr;
@@ -450,13 +664,17 @@ struct svl_xnm {
     // state (total dofs) and scratch
     double *U = nullptr, *V = nullptr, *A = nullptr, *Ub = nullptr, *Us = nullptr;
     double *W = nullptr, *Wg = nullptr, *yt = nullptr, *ys = nullptr, *pt = nullptr, *sm = nullptr, *dUt = nullptr;
+    double* Ui = nullptr;                    // U + T dU: the PML elements' displacement
+    bool newmark = false;                    // NewmarkBeta instead of ExtendedNewmarkBeta
     // free-dof vectors
-    double *b = nullptr, *x = nullptr, *r1 = nullptr, *r2 = nullptr, *yv = nullptr, *v = nullptr;
+    double *b = nullptr, *x = nullptr, *dUf = nullptr, *r1 = nullptr, *r2 = nullptr, *yv = nullptr, *v = nullptr;
     double *w = nullptr, *w1 = nullptr, *w2 = nullptr, *dinv = nullptr, *tmp = nullptr;
     double *partial = nullptr, *scal = nullptr;
     int* bad = nullptr;
     int64_t iters_total = 0, iters_last = 0;
     double res_last = 0.0;
+    int64_t newton_total = 0, newton_last = 0;
+    double newton_res = 0.0;
 
     ~svl_xnm() {
         if (stream) cudaStreamSynchronize(stream);
@@ -505,9 +723,23 @@ int x_gather(svl_xnm* X, double* y, double cn, const double* xn, double cdp, con
 XSolid solid_args(svl_xnm* X) {
     XSolid S{};
     S.n = X->nsol; S.ngp = X->m.ngp; S.edof = X->s_edof; S.egeo = X->s_egeo; S.geo = X->s_geo;
-    S.coef = X->s_coef; S.ray = X->s_ray; S.mlump = X->s_mlump; S.ftol = -1.0; S.yscale = 1.0;
+    S.coef = X->s_coef; S.kind = X->s_kind; S.ctan = X->s_ctan;
+    S.ray = X->s_ray; S.mlump = X->s_mlump; S.ftol = -1.0; S.yscale = 1.0;
     S.y = X->fe;
     return S;
+}
+// solid element states and filtered internal forces from X->Us
+int x_state(svl_xnm* X) {
+    if (X->nsol <= 0) return SVL_OK;
+    XState S{};
+    S.n = X->nsol; S.ngp = X->m.ngp; S.edof = X->s_edof; S.egeo = X->s_egeo; S.geo = X->s_geo;
+    S.coef = X->s_coef; S.kind = X->s_kind; S.j2p = X->s_j2p; S.state = X->s_state; S.ctan = X->s_ctan;
+    S.Us = X->Us; S.ftol = X->opts.ftol; S.fint = X->s_fint;
+    const int g = (S.n + 127) / 128;
+    if (X->m.ndim == 2) k_xstate<2, 4><<<g, 128, 0, X->stream>>>(S);
+    else k_xstate<3, 8><<<g, 128, 0, X->stream>>>(S);
+    XCUDA(cudaGetLastError());
+    return SVL_OK;
 }
 PmlArgs pml_args(svl_xnm* X) {
     PmlArgs P{};
@@ -531,7 +763,7 @@ int x_op_total(svl_xnm* X, const double* p, double* out) {
     S.xK = p; S.xK2 = p; S.cK2 = cc; S.xM = p; S.sM = cm; S.xM2 = p; S.cM2 = cc;
     XTRY(launch_solid(X, S));
     PmlArgs P = pml_args(X);
-    P.coef[0] = cm; P.coef[1] = cc; P.coef[2] = 1.0; P.coef[3] = X->m.ndim == 3 ? dt / 3.0 : 0.0;
+    P.coef[0] = cm; P.coef[1] = cc; P.coef[2] = 1.0; P.coef[3] = (X->m.ndim == 3 && !X->newmark) ? dt / 3.0 : 0.0;
     for (int i = 0; i < 4; ++i) P.u[i] = p;
     XTRY(pml_action_launch(X->m.ndim, P, X->stream));
     return x_gather(X, out, cm, p, cc, p, 0, false);
@@ -647,28 +879,59 @@ int x_solve(svl_xnm* X) {
     return SVL_OK;
 }
 
-// One ExtendedNewmarkBeta step k with the Linear algorithm.
-int x_step(svl_xnm* X, int k) {
+// ExtendedNewmarkBeta (ExtendedNewmarkBeta.cpp:208-229, 190-204):
+//   b = T^T (Fext - Fint - G Wg + C V + M W) - T^T (Keff SM),
+//   W = 4/dt V + A, Wg = Ubar + dt U + dt^2/6 V (set once per step);
+// NewmarkBeta (NewmarkBeta.cpp:180-235):
+//   b = T^T (Fext - Fint + M W + C Vd) - T^T (Keff SM),
+//   W = 4/dt V + A - 4/dt^2 dU, Vd = V - 2/dt dU (set here, in Wg).
+// Fint of the solid elements from their stored forces, of the PML elements
+// K_e (U + T dU) (PML3DHexa8.cpp:716-742 with the node increments of the
+// iterate); dUt, SM and the DRM forces of the step must be in place.
+int x_rhs(svl_xnm* X, int k) {
     const HostModel& m = X->m;
     const int nt = m.ntotal, gt = grid_of(nt);
     const double dt = X->opts.dt;
-    k_xrhs_vec<<<gt, 256, 0, X->stream>>>(nt, X->U, X->V, X->A, X->Ub, dt, X->W, X->Wg);
-    // solid: -Fint(Us) filtered, then + K (ak V) + M (W + am V)
+    if (X->newmark) k_xrhs_nm<<<gt, 256, 0, X->stream>>>(nt, X->V, X->A, X->dUt, dt, X->W, X->Wg);
+    const double* vd = X->newmark ? X->Wg : X->V;
+    const size_t ns = (size_t)X->nsol * X->ncs;
+    if (ns > 0) k_xneg<<<(unsigned)((ns + 255) / 256), 256, 0, X->stream>>>(ns, X->s_fint, X->fe);
     XSolid S = solid_args(X);
-    S.xK = X->Us; S.ftol = X->opts.ftol; S.yscale = -1.0;
+    S.xK2 = vd; S.cK2 = 1.0; S.xM = X->W; S.sM = 1.0; S.xM2 = vd; S.cM2 = 1.0; S.accumulate = 1;
     XTRY(launch_solid(X, S));
-    S = solid_args(X);
-    S.xK2 = X->V; S.cK2 = 1.0; S.xM = X->W; S.sM = 1.0; S.xM2 = X->V; S.cM2 = 1.0; S.accumulate = 1;
-    XTRY(launch_solid(X, S));
-    // PML: -Fint(U) filtered, then + M W + C V - G Wg
-    PmlArgs P = pml_args(X);
-    P.coef[2] = 1.0; P.u[2] = X->U; P.ftol = X->opts.ftol; P.yscale = -1.0;
-    XTRY(pml_action_launch(m.ndim, P, X->stream));
-    P = pml_args(X);
-    P.coef[0] = 1.0; P.u[0] = X->W; P.coef[1] = 1.0; P.u[1] = X->V;
-    if (m.ndim == 3) { P.coef[3] = -1.0; P.u[3] = X->Wg; }
-    P.accumulate = 1;
-    XTRY(pml_action_launch(m.ndim, P, X->stream));
+    if (X->npml > 0) {
+        // PML: -Fint(U + T dU) filtered, then + M W + C vd (- G Wg)
+        k_xadd<<<gt, 256, 0, X->stream>>>(nt, X->U, X->dUt, X->Ui);
+        PmlArgs P = pml_args(X);
+        P.coef[2] = 1.0; P.u[2] = X->Ui; P.ftol = X->opts.ftol; P.yscale = -1.0;
+        XTRY(pml_action_launch(m.ndim, P, X->stream));
+        P = pml_args(X);
+        P.coef[0] = 1.0; P.u[0] = X->W; P.coef[1] = 1.0; P.u[1] = vd;
+        if (m.ndim == 3 && !X->newmark) { P.coef[3] = -1.0; P.u[3] = X->Wg; }
+        P.accumulate = 1;
+        XTRY(pml_action_launch(m.ndim, P, X->stream));
+    }
+    XTRY(x_gather(X, X->yt, 1.0, X->W, 1.0, vd, k, true));
+    const double* sub = nullptr;
+    if (X->lt.has_sm) {
+        XTRY(x_op_total(X, X->sm, X->ys));       // Keff (current tangent) SM
+        sub = X->ys;
+    }
+    k_xreduce<<<grid_of(m.nfree), 256, 0, X->stream>>>(m.nfree, X->TTp, X->TTr, X->TTv, X->yt, sub, X->b);
+    XCUDA(cudaGetLastError());
+    return SVL_OK;
+}
+
+// One ExtendedNewmarkBeta step k with the Linear algorithm (one iteration)
+// or NewtonRaphson (NewtonRaphson.cpp:24-75): effective force, tangent
+// solve, dU += du, convergence test (Algorithm.cpp:122-188), solid states
+// from U + T dU; then the step's state update (:123-153).
+int x_step(svl_xnm* X, int k) {
+    const HostModel& m = X->m;
+    const int nt = m.ntotal, gt = grid_of(nt), nf = m.nfree;
+    const double dt = X->opts.dt;
+    if (!X->newmark) k_xrhs_vec<<<gt, 256, 0, X->stream>>>(nt, X->U, X->V, X->A, X->Ub, dt, X->W, X->Wg);
+    XCUDA(cudaMemsetAsync(X->dUt, 0, sizeof(double) * nt, X->stream));
     if (X->ndrm > 0) {
         XDrm D{};
         D.n = X->ndrm; D.nt = X->drm_nt; D.k = k; D.ngp = m.ngp;
@@ -680,19 +943,52 @@ int x_step(svl_xnm* X, int k) {
         else k_xdrm<3, 8><<<gd, 128, 0, X->stream>>>(D);
         XCUDA(cudaGetLastError());
     }
-    XTRY(x_gather(X, X->yt, 1.0, X->W, 1.0, X->V, k, true));
-    const double* sub = nullptr;
-    if (X->lt.has_sm) {
-        k_xsm<<<gt, 256, 0, X->stream>>>(nt, X->sm_ptr, X->sm_ser, X->sm_fac, X->s_ptr, X->s_val, k, X->sm);
-        XTRY(x_op_total(X, X->sm, X->ys));
-        sub = X->ys;
+    // the support-motion increment of step k (ExtendedNewmarkBeta.cpp:196) or
+    // of step k - 1 (NewmarkBeta.cpp:187)
+    if (X->lt.has_sm)
+        k_xsm<<<gt, 256, 0, X->stream>>>(nt, X->sm_ptr, X->sm_ser, X->sm_fac, X->s_ptr, X->s_val,
+                                         X->newmark ? k - 1 : k, X->sm);
+    XCUDA(cudaMemsetAsync(X->dUf, 0, sizeof(double) * std::max(nf, 1), X->stream));
+    const int maxit = X->newton ? X->opts.newton_maxit : 1;
+    const int test = X->opts.cnvgtest;
+    double norm0 = 0.0, res = 0.0;
+    int it = 0;
+    for (;;) {
+        XTRY(x_rhs(X, k));
+        double fn = 0.0;
+        if (X->newton && test == 4) {
+            XTRY(x_dot(X, X->b, X->b, 3));
+            XTRY(x_read(X, 3, &fn));
+            fn = std::sqrt(fn);
+        }
+        XTRY(x_solve(X));
+        k_xaxpby<<<grid_of(nf), 256, 0, X->stream>>>(nf, 1.0, X->x, 1.0, X->dUf);
+        if (X->newton) {
+            if (test == 5) {
+                double dn = 0.0, Dn = 0.0;
+                XTRY(x_dot(X, X->x, X->x, 3));
+                XTRY(x_read(X, 3, &dn));
+                XTRY(x_dot(X, X->dUf, X->dUf, 4));
+                XTRY(x_read(X, 4, &Dn));
+                dn = std::sqrt(dn); Dn = std::sqrt(Dn);
+                if (it == 0) { norm0 = Dn; res = dn; } else res = dn / norm0;
+            } else {
+                if (it == 0) { norm0 = fn; res = fn; } else res = fn / norm0;
+            }
+        }
+        // UpdateStatesIncrements: solid states from U + T dU
+        k_xexpand<<<gt, 256, 0, X->stream>>>(nt, X->Tp, X->Tc, X->Tv, X->dUf, X->dUt);
+        k_xadd<<<gt, 256, 0, X->stream>>>(nt, X->U, X->dUt, X->Us);
+        XCUDA(cudaGetLastError());
+        XTRY(x_state(X));
+        ++it;
+        if (!X->newton || !(res > X->opts.cnvgtol) || it >= maxit) break;
     }
-    k_xreduce<<<grid_of(m.nfree), 256, 0, X->stream>>>(m.nfree, X->TTp, X->TTr, X->TTv, X->yt, sub, X->b);
-    XCUDA(cudaGetLastError());
-    XTRY(x_solve(X));
-    k_xexpand<<<gt, 256, 0, X->stream>>>(nt, X->Tp, X->Tc, X->Tv, X->x, X->dUt);
+    X->newton_last = it;
+    X->newton_total += it;
+    X->newton_res = res;
     k_xupdate<<<gt, 256, 0, X->stream>>>(nt, X->U, X->V, X->A, X->Ub, X->Us, X->dUt, X->lt.has_sm ? X->sm : nullptr,
-                                         dt, X->bad);
+                                         dt, X->newmark ? 0 : 1, X->bad);
     XCUDA(cudaGetLastError());
     return SVL_OK;
 }
@@ -734,7 +1030,9 @@ int x_setup(svl_xnm* X, const svl_load_desc* L) {
     }
     // solid tables
     std::vector<int32_t> s_edof((size_t)X->nsol * X->ncs), s_egeo(X->nsol);
-    std::vector<double> s_geo, s_coef((size_t)X->nsol * 3), s_ray, s_ml((size_t)X->nsol * nen);
+    std::vector<double> s_geo, s_coef((size_t)X->nsol * 3), s_ray, s_ml((size_t)X->nsol * nen),
+        s_j2p((size_t)X->nsol * 5, 0.0);
+    std::vector<int32_t> s_kind(X->nsol, 0);
     std::vector<double> diag(m.ntotal, 0.0);
     const double dt = X->opts.dt, cm = 4.0 / dt / dt, cc = 2.0 / dt;
     {
@@ -769,10 +1067,25 @@ int x_setup(svl_xnm* X, const svl_load_desc* L) {
                 for (int b2 = 0; b2 < nen; ++b2) if (b2 != a) d += mab[a][b2];
                 s_ml[(size_t)i * nen + a] = std::fabs(d) > X->opts.mtol ? d : 0.0;
             }
-            const double E = pr[0], nu = pr[1];
-            const double c1 = E * (1.0 - nu) / (1.0 - 2.0 * nu) / (1.0 + nu);
-            const double c2 = E * nu / (1.0 - 2.0 * nu) / (1.0 + nu);
-            const double c3 = E / (2.0 * (1.0 + nu));
+            double c1, c2, c3;
+            const int mt = m.mat_type(e);
+            if (mt == SVL_MAT_ELASTIC2DPLANESTRAIN || mt == SVL_MAT_ELASTIC3DLINEAR) {
+                const double E = pr[0], nu = pr[1];
+                c1 = E * (1.0 - nu) / (1.0 - 2.0 * nu) / (1.0 + nu);
+                c2 = E * nu / (1.0 - 2.0 * nu) / (1.0 + nu);
+                c3 = E / (2.0 * (1.0 + nu));
+            } else {
+                // J2 (K, G, rho, H, beta, SY): initial tangent K 1(x)1 + 2G (I - 1/3 1(x)1)
+                // with shear entries 1/2 (PlasticPlaneStrainJ2.cpp:163-180)
+                const double K = pr[0], G = pr[1];
+                c1 = K * 1.0 + 2.0 * G * (1.0 - 1.0 / 3.0);
+                c2 = K * 1.0 + 2.0 * G * (0.0 - 1.0 / 3.0);
+                c3 = 2.0 * G * 0.5;
+                s_kind[i] = 1;
+                s_j2p[5 * (size_t)i] = K; s_j2p[5 * (size_t)i + 1] = G; s_j2p[5 * (size_t)i + 2] = pr[3];
+                s_j2p[5 * (size_t)i + 3] = pr[4]; s_j2p[5 * (size_t)i + 4] = pr[5];
+                X->has_j2 = true;
+            }
             s_coef[3 * i] = c1; s_coef[3 * i + 1] = c2; s_coef[3 * i + 2] = c3;
             const double am = m.ray.empty() ? 0.0 : m.ray[2 * (size_t)e], ak = m.ray.empty() ? 0.0 : m.ray[2 * (size_t)e + 1];
             if (!s_ray.empty()) { s_ray[2 * i] = am; s_ray[2 * i + 1] = ak; }
@@ -839,6 +1152,10 @@ int x_setup(svl_xnm* X, const svl_load_desc* L) {
         for (int i = 0; i < L->ndrm; ++i) {
             const int e = L->drm_elem[i];
             if (e < 0 || e >= m.nelem || sidx_of[e] < 0) { set_error("DRM entry %d: element %d is not a solid element", i, e); return SVL_ERR_INVALID; }
+            if (s_kind[sidx_of[e]]) {
+                set_error("DRM entry %d: element %d has a J2 material (the GPU DRM forces use the elastic stiffness)", i, e);
+                return SVL_ERR_UNSUPPORTED;
+            }
             dsidx.push_back(sidx_of[e]);
             dfac.push_back(L->drm_factor[i]);
             dak.push_back(m.ray.empty() ? 0.0 : m.ray[2 * (size_t)e + 1]);
@@ -864,6 +1181,13 @@ int x_setup(svl_xnm* X, const svl_load_desc* L) {
     // uploads
     XTRY(X->upload(s_edof, &X->s_edof)); XTRY(X->upload(s_egeo, &X->s_egeo)); XTRY(X->upload(s_geo, &X->s_geo));
     XTRY(X->upload(s_coef, &X->s_coef)); XTRY(X->upload(s_ml, &X->s_mlump));
+    XTRY(X->alloc((size_t)X->nsol * X->ncs, &X->s_fint));
+    if (X->has_j2) {
+        const int ns = nd == 2 ? 3 : 6;
+        XTRY(X->upload(s_kind, &X->s_kind)); XTRY(X->upload(s_j2p, &X->s_j2p));
+        XTRY(X->alloc((size_t)kJ2State * m.ngp * X->nsol, &X->s_state));
+        XTRY(X->alloc((size_t)ns * ns * m.ngp * X->nsol, &X->s_ctan));
+    }
     if (!s_ray.empty()) XTRY(X->upload(s_ray, &X->s_ray));
     XTRY(X->upload(p_X, &X->p_X)); XTRY(X->upload(p_mat, &X->p_mat)); XTRY(X->upload(p_thick, &X->p_thick));
     XTRY(X->upload(p_par, &X->p_par)); XTRY(X->upload(p_edof, &X->p_edof));
@@ -890,9 +1214,10 @@ int x_setup(svl_xnm* X, const svl_load_desc* L) {
     XTRY(X->upload(X->lt.ld_ptr, &X->ld_ptr)); XTRY(X->upload(X->lt.ld_ser, &X->ld_ser)); XTRY(X->upload(X->lt.ld_coef, &X->ld_coef));
     XTRY(X->upload(X->lt.s_ptr, &X->s_ptr)); XTRY(X->upload(X->lt.s_val, &X->s_val));
     XTRY(X->upload(X->lt.sm_ptr, &X->sm_ptr)); XTRY(X->upload(X->lt.sm_ser, &X->sm_ser)); XTRY(X->upload(X->lt.sm_fac, &X->sm_fac));
-    double** tvec[] = {&X->U, &X->V, &X->A, &X->Ub, &X->Us, &X->W, &X->Wg, &X->yt, &X->ys, &X->pt, &X->sm, &X->dUt};
+    double** tvec[] = {&X->U, &X->V, &X->A, &X->Ub, &X->Us, &X->W, &X->Wg, &X->yt, &X->ys, &X->pt, &X->sm, &X->dUt,
+                       &X->Ui};
     for (double** p : tvec) XTRY(X->alloc((size_t)m.ntotal, p));
-    double** fvec[] = {&X->b, &X->x, &X->r1, &X->r2, &X->yv, &X->v, &X->w, &X->w1, &X->w2, &X->tmp};
+    double** fvec[] = {&X->b, &X->x, &X->dUf, &X->r1, &X->r2, &X->yv, &X->v, &X->w, &X->w1, &X->w2, &X->tmp};
     for (double** p : fvec) XTRY(X->alloc((size_t)std::max(m.nfree, 1), p));
     XTRY(X->alloc(kBlocks, &X->partial));
     XTRY(X->alloc(8, &X->scal));
@@ -905,7 +1230,7 @@ int x_setup(svl_xnm* X, const svl_load_desc* L) {
         PmlArgs P{};
         P.nelem = X->npml; P.X = X->p_X; P.mat = X->p_mat; P.thick = X->p_thick; P.par = X->p_par;
         P.edof = nullptr; P.y = yb; P.ftol = -1.0; P.yscale = 1.0;
-        P.coef[0] = cm; P.coef[1] = cc; P.coef[2] = 1.0; P.coef[3] = nd == 3 ? dt / 3.0 : 0.0;
+        P.coef[0] = cm; P.coef[1] = cc; P.coef[2] = 1.0; P.coef[3] = (nd == 3 && !X->newmark) ? dt / 3.0 : 0.0;
         for (int i = 0; i < 4; ++i) P.u[i] = ub;
         const int gu = (int)((ne + 255) / 256), ge = grid_of(X->npml);
         for (int i = 0; i < X->ncp; ++i) {
@@ -926,6 +1251,7 @@ int x_setup(svl_xnm* X, const svl_load_desc* L) {
         for (int i = Tp[t]; i < Tp[t + 1]; ++i) dfree[Tc[i]] += Tv[i] * Tv[i] * diag[t];
     for (double& d : dfree) d = std::fabs(d) > 0.0 ? 1.0 / std::fabs(d) : 1.0;
     XTRY(X->upload(dfree, &X->dinv));
+    XTRY(x_state(X));                         // Us = 0: zero forces, initial tangents
     XCUDA(cudaStreamSynchronize(X->stream));
     return SVL_OK;
 }
@@ -938,13 +1264,28 @@ int svl_xnm_create(const svl_model_desc* model, const svl_load_desc* loads, cons
     if (!out || !opts) { set_error("NULL argument"); return SVL_ERR_INVALID; }
     *out = nullptr;
     if (!(opts->dt > 0.0) || !(opts->tol > 0.0) || opts->maxit <= 0) { set_error("bad ExtendedNewmark options"); return SVL_ERR_INVALID; }
+    if (opts->algorithm != SVL_ALGO_LINEAR && opts->algorithm != SVL_ALGO_NEWTON) { set_error("unknown algorithm %d", opts->algorithm); return SVL_ERR_INVALID; }
+    if (opts->algorithm == SVL_ALGO_NEWTON &&
+        (opts->newton_maxit <= 0 || (opts->cnvgtest != 4 && opts->cnvgtest != 5) || !(opts->cnvgtol >= 0.0))) {
+        set_error("Newton needs newton_maxit > 0, cnvgtest 4 or 5 and cnvgtol >= 0"); return SVL_ERR_INVALID;
+    }
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) { set_error("no CUDA device available"); return SVL_ERR_NODEVICE; }
     svl_xnm* X = new svl_xnm();
     X->opts = *opts;
     auto fail = [&](int st) { delete X; return st; };
     if (!model_from_desc(model, X->m)) return fail(SVL_ERR_INVALID);
-    if (X->m.has_j2()) { set_error("the ExtendedNewmark path covers elastic solid materials"); return fail(SVL_ERR_UNSUPPORTED); }
+    X->newton = opts->algorithm == SVL_ALGO_NEWTON;
+    if (opts->integrator != SVL_XNM_EXTENDED_NEWMARK && opts->integrator != SVL_XNM_NEWMARK) {
+        set_error("unknown integrator %d", opts->integrator); return fail(SVL_ERR_INVALID);
+    }
+    X->newmark = opts->integrator == SVL_XNM_NEWMARK;
+    for (int e = 0; X->m.has_pml() && e < X->m.nelem; ++e) {
+        const int t = X->m.mat_type(e);
+        if (X->m.epml[e] && t != SVL_MAT_ELASTIC2DPLANESTRAIN && t != SVL_MAT_ELASTIC3DLINEAR) {
+            set_error("PML element %d needs an elastic material", e); return fail(SVL_ERR_INVALID);
+        }
+    }
     if (!X->m.lumped) { set_error("the ExtendedNewmark path needs a lumped mass for the solid elements"); return fail(SVL_ERR_UNSUPPORTED); }
     if ((int64_t)X->m.nelem * X->m.nen * X->m.pml_ndof() > ((int64_t)1 << 40)) { set_error("model too large"); return fail(SVL_ERR_UNSUPPORTED); }
     if (cudaStreamCreateWithFlags(&X->stream, cudaStreamNonBlocking) != cudaSuccess) { set_error("cudaStreamCreate failed"); return fail(SVL_ERR_CUDA); }
@@ -964,6 +1305,7 @@ int svl_xnm_set_initial(svl_xnm* X, const double* U0, const double* V0, const do
         else XCUDA(cudaMemsetAsync(dst[i], 0, bytes, X->stream));
     }
     XCUDA(cudaMemcpyAsync(X->Us, X->U, bytes, cudaMemcpyDeviceToDevice, X->stream));
+    XTRY(x_state(X));                         // element states from U0 (oracle: UpdateState + commit)
     XCUDA(cudaStreamSynchronize(X->stream));
     return SVL_OK;
 }
@@ -995,6 +1337,14 @@ int svl_xnm_stats(svl_xnm* X, int64_t* iters_total, int64_t* iters_last, double*
     if (iters_total) *iters_total = X->iters_total;
     if (iters_last) *iters_last = X->iters_last;
     if (res_last) *res_last = X->res_last;
+    return SVL_OK;
+}
+
+int svl_xnm_newton_stats(svl_xnm* X, int64_t* iters_total, int64_t* iters_last, double* residual_last) {
+    if (!X) { set_error("NULL handle"); return SVL_ERR_INVALID; }
+    if (iters_total) *iters_total = X->newton_total;
+    if (iters_last) *iters_last = X->newton_last;
+    if (residual_last) *residual_last = X->newton_res;
     return SVL_OK;
 }
 

@@ -69,6 +69,14 @@ private:
     int ntotal_ = 0;
 };
 
+// NewtonRaphson(solver, mesh, cnvgtol, nstep, cnvgtest) as the Driver builds it
+// (RP/12-Utilities/Driver.hpp:1791-1795); integrators given none use Linear.
+struct NewtonRaphson {
+    double cnvgtol = 1e-6;
+    int nstep = 50;
+    int cnvgtest = 4;
+};
+
 // NewmarkBeta(mesh, dt, mtol, ktol, ftol) with the Linear algorithm and an
 // iterative LinearSystem (RP/10-Integrators/03-Newmark/NewmarkBeta.cpp:6-141,
 // RP/11-Solvers/02-Iterative/PetscSolver.cc:16-150): the effective-stiffness
@@ -77,7 +85,7 @@ private:
 class NewmarkBeta {
 public:
     NewmarkBeta(const svl_model_desc& model, const svl_load_desc& loads, double dt, double tol = 1e-8,
-                double mtol = 1e-12, double ftol = 1e-12, int maxit = 20000)
+                double mtol = 1e-12, double ftol = 1e-12, int maxit = 20000, const NewtonRaphson* newton = nullptr)
         : ntotal_(model.ntotal) {
         svl_nm_opts o{};
         o.dt = dt;
@@ -86,6 +94,13 @@ public:
         o.pcg_tol = tol;
         o.pcg_maxit = maxit;
         o.precond = SVL_PRECOND_JACOBI;
+        o.algorithm = SVL_ALGO_LINEAR;
+        if (newton) {
+            o.algorithm = SVL_ALGO_NEWTON;
+            o.maxit = newton->nstep;
+            o.cnvgtol = newton->cnvgtol;
+            o.cnvgtest = newton->cnvgtest;
+        }
         check(svl_nm_create(&model, &loads, &o, &h_));
     }
     ~NewmarkBeta() { svl_nm_destroy(h_); }
@@ -126,14 +141,16 @@ private:
     int ntotal_ = 0;
 };
 
-// ExtendedNewmarkBeta(mesh, dt, mtol, ktol, ftol) with the Linear algorithm
-// (RP/10-Integrators/03-Newmark/ExtendedNewmarkBeta.cpp:37-245) for meshes with
-// PML2DQuad4 / PML3DHexa8 layers: the effective-stiffness solve is
-// matrix-free MINRES on the GPU to a relative residual `tol` (|diag|^-1 norm).
+// ExtendedNewmarkBeta(mesh, dt, mtol, ktol, ftol) with the Linear algorithm or
+// NewtonRaphson (RP/10-Integrators/03-Newmark/ExtendedNewmarkBeta.cpp:37-245)
+// for meshes with PML2DQuad4 / PML3DHexa8 layers and elastic or J2 solids: the
+// effective-stiffness solve is matrix-free MINRES on the GPU to a relative
+// residual `tol` (|diag|^-1 norm).
 class ExtendedNewmarkBeta {
 public:
     ExtendedNewmarkBeta(const svl_model_desc& model, const svl_load_desc& loads, double dt, double tol = 1e-10,
-                        double mtol = 1e-12, double ftol = 1e-12, int maxit = 100000)
+                        double mtol = 1e-12, double ftol = 1e-12, int maxit = 100000,
+                        const NewtonRaphson* newton = nullptr)
         : ntotal_(model.ntotal) {
         svl_xnm_opts o{};
         o.dt = dt;
@@ -141,6 +158,13 @@ public:
         o.mtol = mtol;
         o.tol = tol;
         o.maxit = maxit;
+        o.algorithm = SVL_ALGO_LINEAR;
+        if (newton) {
+            o.algorithm = SVL_ALGO_NEWTON;
+            o.newton_maxit = newton->nstep;
+            o.cnvgtol = newton->cnvgtol;
+            o.cnvgtest = newton->cnvgtest;
+        }
         check(svl_xnm_create(&model, &loads, &o, &h_));
     }
     ~ExtendedNewmarkBeta() { svl_xnm_destroy(h_); }

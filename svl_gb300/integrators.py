@@ -172,19 +172,30 @@ class StructuredCentralDifference:
 
 class ExtendedNewmarkBeta:
     """ExtendedNewmarkBeta (RP/10-Integrators/03-Newmark/ExtendedNewmarkBeta.cpp)
-    with the Linear algorithm for meshes with PML2DQuad4 / PML3DHexa8 layers
-    (svl_xnm_*): the PML history term G (Ubar + dt U + dt^2/6 V), Rayleigh and
-    PML damping, support motion of step k, and a matrix-free MINRES solve of
-    the symmetric indefinite effective matrix to the relative true residual
-    `tol` in the |diag|^-1 norm.  GetPMLHistoryVector returns Ubar."""
+    for meshes with PML2DQuad4 / PML3DHexa8 layers and elastic or J2 solid
+    elements (svl_xnm_*): the PML history term G (Ubar + dt U + dt^2/6 V),
+    Rayleigh and PML damping, support motion of step k, and a matrix-free
+    MINRES solve of the symmetric indefinite effective matrix to the relative
+    true residual `tol` in the |diag|^-1 norm (at most `solver_maxit`
+    iterations).  algorithm "linear" (Linear.cpp) or "newton"
+    (NewtonRaphson.cpp with `maxit` iterations, tolerance `cnvgtol`, test
+    `cnvgtest`).  GetPMLHistoryVector returns Ubar."""
 
-    def __init__(self, model: Model, loads: Loads | None, dt: float, tol: float = 1e-10, maxit: int = 100000,
-                 ftol: float = 1e-12, mtol: float = 1e-12):
+    def __init__(self, model: Model, loads: Loads | None, dt: float, tol: float = 1e-10,
+                 solver_maxit: int = 100000, ftol: float = 1e-12, mtol: float = 1e-12, algorithm: str = "linear",
+                 maxit: int = 50, cnvgtol: float = 1e-6, cnvgtest: int = 4, integrator: str = "extendednewmark"):
+        """integrator "extendednewmark" (ExtendedNewmarkBeta.cpp) or "newmark"
+        (NewmarkBeta.cpp on the same elements: the PML history matrix is not
+        used; NewmarkBeta(model with PML layers, ...) builds this)."""
         self.model = model
         self.dt = float(dt)
         self._md = model.desc()
         self._ld = (loads or Loads()).desc()
-        opts = capi.XnmOpts(dt=self.dt, ftol=ftol, mtol=mtol, tol=float(tol), maxit=int(maxit))
+        algo = {"linear": capi.SVL_ALGO_LINEAR, "newton": capi.SVL_ALGO_NEWTON}[algorithm.lower()]
+        integ = {"extendednewmark": capi.SVL_XNM_EXTENDED_NEWMARK, "newmark": capi.SVL_XNM_NEWMARK}[integrator.lower()]
+        opts = capi.XnmOpts(dt=self.dt, ftol=ftol, mtol=mtol, tol=float(tol), maxit=int(solver_maxit),
+                            algorithm=algo, newton_maxit=int(maxit), cnvgtest=int(cnvgtest), cnvgtol=float(cnvgtol),
+                            integrator=integ)
         h = C.c_void_p()
         check(lib().svl_xnm_create(C.byref(self._md), C.byref(self._ld), C.byref(opts), C.byref(h)))
         self._h = h
@@ -226,6 +237,12 @@ class ExtendedNewmarkBeta:
         check(lib().svl_xnm_stats(self._h, C.byref(a), C.byref(b), C.byref(r)))
         return a.value, b.value, r.value
 
+    def newton_stats(self):
+        """(Newton iterations over all steps, of the last step, last convergence-test value)."""
+        a, b, r = C.c_int64(), C.c_int64(), C.c_double()
+        check(lib().svl_xnm_newton_stats(self._h, C.byref(a), C.byref(b), C.byref(r)))
+        return a.value, b.value, r.value
+
     def close(self):
         if getattr(self, "_h", None):
             lib().svl_xnm_destroy(self._h)
@@ -245,7 +262,17 @@ class NewmarkBeta:
     on the true relative residual (svl_nm_*).  Mirrors NewmarkBeta
     (RP/10-Integrators/03-Newmark/NewmarkBeta.cpp) driven by Linear
     (RP/09-Algorithms/01-Linear/Linear.cpp) over an iterative LinearSystem
-    (RP/11-Solvers/02-Iterative/PetscSolver.cc, KSPCG, rtol `pcg_tol`)."""
+    (RP/11-Solvers/02-Iterative/PetscSolver.cc, KSPCG, rtol `pcg_tol`).
+
+    A model with PML layers (symmetric indefinite effective matrix) is served
+    by the PML-capable handle in NewmarkBeta mode (svl_xnm_*, MINRES to
+    `pcg_tol`); the object returned is then an ExtendedNewmarkBeta instance
+    with the same step methods."""
+
+    def __new__(cls, model: Model, *args, **kw):
+        if cls is NewmarkBeta and getattr(model, "elem_pml", None) is not None and np.any(model.elem_pml):
+            return _newmark_pml(model, *args, **kw)
+        return super().__new__(cls)
 
     def __init__(self, model: Model, loads: Loads | None, dt: float, pcg_tol: float = 1e-8,
                  pcg_maxit: int = 20000, ftol: float = 1e-12, mtol: float = 1e-12, precond: int = 0,
@@ -390,3 +417,13 @@ class NewmarkBeta:
             self.close()
         except Exception:
             pass
+
+
+def _newmark_pml(model: Model, loads: Loads | None, dt: float, pcg_tol: float = 1e-8, pcg_maxit: int = 20000,
+                 ftol: float = 1e-12, mtol: float = 1e-12, precond: int = 0, algorithm: str = "linear",
+                 maxit: int = 50, cnvgtol: float = 1e-6, cnvgtest: int = 4):
+    if precond != capi.SVL_PRECOND_JACOBI:
+        raise capi.SvlError(capi.SVL_ERR_UNSUPPORTED, "the learned preconditioner does not cover PML models")
+    return ExtendedNewmarkBeta(model, loads, dt, tol=pcg_tol, solver_maxit=int(pcg_maxit), ftol=ftol,
+                               mtol=mtol, algorithm=algorithm, maxit=maxit, cnvgtol=cnvgtol, cnvgtest=cnvgtest,
+                               integrator="newmark")

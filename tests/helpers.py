@@ -154,6 +154,29 @@ def pml_box(ndim=2, ni=(6, 4), npml=2, h=1.0, E=2.0e8, nu=0.25, rho=2000.0, nt=8
     return m, L, dt
 
 
+def pml_j2_box(ndim=2, ni=(10, 6), npml=2, nj2=3, su=15e3, **kw):
+    """pml_box whose solid elements in the top `nj2` element layers carry a
+    J2 material with the same elastic moduli (H = 0.02 G, beta = 0.5, pure
+    shear yield su): plastic layers over an elastic half-space with PML."""
+    m, L, dt = pml_box(ndim, ni, npml=npml, **kw)
+    E, nu, rho = m.mat_param[0, :3]
+    G = E / (2 * (1 + nu))
+    K = E / (3 * (1 - 2 * nu))
+    mt = capi.SVL_MAT_PLASTICPLANESTRAINJ2 if ndim == 2 else capi.SVL_MAT_PLASTIC3DJ2
+    m.mat_type = np.array([m.mat_type[0], mt], np.int32)
+    m.mat_param = np.vstack([m.mat_param[0], j2_params(K, G, rho, 0.02 * G, 0.5, np.sqrt(3.0) * su)])
+    vert = ndim - 1
+    X = m.coords
+    h = kw.get("h", 1.0)
+    ytop = X[:, vert].max()
+    emat = np.array(m.elem_mat, np.int32)
+    for e in range(m.nelem):
+        if not m.elem_pml[e] and X[m.conn[e], vert].min() >= ytop - nj2 * h - 1e-9:
+            emat[e] = 1
+    m.elem_mat = emat
+    return m, L, dt
+
+
 def lysmer_box(nx=12, ny=6, h=1.0, E=2.0e8, nu=0.25, rho=2000.0, nt=200, amp=1.0e6, f0=8.0, dt_factor=0.5):
     """Plane-strain box whose sides and bottom are free but held by Lysmer
     dashpots (ZeroLength1D + Viscous1DLinear) to anchor nodes that are fixed:

@@ -2,7 +2,8 @@
 oracle's ExtendedNewmarkBeta (dense LDL^T of the assembled K + 4/dt^2 M +
 2/dt C + dt/3 G): PML2DQuad4 and PML3DHexa8 boxes, the PML history vector,
 the reduction to NewmarkBeta without PML, constraints with support motion,
-and the paths that reject PML models."""
+J2 layers over a PML half-space with Linear and NewtonRaphson, and the paths
+that reject PML models."""
 import numpy as np
 import pytest
 
@@ -58,15 +59,17 @@ def test_constraints_and_support_motion(gpu):
 
 def test_other_paths_reject_pml_models(gpu):
     m, L, dt = pml_box(2, (4, 3), npml=2, nt=10)
-    for make in (lambda: CentralDifference(m, L, dt), lambda: NewmarkBeta(m, L, dt)):
+    for make in (lambda: CentralDifference(m, L, dt),
+                 lambda: NewmarkBeta(m, L, dt, precond=capi.SVL_PRECOND_LEARNED)):
         with pytest.raises(SvlError) as ei:
             make()
         assert ei.value.code == capi.SVL_ERR_UNSUPPORTED
-    m2, L2, dt2 = q4_box(4, 3, nt=10)
+    # a PML element needs an elastic material
+    m2, L2, dt2 = pml_box(2, (4, 3), npml=2, nt=10)
     m2.mat_type = np.array([capi.SVL_MAT_PLASTICPLANESTRAINJ2], np.int32)
     with pytest.raises(SvlError) as ei:
         ExtendedNewmarkBeta(m2, L2, dt2)
-    assert ei.value.code == capi.SVL_ERR_UNSUPPORTED
+    assert ei.value.code == capi.SVL_ERR_INVALID
 
 
 def test_domain_reduction_with_pml_layers(gpu):
@@ -103,3 +106,96 @@ def test_domain_reduction_with_pml_layers(gpu):
     ho, *_ = O.xnewmark_run(m, L, dt, 60)
     assert np.abs(ho).max() > 0
     assert rel_l2(hist, ho) <= 1e-8
+
+
+@pytest.mark.parametrize("ndim,ni,npml,nj2,nt,amp", [(2, (10, 6), 2, 3, 60, 1.0e6), (3, (3, 3, 2), 1, 1, 30, 4.0e6)],
+                         ids=["quad", "hexa"])
+def test_newmark_newton_j2_layers_over_pml(gpu, ndim, ni, npml, nj2, nt, amp):
+    """Config-5 form: J2 top layers over an elastic half-space with PML,
+    NewmarkBeta + NewtonRaphson with 3 iterations per step (test 4, cnvgtol 0):
+    NewmarkBeta(model with PML) runs on the PML-capable handle."""
+    from tests.helpers import pml_j2_box
+    m, L, dt = pml_j2_box(ndim, ni, npml=npml, nj2=nj2, nt=nt, dt_factor=1.0, f0=10.0, amp=amp)
+    nm = NewmarkBeta(m, L, dt, pcg_tol=1e-12, algorithm="newton", maxit=3, cnvgtol=0.0, cnvgtest=4)
+    assert isinstance(nm, ExtendedNewmarkBeta)
+    nm.Initialize()
+    hist = nm.run(1, nt, history=True)
+    its, last, _ = nm.newton_stats()
+    nm.close()
+    ho, *_ = O.xnewmark_run(m, L, dt, nt, algo=2, maxit=3, cnvgtol=0.0, newmark=True)
+    hl, *_ = O.xnewmark_run(m, L, dt, nt, newmark=True)
+    assert its == 3 * nt and last == 3
+    assert rel_l2(ho, hl) > 1e-4                     # the layers yield
+    assert rel_l2(hist, ho) <= 1e-8
+
+
+def test_newmark_newton_displacement_test_with_tolerance(gpu):
+    """Test 5 (relative displacement increment) with a tolerance: the GPU
+    takes the oracle's iteration count on every step."""
+    from tests.helpers import pml_j2_box
+    m, L, dt = pml_j2_box(2, (10, 6), npml=2, nj2=3, nt=40, dt_factor=1.0, f0=10.0)
+    its_o = np.zeros(40, np.int32)
+    ho, *_ = O.xnewmark_run(m, L, dt, 40, algo=1, maxit=10, cnvgtol=1e-3, step_iters=its_o, newmark=True)
+    nm = NewmarkBeta(m, L, dt, pcg_tol=1e-12, algorithm="newton", maxit=10, cnvgtol=1e-3, cnvgtest=5)
+    nm.Initialize()
+    hist = nm.run(1, 40, history=True)
+    its, _, _ = nm.newton_stats()
+    nm.close()
+    assert its == int(its_o.sum()) and its_o.max() > 1
+    assert rel_l2(hist, ho) <= 1e-8
+
+
+def test_extended_j2_layers_over_pml_linear(gpu):
+    from tests.helpers import pml_j2_box
+    m, L, dt = pml_j2_box(2, (10, 6), npml=2, nj2=3, nt=60, dt_factor=1.0, f0=10.0)
+    x = ExtendedNewmarkBeta(m, L, dt, tol=1e-12)
+    x.Initialize()
+    hist = x.run(1, 60, history=True)
+    x.close()
+    ho, *_ = O.xnewmark_run(m, L, dt, 60)
+    m0, L0, _ = pml_box(2, (10, 6), npml=2, nt=60, dt_factor=1.0, f0=10.0)
+    he, *_ = O.xnewmark_run(m0, L0, dt, 60)
+    assert rel_l2(ho, he) > 1e-4
+    assert rel_l2(hist, ho) <= 1e-8
+
+
+def test_extended_newton_follows_the_reference_iteration(gpu):
+    """ExtendedNewmarkBeta + NewtonRaphson: the effective force has no
+    increment terms, only Fint (solid states and PML K_e (U + T dU)) follows
+    the iterate.  The GPU reproduces the oracle's iterates over the first
+    steps (the iteration grows without bound later, as the oracle's does)."""
+    from tests.helpers import pml_j2_box
+    m, L, dt = pml_j2_box(2, (10, 6), npml=2, nj2=3, nt=60, dt_factor=1.0, f0=10.0)
+    nt = 8
+    x = ExtendedNewmarkBeta(m, L, dt, tol=1e-12, algorithm="newton", maxit=3, cnvgtol=0.0, cnvgtest=4)
+    x.Initialize()
+    hist = x.run(1, nt, history=True)
+    Ub = x.GetPMLHistoryVector()
+    x.close()
+    ho, _, _, _, Ubo = O.xnewmark_run(m, L, dt, nt, algo=2, maxit=3, cnvgtol=0.0)
+    hl, *_ = O.xnewmark_run(m, L, dt, nt)
+    assert rel_l2(ho, hl) > 1e-3
+    assert rel_l2(hist, ho) <= 1e-8
+    assert rel_l2(Ub, Ubo) <= 1e-8
+
+
+def test_j2_columns_newton_constraints_support_motion(gpu):
+    """Periodic-side J2 soil columns with base support motion through the
+    PML-capable handle in both modes: NewmarkBeta mode against the NewmarkBeta
+    oracle (increment of step k - 1), ExtendedNewmarkBeta Linear against its
+    oracle (increment of step k)."""
+    from tests.test_gpu_newton import _columns
+    m, L, dt = _columns(elastic=False)
+    x = ExtendedNewmarkBeta(m, L, 4 * dt, tol=1e-13, algorithm="newton", maxit=3, cnvgtol=0.0, integrator="newmark")
+    x.Initialize()
+    hist = x.run(1, 50, history=True)
+    x.close()
+    ho, _ = O.newmark_run(m, L, 4 * dt, 50, algo=2, maxit=3, cnvgtol=0.0, solver=0)
+    assert np.abs(ho).max() > 0
+    assert rel_l2(hist, ho) <= 1e-9
+    x = ExtendedNewmarkBeta(m, L, 4 * dt, tol=1e-13)
+    x.Initialize()
+    hist = x.run(1, 50, history=True)
+    x.close()
+    ho, *_ = O.xnewmark_run(m, L, 4 * dt, 50)
+    assert rel_l2(hist, ho) <= 1e-9

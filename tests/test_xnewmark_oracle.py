@@ -64,3 +64,110 @@ def test_layers_absorb_the_outgoing_wave():
     e = (h[:, interior] ** 2).sum(axis=1)
     assert np.all(np.isfinite(h)) and np.abs(Ub).max() > 0
     assert e[-1] < 1e-4 * e.max()
+
+
+def test_j2_linear_without_pml_equals_newmark_linear():
+    """With G = 0, no support motion and the Linear algorithm the two
+    integrators solve the same system; with J2 elements both take one
+    tangent solve and one state update per step."""
+    from tests.test_gpu_newton import j2_box
+    m, L, dt = j2_box(2, (8, 6), amp=4e5, nt=40)
+    h0, _ = O.newmark_run(m, L, dt, 30, algo=0, solver=0)
+    h1, *_ = O.xnewmark_run(m, L, dt, 30)
+    assert np.abs(h0).max() > 0
+    assert rel_l2(h1, h0) <= 1e-12
+
+
+def _dense_xnewton(m, L, dt, nsteps, niter):
+    """ExtendedNewmarkBeta + NewtonRaphson on an elastic model without PML or
+    support motion, restated densely: every iteration solves
+    Keff du = T^T (Fext - K (U + dU) + C V + M (4/dt V + A)) -- the effective
+    force has no increment terms (ExtendedNewmarkBeta.cpp:208-229), only Fint
+    follows dU through the element states."""
+    K, M, Cm, _ = O.xnewmark_matrices(m)
+    nt = m.ntotal
+    free = np.full(nt, -1)
+    free[m.totaldof.reshape(-1)] = m.freedof.reshape(-1)
+    idx = np.flatnonzero(free >= 0)
+    fr = idx[np.argsort(free[idx])]
+    Keff = (K + 4.0 / dt ** 2 * M + 2.0 / dt * Cm)[np.ix_(fr, fr)]
+    U, V, A = np.zeros(nt), np.zeros(nt), np.zeros(nt)
+    hist = np.zeros((nsteps, nt))
+    for i in range(nsteps):
+        f = np.zeros(nt)
+        for d, sidx, c in zip(L.force_dof, L.force_series, L.force_coef):
+            ser = L.series[sidx]
+            if 1 + i < ser.size:
+                f[d] += c * ser[1 + i]
+        dU = np.zeros(nt)
+        for _ in range(niter):
+            F = f - K @ (U + dU) + Cm @ V + M @ (4.0 / dt * V + A)
+            dU[fr] += np.linalg.solve(Keff, F[fr])
+        A = 4.0 / dt ** 2 * dU - 4.0 / dt * V - A
+        V = 2.0 / dt * dU - V
+        U = U + dU
+        hist[i] = U
+    return hist
+
+
+def test_newton_effective_force_has_no_increment_terms():
+    m, L, dt = q4_box(8, 5, nt=40)
+    m.rayleigh = np.tile([1.5, 1.0e-3], (m.nelem, 1))
+    h3, *_ = O.xnewmark_run(m, L, 4 * dt, 30, algo=2, maxit=3, cnvgtol=0.0)
+    h1, *_ = O.xnewmark_run(m, L, 4 * dt, 30)
+    assert rel_l2(h3, _dense_xnewton(m, L, 4 * dt, 30, 3)) <= 1e-9
+    assert rel_l2(h1, _dense_xnewton(m, L, 4 * dt, 30, 1)) <= 1e-9
+    assert rel_l2(h3, h1) > 1e-3                      # the extra iterations change the answer
+
+
+def test_extended_newton_iterates_without_increment_terms_grow():
+    """ExtendedNewmarkBeta + NewtonRaphson iterates dU <- dU + Keff^-1 (R0 -
+    (Fint(U + dU) - Fint(U))): without the increment's inertia terms in the
+    force the iterates drift to the static solution of each step and the time
+    stepping grows without bound.  Recorded here as the reference's behaviour
+    (ExtendedNewmarkBeta.cpp:208-229 reads dU and does not use it)."""
+    from tests.helpers import pml_j2_box
+    m, L, dt = pml_j2_box(2, (10, 6), npml=2, nj2=3, nt=60, dt_factor=1.0, f0=10.0)
+    its = np.zeros(40, np.int32)
+    hn, *_ = O.xnewmark_run(m, L, dt, 40, algo=2, maxit=3, cnvgtol=0.0, step_iters=its)
+    hl, *_ = O.xnewmark_run(m, L, dt, 40)
+    assert np.all(its == 3)
+    assert np.abs(hn[-1]).max() > 1e6 * np.abs(hl).max()
+
+
+def test_newmark_mode_without_pml_equals_newmark():
+    """The oracle's PML-capable integrator in NewmarkBeta mode reproduces the
+    NewmarkBeta oracle on J2 soil columns with EQUAL constraints and support
+    motion, Linear and Newton."""
+    from tests.test_gpu_newton import _columns
+    m, L, dt = _columns(elastic=False)
+    m.rayleigh = np.tile([1.0, 5.0e-4], (m.nelem, 1))
+    for algo, maxit in ((0, 1), (2, 3)):
+        hn, _ = O.newmark_run(m, L, 4 * dt, 40, algo=algo, maxit=maxit, cnvgtol=0.0, solver=0)
+        hx, *_ = O.xnewmark_run(m, L, 4 * dt, 40, algo=algo, maxit=maxit, cnvgtol=0.0, newmark=True)
+        assert np.abs(hn).max() > 0
+        assert rel_l2(hx, hn) <= 1e-12
+
+
+def test_newmark_mode_on_2d_pml_equals_extended_linear():
+    """PML2DQuad4 has no history matrix and, without support motion, the two
+    integrators' Linear steps coincide."""
+    m, L, dt = pml_box(2, (10, 6), npml=2, nt=60, dt_factor=1.0, f0=10.0)
+    hx, *_ = O.xnewmark_run(m, L, dt, 50)
+    hn, *_ = O.xnewmark_run(m, L, dt, 50, newmark=True)
+    assert np.abs(hx).max() > 0
+    assert rel_l2(hn, hx) <= 1e-12
+
+
+def test_newmark_newton_j2_over_pml_converges():
+    """NewmarkBeta + NewtonRaphson on J2 layers over PML: the effective force
+    carries the increment terms, so the iterations converge (ExtendedNewmarkBeta's
+    do not, its force lacks them)."""
+    from tests.helpers import pml_j2_box
+    m, L, dt = pml_j2_box(2, (10, 6), npml=2, nj2=3, nt=60, dt_factor=1.0, f0=10.0)
+    its = np.zeros(50, np.int32)
+    hn, *_ = O.xnewmark_run(m, L, dt, 50, algo=2, maxit=10, cnvgtol=1e-8, newmark=True, step_iters=its)
+    hl, *_ = O.xnewmark_run(m, L, dt, 50, newmark=True)
+    assert its.max() < 10 and its.max() >= 2
+    assert np.abs(hn).max() < 10 * np.abs(hl).max()
+    assert rel_l2(hn, hl) > 1e-4
