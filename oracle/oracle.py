@@ -34,7 +34,8 @@ def lib():
         L.oracle_pml_matrices.argtypes = [C.c_int, f64p, C.c_double, C.c_double, C.c_double, C.c_double, f64p,
                                           f64p, f64p, f64p, f64p]
         L.oracle_xnewmark_run.argtypes = [vp, vp, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double,
-                                          C.c_int, f64p, f64p, f64p, f64p, f64p, C.POINTER(C.c_int)]
+                                          C.c_int, f64p, f64p, f64p, f64p, f64p, C.POINTER(C.c_int),
+                                          C.POINTER(C.c_double)]
         L.oracle_xnewmark_matrices.argtypes = [vp, f64p, f64p, f64p, f64p]
         _lib = L
     return _lib
@@ -71,7 +72,8 @@ def cd_run(model, loads, dt, nsteps, k_first=1, ftol=1e-12, mtol=1e-12, mode=0, 
 
 def newmark_run(model, loads, dt, nsteps, k_first=1, algo=0, maxit=50, cnvgtol=1e-6, solver=0, pcg_tol=1e-12,
                 step_iters=None):
-    """algo 0 Linear, 1 Newton with test 5, 2 Newton with test 4; solver 0
+    """algo 0 Linear, 1 Newton with test 5, 2 Newton with test 4, 10 + t
+    Newton with test t (1..8); solver 0
     dense LDL^T, 1 Jacobi-PCG.  step_iters (int32 [nsteps]) receives the
     Newton iterations of every step."""
     md = model.desc()
@@ -157,11 +159,13 @@ def pml_matrices(ndim, X, E, nu, rho, par, t=1.0):
 
 
 def xnewmark_run(model, loads, dt, nsteps, k_first=1, algo=0, maxit=50, cnvgtol=1e-6, step_iters=None,
-                 newmark=False):
+                 newmark=False, last_res=None):
     """ExtendedNewmarkBeta (or, newmark=True, NewmarkBeta) on models with PML
     elements (dense LDL^T); algo 0 Linear, 1 Newton with test 5, 2 Newton
-    with test 4.  Returns (history of U [nsteps, ntotal], final U, V, A,
-    Ubar); step_iters (int32 [nsteps]) receives the iterations of every step."""
+    with test 4, 10 + t Newton with test t (Algorithm.cpp:122-188).  Returns
+    (history of U [nsteps, ntotal], final U, V, A, Ubar); step_iters (int32
+    [nsteps]) receives the iterations of every step, last_res (float64 [1])
+    the last step's final convergence-test value."""
     md = model.desc()
     ld = loads.desc() if loads is not None else None
     nt = model.ntotal
@@ -171,7 +175,7 @@ def xnewmark_run(model, loads, dt, nsteps, k_first=1, algo=0, maxit=50, cnvgtol=
     si = None if step_iters is None else step_iters.ctypes.data_as(C.POINTER(C.c_int))
     st = lib().oracle_xnewmark_run(C.addressof(md), C.addressof(ld) if ld is not None else None, dt, k_first,
                                    nsteps, algo, maxit, cnvgtol, int(bool(newmark)), f(hist), f(U), f(V), f(A),
-                                   f(Ub), si)
+                                   f(Ub), si, None if last_res is None else f(last_res))
     if st != 0:
         raise RuntimeError("oracle_xnewmark_run failed with status %d" % st)
     return hist, U, V, A, Ub

@@ -1002,6 +1002,27 @@ int pcg_solve(const CSR& A, const std::vector<double>& b, std::vector<double>& x
 
 /* ---------------- Newmark (NewmarkBeta.cpp, beta=1/4, gamma=1/2) -------- */
 
+/* Algorithm::ComputeConvergence (Algorithm.cpp:122-188).  The run entry
+ * points encode the algorithm as algo 0 Linear, 1 Newton with test 5, 2
+ * Newton with test 4, 10 + t Newton with test t (1..8). */
+int newton_test(int algo) { return algo == 1 ? 5 : algo == 2 ? 4 : algo - 10; }
+double convergence(int test, int it, const std::vector<double>& F, const std::vector<double>& dU,
+                   const std::vector<double>& du, double& norm0) {
+    auto nrm = [](const std::vector<double>& v) { double s2 = 0; for (double x : v) s2 += x * x; return std::sqrt(s2); };
+    std::vector<double> en(du.size());
+    for (size_t i = 0; i < du.size(); ++i) en[i] = du[i] * F[i];
+    switch (test) {
+    case 1: return nrm(F);
+    case 2: return nrm(du);
+    case 3: return nrm(en);
+    case 4: if (it == 0) { norm0 = nrm(F); return norm0; } return nrm(F) / norm0;
+    case 5: if (it == 0) { norm0 = nrm(dU); return nrm(du); } return nrm(du) / norm0;
+    case 6: if (it == 0) { norm0 = nrm(en); return norm0; } return nrm(en) / norm0;
+    case 7: return nrm(du) / nrm(dU);
+    default: return -1.0;        // 8: maximum number of iterations
+    }
+}
+
 struct Newmark {
     Sim s; double dt;
     std::vector<double> U, V, A, Mfull_diag;
@@ -1149,21 +1170,8 @@ struct Newmark {
             }
             if (!solve(K, Feff, du)) return SVL_ERR_BREAKDOWN;
             for (int f = 0; f < nf; ++f) dUf[f] += du[f];
-            // convergence (Algorithm.cpp:122-188): algo 1 = test 5 (relative
-            // displacement increment), algo 2 = test 4 (relative unbalanced
-            // force, the norm of the effective force this iteration solved for)
-            double res = 0.0;
-            if (algo == 1) {
-                double dn = 0, Dn = 0;
-                for (int f = 0; f < nf; ++f) { dn += du[f] * du[f]; Dn += dUf[f] * dUf[f]; }
-                dn = std::sqrt(dn); Dn = std::sqrt(Dn);
-                if (it == 0) { norm0 = Dn; res = dn; } else res = dn / norm0;
-            } else if (algo == 2) {
-                double fn = 0;
-                for (int f = 0; f < nf; ++f) fn += Feff[f] * Feff[f];
-                fn = std::sqrt(fn);
-                if (it == 0) { norm0 = fn; res = fn; } else res = fn / norm0;
-            }
+            // convergence on the effective force this iteration solved for
+            const double res = algo == 0 ? 0.0 : convergence(newton_test(algo), it, Feff, dUf, du, norm0);
             s.T_apply(dUf, dUt);
             for (int t = 0; t < nt; ++t) Us[t] = U[t] + dUt[t];
             for (int e = 0; e < s.m.nelem; ++e) s.element_update(e, Us);
@@ -1366,6 +1374,7 @@ struct XNewmark {
     bool nonlinear = false;                  // J2 solid elements present
     bool newmark = false;                    // NewmarkBeta's force, stiffness and update
     int last_iters = 0;
+    double last_res = 0.0;
 
     bool pml(int e) const { return !s.m.epml.empty() && s.m.epml[e]; }
     void pml_elem(int e, double* Me, double* Ce, double* Ke, double* Ge) const {
@@ -1555,17 +1564,7 @@ struct XNewmark {
             if (solver == 0) { if (!dense_ldlt_solve(Kff, Feff, du)) return SVL_ERR_BREAKDOWN; }
             else return SVL_ERR_INVALID;
             for (int f = 0; f < nf; ++f) dUf[f] += du[f];
-            if (algo == 1) {
-                double dn = 0, Dn = 0;
-                for (int f = 0; f < nf; ++f) { dn += du[f] * du[f]; Dn += dUf[f] * dUf[f]; }
-                dn = std::sqrt(dn); Dn = std::sqrt(Dn);
-                if (it == 0) { norm0 = Dn; res = dn; } else res = dn / norm0;
-            } else if (algo == 2) {
-                double fn = 0;
-                for (int f = 0; f < nf; ++f) fn += Feff[f] * Feff[f];
-                fn = std::sqrt(fn);
-                if (it == 0) { norm0 = fn; res = fn; } else res = fn / norm0;
-            }
+            if (algo != 0) res = convergence(newton_test(algo), it, Feff, dUf, du, norm0);
             s.T_apply(dUf, dUt);
             for (int t = 0; t < nt; ++t) Us[t] = U[t] + dUt[t];
             for (int e = 0; e < m.nelem; ++e) if (!pml(e)) s.element_update(e, Us);
@@ -1573,6 +1572,7 @@ struct XNewmark {
             if (algo == 0 || !(res > cnvgtol) || it >= maxit) break;
         }
         last_iters = it;
+        last_res = res;
         for (int t = 0; t < nt; ++t) {
             const double d = dUt[t], D = d + SM[t];
             if (!newmark) Ubar[t] = Ubar[t] + dt * U[t] + dt / 3.0 * D + dt * dt / 6.0 * V[t];
@@ -1637,7 +1637,8 @@ int oracle_newmark_run(const svl_model_desc* model, const svl_load_desc* loads, 
  * 2 Newton with test 4; step_iters [nsteps] or NULL. */
 int oracle_xnewmark_run(const svl_model_desc* model, const svl_load_desc* loads, double dt, int k_first, int nsteps,
                         int algo, int maxit, double cnvgtol, int newmark,
-                        double* hist_U, double* U_out, double* V_out, double* A_out, double* Ubar_out, int* step_iters) {
+                        double* hist_U, double* U_out, double* V_out, double* A_out, double* Ubar_out, int* step_iters,
+                        double* last_res) {
     XNewmark x;
     x.newmark = newmark != 0;
     if (!x.init(model, loads, dt)) return SVL_ERR_INVALID;
@@ -1647,6 +1648,7 @@ int oracle_xnewmark_run(const svl_model_desc* model, const svl_load_desc* loads,
         int st = x.step(k_first + i, algo, algo == 0 ? 1 : maxit, cnvgtol);
         if (st) return st;
         if (step_iters) step_iters[i] = x.last_iters;
+        if (last_res) *last_res = x.last_res;
         if (hist_U) std::memcpy(hist_U + (size_t)i * nt, x.U.data(), sizeof(double) * nt);
     }
     if (U_out) std::memcpy(U_out, x.U.data(), sizeof(double) * nt);

@@ -1937,8 +1937,8 @@ int svl_nm_create(const svl_model_desc* model, const svl_load_desc* loads, const
     nm->general = !cd->identity_T || cd->has_sm || nm->damped;
     if (opts->algorithm != SVL_ALGO_LINEAR && opts->algorithm != SVL_ALGO_NEWTON) { set_error("unknown algorithm %d", opts->algorithm); return fail(SVL_ERR_INVALID); }
     nm->newton = opts->algorithm == SVL_ALGO_NEWTON;
-    if (nm->newton && (opts->maxit <= 0 || !(opts->cnvgtol >= 0.0) || (opts->cnvgtest != 4 && opts->cnvgtest != 5))) {
-        set_error("Newton needs maxit > 0, cnvgtol >= 0 (0: always maxit iterations) and cnvgtest 4 or 5");
+    if (nm->newton && (opts->maxit <= 0 || !(opts->cnvgtol >= 0.0) || opts->cnvgtest < 1 || opts->cnvgtest > 8)) {
+        set_error("Newton needs maxit > 0, cnvgtol >= 0 (0: always maxit iterations) and cnvgtest 1..8");
         return fail(SVL_ERR_INVALID);
     }
     if (m.has_j2() && !nm->newton) {
@@ -2251,22 +2251,24 @@ static int nm_step_newton(svl_nm* nm, double* U_hist_row) {
             else k_nm_rhs<3><<<ng, tb, 0, cd->stream>>>(cd->d, nm->b, 4.0 / dt, nm->dUf, 4.0 / dt / dt);
         }
         CUDA_TRY(cudaGetLastError());
-        double fn = 0.0;
-        if (nm->opts.cnvgtest == 4) {
-            nm_dot(nm, nm->b, nm->b, S_RP);
-            TRY(nm_scalars(nm, hs));
-            fn = std::sqrt(hs[S_RP]);
-        }
-        TRY(nm_solve(nm));                                  // x = du
+        TRY(nm_solve(nm));                                  // x = du; b is left as it was
         k_axpy1<<<gf, tb, 0, cd->stream>>>(nm->dUf, nm->x, n);
-        if (nm->opts.cnvgtest == 5) {
-            nm_dot2(nm, nm->x, nm->x, S_RP, nm->dUf, nm->dUf, S_ZQ);
-            TRY(nm_scalars(nm, hs));
-            const double dn = std::sqrt(hs[S_RP]), Dn = std::sqrt(hs[S_ZQ]);
-            if (it == 0) { norm0 = Dn; res = dn; } else res = dn / norm0;
-        } else {
-            if (it == 0) { norm0 = fn; res = fn; } else res = fn / norm0;
+        // the norms the convergence test reads (Algorithm.cpp:122-188)
+        const int test = nm->opts.cnvgtest;
+        double fn = 0.0, dn = 0.0, Dn = 0.0, en = 0.0;
+        if (test == 1 || test == 4) nm_dot(nm, nm->b, nm->b, S_RP);
+        if (test == 2 || test == 5 || test == 7) nm_dot2(nm, nm->x, nm->x, S_RZN, nm->dUf, nm->dUf, S_ZQ);
+        if (test == 3 || test == 6) {
+            k_vmul<<<gf, tb, 0, cd->stream>>>(nm->x, nm->b, nm->z, n);
+            nm_dot(nm, nm->z, nm->z, S_RP);
         }
+        if (test != 8) {
+            TRY(nm_scalars(nm, hs));
+            fn = en = std::sqrt(hs[S_RP]);
+            dn = std::sqrt(hs[S_RZN]);
+            Dn = std::sqrt(hs[S_ZQ]);
+        }
+        res = convergence_test(test, it, fn, dn, Dn, en, norm0);
         // UpdateStatesIncrements: element states from U + T dU (Algorithm.cpp:18-56)
         if (nm->general) {
             k_nmg_expand<<<gt, tb, 0, cd->stream>>>(cd->d, nm->dUf, nm->dUt);

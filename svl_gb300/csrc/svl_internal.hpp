@@ -14,6 +14,25 @@ namespace svl {
 
 void set_error(const char* fmt, ...);
 
+// Algorithm::ComputeConvergence (RP/09-Algorithms/Algorithm.cpp:122-188) from
+// the 2-norms of the effective force F, of the iteration's increment du, of
+// the accumulated increment dU and of du .* F, at iteration `it` (0-based);
+// norm0 holds the first iteration's reference for the relative tests.
+//   1 |F|  2 |du|  3 |du.*F|  4 |F|/|F_0|  5 |du|/|dU_0|  6 |du.*F|/|(du.*F)_0|
+//   7 |du|/|dU|  8 -1 (the loop stops after one iteration)
+inline double convergence_test(int test, int it, double fn, double dn, double Dn, double en, double& norm0) {
+    switch (test) {
+    case 1: return fn;
+    case 2: return dn;
+    case 3: return en;
+    case 4: if (it == 0) { norm0 = fn; return fn; } return fn / norm0;
+    case 5: if (it == 0) { norm0 = Dn; return dn; } return dn / norm0;
+    case 6: if (it == 0) { norm0 = en; return en; } return en / norm0;
+    case 7: return dn / Dn;
+    default: return -1.0;
+    }
+}
+
 // Gauss abscissa of the 2x2 / 2x2x2 rules, truncated to 15 digits exactly as
 // RP/04-Elements/11-Integration/GaussQuadrature.cpp:303-316 tabulates it.
 constexpr double kGaussAbscissa = 0.577350269189626;

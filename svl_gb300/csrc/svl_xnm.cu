@@ -955,26 +955,21 @@ int x_step(svl_xnm* X, int k) {
     int it = 0;
     for (;;) {
         XTRY(x_rhs(X, k));
-        double fn = 0.0;
-        if (X->newton && test == 4) {
-            XTRY(x_dot(X, X->b, X->b, 3));
-            XTRY(x_read(X, 3, &fn));
-            fn = std::sqrt(fn);
-        }
-        XTRY(x_solve(X));
+        XTRY(x_solve(X));                         // x = du; b is left as it was
         k_xaxpby<<<grid_of(nf), 256, 0, X->stream>>>(nf, 1.0, X->x, 1.0, X->dUf);
         if (X->newton) {
-            if (test == 5) {
-                double dn = 0.0, Dn = 0.0;
-                XTRY(x_dot(X, X->x, X->x, 3));
-                XTRY(x_read(X, 3, &dn));
-                XTRY(x_dot(X, X->dUf, X->dUf, 4));
-                XTRY(x_read(X, 4, &Dn));
-                dn = std::sqrt(dn); Dn = std::sqrt(Dn);
-                if (it == 0) { norm0 = Dn; res = dn; } else res = dn / norm0;
-            } else {
-                if (it == 0) { norm0 = fn; res = fn; } else res = fn / norm0;
+            // the norms the convergence test reads (Algorithm.cpp:122-188)
+            double fn = 0.0, dn = 0.0, Dn = 0.0, en = 0.0;
+            if (test == 1 || test == 4) { XTRY(x_dot(X, X->b, X->b, 3)); XTRY(x_read(X, 3, &fn)); }
+            if (test == 2 || test == 5 || test == 7) {
+                XTRY(x_dot(X, X->x, X->x, 3)); XTRY(x_read(X, 3, &dn));
+                XTRY(x_dot(X, X->dUf, X->dUf, 4)); XTRY(x_read(X, 4, &Dn));
             }
+            if (test == 3 || test == 6) {
+                k_xvmul<<<grid_of(nf), 256, 0, X->stream>>>(nf, X->x, X->b, X->tmp);
+                XTRY(x_dot(X, X->tmp, X->tmp, 3)); XTRY(x_read(X, 3, &en));
+            }
+            res = convergence_test(test, it, std::sqrt(fn), std::sqrt(dn), std::sqrt(Dn), std::sqrt(en), norm0);
         }
         // UpdateStatesIncrements: solid states from U + T dU
         k_xexpand<<<gt, 256, 0, X->stream>>>(nt, X->Tp, X->Tc, X->Tv, X->dUf, X->dUt);
@@ -1266,8 +1261,8 @@ int svl_xnm_create(const svl_model_desc* model, const svl_load_desc* loads, cons
     if (!(opts->dt > 0.0) || !(opts->tol > 0.0) || opts->maxit <= 0) { set_error("bad ExtendedNewmark options"); return SVL_ERR_INVALID; }
     if (opts->algorithm != SVL_ALGO_LINEAR && opts->algorithm != SVL_ALGO_NEWTON) { set_error("unknown algorithm %d", opts->algorithm); return SVL_ERR_INVALID; }
     if (opts->algorithm == SVL_ALGO_NEWTON &&
-        (opts->newton_maxit <= 0 || (opts->cnvgtest != 4 && opts->cnvgtest != 5) || !(opts->cnvgtol >= 0.0))) {
-        set_error("Newton needs newton_maxit > 0, cnvgtest 4 or 5 and cnvgtol >= 0"); return SVL_ERR_INVALID;
+        (opts->newton_maxit <= 0 || opts->cnvgtest < 1 || opts->cnvgtest > 8 || !(opts->cnvgtol >= 0.0))) {
+        set_error("Newton needs newton_maxit > 0, cnvgtest 1..8 and cnvgtol >= 0"); return SVL_ERR_INVALID;
     }
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) { set_error("no CUDA device available"); return SVL_ERR_NODEVICE; }

@@ -111,21 +111,29 @@ class Partition:
 
     def make_integrator(self, pcg_tol: Optional[float] = None):
         """The GPU integrator the simulation block asks for: CENTRALDIFFERENCE,
-        NEWMARK (NewmarkBeta) or EXTENDEDNEWMARK (ExtendedNewmarkBeta, the one
-        that takes PML layers), with the Linear algorithm (Driver.hpp:1808-1822);
-        an iterative solver's `tol` is the solve tolerance, a direct solver
-        gets 1e-12."""
+        NEWMARK (NewmarkBeta; on a model with PML layers the PML-capable
+        handle in NewmarkBeta mode) or EXTENDEDNEWMARK (ExtendedNewmarkBeta),
+        with the algorithm LINEAR or NEWTON (`cnvgtol` 1e-6, `nstep` 50,
+        `cnvgtest` 4 by default, Driver.hpp:1786-1822); an iterative solver's
+        `tol` is the solve tolerance, a direct solver gets 1e-12."""
         from .integrators import CentralDifference, ExtendedNewmarkBeta, NewmarkBeta
+        algo = str(self.algorithm.get("name", "LINEAR")).upper()
+        if algo not in ("LINEAR", "NEWTON"):
+            raise PartitionError("algorithm %s is not covered (LINEAR, NEWTON)" % algo)
         if self.integrator == "CENTRALDIFFERENCE":
+            if algo != "LINEAR":
+                raise PartitionError("CENTRALDIFFERENCE is covered with the LINEAR algorithm")
             return CentralDifference(self.model, self.loads, self.dt, ftol=self.ftol, mtol=self.mtol)
         if self.integrator in ("NEWMARK", "EXTENDEDNEWMARK"):
-            if self.algorithm.get("name", "LINEAR").upper() != "LINEAR":
-                raise PartitionError("algorithm %s is not covered (Linear only)" % self.algorithm.get("name"))
             tol = pcg_tol if pcg_tol is not None else (float(self.solver.get("tol", 1e-12))
                                                        if self.solver.get("name", "").upper() == "PETSC" else 1e-12)
+            kw = dict(algorithm=algo.lower(), maxit=int(self.algorithm.get("nstep", 50)),
+                      cnvgtol=float(self.algorithm.get("cnvgtol", 1e-6)),
+                      cnvgtest=int(self.algorithm.get("cnvgtest", 4)))
             if self.integrator == "EXTENDEDNEWMARK":
-                return ExtendedNewmarkBeta(self.model, self.loads, self.dt, tol=tol, ftol=self.ftol, mtol=self.mtol)
-            return NewmarkBeta(self.model, self.loads, self.dt, pcg_tol=tol, ftol=self.ftol, mtol=self.mtol)
+                return ExtendedNewmarkBeta(self.model, self.loads, self.dt, tol=tol, ftol=self.ftol, mtol=self.mtol,
+                                           **kw)
+            return NewmarkBeta(self.model, self.loads, self.dt, pcg_tol=tol, ftol=self.ftol, mtol=self.mtol, **kw)
         raise PartitionError("integrator %s is not covered (the run-process names CENTRALDIFFERENCE, NEWMARK, "
                              "EXTENDEDNEWMARK)" % self.integrator)
 

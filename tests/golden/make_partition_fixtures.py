@@ -4,7 +4,8 @@ CreateRunAnalysisFiles) on small models that exercise every field the
 partition reader maps: materials (elastic and J2), restraints, EQUAL
 constraints, point and element body loads (constant and time series),
 support motions, Rayleigh dampings, PML layers, Lysmer dashpots,
-domain-reduction loads, node recorders, the integrator/solver settings.
+domain-reduction loads, node recorders, the integrator/algorithm/solver
+settings.
 
 Run from the repository root where the reference tree is available:
     python tests/golden/make_partition_fixtures.py /path/to/SVL
@@ -226,6 +227,49 @@ SVL.addRecorder(tag=1, attributes={"name": "NODE", "file": "Disp.out", "ndps": 8
 SVL.addAnalysis(tag=1, attributes={"name": "Dynamic", "nt": nt})
 SVL.addAlgorithm(tag=1, attributes={"name": "Linear", "nstep": 1})
 SVL.addIntegrator(tag=1, attributes={"name": "ExtendedNewmark", "dt": dt})
+SVL.addSolver(tag=1, attributes={"name": "Eigen", "update": "OFF"})
+SVL.addSimulation(tag=1, combo=1, attributes={"analysis": 1, "algorithm": 1, "integrator": 1, "solver": 1})
+SVL.CreateRunAnalysisFiles()
+''',
+    # The PML box with J2 (PlasticPlaneStrainJ2) top soil layers, Newmark +
+    # Newton (3 iterations, the pre-processor's default convergence test)
+    "q4_pml_j2_newton": COMMON + r'''
+SVL.Options["dimension"] = 2
+SVL.Options["massform"] = "lumped"
+W, H, P, dt, nt = 6.0, 4.0, 2.0, 2.0e-3, 41
+G = 2.0e8 / 2.5
+K = 2.0e8 / 1.5
+SVL.addMaterial(tag=1, name="Elastic2DPlaneStrain", attributes={"E": 2.0e8, "nu": 0.25, "rho": 2000.0})
+SVL.addMaterial(tag=2, name="PlasticPlaneStrainJ2", attributes={"K": K, "G": G, "rho": 2000.0, "h": 0.02 * G,
+                                                                 "beta": 0.5, "Sy": math.sqrt(3.0) * 15.0e3})
+soil = SVL.makeDomainArea(options={"ne": [6, 4], "ndof": 2, "class": "LIN2DQUAD4", "elems": "QUAD4",
+    "P0": [0.0, 0.0], "P1": [W, 0.0], "P2": [0.0, H],
+    "attributes": {"material": 1, "th": 1.0, "rule": "Gauss", "np": 4}})
+for tag in soil["Elements"]:
+    el = soil["Elements"][tag]
+    if min(soil["Nodes"][n]["coords"][1] for n in el["conn"]) >= H - 2.0 - 1e-9:
+        el["attributes"]["material"] = 2
+pml = SVL.setPMLDomain({"ne": [10, 6], "ndof": 5, "class": "PML2DQUAD4", "elems": "QUAD4",
+    "P0": [-P, -P], "P1": [W + P, -P], "P2": [-P, H],
+    "attributes": {"material": 1, "th": 1.0, "n": 2.0, "L": P, "R": 1.0e-6, "rule": "Gauss", "np": 4}},
+    [W / 2.0, H / 2.0], [W / 2.0, H / 2.0])
+mesh = SVL.mergeDomain(soil, pml)
+SVL.Entities["Nodes"] = mesh["Nodes"]
+SVL.Entities["Elements"] = mesh["Elements"]
+SVL.Entities["Constraints"] = mesh["Constraints"]
+for tag in sorted(mesh["Nodes"]):
+    x, y = mesh["Nodes"][tag]["coords"][:2]
+    if abs(x + P) < 1e-9 or abs(x - W - P) < 1e-9 or abs(y + P) < 1e-9:
+        SVL.addRestrain(tag=tag, dof=[1, 2])
+top = [t for t in sorted(mesh["Nodes"]) if abs(mesh["Nodes"][t]["coords"][1] - H) < 1e-9 and abs(mesh["Nodes"][t]["coords"][0] - W / 2) < 1e-9][0]
+write_series("ricker.txt", ricker(nt, dt, 25.0, 1.0e6))
+SVL.addFunction(tag=1, name="TimeSeries", attributes={"file": "ricker.txt", "dir": [1.0, -1.0]})
+SVL.addLoad(tag=1, name="PointLoad", attributes={"type": "Concentrated", "fun": 1, "list": [top]})
+SVL.addCombinationCase(tag=1, name="Fixture", attributes={"load": [1], "factor": [1.0]})
+SVL.addRecorder(tag=1, attributes={"name": "NODE", "file": "Disp.out", "ndps": 8, "resp": "disp", "list": [top]})
+SVL.addAnalysis(tag=1, attributes={"name": "Dynamic", "nt": nt})
+SVL.addAlgorithm(tag=1, attributes={"name": "Newton", "nstep": 3, "cnvgtol": 1.0e-12})
+SVL.addIntegrator(tag=1, attributes={"name": "Newmark", "dt": dt})
 SVL.addSolver(tag=1, attributes={"name": "Eigen", "update": "OFF"})
 SVL.addSimulation(tag=1, combo=1, attributes={"analysis": 1, "algorithm": 1, "integrator": 1, "solver": 1})
 SVL.CreateRunAnalysisFiles()

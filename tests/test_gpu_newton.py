@@ -142,3 +142,34 @@ def test_newton_j2_columns_with_constraints_and_support_motion(gpu):
     ho, _ = O.newmark_run(m, L, 4 * dt, nt, algo=2, maxit=3, cnvgtol=0.0, solver=0)
     assert np.abs(ho).max() > 0
     assert rel_l2(hist, ho) <= 1e-9
+
+
+@pytest.mark.parametrize("test", [1, 2, 3, 4, 5, 6, 7, 8])
+def test_convergence_tests_on_both_newmark_handles(gpu, test):
+    """Algorithm::ComputeConvergence tests 1-8 on J2 soil columns: the last
+    step's final test value of the NewmarkBeta handle (PCG) and of the
+    PML-capable handle in NewmarkBeta mode (MINRES) against the oracle's."""
+    from svl_gb300 import ExtendedNewmarkBeta
+    m, L, dt = _columns(elastic=False)
+    nt = 40
+    res = np.zeros(1)
+    its_o = np.zeros(nt, np.int32)
+    ho, *_ = O.xnewmark_run(m, L, 4 * dt, nt, algo=10 + test, maxit=3, cnvgtol=0.0, newmark=True, last_res=res,
+                            step_iters=its_o)
+    want_its = int(its_o.sum())          # steps whose force is exactly zero stop after one iteration
+    assert want_its == nt if test == 8 else want_its > 2 * nt
+    nm = NewmarkBeta(m, L, 4 * dt, pcg_tol=1e-13, algorithm="newton", maxit=3, cnvgtol=0.0, cnvgtest=test)
+    nm.Initialize()
+    h1 = nm.run(1, nt, history=True)
+    its1, _, r1 = nm.newton_stats()
+    nm.close()
+    x = ExtendedNewmarkBeta(m, L, 4 * dt, tol=1e-13, algorithm="newton", maxit=3, cnvgtol=0.0, cnvgtest=test,
+                            integrator="newmark")
+    x.Initialize()
+    h2 = x.run(1, nt, history=True)
+    its2, _, r2 = x.newton_stats()
+    x.close()
+    assert its1 == want_its and its2 == want_its
+    assert rel_l2(h1, ho) <= 1e-9 and rel_l2(h2, ho) <= 1e-9
+    for r in (r1, r2):
+        assert abs(r - res[0]) <= 1e-6 * abs(res[0])

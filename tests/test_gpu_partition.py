@@ -70,6 +70,17 @@ def test_pml_partition_extended_newmark_matches_oracle(gpu, tmp_path):
     assert ntotal == p.model.ntotal and rows.shape == (p.nt - 1, ndofs)
 
 
+def test_pml_j2_newton_partition_matches_oracle(gpu, tmp_path):
+    """NEWMARK + NEWTON on J2 layers over PML: NewmarkBeta on a PML model runs
+    on the PML-capable handle in NewmarkBeta mode."""
+    p = _part("q4_pml_j2_newton")
+    U = p.run(solution_dir=tmp_path)
+    ho, *_ = O.xnewmark_run(p.model, p.loads, p.dt, p.nt - 1, algo=10 + int(p.algorithm["cnvgtest"]),
+                            maxit=int(p.algorithm["nstep"]), cnvgtol=float(p.algorithm["cnvgtol"]), newmark=True)
+    assert np.abs(ho).max() > 0
+    assert rel_l2(U, ho) <= 1e-8
+
+
 def test_drm_partition_newmark_matches_oracle(gpu, tmp_path):
     p = _part("q4_drm_newmark")
     U = p.run(solution_dir=tmp_path)

@@ -20,7 +20,7 @@ def _part(case):
 
 
 @pytest.mark.parametrize("case", ["q4_cd", "h8_newmark_body", "q4_j2_column", "q4_newmark_rayleigh", "q4_pml_extended",
-                                  "q4_lysmer_cd", "q4_drm_newmark"])
+                                  "q4_pml_j2_newton", "q4_lysmer_cd", "q4_drm_newmark"])
 def test_numbering_and_connectivity_follow_the_file(case):
     p = load_partition(_part(case))
     d = json.loads(_part(case).read_text())
@@ -177,3 +177,19 @@ def test_uncovered_content_is_named(tmp_path):
     (tmp_path / "ricker.txt").write_text((GOLD / "partition_q4_cd" / "ricker.txt").read_text())
     with pytest.raises(PartitionError, match="CAUGHEY"):
         load_partition(f)
+
+
+def test_newton_algorithm_and_j2_layers_over_pml():
+    """Newton settings (nstep, cnvgtol, cnvgtest as the pre-processor writes
+    them) and a J2 material on the top solid layers of a PML model; the
+    reference oracle in NewmarkBeta mode runs it."""
+    from oracle import oracle as O
+    p = load_partition(_part("q4_pml_j2_newton"))
+    assert p.integrator == "NEWMARK"
+    assert p.algorithm["name"] == "NEWTON" and p.algorithm["nstep"] == 3 and p.algorithm["cnvgtest"] == 1
+    mt = p.model.mat_type[p.model.elem_mat]
+    assert (mt == capi.SVL_MAT_PLASTICPLANESTRAINJ2).sum() == 12 and p.model.elem_pml.sum() == 36
+    its = np.zeros(10, np.int32)
+    h, *_ = O.xnewmark_run(p.model, p.loads, p.dt, 10, algo=10 + 1, maxit=3, cnvgtol=1e-12, newmark=True,
+                           step_iters=its)
+    assert np.abs(h).max() > 0 and np.all(its == 3)

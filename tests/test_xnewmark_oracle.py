@@ -171,3 +171,44 @@ def test_newmark_newton_j2_over_pml_converges():
     assert its.max() < 10 and its.max() >= 2
     assert np.abs(hn).max() < 10 * np.abs(hl).max()
     assert rel_l2(hn, hl) > 1e-4
+
+
+@pytest.mark.parametrize("test", [1, 2, 3, 4, 5, 6, 7, 8])
+def test_convergence_tests_match_a_restatement(test):
+    """Algorithm::ComputeConvergence (Algorithm.cpp:122-188), tests 1-8: the
+    first iteration's value of a NewmarkBeta + Newton run against the dense
+    restatement's (elastic box: later iterations only see round-off); the
+    relative forms of later iterations are checked on J2 models on the GPU."""
+    m, L, dt = q4_box(8, 5, nt=20)
+    dt4 = 4 * dt
+    res = np.zeros(1)
+    its = np.zeros(6, np.int32)
+    O.xnewmark_run(m, L, dt4, 6, algo=10 + test, maxit=1, cnvgtol=0.0, newmark=True, step_iters=its,
+                   last_res=res)
+    hn, _ = O.newmark_run(m, L, dt4, 6, algo=10 + test, maxit=2, cnvgtol=0.0, solver=0)
+    hx, *_ = O.xnewmark_run(m, L, dt4, 6, algo=10 + test, maxit=2, cnvgtol=0.0, newmark=True)
+    assert rel_l2(hx, hn) <= 1e-12
+    K, M, _, _ = O.xnewmark_matrices(m)
+    nt = m.ntotal
+    free = np.full(nt, -1)
+    free[m.totaldof.reshape(-1)] = m.freedof.reshape(-1)
+    idx = np.flatnonzero(free >= 0)
+    fr = idx[np.argsort(free[idx])]
+    Keff = (K + 4.0 / dt4 ** 2 * M)[np.ix_(fr, fr)]
+    U, V, A = np.zeros(nt), np.zeros(nt), np.zeros(nt)
+    n = np.linalg.norm
+    for i in range(6):
+        f = np.zeros(nt)
+        for d, s_, c in zip(L.force_dof, L.force_series, L.force_coef):
+            if 1 + i < L.series[s_].size:
+                f[d] += c * L.series[s_][1 + i]
+        F = (f - K @ U + M @ (4.0 / dt4 * V + A))[fr]
+        du = np.linalg.solve(Keff, F)
+        dU = np.zeros(nt)
+        dU[fr] = du
+        A = 4.0 / dt4 ** 2 * dU - 4.0 / dt4 * V - A
+        V = 2.0 / dt4 * dU - V
+        U = U + dU
+    want = {1: n(F), 2: n(du), 3: n(du * F), 4: n(F), 5: n(du), 6: n(du * F), 7: 1.0, 8: -1.0}[test]
+    assert np.all(its == 1)
+    assert abs(res[0] - want) <= 1e-9 * abs(want)
