@@ -216,6 +216,39 @@ def nonlinear_newton(steps=8, warm=4, tol=1e-8, size=(64, 64, 32), n_j2=8):
             "dof_newton_iters_per_s": m.nfree * (n1 - n0) / (ms / 1e3)}
 
 
+def nonlinear_newton_pml(steps=3, warm=2, tol=1e-8, size=(64, 64, 32), npml=5, n_j2=8):
+    """NewmarkBeta + NewtonRaphson (3 iterations per step, cnvgtol = 0) on the
+    config-5 model with a PML half-space at a reduced size: PML3DHexa8 layers
+    on the sides and the bottom, J2 top layers, an up-going plane-wave source
+    plane.  NewmarkBeta on a PML model runs on the MINRES handle (symmetric
+    indefinite effective matrix) to a relative residual of `tol` in the
+    |diag|^-1 norm.  Timed by the host clock around the step loop (the solver
+    reads its scalars every iteration, so the stream is synchronous)."""
+    from svl_gb300 import NewmarkBeta, workloads
+    m, L, dt = workloads.config5_pml(*size, npml=npml, n_j2=n_j2, nt=warm + steps + 2)
+    nm = NewmarkBeta(m, L, dt, pcg_tol=tol, pcg_maxit=200000, algorithm="newton", maxit=3, cnvgtol=0.0,
+                     cnvgtest=4)
+    nm.Initialize()
+    nm.run(1, warm)
+    it0 = nm.stats()[0]
+    n0 = nm.newton_stats()[0]
+    t0 = time.perf_counter()
+    nm.run(1 + warm, steps)
+    sec = time.perf_counter() - t0
+    it1, _, res = nm.stats()
+    n1 = nm.newton_stats()[0]
+    U = nm.GetDisplacements()
+    nm.close()
+    return {"workload": "lin3DHexa8 %dx%dx%d (h=2 m) with %d-element PML3DHexa8 layers on the sides and bottom, "
+                        "top %d solid layers Plastic3DJ2, plane-wave source plane (PGA 0.3 g), "
+                        "NewmarkBeta-Newton 3 iterations per step, MINRES" % (size + (npml, n_j2)),
+            "total_dof": m.ntotal, "free_dof": m.nfree, "pml_elements": int(m.elem_pml.sum()), "steps": steps,
+            "ms_per_step": sec * 1e3 / steps, "newton_iters_per_step": (n1 - n0) / steps,
+            "minres_iters_per_newton_iter": (it1 - it0) / max(n1 - n0, 1), "tol": tol,
+            "rel_residual_last": res, "finite": bool(np.all(np.isfinite(U))),
+            "dof_newton_iters_per_s": m.nfree * (n1 - n0) / sec}
+
+
 def implicit_profile():
     from svl_gb300 import NewmarkBeta, workloads
     from svl_gb300 import _capi as capi
@@ -260,9 +293,17 @@ def main():
     ap.add_argument("--implicit-profile", action="store_true",
                     help="profiling aid: 2 Jacobi-PCG steps and 1 flexible-CG step with a fixed untrained "
                          "network on the 64^3 implicit workload, then exit (for an ncu launch list)")
+    ap.add_argument("--config5-pml", default=None, metavar="NX,NY,NZ,NPML,NJ2,STEPS",
+                    help="time only NewmarkBeta-Newton on the config-5 model with PML layers at this size "
+                         "(e.g. 64,64,32,5,8,3) and print it as one JSON line")
     args = ap.parse_args()
     if args.implicit_profile:
         return implicit_profile()
+    if args.config5_pml:
+        nx, ny, nz, npml, nj2, st = (int(v) for v in args.config5_pml.split(","))
+        print(json.dumps({"nonlinear_newton_j2_pml": nonlinear_newton_pml(steps=st, size=(nx, ny, nz), npml=npml,
+                                                                          n_j2=nj2)}))
+        return 0
     if args.implicit_steps is None:
         args.implicit_steps = 10 if args.workload == "config2" else 0
     ws, rank, local = dist_info()

@@ -59,6 +59,16 @@ __global__ void __launch_bounds__(128) k_pml_action(PmlArgs A) {
     double y[NC];
 #pragma unroll
     for (int i = 0; i < NC; ++i) y[i] = 0.0;
+    // all active matrices on one input vector: a single weighted pass
+    bool fused = true;
+    {
+        const double* u0 = nullptr;
+        for (int k = 0; k < 4; ++k) {
+            if (A.coef[k] == 0.0 || (ND == 2 && k == 3)) continue;
+            if (!u0) u0 = A.u[k];
+            else if (A.u[k] != u0) fused = false;
+        }
+    }
     for (int q = 0; q < NEN; ++q) {
         const double xi[3] = {(q & 1) ? g : -g, (q & 2) ? g : -g, (q & 4) ? g : -g};
         double N[NEN], dN[NEN][3];
@@ -131,12 +141,9 @@ __global__ void __launch_bounds__(128) k_pml_action(PmlArgs A) {
             as[i] = 1.0 + a0 * r;
             bs[i] = b0 * r;
         }
-        for (int mi = 0; mi < 4; ++mi) {
-            const double c = A.coef[mi];
-            if (c == 0.0 || (ND == 2 && mi == 3)) continue;
-            const double* u = A.u[mi] + (A.edof ? 0 : (size_t)e * NC);
-            const int32_t* ed = A.edof ? A.edof + (size_t)e * NC : nullptr;
-            double s, qx, qy, qz = 0.0;
+        // stretching combinations of matrix mi (see the header)
+        auto combo = [&](int mi, double& s, double& qx, double& qy, double& qz) {
+            qz = 0.0;
             if (ND == 2) {
                 if (mi == 0) { s = as[0] * as[1]; qx = 0; qy = 0; }
                 else if (mi == 1) { s = as[0] * bs[1] + as[1] * bs[0]; qx = as[1]; qy = as[0]; }
@@ -154,6 +161,33 @@ __global__ void __launch_bounds__(128) k_pml_action(PmlArgs A) {
                     qx = bs[1] * bs[2]; qy = bs[0] * bs[2]; qz = bs[0] * bs[1];
                 }
             }
+        };
+        // Every matrix is linear in (s, q) for a fixed input vector, so when all
+        // active matrices act on the same vector (an operator application) one
+        // pass with the coefficient-weighted combination replaces four.
+        const int npass = fused ? 1 : 4;
+        for (int mi = 0; mi < npass; ++mi) {
+            double c, s, qx, qy, qz;
+            const double* ubase;
+            if (fused) {
+                c = 1.0; s = qx = qy = qz = 0.0;
+                ubase = nullptr;
+                for (int k = 0; k < 4; ++k) {
+                    if (A.coef[k] == 0.0 || (ND == 2 && k == 3)) continue;
+                    double sk, xk, yk, zk;
+                    combo(k, sk, xk, yk, zk);
+                    s += A.coef[k] * sk; qx += A.coef[k] * xk; qy += A.coef[k] * yk; qz += A.coef[k] * zk;
+                    ubase = A.u[k];
+                }
+                if (!ubase) continue;
+            } else {
+                c = A.coef[mi];
+                if (c == 0.0 || (ND == 2 && mi == 3)) continue;
+                combo(mi, s, qx, qy, qz);
+                ubase = A.u[mi];
+            }
+            const double* u = ubase + (A.edof ? 0 : (size_t)e * NC);
+            const int32_t* ed = A.edof ? A.edof + (size_t)e * NC : nullptr;
             // interpolated displacement, stress and displacement gradient
             double U[3] = {0, 0, 0}, S[NS], Gd[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
 #pragma unroll

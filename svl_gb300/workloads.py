@@ -257,3 +257,87 @@ def config5(nx=128, ny=128, nz=64, n_j2=16, nt=301, seed=0, h=2.0, pga=0.3 * 9.8
             L.force_series.append(s)
             L.force_coef.append(2.0 * rho * vs_el * area[i])
     return m, L, dt
+
+
+def config5_pml(nx=128, ny=128, nz=64, npml=10, n_j2=16, nt=301, seed=0, h=2.0, pga=0.3 * 9.81, pml_m=2.0,
+                pml_R=1.0e-6):
+    """Nonlinear implicit model with a PML half-space: lin3DHexa8 grid of
+    nx x ny x nz elements whose outer `npml` element layers on the four sides
+    and the bottom are PML3DHexa8 (9 dofs at their nodes; n = pml_m, L = npml h,
+    R = pml_R; the outer PML boundary fixed in displacement); the top `n_j2`
+    layers of the solid region Plastic3DJ2 (su uniform in [40, 150] kPa by
+    depth, seeded; H = 0.02 G, beta = 1), elastic below (Vs 300 m/s, J2
+    layers 200 m/s, nu = 0.3, rho = 2000).  The band-limited plane wave
+    (0.1-10 Hz, PGA `pga`) enters as the x force 2 rho Vs A v_in(t) on the
+    solid nodes of the plane two elements above the bottom PML (an up-going
+    plane-wave source; the down-going half leaves through the bottom PML).
+    Dofs numbered node by node with each node's own count (PlainScheme
+    order).  dt = 0.5 h / Vp of the elastic layers."""
+    from .model import j2_params
+    rng = np.random.default_rng(seed + 55)
+    rho, nu = 2000.0, 0.3
+    vs_el, vs_j2 = 300.0, 200.0
+    ne = nx * ny * nz
+    e = np.arange(ne)
+    ix, iy, iz = e % nx, (e // nx) % ny, e // (nx * ny)
+    # PML normal and reference point per element
+    nvec = np.zeros((ne, 3))
+    x0 = np.zeros((ne, 3))
+    lo, hi = npml * h, np.array([nx - npml, ny - npml]) * h
+    for d, i, n in ((0, ix, nx), (1, iy, ny)):
+        m_lo, m_hi = i < npml, i >= n - npml
+        nvec[m_lo, d], x0[m_lo, d] = -1.0, lo
+        nvec[m_hi, d], x0[m_hi, d] = 1.0, hi[d]
+    m_bot = iz < npml
+    nvec[m_bot, 2], x0[m_bot, 2] = -1.0, lo
+    epml = np.any(nvec != 0.0, axis=1).astype(np.int32)
+    par = np.zeros((ne, 9))
+    par[:, 0], par[:, 1], par[:, 2] = pml_m, npml * h, pml_R
+    par[:, 3:6], par[:, 6:9] = x0, nvec
+    par[epml == 0] = 0.0
+    # materials: J2 in the top n_j2 layers of the solid region, elastic elsewhere
+    j2 = (iz >= nz - n_j2) & (epml == 0)
+    mt = np.where(j2, capi.SVL_MAT_PLASTIC3DJ2, capi.SVL_MAT_ELASTIC3DLINEAR).astype(np.int32)
+    G_el, G_j2 = rho * vs_el ** 2, rho * vs_j2 ** 2
+    E_el = 2 * G_el * (1 + nu)
+    K_j2 = 2 * G_j2 * (1 + nu) / (3 * (1 - 2 * nu))
+    su_layer = np.sort(rng.uniform(40e3, 150e3, n_j2))[::-1]
+    mp = np.zeros((ne, 8))
+    mp[~j2, 0], mp[~j2, 1], mp[~j2, 2] = E_el, nu, rho
+    layer = nz - 1 - iz[j2]
+    H = 0.02 * G_j2
+    mp[j2] = np.stack([np.full(layer.size, K_j2), np.full(layer.size, G_j2), np.full(layer.size, rho),
+                       np.full(layer.size, H), np.ones(layer.size), np.sqrt(3.0) * su_layer[layer],
+                       np.zeros(layer.size), np.zeros(layer.size)], axis=1)
+    g = Model.grid(3, (nx, ny, nz), (h, h, h), mat_type=mt, mat_param=mp, elem_mat=np.arange(ne, dtype=np.int32))
+    # dofs: 9 at the nodes of PML elements, 3 elsewhere, node by node
+    nn = g.nnode
+    pnode = np.zeros(nn, bool)
+    pnode[g.conn[epml == 1].ravel()] = True
+    ndof_n = np.where(pnode, 9, 3).astype(np.int32)
+    X = g.coords
+    outer = (np.isclose(X[:, 0], 0.0) | np.isclose(X[:, 0], nx * h) | np.isclose(X[:, 1], 0.0)
+             | np.isclose(X[:, 1], ny * h) | np.isclose(X[:, 2], 0.0))
+    j = np.arange(9)[None, :]
+    has = j < ndof_n[:, None]
+    off = np.concatenate([[0], np.cumsum(ndof_n)[:-1]]).astype(np.int64)
+    tdof = np.where(has, off[:, None] + j, -1).astype(np.int32)
+    free = has & ~(outer[:, None] & (j < 3))
+    fdof = np.full((nn, 9), -1, np.int64)
+    fdof[free] = np.arange(int(free.sum()))          # row-major = node by node
+    m = Model(ndim=3, coords=X, totaldof=tdof, freedof=fdof.astype(np.int32), conn=g.conn, elem_type=g.elem_type,
+              elem_mat=g.elem_mat, mat_type=g.mat_type, mat_param=g.mat_param, lumped=True,
+              node_ndof=ndof_n, elem_pml=epml, pml_param=par)
+    vp = vs_el * np.sqrt(2 * (1 - nu) / (1 - 2 * nu))
+    dt = 0.5 * h / vp
+    disp = base_motion(max(nt + 2, int(20.0 / dt)), dt, 0.1, 10.0, pga, rng)[:nt + 2]
+    v_in = np.gradient(disp, dt)
+    L = Loads()
+    s = L.add_series(v_in)
+    zs = (npml + 2) * h
+    src = np.flatnonzero(np.isclose(X[:, 2], zs) & ~pnode)
+    for n in src:
+        L.force_dof.append(int(tdof[n, 0]))
+        L.force_series.append(s)
+        L.force_coef.append(2.0 * rho * vs_el * h * h)
+    return m, L, dt

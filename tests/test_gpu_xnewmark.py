@@ -199,3 +199,17 @@ def test_j2_columns_newton_constraints_support_motion(gpu):
     x.close()
     ho, *_ = O.xnewmark_run(m, L, 4 * dt, 50)
     assert rel_l2(hist, ho) <= 1e-9
+
+
+def test_config5_pml_small_matches_oracle(gpu):
+    """The config-5 model with a PML half-space (workloads.config5_pml) at a
+    small size: NewmarkBeta-Newton, 3 iterations per step, against the oracle."""
+    from svl_gb300 import workloads
+    m, L, dt = workloads.config5_pml(6, 6, 6, npml=1, n_j2=2, nt=30)
+    nm = NewmarkBeta(m, L, dt, pcg_tol=1e-12, algorithm="newton", maxit=3, cnvgtol=0.0, cnvgtest=4)
+    nm.Initialize()
+    hist = nm.run(1, 25, history=True)
+    nm.close()
+    ho, *_ = O.xnewmark_run(m, L, dt, 25, algo=2, maxit=3, cnvgtol=0.0, newmark=True)
+    assert np.abs(ho).max() > 0
+    assert rel_l2(hist, ho) <= 1e-8
