@@ -398,7 +398,10 @@ typedef struct svl_xnm_opts {
                             displacement increment (Algorithm.cpp:122-188)        */
     double  cnvgtol;     /* Newton: convergence tolerance (0 = always newton_maxit) */
     int32_t integrator;  /* SVL_XNM_EXTENDED_NEWMARK or SVL_XNM_NEWMARK              */
-    int32_t reserved;
+    int32_t single_inner;/* 1: the inner MINRES iterations apply the element
+                            operators in single precision; every restart forms
+                            the true residual with the double operator and the
+                            stopping test is on it (iterative refinement)      */
 } svl_xnm_opts;
 int  svl_xnm_create(const svl_model_desc* model, const svl_load_desc* loads, const svl_xnm_opts* opts,
                     svl_xnm** out);

@@ -97,7 +97,7 @@ class XnmOpts(C.Structure):
     _fields_ = [("dt", C.c_double), ("ftol", C.c_double), ("mtol", C.c_double), ("tol", C.c_double),
                 ("maxit", C.c_int32), ("algorithm", C.c_int32), ("newton_maxit", C.c_int32),
                 ("cnvgtest", C.c_int32), ("cnvgtol", C.c_double), ("integrator", C.c_int32),
-                ("reserved", C.c_int32)]
+                ("single_inner", C.c_int32)]
 
 
 SVL_XNM_EXTENDED_NEWMARK = 0

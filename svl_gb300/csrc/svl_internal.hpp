@@ -119,6 +119,7 @@ struct PmlArgs {
     double ftol;           // >= 0: entries with |y| <= ftol are dropped (force filter)
     double yscale;         // y is scaled by this after the filter
     int accumulate;        // 1: y += result
+    int single;            // 1: single-precision arithmetic (inner solver iterations)
 };
 int pml_action_launch(int ndim, const PmlArgs& A, cudaStream_t st);
 

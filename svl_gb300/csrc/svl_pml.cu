@@ -39,61 +39,72 @@ namespace {
 
 namespace svl {
 
-template <int ND>
+// T = double: the reference's arithmetic.  T = float: the same operator in
+// single precision (coordinates taken relative to the element's first node,
+// material and stretching constants formed in double), for the inner
+// iterations of a solve whose residual is checked with the double operator.
+template <int ND, typename T>
 __global__ void __launch_bounds__(128) k_pml_action(PmlArgs A) {
     constexpr int NEN = ND == 2 ? 4 : 8, NN = ND == 2 ? 5 : 9, NC = NEN * NN, NS = ND == 2 ? 3 : 6;
     constexpr int NPAR = 3 + 2 * ND;
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= A.nelem) return;
-    const double* X = A.X + (size_t)e * NEN * ND;
-    const double E = A.mat[3 * e], nu = A.mat[3 * e + 1], rho = A.mat[3 * e + 2];
-    const double t = (ND == 2 && A.thick) ? A.thick[e] : 1.0;
+    const double* Xd = A.X + (size_t)e * NEN * ND;
+    const double E_ = A.mat[3 * e], nu_ = A.mat[3 * e + 1], rho_ = A.mat[3 * e + 2];
     const double* par = A.par + (size_t)e * NPAR;
-    const double mu = E / 2.0 / (1 + nu);
-    const double lambda = E * nu / (1.0 + nu) / (1.0 - 2.0 * nu);
-    const double Vp = sqrt((lambda + 2.0 * mu) / rho);
-    const double pm = par[0], L = par[1], R = par[2];
-    const double a0 = (pm + 1.0) * (L / 10.0) / 2.0 / L * log(1.0 / R);
-    const double b0 = (pm + 1.0) * Vp / 2.0 / L * log(1.0 / R);
-    const double g = 0.577350269189626;       // GaussQuadrature.cpp:303-316
-    double y[NC];
+    const double mu_ = E_ / 2.0 / (1 + nu_);
+    const double lambda_ = E_ * nu_ / (1.0 + nu_) / (1.0 - 2.0 * nu_);
+    const double Vp_ = sqrt((lambda_ + 2.0 * mu_) / rho_);
+    const double pm_ = par[0], L_ = par[1], R_ = par[2];
+    const T mu = (T)mu_, lambda = (T)lambda_, rho = (T)rho_;
+    const T t = (T)((ND == 2 && A.thick) ? A.thick[e] : 1.0);
+    const T pm = (T)pm_, L = (T)L_;
+    const T a0 = (T)((pm_ + 1.0) * (L_ / 10.0) / 2.0 / L_ * log(1.0 / R_));
+    const T b0 = (T)((pm_ + 1.0) * Vp_ / 2.0 / L_ * log(1.0 / R_));
+    const T g = (T)0.577350269189626;       // GaussQuadrature.cpp:303-316
+    T X[NEN * ND], xoff[3] = {0, 0, 0};       // node coordinates relative to node 0; node 0 - x0
 #pragma unroll
-    for (int i = 0; i < NC; ++i) y[i] = 0.0;
+    for (int i = 0; i < NEN * ND; ++i) X[i] = (T)(Xd[i] - Xd[i % ND]);
+#pragma unroll
+    for (int i = 0; i < ND; ++i) xoff[i] = (T)(Xd[i] - par[3 + i]);
+    T y[NC];
+#pragma unroll
+    for (int i = 0; i < NC; ++i) y[i] = 0;
     // all active matrices on one input vector: a single weighted pass
     bool fused = true;
     {
         const double* u0 = nullptr;
         for (int k = 0; k < 4; ++k) {
-            if (A.coef[k] == 0.0 || (ND == 2 && k == 3)) continue;
+            if (A.coef[k] == T(0.0) || (ND == 2 && k == 3)) continue;
             if (!u0) u0 = A.u[k];
             else if (A.u[k] != u0) fused = false;
         }
     }
     for (int q = 0; q < NEN; ++q) {
-        const double xi[3] = {(q & 1) ? g : -g, (q & 2) ? g : -g, (q & 4) ? g : -g};
-        double N[NEN], dN[NEN][3];
+        const T xi[3] = {(q & 1) ? g : -g, (q & 2) ? g : -g, (q & 4) ? g : -g};
+        T N[NEN], dN[NEN][3];
         if (ND == 2) {
-            const double sr[4] = {-1, 1, 1, -1}, ss[4] = {-1, -1, 1, 1};
+            const T sr[4] = {-1, 1, 1, -1}, ss[4] = {-1, -1, 1, 1};
 #pragma unroll
             for (int a = 0; a < NEN; ++a) {
-                N[a] = 0.25 * (1.0 + sr[a] * xi[0]) * (1.0 + ss[a] * xi[1]);
-                dN[a][0] = 0.25 * sr[a] * (1.0 + ss[a] * xi[1]);
-                dN[a][1] = 0.25 * ss[a] * (1.0 + sr[a] * xi[0]);
-                dN[a][2] = 0.0;
+                N[a] = T(0.25) * (T(1.0) + sr[a] * xi[0]) * (T(1.0) + ss[a] * xi[1]);
+                dN[a][0] = T(0.25) * sr[a] * (T(1.0) + ss[a] * xi[1]);
+                dN[a][1] = T(0.25) * ss[a] * (T(1.0) + sr[a] * xi[0]);
+                dN[a][2] = T(0.0);
             }
         } else {
-            const double sr[8] = {-1, 1, 1, -1, -1, 1, 1, -1}, ss[8] = {-1, -1, 1, 1, -1, -1, 1, 1};
-            const double st[8] = {-1, -1, -1, -1, 1, 1, 1, 1};
+            const T sr[8] = {-1, 1, 1, -1, -1, 1, 1, -1}, ss[8] = {-1, -1, 1, 1, -1, -1, 1, 1};
+            const T st[8] = {-1, -1, -1, -1, 1, 1, 1, 1};
 #pragma unroll
             for (int a = 0; a < NEN; ++a) {
-                const double fr = 1.0 + sr[a] * xi[0], fs = 1.0 + ss[a] * xi[1], ft = 1.0 + st[a] * xi[2];
-                N[a] = 0.125 * fr * fs * ft;
-                dN[a][0] = 0.125 * sr[a] * fs * ft;
-                dN[a][1] = 0.125 * ss[a] * fr * ft;
-                dN[a][2] = 0.125 * st[a] * fr * fs;
+                const T fr = T(1.0) + sr[a] * xi[0], fs = T(1.0) + ss[a] * xi[1], ft = T(1.0) + st[a] * xi[2];
+                N[a] = T(0.125) * fr * fs * ft;
+                dN[a][0] = T(0.125) * sr[a] * fs * ft;
+                dN[a][1] = T(0.125) * ss[a] * fr * ft;
+                dN[a][2] = T(0.125) * st[a] * fr * fs;
             }
         }
-        double J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, xg[3] = {0, 0, 0};
+        T J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, xg[3] = {0, 0, 0};
 #pragma unroll
         for (int a = 0; a < NEN; ++a)
 #pragma unroll
@@ -102,15 +113,15 @@ __global__ void __launch_bounds__(128) k_pml_action(PmlArgs A) {
 #pragma unroll
                 for (int j = 0; j < ND; ++j) J[i][j] += dN[a][i] * X[a * ND + j];
             }
-        double det, Ji[3][3];
+        T det, Ji[3][3];
         if (ND == 2) {
             det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
             Ji[0][0] = J[1][1] / det; Ji[0][1] = -J[0][1] / det;
             Ji[1][0] = -J[1][0] / det; Ji[1][1] = J[0][0] / det;
         } else {
-            const double c00 = J[1][1] * J[2][2] - J[1][2] * J[2][1];
-            const double c01 = J[1][2] * J[2][0] - J[1][0] * J[2][2];
-            const double c02 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+            const T c00 = J[1][1] * J[2][2] - J[1][2] * J[2][1];
+            const T c01 = J[1][2] * J[2][0] - J[1][0] * J[2][2];
+            const T c02 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
             det = J[0][0] * c00 + J[0][1] * c01 + J[0][2] * c02;
             Ji[0][0] = c00 / det;
             Ji[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) / det;
@@ -122,34 +133,34 @@ __global__ void __launch_bounds__(128) k_pml_action(PmlArgs A) {
             Ji[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) / det;
             Ji[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) / det;
         }
-        double dx[NEN][3];
+        T dx[NEN][3];
 #pragma unroll
         for (int a = 0; a < NEN; ++a)
 #pragma unroll
             for (int j = 0; j < 3; ++j) {
-                double v = 0.0;
+                T v = T(0.0);
                 if (j < ND)
 #pragma unroll
                     for (int i = 0; i < ND; ++i) v += Ji[j][i] * dN[a][i];
                 dx[a][j] = v;
             }
-        const double f = ND == 2 ? t * 1.0 * fabs(det) : 1.0 * fabs(det);
-        double as[3] = {1, 1, 1}, bs[3] = {0, 0, 0};
+        const T f = ND == 2 ? t * T(1.0) * fabs(det) : T(1.0) * fabs(det);
+        T as[3] = {1, 1, 1}, bs[3] = {0, 0, 0};
 #pragma unroll
         for (int i = 0; i < ND; ++i) {
-            const double r = pow((xg[i] - par[3 + i]) * par[3 + ND + i] / L, pm);
-            as[i] = 1.0 + a0 * r;
+            const T r = pow((xoff[i] + xg[i]) * (T)par[3 + ND + i] / L, pm);
+            as[i] = T(1.0) + a0 * r;
             bs[i] = b0 * r;
         }
         // stretching combinations of matrix mi (see the header)
-        auto combo = [&](int mi, double& s, double& qx, double& qy, double& qz) {
-            qz = 0.0;
+        auto combo = [&](int mi, T& s, T& qx, T& qy, T& qz) {
+            qz = T(0.0);
             if (ND == 2) {
                 if (mi == 0) { s = as[0] * as[1]; qx = 0; qy = 0; }
                 else if (mi == 1) { s = as[0] * bs[1] + as[1] * bs[0]; qx = as[1]; qy = as[0]; }
                 else { s = bs[0] * bs[1]; qx = bs[1]; qy = bs[0]; }
             } else {
-                if (mi == 0) { s = as[0] * as[1] * as[2]; qx = qy = qz = 0.0; }
+                if (mi == 0) { s = as[0] * as[1] * as[2]; qx = qy = qz = T(0.0); }
                 else if (mi == 1) {
                     s = as[0] * as[1] * bs[2] + as[0] * bs[1] * as[2] + bs[0] * as[1] * as[2];
                     qx = as[1] * as[2]; qy = as[0] * as[2]; qz = as[0] * as[1];
@@ -167,52 +178,53 @@ __global__ void __launch_bounds__(128) k_pml_action(PmlArgs A) {
         // pass with the coefficient-weighted combination replaces four.
         const int npass = fused ? 1 : 4;
         for (int mi = 0; mi < npass; ++mi) {
-            double c, s, qx, qy, qz;
+            T c, s, qx, qy, qz;
             const double* ubase;
             if (fused) {
-                c = 1.0; s = qx = qy = qz = 0.0;
+                c = T(1.0); s = qx = qy = qz = T(0.0);
                 ubase = nullptr;
                 for (int k = 0; k < 4; ++k) {
-                    if (A.coef[k] == 0.0 || (ND == 2 && k == 3)) continue;
-                    double sk, xk, yk, zk;
+                    if (A.coef[k] == T(0.0) || (ND == 2 && k == 3)) continue;
+                    T sk, xk, yk, zk;
                     combo(k, sk, xk, yk, zk);
-                    s += A.coef[k] * sk; qx += A.coef[k] * xk; qy += A.coef[k] * yk; qz += A.coef[k] * zk;
+                    const T ck = (T)A.coef[k];
+                    s += ck * sk; qx += ck * xk; qy += ck * yk; qz += ck * zk;
                     ubase = A.u[k];
                 }
                 if (!ubase) continue;
             } else {
-                c = A.coef[mi];
-                if (c == 0.0 || (ND == 2 && mi == 3)) continue;
+                c = (T)A.coef[mi];
+                if (c == T(0.0) || (ND == 2 && mi == 3)) continue;
                 combo(mi, s, qx, qy, qz);
                 ubase = A.u[mi];
             }
             const double* u = ubase + (A.edof ? 0 : (size_t)e * NC);
             const int32_t* ed = A.edof ? A.edof + (size_t)e * NC : nullptr;
             // interpolated displacement, stress and displacement gradient
-            double U[3] = {0, 0, 0}, S[NS], Gd[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+            T U[3] = {0, 0, 0}, S[NS], Gd[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
 #pragma unroll
-            for (int i = 0; i < NS; ++i) S[i] = 0.0;
+            for (int i = 0; i < NS; ++i) S[i] = T(0.0);
 #pragma unroll
             for (int a = 0; a < NEN; ++a) {
 #pragma unroll
                 for (int d = 0; d < ND; ++d) {
-                    const double ua = ed ? u[ed[a * NN + d]] : u[a * NN + d];
+                    const T ua = (T)(ed ? u[ed[a * NN + d]] : u[a * NN + d]);
                     U[d] += N[a] * ua;
 #pragma unroll
                     for (int j = 0; j < ND; ++j) Gd[d][j] += ua * dx[a][j];
                 }
 #pragma unroll
-                for (int i = 0; i < NS; ++i) S[i] += N[a] * (ed ? u[ed[a * NN + ND + i]] : u[a * NN + ND + i]);
+                for (int i = 0; i < NS; ++i) S[i] += N[a] * (T)(ed ? u[ed[a * NN + ND + i]] : u[a * NN + ND + i]);
             }
-            const double cf = c * f;
+            const T cf = c * f;
 #pragma unroll
             for (int j = 0; j < NEN; ++j) {
-                const double Nj = N[j];
-                double* yj = y + j * NN;
+                const T Nj = N[j];
+                T* yj = y + j * NN;
                 if (ND == 2) {
                     // dofs: ux uy s11 s22 s12
-                    const double k2 = s * (lambda + 2.0 * mu) / 4.0 / mu / (lambda + mu);
-                    const double l2 = s * lambda / 4.0 / mu / (lambda + mu);
+                    const T k2 = s * (lambda + T(2.0) * mu) / T(4.0) / mu / (lambda + mu);
+                    const T l2 = s * lambda / T(4.0) / mu / (lambda + mu);
                     yj[0] += cf * (rho * s * Nj * U[0] + qx * dx[j][0] * S[0] + qy * dx[j][1] * S[2]);
                     yj[1] += cf * (rho * s * Nj * U[1] + qy * dx[j][1] * S[1] + qx * dx[j][0] * S[2]);
                     yj[2] += cf * Nj * (-k2 * S[0] + l2 * S[1] + qx * Gd[0][0]);
@@ -220,9 +232,9 @@ __global__ void __launch_bounds__(128) k_pml_action(PmlArgs A) {
                     yj[4] += cf * Nj * (-s / mu * S[2] + qy * Gd[0][1] + qx * Gd[1][0]);
                 } else {
                     // dofs: ux uy uz s11 s22 s33 s12 s23 s13
-                    const double kap = s * (lambda + mu) / mu / (3.0 * lambda + 2.0 * mu);
-                    const double lam = s * lambda / 2.0 / mu / (3.0 * lambda + 2.0 * mu);
-                    const double dxj = dx[j][0], dyj = dx[j][1], dzj = dx[j][2];
+                    const T kap = s * (lambda + mu) / mu / (T(3.0) * lambda + T(2.0) * mu);
+                    const T lam = s * lambda / T(2.0) / mu / (T(3.0) * lambda + T(2.0) * mu);
+                    const T dxj = dx[j][0], dyj = dx[j][1], dzj = dx[j][2];
                     yj[0] += cf * (rho * s * Nj * U[0] + qx * dxj * S[0] + qy * dyj * S[3] + qz * dzj * S[5]);
                     yj[1] += cf * (rho * s * Nj * U[1] + qy * dyj * S[1] + qx * dxj * S[3] + qz * dzj * S[4]);
                     yj[2] += cf * (rho * s * Nj * U[2] + qz * dzj * S[2] + qx * dxj * S[5] + qy * dyj * S[4]);
@@ -239,7 +251,207 @@ __global__ void __launch_bounds__(128) k_pml_action(PmlArgs A) {
     double* out = A.y + (size_t)e * NC;
 #pragma unroll
     for (int i = 0; i < NC; ++i) {
-        double v = y[i];
+        double v = (double)y[i];
+        if (A.ftol >= 0.0 && !(fabs(v) > A.ftol)) v = 0.0;
+        v *= A.yscale;
+        out[i] = A.accumulate ? out[i] + v : v;
+    }
+}
+
+// The operator form of k_pml_action (every active matrix on one vector, one
+// weighted pass) with one thread per (element, Gauss point): the NEN threads
+// of an element are consecutive lanes, lane q loads node q's dofs and forms
+// Gauss point q, node values reach the other lanes by shuffles, and a
+// butterfly over the NEN lanes sums the element vector; lane q writes node q.
+template <int ND, typename T>
+__global__ void __launch_bounds__(128) k_pml_action_gp(PmlArgs A) {
+    constexpr int NEN = ND == 2 ? 4 : 8, NN = ND == 2 ? 5 : 9, NC = NEN * NN, NS = ND == 2 ? 3 : 6;
+    constexpr int NPAR = 3 + 2 * ND;
+    const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int e = gtid / NEN, q = gtid % NEN;
+    const bool valid = e < A.nelem;
+    const int ec = valid ? e : A.nelem - 1;
+    const int lane = threadIdx.x & 31, base = lane - q;
+    const double* Xd = A.X + (size_t)ec * NEN * ND;
+    const double* par = A.par + (size_t)ec * NPAR;
+    const T E = (T)A.mat[3 * ec], nu = (T)A.mat[3 * ec + 1], rho = (T)A.mat[3 * ec + 2];
+    const T mu = E / T(2.0) / (T(1.0) + nu);
+    const T lambda = E * nu / (T(1.0) + nu) / (T(1.0) - T(2.0) * nu);
+    const T Vp = sqrt((lambda + T(2.0) * mu) / rho);
+    const T pm = (T)par[0], L = (T)par[1], R = (T)par[2];
+    const T lr = log(T(1.0) / R);
+    const T a0 = (pm + T(1.0)) * (L / T(10.0)) / T(2.0) / L * lr;
+    const T b0 = (pm + T(1.0)) * Vp / T(2.0) / L * lr;
+    const T t = (T)((ND == 2 && A.thick) ? A.thick[ec] : 1.0);
+    const T g = (T)0.577350269189626;       // GaussQuadrature.cpp:303-316
+    T X[NEN * ND], xoff[3] = {0, 0, 0};
+#pragma unroll
+    for (int i = 0; i < NEN * ND; ++i) X[i] = (T)(Xd[i] - Xd[i % ND]);
+#pragma unroll
+    for (int i = 0; i < ND; ++i) xoff[i] = (T)(Xd[i] - par[3 + i]);
+    // this lane's node dofs
+    const double* u0 = nullptr;
+    for (int k = 0; k < 4; ++k)
+        if (A.coef[k] != 0.0 && !(ND == 2 && k == 3)) { u0 = A.u[k]; break; }
+    T uq[NN];
+#pragma unroll
+    for (int i = 0; i < NN; ++i)
+        uq[i] = u0 ? (T)(A.edof ? u0[A.edof[(size_t)ec * NC + q * NN + i]] : u0[(size_t)ec * NC + q * NN + i]) : T(0.0);
+    // Gauss point q
+    const T xi[3] = {(q & 1) ? g : -g, (q & 2) ? g : -g, (q & 4) ? g : -g};
+    T N[NEN], dN[NEN][3];
+    if (ND == 2) {
+        const T sr[4] = {-1, 1, 1, -1}, ss[4] = {-1, -1, 1, 1};
+#pragma unroll
+        for (int a = 0; a < NEN; ++a) {
+            N[a] = T(0.25) * (T(1.0) + sr[a] * xi[0]) * (T(1.0) + ss[a] * xi[1]);
+            dN[a][0] = T(0.25) * sr[a] * (T(1.0) + ss[a] * xi[1]);
+            dN[a][1] = T(0.25) * ss[a] * (T(1.0) + sr[a] * xi[0]);
+            dN[a][2] = T(0.0);
+        }
+    } else {
+        const T sr[8] = {-1, 1, 1, -1, -1, 1, 1, -1}, ss[8] = {-1, -1, 1, 1, -1, -1, 1, 1};
+        const T st[8] = {-1, -1, -1, -1, 1, 1, 1, 1};
+#pragma unroll
+        for (int a = 0; a < NEN; ++a) {
+            const T fr = T(1.0) + sr[a] * xi[0], fs = T(1.0) + ss[a] * xi[1], ft = T(1.0) + st[a] * xi[2];
+            N[a] = T(0.125) * fr * fs * ft;
+            dN[a][0] = T(0.125) * sr[a] * fs * ft;
+            dN[a][1] = T(0.125) * ss[a] * fr * ft;
+            dN[a][2] = T(0.125) * st[a] * fr * fs;
+        }
+    }
+    T J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, xg[3] = {0, 0, 0};
+#pragma unroll
+    for (int a = 0; a < NEN; ++a)
+#pragma unroll
+        for (int i = 0; i < ND; ++i) {
+            xg[i] += N[a] * X[a * ND + i];
+#pragma unroll
+            for (int j = 0; j < ND; ++j) J[i][j] += dN[a][i] * X[a * ND + j];
+        }
+    T det, Ji[3][3];
+    if (ND == 2) {
+        det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+        Ji[0][0] = J[1][1] / det; Ji[0][1] = -J[0][1] / det;
+        Ji[1][0] = -J[1][0] / det; Ji[1][1] = J[0][0] / det;
+    } else {
+        const T c00 = J[1][1] * J[2][2] - J[1][2] * J[2][1];
+        const T c01 = J[1][2] * J[2][0] - J[1][0] * J[2][2];
+        const T c02 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+        det = J[0][0] * c00 + J[0][1] * c01 + J[0][2] * c02;
+        Ji[0][0] = c00 / det;
+        Ji[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) / det;
+        Ji[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) / det;
+        Ji[1][0] = c01 / det;
+        Ji[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) / det;
+        Ji[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) / det;
+        Ji[2][0] = c02 / det;
+        Ji[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) / det;
+        Ji[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) / det;
+    }
+    T dx[NEN][3];
+#pragma unroll
+    for (int a = 0; a < NEN; ++a)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            T v = T(0.0);
+            if (j < ND)
+#pragma unroll
+                for (int i = 0; i < ND; ++i) v += Ji[j][i] * dN[a][i];
+            dx[a][j] = v;
+        }
+    const T f = ND == 2 ? t * fabs(det) : fabs(det);
+    T as[3] = {1, 1, 1}, bs[3] = {0, 0, 0};
+#pragma unroll
+    for (int i = 0; i < ND; ++i) {
+        const T r = pow((xoff[i] + xg[i]) * (T)par[3 + ND + i] / L, pm);
+        as[i] = T(1.0) + a0 * r;
+        bs[i] = b0 * r;
+    }
+    // coefficient-weighted stretching combination of the active matrices
+    T s = 0, qx = 0, qy = 0, qz = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        if (A.coef[k] == 0.0 || (ND == 2 && k == 3)) continue;
+        T sk, xk, yk, zk = 0;
+        if (ND == 2) {
+            if (k == 0) { sk = as[0] * as[1]; xk = 0; yk = 0; }
+            else if (k == 1) { sk = as[0] * bs[1] + as[1] * bs[0]; xk = as[1]; yk = as[0]; }
+            else { sk = bs[0] * bs[1]; xk = bs[1]; yk = bs[0]; }
+        } else {
+            if (k == 0) { sk = as[0] * as[1] * as[2]; xk = yk = zk = 0; }
+            else if (k == 1) {
+                sk = as[0] * as[1] * bs[2] + as[0] * bs[1] * as[2] + bs[0] * as[1] * as[2];
+                xk = as[1] * as[2]; yk = as[0] * as[2]; zk = as[0] * as[1];
+            } else if (k == 2) {
+                sk = as[0] * bs[1] * bs[2] + bs[0] * bs[1] * as[2] + bs[0] * as[1] * bs[2];
+                xk = as[1] * bs[2] + as[2] * bs[1]; yk = as[0] * bs[2] + as[2] * bs[0]; zk = as[0] * bs[1] + as[1] * bs[0];
+            } else {
+                sk = bs[0] * bs[1] * bs[2];
+                xk = bs[1] * bs[2]; yk = bs[0] * bs[2]; zk = bs[0] * bs[1];
+            }
+        }
+        const T ck = (T)A.coef[k];
+        s += ck * sk; qx += ck * xk; qy += ck * yk; qz += ck * zk;
+    }
+    // interpolated displacement, stress and displacement gradient at this point
+    T U[3] = {0, 0, 0}, S[NS], Gd[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+#pragma unroll
+    for (int i = 0; i < NS; ++i) S[i] = T(0.0);
+#pragma unroll
+    for (int a = 0; a < NEN; ++a) {
+#pragma unroll
+        for (int d = 0; d < ND; ++d) {
+            const T ua = __shfl_sync(0xffffffffu, uq[d], base + a);
+            U[d] += N[a] * ua;
+#pragma unroll
+            for (int j = 0; j < ND; ++j) Gd[d][j] += ua * dx[a][j];
+        }
+#pragma unroll
+        for (int i = 0; i < NS; ++i) S[i] += N[a] * __shfl_sync(0xffffffffu, uq[ND + i], base + a);
+    }
+    T y[NC];
+#pragma unroll
+    for (int j = 0; j < NEN; ++j) {
+        const T Nj = N[j];
+        T* yj = y + j * NN;
+        if (ND == 2) {
+            const T k2 = s * (lambda + T(2.0) * mu) / T(4.0) / mu / (lambda + mu);
+            const T l2 = s * lambda / T(4.0) / mu / (lambda + mu);
+            yj[0] = f * (rho * s * Nj * U[0] + qx * dx[j][0] * S[0] + qy * dx[j][1] * S[2]);
+            yj[1] = f * (rho * s * Nj * U[1] + qy * dx[j][1] * S[1] + qx * dx[j][0] * S[2]);
+            yj[2] = f * Nj * (-k2 * S[0] + l2 * S[1] + qx * Gd[0][0]);
+            yj[3] = f * Nj * (-k2 * S[1] + l2 * S[0] + qy * Gd[1][1]);
+            yj[4] = f * Nj * (-s / mu * S[2] + qy * Gd[0][1] + qx * Gd[1][0]);
+        } else {
+            const T kap = s * (lambda + mu) / mu / (T(3.0) * lambda + T(2.0) * mu);
+            const T lam = s * lambda / T(2.0) / mu / (T(3.0) * lambda + T(2.0) * mu);
+            const T dxj = dx[j][0], dyj = dx[j][1], dzj = dx[j][2];
+            yj[0] = f * (rho * s * Nj * U[0] + qx * dxj * S[0] + qy * dyj * S[3] + qz * dzj * S[5]);
+            yj[1] = f * (rho * s * Nj * U[1] + qy * dyj * S[1] + qx * dxj * S[3] + qz * dzj * S[4]);
+            yj[2] = f * (rho * s * Nj * U[2] + qz * dzj * S[2] + qx * dxj * S[5] + qy * dyj * S[4]);
+            yj[3] = f * Nj * (-kap * S[0] + lam * (S[1] + S[2]) + qx * Gd[0][0]);
+            yj[4] = f * Nj * (-kap * S[1] + lam * (S[0] + S[2]) + qy * Gd[1][1]);
+            yj[5] = f * Nj * (-kap * S[2] + lam * (S[0] + S[1]) + qz * Gd[2][2]);
+            yj[6] = f * Nj * (-s / mu * S[3] + qy * Gd[0][1] + qx * Gd[1][0]);
+            yj[7] = f * Nj * (-s / mu * S[4] + qz * Gd[1][2] + qy * Gd[2][1]);
+            yj[8] = f * Nj * (-s / mu * S[5] + qz * Gd[0][2] + qx * Gd[2][0]);
+        }
+    }
+#pragma unroll
+    for (int off = 1; off < NEN; off <<= 1)
+#pragma unroll
+        for (int j = 0; j < NC; ++j) y[j] += __shfl_xor_sync(0xffffffffu, y[j], off);
+    if (!valid) return;
+    double* out = A.y + (size_t)ec * NC + q * NN;
+#pragma unroll
+    for (int i = 0; i < NN; ++i) {
+        T mine = 0;
+#pragma unroll
+        for (int a = 0; a < NEN; ++a)
+            if (a == q) mine = y[a * NN + i];
+        double v = (double)mine;
         if (A.ftol >= 0.0 && !(fabs(v) > A.ftol)) v = 0.0;
         v *= A.yscale;
         out[i] = A.accumulate ? out[i] + v : v;
@@ -249,8 +461,35 @@ __global__ void __launch_bounds__(128) k_pml_action(PmlArgs A) {
 int pml_action_launch(int ndim, const PmlArgs& A, cudaStream_t st) {
     if (A.nelem <= 0) return SVL_OK;
     const int tb = 128, gb = (A.nelem + tb - 1) / tb;
-    if (ndim == 2) k_pml_action<2><<<gb, tb, 0, st>>>(A);
-    else k_pml_action<3><<<gb, tb, 0, st>>>(A);
+    // one input vector for every active matrix (an operator application):
+    // the Gauss-point-parallel form
+    bool one = true;
+    const double* u0 = nullptr;
+    for (int k = 0; k < 4; ++k) {
+        if (A.coef[k] == 0.0 || (ndim == 2 && k == 3)) continue;
+        if (!u0) u0 = A.u[k];
+        else if (A.u[k] != u0) one = false;
+    }
+    if (one && A.edof) {
+        const int nen = ndim == 2 ? 4 : 8;
+        const int gg = (int)(((int64_t)A.nelem * nen + tb - 1) / tb);
+        if (A.single) {
+            if (ndim == 2) k_pml_action_gp<2, float><<<gg, tb, 0, st>>>(A);
+            else k_pml_action_gp<3, float><<<gg, tb, 0, st>>>(A);
+        } else {
+            if (ndim == 2) k_pml_action_gp<2, double><<<gg, tb, 0, st>>>(A);
+            else k_pml_action_gp<3, double><<<gg, tb, 0, st>>>(A);
+        }
+        PML_TRY(cudaGetLastError());
+        return SVL_OK;
+    }
+    if (A.single) {
+        if (ndim == 2) k_pml_action<2, float><<<gb, tb, 0, st>>>(A);
+        else k_pml_action<3, float><<<gb, tb, 0, st>>>(A);
+    } else {
+        if (ndim == 2) k_pml_action<2, double><<<gb, tb, 0, st>>>(A);
+        else k_pml_action<3, double><<<gb, tb, 0, st>>>(A);
+    }
     PML_TRY(cudaGetLastError());
     return SVL_OK;
 }

@@ -64,8 +64,8 @@ struct XSolid {
 };
 
 // Strain (engineering shear) of the element vector u at one Gauss point.
-template <int ND, int NEN>
-__device__ __forceinline__ void xstrain(const double (&b)[NEN][3], const double* u, double ev[6]) {
+template <int ND, int NEN, typename T>
+__device__ __forceinline__ void xstrain(const T (&b)[NEN][3], const T* u, T ev[6]) {
 #pragma unroll
     for (int i = 0; i < 6; ++i) ev[i] = 0.0;
 #pragma unroll
@@ -86,8 +86,8 @@ __device__ __forceinline__ void xstrain(const double (&b)[NEN][3], const double*
     }
 }
 // y += w B^T sig (sig in the strain's order: 2D xx yy xy, 3D xx yy zz xy yz zx)
-template <int ND, int NEN>
-__device__ __forceinline__ void xbts(const double (&b)[NEN][3], double w, const double sig[6], double* y) {
+template <int ND, int NEN, typename T>
+__device__ __forceinline__ void xbts(const T (&b)[NEN][3], T w, const T sig[6], T* y) {
 #pragma unroll
     for (int a = 0; a < NEN; ++a) {
         if (ND == 2) {
@@ -102,8 +102,8 @@ __device__ __forceinline__ void xbts(const double (&b)[NEN][3], double w, const 
     }
 }
 // sig = C0 ev with the elastic coefficients c1 c2 c3
-template <int ND>
-__device__ __forceinline__ void xelastic(double c1, double c2, double c3, const double ev[6], double sig[6]) {
+template <int ND, typename T>
+__device__ __forceinline__ void xelastic(T c1, T c2, T c3, const T ev[6], T sig[6]) {
     if (ND == 2) {
         sig[0] = c1 * ev[0] + c2 * ev[1];
         sig[1] = c2 * ev[0] + c1 * ev[1];
@@ -119,42 +119,42 @@ __device__ __forceinline__ void xelastic(double c1, double c2, double c3, const 
 
 // Operator action of one J2 element: the stored tangent on xK, the initial
 // elastic tangent on the stiffness-proportional damping input, lumped mass.
-template <int ND, int NEN>
+template <int ND, int NEN, typename T>
 __device__ void xsolid_j2(const XSolid& S, int e, double ak, double am) {
     constexpr int NC = ND * NEN, PER = NEN * ND + 1, NS = ND == 2 ? 3 : 6;
     const int32_t* ed = S.edof + (size_t)e * NC;
-    double u1[NC], u2[NC], y[NC];
+    T u1[NC], u2[NC], y[NC];
 #pragma unroll
     for (int j = 0; j < NC; ++j) {
         const int t = ed[j];
-        u1[j] = S.xK ? S.xK[t] : 0.0;
-        u2[j] = (S.xK2 && S.cK2 != 0.0) ? S.cK2 * ak * S.xK2[t] : 0.0;
+        u1[j] = (T)(S.xK ? S.xK[t] : 0.0);
+        u2[j] = (T)((S.xK2 && S.cK2 != 0.0) ? S.cK2 * ak * S.xK2[t] : 0.0);
         y[j] = 0.0;
     }
-    const double c1 = S.coef[3 * e], c2 = S.coef[3 * e + 1], c3 = S.coef[3 * e + 2];
+    const T c1 = (T)S.coef[3 * e], c2 = (T)S.coef[3 * e + 1], c3 = (T)S.coef[3 * e + 2];
     const double* g0 = S.geo + (size_t)S.egeo[e] * S.ngp * PER;
     const size_t cs = (size_t)S.ngp * S.n;
     for (int q = 0; q < S.ngp; ++q) {
         const double* g = g0 + q * PER;
-        double b[NEN][3];
+        T b[NEN][3];
 #pragma unroll
         for (int a = 0; a < NEN; ++a)
 #pragma unroll
-            for (int j = 0; j < 3; ++j) b[a][j] = (j < ND) ? g[a * ND + j] : 0.0;
-        const double w = g[PER - 1];
-        double e1[6], e2[6], sig[6];
-        xstrain<ND, NEN>(b, u1, e1);
-        xstrain<ND, NEN>(b, u2, e2);
-        xelastic<ND>(c1, c2, c3, e2, sig);
+            for (int j = 0; j < 3; ++j) b[a][j] = (T)((j < ND) ? g[a * ND + j] : 0.0);
+        const T w = (T)g[PER - 1];
+        T e1[6], e2[6], sig[6];
+        xstrain<ND, NEN, T>(b, u1, e1);
+        xstrain<ND, NEN, T>(b, u2, e2);
+        xelastic<ND, T>(c1, c2, c3, e2, sig);
         const double* ct = S.ctan + (size_t)q * S.n + e;
 #pragma unroll
         for (int a = 0; a < NS; ++a) {
-            double v = 0.0;
+            T v = 0;
 #pragma unroll
-            for (int bb = 0; bb < NS; ++bb) v += ct[(size_t)(a * NS + bb) * cs] * e1[bb];
+            for (int bb = 0; bb < NS; ++bb) v += (T)ct[(size_t)(a * NS + bb) * cs] * e1[bb];
             sig[a] += v;
         }
-        xbts<ND, NEN>(b, w, sig, y);
+        xbts<ND, NEN, T>(b, w, sig, y);
     }
     if (S.xM || S.xM2) {
         const double* ml = S.mlump + (size_t)e * NEN;
@@ -163,13 +163,13 @@ __device__ void xsolid_j2(const XSolid& S, int e, double ak, double am) {
             const int t = ed[j];
             double v = S.xM ? S.sM * S.xM[t] : 0.0;
             if (S.xM2 && S.cM2 != 0.0) v += S.cM2 * am * S.xM2[t];
-            y[j] += ml[j / ND] * v;
+            y[j] += (T)(ml[j / ND] * v);
         }
     }
     double* out = S.y + (size_t)e * NC;
 #pragma unroll
     for (int j = 0; j < NC; ++j) {
-        double v = y[j];
+        double v = (double)y[j];
         if (S.ftol >= 0.0 && !(fabs(v) > S.ftol)) v = 0.0;
         v *= S.yscale;
         out[j] = S.accumulate ? out[j] + v : v;
@@ -214,9 +214,9 @@ __global__ void __launch_bounds__(128) k_xstate(XState S) {
             for (int j = 0; j < 3; ++j) b[a][j] = (j < ND) ? g[a * ND + j] : 0.0;
         const double w = g[PER - 1];
         double ev[6], sig[6];
-        xstrain<ND, NEN>(b, ue, ev);
+        xstrain<ND, NEN, double>(b, ue, ev);
         if (!j2) {
-            xelastic<ND>(c1, c2, c3, ev, sig);
+            xelastic<ND, double>(c1, c2, c3, ev, sig);
         } else {
             const double* p = S.j2p + (size_t)e * 5;
             double st[kJ2State];
@@ -238,7 +238,7 @@ __global__ void __launch_bounds__(128) k_xstate(XState S) {
 #pragma unroll
             for (int i = 0; i < kJ2State; ++i) sp[(size_t)i * gs] = st[i];
         }
-        xbts<ND, NEN>(b, w, sig, fe);
+        xbts<ND, NEN, double>(b, w, sig, fe);
     }
     double* out = S.fint + (size_t)e * NC;
 #pragma unroll
@@ -250,7 +250,8 @@ __global__ void k_xneg(size_t n, const double* __restrict__ a, double* __restric
     if (i < n) out[i] = -a[i];
 }
 
-template <int ND, int NEN>
+// T = double, or float for the inner solver iterations (see k_pml_action)
+template <int ND, int NEN, typename T>
 __global__ void __launch_bounds__(128) k_xsolid(XSolid S) {
     constexpr int NC = ND * NEN, PER = NEN * ND + 1;
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
@@ -258,47 +259,58 @@ __global__ void __launch_bounds__(128) k_xsolid(XSolid S) {
     const int32_t* ed = S.edof + (size_t)e * NC;
     const double am = S.ray ? S.ray[2 * e] : 0.0, ak = S.ray ? S.ray[2 * e + 1] : 0.0;
     if (S.kind && S.kind[e]) {
-        xsolid_j2<ND, NEN>(S, e, ak, am);
+        xsolid_j2<ND, NEN, T>(S, e, ak, am);
         return;
     }
-    double uk[NC], y[NC];
+    T uk[NC], y[NC];
+    // an operator application passes one vector for every input: load it once
+    const bool one = S.xK && S.xK2 == S.xK && S.xM == S.xK && S.xM2 == S.xK;
+    double pm[NC];
 #pragma unroll
     for (int j = 0; j < NC; ++j) {
         const int t = ed[j];
-        double v = S.xK ? S.xK[t] : 0.0;
-        if (S.xK2 && S.cK2 != 0.0) v += S.cK2 * ak * S.xK2[t];
-        uk[j] = v;
-        y[j] = 0.0;
+        double v;
+        if (one) {
+            const double p = S.xK[t];
+            pm[j] = p;
+            v = p;
+            if (S.cK2 != 0.0) v += S.cK2 * ak * p;
+        } else {
+            v = S.xK ? S.xK[t] : 0.0;
+            if (S.xK2 && S.cK2 != 0.0) v += S.cK2 * ak * S.xK2[t];
+        }
+        uk[j] = (T)v;
+        y[j] = 0;
     }
-    const double c1 = S.coef[3 * e], c2 = S.coef[3 * e + 1], c3 = S.coef[3 * e + 2];
+    const T c1 = (T)S.coef[3 * e], c2 = (T)S.coef[3 * e + 1], c3 = (T)S.coef[3 * e + 2];
     const double* g0 = S.geo + (size_t)S.egeo[e] * S.ngp * PER;
     for (int q = 0; q < S.ngp; ++q) {
         const double* g = g0 + q * PER;
-        double b[NEN][3];
+        T b[NEN][3];
 #pragma unroll
         for (int a = 0; a < NEN; ++a)
 #pragma unroll
-            for (int j = 0; j < 3; ++j) b[a][j] = (j < ND) ? g[a * ND + j] : 0.0;
-        const double w = g[PER - 1];
+            for (int j = 0; j < 3; ++j) b[a][j] = (T)((j < ND) ? g[a * ND + j] : 0.0);
+        const T w = (T)g[PER - 1];
         if (ND == 2) {
-            double exx = 0, eyy = 0, gxy = 0;
+            T exx = 0, eyy = 0, gxy = 0;
 #pragma unroll
             for (int a = 0; a < NEN; ++a) {
                 exx += b[a][0] * uk[2 * a];
                 eyy += b[a][1] * uk[2 * a + 1];
                 gxy += b[a][1] * uk[2 * a] + b[a][0] * uk[2 * a + 1];
             }
-            const double s0 = c1 * exx + c2 * eyy, s1 = c2 * exx + c1 * eyy, s2 = c3 * gxy;
+            const T s0 = c1 * exx + c2 * eyy, s1 = c2 * exx + c1 * eyy, s2 = c3 * gxy;
 #pragma unroll
             for (int a = 0; a < NEN; ++a) {
                 y[2 * a] += w * (b[a][0] * s0 + b[a][1] * s2);
                 y[2 * a + 1] += w * (b[a][1] * s1 + b[a][0] * s2);
             }
         } else {
-            double ev[6] = {0, 0, 0, 0, 0, 0};
+            T ev[6] = {0, 0, 0, 0, 0, 0};
 #pragma unroll
             for (int a = 0; a < NEN; ++a) {
-                const double ux = uk[3 * a], uy = uk[3 * a + 1], uz = uk[3 * a + 2];
+                const T ux = uk[3 * a], uy = uk[3 * a + 1], uz = uk[3 * a + 2];
                 ev[0] += b[a][0] * ux;
                 ev[1] += b[a][1] * uy;
                 ev[2] += b[a][2] * uz;
@@ -306,14 +318,14 @@ __global__ void __launch_bounds__(128) k_xsolid(XSolid S) {
                 ev[4] += b[a][2] * uy + b[a][1] * uz;
                 ev[5] += b[a][2] * ux + b[a][0] * uz;
             }
-            double sg[6];
+            T sg[6];
             sg[0] = c1 * ev[0] + c2 * ev[1] + c2 * ev[2];
             sg[1] = c2 * ev[0] + c1 * ev[1] + c2 * ev[2];
             sg[2] = c2 * ev[0] + c2 * ev[1] + c1 * ev[2];
             sg[3] = c3 * ev[3]; sg[4] = c3 * ev[4]; sg[5] = c3 * ev[5];
 #pragma unroll
             for (int a = 0; a < NEN; ++a) {
-                const double bx = b[a][0], by = b[a][1], bz = b[a][2];
+                const T bx = b[a][0], by = b[a][1], bz = b[a][2];
                 y[3 * a] += w * (bx * sg[0] + by * sg[3] + bz * sg[5]);
                 y[3 * a + 1] += w * (by * sg[1] + bx * sg[3] + bz * sg[4]);
                 y[3 * a + 2] += w * (bz * sg[2] + by * sg[4] + bx * sg[5]);
@@ -324,19 +336,120 @@ __global__ void __launch_bounds__(128) k_xsolid(XSolid S) {
         const double* ml = S.mlump + (size_t)e * NEN;
 #pragma unroll
         for (int j = 0; j < NC; ++j) {
-            const int t = ed[j];
-            double v = S.xM ? S.sM * S.xM[t] : 0.0;
-            if (S.xM2 && S.cM2 != 0.0) v += S.cM2 * am * S.xM2[t];
-            y[j] += ml[j / ND] * v;
+            double v;
+            if (one) {
+                v = S.sM * pm[j];
+                if (S.cM2 != 0.0) v += S.cM2 * am * pm[j];
+            } else {
+                const int t = ed[j];
+                v = S.xM ? S.sM * S.xM[t] : 0.0;
+                if (S.xM2 && S.cM2 != 0.0) v += S.cM2 * am * S.xM2[t];
+            }
+            y[j] += (T)(ml[j / ND] * v);
         }
     }
     double* out = S.y + (size_t)e * NC;
 #pragma unroll
     for (int j = 0; j < NC; ++j) {
-        double v = y[j];
+        double v = (double)y[j];
         if (S.ftol >= 0.0 && !(fabs(v) > S.ftol)) v = 0.0;
         v *= S.yscale;
         out[j] = S.accumulate ? out[j] + v : v;
+    }
+}
+
+// Operator action y_e = (K_e + cK2 ak_e K0_e + sM M_e + cM2 am_e M_e) p_e with
+// one thread per (element, Gauss point): the NEN (= number of Gauss points)
+// threads of an element are consecutive lanes of a warp, lane q loads node
+// q's dofs, the element vector reaches the other lanes by shuffles, each lane
+// forms its Gauss point's w B^T sigma and a butterfly over the NEN lanes sums
+// them; lane q adds node q's lumped mass term and writes node q's entries.
+// Eight times the threads of k_xsolid at about a third of its registers: the
+// element-per-thread form is bound by load latency at low occupancy.
+template <int ND, int NEN, typename T>
+__global__ void __launch_bounds__(128) k_xsolid_gp(XSolid S) {
+    constexpr int NC = ND * NEN, PER = NEN * ND + 1, NS = ND == 2 ? 3 : 6;
+    const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int e = gtid / NEN, q = gtid % NEN;
+    const bool valid = e < S.n;
+    const int ec = valid ? e : S.n - 1;
+    const int lane = threadIdx.x & 31, base = lane - q;
+    const int32_t* ed = S.edof + (size_t)ec * NC;
+    const double am = S.ray ? S.ray[2 * ec] : 0.0, ak = S.ray ? S.ray[2 * ec + 1] : 0.0;
+    const bool j2 = S.kind && S.kind[ec];
+    double pq[ND];
+#pragma unroll
+    for (int c = 0; c < ND; ++c) pq[c] = S.xK[ed[q * ND + c]];
+    const double kscale = S.cK2 != 0.0 ? S.cK2 * ak : 0.0;        // stiffness-proportional damping
+    const T c1 = (T)S.coef[3 * ec], c2 = (T)S.coef[3 * ec + 1], c3 = (T)S.coef[3 * ec + 2];
+    const double* g = S.geo + ((size_t)S.egeo[ec] * S.ngp + q) * PER;
+    T b[NEN][3];
+#pragma unroll
+    for (int a = 0; a < NEN; ++a)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) b[a][j] = (T)((j < ND) ? g[a * ND + j] : 0.0);
+    const T w = (T)g[PER - 1];
+    // strain of p at this Gauss point
+    T ev[6] = {0, 0, 0, 0, 0, 0};
+#pragma unroll
+    for (int a = 0; a < NEN; ++a) {
+        T ua[3] = {0, 0, 0};
+#pragma unroll
+        for (int c = 0; c < ND; ++c) ua[c] = __shfl_sync(0xffffffffu, (T)pq[c], base + a);
+        if (ND == 2) {
+            ev[0] += b[a][0] * ua[0];
+            ev[1] += b[a][1] * ua[1];
+            ev[2] += b[a][1] * ua[0] + b[a][0] * ua[1];
+        } else {
+            ev[0] += b[a][0] * ua[0];
+            ev[1] += b[a][1] * ua[1];
+            ev[2] += b[a][2] * ua[2];
+            ev[3] += b[a][1] * ua[0] + b[a][0] * ua[1];
+            ev[4] += b[a][2] * ua[1] + b[a][1] * ua[2];
+            ev[5] += b[a][2] * ua[0] + b[a][0] * ua[2];
+        }
+    }
+    T sig[6];
+    xelastic<ND, T>(c1, c2, c3, ev, sig);
+    if (j2) {
+        // tangent on p plus the initial elastic tangent on kscale p
+        const double* ct = S.ctan + (size_t)q * S.n + ec;
+        const size_t cs = (size_t)S.ngp * S.n;
+#pragma unroll
+        for (int i = 0; i < NS; ++i) {
+            T v = 0;
+#pragma unroll
+            for (int jj = 0; jj < NS; ++jj) v += (T)ct[(size_t)(i * NS + jj) * cs] * ev[jj];
+            sig[i] = (T)kscale * sig[i] + v;
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < NS; ++i) sig[i] *= (T)(1.0 + kscale);
+    }
+    T y[NC];
+#pragma unroll
+    for (int j = 0; j < NC; ++j) y[j] = 0;
+    xbts<ND, NEN, T>(b, w, sig, y);
+#pragma unroll
+    for (int off = 1; off < NEN; off <<= 1)
+#pragma unroll
+        for (int j = 0; j < NC; ++j) y[j] += __shfl_xor_sync(0xffffffffu, y[j], off);
+    if (!valid) return;
+    const double ml = S.mlump[(size_t)ec * NEN + q];
+    double* out = S.y + (size_t)ec * NC + q * ND;
+#pragma unroll
+    for (int c = 0; c < ND; ++c) {
+        T mine = 0;
+#pragma unroll
+        for (int a = 0; a < NEN; ++a)
+            if (a == q) mine = y[a * ND + c];
+        double v = (double)mine;
+        double mv = S.sM * pq[c];
+        if (S.cM2 != 0.0) mv += S.cM2 * am * pq[c];
+        v += ml * mv;
+        if (S.ftol >= 0.0 && !(fabs(v) > S.ftol)) v = 0.0;
+        v *= S.yscale;
+        out[c] = S.accumulate ? out[c] + v : v;
     }
 }
 
@@ -747,22 +860,43 @@ PmlArgs pml_args(svl_xnm* X) {
     P.edof = X->p_edof; P.y = X->fe + (size_t)X->nsol * X->ncs; P.ftol = -1.0; P.yscale = 1.0;
     return P;
 }
-int launch_solid(svl_xnm* X, const XSolid& S) {
+int launch_solid(svl_xnm* X, const XSolid& S, bool single = false) {
     if (S.n <= 0) return SVL_OK;
     const int g = (S.n + 127) / 128;
-    if (X->m.ndim == 2) k_xsolid<2, 4><<<g, 128, 0, X->stream>>>(S);
-    else k_xsolid<3, 8><<<g, 128, 0, X->stream>>>(S);
+    const bool one = S.xK && S.xK2 == S.xK && S.xM == S.xK && S.xM2 == S.xK && S.mlump;
+    if (one) {                                 // operator application: Gauss-point threads
+        const int nen = X->m.nen;
+        const int gg = (int)(((int64_t)S.n * nen + 127) / 128);
+        if (single) {
+            if (X->m.ndim == 2) k_xsolid_gp<2, 4, float><<<gg, 128, 0, X->stream>>>(S);
+            else k_xsolid_gp<3, 8, float><<<gg, 128, 0, X->stream>>>(S);
+        } else {
+            if (X->m.ndim == 2) k_xsolid_gp<2, 4, double><<<gg, 128, 0, X->stream>>>(S);
+            else k_xsolid_gp<3, 8, double><<<gg, 128, 0, X->stream>>>(S);
+        }
+        XCUDA(cudaGetLastError());
+        return SVL_OK;
+    }
+    if (single) {
+        if (X->m.ndim == 2) k_xsolid<2, 4, float><<<g, 128, 0, X->stream>>>(S);
+        else k_xsolid<3, 8, float><<<g, 128, 0, X->stream>>>(S);
+    } else {
+        if (X->m.ndim == 2) k_xsolid<2, 4, double><<<g, 128, 0, X->stream>>>(S);
+        else k_xsolid<3, 8, double><<<g, 128, 0, X->stream>>>(S);
+    }
     XCUDA(cudaGetLastError());
     return SVL_OK;
 }
 
-// out_total = (K + 4/dt^2 M + 2/dt C + dt/3 G) p_total
-int x_op_total(svl_xnm* X, const double* p, double* out) {
+// out_total = (K + 4/dt^2 M + 2/dt C + dt/3 G) p_total; single: element
+// arithmetic in single precision (inner MINRES iterations)
+int x_op_total(svl_xnm* X, const double* p, double* out, bool single = false) {
     const double dt = X->opts.dt, cm = 4.0 / dt / dt, cc = 2.0 / dt;
     XSolid S = solid_args(X);
     S.xK = p; S.xK2 = p; S.cK2 = cc; S.xM = p; S.sM = cm; S.xM2 = p; S.cM2 = cc;
-    XTRY(launch_solid(X, S));
+    XTRY(launch_solid(X, S, single));
     PmlArgs P = pml_args(X);
+    P.single = single ? 1 : 0;
     P.coef[0] = cm; P.coef[1] = cc; P.coef[2] = 1.0; P.coef[3] = (X->m.ndim == 3 && !X->newmark) ? dt / 3.0 : 0.0;
     for (int i = 0; i < 4; ++i) P.u[i] = p;
     XTRY(pml_action_launch(X->m.ndim, P, X->stream));
@@ -770,9 +904,9 @@ int x_op_total(svl_xnm* X, const double* p, double* out) {
 }
 
 // q_free = T^T Keff T v
-int x_apply(svl_xnm* X, const double* v, double* q) {
+int x_apply(svl_xnm* X, const double* v, double* q, bool single = false) {
     k_xexpand<<<grid_of(X->m.ntotal), 256, 0, X->stream>>>(X->m.ntotal, X->Tp, X->Tc, X->Tv, v, X->pt);
-    XTRY(x_op_total(X, X->pt, X->yt));
+    XTRY(x_op_total(X, X->pt, X->yt, single));
     k_xreduce<<<grid_of(X->m.nfree), 256, 0, X->stream>>>(X->m.nfree, X->TTp, X->TTr, X->TTv, X->yt, nullptr, q);
     XCUDA(cudaGetLastError());
     return SVL_OK;
@@ -794,6 +928,10 @@ int x_read(svl_xnm* X, int slot, double* out) {
 // iterate until the true residual meets ||b - A x||_{D^-1} <= tol ||b||_{D^-1}
 // with D = |diag(A)| (the norm MINRES minimises with this preconditioner; the
 // plain 2-norm mixes displacement rows ~1e9 and stress rows ~1e-4 in PML models).
+// The true residual always uses the double-precision operator; the inner
+// iterations may apply it in single precision (opts.single_inner): FP64
+// arithmetic is the scarce resource on this GPU and the element kernels are
+// bound by it, while the restarts keep the result's accuracy.
 int x_solve(svl_xnm* X) {
     const int n = X->m.nfree, g = grid_of(n);
     X->iters_last = 0;
@@ -830,12 +968,17 @@ int x_solve(svl_xnm* X) {
         double beta = beta1, oldb = 0.0, dbar = 0.0, epsln = 0.0, phibar = beta1, cs = -1.0, sn = 0.0;
         XCUDA(cudaMemsetAsync(X->w, 0, sizeof(double) * n, X->stream));
         XCUDA(cudaMemsetAsync(X->w2, 0, sizeof(double) * n, X->stream));
-        const double inner = 0.5 * tol * bs;     // the recurrence estimates ||r||_{D^-1}
+        // the recurrence estimates ||r||_{D^-1}; with single-precision inner
+        // iterations each restart reduces the residual by at most 1e-5 before
+        // the double-precision true residual is formed again (iterative
+        // refinement: the final test is always on the double operator)
+        const bool single = X->opts.single_inner != 0;
+        const double inner = single ? std::max(0.5 * tol * bs, 1e-5 * beta1) : 0.5 * tol * bs;
         for (int it = 0; its < X->opts.maxit; ++it) {
             ++its;
             // v = y / beta; y = A v - (beta / oldb) r1 - (alfa / beta) r2
             k_xaxpby<<<g, 256, 0, X->stream>>>(n, 1.0 / beta, X->yv, 0.0, X->v);
-            XTRY(x_apply(X, X->v, X->yv));
+            XTRY(x_apply(X, X->v, X->yv, single));
             if (it > 0) k_xaxpby<<<g, 256, 0, X->stream>>>(n, -beta / oldb, X->r1, 1.0, X->yv);
             XTRY(x_dot(X, X->v, X->yv, 1));
             double alfa = 0.0;

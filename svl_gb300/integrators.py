@@ -183,10 +183,14 @@ class ExtendedNewmarkBeta:
 
     def __init__(self, model: Model, loads: Loads | None, dt: float, tol: float = 1e-10,
                  solver_maxit: int = 100000, ftol: float = 1e-12, mtol: float = 1e-12, algorithm: str = "linear",
-                 maxit: int = 50, cnvgtol: float = 1e-6, cnvgtest: int = 4, integrator: str = "extendednewmark"):
+                 maxit: int = 50, cnvgtol: float = 1e-6, cnvgtest: int = 4, integrator: str = "extendednewmark",
+                 single_inner: bool = True):
         """integrator "extendednewmark" (ExtendedNewmarkBeta.cpp) or "newmark"
         (NewmarkBeta.cpp on the same elements: the PML history matrix is not
-        used; NewmarkBeta(model with PML layers, ...) builds this)."""
+        used; NewmarkBeta(model with PML layers, ...) builds this).
+        single_inner: the inner MINRES iterations apply the element operators
+        in single precision, the restarts' true residual and the stopping test
+        stay in double (iterative refinement)."""
         self.model = model
         self.dt = float(dt)
         self._md = model.desc()
@@ -195,7 +199,7 @@ class ExtendedNewmarkBeta:
         integ = {"extendednewmark": capi.SVL_XNM_EXTENDED_NEWMARK, "newmark": capi.SVL_XNM_NEWMARK}[integrator.lower()]
         opts = capi.XnmOpts(dt=self.dt, ftol=ftol, mtol=mtol, tol=float(tol), maxit=int(solver_maxit),
                             algorithm=algo, newton_maxit=int(maxit), cnvgtest=int(cnvgtest), cnvgtol=float(cnvgtol),
-                            integrator=integ)
+                            integrator=integ, single_inner=1 if single_inner else 0)
         h = C.c_void_p()
         check(lib().svl_xnm_create(C.byref(self._md), C.byref(self._ld), C.byref(opts), C.byref(h)))
         self._h = h
