@@ -120,7 +120,15 @@ struct PmlArgs {
     double yscale;         // y is scaled by this after the filter
     int accumulate;        // 1: y += result
     int single;            // 1: single-precision arithmetic (inner solver iterations)
+    const float* tab;      // [nelem][pml_tab_stride(nd)] single-precision element constants
+                           // (pml_tab_fill), or null; used by the single-precision operator
+    float coef_f[4];       // coef in single precision (set by pml_action_launch)
 };
+// per element: node coordinates relative to node 0 [nen][nd], node 0 - x0 [nd],
+// n [nd], then mu, lambda, rho, a0, b0, m, L, thickness
+inline int pml_tab_stride(int nd) { return ((nd == 2 ? 4 : 8) * nd + 2 * nd + 8 + 3) / 4 * 4; }
+void pml_tab_fill(int nd, int nelem, const double* X, const double* mat, const double* thick, const double* par,
+                  std::vector<float>& tab);
 int pml_action_launch(int ndim, const PmlArgs& A, cudaStream_t st);
 
 // T (total <- free) rows as CSR over total dofs, sorted columns, duplicates summed.

@@ -16,6 +16,7 @@
 // ax by + ay bx); G: s = bx by bz, q = (by bz, bx bz, bx by); in 2D M: ax ay,
 // C: ax by + ay bx with q = (ay, ax), K: bx by with q = (by, bx), no G).
 #include <cmath>
+#include <type_traits>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -272,27 +273,43 @@ __global__ void __launch_bounds__(128) k_pml_action_gp(PmlArgs A) {
     const bool valid = e < A.nelem;
     const int ec = valid ? e : A.nelem - 1;
     const int lane = threadIdx.x & 31, base = lane - q;
-    const double* Xd = A.X + (size_t)ec * NEN * ND;
-    const double* par = A.par + (size_t)ec * NPAR;
-    const T E = (T)A.mat[3 * ec], nu = (T)A.mat[3 * ec + 1], rho = (T)A.mat[3 * ec + 2];
-    const T mu = E / T(2.0) / (T(1.0) + nu);
-    const T lambda = E * nu / (T(1.0) + nu) / (T(1.0) - T(2.0) * nu);
-    const T Vp = sqrt((lambda + T(2.0) * mu) / rho);
-    const T pm = (T)par[0], L = (T)par[1], R = (T)par[2];
-    const T lr = log(T(1.0) / R);
-    const T a0 = (pm + T(1.0)) * (L / T(10.0)) / T(2.0) / L * lr;
-    const T b0 = (pm + T(1.0)) * Vp / T(2.0) / L * lr;
-    const T t = (T)((ND == 2 && A.thick) ? A.thick[ec] : 1.0);
+    T X[NEN * ND], xoff[3] = {0, 0, 0}, nrm[3] = {0, 0, 0};
+    T mu, lambda, rho, a0, b0, pm, L, t;
+    if constexpr (std::is_same<T, float>::value) {
+        // precomputed single-precision constants (conversions from double run
+        // at the FP64 rate on this GPU)
+        constexpr int TS = (NEN * ND + 2 * ND + 8 + 3) / 4 * 4;      // pml_tab_stride(ND)
+        const float* tb = A.tab + (size_t)ec * TS;
+#pragma unroll
+        for (int i = 0; i < NEN * ND; ++i) X[i] = tb[i];
+#pragma unroll
+        for (int i = 0; i < ND; ++i) { xoff[i] = tb[NEN * ND + i]; nrm[i] = tb[NEN * ND + ND + i]; }
+        const float* c = tb + NEN * ND + 2 * ND;
+        mu = c[0]; lambda = c[1]; rho = c[2]; a0 = c[3]; b0 = c[4]; pm = c[5]; L = c[6]; t = c[7];
+    } else {
+        const double* Xd = A.X + (size_t)ec * NEN * ND;
+        const double* par = A.par + (size_t)ec * NPAR;
+        const T E = (T)A.mat[3 * ec], nu = (T)A.mat[3 * ec + 1];
+        rho = (T)A.mat[3 * ec + 2];
+        mu = E / T(2.0) / (T(1.0) + nu);
+        lambda = E * nu / (T(1.0) + nu) / (T(1.0) - T(2.0) * nu);
+        const T Vp = sqrt((lambda + T(2.0) * mu) / rho);
+        pm = (T)par[0]; L = (T)par[1];
+        const T R = (T)par[2];
+        const T lr = log(T(1.0) / R);
+        a0 = (pm + T(1.0)) * (L / T(10.0)) / T(2.0) / L * lr;
+        b0 = (pm + T(1.0)) * Vp / T(2.0) / L * lr;
+        t = (T)((ND == 2 && A.thick) ? A.thick[ec] : 1.0);
+#pragma unroll
+        for (int i = 0; i < NEN * ND; ++i) X[i] = (T)(Xd[i] - Xd[i % ND]);
+#pragma unroll
+        for (int i = 0; i < ND; ++i) { xoff[i] = (T)(Xd[i] - par[3 + i]); nrm[i] = (T)par[3 + ND + i]; }
+    }
     const T g = (T)0.577350269189626;       // GaussQuadrature.cpp:303-316
-    T X[NEN * ND], xoff[3] = {0, 0, 0};
-#pragma unroll
-    for (int i = 0; i < NEN * ND; ++i) X[i] = (T)(Xd[i] - Xd[i % ND]);
-#pragma unroll
-    for (int i = 0; i < ND; ++i) xoff[i] = (T)(Xd[i] - par[3 + i]);
     // this lane's node dofs
     const double* u0 = nullptr;
     for (int k = 0; k < 4; ++k)
-        if (A.coef[k] != 0.0 && !(ND == 2 && k == 3)) { u0 = A.u[k]; break; }
+        if (A.coef_f[k] != 0.0f && !(ND == 2 && k == 3)) { u0 = A.u[k]; break; }
     T uq[NN];
 #pragma unroll
     for (int i = 0; i < NN; ++i)
@@ -365,7 +382,7 @@ __global__ void __launch_bounds__(128) k_pml_action_gp(PmlArgs A) {
     T as[3] = {1, 1, 1}, bs[3] = {0, 0, 0};
 #pragma unroll
     for (int i = 0; i < ND; ++i) {
-        const T r = pow((xoff[i] + xg[i]) * (T)par[3 + ND + i] / L, pm);
+        const T r = pow((xoff[i] + xg[i]) * nrm[i] / L, pm);
         as[i] = T(1.0) + a0 * r;
         bs[i] = b0 * r;
     }
@@ -373,7 +390,10 @@ __global__ void __launch_bounds__(128) k_pml_action_gp(PmlArgs A) {
     T s = 0, qx = 0, qy = 0, qz = 0;
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
-        if (A.coef[k] == 0.0 || (ND == 2 && k == 3)) continue;
+        T ck;
+        if constexpr (std::is_same<T, float>::value) ck = A.coef_f[k];
+        else ck = A.coef[k];
+        if (ck == T(0.0) || (ND == 2 && k == 3)) continue;
         T sk, xk, yk, zk = 0;
         if (ND == 2) {
             if (k == 0) { sk = as[0] * as[1]; xk = 0; yk = 0; }
@@ -392,7 +412,6 @@ __global__ void __launch_bounds__(128) k_pml_action_gp(PmlArgs A) {
                 xk = bs[1] * bs[2]; yk = bs[0] * bs[2]; zk = bs[0] * bs[1];
             }
         }
-        const T ck = (T)A.coef[k];
         s += ck * sk; qx += ck * xk; qy += ck * yk; qz += ck * zk;
     }
     // interpolated displacement, stress and displacement gradient at this point
@@ -458,6 +477,28 @@ __global__ void __launch_bounds__(128) k_pml_action_gp(PmlArgs A) {
     }
 }
 
+void pml_tab_fill(int nd, int nelem, const double* X, const double* mat, const double* thick, const double* par,
+                  std::vector<float>& tab) {
+    const int nen = nd == 2 ? 4 : 8, npar = 3 + 2 * nd, st = pml_tab_stride(nd);
+    tab.assign((size_t)nelem * st, 0.0f);
+    for (int e = 0; e < nelem; ++e) {
+        float* t = &tab[(size_t)e * st];
+        const double* x = X + (size_t)e * nen * nd;
+        const double* p = par + (size_t)e * npar;
+        for (int i = 0; i < nen * nd; ++i) t[i] = (float)(x[i] - x[i % nd]);
+        for (int i = 0; i < nd; ++i) { t[nen * nd + i] = (float)(x[i] - p[3 + i]); t[nen * nd + nd + i] = (float)p[3 + nd + i]; }
+        const double E = mat[3 * e], nu = mat[3 * e + 1], rho = mat[3 * e + 2];
+        const double mu = E / 2.0 / (1 + nu), lambda = E * nu / (1.0 + nu) / (1.0 - 2.0 * nu);
+        const double Vp = std::sqrt((lambda + 2.0 * mu) / rho);
+        const double m = p[0], L = p[1], R = p[2];
+        float* c = t + nen * nd + 2 * nd;
+        c[0] = (float)mu; c[1] = (float)lambda; c[2] = (float)rho;
+        c[3] = (float)((m + 1.0) * (L / 10.0) / 2.0 / L * std::log(1.0 / R));
+        c[4] = (float)((m + 1.0) * Vp / 2.0 / L * std::log(1.0 / R));
+        c[5] = (float)m; c[6] = (float)L; c[7] = (float)((nd == 2 && thick) ? thick[e] : 1.0);
+    }
+}
+
 int pml_action_launch(int ndim, const PmlArgs& A, cudaStream_t st) {
     if (A.nelem <= 0) return SVL_OK;
     const int tb = 128, gb = (A.nelem + tb - 1) / tb;
@@ -470,15 +511,17 @@ int pml_action_launch(int ndim, const PmlArgs& A, cudaStream_t st) {
         if (!u0) u0 = A.u[k];
         else if (A.u[k] != u0) one = false;
     }
-    if (one && A.edof) {
+    if (one && A.edof && (!A.single || A.tab)) {
         const int nen = ndim == 2 ? 4 : 8;
         const int gg = (int)(((int64_t)A.nelem * nen + tb - 1) / tb);
+        PmlArgs B = A;
+        for (int k = 0; k < 4; ++k) B.coef_f[k] = (float)A.coef[k];
         if (A.single) {
-            if (ndim == 2) k_pml_action_gp<2, float><<<gg, tb, 0, st>>>(A);
-            else k_pml_action_gp<3, float><<<gg, tb, 0, st>>>(A);
+            if (ndim == 2) k_pml_action_gp<2, float><<<gg, tb, 0, st>>>(B);
+            else k_pml_action_gp<3, float><<<gg, tb, 0, st>>>(B);
         } else {
-            if (ndim == 2) k_pml_action_gp<2, double><<<gg, tb, 0, st>>>(A);
-            else k_pml_action_gp<3, double><<<gg, tb, 0, st>>>(A);
+            if (ndim == 2) k_pml_action_gp<2, double><<<gg, tb, 0, st>>>(B);
+            else k_pml_action_gp<3, double><<<gg, tb, 0, st>>>(B);
         }
         PML_TRY(cudaGetLastError());
         return SVL_OK;

@@ -24,6 +24,7 @@
 #include <cmath>
 #include <cstring>
 #include <map>
+#include <type_traits>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -55,6 +56,10 @@ struct XSolid {
     const double* coef;      // [n][3] c1 c2 c3 of the initial elastic tangent
     const int32_t* kind;     // [n] 1 for a J2 element, or null (all elastic)
     const double* ctan;      // [NS*NS][ngp][n] J2 tangents of the last update
+    const float* geo_f;      // single-precision copies for the single-precision
+    const float* ctan_f;     // operator (conversions from double run at the FP64 rate)
+    const float* opf;        // [n][NEN + 4] operator constants of Keff: m_a (4/dt^2 + 2/dt am),
+                             // 2/dt ak, c1, c2, c3 (single-precision operator only)
     const double* ray;       // [n][2] am ak, or null
     const double* mlump;     // [n][NEN] row-sum lumped mass per element node
     const double *xK, *xK2, *xM, *xM2;   // total-dof inputs (null = 0)
@@ -187,6 +192,7 @@ struct XState {
     const double* j2p;       // [n][5] K G H beta SY
     double* state;           // [13][ngp][n]
     double* ctan;            // [NS*NS][ngp][n]
+    float* ctan_f;           // [NS*NS][ngp][n] single-precision copy, or null
     const double* Us;
     double ftol;
     double* fint;            // [n][NC]
@@ -234,6 +240,13 @@ __global__ void __launch_bounds__(128) k_xstate(XState S) {
                 j2_return<3>(Ev, st, p[0], p[1], p[2], p[3], p[4], s6, S.ctan + (size_t)q * S.n + e, gs);
 #pragma unroll
                 for (int i = 0; i < 6; ++i) sig[i] = s6[i];
+            }
+            if (S.ctan_f) {
+                constexpr int NS = ND == 2 ? 3 : 6;
+                const double* ct = S.ctan + (size_t)q * S.n + e;
+                float* cf = S.ctan_f + (size_t)q * S.n + e;
+#pragma unroll
+                for (int i = 0; i < NS * NS; ++i) cf[(size_t)i * gs] = (float)ct[(size_t)i * gs];
             }
 #pragma unroll
             for (int i = 0; i < kJ2State; ++i) sp[(size_t)i * gs] = st[i];
@@ -375,27 +388,47 @@ __global__ void __launch_bounds__(128) k_xsolid_gp(XSolid S) {
     const int ec = valid ? e : S.n - 1;
     const int lane = threadIdx.x & 31, base = lane - q;
     const int32_t* ed = S.edof + (size_t)ec * NC;
-    const double am = S.ray ? S.ray[2 * ec] : 0.0, ak = S.ray ? S.ray[2 * ec + 1] : 0.0;
     const bool j2 = S.kind && S.kind[ec];
     double pq[ND];
 #pragma unroll
     for (int c = 0; c < ND; ++c) pq[c] = S.xK[ed[q * ND + c]];
-    const double kscale = S.cK2 != 0.0 ? S.cK2 * ak : 0.0;        // stiffness-proportional damping
-    const T c1 = (T)S.coef[3 * ec], c2 = (T)S.coef[3 * ec + 1], c3 = (T)S.coef[3 * ec + 2];
-    const double* g = S.geo + ((size_t)S.egeo[ec] * S.ngp + q) * PER;
-    T b[NEN][3];
+    double am = 0.0;
+    T kscale, c1, c2, c3;                      // kscale: stiffness-proportional damping factor
+    if constexpr (std::is_same<T, float>::value) {
+        const float* o = S.opf + (size_t)ec * (NEN + 4);
+        kscale = o[NEN]; c1 = o[NEN + 1]; c2 = o[NEN + 2]; c3 = o[NEN + 3];
+    } else {
+        am = S.ray ? S.ray[2 * ec] : 0.0;
+        const double ak = S.ray ? S.ray[2 * ec + 1] : 0.0;
+        kscale = S.cK2 != 0.0 ? S.cK2 * ak : 0.0;
+        c1 = S.coef[3 * ec]; c2 = S.coef[3 * ec + 1]; c3 = S.coef[3 * ec + 2];
+    }
+    T b[NEN][3], w;
+    if constexpr (std::is_same<T, float>::value) {
+        const float* g = S.geo_f + ((size_t)S.egeo[ec] * S.ngp + q) * PER;
 #pragma unroll
-    for (int a = 0; a < NEN; ++a)
+        for (int a = 0; a < NEN; ++a)
 #pragma unroll
-        for (int j = 0; j < 3; ++j) b[a][j] = (T)((j < ND) ? g[a * ND + j] : 0.0);
-    const T w = (T)g[PER - 1];
+            for (int j = 0; j < 3; ++j) b[a][j] = (j < ND) ? g[a * ND + j] : 0.0f;
+        w = g[PER - 1];
+    } else {
+        const double* g = S.geo + ((size_t)S.egeo[ec] * S.ngp + q) * PER;
+#pragma unroll
+        for (int a = 0; a < NEN; ++a)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) b[a][j] = (j < ND) ? g[a * ND + j] : 0.0;
+        w = g[PER - 1];
+    }
     // strain of p at this Gauss point
     T ev[6] = {0, 0, 0, 0, 0, 0};
+    T pt[ND];
+#pragma unroll
+    for (int c = 0; c < ND; ++c) pt[c] = (T)pq[c];
 #pragma unroll
     for (int a = 0; a < NEN; ++a) {
         T ua[3] = {0, 0, 0};
 #pragma unroll
-        for (int c = 0; c < ND; ++c) ua[c] = __shfl_sync(0xffffffffu, (T)pq[c], base + a);
+        for (int c = 0; c < ND; ++c) ua[c] = __shfl_sync(0xffffffffu, pt[c], base + a);
         if (ND == 2) {
             ev[0] += b[a][0] * ua[0];
             ev[1] += b[a][1] * ua[1];
@@ -413,18 +446,22 @@ __global__ void __launch_bounds__(128) k_xsolid_gp(XSolid S) {
     xelastic<ND, T>(c1, c2, c3, ev, sig);
     if (j2) {
         // tangent on p plus the initial elastic tangent on kscale p
-        const double* ct = S.ctan + (size_t)q * S.n + ec;
         const size_t cs = (size_t)S.ngp * S.n;
 #pragma unroll
         for (int i = 0; i < NS; ++i) {
             T v = 0;
 #pragma unroll
-            for (int jj = 0; jj < NS; ++jj) v += (T)ct[(size_t)(i * NS + jj) * cs] * ev[jj];
-            sig[i] = (T)kscale * sig[i] + v;
+            for (int jj = 0; jj < NS; ++jj) {
+                T c;
+                if constexpr (std::is_same<T, float>::value) c = S.ctan_f[(size_t)(i * NS + jj) * cs + (size_t)q * S.n + ec];
+                else c = S.ctan[(size_t)(i * NS + jj) * cs + (size_t)q * S.n + ec];
+                v += c * ev[jj];
+            }
+            sig[i] = kscale * sig[i] + v;
         }
     } else {
 #pragma unroll
-        for (int i = 0; i < NS; ++i) sig[i] *= (T)(1.0 + kscale);
+        for (int i = 0; i < NS; ++i) sig[i] *= (T(1.0) + kscale);
     }
     T y[NC];
 #pragma unroll
@@ -435,18 +472,27 @@ __global__ void __launch_bounds__(128) k_xsolid_gp(XSolid S) {
 #pragma unroll
         for (int j = 0; j < NC; ++j) y[j] += __shfl_xor_sync(0xffffffffu, y[j], off);
     if (!valid) return;
-    const double ml = S.mlump[(size_t)ec * NEN + q];
     double* out = S.y + (size_t)ec * NC + q * ND;
+    // single precision: the mass term from the table (one conversion per value)
+    float mmf = 0.0f;
+    double ml = 0.0;
+    if constexpr (std::is_same<T, float>::value) mmf = S.opf[(size_t)ec * (NEN + 4) + q];
+    else ml = S.mlump[(size_t)ec * NEN + q];
 #pragma unroll
     for (int c = 0; c < ND; ++c) {
         T mine = 0;
 #pragma unroll
         for (int a = 0; a < NEN; ++a)
             if (a == q) mine = y[a * ND + c];
-        double v = (double)mine;
-        double mv = S.sM * pq[c];
-        if (S.cM2 != 0.0) mv += S.cM2 * am * pq[c];
-        v += ml * mv;
+        double v;
+        if constexpr (std::is_same<T, float>::value) {
+            v = (double)(mine + mmf * pt[c]);
+        } else {
+            v = (double)mine;
+            double mv = S.sM * pq[c];
+            if (S.cM2 != 0.0) mv += S.cM2 * am * pq[c];
+            v += ml * mv;
+        }
         if (S.ftol >= 0.0 && !(fabs(v) > S.ftol)) v = 0.0;
         v *= S.yscale;
         out[c] = S.accumulate ? out[c] + v : v;
@@ -752,9 +798,12 @@ struct svl_xnm {
     int32_t *s_edof = nullptr, *s_egeo = nullptr, *s_kind = nullptr;
     double *s_geo = nullptr, *s_coef = nullptr, *s_ray = nullptr, *s_mlump = nullptr;
     double *s_j2p = nullptr, *s_state = nullptr, *s_ctan = nullptr, *s_fint = nullptr;
+    float *s_geo_f = nullptr, *s_ctan_f = nullptr;   // single-precision copies
+    float* s_opf = nullptr;                           // [nsol][nen + 4] (XSolid::opf)
     bool has_j2 = false, newton = false;
     // PML elements
     double *p_X = nullptr, *p_mat = nullptr, *p_thick = nullptr, *p_par = nullptr;
+    float* p_tab = nullptr;                  // single-precision element constants
     int32_t* p_edof = nullptr;
     // element vectors and their ordered gather
     double* fe = nullptr;
@@ -836,7 +885,7 @@ int x_gather(svl_xnm* X, double* y, double cn, const double* xn, double cdp, con
 XSolid solid_args(svl_xnm* X) {
     XSolid S{};
     S.n = X->nsol; S.ngp = X->m.ngp; S.edof = X->s_edof; S.egeo = X->s_egeo; S.geo = X->s_geo;
-    S.coef = X->s_coef; S.kind = X->s_kind; S.ctan = X->s_ctan;
+    S.coef = X->s_coef; S.kind = X->s_kind; S.ctan = X->s_ctan; S.geo_f = X->s_geo_f; S.ctan_f = X->s_ctan_f;
     S.ray = X->s_ray; S.mlump = X->s_mlump; S.ftol = -1.0; S.yscale = 1.0;
     S.y = X->fe;
     return S;
@@ -847,6 +896,7 @@ int x_state(svl_xnm* X) {
     XState S{};
     S.n = X->nsol; S.ngp = X->m.ngp; S.edof = X->s_edof; S.egeo = X->s_egeo; S.geo = X->s_geo;
     S.coef = X->s_coef; S.kind = X->s_kind; S.j2p = X->s_j2p; S.state = X->s_state; S.ctan = X->s_ctan;
+    S.ctan_f = X->s_ctan_f;
     S.Us = X->Us; S.ftol = X->opts.ftol; S.fint = X->s_fint;
     const int g = (S.n + 127) / 128;
     if (X->m.ndim == 2) k_xstate<2, 4><<<g, 128, 0, X->stream>>>(S);
@@ -858,12 +908,13 @@ PmlArgs pml_args(svl_xnm* X) {
     PmlArgs P{};
     P.nelem = X->npml; P.X = X->p_X; P.mat = X->p_mat; P.thick = X->p_thick; P.par = X->p_par;
     P.edof = X->p_edof; P.y = X->fe + (size_t)X->nsol * X->ncs; P.ftol = -1.0; P.yscale = 1.0;
+    P.tab = X->p_tab;
     return P;
 }
 int launch_solid(svl_xnm* X, const XSolid& S, bool single = false) {
     if (S.n <= 0) return SVL_OK;
     const int g = (S.n + 127) / 128;
-    const bool one = S.xK && S.xK2 == S.xK && S.xM == S.xK && S.xM2 == S.xK && S.mlump;
+    const bool one = S.xK && S.xK2 == S.xK && S.xM == S.xK && S.xM2 == S.xK && S.mlump && (!single || S.opf);
     if (one) {                                 // operator application: Gauss-point threads
         const int nen = X->m.nen;
         const int gg = (int)(((int64_t)S.n * nen + 127) / 128);
@@ -894,6 +945,7 @@ int x_op_total(svl_xnm* X, const double* p, double* out, bool single = false) {
     const double dt = X->opts.dt, cm = 4.0 / dt / dt, cc = 2.0 / dt;
     XSolid S = solid_args(X);
     S.xK = p; S.xK2 = p; S.cK2 = cc; S.xM = p; S.sM = cm; S.xM2 = p; S.cM2 = cc;
+    S.opf = X->s_opf;                          // built for exactly these coefficients
     XTRY(launch_solid(X, S, single));
     PmlArgs P = pml_args(X);
     P.single = single ? 1 : 0;
@@ -1318,6 +1370,21 @@ int x_setup(svl_xnm* X, const svl_load_desc* L) {
     }
     // uploads
     XTRY(X->upload(s_edof, &X->s_edof)); XTRY(X->upload(s_egeo, &X->s_egeo)); XTRY(X->upload(s_geo, &X->s_geo));
+    {
+        std::vector<float> gf(s_geo.begin(), s_geo.end());
+        XTRY(X->upload(gf, &X->s_geo_f));
+        // single-precision operator constants of Keff = K + 4/dt^2 M + 2/dt C
+        std::vector<float> opf((size_t)X->nsol * (nen + 4));
+        for (int i = 0; i < X->nsol; ++i) {
+            const int e = sol[i];
+            const double am = m.ray.empty() ? 0.0 : m.ray[2 * (size_t)e], ak = m.ray.empty() ? 0.0 : m.ray[2 * (size_t)e + 1];
+            float* o = &opf[(size_t)i * (nen + 4)];
+            for (int a = 0; a < nen; ++a) o[a] = (float)(s_ml[(size_t)i * nen + a] * (cm + cc * am));
+            o[nen] = (float)(cc * ak);
+            for (int j = 0; j < 3; ++j) o[nen + 1 + j] = (float)s_coef[3 * (size_t)i + j];
+        }
+        XTRY(X->upload(opf, &X->s_opf));
+    }
     XTRY(X->upload(s_coef, &X->s_coef)); XTRY(X->upload(s_ml, &X->s_mlump));
     XTRY(X->alloc((size_t)X->nsol * X->ncs, &X->s_fint));
     if (X->has_j2) {
@@ -1325,10 +1392,16 @@ int x_setup(svl_xnm* X, const svl_load_desc* L) {
         XTRY(X->upload(s_kind, &X->s_kind)); XTRY(X->upload(s_j2p, &X->s_j2p));
         XTRY(X->alloc((size_t)kJ2State * m.ngp * X->nsol, &X->s_state));
         XTRY(X->alloc((size_t)ns * ns * m.ngp * X->nsol, &X->s_ctan));
+        XTRY(X->alloc((size_t)ns * ns * m.ngp * X->nsol, &X->s_ctan_f));
     }
     if (!s_ray.empty()) XTRY(X->upload(s_ray, &X->s_ray));
     XTRY(X->upload(p_X, &X->p_X)); XTRY(X->upload(p_mat, &X->p_mat)); XTRY(X->upload(p_thick, &X->p_thick));
     XTRY(X->upload(p_par, &X->p_par)); XTRY(X->upload(p_edof, &X->p_edof));
+    if (X->npml > 0) {
+        std::vector<float> tab;
+        pml_tab_fill(nd, X->npml, p_X.data(), p_mat.data(), nd == 2 ? p_thick.data() : nullptr, p_par.data(), tab);
+        XTRY(X->upload(tab, &X->p_tab));
+    }
     XTRY(X->alloc((size_t)X->nsol * X->ncs + (size_t)X->npml * X->ncp, &X->fe));
     XTRY(X->upload(inv_ptr, &X->inv_ptr)); XTRY(X->upload(inv_idx, &X->inv_idx));
     if (!m.dp_eta.empty()) {                 // ZeroLength1D dashpots
