@@ -123,6 +123,8 @@ struct PmlArgs {
     const float* tab;      // [nelem][pml_tab_stride(nd)] single-precision element constants
                            // (pml_tab_fill), or null; used by the single-precision operator
     float coef_f[4];       // coef in single precision (set by pml_action_launch)
+    const float* u_f;      // single precision, gather mode: the input vector in float and
+    float* y_f;            // the element vectors in float (no filter, scale or accumulate)
 };
 // per element: node coordinates relative to node 0 [nen][nd], node 0 - x0 [nd],
 // n [nd], then mu, lambda, rho, a0, b0, m, L, thickness

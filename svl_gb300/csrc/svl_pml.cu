@@ -311,9 +311,14 @@ __global__ void __launch_bounds__(128) k_pml_action_gp(PmlArgs A) {
     for (int k = 0; k < 4; ++k)
         if (A.coef_f[k] != 0.0f && !(ND == 2 && k == 3)) { u0 = A.u[k]; break; }
     T uq[NN];
+    if constexpr (std::is_same<T, float>::value) {
 #pragma unroll
-    for (int i = 0; i < NN; ++i)
-        uq[i] = u0 ? (T)(A.edof ? u0[A.edof[(size_t)ec * NC + q * NN + i]] : u0[(size_t)ec * NC + q * NN + i]) : T(0.0);
+        for (int i = 0; i < NN; ++i) uq[i] = u0 ? A.u_f[A.edof[(size_t)ec * NC + q * NN + i]] : 0.0f;
+    } else {
+#pragma unroll
+        for (int i = 0; i < NN; ++i)
+            uq[i] = u0 ? (T)(A.edof ? u0[A.edof[(size_t)ec * NC + q * NN + i]] : u0[(size_t)ec * NC + q * NN + i]) : T(0.0);
+    }
     // Gauss point q
     const T xi[3] = {(q & 1) ? g : -g, (q & 2) ? g : -g, (q & 4) ? g : -g};
     T N[NEN], dN[NEN][3];
@@ -463,6 +468,18 @@ __global__ void __launch_bounds__(128) k_pml_action_gp(PmlArgs A) {
 #pragma unroll
         for (int j = 0; j < NC; ++j) y[j] += __shfl_xor_sync(0xffffffffu, y[j], off);
     if (!valid) return;
+    if constexpr (std::is_same<T, float>::value) {
+        float* outf = A.y_f + (size_t)ec * NC + q * NN;
+#pragma unroll
+        for (int i = 0; i < NN; ++i) {
+            T mine = 0;
+#pragma unroll
+            for (int a = 0; a < NEN; ++a)
+                if (a == q) mine = y[a * NN + i];
+            outf[i] = mine;
+        }
+        return;
+    }
     double* out = A.y + (size_t)ec * NC + q * NN;
 #pragma unroll
     for (int i = 0; i < NN; ++i) {
@@ -511,7 +528,7 @@ int pml_action_launch(int ndim, const PmlArgs& A, cudaStream_t st) {
         if (!u0) u0 = A.u[k];
         else if (A.u[k] != u0) one = false;
     }
-    if (one && A.edof && (!A.single || A.tab)) {
+    if (one && A.edof && (!A.single || (A.tab && A.u_f && A.y_f))) {
         const int nen = ndim == 2 ? 4 : 8;
         const int gg = (int)(((int64_t)A.nelem * nen + tb - 1) / tb);
         PmlArgs B = A;

@@ -60,6 +60,8 @@ struct XSolid {
     const float* ctan_f;     // operator (conversions from double run at the FP64 rate)
     const float* opf;        // [n][NEN + 4] operator constants of Keff: m_a (4/dt^2 + 2/dt am),
                              // 2/dt ak, c1, c2, c3 (single-precision operator only)
+    const float* xK_f;       // single-precision operator: the input vector and the
+    float* y_f;              // element vectors in float (no filter, scale or accumulate)
     const double* ray;       // [n][2] am ak, or null
     const double* mlump;     // [n][NEN] row-sum lumped mass per element node
     const double *xK, *xK2, *xM, *xM2;   // total-dof inputs (null = 0)
@@ -80,7 +82,7 @@ __device__ __forceinline__ void xstrain(const T (&b)[NEN][3], const T* u, T ev[6
             ev[1] += b[a][1] * u[2 * a + 1];
             ev[2] += b[a][1] * u[2 * a] + b[a][0] * u[2 * a + 1];
         } else {
-            const double ux = u[3 * a], uy = u[3 * a + 1], uz = u[3 * a + 2];
+            const T ux = u[3 * a], uy = u[3 * a + 1], uz = u[3 * a + 2];
             ev[0] += b[a][0] * ux;
             ev[1] += b[a][1] * uy;
             ev[2] += b[a][2] * uz;
@@ -99,7 +101,7 @@ __device__ __forceinline__ void xbts(const T (&b)[NEN][3], T w, const T sig[6], 
             y[2 * a] += w * (b[a][0] * sig[0] + b[a][1] * sig[2]);
             y[2 * a + 1] += w * (b[a][1] * sig[1] + b[a][0] * sig[2]);
         } else {
-            const double bx = b[a][0], by = b[a][1], bz = b[a][2];
+            const T bx = b[a][0], by = b[a][1], bz = b[a][2];
             y[3 * a] += w * (bx * sig[0] + by * sig[3] + bz * sig[5]);
             y[3 * a + 1] += w * (by * sig[1] + bx * sig[3] + bz * sig[4]);
             y[3 * a + 2] += w * (bz * sig[2] + by * sig[4] + bx * sig[5]);
@@ -390,8 +392,14 @@ __global__ void __launch_bounds__(128) k_xsolid_gp(XSolid S) {
     const int32_t* ed = S.edof + (size_t)ec * NC;
     const bool j2 = S.kind && S.kind[ec];
     double pq[ND];
+    T pt[ND];
+    if constexpr (std::is_same<T, float>::value) {
 #pragma unroll
-    for (int c = 0; c < ND; ++c) pq[c] = S.xK[ed[q * ND + c]];
+        for (int c = 0; c < ND; ++c) { pt[c] = S.xK_f[ed[q * ND + c]]; pq[c] = 0.0; }
+    } else {
+#pragma unroll
+        for (int c = 0; c < ND; ++c) { pq[c] = S.xK[ed[q * ND + c]]; pt[c] = pq[c]; }
+    }
     double am = 0.0;
     T kscale, c1, c2, c3;                      // kscale: stiffness-proportional damping factor
     if constexpr (std::is_same<T, float>::value) {
@@ -421,9 +429,6 @@ __global__ void __launch_bounds__(128) k_xsolid_gp(XSolid S) {
     }
     // strain of p at this Gauss point
     T ev[6] = {0, 0, 0, 0, 0, 0};
-    T pt[ND];
-#pragma unroll
-    for (int c = 0; c < ND; ++c) pt[c] = (T)pq[c];
 #pragma unroll
     for (int a = 0; a < NEN; ++a) {
         T ua[3] = {0, 0, 0};
@@ -472,23 +477,30 @@ __global__ void __launch_bounds__(128) k_xsolid_gp(XSolid S) {
 #pragma unroll
         for (int j = 0; j < NC; ++j) y[j] += __shfl_xor_sync(0xffffffffu, y[j], off);
     if (!valid) return;
+    if constexpr (std::is_same<T, float>::value) {
+        // single precision: mass term from the table, float element vector
+        const float mmf = S.opf[(size_t)ec * (NEN + 4) + q];
+        float* outf = S.y_f + (size_t)ec * NC + q * ND;
+#pragma unroll
+        for (int c = 0; c < ND; ++c) {
+            T mine = 0;
+#pragma unroll
+            for (int a = 0; a < NEN; ++a)
+                if (a == q) mine = y[a * ND + c];
+            outf[c] = mine + mmf * pt[c];
+        }
+        return;
+    }
     double* out = S.y + (size_t)ec * NC + q * ND;
-    // single precision: the mass term from the table (one conversion per value)
-    float mmf = 0.0f;
-    double ml = 0.0;
-    if constexpr (std::is_same<T, float>::value) mmf = S.opf[(size_t)ec * (NEN + 4) + q];
-    else ml = S.mlump[(size_t)ec * NEN + q];
+    const double ml = S.mlump[(size_t)ec * NEN + q];
 #pragma unroll
     for (int c = 0; c < ND; ++c) {
         T mine = 0;
 #pragma unroll
         for (int a = 0; a < NEN; ++a)
             if (a == q) mine = y[a * ND + c];
-        double v;
-        if constexpr (std::is_same<T, float>::value) {
-            v = (double)(mine + mmf * pt[c]);
-        } else {
-            v = (double)mine;
+        double v = (double)mine;
+        {
             double mv = S.sM * pq[c];
             if (S.cM2 != 0.0) mv += S.cM2 * am * pq[c];
             v += ml * mv;
@@ -647,12 +659,36 @@ __global__ void k_xgather(XGather G) {
 
 // out_t = sum_f T_tf x_f
 __global__ void k_xexpand(int ntotal, const int32_t* __restrict__ Tp, const int32_t* __restrict__ Tc,
-                          const double* __restrict__ Tv, const double* __restrict__ x, double* __restrict__ out) {
+                          const double* __restrict__ Tv, const double* __restrict__ x, double* __restrict__ out,
+                          float* __restrict__ out_f = nullptr) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= ntotal) return;
     double v = 0.0;
     for (int i = Tp[t]; i < Tp[t + 1]; ++i) v += Tv[i] * x[Tc[i]];
     out[t] = v;
+    if (out_f) out_f[t] = (float)v;
+}
+
+// y_t = sum of the float element entries of dof t in element order (summed in
+// float, converted once) + cn m_t x_t + cdp sum eta (x_t - x_partner): the
+// gather of the single-precision operator
+__global__ void k_xgather_f(int ntotal, const int64_t* __restrict__ inv_ptr, const int64_t* __restrict__ inv_idx,
+                            const float* __restrict__ fe, const double* nodemass, double cn, const double* xn,
+                            const int32_t* dp_ptr, const int32_t* dp_col, const double* dp_eta, double cdp,
+                            const double* xdp, double* __restrict__ y) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ntotal) return;
+    float vf = 0.0f;
+    for (int64_t i = inv_ptr[t]; i < inv_ptr[t + 1]; ++i) vf += fe[inv_idx[i]];
+    double v = (double)vf;
+    if (nodemass) v += cn * nodemass[t] * xn[t];
+    if (dp_ptr && dp_ptr[t + 1] > dp_ptr[t]) {
+        double c = 0.0;
+        const double xt = xdp[t];
+        for (int i = dp_ptr[t]; i < dp_ptr[t + 1]; ++i) c += dp_eta[i] * (xt - xdp[dp_col[i]]);
+        v += cdp * c;
+    }
+    y[t] = v;
 }
 
 // out_f = sum_t T_tf y_t (- sum_t T_tf z_t)
@@ -827,6 +863,7 @@ struct svl_xnm {
     double *U = nullptr, *V = nullptr, *A = nullptr, *Ub = nullptr, *Us = nullptr;
     double *W = nullptr, *Wg = nullptr, *yt = nullptr, *ys = nullptr, *pt = nullptr, *sm = nullptr, *dUt = nullptr;
     double* Ui = nullptr;                    // U + T dU: the PML elements' displacement
+    float *pt_f = nullptr, *fe_f = nullptr;  // single-precision operator input and element vectors
     bool newmark = false;                    // NewmarkBeta instead of ExtendedNewmarkBeta
     // free-dof vectors
     double *b = nullptr, *x = nullptr, *dUf = nullptr, *r1 = nullptr, *r2 = nullptr, *yv = nullptr, *v = nullptr;
@@ -914,7 +951,8 @@ PmlArgs pml_args(svl_xnm* X) {
 int launch_solid(svl_xnm* X, const XSolid& S, bool single = false) {
     if (S.n <= 0) return SVL_OK;
     const int g = (S.n + 127) / 128;
-    const bool one = S.xK && S.xK2 == S.xK && S.xM == S.xK && S.xM2 == S.xK && S.mlump && (!single || S.opf);
+    const bool one = S.xK && S.xK2 == S.xK && S.xM == S.xK && S.xM2 == S.xK && S.mlump &&
+                     (!single || (S.opf && S.xK_f && S.y_f));
     if (one) {                                 // operator application: Gauss-point threads
         const int nen = X->m.nen;
         const int gg = (int)(((int64_t)S.n * nen + 127) / 128);
@@ -941,24 +979,33 @@ int launch_solid(svl_xnm* X, const XSolid& S, bool single = false) {
 
 // out_total = (K + 4/dt^2 M + 2/dt C + dt/3 G) p_total; single: element
 // arithmetic in single precision (inner MINRES iterations)
-int x_op_total(svl_xnm* X, const double* p, double* out, bool single = false) {
+int x_op_total(svl_xnm* X, const double* p, double* out, bool single = false, const float* p_f = nullptr) {
     const double dt = X->opts.dt, cm = 4.0 / dt / dt, cc = 2.0 / dt;
+    // the single-precision data path needs the float copy of p
+    if (single && !p_f) single = false;
     XSolid S = solid_args(X);
     S.xK = p; S.xK2 = p; S.cK2 = cc; S.xM = p; S.sM = cm; S.xM2 = p; S.cM2 = cc;
     S.opf = X->s_opf;                          // built for exactly these coefficients
+    if (single) { S.xK_f = p_f; S.y_f = X->fe_f; }
     XTRY(launch_solid(X, S, single));
     PmlArgs P = pml_args(X);
     P.single = single ? 1 : 0;
     P.coef[0] = cm; P.coef[1] = cc; P.coef[2] = 1.0; P.coef[3] = (X->m.ndim == 3 && !X->newmark) ? dt / 3.0 : 0.0;
     for (int i = 0; i < 4; ++i) P.u[i] = p;
+    if (single) { P.u_f = p_f; P.y_f = X->fe_f + (size_t)X->nsol * X->ncs; }
     XTRY(pml_action_launch(X->m.ndim, P, X->stream));
-    return x_gather(X, out, cm, p, cc, p, 0, false);
+    if (!single) return x_gather(X, out, cm, p, cc, p, 0, false);
+    k_xgather_f<<<grid_of(X->m.ntotal), 256, 0, X->stream>>>(X->m.ntotal, X->inv_ptr, X->inv_idx, X->fe_f, X->nodemass,
+                                                             cm, p, X->dp_ptr, X->dp_col, X->dp_eta, cc, p, out);
+    XCUDA(cudaGetLastError());
+    return SVL_OK;
 }
 
 // q_free = T^T Keff T v
 int x_apply(svl_xnm* X, const double* v, double* q, bool single = false) {
-    k_xexpand<<<grid_of(X->m.ntotal), 256, 0, X->stream>>>(X->m.ntotal, X->Tp, X->Tc, X->Tv, v, X->pt);
-    XTRY(x_op_total(X, X->pt, X->yt, single));
+    k_xexpand<<<grid_of(X->m.ntotal), 256, 0, X->stream>>>(X->m.ntotal, X->Tp, X->Tc, X->Tv, v, X->pt,
+                                                           single ? X->pt_f : nullptr);
+    XTRY(x_op_total(X, X->pt, X->yt, single, single ? X->pt_f : nullptr));
     k_xreduce<<<grid_of(X->m.nfree), 256, 0, X->stream>>>(X->m.nfree, X->TTp, X->TTr, X->TTv, X->yt, nullptr, q);
     XCUDA(cudaGetLastError());
     return SVL_OK;
@@ -1403,6 +1450,10 @@ int x_setup(svl_xnm* X, const svl_load_desc* L) {
         XTRY(X->upload(tab, &X->p_tab));
     }
     XTRY(X->alloc((size_t)X->nsol * X->ncs + (size_t)X->npml * X->ncp, &X->fe));
+    if (X->opts.single_inner) {
+        XTRY(X->alloc((size_t)X->nsol * X->ncs + (size_t)X->npml * X->ncp, &X->fe_f));
+        XTRY(X->alloc((size_t)m.ntotal, &X->pt_f));
+    }
     XTRY(X->upload(inv_ptr, &X->inv_ptr)); XTRY(X->upload(inv_idx, &X->inv_idx));
     if (!m.dp_eta.empty()) {                 // ZeroLength1D dashpots
         std::vector<int32_t> dpp, dpc;
