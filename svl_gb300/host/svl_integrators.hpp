@@ -87,6 +87,19 @@ public:
     NewmarkBeta(const svl_model_desc& model, const svl_load_desc& loads, double dt, double tol = 1e-8,
                 double mtol = 1e-12, double ftol = 1e-12, int maxit = 20000, const NewtonRaphson* newton = nullptr)
         : ntotal_(model.ntotal) {
+        bool pml = false;
+        for (int e = 0; model.elem_pml && e < model.nelem; ++e) pml = pml || model.elem_pml[e] != 0;
+        if (pml) {
+            // PML layers: symmetric indefinite Keff, the MINRES handle in NewmarkBeta mode
+            svl_xnm_opts x{};
+            x.dt = dt; x.ftol = ftol; x.mtol = mtol; x.tol = tol; x.maxit = maxit;
+            x.algorithm = newton ? SVL_ALGO_NEWTON : SVL_ALGO_LINEAR;
+            if (newton) { x.newton_maxit = newton->nstep; x.cnvgtol = newton->cnvgtol; x.cnvgtest = newton->cnvgtest; }
+            x.integrator = SVL_XNM_NEWMARK;
+            x.single_inner = 1;
+            check(svl_xnm_create(&model, &loads, &x, &x_));
+            return;
+        }
         svl_nm_opts o{};
         o.dt = dt;
         o.ftol = ftol;
@@ -103,21 +116,27 @@ public:
         }
         check(svl_nm_create(&model, &loads, &o, &h_));
     }
-    ~NewmarkBeta() { svl_nm_destroy(h_); }
+    ~NewmarkBeta() {
+        if (h_) svl_nm_destroy(h_);
+        if (x_) svl_xnm_destroy(x_);
+    }
     NewmarkBeta(const NewmarkBeta&) = delete;
     NewmarkBeta& operator=(const NewmarkBeta&) = delete;
 
     void Initialize(const double* U0 = nullptr, const double* V0 = nullptr, const double* A0 = nullptr) {
-        check(svl_nm_set_initial(h_, U0, V0, A0));
+        check(x_ ? svl_xnm_set_initial(x_, U0, V0, A0, nullptr) : svl_nm_set_initial(h_, U0, V0, A0));
     }
     // ComputeNewStep(mesh, k) -> stop (NewmarkBeta.cpp:117-141)
-    bool ComputeNewStep(unsigned int k) { return svl_nm_run(h_, (int32_t)k, 1, nullptr) != SVL_OK; }
+    bool ComputeNewStep(unsigned int k) { return ComputeNewSteps(k, 1); }
     bool ComputeNewSteps(unsigned int k_first, unsigned int n, double* U_hist = nullptr) {
-        return svl_nm_run(h_, (int32_t)k_first, (int32_t)n, U_hist) != SVL_OK;
+        const int st = x_ ? svl_xnm_run(x_, (int32_t)k_first, (int32_t)n, U_hist)
+                          : svl_nm_run(h_, (int32_t)k_first, (int32_t)n, U_hist);
+        return st != SVL_OK;
     }
     // Trains the learned preconditioner on synthetic pairs of this model's
-    // effective stiffness and switches to it (lattice meshes only).
+    // effective stiffness and switches to it (lattice meshes without PML only).
     float TrainPreconditioner(unsigned int k_next) {
+        if (x_) throw Error(SVL_ERR_UNSUPPORTED, "the learned preconditioner does not cover PML models");
         svl_nn_train_opts t{};
         t.n_synthetic = 300;
         t.iters = 1500;
@@ -134,10 +153,11 @@ public:
 private:
     std::vector<double> get(int which) const {
         std::vector<double> v(ntotal_);
-        check(svl_nm_get(h_, which, v.data()));
+        check(x_ ? svl_xnm_get(x_, which, v.data()) : svl_nm_get(h_, which, v.data()));
         return v;
     }
     svl_nm* h_ = nullptr;
+    svl_xnm* x_ = nullptr;                 // set instead of h_ for models with PML layers
     int ntotal_ = 0;
 };
 
@@ -165,6 +185,8 @@ public:
             o.cnvgtol = newton->cnvgtol;
             o.cnvgtest = newton->cnvgtest;
         }
+        o.integrator = SVL_XNM_EXTENDED_NEWMARK;
+        o.single_inner = 1;
         check(svl_xnm_create(&model, &loads, &o, &h_));
     }
     ~ExtendedNewmarkBeta() { svl_xnm_destroy(h_); }

@@ -48,7 +48,16 @@ int main() {
         double mxn = 0, dmax = 0;
         const std::vector<double> ux = xn.GetDisplacements(), un = nm.GetDisplacements();
         for (size_t i = 0; i < ux.size(); ++i) { mxn = std::fmax(mxn, std::fabs(ux[i])); dmax = std::fmax(dmax, std::fabs(ux[i] - un[i])); }
-        std::printf("max|U| %.6e newmark %.6e extended %.6e (diff %.3e)\n", mx, mn, mxn, dmax);
+        // NewtonRaphson (2 iterations, cnvgtol 0) on the elastic box: the second
+        // iteration only corrects the first solve's residual
+        svl::gpu::NewtonRaphson newton{0.0, 2, 4};
+        svl::gpu::NewmarkBeta nw(md, ld, 4.0 * dt, 1e-12, 1e-12, 1e-12, 20000, &newton);
+        nw.Initialize();
+        if (nw.ComputeNewSteps(1, 20)) { std::printf("newton stop\n"); return 5; }
+        double dnw = 0;
+        const std::vector<double> uw = nw.GetDisplacements();
+        for (size_t i = 0; i < uw.size(); ++i) dnw = std::fmax(dnw, std::fabs(uw[i] - un[i]));
+        std::printf("max|U| %.6e newmark %.6e extended %.6e (diff %.3e) newton-diff %.3e\n", mx, mn, mxn, dmax, dnw);
     } catch (const svl::gpu::Error& e) {
         if (e.code == SVL_ERR_NODEVICE) { std::printf("nodevice\n"); return 0; }
         std::printf("error %d %s\n", e.code, e.what());

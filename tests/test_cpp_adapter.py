@@ -37,3 +37,6 @@ def test_cpp_adapter_steps_on_gpu(tmp_path, gpu):
     assert 0.0 < umax < 1.0 and 0.0 < unm < 1.0
     # ExtendedNewmarkBeta without PML, loads or damping is NewmarkBeta
     assert abs(uxn - unm) <= 1e-9 * unm and diff <= 1e-9 * unm
+    # NewmarkBeta + NewtonRaphson on an elastic model: the Linear answer up to
+    # the PCG tolerance of the Linear run (1e-8)
+    assert tok[8] == "newton-diff" and float(tok[9]) <= 1e-6 * unm
