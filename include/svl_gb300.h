@@ -244,6 +244,13 @@ int  svl_cd_set_initial(svl_cd* cd, const double* U0, const double* V0, const do
 int  svl_cd_run(svl_cd* cd, int32_t k_first, int32_t nsteps, double* U_hist);
 /* which: 0 = U, 1 = V, 2 = A (total dofs, host copy). */
 int  svl_cd_get(svl_cd* cd, int32_t which, double* out);
+/* Reaction forces after step k (the step just run), as DynamicAnalysis::
+ * UpdateDomain stores them (DynamicAnalysis.cpp:128-150) through
+ * CentralDifference::ComputeReactionForce (CentralDifference.cpp:156-171):
+ * R = m A + sum over the elements with a fixed node (a node with a free-dof
+ * entry of -1) of Fint_e + C_e V_e + M_e A_e, minus Fext(k), on the dofs of
+ * fixed nodes; zeros elsewhere (Node::GetReaction).  R: [ntotal] host array. */
+int  svl_cd_reaction(svl_cd* cd, int32_t k, double* R);
 /* Device pointer of U / V / A (valid until the next svl_cd_run). */
 int  svl_cd_device_ptr(svl_cd* cd, int32_t which, const double** dptr);
 /* Number of kernel launches the last svl_cd_run issued. */
@@ -347,6 +354,8 @@ int  svl_nm_run(svl_nm* nm, int32_t k_first, int32_t nsteps, double* U_hist);
  * stream; *ms = elapsed time (measurement hook, no counterpart). */
 int  svl_nm_run_timed(svl_nm* nm, int32_t k_first, int32_t nsteps, float* ms);
 int  svl_nm_get(svl_nm* nm, int32_t which, double* out);
+/* NewmarkBeta::ComputeReactionForce after step k (as svl_cd_reaction). */
+int  svl_nm_reaction(svl_nm* nm, int32_t k, double* R);
 /* Conjugate-gradient iterations summed over all solves, of the last solve,
  * and the last solve's true relative residual. */
 int  svl_nm_stats(svl_nm* nm, int64_t* iters_total, int64_t* iters_last, double* rel_residual_last);

@@ -33,6 +33,8 @@ def lib():
         L.oracle_j2_path.argtypes = [C.c_int, f64p, C.c_int, f64p, f64p]
         L.oracle_pml_matrices.argtypes = [C.c_int, f64p, C.c_double, C.c_double, C.c_double, C.c_double, f64p,
                                           f64p, f64p, f64p, f64p]
+        L.oracle_reaction_run.argtypes = [vp, vp, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double,
+                                          f64p]
         L.oracle_xnewmark_run.argtypes = [vp, vp, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double,
                                           C.c_int, f64p, f64p, f64p, f64p, f64p, C.POINTER(C.c_int),
                                           C.POINTER(C.c_double)]
@@ -179,6 +181,20 @@ def xnewmark_run(model, loads, dt, nsteps, k_first=1, algo=0, maxit=50, cnvgtol=
     if st != 0:
         raise RuntimeError("oracle_xnewmark_run failed with status %d" % st)
     return hist, U, V, A, Ub
+
+
+def reaction_run(model, loads, dt, nsteps, k_first=1, integrator="cd", algo=0, maxit=50, cnvgtol=1e-6):
+    """Reaction forces (total dofs; zeros off the fixed nodes) after nsteps of
+    central difference or NewmarkBeta (algo as newmark_run)."""
+    md = model.desc()
+    ld = loads.desc() if loads is not None else None
+    R = np.zeros(model.ntotal)
+    st = lib().oracle_reaction_run(C.addressof(md), C.addressof(ld) if ld is not None else None, dt, k_first, nsteps,
+                                   0 if integrator == "cd" else 1, algo, maxit, cnvgtol,
+                                   R.ctypes.data_as(C.POINTER(C.c_double)))
+    if st != 0:
+        raise RuntimeError("oracle_reaction_run failed with status %d" % st)
+    return R
 
 
 def xnewmark_matrices(model):

@@ -740,6 +740,60 @@ struct Sim {
         }
     }
     // Assembler::ComputeSupportMotionIncrement (Assembler.cpp:493-532).
+    // Reaction forces after a step (DynamicAnalysis::UpdateDomain,
+    // DynamicAnalysis.cpp:128-150): Integrator::ComputeReactionForce =
+    // ComputeDynamicInternalForceVector - Fext(k) - Fbar (CentralDifference.cpp:
+    // 156-171, NewmarkBeta.cpp), the dynamic vector being the node inertia m A
+    // (Assembler.cpp:569-592) and then, in element order, Fint_e + C_e V_e +
+    // M_e A_e of every element with a fixed node (lin2DQuad4.cpp:416-434,
+    // ZeroLength1D.cpp:257-277; Assembler.cpp:596-619, unfiltered).  A node is
+    // fixed when one of its free-dof entries is -1 (Driver.hpp:338-341); the
+    // other nodes report zeros (Node::GetReaction).  Element states are the
+    // ones of the last update; C_e = am M_e + ak K0_e, dashpots eta a a^T.
+    void reaction(int k, const std::vector<double>& V, const std::vector<double>& A, std::vector<double>& R) const {
+        const int nt = m.ntotal, nen = m.nen, nc = nen * m.ndof;
+        std::vector<char> fixed(m.nnode, 0), dof_fixed(nt, 0);
+        for (int n = 0; n < m.nnode; ++n) {
+            for (int j = 0; j < m.nndof[n]; ++j) if (m.fdof_all[(size_t)n * m.dstride + j] == -1) fixed[n] = 1;
+            if (fixed[n]) for (int j = 0; j < m.nndof[n]; ++j) dof_fixed[m.tdof_all[(size_t)n * m.dstride + j]] = 1;
+        }
+        std::vector<double> F(nt, 0.0);
+        if (!m.nodemass.empty()) for (int t = 0; t < nt; ++t) F[t] += m.nodemass[t] * A[t];
+        std::vector<double> fe(72), Me((size_t)nc * nc), K0((size_t)nc * nc);
+        for (int e = 0; e < m.nelem; ++e) {
+            bool hf = false;
+            for (int a = 0; a < nen; ++a) hf = hf || fixed[m.conn[(size_t)e * nen + a]];
+            if (!hf) continue;
+            element_fint(e, fe.data());
+            element_M(e, Me.data(), m.lumped != 0);
+            const double am = m.ray.empty() ? 0.0 : m.ray[2 * e], ak = m.ray.empty() ? 0.0 : m.ray[2 * e + 1];
+            if (ak != 0.0) element_K0(e, K0.data());
+            const int* ed = &edofs[(size_t)e * nc];
+            for (int i = 0; i < nc; ++i) {
+                double cv = 0.0, ma = 0.0;
+                for (int j = 0; j < nc; ++j) {
+                    const double c = am * Me[(size_t)i * nc + j] + (ak != 0.0 ? ak * K0[(size_t)i * nc + j] : 0.0);
+                    cv += c * V[ed[j]];
+                    ma += Me[(size_t)i * nc + j] * A[ed[j]];
+                }
+                F[ed[i]] += (fe[i] + cv) + ma;
+            }
+        }
+        std::vector<int> node_of(nt, -1);
+        for (int n = 0; n < m.nnode; ++n)
+            for (int j = 0; j < m.nndof[n]; ++j) node_of[m.tdof_all[(size_t)n * m.dstride + j]] = n;
+        for (size_t i = 0; i < m.dp_eta.size(); ++i) {
+            const int a = m.dp_dof[2 * i], b = m.dp_dof[2 * i + 1];
+            if (!fixed[node_of[a]] && !fixed[node_of[b]]) continue;
+            const double eta = m.dp_eta[i];
+            F[a] += eta * (V[a] - V[b]);
+            F[b] += eta * (V[b] - V[a]);
+        }
+        std::vector<double> Fx;
+        fext(k, Fx);
+        R.assign(nt, 0.0);
+        for (int t = 0; t < nt; ++t) if (dof_fixed[t]) R[t] = (F[t] - Fx[t]) - 0.0;
+    }
     void support_increment(int k, std::vector<double>& SM) const {
         SM.assign(m.ntotal, 0.0);
         for (size_t i = 0; i < L.smdof.size(); ++i) {
@@ -1655,6 +1709,32 @@ int oracle_xnewmark_run(const svl_model_desc* model, const svl_load_desc* loads,
     if (V_out) std::memcpy(V_out, x.V.data(), sizeof(double) * nt);
     if (A_out) std::memcpy(A_out, x.A.data(), sizeof(double) * nt);
     if (Ubar_out) std::memcpy(Ubar_out, x.Ubar.data(), sizeof(double) * nt);
+    return 0;
+}
+
+/* Reaction forces after `nsteps` steps from k_first of the central-difference
+ * (integrator 0) or NewmarkBeta (1, algo/maxit/cnvgtol as oracle_newmark_run)
+ * run; R_out [ntotal]. */
+int oracle_reaction_run(const svl_model_desc* model, const svl_load_desc* loads, double dt, int k_first, int nsteps,
+                        int integrator, int algo, int maxit, double cnvgtol, double* R_out) {
+    std::vector<double> R;
+    const int klast = k_first + nsteps - 1;
+    if (integrator == 0) {
+        CD cd;
+        if (!cd.init(model, loads, dt, 1e-12, 1e-12)) return SVL_ERR_INVALID;
+        cd.set_initial(nullptr, nullptr, nullptr);
+        for (int i = 0; i < nsteps; ++i) cd.step(k_first + i);
+        cd.s.reaction(klast, cd.V, cd.A, R);
+    } else {
+        Newmark nm;
+        if (!nm.init(model, loads, dt)) return SVL_ERR_INVALID;
+        for (int i = 0; i < nsteps; ++i) {
+            int st = nm.step(k_first + i, algo, algo == 0 ? 1 : maxit, cnvgtol);
+            if (st) return st;
+        }
+        nm.s.reaction(klast, nm.V, nm.A, R);
+    }
+    std::memcpy(R_out, R.data(), sizeof(double) * R.size());
     return 0;
 }
 

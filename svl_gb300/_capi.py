@@ -147,6 +147,7 @@ def lib():
     L.svl_cd_set_initial.argtypes = [C.c_void_p, f64p, f64p, f64p]
     L.svl_cd_run.argtypes = [C.c_void_p, C.c_int32, C.c_int32, f64p]
     L.svl_cd_get.argtypes = [C.c_void_p, C.c_int32, f64p]
+    L.svl_cd_reaction.argtypes = [C.c_void_p, C.c_int32, f64p]
     L.svl_cd_device_ptr.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_void_p)]
     L.svl_cd_launch_count.argtypes = [C.c_void_p, C.POINTER(C.c_int64)]
     L.svl_cd_sync.argtypes = [C.c_void_p]
@@ -181,6 +182,7 @@ def lib():
     L.svl_nm_run.argtypes = [C.c_void_p, C.c_int32, C.c_int32, f64p]
     L.svl_nm_run_timed.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(C.c_float)]
     L.svl_nm_get.argtypes = [C.c_void_p, C.c_int32, f64p]
+    L.svl_nm_reaction.argtypes = [C.c_void_p, C.c_int32, f64p]
     L.svl_nm_stats.argtypes = [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_double)]
     L.svl_nm_launch_count.argtypes = [C.c_void_p, C.POINTER(C.c_int64)]
     L.svl_nm_newton_stats.argtypes = [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_double)]

@@ -328,6 +328,145 @@ __global__ void __launch_bounds__(128) k_element_tan(DevView d, const double* __
     for (int j = 0; j < NC; ++j) d.fe[(size_t)j * E + e] = fe[j];
 }
 
+// Reaction forces (DynamicAnalysis::UpdateDomain, DynamicAnalysis.cpp:128-150;
+// CentralDifference.cpp:156-171): one thread per element with a fixed node,
+// Fint_e + C_e V_e + M_e A_e unfiltered (lin2DQuad4.cpp:416-434) from the
+// strain displacement of the last update.  map_state = 1: J2 elements take the
+// return mapping of that strain on a copy of their state (the explicit path
+// updates the states at the start of the next step); 0: their stress follows
+// from the updated state, K tr(eps) 1 + 2G (dev eps - eps_p) (the Newmark path
+// updated them in place).  C_e = am_e M_e + ak_e K0_e with a lumped M_e.
+template <int ND, int NEN>
+__global__ void __launch_bounds__(128) k_react_elem(DevView d, const int32_t* __restrict__ list, int nlist,
+                                                    const double* __restrict__ rm, const double* __restrict__ ram,
+                                                    int ngp, int map_state, double* __restrict__ out) {
+    constexpr int NC = ND * NEN, PER = NEN * ND + 1;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nlist) return;
+    const int E = d.nelem, e = list[i];
+    double ue[NC], ve[NC], fi[NC], cv[NC];
+#pragma unroll
+    for (int j = 0; j < NC; ++j) {
+        const int t = d.edof[(size_t)j * E + e];
+        ue[j] = d.Us[t]; ve[j] = d.V[t]; fi[j] = 0.0; cv[j] = 0.0;
+    }
+    const int kind = d.ekind[e];
+    const double c1 = d.ecoef[e], c2 = d.ecoef[(size_t)E + e], c3 = d.ecoef[2 * (size_t)E + e];
+    const double* g0 = d.geo + (size_t)d.egeo[e] * ngp * PER;
+    for (int q = 0; q < ngp; ++q) {
+        const double* g = g0 + q * PER;
+        double b[NEN][3];
+#pragma unroll
+        for (int a = 0; a < NEN; ++a)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) b[a][j] = (j < ND) ? g[a * ND + j] : 0.0;
+        const double w = g[PER - 1];
+        // strain (engineering shear) of U_s and of V
+        double ev[6] = {0, 0, 0, 0, 0, 0}, vv[6] = {0, 0, 0, 0, 0, 0};
+#pragma unroll
+        for (int a = 0; a < NEN; ++a) {
+            if (ND == 2) {
+                ev[0] += b[a][0] * ue[2 * a]; ev[1] += b[a][1] * ue[2 * a + 1];
+                ev[2] += b[a][1] * ue[2 * a] + b[a][0] * ue[2 * a + 1];
+                vv[0] += b[a][0] * ve[2 * a]; vv[1] += b[a][1] * ve[2 * a + 1];
+                vv[2] += b[a][1] * ve[2 * a] + b[a][0] * ve[2 * a + 1];
+            } else {
+                const double* u = ue + 3 * a;
+                const double* v = ve + 3 * a;
+                ev[0] += b[a][0] * u[0]; ev[1] += b[a][1] * u[1]; ev[2] += b[a][2] * u[2];
+                ev[3] += b[a][1] * u[0] + b[a][0] * u[1]; ev[4] += b[a][2] * u[1] + b[a][1] * u[2];
+                ev[5] += b[a][2] * u[0] + b[a][0] * u[2];
+                vv[0] += b[a][0] * v[0]; vv[1] += b[a][1] * v[1]; vv[2] += b[a][2] * v[2];
+                vv[3] += b[a][1] * v[0] + b[a][0] * v[1]; vv[4] += b[a][2] * v[1] + b[a][1] * v[2];
+                vv[5] += b[a][2] * v[0] + b[a][0] * v[2];
+            }
+        }
+        double sig[6] = {0, 0, 0, 0, 0, 0};
+        if (kind == kMatElastic) {
+            if (ND == 2) { sig[0] = c1 * ev[0] + c2 * ev[1]; sig[1] = c2 * ev[0] + c1 * ev[1]; sig[2] = c3 * ev[2]; }
+            else {
+                sig[0] = c1 * ev[0] + c2 * ev[1] + c2 * ev[2];
+                sig[1] = c2 * ev[0] + c1 * ev[1] + c2 * ev[2];
+                sig[2] = c2 * ev[0] + c2 * ev[1] + c1 * ev[2];
+                sig[3] = c3 * ev[3]; sig[4] = c3 * ev[4]; sig[5] = c3 * ev[5];
+            }
+        } else {
+            double st[kJ2State];
+            const double* gs = d.gstate + (size_t)q * E + e;
+#pragma unroll
+            for (int k2 = 0; k2 < kJ2State; ++k2) st[k2] = gs[(size_t)k2 * ngp * E];
+            double Ev[6];
+            if (ND == 2) { Ev[0] = 0.0; Ev[1] = ev[0]; Ev[2] = ev[1]; Ev[3] = 0.0; Ev[4] = 0.5 * ev[2]; Ev[5] = 0.0; }
+            else { Ev[0] = ev[0]; Ev[1] = ev[1]; Ev[2] = ev[2]; Ev[3] = 0.5 * ev[3]; Ev[4] = 0.5 * ev[4]; Ev[5] = 0.5 * ev[5]; }
+            const double K = c1, G = c2;
+            double s6[6];
+            if (map_state) {
+                j2_return<ND>(Ev, st, K, G, c3, d.ecoef[3 * (size_t)E + e], d.ecoef[4 * (size_t)E + e], s6);
+            } else {
+                const double tr = Ev[0] + Ev[1] + Ev[2];
+#pragma unroll
+                for (int k2 = 0; k2 < 6; ++k2)
+                    s6[k2] = (k2 < 3 ? K * tr : 0.0) + 2.0 * G * (Ev[k2] - (k2 < 3 ? 1.0 / 3.0 * tr : 0.0) - st[k2]);
+            }
+            if (ND == 2) { sig[0] = s6[1]; sig[1] = s6[2]; sig[2] = s6[4]; }
+            else for (int k2 = 0; k2 < 6; ++k2) sig[k2] = s6[k2];
+        }
+        double sk[6] = {0, 0, 0, 0, 0, 0};
+        if (d.dk0) {
+            const double k1 = d.dk0[e], k2c = d.dk0[(size_t)E + e], k3 = d.dk0[2 * (size_t)E + e];
+            if (ND == 2) { sk[0] = k1 * vv[0] + k2c * vv[1]; sk[1] = k2c * vv[0] + k1 * vv[1]; sk[2] = k3 * vv[2]; }
+            else {
+                sk[0] = k1 * vv[0] + k2c * vv[1] + k2c * vv[2];
+                sk[1] = k2c * vv[0] + k1 * vv[1] + k2c * vv[2];
+                sk[2] = k2c * vv[0] + k2c * vv[1] + k1 * vv[2];
+                sk[3] = k3 * vv[3]; sk[4] = k3 * vv[4]; sk[5] = k3 * vv[5];
+            }
+        }
+#pragma unroll
+        for (int a = 0; a < NEN; ++a) {
+            if (ND == 2) {
+                fi[2 * a] += w * (b[a][0] * sig[0] + b[a][1] * sig[2]);
+                fi[2 * a + 1] += w * (b[a][1] * sig[1] + b[a][0] * sig[2]);
+                cv[2 * a] += w * (b[a][0] * sk[0] + b[a][1] * sk[2]);
+                cv[2 * a + 1] += w * (b[a][1] * sk[1] + b[a][0] * sk[2]);
+            } else {
+                const double bx = b[a][0], by = b[a][1], bz = b[a][2];
+                fi[3 * a] += w * (bx * sig[0] + by * sig[3] + bz * sig[5]);
+                fi[3 * a + 1] += w * (by * sig[1] + bx * sig[3] + bz * sig[4]);
+                fi[3 * a + 2] += w * (bz * sig[2] + by * sig[4] + bx * sig[5]);
+                cv[3 * a] += w * (bx * sk[0] + by * sk[3] + bz * sk[5]);
+                cv[3 * a + 1] += w * (by * sk[1] + bx * sk[3] + bz * sk[4]);
+                cv[3 * a + 2] += w * (bz * sk[2] + by * sk[4] + bx * sk[5]);
+            }
+        }
+    }
+    double* o = out + (size_t)i * NC;
+#pragma unroll
+    for (int j = 0; j < NC; ++j) {
+        const int a = j / ND;
+        const int t = d.edof[(size_t)j * E + e];
+        const double c = ram[(size_t)i * NEN + a] * ve[j] + cv[j];
+        o[j] = (fi[j] + c) + rm[(size_t)i * NEN + a] * d.A[t];
+    }
+}
+
+// R_t = (m_t A_t + sum of the listed elements' entries of t in element order
+// + dashpots with a fixed node eta (V_t - V_partner)) - Fext_t(k), for the
+// dofs of fixed nodes
+__global__ void k_react_dof(DevView d, int k, int nr, const int32_t* __restrict__ rdof,
+                            const int32_t* __restrict__ rptr, const int32_t* __restrict__ ridx,
+                            const double* __restrict__ elem_out, const double* __restrict__ rnm,
+                            const int32_t* __restrict__ dptr, const int32_t* __restrict__ dcol,
+                            const double* __restrict__ deta, double* __restrict__ R) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nr) return;
+    const int t = rdof[i];
+    double v = rnm ? rnm[i] * d.A[t] : 0.0;
+    for (int p = rptr[i]; p < rptr[i + 1]; ++p) v += elem_out[ridx[p]];
+    for (int p = dptr[i]; p < dptr[i + 1]; ++p) v += deta[p] * (d.V[t] - d.V[dcol[p]]);
+    R[t] = (v - fext_at(d, t, k)) - 0.0;
+}
+
 // Domain-reduction forces of step d.step[0] (lin2DQuad4.cpp:564-614,
 // lin3DHexa8.cpp:661-718) for elastic elements with a lumped mass: the
 // lumped mass is diagonal, so M~ (equal-condition blocks zeroed) vanishes and
@@ -544,6 +683,13 @@ struct svl_cd {
     int hist_cap = 0;
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t filled[2] = {nullptr, nullptr}, drained[2] = {nullptr, nullptr};
+    // reaction tables (built on the first svl_cd_reaction call)
+    bool react_ready = false;
+    int r_nlist = 0, r_ndof = 0;
+    const int32_t *r_list = nullptr, *r_dof = nullptr, *r_ptr = nullptr, *r_idx = nullptr;
+    const int32_t *r_dptr = nullptr, *r_dcol = nullptr;
+    const double *r_m = nullptr, *r_am = nullptr, *r_nm = nullptr, *r_deta = nullptr;
+    double *r_out = nullptr, *r_R = nullptr;
 
     template <typename T>
     int upload(const std::vector<T>& h, const T** out) {
@@ -1115,6 +1261,103 @@ int svl_cd_profile(svl_cd* cd, int32_t k_first, int32_t nsteps, double* ms_kerne
     }
     for (int i = 0; i < 6; ++i) cudaEventDestroy(ev[i]);
     return SVL_OK;
+}
+
+}  // extern "C"
+
+// Reaction forces after step k (see k_react_elem); map_state as there.
+static int cd_reaction(svl_cd* cd, int k, int map_state, double* R) {
+    const HostModel& m = cd->m;
+    const int nen = m.nen, nd = m.ndim, E = m.nelem, NC = nen * nd;
+    if (!cd->react_ready) {
+        std::vector<char> fixed(m.nnode, 0);
+        for (int n = 0; n < m.nnode; ++n)
+            for (int j = 0; j < m.nndof[n]; ++j)
+                if (m.fdof_all[(size_t)n * m.dstride + j] == -1) fixed[n] = 1;
+        std::vector<int32_t> list, pos_of(E, -1);
+        for (int e = 0; e < E; ++e) {
+            bool hf = false;
+            for (int a = 0; a < nen; ++a) hf = hf || fixed[m.conn[(size_t)e * nen + a]];
+            if (hf) { pos_of[e] = (int32_t)list.size(); list.push_back(e); }
+        }
+        std::vector<double> diag;
+        element_lumped_masses(m, diag);
+        std::vector<double> rm((size_t)list.size() * nen), ram(rm.size());
+        for (size_t i = 0; i < list.size(); ++i) {
+            const int e = list[i];
+            const double am = m.ray.empty() ? 0.0 : m.ray[2 * (size_t)e];
+            for (int a = 0; a < nen; ++a) {
+                rm[i * nen + a] = diag[((size_t)e * nen + a) * nd];
+                ram[i * nen + a] = am * rm[i * nen + a];
+            }
+        }
+        // dofs of fixed nodes, their element entries (element order) and dashpots
+        std::vector<int32_t> rdof, dof_pos(m.ntotal, -1), node_of(m.ntotal, -1);
+        for (int n = 0; n < m.nnode; ++n)
+            for (int j = 0; j < m.nndof[n]; ++j) node_of[m.tdof_all[(size_t)n * m.dstride + j]] = n;
+        for (int n = 0; n < m.nnode; ++n)
+            if (fixed[n])
+                for (int j = 0; j < m.nndof[n]; ++j) {
+                    const int t = m.tdof_all[(size_t)n * m.dstride + j];
+                    dof_pos[t] = (int32_t)rdof.size();
+                    rdof.push_back(t);
+                }
+        const int nr = (int)rdof.size();
+        std::vector<std::vector<int32_t>> ent(nr);
+        for (size_t i = 0; i < list.size(); ++i) {
+            const int e = list[i];
+            for (int a = 0; a < nen; ++a)
+                for (int c = 0; c < nd; ++c) {
+                    const int t = m.tdof[(size_t)m.conn[(size_t)e * nen + a] * nd + c];
+                    if (dof_pos[t] >= 0) ent[dof_pos[t]].push_back((int32_t)(i * NC + a * nd + c));
+                }
+        }
+        std::vector<int32_t> rptr(nr + 1, 0), ridx;
+        for (int i = 0; i < nr; ++i) { ridx.insert(ridx.end(), ent[i].begin(), ent[i].end()); rptr[i + 1] = (int32_t)ridx.size(); }
+        std::vector<std::vector<std::pair<int32_t, double>>> dps(nr);
+        for (size_t i = 0; i < m.dp_eta.size(); ++i) {
+            const int a = m.dp_dof[2 * i], b = m.dp_dof[2 * i + 1];
+            if (!fixed[node_of[a]] && !fixed[node_of[b]]) continue;
+            if (dof_pos[a] >= 0) dps[dof_pos[a]].push_back({b, m.dp_eta[i]});
+            if (dof_pos[b] >= 0) dps[dof_pos[b]].push_back({a, m.dp_eta[i]});
+        }
+        std::vector<int32_t> dptr(nr + 1, 0), dcol;
+        std::vector<double> deta, rnm;
+        for (int i = 0; i < nr; ++i) {
+            for (auto& pr : dps[i]) { dcol.push_back(pr.first); deta.push_back(pr.second); }
+            dptr[i + 1] = (int32_t)dcol.size();
+        }
+        if (!m.nodemass.empty()) { rnm.resize(nr); for (int i = 0; i < nr; ++i) rnm[i] = m.nodemass[rdof[i]]; }
+        TRY(cd->upload(list, &cd->r_list)); TRY(cd->upload(rm, &cd->r_m)); TRY(cd->upload(ram, &cd->r_am));
+        TRY(cd->upload(rdof, &cd->r_dof)); TRY(cd->upload(rptr, &cd->r_ptr)); TRY(cd->upload(ridx, &cd->r_idx));
+        TRY(cd->upload(dptr, &cd->r_dptr)); TRY(cd->upload(dcol, &cd->r_dcol)); TRY(cd->upload(deta, &cd->r_deta));
+        if (!rnm.empty()) TRY(cd->upload(rnm, &cd->r_nm));
+        TRY(cd->zeros((size_t)list.size() * NC, &cd->r_out));
+        TRY(cd->zeros((size_t)m.ntotal, &cd->r_R));
+        cd->r_nlist = (int)list.size();
+        cd->r_ndof = nr;
+        cd->react_ready = true;
+    }
+    if (cd->r_nlist > 0) {
+        const int g = (cd->r_nlist + 127) / 128;
+        if (nd == 2) k_react_elem<2, 4><<<g, 128, 0, cd->stream>>>(cd->d, cd->r_list, cd->r_nlist, cd->r_m, cd->r_am, m.ngp, map_state, cd->r_out);
+        else k_react_elem<3, 8><<<g, 128, 0, cd->stream>>>(cd->d, cd->r_list, cd->r_nlist, cd->r_m, cd->r_am, m.ngp, map_state, cd->r_out);
+    }
+    if (cd->r_ndof > 0)
+        k_react_dof<<<(cd->r_ndof + 255) / 256, 256, 0, cd->stream>>>(cd->d, k, cd->r_ndof, cd->r_dof, cd->r_ptr, cd->r_idx,
+                                                                     cd->r_out, cd->r_nm, cd->r_dptr, cd->r_dcol,
+                                                                     cd->r_deta, cd->r_R);
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaMemcpyAsync(R, cd->r_R, sizeof(double) * m.ntotal, cudaMemcpyDeviceToHost, cd->stream));
+    CUDA_TRY(cudaStreamSynchronize(cd->stream));
+    return SVL_OK;
+}
+
+extern "C" {
+
+int svl_cd_reaction(svl_cd* cd, int32_t k, double* R) {
+    if (!cd || !R) { set_error("NULL argument"); return SVL_ERR_INVALID; }
+    return cd_reaction(cd, k, 1, R);
 }
 
 int svl_cd_get(svl_cd* cd, int32_t which, double* out) {
@@ -2522,6 +2765,11 @@ void svl_host_free(void* p) {
 int svl_nm_get(svl_nm* nm, int32_t which, double* out) {
     if (!nm) { set_error("NULL handle"); return SVL_ERR_INVALID; }
     return svl_cd_get(nm->cd, which, out);
+}
+
+int svl_nm_reaction(svl_nm* nm, int32_t k, double* R) {
+    if (!nm || !R) { set_error("NULL argument"); return SVL_ERR_INVALID; }
+    return cd_reaction(nm->cd, k, 0, R);
 }
 
 int svl_nm_stats(svl_nm* nm, int64_t* iters_total, int64_t* iters_last, double* rel_residual_last) {

@@ -279,6 +279,8 @@ static void lumped_element_diag(const HostModel& m, std::vector<double>& diag) {
     });
 }
 
+void element_lumped_masses(const HostModel& m, std::vector<double>& diag) { lumped_element_diag(m, diag); }
+
 void lumped_mass_diag(const HostModel& m, double mtol, std::vector<double>& M) {
     const int nd = m.ndim, nen = m.nen;
     // element diagonals in parallel, assembled afterwards in element order

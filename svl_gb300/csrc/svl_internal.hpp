@@ -84,6 +84,8 @@ void parallel_for(int64_t n, const std::function<void(int64_t, int64_t)>& body);
 
 // Diagonal of the assembled row-sum-lumped mass on total dofs.
 void lumped_mass_diag(const HostModel& m, double mtol, std::vector<double>& M);
+// row-sum lumped mass of every element node and component, [(e nen + a) nd + j]
+void element_lumped_masses(const HostModel& m, std::vector<double>& diag);
 // Dashpot couplings per total dof, CSR: y_t += c * sum eta (x_t - x_partner)
 // for every dashpot that touches t (element order); empty without dashpots.
 void dashpot_tables(const HostModel& m, std::vector<int32_t>& ptr, std::vector<int32_t>& col,

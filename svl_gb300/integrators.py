@@ -49,6 +49,13 @@ class CentralDifference:
     def GetAccelerations(self) -> np.ndarray:
         return self._get(2)
 
+    def ComputeReactionForce(self, k: int) -> np.ndarray:
+        """Reaction forces after step k (CentralDifference.cpp:156-171): total-dof
+        vector, zeros off the fixed nodes."""
+        R = np.zeros(self.ntotal)
+        check(lib().svl_cd_reaction(self._h, int(k), ptr(R, C.c_double)))
+        return R
+
     # -- batch interface -------------------------------------------------
     def run(self, k_first: int, nsteps: int, history: bool = False, out=None):
         """Steps k_first .. k_first+nsteps-1; with history=True (or a
@@ -313,6 +320,13 @@ class NewmarkBeta:
 
     def GetAccelerations(self) -> np.ndarray:
         return self._get(2)
+
+    def ComputeReactionForce(self, k: int) -> np.ndarray:
+        """Reaction forces after step k (NewmarkBeta::ComputeReactionForce):
+        total-dof vector, zeros off the fixed nodes."""
+        R = np.zeros(self.ntotal)
+        check(lib().svl_nm_reaction(self._h, int(k), ptr(R, C.c_double)))
+        return R
 
     def run(self, k_first: int, nsteps: int, history: bool = False):
         hist = np.zeros((nsteps, self.ntotal)) if history else None

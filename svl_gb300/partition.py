@@ -142,18 +142,28 @@ class Partition:
         k = 1 .. nt-1 and every node recorder written after each step.  Returns
         the displacement history [nt-1][ntotal]."""
         h = self.make_integrator()
+        need_r = any(r.response == "REACTION" for r in self.recorders)
+        if need_r and not hasattr(h, "ComputeReactionForce"):
+            h.close()
+            raise PartitionError("REACTION recorders are covered for CENTRALDIFFERENCE and NEWMARK without PML")
         h.Initialize()
         nsteps = self.nt - 1
         need_va = any(r.response in ("VEL", "ACCEL") for r in self.recorders)
-        if need_va:
+        R = None
+        if need_va or need_r:
             U = np.zeros((nsteps, self.model.ntotal))
-            V = np.zeros_like(U)
-            A = np.zeros_like(U)
+            V = np.zeros_like(U) if need_va else None
+            A = np.zeros_like(U) if need_va else None
+            R = np.zeros_like(U) if need_r else None
             for s in range(nsteps):
                 if h.ComputeNewStep(s + 1):
                     raise RuntimeError("A PROBLEM WAS ENCOUNTERED at step %d: %s"
                                        % (s + 1, capi.lib().svl_last_error().decode()))
-                U[s], V[s], A[s] = h.GetDisplacements(), h.GetVelocities(), h.GetAccelerations()
+                U[s] = h.GetDisplacements()
+                if need_va:
+                    V[s], A[s] = h.GetVelocities(), h.GetAccelerations()
+                if need_r:                     # DynamicAnalysis::UpdateDomain (DynamicAnalysis.cpp:128-150)
+                    R[s] = h.ComputeReactionForce(s + 1)
         else:
             U = h.run(1, nsteps, history=True)
             V = A = None
@@ -162,7 +172,7 @@ class Partition:
             out = Path(solution_dir) if solution_dir else (self.root / "Solution" / self.combo_folder)
             out.mkdir(parents=True, exist_ok=True)
             for r in self.recorders:
-                hist = {"DISP": U, "VEL": V, "ACCEL": A}[r.response]
+                hist = {"DISP": U, "VEL": V, "ACCEL": A, "REACTION": R}[r.response]
                 write_node_recorder(out / r.file, self, r, hist)
         return U
 
@@ -361,7 +371,7 @@ def load_partition(path, run_dir=None) -> Partition:
         if r["name"].upper() != "NODE":
             raise PartitionError("recorder %s is not covered (NODE only)" % r["name"])
         resp = r["resp"].upper()
-        if resp not in ("DISP", "VEL", "ACCEL"):
+        if resp not in ("DISP", "VEL", "ACCEL", "REACTION"):
             raise PartitionError("node recorder response %s is not covered" % r["resp"])
         recs.append(Recorder(name="NODE", file=r["file"], response=resp, ids=[int(x) for x in r["list"]],
                              precision=int(r.get("ndps", 8)), nsamp=int(r.get("nsamp", 1))))

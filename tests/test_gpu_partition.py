@@ -81,6 +81,19 @@ def test_pml_j2_newton_partition_matches_oracle(gpu, tmp_path):
     assert rel_l2(U, ho) <= 1e-8
 
 
+def test_reaction_recorder_matches_oracle(gpu, tmp_path):
+    """A REACTION node recorder written by the pre-processor: its last row
+    against the oracle's reactions after the last step."""
+    p = _part("q4_reaction_cd")
+    p.run(solution_dir=tmp_path)
+    rec = [r for r in p.recorders if r.response == "REACTION"][0]
+    (nn, ndofs, ntotal, nt), head, rows = _read_recorder(tmp_path / rec.file)
+    Ro = O.reaction_run(p.model, p.loads, p.dt, p.nt - 1, integrator="cd")
+    want = Ro[[d for h in head for d in h[2:]]]
+    assert rows.shape[0] == p.nt - 1 and np.abs(want).max() > 0
+    assert np.allclose(rows[-1], want, rtol=1e-6, atol=1e-6 * np.abs(want).max())
+
+
 def test_drm_partition_newmark_matches_oracle(gpu, tmp_path):
     p = _part("q4_drm_newmark")
     U = p.run(solution_dir=tmp_path)

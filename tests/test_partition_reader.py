@@ -20,7 +20,7 @@ def _part(case):
 
 
 @pytest.mark.parametrize("case", ["q4_cd", "h8_newmark_body", "q4_j2_column", "q4_newmark_rayleigh", "q4_pml_extended",
-                                  "q4_pml_j2_newton", "q4_lysmer_cd", "q4_drm_newmark"])
+                                  "q4_pml_j2_newton", "q4_lysmer_cd", "q4_drm_newmark", "q4_reaction_cd"])
 def test_numbering_and_connectivity_follow_the_file(case):
     p = load_partition(_part(case))
     d = json.loads(_part(case).read_text())
@@ -193,3 +193,11 @@ def test_newton_algorithm_and_j2_layers_over_pml():
     h, *_ = O.xnewmark_run(p.model, p.loads, p.dt, 10, algo=10 + 1, maxit=3, cnvgtol=1e-12, newmark=True,
                            step_iters=its)
     assert np.abs(h).max() > 0 and np.all(its == 3)
+
+
+def test_reaction_recorder_is_read():
+    p = load_partition(_part("q4_reaction_cd"))
+    resp = sorted(r.response for r in p.recorders)
+    assert resp == ["DISP", "REACTION"]
+    rec = [r for r in p.recorders if r.response == "REACTION"][0]
+    assert len(rec.ids) == 4
