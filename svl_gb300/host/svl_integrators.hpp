@@ -58,6 +58,13 @@ public:
     std::vector<double> GetDisplacements() const { return get(0); }
     std::vector<double> GetVelocities() const { return get(1); }
     std::vector<double> GetAccelerations() const { return get(2); }
+    // ComputeReactionForce(mesh, k) after step k (CentralDifference.cpp:156-171),
+    // as DynamicAnalysis::UpdateDomain stores it at the fixed nodes
+    std::vector<double> ComputeReactionForce(unsigned int k) const {
+        std::vector<double> r(ntotal_);
+        check(svl_cd_reaction(h_, (int32_t)k, r.data()));
+        return r;
+    }
 
 private:
     std::vector<double> get(int which) const {
@@ -149,6 +156,13 @@ public:
     std::vector<double> GetDisplacements() const { return get(0); }
     std::vector<double> GetVelocities() const { return get(1); }
     std::vector<double> GetAccelerations() const { return get(2); }
+    // NewmarkBeta::ComputeReactionForce after step k (models without PML layers)
+    std::vector<double> ComputeReactionForce(unsigned int k) const {
+        if (x_) throw Error(SVL_ERR_UNSUPPORTED, "reactions are not covered for PML models");
+        std::vector<double> r(ntotal_);
+        check(svl_nm_reaction(h_, (int32_t)k, r.data()));
+        return r;
+    }
 
 private:
     std::vector<double> get(int which) const {

@@ -36,6 +36,8 @@ int main() {
             if (cd.ComputeNewStep(k)) { std::printf("stop at %u\n", k); return 2; }
         double mx = 0;
         for (double u : cd.GetDisplacements()) mx = std::fmax(mx, std::fabs(u));
+        double rmax = 0;
+        for (double r : cd.ComputeReactionForce(100)) rmax = std::fmax(rmax, std::fabs(r));
         svl::gpu::NewmarkBeta nm(md, ld, 4.0 * dt);
         nm.Initialize();
         for (unsigned k = 1; k <= 20; ++k)
@@ -57,7 +59,8 @@ int main() {
         double dnw = 0;
         const std::vector<double> uw = nw.GetDisplacements();
         for (size_t i = 0; i < uw.size(); ++i) dnw = std::fmax(dnw, std::fabs(uw[i] - un[i]));
-        std::printf("max|U| %.6e newmark %.6e extended %.6e (diff %.3e) newton-diff %.3e\n", mx, mn, mxn, dmax, dnw);
+        std::printf("max|U| %.6e newmark %.6e extended %.6e (diff %.3e) newton-diff %.3e reaction %.6e\n", mx, mn,
+                    mxn, dmax, dnw, rmax);
     } catch (const svl::gpu::Error& e) {
         if (e.code == SVL_ERR_NODEVICE) { std::printf("nodevice\n"); return 0; }
         std::printf("error %d %s\n", e.code, e.what());

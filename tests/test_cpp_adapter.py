@@ -40,3 +40,5 @@ def test_cpp_adapter_steps_on_gpu(tmp_path, gpu):
     # NewmarkBeta + NewtonRaphson on an elastic model: the Linear answer up to
     # the PCG tolerance of the Linear run (1e-8)
     assert tok[8] == "newton-diff" and float(tok[9]) <= 1e-6 * unm
+    # reactions at the fixed base after 100 explicit steps
+    assert tok[10] == "reaction" and float(tok[11]) > 0.0
