@@ -212,3 +212,30 @@ def test_convergence_tests_match_a_restatement(test):
     want = {1: n(F), 2: n(du), 3: n(du * F), 4: n(F), 5: n(du), 6: n(du * F), 7: 1.0, 8: -1.0}[test]
     assert np.all(its == 1)
     assert abs(res[0] - want) <= 1e-9 * abs(want)
+
+
+def test_config5_pml_workload_structure():
+    """workloads.config5_pml: PML3DHexa8 layers on the sides and the bottom
+    with 9 dofs at their nodes, J2 only in the solid top layers, the outer PML
+    boundary fixed in displacement, dofs numbered node by node; a few
+    NewmarkBeta + Newton steps on it in the oracle stay finite (the GPU parity
+    test runs 25 steps)."""
+    from svl_gb300 import _capi as capi
+    from svl_gb300 import workloads
+    m, L, dt = workloads.config5_pml(6, 6, 6, npml=1, n_j2=2, nt=30)
+    assert m.elem_pml.sum() == 6 * 6 * 6 - 4 * 4 * 5
+    mt = m.mat_type[m.elem_mat]
+    assert np.all(mt[m.elem_pml == 1] == capi.SVL_MAT_ELASTIC3DLINEAR)
+    assert (mt == capi.SVL_MAT_PLASTIC3DJ2).sum() == 4 * 4 * 2
+    nd = m.node_ndof
+    assert set(np.unique(nd)) == {3, 9}
+    td = np.concatenate([m.totaldof[n, :nd[n]] for n in range(m.nnode)])
+    assert np.array_equal(td, np.arange(m.ntotal))
+    X = m.coords
+    outer = np.isclose(X[:, 0], 0) | np.isclose(X[:, 0], 12) | np.isclose(X[:, 1], 0) | np.isclose(X[:, 1], 12) \
+        | np.isclose(X[:, 2], 0)
+    assert np.all(m.freedof[outer, :3] == -1) and np.all(m.freedof[~outer, :3] >= 0)
+    its = np.zeros(4, np.int32)
+    h, *_ = O.xnewmark_run(m, L, dt, 4, algo=2, maxit=2, cnvgtol=0.0, newmark=True, step_iters=its)
+    disp = m.totaldof[:, :3].ravel()
+    assert np.all(its == 2) and np.all(np.isfinite(h)) and 0 < np.abs(h[:, disp]).max() < 1.0
