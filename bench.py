@@ -147,8 +147,19 @@ def cpu_baseline(m, L, dt, steps_cap, budget_s=20.0):
     n = int(max(1, min(steps_cap, budget_s / per)))
     O.cd_run(m, L, dt, n, mode=1, history=False, timing=t)
     val = m.nfree * n / t["seconds"]
-    return {"value": val, "unit": "DOF-steps/s", "cores": nthreads, "kind": "port",
-            "sample": "%d time steps of the same model on the CPU oracle (OpenMP element loop, ordered scatter)" % n}
+    out = {"value": val, "unit": "DOF-steps/s", "cores": nthreads, "kind": "port",
+           "sample": "%d time steps of the same model on the CPU oracle (OpenMP element loop, ordered scatter)" % n}
+    # the reference's own structure, single-threaded per rank: J, J^-1 and B
+    # recomputed per Gauss point per call (one step)
+    try:
+        t1 = {}
+        O.cd_run(m, L, dt, 1, mode=0, history=False, timing=t1)
+        out["single_thread_reference_faithful"] = {
+            "value": m.nfree / t1["seconds"], "unit": "DOF-steps/s", "cores": 1,
+            "sample": "1 time step of the same model, the oracle's reference-faithful mode"}
+    except Exception as exc:  # noqa: BLE001
+        out["single_thread_reference_faithful"] = {"error": str(exc)[:200]}
+    return out
 
 
 def implicit_pcg(steps, warm=20, tol=1e-8):
