@@ -279,6 +279,30 @@ def implicit_profile():
 NN_TRAIN = {"solve_steps": 0, "n_synthetic": 300, "iters": 1500, "batch": 8, "lr": 2e-3, "seed": 1, "max_sweeps": 5}
 
 
+def max_over_ranks(pg, ms, device="cuda"):
+    """The slowest rank's time: all-reduce MAX (every rank receives it), then a
+    barrier.  pg = None (one process) returns ms."""
+    if not pg:
+        return ms
+    import torch
+    t = torch.tensor([float(ms)], device=device)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    pg.barrier()
+    return float(t.item())
+
+
+def job_value(world_size, nfree_per_rank, steps, ms):
+    """Whole-job DOF-steps/s: every rank advances its own instances (weak
+    scaling), so the job's work is world_size x one rank's."""
+    return world_size * nfree_per_rank * steps / (ms / 1e3)
+
+
+def rank_seed(rank, workload, b):
+    """Seed of instance b on `rank`: ensembles (config 3) get different
+    columns per rank; the single-mesh workloads run the same model as replicas."""
+    return (rank * 1000 if workload == "config3" else 0) + b
+
+
 def dist_info():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -350,8 +374,7 @@ def main():
     capi.check(capi.lib().svl_set_device(local))
 
     # ensembles shard across ranks: every rank advances its own 256 columns (weak scaling)
-    seed0 = rank * 1000 if args.workload == "config3" else 0
-    insts = [build_workload(args.workload, seed=seed0 + b) for b in range(nb)]
+    insts = [build_workload(args.workload, seed=rank_seed(rank, args.workload, b)) for b in range(nb)]
     m, L, dt0, desc = insts[0]
     dt = min(x[2] for x in insts)
     nd = m.ndim
@@ -382,16 +405,11 @@ def main():
         pg.barrier()
     with ClockSampler(local) as clk:
         ms = cd.run_timed(1, args.steps)
-    if pg:
-        import torch
-        t = torch.tensor([ms], device="cuda")
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        ms = float(t.item())
-        pg.barrier()
+    ms = max_over_ranks(pg, ms)
     launches = cd.launches()
     clocks = clk.summary()
     ms_step = ms / args.steps
-    value = ws * nfree_total * args.steps / (ms / 1e3)
+    value = job_value(ws, nfree_total, args.steps, ms)
     U_last = cd.get(0, 0) if args.precision == "mixed" else cd.GetDisplacements()
     finite = bool(np.isfinite(U_last).all())
     cd.close()
