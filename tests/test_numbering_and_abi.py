@@ -101,3 +101,32 @@ def test_cd_create_without_gpu_reports_no_device():
     h = C.c_void_p()
     st = capi.lib().svl_cd_create(C.byref(md), C.byref(ld), C.byref(opts), C.byref(h))
     assert st == capi.SVL_ERR_NODEVICE
+
+
+def test_xnm_options_are_checked_before_any_device_work():
+    """svl_xnm_create rejects an unknown algorithm and Newton settings outside
+    the reference's (nstep > 0, cnvgtest 1-8, cnvgtol >= 0) with
+    SVL_ERR_INVALID, on any machine; valid options without a GPU give
+    SVL_ERR_NODEVICE."""
+    from tests.conftest import gpu_available
+    from tests.helpers import pml_box
+    m, L, dt = pml_box(2, (4, 3), npml=2, nt=10)
+    md, ld = m.desc(), L.desc()
+
+    def create(**kw):
+        o = dict(dt=dt, ftol=1e-12, mtol=1e-12, tol=1e-10, maxit=1000, algorithm=capi.SVL_ALGO_LINEAR,
+                 newton_maxit=0, cnvgtest=4, cnvgtol=0.0, integrator=capi.SVL_XNM_EXTENDED_NEWMARK, single_inner=1)
+        o.update(kw)
+        h = C.c_void_p()
+        st = capi.lib().svl_xnm_create(C.byref(md), C.byref(ld), C.byref(capi.XnmOpts(**o)), C.byref(h))
+        if st == capi.SVL_OK:
+            capi.lib().svl_xnm_destroy(h)
+        return st
+
+    assert create(algorithm=7) == capi.SVL_ERR_INVALID
+    assert create(algorithm=capi.SVL_ALGO_NEWTON, newton_maxit=0) == capi.SVL_ERR_INVALID
+    assert create(algorithm=capi.SVL_ALGO_NEWTON, newton_maxit=3, cnvgtest=9) == capi.SVL_ERR_INVALID
+    assert create(algorithm=capi.SVL_ALGO_NEWTON, newton_maxit=3, cnvgtol=-1.0) == capi.SVL_ERR_INVALID
+    assert create(dt=0.0) == capi.SVL_ERR_INVALID
+    if not gpu_available():
+        assert create(algorithm=capi.SVL_ALGO_NEWTON, newton_maxit=3, cnvgtest=1) == capi.SVL_ERR_NODEVICE
