@@ -1,4 +1,7 @@
-// ExtendedNewmarkBeta with PML elements on the GPU (svl_xnm_*).
+// ExtendedNewmarkBeta with PML elements on the GPU (svl_xnm_*), and
+// NewmarkBeta on the same elements (integrator SVL_XNM_NEWMARK: the increment
+// terms in the effective force, no history matrix, the support-motion
+// increment of step k - 1; NewmarkBeta.cpp:117-235).
 //
 // The reference assembles M, C, K and G once (ExtendedNewmarkBeta.cpp:64-70),
 // re-assembles K and forms K + 4/dt^2 M + 2/dt C + dt/3 G every step
@@ -20,6 +23,10 @@
 // preconditioner |diag(Keff)|^-1, restarted from its iterate until the true
 // residual meets the tolerance.  Reductions are two-stage with a fixed block
 // count, so results do not depend on scheduling.
+// Operator applications (all element inputs one vector) use one thread per
+// (element, Gauss point): k_xsolid_gp / k_pml_action_gp.  In the MINRES inner
+// iterations they run in single precision on float tables and float element
+// vectors (k_xgather_f); the restarts' true residual uses the double operator.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
