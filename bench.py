@@ -5,7 +5,8 @@ A "step" is one time step of the whole batch: element forces, the ordered
 node gather, the diagonal solve and the state update.  Default workload: the
 3D configuration (lin3DHexa8 128 x 128 x 64, h = 2 m, log-normal Vs field,
 double-couple body force), as a batch of 4 seeded realisations advanced by
-the mixed-precision path (tensor-core element forces, FP64 update); the FP64
+the mixed-precision path (tensor-core TF32 hi/lo element forces, compensated
+FP32-pair state update); the FP64
 plain path is timed on one realisation beside it, and the mixed result's
 error against it is reported.  The PML layers of that configuration are not
 built yet; the box has fixed/roller faces instead (stated in the config).
@@ -493,7 +494,7 @@ def main():
         line = {
             "metric": "DOF-steps/s", "value": value, "unit": "DOF-steps/s", "n_gpus": ws, "steps": args.steps,
             "warmup": warm, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "tf32x3+f64" if args.precision == "mixed" else "f64",
+            "vs_baseline": None, "dtype": "tf32x3+f32x2" if args.precision == "mixed" else "f64",
             "data": "synthetic (seeded)",
             "config": {"workload": desc, "instances": nb, "free_dof_per_instance": m.nfree,
                        "elements_per_instance": m.nelem, "dt": dt,

@@ -221,7 +221,8 @@ int svl_lumped_mass(const svl_model_desc* model, double mtol, double* mass_total
  *     291-532),
  *   and the element/material calls under them.                              */
 #define SVL_PREC_FP64   0   /* everything in FP64 (the plain form)             */
-#define SVL_PREC_MIXED  1   /* FP32/TF32 element forces, FP64 state update      */
+#define SVL_PREC_MIXED  1   /* TF32 hi/lo element forces with FP32 accumulation;
+                               displacement state as a compensated FP32 pair */
 
 typedef struct svl_cd_opts {
     double  dt;
@@ -275,7 +276,10 @@ void svl_cd_destroy(svl_cd* cd);
  * tensor-core contraction F_e = lambda_e (K_lambda u_e) + mu_e (K_mu u_e):
  * the 48 x 24 stacked reference matrix times the 24 x elements displacement
  * block, TF32 hi/lo split operands (three products) with FP32 accumulation
- * in TMEM; the displacement update stays in FP64.  Reference summation order
+ * in TMEM.  The displacement state is a compensated pair of FP32 numbers per
+ * dof (hi + lo, about 48 significant bits, updated with error-free TwoSum
+ * transformations), not FP64; results state their error against the FP64
+ * path (<= 1e-5 relative L2 over the history in the tests).  Reference summation order
  * at every node is kept; the assembler's force tolerance filter is not
  * applied on this path.  `models` and `loads` are arrays of ninst
  * descriptors (one per instance, same grid).  precision must be
@@ -295,6 +299,13 @@ int  svl_cdx_run_timed(svl_cdx* cdx, int32_t k_first, int32_t nsteps, float* ms)
 /* which: 0 = U, 1 = V, 2 = A of instance `inst` after the last step. */
 int  svl_cdx_get(svl_cdx* cdx, int32_t inst, int32_t which, double* out);
 int  svl_cdx_launch_count(svl_cdx* cdx, int64_t* launches);
+/* Persistent-grid size of the fused step kernel: `ctas` CTAs (one per SM at
+ * most; 0 = one per SM, the default), each looping over the node tiles
+ * blockIdx.x, blockIdx.x + ctas, ...  Fewer CTAs give each one more tiles
+ * (a test and tuning hook: the results do not depend on it).  No
+ * counterpart in the reference. */
+int  svl_cdx_set_ctas(svl_cdx* cdx, int32_t ctas);
+int  svl_cdx_get_ctas(svl_cdx* cdx, int32_t* ctas);
 void svl_cdx_destroy(svl_cdx* cdx);
 
 /* ---- implicit Newmark (average acceleration), Linear algorithm --------- */
@@ -516,11 +527,14 @@ int  svl_pml_element_action(int32_t ndim, int32_t nelem, const double* X, const 
  * buffer when a history is requested); svl_cd_run_noalloc never allocates.
  *
  * It advances the handle's state exactly like svl_cd_run(cd, k_first,
- * nsteps, NULL) -- same kernels, same results -- but the per-step element
- * force block lives in one library-wide static device array of
- * SVL_NOALLOC_SCRATCH_BYTES instead of the handle's own buffer, and the
- * kernels are launched directly (no graph).  Every GPU that loads the
- * library holds that array until the process exits.
+ * nsteps, NULL) -- the same launch sequence per step (element forces,
+ * domain-reduction forces when the loads have them, then the node kernels),
+ * the same results -- but the per-step element force block lives in one
+ * library-wide static device array of SVL_NOALLOC_SCRATCH_BYTES instead of
+ * the handle's own buffer, and the kernels are launched directly (no graph).
+ * Every GPU that loads the library holds that array until the process exits.
+ * svl_cd_launch_count then reports this call's kernels (one step-index
+ * set-up kernel plus the per-step kernels).
  *
  * Limit: nelem * nen * ndof * 8 bytes must fit in SVL_NOALLOC_SCRATCH_BYTES
  * (8 MiB: at most 43690 lin3DHexa8 or 131072 lin2DQuad4 elements); larger

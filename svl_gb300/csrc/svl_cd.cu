@@ -979,10 +979,11 @@ static int cd_setup(svl_cd* cd, const svl_load_desc* L) {
 }
 
 // Launches kernel `kind` of one step (0 element, 1 node, 2 residual,
-// 3 free, 4 update); returns SVL_OK, or 1 when the kind is not used.
-static int cd_launch_kind(svl_cd* cd, int kind) {
+// 3 free, 4 update) on the buffers of view `d` (the handle's own view, or
+// the no-alloc copy whose element force block is the static scratch);
+// returns SVL_OK, or 1 when the kind is not used.
+static int cd_launch_kind(svl_cd* cd, const DevView& d, int kind) {
     const HostModel& m = cd->m;
-    const DevView& d = cd->d;
     const int eb = 128, nb = 256;
     const int eg = (m.nelem + eb - 1) / eb, ng = (m.nnode + nb - 1) / nb, fg = (m.nfree + nb - 1) / nb;
     switch (kind) {
@@ -1025,15 +1026,21 @@ static int cd_launch_kind(svl_cd* cd, int kind) {
     return SVL_OK;
 }
 
-static int cd_launch_step(svl_cd* cd) {
+static int cd_launch_step_view(svl_cd* cd, const DevView& d) {
     for (int kind = 0; kind < 5; ++kind) {
-        const int st = cd_launch_kind(cd, kind);
+        const int st = cd_launch_kind(cd, d, kind);
         if (st != SVL_OK && st != 1) return st;
     }
     return SVL_OK;
 }
 
-static int launches_per_step(const svl_cd* cd) { return cd->identity_T ? 2 : (cd->m.nfree > 0 ? 4 : 3); }
+static int cd_launch_step(svl_cd* cd) { return cd_launch_step_view(cd, cd->d); }
+
+// kernels per step: element forces (+ domain-reduction forces), then the
+// node kernel, or residual / free-dof solve / update with constraints
+static int launches_per_step(const svl_cd* cd) {
+    return (cd->identity_T ? 2 : (cd->m.nfree > 0 ? 4 : 3)) + (cd->d.ndrm > 0 ? 1 : 0);
+}
 
 extern "C" {
 
@@ -1246,7 +1253,7 @@ int svl_cd_profile(svl_cd* cd, int32_t k_first, int32_t nsteps, double* ms_kerne
         int used[5];
         CUDA_TRY(cudaEventRecord(ev[0], cd->stream));
         for (int kind = 0; kind < 5; ++kind) {
-            const int st = cd_launch_kind(cd, kind);
+            const int st = cd_launch_kind(cd, cd->d, kind);
             if (st != SVL_OK && st != 1) return st;
             used[kind] = (st == SVL_OK);
             CUDA_TRY(cudaEventRecord(ev[kind + 1], cd->stream));
@@ -1435,28 +1442,6 @@ int noalloc_scratch(int dev, double** out) {
 
 __global__ void k_set_step(int* step, int value) { step[0] = value; }
 
-// The launches of one step, as in svl_cd_run, on a view whose element force
-// block points at the static scratch.
-int noalloc_launch_step(svl_cd* cd, const DevView& d) {
-    const HostModel& m = cd->m;
-    const int eb = 128, nb = 256;
-    const int eg = (m.nelem + eb - 1) / eb, ng = (m.nnode + nb - 1) / nb, fg = (m.nfree + nb - 1) / nb;
-    if (m.ndim == 2) k_element<2, 4><<<eg, eb, 0, cd->stream>>>(d, d.Us, m.ngp, 1);
-    else k_element<3, 8><<<eg, eb, 0, cd->stream>>>(d, d.Us, m.ngp, 1);
-    if (cd->identity_T) {
-        if (m.ndim == 2) k_node<2><<<ng, nb, 0, cd->stream>>>(d);
-        else k_node<3><<<ng, nb, 0, cd->stream>>>(d);
-    } else {
-        if (m.ndim == 2) k_residual<2><<<ng, nb, 0, cd->stream>>>(d);
-        else k_residual<3><<<ng, nb, 0, cd->stream>>>(d);
-        if (m.nfree > 0) k_free<<<fg, nb, 0, cd->stream>>>(d);
-        if (m.ndim == 2) k_update<2><<<ng, nb, 0, cd->stream>>>(d);
-        else k_update<3><<<ng, nb, 0, cd->stream>>>(d);
-    }
-    CUDA_TRY(cudaGetLastError());
-    return SVL_OK;
-}
-
 }  // namespace
 
 extern "C" int svl_cd_run_noalloc(svl_cd* cd, int32_t k_first, int32_t nsteps, double* d_U_out) {
@@ -1476,9 +1461,13 @@ extern "C" int svl_cd_run_noalloc(svl_cd* cd, int32_t k_first, int32_t nsteps, d
     TRY(noalloc_scratch(attr.device, &scratch));
     DevView d = cd->d;
     d.fe = scratch;
+    const int64_t l0 = cd->launches;
     k_set_step<<<1, 1, 0, cd->stream>>>(d.step, k_first - 1);
     CUDA_TRY(cudaGetLastError());
-    for (int s = 0; s < nsteps; ++s) TRY(noalloc_launch_step(cd, d));
+    ++cd->launches;
+    // the launch sequence of svl_cd_run, kernel for kernel, on the swapped view
+    for (int s = 0; s < nsteps; ++s) TRY(cd_launch_step_view(cd, d));
+    cd->launches_last = cd->launches - l0;
     if (d_U_out)
         CUDA_TRY(cudaMemcpyAsync(d_U_out, d.U, sizeof(double) * m.ntotal, cudaMemcpyDeviceToDevice, cd->stream));
     return SVL_OK;

@@ -1073,6 +1073,22 @@ int svl_cdx_get(svl_cdx* h, int32_t inst, int32_t which, double* out) {
     return SVL_OK;
 }
 
+int svl_cdx_set_ctas(svl_cdx* h, int32_t ctas) {
+    if (!h || ctas < 0) { set_error("bad argument"); return SVL_ERR_INVALID; }
+    int dev = 0, sms = 0;
+    CUDA_TRY(cudaGetDevice(&dev));
+    CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const int cap = ctas == 0 ? sms : std::min(ctas, sms);
+    h->grid = std::max(1, std::min(h->ntiles, cap));
+    return SVL_OK;
+}
+
+int svl_cdx_get_ctas(svl_cdx* h, int32_t* ctas) {
+    if (!h || !ctas) { set_error("bad argument"); return SVL_ERR_INVALID; }
+    *ctas = h->grid;
+    return SVL_OK;
+}
+
 int svl_cdx_launch_count(svl_cdx* h, int64_t* launches) {
     if (!h || !launches) { set_error("bad argument"); return SVL_ERR_INVALID; }
     *launches = h->launches_last;

@@ -107,7 +107,8 @@ class CentralDifference:
 class StructuredCentralDifference:
     """Mixed-precision batched central difference for `ninst` instances of one
     uniform lin3DHexa8 grid (svl_cdx_*): tensor-core element forces (TF32
-    hi/lo, FP32 accumulation), FP64 displacement update.  Same step as
+    hi/lo, FP32 accumulation), displacement state as a compensated FP32 pair
+    (hi + lo, ~48 significant bits; not FP64).  Same step as
     CentralDifference; `instances` is a list of (Model, Loads) built on the
     grid given by `ne`, `h`, `origin`."""
 
@@ -163,6 +164,14 @@ class StructuredCentralDifference:
     def launches(self) -> int:
         n = C.c_int64()
         check(lib().svl_cdx_launch_count(self._h, C.byref(n)))
+        return int(n.value)
+
+    def set_ctas(self, ctas: int) -> int:
+        """CTAs of the persistent step kernel (0 = one per SM); returns the
+        grid size in effect."""
+        check(lib().svl_cdx_set_ctas(self._h, int(ctas)))
+        n = C.c_int32()
+        check(lib().svl_cdx_get_ctas(self._h, C.byref(n)))
         return int(n.value)
 
     def close(self):

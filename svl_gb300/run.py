@@ -2,13 +2,19 @@
 
     python -m svl_gb300.run -dir /path/to/Partition/ -file 'Model.1.$.json' [more files]
 
-Each file is a partition written by the pre-processor; `$` stands for the
+The file is a partition written by the pre-processor; `$` stands for the
 process rank (RP/12-Utilities/Driver.hpp:255-265), 0 here: one GPU runs one
-partition.  Files are run in the order given (the run-process's stages), each
-with its integrator, algorithm and recorders; node recorders go to
-`<dir>/../Solution/<combination>/` as the run-process writes them
+partition, with its integrator, algorithm and recorders; node recorders go
+to `<dir>/../Solution/<combination>/` as the run-process writes them
 (RP/12-Utilities/Recorder.cpp:73-106).  Exit status 0 on success, 1 when a
-step fails ("A PROBLEM WAS ENCOUNTERED"), 2 for bad arguments or files."""
+step fails ("A PROBLEM WAS ENCOUNTERED"), 2 for bad arguments or files.
+
+One file per run.  The run-process's RunDriverFile (Driver.hpp:2049-2101)
+treats several -file arguments as consecutive stages on ONE mesh: later
+files add, delete or modify entities of it and continue from the previous
+stage's displacements and material states.  Those stage updates are not
+covered here, so more than one file is rejected (status 2) rather than run
+from rest on a fresh model, which would give different results."""
 from __future__ import annotations
 
 import sys
@@ -61,6 +67,10 @@ def main(argv: Optional[List[str]] = None) -> int:
     path, names = parse_args(argv)
     if path is None or not names:
         print("ERROR: NOT ENOUGH Command line input arguments (-dir and -file).")
+        return 2
+    if len(names) > 1:
+        print("ERROR: %d files given; staged runs (several -file arguments continuing on one mesh) are not "
+              "covered, run one partition file per call." % len(names))
         return 2
     try:
         parts = load_all(path, names)

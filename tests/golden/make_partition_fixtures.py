@@ -451,4 +451,7 @@ def main(ref_root: str):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("SVL_REFERENCE_ROOT")
+    if not root:
+        raise SystemExit("usage: %s <SVL source tree>  (or set SVL_REFERENCE_ROOT)" % Path(__file__).name)
+    main(root)

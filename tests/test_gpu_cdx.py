@@ -8,15 +8,24 @@ import pytest
 from oracle import oracle as O
 from svl_gb300 import SvlError, StructuredCentralDifference
 from svl_gb300 import _capi as capi
+from svl_gb300 import ricker
 from tests.helpers import h8_box, rel_l2
 
 pytestmark = pytest.mark.gpu
 TOL_MIXED = 1e-5
 
 
-def _instances(nx, ny, nz, seeds, nt, amp=1.0e7):
+def _instances(nx, ny, nz, seeds, nt, amp=1.0e7, corner_loads=False):
     inst = [h8_box(nx, ny, nz, seed=s, nt=nt, amp=amp) for s in seeds]
     dt = min(d for _, _, d in inst)        # one step for the batch
+    if corner_loads:
+        # vertical point loads on surface nodes near the far corner, i.e. in the
+        # last node tiles of the instance, with a different delay per instance
+        for b, (m, L, _) in enumerate(inst):
+            s = L.add_series(ricker(nt + 1, dt, 4.0 + b, amp=amp * 8.0))
+            for (i, j) in ((nx - 2, ny - 2), (nx - 1, ny - 3), (nx // 3, ny - 1 - b)):
+                node = nz * (nx + 1) * (ny + 1) + j * (nx + 1) + i
+                L.add_point_load(m, node, (0.0, 0.0, -1.0), s)
     return [(m, L) for m, L, _ in inst], dt
 
 
@@ -79,3 +88,54 @@ def test_cdx_rejects_unsupported_models(gpu):
     with pytest.raises(SvlError) as ei:     # wrong grid spacing
         StructuredCentralDifference((6, 5, 4), (1.0, 2.0, 2.0), [(m, L)], dt)
     assert ei.value.code == capi.SVL_ERR_INVALID
+
+
+def test_cdx_persistent_tiles_match_oracle(gpu):
+    """Every CTA of the persistent kernel runs many node tiles: 3 instances of
+    20x18x14 elements (18 tiles each, 54 in all) on 8 CTAs, i.e. 6-7 tiles and
+    40 MMA tiles per CTA, so the halo prefetch into reused buffers, the reload
+    of the owned state, the mbarrier phase flips past the first pass, the reuse
+    of the eight TMEM accumulator slots and the load-table walk of later tiles
+    all run.  Loads sit in the last tiles.  The full history of every instance
+    must match the FP64 oracle, and a one-CTA run (54 tiles in one CTA) must be
+    bitwise identical to the one-CTA-per-SM run."""
+    nx, ny, nz = 20, 18, 14
+    nt = 250
+    inst, dt = _instances(nx, ny, nz, (11, 12, 13), nt, corner_loads=True)
+    runs = {}
+    for ctas in (8, 1, 0):
+        cdx = StructuredCentralDifference((nx, ny, nz), (2.0, 2.0, 2.0), inst, dt)
+        got = cdx.set_ctas(ctas)
+        assert got == (54 if ctas == 0 else ctas) or (ctas == 0 and got < 54)
+        for b in range(len(inst)):
+            cdx.Initialize(b)
+        runs[ctas] = cdx.run(1, nt, history=True)
+        cdx.close()
+    assert np.array_equal(runs[1], runs[0]) and np.array_equal(runs[8], runs[0])
+    for b, (m, L) in enumerate(inst):
+        ho, *_ = O.cd_run(m, L, dt, nt, mode=1)
+        # the corner loads move the last tiles
+        corner = nz * (nx + 1) * (ny + 1) + (ny - 2) * (nx + 1) + (nx - 2)
+        assert np.abs(ho[:, 3 * corner + 2]).max() > 1e-3 * np.abs(ho).max()
+        err = rel_l2(runs[8][:, b, :], ho)
+        assert err <= TOL_MIXED, (b, err)
+
+
+def test_cdx_many_tiles_per_sm_match_oracle(gpu):
+    """Default grid (one CTA per SM) on 4 instances of 48x48x32 elements: 245
+    tiles each, 980 in all, about 6.4 tiles per CTA on 152 SMs.  Full history
+    of every instance against the FP64 oracle over 200 steps."""
+    nx, ny, nz = 48, 48, 32
+    nt = 200
+    inst, dt = _instances(nx, ny, nz, (21, 22, 23, 24), nt, corner_loads=True)
+    cdx = StructuredCentralDifference((nx, ny, nz), (2.0, 2.0, 2.0), inst, dt)
+    assert cdx.set_ctas(0) <= 980
+    for b in range(len(inst)):
+        cdx.Initialize(b)
+    hist = cdx.run(1, nt, history=True)
+    cdx.close()
+    for b, (m, L) in enumerate(inst):
+        ho, *_ = O.cd_run(m, L, dt, nt, mode=1, history=True)
+        assert np.abs(ho).max() > 0
+        err = rel_l2(hist[:, b, :], ho)
+        assert err <= TOL_MIXED, (b, err)

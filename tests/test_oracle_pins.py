@@ -9,10 +9,10 @@
 * Internal consistency: lumped mass, body loads, element symmetry, the
   faithful and fast central-difference modes, and the J2 return mapping.
 
-The zips are read at test time from the reference tree when it is present.
+The validation data are committed under tests/golden/pins/, copied byte for
+byte from the reference's 03-Validations/01-Debugging/<case>.zip by
+tests/golden/make_pin_fixtures.py.
 """
-import io
-import zipfile
 from pathlib import Path
 
 import numpy as np
@@ -23,19 +23,12 @@ from svl_gb300 import _capi as capi
 from svl_gb300.model import Loads, Model
 from tests.helpers import h8_box, q4_box, q4_j2_columns, rel_l2
 
-REF = Path("/root/reference/03-Validations/01-Debugging")
-
-
-def _zip_text(case, member):
-    z = REF / (case + ".zip")
-    if not z.exists():
-        pytest.skip("reference validation case %s not available" % case)
-    with zipfile.ZipFile(z) as f:
-        return f.read(case + "/" + member).decode()
+PINS = Path(__file__).resolve().parent / "golden" / "pins"
 
 
 def _loadtxt(case, member, skip=0):
-    return np.loadtxt(io.StringIO(_zip_text(case, member)), skiprows=skip)
+    f = PINS / (case.split("-")[0] + "_" + member.replace("/", "_"))
+    return np.loadtxt(f, skiprows=skip)
 
 
 def _one_quad(j2=False):

@@ -29,6 +29,14 @@ def test_loads_the_fixture_and_reports_missing_files(tmp_path):
     assert R.main(["-file", "Fixture.1.$.json"]) == 2
 
 
+def test_staged_multi_file_runs_are_rejected(capsys):
+    """Several -file arguments are stages on one mesh in the run-process
+    (Driver.hpp:2049-2101); they are refused, not run from rest one by one."""
+    d = GOLD / "partition_q4_cd" / "Partition"
+    assert R.main(["-dir", str(d), "-file", "Fixture.1.$.json", "Fixture.1.$.json"]) == 2
+    assert "staged runs" in capsys.readouterr().out
+
+
 def test_without_a_gpu_the_run_fails_loudly(tmp_path):
     from tests.conftest import gpu_available
     if gpu_available():

@@ -16,7 +16,7 @@ import pytest
 from svl_gb300 import CentralDifference
 from svl_gb300 import _capi as capi
 from svl_gb300.model import Model
-from tests.helpers import h8_box, q4_box, q4_j2_columns, rel_l2
+from tests.helpers import drm_box, h8_box, q4_box, q4_j2_columns, rel_l2
 
 pytestmark = pytest.mark.gpu
 TOL = 1e-12   # the FP64 parity tolerance used by the other GPU tests
@@ -26,9 +26,11 @@ def _models():
     yield "q4_box", q4_box(40, 20, nt=200)
     yield "q4_j2_periodic_columns", q4_j2_columns(3, 4, (10, 16, 22), nt=200, pga=6.0)
     yield "h8_box", h8_box(10, 9, 8, nt=200)
+    m, L, dt, _, _ = drm_box(nt=140)
+    yield "q4_drm_box", (m, L, dt)
 
 
-@pytest.mark.parametrize("name", ["q4_box", "q4_j2_periodic_columns", "h8_box"])
+@pytest.mark.parametrize("name", ["q4_box", "q4_j2_periodic_columns", "h8_box", "q4_drm_box"])
 def test_noalloc_matches_run_on_two_calls_in_a_row(gpu, name):
     torch = pytest.importorskip("torch")
     m, L, dt = dict(_models())[name]
@@ -49,7 +51,14 @@ def test_noalloc_matches_run_on_two_calls_in_a_row(gpu, name):
     capi.check(capi.lib().svl_cd_run_noalloc(na._h, 61, 70, C.c_void_p(out.data_ptr())))
     na.sync()
     V2 = out.cpu().numpy().copy()
+    launches = na.launches()
     na.close()
+    # the no-alloc call reports its own kernel count: one step-index set-up
+    # plus the same kernels per step as svl_cd_run
+    per_step = 2 if m.nconstraint == 0 else 4
+    if L is not None and len(L.drm_elem):
+        per_step += 1
+    assert launches == 1 + 70 * per_step
     assert np.abs(U2).max() > 0
     assert rel_l2(V1, U1) <= TOL
     assert rel_l2(V2, U2) <= TOL
