@@ -405,6 +405,36 @@ void svl_nm_destroy(svl_nm* nm);
                                               + C (V - 2/dt dU) - T^T Keff SM(k-1),
                                        Keff = K + 4/dt^2 M + 2/dt C (G is not used;
                                        the NEWMARK integrator of a PML model)     */
+/* SVL_XNM_CENTRAL_DIFFERENCE: explicit central difference on a model with PML
+ * layers -- a scheme of this library, for the CENTRALDIFFERENCE integrator of
+ * a PML model.  The reference's CentralDifference applies no PML history
+ * (CentralDifference.cpp:114-120) and keeps the PML mass consistent with a
+ * negative stress block (PML3DHexa8.cpp:214-284), so its M/dt^2 + C/2dt is
+ * sparse and indefinite.  Here the same element matrices M, C, K, G are
+ * advanced explicitly: displacements at the integer steps, the PML stress
+ * dofs S at the half steps (leapfrog); the N N blocks of the PML matrices are
+ * row-sum lumped per node (diagonal on displacement dofs, one ns x ns block
+ * per node on its stress dofs), the displacement-stress couplings act
+ * through the element action, and ubar / Sbar integrate by the trapezoid /
+ * midpoint rules:
+ *   (Mu/dt^2 + Cu/2dt) du = Fext(k) - Fint_solid(u^k)
+ *       - (C_uS sdot + K_uS smid + G_uS Sbar^k) - Ku u^k - Gu ubar^k
+ *       + (Mu/dt^2 - Cu/2dt)(u^k - u^(k-1)),
+ *   sdot = (S^(k+1/2) - S^(k-1/2))/dt, smid = (S^(k+1/2) + S^(k-1/2))/2;
+ *   (Ms/dt^2 + Cs/2dt) dS = -(C_Su udot + K_Su umid + G_Su ubar^(k+1/2))
+ *       - Ks S^(k+1/2) - Gs Sbar^(k+1/2) + (Ms/dt^2 - Cs/2dt)(S^(k+1/2) - S^(k-1/2)),
+ *   udot = (u^(k+1) - u^k)/dt, umid = (u^(k+1) + u^k)/2.
+ * Without PML elements it is the plain central difference.  Element forces
+ * on displacement rows carry the force filter.  U on a PML node's stress
+ * dofs holds S at the half step after U's time; V and A follow
+ * CentralDifference.cpp:141-144 on every dof.  The Linear algorithm only;
+ * constraints with one master per constrained displacement dof (the EQUAL
+ * ties mergeDomain writes; the solve is T^T d T, diagonal), none on stress
+ * dofs; no dashpots or domain-reduction loads; support motion on
+ * displacement dofs; mass-proportional Rayleigh damping on solid elements;
+ * tol and maxit are not used.  Stable below the lumped-mass step limit of
+ * the solid region (measured: 0.9 h/Vp on 2D boxes). */
+#define SVL_XNM_CENTRAL_DIFFERENCE 2
 typedef struct svl_xnm svl_xnm;
 typedef struct svl_xnm_opts {
     double  dt;
@@ -417,7 +447,8 @@ typedef struct svl_xnm_opts {
     int32_t cnvgtest;    /* Newton: 4 relative unbalanced force, 5 relative
                             displacement increment (Algorithm.cpp:122-188)        */
     double  cnvgtol;     /* Newton: convergence tolerance (0 = always newton_maxit) */
-    int32_t integrator;  /* SVL_XNM_EXTENDED_NEWMARK or SVL_XNM_NEWMARK              */
+    int32_t integrator;  /* SVL_XNM_EXTENDED_NEWMARK, SVL_XNM_NEWMARK or
+                            SVL_XNM_CENTRAL_DIFFERENCE                          */
     int32_t single_inner;/* 1: the inner MINRES iterations apply the element
                             operators in single precision; every restart forms
                             the true residual with the double operator and the

@@ -39,6 +39,8 @@ def lib():
                                           C.c_int, f64p, f64p, f64p, f64p, f64p, C.POINTER(C.c_int),
                                           C.POINTER(C.c_double)]
         L.oracle_xnewmark_matrices.argtypes = [vp, f64p, f64p, f64p, f64p]
+        L.oracle_cdpml_run.argtypes = [vp, vp, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int,
+                                       f64p, f64p, f64p, f64p, f64p, f64p, f64p, f64p, f64p]
         _lib = L
     return _lib
 
@@ -180,6 +182,29 @@ def xnewmark_run(model, loads, dt, nsteps, k_first=1, algo=0, maxit=50, cnvgtol=
                                    f(Ub), si, None if last_res is None else f(last_res))
     if st != 0:
         raise RuntimeError("oracle_xnewmark_run failed with status %d" % st)
+    return hist, U, V, A, Ub
+
+
+def cdpml_run(model, loads, dt, nsteps, k_first=1, ftol=1e-12, mtol=1e-12, history=True, timing=None):
+    """Explicit central difference on a model with PML layers (the staggered
+    scheme of CDPml in svl_oracle.cpp).  Returns (history of the total-dof
+    vector [nsteps, ntotal] or None, U, V, A, Ubar); on PML nodes the stress
+    dofs hold S at the half step after U's time.  timing['seconds'] receives
+    the step-loop wall time when `timing` is a dict."""
+    md = model.desc()
+    ld = loads.desc() if loads is not None else None
+    nt = model.ntotal
+    hist = np.zeros((nsteps, nt)) if history else None
+    U, V, A, Ub = (np.zeros(nt) for _ in range(4))
+    secs = np.zeros(1)
+    f = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))  # noqa: E731
+    st = lib().oracle_cdpml_run(C.addressof(md), C.addressof(ld) if ld is not None else None, dt, ftol, mtol,
+                                k_first, nsteps, _p(None), _p(None), _p(None), f(hist) if hist is not None else _p(None),
+                                f(U), f(V), f(A), f(Ub), f(secs))
+    if st != 0:
+        raise RuntimeError("oracle_cdpml_run failed with status %d" % st)
+    if timing is not None:
+        timing["seconds"] = float(secs[0])
     return hist, U, V, A, Ub
 
 

@@ -1639,6 +1639,378 @@ struct XNewmark {
     }
 };
 
+/* ---------------- Explicit central difference with PML layers -------------- */
+
+/* A scheme of this library, not a restatement: the reference's
+ * CentralDifference never applies the PML history matrix G
+ * (CentralDifference::GetPMLHistoryVector returns an empty vector,
+ * CentralDifference.cpp:114-120) and keeps the PML mass consistent with a
+ * negative stress block (PML3DHexa8.cpp:214-284), so M/dt^2 + C/2dt is sparse
+ * and indefinite there.  This scheme advances the same semi-discrete system
+ *   M x'' + C x' + K x + G xbar = F,   xbar = integral of x,
+ * with the element matrices M, C, K, G of PML2DQuad4 / PML3DHexa8
+ * (pml_matrices above, PML3DHexa8.cpp:214-712) and of the solid elements
+ * (lumped mass, internal force from the material state), explicitly:
+ *
+ * 1. Split of the PML element matrices.  Every PML matrix is a "mass-like"
+ *    part (the displacement-displacement and stress-stress blocks, which are
+ *    N_j N_k integrals) plus the displacement-stress coupling (dN N blocks).
+ *    The mass-like parts are row-sum lumped per node: diagonal on the
+ *    displacement dofs (Mu, Cu, Ku, Gu) and one ns x ns block per node on its
+ *    stress dofs (Ms, Cs, Ks, Gs; ns = 3 in 2D, 6 in 3D).  The couplings act
+ *    as element matrix products.  Solid elements contribute their lumped mass
+ *    (with the mass tolerance, as CentralDifference) to Mu and their internal
+ *    force to the displacement rows.
+ * 2. Staggered time levels.  Displacements u live at the integer steps,
+ *    the PML stress dofs S (the time integral of the stress, so S' is the
+ *    stress) at the half steps: at the start of step k the state holds u^k,
+ *    u^(k-1), S^(k+1/2), S^(k-1/2), ubar^k and Sbar^k.
+ * 3. Displacement rows at t_k (central differences; the increment form of
+ *    CentralDifference.cpp:206-221, diagonal solve):
+ *      (Mu/dt^2 + Cu/2dt) du = Fext(k) - Fint_solid(u^k)
+ *          - [C_uS sdot + K_uS smid + G_uS Sbar^k]_elements
+ *          - Ku u^k - Gu ubar^k + (Mu/dt^2 - Cu/2dt)(u^k - u^(k-1)),
+ *    sdot = (S^(k+1/2) - S^(k-1/2))/dt, smid = (S^(k+1/2) + S^(k-1/2))/2;
+ *    u^(k+1) = u^k + du on free dofs (restrained: 0, or the support-motion
+ *    increment).
+ * 4. ubar^(k+1) = ubar^k + dt (u^k + u^(k+1))/2, Sbar^(k+1) = Sbar^k + dt S^(k+1/2).
+ * 5. Stress rows at t_(k+1/2):
+ *      (Ms/dt^2 + Cs/2dt) dS = - [C_Su udot + K_Su umid + G_Su ubar^(k+1/2)]_elements
+ *          - Ks S^(k+1/2) - Gs Sbar^(k+1/2) + (Ms/dt^2 - Cs/2dt)(S^(k+1/2) - S^(k-1/2)),
+ *    udot = (u^(k+1) - u^k)/dt, umid = (u^(k+1) + u^k)/2,
+ *    ubar^(k+1/2) = (ubar^k + ubar^(k+1))/2, Sbar^(k+1/2) = Sbar^k + dt/2 S^(k+1/2);
+ *    S^(k+3/2) = S^(k+1/2) + dS (one ns x ns solve per PML node).
+ * Away from the PML (a = 1, b = c = d = 0) this is the leapfrog scheme of the
+ * velocity-stress system, stable for dt below the lumped-mass limit.  Element
+ * contributions are summed per dof in element order, unfiltered; the total-dof
+ * vector U holds u^k on displacement dofs and S^(k+1/2) on stress dofs, Up
+ * u^(k-1) and S^(k-1/2), Ubar ubar^k and Sbar^k.  V and A are the central
+ * difference formulas of CentralDifference.cpp:141-144 on every dof.
+ * Restrictions: constraints only with one master per constrained dof (the
+ * EQUAL ties of mergeDomain) and not on stress dofs, no dashpots, no
+ * domain-reduction loads, no restrained stress dofs, support motion only on displacement dofs, Rayleigh
+ * damping only mass-proportional on solid elements. */
+struct CDPml {
+    Sim s; double dt;
+    int ns = 0, pnd = 0;
+    std::vector<double> U, Up, Ubar, V, A;
+    std::vector<char> sdof;                 // [ntotal] 1 for a PML stress dof
+    std::vector<double> Mu, Cu, Ku, Gu;     // [ntotal] lumped diagonals of the displacement rows
+    std::vector<int> sfirst;                // [nnode] first total dof of the node's stress block, or -1
+    std::vector<int> snodes;                // nodes with a stress block
+    std::vector<double> Ms, Cs, Ks, Gs, Dinv;   // [nnode][ns*ns] (only rows of snodes used)
+    std::vector<double> Kff_inv;            // [nfree] 1 / (T^T d T) on displacement free dofs, 0 on stress ones
+    std::vector<std::vector<int>> edof;
+    bool pml(int e) const { return !s.m.epml.empty() && s.m.epml[e]; }
+
+    void pml_elem(int e, double* Me, double* Ce, double* Ke, double* Ge) const {
+        const Model& m = s.m;
+        double X[8 * 3];
+        for (int a = 0; a < m.nen; ++a)
+            for (int i = 0; i < m.ndim; ++i) X[a * m.ndim + i] = m.X[(size_t)m.conn[(size_t)e * m.nen + a] * m.ndim + i];
+        const double* p = s.mp(e);
+        pml_matrices(m.ndim, X, p[0], p[1], p[2], m.ndim == 2 ? m.thick[e] : 1.0,
+                     &m.pml_par[(size_t)e * (3 + 2 * m.ndim)], Me, Ce, Ke, Ge);
+    }
+
+    int init(const svl_model_desc* d, const svl_load_desc* l, double dt_, double mtol) {
+        if (!s.init(d, l)) return SVL_ERR_INVALID;
+        Model& m = s.m;
+        dt = dt_; s.mtol = mtol;
+        if (!m.lumped || !m.dp_eta.empty() || !s.L.drm_elem.empty()) return SVL_ERR_UNSUPPORTED;
+        pnd = m.ndim == 2 ? 5 : 9;
+        ns = pnd - m.ndim;
+        const int nt = m.ntotal;
+        for (int e = 0; e < m.nelem; ++e) {
+            const int t = s.mt(e);
+            const bool el = t == SVL_MAT_ELASTIC2DPLANESTRAIN || t == SVL_MAT_ELASTIC3DLINEAR;
+            if (!el && pml(e)) return SVL_ERR_UNSUPPORTED;
+            if (!m.ray.empty() && (m.ray[2 * e + 1] != 0.0 || (pml(e) && m.ray[2 * e] != 0.0))) return SVL_ERR_UNSUPPORTED;
+        }
+        U.assign(nt, 0); Up.assign(nt, 0); Ubar.assign(nt, 0); V.assign(nt, 0); A.assign(nt, 0);
+        sdof.assign(nt, 0);
+        sfirst.assign(m.nnode, -1);
+        edof.resize(m.nelem);
+        std::vector<char> pnode(m.nnode, 0);
+        for (int e = 0; e < m.nelem; ++e) {
+            const int k = pml(e) ? pnd : m.ndim;
+            for (int a = 0; a < m.nen; ++a) {
+                const int n = m.conn[(size_t)e * m.nen + a];
+                if (k > m.nndof[n]) return SVL_ERR_INVALID;
+                if (pml(e)) pnode[n] = 1;
+                for (int j = 0; j < k; ++j) edof[e].push_back(m.tdof_all[(size_t)n * m.dstride + j]);
+            }
+        }
+        for (int n = 0; n < m.nnode; ++n) {
+            if (!pnode[n]) continue;
+            snodes.push_back(n);
+            sfirst[n] = m.tdof_all[(size_t)n * m.dstride + m.ndim];
+            for (int j = 0; j < ns; ++j) {
+                const int t = m.tdof_all[(size_t)n * m.dstride + m.ndim + j];
+                if (t != sfirst[n] + j) return SVL_ERR_UNSUPPORTED;       // stress dofs consecutive
+                if (m.fdof_all[(size_t)n * m.dstride + m.ndim + j] < 0) return SVL_ERR_UNSUPPORTED;
+                sdof[t] = 1;
+            }
+        }
+        for (int d0 : s.L.smdof) if (sdof[d0]) return SVL_ERR_UNSUPPORTED;
+        // lumped mass-like parts, element order
+        Mu.assign(nt, 0); Cu.assign(nt, 0); Ku.assign(nt, 0); Gu.assign(nt, 0);
+        const size_t nb = (size_t)ns * ns;
+        Ms.assign((size_t)m.nnode * nb, 0); Cs = Ms; Ks = Ms; Gs = Ms; Dinv = Ms;
+        const int ncmax = m.nen * pnd;
+        std::vector<double> Xe[4];
+        for (auto& x : Xe) x.assign((size_t)ncmax * ncmax, 0.0);
+        const int ncs = m.nen * m.ndim;
+        std::vector<double> Me((size_t)ncs * ncs);
+        std::vector<double> Msolid(nt, 0.0);
+        for (int e = 0; e < m.nelem; ++e) {
+            if (!pml(e)) {
+                // lumped solid mass with the mass tolerance (Assembler.cpp:623-697)
+                s.element_M(e, Me.data(), true);
+                for (int i = 0; i < ncs; ++i) {
+                    const double v = Me[(size_t)i * ncs + i];
+                    if (std::fabs(v) > mtol) Mu[edof[e][i]] += v;
+                }
+                if (!m.ray.empty() && m.ray[2 * e] != 0.0)
+                    for (int i = 0; i < ncs; ++i) {
+                        const double v = m.ray[2 * e] * Me[(size_t)i * ncs + i];
+                        if (std::fabs(v) > s.ktol) Cu[edof[e][i]] += v;
+                    }
+                continue;
+            }
+            pml_elem(e, Xe[0].data(), Xe[1].data(), Xe[2].data(), m.ndim == 3 ? Xe[3].data() : nullptr);
+            const int nc = m.nen * pnd;
+            std::vector<double>* du[4] = {&Mu, &Cu, &Ku, &Gu};
+            std::vector<double>* bs[4] = {&Ms, &Cs, &Ks, &Gs};
+            for (int w = 0; w < (m.ndim == 3 ? 4 : 3); ++w) {
+                const double* X = Xe[w].data();
+                for (int j = 0; j < m.nen; ++j) {
+                    const int n = m.conn[(size_t)e * m.nen + j];
+                    for (int c = 0; c < m.ndim; ++c) {
+                        double v = 0.0;
+                        for (int k = 0; k < m.nen; ++k) v += X[(size_t)(j * pnd + c) * nc + k * pnd + c];
+                        (*du[w])[edof[e][j * pnd + c]] += v;
+                    }
+                    for (int r = 0; r < ns; ++r)
+                        for (int c = 0; c < ns; ++c) {
+                            double v = 0.0;
+                            for (int k = 0; k < m.nen; ++k) v += X[(size_t)(j * pnd + m.ndim + r) * nc + k * pnd + m.ndim + c];
+                            (*bs[w])[(size_t)n * nb + r * ns + c] += v;
+                        }
+                }
+            }
+        }
+        if (!m.nodemass.empty())
+            for (int t = 0; t < nt; ++t) if (std::fabs(m.nodemass[t]) > mtol) Mu[t] += m.nodemass[t];
+        // T^T (Mu/dt^2 + Cu/2dt) T, diagonal when every constrained dof has one
+        // master (the EQUAL constraints of mergeDomain); stress dofs are free and
+        // unconstrained, solved per node below
+        {
+            std::vector<double> kf(m.nfree, 0.0);
+            std::vector<int> ncol(nt, 0);
+            for (int t = 0; t < nt; ++t) {
+                if (sdof[t]) continue;
+                ncol[t] = s.Tptr[t + 1] - s.Tptr[t];
+                if (ncol[t] > 1) return SVL_ERR_UNSUPPORTED;
+                const double d = 1.0 / dt / dt * Mu[t] + 1.0 / 2.0 / dt * Cu[t];
+                for (int i = s.Tptr[t]; i < s.Tptr[t + 1]; ++i) kf[s.Tcol[i]] += s.Tval[i] * d * s.Tval[i];
+            }
+            Kff_inv.assign(m.nfree, 0.0);
+            std::vector<char> sfree(m.nfree, 0);
+            for (int t = 0; t < nt; ++t)
+                if (sdof[t]) for (int i = s.Tptr[t]; i < s.Tptr[t + 1]; ++i) sfree[s.Tcol[i]] = 1;
+            for (int f = 0; f < m.nfree; ++f) {
+                if (sfree[f]) continue;
+                if (!(kf[f] > 0.0)) return SVL_ERR_INVALID;
+                Kff_inv[f] = 1.0 / kf[f];
+            }
+        }
+        // inverse of Ms/dt^2 + Cs/2dt per node (Gauss-Jordan with partial pivoting)
+        for (int n : snodes) {
+            double Aa[36], B[36];
+            for (size_t i = 0; i < nb; ++i) {
+                Aa[i] = Ms[(size_t)n * nb + i] / dt / dt + Cs[(size_t)n * nb + i] / 2.0 / dt;
+                B[i] = 0.0;
+            }
+            for (int i = 0; i < ns; ++i) B[i * ns + i] = 1.0;
+            for (int c = 0; c < ns; ++c) {
+                int p = c;
+                for (int r = c + 1; r < ns; ++r) if (std::fabs(Aa[r * ns + c]) > std::fabs(Aa[p * ns + c])) p = r;
+                if (!(std::fabs(Aa[p * ns + c]) > 0.0)) return SVL_ERR_INVALID;
+                if (p != c) for (int j = 0; j < ns; ++j) { std::swap(Aa[p * ns + j], Aa[c * ns + j]); std::swap(B[p * ns + j], B[c * ns + j]); }
+                const double piv = Aa[c * ns + c];
+                for (int j = 0; j < ns; ++j) { Aa[c * ns + j] /= piv; B[c * ns + j] /= piv; }
+                for (int r = 0; r < ns; ++r) {
+                    if (r == c) continue;
+                    const double f = Aa[r * ns + c];
+                    if (f == 0.0) continue;
+                    for (int j = 0; j < ns; ++j) { Aa[r * ns + j] -= f * Aa[c * ns + j]; B[r * ns + j] -= f * B[c * ns + j]; }
+                }
+            }
+            for (size_t i = 0; i < nb; ++i) Dinv[(size_t)n * nb + i] = B[i];
+        }
+        return SVL_OK;
+    }
+    void set_initial(const double* U0, const double* V0, const double* A0) {
+        for (int t = 0; t < s.m.ntotal; ++t) {
+            const double u = U0 ? U0[t] : 0.0, v = V0 ? V0[t] : 0.0, a = A0 ? A0[t] : 0.0;
+            U[t] = u; V[t] = v; A[t] = a;
+            Up[t] = u - dt * v + dt * dt / 2.0 * a;
+            Ubar[t] = 0.0;
+        }
+        for (int e = 0; e < s.m.nelem; ++e) if (!pml(e)) s.element_update(e, U);
+        s.commit_all();
+    }
+    // u-rows (which = 0) or S-rows (which = 1) of X_e w_e summed over the three
+    // (2D: two) coupling matrices C, K, G with the inputs in0, in1, in2
+    // (entries of the other class are zero), element order, into F.
+    void couple(int which, const std::vector<double>& in0, const std::vector<double>& in1,
+                const std::vector<double>& in2, std::vector<double>& F) const {
+        const Model& m = s.m;
+        const int nc = m.nen * pnd;
+        std::vector<double> Ce((size_t)nc * nc), Ke(Ce.size()), Ge(Ce.size());
+        std::vector<double> fe_all;
+        std::vector<int> pe;
+        for (int e = 0; e < m.nelem; ++e) if (pml(e)) pe.push_back(e);
+        fe_all.assign(pe.size() * nc, 0.0);
+        #pragma omp parallel for schedule(dynamic, 16) firstprivate(Ce, Ke, Ge)
+        for (long ii = 0; ii < (long)pe.size(); ++ii) {
+            const int e = pe[ii];
+            pml_elem(e, nullptr, Ce.data(), Ke.data(), m.ndim == 3 ? Ge.data() : nullptr);
+            double* fe = &fe_all[(size_t)ii * nc];
+            const std::vector<double>* ins[3] = {&in0, &in1, &in2};
+            const double* mats[3] = {Ce.data(), Ke.data(), Ge.data()};
+            for (int w = 0; w < (m.ndim == 3 ? 3 : 2); ++w) {
+                double x[72];
+                for (int i = 0; i < nc; ++i) {
+                    const int t = edof[e][i];
+                    const bool is_s = (i % pnd) >= m.ndim;
+                    x[i] = (which == 0) == is_s ? (*ins[w])[t] : 0.0;
+                }
+                for (int r = 0; r < nc; ++r) {
+                    if (((r % pnd) >= m.ndim) != (which == 1)) continue;
+                    double acc = 0.0;
+                    for (int c = 0; c < nc; ++c) acc += mats[w][(size_t)r * nc + c] * x[c];
+                    fe[r] += acc;
+                }
+            }
+        }
+        for (size_t ii = 0; ii < pe.size(); ++ii) {
+            const int e = pe[ii];
+            for (int r = 0; r < nc; ++r)
+                if (((r % pnd) >= m.ndim) == (which == 1)) F[edof[e][r]] += fe_all[ii * nc + r];
+        }
+    }
+    void step(int k) {
+        const Model& m = s.m;
+        const int nt = m.ntotal;
+        const size_t nb = (size_t)ns * ns;
+        const int ncs = m.nen * m.ndim, nc = m.nen * pnd;
+        std::vector<double> Fext, SM, sdot(nt, 0.0), smid(nt, 0.0), dU(nt, 0.0), Us(nt), Ubn(nt), Ubh(nt);
+        // -- displacement rows ------------------------------------------------
+        for (int t = 0; t < nt; ++t)
+            if (sdof[t]) { sdot[t] = (U[t] - Up[t]) / dt; smid[t] = (U[t] + Up[t]) / 2.0; }
+        // element forces on the displacement rows: solid internal force from the
+        // material state, PML couplings C_uS sdot + K_uS smid + G_uS Sbar; summed in
+        // element order with the force filter (Assembler.cpp:240-269)
+        std::vector<double> Fc(nt, 0.0), fe_all((size_t)m.nelem * nc, 0.0);
+        {
+            std::vector<double> Ce((size_t)nc * nc), Ke(Ce.size()), Ge(Ce.size());
+            #pragma omp parallel for schedule(dynamic, 16) firstprivate(Ce, Ke, Ge)
+            for (int e = 0; e < m.nelem; ++e) {
+                double* fe = &fe_all[(size_t)e * nc];
+                if (!pml(e)) { s.element_fint(e, fe); continue; }
+                pml_elem(e, nullptr, Ce.data(), Ke.data(), m.ndim == 3 ? Ge.data() : nullptr);
+                double x0[72], x1[72], x2[72];
+                for (int i = 0; i < nc; ++i) {
+                    const int t = edof[e][i];
+                    const bool is_s = (i % pnd) >= m.ndim;
+                    x0[i] = is_s ? sdot[t] : 0.0; x1[i] = is_s ? smid[t] : 0.0; x2[i] = is_s ? Ubar[t] : 0.0;
+                }
+                for (int r = 0; r < nc; ++r) {
+                    if ((r % pnd) >= m.ndim) continue;
+                    double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+                    for (int c = 0; c < nc; ++c) {
+                        a0 += Ce[(size_t)r * nc + c] * x0[c];
+                        a1 += Ke[(size_t)r * nc + c] * x1[c];
+                        if (m.ndim == 3) a2 += Ge[(size_t)r * nc + c] * x2[c];
+                    }
+                    fe[r] = a0 + a1 + a2;
+                }
+            }
+        }
+        for (int e = 0; e < m.nelem; ++e) {
+            const double* fe = &fe_all[(size_t)e * nc];
+            const int n_e = pml(e) ? nc : ncs;
+            for (int r = 0; r < n_e; ++r) {
+                if (pml(e) && (r % pnd) >= m.ndim) continue;
+                if (std::fabs(fe[r]) > s.ftol) Fc[edof[e][r]] += fe[r];
+            }
+        }
+        s.fext(k, Fext);
+        s.support_increment(k, SM);
+        // the increment form of the plain central difference (CentralDifference.cpp:206-221)
+        // with the lumped PML terms, reduced to the free dofs by T^T, the diagonal
+        // (1/d) b solve, and expanded by T
+        std::vector<double> Rt(nt, 0.0), Feff, du_f, dUt;
+        for (int t = 0; t < nt; ++t) {
+            if (sdof[t]) continue;
+            const double c = 1.0 / dt / dt * Mu[t] - 1.0 / 2.0 / dt * Cu[t];
+            Rt[t] = ((Fext[t] + 0.0 - Fc[t]) - Ku[t] * U[t] - Gu[t] * Ubar[t]) + c * (U[t] - Up[t]);
+        }
+        s.TT_apply(Rt, Feff);
+        du_f.assign(m.nfree, 0.0);
+        for (int f = 0; f < m.nfree; ++f) du_f[f] = Kff_inv[f] * Feff[f];
+        s.T_apply(du_f, dUt);
+        for (int t = 0; t < nt; ++t) {
+            if (sdof[t]) continue;
+            const double du = dUt[t];
+            Us[t] = U[t] + du;                 // strain without the support-motion increment (Algorithm.cpp:23)
+            dU[t] = du + SM[t];
+            const double un = U[t] + dU[t];
+            Ubn[t] = Ubar[t] + dt * (U[t] + un) / 2.0;
+            Ubh[t] = (Ubar[t] + Ubn[t]) / 2.0;
+        }
+        for (int e = 0; e < m.nelem; ++e) if (!pml(e)) s.element_update(e, Us);
+        // -- stress rows --------------------------------------------------------
+        std::vector<double> udot(nt, 0.0), umid(nt, 0.0), ubh(nt, 0.0), Fs(nt, 0.0);
+        for (int t = 0; t < nt; ++t)
+            if (!sdof[t]) {
+                const double un = U[t] + dU[t];
+                udot[t] = (un - U[t]) / dt; umid[t] = (un + U[t]) / 2.0; ubh[t] = Ubh[t];
+            }
+        couple(1, udot, umid, ubh, Fs);
+        for (int n : snodes) {
+            const int t0 = sfirst[n];
+            double R[6];
+            for (int r = 0; r < ns; ++r) {
+                double v = -Fs[t0 + r];
+                for (int c = 0; c < ns; ++c) {
+                    const size_t i = (size_t)n * nb + r * ns + c;
+                    const double sc = U[t0 + c], sp = Up[t0 + c], sbh = Ubar[t0 + c] + dt / 2.0 * sc;
+                    v += -Ks[i] * sc - Gs[i] * sbh + (Ms[i] / dt / dt - Cs[i] / 2.0 / dt) * (sc - sp);
+                }
+                R[r] = v;
+            }
+            for (int r = 0; r < ns; ++r) {
+                double v = 0.0;
+                for (int c = 0; c < ns; ++c) v += Dinv[(size_t)n * nb + r * ns + c] * R[c];
+                dU[t0 + r] = v;
+                Ubn[t0 + r] = Ubar[t0 + r] + dt * U[t0 + r];
+            }
+        }
+        // -- new state (CentralDifference.cpp:138-148 on every dof) -------------
+        for (int t = 0; t < nt; ++t) {
+            V[t] = 1.0 / 2.0 / dt * (U[t] + dU[t] - Up[t]);
+            A[t] = 1.0 / dt / dt * (dU[t] - U[t] + Up[t]);
+            Up[t] = U[t];
+            U[t] += dU[t];
+            Ubar[t] = Ubn[t];
+        }
+        s.commit_all();
+    }
+};
+
 /* ---------------- C ABI of the oracle ------------------------------------ */
 extern "C" {
 
@@ -1662,6 +2034,33 @@ int oracle_cd_run(const svl_model_desc* model, const svl_load_desc* loads, doubl
     if (U_out) std::memcpy(U_out, cd.U.data(), sizeof(double) * nt);
     if (V_out) std::memcpy(V_out, cd.V.data(), sizeof(double) * nt);
     if (A_out) std::memcpy(A_out, cd.A.data(), sizeof(double) * nt);
+    return 0;
+}
+
+/* Explicit central difference with PML layers (the staggered scheme of
+ * CDPml above).  hist_U [nsteps][ntotal] or NULL; U/V/A/Ubar out [ntotal] or
+ * NULL.  Returns an SVL_* status (UNSUPPORTED for models outside its scope). */
+int oracle_cdpml_run(const svl_model_desc* model, const svl_load_desc* loads, double dt, double ftol, double mtol,
+                     int k_first, int nsteps, const double* U0, const double* V0, const double* A0,
+                     double* hist_U, double* U_out, double* V_out, double* A_out, double* Ubar_out,
+                     double* step_seconds) {
+    CDPml c;
+    c.s.ftol = ftol;
+    const int st = c.init(model, loads, dt, mtol);
+    if (st) return st;
+    c.s.ftol = ftol;
+    c.set_initial(U0, V0, A0);
+    const int nt = c.s.m.ntotal;
+    const auto t0 = std::chrono::steady_clock::now();
+    for (int i = 0; i < nsteps; ++i) {
+        c.step(k_first + i);
+        if (hist_U) std::memcpy(hist_U + (size_t)i * nt, c.U.data(), sizeof(double) * nt);
+    }
+    if (step_seconds) step_seconds[0] = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    if (U_out) std::memcpy(U_out, c.U.data(), sizeof(double) * nt);
+    if (V_out) std::memcpy(V_out, c.V.data(), sizeof(double) * nt);
+    if (A_out) std::memcpy(A_out, c.A.data(), sizeof(double) * nt);
+    if (Ubar_out) std::memcpy(Ubar_out, c.Ubar.data(), sizeof(double) * nt);
     return 0;
 }
 

@@ -102,6 +102,7 @@ class XnmOpts(C.Structure):
 
 SVL_XNM_EXTENDED_NEWMARK = 0
 SVL_XNM_NEWMARK = 1
+SVL_XNM_CENTRAL_DIFFERENCE = 2
 
 
 class NnTrainOpts(C.Structure):

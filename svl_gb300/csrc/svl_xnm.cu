@@ -829,6 +829,138 @@ __global__ void k_xtake(int nel, int nc, int i, const double* y, double* d) {
     if (e < nel) d[(size_t)e * nc + i] = y[(size_t)e * nc + i];
 }
 
+// ---- explicit central difference with PML layers (integrator
+// SVL_XNM_CENTRAL_DIFFERENCE).  A scheme of this library: the reference's
+// CentralDifference applies no PML history and keeps the PML mass consistent
+// and indefinite (CentralDifference.cpp:114-120, PML3DHexa8.cpp:214-284).
+// Displacements live at the integer steps, the PML stress dofs S at the half
+// steps; the N N blocks of the PML element matrices are row-sum lumped per
+// node (a diagonal on displacement dofs, an ns x ns block on a node's stress
+// dofs) and the displacement-stress couplings act through the element action
+// (svl_pml.cu) on vectors whose other class of dofs is zero.
+
+// inputs of the displacement rows: on stress dofs sdot = (S - Sp)/dt,
+// smid = (S + Sp)/2 and Sbar; zero on displacement dofs
+__global__ void k_cdp_sin(int n, const int8_t* __restrict__ sdof, const double* __restrict__ U,
+                          const double* __restrict__ Up, const double* __restrict__ Ub, double dt,
+                          double* __restrict__ x0, double* __restrict__ x1, double* __restrict__ x2) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    if (sdof[t]) {
+        x0[t] = (U[t] - Up[t]) / dt;
+        x1[t] = (U[t] + Up[t]) / 2.0;
+        x2[t] = Ub[t];
+    } else {
+        x0[t] = 0.0; x1[t] = 0.0; x2[t] = 0.0;
+    }
+}
+
+// displacement rows: R = (y - Ku u - Gu ubar) + (Mu/dt^2 - Cu/2dt)(u - up),
+// y = Fext(k) - (solid internal force + couplings): the increment form of
+// the plain central difference (CentralDifference.cpp:206-221) with the
+// lumped PML terms; zero on stress dofs
+__global__ void k_cdp_r(int n, const int8_t* __restrict__ sdof, const double* __restrict__ y,
+                        const double* __restrict__ Mu, const double* __restrict__ Cu, const double* __restrict__ Ku,
+                        const double* __restrict__ Gu, double dt, const double* __restrict__ U,
+                        const double* __restrict__ Up, const double* __restrict__ Ub, double* __restrict__ R) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    if (sdof[t]) { R[t] = 0.0; return; }
+    const double c = 1.0 / dt / dt * Mu[t] - 1.0 / 2.0 / dt * Cu[t];
+    R[t] = (y[t] - Ku[t] * U[t] - Gu[t] * Ub[t]) + c * (U[t] - Up[t]);
+}
+
+// the diagonal solve of T^T (Mu/dt^2 + Cu/2dt) T as (1/d) b (0 on stress dofs)
+__global__ void k_cdp_solve(int nf, const double* __restrict__ kinv, const double* __restrict__ b, double* __restrict__ x) {
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= nf) return;
+    x[f] = kinv[f] * b[f];
+}
+
+// displacement increment dUt = T du (+ the support-motion increment), the
+// trapezoid ubar, the solid strain displacement U + T du, and the inputs of
+// the stress rows (udot, umid, ubar at the half step; zero on stress dofs)
+__global__ void k_cdp_u(int n, const int8_t* __restrict__ sdof, const double* __restrict__ dUt,
+                        const double* __restrict__ sm, double dt, const double* __restrict__ U,
+                        const double* __restrict__ Ub, double* __restrict__ dU, double* __restrict__ Us,
+                        double* __restrict__ Ubn, double* __restrict__ x0, double* __restrict__ x1,
+                        double* __restrict__ x2) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    if (sdof[t]) { x0[t] = 0.0; x1[t] = 0.0; x2[t] = 0.0; return; }
+    const double u = U[t], du = dUt[t];
+    Us[t] = u + du;                                  // strain without the support-motion increment
+    const double D = du + (sm ? sm[t] : 0.0);
+    dU[t] = D;
+    const double un = u + D;
+    const double ubn = Ub[t] + dt * (u + un) / 2.0;
+    Ubn[t] = ubn;
+    x0[t] = (un - u) / dt;
+    x1[t] = (un + u) / 2.0;
+    x2[t] = (Ub[t] + ubn) / 2.0;
+}
+
+// stress rows of PML node i: (Ms/dt^2 + Cs/2dt) dS = -Fs - Ks S - Gs Sbar_half
+// + (Ms/dt^2 - Cs/2dt)(S - Sp), solved with the stored inverse
+template <int NS>
+__global__ void k_cdp_s(int nsn, const int32_t* __restrict__ sfirst, const double* __restrict__ Fs,
+                        const double* __restrict__ Ms, const double* __restrict__ Cs, const double* __restrict__ Ks,
+                        const double* __restrict__ Gs, const double* __restrict__ Dinv, const double* __restrict__ U,
+                        const double* __restrict__ Up, const double* __restrict__ Ub, double dt,
+                        double* __restrict__ dU, double* __restrict__ Ubn) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nsn) return;
+    const int t0 = sfirst[i];
+    const size_t b = (size_t)i * NS * NS;
+    double sc[NS], sp[NS], sbh[NS], R[NS];
+#pragma unroll
+    for (int c = 0; c < NS; ++c) {
+        sc[c] = U[t0 + c]; sp[c] = Up[t0 + c];
+        sbh[c] = Ub[t0 + c] + dt / 2.0 * sc[c];
+    }
+#pragma unroll
+    for (int r = 0; r < NS; ++r) {
+        double v = -Fs[t0 + r];
+#pragma unroll
+        for (int c = 0; c < NS; ++c) {
+            const size_t k = b + r * NS + c;
+            v += -Ks[k] * sc[c] - Gs[k] * sbh[c] + (Ms[k] / dt / dt - Cs[k] / 2.0 / dt) * (sc[c] - sp[c]);
+        }
+        R[r] = v;
+    }
+#pragma unroll
+    for (int r = 0; r < NS; ++r) {
+        double v = 0.0;
+#pragma unroll
+        for (int c = 0; c < NS; ++c) v += Dinv[b + r * NS + c] * R[c];
+        dU[t0 + r] = v;
+        Ubn[t0 + r] = Ub[t0 + r] + dt * sc[r];
+    }
+}
+
+// CentralDifference::ComputeNewStep's update on every dof (:138-148)
+__global__ void k_cdp_update(int n, double* __restrict__ U, double* __restrict__ Up, double* __restrict__ V,
+                             double* __restrict__ A, double* __restrict__ Ub, const double* __restrict__ dU,
+                             const double* __restrict__ Ubn, double dt, int* bad) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const double u = U[t], d = dU[t], up = Up[t];
+    V[t] = 1.0 / 2.0 / dt * (u + d - up);
+    A[t] = 1.0 / dt / dt * (d - u + up);
+    Up[t] = u;
+    const double un = u + d;
+    U[t] = un;
+    Ub[t] = Ubn[t];
+    if (!isfinite(un)) atomicOr(bad, 1);
+}
+
+// Up = U - dt V + dt^2/2 A (CentralDifference.cpp:61)
+__global__ void k_cdp_init(int n, const double* U, const double* V, const double* A, double dt, double* Up) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    Up[t] = U[t] - dt * V[t] + dt * dt / 2.0 * A[t];
+}
+
 }  // namespace
 
 struct svl_xnm {
@@ -872,6 +1004,15 @@ struct svl_xnm {
     double* Ui = nullptr;                    // U + T dU: the PML elements' displacement
     float *pt_f = nullptr, *fe_f = nullptr;  // single-precision operator input and element vectors
     bool newmark = false;                    // NewmarkBeta instead of ExtendedNewmarkBeta
+    bool explicit_cd = false;                // explicit central difference with PML (staggered scheme)
+    // explicit scheme: lumped diagonals of the displacement rows, stress dofs,
+    // per-PML-node stress blocks, previous state and the half-step integrals
+    int8_t* cd_sdof = nullptr;
+    double *cd_Mu = nullptr, *cd_Cu = nullptr, *cd_Ku = nullptr, *cd_Gu = nullptr;
+    int cd_nsn = 0;
+    int32_t* cd_sfirst = nullptr;
+    double *cd_Ms = nullptr, *cd_Cs = nullptr, *cd_Ks = nullptr, *cd_Gs = nullptr, *cd_Dinv = nullptr;
+    double *cd_Up = nullptr, *cd_Ubn = nullptr, *cd_kinv = nullptr;
     // free-dof vectors
     double *b = nullptr, *x = nullptr, *dUf = nullptr, *r1 = nullptr, *r2 = nullptr, *yv = nullptr, *v = nullptr;
     double *w = nullptr, *w1 = nullptr, *w2 = nullptr, *dinv = nullptr, *tmp = nullptr;
@@ -1237,6 +1378,224 @@ int x_step(svl_xnm* X, int k) {
     return SVL_OK;
 }
 
+// Explicit scheme tables: row-sum lumped N N blocks of the PML element
+// matrices M, C, K, G (PML2DQuad4.cpp:233-470, PML3DHexa8.cpp:214-712: each
+// block is a stretching combination s times rho N N on the displacement dofs
+// and times -compliance N N on the stress dofs, so its row sum at node j is
+// the Gauss sum of s N_j w |J|), the solid elements' lumped mass with the
+// mass tolerance, the nodal masses, and per PML node the inverse of
+// Ms/dt^2 + Cs/2dt.  Element order throughout.
+int cdp_setup(svl_xnm* X, const std::vector<int>& sol, const std::vector<int>& pml) {
+    const HostModel& m = X->m;
+    const int nd = m.ndim, nen = m.nen, pnd = m.pml_ndof(), ns = pnd - nd, npar = 3 + 2 * nd;
+    const double dt = X->opts.dt;
+    const int nt = m.ntotal;
+    std::vector<int8_t> sdof(nt, 0);
+    std::vector<int32_t> snode_of(m.nnode, -1), sfirst;
+    std::vector<char> pnode(m.nnode, 0);
+    for (int e : pml)
+        for (int a = 0; a < nen; ++a) pnode[m.conn[(size_t)e * nen + a]] = 1;
+    for (int n = 0; n < m.nnode; ++n) {
+        if (!pnode[n]) continue;
+        const int t0 = m.tdof_all[(size_t)n * m.dstride + nd];
+        for (int j = 0; j < ns; ++j) {
+            const int t = m.tdof_all[(size_t)n * m.dstride + nd + j];
+            if (t != t0 + j) { set_error("explicit PML: the stress dofs of node %d are not consecutive", n); return SVL_ERR_UNSUPPORTED; }
+            if (m.fdof_all[(size_t)n * m.dstride + nd + j] < 0) {
+                set_error("explicit PML: node %d has a restrained or constrained stress dof", n); return SVL_ERR_UNSUPPORTED;
+            }
+            sdof[t] = 1;
+        }
+        snode_of[n] = (int32_t)sfirst.size();
+        sfirst.push_back(t0);
+    }
+    for (int t = 0; t < nt; ++t)
+        if (sdof[t] && X->lt.sm_ptr[t + 1] > X->lt.sm_ptr[t]) {
+            set_error("explicit PML: support motion on a stress dof (total dof %d)", t); return SVL_ERR_UNSUPPORTED;
+        }
+    const int nsn = (int)sfirst.size();
+    const size_t nb = (size_t)ns * ns;
+    std::vector<double> Mu(nt, 0.0), Cu(nt, 0.0), Ku(nt, 0.0), Gu(nt, 0.0);
+    std::vector<double> Bl[4];
+    for (auto& v : Bl) v.assign((size_t)nsn * nb, 0.0);
+    std::vector<int> sidx_of(m.nelem, -1), pidx_of(m.nelem, -1);
+    for (size_t i = 0; i < sol.size(); ++i) sidx_of[sol[i]] = (int)i;
+    for (size_t i = 0; i < pml.size(); ++i) pidx_of[pml[i]] = (int)i;
+    std::vector<double> ml;
+    element_lumped_masses(m, ml);                 // [(e nen + a) nd + j]
+    for (int e = 0; e < m.nelem; ++e) {
+        if (sidx_of[e] >= 0) {
+            const double am = m.ray.empty() ? 0.0 : m.ray[2 * (size_t)e];
+            for (int a = 0; a < nen; ++a)
+                for (int j = 0; j < nd; ++j) {
+                    const double v = ml[((size_t)e * nen + a) * nd + j];
+                    const int t = m.tdof_all[(size_t)m.conn[(size_t)e * nen + a] * m.dstride + j];
+                    if (std::fabs(v) > X->opts.mtol) Mu[t] += v;
+                    if (am != 0.0 && std::fabs(am * v) > 1e-12) Cu[t] += am * v;
+                }
+            continue;
+        }
+        const double* pr = m.param(e);
+        const double E = pr[0], nu = pr[1], rho = pr[2];
+        const double mu = E / 2.0 / (1 + nu), lambda = E * nu / (1.0 + nu) / (1.0 - 2.0 * nu);
+        const double* par = &m.pml_par[(size_t)e * npar];
+        const double pm = par[0], L = par[1], R = par[2];
+        const double Vp = std::sqrt((lambda + 2.0 * mu) / rho);
+        const double a0 = (pm + 1.0) * (L / 10.0) / 2.0 / L * std::log(1.0 / R);
+        const double b0 = (pm + 1.0) * Vp / 2.0 / L * std::log(1.0 / R);
+        for (int q = 0; q < m.ngp; ++q) {
+            double dNx[8][3], N[8];
+            const double det = gp_geometry(m, e, q, dNx, N);
+            const double f = gp_factor(m, e, det);
+            double xg[3] = {0, 0, 0};
+            for (int a = 0; a < nen; ++a)
+                for (int i = 0; i < nd; ++i) xg[i] += N[a] * m.X[(size_t)m.conn[(size_t)e * nen + a] * nd + i];
+            double as[3] = {1, 1, 1}, bs[3] = {0, 0, 0};
+            for (int i = 0; i < nd; ++i) {
+                const double r = std::pow((xg[i] - par[3 + i]) * par[3 + nd + i] / L, pm);
+                as[i] = 1.0 + a0 * r;
+                bs[i] = b0 * r;
+            }
+            double sc[4];
+            if (nd == 2) {
+                sc[0] = as[0] * as[1]; sc[1] = as[0] * bs[1] + as[1] * bs[0]; sc[2] = bs[0] * bs[1]; sc[3] = 0.0;
+            } else {
+                sc[0] = as[0] * as[1] * as[2];
+                sc[1] = as[0] * as[1] * bs[2] + as[0] * bs[1] * as[2] + bs[0] * as[1] * as[2];
+                sc[2] = as[0] * bs[1] * bs[2] + bs[0] * bs[1] * as[2] + bs[0] * as[1] * bs[2];
+                sc[3] = bs[0] * bs[1] * bs[2];
+            }
+            std::vector<double>* du[4] = {&Mu, &Cu, &Ku, &Gu};
+            for (int w = 0; w < 4; ++w) {
+                const double sw = sc[w];
+                if (sw == 0.0) continue;
+                for (int j = 0; j < nen; ++j) {
+                    const int n = m.conn[(size_t)e * nen + j];
+                    const double Nf = N[j] * f;
+                    for (int c = 0; c < nd; ++c) (*du[w])[m.tdof_all[(size_t)n * m.dstride + c]] += rho * sw * Nf;
+                    double* B = &Bl[w][(size_t)snode_of[n] * nb];
+                    if (nd == 2) {
+                        const double k2 = sw * (lambda + 2.0 * mu) / 4.0 / mu / (lambda + mu);
+                        const double l2 = sw * lambda / 4.0 / mu / (lambda + mu);
+                        B[0 * 3 + 0] += -k2 * Nf; B[1 * 3 + 1] += -k2 * Nf;
+                        B[0 * 3 + 1] += l2 * Nf; B[1 * 3 + 0] += l2 * Nf;
+                        B[2 * 3 + 2] += -sw / mu * Nf;
+                    } else {
+                        const double kap = sw * (lambda + mu) / mu / (3.0 * lambda + 2.0 * mu);
+                        const double lam = sw * lambda / 2.0 / mu / (3.0 * lambda + 2.0 * mu);
+                        for (int r = 0; r < 3; ++r)
+                            for (int c = 0; c < 3; ++c) B[r * 6 + c] += (r == c ? -kap : lam) * Nf;
+                        for (int r = 3; r < 6; ++r) B[r * 6 + r] += -sw / mu * Nf;
+                    }
+                }
+            }
+        }
+    }
+    if (!m.nodemass.empty())
+        for (int t = 0; t < nt; ++t) if (std::fabs(m.nodemass[t]) > X->opts.mtol) Mu[t] += m.nodemass[t];
+    std::vector<int32_t> Tp, Tc;
+    std::vector<double> Tv;
+    build_total_to_free(m, Tp, Tc, Tv);
+    // T^T (Mu/dt^2 + Cu/2dt) T: diagonal when every constrained displacement
+    // dof has one master (the EQUAL ties of mergeDomain)
+    std::vector<double> kf(std::max(m.nfree, 1), 0.0), kinv(std::max(m.nfree, 1), 0.0);
+    std::vector<char> sfree(std::max(m.nfree, 1), 0);
+    for (int t = 0; t < nt; ++t) {
+        if (sdof[t]) { for (int i = Tp[t]; i < Tp[t + 1]; ++i) sfree[Tc[i]] = 1; continue; }
+        if (Tp[t + 1] - Tp[t] > 1) {
+            set_error("explicit PML: total dof %d is constrained to more than one master (no diagonal solve)", t);
+            return SVL_ERR_UNSUPPORTED;
+        }
+        const double d = 1.0 / dt / dt * Mu[t] + 1.0 / 2.0 / dt * Cu[t];
+        for (int i = Tp[t]; i < Tp[t + 1]; ++i) kf[Tc[i]] += Tv[i] * d * Tv[i];
+    }
+    for (int f = 0; f < m.nfree; ++f) {
+        if (sfree[f]) continue;
+        if (!(kf[f] > 0.0)) { set_error("explicit PML: free displacement dof %d has no mass", f); return SVL_ERR_INVALID; }
+        kinv[f] = 1.0 / kf[f];
+    }
+    std::vector<double> Dinv((size_t)nsn * nb, 0.0);
+    for (int i = 0; i < nsn; ++i) {
+        double A_[36], B[36];
+        for (size_t k = 0; k < nb; ++k) { A_[k] = Bl[0][(size_t)i * nb + k] / dt / dt + Bl[1][(size_t)i * nb + k] / 2.0 / dt; B[k] = 0.0; }
+        for (int r = 0; r < ns; ++r) B[r * ns + r] = 1.0;
+        for (int c = 0; c < ns; ++c) {                   // Gauss-Jordan, partial pivoting
+            int pv = c;
+            for (int r = c + 1; r < ns; ++r) if (std::fabs(A_[r * ns + c]) > std::fabs(A_[pv * ns + c])) pv = r;
+            if (!(std::fabs(A_[pv * ns + c]) > 0.0)) { set_error("explicit PML: singular stress block at PML node %d", i); return SVL_ERR_INVALID; }
+            if (pv != c) for (int j = 0; j < ns; ++j) { std::swap(A_[pv * ns + j], A_[c * ns + j]); std::swap(B[pv * ns + j], B[c * ns + j]); }
+            const double piv = A_[c * ns + c];
+            for (int j = 0; j < ns; ++j) { A_[c * ns + j] /= piv; B[c * ns + j] /= piv; }
+            for (int r = 0; r < ns; ++r) {
+                if (r == c) continue;
+                const double fr = A_[r * ns + c];
+                if (fr == 0.0) continue;
+                for (int j = 0; j < ns; ++j) { A_[r * ns + j] -= fr * A_[c * ns + j]; B[r * ns + j] -= fr * B[c * ns + j]; }
+            }
+        }
+        for (size_t k = 0; k < nb; ++k) Dinv[(size_t)i * nb + k] = B[k];
+    }
+    X->cd_nsn = nsn;
+    XTRY(X->upload(sdof, &X->cd_sdof));
+    XTRY(X->upload(Mu, &X->cd_Mu)); XTRY(X->upload(Cu, &X->cd_Cu)); XTRY(X->upload(Ku, &X->cd_Ku)); XTRY(X->upload(Gu, &X->cd_Gu));
+    XTRY(X->upload(sfirst, &X->cd_sfirst));
+    XTRY(X->upload(Bl[0], &X->cd_Ms)); XTRY(X->upload(Bl[1], &X->cd_Cs)); XTRY(X->upload(Bl[2], &X->cd_Ks));
+    XTRY(X->upload(Bl[3], &X->cd_Gs)); XTRY(X->upload(Dinv, &X->cd_Dinv));
+    XTRY(X->upload(kinv, &X->cd_kinv));
+    XTRY(X->alloc((size_t)nt, &X->cd_Up)); XTRY(X->alloc((size_t)nt, &X->cd_Ubn));
+    return SVL_OK;
+}
+
+// One explicit step k of the staggered PML scheme (see k_cdp_sin).
+int cdp_step(svl_xnm* X, int k) {
+    const HostModel& m = X->m;
+    const int nt = m.ntotal, gt = grid_of(nt);
+    const double dt = X->opts.dt;
+    double *x0 = X->W, *x1 = X->Wg, *x2 = X->pt;
+    // displacement rows: -(solid internal force) and -(C_uS sdot + K_uS smid + G_uS Sbar), filtered
+    const size_t nsv = (size_t)X->nsol * X->ncs;
+    if (nsv > 0) k_xneg<<<(unsigned)((nsv + 255) / 256), 256, 0, X->stream>>>(nsv, X->s_fint, X->fe);
+    k_cdp_sin<<<gt, 256, 0, X->stream>>>(nt, X->cd_sdof, X->U, X->cd_Up, X->Ub, dt, x0, x1, x2);
+    if (X->npml > 0) {
+        PmlArgs P = pml_args(X);
+        P.coef[1] = 1.0; P.u[1] = x0; P.coef[2] = 1.0; P.u[2] = x1;
+        if (m.ndim == 3) { P.coef[3] = 1.0; P.u[3] = x2; }
+        P.ftol = X->opts.ftol; P.yscale = -1.0;
+        XTRY(pml_action_launch(m.ndim, P, X->stream));
+    }
+    XTRY(x_gather(X, X->yt, 0.0, nullptr, 0.0, nullptr, k, true));     // Fext(k) - forces
+    if (X->lt.has_sm)
+        k_xsm<<<gt, 256, 0, X->stream>>>(nt, X->sm_ptr, X->sm_ser, X->sm_fac, X->s_ptr, X->s_val, k, X->sm);
+    const int nf = m.nfree;
+    k_cdp_r<<<gt, 256, 0, X->stream>>>(nt, X->cd_sdof, X->yt, X->cd_Mu, X->cd_Cu, X->cd_Ku, X->cd_Gu, dt, X->U,
+                                       X->cd_Up, X->Ub, X->ys);
+    k_xreduce<<<grid_of(nf), 256, 0, X->stream>>>(nf, X->TTp, X->TTr, X->TTv, X->ys, nullptr, X->b);
+    k_cdp_solve<<<grid_of(nf), 256, 0, X->stream>>>(nf, X->cd_kinv, X->b, X->x);
+    k_xexpand<<<gt, 256, 0, X->stream>>>(nt, X->Tp, X->Tc, X->Tv, X->x, X->Ui);
+    k_cdp_u<<<gt, 256, 0, X->stream>>>(nt, X->cd_sdof, X->Ui, X->lt.has_sm ? X->sm : nullptr, dt, X->U, X->Ub,
+                                       X->dUt, X->Us, X->cd_Ubn, x0, x1, x2);
+    XCUDA(cudaGetLastError());
+    XTRY(x_state(X));                                                   // solid states from U + du
+    // stress rows: C_Su udot + K_Su umid + G_Su ubar (unfiltered), gathered
+    if (X->npml > 0) {
+        PmlArgs P = pml_args(X);
+        P.coef[1] = 1.0; P.u[1] = x0; P.coef[2] = 1.0; P.u[2] = x1;
+        if (m.ndim == 3) { P.coef[3] = 1.0; P.u[3] = x2; }
+        XTRY(pml_action_launch(m.ndim, P, X->stream));
+        XTRY(x_gather(X, X->ys, 0.0, nullptr, 0.0, nullptr, 0, false));
+        const int gs = (X->cd_nsn + 127) / 128;
+        if (m.ndim == 2)
+            k_cdp_s<3><<<gs, 128, 0, X->stream>>>(X->cd_nsn, X->cd_sfirst, X->ys, X->cd_Ms, X->cd_Cs, X->cd_Ks,
+                                                  X->cd_Gs, X->cd_Dinv, X->U, X->cd_Up, X->Ub, dt, X->dUt, X->cd_Ubn);
+        else
+            k_cdp_s<6><<<gs, 128, 0, X->stream>>>(X->cd_nsn, X->cd_sfirst, X->ys, X->cd_Ms, X->cd_Cs, X->cd_Ks,
+                                                  X->cd_Gs, X->cd_Dinv, X->U, X->cd_Up, X->Ub, dt, X->dUt, X->cd_Ubn);
+    }
+    k_cdp_update<<<gt, 256, 0, X->stream>>>(nt, X->U, X->cd_Up, X->V, X->A, X->Ub, X->dUt, X->cd_Ubn, dt, X->bad);
+    XCUDA(cudaGetLastError());
+    return SVL_OK;
+}
+
 int x_setup(svl_xnm* X, const svl_load_desc* L) {
     HostModel& m = X->m;
     const int nd = m.ndim, nen = m.nen, pnd = m.pml_ndof();
@@ -1491,8 +1850,9 @@ int x_setup(svl_xnm* X, const svl_load_desc* L) {
     XTRY(X->alloc(kBlocks, &X->partial));
     XTRY(X->alloc(8, &X->scal));
     XTRY(X->alloc(1, &X->bad));
-    // PML diagonal entries by unit probes of the element action (once)
-    if (X->npml > 0) {
+    // PML diagonal entries by unit probes of the element action (once; the
+    // explicit scheme has no solve)
+    if (X->npml > 0 && !X->explicit_cd) {
         double *ub = nullptr, *yb = nullptr, *db = nullptr;
         const size_t ne = (size_t)X->npml * X->ncp;
         XTRY(X->alloc(ne, &ub)); XTRY(X->alloc(ne, &yb)); XTRY(X->alloc(ne, &db));
@@ -1514,6 +1874,7 @@ int x_setup(svl_xnm* X, const svl_load_desc* L) {
         for (int i = 0; i < X->npml; ++i)
             for (int j = 0; j < X->ncp; ++j) diag[p_edof[(size_t)i * X->ncp + j]] += dh[(size_t)i * X->ncp + j];
     }
+    if (X->explicit_cd) XTRY(cdp_setup(X, sol, pml));
     // Jacobi on the free dofs: |sum_t T_tf^2 diag_t|^-1
     std::vector<double> dfree(std::max(m.nfree, 1), 0.0);
     for (int t = 0; t < m.ntotal; ++t)
@@ -1532,7 +1893,8 @@ extern "C" {
 int svl_xnm_create(const svl_model_desc* model, const svl_load_desc* loads, const svl_xnm_opts* opts, svl_xnm** out) {
     if (!out || !opts) { set_error("NULL argument"); return SVL_ERR_INVALID; }
     *out = nullptr;
-    if (!(opts->dt > 0.0) || !(opts->tol > 0.0) || opts->maxit <= 0) { set_error("bad ExtendedNewmark options"); return SVL_ERR_INVALID; }
+    const bool expl = opts->integrator == SVL_XNM_CENTRAL_DIFFERENCE;
+    if (!(opts->dt > 0.0) || (!expl && (!(opts->tol > 0.0) || opts->maxit <= 0))) { set_error("bad ExtendedNewmark options"); return SVL_ERR_INVALID; }
     if (opts->algorithm != SVL_ALGO_LINEAR && opts->algorithm != SVL_ALGO_NEWTON) { set_error("unknown algorithm %d", opts->algorithm); return SVL_ERR_INVALID; }
     if (opts->algorithm == SVL_ALGO_NEWTON &&
         (opts->newton_maxit <= 0 || opts->cnvgtest < 1 || opts->cnvgtest > 8 || !(opts->cnvgtol >= 0.0))) {
@@ -1545,10 +1907,22 @@ int svl_xnm_create(const svl_model_desc* model, const svl_load_desc* loads, cons
     auto fail = [&](int st) { delete X; return st; };
     if (!model_from_desc(model, X->m)) return fail(SVL_ERR_INVALID);
     X->newton = opts->algorithm == SVL_ALGO_NEWTON;
-    if (opts->integrator != SVL_XNM_EXTENDED_NEWMARK && opts->integrator != SVL_XNM_NEWMARK) {
+    if (opts->integrator != SVL_XNM_EXTENDED_NEWMARK && opts->integrator != SVL_XNM_NEWMARK && !expl) {
         set_error("unknown integrator %d", opts->integrator); return fail(SVL_ERR_INVALID);
     }
     X->newmark = opts->integrator == SVL_XNM_NEWMARK;
+    X->explicit_cd = expl;
+    if (expl) {
+        const HostModel& m = X->m;
+        if (opts->algorithm != SVL_ALGO_LINEAR) { set_error("the explicit PML scheme takes the Linear algorithm"); return fail(SVL_ERR_UNSUPPORTED); }
+        if (!m.dp_eta.empty()) { set_error("the explicit PML scheme does not take dashpots"); return fail(SVL_ERR_UNSUPPORTED); }
+        if (loads && loads->ndrm > 0) { set_error("the explicit PML scheme does not take domain-reduction loads"); return fail(SVL_ERR_UNSUPPORTED); }
+        for (int e = 0; !m.ray.empty() && e < m.nelem; ++e)
+            if (m.ray[2 * (size_t)e + 1] != 0.0 || (m.has_pml() && m.epml[e] && m.ray[2 * (size_t)e] != 0.0)) {
+                set_error("the explicit PML scheme takes mass-proportional Rayleigh damping on solid elements only");
+                return fail(SVL_ERR_UNSUPPORTED);
+            }
+    }
     for (int e = 0; X->m.has_pml() && e < X->m.nelem; ++e) {
         const int t = X->m.mat_type(e);
         if (X->m.epml[e] && t != SVL_MAT_ELASTIC2DPLANESTRAIN && t != SVL_MAT_ELASTIC3DLINEAR) {
@@ -1574,6 +1948,10 @@ int svl_xnm_set_initial(svl_xnm* X, const double* U0, const double* V0, const do
         else XCUDA(cudaMemsetAsync(dst[i], 0, bytes, X->stream));
     }
     XCUDA(cudaMemcpyAsync(X->Us, X->U, bytes, cudaMemcpyDeviceToDevice, X->stream));
+    if (X->explicit_cd) {
+        k_cdp_init<<<grid_of(X->m.ntotal), 256, 0, X->stream>>>(X->m.ntotal, X->U, X->V, X->A, X->opts.dt, X->cd_Up);
+        XCUDA(cudaGetLastError());
+    }
     XTRY(x_state(X));                         // element states from U0 (oracle: UpdateState + commit)
     XCUDA(cudaStreamSynchronize(X->stream));
     return SVL_OK;
@@ -1583,7 +1961,7 @@ int svl_xnm_run(svl_xnm* X, int32_t k_first, int32_t nsteps, double* U_hist) {
     if (!X || nsteps < 0) { set_error("bad argument"); return SVL_ERR_INVALID; }
     const size_t nt = X->m.ntotal;
     for (int i = 0; i < nsteps; ++i) {
-        XTRY(x_step(X, k_first + i));
+        XTRY(X->explicit_cd ? cdp_step(X, k_first + i) : x_step(X, k_first + i));
         if (U_hist) XCUDA(cudaMemcpyAsync(U_hist + (size_t)i * nt, X->U, sizeof(double) * nt, cudaMemcpyDeviceToHost, X->stream));
     }
     int bad = 0;

@@ -18,6 +18,16 @@ from .model import Loads, Model
 
 
 class CentralDifference:
+    """A model with PML layers is served by the PML-capable handle with the
+    library's explicit PML scheme (svl_xnm_*, integrator
+    SVL_XNM_CENTRAL_DIFFERENCE); the object returned is then an
+    ExtendedNewmarkBeta instance with the same step methods."""
+
+    def __new__(cls, model: Model, *args, **kw):
+        if cls is CentralDifference and getattr(model, "elem_pml", None) is not None and np.any(model.elem_pml):
+            return _central_difference_pml(model, *args, **kw)
+        return super().__new__(cls)
+
     def __init__(self, model: Model, loads: Loads | None, dt: float, ftol: float = 1e-12,
                  mtol: float = 1e-12, check_every: int = 0):
         self.model = model
@@ -201,9 +211,13 @@ class ExtendedNewmarkBeta:
                  solver_maxit: int = 100000, ftol: float = 1e-12, mtol: float = 1e-12, algorithm: str = "linear",
                  maxit: int = 50, cnvgtol: float = 1e-6, cnvgtest: int = 4, integrator: str = "extendednewmark",
                  single_inner: bool = True):
-        """integrator "extendednewmark" (ExtendedNewmarkBeta.cpp) or "newmark"
+        """integrator "extendednewmark" (ExtendedNewmarkBeta.cpp), "newmark"
         (NewmarkBeta.cpp on the same elements: the PML history matrix is not
-        used; NewmarkBeta(model with PML layers, ...) builds this).
+        used; NewmarkBeta(model with PML layers, ...) builds this) or
+        "centraldifference" (the library's explicit scheme for PML models:
+        stress dofs at the half steps, lumped N N blocks; tol and solver_maxit
+        are not used; CentralDifference(model with PML layers, ...) builds
+        this).
         single_inner: the inner MINRES iterations apply the element operators
         in single precision, the restarts' true residual and the stopping test
         stay in double (iterative refinement)."""
@@ -212,7 +226,8 @@ class ExtendedNewmarkBeta:
         self._md = model.desc()
         self._ld = (loads or Loads()).desc()
         algo = {"linear": capi.SVL_ALGO_LINEAR, "newton": capi.SVL_ALGO_NEWTON}[algorithm.lower()]
-        integ = {"extendednewmark": capi.SVL_XNM_EXTENDED_NEWMARK, "newmark": capi.SVL_XNM_NEWMARK}[integrator.lower()]
+        integ = {"extendednewmark": capi.SVL_XNM_EXTENDED_NEWMARK, "newmark": capi.SVL_XNM_NEWMARK,
+                 "centraldifference": capi.SVL_XNM_CENTRAL_DIFFERENCE}[integrator.lower()]
         opts = capi.XnmOpts(dt=self.dt, ftol=ftol, mtol=mtol, tol=float(tol), maxit=int(solver_maxit),
                             algorithm=algo, newton_maxit=int(maxit), cnvgtest=int(cnvgtest), cnvgtol=float(cnvgtol),
                             integrator=integ, single_inner=1 if single_inner else 0)
@@ -444,6 +459,12 @@ class NewmarkBeta:
             self.close()
         except Exception:
             pass
+
+
+def _central_difference_pml(model, loads, dt, ftol=1e-12, mtol=1e-12, check_every=0):
+    """CentralDifference on a model with PML layers: the explicit staggered
+    scheme of the PML-capable handle."""
+    return ExtendedNewmarkBeta(model, loads, dt, ftol=ftol, mtol=mtol, integrator="centraldifference")
 
 
 def _newmark_pml(model: Model, loads: Loads | None, dt: float, pcg_tol: float = 1e-8, pcg_maxit: int = 20000,

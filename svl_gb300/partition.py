@@ -110,8 +110,9 @@ class Partition:
     root: Optional[Path] = None
 
     def make_integrator(self, pcg_tol: Optional[float] = None):
-        """The GPU integrator the simulation block asks for: CENTRALDIFFERENCE,
-        NEWMARK (NewmarkBeta; on a model with PML layers the PML-capable
+        """The GPU integrator the simulation block asks for: CENTRALDIFFERENCE
+        (on a model with PML layers the library's explicit PML scheme on the
+        PML-capable handle), NEWMARK (NewmarkBeta; on a model with PML layers the PML-capable
         handle in NewmarkBeta mode) or EXTENDEDNEWMARK (ExtendedNewmarkBeta),
         with the algorithm LINEAR or NEWTON (`cnvgtol` 1e-6, `nstep` 50,
         `cnvgtest` 4 by default, Driver.hpp:1786-1822); an iterative solver's
