@@ -193,7 +193,9 @@ struct CdxView {
     int ntx, nty, ntz, ntiles;
     float* uh_prev;                      // u_{n-1} (read through TMA), u_{n+1} written here
     float* ul_prev;
-    const float* __restrict__ cdof;      // [inst][z][y][pitch]  dt^2/m, 0 on restrained dofs
+    const float* __restrict__ cdof;      // [inst][z][y][pitch]  dt^2/m, 0 on restrained dofs,
+                                         // -1 on the displacement dofs of PML nodes
+    float* fsol;                         // PML nodes: the solid elements' force sum (same layout), or null
     const float* __restrict__ bop;       // [B_ROWS x 24] hi then lo operand image
     // external loads grouped by tile, then by dof
     const int* __restrict__ tl_ptr;      // [ntiles+1] into the unique-dof arrays
@@ -481,6 +483,10 @@ k_cdx_step(const __grid_constant__ CUtensorMap tmap_u, const __grid_constant__ C
                 const float* ah = raw + ((oz + 1) * HY + (oy + 1)) * RAWX + (RAW_SHIFT + ox + 1) * 3;
 #pragma unroll
                 for (int c = 0; c < 3; ++c) {
+                    if (tcd[ob + c] < 0.f) {          // PML node: its update is the PML kernels'
+                        v.fsol[gbase + c] = f[c];
+                        continue;
+                    }
                     const float inc = -tcd[ob + c] * f[c];
                     float dh, dl2, Dh, Dl, nh, nl;
                     df_add(ah[c], tulc[ob + c], -tuhp[ob + c], -tulp[ob + c], dh, dl2);   // u_n - u_{n-1}
@@ -554,16 +560,338 @@ __global__ void k_cdx_va(const float* nh, const float* nl, const float* ch, cons
 
 // FP64 total-dof displacement of every instance from the padded compensated
 // pairs: out[b][t] = hi + lo at the padded position of total dof t = node*3 + c.
-__global__ void k_cdx_hist(const float* __restrict__ uh, const float* __restrict__ ul, double* __restrict__ out,
-                           long long ntotal, int nxn, int nyn, int pitch, long long per, int ninst) {
+// FP64 total-dof vector of every instance from the compensated pairs:
+// omap[t] >= 0 is the padded position of displacement dof t, -(1 + k) the
+// stress entry k = p*6 + c of PML node p (S of the half step after U's time).
+__global__ void k_cdx_hist(const float* __restrict__ uh, const float* __restrict__ ul, const float* __restrict__ sh,
+                           const float* __restrict__ sl, const long long* __restrict__ omap, double* __restrict__ out,
+                           long long ntotal, long long per, long long sper, int ninst) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= ntotal * ninst) return;
     const long long b = i / ntotal, t = i - b * ntotal;
-    const long long n = t / 3;
-    const int c = (int)(t - n * 3);
-    const long long x = n % nxn, y = (n / nxn) % nyn, z = n / ((long long)nxn * nyn);
-    const long long p = b * per + (z * nyn + y) * pitch + x * 3 + c;
-    out[i] = (double)uh[p] + (double)ul[p];
+    const long long m = omap[t];
+    if (m >= 0) out[i] = (double)uh[b * per + m] + (double)ul[b * per + m];
+    else out[i] = (double)sh[b * sper - m - 1] + (double)sl[b * sper - m - 1];
+}
+
+// ---- PML band of the mixed path --------------------------------------------
+// The explicit staggered PML scheme (displacements at the integer steps, the
+// PML stress dofs S at the half steps; lumped N N blocks per node, the
+// displacement-stress couplings of PML3DHexa8's C, K, G, PML3DHexa8.cpp:
+// 430-712, as element actions) in FP32 arithmetic with the state as
+// compensated FP32 pairs.  Each step: k_cdx_step leaves the solid elements'
+// force at PML nodes in fsol; k_cdp_fu forms the coupling forces of the PML
+// elements on the displacement rows, k_cdp_uu updates u and ubar at the PML
+// nodes, k_cdp_fs forms the coupling forces on the stress rows from the new
+// u, k_cdp_su updates S and Sbar.  Elements are uniform cubes of side h:
+// at Gauss point q, N_a and dN_a/dx are fixed tables and w |J| = (h/2)^3.
+struct CdpView {
+    int ninst, np, npe;                 // PML nodes and PML elements per instance
+    float h, dt;
+    long long per;                      // padded state floats per instance
+    const int32_t* __restrict__ enode;  // [npe][8] PML node index of each element node
+    const float* __restrict__ egeo;     // [npe][12] corner xyz, x0 xyz, n xyz, a0, L, m
+    const float* __restrict__ eb0;      // [ninst][npe] b0 of the element's P-wave speed
+    const int32_t* __restrict__ ninv;   // [np][8] element slots e*8 + local node in element order, -1 unused
+    const long long* __restrict__ npad; // [np] padded offset of the node's displacement in instance 0
+    const float* __restrict__ uc;       // [ninst][np][6] 1/d for x y z (0 when restrained), c, Ku, Gu
+    const float* __restrict__ scs;      // [ninst][np][36] Dinv, A, KG, Gs (9 each: xx yy zz xy yz xz | 12 23 13)
+    const float* __restrict__ uh;       // u_n pair (padded)
+    const float* __restrict__ ul;
+    float* uph;                         // u_{n-1} pair in, u_{n+1} out
+    float* upl;
+    const float* __restrict__ fsol;
+    float* ubh; float* ubl;             // [ninst][np][3] ubar pair
+    const float* __restrict__ sh;       // S^{n+1/2} pair [ninst][np][6]
+    const float* __restrict__ sl;
+    float* sph; float* spl;             // S^{n-1/2} in, S^{n+3/2} out
+    float* sbh; float* sbl;             // Sbar pair [ninst][np][6]
+    float* vin;                         // [ninst][np][9] udot, umid, ubar at the half step
+    float* feu;                         // [ninst][npe][8][3]
+    float* fes;                         // [ninst][npe][8][6]
+};
+
+constexpr int CDP_THREADS = 256;
+__constant__ float kHexR[8] = {-1, 1, 1, -1, -1, 1, 1, -1};
+__constant__ float kHexS[8] = {-1, -1, 1, 1, -1, -1, 1, 1};
+__constant__ float kHexT[8] = {-1, -1, -1, -1, 1, 1, 1, 1};
+
+// Gauss point q (r fastest, GaussQuadrature.cpp:303-316 abscissa) of the cube
+// element e: shape values, physical derivatives, w |J|, and the coupling
+// weights of C, K, G per derivative direction from the stretching at the
+// point (PML3DHexa8.cpp:952-996; x: C ay az, K ay bz + az by, G by bz).
+__device__ __forceinline__ void cdp_gauss(const CdpView& v, int e, int inst, int q, float N[8], float dN[8][3],
+                                          float& W, float qC[3], float qK[3], float qG[3]) {
+    const float g = 0.577350269189626f;
+    const float xi[3] = {(q & 1) ? g : -g, (q & 2) ? g : -g, (q & 4) ? g : -g};
+    const float c2 = 2.0f / v.h;
+#pragma unroll
+    for (int a = 0; a < 8; ++a) {
+        const float fr = 1.0f + kHexR[a] * xi[0], fs = 1.0f + kHexS[a] * xi[1], ft = 1.0f + kHexT[a] * xi[2];
+        N[a] = 0.125f * fr * fs * ft;
+        dN[a][0] = c2 * 0.125f * kHexR[a] * fs * ft;
+        dN[a][1] = c2 * 0.125f * kHexS[a] * fr * ft;
+        dN[a][2] = c2 * 0.125f * kHexT[a] * fr * fs;
+    }
+    const float hh = 0.5f * v.h;
+    W = hh * hh * hh;
+    const float* gq = v.egeo + (size_t)e * 12;
+    const float a0 = gq[9], L = gq[10], pm = gq[11], b0 = v.eb0[(size_t)inst * v.npe + e];
+    float as[3], bs[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        const float xg = gq[d] + hh * (1.0f + xi[d]);
+        const float r = powf((xg - gq[3 + d]) * gq[6 + d] / L, pm);
+        as[d] = 1.0f + a0 * r;
+        bs[d] = b0 * r;
+    }
+    qC[0] = as[1] * as[2]; qC[1] = as[0] * as[2]; qC[2] = as[0] * as[1];
+    qK[0] = as[1] * bs[2] + as[2] * bs[1]; qK[1] = as[0] * bs[2] + as[2] * bs[0]; qK[2] = as[0] * bs[1] + as[1] * bs[0];
+    qG[0] = bs[1] * bs[2]; qG[1] = bs[0] * bs[2]; qG[2] = bs[0] * bs[1];
+}
+
+// Sum of x over the 8 lanes of a group, element j of the result on lane j:
+// recursive halving (lane bit 2, then 1, then 0 selects the half it keeps).
+template <int C>
+__device__ __forceinline__ void cdp_reduce8(float (&f)[8][C], int q, float (&out)[C]) {
+    const bool b2 = (q >> 2) & 1, b1 = (q >> 1) & 1, b0 = q & 1;
+    float k4[4][C], k2[2][C];
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+        for (int c = 0; c < C; ++c) {
+            const float send = b2 ? f[j][c] : f[j + 4][c];
+            const float r = __shfl_xor_sync(0xffffffffu, send, 4);
+            k4[j][c] = (b2 ? f[j + 4][c] : f[j][c]) + r;
+        }
+#pragma unroll
+    for (int j = 0; j < 2; ++j)
+#pragma unroll
+        for (int c = 0; c < C; ++c) {
+            const float send = b1 ? k4[j][c] : k4[j + 2][c];
+            const float r = __shfl_xor_sync(0xffffffffu, send, 2);
+            k2[j][c] = (b1 ? k4[j + 2][c] : k4[j][c]) + r;
+        }
+#pragma unroll
+    for (int c = 0; c < C; ++c) {
+        const float send = b0 ? k2[0][c] : k2[1][c];
+        const float r = __shfl_xor_sync(0xffffffffu, send, 1);
+        out[c] = (b0 ? k2[1][c] : k2[0][c]) + r;
+    }
+}
+
+// Coupling forces of the PML elements on the displacement rows:
+// C_uS sdot + K_uS smid + G_uS Sbar, one thread per (element, Gauss point);
+// lane q of a group loads node q, lane j writes node j.
+__global__ void __launch_bounds__(CDP_THREADS) k_cdp_fu(CdpView v) {
+    __shared__ float sm[CDP_THREADS / 8][8][18];
+    const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int q = (int)(gid & 7), lg = threadIdx.x >> 3;
+    const long long grp = gid >> 3;
+    const bool valid = grp < (long long)v.ninst * v.npe;
+    const int inst = valid ? (int)(grp / v.npe) : 0, e = valid ? (int)(grp % v.npe) : 0;
+    if (valid) {
+        const int p = v.enode[(size_t)e * 8 + q];
+        const size_t b = ((size_t)inst * v.np + p) * 6;
+        const float idt = 1.0f / v.dt;
+#pragma unroll
+        for (int c = 0; c < 6; ++c) {
+            const float ch = v.sh[b + c], cl = v.sl[b + c], ph = v.sph[b + c], pl = v.spl[b + c];
+            sm[lg][q][c] = ((ch - ph) + (cl - pl)) * idt;
+            sm[lg][q][6 + c] = 0.5f * (ch + ph);
+            sm[lg][q][12 + c] = v.sbh[b + c];
+        }
+    } else {
+#pragma unroll
+        for (int c = 0; c < 18; ++c) sm[lg][q][c] = 0.f;
+    }
+    __syncwarp();
+    float N[8], dN[8][3], W, qC[3], qK[3], qG[3];
+    cdp_gauss(v, e, inst, q, N, dN, W, qC, qK, qG);
+    float sg[18];
+#pragma unroll
+    for (int k = 0; k < 18; ++k) sg[k] = 0.f;
+#pragma unroll
+    for (int a = 0; a < 8; ++a)
+#pragma unroll
+        for (int k = 0; k < 18; ++k) sg[k] += N[a] * sm[lg][a][k];
+    // T^d_c = qC_d sdot_c + qK_d smid_c + qG_d sbar_c (components xx yy zz xy yz xz)
+    auto T = [&](int d, int c) { return qC[d] * sg[c] + qK[d] * sg[6 + c] + qG[d] * sg[12 + c]; };
+    const float tx0 = T(0, 0), tx3 = T(0, 3), tx5 = T(0, 5);
+    const float ty3 = T(1, 3), ty1 = T(1, 1), ty4 = T(1, 4);
+    const float tz5 = T(2, 5), tz4 = T(2, 4), tz2 = T(2, 2);
+    float f[8][3];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        f[j][0] = W * (dN[j][0] * tx0 + dN[j][1] * ty3 + dN[j][2] * tz5);
+        f[j][1] = W * (dN[j][0] * tx3 + dN[j][1] * ty1 + dN[j][2] * tz4);
+        f[j][2] = W * (dN[j][0] * tx5 + dN[j][1] * ty4 + dN[j][2] * tz2);
+    }
+    float out[3];
+    cdp_reduce8<3>(f, q, out);
+    if (valid) {
+        float* o = v.feu + (((size_t)inst * v.npe + e) * 8 + q) * 3;
+        o[0] = out[0]; o[1] = out[1]; o[2] = out[2];
+    }
+}
+
+// Displacement rows of the PML nodes: R = -(fsol + sum of the element slots)
+// - Ku u - Gu ubar + c (u - u_{n-1}), du = R / d; u_{n+1} = u + du and
+// ubar += dt (u + du/2) as pairs; the stress rows' inputs.
+__global__ void __launch_bounds__(256) k_cdp_uu(CdpView v) {
+    const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid >= (long long)v.ninst * v.np) return;
+    const int inst = (int)(gid / v.np), p = (int)(gid % v.np);
+    const long long pad = (long long)inst * v.per + v.npad[p];
+    float f[3] = {v.fsol[pad], v.fsol[pad + 1], v.fsol[pad + 2]};
+    const size_t fb = (size_t)inst * v.npe * 8;
+#pragma unroll
+    for (int s2 = 0; s2 < 8; ++s2) {
+        const int slot = v.ninv[(size_t)p * 8 + s2];
+        if (slot < 0) break;
+        const float* fe = v.feu + (fb + slot) * 3;
+        f[0] += fe[0]; f[1] += fe[1]; f[2] += fe[2];
+    }
+    const float* c6 = v.uc + ((size_t)inst * v.np + p) * 6;
+    const float cc = c6[3], Ku = c6[4], Gu = c6[5];
+    const size_t ib = ((size_t)inst * v.np + p) * 3;
+    float* vi = v.vin + ((size_t)inst * v.np + p) * 9;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const float uh = v.uh[pad + c], ul = v.ul[pad + c], ph = v.uph[pad + c], pl = v.upl[pad + c];
+        const float bh = v.ubh[ib + c], bl = v.ubl[ib + c];
+        const float u = uh + ul;
+        const float R = -f[c] - Ku * u - Gu * bh + cc * ((uh - ph) + (ul - pl));
+        const float du = c6[c] * R;
+        float nh, nl;
+        df_add(uh, ul, du, 0.f, nh, nl);
+        v.uph[pad + c] = nh;
+        v.upl[pad + c] = nl;
+        const float inc = v.dt * (u + 0.5f * du);
+        float bh2, bl2;
+        df_add(bh, bl, inc, 0.f, bh2, bl2);
+        v.ubh[ib + c] = bh2;
+        v.ubl[ib + c] = bl2;
+        vi[c] = du / v.dt;
+        vi[3 + c] = u + 0.5f * du;
+        vi[6 + c] = bh + 0.5f * inc;
+    }
+}
+
+// Coupling forces of the PML elements on the stress rows:
+// C_Su udot + K_Su umid + G_Su ubar_half = w |J| N_j (stretched strain).
+__global__ void __launch_bounds__(CDP_THREADS) k_cdp_fs(CdpView v) {
+    __shared__ float sm[CDP_THREADS / 8][8][9];
+    const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int q = (int)(gid & 7), lg = threadIdx.x >> 3;
+    const long long grp = gid >> 3;
+    const bool valid = grp < (long long)v.ninst * v.npe;
+    const int inst = valid ? (int)(grp / v.npe) : 0, e = valid ? (int)(grp % v.npe) : 0;
+    if (valid) {
+        const int p = v.enode[(size_t)e * 8 + q];
+        const float* vi = v.vin + ((size_t)inst * v.np + p) * 9;
+#pragma unroll
+        for (int c = 0; c < 9; ++c) sm[lg][q][c] = vi[c];
+    } else {
+#pragma unroll
+        for (int c = 0; c < 9; ++c) sm[lg][q][c] = 0.f;
+    }
+    __syncwarp();
+    float N[8], dN[8][3], W, qC[3], qK[3], qG[3];
+    cdp_gauss(v, e, inst, q, N, dN, W, qC, qK, qG);
+    // gradients: gr[i][d][c] = d (input i)_c / dx_d
+    float gr[3][3][3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int d = 0; d < 3; ++d)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) gr[i][d][c] = 0.f;
+#pragma unroll
+    for (int a = 0; a < 8; ++a)
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int d = 0; d < 3; ++d)
+#pragma unroll
+                for (int c = 0; c < 3; ++c) gr[i][d][c] += dN[a][d] * sm[lg][a][3 * i + c];
+    // stretched strain: weight of direction d per matrix (C udot, K umid, G ubar)
+    auto wd = [&](int d, int c) { return qC[d] * gr[0][d][c] + qK[d] * gr[1][d][c] + qG[d] * gr[2][d][c]; };
+    float eps[6];
+    eps[0] = wd(0, 0);
+    eps[1] = wd(1, 1);
+    eps[2] = wd(2, 2);
+    eps[3] = wd(1, 0) + wd(0, 1);        // s12: y-derivative of u_x, x-derivative of u_y
+    eps[4] = wd(2, 1) + wd(1, 2);        // s23
+    eps[5] = wd(2, 0) + wd(0, 2);        // s13
+    float f[8][6];
+#pragma unroll
+    for (int j = 0; j < 8; ++j)
+#pragma unroll
+        for (int c = 0; c < 6; ++c) f[j][c] = W * N[j] * eps[c];
+    float out[6];
+    cdp_reduce8<6>(f, q, out);
+    if (valid) {
+        float* o = v.fes + (((size_t)inst * v.npe + e) * 8 + q) * 6;
+#pragma unroll
+        for (int c = 0; c < 6; ++c) o[c] = out[c];
+    }
+}
+
+// y = M x for a stress block stored as [xx yy zz xy yz xz | 12 23 13]
+__device__ __forceinline__ void cdp_block(const float* Mb, const float x[6], float y[6]) {
+    y[0] = Mb[0] * x[0] + Mb[3] * x[1] + Mb[5] * x[2];
+    y[1] = Mb[3] * x[0] + Mb[1] * x[1] + Mb[4] * x[2];
+    y[2] = Mb[5] * x[0] + Mb[4] * x[1] + Mb[2] * x[2];
+    y[3] = Mb[6] * x[3];
+    y[4] = Mb[7] * x[4];
+    y[5] = Mb[8] * x[5];
+}
+
+// Stress rows of the PML nodes: R = -Fs - KG S - Gs Sbar + A (S - S_prev),
+// dS = Dinv R; S_next = S + dS and Sbar += dt S as pairs.
+__global__ void __launch_bounds__(256) k_cdp_su(CdpView v) {
+    const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid >= (long long)v.ninst * v.np) return;
+    const int inst = (int)(gid / v.np), p = (int)(gid % v.np);
+    float F[6] = {0, 0, 0, 0, 0, 0};
+    const size_t fb = (size_t)inst * v.npe * 8;
+#pragma unroll
+    for (int s2 = 0; s2 < 8; ++s2) {
+        const int slot = v.ninv[(size_t)p * 8 + s2];
+        if (slot < 0) break;
+        const float* fe = v.fes + (fb + slot) * 6;
+#pragma unroll
+        for (int c = 0; c < 6; ++c) F[c] += fe[c];
+    }
+    const size_t b = ((size_t)inst * v.np + p) * 6;
+    float sc[6], ds[6], sb[6];
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+        const float ch = v.sh[b + c], cl = v.sl[b + c], ph = v.sph[b + c], pl = v.spl[b + c];
+        sc[c] = ch + cl;
+        ds[c] = (ch - ph) + (cl - pl);
+        sb[c] = v.sbh[b + c];
+    }
+    const float* K = v.scs + ((size_t)inst * v.np + p) * 36;
+    float t1[6], t2[6], t3[6], R[6], dS[6];
+    cdp_block(K + 18, sc, t1);            // KG S
+    cdp_block(K + 27, sb, t2);            // Gs Sbar
+    cdp_block(K + 9, ds, t3);             // A (S - S_prev)
+#pragma unroll
+    for (int c = 0; c < 6; ++c) R[c] = -F[c] - t1[c] - t2[c] + t3[c];
+    cdp_block(K, R, dS);                  // Dinv R
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+        float nh, nl;
+        df_add(v.sh[b + c], v.sl[b + c], dS[c], 0.f, nh, nl);
+        v.sph[b + c] = nh;
+        v.spl[b + c] = nl;
+        float bh, bl;
+        df_add(v.sbh[b + c], v.sbl[b + c], v.dt * sc[c], 0.f, bh, bl);
+        v.sbh[b + c] = bh;
+        v.sbl[b + c] = bl;
+    }
 }
 
 float host_tf32(double x) {
@@ -585,6 +913,7 @@ struct svl_cdx {
     long long nstate = 0;                // padded state length (all instances)
     int ntx = 0, nty = 0, ntz = 0, ntiles = 0, grid = 0;
     double dt = 0;
+    double hgrid = 0;                    // element side (uniform cubes)
     cudaStream_t stream = nullptr;
     std::vector<void*> allocs;
     float* uh[2] = {nullptr, nullptr};   // compensated displacement pairs (hi, lo), padded rows
@@ -603,7 +932,17 @@ struct svl_cdx {
     CUtensorMap own_uh[2], own_ul[2];    // owned-node maps of uh[*], ul[*]
     CUtensorMap own_cd;                  // owned-node map of dt^2/m
     CUtensorMap tmap_lam, tmap_mu;
-    std::vector<long long> pad_index;    // total dof (node*3+c) -> padded position, one instance
+    std::vector<long long> pad_index;    // total dof -> padded position (displacement dofs), or
+                                         // -(1 + p*6 + c) for stress dof c of PML node p; one instance
+    long long* d_omap = nullptr;         // pad_index on the device
+    // PML band (np = 0 without PML elements)
+    int np = 0, npe = 0;
+    float* fsol = nullptr;
+    float *sh[2] = {nullptr, nullptr}, *sl[2] = {nullptr, nullptr};
+    float *sbh = nullptr, *sbl = nullptr, *ubh = nullptr, *ubl = nullptr;
+    float *vin = nullptr, *feu = nullptr, *fes = nullptr, *uc = nullptr, *scs = nullptr, *egeo = nullptr, *eb0 = nullptr;
+    int32_t *enode = nullptr, *ninv = nullptr;
+    long long* npad = nullptr;
     int cur = 0;                         // index of u_n in uh/ul
     int64_t launches = 0, launches_last = 0;
     bool va_valid = false;
@@ -675,19 +1014,27 @@ static int cdx_check_instance(const svl_grid_spec* g, const HostModel& m, int in
     if (m.nnode != nn || m.nelem != (long long)nx * ny * nz) { set_error("instance %d does not match the grid size", inst); return SVL_ERR_INVALID; }
     if (m.nconstraint) { set_error("instance %d: constraints are not supported on the structured path", inst); return SVL_ERR_UNSUPPORTED; }
     if (!m.lumped) { set_error("instance %d: the explicit path needs a lumped mass", inst); return SVL_ERR_UNSUPPORTED; }
-    if (m.has_pml()) { set_error("instance %d: PML elements are served by svl_xnm_create", inst); return SVL_ERR_UNSUPPORTED; }
+    if (m.has_pml())
+        for (int e = 0; e < m.nelem; ++e)
+            if (m.epml[e] && m.mtype[m.emat[e]] != SVL_MAT_ELASTIC3DLINEAR) { set_error("instance %d: PML element %d needs Elastic3DLinear", inst, e); return SVL_ERR_UNSUPPORTED; }
     if (!m.ray.empty()) { set_error("instance %d: Rayleigh damping is served by the general path (svl_cd_create)", inst); return SVL_ERR_UNSUPPORTED; }
     for (int k = 0; k < m.nmat; ++k)
         if (m.mtype[k] != SVL_MAT_ELASTIC3DLINEAR) { set_error("instance %d: only Elastic3DLinear on the structured path", inst); return SVL_ERR_UNSUPPORTED; }
-    // node coordinates on the grid, PlainScheme total dofs 3n+c, generator connectivity
+    // node coordinates on the grid, PlainScheme total dofs node by node (3, or 9
+    // at the nodes of PML elements), generator connectivity
+    long long off = 0;
     for (long long n = 0; n < nn; ++n) {
         const int i = (int)(n % (nx + 1)), j = (int)((n / (nx + 1)) % (ny + 1)), k = (int)(n / ((long long)(nx + 1) * (ny + 1)));
         const double X[3] = {g->origin[0] + i * g->h[0], g->origin[1] + j * g->h[1], g->origin[2] + k * g->h[2]};
-        for (int c = 0; c < 3; ++c) {
+        for (int c = 0; c < 3; ++c)
             if (std::fabs(m.X[n * 3 + c] - X[c]) > 1e-9 * (1.0 + std::fabs(X[c]))) { set_error("instance %d: node %lld is off the grid", inst, n); return SVL_ERR_INVALID; }
-            if (m.tdof[n * 3 + c] != n * 3 + c) { set_error("instance %d: total dofs are not in PlainScheme grid order", inst); return SVL_ERR_INVALID; }
-        }
+        const int nd = m.nndof[n];
+        if (nd != 3 && nd != 9) { set_error("instance %d: node %lld has %d dofs", inst, n, nd); return SVL_ERR_INVALID; }
+        for (int c = 0; c < nd; ++c)
+            if (m.tdof_all[(size_t)n * m.dstride + c] != off + c) { set_error("instance %d: total dofs are not in PlainScheme grid order", inst); return SVL_ERR_INVALID; }
+        off += nd;
     }
+    if (off != m.ntotal) { set_error("instance %d: total dof count mismatch", inst); return SVL_ERR_INVALID; }
     const long long layer = (long long)(nx + 1) * (ny + 1);
     long long e = 0;
     for (int k = 0; k < nz; ++k)
@@ -708,15 +1055,22 @@ static void split_pair(double x, float& hi, float& lo) {
 }
 
 // Device pair (hi, lo) of instance `inst` -> FP64 total-dof vector.
-static int fetch_pair(svl_cdx* h, const float* dh, const float* dl, int inst, double* out) {
-    const size_t per = h->nstate / h->ninst;
-    std::vector<float> hi(per), lo(per);
+// Device pairs of instance `inst` -> FP64 total-dof vector: displacement dofs
+// from (dh, dl) (padded layout), stress dofs of PML nodes from (sh, sl) or 0.
+static int fetch_pair(svl_cdx* h, const float* dh, const float* dl, int inst, double* out,
+                      const float* sh = nullptr, const float* sl = nullptr) {
+    const size_t per = h->nstate / h->ninst, n6 = (size_t)h->np * 6;
+    std::vector<float> hi(per), lo(per), shi(n6, 0.f), slo(n6, 0.f);
     CUDA_TRY(cudaMemcpyAsync(hi.data(), dh + (size_t)inst * per, per * 4, cudaMemcpyDeviceToHost, h->stream));
     CUDA_TRY(cudaMemcpyAsync(lo.data(), dl + (size_t)inst * per, per * 4, cudaMemcpyDeviceToHost, h->stream));
+    if (sh && n6 > 0) {
+        CUDA_TRY(cudaMemcpyAsync(shi.data(), sh + (size_t)inst * n6, n6 * 4, cudaMemcpyDeviceToHost, h->stream));
+        CUDA_TRY(cudaMemcpyAsync(slo.data(), sl + (size_t)inst * n6, n6 * 4, cudaMemcpyDeviceToHost, h->stream));
+    }
     CUDA_TRY(cudaStreamSynchronize(h->stream));
     for (long long t = 0; t < h->ntotal; ++t) {
         const long long p = h->pad_index[t];
-        out[t] = (double)hi[p] + (double)lo[p];
+        out[t] = p >= 0 ? (double)hi[p] + (double)lo[p] : (double)shi[-p - 1] + (double)slo[-p - 1];
     }
     return SVL_OK;
 }
@@ -739,7 +1093,7 @@ int svl_cdx_create(const svl_grid_spec* g, int32_t ninst, const svl_model_desc* 
     const int nxn = h->nx + 1, nyn = h->ny + 1, nzn = h->nz + 1;
     h->nn = (long long)nxn * nyn * nzn;
     h->ne = (long long)h->nx * h->ny * h->nz;
-    h->ntotal = h->nn * 3;
+    h->ntotal = 0;                                    // from the first instance's numbering
     h->pitch = (nxn * 3 + 3) / 4 * 4;
     const long long per = (long long)h->pitch * nyn * nzn;
     h->nstate = per * ninst;
@@ -748,12 +1102,16 @@ int svl_cdx_create(const svl_grid_spec* g, int32_t ninst, const svl_model_desc* 
     if (ntiles > INT32_MAX || h->nstate > ((long long)1 << 40)) { set_error("grid too large"); return fail(SVL_ERR_INVALID); }
     h->ntiles = (int)ntiles;
     h->dt = opts->dt;
+    h->hgrid = g->h[0];
     if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) { set_error("cudaStreamCreate failed"); return fail(SVL_ERR_CUDA); }
-    h->pad_index.resize(h->ntotal);
-    for (long long n = 0; n < h->nn; ++n) {
-        const long long x = n % nxn, y = (n / nxn) % nyn, z = n / ((long long)nxn * nyn);
-        for (int c = 0; c < 3; ++c) h->pad_index[n * 3 + c] = (z * nyn + y) * h->pitch + x * 3 + c;
-    }
+    // PML band tables (np = 0 without PML elements)
+    std::vector<int32_t> pidx;                       // node -> PML node index or -1
+    std::vector<int32_t> t2node;                     // total dof -> node (instance 0 numbering)
+    std::vector<int32_t> enode, ninv;
+    std::vector<long long> npad;
+    std::vector<float> egeo, eb0, uc, scs;
+    std::vector<int> pelem;                          // PML elements in element order
+    std::vector<double> par0;                        // instance 0's PML parameters
 
     h->pe = (h->nx + 8 + 3) / 4 * 4;                  // row padding keeps TMA strides 16-byte multiples
     const size_t lm_per = (size_t)h->pe * h->ny * h->nz;
@@ -770,6 +1128,129 @@ int svl_cdx_create(const svl_grid_spec* g, int32_t ninst, const svl_model_desc* 
         if (!model_from_desc(&models[b], m)) return fail(SVL_ERR_INVALID);
         int st = cdx_check_instance(g, m, b);
         if (st) return fail(st);
+        if (b == 0) {
+            // numbering maps and the PML band layout, shared by every instance
+            h->ntotal = m.ntotal;
+            h->pad_index.assign(h->ntotal, 0);
+            t2node.assign(h->ntotal, -1);
+            pidx.assign(h->nn, -1);
+            if (m.has_pml()) {
+                for (int e = 0; e < m.nelem; ++e)
+                    if (m.epml[e]) {
+                        pelem.push_back(e);
+                        for (int a = 0; a < 8; ++a) pidx[m.conn[(size_t)e * 8 + a]] = 0;
+                    }
+                for (long long n = 0; n < h->nn; ++n)
+                    if (pidx[n] == 0) { pidx[n] = h->np; npad.push_back(0); ++h->np; }
+                    else pidx[n] = -1;
+                // pidx was marked 0 for PML nodes: rebuild in node order
+            }
+            for (long long n = 0; n < h->nn; ++n) {
+                const long long x = n % nxn, y = (n / nxn) % nyn, z = n / ((long long)nxn * nyn);
+                for (int c = 0; c < m.nndof[n]; ++c) {
+                    const long long t = m.tdof_all[(size_t)n * m.dstride + c];
+                    t2node[t] = (int32_t)n;
+                    if (c < 3) h->pad_index[t] = (z * nyn + y) * h->pitch + x * 3 + c;
+                    else h->pad_index[t] = -(1 + (long long)pidx[n] * 6 + (c - 3));
+                }
+                if (pidx[n] >= 0) {
+                    npad[pidx[n]] = (z * nyn + y) * h->pitch + x * 3;
+                    if (m.nndof[n] != 9) { set_error("PML node %lld has %d dofs", n, m.nndof[n]); return fail(SVL_ERR_INVALID); }
+                } else if (m.nndof[n] != 3) {
+                    set_error("node %lld of no PML element has %d dofs", n, m.nndof[n]); return fail(SVL_ERR_INVALID);
+                }
+            }
+            h->npe = (int)pelem.size();
+            if (h->npe > 0) {
+                par0.assign(m.pml_par.begin(), m.pml_par.end());
+                enode.resize((size_t)h->npe * 8);
+                egeo.resize((size_t)h->npe * 12);
+                ninv.assign((size_t)h->np * 8, -1);
+                std::vector<int> fill(h->np, 0);
+                for (int i = 0; i < h->npe; ++i) {
+                    const int e = pelem[i];
+                    const double* pp = &m.pml_par[(size_t)e * 9];
+                    for (int a = 0; a < 8; ++a) {
+                        const int pn = pidx[m.conn[(size_t)e * 8 + a]];
+                        enode[(size_t)i * 8 + a] = pn;
+                        if (fill[pn] >= 8) { set_error("PML node %d in more than 8 elements", pn); return fail(SVL_ERR_INVALID); }
+                        ninv[(size_t)pn * 8 + fill[pn]++] = i * 8 + a;
+                    }
+                    const int n1 = m.conn[(size_t)e * 8];
+                    for (int d = 0; d < 3; ++d) {
+                        egeo[(size_t)i * 12 + d] = (float)m.X[(size_t)n1 * 3 + d];
+                        egeo[(size_t)i * 12 + 3 + d] = (float)pp[3 + d];
+                        egeo[(size_t)i * 12 + 6 + d] = (float)pp[6 + d];
+                    }
+                    const double pm = pp[0], L = pp[1], R = pp[2];
+                    egeo[(size_t)i * 12 + 9] = (float)((pm + 1.0) * (L / 10.0) / 2.0 / L * std::log(1.0 / R));
+                    egeo[(size_t)i * 12 + 10] = (float)L;
+                    egeo[(size_t)i * 12 + 11] = (float)pm;
+                }
+            }
+        } else {
+            if (m.ntotal != h->ntotal) { set_error("instance %d: dof count differs from instance 0", b); return fail(SVL_ERR_INVALID); }
+            for (int e = 0; e < m.nelem; ++e) {
+                const bool pe0 = !pelem.empty() && std::binary_search(pelem.begin(), pelem.end(), e);
+                if ((m.has_pml() && m.epml[e]) != pe0) { set_error("instance %d: PML layout differs from instance 0", b); return fail(SVL_ERR_INVALID); }
+                if (pe0)
+                    for (int j = 0; j < 9; ++j)
+                        if (m.pml_par[(size_t)e * 9 + j] != par0[(size_t)e * 9 + j]) { set_error("instance %d: PML parameters differ from instance 0", b); return fail(SVL_ERR_INVALID); }
+            }
+        }
+        if (h->np > 0 && !(g->h[1] == g->h[0] && g->h[2] == g->h[0])) {
+            set_error("the PML band of the structured path needs cubic elements"); return fail(SVL_ERR_UNSUPPORTED);
+        }
+        if (h->np > 0) {
+            // explicit scheme tables of this instance (lumped blocks, solves)
+            LoadTables lt;
+            if ((st = build_load_tables(m, loads ? &loads[b] : nullptr, lt))) return fail(st);
+            ExplicitPmlTables T;
+            if ((st = explicit_pml_tables(m, opts->dt, opts->mtol, lt, T))) return fail(st);
+            const double dt = opts->dt;
+            static const int pk[9][2] = {{0, 0}, {1, 1}, {2, 2}, {0, 1}, {1, 2}, {0, 2}, {3, 3}, {4, 4}, {5, 5}};
+            for (long long n = 0; n < h->nn; ++n) {
+                const int pn = pidx[n];
+                if (pn < 0) continue;
+                const int t0 = m.tdof_all[(size_t)n * m.dstride];
+                float u6[6];
+                for (int c = 0; c < 3; ++c) {
+                    const int f = m.fdof_all[(size_t)n * m.dstride + c];
+                    u6[c] = f >= 0 ? (float)T.kinv[f] : 0.f;
+                    if (T.Mu[t0 + c] != T.Mu[t0] || T.Ku[t0 + c] != T.Ku[t0] || T.Gu[t0 + c] != T.Gu[t0] || T.Cu[t0 + c] != T.Cu[t0]) {
+                        set_error("instance %d: PML node %lld has unequal lumped blocks per component", b, n); return fail(SVL_ERR_UNSUPPORTED);
+                    }
+                    if (f < -1) { set_error("instance %d: constraints are not supported on the structured path", b); return fail(SVL_ERR_UNSUPPORTED); }
+                }
+                u6[3] = (float)(1.0 / dt / dt * T.Mu[t0] - 1.0 / 2.0 / dt * T.Cu[t0]);
+                u6[4] = (float)T.Ku[t0];
+                u6[5] = (float)T.Gu[t0];
+                uc.insert(uc.end(), u6, u6 + 6);
+                const int sn = T.snode_of[n];
+                const double* Ms = &T.Ms[(size_t)sn * 36];
+                const double* Cs = &T.Cs[(size_t)sn * 36];
+                const double* Ks = &T.Ks[(size_t)sn * 36];
+                const double* Gs = &T.Gs[(size_t)sn * 36];
+                const double* Di = &T.Dinv[(size_t)sn * 36];
+                float blk[36];
+                for (int k2 = 0; k2 < 9; ++k2) {
+                    const int i = pk[k2][0] * 6 + pk[k2][1];
+                    blk[k2] = (float)Di[i];
+                    blk[9 + k2] = (float)(Ms[i] / dt / dt - Cs[i] / 2.0 / dt);
+                    blk[18 + k2] = (float)(Ks[i] + dt / 2.0 * Gs[i]);
+                    blk[27 + k2] = (float)Gs[i];
+                }
+                scs.insert(scs.end(), blk, blk + 36);
+            }
+            for (int i = 0; i < h->npe; ++i) {
+                const double* pr = m.param(pelem[i]);
+                const double* pp = &m.pml_par[(size_t)pelem[i] * 9];
+                const double E = pr[0], nu = pr[1], rho = pr[2];
+                const double mu = E / 2.0 / (1 + nu), lambda = E * nu / (1.0 + nu) / (1.0 - 2.0 * nu);
+                const double Vp = std::sqrt((lambda + 2.0 * mu) / rho);
+                eb0.push_back((float)((pp[0] + 1.0) * Vp / 2.0 / pp[1] * std::log(1.0 / pp[2])));
+            }
+        }
         if (b == 0) {
             // reference matrices of the (uniform) element: K = lambda K_lambda + mu K_mu
             for (int q = 0; q < 8; ++q) {
@@ -808,16 +1289,25 @@ int svl_cdx_create(const svl_grid_spec* g, int32_t ninst, const svl_model_desc* 
             const double E = pr[0], nu = pr[1];
             const int ex = e % h->nx, ey = (e / h->nx) % h->ny, ez = e / (h->nx * h->ny);
             const size_t li = (size_t)b * lm_per + ((size_t)ez * h->ny + ey) * h->pe + ex;
-            lam[li] = (float)(E * nu / (1.0 - 2.0 * nu) / (1.0 + nu));
-            mu[li] = (float)(E / (2.0 * (1.0 + nu)));
+            const bool pml_e = m.has_pml() && m.epml[e];      // PML elements: no elastic force here
+            lam[li] = pml_e ? 0.f : (float)(E * nu / (1.0 - 2.0 * nu) / (1.0 + nu));
+            mu[li] = pml_e ? 0.f : (float)(E / (2.0 * (1.0 + nu)));
         }
         std::vector<double> M;
         lumped_mass_diag(m, opts->mtol, M);
-        for (long long t = 0; t < h->ntotal; ++t) {
-            const bool fixed = m.fdof[t] < 0;
-            if (!fixed && !(M[t] > 0)) { set_error("instance %d: free dof %lld has no mass", b, t); return fail(SVL_ERR_INVALID); }
-            cdof[(size_t)b * per + h->pad_index[t]] = fixed ? 0.0f : (float)(dt2 / M[t]);
-        }
+        for (long long n = 0; n < h->nn; ++n)
+            for (int c = 0; c < 3; ++c) {
+                const long long t = m.tdof_all[(size_t)n * m.dstride + c];
+                const int f = m.fdof_all[(size_t)n * m.dstride + c];
+                float cd;
+                if (pidx[n] >= 0) cd = -1.0f;                 // updated by the PML kernels
+                else {
+                    const bool fixed = f < 0;
+                    if (!fixed && !(M[t] > 0)) { set_error("instance %d: free dof %lld has no mass", b, t); return fail(SVL_ERR_INVALID); }
+                    cd = fixed ? 0.0f : (float)(dt2 / M[t]);
+                }
+                cdof[(size_t)b * per + h->pad_index[t]] = cd;
+            }
         if (loads) {
             const svl_load_desc& L = loads[b];
             if (L.ndrm > 0) { set_error("instance %d: domain-reduction loads are served by svl_cd_create", b); return fail(SVL_ERR_UNSUPPORTED); }
@@ -832,6 +1322,10 @@ int svl_cdx_create(const svl_grid_spec* g, int32_t ninst, const svl_model_desc* 
             for (int i2 = 0; i2 < L.nforce; ++i2) {
                 if (L.force_dof[i2] < 0 || L.force_dof[i2] >= h->ntotal || L.force_series[i2] < 0 || L.force_series[i2] >= L.nseries) {
                     set_error("instance %d: load entry %d out of range", b, i2); return fail(SVL_ERR_INVALID);
+                }
+                if (h->pad_index[L.force_dof[i2]] < 0 || pidx[t2node[L.force_dof[i2]]] >= 0) {
+                    set_error("instance %d: load entry %d is on a PML node (not covered on the structured path)", b, i2);
+                    return fail(SVL_ERR_UNSUPPORTED);
                 }
                 fdof.push_back((long long)b * h->ntotal + L.force_dof[i2]);
                 fser.push_back(soff + L.force_series[i2]);
@@ -855,7 +1349,7 @@ int svl_cdx_create(const svl_grid_spec* g, int32_t ninst, const svl_model_desc* 
     std::vector<int> order(fdof.size());
     for (size_t i2 = 0; i2 < order.size(); ++i2) order[i2] = (int)i2;
     auto tile_of = [&](long long gdof) {
-        const long long b = gdof / h->ntotal, t = gdof % h->ntotal, n = t / 3;
+        const long long b = gdof / h->ntotal, t = gdof % h->ntotal, n = t2node[t];
         const long long x = n % nxn, y = (n / nxn) % nyn, z = n / ((long long)nxn * nyn);
         return (((b * h->ntz + z / TZ) * h->nty + y / TY) * h->ntx + x / TX);
     };
@@ -889,8 +1383,21 @@ int svl_cdx_create(const svl_grid_spec* g, int32_t ninst, const svl_model_desc* 
         (st = h->upload(mu, &h->mu)) || (st = h->upload(cdof, &h->cdof)) || (st = h->upload(bop, &h->bop)) ||
         (st = h->alloc(1, &h->status)) || (st = h->upload(tl_ptr, &h->tl_ptr)) || (st = h->upload(ld_dof, &h->ld_dof)) ||
         (st = h->upload(ld_ptr, &h->ld_ptr)) || (st = h->upload(ld_ser, &h->ld_ser)) || (st = h->upload(ld_coef, &h->ld_coef)) ||
-        (st = h->upload(s_ptr, &h->s_ptr)) || (st = h->upload(s_val, &h->s_val)))
+        (st = h->upload(s_ptr, &h->s_ptr)) || (st = h->upload(s_val, &h->s_val)) ||
+        (st = h->upload(h->pad_index, &h->d_omap)))
         return fail(st);
+    if (h->np > 0) {
+        const size_t n6 = (size_t)ninst * h->np * 6, n3 = (size_t)ninst * h->np * 3;
+        if ((st = h->alloc(ns, &h->fsol)) || (st = h->alloc(n6, &h->sh[0])) || (st = h->alloc(n6, &h->sh[1])) ||
+            (st = h->alloc(n6, &h->sl[0])) || (st = h->alloc(n6, &h->sl[1])) || (st = h->alloc(n6, &h->sbh)) ||
+            (st = h->alloc(n6, &h->sbl)) || (st = h->alloc(n3, &h->ubh)) || (st = h->alloc(n3, &h->ubl)) ||
+            (st = h->alloc((size_t)ninst * h->np * 9, &h->vin)) ||
+            (st = h->alloc((size_t)ninst * h->npe * 24, &h->feu)) || (st = h->alloc((size_t)ninst * h->npe * 48, &h->fes)) ||
+            (st = h->upload(uc, &h->uc)) || (st = h->upload(scs, &h->scs)) || (st = h->upload(egeo, &h->egeo)) ||
+            (st = h->upload(eb0, &h->eb0)) || (st = h->upload(enode, &h->enode)) || (st = h->upload(ninv, &h->ninv)) ||
+            (st = h->upload(npad, &h->npad)))
+            return fail(st);
+    }
     if ((st = make_map(h->uh[0], h->pitch, nyn, nzn, ninst, RAWX, HY, HZ, &h->tmap[0])) ||
         (st = make_map(h->uh[1], h->pitch, nyn, nzn, ninst, RAWX, HY, HZ, &h->tmap[1])) ||
         (st = make_map(h->lam, h->pe, h->ny, h->nz, ninst, LMX, EY, EZ, &h->tmap_lam)) ||
@@ -917,10 +1424,18 @@ int svl_cdx_set_initial(svl_cdx* h, int32_t inst, const double* U0, const double
     if (!h || inst < 0 || inst >= h->ninst) { set_error("bad handle or instance"); return SVL_ERR_INVALID; }
     const size_t per = (size_t)(h->nstate / h->ninst);
     std::vector<float> hi(per, 0.f), lo(per, 0.f), phi(per, 0.f), plo(per, 0.f);
+    const size_t n6 = (size_t)h->np * 6;
+    std::vector<float> shi(n6, 0.f), slo(n6, 0.f), sphi(n6, 0.f), splo(n6, 0.f);
     for (long long t = 0; t < h->ntotal; ++t) {
         const double u = U0 ? U0[t] : 0.0, vv = V0 ? V0[t] : 0.0, a = A0 ? A0[t] : 0.0;
         const double up = u - h->dt * vv + h->dt * h->dt / 2.0 * a;
         const long long p = h->pad_index[t];
+        if (p < 0) {                               // stress dof of a PML node
+            const size_t k = (size_t)(-p - 1);
+            split_pair(u, shi[k], slo[k]);
+            split_pair(up, sphi[k], splo[k]);
+            continue;
+        }
         split_pair(u, hi[p], lo[p]);
         split_pair(up, phi[p], plo[p]);
     }
@@ -929,6 +1444,17 @@ int svl_cdx_set_initial(svl_cdx* h, int32_t inst, const double* U0, const double
     CUDA_TRY(cudaMemcpyAsync(h->ul[h->cur] + off, lo.data(), per * 4, cudaMemcpyHostToDevice, h->stream));
     CUDA_TRY(cudaMemcpyAsync(h->uh[1 - h->cur] + off, phi.data(), per * 4, cudaMemcpyHostToDevice, h->stream));
     CUDA_TRY(cudaMemcpyAsync(h->ul[1 - h->cur] + off, plo.data(), per * 4, cudaMemcpyHostToDevice, h->stream));
+    if (h->np > 0) {
+        const size_t o6 = (size_t)inst * n6;
+        CUDA_TRY(cudaMemcpyAsync(h->sh[h->cur] + o6, shi.data(), n6 * 4, cudaMemcpyHostToDevice, h->stream));
+        CUDA_TRY(cudaMemcpyAsync(h->sl[h->cur] + o6, slo.data(), n6 * 4, cudaMemcpyHostToDevice, h->stream));
+        CUDA_TRY(cudaMemcpyAsync(h->sh[1 - h->cur] + o6, sphi.data(), n6 * 4, cudaMemcpyHostToDevice, h->stream));
+        CUDA_TRY(cudaMemcpyAsync(h->sl[1 - h->cur] + o6, splo.data(), n6 * 4, cudaMemcpyHostToDevice, h->stream));
+        CUDA_TRY(cudaMemsetAsync(h->sbh + o6, 0, n6 * 4, h->stream));
+        CUDA_TRY(cudaMemsetAsync(h->sbl + o6, 0, n6 * 4, h->stream));
+        CUDA_TRY(cudaMemsetAsync(h->ubh + (size_t)inst * h->np * 3, 0, (size_t)h->np * 12, h->stream));
+        CUDA_TRY(cudaMemsetAsync(h->ubl + (size_t)inst * h->np * 3, 0, (size_t)h->np * 12, h->stream));
+    }
     CUDA_TRY(cudaStreamSynchronize(h->stream));
     h->va_valid = false;
     return SVL_OK;
@@ -944,6 +1470,7 @@ static int cdx_step(svl_cdx* h, int k, bool want_va) {
     v.s_ptr = h->s_ptr; v.s_val = h->s_val;
     v.k = k;
     v.status = h->status;
+    v.fsol = h->fsol;
     const size_t ns = (size_t)h->nstate;
     if (want_va) {
         CUDA_TRY(cudaMemcpyAsync(h->ph_copy, v.uh_prev, ns * 4, cudaMemcpyDeviceToDevice, h->stream));
@@ -952,6 +1479,26 @@ static int cdx_step(svl_cdx* h, int k, bool want_va) {
     k_cdx_step<<<h->grid, NTHREADS, SMEM_BYTES, h->stream>>>(h->tmap[h->cur], h->tmap_lam, h->tmap_mu, h->own_ul[h->cur],
                                                              h->own_uh[1 - h->cur], h->own_ul[1 - h->cur], h->own_cd, v);
     ++h->launches;
+    if (h->np > 0) {
+        // the PML band: coupling forces and updates of the PML nodes
+        CdpView c{};
+        c.ninst = h->ninst; c.np = h->np; c.npe = h->npe;
+        c.h = (float)h->hgrid; c.dt = (float)h->dt;
+        c.per = (long long)(h->nstate / h->ninst);
+        c.enode = h->enode; c.egeo = h->egeo; c.eb0 = h->eb0; c.ninv = h->ninv; c.npad = h->npad;
+        c.uc = h->uc; c.scs = h->scs;
+        c.uh = h->uh[h->cur]; c.ul = h->ul[h->cur]; c.uph = v.uh_prev; c.upl = v.ul_prev; c.fsol = h->fsol;
+        c.ubh = h->ubh; c.ubl = h->ubl;
+        c.sh = h->sh[h->cur]; c.sl = h->sl[h->cur]; c.sph = h->sh[1 - h->cur]; c.spl = h->sl[1 - h->cur];
+        c.sbh = h->sbh; c.sbl = h->sbl; c.vin = h->vin; c.feu = h->feu; c.fes = h->fes;
+        const long long ge = (long long)h->ninst * h->npe * 8, gn = (long long)h->ninst * h->np;
+        const unsigned be = (unsigned)((ge + CDP_THREADS - 1) / CDP_THREADS), bn = (unsigned)((gn + 255) / 256);
+        k_cdp_fu<<<be, CDP_THREADS, 0, h->stream>>>(c);
+        k_cdp_uu<<<bn, 256, 0, h->stream>>>(c);
+        k_cdp_fs<<<be, CDP_THREADS, 0, h->stream>>>(c);
+        k_cdp_su<<<bn, 256, 0, h->stream>>>(c);
+        h->launches += 4;
+    }
     if (want_va) {
         k_cdx_va<<<(unsigned)((ns + 255) / 256), 256, 0, h->stream>>>(v.uh_prev, v.ul_prev, h->uh[h->cur], h->ul[h->cur], h->ph_copy,
                                                                    h->pl_copy, h->V, h->A, (long long)ns,
@@ -980,8 +1527,8 @@ static int cdx_fill_chunk(svl_cdx* h, int k_first, int s0, int n, int nsteps, in
         const int s = s0 + i;
         TRY(cdx_step(h, k_first + s, s == nsteps - 1));
         k_cdx_hist<<<(unsigned)((per_step + 255) / 256), 256, 0, h->stream>>>(
-            h->uh[h->cur], h->ul[h->cur], h->hist[slot] + (size_t)i * per_step, h->ntotal, h->nx + 1, h->ny + 1, h->pitch,
-            h->nstate / h->ninst, h->ninst);
+            h->uh[h->cur], h->ul[h->cur], h->sh[h->cur], h->sl[h->cur], h->d_omap, h->hist[slot] + (size_t)i * per_step,
+            h->ntotal, h->nstate / h->ninst, (long long)h->np * 6, h->ninst);
         ++h->launches;
     }
     CUDA_TRY(cudaGetLastError());
@@ -1062,8 +1609,34 @@ int svl_cdx_run_timed(svl_cdx* h, int32_t k_first, int32_t nsteps, float* ms) {
 
 int svl_cdx_get(svl_cdx* h, int32_t inst, int32_t which, double* out) {
     if (!h || !out || inst < 0 || inst >= h->ninst) { set_error("bad argument"); return SVL_ERR_INVALID; }
-    if (which < 0 || which > 2) { set_error("which must be 0, 1 or 2"); return SVL_ERR_INVALID; }
-    if (which == 0) return fetch_pair(h, h->uh[h->cur], h->ul[h->cur], inst, out);
+    if (which < 0 || which > 3) { set_error("which must be 0, 1, 2 or 3"); return SVL_ERR_INVALID; }
+    if (which == 0) return fetch_pair(h, h->uh[h->cur], h->ul[h->cur], inst, out, h->sh[h->cur], h->sl[h->cur]);
+    if (which == 3) {                          // ubar / Sbar of the PML nodes, 0 elsewhere
+        const size_t n3 = (size_t)h->np * 3, n6 = (size_t)h->np * 6;
+        std::vector<float> bh(n3), bl(n3), Sh(n6), Sl(n6);
+        if (h->np > 0) {
+            CUDA_TRY(cudaMemcpyAsync(bh.data(), h->ubh + inst * n3, n3 * 4, cudaMemcpyDeviceToHost, h->stream));
+            CUDA_TRY(cudaMemcpyAsync(bl.data(), h->ubl + inst * n3, n3 * 4, cudaMemcpyDeviceToHost, h->stream));
+            CUDA_TRY(cudaMemcpyAsync(Sh.data(), h->sbh + inst * n6, n6 * 4, cudaMemcpyDeviceToHost, h->stream));
+            CUDA_TRY(cudaMemcpyAsync(Sl.data(), h->sbl + inst * n6, n6 * 4, cudaMemcpyDeviceToHost, h->stream));
+            CUDA_TRY(cudaStreamSynchronize(h->stream));
+        }
+        std::vector<long long> upos(h->nstate / h->ninst, -1);
+        std::vector<long long> npd;
+        if (h->np > 0) {
+            npd.resize(h->np);
+            CUDA_TRY(cudaMemcpy(npd.data(), h->npad, (size_t)h->np * 8, cudaMemcpyDeviceToHost));
+            for (int p2 = 0; p2 < h->np; ++p2) upos[npd[p2]] = p2;
+        }
+        for (long long t = 0; t < h->ntotal; ++t) {
+            const long long p = h->pad_index[t];
+            if (p < 0) { out[t] = (double)Sh[-p - 1] + (double)Sl[-p - 1]; continue; }
+            const long long c = (p % h->pitch) % 3;          // rows hold x*3 + c
+            const long long pn = upos[p - c];
+            out[t] = pn >= 0 ? (double)bh[pn * 3 + c] + (double)bl[pn * 3 + c] : 0.0;
+        }
+        return SVL_OK;
+    }
     if (!h->va_valid) { set_error("V/A are only available after svl_cdx_run"); return SVL_ERR_INVALID; }
     const size_t per = (size_t)(h->nstate / h->ninst);
     std::vector<double> tmp(per);

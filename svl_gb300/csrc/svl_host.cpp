@@ -392,6 +392,176 @@ void build_total_to_free(const HostModel& m, std::vector<int32_t>& ptr,
     }
 }
 
+// ---- explicit central difference with PML layers: host tables -------------
+// Row-sum lumped N N blocks of the PML element matrices M, C, K, G
+// (PML2DQuad4.cpp:233-470, PML3DHexa8.cpp:214-712: each block is a
+// stretching combination s times rho N N on the displacement dofs and times
+// -compliance N N on the stress dofs, so its row sum at node j is the Gauss
+// sum of s N_j w |J|), the solid elements' lumped mass with the mass
+// tolerance (and mass-proportional Rayleigh), the nodal masses, 1/(T^T d T)
+// on the displacement free dofs and per PML node the inverse of
+// Ms/dt^2 + Cs/2dt.  Element order throughout.
+int explicit_pml_tables(const HostModel& m, double dt, double mtol, const LoadTables& lt, ExplicitPmlTables& out) {
+    const int nd = m.ndim, nen = m.nen, pnd = m.pml_ndof(), ns = pnd - nd, npar = 3 + 2 * nd;
+    const int nt = m.ntotal;
+    std::vector<int8_t> sdof(nt, 0);
+    std::vector<int32_t> snode_of(m.nnode, -1), sfirst;
+    std::vector<char> pnode(m.nnode, 0);
+    std::vector<int> sol, pml;
+    for (int e = 0; e < m.nelem; ++e) ((m.has_pml() && m.epml[e]) ? pml : sol).push_back(e);
+    for (int e : pml)
+        for (int a = 0; a < nen; ++a) pnode[m.conn[(size_t)e * nen + a]] = 1;
+    for (int n = 0; n < m.nnode; ++n) {
+        if (!pnode[n]) continue;
+        const int t0 = m.tdof_all[(size_t)n * m.dstride + nd];
+        for (int j = 0; j < ns; ++j) {
+            const int t = m.tdof_all[(size_t)n * m.dstride + nd + j];
+            if (t != t0 + j) { set_error("explicit PML: the stress dofs of node %d are not consecutive", n); return SVL_ERR_UNSUPPORTED; }
+            if (m.fdof_all[(size_t)n * m.dstride + nd + j] < 0) {
+                set_error("explicit PML: node %d has a restrained or constrained stress dof", n); return SVL_ERR_UNSUPPORTED;
+            }
+            sdof[t] = 1;
+        }
+        snode_of[n] = (int32_t)sfirst.size();
+        sfirst.push_back(t0);
+    }
+    for (int t = 0; t < nt; ++t)
+        if (sdof[t] && lt.sm_ptr[t + 1] > lt.sm_ptr[t]) {
+            set_error("explicit PML: support motion on a stress dof (total dof %d)", t); return SVL_ERR_UNSUPPORTED;
+        }
+    const int nsn = (int)sfirst.size();
+    const size_t nb = (size_t)ns * ns;
+    std::vector<double> Mu(nt, 0.0), Cu(nt, 0.0), Ku(nt, 0.0), Gu(nt, 0.0);
+    std::vector<double> Bl[4];
+    for (auto& v : Bl) v.assign((size_t)nsn * nb, 0.0);
+    std::vector<int> sidx_of(m.nelem, -1), pidx_of(m.nelem, -1);
+    for (size_t i = 0; i < sol.size(); ++i) sidx_of[sol[i]] = (int)i;
+    for (size_t i = 0; i < pml.size(); ++i) pidx_of[pml[i]] = (int)i;
+    std::vector<double> ml;
+    element_lumped_masses(m, ml);                 // [(e nen + a) nd + j]
+    for (int e = 0; e < m.nelem; ++e) {
+        if (sidx_of[e] >= 0) {
+            const double am = m.ray.empty() ? 0.0 : m.ray[2 * (size_t)e];
+            for (int a = 0; a < nen; ++a)
+                for (int j = 0; j < nd; ++j) {
+                    const double v = ml[((size_t)e * nen + a) * nd + j];
+                    const int t = m.tdof_all[(size_t)m.conn[(size_t)e * nen + a] * m.dstride + j];
+                    if (std::fabs(v) > mtol) Mu[t] += v;
+                    if (am != 0.0 && std::fabs(am * v) > 1e-12) Cu[t] += am * v;
+                }
+            continue;
+        }
+        const double* pr = m.param(e);
+        const double E = pr[0], nu = pr[1], rho = pr[2];
+        const double mu = E / 2.0 / (1 + nu), lambda = E * nu / (1.0 + nu) / (1.0 - 2.0 * nu);
+        const double* par = &m.pml_par[(size_t)e * npar];
+        const double pm = par[0], L = par[1], R = par[2];
+        const double Vp = std::sqrt((lambda + 2.0 * mu) / rho);
+        const double a0 = (pm + 1.0) * (L / 10.0) / 2.0 / L * std::log(1.0 / R);
+        const double b0 = (pm + 1.0) * Vp / 2.0 / L * std::log(1.0 / R);
+        for (int q = 0; q < m.ngp; ++q) {
+            double dNx[8][3], N[8];
+            const double det = gp_geometry(m, e, q, dNx, N);
+            const double f = gp_factor(m, e, det);
+            double xg[3] = {0, 0, 0};
+            for (int a = 0; a < nen; ++a)
+                for (int i = 0; i < nd; ++i) xg[i] += N[a] * m.X[(size_t)m.conn[(size_t)e * nen + a] * nd + i];
+            double as[3] = {1, 1, 1}, bs[3] = {0, 0, 0};
+            for (int i = 0; i < nd; ++i) {
+                const double r = std::pow((xg[i] - par[3 + i]) * par[3 + nd + i] / L, pm);
+                as[i] = 1.0 + a0 * r;
+                bs[i] = b0 * r;
+            }
+            double sc[4];
+            if (nd == 2) {
+                sc[0] = as[0] * as[1]; sc[1] = as[0] * bs[1] + as[1] * bs[0]; sc[2] = bs[0] * bs[1]; sc[3] = 0.0;
+            } else {
+                sc[0] = as[0] * as[1] * as[2];
+                sc[1] = as[0] * as[1] * bs[2] + as[0] * bs[1] * as[2] + bs[0] * as[1] * as[2];
+                sc[2] = as[0] * bs[1] * bs[2] + bs[0] * bs[1] * as[2] + bs[0] * as[1] * bs[2];
+                sc[3] = bs[0] * bs[1] * bs[2];
+            }
+            std::vector<double>* du[4] = {&Mu, &Cu, &Ku, &Gu};
+            for (int w = 0; w < 4; ++w) {
+                const double sw = sc[w];
+                if (sw == 0.0) continue;
+                for (int j = 0; j < nen; ++j) {
+                    const int n = m.conn[(size_t)e * nen + j];
+                    const double Nf = N[j] * f;
+                    for (int c = 0; c < nd; ++c) (*du[w])[m.tdof_all[(size_t)n * m.dstride + c]] += rho * sw * Nf;
+                    double* B = &Bl[w][(size_t)snode_of[n] * nb];
+                    if (nd == 2) {
+                        const double k2 = sw * (lambda + 2.0 * mu) / 4.0 / mu / (lambda + mu);
+                        const double l2 = sw * lambda / 4.0 / mu / (lambda + mu);
+                        B[0 * 3 + 0] += -k2 * Nf; B[1 * 3 + 1] += -k2 * Nf;
+                        B[0 * 3 + 1] += l2 * Nf; B[1 * 3 + 0] += l2 * Nf;
+                        B[2 * 3 + 2] += -sw / mu * Nf;
+                    } else {
+                        const double kap = sw * (lambda + mu) / mu / (3.0 * lambda + 2.0 * mu);
+                        const double lam = sw * lambda / 2.0 / mu / (3.0 * lambda + 2.0 * mu);
+                        for (int r = 0; r < 3; ++r)
+                            for (int c = 0; c < 3; ++c) B[r * 6 + c] += (r == c ? -kap : lam) * Nf;
+                        for (int r = 3; r < 6; ++r) B[r * 6 + r] += -sw / mu * Nf;
+                    }
+                }
+            }
+        }
+    }
+    if (!m.nodemass.empty())
+        for (int t = 0; t < nt; ++t) if (std::fabs(m.nodemass[t]) > mtol) Mu[t] += m.nodemass[t];
+    std::vector<int32_t> Tp, Tc;
+    std::vector<double> Tv;
+    build_total_to_free(m, Tp, Tc, Tv);
+    // T^T (Mu/dt^2 + Cu/2dt) T: diagonal when every constrained displacement
+    // dof has one master (the EQUAL ties of mergeDomain)
+    std::vector<double> kf(std::max(m.nfree, 1), 0.0), kinv(std::max(m.nfree, 1), 0.0);
+    std::vector<char> sfree(std::max(m.nfree, 1), 0);
+    for (int t = 0; t < nt; ++t) {
+        if (sdof[t]) { for (int i = Tp[t]; i < Tp[t + 1]; ++i) sfree[Tc[i]] = 1; continue; }
+        if (Tp[t + 1] - Tp[t] > 1) {
+            set_error("explicit PML: total dof %d is constrained to more than one master (no diagonal solve)", t);
+            return SVL_ERR_UNSUPPORTED;
+        }
+        const double d = 1.0 / dt / dt * Mu[t] + 1.0 / 2.0 / dt * Cu[t];
+        for (int i = Tp[t]; i < Tp[t + 1]; ++i) kf[Tc[i]] += Tv[i] * d * Tv[i];
+    }
+    for (int f = 0; f < m.nfree; ++f) {
+        if (sfree[f]) continue;
+        if (!(kf[f] > 0.0)) { set_error("explicit PML: free displacement dof %d has no mass", f); return SVL_ERR_INVALID; }
+        kinv[f] = 1.0 / kf[f];
+    }
+    std::vector<double> Dinv((size_t)nsn * nb, 0.0);
+    for (int i = 0; i < nsn; ++i) {
+        double A_[36], B[36];
+        for (size_t k = 0; k < nb; ++k) { A_[k] = Bl[0][(size_t)i * nb + k] / dt / dt + Bl[1][(size_t)i * nb + k] / 2.0 / dt; B[k] = 0.0; }
+        for (int r = 0; r < ns; ++r) B[r * ns + r] = 1.0;
+        for (int c = 0; c < ns; ++c) {                   // Gauss-Jordan, partial pivoting
+            int pv = c;
+            for (int r = c + 1; r < ns; ++r) if (std::fabs(A_[r * ns + c]) > std::fabs(A_[pv * ns + c])) pv = r;
+            if (!(std::fabs(A_[pv * ns + c]) > 0.0)) { set_error("explicit PML: singular stress block at PML node %d", i); return SVL_ERR_INVALID; }
+            if (pv != c) for (int j = 0; j < ns; ++j) { std::swap(A_[pv * ns + j], A_[c * ns + j]); std::swap(B[pv * ns + j], B[c * ns + j]); }
+            const double piv = A_[c * ns + c];
+            for (int j = 0; j < ns; ++j) { A_[c * ns + j] /= piv; B[c * ns + j] /= piv; }
+            for (int r = 0; r < ns; ++r) {
+                if (r == c) continue;
+                const double fr = A_[r * ns + c];
+                if (fr == 0.0) continue;
+                for (int j = 0; j < ns; ++j) { A_[r * ns + j] -= fr * A_[c * ns + j]; B[r * ns + j] -= fr * B[c * ns + j]; }
+            }
+        }
+        for (size_t k = 0; k < nb; ++k) Dinv[(size_t)i * nb + k] = B[k];
+    }
+    out.sdof = std::move(sdof);
+    out.sfirst = std::move(sfirst);
+    out.snode_of = std::move(snode_of);
+    out.Mu = std::move(Mu); out.Cu = std::move(Cu); out.Ku = std::move(Ku); out.Gu = std::move(Gu);
+    out.Ms = std::move(Bl[0]); out.Cs = std::move(Bl[1]); out.Ks = std::move(Bl[2]); out.Gs = std::move(Bl[3]);
+    out.Dinv = std::move(Dinv);
+    out.kinv = std::move(kinv);
+    out.ns = ns;
+    return SVL_OK;
+}
+
 }  // namespace svl
 
 using namespace svl;

@@ -106,6 +106,21 @@ struct LoadTables {
 // Returns SVL_OK or an error code with svl_last_error set.
 int build_load_tables(const HostModel& m, const svl_load_desc* L, LoadTables& out);
 
+// Tables of the explicit central difference with PML layers (see
+// explicit_pml_tables in svl_host.cpp): per total dof the stress-dof flag and
+// the lumped diagonals of the displacement rows; per free dof 1/(T^T d T)
+// (0 on stress dofs); per PML node (in node order) the first total dof of its
+// stress block and the ns x ns lumped blocks and the inverse of
+// Ms/dt^2 + Cs/2dt; snode_of[n] is the PML node index of node n or -1.
+struct ExplicitPmlTables {
+    int ns = 0;
+    std::vector<int8_t> sdof;
+    std::vector<int32_t> sfirst, snode_of;
+    std::vector<double> Mu, Cu, Ku, Gu, kinv;
+    std::vector<double> Ms, Cs, Ks, Gs, Dinv;
+};
+int explicit_pml_tables(const HostModel& m, double dt, double mtol, const LoadTables& lt, ExplicitPmlTables& out);
+
 // PML element action y_e = coef_M M u_M + coef_C C u_C + coef_K K u_K + coef_G G u_G
 // (PML2DQuad4 / PML3DHexa8), one thread per element; see svl_pml.cu.
 struct PmlArgs {

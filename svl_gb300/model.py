@@ -277,11 +277,13 @@ class Loads:
                 self.force_coef.append(factor * float(v))
 
     def add_body_load(self, model: Model, elems: Sequence[int], direction: Sequence[float], series: int,
-                      factor: float = 1.0):
-        """Element body load (Assembler.cpp:439-459) resolved to dof entries."""
+                      factor: float = 1.0, element_force=None):
+        """Element body load (Assembler.cpp:439-459) resolved to dof entries.
+        element_force(e, direction) -> nodal vector of one element (default
+        Model.body_force, the library's svl_element_body_force)."""
         nen = model.conn.shape[1]
         for e in elems:
-            fe = model.body_force(int(e), direction)
+            fe = (element_force or model.body_force)(int(e), direction)
             for a in range(nen):
                 for j in range(model.ndim):
                     v = fe[a * model.ndim + j]

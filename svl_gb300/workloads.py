@@ -7,8 +7,11 @@ benchmark configurations (no reference data is used):
 * config2: 128 x 128 x 64 lin3DHexa8 box, h = 2 m, Vs log-normal (mean 400,
   COV 0.2, exponential correlation 20 m), nu = 0.3, rho = 2100,
   double-couple-like body force (four element groups) with a Ricker
-  f0 = 3 Hz, dt = 0.5 h / max Vp.  Boundary: fixed bottom, rollers on the
-  sides (the PML layers of the configuration are not built yet).
+  f0 = 3 Hz, dt = 0.5 h / max Vp.  config2_pml: the configuration as
+  specified, whose outer 10 element layers on the four sides and the bottom
+  are PML3DHexa8 (9 dofs at their nodes, the pre-processor's reference points
+  and normals, the outer PML boundary fixed in displacement); config2: the
+  same box with a fixed bottom and roller sides instead of the PML band.
 * config3: an ensemble of 2D plane-strain soil columns, 10 lin2DQuad4
   elements wide, heights uniform in [50, 400] elements of 0.5 m (seeded),
   PlasticPlaneStrainJ2 (G = rho Vs^2 with Vs uniform in [150, 500] m/s,
@@ -340,4 +343,104 @@ def config5_pml(nx=128, ny=128, nz=64, npml=10, n_j2=16, nt=301, seed=0, h=2.0, 
         L.force_dof.append(int(tdof[n, 0]))
         L.force_series.append(s)
         L.force_coef.append(2.0 * rho * vs_el * h * h)
+    return m, L, dt
+
+
+def grid_nodes_conn(ne, h):
+    """Node coordinates (x fastest) and lin3DHexa8 connectivity of an
+    nx x ny x nz box (PP/Method/Builder.py makeDomainVolume: nodes x-fastest,
+    element nodes n1..n8 as Builder.py:167-183), in numpy."""
+    nx, ny, nz = ne
+    i, j, k = np.meshgrid(np.arange(nx + 1), np.arange(ny + 1), np.arange(nz + 1), indexing="ij")
+    X = np.stack([i.transpose(2, 1, 0).ravel() * h, j.transpose(2, 1, 0).ravel() * h,
+                  k.transpose(2, 1, 0).ravel() * h], axis=1).astype(np.float64)
+    ei, ej, ek = np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing="ij")
+    ei, ej, ek = (a.transpose(2, 1, 0).ravel() for a in (ei, ej, ek))
+    layer = (nx + 1) * (ny + 1)
+    n1 = layer * ek + ej * (nx + 1) + ei
+    conn = np.stack([n1, n1 + 1, n1 + 1 + (nx + 1), n1 + (nx + 1),
+                     n1 + layer, n1 + layer + 1, n1 + layer + 1 + (nx + 1), n1 + layer + (nx + 1)], axis=1)
+    return X, conn.astype(np.int32)
+
+
+def pml_attributes(ne, h, npml):
+    """PML3DHexa8 parameters of the outer `npml` element layers on the four
+    sides and the bottom of an nx x ny x nz box, as the pre-processor's
+    setPMLattributes writes them (PP/Method/Builder.py:804-901): the
+    reference point x0 is the corner, edge or face point of the inner box the
+    element lies beyond, and the normal npml the unit vector towards the
+    element (1/sqrt(2), 1/sqrt(3) components at edges and corners).  Returns
+    the PML flag [nelem] and the parameter rows [nelem, 9] = m (set by the
+    caller), L, R (set by the caller), x0[3], npml[3]."""
+    nx, ny, nz = ne
+    e = np.arange(nx * ny * nz)
+    ix, iy, iz = e % nx, (e // nx) % ny, e // (nx * ny)
+    side = np.zeros((e.size, 3), np.int64)          # -1 below / 0 inside / +1 above, per direction
+    side[ix < npml, 0] = -1
+    side[ix >= nx - npml, 0] = 1
+    side[iy < npml, 1] = -1
+    side[iy >= ny - npml, 1] = 1
+    side[iz < npml, 2] = -1
+    epml = np.any(side != 0, axis=1).astype(np.int32)
+    lo = np.array([npml * h, npml * h, npml * h])
+    hi = np.array([(nx - npml) * h, (ny - npml) * h, np.inf])
+    ctr = np.array([nx * h / 2.0, ny * h / 2.0, (nz * h + npml * h) / 2.0])
+    par = np.zeros((e.size, 9))
+    cnt = np.sum(side != 0, axis=1)
+    for d in range(3):
+        x0 = np.where(side[:, d] < 0, lo[d], np.where(side[:, d] > 0, hi[d], ctr[d]))
+        par[:, 3 + d] = x0
+        par[:, 6 + d] = np.where(cnt > 0, side[:, d] / np.sqrt(np.maximum(cnt, 1)), 0.0)
+    par[epml == 0] = 0.0
+    return epml, par
+
+
+def config2_pml(nx=128, ny=128, nz=64, npml=10, nt=4001, seed=0, amp=1.0e3, pml_m=2.0, pml_R=1.0e-6,
+                element_force=None):
+    """Config 2 as specified: the config2 box and source with its outer `npml`
+    element layers on the four sides and the bottom PML3DHexa8 (m = pml_m,
+    L = npml h, R = pml_R; the log-normal Vs field everywhere), 9 dofs at the
+    nodes of PML elements and 3 elsewhere (node-by-node PlainScheme order),
+    the outer PML boundary fixed in displacement, the top free.  Built in
+    numpy (element_force: the element body-force routine, default the
+    library's)."""
+    h, rho, nu = 2.0, 2100.0, 0.3
+    vs = lognormal_field((nx, ny, nz), h, 400.0, 0.2, 20.0, seed)
+    vs_e = np.transpose(vs, (2, 1, 0)).reshape(-1)
+    ne = nx * ny * nz
+    G = rho * vs_e ** 2
+    E = 2 * G * (1 + nu)
+    mp = np.zeros((ne, 8))
+    mp[:, 0], mp[:, 1], mp[:, 2] = E, nu, rho
+    X, conn = grid_nodes_conn((nx, ny, nz), h)
+    epml, par = pml_attributes((nx, ny, nz), h, npml)
+    par[epml == 1, 0], par[epml == 1, 1], par[epml == 1, 2] = pml_m, npml * h, pml_R
+    nn = X.shape[0]
+    pnode = np.zeros(nn, bool)
+    pnode[conn[epml == 1].ravel()] = True
+    ndof_n = np.where(pnode, 9, 3).astype(np.int32)
+    outer = (np.isclose(X[:, 0], 0.0) | np.isclose(X[:, 0], nx * h) | np.isclose(X[:, 1], 0.0)
+             | np.isclose(X[:, 1], ny * h) | np.isclose(X[:, 2], 0.0))
+    j = np.arange(9)[None, :]
+    has = j < ndof_n[:, None]
+    off = np.concatenate([[0], np.cumsum(ndof_n)[:-1]]).astype(np.int64)
+    tdof = np.where(has, off[:, None] + j, -1).astype(np.int32)
+    free = has & ~(outer[:, None] & (j < 3))
+    fdof = np.full((nn, 9), -1, np.int64)
+    fdof[free] = np.arange(int(free.sum()))
+    m = Model(ndim=3, coords=X, totaldof=tdof, freedof=fdof.astype(np.int32), conn=conn,
+              elem_type=capi.SVL_ELEM_LIN3DHEXA8, elem_mat=np.arange(ne, dtype=np.int32),
+              mat_type=np.full(ne, capi.SVL_MAT_ELASTIC3DLINEAR, np.int32), mat_param=mp, lumped=True,
+              node_ndof=ndof_n, elem_pml=epml, pml_param=par, grid_shape=(nx, ny, nz))
+    vp_max = np.sqrt(E.max() * (1 - nu) / ((1 + nu) * (1 - 2 * nu)) / rho)
+    dt = 0.5 * h / vp_max
+    L = Loads()
+    s = L.add_series(ricker(nt, dt, 3.0, amp=1.0))
+    cx, cy, cz = nx // 2, ny // 2, (nz + npml) // 2
+
+    def eid(i, j, k):
+        return (k * ny + j) * nx + i
+    for e, d in ((eid(cx, cy + 1, cz), (amp, 0.0, 0.0)), (eid(cx, cy - 1, cz), (-amp, 0.0, 0.0)),
+                 (eid(cx + 1, cy, cz), (0.0, amp, 0.0)), (eid(cx - 1, cy, cz), (0.0, -amp, 0.0))):
+        L.add_body_load(m, [e], d, s, element_force=element_force)
     return m, L, dt

@@ -48,7 +48,8 @@ def test_explicit_pml_matches_oracle(gpu, ndim):
     assert rel_l2(hg[:, u], ho[:, u]) <= TOL
     assert rel_l2(hg[:, s], ho[:, s]) <= TOL
     assert rel_l2(Vg[u], Vo[u]) <= 1e-10 and rel_l2(Ag[u], Ao[u]) <= 1e-9
-    assert rel_l2(Ubg, Ubo) <= TOL
+    # the PML history integral sums every step's rounding: 1e-11
+    assert rel_l2(Ubg, Ubo) <= 1e-11
 
 
 def test_explicit_pml_with_j2_layers_matches_oracle(gpu):
