@@ -1,27 +1,34 @@
 #!/usr/bin/env python3
 """Benchmark of the explicit central-difference hot path (DOF-steps/s).
 
-A "step" is one time step of the whole batch: element forces, the ordered
-node gather, the diagonal solve and the state update.  Default workload: the
-3D configuration (lin3DHexa8 128 x 128 x 64, h = 2 m, log-normal Vs field,
-double-couple body force), as a batch of 4 seeded realisations advanced by
-the mixed-precision path (tensor-core TF32 hi/lo element forces, compensated
-FP32-pair state update); the FP64
-plain path is timed on one realisation beside it, and the mixed result's
-error against it is reported.  The PML layers of that configuration are not
-built yet; the box has fixed/roller faces instead (stated in the config).
+A "step" is one time step of the whole batch.  Default workload: the 3D
+configuration as specified -- lin3DHexa8 128 x 128 x 64, h = 2 m, log-normal
+Vs field (mean 400 m/s, COV 0.2, exponential correlation 20 m), nu = 0.3,
+rho = 2100, double-couple body force (Ricker 3 Hz), dt = 0.5 h / max Vp, with
+10-element PML3DHexa8 layers on the four sides and the bottom (9 dofs at
+their nodes) advanced by the library's explicit PML scheme -- as a batch of 4
+seeded realisations on the mixed-precision path: the elastic interior by the
+tcgen05 tensor-core step (TF32 hi/lo element forces, FP32 accumulation), the
+PML band by FP32 kernels, the state as compensated FP32 pairs ("tf32x3+f32x2").
+The FP64 plain path (the same scheme in FP64 on the general handle) is timed
+on one realisation beside it, with the mixed result's error against it.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--precision mixed|fp64] [--instances B] [--workload config2|config1|config3]
+                    [--precision mixed|fp64] [--instances B]
+                    [--workload config2|config2_box|config1|config3]
 
-value   : free DOF x instances x steps / device time of the K steps (CUDA
-          events on the library's stream, inputs resident in HBM, working
-          set > L2: 4 instances hold ~300 MB of state).
-e2e     : the same metric through the C ABI with host buffers: model arrays
-          copied in by the create call and every instance's full displacement
-          field copied back to a host buffer after every step.
-roofline: algorithmic bytes of one step (37 B per free DOF for H8, 40 for
-          Q4) over the measured step time, against MEASURED_PEAKS.json.
+value   : free displacement DOF x instances x steps / device time of the K
+          steps (CUDA events on the library's stream, inputs resident in HBM,
+          working set ~1.9 GB > L2, no flush needed).
+e2e     : the same metric through the C ABI with host buffers: handle creation
+          from the host model arrays, then the configured run length with every
+          instance's full total-dof vector copied to a page-locked host buffer
+          after every step.
+roofline: the dominant kernel's algorithmic bytes over its own device time
+          (per-kernel CUDA events), against MEASURED_PEAKS.json.
+reference arm (--impl reference): the CPU oracle of the same scheme on the
+          box's host cores, on the same workload and instance count (a bounded
+          sample of steps), built without the product library.
 """
 from __future__ import annotations
 
@@ -39,18 +46,11 @@ import numpy as np
 
 ROOT = Path(__file__).resolve().parent
 
-# DRAM bytes (read + write) per free DOF of one k_cdx_step launch on the
-# lin3DHexa8 128x128x64 workload, from an ncu capture (dram__bytes_read.sum,
-# dram__bytes_write.sum) of the 2-instance case: 148.05 MB read + 20.07 MB
-# written per launch over 6 324 096 free DOF.  Part of the state written by one step is
-# still in L2 when the next step reads it, so this is below the 37 B/DOF of
-# algorithmic traffic.
-DRAM_BYTES_PER_DOF_STEP_MIXED_H8 = 26.585
 sys.path.insert(0, str(ROOT))
 
 ALGO_BYTES_PER_DOF = {2: 40.0, 3: 37.0}
 # steps of the end-to-end run per workload (the configured run lengths)
-E2E_STEPS = {"config1": 2000, "config2": 4000, "config3": 4000}
+E2E_STEPS = {"config1": 2000, "config2": 4000, "config2_box": 4000, "config3": 4000}
 # plane-strain J2 state read + written per element and step: 2 x 9 doubles x 4 Gauss points
 J2_STATE_BYTES_PER_ELEMENT = 576.0
 
@@ -64,60 +64,113 @@ def measured_peaks():
 
 
 class ClockSampler:
-    """nvidia-smi clocks/throttle sampling during the timed region."""
+    """SM clock and clock-event reasons sampled DURING the timed region, read
+    in-process through NVML (libnvidia-ml, read-only queries) every 2 ms on a
+    helper thread; falls back to `nvidia-smi -lms 20` when NVML cannot be
+    loaded.  Nothing is set."""
+
+    # clock-event reason bits of nvmlDeviceGetCurrentClocksEventReasons
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown", 0x40: "hw_thermal_slowdown",
+               0x80: "hw_power_brake_slowdown"}
 
     def __init__(self, gpu_index=0):
-        self.proc = None
-        self.path = None
         self.gpu = gpu_index
+        self.samples = []
+        self.max_mhz = None
+        self._stop = False
+        self._thread = None
+        self._proc = None
+        self._path = None
+        self._nvml = None
+
+    def _nvml_handle(self):
+        import ctypes as C
+        nv = C.CDLL("libnvidia-ml.so.1")
+        if nv.nvmlInit_v2() != 0:
+            raise RuntimeError("nvmlInit failed")
+        h = C.c_void_p()
+        bus = None
+        try:
+            import torch
+            pr = torch.cuda.get_device_properties(self.gpu)
+            bus = ("%08x:%02x:%02x.0" % (pr.pci_domain_id, pr.pci_bus_id, pr.pci_device_id)).encode()
+        except Exception:
+            bus = None
+        if bus is None or nv.nvmlDeviceGetHandleByPciBusId_v2(bus, C.byref(h)) != 0:
+            if nv.nvmlDeviceGetHandleByIndex_v2(self.gpu, C.byref(h)) != 0:
+                raise RuntimeError("no NVML handle")
+        mx = C.c_uint()
+        if nv.nvmlDeviceGetMaxClockInfo(h, 1, C.byref(mx)) == 0:          # NVML_CLOCK_SM
+            self.max_mhz = float(mx.value)
+        return nv, h
+
+    def _loop(self):
+        import ctypes as C
+        nv, h = self._nvml
+        clk, rs = C.c_uint(), C.c_ulonglong()
+        while not self._stop:
+            a = nv.nvmlDeviceGetClockInfo(h, 1, C.byref(clk))
+            b = nv.nvmlDeviceGetCurrentClocksEventReasons(h, C.byref(rs))
+            if a == 0:
+                self.samples.append((float(clk.value), int(rs.value) if b == 0 else 0))
+            time.sleep(0.002)
 
     def __enter__(self):
         try:
-            fd, self.path = tempfile.mkstemp(suffix=".csv")
-            os.close(fd)
-            self.proc = subprocess.Popen(
-                ["nvidia-smi", "-i", str(self.gpu),
-                 "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
-                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
-                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
-                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+            self._nvml = self._nvml_handle()
+            import threading
+            self._thread = threading.Thread(target=self._loop, daemon=True)
+            self._thread.start()
         except Exception:
-            self.proc = None
+            self._nvml = None
+            try:
+                fd, self._path = tempfile.mkstemp(suffix=".csv")
+                os.close(fd)
+                self._proc = subprocess.Popen(
+                    ["nvidia-smi", "-i", str(self.gpu),
+                     "--query-gpu=clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,"
+                     "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+                     "clocks_event_reasons.sw_power_cap", "--format=csv,noheader,nounits", "-lms", "20"],
+                    stdout=open(self._path, "w"), stderr=subprocess.DEVNULL)
+            except Exception:
+                self._proc = None
         return self
 
     def __exit__(self, *a):
-        if self.proc is not None:
-            self.proc.terminate()
+        self._stop = True
+        if self._thread is not None:
+            self._thread.join(timeout=2)
+        if self._proc is not None:
+            self._proc.terminate()
             try:
-                self.proc.wait(timeout=5)
+                self._proc.wait(timeout=5)
             except Exception:
-                self.proc.kill()
+                self._proc.kill()
 
     def summary(self):
-        if not self.path or not os.path.exists(self.path):
+        if self._nvml is not None:
+            if not self.samples:
+                return None
+            reasons = sorted({n for _, r in self.samples for bit, n in self.REASONS.items() if r & bit})
+            return {"sm_mhz": statistics.median(c for c, _ in self.samples), "sm_max_mhz": self.max_mhz,
+                    "reasons": reasons, "samples": len(self.samples), "source": "nvml, 2 ms"}
+        if not self._path or not os.path.exists(self._path):
             return None
-        rows = []
-        for line in open(self.path):
-            parts = [p.strip() for p in line.split(",")]
-            if len(parts) >= 9:
-                rows.append(parts)
-        os.unlink(self.path)
+        rows = [[x.strip() for x in line.split(",")] for line in open(self._path)]
+        os.unlink(self._path)
+        rows = [r for r in rows if len(r) >= 6 and r[0].replace(".", "").isdigit()]
         if not rows:
             return None
-        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
-        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
-        reasons = set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for r in rows:
-            for n, v in zip(names, r[5:9]):
-                if v.lower() == "active":
-                    reasons.add(n)
-        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": sorted(reasons), "samples": len(rows)}
+        reasons = sorted({n for r in rows for n, v in zip(names, r[2:6]) if v.lower() == "active"})
+        return {"sm_mhz": statistics.median(float(r[0]) for r in rows), "sm_max_mhz": max(float(r[1]) for r in rows),
+                "reasons": reasons, "samples": len(rows), "source": "nvidia-smi, 20 ms"}
 
 
-def build_workload(name, seed=0):
+def build_workload(name, seed=0, native=True):
+    """(model, loads, dt, description) of a workload.  native=False builds the
+    config-2 model without the product library (numpy grid and numbering, the
+    oracle's element body force), for the reference arm."""
     from svl_gb300 import workloads
     if name == "config3":
         m, L, dt, info = workloads.config3(seed=seed, nt=4001)
@@ -129,35 +182,87 @@ def build_workload(name, seed=0):
         m, L, dt = workloads.config1()
         desc = "lin2DQuad4 200x100 plane-strain box, CD"
     elif name == "config2":
+        m, L, dt = workloads.config2_pml(seed=seed, element_force=None if native else _oracle_body_force)
+        desc = ("lin3DHexa8 128x128x64 (h=2 m, log-normal Vs mean 400 m/s, COV 0.2, corr 20 m, nu=0.3, rho=2100), "
+                "10-element PML3DHexa8 layers on the sides and bottom (9 dofs at their nodes), double-couple Ricker "
+                "3 Hz body force, explicit central difference with the staggered PML scheme, dt=0.5 h/max Vp")
+    elif name == "config2_box":
         m, L, dt = workloads.config2(seed=seed)
-        desc = ("lin3DHexa8 128x128x64 box (h=2 m, log-normal Vs, COV 0.2, corr 20 m), CD; "
-                "PML layers not built (fixed bottom, roller sides)")
+        desc = ("lin3DHexa8 128x128x64 box (h=2 m, log-normal Vs, COV 0.2, corr 20 m), CD; fixed bottom and roller "
+                "sides instead of the PML band")
     else:
         raise SystemExit("unknown workload %s" % name)
     return m, L, dt, desc
 
 
-def cpu_baseline(m, L, dt, steps_cap, budget_s=20.0):
-    """Oracle (CPU port of the reference path), fast mode, all host threads."""
+def _oracle_body_force(m, e, q):
+    """Element body force by the CPU oracle (lin3DHexa8 rho * int(N^T q)), on a
+    one-element model holding element e's nodes and material."""
+    from oracle import oracle as O
+    from svl_gb300.model import Model
+    nodes = m.conn[e]
+    one = Model(ndim=3, coords=np.ascontiguousarray(m.coords[nodes]), totaldof=np.arange(24, dtype=np.int32).reshape(8, 3),
+                freedof=np.arange(24, dtype=np.int32).reshape(8, 3), conn=np.arange(8, dtype=np.int32)[None, :],
+                elem_type=m.elem_type, elem_mat=np.zeros(1, np.int32),
+                mat_type=np.ascontiguousarray(m.mat_type[[m.elem_mat[e]]]),
+                mat_param=np.ascontiguousarray(m.mat_param[[m.elem_mat[e]]]))
+    return O.body_force(one, 0, q)
+
+
+def free_disp_dofs(m):
+    """Free displacement dofs (the metric's DOF count; PML stress dofs excluded)."""
+    return int(np.sum(np.asarray(m.freedof)[:, :m.ndim] >= 0))
+
+
+def has_pml(m):
+    return m.elem_pml is not None and bool(np.any(m.elem_pml))
+
+
+def cpu_run(m, L, dt, nsteps, timing):
+    """The CPU oracle of the workload's scheme: the explicit PML scheme on PML
+    models, the plain central difference (fast mode) otherwise."""
+    from oracle import oracle as O
+    if has_pml(m):
+        return O.cdpml_run(m, L, dt, nsteps, history=False, timing=timing)
+    return O.cd_run(m, L, dt, nsteps, mode=1, history=False, timing=timing)
+
+
+def cpu_baseline(insts, dt, steps_cap, budget_s=20.0):
+    """Oracle (CPU port of the path) on all host threads.  The plain central
+    difference: a bounded number of steps of every instance, sized to about
+    budget_s.  The explicit PML scheme (whose oracle forms every PML element's
+    72 x 72 matrices each step, as PML3DHexa8 does, about 10 s per step at the
+    full configuration): 2 steps of instance 0, all instances being the same
+    size.  Set-up is not timed."""
     from oracle import oracle as O
     nthreads = O.num_threads()
     t = {}
-    n = max(1, steps_cap)
-    O.cd_run(m, L, dt, 1, mode=1, history=False, timing=t)   # warm-up / sizing step
-    per = max(t["seconds"], 1e-6)
+    m0, L0 = insts[0][0], insts[0][1]
+    if has_pml(m0):
+        n = max(1, min(steps_cap, 2))
+        cpu_run(m0, L0, dt, n, t)
+        val = free_disp_dofs(m0) * n / t["seconds"]
+        return {"value": val, "unit": "DOF-steps/s", "cores": nthreads, "kind": "port",
+                "sample": "%d time steps of instance 0 of the %d (same size) on the CPU oracle's explicit PML scheme "
+                          "(CDPml: element matrices of PML3DHexa8 formed per step, OpenMP element loops, "
+                          "element-order assembly); set-up not timed" % (n, len(insts))}
+    cpu_run(m0, L0, dt, 1, t)                             # sizing step
+    per = max(t["seconds"], 1e-6) * len(insts)
     n = int(max(1, min(steps_cap, budget_s / per)))
-    O.cd_run(m, L, dt, n, mode=1, history=False, timing=t)
-    val = m.nfree * n / t["seconds"]
-    out = {"value": val, "unit": "DOF-steps/s", "cores": nthreads, "kind": "port",
-           "sample": "%d time steps of the same model on the CPU oracle (OpenMP element loop, ordered scatter)" % n}
-    # the reference's own structure, single-threaded per rank: J, J^-1 and B
-    # recomputed per Gauss point per call (one step)
+    secs, work = 0.0, 0
+    for m, L in ((x[0], x[1]) for x in insts):
+        cpu_run(m, L, dt, n, t)
+        secs += t["seconds"]
+        work += free_disp_dofs(m) * n
+    out = {"value": work / secs, "unit": "DOF-steps/s", "cores": nthreads, "kind": "port",
+           "sample": "%d time step(s) of each of the %d instances on the CPU oracle's central difference (fast "
+                     "mode: OpenMP element loop, element-order assembly)" % (n, len(insts))}
     try:
         t1 = {}
-        O.cd_run(m, L, dt, 1, mode=0, history=False, timing=t1)
+        O.cd_run(m0, L0, dt, 1, mode=0, history=False, timing=t1)
         out["single_thread_reference_faithful"] = {
-            "value": m.nfree / t1["seconds"], "unit": "DOF-steps/s", "cores": 1,
-            "sample": "1 time step of the same model, the oracle's reference-faithful mode"}
+            "value": free_disp_dofs(m0) / t1["seconds"], "unit": "DOF-steps/s", "cores": 1,
+            "sample": "1 time step of instance 0, the oracle's reference-faithful mode"}
     except Exception as exc:  # noqa: BLE001
         out["single_thread_reference_faithful"] = {"error": str(exc)[:200]}
     return out
@@ -311,13 +416,73 @@ def dist_info():
     return ws, rank, local
 
 
+# Algorithmic bytes of the PML band per step (FP32 pairs): per PML node the
+# state read (u_n, u_{n-1}, ubar: 3 pairs each; S^{n+1/2}, S^{n-1/2}, Sbar:
+# 6 pairs each = 216 B) and written (u_{n+1}, ubar, S^{n+3/2}, Sbar = 144 B),
+# its constants (1/d x3, c, Ku, Gu = 24 B; four 9-entry stress blocks = 144 B)
+# and the solid force handed over by the tensor-core step (12 B): 540 B; per
+# PML element its geometry, node indices and b0 (84 B).
+PML_BYTES_PER_NODE = 540.0
+PML_BYTES_PER_ELEMENT = 84.0
+
+
+def workload_config(desc, insts, dt, e2e_steps):
+    """The workload's identity, the same dict on both arms."""
+    m = insts[0][0]
+    return {"workload": desc, "instances": len(insts), "free_dof_per_instance": free_disp_dofs(m),
+            "total_dof_per_instance": int(m.ntotal), "elements_per_instance": int(m.nelem),
+            "pml_elements_per_instance": int(np.sum(m.elem_pml)) if has_pml(m) else 0,
+            "dt": dt, "run_steps": e2e_steps, "data": "synthetic (seeded realisations)"}
+
+
+def reference_arm(args, warm):
+    """The reference's CPU path of the hot path on the machine's host cores: the
+    oracle of the same scheme (reference-faithful restatement; the SVL binary
+    needs Eigen/PETSc/MUMPS, absent here) on the same workload and instance
+    count, a bounded sample of steps of every instance; built without the
+    product library."""
+    nb = args.instances if args.workload in ("config2", "config2_box") else 1
+    insts = [build_workload(args.workload, seed=b, native=False) for b in range(nb)]
+    # the instances differ only in their Vs field; the PML scheme's sample runs instance 0
+    dt = min(x[2] for x in insts)
+    cb = cpu_baseline(insts, dt, steps_cap=max(1, min(args.steps, 20)), budget_s=25.0)
+    line = {"metric": "DOF-steps/s", "value": cb["value"], "unit": "DOF-steps/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": warm, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)", "impl": "reference",
+            "config": workload_config(insts[0][3], insts, dt, E2E_STEPS[args.workload]),
+            "cpu_baseline": cb,
+            "e2e": {"value": cb["value"], "unit": "DOF-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def fp64_plain_run(m, L, dt, steps):
+    """The FP64 plain path on one realisation: the general handle (the explicit
+    PML scheme in FP64 on a PML model, svl_cd otherwise); returns (ms per step,
+    final total-dof vector, launches per step or None)."""
+    from svl_gb300 import CentralDifference
+    h = CentralDifference(m, L, dt)
+    h.Initialize()
+    h.run(1, 2)
+    h.Initialize()
+    if hasattr(h, "run_timed"):
+        ms = h.run_timed(1, steps)
+    else:
+        t0 = time.perf_counter()
+        h.run(1, steps)                   # synchronises at the end (reads its status)
+        ms = (time.perf_counter() - t0) * 1e3
+    U = h.GetDisplacements()
+    h.close()
+    return ms / steps, U
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=400)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="config2", choices=["config1", "config2", "config3"])
+    ap.add_argument("--workload", default="config2", choices=["config1", "config2", "config2_box", "config3"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--instances", type=int, default=4)
     ap.add_argument("--no-e2e", action="store_true")
@@ -351,16 +516,7 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return 0
-        m, L, dt, desc = build_workload(args.workload)
-        cb = cpu_baseline(m, L, dt, steps_cap=min(args.steps, 20))
-        line = {"metric": "DOF-steps/s", "value": cb["value"], "unit": "DOF-steps/s", "n_gpus": args.gpus,
-                "steps": args.steps, "warmup": warm, "higher_is_better": True, "scaling": "weak",
-                "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)", "impl": "reference",
-                "config": {"workload": desc, "free_dof": m.nfree, "elements": m.nelem},
-                "cpu_baseline": cb,
-                "e2e": {"value": cb["value"], "unit": "DOF-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-        print(json.dumps(line))
-        return 0
+        return reference_arm(args, warm)
 
     from svl_gb300 import CentralDifference, StructuredCentralDifference
     from svl_gb300 import _capi as capi
@@ -379,8 +535,9 @@ def main():
     m, L, dt0, desc = insts[0]
     dt = min(x[2] for x in insts)
     nd = m.ndim
-    nfree_total = sum(x[0].nfree for x in insts)
+    nfree_total = sum(free_disp_dofs(x[0]) for x in insts)
     grid = m.grid_shape
+    pml = has_pml(m)
 
     def make_handle():
         if args.precision == "mixed":
@@ -394,9 +551,7 @@ def main():
 
     cd = make_handle()
     cd.run(1, warm)                                   # warm-up
-    prof = None
-    if args.precision == "fp64":
-        prof = cd.profile(1 + warm, 20)
+    prof = cd.profile(1 + warm, 20) if hasattr(cd, "profile") else None
     if args.precision == "mixed":
         for b in range(nb):
             cd.Initialize(b)
@@ -404,66 +559,89 @@ def main():
         cd.Initialize()
     if pg:
         pg.barrier()
-    with ClockSampler(local) as clk:
-        ms = cd.run_timed(1, args.steps)
+    if hasattr(cd, "run_timed"):
+        with ClockSampler(local) as clk:
+            ms = cd.run_timed(1, args.steps)
+    else:
+        with ClockSampler(local) as clk:
+            t0 = time.perf_counter()
+            cd.run(1, args.steps)
+            ms = (time.perf_counter() - t0) * 1e3
     ms = max_over_ranks(pg, ms)
-    launches = cd.launches()
+    launches = cd.launches() if hasattr(cd, "launches") else None
     clocks = clk.summary()
     ms_step = ms / args.steps
     value = job_value(ws, nfree_total, args.steps, ms)
     U_last = cd.get(0, 0) if args.precision == "mixed" else cd.GetDisplacements()
     finite = bool(np.isfinite(U_last).all())
     cd.close()
+    udofs = np.concatenate([m.totaldof[n, :nd] for n in range(m.nnode)]) if pml else np.arange(m.ntotal)
 
     # FP64 plain path on instance 0, same steps: speed and the mixed result's error
     fp64 = None
     if args.precision == "mixed" and not args.no_fp64_compare:
-        ref = CentralDifference(m, L, dt)
-        ref.Initialize()
-        ms64 = ref.run_timed(1, args.steps)
-        U64 = ref.GetDisplacements()
-        ref.close()
-        err = float(np.linalg.norm(U_last - U64) / max(np.linalg.norm(U64), 1e-300))
-        v64 = m.nfree * args.steps / (ms64 / 1e3)
-        fp64 = {"value": ws * v64, "unit": "DOF-steps/s", "ms_per_step": ms64 / args.steps,
+        ms64, U64 = fp64_plain_run(m, L, dt, args.steps)
+        err = float(np.linalg.norm(U_last[udofs] - U64[udofs]) / max(np.linalg.norm(U64[udofs]), 1e-300))
+        v64 = free_disp_dofs(m) * args.steps / (ms64 * args.steps / 1e3)
+        fp64 = {"value": ws * v64, "unit": "DOF-steps/s", "ms_per_step": ms64,
                 "speedup_mixed_over_fp64": value / (ws * v64),
-                "mixed_rel_l2_final_u_vs_fp64": err, "steps": args.steps, "instance": 0}
+                "mixed_rel_l2_final_u_vs_fp64": err, "steps": args.steps, "instance": 0,
+                "path": ("the explicit PML scheme in FP64 on the general PML-capable handle (svl_xnm_*)" if pml
+                         else "FP64 central difference (svl_cd_*)")}
 
     peak, peak_kind = measured_peaks()
-    algo_bytes = ALGO_BYTES_PER_DOF[nd] * nfree_total
-    if args.workload == "config3":
-        algo_bytes += J2_STATE_BYTES_PER_ELEMENT * m.nelem
-    achieved = algo_bytes / (ms_step / 1e3) / 1e9
-    if args.precision == "fp64":
-        kernel_names = ["k_element", "k_node", "k_residual", "k_free", "k_update"]
-        shares = {kernel_names[i]: round(float(prof[i] / max(prof.sum(), 1e-12)), 4) for i in range(5) if prof[i] > 0}
-        kname = "one FP64 CD step (all its kernels)"
+    npml_nodes = int(np.sum(m.node_ndof == 9)) if pml else 0
+    npml_el = int(np.sum(m.elem_pml)) if pml else 0
+    if args.precision == "mixed":
+        grid_dofs = 3 * int(np.prod([g + 1 for g in grid]))
+        kinds = {"k_cdx_step (tensor-core interior step, all instances)": (0, ALGO_BYTES_PER_DOF[3] * grid_dofs * nb),
+                 "k_cdp_fu + k_cdp_uu (PML band, displacement rows)":
+                     (1, (PML_BYTES_PER_NODE * 0.5 * npml_nodes + PML_BYTES_PER_ELEMENT * npml_el) * nb),
+                 "k_cdp_fs + k_cdp_su (PML band, stress rows)":
+                     (2, (PML_BYTES_PER_NODE * 0.5 * npml_nodes + PML_BYTES_PER_ELEMENT * npml_el) * nb)}
+        kinds = {k: v for k, v in kinds.items() if prof[v[0]] > 0}
+        kname = max(kinds, key=lambda k: prof[kinds[k][0]])
+        kidx, algo_bytes = kinds[kname]
+        k_ms = prof[kidx] / 20.0
+        shares = {k: round(float(prof[v[0]] / max(prof.sum(), 1e-12)), 4) for k, v in kinds.items()}
+        per_kernel = {k: {"ms_per_step": float(prof[v[0]] / 20.0),
+                          "algorithmic_bytes": v[1],
+                          "achieved_gbs": v[1] / (prof[v[0]] / 20.0 / 1e3) / 1e9} for k, v in kinds.items()}
     else:
-        shares = None
-        kname = "k_cdx_step (fused mixed-precision step, all instances) + k_cdx_loads"
+        algo_bytes = ALGO_BYTES_PER_DOF[nd] * nfree_total
+        if args.workload == "config3":
+            algo_bytes += J2_STATE_BYTES_PER_ELEMENT * m.nelem
+        k_ms = ms_step
+        kname = "one FP64 step (all its kernels)"
+        shares, per_kernel = None, None
+        if prof is not None:
+            names = ["k_element", "k_node", "k_residual", "k_free", "k_update"]
+            shares = {names[i]: round(float(prof[i] / max(prof.sum(), 1e-12)), 4) for i in range(5) if prof[i] > 0}
+    achieved = algo_bytes / (k_ms / 1e3) / 1e9
 
     e2e = None
     if not args.no_e2e:
         # the whole run through the public API: handle creation from host arrays,
-        # then every step with every instance's full displacement field copied to a
+        # then every step with every instance's full total-dof vector copied to a
         # page-locked host buffer (allocated once, outside the timed region)
-        # (the configured run length: 4000 steps for the 3D and ensemble
-        # workloads, 2000 for the 2D box; the history goes through one reused
-        # page-locked chunk, as a recorder writing it out would)
         from svl_gb300 import pinned_empty
         ne2e = E2E_STEPS[args.workload]
-        chunk = 100 if args.precision == "mixed" else (ne2e if args.workload == "config1" else 200)
+        chunk = 10 if args.precision == "mixed" else (ne2e if args.workload == "config1" else 200)
         hbuf = pinned_empty((chunk, nb, m.ntotal) if args.precision == "mixed" else (chunk, m.ntotal))
         t0 = time.perf_counter()
         cd2 = make_handle()                             # host arrays -> device
         t1 = time.perf_counter()
         for s0 in range(0, ne2e, chunk):
             n = min(chunk, ne2e - s0)
-            cd2.run(1 + s0, n, out=hbuf[:n])
+            if args.precision == "mixed" or not pml:
+                cd2.run(1 + s0, n, out=hbuf[:n])
+            else:                                       # the FP64 PML handle copies its history itself
+                hbuf[:n] = cd2.run(1 + s0, n, history=True)
         t2 = time.perf_counter()
         cd2.close()
         md_bytes = nb * (m.coords.nbytes + m.totaldof.nbytes + m.freedof.nbytes + m.conn.nbytes +
                          m.elem_mat.nbytes + m.mat_param.nbytes + m.mat_type.nbytes +
+                         (m.pml_param.nbytes if pml else 0) +
                          sum(x.nbytes for x in L.series) + 20 * len(L.force_dof) + 16 * len(L.sm_dof))
         e2e = {"value": ws * nfree_total * ne2e / (t2 - t0), "unit": "DOF-steps/s",
                "h2d_bytes_per_step": int(md_bytes / ne2e), "d2h_bytes_per_step": int(nb * m.ntotal * 8),
@@ -471,12 +649,13 @@ def main():
                "run_only_value": ws * nfree_total * ne2e / (t2 - t1),
                "chunk_steps": chunk,
                "includes": "handle creation from host arrays (model, loads) + the whole run with every instance's "
-                           "full displacement field copied to page-locked host memory every step"}
+                           "full total-dof vector (displacements and PML stress dofs) copied to page-locked host "
+                           "memory every step"}
         del hbuf
 
     cb = None
     if rank == 0 and not args.no_cpu:
-        cb = cpu_baseline(m, L, dt, steps_cap=10)
+        cb = cpu_baseline([(x[0], x[1]) for x in insts], dt, steps_cap=10)
     implicit = implicit_pcg(args.implicit_steps) if (rank == 0 and args.implicit_steps > 0) else None
     newton = nonlinear_newton() if (rank == 0 and args.implicit_steps > 0 and args.workload == "config2") else None
     newton_pml = None
@@ -489,32 +668,27 @@ def main():
             newton_pml = {"error": str(exc)[:300]}
 
     if rank == 0:
-        ws_mb = (nb * m.ntotal * 8 * (2 if args.precision == "mixed" else 7) + nb * m.ntotal * 4
-                 + (m.nelem * 24 * 8 if args.precision == "fp64" else nb * m.nelem * 8)) // 2 ** 20
+        ws_mb = (nb * m.ntotal * 8 * 2 + nb * npml_el * 72 * 4 * 2) // 2 ** 20
         line = {
             "metric": "DOF-steps/s", "value": value, "unit": "DOF-steps/s", "n_gpus": ws, "steps": args.steps,
             "warmup": warm, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "tf32x3+f32x2" if args.precision == "mixed" else "f64",
             "data": "synthetic (seeded)",
-            "config": {"workload": desc, "instances": nb, "free_dof_per_instance": m.nfree,
-                       "elements_per_instance": m.nelem, "dt": dt,
-                       "precision": ("mixed: TF32 hi/lo tensor-core element forces, FP32 accumulate, "
-                                     "compensated FP32-pair displacement state (~48 bits)"
-                                     if args.precision == "mixed" else "fp64 plain"),
-                       "parallelism": "replicas" if ws > 1 else "single GPU",
-                       "l2": "no flush; working set ~%d MB > 129 MB L2" % ws_mb},
+            "config": workload_config(desc, insts, dt, E2E_STEPS[args.workload]),
+            "precision": ("mixed: TF32 hi/lo tensor-core element forces with FP32 accumulation in the elastic "
+                          "interior, FP32 PML-band kernels, state as compensated FP32 pairs (~48 bits)"
+                          if args.precision == "mixed" else "fp64 plain"),
+            "parallelism": "replicas" if ws > 1 else "single GPU",
+            "l2": "no flush; working set ~%d MB > 129 MB L2" % ws_mb,
             "roofline": {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "peak_source": peak_kind,
-                         "traffic": (DRAM_BYTES_PER_DOF_STEP_MIXED_H8 * nfree_total
-                                     if args.precision == "mixed" and args.workload == "config2" else None),
-                         "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum of k_cdx_step, "
-                                            "2-instance case (6.3 M DOF), scaled per free DOF to this launch"
-                                            if args.precision == "mixed" and args.workload == "config2" else None),
-                         "algorithmic_bytes_per_step": algo_bytes, "kernel_share": shares},
+                         "frac": achieved / peak, "peak_source": peak_kind + " (HBM copy)",
+                         "traffic": None,
+                         "algorithmic_bytes_per_step": algo_bytes, "kernel_ms_per_step": k_ms,
+                         "kernel_share": shares, "per_kernel": per_kernel},
             "fp64_plain": fp64, "implicit_pcg_time_to_1e-8": implicit, "nonlinear_newton_j2": newton,
             "nonlinear_newton_j2_pml": newton_pml,
-            "cpu_baseline": cb, "e2e": e2e, "gpu_launches": int(launches), "clocks": clocks,
-            "finite": finite,
+            "cpu_baseline": cb, "e2e": e2e, "gpu_launches": int(launches) if launches is not None else None,
+            "clocks": clocks, "finite": finite,
         }
         print(json.dumps(line))
     if pg:

@@ -305,6 +305,11 @@ int  svl_cdx_launch_count(svl_cdx* cdx, int64_t* launches);
  * (a test and tuning hook: the results do not depend on it).  No
  * counterpart in the reference. */
 int  svl_cdx_set_ctas(svl_cdx* cdx, int32_t ctas);
+/* Runs nsteps (no history) with CUDA events between the kernel kinds of each
+ * step; ms_kernel[i] receives the summed device time of kind i: 0 = the fused
+ * tensor-core step, 1 = the PML band's displacement rows, 2 = its stress
+ * rows (3, 4 unused).  No counterpart in the reference (measurement hook). */
+int  svl_cdx_profile(svl_cdx* cdx, int32_t k_first, int32_t nsteps, double* ms_kernel);
 int  svl_cdx_get_ctas(svl_cdx* cdx, int32_t* ctas);
 void svl_cdx_destroy(svl_cdx* cdx);
 

@@ -1698,7 +1698,8 @@ struct CDPml {
     std::vector<double> Mu, Cu, Ku, Gu;     // [ntotal] lumped diagonals of the displacement rows
     std::vector<int> sfirst;                // [nnode] first total dof of the node's stress block, or -1
     std::vector<int> snodes;                // nodes with a stress block
-    std::vector<double> Ms, Cs, Ks, Gs, Dinv;   // [nnode][ns*ns] (only rows of snodes used)
+    std::vector<int> snode_idx;             // [nnode] index into snodes, or -1
+    std::vector<double> Ms, Cs, Ks, Gs, Dinv;   // [snodes][ns*ns]
     std::vector<double> Kff_inv;            // [nfree] 1 / (T^T d T) on displacement free dofs, 0 on stress ones
     std::vector<std::vector<int>> edof;
     bool pml(int e) const { return !s.m.epml.empty() && s.m.epml[e]; }
@@ -1753,50 +1754,76 @@ struct CDPml {
             }
         }
         for (int d0 : s.L.smdof) if (sdof[d0]) return SVL_ERR_UNSUPPORTED;
-        // lumped mass-like parts, element order
+        // lumped mass-like parts, summed in element order; the element row sums
+        // are formed in parallel in chunks of elements, then added in order
         Mu.assign(nt, 0); Cu.assign(nt, 0); Ku.assign(nt, 0); Gu.assign(nt, 0);
         const size_t nb = (size_t)ns * ns;
-        Ms.assign((size_t)m.nnode * nb, 0); Cs = Ms; Ks = Ms; Gs = Ms; Dinv = Ms;
+        snode_idx.assign(m.nnode, -1);
+        for (size_t i = 0; i < snodes.size(); ++i) snode_idx[snodes[i]] = (int)i;
+        Ms.assign(snodes.size() * nb, 0); Cs = Ms; Ks = Ms; Gs = Ms; Dinv = Ms;
         const int ncmax = m.nen * pnd;
-        std::vector<double> Xe[4];
-        for (auto& x : Xe) x.assign((size_t)ncmax * ncmax, 0.0);
         const int ncs = m.nen * m.ndim;
-        std::vector<double> Me((size_t)ncs * ncs);
-        std::vector<double> Msolid(nt, 0.0);
-        for (int e = 0; e < m.nelem; ++e) {
-            if (!pml(e)) {
-                // lumped solid mass with the mass tolerance (Assembler.cpp:623-697)
-                s.element_M(e, Me.data(), true);
-                for (int i = 0; i < ncs; ++i) {
-                    const double v = Me[(size_t)i * ncs + i];
-                    if (std::fabs(v) > mtol) Mu[edof[e][i]] += v;
+        const int nw = m.ndim == 3 ? 4 : 3;
+        const size_t per = (size_t)nw * (ncs + m.nen * nb);      // row sums of one element
+        const int chunk = 4096;
+        std::vector<double> rs((size_t)chunk * per);
+        for (int e0 = 0; e0 < m.nelem; e0 += chunk) {
+            const int e1 = std::min(m.nelem, e0 + chunk);
+            std::vector<double> Xe0((size_t)ncmax * ncmax), Xe1(Xe0.size()), Xe2(Xe0.size()), Xe3(Xe0.size());
+            std::vector<double> Me((size_t)ncs * ncs);
+            #pragma omp parallel for schedule(dynamic, 16) firstprivate(Xe0, Xe1, Xe2, Xe3, Me)
+            for (int e = e0; e < e1; ++e) {
+                double* r = &rs[(size_t)(e - e0) * per];
+                if (!pml(e)) {
+                    s.element_M(e, Me.data(), true);
+                    for (int i = 0; i < ncs; ++i) r[i] = Me[(size_t)i * ncs + i];
+                    continue;
                 }
-                if (!m.ray.empty() && m.ray[2 * e] != 0.0)
-                    for (int i = 0; i < ncs; ++i) {
-                        const double v = m.ray[2 * e] * Me[(size_t)i * ncs + i];
-                        if (std::fabs(v) > s.ktol) Cu[edof[e][i]] += v;
-                    }
-                continue;
-            }
-            pml_elem(e, Xe[0].data(), Xe[1].data(), Xe[2].data(), m.ndim == 3 ? Xe[3].data() : nullptr);
-            const int nc = m.nen * pnd;
-            std::vector<double>* du[4] = {&Mu, &Cu, &Ku, &Gu};
-            std::vector<double>* bs[4] = {&Ms, &Cs, &Ks, &Gs};
-            for (int w = 0; w < (m.ndim == 3 ? 4 : 3); ++w) {
-                const double* X = Xe[w].data();
-                for (int j = 0; j < m.nen; ++j) {
-                    const int n = m.conn[(size_t)e * m.nen + j];
-                    for (int c = 0; c < m.ndim; ++c) {
-                        double v = 0.0;
-                        for (int k = 0; k < m.nen; ++k) v += X[(size_t)(j * pnd + c) * nc + k * pnd + c];
-                        (*du[w])[edof[e][j * pnd + c]] += v;
-                    }
-                    for (int r = 0; r < ns; ++r)
-                        for (int c = 0; c < ns; ++c) {
+                pml_elem(e, Xe0.data(), Xe1.data(), Xe2.data(), m.ndim == 3 ? Xe3.data() : nullptr);
+                const double* Xs[4] = {Xe0.data(), Xe1.data(), Xe2.data(), Xe3.data()};
+                const int nc = m.nen * pnd;
+                for (int w = 0; w < nw; ++w) {
+                    const double* X = Xs[w];
+                    double* ru = r + (size_t)w * (ncs + m.nen * nb);
+                    double* rb = ru + ncs;
+                    for (int j = 0; j < m.nen; ++j) {
+                        for (int c = 0; c < m.ndim; ++c) {
                             double v = 0.0;
-                            for (int k = 0; k < m.nen; ++k) v += X[(size_t)(j * pnd + m.ndim + r) * nc + k * pnd + m.ndim + c];
-                            (*bs[w])[(size_t)n * nb + r * ns + c] += v;
+                            for (int k = 0; k < m.nen; ++k) v += X[(size_t)(j * pnd + c) * nc + k * pnd + c];
+                            ru[j * m.ndim + c] = v;
                         }
+                        for (int rr = 0; rr < ns; ++rr)
+                            for (int c = 0; c < ns; ++c) {
+                                double v = 0.0;
+                                for (int k = 0; k < m.nen; ++k) v += X[(size_t)(j * pnd + m.ndim + rr) * nc + k * pnd + m.ndim + c];
+                                rb[(size_t)j * nb + rr * ns + c] = v;
+                            }
+                    }
+                }
+            }
+            for (int e = e0; e < e1; ++e) {
+                const double* r = &rs[(size_t)(e - e0) * per];
+                if (!pml(e)) {
+                    // lumped solid mass with the mass tolerance (Assembler.cpp:623-697)
+                    for (int i = 0; i < ncs; ++i) if (std::fabs(r[i]) > mtol) Mu[edof[e][i]] += r[i];
+                    if (!m.ray.empty() && m.ray[2 * e] != 0.0)
+                        for (int i = 0; i < ncs; ++i) {
+                            const double v = m.ray[2 * e] * r[i];
+                            if (std::fabs(v) > s.ktol) Cu[edof[e][i]] += v;
+                        }
+                    continue;
+                }
+                std::vector<double>* du[4] = {&Mu, &Cu, &Ku, &Gu};
+                std::vector<double>* bs[4] = {&Ms, &Cs, &Ks, &Gs};
+                for (int w = 0; w < nw; ++w) {
+                    const double* ru = r + (size_t)w * (ncs + m.nen * nb);
+                    const double* rb = ru + ncs;
+                    for (int j = 0; j < m.nen; ++j) {
+                        const int n = m.conn[(size_t)e * m.nen + j];
+                        for (int c = 0; c < m.ndim; ++c) (*du[w])[edof[e][j * pnd + c]] += ru[j * m.ndim + c];
+                        double* B = &(*bs[w])[(size_t)snode_idx[n] * nb];
+                        for (size_t k = 0; k < nb; ++k) B[k] += rb[(size_t)j * nb + k];
+                    }
                 }
             }
         }
@@ -1827,9 +1854,10 @@ struct CDPml {
         }
         // inverse of Ms/dt^2 + Cs/2dt per node (Gauss-Jordan with partial pivoting)
         for (int n : snodes) {
+            const size_t sb = (size_t)snode_idx[n] * nb;
             double Aa[36], B[36];
             for (size_t i = 0; i < nb; ++i) {
-                Aa[i] = Ms[(size_t)n * nb + i] / dt / dt + Cs[(size_t)n * nb + i] / 2.0 / dt;
+                Aa[i] = Ms[sb + i] / dt / dt + Cs[sb + i] / 2.0 / dt;
                 B[i] = 0.0;
             }
             for (int i = 0; i < ns; ++i) B[i * ns + i] = 1.0;
@@ -1847,7 +1875,7 @@ struct CDPml {
                     for (int j = 0; j < ns; ++j) { Aa[r * ns + j] -= f * Aa[c * ns + j]; B[r * ns + j] -= f * B[c * ns + j]; }
                 }
             }
-            for (size_t i = 0; i < nb; ++i) Dinv[(size_t)n * nb + i] = B[i];
+            for (size_t i = 0; i < nb; ++i) Dinv[sb + i] = B[i];
         }
         return SVL_OK;
     }
@@ -1982,11 +2010,12 @@ struct CDPml {
         couple(1, udot, umid, ubh, Fs);
         for (int n : snodes) {
             const int t0 = sfirst[n];
+            const size_t sb = (size_t)snode_idx[n] * nb;
             double R[6];
             for (int r = 0; r < ns; ++r) {
                 double v = -Fs[t0 + r];
                 for (int c = 0; c < ns; ++c) {
-                    const size_t i = (size_t)n * nb + r * ns + c;
+                    const size_t i = sb + r * ns + c;
                     const double sc = U[t0 + c], sp = Up[t0 + c], sbh = Ubar[t0 + c] + dt / 2.0 * sc;
                     v += -Ks[i] * sc - Gs[i] * sbh + (Ms[i] / dt / dt - Cs[i] / 2.0 / dt) * (sc - sp);
                 }
@@ -1994,7 +2023,7 @@ struct CDPml {
             }
             for (int r = 0; r < ns; ++r) {
                 double v = 0.0;
-                for (int c = 0; c < ns; ++c) v += Dinv[(size_t)n * nb + r * ns + c] * R[c];
+                for (int c = 0; c < ns; ++c) v += Dinv[sb + r * ns + c] * R[c];
                 dU[t0 + r] = v;
                 Ubn[t0 + r] = Ubar[t0 + r] + dt * U[t0 + r];
             }

@@ -162,6 +162,7 @@ def lib():
     L.svl_cdx_get.argtypes = [C.c_void_p, C.c_int32, C.c_int32, f64p]
     L.svl_cdx_launch_count.argtypes = [C.c_void_p, C.POINTER(C.c_int64)]
     L.svl_cdx_set_ctas.argtypes = [C.c_void_p, C.c_int32]
+    L.svl_cdx_profile.argtypes = [C.c_void_p, C.c_int32, C.c_int32, f64p]
     L.svl_cdx_get_ctas.argtypes = [C.c_void_p, C.POINTER(C.c_int32)]
     L.svl_cdx_destroy.argtypes = [C.c_void_p]
     L.svl_cdx_destroy.restype = None

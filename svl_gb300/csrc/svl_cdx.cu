@@ -1460,6 +1460,22 @@ int svl_cdx_set_initial(svl_cdx* h, int32_t inst, const double* U0, const double
     return SVL_OK;
 }
 
+// The PML band's view of the handle for the step from u_n (index cur).
+static CdpView cdp_view(svl_cdx* h) {
+    CdpView c{};
+    c.ninst = h->ninst; c.np = h->np; c.npe = h->npe;
+    c.h = (float)h->hgrid; c.dt = (float)h->dt;
+    c.per = (long long)(h->nstate / h->ninst);
+    c.enode = h->enode; c.egeo = h->egeo; c.eb0 = h->eb0; c.ninv = h->ninv; c.npad = h->npad;
+    c.uc = h->uc; c.scs = h->scs;
+    c.uh = h->uh[h->cur]; c.ul = h->ul[h->cur]; c.uph = h->uh[1 - h->cur]; c.upl = h->ul[1 - h->cur];
+    c.fsol = h->fsol;
+    c.ubh = h->ubh; c.ubl = h->ubl;
+    c.sh = h->sh[h->cur]; c.sl = h->sl[h->cur]; c.sph = h->sh[1 - h->cur]; c.spl = h->sl[1 - h->cur];
+    c.sbh = h->sbh; c.sbl = h->sbl; c.vin = h->vin; c.feu = h->feu; c.fes = h->fes;
+    return c;
+}
+
 static int cdx_step(svl_cdx* h, int k, bool want_va) {
     CdxView v;
     v.nx = h->nx; v.ny = h->ny; v.nz = h->nz; v.ninst = h->ninst;
@@ -1481,16 +1497,7 @@ static int cdx_step(svl_cdx* h, int k, bool want_va) {
     ++h->launches;
     if (h->np > 0) {
         // the PML band: coupling forces and updates of the PML nodes
-        CdpView c{};
-        c.ninst = h->ninst; c.np = h->np; c.npe = h->npe;
-        c.h = (float)h->hgrid; c.dt = (float)h->dt;
-        c.per = (long long)(h->nstate / h->ninst);
-        c.enode = h->enode; c.egeo = h->egeo; c.eb0 = h->eb0; c.ninv = h->ninv; c.npad = h->npad;
-        c.uc = h->uc; c.scs = h->scs;
-        c.uh = h->uh[h->cur]; c.ul = h->ul[h->cur]; c.uph = v.uh_prev; c.upl = v.ul_prev; c.fsol = h->fsol;
-        c.ubh = h->ubh; c.ubl = h->ubl;
-        c.sh = h->sh[h->cur]; c.sl = h->sl[h->cur]; c.sph = h->sh[1 - h->cur]; c.spl = h->sl[1 - h->cur];
-        c.sbh = h->sbh; c.sbl = h->sbl; c.vin = h->vin; c.feu = h->feu; c.fes = h->fes;
+        CdpView c = cdp_view(h);
         const long long ge = (long long)h->ninst * h->npe * 8, gn = (long long)h->ninst * h->np;
         const unsigned be = (unsigned)((ge + CDP_THREADS - 1) / CDP_THREADS), bn = (unsigned)((gn + 255) / 256);
         k_cdp_fu<<<be, CDP_THREADS, 0, h->stream>>>(c);
@@ -1644,6 +1651,51 @@ int svl_cdx_get(svl_cdx* h, int32_t inst, int32_t which, double* out) {
     CUDA_TRY(cudaStreamSynchronize(h->stream));
     for (long long t = 0; t < h->ntotal; ++t) out[t] = tmp[h->pad_index[t]];
     return SVL_OK;
+}
+
+int svl_cdx_profile(svl_cdx* h, int32_t k_first, int32_t nsteps, double* ms_kernel) {
+    if (!h || !ms_kernel || nsteps < 0) { set_error("bad argument"); return SVL_ERR_INVALID; }
+    for (int i = 0; i < 5; ++i) ms_kernel[i] = 0.0;
+    cudaEvent_t ev[6];
+    for (int i = 0; i < 6; ++i) CUDA_TRY(cudaEventCreate(&ev[i]));
+    for (int s2 = 0; s2 < nsteps; ++s2) {
+        // the same launches as cdx_step, with events between the kernel kinds:
+        // 0 fused tensor-core step, 1 PML displacement rows (k_cdp_fu + k_cdp_uu),
+        // 2 PML stress rows (k_cdp_fs + k_cdp_su)
+        CUDA_TRY(cudaEventRecord(ev[0], h->stream));
+        const int np = h->np;
+        h->np = 0;                                   // tensor-core kernel alone
+        int st = cdx_step(h, k_first + s2, false);
+        h->np = np;
+        if (st) return st;
+        h->cur = 1 - h->cur;                         // cdx_step flipped it; the band still belongs to this step
+        CUDA_TRY(cudaEventRecord(ev[1], h->stream));
+        if (np > 0) {
+            CdpView c = cdp_view(h);
+            const long long ge = (long long)h->ninst * h->npe * 8, gn = (long long)h->ninst * h->np;
+            const unsigned be = (unsigned)((ge + CDP_THREADS - 1) / CDP_THREADS), bn = (unsigned)((gn + 255) / 256);
+            k_cdp_fu<<<be, CDP_THREADS, 0, h->stream>>>(c);
+            k_cdp_uu<<<bn, 256, 0, h->stream>>>(c);
+            CUDA_TRY(cudaEventRecord(ev[2], h->stream));
+            k_cdp_fs<<<be, CDP_THREADS, 0, h->stream>>>(c);
+            k_cdp_su<<<bn, 256, 0, h->stream>>>(c);
+            h->launches += 4;
+        } else {
+            CUDA_TRY(cudaEventRecord(ev[2], h->stream));
+        }
+        CUDA_TRY(cudaEventRecord(ev[3], h->stream));
+        CUDA_TRY(cudaGetLastError());
+        h->cur = 1 - h->cur;
+        CUDA_TRY(cudaEventSynchronize(ev[3]));
+        for (int kind = 0; kind < 3; ++kind) {
+            float t = 0.f;
+            CUDA_TRY(cudaEventElapsedTime(&t, ev[kind], ev[kind + 1]));
+            ms_kernel[kind] += t;
+        }
+    }
+    for (int i = 0; i < 6; ++i) cudaEventDestroy(ev[i]);
+    h->va_valid = false;
+    return cdx_status(h);
 }
 
 int svl_cdx_set_ctas(svl_cdx* h, int32_t ctas) {

@@ -176,6 +176,13 @@ class StructuredCentralDifference:
         check(lib().svl_cdx_launch_count(self._h, C.byref(n)))
         return int(n.value)
 
+    def profile(self, k_first: int, nsteps: int) -> np.ndarray:
+        """Device time (ms) per kernel kind over nsteps: [tensor-core step, PML
+        displacement rows, PML stress rows, 0, 0]."""
+        out = np.zeros(5)
+        check(lib().svl_cdx_profile(self._h, int(k_first), int(nsteps), ptr(out, C.c_double)))
+        return out
+
     def set_ctas(self, ctas: int) -> int:
         """CTAs of the persistent step kernel (0 = one per SM); returns the
         grid size in effect."""

@@ -402,8 +402,8 @@ def config2_pml(nx=128, ny=128, nz=64, npml=10, nt=4001, seed=0, amp=1.0e3, pml_
     L = npml h, R = pml_R; the log-normal Vs field everywhere), 9 dofs at the
     nodes of PML elements and 3 elsewhere (node-by-node PlainScheme order),
     the outer PML boundary fixed in displacement, the top free.  Built in
-    numpy (element_force: the element body-force routine, default the
-    library's)."""
+    numpy; element_force(model, e, direction) is the element body-force
+    routine (default the library's svl_element_body_force)."""
     h, rho, nu = 2.0, 2100.0, 0.3
     vs = lognormal_field((nx, ny, nz), h, 400.0, 0.2, 20.0, seed)
     vs_e = np.transpose(vs, (2, 1, 0)).reshape(-1)
@@ -442,5 +442,6 @@ def config2_pml(nx=128, ny=128, nz=64, npml=10, nt=4001, seed=0, amp=1.0e3, pml_
         return (k * ny + j) * nx + i
     for e, d in ((eid(cx, cy + 1, cz), (amp, 0.0, 0.0)), (eid(cx, cy - 1, cz), (-amp, 0.0, 0.0)),
                  (eid(cx + 1, cy, cz), (0.0, amp, 0.0)), (eid(cx - 1, cy, cz), (0.0, -amp, 0.0))):
-        L.add_body_load(m, [e], d, s, element_force=element_force)
+        L.add_body_load(m, [e], d, s,
+                        element_force=None if element_force is None else (lambda e2, q, m_=m: element_force(m_, e2, q)))
     return m, L, dt
