@@ -590,7 +590,7 @@ struct CdpView {
     float h, dt;
     long long per;                      // padded state floats per instance
     const int32_t* __restrict__ enode;  // [npe][8] PML node index of each element node
-    const float* __restrict__ egeo;     // [npe][12] corner xyz, x0 xyz, n xyz, a0, L, m
+    const float* __restrict__ estr;     // [npe][12] per axis d: a(-g), a(+g), r(-g), r(+g); b = b0 r
     const float* __restrict__ eb0;      // [ninst][npe] b0 of the element's P-wave speed
     const int32_t* __restrict__ ninv;   // [np][8] element slots e*8 + local node in element order, -1 unused
     const long long* __restrict__ npad; // [np] padded offset of the node's displacement in instance 0
@@ -606,132 +606,125 @@ struct CdpView {
     const float* __restrict__ sl;
     float* sph; float* spl;             // S^{n-1/2} in, S^{n+3/2} out
     float* sbh; float* sbl;             // Sbar pair [ninst][np][6]
-    float* vin;                         // [ninst][np][9] udot, umid, ubar at the half step
+    float* vsu;                         // [ninst][np][20] displacement rows' inputs: sdot, smid, Sbar (written by k_cdp_su for the next step)
+    float* vin;                         // [ninst][np][12] stress rows' inputs: udot, umid, ubar at the half step
     float* feu;                         // [ninst][npe][8][3]
     float* fes;                         // [ninst][npe][8][6]
 };
 
 constexpr int CDP_THREADS = 256;
+constexpr int CDP_GROUPS = CDP_THREADS / 8;
 __constant__ float kHexR[8] = {-1, 1, 1, -1, -1, 1, 1, -1};
 __constant__ float kHexS[8] = {-1, -1, 1, 1, -1, -1, 1, 1};
 __constant__ float kHexT[8] = {-1, -1, -1, -1, 1, 1, 1, 1};
 
-// Gauss point q (r fastest, GaussQuadrature.cpp:303-316 abscissa) of the cube
-// element e: shape values, physical derivatives, w |J|, and the coupling
-// weights of C, K, G per derivative direction from the stretching at the
-// point (PML3DHexa8.cpp:952-996; x: C ay az, K ay bz + az by, G by bz).
-__device__ __forceinline__ void cdp_gauss(const CdpView& v, int e, int inst, int q, float N[8], float dN[8][3],
-                                          float& W, float qC[3], float qK[3], float qG[3]) {
+// Shape values N_a and physical derivatives dN_a/dx of a cube of side h at
+// Gauss point q (r fastest; GaussQuadrature.cpp:303-316 abscissa).
+__device__ __forceinline__ void cdp_shape(float h, int q, float N[8], float dN[8][3]) {
     const float g = 0.577350269189626f;
     const float xi[3] = {(q & 1) ? g : -g, (q & 2) ? g : -g, (q & 4) ? g : -g};
-    const float c2 = 2.0f / v.h;
+    const float c2 = 0.25f / h;                    // (2/h) * 1/8
 #pragma unroll
     for (int a = 0; a < 8; ++a) {
         const float fr = 1.0f + kHexR[a] * xi[0], fs = 1.0f + kHexS[a] * xi[1], ft = 1.0f + kHexT[a] * xi[2];
         N[a] = 0.125f * fr * fs * ft;
-        dN[a][0] = c2 * 0.125f * kHexR[a] * fs * ft;
-        dN[a][1] = c2 * 0.125f * kHexS[a] * fr * ft;
-        dN[a][2] = c2 * 0.125f * kHexT[a] * fr * fs;
-    }
-    const float hh = 0.5f * v.h;
-    W = hh * hh * hh;
-    const float* gq = v.egeo + (size_t)e * 12;
-    const float a0 = gq[9], L = gq[10], pm = gq[11], b0 = v.eb0[(size_t)inst * v.npe + e];
-    float as[3], bs[3];
-#pragma unroll
-    for (int d = 0; d < 3; ++d) {
-        const float xg = gq[d] + hh * (1.0f + xi[d]);
-        const float r = powf((xg - gq[3 + d]) * gq[6 + d] / L, pm);
-        as[d] = 1.0f + a0 * r;
-        bs[d] = b0 * r;
-    }
-    qC[0] = as[1] * as[2]; qC[1] = as[0] * as[2]; qC[2] = as[0] * as[1];
-    qK[0] = as[1] * bs[2] + as[2] * bs[1]; qK[1] = as[0] * bs[2] + as[2] * bs[0]; qK[2] = as[0] * bs[1] + as[1] * bs[0];
-    qG[0] = bs[1] * bs[2]; qG[1] = bs[0] * bs[2]; qG[2] = bs[0] * bs[1];
-}
-
-// Sum of x over the 8 lanes of a group, element j of the result on lane j:
-// recursive halving (lane bit 2, then 1, then 0 selects the half it keeps).
-template <int C>
-__device__ __forceinline__ void cdp_reduce8(float (&f)[8][C], int q, float (&out)[C]) {
-    const bool b2 = (q >> 2) & 1, b1 = (q >> 1) & 1, b0 = q & 1;
-    float k4[4][C], k2[2][C];
-#pragma unroll
-    for (int j = 0; j < 4; ++j)
-#pragma unroll
-        for (int c = 0; c < C; ++c) {
-            const float send = b2 ? f[j][c] : f[j + 4][c];
-            const float r = __shfl_xor_sync(0xffffffffu, send, 4);
-            k4[j][c] = (b2 ? f[j + 4][c] : f[j][c]) + r;
-        }
-#pragma unroll
-    for (int j = 0; j < 2; ++j)
-#pragma unroll
-        for (int c = 0; c < C; ++c) {
-            const float send = b1 ? k4[j][c] : k4[j + 2][c];
-            const float r = __shfl_xor_sync(0xffffffffu, send, 2);
-            k2[j][c] = (b1 ? k4[j + 2][c] : k4[j][c]) + r;
-        }
-#pragma unroll
-    for (int c = 0; c < C; ++c) {
-        const float send = b0 ? k2[0][c] : k2[1][c];
-        const float r = __shfl_xor_sync(0xffffffffu, send, 1);
-        out[c] = (b0 ? k2[1][c] : k2[0][c]) + r;
+        dN[a][0] = c2 * kHexR[a] * fs * ft;
+        dN[a][1] = c2 * kHexS[a] * fr * ft;
+        dN[a][2] = c2 * kHexT[a] * fr * fs;
     }
 }
 
-// Coupling forces of the PML elements on the displacement rows:
-// C_uS sdot + K_uS smid + G_uS Sbar, one thread per (element, Gauss point);
-// lane q of a group loads node q, lane j writes node j.
+// Shape value and physical derivatives of node a (runtime index, signs from
+// constant memory) at Gauss point gp (compile-time index after unrolling).
+__device__ __forceinline__ void cdp_node_at(float h, int a, int gp, float& n, float& dx, float& dy, float& dz) {
+    const float g = 0.577350269189626f;
+    const float r = kHexR[a], s2 = kHexS[a], t = kHexT[a];
+    const float fr = 1.0f + r * ((gp & 1) ? g : -g), fs = 1.0f + s2 * ((gp & 2) ? g : -g),
+                ft = 1.0f + t * ((gp & 4) ? g : -g);
+    const float c2 = 0.25f / h;
+    n = 0.125f * fr * fs * ft;
+    dx = c2 * r * fs * ft;
+    dy = c2 * s2 * fr * ft;
+    dz = c2 * t * fr * fs;
+}
+
+// Coupling weights of C, K, G per derivative direction at Gauss point q of
+// element e from the stretching there (PML3DHexa8.cpp:952-996, tabulated per
+// element and axis at the two abscissae; x: C ay az, K ay bz + az by, G by bz).
+__device__ __forceinline__ void cdp_weights(const CdpView& v, int e, int inst, int q, float qC[3], float qK[3],
+                                            float qG[3]) {
+    const float4* t = reinterpret_cast<const float4*>(v.estr + (size_t)e * 12);
+    const float4 tx = t[0], ty = t[1], tz = t[2];
+    const float b0 = v.eb0[(size_t)inst * v.npe + e];
+    const float ax = (q & 1) ? tx.y : tx.x, ay = (q & 2) ? ty.y : ty.x, az = (q & 4) ? tz.y : tz.x;
+    const float bx = b0 * ((q & 1) ? tx.w : tx.z), by = b0 * ((q & 2) ? ty.w : ty.z), bz = b0 * ((q & 4) ? tz.w : tz.z);
+    qC[0] = ay * az; qC[1] = ax * az; qC[2] = ax * ay;
+    qK[0] = ay * bz + az * by; qK[1] = ax * bz + az * bx; qK[2] = ax * by + ay * bx;
+    qG[0] = by * bz; qG[1] = bx * bz; qG[2] = bx * by;
+}
+
+// Coupling forces of the PML elements on the displacement rows,
+// C_uS sdot + K_uS smid + G_uS Sbar, one thread per (element, Gauss point):
+// lane q stages node q's inputs, forms Gauss point q's weighted stress
+// combinations T (9 values) into shared memory, then lane j sums node j's
+// force over the 8 points: f_j = w|J| sum_q dN_j(q) . T(q).
 __global__ void __launch_bounds__(CDP_THREADS) k_cdp_fu(CdpView v) {
-    __shared__ float sm[CDP_THREADS / 8][8][18];
+    __shared__ __align__(16) float sm[CDP_GROUPS][8][20];
+    __shared__ __align__(16) float st[CDP_GROUPS][8][12];
     const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const int q = (int)(gid & 7), lg = threadIdx.x >> 3;
     const long long grp = gid >> 3;
     const bool valid = grp < (long long)v.ninst * v.npe;
     const int inst = valid ? (int)(grp / v.npe) : 0, e = valid ? (int)(grp % v.npe) : 0;
+    float4* srow = reinterpret_cast<float4*>(&sm[lg][q][0]);
     if (valid) {
         const int p = v.enode[(size_t)e * 8 + q];
-        const size_t b = ((size_t)inst * v.np + p) * 6;
-        const float idt = 1.0f / v.dt;
+        const float4* src = reinterpret_cast<const float4*>(v.vsu + ((size_t)inst * v.np + p) * 20);
 #pragma unroll
-        for (int c = 0; c < 6; ++c) {
-            const float ch = v.sh[b + c], cl = v.sl[b + c], ph = v.sph[b + c], pl = v.spl[b + c];
-            sm[lg][q][c] = ((ch - ph) + (cl - pl)) * idt;
-            sm[lg][q][6 + c] = 0.5f * (ch + ph);
-            sm[lg][q][12 + c] = v.sbh[b + c];
-        }
+        for (int i = 0; i < 5; ++i) srow[i] = src[i];
     } else {
 #pragma unroll
-        for (int c = 0; c < 18; ++c) sm[lg][q][c] = 0.f;
+        for (int i = 0; i < 5; ++i) srow[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
     __syncwarp();
-    float N[8], dN[8][3], W, qC[3], qK[3], qG[3];
-    cdp_gauss(v, e, inst, q, N, dN, W, qC, qK, qG);
-    float sg[18];
+    float N[8], dN[8][3], qC[3], qK[3], qG[3];
+    cdp_shape(v.h, q, N, dN);
+    cdp_weights(v, e, inst, q, qC, qK, qG);
+    float sg[20];
 #pragma unroll
-    for (int k = 0; k < 18; ++k) sg[k] = 0.f;
+    for (int k = 0; k < 20; ++k) sg[k] = 0.f;
 #pragma unroll
-    for (int a = 0; a < 8; ++a)
+    for (int a = 0; a < 8; ++a) {
+        const float4* r = reinterpret_cast<const float4*>(&sm[lg][a][0]);
 #pragma unroll
-        for (int k = 0; k < 18; ++k) sg[k] += N[a] * sm[lg][a][k];
-    // T^d_c = qC_d sdot_c + qK_d smid_c + qG_d sbar_c (components xx yy zz xy yz xz)
-    auto T = [&](int d, int c) { return qC[d] * sg[c] + qK[d] * sg[6 + c] + qG[d] * sg[12 + c]; };
-    const float tx0 = T(0, 0), tx3 = T(0, 3), tx5 = T(0, 5);
-    const float ty3 = T(1, 3), ty1 = T(1, 1), ty4 = T(1, 4);
-    const float tz5 = T(2, 5), tz4 = T(2, 4), tz2 = T(2, 2);
-    float f[8][3];
-#pragma unroll
-    for (int j = 0; j < 8; ++j) {
-        f[j][0] = W * (dN[j][0] * tx0 + dN[j][1] * ty3 + dN[j][2] * tz5);
-        f[j][1] = W * (dN[j][0] * tx3 + dN[j][1] * ty1 + dN[j][2] * tz4);
-        f[j][2] = W * (dN[j][0] * tx5 + dN[j][1] * ty4 + dN[j][2] * tz2);
+        for (int i = 0; i < 5; ++i) {
+            const float4 x = r[i];
+            sg[4 * i] += N[a] * x.x; sg[4 * i + 1] += N[a] * x.y; sg[4 * i + 2] += N[a] * x.z; sg[4 * i + 3] += N[a] * x.w;
+        }
     }
-    float out[3];
-    cdp_reduce8<3>(f, q, out);
+    // T^d_c = qC_d sdot_c + qK_d smid_c + qG_d Sbar_c (components xx yy zz xy yz xz)
+    auto T = [&](int d, int c) { return qC[d] * sg[c] + qK[d] * sg[6 + c] + qG[d] * sg[12 + c]; };
+    float4* trow = reinterpret_cast<float4*>(&st[lg][q][0]);
+    trow[0] = make_float4(T(0, 0), T(0, 3), T(0, 5), T(1, 3));
+    trow[1] = make_float4(T(1, 1), T(1, 4), T(2, 5), T(2, 4));
+    trow[2] = make_float4(T(2, 2), 0.f, 0.f, 0.f);
+    __syncwarp();
+    // node q's force: sum over the Gauss points p of dN_q(p) . T(p)
+    const float hh = 0.5f * v.h, W = hh * hh * hh;
+    float f0 = 0.f, f1 = 0.f, f2 = 0.f;
+#pragma unroll
+    for (int gp = 0; gp < 8; ++gp) {
+        float n, dx, dy, dz;
+        cdp_node_at(v.h, q, gp, n, dx, dy, dz);
+        const float4* r = reinterpret_cast<const float4*>(&st[lg][gp][0]);
+        const float4 t0 = r[0], t1 = r[1], t2 = r[2];
+        f0 += dx * t0.x + dy * t0.w + dz * t1.z;          // x: xx(d=x) xy(d=y) xz(d=z)
+        f1 += dx * t0.y + dy * t1.x + dz * t1.w;          // y: xy(x) yy(y) yz(z)
+        f2 += dx * t0.z + dy * t1.y + dz * t2.x;          // z: xz(x) yz(y) zz(z)
+    }
     if (valid) {
         float* o = v.feu + (((size_t)inst * v.npe + e) * 8 + q) * 3;
-        o[0] = out[0]; o[1] = out[1]; o[2] = out[2];
+        o[0] = W * f0; o[1] = W * f1; o[2] = W * f2;
     }
 }
 
@@ -755,7 +748,7 @@ __global__ void __launch_bounds__(256) k_cdp_uu(CdpView v) {
     const float* c6 = v.uc + ((size_t)inst * v.np + p) * 6;
     const float cc = c6[3], Ku = c6[4], Gu = c6[5];
     const size_t ib = ((size_t)inst * v.np + p) * 3;
-    float* vi = v.vin + ((size_t)inst * v.np + p) * 9;
+    float vi[12];
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
         const float uh = v.uh[pad + c], ul = v.ul[pad + c], ph = v.uph[pad + c], pl = v.upl[pad + c];
@@ -776,29 +769,40 @@ __global__ void __launch_bounds__(256) k_cdp_uu(CdpView v) {
         vi[3 + c] = u + 0.5f * du;
         vi[6 + c] = bh + 0.5f * inc;
     }
+    vi[9] = vi[10] = vi[11] = 0.f;
+    float4* o = reinterpret_cast<float4*>(v.vin + ((size_t)inst * v.np + p) * 12);
+    o[0] = make_float4(vi[0], vi[1], vi[2], vi[3]);
+    o[1] = make_float4(vi[4], vi[5], vi[6], vi[7]);
+    o[2] = make_float4(vi[8], vi[9], vi[10], vi[11]);
 }
 
 // Coupling forces of the PML elements on the stress rows:
-// C_Su udot + K_Su umid + G_Su ubar_half = w |J| N_j (stretched strain).
+// C_Su udot + K_Su umid + G_Su ubar_half = w |J| N_j (stretched strain):
+// lane q forms Gauss point q's stretched strain (6 values) into shared
+// memory, lane j sums node j's vector over the 8 points.
 __global__ void __launch_bounds__(CDP_THREADS) k_cdp_fs(CdpView v) {
-    __shared__ float sm[CDP_THREADS / 8][8][9];
+    __shared__ __align__(16) float sm[CDP_GROUPS][8][12];
+    __shared__ __align__(16) float st[CDP_GROUPS][8][8];
     const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const int q = (int)(gid & 7), lg = threadIdx.x >> 3;
     const long long grp = gid >> 3;
     const bool valid = grp < (long long)v.ninst * v.npe;
     const int inst = valid ? (int)(grp / v.npe) : 0, e = valid ? (int)(grp % v.npe) : 0;
+    float4* srow = reinterpret_cast<float4*>(&sm[lg][q][0]);
     if (valid) {
         const int p = v.enode[(size_t)e * 8 + q];
-        const float* vi = v.vin + ((size_t)inst * v.np + p) * 9;
+        const float4* src = reinterpret_cast<const float4*>(v.vin + ((size_t)inst * v.np + p) * 12);
 #pragma unroll
-        for (int c = 0; c < 9; ++c) sm[lg][q][c] = vi[c];
+        for (int i = 0; i < 3; ++i) srow[i] = src[i];
     } else {
 #pragma unroll
-        for (int c = 0; c < 9; ++c) sm[lg][q][c] = 0.f;
+        for (int i = 0; i < 3; ++i) srow[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
     __syncwarp();
-    float N[8], dN[8][3], W, qC[3], qK[3], qG[3];
-    cdp_gauss(v, e, inst, q, N, dN, W, qC, qK, qG);
+    float N[8], dN[8][3], qC[3], qK[3], qG[3];
+    cdp_shape(v.h, q, N, dN);
+    (void)N;
+    cdp_weights(v, e, inst, q, qC, qK, qG);
     // gradients: gr[i][d][c] = d (input i)_c / dx_d
     float gr[3][3][3];
 #pragma unroll
@@ -808,33 +812,36 @@ __global__ void __launch_bounds__(CDP_THREADS) k_cdp_fs(CdpView v) {
 #pragma unroll
             for (int c = 0; c < 3; ++c) gr[i][d][c] = 0.f;
 #pragma unroll
-    for (int a = 0; a < 8; ++a)
+    for (int a = 0; a < 8; ++a) {
+        const float4* r = reinterpret_cast<const float4*>(&sm[lg][a][0]);
+        const float4 x0 = r[0], x1 = r[1], x2 = r[2];
+        const float in[9] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w, x2.x};
 #pragma unroll
         for (int i = 0; i < 3; ++i)
 #pragma unroll
             for (int d = 0; d < 3; ++d)
 #pragma unroll
-                for (int c = 0; c < 3; ++c) gr[i][d][c] += dN[a][d] * sm[lg][a][3 * i + c];
-    // stretched strain: weight of direction d per matrix (C udot, K umid, G ubar)
+                for (int c = 0; c < 3; ++c) gr[i][d][c] += dN[a][d] * in[3 * i + c];
+    }
     auto wd = [&](int d, int c) { return qC[d] * gr[0][d][c] + qK[d] * gr[1][d][c] + qG[d] * gr[2][d][c]; };
-    float eps[6];
-    eps[0] = wd(0, 0);
-    eps[1] = wd(1, 1);
-    eps[2] = wd(2, 2);
-    eps[3] = wd(1, 0) + wd(0, 1);        // s12: y-derivative of u_x, x-derivative of u_y
-    eps[4] = wd(2, 1) + wd(1, 2);        // s23
-    eps[5] = wd(2, 0) + wd(0, 2);        // s13
-    float f[8][6];
+    float4* trow = reinterpret_cast<float4*>(&st[lg][q][0]);
+    trow[0] = make_float4(wd(0, 0), wd(1, 1), wd(2, 2), wd(1, 0) + wd(0, 1));
+    trow[1] = make_float4(wd(2, 1) + wd(1, 2), wd(2, 0) + wd(0, 2), 0.f, 0.f);
+    __syncwarp();
+    const float hh = 0.5f * v.h, W = hh * hh * hh;
+    float r6[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
 #pragma unroll
-    for (int j = 0; j < 8; ++j)
-#pragma unroll
-        for (int c = 0; c < 6; ++c) f[j][c] = W * N[j] * eps[c];
-    float out[6];
-    cdp_reduce8<6>(f, q, out);
+    for (int gp = 0; gp < 8; ++gp) {
+        float n, dx, dy, dz;
+        cdp_node_at(v.h, q, gp, n, dx, dy, dz);
+        const float4* r = reinterpret_cast<const float4*>(&st[lg][gp][0]);
+        const float4 t0 = r[0], t1 = r[1];
+        r6[0] += n * t0.x; r6[1] += n * t0.y; r6[2] += n * t0.z; r6[3] += n * t0.w; r6[4] += n * t1.x; r6[5] += n * t1.y;
+    }
     if (valid) {
         float* o = v.fes + (((size_t)inst * v.npe + e) * 8 + q) * 6;
 #pragma unroll
-        for (int c = 0; c < 6; ++c) o[c] = out[c];
+        for (int c = 0; c < 6; ++c) o[c] = W * r6[c];
     }
 }
 
@@ -849,7 +856,8 @@ __device__ __forceinline__ void cdp_block(const float* Mb, const float x[6], flo
 }
 
 // Stress rows of the PML nodes: R = -Fs - KG S - Gs Sbar + A (S - S_prev),
-// dS = Dinv R; S_next = S + dS and Sbar += dt S as pairs.
+// dS = Dinv R; S_next = S + dS and Sbar += dt S as pairs; and the next
+// step's displacement-row inputs (sdot = dS/dt, smid = S + dS/2, Sbar).
 __global__ void __launch_bounds__(256) k_cdp_su(CdpView v) {
     const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (gid >= (long long)v.ninst * v.np) return;
@@ -881,6 +889,8 @@ __global__ void __launch_bounds__(256) k_cdp_su(CdpView v) {
 #pragma unroll
     for (int c = 0; c < 6; ++c) R[c] = -F[c] - t1[c] - t2[c] + t3[c];
     cdp_block(K, R, dS);                  // Dinv R
+    float nx[20];
+    const float idt = 1.0f / v.dt;
 #pragma unroll
     for (int c = 0; c < 6; ++c) {
         float nh, nl;
@@ -891,7 +901,14 @@ __global__ void __launch_bounds__(256) k_cdp_su(CdpView v) {
         df_add(v.sbh[b + c], v.sbl[b + c], v.dt * sc[c], 0.f, bh, bl);
         v.sbh[b + c] = bh;
         v.sbl[b + c] = bl;
+        nx[c] = dS[c] * idt;
+        nx[6 + c] = sc[c] + 0.5f * dS[c];
+        nx[12 + c] = bh + bl;
     }
+    nx[18] = nx[19] = 0.f;
+    float4* o = reinterpret_cast<float4*>(v.vsu + ((size_t)inst * v.np + p) * 20);
+#pragma unroll
+    for (int i = 0; i < 5; ++i) o[i] = make_float4(nx[4 * i], nx[4 * i + 1], nx[4 * i + 2], nx[4 * i + 3]);
 }
 
 float host_tf32(double x) {
@@ -940,7 +957,7 @@ struct svl_cdx {
     float* fsol = nullptr;
     float *sh[2] = {nullptr, nullptr}, *sl[2] = {nullptr, nullptr};
     float *sbh = nullptr, *sbl = nullptr, *ubh = nullptr, *ubl = nullptr;
-    float *vin = nullptr, *feu = nullptr, *fes = nullptr, *uc = nullptr, *scs = nullptr, *egeo = nullptr, *eb0 = nullptr;
+    float *vin = nullptr, *vsu = nullptr, *feu = nullptr, *fes = nullptr, *uc = nullptr, *scs = nullptr, *estr = nullptr, *eb0 = nullptr;
     int32_t *enode = nullptr, *ninv = nullptr;
     long long* npad = nullptr;
     int cur = 0;                         // index of u_n in uh/ul
@@ -1109,7 +1126,7 @@ int svl_cdx_create(const svl_grid_spec* g, int32_t ninst, const svl_model_desc* 
     std::vector<int32_t> t2node;                     // total dof -> node (instance 0 numbering)
     std::vector<int32_t> enode, ninv;
     std::vector<long long> npad;
-    std::vector<float> egeo, eb0, uc, scs;
+    std::vector<float> estr, eb0, uc, scs;
     std::vector<int> pelem;                          // PML elements in element order
     std::vector<double> par0;                        // instance 0's PML parameters
 
@@ -1164,7 +1181,7 @@ int svl_cdx_create(const svl_grid_spec* g, int32_t ninst, const svl_model_desc* 
             if (h->npe > 0) {
                 par0.assign(m.pml_par.begin(), m.pml_par.end());
                 enode.resize((size_t)h->npe * 8);
-                egeo.resize((size_t)h->npe * 12);
+                estr.resize((size_t)h->npe * 12);
                 ninv.assign((size_t)h->np * 8, -1);
                 std::vector<int> fill(h->np, 0);
                 for (int i = 0; i < h->npe; ++i) {
@@ -1176,16 +1193,20 @@ int svl_cdx_create(const svl_grid_spec* g, int32_t ninst, const svl_model_desc* 
                         if (fill[pn] >= 8) { set_error("PML node %d in more than 8 elements", pn); return fail(SVL_ERR_INVALID); }
                         ninv[(size_t)pn * 8 + fill[pn]++] = i * 8 + a;
                     }
+                    // stretching at the two Gauss abscissae of every axis
+                    // (PML3DHexa8.cpp:952-996): a = 1 + a0 r, b = b0 r with
+                    // r = ((x - x0) n / L)^m; b0 depends on the material (per instance)
                     const int n1 = m.conn[(size_t)e * 8];
-                    for (int d = 0; d < 3; ++d) {
-                        egeo[(size_t)i * 12 + d] = (float)m.X[(size_t)n1 * 3 + d];
-                        egeo[(size_t)i * 12 + 3 + d] = (float)pp[3 + d];
-                        egeo[(size_t)i * 12 + 6 + d] = (float)pp[6 + d];
-                    }
                     const double pm = pp[0], L = pp[1], R = pp[2];
-                    egeo[(size_t)i * 12 + 9] = (float)((pm + 1.0) * (L / 10.0) / 2.0 / L * std::log(1.0 / R));
-                    egeo[(size_t)i * 12 + 10] = (float)L;
-                    egeo[(size_t)i * 12 + 11] = (float)pm;
+                    const double a0 = (pm + 1.0) * (L / 10.0) / 2.0 / L * std::log(1.0 / R);
+                    for (int d = 0; d < 3; ++d)
+                        for (int sgn = 0; sgn < 2; ++sgn) {
+                            const double xi = sgn ? kGaussAbscissa : -kGaussAbscissa;
+                            const double xg = m.X[(size_t)n1 * 3 + d] + 0.5 * g->h[d] * (1.0 + xi);
+                            const double r = std::pow((xg - pp[3 + d]) * pp[6 + d] / L, pm);
+                            estr[(size_t)i * 12 + 4 * d + sgn] = (float)(1.0 + a0 * r);
+                            estr[(size_t)i * 12 + 4 * d + 2 + sgn] = (float)r;
+                        }
                 }
             }
         } else {
@@ -1391,9 +1412,9 @@ int svl_cdx_create(const svl_grid_spec* g, int32_t ninst, const svl_model_desc* 
         if ((st = h->alloc(ns, &h->fsol)) || (st = h->alloc(n6, &h->sh[0])) || (st = h->alloc(n6, &h->sh[1])) ||
             (st = h->alloc(n6, &h->sl[0])) || (st = h->alloc(n6, &h->sl[1])) || (st = h->alloc(n6, &h->sbh)) ||
             (st = h->alloc(n6, &h->sbl)) || (st = h->alloc(n3, &h->ubh)) || (st = h->alloc(n3, &h->ubl)) ||
-            (st = h->alloc((size_t)ninst * h->np * 9, &h->vin)) ||
+            (st = h->alloc((size_t)ninst * h->np * 12, &h->vin)) || (st = h->alloc((size_t)ninst * h->np * 20, &h->vsu)) ||
             (st = h->alloc((size_t)ninst * h->npe * 24, &h->feu)) || (st = h->alloc((size_t)ninst * h->npe * 48, &h->fes)) ||
-            (st = h->upload(uc, &h->uc)) || (st = h->upload(scs, &h->scs)) || (st = h->upload(egeo, &h->egeo)) ||
+            (st = h->upload(uc, &h->uc)) || (st = h->upload(scs, &h->scs)) || (st = h->upload(estr, &h->estr)) ||
             (st = h->upload(eb0, &h->eb0)) || (st = h->upload(enode, &h->enode)) || (st = h->upload(ninv, &h->ninv)) ||
             (st = h->upload(npad, &h->npad)))
             return fail(st);
@@ -1454,6 +1475,16 @@ int svl_cdx_set_initial(svl_cdx* h, int32_t inst, const double* U0, const double
         CUDA_TRY(cudaMemsetAsync(h->sbl + o6, 0, n6 * 4, h->stream));
         CUDA_TRY(cudaMemsetAsync(h->ubh + (size_t)inst * h->np * 3, 0, (size_t)h->np * 12, h->stream));
         CUDA_TRY(cudaMemsetAsync(h->ubl + (size_t)inst * h->np * 3, 0, (size_t)h->np * 12, h->stream));
+        // the first step's displacement-row inputs: sdot, smid, Sbar = 0
+        std::vector<float> vs((size_t)h->np * 20, 0.f);
+        for (size_t k = 0; k < n6; ++k) {
+            const size_t p = k / 6, c = k % 6;
+            const double sc = (double)shi[k] + slo[k], sp = (double)sphi[k] + splo[k];
+            vs[p * 20 + c] = (float)((sc - sp) / h->dt);
+            vs[p * 20 + 6 + c] = (float)((sc + sp) / 2.0);
+        }
+        CUDA_TRY(cudaMemcpyAsync(h->vsu + (size_t)inst * h->np * 20, vs.data(), vs.size() * 4, cudaMemcpyHostToDevice,
+                                 h->stream));
     }
     CUDA_TRY(cudaStreamSynchronize(h->stream));
     h->va_valid = false;
@@ -1466,13 +1497,13 @@ static CdpView cdp_view(svl_cdx* h) {
     c.ninst = h->ninst; c.np = h->np; c.npe = h->npe;
     c.h = (float)h->hgrid; c.dt = (float)h->dt;
     c.per = (long long)(h->nstate / h->ninst);
-    c.enode = h->enode; c.egeo = h->egeo; c.eb0 = h->eb0; c.ninv = h->ninv; c.npad = h->npad;
+    c.enode = h->enode; c.estr = h->estr; c.eb0 = h->eb0; c.ninv = h->ninv; c.npad = h->npad;
     c.uc = h->uc; c.scs = h->scs;
     c.uh = h->uh[h->cur]; c.ul = h->ul[h->cur]; c.uph = h->uh[1 - h->cur]; c.upl = h->ul[1 - h->cur];
     c.fsol = h->fsol;
     c.ubh = h->ubh; c.ubl = h->ubl;
     c.sh = h->sh[h->cur]; c.sl = h->sl[h->cur]; c.sph = h->sh[1 - h->cur]; c.spl = h->sl[1 - h->cur];
-    c.sbh = h->sbh; c.sbl = h->sbl; c.vin = h->vin; c.feu = h->feu; c.fes = h->fes;
+    c.sbh = h->sbh; c.sbl = h->sbl; c.vin = h->vin; c.vsu = h->vsu; c.feu = h->feu; c.fes = h->fes;
     return c;
 }
 

@@ -439,6 +439,49 @@ int explicit_pml_tables(const HostModel& m, double dt, double mtol, const LoadTa
     for (size_t i = 0; i < pml.size(); ++i) pidx_of[pml[i]] = (int)i;
     std::vector<double> ml;
     element_lumped_masses(m, ml);                 // [(e nen + a) nd + j]
+    // per PML element, matrix w and node j the Gauss sum g = sum_q s_w N_j w|J|
+    // (every entry of the node's lumped blocks is g times a material constant),
+    // in parallel; assembled below in element order
+    std::vector<double> gs((size_t)pml.size() * 4 * nen, 0.0);
+    parallel_for((int64_t)pml.size(), [&](int64_t i0, int64_t i1) {
+        for (int64_t i = i0; i < i1; ++i) {
+            const int e = pml[i];
+            const double* pr = m.param(e);
+            const double E = pr[0], nu = pr[1], rho = pr[2];
+            const double mu = E / 2.0 / (1 + nu), lambda = E * nu / (1.0 + nu) / (1.0 - 2.0 * nu);
+            const double* par = &m.pml_par[(size_t)e * npar];
+            const double pm = par[0], L = par[1], R = par[2];
+            const double Vp = std::sqrt((lambda + 2.0 * mu) / rho);
+            const double a0 = (pm + 1.0) * (L / 10.0) / 2.0 / L * std::log(1.0 / R);
+            const double b0 = (pm + 1.0) * Vp / 2.0 / L * std::log(1.0 / R);
+            double* g = &gs[(size_t)i * 4 * nen];
+            for (int q = 0; q < m.ngp; ++q) {
+                double dNx[8][3], N[8];
+                const double det = gp_geometry(m, e, q, dNx, N);
+                const double f = gp_factor(m, e, det);
+                double xg[3] = {0, 0, 0};
+                for (int a = 0; a < nen; ++a)
+                    for (int k = 0; k < nd; ++k) xg[k] += N[a] * m.X[(size_t)m.conn[(size_t)e * nen + a] * nd + k];
+                double as[3] = {1, 1, 1}, bs[3] = {0, 0, 0};
+                for (int k = 0; k < nd; ++k) {
+                    const double r = std::pow((xg[k] - par[3 + k]) * par[3 + nd + k] / L, pm);
+                    as[k] = 1.0 + a0 * r;
+                    bs[k] = b0 * r;
+                }
+                double sc[4];
+                if (nd == 2) {
+                    sc[0] = as[0] * as[1]; sc[1] = as[0] * bs[1] + as[1] * bs[0]; sc[2] = bs[0] * bs[1]; sc[3] = 0.0;
+                } else {
+                    sc[0] = as[0] * as[1] * as[2];
+                    sc[1] = as[0] * as[1] * bs[2] + as[0] * bs[1] * as[2] + bs[0] * as[1] * as[2];
+                    sc[2] = as[0] * bs[1] * bs[2] + bs[0] * bs[1] * as[2] + bs[0] * as[1] * bs[2];
+                    sc[3] = bs[0] * bs[1] * bs[2];
+                }
+                for (int w = 0; w < 4; ++w)
+                    for (int j = 0; j < nen; ++j) g[w * nen + j] += sc[w] * (N[j] * f);
+            }
+        }
+    });
     for (int e = 0; e < m.nelem; ++e) {
         if (sidx_of[e] >= 0) {
             const double am = m.ray.empty() ? 0.0 : m.ray[2 * (size_t)e];
@@ -454,58 +497,29 @@ int explicit_pml_tables(const HostModel& m, double dt, double mtol, const LoadTa
         const double* pr = m.param(e);
         const double E = pr[0], nu = pr[1], rho = pr[2];
         const double mu = E / 2.0 / (1 + nu), lambda = E * nu / (1.0 + nu) / (1.0 - 2.0 * nu);
-        const double* par = &m.pml_par[(size_t)e * npar];
-        const double pm = par[0], L = par[1], R = par[2];
-        const double Vp = std::sqrt((lambda + 2.0 * mu) / rho);
-        const double a0 = (pm + 1.0) * (L / 10.0) / 2.0 / L * std::log(1.0 / R);
-        const double b0 = (pm + 1.0) * Vp / 2.0 / L * std::log(1.0 / R);
-        for (int q = 0; q < m.ngp; ++q) {
-            double dNx[8][3], N[8];
-            const double det = gp_geometry(m, e, q, dNx, N);
-            const double f = gp_factor(m, e, det);
-            double xg[3] = {0, 0, 0};
-            for (int a = 0; a < nen; ++a)
-                for (int i = 0; i < nd; ++i) xg[i] += N[a] * m.X[(size_t)m.conn[(size_t)e * nen + a] * nd + i];
-            double as[3] = {1, 1, 1}, bs[3] = {0, 0, 0};
-            for (int i = 0; i < nd; ++i) {
-                const double r = std::pow((xg[i] - par[3 + i]) * par[3 + nd + i] / L, pm);
-                as[i] = 1.0 + a0 * r;
-                bs[i] = b0 * r;
-            }
-            double sc[4];
-            if (nd == 2) {
-                sc[0] = as[0] * as[1]; sc[1] = as[0] * bs[1] + as[1] * bs[0]; sc[2] = bs[0] * bs[1]; sc[3] = 0.0;
-            } else {
-                sc[0] = as[0] * as[1] * as[2];
-                sc[1] = as[0] * as[1] * bs[2] + as[0] * bs[1] * as[2] + bs[0] * as[1] * as[2];
-                sc[2] = as[0] * bs[1] * bs[2] + bs[0] * bs[1] * as[2] + bs[0] * as[1] * bs[2];
-                sc[3] = bs[0] * bs[1] * bs[2];
-            }
-            std::vector<double>* du[4] = {&Mu, &Cu, &Ku, &Gu};
-            for (int w = 0; w < 4; ++w) {
-                const double sw = sc[w];
-                if (sw == 0.0) continue;
-                for (int j = 0; j < nen; ++j) {
-                    const int n = m.conn[(size_t)e * nen + j];
-                    const double Nf = N[j] * f;
-                    for (int c = 0; c < nd; ++c) (*du[w])[m.tdof_all[(size_t)n * m.dstride + c]] += rho * sw * Nf;
-                    double* B = &Bl[w][(size_t)snode_of[n] * nb];
-                    if (nd == 2) {
-                        const double k2 = sw * (lambda + 2.0 * mu) / 4.0 / mu / (lambda + mu);
-                        const double l2 = sw * lambda / 4.0 / mu / (lambda + mu);
-                        B[0 * 3 + 0] += -k2 * Nf; B[1 * 3 + 1] += -k2 * Nf;
-                        B[0 * 3 + 1] += l2 * Nf; B[1 * 3 + 0] += l2 * Nf;
-                        B[2 * 3 + 2] += -sw / mu * Nf;
-                    } else {
-                        const double kap = sw * (lambda + mu) / mu / (3.0 * lambda + 2.0 * mu);
-                        const double lam = sw * lambda / 2.0 / mu / (3.0 * lambda + 2.0 * mu);
-                        for (int r = 0; r < 3; ++r)
-                            for (int c = 0; c < 3; ++c) B[r * 6 + c] += (r == c ? -kap : lam) * Nf;
-                        for (int r = 3; r < 6; ++r) B[r * 6 + r] += -sw / mu * Nf;
-                    }
+        const double* g = &gs[(size_t)pidx_of[e] * 4 * nen];
+        std::vector<double>* du[4] = {&Mu, &Cu, &Ku, &Gu};
+        for (int w = 0; w < 4; ++w)
+            for (int j = 0; j < nen; ++j) {
+                const double gw = g[w * nen + j];
+                if (gw == 0.0) continue;
+                const int n = m.conn[(size_t)e * nen + j];
+                for (int c = 0; c < nd; ++c) (*du[w])[m.tdof_all[(size_t)n * m.dstride + c]] += rho * gw;
+                double* B = &Bl[w][(size_t)snode_of[n] * nb];
+                if (nd == 2) {
+                    const double k2 = (lambda + 2.0 * mu) / 4.0 / mu / (lambda + mu);
+                    const double l2 = lambda / 4.0 / mu / (lambda + mu);
+                    B[0 * 3 + 0] += -k2 * gw; B[1 * 3 + 1] += -k2 * gw;
+                    B[0 * 3 + 1] += l2 * gw; B[1 * 3 + 0] += l2 * gw;
+                    B[2 * 3 + 2] += -gw / mu;
+                } else {
+                    const double kap = (lambda + mu) / mu / (3.0 * lambda + 2.0 * mu);
+                    const double lam = lambda / 2.0 / mu / (3.0 * lambda + 2.0 * mu);
+                    for (int r = 0; r < 3; ++r)
+                        for (int c = 0; c < 3; ++c) B[r * 6 + c] += (r == c ? -kap : lam) * gw;
+                    for (int r = 3; r < 6; ++r) B[r * 6 + r] += -gw / mu;
                 }
             }
-        }
     }
     if (!m.nodemass.empty())
         for (int t = 0; t < nt; ++t) if (std::fabs(m.nodemass[t]) > mtol) Mu[t] += m.nodemass[t];
