@@ -356,7 +356,13 @@ typedef struct svl_nm_opts {
     int32_t cnvgtest;    /* Newton: 4 relative unbalanced force (the reference's
                             default), 5 relative displacement increment
                             (Algorithm.cpp:122-188)                               */
-    int32_t reserved;
+    int32_t single_inner;/* 1: the inner iterations of each solve apply the
+                            effective stiffness in single precision (elastic
+                            models without damping or constraints; others
+                            ignore it); every answer is confirmed with the FP64
+                            operator -- the true residual -- and the solve
+                            restarts from it until pcg_tol holds, so the result
+                            keeps the FP64 tolerance.  0: FP64 throughout.      */
 } svl_nm_opts;
 
 typedef struct svl_nm svl_nm;

@@ -1703,6 +1703,122 @@ __global__ void __launch_bounds__(256) k_nm_apply(DevView d, const double* __res
     }
 }
 
+// ---- single-precision operator of the inner solve iterations ----------------
+// q = (K + 4/dt^2 M) v for elastic models without damping or constraints:
+// the element action in FP32, one thread per (element, Gauss point) on float
+// geometry tables, node values shared by warp shuffles, the element vector
+// summed by a butterfly over the element's lanes; the per-node gather sums
+// the float element entries in element order and adds the lumped-mass term
+// in FP64.  The solves confirm every answer with the FP64 operator (true
+// residual) and restart from it, so the result keeps the FP64 tolerance.
+__global__ void k_nm_expand_f(DevView d, const double* __restrict__ pf, double* __restrict__ pt,
+                              float* __restrict__ pt_f) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= d.ntotal) return;
+    const int f = d.tfree[t];
+    const double v = f >= 0 ? pf[f] : 0.0;
+    pt[t] = v;
+    pt_f[t] = (float)v;
+}
+
+template <int ND, int NEN>
+__global__ void __launch_bounds__(128) k_nm_op_f(DevView d, const float* __restrict__ geo_f,
+                                                  const float* __restrict__ coef_f, const float* __restrict__ pt,
+                                                  float* __restrict__ fe_f) {
+    constexpr int NC = ND * NEN, PER = NEN * ND + 1;
+    const int E = d.nelem;
+    const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int e = gtid / NEN, q = gtid % NEN;
+    const bool valid = e < E;
+    const int ec = valid ? e : E - 1;
+    const int lane = threadIdx.x & 31, base = lane - q;
+    float pq[ND];
+#pragma unroll
+    for (int c = 0; c < ND; ++c) pq[c] = pt[d.edof[(size_t)(q * ND + c) * E + ec]];
+    const float c1 = coef_f[ec], c2 = coef_f[(size_t)E + ec], c3 = coef_f[2 * (size_t)E + ec];
+    const float* g = geo_f + ((size_t)d.egeo[ec] * NEN + q) * PER;
+    float b[NEN][3];
+#pragma unroll
+    for (int a = 0; a < NEN; ++a)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) b[a][j] = (j < ND) ? g[a * ND + j] : 0.0f;
+    const float w = g[PER - 1];
+    float ev[6] = {0, 0, 0, 0, 0, 0};
+#pragma unroll
+    for (int a = 0; a < NEN; ++a) {
+        float ua[3] = {0, 0, 0};
+#pragma unroll
+        for (int c = 0; c < ND; ++c) ua[c] = __shfl_sync(0xffffffffu, pq[c], base + a);
+        if (ND == 2) {
+            ev[0] += b[a][0] * ua[0];
+            ev[1] += b[a][1] * ua[1];
+            ev[2] += b[a][1] * ua[0] + b[a][0] * ua[1];
+        } else {
+            ev[0] += b[a][0] * ua[0];
+            ev[1] += b[a][1] * ua[1];
+            ev[2] += b[a][2] * ua[2];
+            ev[3] += b[a][1] * ua[0] + b[a][0] * ua[1];
+            ev[4] += b[a][2] * ua[1] + b[a][1] * ua[2];
+            ev[5] += b[a][2] * ua[0] + b[a][0] * ua[2];
+        }
+    }
+    float sig[6];
+    if (ND == 2) {
+        sig[0] = c1 * ev[0] + c2 * ev[1]; sig[1] = c2 * ev[0] + c1 * ev[1]; sig[2] = c3 * ev[2];
+    } else {
+        sig[0] = c1 * ev[0] + c2 * ev[1] + c2 * ev[2];
+        sig[1] = c2 * ev[0] + c1 * ev[1] + c2 * ev[2];
+        sig[2] = c2 * ev[0] + c2 * ev[1] + c1 * ev[2];
+        sig[3] = c3 * ev[3]; sig[4] = c3 * ev[4]; sig[5] = c3 * ev[5];
+    }
+    float y[NC];
+#pragma unroll
+    for (int a = 0; a < NEN; ++a) {
+        if (ND == 2) {
+            y[2 * a] = w * (b[a][0] * sig[0] + b[a][1] * sig[2]);
+            y[2 * a + 1] = w * (b[a][1] * sig[1] + b[a][0] * sig[2]);
+        } else {
+            const float bx = b[a][0], by = b[a][1], bz = b[a][2];
+            y[3 * a] = w * (bx * sig[0] + by * sig[3] + bz * sig[5]);
+            y[3 * a + 1] = w * (by * sig[1] + bx * sig[3] + bz * sig[4]);
+            y[3 * a + 2] = w * (bz * sig[2] + by * sig[4] + bx * sig[5]);
+        }
+    }
+#pragma unroll
+    for (int off = 1; off < NEN; off <<= 1)
+#pragma unroll
+        for (int j = 0; j < NC; ++j) y[j] += __shfl_xor_sync(0xffffffffu, y[j], off);
+    if (!valid) return;
+#pragma unroll
+    for (int c = 0; c < ND; ++c) {
+        float mine = 0.f;
+#pragma unroll
+        for (int a = 0; a < NEN; ++a)
+            if (a == q) mine = y[a * ND + c];
+        fe_f[(size_t)(q * ND + c) * E + e] = mine;
+    }
+}
+
+template <int ND>
+__global__ void __launch_bounds__(256) k_nm_apply_f(DevView d, const float* __restrict__ fe_f,
+                                                     const double* __restrict__ pt, double* __restrict__ q, double c_m) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= d.nnode) return;
+    const int E = d.nelem;
+#pragma unroll
+    for (int c = 0; c < ND; ++c) {
+        const int t = d.ntdof[n * ND + c];
+        const int f = d.tfree[t];
+        if (f < 0) continue;
+        float s = 0.f;
+        for (int i = d.inv_ptr[n]; i < d.inv_ptr[n + 1]; ++i) {
+            const int ent = d.inv_ent[i];
+            s += fe_f[(size_t)((ent & 7) * ND + c) * E + (ent >> 3)];
+        }
+        q[f] = (double)s + c_m * d.Md[t] * pt[t];
+    }
+}
+
 // x += alpha p; r -= alpha q; z = Dinv r   (alpha = rz / pq)
 __global__ void k_pcg_xr(const double* __restrict__ sc, const double* __restrict__ p, const double* __restrict__ q,
                          const double* __restrict__ dinv, double* x, double* r, double* z, int n) {
@@ -1874,6 +1990,9 @@ struct svl_nm {
     bool newton = false, tangent = false;   // tangent: J2 elements present (stored tangents)
     int64_t newton_iters_total = 0, newton_iters_last = 0;
     double newton_res_last = 0.0;
+    // single-precision operator of the inner iterations (eligible models only)
+    bool fast_op = false;
+    float *geo_f = nullptr, *coef_f = nullptr, *pt_f = nullptr, *fe_f = nullptr;
     // CG iterates recorded for training pairs
     int rec_every = 0, rec_n = 0;
     std::vector<double*> rec_x, rec_r;
@@ -1928,11 +2047,25 @@ static int nm_op_total(svl_nm* nm, const double* pt, double* out) {
     return SVL_OK;
 }
 
-// q = Keff v (free dofs)
-static int nm_apply(svl_nm* nm, const double* v, double* q) {
+// q = Keff v (free dofs); inner: an inner solve iteration, which takes the
+// single-precision operator when the handle has one
+static int nm_apply(svl_nm* nm, const double* v, double* q, bool inner = false) {
     svl_cd* cd = nm->cd;
     const HostModel& m = cd->m;
     const int tb = 256;
+    if (inner && nm->fast_op) {
+        DevView d = cd->d;
+        k_nm_expand_f<<<(m.ntotal + tb - 1) / tb, tb, 0, cd->stream>>>(d, v, nm->pt, nm->pt_f);
+        const int gg = (int)(((int64_t)m.nelem * m.nen + 127) / 128);
+        if (m.ndim == 2) k_nm_op_f<2, 4><<<gg, 128, 0, cd->stream>>>(d, nm->geo_f, nm->coef_f, nm->pt_f, nm->fe_f);
+        else k_nm_op_f<3, 8><<<gg, 128, 0, cd->stream>>>(d, nm->geo_f, nm->coef_f, nm->pt_f, nm->fe_f);
+        const double c_m = 4.0 / nm->opts.dt / nm->opts.dt;
+        if (m.ndim == 2) k_nm_apply_f<2><<<(m.nnode + tb - 1) / tb, tb, 0, cd->stream>>>(d, nm->fe_f, nm->pt, q, c_m);
+        else k_nm_apply_f<3><<<(m.nnode + tb - 1) / tb, tb, 0, cd->stream>>>(d, nm->fe_f, nm->pt, q, c_m);
+        cd->launches += 3;
+        CUDA_TRY(cudaGetLastError());
+        return SVL_OK;
+    }
     if (nm->general) {                      // q = T^T (K + c_m M) T v
         k_nmg_expand<<<(m.ntotal + tb - 1) / tb, tb, 0, cd->stream>>>(cd->d, v, nm->pt);
         TRY(nm_op_total(nm, nm->pt, nm->ft));
@@ -1992,7 +2125,7 @@ static int nm_solve_jacobi(svl_nm* nm, bool warm, int64_t maxit) {
     if (warm && hs[S_RR] <= tol2) { nm->res_last = std::sqrt(hs[S_RR] / bb); return SVL_OK; }
     const int check = 4;
     for (int64_t it = 1; it <= maxit; ++it) {
-        TRY(nm_apply(nm, nm->p, nm->q));
+        TRY(nm_apply(nm, nm->p, nm->q, true));
         nm_dot(nm, nm->p, nm->q, S_PQ);
         k_pcg_xr<<<g, tb, 0, cd->stream>>>(nm->sc, nm->p, nm->q, nm->dinv, nm->x, nm->r, nm->z, n);
         nm_dot2(nm, nm->r, nm->z, S_RZN, nm->r, nm->r, S_RR);
@@ -2050,7 +2183,7 @@ static int nm_solve_learned(svl_nm* nm, bool allow_fallback = true) {
     const int check = 4;
     bool cold = false;
     for (int64_t it = 1; it <= budget; ++it) {
-        TRY(nm_apply(nm, nm->p, nm->q));
+        TRY(nm_apply(nm, nm->p, nm->q, true));
         nm_dot2(nm, nm->p, nm->q, S_PQ, nm->r, nm->p, S_RP);
         k_fcg_xr<<<g, tb, 0, cd->stream>>>(nm->sc, nm->p, nm->q, nm->x, nm->r, n);
         TRY(svl::nn_apply(nm->nn, nm->r, nm->z));
@@ -2265,6 +2398,24 @@ int svl_nm_create(const svl_model_desc* model, const svl_load_desc* loads, const
         double* ct = nullptr;
         if ((st = cd->zeros((size_t)(m.ndim == 2 ? 9 : 36) * m.ngp * m.nelem, &ct))) return fail(st);
         cd->d.ctan = ct;
+    }
+    // single-precision operator of the inner iterations: elastic models without
+    // damping or constraints (the FP64 operator confirms every answer)
+    if (opts->single_inner && !nm->general && !nm->tangent && !m.has_j2() && !cd->d.dk0 && m.nelem > 0 && m.nfree > 0) {
+        const int per = m.nen * m.ndim + 1;
+        std::vector<double> gh((size_t)cd->ngeo * m.ngp * per), ch((size_t)3 * m.nelem);
+        if (cudaMemcpy(gh.data(), cd->d.geo, gh.size() * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess ||
+            cudaMemcpy(ch.data(), cd->d.ecoef, ch.size() * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess) {
+            set_error("reading the operator tables failed"); return fail(SVL_ERR_CUDA);
+        }
+        std::vector<float> gf(gh.begin(), gh.end()), cf(ch.begin(), ch.end());
+        const float *g2 = nullptr, *c2 = nullptr;
+        float *p2 = nullptr, *f2 = nullptr;
+        if ((st = cd->upload(gf, &g2)) || (st = cd->upload(cf, &c2)) || (st = cd->zeros((size_t)m.ntotal, &p2)) ||
+            (st = cd->zeros((size_t)nc * m.nelem, &f2)))
+            return fail(st);
+        nm->geo_f = const_cast<float*>(g2); nm->coef_f = const_cast<float*>(c2); nm->pt_f = p2; nm->fe_f = f2;
+        nm->fast_op = true;
     }
     // lattice models: the maps and scalings of the learned preconditioner
     int dims[3];

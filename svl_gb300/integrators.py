@@ -318,10 +318,15 @@ class NewmarkBeta:
 
     def __init__(self, model: Model, loads: Loads | None, dt: float, pcg_tol: float = 1e-8,
                  pcg_maxit: int = 20000, ftol: float = 1e-12, mtol: float = 1e-12, precond: int = 0,
-                 algorithm: str = "linear", maxit: int = 50, cnvgtol: float = 1e-6, cnvgtest: int = 4):
+                 algorithm: str = "linear", maxit: int = 50, cnvgtol: float = 1e-6, cnvgtest: int = 4,
+                 single_inner: bool = True):
         """algorithm "linear" (Linear.cpp) or "newton" (NewtonRaphson.cpp, with
         `maxit` iterations, tolerance `cnvgtol` and convergence test `cnvgtest`:
-        4 relative unbalanced force, 5 relative displacement increment)."""
+        4 relative unbalanced force, 5 relative displacement increment).
+        single_inner: the inner iterations of each solve apply the effective
+        stiffness in single precision on elastic models without damping or
+        constraints; every answer is confirmed with the FP64 operator (true
+        residual) and the solve restarts from it, so the tolerance holds."""
         self.model = model
         self.dt = float(dt)
         self._md = model.desc()
@@ -329,7 +334,7 @@ class NewmarkBeta:
         algo = {"linear": capi.SVL_ALGO_LINEAR, "newton": capi.SVL_ALGO_NEWTON}[algorithm.lower()]
         opts = capi.NmOpts(dt=self.dt, ftol=ftol, mtol=mtol, pcg_tol=float(pcg_tol), pcg_maxit=int(pcg_maxit),
                            precond=int(precond), algorithm=algo, maxit=int(maxit), cnvgtol=float(cnvgtol),
-                           cnvgtest=int(cnvgtest))
+                           cnvgtest=int(cnvgtest), single_inner=1 if single_inner else 0)
         h = C.c_void_p()
         check(lib().svl_nm_create(C.byref(self._md), C.byref(self._ld), C.byref(opts), C.byref(h)))
         self._h = h
@@ -476,7 +481,7 @@ def _central_difference_pml(model, loads, dt, ftol=1e-12, mtol=1e-12, check_ever
 
 def _newmark_pml(model: Model, loads: Loads | None, dt: float, pcg_tol: float = 1e-8, pcg_maxit: int = 20000,
                  ftol: float = 1e-12, mtol: float = 1e-12, precond: int = 0, algorithm: str = "linear",
-                 maxit: int = 50, cnvgtol: float = 1e-6, cnvgtest: int = 4):
+                 maxit: int = 50, cnvgtol: float = 1e-6, cnvgtest: int = 4, single_inner: bool = True):
     if precond != capi.SVL_PRECOND_JACOBI:
         raise capi.SvlError(capi.SVL_ERR_UNSUPPORTED, "the learned preconditioner does not cover PML models")
     return ExtendedNewmarkBeta(model, loads, dt, tol=pcg_tol, solver_maxit=int(pcg_maxit), ftol=ftol,
