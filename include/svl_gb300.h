@@ -505,7 +505,10 @@ typedef struct svl_nn_train_opts {
     uint64_t seed;
     int32_t  max_sweeps;   /* synthetic pair i gets i % (max_sweeps + 1)
                               smoothing sweeps (0 = the default, 5)           */
-    int32_t  reserved;
+    int32_t  crop;         /* > 0: every sample is a random crop x crop x crop
+                              window of a pair, the loss masked 4 nodes inside
+                              window faces that lie inside the lattice (the
+                              network's reach); 0: the whole lattice          */
 } svl_nn_train_opts;
 /* Runs the solve_steps steps k_first.. (they advance the state), generates
  * the synthetic pairs, trains, and switches the handle to

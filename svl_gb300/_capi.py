@@ -108,7 +108,7 @@ SVL_XNM_CENTRAL_DIFFERENCE = 2
 class NnTrainOpts(C.Structure):
     _fields_ = [("solve_steps", C.c_int32), ("record_every", C.c_int32), ("n_synthetic", C.c_int32),
                 ("iters", C.c_int32), ("batch", C.c_int32), ("lr", C.c_float), ("seed", C.c_uint64),
-                ("max_sweeps", C.c_int32), ("reserved", C.c_int32)]
+                ("max_sweeps", C.c_int32), ("crop", C.c_int32)]
 
 
 def ptr(a, ctype):

@@ -2754,6 +2754,7 @@ int svl_nm_train_preconditioner(svl_nm* nm, int32_t k_first, const svl_nn_train_
     }
     svl_cd* cd = nm->cd;
     if (!nm->nn) TRY(svl::nn_create(nm->lnx, nm->lny, nm->lnz, nm->gmap, nm->sdinv_h, nm->rho_h, cd->stream, &nm->nn));
+    TRY(svl::nn_set_crop(nm->nn, o->crop));
     // 1. Newmark steps with Jacobi-PCG, recording CG iterates
     if (o->solve_steps > 0) {
         while ((int)nm->rec_x.size() < kRecMax) {
@@ -2777,13 +2778,15 @@ int svl_nm_train_preconditioner(svl_nm* nm, int32_t k_first, const svl_nn_train_
     double hs[S_NSCAL];
     for (int i = 0; i < o->n_synthetic; ++i) {
         k_randn<<<g, tb, 0, cd->stream>>>(nm->e1, n, o->seed * 0x9E3779B97F4A7C15ull + (uint64_t)i * 0x100000001B3ull);
+        // (the single-precision operator where the handle has one: training
+        // data need no FP64 accuracy)
         for (int sweep = 0; sweep < i % (max_sweeps + 1); ++sweep) {
             k_vmul<<<g, tb, 0, cd->stream>>>(nm->e1, nm->sdinv, nm->e2, n);
-            TRY(nm_apply(nm, nm->e2, nm->q));
+            TRY(nm_apply(nm, nm->e2, nm->q, true));
             k_smooth<<<g, tb, 0, cd->stream>>>(nm->e1, nm->q, nm->sdinv, 0.5, n);
         }
         k_vmul<<<g, tb, 0, cd->stream>>>(nm->e1, nm->sdinv, nm->e2, n);
-        TRY(nm_apply(nm, nm->e2, nm->q));
+        TRY(nm_apply(nm, nm->e2, nm->q, true));
         k_vmul<<<g, tb, 0, cd->stream>>>(nm->q, nm->sdinv, nm->e2, n);
         nm_dot(nm, nm->e1, nm->e1, S_RP);
         TRY(nm_scalars(nm, hs));

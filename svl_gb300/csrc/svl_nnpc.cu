@@ -146,6 +146,33 @@ __global__ void k_feat_grid(const float* __restrict__ x, const float* __restrict
     f[n3 + i] = rho[i] * v;
 }
 
+// dst[c][k][j][i] = src[c][oz + k][oy + j][ox + i], c < 3: a window of a
+// lattice grid (training on crops)
+__global__ void k_crop(const float* __restrict__ src, float* __restrict__ dst, Dims full, Dims cr, int ox, int oy, int oz) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= 3 * cr.V) return;
+    const int c = i / cr.V, v = i % cr.V;
+    const int x = v % cr.nx, y = (v / cr.nx) % cr.ny, z = v / (cr.nx * cr.ny);
+    dst[i] = src[(size_t)c * full.V + ((size_t)(oz + z) * full.ny + (oy + y)) * full.nx + (ox + x)];
+}
+
+// loss mask of a window: the lattice mask, zero within `margin` voxels of a
+// window face that lies inside the lattice (there the zero padding of the
+// window differs from the lattice's neighbours; 4 = the network's reach)
+__global__ void k_crop_mask(const float* __restrict__ mask, float* __restrict__ dst, Dims full, Dims cr, int ox, int oy,
+                            int oz, int margin) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= 3 * cr.V) return;
+    const int c = i / cr.V, v = i % cr.V;
+    const int x = v % cr.nx, y = (v / cr.nx) % cr.ny, z = v / (cr.nx * cr.ny);
+    float m = mask[(size_t)c * full.V + ((size_t)(oz + z) * full.ny + (oy + y)) * full.nx + (ox + x)];
+    if ((ox > 0 && x < margin) || (ox + cr.nx < full.nx && x >= cr.nx - margin) ||
+        (oy > 0 && y < margin) || (oy + cr.ny < full.ny && y >= cr.ny - margin) ||
+        (oz > 0 && z < margin) || (oz + cr.nz < full.nz && z >= cr.nz - margin))
+        m = 0.f;
+    dst[i] = m;
+}
+
 // features from a free-dof residual (grid pre-zeroed)
 __global__ void k_feat_free(const double* __restrict__ r, const double* __restrict__ sdinv,
                             const float* __restrict__ rho_grid, const int32_t* __restrict__ gmap, float* __restrict__ f,
@@ -519,6 +546,9 @@ struct NnPrecond {
     float* lsum = nullptr;     // loss accumulator(s)
     std::vector<float*> X, Y;  // training pairs [3][V] each
     int nblk_wg = 0;
+    // training on crops: window side (0 = the whole lattice) and window buffers
+    int crop = 0;
+    float *cx = nullptr, *ct = nullptr, *crho = nullptr, *cmask = nullptr;
     // tensor-core inference
     int use_tc = 1;
     bool tc_ready = false;
@@ -544,16 +574,18 @@ struct NnPrecond {
         for (void* p : allocs) cudaFree(p);
     }
 
-    // forward of features already in `feat`; keeps activations
-    int forward() {
-        const int g = nblocks(d.V);
-        k_conv<kNnIn, kNnHid, true><<<g, kThreads, 0, stream>>>(feat, W + kLayers[0].off, a0, d, nullptr);
-        k_conv<kNnHid, kNnHid, true><<<g, kThreads, 0, stream>>>(a0, W + kLayers[1].off, a1, d, nullptr);
-        k_conv<kNnHid, kNnHid, true><<<g, kThreads, 0, stream>>>(a1, W + kLayers[2].off, a2, d, nullptr);
-        k_conv<kNnHid, kNnOut, false><<<g, kThreads, 0, stream>>>(a2, W + kLayers[3].off, y, d, nullptr);
+    // forward of features already in `feat` on grid dd (the lattice or a
+    // window of it); keeps activations
+    int forward(const Dims& dd) {
+        const int g = nblocks(dd.V);
+        k_conv<kNnIn, kNnHid, true><<<g, kThreads, 0, stream>>>(feat, W + kLayers[0].off, a0, dd, nullptr);
+        k_conv<kNnHid, kNnHid, true><<<g, kThreads, 0, stream>>>(a0, W + kLayers[1].off, a1, dd, nullptr);
+        k_conv<kNnHid, kNnHid, true><<<g, kThreads, 0, stream>>>(a1, W + kLayers[2].off, a2, dd, nullptr);
+        k_conv<kNnHid, kNnOut, false><<<g, kThreads, 0, stream>>>(a2, W + kLayers[3].off, y, dd, nullptr);
         NN_TRY(cudaGetLastError());
         return SVL_OK;
     }
+    int forward() { return forward(d); }
 
     int prepare_tc() {
         for (int l = 0; l < 4; ++l)
@@ -579,40 +611,46 @@ struct NnPrecond {
     }
 
     template <int CIN, int COUT>
-    int wgrad(const float* gout, const float* ain, int layer) {
-        dim3 grid(nblk_wg, kNnTaps);
-        k_wgrad<CIN, COUT><<<grid, kThreads, 0, stream>>>(gout, ain, partial, d);
+    int wgrad(const float* gout, const float* ain, int layer, const Dims& dd) {
+        const int nb = (dd.V + kWgChunk - 1) / kWgChunk;
+        dim3 grid(nb, kNnTaps);
+        k_wgrad<CIN, COUT><<<grid, kThreads, 0, stream>>>(gout, ain, partial, dd);
         const int n = CIN * COUT * kNnTaps;
-        k_wgrad_reduce<<<nblocks(n), kThreads, 0, stream>>>(partial, G + kLayers[layer].off, CIN, COUT, nblk_wg);
+        k_wgrad_reduce<<<nblocks(n), kThreads, 0, stream>>>(partial, G + kLayers[layer].off, CIN, COUT, nb);
         NN_TRY(cudaGetLastError());
         return SVL_OK;
     }
 
     // data gradient through layer `layer` (cout -> cin), gated by the layer input's relu
     template <int CIN, int COUT>
-    int dgrad(const float* gout, float* gin, const float* gate, int layer) {
+    int dgrad(const float* gout, float* gin, const float* gate, int layer, const Dims& dd) {
         const int n = CIN * COUT * kNnTaps;
         k_flip<<<nblocks(n), kThreads, 0, stream>>>(W + kLayers[layer].off, Wt, CIN, COUT);
-        k_conv<COUT, CIN, false><<<nblocks(d.V), kThreads, 0, stream>>>(gout, Wt, gin, d, gate);
+        k_conv<COUT, CIN, false><<<nblocks(dd.V), kThreads, 0, stream>>>(gout, Wt, gin, dd, gate);
         NN_TRY(cudaGetLastError());
         return SVL_OK;
     }
 
-    // features of pair p, forward, loss into lsum[slot], gradient accumulated into G
-    int sample(const float* x, const float* t, float gscale, float* lslot) {
-        const int n3 = 3 * d.V;
-        k_feat_grid<<<nblocks(n3), kThreads, 0, stream>>>(x, rho, feat, n3);
-        if (int st = forward()) return st;
-        k_loss<<<kRedBlocks, kThreads, 0, stream>>>(y, x, t, mask, g3, gscale, lpart, n3);
+    // features of one pair on grid dd (rho and mask of that grid), forward,
+    // loss into lslot, gradient accumulated into G
+    int sample(const float* x, const float* t, float gscale, float* lslot, const Dims& dd, const float* rg,
+               const float* mg) {
+        const int n3 = 3 * dd.V;
+        k_feat_grid<<<nblocks(n3), kThreads, 0, stream>>>(x, rg, feat, n3);
+        if (int st = forward(dd)) return st;
+        k_loss<<<kRedBlocks, kThreads, 0, stream>>>(y, x, t, mg, g3, gscale, lpart, n3);
         k_loss_final<<<1, 32, 0, stream>>>(lpart, lslot, kRedBlocks);
-        if (int st = wgrad<kNnHid, kNnOut>(g3, a2, 3)) return st;
-        if (int st = dgrad<kNnHid, kNnOut>(g3, gA, a2, 3)) return st;
-        if (int st = wgrad<kNnHid, kNnHid>(gA, a1, 2)) return st;
-        if (int st = dgrad<kNnHid, kNnHid>(gA, gB, a1, 2)) return st;
-        if (int st = wgrad<kNnHid, kNnHid>(gB, a0, 1)) return st;
-        if (int st = dgrad<kNnHid, kNnHid>(gB, gA, a0, 1)) return st;
-        if (int st = wgrad<kNnIn, kNnHid>(gA, feat, 0)) return st;
+        if (int st = wgrad<kNnHid, kNnOut>(g3, a2, 3, dd)) return st;
+        if (int st = dgrad<kNnHid, kNnOut>(g3, gA, a2, 3, dd)) return st;
+        if (int st = wgrad<kNnHid, kNnHid>(gA, a1, 2, dd)) return st;
+        if (int st = dgrad<kNnHid, kNnHid>(gA, gB, a1, 2, dd)) return st;
+        if (int st = wgrad<kNnHid, kNnHid>(gB, a0, 1, dd)) return st;
+        if (int st = dgrad<kNnHid, kNnHid>(gB, gA, a0, 1, dd)) return st;
+        if (int st = wgrad<kNnIn, kNnHid>(gA, feat, 0, dd)) return st;
         return SVL_OK;
+    }
+    int sample(const float* x, const float* t, float gscale, float* lslot) {
+        return sample(x, t, gscale, lslot, d, rho, mask);
     }
 };
 
@@ -745,6 +783,24 @@ int nn_train_segment(NnPrecond* nn, int it_begin, int it_end, int iters, int bat
             uint64_t h = seed ^ (0x9E3779B97F4A7C15ull * (uint64_t)(it * 131 + b + 1));
             h ^= h >> 31; h *= 0xBF58476D1CE4E5B9ull; h ^= h >> 29;
             const int p = (int)(h % (uint64_t)np);
+            if (nn->crop > 0) {
+                // a window of side crop at an offset drawn from the same hash
+                const Dims& f = nn->d;
+                Dims cr{std::min(nn->crop, f.nx), std::min(nn->crop, f.ny), std::min(nn->crop, f.nz), 0};
+                cr.V = cr.nx * cr.ny * cr.nz;
+                uint64_t h2 = h * 0x94D049BB133111EBull;
+                h2 ^= h2 >> 31;
+                const int ox = (int)(h2 % (uint64_t)(f.nx - cr.nx + 1));
+                const int oy = (int)((h2 >> 20) % (uint64_t)(f.ny - cr.ny + 1));
+                const int oz = (int)((h2 >> 40) % (uint64_t)(f.nz - cr.nz + 1));
+                const int g3 = nblocks(3 * cr.V);
+                k_crop<<<g3, kThreads, 0, nn->stream>>>(nn->X[p], nn->cx, f, cr, ox, oy, oz);
+                k_crop<<<g3, kThreads, 0, nn->stream>>>(nn->Y[p], nn->ct, f, cr, ox, oy, oz);
+                k_crop<<<g3, kThreads, 0, nn->stream>>>(nn->rho, nn->crho, f, cr, ox, oy, oz);
+                k_crop_mask<<<g3, kThreads, 0, nn->stream>>>(nn->mask, nn->cmask, f, cr, ox, oy, oz, 4);
+                if (int st = nn->sample(nn->cx, nn->ct, 1.f / batch, nn->lsum + it, cr, nn->crho, nn->cmask)) return st;
+                continue;
+            }
             if (int st = nn->sample(nn->X[p], nn->Y[p], 1.f / batch, nn->lsum + it)) return st;
         }
         const float frac = (float)it / iters;
@@ -764,6 +820,22 @@ int nn_train_segment(NnPrecond* nn, int it_begin, int it_end, int iters, int bat
     for (int i = n - tail; i < n; ++i) acc += lh[i];
     if (loss) *loss = (float)(acc / tail / batch);
     if (!std::isfinite(acc)) { set_error("training diverged"); return SVL_ERR_NONFINITE; }
+    return SVL_OK;
+}
+
+int nn_set_crop(NnPrecond* nn, int crop) {
+    if (crop < 0) { set_error("crop must be >= 0"); return SVL_ERR_INVALID; }
+    if (crop > 0 && crop < 9) { set_error("crop windows need at least 9 voxels a side"); return SVL_ERR_INVALID; }
+    if (crop > 0 && !nn->cx) {
+        const size_t n = (size_t)3 * std::min(crop, nn->d.nx) * std::min(crop, nn->d.ny) * std::min(crop, nn->d.nz);
+        int st;
+        if ((st = nn->alloc(n, &nn->cx)) || (st = nn->alloc(n, &nn->ct)) || (st = nn->alloc(n, &nn->crho)) ||
+            (st = nn->alloc(n, &nn->cmask)))
+            return st;
+    } else if (crop > nn->crop && nn->cx && nn->crop > 0) {
+        set_error("the crop size is fixed by the first training with crops"); return SVL_ERR_INVALID;
+    }
+    nn->crop = crop;
     return SVL_OK;
 }
 

@@ -42,6 +42,10 @@ int nn_train(NnPrecond* nn, int iters, int batch, float lr, uint64_t seed, float
 // Iterations [it_begin, it_end) of an `iters`-long Adam run (learning-rate
 // schedule over the whole run; moments reset when it_begin == 0).
 int nn_train_segment(NnPrecond* nn, int it_begin, int it_end, int iters, int batch, float lr, uint64_t seed, float* loss);
+// Training windows: each sample is a random crop x crop x crop window of a
+// pair (loss masked 4 voxels inside window faces interior to the lattice);
+// 0 = whole lattice.
+int nn_set_crop(NnPrecond* nn, int crop);
 int nn_set_weights(NnPrecond* nn, const float* w);
 int nn_get_weights(NnPrecond* nn, float* w);
 // Device forward + loss + backward of one sample given as host grids

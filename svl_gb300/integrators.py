@@ -377,15 +377,17 @@ class NewmarkBeta:
     # -- learned preconditioner (lattice models) ---------------------------
     def train_preconditioner(self, k_first: int, solve_steps: int = 0, record_every: int = 4,
                              n_synthetic: int = 300, iters: int = 1500, batch: int = 8, lr: float = 2e-3,
-                             seed: int = 0, max_sweeps: int = 0) -> float:
+                             seed: int = 0, max_sweeps: int = 0, crop: int = 0) -> float:
         """Optionally advance solve_steps steps with Jacobi-PCG recording CG
         iterates, add synthetic pairs (K_eff e for random e with 0..max_sweeps
         smoothing sweeps), train the network in segments keeping the weights
         whose trial flexible-CG solve of step k_first + solve_steps needs the
-        fewest iterations, and switch to the learned preconditioner.  Returns
-        the training loss (mean relative squared error) of the kept weights."""
+        fewest iterations, and switch to the learned preconditioner.  crop > 0
+        trains on random crop^3 windows of the pairs instead of the whole
+        lattice.  Returns the training loss (mean relative squared error) of
+        the kept weights."""
         o = capi.NnTrainOpts(solve_steps=solve_steps, record_every=record_every, n_synthetic=n_synthetic,
-                             iters=iters, batch=batch, lr=lr, seed=seed, max_sweeps=max_sweeps)
+                             iters=iters, batch=batch, lr=lr, seed=seed, max_sweeps=max_sweeps, crop=crop)
         loss = C.c_float()
         check(lib().svl_nm_train_preconditioner(self._h, int(k_first), C.byref(o), C.byref(loss)))
         return float(loss.value)
