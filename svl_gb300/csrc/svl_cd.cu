@@ -71,7 +71,9 @@ struct DevView {
     const int32_t* inv_ptr;  // [nnode+1]
     const int32_t* inv_ent;  // element*8 + local node
     const int32_t* tfree;    // [ntotal] free dof or -1 (identity-T path)
-    const double* Md;        // [ntotal]
+    const double* Md;        // [ntotal] lumped mass (consistent-mass models: the nodal masses only)
+    const double* erho;      // [E] density per element for the consistent mass action, or null (lumped)
+    const double* fem;       // [nen*ndof][E] consistent mass action of the effective force, or null
     const double* kinv;      // [nfree]  1 / (T^T K T)_ff
     const double* Kd;        // [ntotal] 1/dt^2 M
     // Rayleigh damping C = sum_e (am_e M_e + ak_e K0_e) (lin2DQuad4.cpp:355-366)
@@ -573,6 +575,70 @@ __device__ __forceinline__ double gather_fint(const DevView& d, int n, int c) {
     return f;
 }
 
+// Sum of an element-vector block (layout of fe) at node n, component c, in
+// element order.
+template <int ND>
+__device__ __forceinline__ double gather_block(const DevView& d, const double* __restrict__ blk, int n, int c) {
+    double f = 0.0;
+    const int E = d.nelem;
+    for (int i = d.inv_ptr[n]; i < d.inv_ptr[n + 1]; ++i) {
+        const int ent = d.inv_ent[i];
+        f += blk[(size_t)((ent & 7) * ND + c) * E + (ent >> 3)];
+    }
+    return f;
+}
+
+// Consistent mass action of every element, M_e = rho sum_q w t |J| N_a N_b on
+// each displacement component (lin2DQuad4.cpp:243-285 and lin3DHexa8.cpp:
+// 243-285 without the lumping branch): fe = scale M_e x_e, or fe += when
+// accumulate.  Gauss points and shape functions as the element's.
+template <int ND, int NEN>
+__global__ void __launch_bounds__(128) k_mass_elem(DevView d, const double* __restrict__ x, double* __restrict__ fe,
+                                                    double scale, int accumulate) {
+    constexpr int NC = ND * NEN, PER = NEN * ND + 1;
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    const int E = d.nelem;
+    if (e >= E) return;
+    double xe[NC], y[NC];
+#pragma unroll
+    for (int j = 0; j < NC; ++j) { xe[j] = x[d.edof[(size_t)j * E + e]]; y[j] = 0.0; }
+    const double rho = d.erho[e];
+    const double* g0 = d.geo + (size_t)d.egeo[e] * NEN * PER;
+    const double g = kGaussAbscissa;
+    for (int q = 0; q < NEN; ++q) {
+        const double r = (q & 1) ? g : -g, s2 = (q & 2) ? g : -g, t = (q & 4) ? g : -g;
+        double N[NEN];
+        if (ND == 2) {
+            const double sr[4] = {-1, 1, 1, -1}, ss[4] = {-1, -1, 1, 1};
+#pragma unroll
+            for (int a = 0; a < NEN; ++a) N[a] = 0.25 * (1.0 + sr[a % 4] * r) * (1.0 + ss[a % 4] * s2);
+        } else {
+            const double sr[8] = {-1, 1, 1, -1, -1, 1, 1, -1}, ss[8] = {-1, -1, 1, 1, -1, -1, 1, 1},
+                         st[8] = {-1, -1, -1, -1, 1, 1, 1, 1};
+#pragma unroll
+            for (int a = 0; a < NEN; ++a) N[a] = 0.125 * (1.0 + sr[a] * r) * (1.0 + ss[a] * s2) * (1.0 + st[a] * t);
+        }
+        const double c = rho * g0[q * PER + PER - 1];
+        double xg[ND];
+#pragma unroll
+        for (int k = 0; k < ND; ++k) {
+            double v = 0.0;
+#pragma unroll
+            for (int a = 0; a < NEN; ++a) v += N[a] * xe[a * ND + k];
+            xg[k] = v;
+        }
+#pragma unroll
+        for (int a = 0; a < NEN; ++a)
+#pragma unroll
+            for (int k = 0; k < ND; ++k) y[a * ND + k] += c * N[a] * xg[k];
+    }
+#pragma unroll
+    for (int j = 0; j < NC; ++j) {
+        double* o = fe + (size_t)j * E + e;
+        *o = accumulate ? *o + scale * y[j] : scale * y[j];
+    }
+}
+
 // Identity-T path: everything after the element forces, per node.
 template <int ND>
 __global__ void __launch_bounds__(256) k_node(DevView d) {
@@ -943,6 +1009,15 @@ static int cd_setup(svl_cd* cd, const svl_load_desc* L) {
     TRY(cd->upload(inv_ptr, &d.inv_ptr));
     TRY(cd->upload(inv_ent, &d.inv_ent));
     TRY(cd->upload(tfree, &d.tfree));
+    if (!m.lumped) {
+        // consistent mass (implicit path): the element masses act through
+        // k_mass_elem; the diagonal keeps the nodal (point) masses only
+        for (int t = 0; t < m.ntotal; ++t)
+            Md[t] = (!m.nodemass.empty() && std::fabs(m.nodemass[t]) > cd->opts.mtol) ? m.nodemass[t] : 0.0;
+        std::vector<double> erho(m.nelem);
+        for (int e = 0; e < m.nelem; ++e) erho[e] = m.param(e)[2];
+        TRY(cd->upload(erho, &d.erho));
+    }
     TRY(cd->upload(Md, &d.Md));
     TRY(cd->upload(kinv, &d.kinv));
     TRY(cd->upload(Kd, &d.Kd));
@@ -1090,7 +1165,7 @@ static int cd_create(const svl_model_desc* model, const svl_load_desc* loads, co
     svl_cd* cd = new svl_cd();
     cd->opts = *opts;
     if (!model_from_desc(model, cd->m)) { delete cd; return SVL_ERR_INVALID; }
-    if (!cd->m.lumped) { delete cd; set_error("the explicit path needs a lumped mass (massform LUMPED)"); return SVL_ERR_UNSUPPORTED; }
+    if (!cd->m.lumped && !implicit) { delete cd; set_error("the explicit path needs a lumped mass (massform LUMPED)"); return SVL_ERR_UNSUPPORTED; }
     if (cd->m.has_pml()) {
         delete cd;
         set_error("PML elements are served by svl_xnm_create (ExtendedNewmarkBeta)");
@@ -1545,7 +1620,17 @@ __global__ void __launch_bounds__(256) k_nm_rhs(DevView d, double* __restrict__ 
         // Fext - Fint + M (4/dt V + A - 4/dt^2 dU)   (NewmarkBeta.cpp:215, C = 0)
         const double w = dUf ? (c_v * d.V[t] + d.A[t]) - c_m * dUf[f] : c_v * d.V[t] + d.A[t];
         b[f] = ((fext + 0.0) - fint) + d.Md[t] * w;
+        if (d.fem) b[f] += gather_block<ND>(d, d.fem, n, c);    // consistent mass: sum_e M_e w_e
     }
+}
+
+// w = 4/dt V + A (- 4/dt^2 dU on free dofs): the vector the effective force's
+// mass term multiplies (NewmarkBeta.cpp:215)
+__global__ void k_nm_wvec(DevView d, const double* __restrict__ dUf, double c_v, double c_m, double* __restrict__ w) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= d.ntotal) return;
+    const int f = d.tfree[t];
+    w[t] = (dUf && f >= 0) ? (c_v * d.V[t] + d.A[t]) - c_m * dUf[f] : c_v * d.V[t] + d.A[t];
 }
 
 // Us = U + dU on total dofs (identity T) for the state update of a Newton iteration
@@ -1990,6 +2075,9 @@ struct svl_nm {
     bool newton = false, tangent = false;   // tangent: J2 elements present (stored tangents)
     int64_t newton_iters_total = 0, newton_iters_last = 0;
     double newton_res_last = 0.0;
+    // consistent mass: the mass term of the effective force through element actions
+    bool consistent = false;
+    double* wvec = nullptr;                 // [ntotal] 4/dt V + A - 4/dt^2 dU
     // single-precision operator of the inner iterations (eligible models only)
     bool fast_op = false;
     float *geo_f = nullptr, *coef_f = nullptr, *pt_f = nullptr, *fe_f = nullptr;
@@ -2087,6 +2175,11 @@ static int nm_apply(svl_nm* nm, const double* v, double* q, bool inner = false) 
         else k_element<3, 8><<<eg, 128, 0, cd->stream>>>(d, nm->pt, m.ngp, 0);
     }
     const double c_m = 4.0 / nm->opts.dt / nm->opts.dt;
+    if (nm->consistent) {                   // + 4/dt^2 M_e p_e in the same element vectors
+        if (m.ndim == 2) k_mass_elem<2, 4><<<eg, 128, 0, cd->stream>>>(d, nm->pt, d.fe, c_m, 1);
+        else k_mass_elem<3, 8><<<eg, 128, 0, cd->stream>>>(d, nm->pt, d.fe, c_m, 1);
+        cd->launches += 1;
+    }
     if (m.ndim == 2) k_nm_apply<2><<<(m.nnode + tb - 1) / tb, tb, 0, cd->stream>>>(d, nm->pt, q, c_m);
     else k_nm_apply<3><<<(m.nnode + tb - 1) / tb, tb, 0, cd->stream>>>(d, nm->pt, q, c_m);
     cd->launches += 3;
@@ -2355,6 +2448,26 @@ int svl_nm_create(const svl_model_desc* model, const svl_load_desc* loads, const
     }
     std::vector<double> M;
     lumped_mass_diag(m, opts->mtol, M);
+    nm->consistent = !m.lumped;
+    if (nm->consistent) {
+        if (nm->general) {
+            set_error("a consistent mass is covered without constraints, support motion or damping");
+            return fail(SVL_ERR_UNSUPPORTED);
+        }
+        // diagonal of the consistent mass: rho sum_q w t |J| N_a^2, plus the nodal masses
+        std::fill(M.begin(), M.end(), 0.0);
+        for (int e = 0; e < m.nelem; ++e) {
+            const double rho = m.param(e)[2];
+            for (int q = 0; q < m.ngp; ++q) {
+                double dNx[8][3], N[8];
+                const double w = gp_factor(m, e, gp_geometry(m, e, q, dNx, N));
+                for (int a = 0; a < m.nen; ++a)
+                    for (int c = 0; c < m.ndof; ++c) M[m.tdof[(size_t)m.conn[(size_t)e * m.nen + a] * m.ndof + c]] += rho * w * N[a] * N[a];
+            }
+        }
+        if (!m.nodemass.empty())
+            for (int t = 0; t < m.ntotal; ++t) if (std::fabs(m.nodemass[t]) > opts->mtol) M[t] += m.nodemass[t];
+    }
     if (nm->damped) {                       // + 2/dt (sum_e am_e M_e + dashpot diagonal)
         std::vector<double> Cm;
         rayleigh_mass_diag(m, Cm);
@@ -2390,6 +2503,11 @@ int svl_nm_create(const svl_model_desc* model, const svl_load_desc* loads, const
     nm->dinv = const_cast<double*>(dd);
     if ((st = cd->zeros((size_t)nc * m.nelem, &nm->fe_op)) || (st = cd->zeros((size_t)std::max(m.nfree, 1), &nm->dUf)))
         return fail(st);
+    if (nm->consistent) {
+        double* fm = nullptr;
+        if ((st = cd->zeros((size_t)nc * m.nelem, &fm)) || (st = cd->zeros((size_t)m.ntotal, &nm->wvec))) return fail(st);
+        cd->d.fem = fm;
+    }
     if (nm->general) {
         double** tv[] = {&nm->ft, &nm->dUt, &nm->smv, &nm->lg, &nm->pt2};
         for (double** pv : tv) if ((st = cd->zeros((size_t)m.ntotal, pv))) return fail(st);
@@ -2401,7 +2519,8 @@ int svl_nm_create(const svl_model_desc* model, const svl_load_desc* loads, const
     }
     // single-precision operator of the inner iterations: elastic models without
     // damping or constraints (the FP64 operator confirms every answer)
-    if (opts->single_inner && !nm->general && !nm->tangent && !m.has_j2() && !cd->d.dk0 && m.nelem > 0 && m.nfree > 0) {
+    if (opts->single_inner && !nm->general && !nm->tangent && !m.has_j2() && !cd->d.dk0 && !nm->consistent &&
+        m.nelem > 0 && m.nfree > 0) {
         const int per = m.nen * m.ndim + 1;
         std::vector<double> gh((size_t)cd->ngeo * m.ngp * per), ch((size_t)3 * m.nelem);
         if (cudaMemcpy(gh.data(), cd->d.geo, gh.size() * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess ||
@@ -2488,6 +2607,22 @@ static int nm_drm(svl_nm* nm) {
 static int nmg_rhs(svl_nm* nm);
 
 // Effective force of step k into nm->b (state untouched).
+// Consistent mass: the element actions M_e w_e of the effective force's mass
+// term into d.fem (k_nm_rhs gathers them); nothing with a lumped mass.
+static int nm_mass_rhs(svl_nm* nm, const double* dUf, double c_m) {
+    if (!nm->consistent) return SVL_OK;
+    svl_cd* cd = nm->cd;
+    const HostModel& m = cd->m;
+    const int tb = 256, eg = (m.nelem + 127) / 128;
+    k_nm_wvec<<<(m.ntotal + tb - 1) / tb, tb, 0, cd->stream>>>(cd->d, dUf, 4.0 / nm->opts.dt, c_m, nm->wvec);
+    DevView d = cd->d;
+    if (m.ndim == 2) k_mass_elem<2, 4><<<eg, 128, 0, cd->stream>>>(d, nm->wvec, const_cast<double*>(d.fem), 1.0, 0);
+    else k_mass_elem<3, 8><<<eg, 128, 0, cd->stream>>>(d, nm->wvec, const_cast<double*>(d.fem), 1.0, 0);
+    cd->launches += 2;
+    CUDA_TRY(cudaGetLastError());
+    return SVL_OK;
+}
+
 static int nm_rhs(svl_nm* nm, int k) {
     svl_cd* cd = nm->cd;
     const HostModel& m = cd->m;
@@ -2504,6 +2639,7 @@ static int nm_rhs(svl_nm* nm, int k) {
         CUDA_TRY(cudaMemsetAsync(nm->dUt, 0, sizeof(double) * m.ntotal, cd->stream));
         return nmg_rhs(nm);
     }
+    TRY(nm_mass_rhs(nm, nullptr, 0.0));
     if (m.ndim == 2) k_nm_rhs<2><<<ng, tb, 0, cd->stream>>>(cd->d, nm->b, 4.0 / dt, nullptr, 0.0);
     else k_nm_rhs<3><<<ng, tb, 0, cd->stream>>>(cd->d, nm->b, 4.0 / dt, nullptr, 0.0);
     CUDA_TRY(cudaGetLastError());
@@ -2630,6 +2766,7 @@ static int nm_step_newton(svl_nm* nm, double* U_hist_row) {
         if (nm->general) {
             TRY(nmg_rhs(nm));               // K SM with the current tangent, every iteration
         } else {
+            TRY(nm_mass_rhs(nm, nm->dUf, 4.0 / dt / dt));
             if (m.ndim == 2) k_nm_rhs<2><<<ng, tb, 0, cd->stream>>>(cd->d, nm->b, 4.0 / dt, nm->dUf, 4.0 / dt / dt);
             else k_nm_rhs<3><<<ng, tb, 0, cd->stream>>>(cd->d, nm->b, 4.0 / dt, nm->dUf, 4.0 / dt / dt);
         }
@@ -2695,6 +2832,7 @@ static int nm_step(svl_nm* nm, double* U_hist_row) {
     // internal force from the committed state (filtered like the assembler)
     if (m.ndim == 2) k_element<2, 4><<<eg, 128, 0, cd->stream>>>(cd->d, cd->d.Us, m.ngp, 0);
     else k_element<3, 8><<<eg, 128, 0, cd->stream>>>(cd->d, cd->d.Us, m.ngp, 0);
+    TRY(nm_mass_rhs(nm, nullptr, 0.0));
     if (m.ndim == 2) k_nm_rhs<2><<<ng, tb, 0, cd->stream>>>(cd->d, nm->b, 4.0 / dt, nullptr, 0.0);
     else k_nm_rhs<3><<<ng, tb, 0, cd->stream>>>(cd->d, nm->b, 4.0 / dt, nullptr, 0.0);
     cd->launches += 3;
@@ -2912,6 +3050,7 @@ int svl_nm_get(svl_nm* nm, int32_t which, double* out) {
 
 int svl_nm_reaction(svl_nm* nm, int32_t k, double* R) {
     if (!nm || !R) { set_error("NULL argument"); return SVL_ERR_INVALID; }
+    if (nm->consistent) { set_error("reaction forces are covered with a lumped mass"); return SVL_ERR_UNSUPPORTED; }
     return cd_reaction(nm->cd, k, 0, R);
 }
 

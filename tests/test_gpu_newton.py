@@ -55,6 +55,20 @@ def test_newton_fixed_iterations_match_oracle(gpu, ndim, ne, amp, nt):
     assert rel_l2(hist, ho) <= 1e-9
 
 
+def test_newton_consistent_mass_matches_oracle(gpu):
+    """Newton with J2 tangents and a consistent mass (the element mass action
+    in the tangent operator and the effective force) against the oracle."""
+    m, L, dt = j2_box(2, (8, 6), amp=4e5, nt=40)
+    m.lumped = False
+    nm = NewmarkBeta(m, L, dt, pcg_tol=1e-13, algorithm="newton", maxit=3, cnvgtol=0.0, cnvgtest=4)
+    nm.Initialize()
+    hist = nm.run(1, 40, history=True)
+    nm.close()
+    ho, _ = O.newmark_run(m, L, dt, 40, algo=2, maxit=3, cnvgtol=0.0, solver=0)
+    assert np.abs(ho).max() > 0
+    assert rel_l2(hist, ho) <= 1e-9
+
+
 @pytest.mark.parametrize("test", [4, 5])
 def test_newton_convergence_tests_track_oracle(gpu, test):
     m, L, dt = j2_box(2, (8, 6))

@@ -102,6 +102,32 @@ def test_nm_rejects_models_it_does_not_cover(gpu):
         NewmarkBeta(m, L, dt, precond=capi.SVL_PRECOND_LEARNED)
     assert ei.value.code == capi.SVL_ERR_UNSUPPORTED
     m.lumped = False
-    with pytest.raises(SvlError) as ei:        # consistent mass
+    with pytest.raises(SvlError) as ei:        # consistent mass with constraints / support motion
         NewmarkBeta(m, L, dt)
     assert ei.value.code == capi.SVL_ERR_UNSUPPORTED
+
+
+@pytest.mark.parametrize("shape", [(16, 8), (6, 5, 4)], ids=["quad", "hexa"])
+def test_nm_consistent_mass_matches_oracle(gpu, shape):
+    """massform Consistent, the pre-processor's default: the element mass
+    matrices act element by element (operator and effective force) against
+    the oracle's assembled consistent mass and dense LDL^T."""
+    if len(shape) == 2:
+        m, L, dt = q4_box(*shape, nt=120)
+        dt *= 5.0
+    else:
+        m, L, dt = h8_box(*shape, seed=5, nt=80)
+        dt *= 10.0
+    m.lumped = False
+    nt = 40
+    nm = NewmarkBeta(m, L, dt, pcg_tol=TOL_SOLVE)
+    nm.Initialize()
+    hist = nm.run(1, nt, history=True)
+    res = nm.stats()[2]
+    nm.close()
+    ho, _ = O.newmark_run(m, L, dt, nt, solver=0)
+    m.lumped = True
+    hl, _ = O.newmark_run(m, L, dt, nt, solver=0)
+    assert np.abs(ho).max() > 0 and res <= TOL_SOLVE
+    assert rel_l2(ho, hl) > 1e-4               # the mass form matters
+    assert rel_l2(hist, ho) <= TOL_HIST
