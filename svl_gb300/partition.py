@@ -293,10 +293,12 @@ def load_partition(path, run_dir=None) -> Partition:
                 ray[epos[int(e)]] = par
     # nodal masses
     node_mass = None
+    nmass = {}                                   # node position -> its mass entries (Node::GetMass)
     if d.get("Masses"):
         node_mass = np.zeros(int(g["ntotal"]))
         for t, ms in d["Masses"].items():
             i = npos[int(t)]
+            nmass[i] = [float(v) for v in ms["mass"]]
             for k, v in enumerate(ms["mass"]):
                 node_mass[totaldof[i, k]] += float(v)
     # constraints: slave total dof <- sum factor * master free dof
@@ -349,9 +351,26 @@ def load_partition(path, run_dir=None) -> Partition:
             raise PartitionError("load function %s is not covered" % la["name"])
         s = loads.add_series(series)
         direction = [float(x) for x in la["dir"]]
+        # Assembler::ComputeExternalForceVector (Assembler.cpp:291-489) assembles
+        # every load into its own zeroed vector by assignment, Fext(dof) = Fn(i)
+        # (point loads) or Fn(i) * Mn(i) (body point loads, Mn the node's mass
+        # entries; nodes without a Masses entry get nothing), then adds
+        # factor * Fext: across loads the entries add, within one load a node
+        # listed twice counts once
+        nodes = list(dict.fromkeys(int(t) for t in la.get("list", [])))
         if ld["name"].upper() == "POINTLOAD" and kind == "CONCENTRATED":
-            for ntag in la["list"]:
+            for ntag in nodes:
                 loads.add_point_load(model, npos[int(ntag)], direction, s, factor=float(fac))
+        elif ld["name"].upper() == "POINTLOAD" and kind == "BODY":
+            for ntag in nodes:
+                i = npos[int(ntag)]
+                if i not in nmass:
+                    continue
+                mn = nmass[i]
+                for j, v in enumerate(direction[:len(mn)]):
+                    loads.force_dof.append(int(model.totaldof[i, j]))
+                    loads.force_series.append(s)
+                    loads.force_coef.append(float(fac) * v * mn[j])
         elif ld["name"].upper() == "ELEMENTLOAD" and kind == "BODY":
             loads.add_body_load(model, [epos[int(e)] for e in la["list"]], direction, s, factor=float(fac))
         else:

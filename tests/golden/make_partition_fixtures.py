@@ -87,6 +87,45 @@ SVL.addSolver(tag=1, attributes={"name": "Eigen", "update": "OFF"})
 SVL.addSimulation(tag=1, combo=1, attributes={"analysis": 1, "algorithm": 1, "integrator": 1, "solver": 1})
 SVL.CreateRunAnalysisFiles()
 ''',
+    # Q4 box with nodal masses and a body point load (acceleration times the
+    # node's mass) beside a concentrated load on the same node, CD
+    "q4_bodypoint_cd": COMMON + r'''
+SVL.Options["dimension"] = 2
+SVL.Options["massform"] = "lumped"
+nx, ny, dt, nt = 6, 4, 1.0e-3, 41
+SVL.addMaterial(tag=1, name="Elastic2DPlaneStrain", attributes={"E": 2.0e8, "nu": 0.25, "rho": 2000.0})
+mesh = SVL.makeDomainArea(options={"ne": [nx, ny], "ndof": 2, "class": "LIN2DQUAD4", "elems": "QUAD4",
+    "P0": [0.0, 0.0], "P1": [nx * 1.0, 0.0], "P2": [0.0, ny * 1.0],
+    "attributes": {"material": 1, "th": 1.0, "rule": "Gauss", "np": 4}})
+for tag in sorted(mesh["Nodes"]):
+    n = mesh["Nodes"][tag]
+    SVL.addNode(tag=tag, ndof=n["ndof"], coords=list(map(float, n["coords"])))
+for tag in sorted(mesh["Elements"]):
+    el = mesh["Elements"][tag]
+    SVL.addElement(tag=tag, conn=list(el["conn"]), name=el["name"], attributes=dict(el["attributes"]))
+for tag in sorted(mesh["Nodes"]):
+    t = tag - 1; i = t % (nx + 1); j = t // (nx + 1)
+    if j == 0:
+        SVL.addRestrain(tag=tag, dof=[1, 2])
+    elif i == 0 or i == nx:
+        SVL.addRestrain(tag=tag, dof=1)
+top = ny * (nx + 1) + nx // 2 + 1
+SVL.addMass(tag=top, dof=[1, 2], vals=[250.0, 400.0])
+SVL.addMass(tag=top - 1, dof=[1, 2], vals=[120.0, 120.0])
+write_series("accel.txt", ricker(nt, dt, 25.0, 40.0))
+SVL.addFunction(tag=1, name="TimeSeries", attributes={"file": "accel.txt", "dir": [0.6, -0.8]})
+SVL.addFunction(tag=2, name="Constant", attributes={"mag": 2.0e3, "dir": [1.0, 0.0]})
+SVL.addLoad(tag=1, name="PointLoad", attributes={"type": "Body", "fun": 1, "list": [top, top - 1, top + 1]})
+SVL.addLoad(tag=2, name="PointLoad", attributes={"type": "Concentrated", "fun": 2, "list": [top]})
+SVL.addCombinationCase(tag=1, name="Fixture", attributes={"load": [1, 2], "factor": [1.0, 0.5]})
+SVL.addRecorder(tag=1, attributes={"name": "NODE", "file": "Disp.out", "ndps": 8, "resp": "disp", "list": [top, top - 1]})
+SVL.addAnalysis(tag=1, attributes={"name": "Dynamic", "nt": nt})
+SVL.addAlgorithm(tag=1, attributes={"name": "Linear", "nstep": 1})
+SVL.addIntegrator(tag=1, attributes={"name": "CentralDifference", "dt": dt})
+SVL.addSolver(tag=1, attributes={"name": "Eigen", "update": "OFF"})
+SVL.addSimulation(tag=1, combo=1, attributes={"analysis": 1, "algorithm": 1, "integrator": 1, "solver": 1})
+SVL.CreateRunAnalysisFiles()
+''',
     # H8 elastic box, element body load time series, Newmark + PETSc CG
     "h8_newmark_body": COMMON + r'''
 SVL.Options["dimension"] = 3
@@ -418,7 +457,7 @@ SVL.CreateRunAnalysisFiles()
 }
 
 
-def main(ref_root: str):
+def main(ref_root: str, only=None):
     pp = Path(ref_root) / "01-Pre_Process"
     scratch = HERE / ".pp_scratch"
     if scratch.exists():
@@ -430,6 +469,8 @@ def main(ref_root: str):
         (stub / mod).write_text("def __getattr__(name):\n    return lambda *a, **k: None\n")
     env = dict(os.environ, PYTHONPATH=os.pathsep.join([str(scratch / "stub"), str(pp)]))
     for name, script in CASES.items():
+        if only and name not in only:
+            continue
         work = scratch / name
         work.mkdir(parents=True)
         r = subprocess.run([sys.executable, "-c", script, name], cwd=work, env=env, capture_output=True, text=True,
@@ -453,5 +494,5 @@ def main(ref_root: str):
 if __name__ == "__main__":
     root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("SVL_REFERENCE_ROOT")
     if not root:
-        raise SystemExit("usage: %s <SVL source tree>  (or set SVL_REFERENCE_ROOT)" % Path(__file__).name)
-    main(root)
+        raise SystemExit("usage: %s <SVL source tree> [case ...]  (or set SVL_REFERENCE_ROOT)" % Path(__file__).name)
+    main(root, set(sys.argv[2:]) or None)

@@ -100,3 +100,33 @@ def test_drm_partition_newmark_matches_oracle(gpu, tmp_path):
     ho, _ = O.newmark_run(p.model, p.loads, p.dt, p.nt - 1, solver=0)
     assert np.abs(ho).max() > 0
     assert rel_l2(U, ho) <= 1e-9
+
+
+def test_consistent_mass_partition_newmark_matches_oracle(gpu, tmp_path):
+    """The pre-processor's default massform (CONSISTENT) on a NEWMARK
+    partition: the body-load fixture with its massform switched."""
+    import json
+    import shutil
+    from svl_gb300.partition import load_partition
+    src = Path(__file__).resolve().parent / "golden" / "partition_h8_newmark_body"
+    shutil.copytree(src, tmp_path / "case")
+    f = tmp_path / "case" / "Partition" / "Fixture.1.0.json"
+    d = json.loads(f.read_text())
+    d["Global"]["massform"] = "CONSISTENT"
+    f.write_text(json.dumps(d))
+    p = load_partition(f)
+    assert not p.model.lumped
+    U = p.run(write_recorders=False)
+    ho, _ = O.newmark_run(p.model, p.loads, p.dt, p.nt - 1, solver=0)
+    assert np.abs(ho).max() > 0
+    assert rel_l2(U, ho) <= 1e-9
+
+
+def test_body_point_load_partition_cd_matches_oracle(gpu, tmp_path):
+    """POINTLOAD BODY (nodal acceleration times the node's mass) beside a
+    concentrated load, central difference, written by the pre-processor."""
+    p = _part("q4_bodypoint_cd")
+    U = p.run(solution_dir=tmp_path)
+    ho, *_ = O.cd_run(p.model, p.loads, p.dt, p.nt - 1)
+    assert np.abs(ho).max() > 0
+    assert rel_l2(U, ho) <= 1e-12

@@ -20,7 +20,8 @@ def _part(case):
 
 
 @pytest.mark.parametrize("case", ["q4_cd", "h8_newmark_body", "q4_j2_column", "q4_newmark_rayleigh", "q4_pml_extended",
-                                  "q4_pml_j2_newton", "q4_lysmer_cd", "q4_drm_newmark", "q4_reaction_cd"])
+                                  "q4_pml_j2_newton", "q4_lysmer_cd", "q4_drm_newmark", "q4_reaction_cd",
+                                  "q4_bodypoint_cd"])
 def test_numbering_and_connectivity_follow_the_file(case):
     p = load_partition(_part(case))
     d = json.loads(_part(case).read_text())
@@ -201,3 +202,30 @@ def test_reaction_recorder_is_read():
     assert resp == ["DISP", "REACTION"]
     rec = [r for r in p.recorders if r.response == "REACTION"][0]
     assert len(rec.ids) == 4
+
+
+def test_body_point_load_is_acceleration_times_nodal_mass():
+    """POINTLOAD BODY (Assembler.cpp:373-394): Fn(i) * Mn(i) with Mn the
+    node's mass entries, nothing at nodes without a Masses entry; every load
+    is assembled into its own vector and added with its combination factor."""
+    p = load_partition(_part("q4_bodypoint_cd"))
+    d = json.loads(_part("q4_bodypoint_cd").read_text())
+    tags = list(p.node_tags)
+    L = p.loads
+    acc = read_series(_part("q4_bodypoint_cd").parent.parent / "accel.txt")
+    entries = {}
+    for dof, ser, coef in zip(L.force_dof, L.force_series, L.force_coef):
+        entries.setdefault(dof, []).append((ser, coef))
+    n31, n32, n33 = tags.index(31), tags.index(32), tags.index(33)
+    m = p.model
+    # node 31: mass 120 on both dofs, body load only
+    assert entries[int(m.totaldof[n31, 0])] == [(0, 0.6 * 120.0)]
+    assert entries[int(m.totaldof[n31, 1])] == [(0, -0.8 * 120.0)]
+    # node 32: body load with its masses, then the concentrated load (factor 0.5)
+    assert entries[int(m.totaldof[n32, 0])] == [(0, 0.6 * 250.0), (1, 0.5 * 1.0)]
+    assert entries[int(m.totaldof[n32, 1])] == [(0, -0.8 * 400.0)]
+    # node 33 has no mass entry: no body load
+    assert int(m.totaldof[n33, 0]) not in entries and int(m.totaldof[n33, 1]) not in entries
+    assert np.allclose(L.series[0], acc)
+    h, *_ = O.cd_run(m, L, p.dt, 20)
+    assert np.abs(h[:, int(m.totaldof[n31, 1])]).max() > 0
