@@ -303,8 +303,8 @@ def implicit_pcg(steps=500, warm=100, tol=1e-8):
     l_per = ms_l / (steps - warm)
     end_j = ms_j / 1e3
     end_l = ms_w / 1e3 + train_s + ms_l / 1e3
-    return {"workload": "lin3DHexa8 64x64x64 (h=1 m), layered G (100x contrast) x 10% log-normal, "
-                        "Newmark beta=1/4 gamma=1/2, dt=10x explicit limit, fixed bottom, roller sides, %d steps" % steps,
+    return {"workload": ("lin3DHexa8 64x64x64 (h=1 m), layered G (100x contrast) x 10%% log-normal, "
+                         "Newmark beta=1/4 gamma=1/2, dt=10x explicit limit, fixed bottom, roller sides, %d steps" % steps),
             "free_dof": m.nfree, "steps": steps, "tol": tol, "residual": "true |b - K_eff x| / |b|, FP64",
             "operator": "single-precision stiffness action in the inner iterations, FP64 true residual",
             "jacobi": {"ms_per_step": j_per, "pcg_iters_per_step": itj / steps, "seconds": end_j},
