@@ -634,11 +634,15 @@ __device__ __forceinline__ void cdp_shape(float h, int q, float N[8], float dN[8
     }
 }
 
-// Shape value and physical derivatives of node a (runtime index, signs from
-// constant memory) at Gauss point gp (compile-time index after unrolling).
+// Shape value and physical derivatives of node a (runtime index) at Gauss
+// point gp (compile-time index after unrolling).
 __device__ __forceinline__ void cdp_node_at(float h, int a, int gp, float& n, float& dx, float& dy, float& dz) {
     const float g = 0.577350269189626f;
-    const float r = kHexR[a], s2 = kHexS[a], t = kHexT[a];
+    // corner signs of node a in the element's node order (-,-,-) (+,-,-) (+,+,-)
+    // (-,+,-) then the same at +z, from the index bits (no per-lane table
+    // lookup: a varies across the lanes of a warp)
+    const int a4 = a & 3;
+    const float r = (a4 == 1 || a4 == 2) ? 1.0f : -1.0f, s2 = (a4 >= 2) ? 1.0f : -1.0f, t = (a >= 4) ? 1.0f : -1.0f;
     const float fr = 1.0f + r * ((gp & 1) ? g : -g), fs = 1.0f + s2 * ((gp & 2) ? g : -g),
                 ft = 1.0f + t * ((gp & 4) ? g : -g);
     const float c2 = 0.25f / h;
