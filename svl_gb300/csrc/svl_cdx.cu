@@ -606,130 +606,155 @@ struct CdpView {
     const float* __restrict__ sl;
     float* sph; float* spl;             // S^{n-1/2} in, S^{n+3/2} out
     float* sbh; float* sbl;             // Sbar pair [ninst][np][6]
-    float* vsu;                         // [ninst][np][20] displacement rows' inputs: sdot, smid, Sbar (written by k_cdp_su for the next step)
-    float* vin;                         // [ninst][np][12] stress rows' inputs: udot, umid, ubar at the half step
+    float* vsu;                         // [ninst][np][24] displacement rows' inputs: sdot, smid, Sbar, 8 floats each (written by k_cdp_su for the next step)
+    float* vin;                         // [ninst][np][12] stress rows' inputs: udot, umid, ubar at the half step, 4 floats each
     float* feu;                         // [ninst][npe][8][3]
     float* fes;                         // [ninst][npe][8][6]
 };
 
 constexpr int CDP_THREADS = 256;
-constexpr int CDP_GROUPS = CDP_THREADS / 8;
-__constant__ float kHexR[8] = {-1, 1, 1, -1, -1, 1, 1, -1};
-__constant__ float kHexS[8] = {-1, -1, 1, 1, -1, -1, 1, 1};
-__constant__ float kHexT[8] = {-1, -1, -1, -1, 1, 1, 1, 1};
+constexpr int VSU_ROW = 24;             // [sdot | smid | Sbar] x (xx yy zz xy yz xz, 2 pad)
+constexpr int VIN_ROW = 12;             // [udot | umid | ubar at the half step] x (x y z, 1 pad)
 
-// Shape values N_a and physical derivatives dN_a/dx of a cube of side h at
-// Gauss point q (r fastest; GaussQuadrature.cpp:303-316 abscissa).
-__device__ __forceinline__ void cdp_shape(float h, int q, float N[8], float dN[8][3]) {
-    const float g = 0.577350269189626f;
-    const float xi[3] = {(q & 1) ? g : -g, (q & 2) ? g : -g, (q & 4) ? g : -g};
-    const float c2 = 0.25f / h;                    // (2/h) * 1/8
-#pragma unroll
-    for (int a = 0; a < 8; ++a) {
-        const float fr = 1.0f + kHexR[a] * xi[0], fs = 1.0f + kHexS[a] * xi[1], ft = 1.0f + kHexT[a] * xi[2];
-        N[a] = 0.125f * fr * fs * ft;
-        dN[a][0] = c2 * kHexR[a] * fs * ft;
-        dN[a][1] = c2 * kHexS[a] * fr * ft;
-        dN[a][2] = c2 * kHexT[a] * fr * fs;
-    }
+// Linear shape functions of one axis at its two Gauss points:
+// B[q][i] = (1 + s_i xi_q) / 2 with s = (-1, +1), xi = (-g, +g)
+// (GaussQuadrature.cpp:303-316 abscissa); B is symmetric.  Their derivative
+// is s_i / h at both points, so a derivative along an axis is a difference
+// of the two nodes along it.
+constexpr float CDP_G = 0.577350269189626f;
+constexpr float CDP_P = 0.5f * (1.0f + CDP_G), CDP_Q = 0.5f * (1.0f - CDP_G);
+
+// Element node (the element's own order: (-,-,-) (+,-,-) (+,+,-) (-,+,-),
+// then the same at +z) of lexicographic corner l = ir + 2 is + 4 it.
+__device__ __forceinline__ constexpr int cdp_lex_node(int l) {
+    return (l & 4) | ((l & 2) ? ((l & 1) ? 2 : 3) : (l & 1));
 }
 
-// Shape value and physical derivatives of node a (runtime index) at Gauss
-// point gp (compile-time index after unrolling).
-__device__ __forceinline__ void cdp_node_at(float h, int a, int gp, float& n, float& dx, float& dy, float& dz) {
-    const float g = 0.577350269189626f;
-    // corner signs of node a in the element's node order (-,-,-) (+,-,-) (+,+,-)
-    // (-,+,-) then the same at +z, from the index bits (no per-lane table
-    // lookup: a varies across the lanes of a warp)
-    const int a4 = a & 3;
-    const float r = (a4 == 1 || a4 == 2) ? 1.0f : -1.0f, s2 = (a4 >= 2) ? 1.0f : -1.0f, t = (a >= 4) ? 1.0f : -1.0f;
-    const float fr = 1.0f + r * ((gp & 1) ? g : -g), fs = 1.0f + s2 * ((gp & 2) ? g : -g),
-                ft = 1.0f + t * ((gp & 4) ? g : -g);
-    const float c2 = 0.25f / h;
-    n = 0.125f * fr * fs * ft;
-    dx = c2 * r * fs * ft;
-    dy = c2 * s2 * fr * ft;
-    dz = c2 * t * fr * fs;
+// Lexicographic corner with bit `bit` along axis d and index m = i + 2 j
+// over the two other axes (in axis order).
+__device__ __forceinline__ constexpr int cdp_lex(int d, int m, int bit) {
+    return d == 0 ? bit + 2 * m : (d == 1 ? (m & 1) + 2 * bit + 4 * (m >> 1) : m + 4 * bit);
 }
 
-// Coupling weights of C, K, G per derivative direction at Gauss point q of
-// element e from the stretching there (PML3DHexa8.cpp:952-996, tabulated per
-// element and axis at the two abscissae; x: C ay az, K ay bz + az by, G by bz).
-__device__ __forceinline__ void cdp_weights(const CdpView& v, int e, int inst, int q, float qC[3], float qK[3],
-                                            float qG[3]) {
+// B (x) B over two axes on z[i + 2 j]: the values at the four Gauss points
+// (same order) of the bilinear interpolant; B symmetric, so the same map is
+// its transpose (Gauss-point values -> nodal sums).
+__device__ __forceinline__ void cdp_interp2(float z[4]) {
+    const float a0 = CDP_P * z[0] + CDP_Q * z[1], a1 = CDP_Q * z[0] + CDP_P * z[1];
+    const float a2 = CDP_P * z[2] + CDP_Q * z[3], a3 = CDP_Q * z[2] + CDP_P * z[3];
+    z[0] = CDP_P * a0 + CDP_Q * a2;
+    z[2] = CDP_Q * a0 + CDP_P * a2;
+    z[1] = CDP_P * a1 + CDP_Q * a3;
+    z[3] = CDP_Q * a1 + CDP_P * a3;
+}
+
+// Stretching of one element at the two abscissae of each axis.
+struct CdpStretch {
+    float a[3][2], b[3][2];
+};
+__device__ __forceinline__ CdpStretch cdp_stretch(const CdpView& v, int e, int inst) {
     const float4* t = reinterpret_cast<const float4*>(v.estr + (size_t)e * 12);
-    const float4 tx = t[0], ty = t[1], tz = t[2];
     const float b0 = v.eb0[(size_t)inst * v.npe + e];
-    const float ax = (q & 1) ? tx.y : tx.x, ay = (q & 2) ? ty.y : ty.x, az = (q & 4) ? tz.y : tz.x;
-    const float bx = b0 * ((q & 1) ? tx.w : tx.z), by = b0 * ((q & 2) ? ty.w : ty.z), bz = b0 * ((q & 4) ? tz.w : tz.z);
-    qC[0] = ay * az; qC[1] = ax * az; qC[2] = ax * ay;
-    qK[0] = ay * bz + az * by; qK[1] = ax * bz + az * bx; qK[2] = ax * by + ay * bx;
-    qG[0] = by * bz; qG[1] = bx * bz; qG[2] = bx * by;
+    CdpStretch s;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        const float4 x = t[d];
+        s.a[d][0] = x.x; s.a[d][1] = x.y; s.b[d][0] = b0 * x.z; s.b[d][1] = b0 * x.w;
+    }
+    return s;
+}
+
+// Coupling weight of derivative direction d at Gauss point m over the two
+// other axes (it does not depend on the abscissa along d), for the C (type
+// 0), K (1) and G (2) parts (PML3DHexa8.cpp:952-996; for x: ay az,
+// ay bz + az by, by bz).
+__device__ __forceinline__ float cdp_w(const CdpStretch& s, int d, int m, int type) {
+    const int d1 = d == 0 ? 1 : 0, d2 = d == 2 ? 1 : 2;
+    const float a1 = s.a[d1][m & 1], a2 = s.a[d2][m >> 1], b1 = s.b[d1][m & 1], b2 = s.b[d2][m >> 1];
+    return type == 0 ? a1 * a2 : (type == 1 ? a1 * b2 + a2 * b1 : b1 * b2);
+}
+
+// Stress component (xx yy zz xy yz xz = 0..5) that acts on force component
+// j through derivative direction d.
+__device__ __forceinline__ constexpr int cdp_fcomp(int d, int j) {
+    return d == 0 ? (j == 0 ? 0 : (j == 1 ? 3 : 5)) : (d == 1 ? (j == 0 ? 3 : (j == 1 ? 1 : 4)) : (j == 0 ? 5 : (j == 1 ? 4 : 2)));
+}
+
+// Strain component that derivative direction d of displacement component c
+// feeds (symmetric pairs share one).
+__device__ __forceinline__ constexpr int cdp_scomp(int d, int c) {
+    return d == c ? d : (d + c == 1 ? 3 : (d + c == 3 ? 4 : 5));
 }
 
 // Coupling forces of the PML elements on the displacement rows,
-// C_uS sdot + K_uS smid + G_uS Sbar, one thread per (element, Gauss point):
-// lane q stages node q's inputs, forms Gauss point q's weighted stress
-// combinations T (9 values) into shared memory, then lane j sums node j's
-// force over the 8 points: f_j = w|J| sum_q dN_j(q) . T(q).
+// C_uS sdot + K_uS smid + G_uS Sbar, one thread per element:
+//   f_j = w|J| sum_q sum_d dN_j,d(q) T_d(q),  T_d = C_d sdot + K_d smid + G_d Sbar
+// interpolated at Gauss point q.  The shape functions are tensor products and
+// dN_j,d is constant along d while the weights of direction d do not depend
+// on the abscissa along d, so the sum over the two points along d acts on the
+// node values first (their sum), and everything else is a 2 x 2 x 2 map
+// over the two other axes (sum factorisation): no per-point 8 x 8 products.
 __global__ void __launch_bounds__(CDP_THREADS) k_cdp_fu(CdpView v) {
-    __shared__ __align__(16) float sm[CDP_GROUPS][8][20];
-    __shared__ __align__(16) float st[CDP_GROUPS][8][12];
     const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const int q = (int)(gid & 7), lg = threadIdx.x >> 3;
-    const long long grp = gid >> 3;
-    const bool valid = grp < (long long)v.ninst * v.npe;
-    const int inst = valid ? (int)(grp / v.npe) : 0, e = valid ? (int)(grp % v.npe) : 0;
-    float4* srow = reinterpret_cast<float4*>(&sm[lg][q][0]);
-    if (valid) {
-        const int p = v.enode[(size_t)e * 8 + q];
-        const float4* src = reinterpret_cast<const float4*>(v.vsu + ((size_t)inst * v.np + p) * 20);
+    if (gid >= (long long)v.ninst * v.npe) return;
+    const int inst = (int)(gid / v.npe), e = (int)(gid % v.npe);
+    const CdpStretch s = cdp_stretch(v, e, inst);
+    const float* base = v.vsu + (size_t)inst * v.np * VSU_ROW;
+    const float* row[8];
 #pragma unroll
-        for (int i = 0; i < 5; ++i) srow[i] = src[i];
-    } else {
+    for (int l = 0; l < 8; ++l) row[l] = base + (size_t)v.enode[(size_t)e * 8 + cdp_lex_node(l)] * VSU_ROW;
+    float acc[3][3][4];
 #pragma unroll
-        for (int i = 0; i < 5; ++i) srow[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-    }
-    __syncwarp();
-    float N[8], dN[8][3], qC[3], qK[3], qG[3];
-    cdp_shape(v.h, q, N, dN);
-    cdp_weights(v, e, inst, q, qC, qK, qG);
-    float sg[20];
+    for (int d = 0; d < 3; ++d)
 #pragma unroll
-    for (int k = 0; k < 20; ++k) sg[k] = 0.f;
+        for (int j = 0; j < 3; ++j)
 #pragma unroll
-    for (int a = 0; a < 8; ++a) {
-        const float4* r = reinterpret_cast<const float4*>(&sm[lg][a][0]);
+            for (int m = 0; m < 4; ++m) acc[d][j][m] = 0.f;
 #pragma unroll
-        for (int i = 0; i < 5; ++i) {
-            const float4 x = r[i];
-            sg[4 * i] += N[a] * x.x; sg[4 * i + 1] += N[a] * x.y; sg[4 * i + 2] += N[a] * x.z; sg[4 * i + 3] += N[a] * x.w;
+    for (int type = 0; type < 3; ++type) {
+        float x[8][6];
+#pragma unroll
+        for (int l = 0; l < 8; ++l) {
+            const float4 a = *reinterpret_cast<const float4*>(row[l] + type * 8);
+            const float2 b = *reinterpret_cast<const float2*>(row[l] + type * 8 + 4);
+            x[l][0] = a.x; x[l][1] = a.y; x[l][2] = a.z; x[l][3] = a.w; x[l][4] = b.x; x[l][5] = b.y;
         }
-    }
-    // T^d_c = qC_d sdot_c + qK_d smid_c + qG_d Sbar_c (components xx yy zz xy yz xz)
-    auto T = [&](int d, int c) { return qC[d] * sg[c] + qK[d] * sg[6 + c] + qG[d] * sg[12 + c]; };
-    float4* trow = reinterpret_cast<float4*>(&st[lg][q][0]);
-    trow[0] = make_float4(T(0, 0), T(0, 3), T(0, 5), T(1, 3));
-    trow[1] = make_float4(T(1, 1), T(1, 4), T(2, 5), T(2, 4));
-    trow[2] = make_float4(T(2, 2), 0.f, 0.f, 0.f);
-    __syncwarp();
-    // node q's force: sum over the Gauss points p of dN_q(p) . T(p)
-    const float hh = 0.5f * v.h, W = hh * hh * hh;
-    float f0 = 0.f, f1 = 0.f, f2 = 0.f;
 #pragma unroll
-    for (int gp = 0; gp < 8; ++gp) {
-        float n, dx, dy, dz;
-        cdp_node_at(v.h, q, gp, n, dx, dy, dz);
-        const float4* r = reinterpret_cast<const float4*>(&st[lg][gp][0]);
-        const float4 t0 = r[0], t1 = r[1], t2 = r[2];
-        f0 += dx * t0.x + dy * t0.w + dz * t1.z;          // x: xx(d=x) xy(d=y) xz(d=z)
-        f1 += dx * t0.y + dy * t1.x + dz * t1.w;          // y: xy(x) yy(y) yz(z)
-        f2 += dx * t0.z + dy * t1.y + dz * t2.x;          // z: xz(x) yz(y) zz(z)
+        for (int d = 0; d < 3; ++d)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                const int c = cdp_fcomp(d, j);
+                float z[4];
+#pragma unroll
+                for (int m = 0; m < 4; ++m) z[m] = x[cdp_lex(d, m, 0)][c] + x[cdp_lex(d, m, 1)][c];
+                cdp_interp2(z);
+#pragma unroll
+                for (int m = 0; m < 4; ++m) acc[d][j][m] += cdp_w(s, d, m, type) * z[m];
+            }
     }
-    if (valid) {
-        float* o = v.feu + (((size_t)inst * v.npe + e) * 8 + q) * 3;
-        o[0] = W * f0; o[1] = W * f1; o[2] = W * f2;
-    }
+    float f[8][3];
+#pragma unroll
+    for (int l = 0; l < 8; ++l) f[l][0] = f[l][1] = f[l][2] = 0.f;
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            cdp_interp2(acc[d][j]);
+#pragma unroll
+            for (int m = 0; m < 4; ++m) {
+                f[cdp_lex(d, m, 1)][j] += acc[d][j][m];
+                f[cdp_lex(d, m, 0)][j] -= acc[d][j][m];
+            }
+        }
+    const float hh = 0.5f * v.h, scale = hh * hh * hh / v.h;     // w|J| times the 1/h of the derivative
+    float o[24];
+#pragma unroll
+    for (int l = 0; l < 8; ++l)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) o[cdp_lex_node(l) * 3 + j] = scale * f[l][j];
+    float4* out = reinterpret_cast<float4*>(v.feu + (size_t)gid * 24);
+#pragma unroll
+    for (int i = 0; i < 6; ++i) out[i] = make_float4(o[4 * i], o[4 * i + 1], o[4 * i + 2], o[4 * i + 3]);
 }
 
 // Displacement rows of the PML nodes: R = -(fsol + sum of the element slots)
@@ -752,7 +777,7 @@ __global__ void __launch_bounds__(256) k_cdp_uu(CdpView v) {
     const float* c6 = v.uc + ((size_t)inst * v.np + p) * 6;
     const float cc = c6[3], Ku = c6[4], Gu = c6[5];
     const size_t ib = ((size_t)inst * v.np + p) * 3;
-    float vi[12];
+    float vi[9];
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
         const float uh = v.uh[pad + c], ul = v.ul[pad + c], ph = v.uph[pad + c], pl = v.upl[pad + c];
@@ -773,80 +798,82 @@ __global__ void __launch_bounds__(256) k_cdp_uu(CdpView v) {
         vi[3 + c] = u + 0.5f * du;
         vi[6 + c] = bh + 0.5f * inc;
     }
-    vi[9] = vi[10] = vi[11] = 0.f;
-    float4* o = reinterpret_cast<float4*>(v.vin + ((size_t)inst * v.np + p) * 12);
-    o[0] = make_float4(vi[0], vi[1], vi[2], vi[3]);
-    o[1] = make_float4(vi[4], vi[5], vi[6], vi[7]);
-    o[2] = make_float4(vi[8], vi[9], vi[10], vi[11]);
+    float4* o = reinterpret_cast<float4*>(v.vin + ((size_t)inst * v.np + p) * VIN_ROW);
+    o[0] = make_float4(vi[0], vi[1], vi[2], 0.f);
+    o[1] = make_float4(vi[3], vi[4], vi[5], 0.f);
+    o[2] = make_float4(vi[6], vi[7], vi[8], 0.f);
 }
 
 // Coupling forces of the PML elements on the stress rows:
-// C_Su udot + K_Su umid + G_Su ubar_half = w |J| N_j (stretched strain):
-// lane q forms Gauss point q's stretched strain (6 values) into shared
-// memory, lane j sums node j's vector over the 8 points.
+// C_Su udot + K_Su umid + G_Su ubar_half = w |J| sum_q N_j(q) E(q), E the
+// stretched strain: E_(d,c) = C_d d(udot_c)/dx_d + K_d d(umid_c)/dx_d +
+// G_d d(ubar_c)/dx_d, symmetric pairs added.  One thread per element; the
+// derivative along d is a difference along d, E_(d,c) does not depend on the
+// abscissa along d, and the shape functions along d sum to one over its two
+// points, so each term is a 2 x 2 x 2 map over the two other axes whose
+// result is the same at both nodes along d.
 __global__ void __launch_bounds__(CDP_THREADS) k_cdp_fs(CdpView v) {
-    __shared__ __align__(16) float sm[CDP_GROUPS][8][12];
-    __shared__ __align__(16) float st[CDP_GROUPS][8][8];
     const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const int q = (int)(gid & 7), lg = threadIdx.x >> 3;
-    const long long grp = gid >> 3;
-    const bool valid = grp < (long long)v.ninst * v.npe;
-    const int inst = valid ? (int)(grp / v.npe) : 0, e = valid ? (int)(grp % v.npe) : 0;
-    float4* srow = reinterpret_cast<float4*>(&sm[lg][q][0]);
-    if (valid) {
-        const int p = v.enode[(size_t)e * 8 + q];
-        const float4* src = reinterpret_cast<const float4*>(v.vin + ((size_t)inst * v.np + p) * 12);
+    if (gid >= (long long)v.ninst * v.npe) return;
+    const int inst = (int)(gid / v.npe), e = (int)(gid % v.npe);
+    const CdpStretch s = cdp_stretch(v, e, inst);
+    const float* base = v.vin + (size_t)inst * v.np * VIN_ROW;
+    const float* row[8];
 #pragma unroll
-        for (int i = 0; i < 3; ++i) srow[i] = src[i];
-    } else {
+    for (int l = 0; l < 8; ++l) row[l] = base + (size_t)v.enode[(size_t)e * 8 + cdp_lex_node(l)] * VIN_ROW;
+    float acc[3][3][4];                 // [d][c][m]
 #pragma unroll
-        for (int i = 0; i < 3; ++i) srow[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-    }
-    __syncwarp();
-    float N[8], dN[8][3], qC[3], qK[3], qG[3];
-    cdp_shape(v.h, q, N, dN);
-    (void)N;
-    cdp_weights(v, e, inst, q, qC, qK, qG);
-    // gradients: gr[i][d][c] = d (input i)_c / dx_d
-    float gr[3][3][3];
+    for (int d = 0; d < 3; ++d)
 #pragma unroll
-    for (int i = 0; i < 3; ++i)
+        for (int c = 0; c < 3; ++c)
+#pragma unroll
+            for (int m = 0; m < 4; ++m) acc[d][c][m] = 0.f;
+#pragma unroll
+    for (int type = 0; type < 3; ++type) {
+        float x[8][3];
+#pragma unroll
+        for (int l = 0; l < 8; ++l) {
+            const float4 a = *reinterpret_cast<const float4*>(row[l] + type * 4);
+            x[l][0] = a.x; x[l][1] = a.y; x[l][2] = a.z;
+        }
 #pragma unroll
         for (int d = 0; d < 3; ++d)
 #pragma unroll
-            for (int c = 0; c < 3; ++c) gr[i][d][c] = 0.f;
+            for (int c = 0; c < 3; ++c) {
+                float z[4];
 #pragma unroll
-    for (int a = 0; a < 8; ++a) {
-        const float4* r = reinterpret_cast<const float4*>(&sm[lg][a][0]);
-        const float4 x0 = r[0], x1 = r[1], x2 = r[2];
-        const float in[9] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w, x2.x};
+                for (int m = 0; m < 4; ++m) z[m] = x[cdp_lex(d, m, 1)][c] - x[cdp_lex(d, m, 0)][c];
+                cdp_interp2(z);
 #pragma unroll
-        for (int i = 0; i < 3; ++i)
-#pragma unroll
-            for (int d = 0; d < 3; ++d)
-#pragma unroll
-                for (int c = 0; c < 3; ++c) gr[i][d][c] += dN[a][d] * in[3 * i + c];
+                for (int m = 0; m < 4; ++m) acc[d][c][m] += cdp_w(s, d, m, type) * z[m];
+            }
     }
-    auto wd = [&](int d, int c) { return qC[d] * gr[0][d][c] + qK[d] * gr[1][d][c] + qG[d] * gr[2][d][c]; };
-    float4* trow = reinterpret_cast<float4*>(&st[lg][q][0]);
-    trow[0] = make_float4(wd(0, 0), wd(1, 1), wd(2, 2), wd(1, 0) + wd(0, 1));
-    trow[1] = make_float4(wd(2, 1) + wd(1, 2), wd(2, 0) + wd(0, 2), 0.f, 0.f);
-    __syncwarp();
-    const float hh = 0.5f * v.h, W = hh * hh * hh;
-    float r6[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    float r[8][6];
 #pragma unroll
-    for (int gp = 0; gp < 8; ++gp) {
-        float n, dx, dy, dz;
-        cdp_node_at(v.h, q, gp, n, dx, dy, dz);
-        const float4* r = reinterpret_cast<const float4*>(&st[lg][gp][0]);
-        const float4 t0 = r[0], t1 = r[1];
-        r6[0] += n * t0.x; r6[1] += n * t0.y; r6[2] += n * t0.z; r6[3] += n * t0.w; r6[4] += n * t1.x; r6[5] += n * t1.y;
-    }
-    if (valid) {
-        float* o = v.fes + (((size_t)inst * v.npe + e) * 8 + q) * 6;
+    for (int l = 0; l < 8; ++l)
 #pragma unroll
-        for (int c = 0; c < 6; ++c) o[c] = W * r6[c];
-    }
+        for (int k = 0; k < 6; ++k) r[l][k] = 0.f;
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const int k = cdp_scomp(d, c);
+            cdp_interp2(acc[d][c]);
+#pragma unroll
+            for (int m = 0; m < 4; ++m) {
+                r[cdp_lex(d, m, 0)][k] += acc[d][c][m];
+                r[cdp_lex(d, m, 1)][k] += acc[d][c][m];
+            }
+        }
+    const float hh = 0.5f * v.h, scale = hh * hh * hh / v.h;
+    float o[48];
+#pragma unroll
+    for (int l = 0; l < 8; ++l)
+#pragma unroll
+        for (int k = 0; k < 6; ++k) o[cdp_lex_node(l) * 6 + k] = scale * r[l][k];
+    float4* out = reinterpret_cast<float4*>(v.fes + (size_t)gid * 48);
+#pragma unroll
+    for (int i = 0; i < 12; ++i) out[i] = make_float4(o[4 * i], o[4 * i + 1], o[4 * i + 2], o[4 * i + 3]);
 }
 
 // y = M x for a stress block stored as [xx yy zz xy yz xz | 12 23 13]
@@ -893,7 +920,7 @@ __global__ void __launch_bounds__(256) k_cdp_su(CdpView v) {
 #pragma unroll
     for (int c = 0; c < 6; ++c) R[c] = -F[c] - t1[c] - t2[c] + t3[c];
     cdp_block(K, R, dS);                  // Dinv R
-    float nx[20];
+    float nx[18];
     const float idt = 1.0f / v.dt;
 #pragma unroll
     for (int c = 0; c < 6; ++c) {
@@ -909,10 +936,12 @@ __global__ void __launch_bounds__(256) k_cdp_su(CdpView v) {
         nx[6 + c] = sc[c] + 0.5f * dS[c];
         nx[12 + c] = bh + bl;
     }
-    nx[18] = nx[19] = 0.f;
-    float4* o = reinterpret_cast<float4*>(v.vsu + ((size_t)inst * v.np + p) * 20);
+    float4* o = reinterpret_cast<float4*>(v.vsu + ((size_t)inst * v.np + p) * VSU_ROW);
 #pragma unroll
-    for (int i = 0; i < 5; ++i) o[i] = make_float4(nx[4 * i], nx[4 * i + 1], nx[4 * i + 2], nx[4 * i + 3]);
+    for (int t = 0; t < 3; ++t) {
+        o[2 * t] = make_float4(nx[6 * t], nx[6 * t + 1], nx[6 * t + 2], nx[6 * t + 3]);
+        o[2 * t + 1] = make_float4(nx[6 * t + 4], nx[6 * t + 5], 0.f, 0.f);
+    }
 }
 
 float host_tf32(double x) {
@@ -1416,7 +1445,7 @@ int svl_cdx_create(const svl_grid_spec* g, int32_t ninst, const svl_model_desc* 
         if ((st = h->alloc(ns, &h->fsol)) || (st = h->alloc(n6, &h->sh[0])) || (st = h->alloc(n6, &h->sh[1])) ||
             (st = h->alloc(n6, &h->sl[0])) || (st = h->alloc(n6, &h->sl[1])) || (st = h->alloc(n6, &h->sbh)) ||
             (st = h->alloc(n6, &h->sbl)) || (st = h->alloc(n3, &h->ubh)) || (st = h->alloc(n3, &h->ubl)) ||
-            (st = h->alloc((size_t)ninst * h->np * 12, &h->vin)) || (st = h->alloc((size_t)ninst * h->np * 20, &h->vsu)) ||
+            (st = h->alloc((size_t)ninst * h->np * VIN_ROW, &h->vin)) || (st = h->alloc((size_t)ninst * h->np * VSU_ROW, &h->vsu)) ||
             (st = h->alloc((size_t)ninst * h->npe * 24, &h->feu)) || (st = h->alloc((size_t)ninst * h->npe * 48, &h->fes)) ||
             (st = h->upload(uc, &h->uc)) || (st = h->upload(scs, &h->scs)) || (st = h->upload(estr, &h->estr)) ||
             (st = h->upload(eb0, &h->eb0)) || (st = h->upload(enode, &h->enode)) || (st = h->upload(ninv, &h->ninv)) ||
@@ -1480,14 +1509,14 @@ int svl_cdx_set_initial(svl_cdx* h, int32_t inst, const double* U0, const double
         CUDA_TRY(cudaMemsetAsync(h->ubh + (size_t)inst * h->np * 3, 0, (size_t)h->np * 12, h->stream));
         CUDA_TRY(cudaMemsetAsync(h->ubl + (size_t)inst * h->np * 3, 0, (size_t)h->np * 12, h->stream));
         // the first step's displacement-row inputs: sdot, smid, Sbar = 0
-        std::vector<float> vs((size_t)h->np * 20, 0.f);
+        std::vector<float> vs((size_t)h->np * VSU_ROW, 0.f);
         for (size_t k = 0; k < n6; ++k) {
             const size_t p = k / 6, c = k % 6;
             const double sc = (double)shi[k] + slo[k], sp = (double)sphi[k] + splo[k];
-            vs[p * 20 + c] = (float)((sc - sp) / h->dt);
-            vs[p * 20 + 6 + c] = (float)((sc + sp) / 2.0);
+            vs[p * VSU_ROW + c] = (float)((sc - sp) / h->dt);
+            vs[p * VSU_ROW + 8 + c] = (float)((sc + sp) / 2.0);
         }
-        CUDA_TRY(cudaMemcpyAsync(h->vsu + (size_t)inst * h->np * 20, vs.data(), vs.size() * 4, cudaMemcpyHostToDevice,
+        CUDA_TRY(cudaMemcpyAsync(h->vsu + (size_t)inst * h->np * VSU_ROW, vs.data(), vs.size() * 4, cudaMemcpyHostToDevice,
                                  h->stream));
     }
     CUDA_TRY(cudaStreamSynchronize(h->stream));
@@ -1511,6 +1540,22 @@ static CdpView cdp_view(svl_cdx* h) {
     return c;
 }
 
+// One half of the band's step: 0 = displacement rows (element forces, then
+// the node update), 1 = stress rows.  One thread per PML element, then one per
+// PML node, over all instances.
+static void cdp_launch(svl_cdx* h, const CdpView& c, int half) {
+    const long long ge = (long long)h->ninst * h->npe, gn = (long long)h->ninst * h->np;
+    const unsigned be = (unsigned)((ge + CDP_THREADS - 1) / CDP_THREADS), bn = (unsigned)((gn + 255) / 256);
+    if (half == 0) {
+        k_cdp_fu<<<be, CDP_THREADS, 0, h->stream>>>(c);
+        k_cdp_uu<<<bn, 256, 0, h->stream>>>(c);
+    } else {
+        k_cdp_fs<<<be, CDP_THREADS, 0, h->stream>>>(c);
+        k_cdp_su<<<bn, 256, 0, h->stream>>>(c);
+    }
+    h->launches += 2;
+}
+
 static int cdx_step(svl_cdx* h, int k, bool want_va) {
     CdxView v;
     v.nx = h->nx; v.ny = h->ny; v.nz = h->nz; v.ninst = h->ninst;
@@ -1532,14 +1577,9 @@ static int cdx_step(svl_cdx* h, int k, bool want_va) {
     ++h->launches;
     if (h->np > 0) {
         // the PML band: coupling forces and updates of the PML nodes
-        CdpView c = cdp_view(h);
-        const long long ge = (long long)h->ninst * h->npe * 8, gn = (long long)h->ninst * h->np;
-        const unsigned be = (unsigned)((ge + CDP_THREADS - 1) / CDP_THREADS), bn = (unsigned)((gn + 255) / 256);
-        k_cdp_fu<<<be, CDP_THREADS, 0, h->stream>>>(c);
-        k_cdp_uu<<<bn, 256, 0, h->stream>>>(c);
-        k_cdp_fs<<<be, CDP_THREADS, 0, h->stream>>>(c);
-        k_cdp_su<<<bn, 256, 0, h->stream>>>(c);
-        h->launches += 4;
+        const CdpView c = cdp_view(h);
+        cdp_launch(h, c, 0);
+        cdp_launch(h, c, 1);
     }
     if (want_va) {
         k_cdx_va<<<(unsigned)((ns + 255) / 256), 256, 0, h->stream>>>(v.uh_prev, v.ul_prev, h->uh[h->cur], h->ul[h->cur], h->ph_copy,
@@ -1706,15 +1746,10 @@ int svl_cdx_profile(svl_cdx* h, int32_t k_first, int32_t nsteps, double* ms_kern
         h->cur = 1 - h->cur;                         // cdx_step flipped it; the band still belongs to this step
         CUDA_TRY(cudaEventRecord(ev[1], h->stream));
         if (np > 0) {
-            CdpView c = cdp_view(h);
-            const long long ge = (long long)h->ninst * h->npe * 8, gn = (long long)h->ninst * h->np;
-            const unsigned be = (unsigned)((ge + CDP_THREADS - 1) / CDP_THREADS), bn = (unsigned)((gn + 255) / 256);
-            k_cdp_fu<<<be, CDP_THREADS, 0, h->stream>>>(c);
-            k_cdp_uu<<<bn, 256, 0, h->stream>>>(c);
+            const CdpView c = cdp_view(h);
+            cdp_launch(h, c, 0);
             CUDA_TRY(cudaEventRecord(ev[2], h->stream));
-            k_cdp_fs<<<be, CDP_THREADS, 0, h->stream>>>(c);
-            k_cdp_su<<<bn, 256, 0, h->stream>>>(c);
-            h->launches += 4;
+            cdp_launch(h, c, 1);
         } else {
             CUDA_TRY(cudaEventRecord(ev[2], h->stream));
         }
