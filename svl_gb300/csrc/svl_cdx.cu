@@ -595,7 +595,7 @@ struct CdpView {
     const int32_t* __restrict__ ninv;   // [np][8] element slots e*8 + local node in element order, -1 unused
     const long long* __restrict__ npad; // [np] padded offset of the node's displacement in instance 0
     const float* __restrict__ uc;       // [ninst][np][6] 1/d for x y z (0 when restrained), c, Ku, Gu
-    const float* __restrict__ scs;      // [ninst][np][36] Dinv, A, KG, Gs (9 each: xx yy zz xy yz xz | 12 23 13)
+    const float* __restrict__ scs;      // [ninst][np][12] Dinv, A, KG, Gs as (diagonal, off-diagonal, shear)
     const float* __restrict__ uh;       // u_n pair (padded)
     const float* __restrict__ ul;
     float* uph;                         // u_{n-1} pair in, u_{n+1} out
@@ -615,6 +615,7 @@ struct CdpView {
 constexpr int CDP_THREADS = 256;
 constexpr int VSU_ROW = 24;             // [sdot | smid | Sbar] x (xx yy zz xy yz xz, 2 pad)
 constexpr int VIN_ROW = 12;             // [udot | umid | ubar at the half step] x (x y z, 1 pad)
+constexpr int SCS_ROW = 12;             // Dinv, A, KG, Gs stress blocks, (diagonal, off-diagonal, shear) each
 
 // Linear shape functions of one axis at its two Gauss points:
 // B[q][i] = (1 + s_i xi_q) / 2 with s = (-1, +1), xi = (-g, +g)
@@ -652,14 +653,11 @@ __device__ __forceinline__ void cdp_interp2(float z[4]) {
 struct CdpStretch {
     float a[3][2], b[3][2];
 };
-__device__ __forceinline__ CdpStretch cdp_stretch(const CdpView& v, int e, int inst) {
-    const float4* t = reinterpret_cast<const float4*>(v.estr + (size_t)e * 12);
-    const float b0 = v.eb0[(size_t)inst * v.npe + e];
+__device__ __forceinline__ CdpStretch cdp_stretch(const float4 t[3], float b0) {
     CdpStretch s;
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-        const float4 x = t[d];
-        s.a[d][0] = x.x; s.a[d][1] = x.y; s.b[d][0] = b0 * x.z; s.b[d][1] = b0 * x.w;
+        s.a[d][0] = t[d].x; s.a[d][1] = t[d].y; s.b[d][0] = b0 * t[d].z; s.b[d][1] = b0 * t[d].w;
     }
     return s;
 }
@@ -694,15 +692,23 @@ __device__ __forceinline__ constexpr int cdp_scomp(int d, int c) {
 // on the abscissa along d, so the sum over the two points along d acts on the
 // node values first (their sum), and everything else is a 2 x 2 x 2 map
 // over the two other axes (sum factorisation): no per-point 8 x 8 products.
-__global__ void __launch_bounds__(CDP_THREADS) k_cdp_fu(CdpView v) {
+__global__ void __launch_bounds__(CDP_THREADS, 2) k_cdp_fu(CdpView v) {
     const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (gid >= (long long)v.ninst * v.npe) return;
-    const int inst = (int)(gid / v.npe), e = (int)(gid % v.npe);
-    const CdpStretch s = cdp_stretch(v, e, inst);
+    if (gid >= (long long)v.npe) return;
+    const int e = (int)gid;
+    int node[8];
+#pragma unroll
+    for (int l = 0; l < 8; ++l) node[l] = v.enode[(size_t)e * 8 + cdp_lex_node(l)];
+    float4 t[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) t[d] = reinterpret_cast<const float4*>(v.estr + (size_t)e * 12)[d];
+#pragma unroll 1
+    for (int inst = 0; inst < v.ninst; ++inst) {
+    const CdpStretch s = cdp_stretch(t, v.eb0[(size_t)inst * v.npe + e]);
     const float* base = v.vsu + (size_t)inst * v.np * VSU_ROW;
     const float* row[8];
 #pragma unroll
-    for (int l = 0; l < 8; ++l) row[l] = base + (size_t)v.enode[(size_t)e * 8 + cdp_lex_node(l)] * VSU_ROW;
+    for (int l = 0; l < 8; ++l) row[l] = base + (size_t)node[l] * VSU_ROW;
     float acc[3][3][4];
 #pragma unroll
     for (int d = 0; d < 3; ++d)
@@ -752,56 +758,64 @@ __global__ void __launch_bounds__(CDP_THREADS) k_cdp_fu(CdpView v) {
     for (int l = 0; l < 8; ++l)
 #pragma unroll
         for (int j = 0; j < 3; ++j) o[cdp_lex_node(l) * 3 + j] = scale * f[l][j];
-    float4* out = reinterpret_cast<float4*>(v.feu + (size_t)gid * 24);
+    float4* out = reinterpret_cast<float4*>(v.feu + ((size_t)inst * v.npe + e) * 24);
 #pragma unroll
     for (int i = 0; i < 6; ++i) out[i] = make_float4(o[4 * i], o[4 * i + 1], o[4 * i + 2], o[4 * i + 3]);
+    }
 }
 
 // Displacement rows of the PML nodes: R = -(fsol + sum of the element slots)
 // - Ku u - Gu ubar + c (u - u_{n-1}), du = R / d; u_{n+1} = u + du and
-// ubar += dt (u + du/2) as pairs; the stress rows' inputs.
+// ubar += dt (u + du/2) as pairs; the stress rows' inputs.  One thread per
+// PML node, looping over the instances.
 __global__ void __launch_bounds__(256) k_cdp_uu(CdpView v) {
     const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (gid >= (long long)v.ninst * v.np) return;
-    const int inst = (int)(gid / v.np), p = (int)(gid % v.np);
-    const long long pad = (long long)inst * v.per + v.npad[p];
-    float f[3] = {v.fsol[pad], v.fsol[pad + 1], v.fsol[pad + 2]};
-    const size_t fb = (size_t)inst * v.npe * 8;
+    if (gid >= (long long)v.np) return;
+    const int p = (int)gid;
+    int slots[8];
 #pragma unroll
-    for (int s2 = 0; s2 < 8; ++s2) {
-        const int slot = v.ninv[(size_t)p * 8 + s2];
-        if (slot < 0) break;
-        const float* fe = v.feu + (fb + slot) * 3;
-        f[0] += fe[0]; f[1] += fe[1]; f[2] += fe[2];
-    }
-    const float* c6 = v.uc + ((size_t)inst * v.np + p) * 6;
-    const float cc = c6[3], Ku = c6[4], Gu = c6[5];
-    const size_t ib = ((size_t)inst * v.np + p) * 3;
-    float vi[9];
+    for (int s2 = 0; s2 < 8; ++s2) slots[s2] = v.ninv[(size_t)p * 8 + s2];
+    const long long np0 = v.npad[p];
+#pragma unroll 1
+    for (int inst = 0; inst < v.ninst; ++inst) {
+        const long long pad = (long long)inst * v.per + np0;
+        float f[3] = {v.fsol[pad], v.fsol[pad + 1], v.fsol[pad + 2]};
+        const size_t fb = (size_t)inst * v.npe * 8;
 #pragma unroll
-    for (int c = 0; c < 3; ++c) {
-        const float uh = v.uh[pad + c], ul = v.ul[pad + c], ph = v.uph[pad + c], pl = v.upl[pad + c];
-        const float bh = v.ubh[ib + c], bl = v.ubl[ib + c];
-        const float u = uh + ul;
-        const float R = -f[c] - Ku * u - Gu * bh + cc * ((uh - ph) + (ul - pl));
-        const float du = c6[c] * R;
-        float nh, nl;
-        df_add(uh, ul, du, 0.f, nh, nl);
-        v.uph[pad + c] = nh;
-        v.upl[pad + c] = nl;
-        const float inc = v.dt * (u + 0.5f * du);
-        float bh2, bl2;
-        df_add(bh, bl, inc, 0.f, bh2, bl2);
-        v.ubh[ib + c] = bh2;
-        v.ubl[ib + c] = bl2;
-        vi[c] = du / v.dt;
-        vi[3 + c] = u + 0.5f * du;
-        vi[6 + c] = bh + 0.5f * inc;
+        for (int s2 = 0; s2 < 8; ++s2) {
+            if (slots[s2] < 0) break;
+            const float* fe = v.feu + (fb + slots[s2]) * 3;
+            f[0] += fe[0]; f[1] += fe[1]; f[2] += fe[2];
+        }
+        const float* c6 = v.uc + ((size_t)inst * v.np + p) * 6;
+        const float cc = c6[3], Ku = c6[4], Gu = c6[5];
+        const size_t ib = ((size_t)inst * v.np + p) * 3;
+        float vi[9];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const float uh = v.uh[pad + c], ul = v.ul[pad + c], ph = v.uph[pad + c], pl = v.upl[pad + c];
+            const float bh = v.ubh[ib + c], bl = v.ubl[ib + c];
+            const float u = uh + ul;
+            const float R = -f[c] - Ku * u - Gu * bh + cc * ((uh - ph) + (ul - pl));
+            const float du = c6[c] * R;
+            float nh, nl;
+            df_add(uh, ul, du, 0.f, nh, nl);
+            v.uph[pad + c] = nh;
+            v.upl[pad + c] = nl;
+            const float inc = v.dt * (u + 0.5f * du);
+            float bh2, bl2;
+            df_add(bh, bl, inc, 0.f, bh2, bl2);
+            v.ubh[ib + c] = bh2;
+            v.ubl[ib + c] = bl2;
+            vi[c] = du / v.dt;
+            vi[3 + c] = u + 0.5f * du;
+            vi[6 + c] = bh + 0.5f * inc;
+        }
+        float4* o = reinterpret_cast<float4*>(v.vin + ((size_t)inst * v.np + p) * VIN_ROW);
+        o[0] = make_float4(vi[0], vi[1], vi[2], 0.f);
+        o[1] = make_float4(vi[3], vi[4], vi[5], 0.f);
+        o[2] = make_float4(vi[6], vi[7], vi[8], 0.f);
     }
-    float4* o = reinterpret_cast<float4*>(v.vin + ((size_t)inst * v.np + p) * VIN_ROW);
-    o[0] = make_float4(vi[0], vi[1], vi[2], 0.f);
-    o[1] = make_float4(vi[3], vi[4], vi[5], 0.f);
-    o[2] = make_float4(vi[6], vi[7], vi[8], 0.f);
 }
 
 // Coupling forces of the PML elements on the stress rows:
@@ -812,15 +826,23 @@ __global__ void __launch_bounds__(256) k_cdp_uu(CdpView v) {
 // abscissa along d, and the shape functions along d sum to one over its two
 // points, so each term is a 2 x 2 x 2 map over the two other axes whose
 // result is the same at both nodes along d.
-__global__ void __launch_bounds__(CDP_THREADS) k_cdp_fs(CdpView v) {
+__global__ void __launch_bounds__(CDP_THREADS, 2) k_cdp_fs(CdpView v) {
     const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (gid >= (long long)v.ninst * v.npe) return;
-    const int inst = (int)(gid / v.npe), e = (int)(gid % v.npe);
-    const CdpStretch s = cdp_stretch(v, e, inst);
+    if (gid >= (long long)v.npe) return;
+    const int e = (int)gid;
+    int node[8];
+#pragma unroll
+    for (int l = 0; l < 8; ++l) node[l] = v.enode[(size_t)e * 8 + cdp_lex_node(l)];
+    float4 t[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) t[d] = reinterpret_cast<const float4*>(v.estr + (size_t)e * 12)[d];
+#pragma unroll 1
+    for (int inst = 0; inst < v.ninst; ++inst) {
+    const CdpStretch s = cdp_stretch(t, v.eb0[(size_t)inst * v.npe + e]);
     const float* base = v.vin + (size_t)inst * v.np * VIN_ROW;
     const float* row[8];
 #pragma unroll
-    for (int l = 0; l < 8; ++l) row[l] = base + (size_t)v.enode[(size_t)e * 8 + cdp_lex_node(l)] * VIN_ROW;
+    for (int l = 0; l < 8; ++l) row[l] = base + (size_t)node[l] * VIN_ROW;
     float acc[3][3][4];                 // [d][c][m]
 #pragma unroll
     for (int d = 0; d < 3; ++d)
@@ -871,76 +893,86 @@ __global__ void __launch_bounds__(CDP_THREADS) k_cdp_fs(CdpView v) {
     for (int l = 0; l < 8; ++l)
 #pragma unroll
         for (int k = 0; k < 6; ++k) o[cdp_lex_node(l) * 6 + k] = scale * r[l][k];
-    float4* out = reinterpret_cast<float4*>(v.fes + (size_t)gid * 48);
+    float4* out = reinterpret_cast<float4*>(v.fes + ((size_t)inst * v.npe + e) * 48);
 #pragma unroll
     for (int i = 0; i < 12; ++i) out[i] = make_float4(o[4 * i], o[4 * i + 1], o[4 * i + 2], o[4 * i + 3]);
+    }
 }
 
-// y = M x for a stress block stored as [xx yy zz xy yz xz | 12 23 13]
-__device__ __forceinline__ void cdp_block(const float* Mb, const float x[6], float y[6]) {
-    y[0] = Mb[0] * x[0] + Mb[3] * x[1] + Mb[5] * x[2];
-    y[1] = Mb[3] * x[0] + Mb[1] * x[1] + Mb[4] * x[2];
-    y[2] = Mb[5] * x[0] + Mb[4] * x[1] + Mb[2] * x[2];
-    y[3] = Mb[6] * x[3];
-    y[4] = Mb[7] * x[4];
-    y[5] = Mb[8] * x[5];
+// y = M x for a stress block of isotropic structure: diagonal d and
+// off-diagonal o on the normal components (xx yy zz), s on the shear ones.
+__device__ __forceinline__ void cdp_block(float d, float o, float s, const float x[6], float y[6]) {
+    y[0] = d * x[0] + o * (x[1] + x[2]);
+    y[1] = d * x[1] + o * (x[0] + x[2]);
+    y[2] = d * x[2] + o * (x[0] + x[1]);
+    y[3] = s * x[3];
+    y[4] = s * x[4];
+    y[5] = s * x[5];
 }
 
 // Stress rows of the PML nodes: R = -Fs - KG S - Gs Sbar + A (S - S_prev),
 // dS = Dinv R; S_next = S + dS and Sbar += dt S as pairs; and the next
-// step's displacement-row inputs (sdot = dS/dt, smid = S + dS/2, Sbar).
+// step's displacement-row inputs (sdot = dS/dt, smid = S + dS/2, Sbar).  One
+// thread per PML node, looping over the instances.
 __global__ void __launch_bounds__(256) k_cdp_su(CdpView v) {
     const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (gid >= (long long)v.ninst * v.np) return;
-    const int inst = (int)(gid / v.np), p = (int)(gid % v.np);
-    float F[6] = {0, 0, 0, 0, 0, 0};
-    const size_t fb = (size_t)inst * v.npe * 8;
+    if (gid >= (long long)v.np) return;
+    const int p = (int)gid;
+    int slots[8];
 #pragma unroll
-    for (int s2 = 0; s2 < 8; ++s2) {
-        const int slot = v.ninv[(size_t)p * 8 + s2];
-        if (slot < 0) break;
-        const float* fe = v.fes + (fb + slot) * 6;
+    for (int s2 = 0; s2 < 8; ++s2) slots[s2] = v.ninv[(size_t)p * 8 + s2];
+#pragma unroll 1
+    for (int inst = 0; inst < v.ninst; ++inst) {
+        float F[6] = {0, 0, 0, 0, 0, 0};
+        const size_t fb = (size_t)inst * v.npe * 8;
 #pragma unroll
-        for (int c = 0; c < 6; ++c) F[c] += fe[c];
-    }
-    const size_t b = ((size_t)inst * v.np + p) * 6;
-    float sc[6], ds[6], sb[6];
+        for (int s2 = 0; s2 < 8; ++s2) {
+            if (slots[s2] < 0) break;
+            const float2* fe = reinterpret_cast<const float2*>(v.fes + (fb + slots[s2]) * 6);
+            const float2 a = fe[0], b2 = fe[1], c2 = fe[2];
+            F[0] += a.x; F[1] += a.y; F[2] += b2.x; F[3] += b2.y; F[4] += c2.x; F[5] += c2.y;
+        }
+        const size_t b = ((size_t)inst * v.np + p) * 6;
+        float sc[6], ds[6], sb[6], ch[6], cl[6];
 #pragma unroll
-    for (int c = 0; c < 6; ++c) {
-        const float ch = v.sh[b + c], cl = v.sl[b + c], ph = v.sph[b + c], pl = v.spl[b + c];
-        sc[c] = ch + cl;
-        ds[c] = (ch - ph) + (cl - pl);
-        sb[c] = v.sbh[b + c];
-    }
-    const float* K = v.scs + ((size_t)inst * v.np + p) * 36;
-    float t1[6], t2[6], t3[6], R[6], dS[6];
-    cdp_block(K + 18, sc, t1);            // KG S
-    cdp_block(K + 27, sb, t2);            // Gs Sbar
-    cdp_block(K + 9, ds, t3);             // A (S - S_prev)
+        for (int c = 0; c < 6; ++c) {
+            ch[c] = v.sh[b + c]; cl[c] = v.sl[b + c];
+            const float ph = v.sph[b + c], pl = v.spl[b + c];
+            sc[c] = ch[c] + cl[c];
+            ds[c] = (ch[c] - ph) + (cl[c] - pl);
+            sb[c] = v.sbh[b + c];
+        }
+        const float4* K4 = reinterpret_cast<const float4*>(v.scs + ((size_t)inst * v.np + p) * SCS_ROW);
+        const float4 k0 = K4[0], k1 = K4[1], k2 = K4[2];
+        float t1[6], t2[6], t3[6], R[6], dS[6];
+        cdp_block(k1.z, k1.w, k2.x, sc, t1);      // KG S
+        cdp_block(k2.y, k2.z, k2.w, sb, t2);      // Gs Sbar
+        cdp_block(k0.w, k1.x, k1.y, ds, t3);      // A (S - S_prev)
 #pragma unroll
-    for (int c = 0; c < 6; ++c) R[c] = -F[c] - t1[c] - t2[c] + t3[c];
-    cdp_block(K, R, dS);                  // Dinv R
-    float nx[18];
-    const float idt = 1.0f / v.dt;
+        for (int c = 0; c < 6; ++c) R[c] = -F[c] - t1[c] - t2[c] + t3[c];
+        cdp_block(k0.x, k0.y, k0.z, R, dS);       // Dinv R
+        float nx[18];
+        const float idt = 1.0f / v.dt;
 #pragma unroll
-    for (int c = 0; c < 6; ++c) {
-        float nh, nl;
-        df_add(v.sh[b + c], v.sl[b + c], dS[c], 0.f, nh, nl);
-        v.sph[b + c] = nh;
-        v.spl[b + c] = nl;
-        float bh, bl;
-        df_add(v.sbh[b + c], v.sbl[b + c], v.dt * sc[c], 0.f, bh, bl);
-        v.sbh[b + c] = bh;
-        v.sbl[b + c] = bl;
-        nx[c] = dS[c] * idt;
-        nx[6 + c] = sc[c] + 0.5f * dS[c];
-        nx[12 + c] = bh + bl;
-    }
-    float4* o = reinterpret_cast<float4*>(v.vsu + ((size_t)inst * v.np + p) * VSU_ROW);
+        for (int c = 0; c < 6; ++c) {
+            float nh, nl;
+            df_add(ch[c], cl[c], dS[c], 0.f, nh, nl);
+            v.sph[b + c] = nh;
+            v.spl[b + c] = nl;
+            float bh, bl;
+            df_add(sb[c], v.sbl[b + c], v.dt * sc[c], 0.f, bh, bl);
+            v.sbh[b + c] = bh;
+            v.sbl[b + c] = bl;
+            nx[c] = dS[c] * idt;
+            nx[6 + c] = sc[c] + 0.5f * dS[c];
+            nx[12 + c] = bh + bl;
+        }
+        float4* o = reinterpret_cast<float4*>(v.vsu + ((size_t)inst * v.np + p) * VSU_ROW);
 #pragma unroll
-    for (int t = 0; t < 3; ++t) {
-        o[2 * t] = make_float4(nx[6 * t], nx[6 * t + 1], nx[6 * t + 2], nx[6 * t + 3]);
-        o[2 * t + 1] = make_float4(nx[6 * t + 4], nx[6 * t + 5], 0.f, 0.f);
+        for (int t = 0; t < 3; ++t) {
+            o[2 * t] = make_float4(nx[6 * t], nx[6 * t + 1], nx[6 * t + 2], nx[6 * t + 3]);
+            o[2 * t + 1] = make_float4(nx[6 * t + 4], nx[6 * t + 5], 0.f, 0.f);
+        }
     }
 }
 
@@ -1286,15 +1318,29 @@ int svl_cdx_create(const svl_grid_spec* g, int32_t ninst, const svl_model_desc* 
                 const double* Ks = &T.Ks[(size_t)sn * 36];
                 const double* Gs = &T.Gs[(size_t)sn * 36];
                 const double* Di = &T.Dinv[(size_t)sn * 36];
-                float blk[36];
+                double blk[36];
                 for (int k2 = 0; k2 < 9; ++k2) {
                     const int i = pk[k2][0] * 6 + pk[k2][1];
-                    blk[k2] = (float)Di[i];
-                    blk[9 + k2] = (float)(Ms[i] / dt / dt - Cs[i] / 2.0 / dt);
-                    blk[18 + k2] = (float)(Ks[i] + dt / 2.0 * Gs[i]);
-                    blk[27 + k2] = (float)Gs[i];
+                    blk[k2] = Di[i];
+                    blk[9 + k2] = Ms[i] / dt / dt - Cs[i] / 2.0 / dt;
+                    blk[18 + k2] = Ks[i] + dt / 2.0 * Gs[i];
+                    blk[27 + k2] = Gs[i];
                 }
-                scs.insert(scs.end(), blk, blk + 36);
+                // isotropic materials give every block the form d I + o (1 1^T - I) on the
+                // normal components and s I on the shear ones: three numbers per block
+                for (int kb = 0; kb < 4; ++kb) {
+                    const double* B = blk + 9 * kb;
+                    const double sc2 = std::max(std::fabs(B[0]), std::fabs(B[3])), tol = 1e-10;
+                    if (std::fabs(B[1] - B[0]) > tol * sc2 || std::fabs(B[2] - B[0]) > tol * sc2 ||
+                        std::fabs(B[4] - B[3]) > tol * sc2 || std::fabs(B[5] - B[3]) > tol * sc2 ||
+                        std::fabs(B[7] - B[6]) > tol * std::fabs(B[6]) || std::fabs(B[8] - B[6]) > tol * std::fabs(B[6])) {
+                        set_error("instance %d: PML node %lld has a stress block without isotropic structure", b, n);
+                        return fail(SVL_ERR_UNSUPPORTED);
+                    }
+                    scs.push_back((float)B[0]);
+                    scs.push_back((float)B[3]);
+                    scs.push_back((float)B[6]);
+                }
             }
             for (int i = 0; i < h->npe; ++i) {
                 const double* pr = m.param(pelem[i]);
@@ -1542,9 +1588,9 @@ static CdpView cdp_view(svl_cdx* h) {
 
 // One half of the band's step: 0 = displacement rows (element forces, then
 // the node update), 1 = stress rows.  One thread per PML element, then one per
-// PML node, over all instances.
+// PML node, each looping over the instances (their tables are read once).
 static void cdp_launch(svl_cdx* h, const CdpView& c, int half) {
-    const long long ge = (long long)h->ninst * h->npe, gn = (long long)h->ninst * h->np;
+    const long long ge = h->npe, gn = h->np;
     const unsigned be = (unsigned)((ge + CDP_THREADS - 1) / CDP_THREADS), bn = (unsigned)((gn + 255) / 256);
     if (half == 0) {
         k_cdp_fu<<<be, CDP_THREADS, 0, h->stream>>>(c);
