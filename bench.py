@@ -608,19 +608,23 @@ def main():
     npml_el = int(np.sum(m.elem_pml)) if pml else 0
     if args.precision == "mixed":
         grid_dofs = 3 * int(np.prod([g + 1 for g in grid]))
-        kinds = {"k_cdx_step (tensor-core interior step, all instances)": (0, ALGO_BYTES_PER_DOF[3] * grid_dofs * nb),
-                 "k_cdp_fu + k_cdp_uu (PML band, displacement rows)":
-                     (1, (PML_BYTES_PER_NODE * 0.5 * npml_nodes + PML_BYTES_PER_ELEMENT * npml_el) * nb),
-                 "k_cdp_fs + k_cdp_su (PML band, stress rows)":
-                     (2, (PML_BYTES_PER_NODE * 0.5 * npml_nodes + PML_BYTES_PER_ELEMENT * npml_el) * nb)}
-        kinds = {k: v for k, v in kinds.items() if prof[v[0]] > 0}
-        kname = max(kinds, key=lambda k: prof[kinds[k][0]])
-        kidx, algo_bytes = kinds[kname]
-        k_ms = prof[kidx] / 20.0
-        shares = {k: round(float(prof[v[0]] / max(prof.sum(), 1e-12)), 4) for k, v in kinds.items()}
-        per_kernel = {k: {"ms_per_step": float(prof[v[0]] / 20.0),
-                          "algorithmic_bytes": v[1],
-                          "achieved_gbs": v[1] / (prof[v[0]] / 20.0 / 1e3) / 1e9} for k, v in kinds.items()}
+        half = (PML_BYTES_PER_NODE * 0.5 * npml_nodes + PML_BYTES_PER_ELEMENT * npml_el) * nb
+        # profile slots: 0 k_cdx_step, 1 k_cdp_fu, 2 k_cdp_uu, 3 k_cdp_fs, 4 k_cdp_su
+        kinds = {"k_cdx_step (tensor-core interior step, all instances)": ((0,), ALGO_BYTES_PER_DOF[3] * grid_dofs * nb),
+                 "k_cdp_fu + k_cdp_uu (PML band, displacement rows)": ((1, 2), half),
+                 "k_cdp_fs + k_cdp_su (PML band, stress rows)": ((3, 4), half)}
+        pms = {k: float(sum(prof[i] for i in v[0])) / 20.0 for k, v in kinds.items()}
+        kinds = {k: v for k, v in kinds.items() if pms[k] > 0}
+        kname = max(kinds, key=lambda k: pms[k])
+        algo_bytes = kinds[kname][1]
+        k_ms = pms[kname]
+        tot = sum(pms[k] for k in kinds)
+        shares = {k: round(pms[k] / max(tot, 1e-12), 4) for k in kinds}
+        per_kernel = {k: {"ms_per_step": pms[k], "algorithmic_bytes": v[1],
+                          "achieved_gbs": v[1] / (pms[k] / 1e3) / 1e9} for k, v in kinds.items()}
+        if pml:
+            per_kernel["band kernels, ms per step"] = {n: float(prof[i] / 20.0) for i, n in
+                                                       enumerate(["k_cdp_fu", "k_cdp_uu", "k_cdp_fs", "k_cdp_su"], 1)}
     else:
         algo_bytes = ALGO_BYTES_PER_DOF[nd] * nfree_total
         if args.workload == "config3":

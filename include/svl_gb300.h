@@ -305,10 +305,12 @@ int  svl_cdx_launch_count(svl_cdx* cdx, int64_t* launches);
  * (a test and tuning hook: the results do not depend on it).  No
  * counterpart in the reference. */
 int  svl_cdx_set_ctas(svl_cdx* cdx, int32_t ctas);
-/* Runs nsteps (no history) with CUDA events between the kernel kinds of each
- * step; ms_kernel[i] receives the summed device time of kind i: 0 = the fused
- * tensor-core step, 1 = the PML band's displacement rows, 2 = its stress
- * rows (3, 4 unused).  No counterpart in the reference (measurement hook). */
+/* Runs nsteps (no history) with CUDA events between the kernels of each
+ * step; ms_kernel[i] receives the summed device time of kernel i: 0 = the
+ * fused tensor-core step, then the PML band's 1 = element forces on the
+ * displacement rows, 2 = displacement-row update, 3 = element forces on the
+ * stress rows, 4 = stress-row update (0 without a band).  No counterpart in
+ * the reference (measurement hook). */
 int  svl_cdx_profile(svl_cdx* cdx, int32_t k_first, int32_t nsteps, double* ms_kernel);
 int  svl_cdx_get_ctas(svl_cdx* cdx, int32_t* ctas);
 void svl_cdx_destroy(svl_cdx* cdx);

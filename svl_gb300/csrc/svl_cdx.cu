@@ -606,15 +606,19 @@ struct CdpView {
     const float* __restrict__ sl;
     float* sph; float* spl;             // S^{n-1/2} in, S^{n+3/2} out
     float* sbh; float* sbl;             // Sbar pair [ninst][np][6]
-    float* vsu;                         // [ninst][np][24] displacement rows' inputs: sdot, smid, Sbar, 8 floats each (written by k_cdp_su for the next step)
-    float* vin;                         // [ninst][np][12] stress rows' inputs: udot, umid, ubar at the half step, 4 floats each
-    float* feu;                         // [ninst][npe][8][3]
-    float* fes;                         // [ninst][npe][8][6]
+    float* vsu;                         // [ninst][18][np] displacement rows' inputs: sdot, smid, Sbar (written by k_cdp_su for the next step)
+    float* vin;                         // [ninst][9][np] stress rows' inputs: udot, umid, ubar at the half step
+    float* feu;                         // [ninst][8][3][npe] element slots (local node, component, element)
+    float* fes;                         // [ninst][8][6][npe]
 };
 
-constexpr int CDP_THREADS = 256;
-constexpr int VSU_ROW = 24;             // [sdot | smid | Sbar] x (xx yy zz xy yz xz, 2 pad)
-constexpr int VIN_ROW = 12;             // [udot | umid | ubar at the half step] x (x y z, 1 pad)
+constexpr int CDP_THREADS = 128;
+// Node rows and element slots are stored component-major ([..][component][node]
+// and [..][local node][component][element]): consecutive threads handle
+// consecutive nodes / elements, so every load and store of a warp is one
+// contiguous run.
+constexpr int VSU_K = 18;               // sdot, smid, Sbar x (xx yy zz xy yz xz)
+constexpr int VIN_K = 9;                // udot, umid, ubar at the half step x (x y z)
 constexpr int SCS_ROW = 12;             // Dinv, A, KG, Gs stress blocks, (diagonal, off-diagonal, shear) each
 
 // Linear shape functions of one axis at its two Gauss points:
@@ -692,7 +696,7 @@ __device__ __forceinline__ constexpr int cdp_scomp(int d, int c) {
 // on the abscissa along d, so the sum over the two points along d acts on the
 // node values first (their sum), and everything else is a 2 x 2 x 2 map
 // over the two other axes (sum factorisation): no per-point 8 x 8 products.
-__global__ void __launch_bounds__(CDP_THREADS, 2) k_cdp_fu(CdpView v) {
+__global__ void __launch_bounds__(CDP_THREADS, 4) k_cdp_fu(CdpView v) {
     const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (gid >= (long long)v.npe) return;
     const int e = (int)gid;
@@ -705,10 +709,7 @@ __global__ void __launch_bounds__(CDP_THREADS, 2) k_cdp_fu(CdpView v) {
 #pragma unroll 1
     for (int inst = 0; inst < v.ninst; ++inst) {
     const CdpStretch s = cdp_stretch(t, v.eb0[(size_t)inst * v.npe + e]);
-    const float* base = v.vsu + (size_t)inst * v.np * VSU_ROW;
-    const float* row[8];
-#pragma unroll
-    for (int l = 0; l < 8; ++l) row[l] = base + (size_t)node[l] * VSU_ROW;
+    const float* base = v.vsu + (size_t)inst * VSU_K * v.np;
     float acc[3][3][4];
 #pragma unroll
     for (int d = 0; d < 3; ++d)
@@ -720,11 +721,9 @@ __global__ void __launch_bounds__(CDP_THREADS, 2) k_cdp_fu(CdpView v) {
     for (int type = 0; type < 3; ++type) {
         float x[8][6];
 #pragma unroll
-        for (int l = 0; l < 8; ++l) {
-            const float4 a = *reinterpret_cast<const float4*>(row[l] + type * 8);
-            const float2 b = *reinterpret_cast<const float2*>(row[l] + type * 8 + 4);
-            x[l][0] = a.x; x[l][1] = a.y; x[l][2] = a.z; x[l][3] = a.w; x[l][4] = b.x; x[l][5] = b.y;
-        }
+        for (int l = 0; l < 8; ++l)
+#pragma unroll
+            for (int c = 0; c < 6; ++c) x[l][c] = base[(size_t)(type * 6 + c) * v.np + node[l]];
 #pragma unroll
         for (int d = 0; d < 3; ++d)
 #pragma unroll
@@ -758,9 +757,9 @@ __global__ void __launch_bounds__(CDP_THREADS, 2) k_cdp_fu(CdpView v) {
     for (int l = 0; l < 8; ++l)
 #pragma unroll
         for (int j = 0; j < 3; ++j) o[cdp_lex_node(l) * 3 + j] = scale * f[l][j];
-    float4* out = reinterpret_cast<float4*>(v.feu + ((size_t)inst * v.npe + e) * 24);
+    float* out = v.feu + (size_t)inst * 24 * v.npe + e;
 #pragma unroll
-    for (int i = 0; i < 6; ++i) out[i] = make_float4(o[4 * i], o[4 * i + 1], o[4 * i + 2], o[4 * i + 3]);
+    for (int i = 0; i < 24; ++i) out[(size_t)i * v.npe] = o[i];
     }
 }
 
@@ -768,7 +767,7 @@ __global__ void __launch_bounds__(CDP_THREADS, 2) k_cdp_fu(CdpView v) {
 // - Ku u - Gu ubar + c (u - u_{n-1}), du = R / d; u_{n+1} = u + du and
 // ubar += dt (u + du/2) as pairs; the stress rows' inputs.  One thread per
 // PML node, looping over the instances.
-__global__ void __launch_bounds__(256) k_cdp_uu(CdpView v) {
+__global__ void __launch_bounds__(256, 4) k_cdp_uu(CdpView v) {
     const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (gid >= (long long)v.np) return;
     const int p = (int)gid;
@@ -780,12 +779,12 @@ __global__ void __launch_bounds__(256) k_cdp_uu(CdpView v) {
     for (int inst = 0; inst < v.ninst; ++inst) {
         const long long pad = (long long)inst * v.per + np0;
         float f[3] = {v.fsol[pad], v.fsol[pad + 1], v.fsol[pad + 2]};
-        const size_t fb = (size_t)inst * v.npe * 8;
+        const size_t fb = (size_t)inst * 24 * v.npe;
 #pragma unroll
         for (int s2 = 0; s2 < 8; ++s2) {
             if (slots[s2] < 0) break;
-            const float* fe = v.feu + (fb + slots[s2]) * 3;
-            f[0] += fe[0]; f[1] += fe[1]; f[2] += fe[2];
+            const float* fe = v.feu + fb + (size_t)(slots[s2] & 7) * 3 * v.npe + (slots[s2] >> 3);
+            f[0] += fe[0]; f[1] += fe[v.npe]; f[2] += fe[2 * (size_t)v.npe];
         }
         const float* c6 = v.uc + ((size_t)inst * v.np + p) * 6;
         const float cc = c6[3], Ku = c6[4], Gu = c6[5];
@@ -811,10 +810,9 @@ __global__ void __launch_bounds__(256) k_cdp_uu(CdpView v) {
             vi[3 + c] = u + 0.5f * du;
             vi[6 + c] = bh + 0.5f * inc;
         }
-        float4* o = reinterpret_cast<float4*>(v.vin + ((size_t)inst * v.np + p) * VIN_ROW);
-        o[0] = make_float4(vi[0], vi[1], vi[2], 0.f);
-        o[1] = make_float4(vi[3], vi[4], vi[5], 0.f);
-        o[2] = make_float4(vi[6], vi[7], vi[8], 0.f);
+        float* o = v.vin + (size_t)inst * VIN_K * v.np + p;
+#pragma unroll
+        for (int k = 0; k < VIN_K; ++k) o[(size_t)k * v.np] = vi[k];
     }
 }
 
@@ -826,7 +824,7 @@ __global__ void __launch_bounds__(256) k_cdp_uu(CdpView v) {
 // abscissa along d, and the shape functions along d sum to one over its two
 // points, so each term is a 2 x 2 x 2 map over the two other axes whose
 // result is the same at both nodes along d.
-__global__ void __launch_bounds__(CDP_THREADS, 2) k_cdp_fs(CdpView v) {
+__global__ void __launch_bounds__(CDP_THREADS, 4) k_cdp_fs(CdpView v) {
     const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (gid >= (long long)v.npe) return;
     const int e = (int)gid;
@@ -839,10 +837,7 @@ __global__ void __launch_bounds__(CDP_THREADS, 2) k_cdp_fs(CdpView v) {
 #pragma unroll 1
     for (int inst = 0; inst < v.ninst; ++inst) {
     const CdpStretch s = cdp_stretch(t, v.eb0[(size_t)inst * v.npe + e]);
-    const float* base = v.vin + (size_t)inst * v.np * VIN_ROW;
-    const float* row[8];
-#pragma unroll
-    for (int l = 0; l < 8; ++l) row[l] = base + (size_t)node[l] * VIN_ROW;
+    const float* base = v.vin + (size_t)inst * VIN_K * v.np;
     float acc[3][3][4];                 // [d][c][m]
 #pragma unroll
     for (int d = 0; d < 3; ++d)
@@ -854,10 +849,9 @@ __global__ void __launch_bounds__(CDP_THREADS, 2) k_cdp_fs(CdpView v) {
     for (int type = 0; type < 3; ++type) {
         float x[8][3];
 #pragma unroll
-        for (int l = 0; l < 8; ++l) {
-            const float4 a = *reinterpret_cast<const float4*>(row[l] + type * 4);
-            x[l][0] = a.x; x[l][1] = a.y; x[l][2] = a.z;
-        }
+        for (int l = 0; l < 8; ++l)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) x[l][c] = base[(size_t)(type * 3 + c) * v.np + node[l]];
 #pragma unroll
         for (int d = 0; d < 3; ++d)
 #pragma unroll
@@ -893,9 +887,9 @@ __global__ void __launch_bounds__(CDP_THREADS, 2) k_cdp_fs(CdpView v) {
     for (int l = 0; l < 8; ++l)
 #pragma unroll
         for (int k = 0; k < 6; ++k) o[cdp_lex_node(l) * 6 + k] = scale * r[l][k];
-    float4* out = reinterpret_cast<float4*>(v.fes + ((size_t)inst * v.npe + e) * 48);
+    float* out = v.fes + (size_t)inst * 48 * v.npe + e;
 #pragma unroll
-    for (int i = 0; i < 12; ++i) out[i] = make_float4(o[4 * i], o[4 * i + 1], o[4 * i + 2], o[4 * i + 3]);
+    for (int i = 0; i < 48; ++i) out[(size_t)i * v.npe] = o[i];
     }
 }
 
@@ -914,7 +908,7 @@ __device__ __forceinline__ void cdp_block(float d, float o, float s, const float
 // dS = Dinv R; S_next = S + dS and Sbar += dt S as pairs; and the next
 // step's displacement-row inputs (sdot = dS/dt, smid = S + dS/2, Sbar).  One
 // thread per PML node, looping over the instances.
-__global__ void __launch_bounds__(256) k_cdp_su(CdpView v) {
+__global__ void __launch_bounds__(256, 4) k_cdp_su(CdpView v) {
     const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (gid >= (long long)v.np) return;
     const int p = (int)gid;
@@ -924,13 +918,13 @@ __global__ void __launch_bounds__(256) k_cdp_su(CdpView v) {
 #pragma unroll 1
     for (int inst = 0; inst < v.ninst; ++inst) {
         float F[6] = {0, 0, 0, 0, 0, 0};
-        const size_t fb = (size_t)inst * v.npe * 8;
+        const size_t fb = (size_t)inst * 48 * v.npe;
 #pragma unroll
         for (int s2 = 0; s2 < 8; ++s2) {
             if (slots[s2] < 0) break;
-            const float2* fe = reinterpret_cast<const float2*>(v.fes + (fb + slots[s2]) * 6);
-            const float2 a = fe[0], b2 = fe[1], c2 = fe[2];
-            F[0] += a.x; F[1] += a.y; F[2] += b2.x; F[3] += b2.y; F[4] += c2.x; F[5] += c2.y;
+            const float* fe = v.fes + fb + (size_t)(slots[s2] & 7) * 6 * v.npe + (slots[s2] >> 3);
+#pragma unroll
+            for (int c = 0; c < 6; ++c) F[c] += fe[(size_t)c * v.npe];
         }
         const size_t b = ((size_t)inst * v.np + p) * 6;
         float sc[6], ds[6], sb[6], ch[6], cl[6];
@@ -967,12 +961,9 @@ __global__ void __launch_bounds__(256) k_cdp_su(CdpView v) {
             nx[6 + c] = sc[c] + 0.5f * dS[c];
             nx[12 + c] = bh + bl;
         }
-        float4* o = reinterpret_cast<float4*>(v.vsu + ((size_t)inst * v.np + p) * VSU_ROW);
+        float* o = v.vsu + (size_t)inst * VSU_K * v.np + p;
 #pragma unroll
-        for (int t = 0; t < 3; ++t) {
-            o[2 * t] = make_float4(nx[6 * t], nx[6 * t + 1], nx[6 * t + 2], nx[6 * t + 3]);
-            o[2 * t + 1] = make_float4(nx[6 * t + 4], nx[6 * t + 5], 0.f, 0.f);
-        }
+        for (int k = 0; k < VSU_K; ++k) o[(size_t)k * v.np] = nx[k];
     }
 }
 
@@ -1032,6 +1023,12 @@ struct svl_cdx {
     double* hist[2] = {nullptr, nullptr};
     int hist_cap = 0;                    // steps per chunk
     cudaStream_t copy_stream = nullptr;
+    // the PML band runs on its own stream: its stress rows and the next step's
+    // element forces overlap the next tensor-core step, which needs only the
+    // band's displacement update (ev_uu).  The band's chain of kernels is the
+    // longer one, so its stream has the higher priority.
+    cudaStream_t bstream = nullptr;
+    cudaEvent_t ev_c = nullptr, ev_uu = nullptr, ev_band = nullptr;
     cudaEvent_t filled[2] = {nullptr, nullptr}, drained[2] = {nullptr, nullptr};
 
     template <typename T>
@@ -1060,6 +1057,10 @@ struct svl_cdx {
             if (drained[i]) cudaEventDestroy(drained[i]);
         }
         if (copy_stream) cudaStreamDestroy(copy_stream);
+        if (bstream) cudaStreamSynchronize(bstream);
+        if (bstream) cudaStreamDestroy(bstream);
+        for (cudaEvent_t e : {ev_c, ev_uu, ev_band})
+            if (e) cudaEventDestroy(e);
         if (stream) cudaStreamDestroy(stream);
     }
 };
@@ -1185,7 +1186,17 @@ int svl_cdx_create(const svl_grid_spec* g, int32_t ninst, const svl_model_desc* 
     h->ntiles = (int)ntiles;
     h->dt = opts->dt;
     h->hgrid = g->h[0];
-    if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) { set_error("cudaStreamCreate failed"); return fail(SVL_ERR_CUDA); }
+    {
+        int lo_pri = 0, hi_pri = 0;
+        if (cudaDeviceGetStreamPriorityRange(&lo_pri, &hi_pri) != cudaSuccess ||
+            cudaStreamCreateWithPriority(&h->stream, cudaStreamNonBlocking, lo_pri) != cudaSuccess ||
+            cudaStreamCreateWithPriority(&h->bstream, cudaStreamNonBlocking, hi_pri) != cudaSuccess ||
+            cudaEventCreateWithFlags(&h->ev_c, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&h->ev_uu, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&h->ev_band, cudaEventDisableTiming) != cudaSuccess) {
+            set_error("cudaStreamCreate failed"); return fail(SVL_ERR_CUDA);
+        }
+    }
     // PML band tables (np = 0 without PML elements)
     std::vector<int32_t> pidx;                       // node -> PML node index or -1
     std::vector<int32_t> t2node;                     // total dof -> node (instance 0 numbering)
@@ -1491,7 +1502,7 @@ int svl_cdx_create(const svl_grid_spec* g, int32_t ninst, const svl_model_desc* 
         if ((st = h->alloc(ns, &h->fsol)) || (st = h->alloc(n6, &h->sh[0])) || (st = h->alloc(n6, &h->sh[1])) ||
             (st = h->alloc(n6, &h->sl[0])) || (st = h->alloc(n6, &h->sl[1])) || (st = h->alloc(n6, &h->sbh)) ||
             (st = h->alloc(n6, &h->sbl)) || (st = h->alloc(n3, &h->ubh)) || (st = h->alloc(n3, &h->ubl)) ||
-            (st = h->alloc((size_t)ninst * h->np * VIN_ROW, &h->vin)) || (st = h->alloc((size_t)ninst * h->np * VSU_ROW, &h->vsu)) ||
+            (st = h->alloc((size_t)ninst * h->np * VIN_K, &h->vin)) || (st = h->alloc((size_t)ninst * h->np * VSU_K, &h->vsu)) ||
             (st = h->alloc((size_t)ninst * h->npe * 24, &h->feu)) || (st = h->alloc((size_t)ninst * h->npe * 48, &h->fes)) ||
             (st = h->upload(uc, &h->uc)) || (st = h->upload(scs, &h->scs)) || (st = h->upload(estr, &h->estr)) ||
             (st = h->upload(eb0, &h->eb0)) || (st = h->upload(enode, &h->enode)) || (st = h->upload(ninv, &h->ninv)) ||
@@ -1555,14 +1566,14 @@ int svl_cdx_set_initial(svl_cdx* h, int32_t inst, const double* U0, const double
         CUDA_TRY(cudaMemsetAsync(h->ubh + (size_t)inst * h->np * 3, 0, (size_t)h->np * 12, h->stream));
         CUDA_TRY(cudaMemsetAsync(h->ubl + (size_t)inst * h->np * 3, 0, (size_t)h->np * 12, h->stream));
         // the first step's displacement-row inputs: sdot, smid, Sbar = 0
-        std::vector<float> vs((size_t)h->np * VSU_ROW, 0.f);
+        std::vector<float> vs((size_t)h->np * VSU_K, 0.f);
         for (size_t k = 0; k < n6; ++k) {
             const size_t p = k / 6, c = k % 6;
             const double sc = (double)shi[k] + slo[k], sp = (double)sphi[k] + splo[k];
-            vs[p * VSU_ROW + c] = (float)((sc - sp) / h->dt);
-            vs[p * VSU_ROW + 8 + c] = (float)((sc + sp) / 2.0);
+            vs[c * h->np + p] = (float)((sc - sp) / h->dt);
+            vs[(6 + c) * h->np + p] = (float)((sc + sp) / 2.0);
         }
-        CUDA_TRY(cudaMemcpyAsync(h->vsu + (size_t)inst * h->np * VSU_ROW, vs.data(), vs.size() * 4, cudaMemcpyHostToDevice,
+        CUDA_TRY(cudaMemcpyAsync(h->vsu + (size_t)inst * h->np * VSU_K, vs.data(), vs.size() * 4, cudaMemcpyHostToDevice,
                                  h->stream));
     }
     CUDA_TRY(cudaStreamSynchronize(h->stream));
@@ -1586,20 +1597,27 @@ static CdpView cdp_view(svl_cdx* h) {
     return c;
 }
 
-// One half of the band's step: 0 = displacement rows (element forces, then
-// the node update), 1 = stress rows.  One thread per PML element, then one per
-// PML node, each looping over the instances (their tables are read once).
-static void cdp_launch(svl_cdx* h, const CdpView& c, int half) {
-    const long long ge = h->npe, gn = h->np;
-    const unsigned be = (unsigned)((ge + CDP_THREADS - 1) / CDP_THREADS), bn = (unsigned)((gn + 255) / 256);
-    if (half == 0) {
-        k_cdp_fu<<<be, CDP_THREADS, 0, h->stream>>>(c);
-        k_cdp_uu<<<bn, 256, 0, h->stream>>>(c);
-    } else {
-        k_cdp_fs<<<be, CDP_THREADS, 0, h->stream>>>(c);
-        k_cdp_su<<<bn, 256, 0, h->stream>>>(c);
+// One kernel of the band's step: 0 = k_cdp_fu, 1 = k_cdp_uu (displacement
+// rows), 2 = k_cdp_fs, 3 = k_cdp_su (stress rows).  One thread per PML element
+// or per PML node, each looping over the instances (their tables are read
+// once).
+static void cdp_launch(svl_cdx* h, const CdpView& c, int which, cudaStream_t st) {
+    const unsigned be = (unsigned)((h->npe + CDP_THREADS - 1) / CDP_THREADS), bn = (unsigned)((h->np + 255) / 256);
+    switch (which) {
+        case 0: k_cdp_fu<<<be, CDP_THREADS, 0, st>>>(c); break;
+        case 1: k_cdp_uu<<<bn, 256, 0, st>>>(c); break;
+        case 2: k_cdp_fs<<<be, CDP_THREADS, 0, st>>>(c); break;
+        default: k_cdp_su<<<bn, 256, 0, st>>>(c); break;
     }
-    h->launches += 2;
+    ++h->launches;
+}
+
+// Makes the compute stream wait for everything the band stream has queued.
+static int cdx_join(svl_cdx* h) {
+    if (h->np == 0) return SVL_OK;
+    CUDA_TRY(cudaEventRecord(h->ev_band, h->bstream));
+    CUDA_TRY(cudaStreamWaitEvent(h->stream, h->ev_band, 0));
+    return SVL_OK;
 }
 
 static int cdx_step(svl_cdx* h, int k, bool want_va) {
@@ -1614,6 +1632,9 @@ static int cdx_step(svl_cdx* h, int k, bool want_va) {
     v.status = h->status;
     v.fsol = h->fsol;
     const size_t ns = (size_t)h->nstate;
+    // u_n at the PML nodes comes from the band's displacement update of the
+    // previous step
+    if (h->np > 0) CUDA_TRY(cudaStreamWaitEvent(h->stream, h->ev_uu, 0));
     if (want_va) {
         CUDA_TRY(cudaMemcpyAsync(h->ph_copy, v.uh_prev, ns * 4, cudaMemcpyDeviceToDevice, h->stream));
         CUDA_TRY(cudaMemcpyAsync(h->pl_copy, v.ul_prev, ns * 4, cudaMemcpyDeviceToDevice, h->stream));
@@ -1622,12 +1643,21 @@ static int cdx_step(svl_cdx* h, int k, bool want_va) {
                                                              h->own_uh[1 - h->cur], h->own_ul[1 - h->cur], h->own_cd, v);
     ++h->launches;
     if (h->np > 0) {
-        // the PML band: coupling forces and updates of the PML nodes
+        // the PML band on its stream: element forces on the displacement rows
+        // (inputs from the previous step's stress update, in stream order), then,
+        // once the tensor-core step has left fsol, the displacement update
+        // (ev_uu), then the stress rows, which overlap the next step
         const CdpView c = cdp_view(h);
-        cdp_launch(h, c, 0);
-        cdp_launch(h, c, 1);
+        CUDA_TRY(cudaEventRecord(h->ev_c, h->stream));
+        cdp_launch(h, c, 0, h->bstream);
+        CUDA_TRY(cudaStreamWaitEvent(h->bstream, h->ev_c, 0));
+        cdp_launch(h, c, 1, h->bstream);
+        CUDA_TRY(cudaEventRecord(h->ev_uu, h->bstream));
+        cdp_launch(h, c, 2, h->bstream);
+        cdp_launch(h, c, 3, h->bstream);
     }
     if (want_va) {
+        if (h->np > 0) CUDA_TRY(cudaStreamWaitEvent(h->stream, h->ev_uu, 0));
         k_cdx_va<<<(unsigned)((ns + 255) / 256), 256, 0, h->stream>>>(v.uh_prev, v.ul_prev, h->uh[h->cur], h->ul[h->cur], h->ph_copy,
                                                                    h->pl_copy, h->V, h->A, (long long)ns,
                                                                    1.0 / 2.0 / h->dt, 1.0 / h->dt / h->dt);
@@ -1654,6 +1684,7 @@ static int cdx_fill_chunk(svl_cdx* h, int k_first, int s0, int n, int nsteps, in
     for (int i = 0; i < n; ++i) {
         const int s = s0 + i;
         TRY(cdx_step(h, k_first + s, s == nsteps - 1));
+        TRY(cdx_join(h));                                                  // S of this step
         k_cdx_hist<<<(unsigned)((per_step + 255) / 256), 256, 0, h->stream>>>(
             h->uh[h->cur], h->ul[h->cur], h->sh[h->cur], h->sl[h->cur], h->d_omap, h->hist[slot] + (size_t)i * per_step,
             h->ntotal, h->nstate / h->ninst, (long long)h->np * 6, h->ninst);
@@ -1669,6 +1700,7 @@ int svl_cdx_run(svl_cdx* h, int32_t k_first, int32_t nsteps, double* U_hist) {
     const int64_t l0 = h->launches;
     if (!U_hist) {
         for (int s = 0; s < nsteps; ++s) TRY(cdx_step(h, k_first + s, s == nsteps - 1));
+        TRY(cdx_join(h));
     } else if (nsteps > 0) {
         // device-side FP64 conversion into two chunk buffers; the copy of chunk
         // c (on copy_stream) overlaps the computation of chunk c + 1
@@ -1725,6 +1757,7 @@ int svl_cdx_run_timed(svl_cdx* h, int32_t k_first, int32_t nsteps, float* ms) {
     const int64_t l0 = h->launches;
     CUDA_TRY(cudaEventRecord(a, h->stream));
     for (int s = 0; s < nsteps; ++s) TRY(cdx_step(h, k_first + s, false));
+    TRY(cdx_join(h));
     CUDA_TRY(cudaEventRecord(b, h->stream));
     CUDA_TRY(cudaEventSynchronize(b));
     CUDA_TRY(cudaEventElapsedTime(ms, a, b));
@@ -1780,9 +1813,8 @@ int svl_cdx_profile(svl_cdx* h, int32_t k_first, int32_t nsteps, double* ms_kern
     cudaEvent_t ev[6];
     for (int i = 0; i < 6; ++i) CUDA_TRY(cudaEventCreate(&ev[i]));
     for (int s2 = 0; s2 < nsteps; ++s2) {
-        // the same launches as cdx_step, with events between the kernel kinds:
-        // 0 fused tensor-core step, 1 PML displacement rows (k_cdp_fu + k_cdp_uu),
-        // 2 PML stress rows (k_cdp_fs + k_cdp_su)
+        // the same launches as cdx_step, with events between the kernels:
+        // 0 fused tensor-core step, 1 k_cdp_fu, 2 k_cdp_uu, 3 k_cdp_fs, 4 k_cdp_su
         CUDA_TRY(cudaEventRecord(ev[0], h->stream));
         const int np = h->np;
         h->np = 0;                                   // tensor-core kernel alone
@@ -1791,19 +1823,15 @@ int svl_cdx_profile(svl_cdx* h, int32_t k_first, int32_t nsteps, double* ms_kern
         if (st) return st;
         h->cur = 1 - h->cur;                         // cdx_step flipped it; the band still belongs to this step
         CUDA_TRY(cudaEventRecord(ev[1], h->stream));
-        if (np > 0) {
-            const CdpView c = cdp_view(h);
-            cdp_launch(h, c, 0);
-            CUDA_TRY(cudaEventRecord(ev[2], h->stream));
-            cdp_launch(h, c, 1);
-        } else {
-            CUDA_TRY(cudaEventRecord(ev[2], h->stream));
+        const CdpView c = cdp_view(h);
+        for (int which = 0; which < 4; ++which) {
+            if (np > 0) cdp_launch(h, c, which, h->stream);
+            CUDA_TRY(cudaEventRecord(ev[2 + which], h->stream));
         }
-        CUDA_TRY(cudaEventRecord(ev[3], h->stream));
         CUDA_TRY(cudaGetLastError());
         h->cur = 1 - h->cur;
-        CUDA_TRY(cudaEventSynchronize(ev[3]));
-        for (int kind = 0; kind < 3; ++kind) {
+        CUDA_TRY(cudaEventSynchronize(ev[5]));
+        for (int kind = 0; kind < 5; ++kind) {
             float t = 0.f;
             CUDA_TRY(cudaEventElapsedTime(&t, ev[kind], ev[kind + 1]));
             ms_kernel[kind] += t;
