@@ -30,9 +30,23 @@ inline void check(int st) {
 class CentralDifference {
 public:
     // CentralDifference(mesh, dt, mtol, ktol, ftol) (CentralDifference.cpp:6-27)
+    // A model with PML2DQuad4 / PML3DHexa8 layers goes to the PML-capable
+    // handle in its explicit mode (the library's staggered explicit PML scheme:
+    // the reference's CentralDifference has no consistent explicit PML, it
+    // never applies G, CentralDifference.cpp:114-120).
     CentralDifference(const svl_model_desc& model, const svl_load_desc& loads, double dt,
                       double mtol = 1e-12, double ftol = 1e-12)
         : ntotal_(model.ntotal) {
+        bool pml = false;
+        for (int e = 0; model.elem_pml && e < model.nelem; ++e) pml = pml || model.elem_pml[e] != 0;
+        if (pml) {
+            svl_xnm_opts x{};
+            x.dt = dt; x.ftol = ftol; x.mtol = mtol; x.tol = 1e-10; x.maxit = 100000;
+            x.algorithm = SVL_ALGO_LINEAR;
+            x.integrator = SVL_XNM_CENTRAL_DIFFERENCE;
+            check(svl_xnm_create(&model, &loads, &x, &x_));
+            return;
+        }
         svl_cd_opts o{};
         o.dt = dt;
         o.mtol = mtol;
@@ -41,19 +55,24 @@ public:
         o.check_every = 1;
         check(svl_cd_create(&model, &loads, &o, &h_));
     }
-    ~CentralDifference() { svl_cd_destroy(h_); }
+    ~CentralDifference() {
+        if (h_) svl_cd_destroy(h_);
+        if (x_) svl_xnm_destroy(x_);
+    }
     CentralDifference(const CentralDifference&) = delete;
     CentralDifference& operator=(const CentralDifference&) = delete;
 
     // Initialize(mesh): initial conditions from the nodes (CentralDifference.cpp:36-71)
     void Initialize(const double* U0 = nullptr, const double* V0 = nullptr, const double* A0 = nullptr) {
-        check(svl_cd_set_initial(h_, U0, V0, A0));
+        check(x_ ? svl_xnm_set_initial(x_, U0, V0, A0, nullptr) : svl_cd_set_initial(h_, U0, V0, A0));
     }
     // ComputeNewStep(mesh, k) -> stop (CentralDifference.cpp:124-151)
-    bool ComputeNewStep(unsigned int k) { return svl_cd_run(h_, (int32_t)k, 1, nullptr) != SVL_OK; }
+    bool ComputeNewStep(unsigned int k) { return ComputeNewSteps(k, 1); }
     // Many steps in one call, optional displacement history [n][ntotal].
     bool ComputeNewSteps(unsigned int k_first, unsigned int n, double* U_hist = nullptr) {
-        return svl_cd_run(h_, (int32_t)k_first, (int32_t)n, U_hist) != SVL_OK;
+        const int st = x_ ? svl_xnm_run(x_, (int32_t)k_first, (int32_t)n, U_hist)
+                          : svl_cd_run(h_, (int32_t)k_first, (int32_t)n, U_hist);
+        return st != SVL_OK;
     }
     std::vector<double> GetDisplacements() const { return get(0); }
     std::vector<double> GetVelocities() const { return get(1); }
@@ -61,6 +80,7 @@ public:
     // ComputeReactionForce(mesh, k) after step k (CentralDifference.cpp:156-171),
     // as DynamicAnalysis::UpdateDomain stores it at the fixed nodes
     std::vector<double> ComputeReactionForce(unsigned int k) const {
+        if (x_) throw Error(SVL_ERR_UNSUPPORTED, "reactions are not covered for PML models");
         std::vector<double> r(ntotal_);
         check(svl_cd_reaction(h_, (int32_t)k, r.data()));
         return r;
@@ -69,10 +89,11 @@ public:
 private:
     std::vector<double> get(int which) const {
         std::vector<double> v(ntotal_);
-        check(svl_cd_get(h_, which, v.data()));
+        check(x_ ? svl_xnm_get(x_, which, v.data()) : svl_cd_get(h_, which, v.data()));
         return v;
     }
     svl_cd* h_ = nullptr;
+    svl_xnm* x_ = nullptr;                 // set instead of h_ for models with PML layers
     int ntotal_ = 0;
 };
 
@@ -114,6 +135,7 @@ public:
         o.pcg_tol = tol;
         o.pcg_maxit = maxit;
         o.precond = SVL_PRECOND_JACOBI;
+        o.single_inner = 1;                // FP32 operator in the inner iterations where the model allows it
         o.algorithm = SVL_ALGO_LINEAR;
         if (newton) {
             o.algorithm = SVL_ALGO_NEWTON;
