@@ -252,6 +252,14 @@ int  svl_cd_get(svl_cd* cd, int32_t which, double* out);
  * entry of -1) of Fint_e + C_e V_e + M_e A_e, minus Fext(k), on the dofs of
  * fixed nodes; zeros elsewhere (Node::GetReaction).  R: [ntotal] host array. */
 int  svl_cd_reaction(svl_cd* cd, int32_t k, double* R);
+/* Element responses after the last step for the ELEMENT recorders
+ * (Recorder.cpp:272-323) of the listed element positions: response 0 =
+ * material strain at each Gauss point (Element::GetStrain: elastic the
+ * engineering strain, J2 the material's strain with tensor shears), 1 =
+ * material total stress at each Gauss point (GetStress), 2 = internal force
+ * (ComputeInternalForces, NC values), 3 = strain rate (GetStrainRate: zeros for
+ * these materials).  out: [nlist][ngp][3 (2D) or 6 (3D)] or [nlist][NC]. */
+int  svl_cd_element_response(svl_cd* cd, int32_t response, int32_t nlist, const int32_t* elems, double* out);
 /* Device pointer of U / V / A (valid until the next svl_cd_run). */
 int  svl_cd_device_ptr(svl_cd* cd, int32_t which, const double** dptr);
 /* Number of kernel launches the last svl_cd_run issued. */
@@ -380,6 +388,8 @@ int  svl_nm_run_timed(svl_nm* nm, int32_t k_first, int32_t nsteps, float* ms);
 int  svl_nm_get(svl_nm* nm, int32_t which, double* out);
 /* NewmarkBeta::ComputeReactionForce after step k (as svl_cd_reaction). */
 int  svl_nm_reaction(svl_nm* nm, int32_t k, double* R);
+/* Element responses after the last step (as svl_cd_element_response). */
+int  svl_nm_element_response(svl_nm* nm, int32_t response, int32_t nlist, const int32_t* elems, double* out);
 /* Conjugate-gradient iterations summed over all solves, of the last solve,
  * and the last solve's true relative residual. */
 int  svl_nm_stats(svl_nm* nm, int64_t* iters_total, int64_t* iters_last, double* rel_residual_last);
@@ -475,6 +485,13 @@ int  svl_xnm_set_initial(svl_xnm* x, const double* U0, const double* V0, const d
 int  svl_xnm_run(svl_xnm* x, int32_t k_first, int32_t nsteps, double* U_hist);
 /* which: 0 U, 1 V, 2 A, 3 Ubar (GetPMLHistoryVector); out [ntotal]. */
 int  svl_xnm_get(svl_xnm* x, int32_t which, double* out);
+/* Reaction forces after step k (as svl_cd_reaction) through ExtendedNewmarkBeta
+ * / NewmarkBeta::ComputeReactionForce (ExtendedNewmarkBeta.cpp:158-172,
+ * NewmarkBeta.cpp:148-162): PML elements with a fixed node add K_e u_e +
+ * C_e v_e + M_e a_e over all their dofs (PML3DHexa8.cpp:746-767, no history
+ * term), so the stress dofs of fixed PML nodes get reactions too.  Not for
+ * the explicit PML scheme (SVL_ERR_UNSUPPORTED).  R: [ntotal] host array. */
+int  svl_xnm_reaction(svl_xnm* x, int32_t k, double* R);
 int  svl_xnm_stats(svl_xnm* x, int64_t* iters_total, int64_t* iters_last, double* res_last);
 /* Newton iterations over all steps, of the last step, and the last step's
  * final convergence-test value (1 iteration per step with Linear). */

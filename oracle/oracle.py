@@ -210,16 +210,44 @@ def cdpml_run(model, loads, dt, nsteps, k_first=1, ftol=1e-12, mtol=1e-12, histo
 
 def reaction_run(model, loads, dt, nsteps, k_first=1, integrator="cd", algo=0, maxit=50, cnvgtol=1e-6):
     """Reaction forces (total dofs; zeros off the fixed nodes) after nsteps of
-    central difference or NewmarkBeta (algo as newmark_run)."""
+    central difference ("cd"), NewmarkBeta ("newmark"), ExtendedNewmarkBeta
+    ("xnewmark") or the PML model's NewmarkBeta mode ("xnewmark_nm"); algo as
+    newmark_run."""
     md = model.desc()
     ld = loads.desc() if loads is not None else None
     R = np.zeros(model.ntotal)
     st = lib().oracle_reaction_run(C.addressof(md), C.addressof(ld) if ld is not None else None, dt, k_first, nsteps,
-                                   0 if integrator == "cd" else 1, algo, maxit, cnvgtol,
+                                   {"cd": 0, "newmark": 1, "xnewmark": 2, "xnewmark_nm": 3}.get(integrator, 1),
+                                   algo, maxit, cnvgtol,
                                    R.ctypes.data_as(C.POINTER(C.c_double)))
     if st != 0:
         raise RuntimeError("oracle_reaction_run failed with status %d" % st)
     return R
+
+
+def element_response_run(model, loads, dt, nsteps, response, elems, k_first=1, integrator="cd", algo=0, maxit=50,
+                         cnvgtol=1e-6):
+    """ELEMENT recorder values (STRAIN, STRESS, INTERNALFORCE, STRAINRATE) of
+    the element positions `elems` after nsteps of central difference or
+    NewmarkBeta; [n, ngp, 3|6] or [n, NC]."""
+    code = {"STRAIN": 0, "STRESS": 1, "INTERNALFORCE": 2, "STRAINRATE": 3}[response.upper()]
+    md = model.desc()
+    ld = loads.desc() if loads is not None else None
+    el = np.ascontiguousarray(np.asarray(elems, dtype=np.int32).ravel())
+    nen = model.conn.shape[1]
+    ngp = 4 if model.ndim == 2 else 8
+    shape = (el.size, nen * model.ndim) if code == 2 else (el.size, ngp, 3 if model.ndim == 2 else 6)
+    out = np.zeros(shape)
+    L = lib()
+    L.oracle_element_response_run.argtypes = [C.c_void_p, C.c_void_p, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int,
+                                              C.c_int, C.c_double, C.c_int, C.c_int, C.POINTER(C.c_int),
+                                              C.POINTER(C.c_double)]
+    st = L.oracle_element_response_run(C.addressof(md), C.addressof(ld) if ld is not None else None, dt, k_first,
+                                       nsteps, 0 if integrator == "cd" else 1, algo, maxit, cnvgtol, code, int(el.size),
+                                       el.ctypes.data_as(C.POINTER(C.c_int)), out.ctypes.data_as(C.POINTER(C.c_double)))
+    if st != 0:
+        raise RuntimeError("oracle_element_response_run failed with status %d" % st)
+    return out
 
 
 def xnewmark_matrices(model):

@@ -548,6 +548,24 @@ struct Sim {
             add_BTsig(m.ndim, m.nen, dNx, sig, c, fe);
         }
     }
+    // ELEMENT recorder values of element e (Recorder.cpp:272-323): 0 strain and
+    // 1 total stress per Gauss point (Material::GetStrain / GetTotalStress:
+    // elastic the engineering strain and C eps; J2 the material strain with
+    // tensor shears, 2D components 1 2 4, PlasticPlaneStrainJ2.cpp:114-147),
+    // 2 the internal force, 3 the strain rate (zeros for these materials).
+    void element_response(int e, int response, double* out) const {
+        const int ns = m.ndim == 2 ? 3 : 6;
+        if (response == 2) { element_fint(e, out); return; }
+        for (int q = 0; q < m.ngp; ++q) {
+            const MatState& st = gp[(size_t)e * m.ngp + q];
+            double* o = out + (size_t)q * ns;
+            const int t = mt(e);
+            if (response == 3) { for (int c = 0; c < ns; ++c) o[c] = 0.0; continue; }
+            if (response == 1) { mat_stress(st, t, mp(e), o); continue; }
+            if (t == SVL_MAT_PLASTICPLANESTRAINJ2) { o[0] = st.strain[1]; o[1] = st.strain[2]; o[2] = st.strain[4]; }
+            else for (int c = 0; c < ns; ++c) o[c] = st.strain[c];
+        }
+    }
     // Element::UpdateState with strain B (U + dU) (lin2DQuad4.cpp:87-107, 618-633).
     void element_update(int e, const std::vector<double>& Ustrain) {
         const int nc = m.nen * m.ndof;
@@ -1543,6 +1561,76 @@ struct XNewmark {
         if (!newmark) add(Gt, dt / 3.0);
         csr_from_triplets(s.m.ntotal, tr, Kt_eff);
     }
+    // Reaction forces after step k (DynamicAnalysis::UpdateDomain,
+    // DynamicAnalysis.cpp:128-150) through ExtendedNewmarkBeta /
+    // NewmarkBeta::ComputeReactionForce (ExtendedNewmarkBeta.cpp:158-172,
+    // NewmarkBeta.cpp:148-162): Fint_dyn - Fext(k) - Fbar (Fbar = 0), Fint_dyn
+    // the node inertia m A (Assembler.cpp:569-592) and then, in element order,
+    // the dynamic force of every element with a fixed node: solids Fint_e +
+    // C_e V_e + M_e A_e (lin3DHexa8 / lin2DQuad4 ComputeInternalDynamicForces),
+    // PML elements K_e u_e + C_e v_e + M_e a_e over all their dofs
+    // (PML3DHexa8.cpp:746-767, PML2DQuad4: no history term), dashpots
+    // eta a a^T V; reported on the dofs of fixed nodes (a node with a free-dof
+    // entry of -1), zeros elsewhere.
+    void reaction(int k, std::vector<double>& R) const {
+        const Model& m = s.m;
+        const int nt = m.ntotal, nen = m.nen;
+        std::vector<char> fixed(m.nnode, 0), dof_fixed(nt, 0);
+        for (int n = 0; n < m.nnode; ++n) {
+            for (int j = 0; j < m.nndof[n]; ++j) if (m.fdof_all[(size_t)n * m.dstride + j] == -1) fixed[n] = 1;
+            if (fixed[n]) for (int j = 0; j < m.nndof[n]; ++j) dof_fixed[m.tdof_all[(size_t)n * m.dstride + j]] = 1;
+        }
+        std::vector<double> F(nt, 0.0);
+        if (!m.nodemass.empty()) for (int t = 0; t < nt; ++t) F[t] += m.nodemass[t] * A[t];
+        std::vector<double> fe(72), Me(72 * 72), Ce(72 * 72), Ke(72 * 72), K0(72 * 72);
+        for (int e = 0; e < m.nelem; ++e) {
+            bool hf = false;
+            for (int a = 0; a < nen; ++a) hf = hf || fixed[m.conn[(size_t)e * nen + a]];
+            if (!hf) continue;
+            const std::vector<int>& ed = edof[e];
+            const int nc = (int)ed.size();
+            if (pml(e)) {
+                pml_elem(e, Me.data(), Ce.data(), Ke.data(), nullptr);
+                for (int i = 0; i < nc; ++i) {
+                    double ku = 0.0, cv = 0.0, ma = 0.0;
+                    for (int j = 0; j < nc; ++j) {
+                        ku += Ke[(size_t)i * nc + j] * U[ed[j]];
+                        cv += Ce[(size_t)i * nc + j] * V[ed[j]];
+                        ma += Me[(size_t)i * nc + j] * A[ed[j]];
+                    }
+                    F[ed[i]] += (ku + cv) + ma;
+                }
+                continue;
+            }
+            s.element_fint(e, fe.data());
+            s.element_M(e, Me.data(), m.lumped != 0);
+            const double am = m.ray.empty() ? 0.0 : m.ray[2 * e], ak = m.ray.empty() ? 0.0 : m.ray[2 * e + 1];
+            if (ak != 0.0) s.element_K0(e, K0.data());
+            for (int i = 0; i < nc; ++i) {
+                double cv = 0.0, ma = 0.0;
+                for (int j = 0; j < nc; ++j) {
+                    const double c = am * Me[(size_t)i * nc + j] + (ak != 0.0 ? ak * K0[(size_t)i * nc + j] : 0.0);
+                    cv += c * V[ed[j]];
+                    ma += Me[(size_t)i * nc + j] * A[ed[j]];
+                }
+                F[ed[i]] += (fe[i] + cv) + ma;
+            }
+        }
+        std::vector<int> node_of(nt, -1);
+        for (int n = 0; n < m.nnode; ++n)
+            for (int j = 0; j < m.nndof[n]; ++j) node_of[m.tdof_all[(size_t)n * m.dstride + j]] = n;
+        for (size_t i = 0; i < m.dp_eta.size(); ++i) {
+            const int a = m.dp_dof[2 * i], b = m.dp_dof[2 * i + 1];
+            if (!fixed[node_of[a]] && !fixed[node_of[b]]) continue;
+            const double eta = m.dp_eta[i];
+            F[a] += eta * (V[a] - V[b]);
+            F[b] += eta * (V[b] - V[a]);
+        }
+        std::vector<double> Fx;
+        s.fext(k, Fx);
+        R.assign(nt, 0.0);
+        for (int t = 0; t < nt; ++t) if (dof_fixed[t]) R[t] = F[t] - Fx[t];
+    }
     // One ExtendedNewmarkBeta::ComputeNewStep with Linear (algo 0) or
     // NewtonRaphson (algo 1: test 5, algo 2: test 4).  Every iteration
     // re-evaluates ComputeEffectiveForce (:208-229, which has no increment
@@ -2141,13 +2229,24 @@ int oracle_xnewmark_run(const svl_model_desc* model, const svl_load_desc* loads,
 }
 
 /* Reaction forces after `nsteps` steps from k_first of the central-difference
- * (integrator 0) or NewmarkBeta (1, algo/maxit/cnvgtol as oracle_newmark_run)
- * run; R_out [ntotal]. */
+ * (integrator 0), NewmarkBeta (1, algo/maxit/cnvgtol as oracle_newmark_run),
+ * ExtendedNewmarkBeta (2) or the NewmarkBeta mode of the PML model's
+ * integrator (3) run; R_out [ntotal]. */
 int oracle_reaction_run(const svl_model_desc* model, const svl_load_desc* loads, double dt, int k_first, int nsteps,
                         int integrator, int algo, int maxit, double cnvgtol, double* R_out) {
     std::vector<double> R;
     const int klast = k_first + nsteps - 1;
-    if (integrator == 0) {
+    if (integrator >= 2) {
+        XNewmark x;
+        x.newmark = integrator == 3;
+        if (!x.init(model, loads, dt)) return SVL_ERR_INVALID;
+        x.set_initial(nullptr, nullptr, nullptr, nullptr);
+        for (int i = 0; i < nsteps; ++i) {
+            int st = x.step(k_first + i, algo, algo == 0 ? 1 : maxit, cnvgtol);
+            if (st) return st;
+        }
+        x.reaction(klast, R);
+    } else if (integrator == 0) {
         CD cd;
         if (!cd.init(model, loads, dt, 1e-12, 1e-12)) return SVL_ERR_INVALID;
         cd.set_initial(nullptr, nullptr, nullptr);
@@ -2163,6 +2262,35 @@ int oracle_reaction_run(const svl_model_desc* model, const svl_load_desc* loads,
         nm.s.reaction(klast, nm.V, nm.A, R);
     }
     std::memcpy(R_out, R.data(), sizeof(double) * R.size());
+    return 0;
+}
+
+/* ELEMENT recorder values (Sim::element_response) of the listed elements
+ * after `nsteps` steps of central difference (integrator 0) or NewmarkBeta
+ * (1, algo/maxit/cnvgtol as oracle_newmark_run); out [nlist][ngp*3|6] or
+ * [nlist][NC]. */
+int oracle_element_response_run(const svl_model_desc* model, const svl_load_desc* loads, double dt, int k_first,
+                                 int nsteps, int integrator, int algo, int maxit, double cnvgtol, int response,
+                                 int nlist, const int* elems, double* out) {
+    auto emit = [&](const Sim& s) {
+        const int per = response == 2 ? s.m.nen * s.m.ndof : s.m.ngp * (s.m.ndim == 2 ? 3 : 6);
+        for (int i = 0; i < nlist; ++i) s.element_response(elems[i], response, out + (size_t)i * per);
+    };
+    if (integrator == 0) {
+        CD cd;
+        if (!cd.init(model, loads, dt, 1e-12, 1e-12)) return SVL_ERR_INVALID;
+        cd.set_initial(nullptr, nullptr, nullptr);
+        for (int i = 0; i < nsteps; ++i) cd.step(k_first + i);
+        emit(cd.s);
+    } else {
+        Newmark nm;
+        if (!nm.init(model, loads, dt)) return SVL_ERR_INVALID;
+        for (int i = 0; i < nsteps; ++i) {
+            int st = nm.step(k_first + i, algo, algo == 0 ? 1 : maxit, cnvgtol);
+            if (st) return st;
+        }
+        emit(nm.s);
+    }
     return 0;
 }
 

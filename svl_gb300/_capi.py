@@ -177,6 +177,9 @@ def lib():
     L.svl_xnm_set_initial.argtypes = [C.c_void_p, f64p, f64p, f64p, f64p]
     L.svl_xnm_run.argtypes = [C.c_void_p, C.c_int32, C.c_int32, f64p]
     L.svl_xnm_get.argtypes = [C.c_void_p, C.c_int32, f64p]
+    L.svl_xnm_reaction.argtypes = [C.c_void_p, C.c_int32, f64p]
+    L.svl_cd_element_response.argtypes = [C.c_void_p, C.c_int32, C.c_int32, i32p, f64p]
+    L.svl_nm_element_response.argtypes = [C.c_void_p, C.c_int32, C.c_int32, i32p, f64p]
     L.svl_xnm_stats.argtypes = [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_double)]
     L.svl_xnm_newton_stats.argtypes = [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_double)]
     L.svl_xnm_destroy.argtypes = [C.c_void_p]

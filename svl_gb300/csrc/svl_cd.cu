@@ -338,11 +338,75 @@ __global__ void __launch_bounds__(128) k_element_tan(DevView d, const double* __
 // updates the states at the start of the next step); 0: their stress follows
 // from the updated state, K tr(eps) 1 + 2G (dev eps - eps_p) (the Newmark path
 // updated them in place).  C_e = am_e M_e + ak_e K0_e with a lumped M_e.
+// Gauss point q of element e with element displacement ue: shape
+// derivatives b and weight w, engineering strain ev (element order: 2D xx yy
+// xy, 3D xx yy zz xy yz zx), the J2 material strain Ev ([0 exx eyy 0 gxy/2 0]
+// in 2D, PlasticPlaneStrainJ2.cpp:236; half shears in 3D, Plastic3DJ2.cpp:215)
+// and the stress sig in the element order (J2 2D: material indices 1 2 4).
+// J2 stress: map_state = 1 maps the strain on a copy of the committed state
+// (explicit path: the states are updated at the start of the next step),
+// 0 reads the state of the last update.
+template <int ND, int NEN>
+__device__ __forceinline__ void gp_state(const DevView& d, int e, int q, int ngp, const double* ue, int map_state,
+                                         double (&b)[NEN][3], double& w, double ev[6], double Ev[6], double sig[6]) {
+    constexpr int PER = NEN * ND + 1;
+    const int E = d.nelem;
+    const double* g = d.geo + ((size_t)d.egeo[e] * ngp + q) * PER;
+#pragma unroll
+    for (int a = 0; a < NEN; ++a)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) b[a][j] = (j < ND) ? g[a * ND + j] : 0.0;
+    w = g[PER - 1];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) { ev[i] = 0.0; sig[i] = 0.0; }
+#pragma unroll
+    for (int a = 0; a < NEN; ++a) {
+        if (ND == 2) {
+            ev[0] += b[a][0] * ue[2 * a]; ev[1] += b[a][1] * ue[2 * a + 1];
+            ev[2] += b[a][1] * ue[2 * a] + b[a][0] * ue[2 * a + 1];
+        } else {
+            const double* u = ue + 3 * a;
+            ev[0] += b[a][0] * u[0]; ev[1] += b[a][1] * u[1]; ev[2] += b[a][2] * u[2];
+            ev[3] += b[a][1] * u[0] + b[a][0] * u[1]; ev[4] += b[a][2] * u[1] + b[a][1] * u[2];
+            ev[5] += b[a][2] * u[0] + b[a][0] * u[2];
+        }
+    }
+    if (ND == 2) { Ev[0] = 0.0; Ev[1] = ev[0]; Ev[2] = ev[1]; Ev[3] = 0.0; Ev[4] = 0.5 * ev[2]; Ev[5] = 0.0; }
+    else { Ev[0] = ev[0]; Ev[1] = ev[1]; Ev[2] = ev[2]; Ev[3] = 0.5 * ev[3]; Ev[4] = 0.5 * ev[4]; Ev[5] = 0.5 * ev[5]; }
+    const double c1 = d.ecoef[e], c2 = d.ecoef[(size_t)E + e], c3 = d.ecoef[2 * (size_t)E + e];
+    if (d.ekind[e] == kMatElastic) {
+        if (ND == 2) { sig[0] = c1 * ev[0] + c2 * ev[1]; sig[1] = c2 * ev[0] + c1 * ev[1]; sig[2] = c3 * ev[2]; }
+        else {
+            sig[0] = c1 * ev[0] + c2 * ev[1] + c2 * ev[2];
+            sig[1] = c2 * ev[0] + c1 * ev[1] + c2 * ev[2];
+            sig[2] = c2 * ev[0] + c2 * ev[1] + c1 * ev[2];
+            sig[3] = c3 * ev[3]; sig[4] = c3 * ev[4]; sig[5] = c3 * ev[5];
+        }
+        return;
+    }
+    double st[kJ2State];
+    const double* gs = d.gstate + (size_t)q * E + e;
+#pragma unroll
+    for (int k2 = 0; k2 < kJ2State; ++k2) st[k2] = gs[(size_t)k2 * ngp * E];
+    const double K = c1, G = c2;
+    double s6[6];
+    if (map_state) {
+        j2_return<ND>(Ev, st, K, G, c3, d.ecoef[3 * (size_t)E + e], d.ecoef[4 * (size_t)E + e], s6);
+    } else {
+        const double tr = Ev[0] + Ev[1] + Ev[2];
+#pragma unroll
+        for (int k2 = 0; k2 < 6; ++k2)
+            s6[k2] = (k2 < 3 ? K * tr : 0.0) + 2.0 * G * (Ev[k2] - (k2 < 3 ? 1.0 / 3.0 * tr : 0.0) - st[k2]);
+    }
+    if (ND == 2) { sig[0] = s6[1]; sig[1] = s6[2]; sig[2] = s6[4]; }
+    else for (int k2 = 0; k2 < 6; ++k2) sig[k2] = s6[k2];
+}
+
 template <int ND, int NEN>
 __global__ void __launch_bounds__(128) k_react_elem(DevView d, const int32_t* __restrict__ list, int nlist,
                                                     const double* __restrict__ rm, const double* __restrict__ ram,
                                                     int ngp, int map_state, double* __restrict__ out) {
-    constexpr int NC = ND * NEN, PER = NEN * ND + 1;
+    constexpr int NC = ND * NEN;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nlist) return;
     const int E = d.nelem, e = list[i];
@@ -352,66 +416,22 @@ __global__ void __launch_bounds__(128) k_react_elem(DevView d, const int32_t* __
         const int t = d.edof[(size_t)j * E + e];
         ue[j] = d.Us[t]; ve[j] = d.V[t]; fi[j] = 0.0; cv[j] = 0.0;
     }
-    const int kind = d.ekind[e];
-    const double c1 = d.ecoef[e], c2 = d.ecoef[(size_t)E + e], c3 = d.ecoef[2 * (size_t)E + e];
-    const double* g0 = d.geo + (size_t)d.egeo[e] * ngp * PER;
     for (int q = 0; q < ngp; ++q) {
-        const double* g = g0 + q * PER;
-        double b[NEN][3];
-#pragma unroll
-        for (int a = 0; a < NEN; ++a)
-#pragma unroll
-            for (int j = 0; j < 3; ++j) b[a][j] = (j < ND) ? g[a * ND + j] : 0.0;
-        const double w = g[PER - 1];
-        // strain (engineering shear) of U_s and of V
-        double ev[6] = {0, 0, 0, 0, 0, 0}, vv[6] = {0, 0, 0, 0, 0, 0};
+        double b[NEN][3], w, ev[6], Ev[6], sig[6];
+        gp_state<ND, NEN>(d, e, q, ngp, ue, map_state, b, w, ev, Ev, sig);
+        // engineering strain rate of V (the stiffness-proportional damping)
+        double vv[6] = {0, 0, 0, 0, 0, 0};
 #pragma unroll
         for (int a = 0; a < NEN; ++a) {
             if (ND == 2) {
-                ev[0] += b[a][0] * ue[2 * a]; ev[1] += b[a][1] * ue[2 * a + 1];
-                ev[2] += b[a][1] * ue[2 * a] + b[a][0] * ue[2 * a + 1];
                 vv[0] += b[a][0] * ve[2 * a]; vv[1] += b[a][1] * ve[2 * a + 1];
                 vv[2] += b[a][1] * ve[2 * a] + b[a][0] * ve[2 * a + 1];
             } else {
-                const double* u = ue + 3 * a;
                 const double* v = ve + 3 * a;
-                ev[0] += b[a][0] * u[0]; ev[1] += b[a][1] * u[1]; ev[2] += b[a][2] * u[2];
-                ev[3] += b[a][1] * u[0] + b[a][0] * u[1]; ev[4] += b[a][2] * u[1] + b[a][1] * u[2];
-                ev[5] += b[a][2] * u[0] + b[a][0] * u[2];
                 vv[0] += b[a][0] * v[0]; vv[1] += b[a][1] * v[1]; vv[2] += b[a][2] * v[2];
                 vv[3] += b[a][1] * v[0] + b[a][0] * v[1]; vv[4] += b[a][2] * v[1] + b[a][1] * v[2];
                 vv[5] += b[a][2] * v[0] + b[a][0] * v[2];
             }
-        }
-        double sig[6] = {0, 0, 0, 0, 0, 0};
-        if (kind == kMatElastic) {
-            if (ND == 2) { sig[0] = c1 * ev[0] + c2 * ev[1]; sig[1] = c2 * ev[0] + c1 * ev[1]; sig[2] = c3 * ev[2]; }
-            else {
-                sig[0] = c1 * ev[0] + c2 * ev[1] + c2 * ev[2];
-                sig[1] = c2 * ev[0] + c1 * ev[1] + c2 * ev[2];
-                sig[2] = c2 * ev[0] + c2 * ev[1] + c1 * ev[2];
-                sig[3] = c3 * ev[3]; sig[4] = c3 * ev[4]; sig[5] = c3 * ev[5];
-            }
-        } else {
-            double st[kJ2State];
-            const double* gs = d.gstate + (size_t)q * E + e;
-#pragma unroll
-            for (int k2 = 0; k2 < kJ2State; ++k2) st[k2] = gs[(size_t)k2 * ngp * E];
-            double Ev[6];
-            if (ND == 2) { Ev[0] = 0.0; Ev[1] = ev[0]; Ev[2] = ev[1]; Ev[3] = 0.0; Ev[4] = 0.5 * ev[2]; Ev[5] = 0.0; }
-            else { Ev[0] = ev[0]; Ev[1] = ev[1]; Ev[2] = ev[2]; Ev[3] = 0.5 * ev[3]; Ev[4] = 0.5 * ev[4]; Ev[5] = 0.5 * ev[5]; }
-            const double K = c1, G = c2;
-            double s6[6];
-            if (map_state) {
-                j2_return<ND>(Ev, st, K, G, c3, d.ecoef[3 * (size_t)E + e], d.ecoef[4 * (size_t)E + e], s6);
-            } else {
-                const double tr = Ev[0] + Ev[1] + Ev[2];
-#pragma unroll
-                for (int k2 = 0; k2 < 6; ++k2)
-                    s6[k2] = (k2 < 3 ? K * tr : 0.0) + 2.0 * G * (Ev[k2] - (k2 < 3 ? 1.0 / 3.0 * tr : 0.0) - st[k2]);
-            }
-            if (ND == 2) { sig[0] = s6[1]; sig[1] = s6[2]; sig[2] = s6[4]; }
-            else for (int k2 = 0; k2 < 6; ++k2) sig[k2] = s6[k2];
         }
         double sk[6] = {0, 0, 0, 0, 0, 0};
         if (d.dk0) {
@@ -450,6 +470,56 @@ __global__ void __launch_bounds__(128) k_react_elem(DevView d, const int32_t* __
         const double c = ram[(size_t)i * NEN + a] * ve[j] + cv[j];
         o[j] = (fi[j] + c) + rm[(size_t)i * NEN + a] * d.A[t];
     }
+}
+
+// Element responses of the listed elements for the ELEMENT recorders
+// (Recorder.cpp:272-323): 0 = material strain per Gauss point (elastic: the
+// engineering strain, Elastic2DPlaneStrain / Elastic3DLinear::GetStrain; J2:
+// the material's strain, tensor shears, PlasticPlaneStrainJ2.cpp:114-119),
+// 1 = material total stress per Gauss point (GetTotalStress), 2 = internal
+// force w t |J| B^T sig (lin2DQuad4.cpp:383-412, unfiltered), 3 = strain rate
+// (zero for these materials, Elastic2DPlaneStrain.cpp:103-109).  out: [nlist]
+// [ngp * ncomp] (0, 1, 3) or [nlist][NC] (2).
+template <int ND, int NEN>
+__global__ void __launch_bounds__(128) k_elem_response(DevView d, const int32_t* __restrict__ list, int nlist,
+                                                       int ngp, int map_state, int response, double* __restrict__ out) {
+    constexpr int NC = ND * NEN, NS = ND == 2 ? 3 : 6;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nlist) return;
+    const int E = d.nelem, e = list[i];
+    double ue[NC], fi[NC];
+#pragma unroll
+    for (int j = 0; j < NC; ++j) { ue[j] = d.Us[d.edof[(size_t)j * E + e]]; fi[j] = 0.0; }
+    const bool j2 = d.ekind[e] != kMatElastic;
+    for (int q = 0; q < ngp; ++q) {
+        double b[NEN][3], w, ev[6], Ev[6], sig[6];
+        gp_state<ND, NEN>(d, e, q, ngp, ue, map_state, b, w, ev, Ev, sig);
+        double* o = out + ((size_t)i * ngp + q) * NS;
+        if (response == 0) {
+            if (!j2) for (int c = 0; c < NS; ++c) o[c] = ev[c];
+            else if (ND == 2) { o[0] = Ev[1]; o[1] = Ev[2]; o[2] = Ev[4]; }
+            else for (int c = 0; c < 6; ++c) o[c] = Ev[c];
+        } else if (response == 1) {
+            for (int c = 0; c < NS; ++c) o[c] = sig[c];
+        } else if (response == 3) {
+            for (int c = 0; c < NS; ++c) o[c] = 0.0;
+        } else {
+#pragma unroll
+            for (int a = 0; a < NEN; ++a) {
+                if (ND == 2) {
+                    fi[2 * a] += w * (b[a][0] * sig[0] + b[a][1] * sig[2]);
+                    fi[2 * a + 1] += w * (b[a][1] * sig[1] + b[a][0] * sig[2]);
+                } else {
+                    const double bx = b[a][0], by = b[a][1], bz = b[a][2];
+                    fi[3 * a] += w * (bx * sig[0] + by * sig[3] + bz * sig[5]);
+                    fi[3 * a + 1] += w * (by * sig[1] + bx * sig[3] + bz * sig[4]);
+                    fi[3 * a + 2] += w * (bz * sig[2] + by * sig[4] + bx * sig[5]);
+                }
+            }
+        }
+    }
+    if (response == 2)
+        for (int j = 0; j < NC; ++j) out[(size_t)i * NC + j] = fi[j];
 }
 
 // R_t = (m_t A_t + sum of the listed elements' entries of t in element order
@@ -756,6 +826,10 @@ struct svl_cd {
     const int32_t *r_dptr = nullptr, *r_dcol = nullptr;
     const double *r_m = nullptr, *r_am = nullptr, *r_nm = nullptr, *r_deta = nullptr;
     double *r_out = nullptr, *r_R = nullptr;
+    // element-response scratch (ELEMENT recorders), grown on demand
+    int32_t* er_list = nullptr;
+    double* er_out = nullptr;
+    int er_cap = 0;
 
     template <typename T>
     int upload(const std::vector<T>& h, const T** out) {
@@ -1440,6 +1514,38 @@ extern "C" {
 int svl_cd_reaction(svl_cd* cd, int32_t k, double* R) {
     if (!cd || !R) { set_error("NULL argument"); return SVL_ERR_INVALID; }
     return cd_reaction(cd, k, 1, R);
+}
+
+// Element responses after the last step (see k_elem_response); map_state as
+// in cd_reaction.
+static int cd_element_response(svl_cd* cd, int map_state, int32_t response, int32_t nlist, const int32_t* elems,
+                               double* out) {
+    const HostModel& m = cd->m;
+    if (response < 0 || response > 3 || nlist < 0 || (nlist > 0 && (!elems || !out))) {
+        set_error("bad argument"); return SVL_ERR_INVALID;
+    }
+    for (int i = 0; i < nlist; ++i)
+        if (elems[i] < 0 || elems[i] >= m.nelem) { set_error("element %d out of range", elems[i]); return SVL_ERR_INVALID; }
+    if (nlist == 0) return SVL_OK;
+    const int nd = m.ndim, nen = m.nen, per = response == 2 ? nen * nd : m.ngp * (nd == 2 ? 3 : 6);
+    if (cd->er_cap < nlist) {
+        TRY(cd->zeros((size_t)nlist, &cd->er_list));
+        TRY(cd->zeros((size_t)nlist * 48, &cd->er_out));
+        cd->er_cap = nlist;
+    }
+    CUDA_TRY(cudaMemcpyAsync(cd->er_list, elems, sizeof(int32_t) * nlist, cudaMemcpyHostToDevice, cd->stream));
+    const int g = (nlist + 127) / 128;
+    if (nd == 2) k_elem_response<2, 4><<<g, 128, 0, cd->stream>>>(cd->d, cd->er_list, nlist, m.ngp, map_state, response, cd->er_out);
+    else k_elem_response<3, 8><<<g, 128, 0, cd->stream>>>(cd->d, cd->er_list, nlist, m.ngp, map_state, response, cd->er_out);
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaMemcpyAsync(out, cd->er_out, sizeof(double) * (size_t)nlist * per, cudaMemcpyDeviceToHost, cd->stream));
+    CUDA_TRY(cudaStreamSynchronize(cd->stream));
+    return SVL_OK;
+}
+
+int svl_cd_element_response(svl_cd* cd, int32_t response, int32_t nlist, const int32_t* elems, double* out) {
+    if (!cd) { set_error("NULL handle"); return SVL_ERR_INVALID; }
+    return cd_element_response(cd, 1, response, nlist, elems, out);
 }
 
 int svl_cd_get(svl_cd* cd, int32_t which, double* out) {
@@ -3052,6 +3158,11 @@ int svl_nm_reaction(svl_nm* nm, int32_t k, double* R) {
     if (!nm || !R) { set_error("NULL argument"); return SVL_ERR_INVALID; }
     if (nm->consistent) { set_error("reaction forces are covered with a lumped mass"); return SVL_ERR_UNSUPPORTED; }
     return cd_reaction(nm->cd, k, 0, R);
+}
+
+int svl_nm_element_response(svl_nm* nm, int32_t response, int32_t nlist, const int32_t* elems, double* out) {
+    if (!nm) { set_error("NULL handle"); return SVL_ERR_INVALID; }
+    return cd_element_response(nm->cd, 0, response, nlist, elems, out);
 }
 
 int svl_nm_stats(svl_nm* nm, int64_t* iters_total, int64_t* iters_last, double* rel_residual_last) {

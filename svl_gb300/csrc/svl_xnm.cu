@@ -810,6 +810,11 @@ __global__ void k_xsub(int n, const double* a, const double* b, double* out) {
     if (i < n) out[i] = a[i] - b[i];
 }
 // MINRES direction and iterate: w = (v - oldeps w1 - delta w2) / gamma; x += phi w
+// R_t = -y_t on the dofs of fixed nodes, 0 elsewhere (Node::GetReaction)
+__global__ void k_xreact(int n, const int8_t* __restrict__ fixed, const double* __restrict__ y, double* __restrict__ R) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) R[t] = fixed[t] ? -y[t] : 0.0;
+}
 __global__ void k_xmr_w(int n, const double* v, const double* w1, const double* w2, double* w, double* x,
                         double oldeps, double delta, double inv_gamma, double phi) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1018,6 +1023,7 @@ struct svl_xnm {
     double *w = nullptr, *w1 = nullptr, *w2 = nullptr, *dinv = nullptr, *tmp = nullptr;
     double *partial = nullptr, *scal = nullptr;
     int* bad = nullptr;
+    int8_t* fixed_dof = nullptr;             // [ntotal] 1 on the dofs of fixed nodes (reactions), built on first use
     int64_t iters_total = 0, iters_last = 0;
     double res_last = 0.0;
     int64_t newton_total = 0, newton_last = 0;
@@ -1823,6 +1829,55 @@ int svl_xnm_get(svl_xnm* X, int32_t which, double* out) {
     if (!X || !out || which < 0 || which > 3) { set_error("bad argument"); return SVL_ERR_INVALID; }
     const double* src[4] = {X->U, X->V, X->A, X->Ub};
     XCUDA(cudaMemcpyAsync(out, src[which], sizeof(double) * X->m.ntotal, cudaMemcpyDeviceToHost, X->stream));
+    XCUDA(cudaStreamSynchronize(X->stream));
+    return SVL_OK;
+}
+
+// Reaction forces after step k (the step just run), as DynamicAnalysis::
+// UpdateDomain stores them (DynamicAnalysis.cpp:128-150) through
+// ExtendedNewmarkBeta / NewmarkBeta::ComputeReactionForce
+// (ExtendedNewmarkBeta.cpp:158-172, NewmarkBeta.cpp:148-162): the dynamic
+// internal force (node inertia m A; solids Fint_e + C_e V_e + M_e A_e; PML
+// elements K_e u_e + C_e v_e + M_e a_e, PML3DHexa8.cpp:746-767, without the
+// history term; dashpots) minus Fext(k), on the dofs of fixed nodes.  Every
+// element touching such a dof has that fixed node, so all elements are
+// evaluated and the other rows dropped: the element order of each row's sum
+// is the reference's.  The element vectors are formed negated and the ordered
+// gather adds Fext(k), so R = -(gathered vector) on those dofs.
+int svl_xnm_reaction(svl_xnm* X, int32_t k, double* R) {
+    if (!X || !R) { set_error("NULL argument"); return SVL_ERR_INVALID; }
+    if (X->explicit_cd) {
+        set_error("reaction forces are not covered for the explicit PML scheme (its stress dofs live at the half steps)");
+        return SVL_ERR_UNSUPPORTED;
+    }
+    const HostModel& m = X->m;
+    const int nt = m.ntotal, gt = grid_of(nt);
+    if (!X->fixed_dof) {
+        std::vector<int8_t> fx(nt, 0);
+        for (int n = 0; n < m.nnode; ++n) {
+            bool f = false;
+            for (int j = 0; j < m.nndof[n]; ++j) f = f || m.fdof_all[(size_t)n * m.dstride + j] == -1;
+            if (f)
+                for (int j = 0; j < m.nndof[n]; ++j) fx[m.tdof_all[(size_t)n * m.dstride + j]] = 1;
+        }
+        XTRY(X->alloc(nt, &X->fixed_dof));
+        XCUDA(cudaMemcpyAsync(X->fixed_dof, fx.data(), nt, cudaMemcpyHostToDevice, X->stream));
+    }
+    const size_t ns = (size_t)X->nsol * X->ncs;
+    if (ns > 0) k_xneg<<<(unsigned)((ns + 255) / 256), 256, 0, X->stream>>>(ns, X->s_fint, X->fe);
+    XSolid S = solid_args(X);
+    S.xK2 = X->V; S.cK2 = -1.0; S.xM = X->A; S.sM = -1.0; S.xM2 = X->V; S.cM2 = -1.0; S.accumulate = 1;
+    XTRY(launch_solid(X, S));
+    if (X->npml > 0) {
+        PmlArgs P = pml_args(X);
+        P.coef[0] = 1.0; P.u[0] = X->A; P.coef[1] = 1.0; P.u[1] = X->V; P.coef[2] = 1.0; P.u[2] = X->U;
+        P.yscale = -1.0;
+        XTRY(pml_action_launch(m.ndim, P, X->stream));
+    }
+    XTRY(x_gather(X, X->yt, -1.0, X->A, -1.0, X->V, k, true));
+    k_xreact<<<gt, 256, 0, X->stream>>>(nt, X->fixed_dof, X->yt, X->ys);
+    XCUDA(cudaGetLastError());
+    XCUDA(cudaMemcpyAsync(R, X->ys, sizeof(double) * nt, cudaMemcpyDeviceToHost, X->stream));
     XCUDA(cudaStreamSynchronize(X->stream));
     return SVL_OK;
 }

@@ -178,11 +178,10 @@ public:
     std::vector<double> GetDisplacements() const { return get(0); }
     std::vector<double> GetVelocities() const { return get(1); }
     std::vector<double> GetAccelerations() const { return get(2); }
-    // NewmarkBeta::ComputeReactionForce after step k (models without PML layers)
+    // NewmarkBeta::ComputeReactionForce after step k
     std::vector<double> ComputeReactionForce(unsigned int k) const {
-        if (x_) throw Error(SVL_ERR_UNSUPPORTED, "reactions are not covered for PML models");
         std::vector<double> r(ntotal_);
-        check(svl_nm_reaction(h_, (int32_t)k, r.data()));
+        check(x_ ? svl_xnm_reaction(x_, (int32_t)k, r.data()) : svl_nm_reaction(h_, (int32_t)k, r.data()));
         return r;
     }
 
@@ -243,6 +242,13 @@ public:
     std::vector<double> GetVelocities() const { return get(1); }
     std::vector<double> GetAccelerations() const { return get(2); }
     std::vector<double> GetPMLHistoryVector() const { return get(3); }
+    // ComputeReactionForce(mesh, k) after step k (:158-172), as
+    // DynamicAnalysis::UpdateDomain stores it at the fixed nodes
+    std::vector<double> ComputeReactionForce(unsigned int k) const {
+        std::vector<double> r(ntotal_);
+        check(svl_xnm_reaction(h_, (int32_t)k, r.data()));
+        return r;
+    }
 
 private:
     std::vector<double> get(int which) const {

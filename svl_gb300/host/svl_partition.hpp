@@ -18,7 +18,7 @@
 // constraints; nodal masses; Free / Rayleigh dampings; ZeroLength1D elements
 // with a Viscous1DLinear material (Lysmer dashpots); point loads (concentrated
 // and body), element body loads and domain-reduction loads; constant and
-// time-series functions; support motions; node recorders.  Anything else
+// time-series functions; support motions; node and element recorders.  Anything else
 // throws svl::gpu::Error with SVL_ERR_UNSUPPORTED naming it.
 #pragma once
 
@@ -217,8 +217,9 @@ inline std::vector<int> sorted_tags(const Json& o) {
 }
 
 struct NodeRecorder {
-    std::string file, response;        // DISP, VEL, ACCEL or REACTION
-    std::vector<int> ids;              // node tags
+    std::string name = "NODE";         // NODE or ELEMENT
+    std::string file, response;        // NODE: DISP, VEL, ACCEL, REACTION; ELEMENT: STRESS, STRAIN, INTERNALFORCE, STRAINRATE
+    std::vector<int> ids;              // node or element tags
     int precision = 8;
     int nsamp = 1;
 };
@@ -687,16 +688,27 @@ inline Partition load_partition(const std::string& path, std::string run_dir = "
                 P.sm_factor.push_back(1.0);
             }
         }
-    // node recorders (Recorder.cpp:73-106, 239-268)
+    // node and element recorders (Recorder.cpp:73-166, 239-323)
     const Json& RC = d.has("Recorders") ? d.at("Recorders") : empty;
     for (int t : sorted_tags(RC)) {
         const Json& r = RC.at(std::to_string(t));
-        if (upper(r.at("name").text()) != "NODE") unsupported("recorder " + r.at("name").text() + " is not covered (NODE only)");
         NodeRecorder nr;
+        nr.name = upper(r.at("name").text());
         nr.file = r.at("file").text();
         nr.response = upper(r.at("resp").text());
-        if (nr.response != "DISP" && nr.response != "VEL" && nr.response != "ACCEL" && nr.response != "REACTION")
-            unsupported("node recorder response " + r.at("resp").text() + " is not covered");
+        if (nr.name == "NODE") {
+            if (nr.response != "DISP" && nr.response != "VEL" && nr.response != "ACCEL" && nr.response != "REACTION")
+                unsupported("node recorder response " + r.at("resp").text() + " is not covered");
+        } else if (nr.name == "ELEMENT") {
+            if (nr.response != "STRESS" && nr.response != "STRAIN" && nr.response != "INTERNALFORCE" && nr.response != "STRAINRATE")
+                unsupported("element recorder response " + r.at("resp").text() + " is not covered");
+            for (const Json& v : r.at("list").list()) {
+                auto it = epos.find((int)v.number());
+                if (it == epos.end() || P.elem_pml[it->second]) unsupported("element recorder " + nr.file + ": element " + v.text() + " is not a solid element of this model");
+            }
+        } else {
+            unsupported("recorder " + r.at("name").text() + " is not covered (NODE, ELEMENT)");
+        }
         for (const Json& v : r.at("list").list()) nr.ids.push_back((int)v.number());
         nr.precision = (int)r.number("ndps", 8);
         nr.nsamp = (int)r.number("nsamp", 1);

@@ -66,6 +66,12 @@ class CentralDifference:
         check(lib().svl_cd_reaction(self._h, int(k), ptr(R, C.c_double)))
         return R
 
+    def element_response(self, response: str, elems) -> np.ndarray:
+        """ELEMENT recorder values after the last step (Recorder.cpp:272-323)
+        of the element positions `elems`: STRAIN / STRESS / STRAINRATE
+        [n, ngp, 3|6], INTERNALFORCE [n, NC]."""
+        return _element_response(lib().svl_cd_element_response, self._h, self.model, response, elems)
+
     # -- batch interface -------------------------------------------------
     def run(self, k_first: int, nsteps: int, history: bool = False, out=None):
         """Steps k_first .. k_first+nsteps-1; with history=True (or a
@@ -268,6 +274,14 @@ class ExtendedNewmarkBeta:
     def GetPMLHistoryVector(self) -> np.ndarray:
         return self._get(3)
 
+    def ComputeReactionForce(self, k: int) -> np.ndarray:
+        """Reactions after step k on the fixed nodes' dofs (ExtendedNewmarkBeta /
+        NewmarkBeta::ComputeReactionForce as DynamicAnalysis::UpdateDomain
+        applies it); PML elements add K u + C v + M a over all their dofs."""
+        out = np.zeros(self.ntotal)
+        check(lib().svl_xnm_reaction(self._h, int(k), ptr(out, C.c_double)))
+        return out
+
     def run(self, k_first: int, nsteps: int, history: bool = False):
         hist = np.zeros((nsteps, self.ntotal)) if history else None
         check(lib().svl_xnm_run(self._h, int(k_first), int(nsteps), ptr(hist, C.c_double)))
@@ -356,6 +370,10 @@ class NewmarkBeta:
 
     def GetAccelerations(self) -> np.ndarray:
         return self._get(2)
+
+    def element_response(self, response: str, elems) -> np.ndarray:
+        """ELEMENT recorder values after the last step (as CentralDifference)."""
+        return _element_response(lib().svl_nm_element_response, self._h, self.model, response, elems)
 
     def ComputeReactionForce(self, k: int) -> np.ndarray:
         """Reaction forces after step k (NewmarkBeta::ComputeReactionForce):
@@ -473,6 +491,20 @@ class NewmarkBeta:
             self.close()
         except Exception:
             pass
+
+
+ELEMENT_RESPONSES = {"STRAIN": 0, "STRESS": 1, "INTERNALFORCE": 2, "STRAINRATE": 3}
+
+
+def _element_response(fn, h, model: Model, response: str, elems) -> np.ndarray:
+    code = ELEMENT_RESPONSES[response.upper()]
+    el = capi.as_i32(np.asarray(elems, dtype=np.int32).ravel())
+    nen = model.conn.shape[1]
+    ngp = 4 if model.ndim == 2 else 8
+    shape = (el.size, nen * model.ndim) if code == 2 else (el.size, ngp, 3 if model.ndim == 2 else 6)
+    out = np.zeros(shape)
+    check(fn(h, code, int(el.size), ptr(el, C.c_int32), ptr(out, C.c_double)))
+    return out
 
 
 def _central_difference_pml(model, loads, dt, ftol=1e-12, mtol=1e-12, check_every=0):

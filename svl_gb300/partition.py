@@ -17,7 +17,8 @@ constraints; nodal masses; Rayleigh dampings; ZeroLength1D elements with a
 Viscous1DLinear material (Lysmer dashpots); domain-reduction (DRM) element
 loads with per-node free-field files; point loads and element body
 loads (constant or time series); support motions (constant or time series);
-node recorders of displacement, velocity or acceleration; the integrators
+node recorders of displacement, velocity, acceleration or reaction; element
+recorders of stress, strain, internal force or strain rate; the integrators
 CentralDifference, Newmark and ExtendedNewmark under the names the run-process
 accepts (Driver.hpp:1808-1822).  Anything else raises PartitionError naming it.
 """
@@ -143,15 +144,24 @@ class Partition:
         k = 1 .. nt-1 and every node recorder written after each step.  Returns
         the displacement history [nt-1][ntotal]."""
         h = self.make_integrator()
-        need_r = any(r.response == "REACTION" for r in self.recorders)
-        if need_r and not hasattr(h, "ComputeReactionForce"):
+        erecs = [r for r in self.recorders if r.name == "ELEMENT"]
+        if erecs and not hasattr(h, "element_response"):
             h.close()
-            raise PartitionError("REACTION recorders are covered for CENTRALDIFFERENCE and NEWMARK without PML")
+            raise PartitionError("ELEMENT recorders are covered for CENTRALDIFFERENCE and NEWMARK on models without "
+                                 "PML layers")
+        need_r = any(r.response == "REACTION" for r in self.recorders)
+        if need_r and self.integrator == "CENTRALDIFFERENCE" and self.model.elem_pml is not None \
+                and np.any(self.model.elem_pml):
+            h.close()
+            raise PartitionError("REACTION recorders are not covered for CENTRALDIFFERENCE on models with PML layers "
+                                 "(the explicit PML scheme's stress dofs live at the half steps)")
         h.Initialize()
         nsteps = self.nt - 1
         need_va = any(r.response in ("VEL", "ACCEL") for r in self.recorders)
         R = None
-        if need_va or need_r:
+        epos = {int(t): i for i, t in enumerate(self.elem_tags)}
+        EH = {id(r): [] for r in erecs}                  # per element recorder: one row per step
+        if need_va or need_r or erecs:
             U = np.zeros((nsteps, self.model.ntotal))
             V = np.zeros_like(U) if need_va else None
             A = np.zeros_like(U) if need_va else None
@@ -165,6 +175,8 @@ class Partition:
                     V[s], A[s] = h.GetVelocities(), h.GetAccelerations()
                 if need_r:                     # DynamicAnalysis::UpdateDomain (DynamicAnalysis.cpp:128-150)
                     R[s] = h.ComputeReactionForce(s + 1)
+                for r in erecs:                # Recorder::WriteElementResponse after every step
+                    EH[id(r)].append(h.element_response(r.response, [epos[t] for t in r.ids]).reshape(-1))
         else:
             U = h.run(1, nsteps, history=True)
             V = A = None
@@ -173,6 +185,9 @@ class Partition:
             out = Path(solution_dir) if solution_dir else (self.root / "Solution" / self.combo_folder)
             out.mkdir(parents=True, exist_ok=True)
             for r in self.recorders:
+                if r.name == "ELEMENT":
+                    write_element_recorder(out / r.file, self, r, np.array(EH[id(r)]))
+                    continue
                 hist = {"DISP": U, "VEL": V, "ACCEL": A, "REACTION": R}[r.response]
                 write_node_recorder(out / r.file, self, r, hist)
         return U
@@ -195,6 +210,30 @@ def write_node_recorder(path: Path, part: Partition, rec: Recorder, hist: np.nda
         for t, d in zip(rec.ids, dofs):
             f.write("%d %d %s\n" % (t, d.size, " ".join(str(int(x)) for x in d)))
         for row in hist[:, cols]:
+            f.write("".join(fmt % v for v in row) + "\n")
+
+
+def write_element_recorder(path: Path, part: Partition, rec: Recorder, rows: np.ndarray):
+    """Element recorder in the run-process's format (Recorder.cpp:107-166 header,
+    272-323 rows): `n_elements ntotal nt`, then per element `tag ndof totaldofs...`
+    (INTERNALFORCE) or `tag n_gauss_points n_components` (STRESS, STRAIN,
+    STRAINRATE), then one line per step with the elements' values (Gauss points
+    row by row) in scientific notation, each followed by a space."""
+    m = part.model
+    epos = {int(t): i for i, t in enumerate(part.elem_tags)}
+    ngp = 4 if m.ndim == 2 else 8
+    ncomp = 3 if m.ndim == 2 else 6
+    fmt = "%." + str(int(rec.precision)) + "e "
+    with open(path, "w") as f:
+        f.write("%d %d %d\n" % (len(rec.ids), m.ntotal, part.nt))
+        for t in rec.ids:
+            if rec.response == "INTERNALFORCE":
+                nodes = m.conn[epos[t]]
+                dofs = [int(x) for n in nodes for x in m.totaldof[n, :m.dof_mask()[n].sum()]]
+                f.write("%d %d %s\n" % (t, m.ndim * m.conn.shape[1], " ".join(str(x) for x in dofs)))
+            else:
+                f.write("%d %d %d\n" % (t, ngp, ncomp))
+        for row in rows:
             f.write("".join(fmt % v for v in row) + "\n")
 
 
@@ -388,12 +427,20 @@ def load_partition(path, run_dir=None) -> Partition:
     recs = []
     for rtag in sorted(d.get("Recorders", {}), key=int):
         r = d["Recorders"][rtag]
-        if r["name"].upper() != "NODE":
-            raise PartitionError("recorder %s is not covered (NODE only)" % r["name"])
-        resp = r["resp"].upper()
-        if resp not in ("DISP", "VEL", "ACCEL", "REACTION"):
-            raise PartitionError("node recorder response %s is not covered" % r["resp"])
-        recs.append(Recorder(name="NODE", file=r["file"], response=resp, ids=[int(x) for x in r["list"]],
+        rname, resp = r["name"].upper(), r["resp"].upper()
+        if rname == "NODE":
+            if resp not in ("DISP", "VEL", "ACCEL", "REACTION"):
+                raise PartitionError("node recorder response %s is not covered" % r["resp"])
+        elif rname == "ELEMENT":
+            if resp not in ("STRAIN", "STRESS", "INTERNALFORCE", "STRAINRATE"):
+                raise PartitionError("element recorder response %s is not covered" % r["resp"])
+            for t in r["list"]:
+                if int(t) not in epos or epml[epos[int(t)]]:
+                    raise PartitionError("element recorder %s: element %s is not a solid element of this model"
+                                         % (r["file"], t))
+        else:
+            raise PartitionError("recorder %s is not covered (NODE, ELEMENT)" % r["name"])
+        recs.append(Recorder(name=rname, file=r["file"], response=resp, ids=[int(x) for x in r["list"]],
                              precision=int(r.get("ndps", 8)), nsamp=int(r.get("nsamp", 1))))
     return Partition(model=model, loads=loads, integrator=integ["name"].upper(), dt=float(integ["dt"]), nt=nt,
                      ftol=float(integ.get("ftol", 1e-12)), mtol=float(integ.get("mtol", 1e-12)),

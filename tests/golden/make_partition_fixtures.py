@@ -454,6 +454,124 @@ SVL.addSolver(tag=1, attributes={"name": "Eigen", "update": "OFF"})
 SVL.addSimulation(tag=1, combo=1, attributes={"analysis": 1, "algorithm": 1, "integrator": 1, "solver": 1})
 SVL.CreateRunAnalysisFiles()
 ''',
+    # the J2 soil column with ELEMENT recorders of stress, strain, internal
+    # force and strain rate (Recorder.cpp:107-166, 272-323), CentralDifference
+    "q4_j2_element_cd": COMMON + r'''
+SVL.Options["dimension"] = 2
+SVL.Options["massform"] = "lumped"
+nx, ny, h, dt, nt = 2, 6, 0.5, 2.0e-4, 61
+G = 2000.0 * 200.0 ** 2; K = 2 * G * 1.3 / (3 * 0.4)
+SVL.addMaterial(tag=1, name="PlasticPlaneStrainJ2", attributes={"K": K, "G": G, "rho": 2000.0, "h": 0.02 * G,
+                                                                 "beta": 1.0, "Sy": math.sqrt(3.0) * 40.0e3})
+mesh = SVL.makeDomainArea(options={"ne": [nx, ny], "ndof": 2, "class": "LIN2DQUAD4", "elems": "QUAD4",
+    "P0": [0.0, 0.0], "P1": [nx * h, 0.0], "P2": [0.0, ny * h],
+    "attributes": {"material": 1, "th": 1.0, "rule": "Gauss", "np": 4}})
+for tag in sorted(mesh["Nodes"]):
+    n = mesh["Nodes"][tag]
+    SVL.addNode(tag=tag, ndof=n["ndof"], coords=list(map(float, n["coords"])))
+for tag in sorted(mesh["Elements"]):
+    el = mesh["Elements"][tag]
+    SVL.addElement(tag=tag, conn=list(el["conn"]), name=el["name"], attributes=dict(el["attributes"]))
+base = [t for t in sorted(mesh["Nodes"]) if (t - 1) // (nx + 1) == 0]
+for tag in base:
+    SVL.addRestrain(tag=tag, dof=[1, 2])
+ctag = -2
+for tag in sorted(mesh["Nodes"]):
+    i = (tag - 1) % (nx + 1)
+    if i != nx or tag in base:
+        continue
+    for d in range(2):
+        SVL.addConstraint(tag=ctag, name="Equal", attributes={"stag": tag, "sdof": d + 1, "mtag": [tag - nx], "mdof": [d + 1]})
+        ctag -= 1
+motion = [0.02 * math.sin(2 * math.pi * 8.0 * k * dt) * (1 - math.exp(-k / 10.0)) for k in range(nt)]
+write_series("base.txt", motion)
+for tag in base:
+    SVL.addSupportMotion(tag=tag, attributes={"type": "TimeSeries", "file": "base.txt", "dof": 1})
+SVL.addFunction(tag=1, name="Constant", attributes={"mag": 0.0, "dir": [0.0, -1.0]})
+SVL.addLoad(tag=1, name="PointLoad", attributes={"type": "Concentrated", "fun": 1, "list": [max(mesh["Nodes"])]})
+SVL.addCombinationCase(tag=1, name="Fixture", attributes={"load": [1], "factor": [1.0]})
+SVL.addRecorder(tag=1, attributes={"name": "NODE", "file": "Top.out", "ndps": 8, "resp": "disp", "list": [max(mesh["Nodes"])]})
+SVL.addRecorder(tag=2, attributes={"name": "ELEMENT", "file": "Stress.out", "ndps": 10, "resp": "stress", "list": [1, 4, 12]})
+SVL.addRecorder(tag=3, attributes={"name": "ELEMENT", "file": "Strain.out", "ndps": 10, "resp": "strain", "list": [2, 11]})
+SVL.addRecorder(tag=4, attributes={"name": "ELEMENT", "file": "Force.out", "ndps": 10, "resp": "internalforce", "list": [1, 12]})
+SVL.addRecorder(tag=5, attributes={"name": "ELEMENT", "file": "Rate.out", "ndps": 6, "resp": "strainrate", "list": [3]})
+SVL.addAnalysis(tag=1, attributes={"name": "Dynamic", "nt": nt})
+SVL.addAlgorithm(tag=1, attributes={"name": "Linear", "nstep": 1})
+SVL.addIntegrator(tag=1, attributes={"name": "CentralDifference", "dt": dt})
+SVL.addSolver(tag=1, attributes={"name": "Eigen", "update": "OFF"})
+SVL.addSimulation(tag=1, combo=1, attributes={"analysis": 1, "algorithm": 1, "integrator": 1, "solver": 1})
+SVL.CreateRunAnalysisFiles()
+''',
+    # the body-loaded H8 box with ELEMENT recorders, Newmark
+    "h8_element_newmark": COMMON + r'''
+SVL.Options["dimension"] = 3
+SVL.Options["massform"] = "lumped"
+nx, ny, nz, dt, nt = 3, 3, 2, 2.0e-3, 31
+SVL.addMaterial(tag=1, name="Elastic3DLinear", attributes={"E": 2.0e8, "nu": 0.3, "rho": 2000.0})
+mesh = SVL.makeDomainVolume(options={"ne": [nx, ny, nz], "ndof": 3, "class": "LIN3DHEXA8", "elems": "HEXA8",
+    "P0": [0.0, 0.0, 0.0], "P1": [nx * 2.0, 0.0, 0.0], "P2": [0.0, ny * 2.0, 0.0], "P3": [0.0, 0.0, nz * 2.0],
+    "attributes": {"material": 1, "rule": "Gauss", "np": 8}})
+for tag in sorted(mesh["Nodes"]):
+    n = mesh["Nodes"][tag]
+    SVL.addNode(tag=tag, ndof=n["ndof"], coords=list(map(float, n["coords"])))
+for tag in sorted(mesh["Elements"]):
+    el = mesh["Elements"][tag]
+    SVL.addElement(tag=tag, conn=list(el["conn"]), name=el["name"], attributes=dict(el["attributes"]))
+for tag in sorted(mesh["Nodes"]):
+    t = tag - 1; k = t // ((nx + 1) * (ny + 1))
+    if k == 0:
+        SVL.addRestrain(tag=tag, dof=[1, 2, 3])
+write_series("body.txt", ricker(nt, dt, 20.0, 1.0))
+SVL.addFunction(tag=1, name="TimeSeries", attributes={"file": "body.txt", "dir": [1.0, 0.0, 0.0]})
+SVL.addLoad(tag=1, name="ElementLoad", attributes={"type": "Body", "fun": 1, "list": [8, 11]})
+SVL.addCombinationCase(tag=1, name="Fixture", attributes={"load": [1], "factor": [2.0e3]})
+SVL.addRecorder(tag=1, attributes={"name": "NODE", "file": "Disp.out", "ndps": 10, "resp": "disp", "list": [40, 48]})
+SVL.addRecorder(tag=2, attributes={"name": "ELEMENT", "file": "Stress.out", "ndps": 10, "resp": "stress", "list": [1, 8, 18]})
+SVL.addRecorder(tag=3, attributes={"name": "ELEMENT", "file": "Force.out", "ndps": 10, "resp": "internalforce", "list": [8]})
+SVL.addAnalysis(tag=1, attributes={"name": "Dynamic", "nt": nt})
+SVL.addAlgorithm(tag=1, attributes={"name": "Linear", "nstep": 1})
+SVL.addIntegrator(tag=1, attributes={"name": "Newmark", "dt": dt})
+SVL.addSolver(tag=1, attributes={"name": "Petsc", "option": "KSPCG", "tol": 1.0e-10})
+SVL.addSimulation(tag=1, combo=1, attributes={"analysis": 1, "algorithm": 1, "integrator": 1, "solver": 1})
+SVL.CreateRunAnalysisFiles()
+''',
+    # the merged PML box with a REACTION recorder on restrained PML nodes,
+    # Newmark (PML elements add K u + C v + M a over all their dofs)
+    "q4_pml_reaction_newmark": COMMON + r'''
+SVL.Options["dimension"] = 2
+SVL.Options["massform"] = "lumped"
+W, H, P, dt, nt = 6.0, 4.0, 2.0, 2.0e-3, 41
+SVL.addMaterial(tag=1, name="Elastic2DPlaneStrain", attributes={"E": 2.0e8, "nu": 0.25, "rho": 2000.0})
+soil = SVL.makeDomainArea(options={"ne": [6, 4], "ndof": 2, "class": "LIN2DQUAD4", "elems": "QUAD4",
+    "P0": [0.0, 0.0], "P1": [W, 0.0], "P2": [0.0, H],
+    "attributes": {"material": 1, "th": 1.0, "rule": "Gauss", "np": 4}})
+pml = SVL.setPMLDomain({"ne": [10, 6], "ndof": 5, "class": "PML2DQUAD4", "elems": "QUAD4",
+    "P0": [-P, -P], "P1": [W + P, -P], "P2": [-P, H],
+    "attributes": {"material": 1, "th": 1.0, "n": 2.0, "L": P, "R": 1.0e-6, "rule": "Gauss", "np": 4}},
+    [W / 2.0, H / 2.0], [W / 2.0, H / 2.0])
+mesh = SVL.mergeDomain(soil, pml)
+SVL.Entities["Nodes"] = mesh["Nodes"]
+SVL.Entities["Elements"] = mesh["Elements"]
+SVL.Entities["Constraints"] = mesh["Constraints"]        # EQUAL ties of the PML interface nodes
+fixed = []
+for tag in sorted(mesh["Nodes"]):
+    x, y = mesh["Nodes"][tag]["coords"][:2]
+    if abs(x + P) < 1e-9 or abs(x - W - P) < 1e-9 or abs(y + P) < 1e-9:
+        SVL.addRestrain(tag=tag, dof=[1, 2]); fixed.append(tag)
+top = [t for t in sorted(mesh["Nodes"]) if abs(mesh["Nodes"][t]["coords"][1] - H) < 1e-9 and abs(mesh["Nodes"][t]["coords"][0] - W / 2) < 1e-9][0]
+write_series("ricker.txt", ricker(nt, dt, 25.0, 1.0e5))
+SVL.addFunction(tag=1, name="TimeSeries", attributes={"file": "ricker.txt", "dir": [0.0, -1.0]})
+SVL.addLoad(tag=1, name="PointLoad", attributes={"type": "Concentrated", "fun": 1, "list": [top]})
+SVL.addCombinationCase(tag=1, name="Fixture", attributes={"load": [1], "factor": [1.0]})
+SVL.addRecorder(tag=1, attributes={"name": "NODE", "file": "Disp.out", "ndps": 8, "resp": "disp", "list": [top]})
+SVL.addRecorder(tag=2, attributes={"name": "NODE", "file": "Reaction.out", "ndps": 8, "resp": "reaction", "list": fixed[:6]})
+SVL.addAnalysis(tag=1, attributes={"name": "Dynamic", "nt": nt})
+SVL.addAlgorithm(tag=1, attributes={"name": "Linear", "nstep": 1})
+SVL.addIntegrator(tag=1, attributes={"name": "Newmark", "dt": dt})
+SVL.addSolver(tag=1, attributes={"name": "Eigen", "update": "OFF"})
+SVL.addSimulation(tag=1, combo=1, attributes={"analysis": 1, "algorithm": 1, "integrator": 1, "solver": 1})
+SVL.CreateRunAnalysisFiles()
+''',
 }
 
 

@@ -130,3 +130,65 @@ def test_body_point_load_partition_cd_matches_oracle(gpu, tmp_path):
     ho, *_ = O.cd_run(p.model, p.loads, p.dt, p.nt - 1)
     assert np.abs(ho).max() > 0
     assert rel_l2(U, ho) <= 1e-12
+
+
+def _read_element_recorder(path):
+    lines = path.read_text().splitlines()
+    ne, ntotal, nt = map(int, lines[0].split())
+    head = [list(map(int, ln.split())) for ln in lines[1:1 + ne]]
+    rows = np.array([[float(v) for v in ln.split()] for ln in lines[1 + ne:]])
+    return (ne, ntotal, nt), head, rows
+
+
+@pytest.mark.parametrize("case,integ", [("q4_j2_element_cd", "cd"), ("h8_element_newmark", "newmark")])
+def test_element_recorders_match_oracle(gpu, case, integ, tmp_path):
+    """ELEMENT recorders written by the pre-processor (stress, strain,
+    internal force, strain rate; J2 and elastic elements): the format of
+    Recorder.cpp and the last row against the oracle's element state after
+    the last step."""
+    p = _part(case)
+    p.run(solution_dir=tmp_path)
+    epos = {int(t): i for i, t in enumerate(p.elem_tags)}
+    nrec = 0
+    for r in p.recorders:
+        if r.name != "ELEMENT":
+            continue
+        nrec += 1
+        (ne, ntotal, nt), head, rows = _read_element_recorder(tmp_path / r.file)
+        assert (ne, ntotal, nt) == (len(r.ids), p.model.ntotal, p.nt) and rows.shape[0] == p.nt - 1
+        ngp, ncomp = (4, 3) if p.model.ndim == 2 else (8, 6)
+        nc = p.model.conn.shape[1] * p.model.ndim
+        if r.response == "INTERNALFORCE":
+            assert all(h[1] == nc and len(h) == 2 + nc for h in head)
+        else:
+            assert all(h[1:] == [ngp, ncomp] for h in head)
+        kw = dict(integrator=integ)
+        if integ == "newmark":
+            kw["algo"] = 0
+        want = O.element_response_run(p.model, p.loads, p.dt, p.nt - 1, r.response, [epos[t] for t in r.ids],
+                                      **kw).reshape(-1)
+        if r.response == "STRAINRATE":
+            assert not np.any(rows)
+            continue
+        assert np.abs(want).max() > 0
+        scale = np.abs(want).max()
+        # the recorder prints ndps digits; the solutions agree to the solver tolerance
+        assert np.allclose(rows[-1], want, rtol=0, atol=max(10.0 ** (1 - r.precision), 1e-7) * scale), \
+            (r.file, np.abs(rows[-1] - want).max() / scale)
+    assert nrec >= 2
+
+
+def test_pml_reaction_recorder_newmark(gpu, tmp_path):
+    """REACTION recorder on restrained PML nodes of the pre-processor's merged
+    PML mesh, NewmarkBeta: PML elements add K u + C v + M a over all their
+    dofs, so the stress dofs of those nodes carry reactions too."""
+    p = _part("q4_pml_reaction_newmark")
+    p.run(solution_dir=tmp_path)
+    rec = [r for r in p.recorders if r.response == "REACTION"][0]
+    (nn, ndofs, ntotal, nt), head, rows = _read_recorder(tmp_path / rec.file)
+    Ro = O.reaction_run(p.model, p.loads, p.dt, p.nt - 1, integrator="xnewmark_nm")
+    cols = [d for h in head for d in h[2:]]
+    want = Ro[cols]
+    assert any(h[1] == 5 for h in head)                  # PML nodes: 2 displacement + 3 stress dofs
+    assert rows.shape[0] == p.nt - 1 and np.abs(want).max() > 0
+    assert np.allclose(rows[-1], want, rtol=1e-6, atol=1e-6 * np.abs(want).max())

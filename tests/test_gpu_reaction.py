@@ -72,3 +72,34 @@ def test_newmark_newton_j2_reaction_with_dashpots(gpu):
     R = nm.ComputeReactionForce(40)
     nm.close()
     _close(R, O.reaction_run(m, L, 2 * dt, 40, integrator="newmark", algo=2, maxit=3, cnvgtol=0.0), 1e-8)
+
+
+@pytest.mark.parametrize("ndim,integ", [(2, "xnewmark"), (3, "xnewmark"), (2, "xnewmark_nm")])
+def test_pml_model_reaction(gpu, ndim, integ):
+    """PML models on the PML-capable handle (ExtendedNewmarkBeta, and the
+    NewmarkBeta mode): PML elements with a fixed node add K u + C v + M a over
+    all their dofs, so fixed PML nodes report stress-dof reactions too."""
+    from svl_gb300 import ExtendedNewmarkBeta
+    from tests.helpers import pml_box
+    m, L, dt = pml_box(ndim=ndim, ni=(6, 4) if ndim == 2 else (3, 3, 2), npml=2, nt=40)
+    n = 30
+    h = ExtendedNewmarkBeta(m, L, dt, tol=1e-13, integrator="newmark" if integ == "xnewmark_nm" else "extendednewmark")
+    h.Initialize()
+    h.run(1, n)
+    R = h.ComputeReactionForce(n)
+    h.close()
+    _close(R, O.reaction_run(m, L, dt, n, integrator=integ), 1e-8)
+
+
+def test_explicit_pml_scheme_rejects_reactions(gpu):
+    from svl_gb300 import SvlError
+    from svl_gb300 import _capi as capi
+    from tests.helpers import pml_box
+    m, L, dt = pml_box(ndim=2, ni=(6, 4), npml=2, nt=20, dt_factor=0.5)
+    cd = CentralDifference(m, L, dt)
+    cd.Initialize()
+    cd.run(1, 5)
+    with pytest.raises(SvlError) as ei:
+        cd.ComputeReactionForce(5)
+    assert ei.value.code == capi.SVL_ERR_UNSUPPORTED
+    cd.close()

@@ -94,3 +94,35 @@ def test_central_difference_reaction_balances_the_model():
     Rd = np.where(fixed, K @ U + Cm @ V + M @ A - _fext(L, m.ntotal, n), 0.0)
     assert np.abs(Rd).max() > 0
     assert np.abs(R - Rd).max() <= 1e-8 * np.abs(Rd).max()
+
+
+@pytest.mark.parametrize("ndim,integ", [(2, "xnewmark"), (3, "xnewmark"), (2, "xnewmark_nm")])
+def test_pml_reaction_matches_dense(ndim, integ):
+    """PML models (ExtendedNewmarkBeta / NewmarkBeta): every element with a
+    fixed node adds K_e u_e + C_e v_e + M_e a_e over all its dofs
+    (PML3DHexa8.cpp:746-767, no history term), so on the fixed nodes' dofs R
+    equals the assembled K U + C V + M A - Fext(k) with the PML element
+    matrices (consistent PML mass) and the run's own final state."""
+    from tests.helpers import pml_box
+    if ndim == 2:
+        m, L, dt = pml_box(ndim=2, ni=(6, 4), npml=2, nt=40)
+        n = 30
+    else:
+        m, L, dt = pml_box(ndim=3, ni=(2, 2, 2), npml=1, nt=20)
+        n = 12
+    R = O.reaction_run(m, L, dt, n, integrator=integ)
+    _, U, V, A, _ = O.xnewmark_run(m, L, dt, n, newmark=integ == "xnewmark_nm")
+    K, M, Cm, _ = O.xnewmark_matrices(m)
+    fixed = np.zeros(m.ntotal, bool)
+    mask = m.dof_mask()
+    for i in range(m.nnode):
+        nd = mask[i].sum()
+        if np.any(m.freedof[i, :nd] == -1):
+            fixed[m.totaldof[i, :nd]] = True
+    Rd = np.where(fixed, K @ U + Cm @ V + M @ A - _fext(L, m.ntotal, n), 0.0)
+    assert np.abs(Rd).max() > 0
+    assert np.abs(R - Rd).max() <= 1e-8 * np.abs(Rd).max()
+    # the stress dofs of fixed PML nodes carry (nonzero) reactions too
+    pnodes = [i for i in range(m.nnode) if mask[i].sum() > ndim and np.any(m.freedof[i, :ndim] == -1)]
+    sd = np.concatenate([m.totaldof[i, ndim:mask[i].sum()] for i in pnodes])
+    assert np.abs(R[sd]).max() > 0
