@@ -296,10 +296,23 @@ void svl_cd_destroy(svl_cd* cd);
 typedef struct svl_cdx svl_cdx;
 int  svl_cdx_create(const svl_grid_spec* grid, int32_t ninst, const svl_model_desc* models,
                     const svl_load_desc* loads, const svl_cd_opts* opts, svl_cdx** out);
+/* Ensembles of uneven grids: instance b lives on grids[b] (every grid with
+ * the element size of grids[0]; models and loads as for svl_cdx_create on
+ * their own grids; no PML layers, support motion or domain reduction).  The
+ * instances are embedded in the grid that bounds them all (restrained nodes
+ * and elements without stiffness or mass fill the rest, so the instances'
+ * results do not change) and the fused kernel schedules only the tiles that
+ * meet an instance's own nodes.  set_initial / get take each instance's own
+ * total dofs; run's history is [nsteps][sum of the instances' ntotal], the
+ * instances one after the other.  No counterpart in the reference (an
+ * ensemble there is one process per model). */
+int  svl_cdx_create_ensemble(const svl_grid_spec* grids, int32_t ninst, const svl_model_desc* models,
+                             const svl_load_desc* loads, const svl_cd_opts* opts, svl_cdx** out);
 /* Initial conditions of instance `inst` (total dofs, NULL = zero). */
 int  svl_cdx_set_initial(svl_cdx* cdx, int32_t inst, const double* U0, const double* V0, const double* A0);
 /* Steps k_first .. k_first+nsteps-1 of every instance; U_hist (host, or
- * NULL) receives [nsteps][ninst][ntotal] displacements. */
+ * NULL) receives [nsteps][ninst][ntotal] displacements (ensembles: the
+ * instances' own ntotal one after the other). */
 int  svl_cdx_run(svl_cdx* cdx, int32_t k_first, int32_t nsteps, double* U_hist);
 /* svl_cdx_run without history bracketed by CUDA events on the handle's
  * stream (measurement hook, no counterpart in the reference). */

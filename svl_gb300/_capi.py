@@ -156,6 +156,8 @@ def lib():
     L.svl_cd_profile.argtypes = [C.c_void_p, C.c_int32, C.c_int32, f64p]
     L.svl_cdx_create.argtypes = [C.POINTER(GridSpec), C.c_int32, C.POINTER(ModelDesc), C.POINTER(LoadDesc),
                                  C.POINTER(CdOpts), C.POINTER(C.c_void_p)]
+    L.svl_cdx_create_ensemble.argtypes = [C.POINTER(GridSpec), C.c_int32, C.POINTER(ModelDesc), C.POINTER(LoadDesc),
+                                          C.POINTER(CdOpts), C.POINTER(C.c_void_p)]
     L.svl_cdx_set_initial.argtypes = [C.c_void_p, C.c_int32, f64p, f64p, f64p]
     L.svl_cdx_run.argtypes = [C.c_void_p, C.c_int32, C.c_int32, f64p]
     L.svl_cdx_run_timed.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(C.c_float)]

@@ -191,6 +191,7 @@ struct CdxView {
     int nx, ny, nz, ninst;
     int pitch;                           // floats per padded x-row of the state arrays
     int ntx, nty, ntz, ntiles;
+    const int32_t* __restrict__ tiles;   // ensembles: compact tile -> tile of the full enumeration, or null
     float* uh_prev;                      // u_{n-1} (read through TMA), u_{n+1} written here
     float* ul_prev;
     const float* __restrict__ cdof;      // [inst][z][y][pitch]  dt^2/m, 0 on restrained dofs,
@@ -242,7 +243,7 @@ __device__ __forceinline__ bool group_and(bool v) {
 struct TileOrigin { int inst, x0, y0, z0; };
 __device__ __forceinline__ TileOrigin tile_origin(const CdxView& v, int tile) {
     TileOrigin o;
-    int r = tile;
+    int r = v.tiles ? v.tiles[tile] : tile;
     const int tx = r % v.ntx; r /= v.ntx;
     const int ty = r % v.nty; r /= v.nty;
     const int tz = r % v.ntz;
@@ -561,17 +562,18 @@ __global__ void k_cdx_va(const float* nh, const float* nl, const float* ch, cons
 // FP64 total-dof displacement of every instance from the padded compensated
 // pairs: out[b][t] = hi + lo at the padded position of total dof t = node*3 + c.
 // FP64 total-dof vector of every instance from the compensated pairs:
-// omap[t] >= 0 is the padded position of displacement dof t, -(1 + k) the
-// stress entry k = p*6 + c of PML node p (S of the half step after U's time).
+// One step's history row: hmap[i] >= 0 is the state position (instance
+// offset included) of entry i (instances one after the other, each in its
+// own total-dof numbering), -(1 + k) the stress entry k of the PML band's
+// arrays (S of the half step after U's time).
 __global__ void k_cdx_hist(const float* __restrict__ uh, const float* __restrict__ ul, const float* __restrict__ sh,
-                           const float* __restrict__ sl, const long long* __restrict__ omap, double* __restrict__ out,
-                           long long ntotal, long long per, long long sper, int ninst) {
+                           const float* __restrict__ sl, const long long* __restrict__ hmap, double* __restrict__ out,
+                           long long n) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= ntotal * ninst) return;
-    const long long b = i / ntotal, t = i - b * ntotal;
-    const long long m = omap[t];
-    if (m >= 0) out[i] = (double)uh[b * per + m] + (double)ul[b * per + m];
-    else out[i] = (double)sh[b * sper - m - 1] + (double)sl[b * sper - m - 1];
+    if (i >= n) return;
+    const long long m = hmap[i];
+    if (m >= 0) out[i] = (double)uh[m] + (double)ul[m];
+    else out[i] = (double)sh[-m - 1] + (double)sl[-m - 1];
 }
 
 // ---- PML band of the mixed path --------------------------------------------
@@ -1007,7 +1009,13 @@ struct svl_cdx {
     CUtensorMap tmap_lam, tmap_mu;
     std::vector<long long> pad_index;    // total dof -> padded position (displacement dofs), or
                                          // -(1 + p*6 + c) for stress dof c of PML node p; one instance
-    long long* d_omap = nullptr;         // pad_index on the device
+    long long* d_hmap = nullptr;         // history map (k_cdx_hist), hist_n entries
+    long long hist_n = 0;                // history entries per step: the instances' total dofs
+    int32_t* d_tiles = nullptr;          // ensembles: compact tile -> tile of the full enumeration
+    // ensembles of uneven grids: each instance is embedded in the bounding grid;
+    // own2emb[b][t] is the embedded total dof of the instance's own dof t
+    std::vector<std::vector<long long>> own2emb;
+    std::vector<long long> own_ntotal;   // total dofs of each instance in its own numbering
     // PML band (np = 0 without PML elements)
     int np = 0, npe = 0;
     float* fsol = nullptr;
@@ -1151,8 +1159,9 @@ static int fetch_pair(svl_cdx* h, const float* dh, const float* dl, int inst, do
         CUDA_TRY(cudaMemcpyAsync(slo.data(), sl + (size_t)inst * n6, n6 * 4, cudaMemcpyDeviceToHost, h->stream));
     }
     CUDA_TRY(cudaStreamSynchronize(h->stream));
-    for (long long t = 0; t < h->ntotal; ++t) {
-        const long long p = h->pad_index[t];
+    const bool emb = !h->own2emb.empty();
+    for (long long t = 0; t < h->own_ntotal[inst]; ++t) {
+        const long long p = h->pad_index[emb ? h->own2emb[inst][t] : t];
         out[t] = p >= 0 ? (double)hi[p] + (double)lo[p] : (double)shi[-p - 1] + (double)slo[-p - 1];
     }
     return SVL_OK;
@@ -1160,8 +1169,13 @@ static int fetch_pair(svl_cdx* h, const float* dh, const float* dl, int inst, do
 
 extern "C" {
 
-int svl_cdx_create(const svl_grid_spec* g, int32_t ninst, const svl_model_desc* models, const svl_load_desc* loads,
-                   const svl_cd_opts* opts, svl_cdx** out) {
+// Creates the handle for ninst instances on grid g.  Ensembles of uneven
+// grids come embedded in their bounding grid: ext [ninst][3] gives each
+// instance's own node extents (the tiles beyond them are not scheduled) and
+// emb its own-to-embedded dof maps; both null for instances of one grid.
+static int cdx_create_impl(const svl_grid_spec* g, int32_t ninst, const svl_model_desc* models,
+                           const svl_load_desc* loads, const svl_cd_opts* opts, svl_cdx** out, const int32_t* ext,
+                           const std::vector<std::vector<long long>>* emb) {
     if (!g || !models || !opts || !out || ninst <= 0) { set_error("NULL argument or ninst <= 0"); return SVL_ERR_INVALID; }
     *out = nullptr;
     if (g->ndim != 3) { set_error("the structured mixed path is 3D (lin3DHexa8)"); return SVL_ERR_UNSUPPORTED; }
@@ -1184,6 +1198,20 @@ int svl_cdx_create(const svl_grid_spec* g, int32_t ninst, const svl_model_desc* 
     const long long ntiles = (long long)h->ntx * h->nty * h->ntz * ninst;
     if (ntiles > INT32_MAX || h->nstate > ((long long)1 << 40)) { set_error("grid too large"); return fail(SVL_ERR_INVALID); }
     h->ntiles = (int)ntiles;
+    std::vector<int32_t> tiles;                      // ensembles: the tiles that meet an instance's own nodes
+    std::vector<int> tile_compact;                   // full tile -> compact index (-1: not scheduled)
+    if (ext) {
+        tile_compact.assign((size_t)ntiles, -1);
+        for (int b = 0; b < ninst; ++b)
+            for (int tz = 0; tz < (ext[3 * b + 2] + TZ - 1) / TZ; ++tz)
+                for (int ty = 0; ty < (ext[3 * b + 1] + TY - 1) / TY; ++ty)
+                    for (int tx = 0; tx < (ext[3 * b] + TX - 1) / TX; ++tx) {
+                        const long long full = (((long long)b * h->ntz + tz) * h->nty + ty) * h->ntx + tx;
+                        tile_compact[full] = (int)tiles.size();
+                        tiles.push_back((int32_t)full);
+                    }
+        h->ntiles = (int)tiles.size();
+    }
     h->dt = opts->dt;
     h->hgrid = g->h[0];
     {
@@ -1462,7 +1490,8 @@ int svl_cdx_create(const svl_grid_spec* g, int32_t ninst, const svl_model_desc* 
     auto tile_of = [&](long long gdof) {
         const long long b = gdof / h->ntotal, t = gdof % h->ntotal, n = t2node[t];
         const long long x = n % nxn, y = (n / nxn) % nyn, z = n / ((long long)nxn * nyn);
-        return (((b * h->ntz + z / TZ) * h->nty + y / TY) * h->ntx + x / TX);
+        const long long full = (((b * h->ntz + z / TZ) * h->nty + y / TY) * h->ntx + x / TX);
+        return ext ? (long long)tile_compact[full] : full;
     };
     std::stable_sort(order.begin(), order.end(), [&](int a, int c) {
         const long long ta = tile_of(fdof[a]), tc = tile_of(fdof[c]);
@@ -1494,9 +1523,25 @@ int svl_cdx_create(const svl_grid_spec* g, int32_t ninst, const svl_model_desc* 
         (st = h->upload(mu, &h->mu)) || (st = h->upload(cdof, &h->cdof)) || (st = h->upload(bop, &h->bop)) ||
         (st = h->alloc(1, &h->status)) || (st = h->upload(tl_ptr, &h->tl_ptr)) || (st = h->upload(ld_dof, &h->ld_dof)) ||
         (st = h->upload(ld_ptr, &h->ld_ptr)) || (st = h->upload(ld_ser, &h->ld_ser)) || (st = h->upload(ld_coef, &h->ld_coef)) ||
-        (st = h->upload(s_ptr, &h->s_ptr)) || (st = h->upload(s_val, &h->s_val)) ||
-        (st = h->upload(h->pad_index, &h->d_omap)))
+        (st = h->upload(s_ptr, &h->s_ptr)) || (st = h->upload(s_val, &h->s_val)))
         return fail(st);
+    if (ext && (st = h->upload(tiles, &h->d_tiles))) return fail(st);
+    // history map: the instances one after the other, each in its own numbering
+    {
+        if (emb) h->own2emb = *emb;
+        const long long sper = (long long)h->np * 6;
+        std::vector<long long> hm;
+        for (int b = 0; b < ninst; ++b) {
+            const long long n = emb ? (long long)(*emb)[b].size() : h->ntotal;
+            h->own_ntotal.push_back(n);
+            for (long long t = 0; t < n; ++t) {
+                const long long p2 = h->pad_index[emb ? (*emb)[b][t] : t];
+                hm.push_back(p2 >= 0 ? b * per + p2 : -(1 + b * sper + (-p2 - 1)));
+            }
+        }
+        h->hist_n = (long long)hm.size();
+        if ((st = h->upload(hm, &h->d_hmap))) return fail(st);
+    }
     if (h->np > 0) {
         const size_t n6 = (size_t)ninst * h->np * 6, n3 = (size_t)ninst * h->np * 3;
         if ((st = h->alloc(ns, &h->fsol)) || (st = h->alloc(n6, &h->sh[0])) || (st = h->alloc(n6, &h->sh[1])) ||
@@ -1531,8 +1576,138 @@ int svl_cdx_create(const svl_grid_spec* g, int32_t ninst, const svl_model_desc* 
     return SVL_OK;
 }
 
+int svl_cdx_create(const svl_grid_spec* g, int32_t ninst, const svl_model_desc* models, const svl_load_desc* loads,
+                   const svl_cd_opts* opts, svl_cdx** out) {
+    return cdx_create_impl(g, ninst, models, loads, opts, out, nullptr, nullptr);
+}
+
+// Ensembles of uneven grids: every instance is embedded in the grid that
+// bounds them all (same element size): its nodes keep their coordinates
+// relative to the grid origin, numbering and restraints; the rest of the
+// bounding lattice gets restrained nodes and elements of a material without
+// stiffness or mass, so nothing there moves or loads the instance; the fused
+// kernel schedules only the tiles that meet an instance's own nodes.
+int svl_cdx_create_ensemble(const svl_grid_spec* grids, int32_t ninst, const svl_model_desc* models,
+                            const svl_load_desc* loads, const svl_cd_opts* opts, svl_cdx** out) {
+    if (!grids || !models || !opts || !out || ninst <= 0) { set_error("NULL argument or ninst <= 0"); return SVL_ERR_INVALID; }
+    *out = nullptr;
+    svl_grid_spec gb = grids[0];
+    for (int b = 0; b < ninst; ++b) {
+        const svl_grid_spec& g = grids[b];
+        if (g.ndim != 3) { set_error("the structured mixed path is 3D (lin3DHexa8)"); return SVL_ERR_UNSUPPORTED; }
+        for (int d = 0; d < 3; ++d) {
+            if (g.ne[d] <= 0) { set_error("instance %d: bad grid", b); return SVL_ERR_INVALID; }
+            if (std::fabs(g.h[d] - grids[0].h[d]) > 1e-12 * std::fabs(grids[0].h[d])) {
+                set_error("instance %d: every instance needs the element size of instance 0", b); return SVL_ERR_UNSUPPORTED;
+            }
+            gb.ne[d] = std::max(gb.ne[d], g.ne[d]);
+        }
+    }
+    const int NX = gb.ne[0], NY = gb.ne[1], NZ = gb.ne[2];
+    const long long nnb = (long long)(NX + 1) * (NY + 1) * (NZ + 1), neb = (long long)NX * NY * NZ;
+    struct Emb {
+        std::vector<double> X, mpar, nmass, sval, fcoef;
+        std::vector<int32_t> tdof, fdof, conn, emat, mtype, sptr, fdofl, fser;
+        svl_model_desc md{};
+        svl_load_desc ld{};
+    };
+    std::vector<Emb> E(ninst);
+    std::vector<std::vector<long long>> own2emb(ninst);
+    std::vector<int32_t> ext(3 * (size_t)ninst);
+    for (int b = 0; b < ninst; ++b) {
+        HostModel m;
+        if (!model_from_desc(&models[b], m)) return SVL_ERR_INVALID;
+        int st = cdx_check_instance(&grids[b], m, b);
+        if (st) return st;
+        if (m.has_pml()) { set_error("instance %d: ensembles of uneven grids are covered without PML layers", b); return SVL_ERR_UNSUPPORTED; }
+        const int nx = grids[b].ne[0], ny = grids[b].ne[1], nz = grids[b].ne[2];
+        ext[3 * b] = nx + 1; ext[3 * b + 1] = ny + 1; ext[3 * b + 2] = nz + 1;
+        Emb& em = E[b];
+        em.X.resize((size_t)nnb * 3);
+        em.tdof.resize((size_t)nnb * 3);
+        em.fdof.assign((size_t)nnb * 3, -1);
+        std::vector<long long> node_emb((size_t)m.nnode);
+        for (long long n = 0; n < nnb; ++n) {
+            const int i = (int)(n % (NX + 1)), j = (int)((n / (NX + 1)) % (NY + 1)), k = (int)(n / ((long long)(NX + 1) * (NY + 1)));
+            const double xyz[3] = {i * gb.h[0], j * gb.h[1], k * gb.h[2]};
+            for (int c = 0; c < 3; ++c) { em.X[n * 3 + c] = gb.origin[c] + xyz[c]; em.tdof[n * 3 + c] = (int32_t)(n * 3 + c); }
+            if (i <= nx && j <= ny && k <= nz) {
+                const long long no = ((long long)k * (ny + 1) + j) * (nx + 1) + i;
+                node_emb[no] = n;
+                for (int c = 0; c < 3; ++c) em.fdof[n * 3 + c] = m.fdof_all[(size_t)no * m.dstride + c];
+            }
+        }
+        own2emb[b].resize((size_t)m.ntotal);
+        for (long long no = 0; no < m.nnode; ++no)
+            for (int c = 0; c < 3; ++c) own2emb[b][(size_t)m.tdof_all[(size_t)no * m.dstride + c]] = node_emb[no] * 3 + c;
+        // elements: the instance's own where they lie, else a material without stiffness or mass
+        em.conn.resize((size_t)neb * 8);
+        em.emat.resize((size_t)neb);
+        em.mtype.assign(m.mtype.begin(), m.mtype.end());
+        em.mtype.push_back(SVL_MAT_ELASTIC3DLINEAR);
+        em.mpar.assign(m.mpar.begin(), m.mpar.end());
+        em.mpar.resize((size_t)(m.nmat + 1) * SVL_MAT_NPARAM, 0.0);
+        em.mpar[(size_t)m.nmat * SVL_MAT_NPARAM + 1] = 0.25;       // E = 0, rho = 0
+        const long long layer = (long long)(NX + 1) * (NY + 1);
+        long long e = 0;
+        for (int k = 0; k < NZ; ++k)
+            for (int j = 0; j < NY; ++j)
+                for (int i = 0; i < NX; ++i, ++e) {
+                    const long long n1 = layer * k + (long long)j * (NX + 1) + i;
+                    const long long c8[8] = {n1, n1 + 1, n1 + 1 + (NX + 1), n1 + (NX + 1),
+                                             n1 + layer, n1 + layer + 1, n1 + layer + 1 + (NX + 1), n1 + layer + (NX + 1)};
+                    for (int a = 0; a < 8; ++a) em.conn[e * 8 + a] = (int32_t)c8[a];
+                    em.emat[e] = (i < nx && j < ny && k < nz) ? m.emat[((long long)k * ny + j) * nx + i] : m.nmat;
+                }
+        if (!m.nodemass.empty()) {
+            em.nmass.assign((size_t)nnb * 3, 0.0);
+            for (long long t = 0; t < m.ntotal; ++t) em.nmass[own2emb[b][t]] = m.nodemass[t];
+        }
+        svl_model_desc& d = em.md;
+        d.ndim = 3; d.nnode = (int32_t)nnb; d.ndof = 3;
+        d.coords = em.X.data(); d.totaldof = em.tdof.data(); d.freedof = em.fdof.data();
+        d.ntotal = (int32_t)(nnb * 3); d.nfree = m.nfree;
+        d.elem_type = SVL_ELEM_LIN3DHEXA8; d.nelem = (int32_t)neb; d.conn = em.conn.data(); d.elem_mat = em.emat.data();
+        d.nmat = m.nmat + 1; d.mat_type = em.mtype.data(); d.mat_param = em.mpar.data();
+        d.lumped = m.lumped ? 1 : 0;
+        d.node_mass = em.nmass.empty() ? nullptr : em.nmass.data();
+        // loads on the embedded numbering
+        if (loads) {
+            const svl_load_desc& L = loads[b];
+            em.sptr.assign(L.series_ptr, L.series_ptr + L.nseries + 1);
+            em.sval.assign(L.series_val, L.series_val + (L.nseries > 0 ? L.series_ptr[L.nseries] : 0));
+            for (int i2 = 0; i2 < L.nforce; ++i2) {
+                if (L.force_dof[i2] < 0 || L.force_dof[i2] >= m.ntotal) { set_error("instance %d: load entry %d out of range", b, i2); return SVL_ERR_INVALID; }
+                em.fdofl.push_back((int32_t)own2emb[b][L.force_dof[i2]]);
+            }
+            em.fser.assign(L.force_series, L.force_series + L.nforce);
+            em.fcoef.assign(L.force_coef, L.force_coef + L.nforce);
+            if (L.nsupport > 0 || L.ndrm > 0) { set_error("instance %d: support motion and domain-reduction loads are served by svl_cd_create", b); return SVL_ERR_UNSUPPORTED; }
+            svl_load_desc& l = em.ld;
+            l.nseries = L.nseries; l.series_ptr = em.sptr.data(); l.series_val = em.sval.data();
+            l.nforce = L.nforce; l.force_dof = em.fdofl.data(); l.force_series = em.fser.data(); l.force_coef = em.fcoef.data();
+        }
+    }
+    std::vector<svl_model_desc> md(ninst);
+    std::vector<svl_load_desc> ld(ninst);
+    for (int b = 0; b < ninst; ++b) { md[b] = E[b].md; ld[b] = E[b].ld; }
+    return cdx_create_impl(&gb, ninst, md.data(), loads ? ld.data() : nullptr, opts, out, ext.data(), &own2emb);
+}
+
 int svl_cdx_set_initial(svl_cdx* h, int32_t inst, const double* U0, const double* V0, const double* A0) {
     if (!h || inst < 0 || inst >= h->ninst) { set_error("bad handle or instance"); return SVL_ERR_INVALID; }
+    std::vector<double> ew[3];                       // ensembles: the instance's vectors on its embedding
+    if (!h->own2emb.empty()) {
+        const double* src[3] = {U0, V0, A0};
+        for (int w = 0; w < 3; ++w) {
+            if (!src[w]) continue;
+            ew[w].assign((size_t)h->ntotal, 0.0);
+            for (size_t t = 0; t < h->own2emb[inst].size(); ++t) ew[w][h->own2emb[inst][t]] = src[w][t];
+        }
+        U0 = U0 ? ew[0].data() : nullptr;
+        V0 = V0 ? ew[1].data() : nullptr;
+        A0 = A0 ? ew[2].data() : nullptr;
+    }
     const size_t per = (size_t)(h->nstate / h->ninst);
     std::vector<float> hi(per, 0.f), lo(per, 0.f), phi(per, 0.f), plo(per, 0.f);
     const size_t n6 = (size_t)h->np * 6;
@@ -1623,7 +1798,7 @@ static int cdx_join(svl_cdx* h) {
 static int cdx_step(svl_cdx* h, int k, bool want_va) {
     CdxView v;
     v.nx = h->nx; v.ny = h->ny; v.nz = h->nz; v.ninst = h->ninst;
-    v.pitch = h->pitch; v.ntx = h->ntx; v.nty = h->nty; v.ntz = h->ntz; v.ntiles = h->ntiles;
+    v.pitch = h->pitch; v.ntx = h->ntx; v.nty = h->nty; v.ntz = h->ntz; v.ntiles = h->ntiles; v.tiles = h->d_tiles;
     v.uh_prev = h->uh[1 - h->cur]; v.ul_prev = h->ul[1 - h->cur];
     v.cdof = h->cdof; v.bop = h->bop;
     v.tl_ptr = h->tl_ptr; v.ld_dof = h->ld_dof; v.ld_ptr = h->ld_ptr; v.ld_ser = h->ld_ser; v.ld_coef = h->ld_coef;
@@ -1679,15 +1854,15 @@ static int cdx_status(svl_cdx* h) {
 // Enqueues steps [s0, s0 + n) of a run on the compute stream, writing each
 // step's FP64 fields into history chunk `slot`.
 static int cdx_fill_chunk(svl_cdx* h, int k_first, int s0, int n, int nsteps, int slot) {
-    const long long per_step = h->ntotal * h->ninst;
+    const long long per_step = h->hist_n;
     CUDA_TRY(cudaStreamWaitEvent(h->stream, h->drained[slot], 0));       // the chunk's previous copy is done
     for (int i = 0; i < n; ++i) {
         const int s = s0 + i;
         TRY(cdx_step(h, k_first + s, s == nsteps - 1));
         TRY(cdx_join(h));                                                  // S of this step
         k_cdx_hist<<<(unsigned)((per_step + 255) / 256), 256, 0, h->stream>>>(
-            h->uh[h->cur], h->ul[h->cur], h->sh[h->cur], h->sl[h->cur], h->d_omap, h->hist[slot] + (size_t)i * per_step,
-            h->ntotal, h->nstate / h->ninst, (long long)h->np * 6, h->ninst);
+            h->uh[h->cur], h->ul[h->cur], h->sh[h->cur], h->sl[h->cur], h->d_hmap, h->hist[slot] + (size_t)i * per_step,
+            per_step);
         ++h->launches;
     }
     CUDA_TRY(cudaGetLastError());
@@ -1704,7 +1879,7 @@ int svl_cdx_run(svl_cdx* h, int32_t k_first, int32_t nsteps, double* U_hist) {
     } else if (nsteps > 0) {
         // device-side FP64 conversion into two chunk buffers; the copy of chunk
         // c (on copy_stream) overlaps the computation of chunk c + 1
-        const long long per_step = h->ntotal * h->ninst;
+        const long long per_step = h->hist_n;
         const int chunk = (int)std::max<long long>(1, std::min<long long>(nsteps, (256ll << 20) / (per_step * 8)));
         if (h->hist_cap < chunk) {
             CUDA_TRY(cudaStreamSynchronize(h->stream));
@@ -1789,8 +1964,9 @@ int svl_cdx_get(svl_cdx* h, int32_t inst, int32_t which, double* out) {
             CUDA_TRY(cudaMemcpy(npd.data(), h->npad, (size_t)h->np * 8, cudaMemcpyDeviceToHost));
             for (int p2 = 0; p2 < h->np; ++p2) upos[npd[p2]] = p2;
         }
-        for (long long t = 0; t < h->ntotal; ++t) {
-            const long long p = h->pad_index[t];
+        const bool emb = !h->own2emb.empty();
+        for (long long t = 0; t < h->own_ntotal[inst]; ++t) {
+            const long long p = h->pad_index[emb ? h->own2emb[inst][t] : t];
             if (p < 0) { out[t] = (double)Sh[-p - 1] + (double)Sl[-p - 1]; continue; }
             const long long c = (p % h->pitch) % 3;          // rows hold x*3 + c
             const long long pn = upos[p - c];
@@ -1803,7 +1979,8 @@ int svl_cdx_get(svl_cdx* h, int32_t inst, int32_t which, double* out) {
     std::vector<double> tmp(per);
     CUDA_TRY(cudaMemcpyAsync(tmp.data(), (which == 1 ? h->V : h->A) + (size_t)inst * per, per * 8, cudaMemcpyDeviceToHost, h->stream));
     CUDA_TRY(cudaStreamSynchronize(h->stream));
-    for (long long t = 0; t < h->ntotal; ++t) out[t] = tmp[h->pad_index[t]];
+    const bool emb = !h->own2emb.empty();
+    for (long long t = 0; t < h->own_ntotal[inst]; ++t) out[t] = tmp[h->pad_index[emb ? h->own2emb[inst][t] : t]];
     return SVL_OK;
 }
 

@@ -183,8 +183,8 @@ class StructuredCentralDifference:
         return int(n.value)
 
     def profile(self, k_first: int, nsteps: int) -> np.ndarray:
-        """Device time (ms) per kernel kind over nsteps: [tensor-core step, PML
-        displacement rows, PML stress rows, 0, 0]."""
+        """Device time (ms) per kernel over nsteps: [tensor-core step, PML
+        band k_cdp_fu, k_cdp_uu, k_cdp_fs, k_cdp_su] (band zeros without PML)."""
         out = np.zeros(5)
         check(lib().svl_cdx_profile(self._h, int(k_first), int(nsteps), ptr(out, C.c_double)))
         return out
@@ -491,6 +491,61 @@ class NewmarkBeta:
             self.close()
         except Exception:
             pass
+
+
+class StructuredEnsemble(StructuredCentralDifference):
+    """Instances of uneven lin3DHexa8 grids (same element size) advanced by
+    one fused tensor-core kernel per step (svl_cdx_create_ensemble): each
+    instance is embedded in the bounding grid and only the tiles that meet its
+    own nodes are scheduled.  `grids` lists (ne, origin) per instance."""
+
+    def __init__(self, grids, h, instances, dt: float, mtol: float = 1e-12):
+        self.dt = float(dt)
+        self.ninst = len(instances)
+        specs = (capi.GridSpec * self.ninst)()
+        for b, (ne, origin) in enumerate(grids):
+            specs[b].ndim = 3
+            for i in range(3):
+                specs[b].ne[i] = int(ne[i])
+                specs[b].h[i] = float(h[i])
+                specs[b].origin[i] = float(origin[i])
+        self._spec = specs
+        md = (capi.ModelDesc * self.ninst)()
+        ld = (capi.LoadDesc * self.ninst)()
+        self._keep = []
+        for i, (m, L) in enumerate(instances):
+            md[i] = m.desc()
+            self._keep.append(m)
+            L = L or Loads()
+            ld[i] = L.desc()
+            self._keep.append(L)
+        self._md, self._ld = md, ld
+        opts = capi.CdOpts(dt=self.dt, ftol=0.0, mtol=mtol, precision=capi.SVL_PREC_MIXED, check_every=0)
+        hnd = C.c_void_p()
+        check(lib().svl_cdx_create_ensemble(specs, self.ninst, md, ld, C.byref(opts), C.byref(hnd)))
+        self._h = hnd
+        self.ntotals = [int(m.ntotal) for m, _ in instances]
+        self.offsets = np.concatenate([[0], np.cumsum(self.ntotals)])
+
+    def run(self, k_first: int, nsteps: int, history: bool = False, out=None):
+        """Steps of every instance; history (or `out`, float64 [nsteps,
+        sum of the instances' total dofs]) receives all displacements, the
+        instances one after the other (see split)."""
+        n = int(self.offsets[-1])
+        hist = out if out is not None else (np.zeros((nsteps, n)) if history else None)
+        if hist is not None:
+            assert hist.shape == (nsteps, n) and hist.dtype == np.float64 and hist.flags["C_CONTIGUOUS"]
+        check(lib().svl_cdx_run(self._h, int(k_first), int(nsteps), ptr(hist, C.c_double)))
+        return hist
+
+    def split(self, hist):
+        """Per-instance views [nsteps, ntotal_b] of a history."""
+        return [hist[:, self.offsets[b]:self.offsets[b + 1]] for b in range(self.ninst)]
+
+    def get(self, inst: int, which: int = 0) -> np.ndarray:
+        out = np.zeros(self.ntotals[inst])
+        check(lib().svl_cdx_get(self._h, int(inst), int(which), ptr(out, C.c_double)))
+        return out
 
 
 ELEMENT_RESPONSES = {"STRAIN": 0, "STRESS": 1, "INTERNALFORCE": 2, "STRAINRATE": 3}

@@ -184,3 +184,43 @@ def test_cdx_pml_band_matches_oracle(gpu):
             pn[m.conn[m.elem_pml == 1].ravel()] = True
             pd = np.concatenate([m.totaldof[n, :m.node_ndof[n]] for n in np.flatnonzero(pn)])
             assert rel_l2(ubar[pd], Ubo[pd]) <= 1e-4
+
+
+def test_uneven_ensemble_matches_oracle_and_single_runs(gpu):
+    """Instances of uneven grids in one fused launch (svl_cdx_create_ensemble):
+    each embedded in the bounding grid, only the tiles meeting its own nodes
+    scheduled, several tiles per CTA.  Every instance's history against the
+    oracle (<= 1e-5) and against the same instance run alone on its own grid
+    (the embedding changes no arithmetic: bit for bit)."""
+    from svl_gb300 import StructuredEnsemble
+    shapes = [(10, 8, 6), (14, 6, 9), (7, 12, 5)]
+    nt = 150
+    models = [h8_box(*s, seed=10 + b, nt=nt) for b, s in enumerate(shapes)]
+    dt = min(d for _, _, d in models)
+    inst = [(m, L) for m, L, _ in models]
+    ens = StructuredEnsemble([(s, (0.0, 0.0, 0.0)) for s in shapes], (2.0, 2.0, 2.0), inst, dt)
+    assert ens.set_ctas(5) == 5
+    for b in range(len(inst)):
+        ens.Initialize(b)
+    hist = ens.split(ens.run(1, nt, history=True))
+    last = [ens.get(b) for b in range(len(inst))]
+    ens.close()
+    for b, ((m, L), s) in enumerate(zip(inst, shapes)):
+        ho, *_ = O.cd_run(m, L, dt, nt, mode=1)
+        assert np.abs(ho).max() > 0
+        assert rel_l2(hist[b], ho) <= TOL_MIXED, b
+        assert np.array_equal(hist[b][-1], last[b])
+        one = StructuredCentralDifference(s, (2.0, 2.0, 2.0), [(m, L)], dt)
+        one.Initialize(0)
+        h1 = one.run(1, nt, history=True)
+        one.close()
+        assert np.array_equal(h1[:, 0, :], hist[b]), b
+
+
+def test_ensemble_rejects_mismatched_element_size(gpu):
+    from svl_gb300 import StructuredEnsemble
+    a = h8_box(6, 5, 4, seed=1, nt=20)
+    b = h8_box(6, 5, 4, seed=2, nt=20, h=1.0)
+    with pytest.raises(SvlError) as ei:
+        StructuredEnsemble([((6, 5, 4), (0.0, 0.0, 0.0))] * 2, (2.0, 2.0, 2.0), [a[:2], b[:2]], a[2])
+    assert ei.value.code in (capi.SVL_ERR_INVALID, capi.SVL_ERR_UNSUPPORTED)
