@@ -565,7 +565,10 @@ def main():
 
     cd = make_handle()
     cd.run(1, warm)                                   # warm-up
-    prof = cd.profile(1 + warm, 20) if hasattr(cd, "profile") else None
+    # schedule autotuner of the fused step (svl_cdx_tune): CTA count, tile
+    # order, band block size and stream priority; the state is reset below
+    sched = cd.tune(1 + warm, 5) if hasattr(cd, "tune") else None
+    prof = cd.profile(1 + warm + 200, 20) if hasattr(cd, "profile") else None
     if args.precision == "mixed":
         for b in range(nb):
             cd.Initialize(b)
@@ -707,6 +710,7 @@ def main():
             "fp64_plain": fp64, "implicit_pcg_time_to_1e-8": implicit, "nonlinear_newton_j2": newton,
             "nonlinear_newton_j2_pml": newton_pml,
             "cpu_baseline": cb, "e2e": e2e, "gpu_launches": int(launches) if launches is not None else None,
+            "schedule": sched,
             "clocks": clocks, "finite": finite,
         }
         print(json.dumps(line))

@@ -334,6 +334,21 @@ int  svl_cdx_set_ctas(svl_cdx* cdx, int32_t ctas);
  * the reference (measurement hook). */
 int  svl_cdx_profile(svl_cdx* cdx, int32_t k_first, int32_t nsteps, double* ms_kernel);
 int  svl_cdx_get_ctas(svl_cdx* cdx, int32_t* ctas);
+/* Schedule of a step: choice[0] persistent CTAs of the fused kernel (0 = one
+ * per SM), choice[1] the order in which the CTAs walk the node tiles (0
+ * natural: x fastest, then y, z, instance; 1 instances interleaved; 2 y
+ * fastest; 3 blocks of 2 x 2 x 2 tiles), choice[2] threads per block of the
+ * PML band's element kernels (128 or 256), choice[3] 1 = the band's stream
+ * has the higher priority.  Results do not depend on it.  No counterpart in
+ * the reference. */
+int  svl_cdx_set_schedule(svl_cdx* cdx, const int32_t* choice);
+int  svl_cdx_get_schedule(svl_cdx* cdx, int32_t* choice);
+/* Autotuner: times nsteps steps (from k_first on, after two warm-up steps) of
+ * every schedule in a small grid (three CTA counts, the four tile orders and,
+ * with a PML band, both block sizes and priorities), keeps the fastest and
+ * returns it in choice[4] (*ms_best: its time per step).  The steps advance
+ * the state: set the initial conditions again before the run that counts. */
+int  svl_cdx_tune(svl_cdx* cdx, int32_t k_first, int32_t nsteps, int32_t* choice, float* ms_best);
 void svl_cdx_destroy(svl_cdx* cdx);
 
 /* ---- implicit Newmark (average acceleration), Linear algorithm --------- */

@@ -166,6 +166,9 @@ def lib():
     L.svl_cdx_set_ctas.argtypes = [C.c_void_p, C.c_int32]
     L.svl_cdx_profile.argtypes = [C.c_void_p, C.c_int32, C.c_int32, f64p]
     L.svl_cdx_get_ctas.argtypes = [C.c_void_p, C.POINTER(C.c_int32)]
+    L.svl_cdx_set_schedule.argtypes = [C.c_void_p, i32p]
+    L.svl_cdx_get_schedule.argtypes = [C.c_void_p, i32p]
+    L.svl_cdx_tune.argtypes = [C.c_void_p, C.c_int32, C.c_int32, i32p, C.POINTER(C.c_float)]
     L.svl_cdx_destroy.argtypes = [C.c_void_p]
     L.svl_cdx_destroy.restype = None
     L.svl_cd_run_noalloc.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p]

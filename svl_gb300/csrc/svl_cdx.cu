@@ -191,7 +191,7 @@ struct CdxView {
     int nx, ny, nz, ninst;
     int pitch;                           // floats per padded x-row of the state arrays
     int ntx, nty, ntz, ntiles;
-    const int32_t* __restrict__ tiles;   // ensembles: compact tile -> tile of the full enumeration, or null
+    const int32_t* __restrict__ tiles;   // the schedule: position -> tile of the full enumeration (null: identity)
     float* uh_prev;                      // u_{n-1} (read through TMA), u_{n+1} written here
     float* ul_prev;
     const float* __restrict__ cdof;      // [inst][z][y][pitch]  dt^2/m, 0 on restrained dofs,
@@ -199,7 +199,7 @@ struct CdxView {
     float* fsol;                         // PML nodes: the solid elements' force sum (same layout), or null
     const float* __restrict__ bop;       // [B_ROWS x 24] hi then lo operand image
     // external loads grouped by tile, then by dof
-    const int* __restrict__ tl_ptr;      // [ntiles+1] into the unique-dof arrays
+    const int* __restrict__ tl_ptr;      // [full tiles + 1] into the unique-dof arrays
     const long long* __restrict__ ld_dof;// padded index of the dof
     const int* __restrict__ ld_ptr;      // [nld+1] into ser/coef
     const int* __restrict__ ld_ser;
@@ -417,7 +417,8 @@ k_cdx_step(const __grid_constant__ CUtensorMap tmap_u, const __grid_constant__ C
             const int tile = blockIdx.x + it * gridDim.x;
             const int buf = it & 1;
             const TileOrigin o = tile_origin(v, tile);
-            const int tl0 = v.tl_ptr[tile], tl1 = v.tl_ptr[tile + 1];     // used at the end of the tile
+            const int full = v.tiles ? v.tiles[tile] : tile;              // loads are keyed by the full tile id
+            const int tl0 = v.tl_ptr[full], tl1 = v.tl_ptr[full + 1];     // used at the end of the tile
             const unsigned char* tt = smem + OFF_TT + buf * TT_STRIDE;
             const float* raw = reinterpret_cast<const float*>(tt);
             const float* tlam = reinterpret_cast<const float*>(tt + TT_LAM);
@@ -614,7 +615,6 @@ struct CdpView {
     float* fes;                         // [ninst][8][6][npe]
 };
 
-constexpr int CDP_THREADS = 128;
 // Node rows and element slots are stored component-major ([..][component][node]
 // and [..][local node][component][element]): consecutive threads handle
 // consecutive nodes / elements, so every load and store of a warp is one
@@ -698,7 +698,8 @@ __device__ __forceinline__ constexpr int cdp_scomp(int d, int c) {
 // on the abscissa along d, so the sum over the two points along d acts on the
 // node values first (their sum), and everything else is a 2 x 2 x 2 map
 // over the two other axes (sum factorisation): no per-point 8 x 8 products.
-__global__ void __launch_bounds__(CDP_THREADS, 4) k_cdp_fu(CdpView v) {
+template <int NT>
+__global__ void __launch_bounds__(NT, 512 / NT) k_cdp_fu(CdpView v) {
     const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (gid >= (long long)v.npe) return;
     const int e = (int)gid;
@@ -826,7 +827,8 @@ __global__ void __launch_bounds__(256, 4) k_cdp_uu(CdpView v) {
 // abscissa along d, and the shape functions along d sum to one over its two
 // points, so each term is a 2 x 2 x 2 map over the two other axes whose
 // result is the same at both nodes along d.
-__global__ void __launch_bounds__(CDP_THREADS, 4) k_cdp_fs(CdpView v) {
+template <int NT>
+__global__ void __launch_bounds__(NT, 512 / NT) k_cdp_fs(CdpView v) {
     const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (gid >= (long long)v.npe) return;
     const int e = (int)gid;
@@ -1037,6 +1039,10 @@ struct svl_cdx {
     // longer one, so its stream has the higher priority.
     cudaStream_t bstream = nullptr;
     cudaEvent_t ev_c = nullptr, ev_uu = nullptr, ev_band = nullptr;
+    // schedule (svl_cdx_set_schedule / svl_cdx_tune): tile order of the fused
+    // kernel, block size of the band's element kernels, band stream priority
+    std::vector<int32_t> tiles_base;     // the scheduled tiles in natural order (full ids)
+    int tile_order = 0, band_threads = 128, band_hi = 1;
     cudaEvent_t filled[2] = {nullptr, nullptr}, drained[2] = {nullptr, nullptr};
 
     template <typename T>
@@ -1199,16 +1205,12 @@ static int cdx_create_impl(const svl_grid_spec* g, int32_t ninst, const svl_mode
     if (ntiles > INT32_MAX || h->nstate > ((long long)1 << 40)) { set_error("grid too large"); return fail(SVL_ERR_INVALID); }
     h->ntiles = (int)ntiles;
     std::vector<int32_t> tiles;                      // ensembles: the tiles that meet an instance's own nodes
-    std::vector<int> tile_compact;                   // full tile -> compact index (-1: not scheduled)
     if (ext) {
-        tile_compact.assign((size_t)ntiles, -1);
         for (int b = 0; b < ninst; ++b)
             for (int tz = 0; tz < (ext[3 * b + 2] + TZ - 1) / TZ; ++tz)
                 for (int ty = 0; ty < (ext[3 * b + 1] + TY - 1) / TY; ++ty)
                     for (int tx = 0; tx < (ext[3 * b] + TX - 1) / TX; ++tx) {
-                        const long long full = (((long long)b * h->ntz + tz) * h->nty + ty) * h->ntx + tx;
-                        tile_compact[full] = (int)tiles.size();
-                        tiles.push_back((int32_t)full);
+                        tiles.push_back((int32_t)((((long long)b * h->ntz + tz) * h->nty + ty) * h->ntx + tx));
                     }
         h->ntiles = (int)tiles.size();
     }
@@ -1490,14 +1492,13 @@ static int cdx_create_impl(const svl_grid_spec* g, int32_t ninst, const svl_mode
     auto tile_of = [&](long long gdof) {
         const long long b = gdof / h->ntotal, t = gdof % h->ntotal, n = t2node[t];
         const long long x = n % nxn, y = (n / nxn) % nyn, z = n / ((long long)nxn * nyn);
-        const long long full = (((b * h->ntz + z / TZ) * h->nty + y / TY) * h->ntx + x / TX);
-        return ext ? (long long)tile_compact[full] : full;
+        return (((b * h->ntz + z / TZ) * h->nty + y / TY) * h->ntx + x / TX);
     };
     std::stable_sort(order.begin(), order.end(), [&](int a, int c) {
         const long long ta = tile_of(fdof[a]), tc = tile_of(fdof[c]);
         return ta < tc || (ta == tc && fdof[a] < fdof[c]);
     });
-    std::vector<int> tl_ptr(h->ntiles + 1, 0), ld_ptr(1, 0), ld_ser;
+    std::vector<int> tl_ptr((size_t)ntiles + 1, 0), ld_ptr(1, 0), ld_ser;
     std::vector<long long> ld_dof;
     std::vector<double> ld_coef;
     long long last = -1;
@@ -1513,7 +1514,7 @@ static int cdx_create_impl(const svl_grid_spec* g, int32_t ninst, const svl_mode
         ld_coef.push_back(fcoef[j2]);
     }
     if (last >= 0) ld_ptr.push_back((int)ld_ser.size());
-    for (int t = 0; t < h->ntiles; ++t) tl_ptr[t + 1] += tl_ptr[t];
+    for (long long t = 0; t < ntiles; ++t) tl_ptr[t + 1] += tl_ptr[t];
 
     int st;
     const size_t ns = (size_t)h->nstate;
@@ -1526,6 +1527,11 @@ static int cdx_create_impl(const svl_grid_spec* g, int32_t ninst, const svl_mode
         (st = h->upload(s_ptr, &h->s_ptr)) || (st = h->upload(s_val, &h->s_val)))
         return fail(st);
     if (ext && (st = h->upload(tiles, &h->d_tiles))) return fail(st);
+    if (ext) h->tiles_base = tiles;
+    else {
+        h->tiles_base.resize((size_t)h->ntiles);
+        for (int t = 0; t < h->ntiles; ++t) h->tiles_base[t] = t;
+    }
     // history map: the instances one after the other, each in its own numbering
     {
         if (emb) h->own2emb = *emb;
@@ -1777,11 +1783,18 @@ static CdpView cdp_view(svl_cdx* h) {
 // or per PML node, each looping over the instances (their tables are read
 // once).
 static void cdp_launch(svl_cdx* h, const CdpView& c, int which, cudaStream_t st) {
-    const unsigned be = (unsigned)((h->npe + CDP_THREADS - 1) / CDP_THREADS), bn = (unsigned)((h->np + 255) / 256);
+    const int nt = h->band_threads;
+    const unsigned be = (unsigned)((h->npe + nt - 1) / nt), bn = (unsigned)((h->np + 255) / 256);
     switch (which) {
-        case 0: k_cdp_fu<<<be, CDP_THREADS, 0, st>>>(c); break;
+        case 0:
+            if (nt == 256) k_cdp_fu<256><<<be, 256, 0, st>>>(c);
+            else k_cdp_fu<128><<<be, 128, 0, st>>>(c);
+            break;
         case 1: k_cdp_uu<<<bn, 256, 0, st>>>(c); break;
-        case 2: k_cdp_fs<<<be, CDP_THREADS, 0, st>>>(c); break;
+        case 2:
+            if (nt == 256) k_cdp_fs<256><<<be, 256, 0, st>>>(c);
+            else k_cdp_fs<128><<<be, 128, 0, st>>>(c);
+            break;
         default: k_cdp_su<<<bn, 256, 0, st>>>(c); break;
     }
     ++h->launches;
@@ -2032,6 +2045,94 @@ int svl_cdx_set_ctas(svl_cdx* h, int32_t ctas) {
 int svl_cdx_get_ctas(svl_cdx* h, int32_t* ctas) {
     if (!h || !ctas) { set_error("bad argument"); return SVL_ERR_INVALID; }
     *ctas = h->grid;
+    return SVL_OK;
+}
+
+// The scheduled tiles in one of the orders the tuner tries: 0 natural
+// (x fastest, then y, z, instance), 1 instances interleaved (tile position
+// first), 2 y fastest, 3 2 x 2 x 2 blocks of tiles.
+static std::vector<int32_t> tile_schedule(const svl_cdx* h, int order) {
+    std::vector<int32_t> t = h->tiles_base;
+    auto key = [&](int32_t full) {
+        long long r = full;
+        const long long tx = r % h->ntx; r /= h->ntx;
+        const long long ty = r % h->nty; r /= h->nty;
+        const long long tz = r % h->ntz, b = r / h->ntz;
+        const long long X = h->ntx, Y = h->nty, Z = h->ntz, B = h->ninst;
+        switch (order) {
+            case 1: return ((tz * Y + ty) * X + tx) * B + b;
+            case 2: return ((b * Z + tz) * X + tx) * Y + ty;
+            case 3: return ((((b * Z + tz / 2) * Y + ty / 2) * X + tx / 2) * 2 + tz % 2) * 4 + (ty % 2) * 2 + tx % 2;
+            default: return (long long)full;
+        }
+    };
+    std::stable_sort(t.begin(), t.end(), [&](int32_t a, int32_t c) { return key(a) < key(c); });
+    return t;
+}
+
+int svl_cdx_set_schedule(svl_cdx* h, const int32_t* choice) {
+    if (!h || !choice) { set_error("bad argument"); return SVL_ERR_INVALID; }
+    if (choice[1] < 0 || choice[1] > 3 || (choice[2] != 128 && choice[2] != 256) || choice[3] < 0 || choice[3] > 1) {
+        set_error("schedule out of range"); return SVL_ERR_INVALID;
+    }
+    TRY(svl_cdx_set_ctas(h, choice[0]));
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    if (h->bstream) CUDA_TRY(cudaStreamSynchronize(h->bstream));
+    if (choice[1] != h->tile_order) {
+        const std::vector<int32_t> t = tile_schedule(h, choice[1]);
+        if (!h->d_tiles) TRY(h->alloc(t.size(), &h->d_tiles));
+        CUDA_TRY(cudaMemcpy(h->d_tiles, t.data(), t.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+        h->tile_order = choice[1];
+    }
+    h->band_threads = choice[2];
+    if (choice[3] != h->band_hi) {
+        int lo_pri = 0, hi_pri = 0;
+        CUDA_TRY(cudaDeviceGetStreamPriorityRange(&lo_pri, &hi_pri));
+        CUDA_TRY(cudaStreamDestroy(h->bstream));
+        h->bstream = nullptr;
+        CUDA_TRY(cudaStreamCreateWithPriority(&h->bstream, cudaStreamNonBlocking, choice[3] ? hi_pri : lo_pri));
+        h->band_hi = choice[3];
+    }
+    return SVL_OK;
+}
+
+int svl_cdx_get_schedule(svl_cdx* h, int32_t* choice) {
+    if (!h || !choice) { set_error("bad argument"); return SVL_ERR_INVALID; }
+    choice[0] = h->grid; choice[1] = h->tile_order; choice[2] = h->band_threads; choice[3] = h->band_hi;
+    return SVL_OK;
+}
+
+int svl_cdx_tune(svl_cdx* h, int32_t k_first, int32_t nsteps, int32_t* choice, float* ms_best) {
+    if (!h || !choice || nsteps <= 0) { set_error("bad argument"); return SVL_ERR_INVALID; }
+    int dev = 0, sms = 0;
+    CUDA_TRY(cudaGetDevice(&dev));
+    CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    std::vector<int> ctas;
+    for (int c : {sms, sms - sms / 16, sms - sms / 8}) {
+        c = std::max(1, std::min(c, h->ntiles));                  // as svl_cdx_set_ctas clamps it
+        if (std::find(ctas.begin(), ctas.end(), c) == ctas.end()) ctas.push_back(c);
+    }
+    std::vector<int> bt = {128}, bh = {1};
+    if (h->np > 0) { bt.push_back(256); bh.push_back(0); }
+    float best = 0.f;
+    int32_t bc[4] = {0, 0, 128, 1};
+    int k = k_first;
+    for (int c : ctas)
+        for (int o = 0; o < 4; ++o)
+            for (int t : bt)
+                for (int p : bh) {
+                    const int32_t ch[4] = {c, o, t, p};
+                    TRY(svl_cdx_set_schedule(h, ch));
+                    for (int w = 0; w < 2; ++w) TRY(cdx_step(h, k++, false));   // warm the choice
+                    float ms = 0.f;
+                    TRY(svl_cdx_run_timed(h, k, nsteps, &ms));
+                    k += nsteps;
+                    if (best == 0.f || ms < best) { best = ms; std::copy(ch, ch + 4, bc); }
+                }
+    TRY(svl_cdx_set_schedule(h, bc));
+    std::copy(bc, bc + 4, choice);
+    if (ms_best) *ms_best = best / (float)nsteps;
+    h->va_valid = false;
     return SVL_OK;
 }
 

@@ -189,6 +189,29 @@ class StructuredCentralDifference:
         check(lib().svl_cdx_profile(self._h, int(k_first), int(nsteps), ptr(out, C.c_double)))
         return out
 
+    SCHEDULE_KEYS = ("ctas", "tile_order", "band_threads", "band_stream_high_priority")
+
+    def schedule(self) -> dict:
+        ch = np.zeros(4, np.int32)
+        check(lib().svl_cdx_get_schedule(self._h, ptr(ch, C.c_int32)))
+        return dict(zip(self.SCHEDULE_KEYS, (int(x) for x in ch)))
+
+    def set_schedule(self, **kw):
+        cur = self.schedule()
+        cur.update(kw)
+        ch = np.array([cur[k] for k in self.SCHEDULE_KEYS], np.int32)
+        check(lib().svl_cdx_set_schedule(self._h, ptr(ch, C.c_int32)))
+
+    def tune(self, k_first: int, nsteps: int = 5) -> dict:
+        """Times a small grid of schedules and keeps the fastest (svl_cdx_tune);
+        the state advances: Initialize again afterwards."""
+        ch = np.zeros(4, np.int32)
+        ms = C.c_float()
+        check(lib().svl_cdx_tune(self._h, int(k_first), int(nsteps), ptr(ch, C.c_int32), C.byref(ms)))
+        out = dict(zip(self.SCHEDULE_KEYS, (int(x) for x in ch)))
+        out["ms_per_step"] = float(ms.value)
+        return out
+
     def set_ctas(self, ctas: int) -> int:
         """CTAs of the persistent step kernel (0 = one per SM); returns the
         grid size in effect."""

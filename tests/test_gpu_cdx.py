@@ -224,3 +224,33 @@ def test_ensemble_rejects_mismatched_element_size(gpu):
     with pytest.raises(SvlError) as ei:
         StructuredEnsemble([((6, 5, 4), (0.0, 0.0, 0.0))] * 2, (2.0, 2.0, 2.0), [a[:2], b[:2]], a[2])
     assert ei.value.code in (capi.SVL_ERR_INVALID, capi.SVL_ERR_UNSUPPORTED)
+
+
+def test_schedules_give_identical_results_and_tuner_keeps_one(gpu):
+    """Every schedule (tile order, CTA count, band block size and stream
+    priority) gives the same bits: the per-node sums keep their element
+    order whatever tile a CTA takes next.  The tuner returns a valid
+    schedule and leaves it in effect."""
+    nx, ny, nz, npml = 16, 16, 12, 3
+    nt = 40
+    inst, dt = _pml_instances(nx, ny, nz, npml, (1, 2), nt)
+    cdx = StructuredCentralDifference((nx, ny, nz), (2.0, 2.0, 2.0), inst, dt)
+    ref = None
+    for sched in ({}, dict(tile_order=1, band_threads=256), dict(tile_order=2, ctas=7, band_stream_high_priority=0),
+                  dict(tile_order=3, ctas=3, band_threads=128)):
+        if sched:
+            cdx.set_schedule(**sched)
+        for b in range(len(inst)):
+            cdx.Initialize(b)
+        hist = cdx.run(1, nt, history=True)
+        if ref is None:
+            ref = hist
+        else:
+            assert np.array_equal(hist, ref), sched
+    best = cdx.tune(1, 3)
+    assert best["tile_order"] in (0, 1, 2, 3) and best["band_threads"] in (128, 256) and best["ms_per_step"] > 0
+    assert {k: best[k] for k in cdx.SCHEDULE_KEYS} == cdx.schedule()
+    for b in range(len(inst)):
+        cdx.Initialize(b)
+    assert np.array_equal(cdx.run(1, nt, history=True), ref)
+    cdx.close()
