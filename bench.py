@@ -319,6 +319,37 @@ def implicit_pcg(steps=500, warm=100, tol=1e-8):
             "rel_l2_final_u_learned_vs_jacobi": float(np.linalg.norm(Ul - Uj) / max(np.linalg.norm(Uj), 1e-300))}
 
 
+def uneven_ensemble(steps=200, warm=20):
+    """Instances of uneven grids in one fused launch per step
+    (svl_cdx_create_ensemble) against the same instances advanced one handle
+    each: four config-2 style boxes (no PML band) of different sizes."""
+    from svl_gb300 import StructuredCentralDifference, StructuredEnsemble, workloads
+    shapes = [(128, 128, 64), (96, 128, 48), (112, 80, 64), (64, 64, 32)]
+    inst = [workloads.config2(*s, seed=20 + b, nt=steps + warm + 10) for b, s in enumerate(shapes)]
+    dt = min(d for _, _, d in inst)
+    pairs = [(m, L) for m, L, _ in inst]
+    ndof = sum(free_disp_dofs(m) for m, _ in pairs)
+    ens = StructuredEnsemble([(s, (0.0, 0.0, 0.0)) for s in shapes], (2.0, 2.0, 2.0), pairs, dt)
+    sched = ens.tune(1, 5)
+    for b in range(len(pairs)):
+        ens.Initialize(b)
+    ens.run(1, warm)
+    ms_ens = ens.run_timed(1 + warm, steps) / steps
+    ens.close()
+    ms_one = 0.0
+    for s, pr in zip(shapes, pairs):
+        one = StructuredCentralDifference(s, (2.0, 2.0, 2.0), [pr], dt)
+        one.Initialize(0)
+        one.run(1, warm)
+        ms_one += one.run_timed(1 + warm, steps) / steps
+        one.close()
+    return {"workload": "4 lin3DHexa8 boxes %s (h=2 m, log-normal Vs), fixed bottom, roller sides, one fused "
+                        "launch per step" % ", ".join("x".join(map(str, s)) for s in shapes),
+            "free_dof": ndof, "steps": steps, "ms_per_step": ms_ens, "value": ndof / (ms_ens / 1e3),
+            "unit": "DOF-steps/s", "separate_handles_ms_per_step": ms_one,
+            "speedup_over_separate_handles": ms_one / ms_ens, "schedule": sched}
+
+
 def nonlinear_newton(steps=8, warm=4, tol=1e-8, size=(64, 64, 32), n_j2=8):
     """Newmark + NewtonRaphson (3 iterations per step, test 4 disabled by
     cnvgtol = 0, as in the configuration) on the config-5 style model at a
@@ -502,6 +533,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64-compare", action="store_true")
+    ap.add_argument("--no-ensemble", action="store_true", help="skip the uneven-ensemble leg")
     ap.add_argument("--implicit-steps", type=int, default=None,
                     help="Newmark steps of the 64^3 implicit workload timed beside the headline "
                          "(default 500, the configured run, with the default workload, else 0)")
@@ -680,6 +712,9 @@ def main():
     implicit = (implicit_pcg(args.implicit_steps, warm=min(100, max(1, args.implicit_steps // 5)))
                 if (rank == 0 and args.implicit_steps > 1) else None)
     newton = nonlinear_newton() if (rank == 0 and args.implicit_steps > 0 and args.workload == "config2") else None
+    ensemble = None
+    if rank == 0 and args.precision == "mixed" and args.workload == "config2" and not args.no_ensemble:
+        ensemble = uneven_ensemble()
     newton_pml = None
     if rank == 0 and args.implicit_steps > 0 and args.workload == "config2":
         # the config-5 model with its PML half-space at 64x64x32 (3 steps); a
@@ -710,7 +745,7 @@ def main():
             "fp64_plain": fp64, "implicit_pcg_time_to_1e-8": implicit, "nonlinear_newton_j2": newton,
             "nonlinear_newton_j2_pml": newton_pml,
             "cpu_baseline": cb, "e2e": e2e, "gpu_launches": int(launches) if launches is not None else None,
-            "schedule": sched,
+            "schedule": sched, "uneven_ensemble": ensemble,
             "clocks": clocks, "finite": finite,
         }
         print(json.dumps(line))
