@@ -679,7 +679,7 @@ def main():
         # page-locked host buffer (allocated once, outside the timed region)
         from svl_gb300 import pinned_empty
         ne2e = E2E_STEPS[args.workload]
-        chunk = 10 if args.precision == "mixed" else (ne2e if args.workload == "config1" else 200)
+        chunk = 20 if args.precision == "mixed" else (ne2e if args.workload == "config1" else 200)
         hbuf = pinned_empty((chunk, nb, m.ntotal) if args.precision == "mixed" else (chunk, m.ntotal))
         t0 = time.perf_counter()
         cd2 = make_handle()                             # host arrays -> device

@@ -31,6 +31,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <thread>
 #include <vector>
 
 #include "svl_internal.hpp"
@@ -1246,11 +1247,32 @@ static int cdx_create_impl(const svl_grid_spec* g, int32_t ninst, const svl_mode
     std::vector<double> fcoef;
     std::vector<int> s_ptr(1, 0);
     std::vector<double> s_val;
+    // the per-instance host work (model, checks, lumped masses, the explicit
+    // PML scheme's tables) runs on one thread per instance
+    std::vector<HostModel> hms(ninst);
+    std::vector<std::vector<double>> masses(ninst);
+    std::vector<ExplicitPmlTables> ptabs(ninst);
+    std::vector<int> pst(ninst, SVL_OK);
+    {
+        auto work = [&](int b) {
+            HostModel& m = hms[b];
+            if (!model_from_desc(&models[b], m)) { pst[b] = SVL_ERR_INVALID; return; }
+            if ((pst[b] = cdx_check_instance(g, m, b))) return;
+            lumped_mass_diag(m, opts->mtol, masses[b]);
+            if (m.has_pml()) {
+                LoadTables lt;
+                if ((pst[b] = build_load_tables(m, loads ? &loads[b] : nullptr, lt))) return;
+                pst[b] = explicit_pml_tables(m, opts->dt, opts->mtol, lt, ptabs[b]);
+            }
+        };
+        std::vector<std::thread> th;
+        for (int b = 0; b < ninst; ++b) th.emplace_back(work, b);
+        for (auto& t : th) t.join();
+    }
     for (int b = 0; b < ninst; ++b) {
-        HostModel m;
-        if (!model_from_desc(&models[b], m)) return fail(SVL_ERR_INVALID);
-        int st = cdx_check_instance(g, m, b);
-        if (st) return fail(st);
+        if (pst[b]) return fail(pst[b]);
+        HostModel& m = hms[b];
+        int st = SVL_OK;
         if (b == 0) {
             // numbering maps and the PML band layout, shared by every instance
             h->ntotal = m.ntotal;
@@ -1330,10 +1352,7 @@ static int cdx_create_impl(const svl_grid_spec* g, int32_t ninst, const svl_mode
         }
         if (h->np > 0) {
             // explicit scheme tables of this instance (lumped blocks, solves)
-            LoadTables lt;
-            if ((st = build_load_tables(m, loads ? &loads[b] : nullptr, lt))) return fail(st);
-            ExplicitPmlTables T;
-            if ((st = explicit_pml_tables(m, opts->dt, opts->mtol, lt, T))) return fail(st);
+            const ExplicitPmlTables& T = ptabs[b];
             const double dt = opts->dt;
             static const int pk[9][2] = {{0, 0}, {1, 1}, {2, 2}, {0, 1}, {1, 2}, {0, 2}, {3, 3}, {4, 4}, {5, 5}};
             for (long long n = 0; n < h->nn; ++n) {
@@ -1434,8 +1453,7 @@ static int cdx_create_impl(const svl_grid_spec* g, int32_t ninst, const svl_mode
             lam[li] = pml_e ? 0.f : (float)(E * nu / (1.0 - 2.0 * nu) / (1.0 + nu));
             mu[li] = pml_e ? 0.f : (float)(E / (2.0 * (1.0 + nu)));
         }
-        std::vector<double> M;
-        lumped_mass_diag(m, opts->mtol, M);
+        const std::vector<double>& M = masses[b];
         for (long long n = 0; n < h->nn; ++n)
             for (int c = 0; c < 3; ++c) {
                 const long long t = m.tdof_all[(size_t)n * m.dstride + c];
