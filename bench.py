@@ -684,12 +684,15 @@ def main():
         t0 = time.perf_counter()
         cd2 = make_handle()                             # host arrays -> device
         t1 = time.perf_counter()
+        call_ms = []
         for s0 in range(0, ne2e, chunk):
             n = min(chunk, ne2e - s0)
+            tc = time.perf_counter()
             if args.precision == "mixed" or not pml:
                 cd2.run(1 + s0, n, out=hbuf[:n])
             else:                                       # the FP64 PML handle copies its history itself
                 hbuf[:n] = cd2.run(1 + s0, n, history=True)
+            call_ms.append((time.perf_counter() - tc) * 1e3 / n)
         t2 = time.perf_counter()
         cd2.close()
         md_bytes = nb * (m.coords.nbytes + m.totaldof.nbytes + m.freedof.nbytes + m.conn.nbytes +
@@ -701,6 +704,8 @@ def main():
                "steps": ne2e, "create_seconds": t1 - t0, "run_seconds": t2 - t1,
                "run_only_value": ws * nfree_total * ne2e / (t2 - t1),
                "chunk_steps": chunk,
+               "call_ms_per_step_p10_p50_p90": [float(x) for x in np.percentile(call_ms, [10, 50, 90])],
+               "first_call_ms_per_step": float(call_ms[0]),
                "includes": "handle creation from host arrays (model, loads) + the whole run with every instance's "
                            "full total-dof vector (displacements and PML stress dofs) copied to page-locked host "
                            "memory every step"}
