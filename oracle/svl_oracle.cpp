@@ -1437,6 +1437,133 @@ void pml_matrices(int nd, const double* X, double E, double nu, double rho, doub
  * step (PML3DHexa8.cpp:716-742 with zero node increments after UpdateDomain).
  * With J2 elements K is re-assembled with their current tangents at every
  * iteration (Rayleigh C keeps the initial stiffness). */
+// CentralDifference with a non-diagonal K = 1/dt/dt*M + 1/2/dt*C
+// (CentralDifference.cpp:64-151, K at :70): a consistent mass (massform
+// Consistent, lin2DQuad4.cpp:243-285 / lin3DHexa8.cpp:243-285 without the
+// lumping branch) or stiffness-proportional Rayleigh damping.  M and C are
+// assembled in element order with the tolerance filters, T^T K T is factorised
+// once (dense LDL^T: SimplicialLDLT with its factor-once flag,
+// EigenSolver.cpp:19-59) and every step solves it for
+// T^T [Fext(k) - Fint + (1/dt/dt*M - 1/2/dt*C)(U - Up)] (:206-221); support
+// motion adds -T^T K SM (:190-202).
+struct CDGen {
+    Sim s; double dt = 0;
+    std::vector<double> U, V, A, Up, Us;
+    CSR Mt, Ct;
+    int nf = 0;
+    std::vector<double> L, D;            // T^T K T = L D L^T, L unit lower [nf][nf]
+
+    static bool needed(const Model& m) {
+        if (!m.lumped) return true;
+        for (size_t e = 0; e < m.ray.size() / 2; ++e) if (m.ray[2 * e + 1] != 0.0) return true;
+        return false;
+    }
+    bool init(const svl_model_desc* d, const svl_load_desc* l, double dt_, double ftol, double mtol) {
+        if (!s.init(d, l)) return false;
+        if (!s.m.epml.empty()) return false;
+        dt = dt_; s.ftol = ftol; s.mtol = mtol;
+        const Model& m = s.m;
+        const int nt = m.ntotal, nc = m.nen * m.ndof;
+        U.assign(nt, 0); V.assign(nt, 0); A.assign(nt, 0); Up.assign(nt, 0); Us.assign(nt, 0);
+        std::vector<Trip> tm, tc;
+        std::vector<double> Me((size_t)nc * nc), K0((size_t)nc * nc);
+        for (int e = 0; e < m.nelem; ++e) {
+            s.element_M(e, Me.data(), m.lumped != 0);
+            const int* ed = &s.edofs[(size_t)e * nc];
+            for (int j = 0; j < nc; ++j)
+                for (int i = 0; i < nc; ++i) {
+                    const double v = Me[(size_t)i * nc + j];
+                    if (std::fabs(v) > s.mtol) tm.push_back({ed[i], ed[j], v});
+                }
+            const double am = m.ray.empty() ? 0.0 : m.ray[2 * e], ak = m.ray.empty() ? 0.0 : m.ray[2 * e + 1];
+            if (am == 0.0 && ak == 0.0) continue;
+            if (ak != 0.0) s.element_K0(e, K0.data());
+            for (int j = 0; j < nc; ++j)
+                for (int i = 0; i < nc; ++i) {
+                    const double v = am * Me[(size_t)i * nc + j] + (ak != 0.0 ? ak * K0[(size_t)i * nc + j] : 0.0);
+                    if (std::fabs(v) > s.ktol) tc.push_back({ed[i], ed[j], v});
+                }
+        }
+        if (!m.nodemass.empty())
+            for (int t = 0; t < nt; ++t) if (std::fabs(m.nodemass[t]) > s.mtol) tm.push_back({t, t, m.nodemass[t]});
+        for (size_t i = 0; i < m.dp_eta.size(); ++i) {
+            const int a = m.dp_dof[2 * i], b = m.dp_dof[2 * i + 1];
+            const double eta = m.dp_eta[i];
+            if (!(std::fabs(eta) > s.ktol)) continue;
+            tc.push_back({a, a, eta}); tc.push_back({b, a, -eta}); tc.push_back({a, b, -eta}); tc.push_back({b, b, eta});
+        }
+        csr_from_triplets(nt, tm, Mt);
+        csr_from_triplets(nt, tc, Ct);
+        // dense T^T K T and its factorisation
+        nf = m.nfree;
+        L.assign((size_t)nf * nf, 0.0);
+        auto addK = [&](const CSR& Mx, double c) {
+            for (int r = 0; r < nt; ++r)
+                for (int p = Mx.ptr[r]; p < Mx.ptr[r + 1]; ++p) {
+                    const int col = Mx.col[p];
+                    const double v = c * Mx.val[p];
+                    for (int i = s.Tptr[r]; i < s.Tptr[r + 1]; ++i)
+                        for (int j = s.Tptr[col]; j < s.Tptr[col + 1]; ++j)
+                            L[(size_t)s.Tcol[i] * nf + s.Tcol[j]] += s.Tval[i] * v * s.Tval[j];
+                }
+        };
+        addK(Mt, 1.0 / dt / dt);
+        addK(Ct, 1.0 / 2.0 / dt);
+        D.assign(nf, 0.0);
+        for (int j = 0; j < nf; ++j) {
+            double dj = L[(size_t)j * nf + j];
+            for (int k = 0; k < j; ++k) dj -= L[(size_t)j * nf + k] * L[(size_t)j * nf + k] * D[k];
+            if (!(dj > 0.0) || !std::isfinite(dj)) return false;
+            D[j] = dj;
+            for (int i = j + 1; i < nf; ++i) {
+                double v = L[(size_t)i * nf + j];
+                for (int k = 0; k < j; ++k) v -= L[(size_t)i * nf + k] * L[(size_t)j * nf + k] * D[k];
+                L[(size_t)i * nf + j] = v / dj;
+            }
+        }
+        return true;
+    }
+    void set_initial(const double* U0, const double* V0, const double* A0) {
+        for (int t = 0; t < s.m.ntotal; ++t) {
+            U[t] = U0 ? U0[t] : 0.0; V[t] = V0 ? V0[t] : 0.0; A[t] = A0 ? A0[t] : 0.0;
+            Up[t] = U[t] - dt * V[t] + dt * dt / 2.0 * A[t];
+        }
+    }
+    void step(int k) {
+        const int nt = s.m.ntotal;
+        std::vector<double> Fint, Fext, w(nt), Mw, Cw, R(nt), Feff, SM, Ksm(nt), MS, CS, lg, dUt;
+        s.assemble_fint(Fint);
+        s.fext(k, Fext);
+        for (int t = 0; t < nt; ++t) w[t] = U[t] - Up[t];
+        csr_mv(Mt, w, Mw);
+        csr_mv(Ct, w, Cw);
+        for (int t = 0; t < nt; ++t) R[t] = (Fext[t] + 0.0 - Fint[t]) + (1.0 / dt / dt * Mw[t] - 1.0 / 2.0 / dt * Cw[t]);
+        s.TT_apply(R, Feff);
+        s.support_increment(k, SM);
+        csr_mv(Mt, SM, MS);
+        csr_mv(Ct, SM, CS);
+        for (int t = 0; t < nt; ++t) Ksm[t] = 1.0 / dt / dt * MS[t] + 1.0 / 2.0 / dt * CS[t];
+        s.TT_apply(Ksm, lg);
+        for (int f = 0; f < nf; ++f) Feff[f] -= lg[f];
+        // L D L^T du = Feff
+        std::vector<double> du(Feff);
+        for (int i = 0; i < nf; ++i) for (int k2 = 0; k2 < i; ++k2) du[i] -= L[(size_t)i * nf + k2] * du[k2];
+        for (int i = 0; i < nf; ++i) du[i] /= D[i];
+        for (int i = nf - 1; i >= 0; --i) for (int k2 = i + 1; k2 < nf; ++k2) du[i] -= L[(size_t)k2 * nf + i] * du[k2];
+        s.T_apply(du, dUt);
+        for (int t = 0; t < nt; ++t) Us[t] = U[t] + dUt[t];
+        for (int e = 0; e < s.m.nelem; ++e) s.element_update(e, Us);
+        for (int t = 0; t < nt; ++t) {
+            const double dU = dUt[t] + SM[t];
+            V[t] = 1.0 / 2.0 / dt * (U[t] + dU - Up[t]);
+            A[t] = 1.0 / dt / dt * (dU - U[t] + Up[t]);
+            Up[t] = U[t];
+            U[t] += dU;
+        }
+        s.commit_all();
+    }
+};
+
 struct XNewmark {
     Sim s; double dt;
     std::vector<double> U, V, A, Ubar;
@@ -2137,6 +2264,28 @@ int oracle_cd_run(const svl_model_desc* model, const svl_load_desc* loads, doubl
                   double ftol, double mtol, int k_first, int nsteps, int mode,
                   const double* U0, const double* V0, const double* A0,
                   double* hist_U, double* U_out, double* V_out, double* A_out, double* step_seconds) {
+    {
+        // a consistent mass or stiffness-proportional damping: the factorised
+        // non-diagonal K (CDGen), one faithful mode
+        Model probe;
+        if (!load_model(model, probe)) return SVL_ERR_INVALID;
+        if (probe.epml.empty() && CDGen::needed(probe)) {
+            CDGen g;
+            if (!g.init(model, loads, dt, ftol, mtol)) return SVL_ERR_INVALID;
+            g.set_initial(U0, V0, A0);
+            const int nt = g.s.m.ntotal;
+            const auto t0 = std::chrono::steady_clock::now();
+            for (int i = 0; i < nsteps; ++i) {
+                g.step(k_first + i);
+                if (hist_U) std::memcpy(hist_U + (size_t)i * nt, g.U.data(), sizeof(double) * nt);
+            }
+            if (step_seconds) step_seconds[0] = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+            if (U_out) std::memcpy(U_out, g.U.data(), sizeof(double) * nt);
+            if (V_out) std::memcpy(V_out, g.V.data(), sizeof(double) * nt);
+            if (A_out) std::memcpy(A_out, g.A.data(), sizeof(double) * nt);
+            return 0;
+        }
+    }
     CD cd;
     if (!cd.init(model, loads, dt, ftol, mtol)) return SVL_ERR_INVALID;
     cd.set_initial(U0, V0, A0);
