@@ -380,6 +380,21 @@ void svl_cdx_destroy(svl_cdx* cdx);
 #define SVL_ALGO_NEWTON     1   /* NewtonRaphson.cpp:24-75: tangent iterations    */
 #define SVL_PRECOND_JACOBI  0
 #define SVL_PRECOND_LEARNED 1   /* see svl_nm_train_preconditioner                */
+/* svl_nm_opts.integrator.  SVL_NM_CENTRAL_DIFFERENCE: CentralDifference with
+ * an effective stiffness K = M/dt^2 + C/2dt that is not diagonal -- a
+ * consistent mass (massform CONSISTENT) and/or stiffness-proportional
+ * Rayleigh damping (ak != 0) -- which the reference factorises once and
+ * solves every step (CentralDifference.cpp:64-70, 122-152, 204-231).  Here the
+ * same Jacobi-PCG applies K element by element: sum_e (1/dt^2 + am_e/2dt)
+ * M_e p_e + (ak_e/2dt) K0_e p_e plus the nodal masses / dt^2, stopping on
+ * the true relative residual <= pcg_tol.  Step: Feff = Fext - Fint +
+ * (M/dt^2 - C/2dt)(U - Up), solve, V = (U + dU - Up)/2dt, A = (dU - U +
+ * Up)/dt^2, Up = U, U += dU.  Covered: elastic materials, identity T, no
+ * support motion, dashpots or domain-reduction loads (SVL_ERR_UNSUPPORTED
+ * otherwise); algorithm must be SVL_ALGO_LINEAR and precond Jacobi.  A
+ * lumped mass without ak is the diagonal path of svl_cd_create. */
+#define SVL_NM_NEWMARK            0
+#define SVL_NM_CENTRAL_DIFFERENCE 1
 typedef struct svl_nm_opts {
     double  dt;
     double  ftol;        /* force assembly tolerance (as svl_cd_opts)             */
@@ -401,6 +416,7 @@ typedef struct svl_nm_opts {
                             operator -- the true residual -- and the solve
                             restarts from it until pcg_tol holds, so the result
                             keeps the FP64 tolerance.  0: FP64 throughout.      */
+    int32_t integrator;  /* SVL_NM_NEWMARK (0) or SVL_NM_CENTRAL_DIFFERENCE     */
 } svl_nm_opts;
 
 typedef struct svl_nm svl_nm;

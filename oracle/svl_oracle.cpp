@@ -2425,7 +2425,15 @@ int oracle_element_response_run(const svl_model_desc* model, const svl_load_desc
         const int per = response == 2 ? s.m.nen * s.m.ndof : s.m.ngp * (s.m.ndim == 2 ? 3 : 6);
         for (int i = 0; i < nlist; ++i) s.element_response(elems[i], response, out + (size_t)i * per);
     };
-    if (integrator == 0) {
+    Model probe;
+    if (!load_model(model, probe)) return SVL_ERR_INVALID;
+    if (integrator == 0 && probe.epml.empty() && CDGen::needed(probe)) {
+        CDGen g;                            // non-diagonal K (consistent mass or ak != 0)
+        if (!g.init(model, loads, dt, 1e-12, 1e-12)) return SVL_ERR_INVALID;
+        g.set_initial(nullptr, nullptr, nullptr);
+        for (int i = 0; i < nsteps; ++i) g.step(k_first + i);
+        emit(g.s);
+    } else if (integrator == 0) {
         CD cd;
         if (!cd.init(model, loads, dt, 1e-12, 1e-12)) return SVL_ERR_INVALID;
         cd.set_initial(nullptr, nullptr, nullptr);

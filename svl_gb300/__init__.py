@@ -6,8 +6,8 @@ Python binding: model/load containers, the structured-grid generator, and a
 mirror of the reference's Integrator interface.
 """
 from ._capi import SvlError, lib, pinned_empty  # noqa: F401
-from .integrators import (CentralDifference, ExtendedNewmarkBeta, NewmarkBeta, StructuredCentralDifference,  # noqa: F401
-                          StructuredEnsemble)
+from .integrators import (CentralDifference, CentralDifferenceSolve, ExtendedNewmarkBeta, NewmarkBeta,  # noqa: F401
+                          StructuredCentralDifference, StructuredEnsemble)
 from .model import Loads, Model, elastic_params, j2_params, ricker  # noqa: F401
 
-__all__ = ["CentralDifference", "ExtendedNewmarkBeta", "NewmarkBeta", "StructuredCentralDifference", "StructuredEnsemble", "Loads", "Model", "SvlError", "lib", "pinned_empty", "ricker", "elastic_params", "j2_params"]
+__all__ = ["CentralDifference", "CentralDifferenceSolve", "ExtendedNewmarkBeta", "NewmarkBeta", "StructuredCentralDifference", "StructuredEnsemble", "Loads", "Model", "SvlError", "lib", "pinned_empty", "ricker", "elastic_params", "j2_params"]

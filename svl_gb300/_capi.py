@@ -90,7 +90,12 @@ SVL_ALGO_NEWTON = 1
 class NmOpts(C.Structure):
     _fields_ = [("dt", C.c_double), ("ftol", C.c_double), ("mtol", C.c_double), ("pcg_tol", C.c_double),
                 ("pcg_maxit", C.c_int32), ("precond", C.c_int32), ("algorithm", C.c_int32), ("maxit", C.c_int32),
-                ("cnvgtol", C.c_double), ("cnvgtest", C.c_int32), ("single_inner", C.c_int32)]
+                ("cnvgtol", C.c_double), ("cnvgtest", C.c_int32), ("single_inner", C.c_int32),
+                ("integrator", C.c_int32)]
+
+
+SVL_NM_NEWMARK = 0
+SVL_NM_CENTRAL_DIFFERENCE = 1
 
 
 class XnmOpts(C.Structure):

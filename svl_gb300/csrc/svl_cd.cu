@@ -660,11 +660,14 @@ __device__ __forceinline__ double gather_block(const DevView& d, const double* _
 
 // Consistent mass action of every element, M_e = rho sum_q w t |J| N_a N_b on
 // each displacement component (lin2DQuad4.cpp:243-285 and lin3DHexa8.cpp:
-// 243-285 without the lumping branch): fe = scale M_e x_e, or fe += when
-// accumulate.  Gauss points and shape functions as the element's.
+// 243-285 without the lumping branch): fe = s_e M_e x_e, or fe += when
+// accumulate, with s_e = scale (+ cam * eam[e] when eam is given: the
+// mass-proportional Rayleigh part of a central-difference operator).  Gauss
+// points and shape functions as the element's.
 template <int ND, int NEN>
 __global__ void __launch_bounds__(128) k_mass_elem(DevView d, const double* __restrict__ x, double* __restrict__ fe,
-                                                    double scale, int accumulate) {
+                                                    double scale, int accumulate,
+                                                    const double* __restrict__ eam = nullptr, double cam = 0.0) {
     constexpr int NC = ND * NEN, PER = NEN * ND + 1;
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     const int E = d.nelem;
@@ -702,10 +705,11 @@ __global__ void __launch_bounds__(128) k_mass_elem(DevView d, const double* __re
 #pragma unroll
             for (int k = 0; k < ND; ++k) y[a * ND + k] += c * N[a] * xg[k];
     }
+    const double se = eam ? scale + cam * eam[e] : scale;
 #pragma unroll
     for (int j = 0; j < NC; ++j) {
         double* o = fe + (size_t)j * E + e;
-        *o = accumulate ? *o + scale * y[j] : scale * y[j];
+        *o = accumulate ? *o + se * y[j] : se * y[j];
     }
 }
 
@@ -1239,7 +1243,12 @@ static int cd_create(const svl_model_desc* model, const svl_load_desc* loads, co
     svl_cd* cd = new svl_cd();
     cd->opts = *opts;
     if (!model_from_desc(model, cd->m)) { delete cd; return SVL_ERR_INVALID; }
-    if (!cd->m.lumped && !implicit) { delete cd; set_error("the explicit path needs a lumped mass (massform LUMPED)"); return SVL_ERR_UNSUPPORTED; }
+    if (!cd->m.lumped && !implicit) {
+        delete cd;
+        set_error("the diagonal explicit path needs a lumped mass (massform LUMPED); a consistent mass is served by "
+                  "svl_nm_create with integrator SVL_NM_CENTRAL_DIFFERENCE");
+        return SVL_ERR_UNSUPPORTED;
+    }
     if (cd->m.has_pml()) {
         delete cd;
         set_error("PML elements are served by svl_xnm_create (ExtendedNewmarkBeta)");
@@ -1250,7 +1259,8 @@ static int cd_create(const svl_model_desc* model, const svl_load_desc* loads, co
             if (cd->m.ray[2 * e + 1] != 0.0) {
                 delete cd;
                 set_error("element %zu: stiffness-proportional Rayleigh damping (ak) makes the central-difference "
-                          "effective stiffness non-diagonal; use NewmarkBeta", e);
+                          "effective stiffness non-diagonal; served by svl_nm_create with integrator "
+                          "SVL_NM_CENTRAL_DIFFERENCE", e);
                 return SVL_ERR_UNSUPPORTED;
             }
     if (cudaStreamCreateWithFlags(&cd->stream, cudaStreamNonBlocking) != cudaSuccess) {
@@ -2042,6 +2052,84 @@ __global__ void k_pcg_reset(const double* __restrict__ b, const double* __restri
     p[i] = zi;
 }
 
+// ---- central difference with a non-diagonal effective stiffness ------------
+// K = M/dt^2 + C/2dt with a consistent mass and/or C containing ak_e K0_e
+// (CentralDifference.cpp:64-151), identity T, no support motion.  The element
+// parts of K p (or of (M/dt^2 - C/2dt) w) arrive in an element block `blk`
+// (k_mass_elem with the per-element Rayleigh scale, k_element_tan with the
+// ak-scaled initial elastic coefficients); the diagonal parts are the nodal
+// or lumped masses Md and, with a lumped mass, the mass-proportional diagonal
+// Cd.
+__global__ void k_ncd_w(DevView d, double* __restrict__ w) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < d.ntotal) w[t] = d.U[t] - d.Up[t];
+}
+
+// q_f = sum_e blk_e + (c_m Md + c_c Cd) p on free dofs
+template <int ND>
+__global__ void __launch_bounds__(256) k_ncd_apply(DevView d, const double* __restrict__ blk, const double* __restrict__ pt,
+                                                   double* __restrict__ q, double c_m, double c_c,
+                                                   const double* __restrict__ Cd) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= d.nnode) return;
+#pragma unroll
+    for (int c = 0; c < ND; ++c) {
+        const int t = d.ntdof[n * ND + c];
+        const int f = d.tfree[t];
+        if (f < 0) continue;
+        const double dg = Cd ? c_m * d.Md[t] + c_c * Cd[t] : c_m * d.Md[t];
+        q[f] = (blk ? gather_block<ND>(d, blk, n, c) : 0.0) + dg * pt[t];
+    }
+}
+
+// b_f = Fext - Fint + (M/dt^2 - C/2dt)(U - Up)   (CentralDifference.cpp:217):
+// Fint gathered from d.fe, the element part of the last term from blk
+template <int ND>
+__global__ void __launch_bounds__(256) k_ncd_rhs(DevView d, const double* __restrict__ blk, const double* __restrict__ w,
+                                                 double* __restrict__ b, double c_m, double c_c,
+                                                 const double* __restrict__ Cd) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= d.nnode) return;
+    const int k = d.step[0];
+#pragma unroll
+    for (int c = 0; c < ND; ++c) {
+        const int t = d.ntdof[n * ND + c];
+        const int f = d.tfree[t];
+        if (f < 0) continue;
+        const double fint = gather_fint<ND>(d, n, c);
+        const double fext = fext_at(d, t, k);
+        const double dg = Cd ? c_m * d.Md[t] - c_c * Cd[t] : c_m * d.Md[t];
+        double v = ((fext + 0.0) - fint) + dg * w[t];
+        if (blk) v += gather_block<ND>(d, blk, n, c);
+        b[f] = v;
+    }
+}
+
+// V = (U + dU - Up)/2dt, A = (dU - U + Up)/dt^2, Up = U, U += dU
+// (CentralDifference.cpp:138-148)
+template <int ND>
+__global__ void __launch_bounds__(256) k_ncd_update(DevView d, const double* __restrict__ du, double c_m, double c_c,
+                                                    int* flag) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= d.nnode) return;
+    bool bad = false;
+#pragma unroll
+    for (int c = 0; c < ND; ++c) {
+        const int t = d.ntdof[n * ND + c];
+        const int f = d.tfree[t];
+        const double dU = f >= 0 ? du[f] : 0.0;
+        const double u = d.U[t], up = d.Up[t];
+        d.V[t] = c_c * (u + dU - up);
+        d.A[t] = c_m * (dU - u + up);
+        d.Up[t] = u;
+        const double un = u + dU;
+        d.U[t] = un;
+        d.Us[t] = un;
+        bad |= !isfinite(un);
+    }
+    if (bad) atomicOr(flag, 1);
+}
+
 // state update after the solve (NewmarkBeta.cpp:130-139), identity T, no support motion
 template <int ND>
 __global__ void __launch_bounds__(256) k_nm_update(DevView d, const double* __restrict__ du, double c_a, double c_av,
@@ -2187,6 +2275,12 @@ struct svl_nm {
     // single-precision operator of the inner iterations (eligible models only)
     bool fast_op = false;
     float *geo_f = nullptr, *coef_f = nullptr, *pt_f = nullptr, *fe_f = nullptr;
+    // central difference with a non-diagonal K = M/dt^2 + C/2dt (integrator
+    // SVL_NM_CENTRAL_DIFFERENCE): element block of (M/dt^2 - C/2dt)(U - Up)
+    // and the per-element mass-proportional Rayleigh factors (consistent mass)
+    bool cdmode = false;
+    double* blk_cd = nullptr;               // [nc][E], or null (lumped mass, ak = 0 everywhere)
+    double* eam = nullptr;                  // [E] am_e, or null
     // CG iterates recorded for training pairs
     int rec_every = 0, rec_n = 0;
     std::vector<double*> rec_x, rec_r;
@@ -2247,6 +2341,33 @@ static int nm_apply(svl_nm* nm, const double* v, double* q, bool inner = false) 
     svl_cd* cd = nm->cd;
     const HostModel& m = cd->m;
     const int tb = 256;
+    if (nm->cdmode) {                       // q = (M/dt^2 + C/2dt) v (CentralDifference.cpp:70)
+        DevView d = cd->d;
+        d.ftol = -1.0;
+        d.fe = nm->fe_op;
+        const int eg = (m.nelem + 127) / 128;
+        const double c_m = 1.0 / nm->opts.dt / nm->opts.dt, c_c = 1.0 / 2.0 / nm->opts.dt;
+        k_nm_expand<<<(m.ntotal + tb - 1) / tb, tb, 0, cd->stream>>>(d, v, nm->pt);
+        const double* blk = nullptr;
+        if (d.dk0) {                        // sum_e ak_e/2dt K0_e p_e
+            if (m.ndim == 2) k_element_tan<2, 4><<<eg, 128, 0, cd->stream>>>(d, nm->pt, m.ngp, 0, c_c);
+            else k_element_tan<3, 8><<<eg, 128, 0, cd->stream>>>(d, nm->pt, m.ngp, 0, c_c);
+            blk = nm->fe_op;
+            cd->launches += 1;
+        }
+        if (nm->consistent) {               // + sum_e (1/dt^2 + am_e/2dt) M_e p_e
+            if (m.ndim == 2) k_mass_elem<2, 4><<<eg, 128, 0, cd->stream>>>(d, nm->pt, nm->fe_op, c_m, blk ? 1 : 0, nm->eam, c_c);
+            else k_mass_elem<3, 8><<<eg, 128, 0, cd->stream>>>(d, nm->pt, nm->fe_op, c_m, blk ? 1 : 0, nm->eam, c_c);
+            blk = nm->fe_op;
+            cd->launches += 1;
+        }
+        const double* Cd = nm->consistent ? nullptr : d.Cd;
+        if (m.ndim == 2) k_ncd_apply<2><<<(m.nnode + tb - 1) / tb, tb, 0, cd->stream>>>(d, blk, nm->pt, q, c_m, c_c, Cd);
+        else k_ncd_apply<3><<<(m.nnode + tb - 1) / tb, tb, 0, cd->stream>>>(d, blk, nm->pt, q, c_m, c_c, Cd);
+        cd->launches += 2;
+        CUDA_TRY(cudaGetLastError());
+        return SVL_OK;
+    }
     if (inner && nm->fast_op) {
         DevView d = cd->d;
         k_nm_expand_f<<<(m.ntotal + tb - 1) / tb, tb, 0, cd->stream>>>(d, v, nm->pt, nm->pt_f);
@@ -2478,6 +2599,129 @@ static bool detect_lattice(const HostModel& m, int dims[3], std::vector<int32_t>
     return true;
 }
 
+// Diagonal of the initial elastic element stiffness K0_e (per element dof,
+// node-major): sum_q w B_a^T D B_a with the elastic moduli (J2: K, G).
+static void elem_k0_diag(const HostModel& m, int e, double* kd) {
+    const double* pr = m.param(e);
+    const int mt = m.mat_type(e);
+    double c1, c3;
+    if (mt == SVL_MAT_ELASTIC2DPLANESTRAIN || mt == SVL_MAT_ELASTIC3DLINEAR) {
+        const double E = pr[0], nu = pr[1];
+        c1 = E * (1.0 - nu) / (1.0 - 2.0 * nu) / (1.0 + nu);
+        c3 = E / (2.0 * (1.0 + nu));
+    } else {                    // J2: the elastic moduli K, G
+        c1 = pr[0] + 4.0 / 3.0 * pr[1];
+        c3 = pr[1];
+    }
+    for (int j = 0; j < m.nen * m.ndof; ++j) kd[j] = 0.0;
+    for (int q = 0; q < m.ngp; ++q) {
+        double dNx[8][3], N[8];
+        const double w = gp_factor(m, e, gp_geometry(m, e, q, dNx, N));
+        for (int a = 0; a < m.nen; ++a) {
+            const double bx = dNx[a][0], by = dNx[a][1], bz = dNx[a][2];
+            if (m.ndim == 2) {
+                kd[2 * a] += w * (c1 * bx * bx + c3 * by * by);
+                kd[2 * a + 1] += w * (c1 * by * by + c3 * bx * bx);
+            } else {
+                kd[3 * a] += w * (c1 * bx * bx + c3 * (by * by + bz * bz));
+                kd[3 * a + 1] += w * (c1 * by * by + c3 * (bx * bx + bz * bz));
+                kd[3 * a + 2] += w * (c1 * bz * bz + c3 * (bx * bx + by * by));
+            }
+        }
+    }
+}
+
+// Diagonal of the consistent element mass per node: rho sum_q w t |J| N_a^2.
+static void elem_cmass_diag(const HostModel& m, int e, double* md) {
+    const double rho = m.param(e)[2];
+    for (int a = 0; a < m.nen; ++a) md[a] = 0.0;
+    for (int q = 0; q < m.ngp; ++q) {
+        double dNx[8][3], N[8];
+        const double w = gp_factor(m, e, gp_geometry(m, e, q, dNx, N));
+        for (int a = 0; a < m.nen; ++a) md[a] += rho * w * N[a] * N[a];
+    }
+}
+
+// Handle set-up of the central-difference mode (SVL_NM_CENTRAL_DIFFERENCE):
+// checks, the Jacobi diagonal of K = M/dt^2 + C/2dt, work vectors.
+static int ncd_setup(svl_nm* nm) {
+    svl_cd* cd = nm->cd;
+    const HostModel& m = cd->m;
+    const svl_nm_opts& o = nm->opts;
+    if (o.algorithm != SVL_ALGO_LINEAR || o.precond != SVL_PRECOND_JACOBI) {
+        set_error("central difference: the Linear algorithm with the Jacobi preconditioner");
+        return SVL_ERR_UNSUPPORTED;
+    }
+    if (m.has_j2()) { set_error("central difference with a non-diagonal effective stiffness covers elastic materials"); return SVL_ERR_UNSUPPORTED; }
+    if (!cd->identity_T || cd->has_sm || !m.dp_eta.empty() || cd->d.ndrm > 0) {
+        set_error("central difference with a non-diagonal effective stiffness is covered without constraints, "
+                  "support motion, dashpots or domain-reduction loads");
+        return SVL_ERR_UNSUPPORTED;
+    }
+    nm->cdmode = true;
+    nm->consistent = !m.lumped;
+    nm->general = nm->damped = nm->newton = nm->tangent = false;
+    nm->nf = m.nfree;
+    const double c_m = 1.0 / o.dt / o.dt, c_c = 1.0 / 2.0 / o.dt;
+    const int nc = m.nen * m.ndof;
+    // diagonal of K: element parts, then the nodal / lumped diagonal
+    std::vector<double> Kd(m.ntotal, 0.0), eam;
+    bool any_am = false;
+    for (int e = 0; e < m.nelem; ++e) {
+        const double am = m.ray.empty() ? 0.0 : m.ray[2 * (size_t)e], ak = m.ray.empty() ? 0.0 : m.ray[2 * (size_t)e + 1];
+        any_am = any_am || am != 0.0;
+        double kd[24], md[8];
+        if (ak != 0.0) elem_k0_diag(m, e, kd);
+        if (nm->consistent) elem_cmass_diag(m, e, md);
+        for (int a = 0; a < m.nen; ++a)
+            for (int c = 0; c < m.ndof; ++c) {
+                double v = 0.0;
+                if (ak != 0.0) v += c_c * ak * kd[a * m.ndof + c];
+                if (nm->consistent) v += (c_m + c_c * am) * md[a];
+                Kd[m.tdof[(size_t)m.conn[(size_t)e * m.nen + a] * m.ndof + c]] += v;
+            }
+    }
+    std::vector<double> Md;
+    if (nm->consistent) {
+        Md.assign(m.ntotal, 0.0);
+        if (!m.nodemass.empty())
+            for (int t = 0; t < m.ntotal; ++t) if (std::fabs(m.nodemass[t]) > o.mtol) Md[t] = m.nodemass[t];
+    } else {
+        lumped_mass_diag(m, o.mtol, Md);
+        std::vector<double> Cm;
+        rayleigh_mass_diag(m, Cm);
+        for (int t = 0; t < m.ntotal; ++t) Kd[t] += c_c * Cm[t];
+    }
+    for (int t = 0; t < m.ntotal; ++t) Kd[t] += c_m * Md[t];
+    std::vector<double> dinv(std::max(m.nfree, 1), 1.0);
+    for (int n = 0; n < m.nnode; ++n)
+        for (int c = 0; c < m.ndof; ++c) {
+            const int t = m.tdof[(size_t)n * m.ndof + c], f = m.fdof[(size_t)n * m.ndof + c];
+            if (f < 0) continue;
+            if (!(Kd[t] > 0.0)) { set_error("free dof %d has no mass", f); return SVL_ERR_INVALID; }
+            dinv[f] = 1.0 / Kd[t];
+        }
+    int st;
+    double** vecs[] = {&nm->b, &nm->x, &nm->r, &nm->z, &nm->p, &nm->q};
+    for (double** pv : vecs) if ((st = cd->zeros((size_t)std::max(m.nfree, 1), pv))) return st;
+    if ((st = cd->zeros((size_t)m.ntotal, &nm->pt)) || (st = cd->zeros(2 * kDotBlocks, &nm->partial)) ||
+        (st = cd->zeros(S_NSCAL, &nm->sc)) || (st = cd->zeros((size_t)m.ntotal, &nm->wvec)))
+        return st;
+    const double* dd = nullptr;
+    if ((st = cd->upload(dinv, &dd))) return st;
+    nm->dinv = const_cast<double*>(dd);
+    if (nm->consistent || cd->d.dk0) {
+        if ((st = cd->zeros((size_t)nc * m.nelem, &nm->fe_op)) || (st = cd->zeros((size_t)nc * m.nelem, &nm->blk_cd))) return st;
+    }
+    if (nm->consistent && any_am) {
+        for (int e = 0; e < m.nelem; ++e) eam.push_back(m.ray[2 * (size_t)e]);
+        const double* ea = nullptr;
+        if ((st = cd->upload(eam, &ea))) return st;
+        nm->eam = const_cast<double*>(ea);
+    }
+    return SVL_OK;
+}
+
 static int nm_step(svl_nm* nm, double* U_hist_row);
 
 extern "C" {
@@ -2487,6 +2731,10 @@ int svl_nm_create(const svl_model_desc* model, const svl_load_desc* loads, const
     *out = nullptr;
     if (!(opts->dt > 0.0) || !(opts->pcg_tol > 0.0) || opts->pcg_maxit <= 0) { set_error("bad Newmark options"); return SVL_ERR_INVALID; }
     if (opts->precond != SVL_PRECOND_JACOBI && opts->precond != SVL_PRECOND_LEARNED) { set_error("unknown preconditioner %d", opts->precond); return SVL_ERR_INVALID; }
+    if (opts->integrator != SVL_NM_NEWMARK && opts->integrator != SVL_NM_CENTRAL_DIFFERENCE) {
+        set_error("unknown integrator %d", opts->integrator);
+        return SVL_ERR_INVALID;
+    }
     svl_cd_opts co{};
     co.dt = opts->dt; co.ftol = opts->ftol; co.mtol = opts->mtol; co.precision = SVL_PREC_FP64; co.check_every = 0;
     svl_cd* cd = nullptr;
@@ -2497,6 +2745,12 @@ int svl_nm_create(const svl_model_desc* model, const svl_load_desc* loads, const
     nm->opts = *opts;
     auto fail = [&](int s2) { delete nm; return s2; };
     const HostModel& m = cd->m;
+    if (opts->integrator == SVL_NM_CENTRAL_DIFFERENCE) {
+        if ((st = ncd_setup(nm))) return fail(st);
+        if (cudaStreamSynchronize(cd->stream) != cudaSuccess) { set_error("upload failed"); return fail(SVL_ERR_CUDA); }
+        *out = nm;
+        return SVL_OK;
+    }
     nm->damped = !m.ray.empty() || !m.dp_eta.empty();
     nm->general = !cd->identity_T || cd->has_sm || nm->damped;
     if (opts->algorithm != SVL_ALGO_LINEAR && opts->algorithm != SVL_ALGO_NEWTON) { set_error("unknown algorithm %d", opts->algorithm); return fail(SVL_ERR_INVALID); }
@@ -2521,33 +2775,8 @@ int svl_nm_create(const svl_model_desc* model, const svl_load_desc* loads, const
     std::vector<double> Kd(m.ntotal, 0.0);
     const int nc = m.nen * m.ndof;
     for (int e = 0; e < m.nelem; ++e) {
-        const double* pr = m.param(e);
-        const int mt = m.mat_type(e);
-        double c1, c3;
-        if (mt == SVL_MAT_ELASTIC2DPLANESTRAIN || mt == SVL_MAT_ELASTIC3DLINEAR) {
-            const double E = pr[0], nu = pr[1];
-            c1 = E * (1.0 - nu) / (1.0 - 2.0 * nu) / (1.0 + nu);
-            c3 = E / (2.0 * (1.0 + nu));
-        } else {                    // J2: the elastic moduli K, G
-            c1 = pr[0] + 4.0 / 3.0 * pr[1];
-            c3 = pr[1];
-        }
-        std::vector<double> kd(nc, 0.0);
-        for (int q = 0; q < m.ngp; ++q) {
-            double dNx[8][3], N[8];
-            const double w = gp_factor(m, e, gp_geometry(m, e, q, dNx, N));
-            for (int a = 0; a < m.nen; ++a) {
-                const double bx = dNx[a][0], by = dNx[a][1], bz = dNx[a][2];
-                if (m.ndim == 2) {
-                    kd[2 * a] += w * (c1 * bx * bx + c3 * by * by);
-                    kd[2 * a + 1] += w * (c1 * by * by + c3 * bx * bx);
-                } else {
-                    kd[3 * a] += w * (c1 * bx * bx + c3 * (by * by + bz * bz));
-                    kd[3 * a + 1] += w * (c1 * by * by + c3 * (bx * bx + bz * bz));
-                    kd[3 * a + 2] += w * (c1 * bz * bz + c3 * (bx * bx + by * by));
-                }
-            }
-        }
+        double kd[24];
+        elem_k0_diag(m, e, kd);
         const double ak = m.ray.empty() ? 0.0 : m.ray[2 * (size_t)e + 1];
         for (int a = 0; a < m.nen; ++a)
             for (int c = 0; c < m.ndof; ++c) Kd[m.tdof[(size_t)m.conn[(size_t)e * m.nen + a] * m.ndof + c]] += (1.0 + c_c * ak) * kd[a * m.ndof + c];
@@ -2563,13 +2792,10 @@ int svl_nm_create(const svl_model_desc* model, const svl_load_desc* loads, const
         // diagonal of the consistent mass: rho sum_q w t |J| N_a^2, plus the nodal masses
         std::fill(M.begin(), M.end(), 0.0);
         for (int e = 0; e < m.nelem; ++e) {
-            const double rho = m.param(e)[2];
-            for (int q = 0; q < m.ngp; ++q) {
-                double dNx[8][3], N[8];
-                const double w = gp_factor(m, e, gp_geometry(m, e, q, dNx, N));
-                for (int a = 0; a < m.nen; ++a)
-                    for (int c = 0; c < m.ndof; ++c) M[m.tdof[(size_t)m.conn[(size_t)e * m.nen + a] * m.ndof + c]] += rho * w * N[a] * N[a];
-            }
+            double md[8];
+            elem_cmass_diag(m, e, md);
+            for (int a = 0; a < m.nen; ++a)
+                for (int c = 0; c < m.ndof; ++c) M[m.tdof[(size_t)m.conn[(size_t)e * m.nen + a] * m.ndof + c]] += md[a];
         }
         if (!m.nodemass.empty())
             for (int t = 0; t < m.ntotal; ++t) if (std::fabs(m.nodemass[t]) > opts->mtol) M[t] += m.nodemass[t];
@@ -2926,7 +3152,51 @@ static int nm_step_newton(svl_nm* nm, double* U_hist_row) {
 }
 
 // one step: effective force, solve, state update (d.step already advanced)
+// One central-difference step with the non-diagonal K (CentralDifference.cpp:
+// 124-152 with the effective force of 204-221): Fint from U, the element and
+// diagonal parts of (M/dt^2 - C/2dt)(U - Up), the PCG solve, the update.
+static int ncd_step(svl_nm* nm, double* U_hist_row) {
+    svl_cd* cd = nm->cd;
+    const HostModel& m = cd->m;
+    const double c_m = 1.0 / nm->opts.dt / nm->opts.dt, c_c = 1.0 / 2.0 / nm->opts.dt;
+    const int tb = 256, ng = (m.nnode + tb - 1) / tb, eg = (m.nelem + 127) / 128;
+    k_step_inc<<<1, 1, 0, cd->stream>>>(cd->d.step);
+    if (m.ndim == 2) k_element<2, 4><<<eg, 128, 0, cd->stream>>>(cd->d, cd->d.Us, m.ngp, 0);
+    else k_element<3, 8><<<eg, 128, 0, cd->stream>>>(cd->d, cd->d.Us, m.ngp, 0);
+    k_ncd_w<<<(m.ntotal + tb - 1) / tb, tb, 0, cd->stream>>>(cd->d, nm->wvec);
+    cd->launches += 3;
+    DevView d = cd->d;
+    d.ftol = -1.0;
+    d.fe = nm->blk_cd;
+    const double* blk = nullptr;
+    if (d.dk0) {                            // - sum_e ak_e/2dt K0_e w_e
+        if (m.ndim == 2) k_element_tan<2, 4><<<eg, 128, 0, cd->stream>>>(d, nm->wvec, m.ngp, 0, -c_c);
+        else k_element_tan<3, 8><<<eg, 128, 0, cd->stream>>>(d, nm->wvec, m.ngp, 0, -c_c);
+        blk = nm->blk_cd;
+        cd->launches += 1;
+    }
+    if (nm->consistent) {                   // + sum_e (1/dt^2 - am_e/2dt) M_e w_e
+        if (m.ndim == 2) k_mass_elem<2, 4><<<eg, 128, 0, cd->stream>>>(d, nm->wvec, nm->blk_cd, c_m, blk ? 1 : 0, nm->eam, -c_c);
+        else k_mass_elem<3, 8><<<eg, 128, 0, cd->stream>>>(d, nm->wvec, nm->blk_cd, c_m, blk ? 1 : 0, nm->eam, -c_c);
+        blk = nm->blk_cd;
+        cd->launches += 1;
+    }
+    const double* Cd = nm->consistent ? nullptr : cd->d.Cd;
+    if (m.ndim == 2) k_ncd_rhs<2><<<ng, tb, 0, cd->stream>>>(cd->d, blk, nm->wvec, nm->b, c_m, c_c, Cd);
+    else k_ncd_rhs<3><<<ng, tb, 0, cd->stream>>>(cd->d, blk, nm->wvec, nm->b, c_m, c_c, Cd);
+    cd->launches += 1;
+    CUDA_TRY(cudaGetLastError());
+    TRY(nm_solve(nm));
+    if (m.ndim == 2) k_ncd_update<2><<<ng, tb, 0, cd->stream>>>(cd->d, nm->x, c_m, c_c, cd->d.flag);
+    else k_ncd_update<3><<<ng, tb, 0, cd->stream>>>(cd->d, nm->x, c_m, c_c, cd->d.flag);
+    cd->launches += 1;
+    CUDA_TRY(cudaGetLastError());
+    if (U_hist_row) CUDA_TRY(cudaMemcpyAsync(U_hist_row, cd->d.U, sizeof(double) * m.ntotal, cudaMemcpyDeviceToHost, cd->stream));
+    return SVL_OK;
+}
+
 static int nm_step(svl_nm* nm, double* U_hist_row) {
+    if (nm->cdmode) return ncd_step(nm, U_hist_row);
     if (nm->newton) return nm_step_newton(nm, U_hist_row);
     if (nm->general) return nmg_step_linear(nm, U_hist_row);
     svl_cd* cd = nm->cd;
@@ -3156,13 +3426,16 @@ int svl_nm_get(svl_nm* nm, int32_t which, double* out) {
 
 int svl_nm_reaction(svl_nm* nm, int32_t k, double* R) {
     if (!nm || !R) { set_error("NULL argument"); return SVL_ERR_INVALID; }
-    if (nm->consistent) { set_error("reaction forces are covered with a lumped mass"); return SVL_ERR_UNSUPPORTED; }
+    if (nm->consistent || nm->cdmode) {
+        set_error("reaction forces are covered with a lumped mass and a diagonal central-difference system");
+        return SVL_ERR_UNSUPPORTED;
+    }
     return cd_reaction(nm->cd, k, 0, R);
 }
 
 int svl_nm_element_response(svl_nm* nm, int32_t response, int32_t nlist, const int32_t* elems, double* out) {
     if (!nm) { set_error("NULL handle"); return SVL_ERR_INVALID; }
-    return cd_element_response(nm->cd, 0, response, nlist, elems, out);
+    return cd_element_response(nm->cd, nm->cdmode ? 1 : 0, response, nlist, elems, out);
 }
 
 int svl_nm_stats(svl_nm* nm, int64_t* iters_total, int64_t* iters_last, double* rel_residual_last) {

@@ -47,6 +47,18 @@ public:
             check(svl_xnm_create(&model, &loads, &x, &x_));
             return;
         }
+        // K = M/dt^2 + C/2dt not diagonal (consistent mass or ak != 0,
+        // CentralDifference.cpp:64-70): a PCG solve of K every step
+        bool nondiag = !model.lumped;
+        for (int e = 0; model.elem_rayleigh && e < model.nelem; ++e) nondiag = nondiag || model.elem_rayleigh[2 * e + 1] != 0.0;
+        if (nondiag) {
+            svl_nm_opts n{};
+            n.dt = dt; n.ftol = ftol; n.mtol = mtol; n.pcg_tol = 1e-12; n.pcg_maxit = 20000;
+            n.precond = SVL_PRECOND_JACOBI; n.algorithm = SVL_ALGO_LINEAR;
+            n.integrator = SVL_NM_CENTRAL_DIFFERENCE;
+            check(svl_nm_create(&model, &loads, &n, &n_));
+            return;
+        }
         svl_cd_opts o{};
         o.dt = dt;
         o.mtol = mtol;
@@ -58,20 +70,23 @@ public:
     ~CentralDifference() {
         if (h_) svl_cd_destroy(h_);
         if (x_) svl_xnm_destroy(x_);
+        if (n_) svl_nm_destroy(n_);
     }
     CentralDifference(const CentralDifference&) = delete;
     CentralDifference& operator=(const CentralDifference&) = delete;
 
     // Initialize(mesh): initial conditions from the nodes (CentralDifference.cpp:36-71)
     void Initialize(const double* U0 = nullptr, const double* V0 = nullptr, const double* A0 = nullptr) {
-        check(x_ ? svl_xnm_set_initial(x_, U0, V0, A0, nullptr) : svl_cd_set_initial(h_, U0, V0, A0));
+        check(x_ ? svl_xnm_set_initial(x_, U0, V0, A0, nullptr)
+                 : n_ ? svl_nm_set_initial(n_, U0, V0, A0) : svl_cd_set_initial(h_, U0, V0, A0));
     }
     // ComputeNewStep(mesh, k) -> stop (CentralDifference.cpp:124-151)
     bool ComputeNewStep(unsigned int k) { return ComputeNewSteps(k, 1); }
     // Many steps in one call, optional displacement history [n][ntotal].
     bool ComputeNewSteps(unsigned int k_first, unsigned int n, double* U_hist = nullptr) {
         const int st = x_ ? svl_xnm_run(x_, (int32_t)k_first, (int32_t)n, U_hist)
-                          : svl_cd_run(h_, (int32_t)k_first, (int32_t)n, U_hist);
+                       : n_ ? svl_nm_run(n_, (int32_t)k_first, (int32_t)n, U_hist)
+                            : svl_cd_run(h_, (int32_t)k_first, (int32_t)n, U_hist);
         return st != SVL_OK;
     }
     std::vector<double> GetDisplacements() const { return get(0); }
@@ -82,18 +97,19 @@ public:
     std::vector<double> ComputeReactionForce(unsigned int k) const {
         if (x_) throw Error(SVL_ERR_UNSUPPORTED, "reactions are not covered for PML models");
         std::vector<double> r(ntotal_);
-        check(svl_cd_reaction(h_, (int32_t)k, r.data()));
+        check(n_ ? svl_nm_reaction(n_, (int32_t)k, r.data()) : svl_cd_reaction(h_, (int32_t)k, r.data()));
         return r;
     }
 
 private:
     std::vector<double> get(int which) const {
         std::vector<double> v(ntotal_);
-        check(x_ ? svl_xnm_get(x_, which, v.data()) : svl_cd_get(h_, which, v.data()));
+        check(x_ ? svl_xnm_get(x_, which, v.data()) : n_ ? svl_nm_get(n_, which, v.data()) : svl_cd_get(h_, which, v.data()));
         return v;
     }
     svl_cd* h_ = nullptr;
     svl_xnm* x_ = nullptr;                 // set instead of h_ for models with PML layers
+    svl_nm* n_ = nullptr;                  // set instead of h_ when K is not diagonal
     int ntotal_ = 0;
 };
 

@@ -21,11 +21,16 @@ class CentralDifference:
     """A model with PML layers is served by the PML-capable handle with the
     library's explicit PML scheme (svl_xnm_*, integrator
     SVL_XNM_CENTRAL_DIFFERENCE); the object returned is then an
-    ExtendedNewmarkBeta instance with the same step methods."""
+    ExtendedNewmarkBeta instance with the same step methods.  A model whose
+    central-difference system K = M/dt^2 + C/2dt is not diagonal (consistent
+    mass, or stiffness-proportional Rayleigh damping) is served by
+    CentralDifferenceSolve (a PCG solve of K every step)."""
 
     def __new__(cls, model: Model, *args, **kw):
         if cls is CentralDifference and getattr(model, "elem_pml", None) is not None and np.any(model.elem_pml):
             return _central_difference_pml(model, *args, **kw)
+        if cls is CentralDifference and _cd_nondiagonal(model):
+            return CentralDifferenceSolve(model, *args, **kw)
         return super().__new__(cls)
 
     def __init__(self, model: Model, loads: Loads | None, dt: float, ftol: float = 1e-12,
@@ -348,6 +353,8 @@ class NewmarkBeta:
     `pcg_tol`); the object returned is then an ExtendedNewmarkBeta instance
     with the same step methods."""
 
+    _integrator = capi.SVL_NM_NEWMARK
+
     def __new__(cls, model: Model, *args, **kw):
         if cls is NewmarkBeta and getattr(model, "elem_pml", None) is not None and np.any(model.elem_pml):
             return _newmark_pml(model, *args, **kw)
@@ -371,7 +378,8 @@ class NewmarkBeta:
         algo = {"linear": capi.SVL_ALGO_LINEAR, "newton": capi.SVL_ALGO_NEWTON}[algorithm.lower()]
         opts = capi.NmOpts(dt=self.dt, ftol=ftol, mtol=mtol, pcg_tol=float(pcg_tol), pcg_maxit=int(pcg_maxit),
                            precond=int(precond), algorithm=algo, maxit=int(maxit), cnvgtol=float(cnvgtol),
-                           cnvgtest=int(cnvgtest), single_inner=1 if single_inner else 0)
+                           cnvgtest=int(cnvgtest), single_inner=1 if single_inner else 0,
+                           integrator=self._integrator)
         h = C.c_void_p()
         check(lib().svl_nm_create(C.byref(self._md), C.byref(self._ld), C.byref(opts), C.byref(h)))
         self._h = h
@@ -514,6 +522,32 @@ class NewmarkBeta:
             self.close()
         except Exception:
             pass
+
+
+def _cd_nondiagonal(model: Model) -> bool:
+    """True when K = M/dt^2 + C/2dt of CentralDifference (CentralDifference.cpp:70)
+    has off-diagonal entries: a consistent mass or ak != 0 on some element."""
+    if not model.lumped:
+        return True
+    ray = getattr(model, "rayleigh", None)
+    return ray is not None and bool(np.any(np.asarray(ray)[:, 1] != 0.0))
+
+
+class CentralDifferenceSolve(NewmarkBeta):
+    """CentralDifference whose effective stiffness K = M/dt^2 + C/2dt is not
+    diagonal (CentralDifference.cpp:64-70 with a consistent mass, massform
+    CONSISTENT, or stiffness-proportional Rayleigh damping): each step solves
+    T^T K T du = Feff (CentralDifference.cpp:204-231) by the matrix-free
+    Jacobi-PCG of svl_nm in its central-difference mode to a true relative
+    residual of `pcg_tol`, where the reference factorises K once.  Same step
+    methods as CentralDifference; reaction forces are not covered."""
+
+    _integrator = capi.SVL_NM_CENTRAL_DIFFERENCE
+
+    def __init__(self, model: Model, loads: Loads | None, dt: float, ftol: float = 1e-12,
+                 mtol: float = 1e-12, check_every: int = 0, pcg_tol: float = 1e-12, pcg_maxit: int = 20000):
+        super().__init__(model, loads, dt, pcg_tol=pcg_tol, pcg_maxit=pcg_maxit, ftol=ftol, mtol=mtol,
+                         single_inner=False)
 
 
 class StructuredEnsemble(StructuredCentralDifference):

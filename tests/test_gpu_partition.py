@@ -122,6 +122,22 @@ def test_consistent_mass_partition_newmark_matches_oracle(gpu, tmp_path):
     assert rel_l2(U, ho) <= 1e-9
 
 
+def test_consistent_mass_partition_cd_matches_oracle(gpu, tmp_path):
+    """massform CONSISTENT with Rayleigh damping (am, ak) under
+    CENTRALDIFFERENCE: the non-diagonal central-difference system, solved by
+    PCG on the GPU, against the oracle's factorisation."""
+    p = _part("q4_consistent_cd")
+    assert not p.model.lumped and p.integrator == "CENTRALDIFFERENCE"
+    U = p.run(solution_dir=tmp_path)
+    ho, *_ = O.cd_run(p.model, p.loads, p.dt, p.nt - 1)
+    assert np.abs(ho).max() > 0
+    assert rel_l2(U, ho) <= 1e-9
+    r = p.recorders[0]
+    (nn, ndofs, ntotal, nt), head, rows = _read_recorder(tmp_path / r.file)
+    cols = [d for h in head for d in h[2:]]
+    assert np.allclose(rows, U[:, cols], rtol=10.0 ** -r.precision, atol=0)
+
+
 def test_body_point_load_partition_cd_matches_oracle(gpu, tmp_path):
     """POINTLOAD BODY (nodal acceleration times the node's mass) beside a
     concentrated load, central difference, written by the pre-processor."""

@@ -130,3 +130,36 @@ def test_xnm_options_are_checked_before_any_device_work():
     assert create(dt=0.0) == capi.SVL_ERR_INVALID
     if not gpu_available():
         assert create(algorithm=capi.SVL_ALGO_NEWTON, newton_maxit=3, cnvgtest=1) == capi.SVL_ERR_NODEVICE
+
+
+def test_nm_options_layout_and_central_difference_dispatch():
+    """svl_nm_opts ends with the integrator field (SVL_NM_NEWMARK or
+    SVL_NM_CENTRAL_DIFFERENCE), checked before any device work; the Python
+    CentralDifference sends a model with a non-diagonal K = M/dt^2 + C/2dt
+    (consistent mass, or ak != 0) to the PCG-solving handle."""
+    from tests.conftest import gpu_available
+    from svl_gb300.integrators import _cd_nondiagonal
+    assert C.sizeof(capi.NmOpts) == 72 and capi.NmOpts.integrator.offset == 64
+    m = Model.grid(2, (3, 2), (1.0, 1.0), fix_mask=(0, 0, 3, 0, 0, 0))
+    md, ld = m.desc(), Loads().desc()
+
+    def create(integrator):
+        o = capi.NmOpts(dt=1e-3, ftol=1e-12, mtol=1e-12, pcg_tol=1e-12, pcg_maxit=100, precond=0, algorithm=0,
+                        maxit=1, cnvgtol=0.0, cnvgtest=4, single_inner=0, integrator=integrator)
+        h = C.c_void_p()
+        st = capi.lib().svl_nm_create(C.byref(md), C.byref(ld), C.byref(o), C.byref(h))
+        if st == capi.SVL_OK:
+            capi.lib().svl_nm_destroy(h)
+        return st
+
+    assert create(7) == capi.SVL_ERR_INVALID
+    if not gpu_available():
+        assert create(capi.SVL_NM_CENTRAL_DIFFERENCE) == capi.SVL_ERR_NODEVICE
+    assert not _cd_nondiagonal(m)
+    m.rayleigh = np.tile([2.0, 0.0], (m.nelem, 1))
+    assert not _cd_nondiagonal(m)
+    m.rayleigh[1, 1] = 1e-4
+    assert _cd_nondiagonal(m)
+    m.rayleigh = None
+    m.lumped = False
+    assert _cd_nondiagonal(m)
