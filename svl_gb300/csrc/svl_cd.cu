@@ -2907,8 +2907,10 @@ int svl_nm_create(const svl_model_desc* model, const svl_load_desc* loads, const
 int svl_nm_set_initial(svl_nm* nm, const double* U0, const double* V0, const double* A0) {
     if (!nm) { set_error("NULL handle"); return SVL_ERR_INVALID; }
     TRY(svl_cd_set_initial(nm->cd, U0, V0, A0));
-    // strain displacement = U0 for an elastic start from given displacements
-    if (U0) CUDA_TRY(cudaMemcpyAsync(nm->cd->d.Us, nm->cd->d.U, sizeof(double) * nm->cd->m.ntotal, cudaMemcpyDeviceToDevice, nm->cd->stream));
+    // strain displacement = U0 for an elastic start from given displacements;
+    // the central-difference mode keeps the virgin element state, as
+    // CentralDifference::Initialize leaves the elements (first Fint = 0)
+    if (U0 && !nm->cdmode) CUDA_TRY(cudaMemcpyAsync(nm->cd->d.Us, nm->cd->d.U, sizeof(double) * nm->cd->m.ntotal, cudaMemcpyDeviceToDevice, nm->cd->stream));
     if (nm->newton) {
         // element states, forces and tangents of the initial displacement
         svl_cd* cd = nm->cd;
