@@ -80,12 +80,26 @@ def test_central_difference_mass_proportional(gpu):
     assert rel_l2(hist, ho) <= 1e-12
 
 
-def test_central_difference_rejects_stiffness_proportional(gpu):
-    m, L, dt = q4_box(6, 4, nt=20)
+def test_central_difference_stiffness_proportional(gpu):
+    """ak != 0 makes M/dt^2 + C/2dt non-diagonal: the diagonal handle rejects
+    it, CentralDifference goes to the PCG-solving handle and matches the
+    oracle's factorised solve."""
+    import ctypes as C
+    from svl_gb300 import CentralDifferenceSolve
+    m, L, dt = q4_box(6, 4, nt=60)
     m.rayleigh = _ray(m, 0.0, 1e-3)
-    with pytest.raises(SvlError) as ei:
-        CentralDifference(m, L, dt)
-    assert ei.value.code == capi.SVL_ERR_UNSUPPORTED
+    md, ld = m.desc(), L.desc()
+    opts = capi.CdOpts(dt=dt, ftol=1e-12, mtol=1e-12, precision=capi.SVL_PREC_FP64, check_every=0)
+    h = C.c_void_p()
+    assert capi.lib().svl_cd_create(C.byref(md), C.byref(ld), C.byref(opts), C.byref(h)) == capi.SVL_ERR_UNSUPPORTED
+    cd = CentralDifference(m, L, dt)
+    assert isinstance(cd, CentralDifferenceSolve)
+    cd.Initialize()
+    hist = cd.run(1, 50, history=True)
+    cd.close()
+    ho, *_ = O.cd_run(m, L, dt, 50)
+    assert np.abs(ho).max() > 0
+    assert rel_l2(hist, ho) <= 1e-9
 
 
 def test_lysmer_dashpots_on_all_paths(gpu):
