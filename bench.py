@@ -330,7 +330,7 @@ def uneven_ensemble(steps=200, warm=20):
     pairs = [(m, L) for m, L, _ in inst]
     ndof = sum(free_disp_dofs(m) for m, _ in pairs)
     ens = StructuredEnsemble([(s, (0.0, 0.0, 0.0)) for s in shapes], (2.0, 2.0, 2.0), pairs, dt)
-    sched = ens.tune(1, 5)
+    sched = ens.tune(1, 8)
     for b in range(len(pairs)):
         ens.Initialize(b)
     ens.run(1, warm)
@@ -599,7 +599,7 @@ def main():
     cd.run(1, warm)                                   # warm-up
     # schedule autotuner of the fused step (svl_cdx_tune): CTA count, tile
     # order, band block size and stream priority; the state is reset below
-    sched = cd.tune(1 + warm, 5) if hasattr(cd, "tune") else None
+    sched = cd.tune(1 + warm, 8) if hasattr(cd, "tune") else None
     prof = cd.profile(1 + warm + 200, 20) if hasattr(cd, "profile") else None
     if args.precision == "mixed":
         for b in range(nb):

@@ -344,10 +344,12 @@ int  svl_cdx_get_ctas(svl_cdx* cdx, int32_t* ctas);
 int  svl_cdx_set_schedule(svl_cdx* cdx, const int32_t* choice);
 int  svl_cdx_get_schedule(svl_cdx* cdx, int32_t* choice);
 /* Autotuner: times nsteps steps (from k_first on, after two warm-up steps) of
- * every schedule in a small grid (three CTA counts, the four tile orders and,
- * with a PML band, both block sizes and priorities), keeps the fastest and
- * returns it in choice[4] (*ms_best: its time per step).  The steps advance
- * the state: set the initial conditions again before the run that counts. */
+ * every schedule in a small grid (five CTA counts from one per SM down to
+ * 5/8 of the SMs, the four tile orders and, with a PML band, both block
+ * sizes and priorities), times the four fastest again over 4 * nsteps steps,
+ * keeps the fastest of those and returns it in choice[4] (*ms_best: its time
+ * per step in the second timing).  The steps advance the state: set the
+ * initial conditions again before the run that counts. */
 int  svl_cdx_tune(svl_cdx* cdx, int32_t k_first, int32_t nsteps, int32_t* choice, float* ms_best);
 void svl_cdx_destroy(svl_cdx* cdx);
 

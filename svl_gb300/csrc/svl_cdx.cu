@@ -2125,31 +2125,47 @@ int svl_cdx_tune(svl_cdx* h, int32_t k_first, int32_t nsteps, int32_t* choice, f
     int dev = 0, sms = 0;
     CUDA_TRY(cudaGetDevice(&dev));
     CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    // CTA counts from one per SM down to 5/8 of the SMs: fewer step CTAs
+    // leave whole SMs to the band kernels, which then overlap the step
     std::vector<int> ctas;
-    for (int c : {sms, sms - sms / 16, sms - sms / 8}) {
+    for (int c : {sms, sms - sms / 16, sms - sms / 8, sms - sms / 4, sms - 3 * sms / 8}) {
         c = std::max(1, std::min(c, h->ntiles));                  // as svl_cdx_set_ctas clamps it
         if (std::find(ctas.begin(), ctas.end(), c) == ctas.end()) ctas.push_back(c);
     }
     std::vector<int> bt = {128}, bh = {1};
     if (h->np > 0) { bt.push_back(256); bh.push_back(0); }
-    float best = 0.f;
-    int32_t bc[4] = {0, 0, 128, 1};
+    struct Trial { float ms; int32_t ch[4]; };
+    std::vector<Trial> trials;
     int k = k_first;
+    auto timed = [&](const int32_t* ch, int n, float* ms) -> int {
+        TRY(svl_cdx_set_schedule(h, ch));
+        for (int w = 0; w < 2; ++w) TRY(cdx_step(h, k++, false));   // warm the choice
+        TRY(svl_cdx_run_timed(h, k, n, ms));
+        k += n;
+        return SVL_OK;
+    };
     for (int c : ctas)
         for (int o = 0; o < 4; ++o)
             for (int t : bt)
                 for (int p : bh) {
-                    const int32_t ch[4] = {c, o, t, p};
-                    TRY(svl_cdx_set_schedule(h, ch));
-                    for (int w = 0; w < 2; ++w) TRY(cdx_step(h, k++, false));   // warm the choice
-                    float ms = 0.f;
-                    TRY(svl_cdx_run_timed(h, k, nsteps, &ms));
-                    k += nsteps;
-                    if (best == 0.f || ms < best) { best = ms; std::copy(ch, ch + 4, bc); }
+                    Trial tr{0.f, {c, o, t, p}};
+                    TRY(timed(tr.ch, nsteps, &tr.ms));
+                    trials.push_back(tr);
                 }
+    // the four fastest again over four times the steps: the pick does not
+    // rest on one short sample
+    std::sort(trials.begin(), trials.end(), [](const Trial& a, const Trial& b) { return a.ms < b.ms; });
+    const size_t nre = std::min<size_t>(4, trials.size());
+    float best = 0.f;
+    int32_t bc[4] = {0, 0, 128, 1};
+    for (size_t i = 0; i < nre; ++i) {
+        float ms = 0.f;
+        TRY(timed(trials[i].ch, 4 * nsteps, &ms));
+        if (best == 0.f || ms < best) { best = ms; std::copy(trials[i].ch, trials[i].ch + 4, bc); }
+    }
     TRY(svl_cdx_set_schedule(h, bc));
     std::copy(bc, bc + 4, choice);
-    if (ms_best) *ms_best = best / (float)nsteps;
+    if (ms_best) *ms_best = best / (float)(4 * nsteps);
     h->va_valid = false;
     return SVL_OK;
 }
