@@ -469,6 +469,10 @@ def dist_info():
 # PML element its geometry, node indices and b0 (84 B).
 PML_BYTES_PER_NODE = 540.0
 PML_BYTES_PER_ELEMENT = 84.0
+# DRAM bytes of one k_cdx_step launch on config 2 with 4 instances
+# (dram__bytes_read.sum 298 MB + dram__bytes_write.sum 59 MB, one ncu capture
+# of the 3-metric pass; the command is in the committed profile summary)
+CDX_STEP_DRAM_BYTES_4INST = 357.0e6
 
 
 def workload_config(desc, insts, dt, e2e_steps):
@@ -601,6 +605,15 @@ def main():
     # order, band block size and stream priority; the state is reset below
     sched = cd.tune(1 + warm, 8) if hasattr(cd, "tune") else None
     prof = cd.profile(1 + warm + 200, 20) if hasattr(cd, "profile") else None
+    prof_full = None
+    if sched is not None:
+        # the step kernel alone with one CTA per SM (the tuned schedule may give
+        # SMs to the band instead): the kernel's own roofline
+        tuned = {k: sched[k] for k in cd.SCHEDULE_KEYS}
+        cd.set_schedule(ctas=0)
+        if cd.schedule()["ctas"] != tuned["ctas"]:
+            prof_full = (cd.schedule()["ctas"], cd.profile(1 + warm + 240, 20))
+        cd.set_schedule(**tuned)
     if args.precision == "mixed":
         for b in range(nb):
             cd.Initialize(b)
@@ -660,17 +673,32 @@ def main():
         if pml:
             per_kernel["band kernels, ms per step"] = {n: float(prof[i] / 20.0) for i, n in
                                                        enumerate(["k_cdp_fu", "k_cdp_uu", "k_cdp_fs", "k_cdp_su"], 1)}
+        full_grid = None
+        if prof_full is not None:
+            fms = float(prof_full[1][0]) / 20.0
+            fab = kinds["k_cdx_step (tensor-core interior step, all instances)"][1]
+            full_grid = {"ctas": prof_full[0], "ms_per_step": fms, "achieved": fab / (fms / 1e3) / 1e9,
+                         "frac": fab / (fms / 1e3) / 1e9 / measured_peaks()[0],
+                         "note": "k_cdx_step with one CTA per SM, profiled alone; the tuned schedule gives SMs "
+                                 "to the PML band's kernels, which then overlap the step"}
     else:
         algo_bytes = ALGO_BYTES_PER_DOF[nd] * nfree_total
         if args.workload == "config3":
             algo_bytes += J2_STATE_BYTES_PER_ELEMENT * m.nelem
         k_ms = ms_step
         kname = "one FP64 step (all its kernels)"
-        shares, per_kernel = None, None
+        shares, per_kernel, full_grid = None, None, None
         if prof is not None:
             names = ["k_element", "k_node", "k_residual", "k_free", "k_update"]
             shares = {names[i]: round(float(prof[i] / max(prof.sum(), 1e-12)), 4) for i in range(5) if prof[i] > 0}
     achieved = algo_bytes / (k_ms / 1e3) / 1e9
+    traffic, traffic_src = None, None
+    if args.precision == "mixed" and pml and kname.startswith("k_cdx_step") and args.workload == "config2":
+        # DRAM bytes of one k_cdx_step launch on this workload (4 instances), one
+        # ncu capture (dram__bytes_read.sum + dram__bytes_write.sum), scaled by
+        # the instance count
+        traffic = CDX_STEP_DRAM_BYTES_4INST * nb / 4.0
+        traffic_src = "ncu, 4-instance capture: 298 MB read + 59 MB write per launch"
 
     e2e = None
     if not args.no_e2e:
@@ -744,9 +772,10 @@ def main():
             "l2": "no flush; working set ~%d MB > 129 MB L2" % ws_mb,
             "roofline": {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_source": peak_kind + " (HBM copy)",
-                         "traffic": None,
+                         "traffic": traffic, "traffic_unit": "bytes per launch" if traffic else None,
+                         "traffic_source": traffic_src,
                          "algorithmic_bytes_per_step": algo_bytes, "kernel_ms_per_step": k_ms,
-                         "kernel_share": shares, "per_kernel": per_kernel},
+                         "kernel_share": shares, "per_kernel": per_kernel, "kernel_one_cta_per_sm": full_grid},
             "fp64_plain": fp64, "implicit_pcg_time_to_1e-8": implicit, "nonlinear_newton_j2": newton,
             "nonlinear_newton_j2_pml": newton_pml,
             "cpu_baseline": cb, "e2e": e2e, "gpu_launches": int(launches) if launches is not None else None,
