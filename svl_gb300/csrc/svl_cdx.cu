@@ -590,14 +590,13 @@ __global__ void k_cdx_hist(const float* __restrict__ uh, const float* __restrict
 // u, k_cdp_su updates S and Sbar.  Elements are uniform cubes of side h:
 // at Gauss point q, N_a and dN_a/dx are fixed tables and w |J| = (h/2)^3.
 struct CdpView {
-    int ninst, np, npe, npp;            // PML nodes, PML elements and element pairs per instance
+    int ninst, np, npe;                 // PML nodes and PML elements per instance
     float h, dt;
     long long per;                      // padded state floats per instance
     const int32_t* __restrict__ enode;  // [npe][8] PML node index of each element node
     const float* __restrict__ estr;     // [npe][12] per axis d: a(-g), a(+g), r(-g), r(+g); b = b0 r
     const float* __restrict__ eb0;      // [ninst][npe] b0 of the element's P-wave speed
-    const int32_t* __restrict__ epair;  // [npp][2] elements of a pair, the second the first's +x neighbour or -1
-    const int32_t* __restrict__ ninv;   // [np][8] pair slots pair*16 + pair node, in pair order, -1 unused
+    const int32_t* __restrict__ ninv;   // [np][8] element slots e*8 + local node in element order, -1 unused
     const long long* __restrict__ npad; // [np] padded offset of the node's displacement in instance 0
     const float* __restrict__ uc;       // [ninst][np][6] 1/d for x y z (0 when restrained), c, Ku, Gu
     const float* __restrict__ scs;      // [ninst][np][12] Dinv, A, KG, Gs as (diagonal, off-diagonal, shear)
@@ -613,15 +612,9 @@ struct CdpView {
     float* sbh; float* sbl;             // Sbar pair [ninst][np][6]
     float* vsu;                         // [ninst][18][np] displacement rows' inputs: sdot, smid, Sbar (written by k_cdp_su for the next step)
     float* vin;                         // [ninst][9][np] stress rows' inputs: udot, umid, ubar at the half step
-    float* feu;                         // [ninst][12][3][npp] pair slots (pair node, component, pair)
-    float* fes;                         // [ninst][12][6][npp]
+    float* feu;                         // [ninst][8][3][npe] element slots (local node, component, element)
+    float* fes;                         // [ninst][8][6][npe]
 };
-
-// Pairs of x-adjacent PML elements: a pair's 12 nodes are (xi, m) with xi =
-// 0, 1, 2 along x and m = is + 2 it over y and z, pair node xi + 3 m; the
-// first element's nodes are xi = 0, 1, the second's xi = 1, 2, so the shared
-// face is summed in the element kernel and the node kernels gather 25 % fewer
-// slots.
 
 // Node rows and element slots are stored component-major ([..][component][node]
 // and [..][local node][component][element]): consecutive threads handle
@@ -641,7 +634,7 @@ constexpr float CDP_P = 0.5f * (1.0f + CDP_G), CDP_Q = 0.5f * (1.0f - CDP_G);
 
 // Element node (the element's own order: (-,-,-) (+,-,-) (+,+,-) (-,+,-),
 // then the same at +z) of lexicographic corner l = ir + 2 is + 4 it.
-__host__ __device__ __forceinline__ constexpr int cdp_lex_node(int l) {
+__device__ __forceinline__ constexpr int cdp_lex_node(int l) {
     return (l & 4) | ((l & 2) ? ((l & 1) ? 2 : 3) : (l & 1));
 }
 
@@ -706,16 +699,20 @@ __device__ __forceinline__ constexpr int cdp_scomp(int d, int c) {
 // on the abscissa along d, so the sum over the two points along d acts on the
 // node values first (their sum), and everything else is a 2 x 2 x 2 map
 // over the two other axes (sum factorisation): no per-point 8 x 8 products.
-// One element's forces, scaled by w|J| / h, added to the pair accumulators:
-// lo[m] takes the corners with ir = 0, hi[m] those with ir = 1 (m = is + 2 it).
-__device__ __forceinline__ void cdp_fu_elem(const CdpView& v, int e, int inst, float lo[4][3], float hi[4][3]) {
+template <int NT>
+__global__ void __launch_bounds__(NT, 512 / NT) k_cdp_fu(CdpView v) {
+    const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid >= (long long)v.npe) return;
+    const int e = (int)gid;
     int node[8];
 #pragma unroll
-    for (int l = 0; l < 8; ++l) node[l] = __ldg(v.enode + (size_t)e * 8 + cdp_lex_node(l));
+    for (int l = 0; l < 8; ++l) node[l] = v.enode[(size_t)e * 8 + cdp_lex_node(l)];
     float4 t[3];
 #pragma unroll
-    for (int d = 0; d < 3; ++d) t[d] = __ldg(reinterpret_cast<const float4*>(v.estr + (size_t)e * 12) + d);
-    const CdpStretch s = cdp_stretch(t, __ldg(v.eb0 + (size_t)inst * v.npe + e));
+    for (int d = 0; d < 3; ++d) t[d] = reinterpret_cast<const float4*>(v.estr + (size_t)e * 12)[d];
+#pragma unroll 1
+    for (int inst = 0; inst < v.ninst; ++inst) {
+    const CdpStretch s = cdp_stretch(t, v.eb0[(size_t)inst * v.npe + e]);
     const float* base = v.vsu + (size_t)inst * VSU_K * v.np;
     float acc[3][3][4];
 #pragma unroll
@@ -759,52 +756,14 @@ __device__ __forceinline__ void cdp_fu_elem(const CdpView& v, int e, int inst, f
             }
         }
     const float hh = 0.5f * v.h, scale = hh * hh * hh / v.h;     // w|J| times the 1/h of the derivative
+    float o[24];
 #pragma unroll
     for (int l = 0; l < 8; ++l)
 #pragma unroll
-        for (int j = 0; j < 3; ++j) {
-            if (l & 1) hi[l >> 1][j] += scale * f[l][j];
-            else lo[l >> 1][j] += scale * f[l][j];
-        }
-}
-
-// Coupling forces on the displacement rows of a pair of x-adjacent PML
-// elements (cdp_fu_elem for each), one thread per pair, into the pair slots.
-template <int NT>
-__global__ void __launch_bounds__(NT, 512 / NT) k_cdp_fu(CdpView v) {
-    const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (gid >= (long long)v.npp) return;
-    const int pr = (int)gid;
-    const int ea = v.epair[2 * (size_t)pr], eb = v.epair[2 * (size_t)pr + 1];
-#pragma unroll 1
-    for (int inst = 0; inst < v.ninst; ++inst) {
-        float a[4][3], b[4][3];
+        for (int j = 0; j < 3; ++j) o[cdp_lex_node(l) * 3 + j] = scale * f[l][j];
+    float* out = v.feu + (size_t)inst * 24 * v.npe + e;
 #pragma unroll
-        for (int m = 0; m < 4; ++m)
-#pragma unroll
-            for (int j = 0; j < 3; ++j) a[m][j] = b[m][j] = 0.f;
-        cdp_fu_elem(v, ea, inst, a, b);
-        float* out = v.feu + (size_t)inst * 36 * v.npp + pr;
-#pragma unroll
-        for (int m = 0; m < 4; ++m)
-#pragma unroll
-            for (int j = 0; j < 3; ++j) out[(size_t)((3 * m) * 3 + j) * v.npp] = a[m][j];
-        if (eb >= 0) {
-            float c[4][3];
-#pragma unroll
-            for (int m = 0; m < 4; ++m)
-#pragma unroll
-                for (int j = 0; j < 3; ++j) c[m][j] = 0.f;
-            cdp_fu_elem(v, eb, inst, b, c);
-#pragma unroll
-            for (int m = 0; m < 4; ++m)
-#pragma unroll
-                for (int j = 0; j < 3; ++j) out[(size_t)((2 + 3 * m) * 3 + j) * v.npp] = c[m][j];
-        }
-#pragma unroll
-        for (int m = 0; m < 4; ++m)
-#pragma unroll
-            for (int j = 0; j < 3; ++j) out[(size_t)((1 + 3 * m) * 3 + j) * v.npp] = b[m][j];
+    for (int i = 0; i < 24; ++i) out[(size_t)i * v.npe] = o[i];
     }
 }
 
@@ -824,12 +783,12 @@ __global__ void __launch_bounds__(256, 4) k_cdp_uu(CdpView v) {
     for (int inst = 0; inst < v.ninst; ++inst) {
         const long long pad = (long long)inst * v.per + np0;
         float f[3] = {v.fsol[pad], v.fsol[pad + 1], v.fsol[pad + 2]};
-        const size_t fb = (size_t)inst * 36 * v.npp;
+        const size_t fb = (size_t)inst * 24 * v.npe;
 #pragma unroll
         for (int s2 = 0; s2 < 8; ++s2) {
             if (slots[s2] < 0) break;
-            const float* fe = v.feu + fb + (size_t)(slots[s2] & 15) * 3 * v.npp + (slots[s2] >> 4);
-            f[0] += fe[0]; f[1] += fe[v.npp]; f[2] += fe[2 * (size_t)v.npp];
+            const float* fe = v.feu + fb + (size_t)(slots[s2] & 7) * 3 * v.npe + (slots[s2] >> 3);
+            f[0] += fe[0]; f[1] += fe[v.npe]; f[2] += fe[2 * (size_t)v.npe];
         }
         const float* c6 = v.uc + ((size_t)inst * v.np + p) * 6;
         const float cc = c6[3], Ku = c6[4], Gu = c6[5];
@@ -869,16 +828,20 @@ __global__ void __launch_bounds__(256, 4) k_cdp_uu(CdpView v) {
 // abscissa along d, and the shape functions along d sum to one over its two
 // points, so each term is a 2 x 2 x 2 map over the two other axes whose
 // result is the same at both nodes along d.
-// One element's coupling forces on the stress rows, scaled by w|J| / h, added
-// to the pair accumulators lo (corners with ir = 0) and hi (ir = 1).
-__device__ __forceinline__ void cdp_fs_elem(const CdpView& v, int e, int inst, float lo[4][6], float hi[4][6]) {
+template <int NT>
+__global__ void __launch_bounds__(NT, 512 / NT) k_cdp_fs(CdpView v) {
+    const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid >= (long long)v.npe) return;
+    const int e = (int)gid;
     int node[8];
 #pragma unroll
-    for (int l = 0; l < 8; ++l) node[l] = __ldg(v.enode + (size_t)e * 8 + cdp_lex_node(l));
+    for (int l = 0; l < 8; ++l) node[l] = v.enode[(size_t)e * 8 + cdp_lex_node(l)];
     float4 t[3];
 #pragma unroll
-    for (int d = 0; d < 3; ++d) t[d] = __ldg(reinterpret_cast<const float4*>(v.estr + (size_t)e * 12) + d);
-    const CdpStretch s = cdp_stretch(t, __ldg(v.eb0 + (size_t)inst * v.npe + e));
+    for (int d = 0; d < 3; ++d) t[d] = reinterpret_cast<const float4*>(v.estr + (size_t)e * 12)[d];
+#pragma unroll 1
+    for (int inst = 0; inst < v.ninst; ++inst) {
+    const CdpStretch s = cdp_stretch(t, v.eb0[(size_t)inst * v.npe + e]);
     const float* base = v.vin + (size_t)inst * VIN_K * v.np;
     float acc[3][3][4];                 // [d][c][m]
 #pragma unroll
@@ -906,7 +869,11 @@ __device__ __forceinline__ void cdp_fs_elem(const CdpView& v, int e, int inst, f
                 for (int m = 0; m < 4; ++m) acc[d][c][m] += cdp_w(s, d, m, type) * z[m];
             }
     }
-    const float hh = 0.5f * v.h, scale = hh * hh * hh / v.h;
+    float r[8][6];
+#pragma unroll
+    for (int l = 0; l < 8; ++l)
+#pragma unroll
+        for (int k = 0; k < 6; ++k) r[l][k] = 0.f;
 #pragma unroll
     for (int d = 0; d < 3; ++d)
 #pragma unroll
@@ -915,54 +882,19 @@ __device__ __forceinline__ void cdp_fs_elem(const CdpView& v, int e, int inst, f
             cdp_interp2(acc[d][c]);
 #pragma unroll
             for (int m = 0; m < 4; ++m) {
-                const float w = scale * acc[d][c][m];
-#pragma unroll
-                for (int bit = 0; bit < 2; ++bit) {
-                    const int l = cdp_lex(d, m, bit);
-                    if (l & 1) hi[l >> 1][k] += w;
-                    else lo[l >> 1][k] += w;
-                }
+                r[cdp_lex(d, m, 0)][k] += acc[d][c][m];
+                r[cdp_lex(d, m, 1)][k] += acc[d][c][m];
             }
         }
-}
-
-// Coupling forces on the stress rows of a pair of x-adjacent PML elements
-// (cdp_fs_elem for each), one thread per pair, into the pair slots.
-template <int NT>
-__global__ void __launch_bounds__(NT, 512 / NT) k_cdp_fs(CdpView v) {
-    const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (gid >= (long long)v.npp) return;
-    const int pr = (int)gid;
-    const int ea = v.epair[2 * (size_t)pr], eb = v.epair[2 * (size_t)pr + 1];
-#pragma unroll 1
-    for (int inst = 0; inst < v.ninst; ++inst) {
-        float a[4][6], b[4][6];
+    const float hh = 0.5f * v.h, scale = hh * hh * hh / v.h;
+    float o[48];
 #pragma unroll
-        for (int m = 0; m < 4; ++m)
+    for (int l = 0; l < 8; ++l)
 #pragma unroll
-            for (int k = 0; k < 6; ++k) a[m][k] = b[m][k] = 0.f;
-        cdp_fs_elem(v, ea, inst, a, b);
-        float* out = v.fes + (size_t)inst * 72 * v.npp + pr;
+        for (int k = 0; k < 6; ++k) o[cdp_lex_node(l) * 6 + k] = scale * r[l][k];
+    float* out = v.fes + (size_t)inst * 48 * v.npe + e;
 #pragma unroll
-        for (int m = 0; m < 4; ++m)
-#pragma unroll
-            for (int k = 0; k < 6; ++k) out[(size_t)((3 * m) * 6 + k) * v.npp] = a[m][k];
-        if (eb >= 0) {
-            float c[4][6];
-#pragma unroll
-            for (int m = 0; m < 4; ++m)
-#pragma unroll
-                for (int k = 0; k < 6; ++k) c[m][k] = 0.f;
-            cdp_fs_elem(v, eb, inst, b, c);
-#pragma unroll
-            for (int m = 0; m < 4; ++m)
-#pragma unroll
-                for (int k = 0; k < 6; ++k) out[(size_t)((2 + 3 * m) * 6 + k) * v.npp] = c[m][k];
-        }
-#pragma unroll
-        for (int m = 0; m < 4; ++m)
-#pragma unroll
-            for (int k = 0; k < 6; ++k) out[(size_t)((1 + 3 * m) * 6 + k) * v.npp] = b[m][k];
+    for (int i = 0; i < 48; ++i) out[(size_t)i * v.npe] = o[i];
     }
 }
 
@@ -991,13 +923,13 @@ __global__ void __launch_bounds__(256, 4) k_cdp_su(CdpView v) {
 #pragma unroll 1
     for (int inst = 0; inst < v.ninst; ++inst) {
         float F[6] = {0, 0, 0, 0, 0, 0};
-        const size_t fb = (size_t)inst * 72 * v.npp;
+        const size_t fb = (size_t)inst * 48 * v.npe;
 #pragma unroll
         for (int s2 = 0; s2 < 8; ++s2) {
             if (slots[s2] < 0) break;
-            const float* fe = v.fes + fb + (size_t)(slots[s2] & 15) * 6 * v.npp + (slots[s2] >> 4);
+            const float* fe = v.fes + fb + (size_t)(slots[s2] & 7) * 6 * v.npe + (slots[s2] >> 3);
 #pragma unroll
-            for (int c = 0; c < 6; ++c) F[c] += fe[(size_t)c * v.npp];
+            for (int c = 0; c < 6; ++c) F[c] += fe[(size_t)c * v.npe];
         }
         const size_t b = ((size_t)inst * v.np + p) * 6;
         float sc[6], ds[6], sb[6], ch[6], cl[6];
@@ -1052,47 +984,6 @@ float host_tf32(double x) {
 
 }  // namespace
 
-// Pairs of x-adjacent PML elements in element order (a run along x pairs
-// greedily; an element whose +x neighbour is not the next PML element stays
-// alone, second entry -1) and each PML node's pair slots (pair * 16 + pair
-// node), in pair order.  Element nodes in the element's own order; a pair's
-// second element shares the first one's +x face.
-int cdp_pairs(int np, int npe, const std::vector<int32_t>& enode, std::vector<int32_t>& epair,
-              std::vector<int32_t>& ninv) {
-    auto en = [&](int e, int l) { return enode[(size_t)e * 8 + cdp_lex_node(l)]; };   // lex corner l
-    epair.clear();
-    for (int i = 0; i < npe;) {
-        bool adj = i + 1 < npe;
-        for (int m = 0; m < 4 && adj; ++m) adj = en(i, 2 * m + 1) == en(i + 1, 2 * m);
-        epair.push_back(i);
-        epair.push_back(adj ? i + 1 : -1);
-        i += adj ? 2 : 1;
-    }
-    const int npp = (int)(epair.size() / 2);
-    if ((long long)npp * 16 > INT32_MAX) { set_error("too many PML elements"); return SVL_ERR_UNSUPPORTED; }
-    ninv.assign((size_t)np * 8, -1);
-    std::vector<int> fill(np, 0);
-    auto add = [&](int pn, int32_t slot) {
-        if (fill[pn] >= 8) { set_error("PML node %d in more than 8 element pairs", pn); return SVL_ERR_INVALID; }
-        ninv[(size_t)pn * 8 + fill[pn]++] = slot;
-        return SVL_OK;
-    };
-    for (int p = 0; p < npp; ++p) {
-        const int ea = epair[2 * (size_t)p], eb = epair[2 * (size_t)p + 1];
-        for (int xi = 0; xi < 3; ++xi)
-            for (int m = 0; m < 4; ++m) {
-                int node;
-                if (xi < 2) node = en(ea, xi + 2 * m);
-                else if (eb >= 0) node = en(eb, 1 + 2 * m);
-                else continue;
-                if (node < 0 || node >= np) { set_error("PML pair %d: node outside the band", p); return SVL_ERR_INVALID; }
-                const int st = add(node, p * 16 + xi + 3 * m);
-                if (st) return st;
-            }
-    }
-    return SVL_OK;
-}
-
 struct svl_cdx {
     int nx = 0, ny = 0, nz = 0, ninst = 0;
     long long nn = 0, ne = 0, ntotal = 0;
@@ -1129,12 +1020,12 @@ struct svl_cdx {
     std::vector<std::vector<long long>> own2emb;
     std::vector<long long> own_ntotal;   // total dofs of each instance in its own numbering
     // PML band (np = 0 without PML elements)
-    int np = 0, npe = 0, npp = 0;
+    int np = 0, npe = 0;
     float* fsol = nullptr;
     float *sh[2] = {nullptr, nullptr}, *sl[2] = {nullptr, nullptr};
     float *sbh = nullptr, *sbl = nullptr, *ubh = nullptr, *ubl = nullptr;
     float *vin = nullptr, *vsu = nullptr, *feu = nullptr, *fes = nullptr, *uc = nullptr, *scs = nullptr, *estr = nullptr, *eb0 = nullptr;
-    int32_t *enode = nullptr, *ninv = nullptr, *epair = nullptr;
+    int32_t *enode = nullptr, *ninv = nullptr;
     long long* npad = nullptr;
     int cur = 0;                         // index of u_n in uh/ul
     int64_t launches = 0, launches_last = 0;
@@ -1340,7 +1231,7 @@ static int cdx_create_impl(const svl_grid_spec* g, int32_t ninst, const svl_mode
     // PML band tables (np = 0 without PML elements)
     std::vector<int32_t> pidx;                       // node -> PML node index or -1
     std::vector<int32_t> t2node;                     // total dof -> node (instance 0 numbering)
-    std::vector<int32_t> enode, ninv, epair;
+    std::vector<int32_t> enode, ninv;
     std::vector<long long> npad;
     std::vector<float> estr, eb0, uc, scs;
     std::vector<int> pelem;                          // PML elements in element order
@@ -1419,13 +1310,16 @@ static int cdx_create_impl(const svl_grid_spec* g, int32_t ninst, const svl_mode
                 par0.assign(m.pml_par.begin(), m.pml_par.end());
                 enode.resize((size_t)h->npe * 8);
                 estr.resize((size_t)h->npe * 12);
+                ninv.assign((size_t)h->np * 8, -1);
+                std::vector<int> fill(h->np, 0);
                 for (int i = 0; i < h->npe; ++i) {
                     const int e = pelem[i];
                     const double* pp = &m.pml_par[(size_t)e * 9];
                     for (int a = 0; a < 8; ++a) {
                         const int pn = pidx[m.conn[(size_t)e * 8 + a]];
-                        if (pn < 0 || pn >= h->np) { set_error("PML element %d: node outside the band", e); return fail(SVL_ERR_INVALID); }
                         enode[(size_t)i * 8 + a] = pn;
+                        if (fill[pn] >= 8) { set_error("PML node %d in more than 8 elements", pn); return fail(SVL_ERR_INVALID); }
+                        ninv[(size_t)pn * 8 + fill[pn]++] = i * 8 + a;
                     }
                     // stretching at the two Gauss abscissae of every axis
                     // (PML3DHexa8.cpp:952-996): a = 1 + a0 r, b = b0 r with
@@ -1442,8 +1336,6 @@ static int cdx_create_impl(const svl_grid_spec* g, int32_t ninst, const svl_mode
                             estr[(size_t)i * 12 + 4 * d + 2 + sgn] = (float)r;
                         }
                 }
-                if ((st = cdp_pairs(h->np, h->npe, enode, epair, ninv))) return fail(st);
-                h->npp = (int)(epair.size() / 2);
             }
         } else {
             if (m.ntotal != h->ntotal) { set_error("instance %d: dof count differs from instance 0", b); return fail(SVL_ERR_INVALID); }
@@ -1680,10 +1572,9 @@ static int cdx_create_impl(const svl_grid_spec* g, int32_t ninst, const svl_mode
             (st = h->alloc(n6, &h->sl[0])) || (st = h->alloc(n6, &h->sl[1])) || (st = h->alloc(n6, &h->sbh)) ||
             (st = h->alloc(n6, &h->sbl)) || (st = h->alloc(n3, &h->ubh)) || (st = h->alloc(n3, &h->ubl)) ||
             (st = h->alloc((size_t)ninst * h->np * VIN_K, &h->vin)) || (st = h->alloc((size_t)ninst * h->np * VSU_K, &h->vsu)) ||
-            (st = h->alloc((size_t)ninst * h->npp * 36, &h->feu)) || (st = h->alloc((size_t)ninst * h->npp * 72, &h->fes)) ||
+            (st = h->alloc((size_t)ninst * h->npe * 24, &h->feu)) || (st = h->alloc((size_t)ninst * h->npe * 48, &h->fes)) ||
             (st = h->upload(uc, &h->uc)) || (st = h->upload(scs, &h->scs)) || (st = h->upload(estr, &h->estr)) ||
             (st = h->upload(eb0, &h->eb0)) || (st = h->upload(enode, &h->enode)) || (st = h->upload(ninv, &h->ninv)) ||
-            (st = h->upload(epair, &h->epair)) ||
             (st = h->upload(npad, &h->npad)))
             return fail(st);
     }
@@ -1892,10 +1783,10 @@ int svl_cdx_set_initial(svl_cdx* h, int32_t inst, const double* U0, const double
 // The PML band's view of the handle for the step from u_n (index cur).
 static CdpView cdp_view(svl_cdx* h) {
     CdpView c{};
-    c.ninst = h->ninst; c.np = h->np; c.npe = h->npe; c.npp = h->npp;
+    c.ninst = h->ninst; c.np = h->np; c.npe = h->npe;
     c.h = (float)h->hgrid; c.dt = (float)h->dt;
     c.per = (long long)(h->nstate / h->ninst);
-    c.enode = h->enode; c.estr = h->estr; c.eb0 = h->eb0; c.epair = h->epair; c.ninv = h->ninv; c.npad = h->npad;
+    c.enode = h->enode; c.estr = h->estr; c.eb0 = h->eb0; c.ninv = h->ninv; c.npad = h->npad;
     c.uc = h->uc; c.scs = h->scs;
     c.uh = h->uh[h->cur]; c.ul = h->ul[h->cur]; c.uph = h->uh[1 - h->cur]; c.upl = h->ul[1 - h->cur];
     c.fsol = h->fsol;
@@ -1906,11 +1797,12 @@ static CdpView cdp_view(svl_cdx* h) {
 }
 
 // One kernel of the band's step: 0 = k_cdp_fu, 1 = k_cdp_uu (displacement
-// rows), 2 = k_cdp_fs, 3 = k_cdp_su (stress rows).  One thread per pair of PML
-// elements or per PML node, each looping over the instances.
+// rows), 2 = k_cdp_fs, 3 = k_cdp_su (stress rows).  One thread per PML element
+// or per PML node, each looping over the instances (their tables are read
+// once).
 static void cdp_launch(svl_cdx* h, const CdpView& c, int which, cudaStream_t st) {
     const int nt = h->band_threads;
-    const unsigned be = (unsigned)((h->npp + nt - 1) / nt), bn = (unsigned)((h->np + 255) / 256);
+    const unsigned be = (unsigned)((h->npe + nt - 1) / nt), bn = (unsigned)((h->np + 255) / 256);
     switch (which) {
         case 0:
             if (nt == 256) k_cdp_fu<256><<<be, 256, 0, st>>>(c);
