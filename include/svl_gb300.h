@@ -391,10 +391,13 @@ void svl_cdx_destroy(svl_cdx* cdx);
  * M_e p_e + (ak_e/2dt) K0_e p_e plus the nodal masses / dt^2, stopping on
  * the true relative residual <= pcg_tol.  Step: Feff = Fext - Fint +
  * (M/dt^2 - C/2dt)(U - Up), solve, V = (U + dU - Up)/2dt, A = (dU - U +
- * Up)/dt^2, Up = U, U += dU.  Covered: elastic materials, identity T, no
- * support motion, dashpots or domain-reduction loads (SVL_ERR_UNSUPPORTED
- * otherwise); algorithm must be SVL_ALGO_LINEAR and precond Jacobi.  A
- * lumped mass without ak is the diagonal path of svl_cd_create. */
+ * Up)/dt^2, Up = U, U += dU.  Covered: elastic and J2 materials (the
+ * element update from U + T du once per step, as the diagonal path), EQUAL
+ * constraints (T^T K T, Feff = T^T R), support motion (dU = T du + SM(k),
+ * Feff -= T^T K SM(k)), ZeroLength1D dashpots (their C in K); not
+ * domain-reduction loads (SVL_ERR_UNSUPPORTED); algorithm must be
+ * SVL_ALGO_LINEAR and precond Jacobi.  A lumped mass without ak is the
+ * diagonal path of svl_cd_create. */
 #define SVL_NM_NEWMARK            0
 #define SVL_NM_CENTRAL_DIFFERENCE 1
 typedef struct svl_nm_opts {

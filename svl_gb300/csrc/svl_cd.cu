@@ -2078,7 +2078,9 @@ __global__ void __launch_bounds__(256) k_ncd_apply(DevView d, const double* __re
         const int f = d.tfree[t];
         if (f < 0) continue;
         const double dg = Cd ? c_m * d.Md[t] + c_c * Cd[t] : c_m * d.Md[t];
-        q[f] = (blk ? gather_block<ND>(d, blk, n, c) : 0.0) + dg * pt[t];
+        double v = (blk ? gather_block<ND>(d, blk, n, c) : 0.0) + dg * pt[t];
+        if (d.dp_ptr) v += c_c * dashpot_sum(d, t, pt);
+        q[f] = v;
     }
 }
 
@@ -2101,8 +2103,81 @@ __global__ void __launch_bounds__(256) k_ncd_rhs(DevView d, const double* __rest
         const double dg = Cd ? c_m * d.Md[t] - c_c * Cd[t] : c_m * d.Md[t];
         double v = ((fext + 0.0) - fint) + dg * w[t];
         if (blk) v += gather_block<ND>(d, blk, n, c);
+        if (d.dp_ptr) v -= c_c * dashpot_sum(d, t, w);
         b[f] = v;
     }
+}
+
+// General T (constraints) and support motion: the same terms on every total
+// dof, reduced to the free dofs by T^T afterwards (k_nmg_reduce).
+// ft = K p = blk + (c_m Md + c_c Cd) p + c_c (dashpots) p
+template <int ND>
+__global__ void __launch_bounds__(256) k_ncd_total(DevView d, const double* __restrict__ blk, const double* __restrict__ pt,
+                                                   double* __restrict__ ft, double c_m, double c_c,
+                                                   const double* __restrict__ Cd) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= d.nnode) return;
+#pragma unroll
+    for (int c = 0; c < ND; ++c) {
+        const int t = d.ntdof[n * ND + c];
+        const double dg = Cd ? c_m * d.Md[t] + c_c * Cd[t] : c_m * d.Md[t];
+        double v = (blk ? gather_block<ND>(d, blk, n, c) : 0.0) + dg * pt[t];
+        if (d.dp_ptr) v += c_c * dashpot_sum(d, t, pt);
+        ft[t] = v;
+    }
+}
+
+// ft = Fext - Fint + (M/dt^2 - C/2dt) w on every total dof
+template <int ND>
+__global__ void __launch_bounds__(256) k_ncd_rtotal(DevView d, const double* __restrict__ blk, const double* __restrict__ w,
+                                                    double* __restrict__ ft, double c_m, double c_c,
+                                                    const double* __restrict__ Cd) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= d.nnode) return;
+    const int k = d.step[0];
+#pragma unroll
+    for (int c = 0; c < ND; ++c) {
+        const int t = d.ntdof[n * ND + c];
+        const double fint = gather_fint<ND>(d, n, c);
+        const double fext = fext_at(d, t, k);
+        const double dg = Cd ? c_m * d.Md[t] - c_c * Cd[t] : c_m * d.Md[t];
+        double v = ((fext + 0.0) - fint) + dg * w[t];
+        if (blk) v += gather_block<ND>(d, blk, n, c);
+        if (d.dp_ptr) v -= c_c * dashpot_sum(d, t, w);
+        ft[t] = v;
+    }
+}
+
+// support-motion increment of step k (CentralDifference.cpp:195)
+__global__ void k_ncd_sm(DevView d, double* __restrict__ sm) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= d.ntotal) return;
+    sm[t] = sm_at(d, t, d.step[0]);
+}
+
+// dU = T du + SM (CentralDifference.cpp:138), Us = U + T du (the strain
+// displacement of the next step's element update), then the update of
+// CentralDifference.cpp:141-148
+template <int ND>
+__global__ void __launch_bounds__(256) k_ncd_gupdate(DevView d, const double* __restrict__ dUt, const double* __restrict__ sm,
+                                                     double c_m, double c_c, int* flag) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= d.nnode) return;
+    bool bad = false;
+#pragma unroll
+    for (int c = 0; c < ND; ++c) {
+        const int t = d.ntdof[n * ND + c];
+        const double dut = dUt[t], dU = sm ? dut + sm[t] : dut;
+        const double u = d.U[t], up = d.Up[t];
+        d.Us[t] = u + dut;
+        d.V[t] = c_c * (u + dU - up);
+        d.A[t] = c_m * (dU - u + up);
+        d.Up[t] = u;
+        const double un = u + dU;
+        d.U[t] = un;
+        bad |= !isfinite(un);
+    }
+    if (bad) atomicOr(flag, 1);
 }
 
 // V = (U + dU - Up)/2dt, A = (dU - U + Up)/dt^2, Up = U, U += dU
@@ -2278,7 +2353,7 @@ struct svl_nm {
     // central difference with a non-diagonal K = M/dt^2 + C/2dt (integrator
     // SVL_NM_CENTRAL_DIFFERENCE): element block of (M/dt^2 - C/2dt)(U - Up)
     // and the per-element mass-proportional Rayleigh factors (consistent mass)
-    bool cdmode = false;
+    bool cdmode = false, cd_general = false; // cd_general: constraints (T not identity) or support motion
     double* blk_cd = nullptr;               // [nc][E], or null (lumped mass, ak = 0 everywhere)
     double* eam = nullptr;                  // [E] am_e, or null
     // CG iterates recorded for training pairs
@@ -2335,6 +2410,32 @@ static int nm_op_total(svl_nm* nm, const double* pt, double* out) {
     return SVL_OK;
 }
 
+// Element parts of (c_m M + c_cs C) x, C's element part being sum_e (am_e M_e
+// with a consistent mass) + ak_e K0_e, into blkbuf; returns blkbuf, or null
+// when the model has no element part (lumped mass and ak = 0: diagonal only).
+static const double* ncd_elem(svl_nm* nm, const double* x, double* blkbuf, double c_m, double c_cs) {
+    svl_cd* cd = nm->cd;
+    const HostModel& m = cd->m;
+    DevView d = cd->d;
+    d.ftol = -1.0;
+    d.fe = blkbuf;
+    const int eg = (m.nelem + 127) / 128;
+    const double* blk = nullptr;
+    if (d.dk0) {                            // sum_e c_cs ak_e K0_e x_e
+        if (m.ndim == 2) k_element_tan<2, 4><<<eg, 128, 0, cd->stream>>>(d, x, m.ngp, 0, c_cs);
+        else k_element_tan<3, 8><<<eg, 128, 0, cd->stream>>>(d, x, m.ngp, 0, c_cs);
+        blk = blkbuf;
+        cd->launches += 1;
+    }
+    if (nm->consistent) {                   // + sum_e (c_m + c_cs am_e) M_e x_e
+        if (m.ndim == 2) k_mass_elem<2, 4><<<eg, 128, 0, cd->stream>>>(d, x, blkbuf, c_m, blk ? 1 : 0, nm->eam, c_cs);
+        else k_mass_elem<3, 8><<<eg, 128, 0, cd->stream>>>(d, x, blkbuf, c_m, blk ? 1 : 0, nm->eam, c_cs);
+        blk = blkbuf;
+        cd->launches += 1;
+    }
+    return blk;
+}
+
 // q = Keff v (free dofs); inner: an inner solve iteration, which takes the
 // single-precision operator when the handle has one
 static int nm_apply(svl_nm* nm, const double* v, double* q, bool inner = false) {
@@ -2342,26 +2443,20 @@ static int nm_apply(svl_nm* nm, const double* v, double* q, bool inner = false) 
     const HostModel& m = cd->m;
     const int tb = 256;
     if (nm->cdmode) {                       // q = (M/dt^2 + C/2dt) v (CentralDifference.cpp:70)
-        DevView d = cd->d;
-        d.ftol = -1.0;
-        d.fe = nm->fe_op;
-        const int eg = (m.nelem + 127) / 128;
+        const DevView& d = cd->d;
         const double c_m = 1.0 / nm->opts.dt / nm->opts.dt, c_c = 1.0 / 2.0 / nm->opts.dt;
-        k_nm_expand<<<(m.ntotal + tb - 1) / tb, tb, 0, cd->stream>>>(d, v, nm->pt);
-        const double* blk = nullptr;
-        if (d.dk0) {                        // sum_e ak_e/2dt K0_e p_e
-            if (m.ndim == 2) k_element_tan<2, 4><<<eg, 128, 0, cd->stream>>>(d, nm->pt, m.ngp, 0, c_c);
-            else k_element_tan<3, 8><<<eg, 128, 0, cd->stream>>>(d, nm->pt, m.ngp, 0, c_c);
-            blk = nm->fe_op;
-            cd->launches += 1;
-        }
-        if (nm->consistent) {               // + sum_e (1/dt^2 + am_e/2dt) M_e p_e
-            if (m.ndim == 2) k_mass_elem<2, 4><<<eg, 128, 0, cd->stream>>>(d, nm->pt, nm->fe_op, c_m, blk ? 1 : 0, nm->eam, c_c);
-            else k_mass_elem<3, 8><<<eg, 128, 0, cd->stream>>>(d, nm->pt, nm->fe_op, c_m, blk ? 1 : 0, nm->eam, c_c);
-            blk = nm->fe_op;
-            cd->launches += 1;
-        }
+        if (nm->cd_general) k_nmg_expand<<<(m.ntotal + tb - 1) / tb, tb, 0, cd->stream>>>(d, v, nm->pt);
+        else k_nm_expand<<<(m.ntotal + tb - 1) / tb, tb, 0, cd->stream>>>(d, v, nm->pt);
+        const double* blk = ncd_elem(nm, nm->pt, nm->fe_op, c_m, c_c);
         const double* Cd = nm->consistent ? nullptr : d.Cd;
+        if (nm->cd_general) {               // q = T^T K T v
+            if (m.ndim == 2) k_ncd_total<2><<<(m.nnode + tb - 1) / tb, tb, 0, cd->stream>>>(d, blk, nm->pt, nm->ft, c_m, c_c, Cd);
+            else k_ncd_total<3><<<(m.nnode + tb - 1) / tb, tb, 0, cd->stream>>>(d, blk, nm->pt, nm->ft, c_m, c_c, Cd);
+            k_nmg_reduce<<<(nm->nf + tb - 1) / tb, tb, 0, cd->stream>>>(cd->d, nm->ft, nullptr, q);
+            cd->launches += 3;
+            CUDA_TRY(cudaGetLastError());
+            return SVL_OK;
+        }
         if (m.ndim == 2) k_ncd_apply<2><<<(m.nnode + tb - 1) / tb, tb, 0, cd->stream>>>(d, blk, nm->pt, q, c_m, c_c, Cd);
         else k_ncd_apply<3><<<(m.nnode + tb - 1) / tb, tb, 0, cd->stream>>>(d, blk, nm->pt, q, c_m, c_c, Cd);
         cd->launches += 2;
@@ -2652,13 +2747,12 @@ static int ncd_setup(svl_nm* nm) {
         set_error("central difference: the Linear algorithm with the Jacobi preconditioner");
         return SVL_ERR_UNSUPPORTED;
     }
-    if (m.has_j2()) { set_error("central difference with a non-diagonal effective stiffness covers elastic materials"); return SVL_ERR_UNSUPPORTED; }
-    if (!cd->identity_T || cd->has_sm || !m.dp_eta.empty() || cd->d.ndrm > 0) {
-        set_error("central difference with a non-diagonal effective stiffness is covered without constraints, "
-                  "support motion, dashpots or domain-reduction loads");
+    if (cd->d.ndrm > 0) {
+        set_error("central difference with a non-diagonal effective stiffness is covered without domain-reduction loads");
         return SVL_ERR_UNSUPPORTED;
     }
     nm->cdmode = true;
+    nm->cd_general = !cd->identity_T || cd->has_sm;
     nm->consistent = !m.lumped;
     nm->general = nm->damped = nm->newton = nm->tangent = false;
     nm->nf = m.nfree;
@@ -2693,14 +2787,21 @@ static int ncd_setup(svl_nm* nm) {
         for (int t = 0; t < m.ntotal; ++t) Kd[t] += c_c * Cm[t];
     }
     for (int t = 0; t < m.ntotal; ++t) Kd[t] += c_m * Md[t];
+    for (size_t i = 0; i < m.dp_eta.size(); ++i) {   // ZeroLength1D dashpots: eta on both dofs
+        Kd[m.dp_dof[2 * i]] += c_c * m.dp_eta[i];
+        Kd[m.dp_dof[2 * i + 1]] += c_c * m.dp_eta[i];
+    }
+    // Jacobi scale: the diagonal of T^T diag(K) T
+    std::vector<int32_t> Tp, Tc;
+    std::vector<double> Tv, dg(std::max(m.nfree, 1), 0.0);
+    build_total_to_free(m, Tp, Tc, Tv);
+    for (int t = 0; t < m.ntotal; ++t)
+        for (int i = Tp[t]; i < Tp[t + 1]; ++i) dg[Tc[i]] += Tv[i] * Tv[i] * Kd[t];
     std::vector<double> dinv(std::max(m.nfree, 1), 1.0);
-    for (int n = 0; n < m.nnode; ++n)
-        for (int c = 0; c < m.ndof; ++c) {
-            const int t = m.tdof[(size_t)n * m.ndof + c], f = m.fdof[(size_t)n * m.ndof + c];
-            if (f < 0) continue;
-            if (!(Kd[t] > 0.0)) { set_error("free dof %d has no mass", f); return SVL_ERR_INVALID; }
-            dinv[f] = 1.0 / Kd[t];
-        }
+    for (int f = 0; f < m.nfree; ++f) {
+        if (!(dg[f] > 0.0)) { set_error("free dof %d has no mass", f); return SVL_ERR_INVALID; }
+        dinv[f] = 1.0 / dg[f];
+    }
     int st;
     double** vecs[] = {&nm->b, &nm->x, &nm->r, &nm->z, &nm->p, &nm->q};
     for (double** pv : vecs) if ((st = cd->zeros((size_t)std::max(m.nfree, 1), pv))) return st;
@@ -2712,6 +2813,10 @@ static int ncd_setup(svl_nm* nm) {
     nm->dinv = const_cast<double*>(dd);
     if (nm->consistent || cd->d.dk0) {
         if ((st = cd->zeros((size_t)nc * m.nelem, &nm->fe_op)) || (st = cd->zeros((size_t)nc * m.nelem, &nm->blk_cd))) return st;
+    }
+    if (nm->cd_general) {
+        double** tv[] = {&nm->ft, &nm->dUt, &nm->smv, &nm->lg};
+        for (double** pv : tv) if ((st = cd->zeros((size_t)m.ntotal, pv))) return st;
     }
     if (nm->consistent && any_am) {
         for (int e = 0; e < m.nelem; ++e) eam.push_back(m.ray[2 * (size_t)e]);
@@ -3161,37 +3266,48 @@ static int ncd_step(svl_nm* nm, double* U_hist_row) {
     svl_cd* cd = nm->cd;
     const HostModel& m = cd->m;
     const double c_m = 1.0 / nm->opts.dt / nm->opts.dt, c_c = 1.0 / 2.0 / nm->opts.dt;
-    const int tb = 256, ng = (m.nnode + tb - 1) / tb, eg = (m.nelem + 127) / 128;
+    const int tb = 256, ng = (m.nnode + tb - 1) / tb, eg = (m.nelem + 127) / 128, gt = (m.ntotal + tb - 1) / tb;
     k_step_inc<<<1, 1, 0, cd->stream>>>(cd->d.step);
     if (m.ndim == 2) k_element<2, 4><<<eg, 128, 0, cd->stream>>>(cd->d, cd->d.Us, m.ngp, 0);
     else k_element<3, 8><<<eg, 128, 0, cd->stream>>>(cd->d, cd->d.Us, m.ngp, 0);
-    k_ncd_w<<<(m.ntotal + tb - 1) / tb, tb, 0, cd->stream>>>(cd->d, nm->wvec);
+    k_ncd_w<<<gt, tb, 0, cd->stream>>>(cd->d, nm->wvec);
     cd->launches += 3;
-    DevView d = cd->d;
-    d.ftol = -1.0;
-    d.fe = nm->blk_cd;
-    const double* blk = nullptr;
-    if (d.dk0) {                            // - sum_e ak_e/2dt K0_e w_e
-        if (m.ndim == 2) k_element_tan<2, 4><<<eg, 128, 0, cd->stream>>>(d, nm->wvec, m.ngp, 0, -c_c);
-        else k_element_tan<3, 8><<<eg, 128, 0, cd->stream>>>(d, nm->wvec, m.ngp, 0, -c_c);
-        blk = nm->blk_cd;
-        cd->launches += 1;
-    }
-    if (nm->consistent) {                   // + sum_e (1/dt^2 - am_e/2dt) M_e w_e
-        if (m.ndim == 2) k_mass_elem<2, 4><<<eg, 128, 0, cd->stream>>>(d, nm->wvec, nm->blk_cd, c_m, blk ? 1 : 0, nm->eam, -c_c);
-        else k_mass_elem<3, 8><<<eg, 128, 0, cd->stream>>>(d, nm->wvec, nm->blk_cd, c_m, blk ? 1 : 0, nm->eam, -c_c);
-        blk = nm->blk_cd;
-        cd->launches += 1;
-    }
+    // element parts of (M/dt^2 - C/2dt)(U - Up)
+    const double* blk = ncd_elem(nm, nm->wvec, nm->blk_cd, c_m, -c_c);
     const double* Cd = nm->consistent ? nullptr : cd->d.Cd;
-    if (m.ndim == 2) k_ncd_rhs<2><<<ng, tb, 0, cd->stream>>>(cd->d, blk, nm->wvec, nm->b, c_m, c_c, Cd);
-    else k_ncd_rhs<3><<<ng, tb, 0, cd->stream>>>(cd->d, blk, nm->wvec, nm->b, c_m, c_c, Cd);
-    cd->launches += 1;
+    if (!nm->cd_general) {
+        if (m.ndim == 2) k_ncd_rhs<2><<<ng, tb, 0, cd->stream>>>(cd->d, blk, nm->wvec, nm->b, c_m, c_c, Cd);
+        else k_ncd_rhs<3><<<ng, tb, 0, cd->stream>>>(cd->d, blk, nm->wvec, nm->b, c_m, c_c, Cd);
+        cd->launches += 1;
+    } else {
+        // Feff = T^T R - T^T (K SM) (CentralDifference.cpp:189-201, 217-220)
+        if (m.ndim == 2) k_ncd_rtotal<2><<<ng, tb, 0, cd->stream>>>(cd->d, blk, nm->wvec, nm->ft, c_m, c_c, Cd);
+        else k_ncd_rtotal<3><<<ng, tb, 0, cd->stream>>>(cd->d, blk, nm->wvec, nm->ft, c_m, c_c, Cd);
+        const double* lg = nullptr;
+        if (cd->has_sm) {
+            k_ncd_sm<<<gt, tb, 0, cd->stream>>>(cd->d, nm->smv);
+            const double* bk = ncd_elem(nm, nm->smv, nm->fe_op, c_m, c_c);
+            if (m.ndim == 2) k_ncd_total<2><<<ng, tb, 0, cd->stream>>>(cd->d, bk, nm->smv, nm->lg, c_m, c_c, Cd);
+            else k_ncd_total<3><<<ng, tb, 0, cd->stream>>>(cd->d, bk, nm->smv, nm->lg, c_m, c_c, Cd);
+            lg = nm->lg;
+            cd->launches += 2;
+        }
+        k_nmg_reduce<<<(nm->nf + tb - 1) / tb, tb, 0, cd->stream>>>(cd->d, nm->ft, lg, nm->b);
+        cd->launches += 2;
+    }
     CUDA_TRY(cudaGetLastError());
     TRY(nm_solve(nm));
-    if (m.ndim == 2) k_ncd_update<2><<<ng, tb, 0, cd->stream>>>(cd->d, nm->x, c_m, c_c, cd->d.flag);
-    else k_ncd_update<3><<<ng, tb, 0, cd->stream>>>(cd->d, nm->x, c_m, c_c, cd->d.flag);
-    cd->launches += 1;
+    if (!nm->cd_general) {
+        if (m.ndim == 2) k_ncd_update<2><<<ng, tb, 0, cd->stream>>>(cd->d, nm->x, c_m, c_c, cd->d.flag);
+        else k_ncd_update<3><<<ng, tb, 0, cd->stream>>>(cd->d, nm->x, c_m, c_c, cd->d.flag);
+        cd->launches += 1;
+    } else {
+        k_nmg_expand<<<gt, tb, 0, cd->stream>>>(cd->d, nm->x, nm->dUt);
+        const double* sm = cd->has_sm ? nm->smv : nullptr;
+        if (m.ndim == 2) k_ncd_gupdate<2><<<ng, tb, 0, cd->stream>>>(cd->d, nm->dUt, sm, c_m, c_c, cd->d.flag);
+        else k_ncd_gupdate<3><<<ng, tb, 0, cd->stream>>>(cd->d, nm->dUt, sm, c_m, c_c, cd->d.flag);
+        cd->launches += 2;
+    }
     CUDA_TRY(cudaGetLastError());
     if (U_hist_row) CUDA_TRY(cudaMemcpyAsync(U_hist_row, cd->d.U, sizeof(double) * m.ntotal, cudaMemcpyDeviceToHost, cd->stream));
     return SVL_OK;

@@ -539,8 +539,9 @@ class CentralDifferenceSolve(NewmarkBeta):
     CONSISTENT, or stiffness-proportional Rayleigh damping): each step solves
     T^T K T du = Feff (CentralDifference.cpp:204-231) by the matrix-free
     Jacobi-PCG of svl_nm in its central-difference mode to a true relative
-    residual of `pcg_tol`, where the reference factorises K once.  Same step
-    methods as CentralDifference; reaction forces are not covered."""
+    residual of `pcg_tol`, where the reference factorises K once.  Elastic
+    and J2 materials, EQUAL constraints, support motion and dashpots; same
+    step methods as CentralDifference; reaction forces are not covered."""
 
     _integrator = capi.SVL_NM_CENTRAL_DIFFERENCE
 

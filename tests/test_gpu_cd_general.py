@@ -93,8 +93,58 @@ def test_nondiagonal_central_difference_steps_and_responses(gpu):
 
 
 def test_nondiagonal_central_difference_rejects_what_it_does_not_cover(gpu):
-    m, L, dt = _case("q4_consistent")
-    m.dashpot_dof = np.array([[int(m.totaldof[3, 0]), int(m.totaldof[4, 0])]], np.int32)
-    m.dashpot_eta = np.array([1.0e5])
+    """Domain-reduction loads are not covered by the solve mode."""
+    from tests.helpers import drm_box
+    m, L, dt, _, _ = drm_box(nt=20)
+    m.lumped = False
     with pytest.raises(SvlError):
         CentralDifference(m, L, dt)
+
+
+def _j2_h8():
+    from svl_gb300 import _capi as capi
+    m, L, dt = h8_box(5, 4, 3, nt=200, amp=4.0e8)
+    ne = m.nelem
+    G = m.mat_param[:, 0] / (2 * 1.3)
+    K = m.mat_param[:, 0] / (3 * (1 - 0.6))
+    m.mat_type = np.full(ne, capi.SVL_MAT_PLASTIC3DJ2, np.int32)
+    mp = np.zeros((ne, 8))
+    mp[:, 0], mp[:, 1], mp[:, 2], mp[:, 3], mp[:, 4], mp[:, 5] = K, G, 2100.0, 0.02 * G, 1.0, 2.0e5
+    m.mat_param = mp
+    m.lumped = False
+    return m, L, 0.5 * dt
+
+
+GENERAL = ["h8_j2_consistent", "q4_j2_columns_consistent_rayleigh", "lysmer_consistent"]
+
+
+def _general(case):
+    from tests.helpers import lysmer_box, q4_j2_columns
+    if case == "h8_j2_consistent":
+        return _j2_h8()
+    if case == "q4_j2_columns_consistent_rayleigh":
+        m, L, dt = q4_j2_columns(3, 4, (10, 16, 22), nt=300, pga=6.0)
+        m.lumped = False
+        m.rayleigh = np.tile([1.0, 1.0e-4], (m.nelem, 1))
+        return m, L, 0.5 * dt
+    m, L, dt = lysmer_box(16, 8, nt=300)
+    m.lumped = False
+    return m, L, 0.5 * dt
+
+
+@pytest.mark.parametrize("case", GENERAL)
+def test_nondiagonal_central_difference_j2_constraints_support_motion_dashpots(case, gpu):
+    """J2 materials (element update once per step), EQUAL constraints with
+    support motion (periodic soil columns shaken at the base: Feff = T^T R -
+    T^T K SM(k), dU = T du + SM(k)) and Lysmer dashpots in K, with a
+    consistent mass, against the oracle's factorised solve."""
+    m, L, dt = _general(case)
+    n = 200
+    cd = CentralDifference(m, L, dt)
+    assert isinstance(cd, CentralDifferenceSolve)
+    cd.Initialize()
+    hg = cd.run(1, n, history=True)
+    cd.close()
+    ho, *_ = O.cd_run(m, L, dt, n)
+    assert np.abs(ho).max() > 0
+    assert rel_l2(hg, ho) <= 1e-8
