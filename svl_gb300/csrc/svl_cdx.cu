@@ -1043,6 +1043,11 @@ struct svl_cdx {
     // schedule (svl_cdx_set_schedule / svl_cdx_tune): tile order of the fused
     // kernel, block size of the band's element kernels, band stream priority
     std::vector<int32_t> tiles_base;     // the scheduled tiles in natural order (full ids)
+    // with a PML band: tiles whose owned nodes and halo hold no PML node
+    // ("far" tiles) come first in d_tiles; they step without waiting for the
+    // band's displacement update of the previous step
+    std::vector<char> tile_near;         // [ntz][nty][ntx] 1: a PML node in the tile or its halo
+    int ntiles_far = 0;
     int tile_order = 0, band_threads = 128, band_hi = 1;
     cudaEvent_t filled[2] = {nullptr, nullptr}, drained[2] = {nullptr, nullptr};
 
@@ -1180,6 +1185,8 @@ extern "C" {
 // grids come embedded in their bounding grid: ext [ninst][3] gives each
 // instance's own node extents (the tiles beyond them are not scheduled) and
 // emb its own-to-embedded dof maps; both null for instances of one grid.
+static int upload_tile_order(svl_cdx* h, int order);
+
 static int cdx_create_impl(const svl_grid_spec* g, int32_t ninst, const svl_model_desc* models,
                            const svl_load_desc* loads, const svl_cd_opts* opts, svl_cdx** out, const int32_t* ext,
                            const std::vector<std::vector<long long>>* emb) {
@@ -1550,6 +1557,22 @@ static int cdx_create_impl(const svl_grid_spec* g, int32_t ninst, const svl_mode
         h->tiles_base.resize((size_t)h->ntiles);
         for (int t = 0; t < h->ntiles; ++t) h->tiles_base[t] = t;
     }
+    if (h->np > 0 && !ext) {
+        // a tile reads nodes x0-1 .. x0+TX (and the same in y, z): mark the
+        // tiles that meet a PML node there (the layout is every instance's)
+        h->tile_near.assign((size_t)h->ntx * h->nty * h->ntz, 0);
+        for (long long n = 0; n < h->nn; ++n) {
+            if (pidx[n] < 0) continue;
+            const int x = (int)(n % nxn), y = (int)((n / nxn) % nyn), z = (int)(n / ((long long)nxn * nyn));
+            const int tx0 = std::max(0, (x - TX + TX - 1) / TX), tx1 = std::min(h->ntx - 1, (x + 1) / TX);
+            const int ty0 = std::max(0, (y - TY + TY - 1) / TY), ty1 = std::min(h->nty - 1, (y + 1) / TY);
+            const int tz0 = std::max(0, (z - TZ + TZ - 1) / TZ), tz1 = std::min(h->ntz - 1, (z + 1) / TZ);
+            for (int tz = tz0; tz <= tz1; ++tz)
+                for (int ty = ty0; ty <= ty1; ++ty)
+                    for (int tx = tx0; tx <= tx1; ++tx) h->tile_near[((size_t)tz * h->nty + ty) * h->ntx + tx] = 1;
+        }
+        if ((st = upload_tile_order(h, 0))) return fail(st);
+    }
     // history map: the instances one after the other, each in its own numbering
     {
         if (emb) h->own2emb = *emb;
@@ -1838,16 +1861,32 @@ static int cdx_step(svl_cdx* h, int k, bool want_va) {
     v.status = h->status;
     v.fsol = h->fsol;
     const size_t ns = (size_t)h->nstate;
-    // u_n at the PML nodes comes from the band's displacement update of the
-    // previous step
-    if (h->np > 0) CUDA_TRY(cudaStreamWaitEvent(h->stream, h->ev_uu, 0));
     if (want_va) {
+        if (h->np > 0) CUDA_TRY(cudaStreamWaitEvent(h->stream, h->ev_uu, 0));
         CUDA_TRY(cudaMemcpyAsync(h->ph_copy, v.uh_prev, ns * 4, cudaMemcpyDeviceToDevice, h->stream));
         CUDA_TRY(cudaMemcpyAsync(h->pl_copy, v.ul_prev, ns * 4, cudaMemcpyDeviceToDevice, h->stream));
     }
-    k_cdx_step<<<h->grid, NTHREADS, SMEM_BYTES, h->stream>>>(h->tmap[h->cur], h->tmap_lam, h->tmap_mu, h->own_ul[h->cur],
-                                                             h->own_uh[1 - h->cur], h->own_ul[1 - h->cur], h->own_cd, v);
-    ++h->launches;
+    auto launch = [&](int first, int count) {
+        CdxView w = v;
+        w.tiles = v.tiles + first;
+        w.ntiles = count;
+        k_cdx_step<<<std::min(count, h->grid), NTHREADS, SMEM_BYTES, h->stream>>>(
+            h->tmap[h->cur], h->tmap_lam, h->tmap_mu, h->own_ul[h->cur], h->own_uh[1 - h->cur], h->own_ul[1 - h->cur],
+            h->own_cd, w);
+        ++h->launches;
+    };
+    if (h->np > 0) {
+        // far tiles (no PML node in the tile or its halo) do not read what the
+        // band's displacement update of the previous step writes: they run
+        // while it finishes; the near tiles wait for it (u_n at the PML nodes)
+        if (h->ntiles_far > 0) launch(0, h->ntiles_far);
+        CUDA_TRY(cudaStreamWaitEvent(h->stream, h->ev_uu, 0));
+        if (h->ntiles > h->ntiles_far) launch(h->ntiles_far, h->ntiles - h->ntiles_far);
+    } else {
+        k_cdx_step<<<h->grid, NTHREADS, SMEM_BYTES, h->stream>>>(h->tmap[h->cur], h->tmap_lam, h->tmap_mu, h->own_ul[h->cur],
+                                                                 h->own_uh[1 - h->cur], h->own_ul[1 - h->cur], h->own_cd, v);
+        ++h->launches;
+    }
     if (h->np > 0) {
         // the PML band on its stream: element forces on the displacement rows
         // (inputs from the previous step's stress update, in stream order), then,
@@ -2088,6 +2127,23 @@ static std::vector<int32_t> tile_schedule(const svl_cdx* h, int order) {
     return t;
 }
 
+// Uploads the tile order: far tiles first (a stable partition, each part in
+// the order's sequence) when the handle has a PML band.
+static int upload_tile_order(svl_cdx* h, int order) {
+    std::vector<int32_t> t = tile_schedule(h, order);
+    h->ntiles_far = 0;
+    if (!h->tile_near.empty()) {
+        const long long per = (long long)h->ntx * h->nty * h->ntz;
+        auto far = [&](int32_t full) { return !h->tile_near[(size_t)(full % per)]; };
+        std::stable_partition(t.begin(), t.end(), far);
+        h->ntiles_far = (int)std::count_if(t.begin(), t.end(), far);
+    }
+    if (!h->d_tiles) TRY(h->alloc(t.size(), &h->d_tiles));
+    CUDA_TRY(cudaMemcpy(h->d_tiles, t.data(), t.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+    h->tile_order = order;
+    return SVL_OK;
+}
+
 int svl_cdx_set_schedule(svl_cdx* h, const int32_t* choice) {
     if (!h || !choice) { set_error("bad argument"); return SVL_ERR_INVALID; }
     if (choice[1] < 0 || choice[1] > 3 || (choice[2] != 128 && choice[2] != 256) || choice[3] < 0 || choice[3] > 1) {
@@ -2096,12 +2152,7 @@ int svl_cdx_set_schedule(svl_cdx* h, const int32_t* choice) {
     TRY(svl_cdx_set_ctas(h, choice[0]));
     CUDA_TRY(cudaStreamSynchronize(h->stream));
     if (h->bstream) CUDA_TRY(cudaStreamSynchronize(h->bstream));
-    if (choice[1] != h->tile_order) {
-        const std::vector<int32_t> t = tile_schedule(h, choice[1]);
-        if (!h->d_tiles) TRY(h->alloc(t.size(), &h->d_tiles));
-        CUDA_TRY(cudaMemcpy(h->d_tiles, t.data(), t.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
-        h->tile_order = choice[1];
-    }
+    if (choice[1] != h->tile_order) TRY(upload_tile_order(h, choice[1]));
     h->band_threads = choice[2];
     if (choice[3] != h->band_hi) {
         int lo_pri = 0, hi_pri = 0;

@@ -186,6 +186,43 @@ def test_cdx_pml_band_matches_oracle(gpu):
             assert rel_l2(ubar[pd], Ubo[pd]) <= 1e-4
 
 
+def test_cdx_pml_far_tiles_step_before_the_band(gpu):
+    """With a PML band the tiles whose nodes and halo hold no PML node run in
+    a launch that does not wait for the band's displacement update of the
+    previous step, the others after it.  A grid with such tiles (32 x 24 x 20,
+    3-element band: 4 far tiles of 60 per instance), two instances, several
+    tiles per CTA in both launches: the displacement and stress histories
+    against the FP64 explicit PML scheme of the PML-capable handle (itself
+    pinned to the oracle) at the mixed bar, and the same bits for every
+    schedule."""
+    from svl_gb300 import CentralDifference
+    nx, ny, nz, npml = 32, 24, 20, 3
+    nt = 150
+    inst, dt = _pml_instances(nx, ny, nz, npml, (3, 4), nt)
+    cdx = StructuredCentralDifference((nx, ny, nz), (2.0, 2.0, 2.0), inst, dt)
+    ref = None
+    for sched in (dict(ctas=5), dict(ctas=3, tile_order=3), dict(ctas=0, tile_order=2, band_threads=256)):
+        cdx.set_schedule(**sched)
+        for b in range(len(inst)):
+            cdx.Initialize(b)
+        hist = cdx.run(1, nt, history=True)
+        if ref is None:
+            ref = hist
+        else:
+            assert np.array_equal(hist, ref), sched
+    cdx.close()
+    for b, (m, L) in enumerate(inst):
+        cd = CentralDifference(m, L, dt)
+        cd.Initialize()
+        h64 = cd.run(1, nt, history=True)
+        cd.close()
+        u, s = _udofs(m)
+        assert np.abs(h64[:, u]).max() > 0 and np.abs(h64[:, s]).max() > 0
+        eu = rel_l2(ref[:, b, u], h64[:, u])
+        es = rel_l2(ref[:, b, s], h64[:, s])
+        assert eu <= TOL_MIXED and es <= TOL_MIXED, (b, eu, es)
+
+
 def test_uneven_ensemble_matches_oracle_and_single_runs(gpu):
     """Instances of uneven grids in one fused launch (svl_cdx_create_ensemble):
     each embedded in the bounding grid, only the tiles meeting its own nodes
