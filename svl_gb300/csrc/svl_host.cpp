@@ -247,9 +247,12 @@ void parallel_for(int64_t n, const std::function<void(int64_t, int64_t)>& body) 
     for (auto& t : th) t.join();
 }
 
-// Row-sum lumped mass of every element node, diag[(e*nen + a)*nd + j].
-static void lumped_element_diag(const HostModel& m, std::vector<double>& diag) {
+// Row-sum lumped mass of every element node, diag[(e*nen + a)*nd + j],
+// computed once per host model into its cache.
+static const std::vector<double>& lumped_element_ref(const HostModel& m) {
     const int nd = m.ndim, nen = m.nen, nc = nen * m.ndof;
+    if (m.elem_lumped.size() == (size_t)m.nelem * nen * nd) return m.elem_lumped;
+    std::vector<double>& diag = m.elem_lumped;
     diag.assign((size_t)m.nelem * nen * nd, 0.0);
     // The consistent mass of a displacement element is block diagonal in the
     // components, Me[(a,j)][(b,j)] = sum_q c_q N_a N_b for every j, so the
@@ -277,15 +280,15 @@ static void lumped_element_diag(const HostModel& m, std::vector<double>& diag) {
             }
         }
     });
+    return diag;
 }
 
-void element_lumped_masses(const HostModel& m, std::vector<double>& diag) { lumped_element_diag(m, diag); }
+void element_lumped_masses(const HostModel& m, std::vector<double>& diag) { diag = lumped_element_ref(m); }
 
 void lumped_mass_diag(const HostModel& m, double mtol, std::vector<double>& M) {
     const int nd = m.ndim, nen = m.nen;
     // element diagonals in parallel, assembled afterwards in element order
-    std::vector<double> diag;
-    lumped_element_diag(m, diag);
+    const std::vector<double>& diag = lumped_element_ref(m);
     std::vector<double> Me_e(m.ntotal, 0.0);
     for (int e = 0; e < m.nelem; ++e)
         for (int a = 0; a < nen; ++a)
@@ -321,8 +324,7 @@ void rayleigh_mass_diag(const HostModel& m, std::vector<double>& C) {
     const int nd = m.ndim, nen = m.nen;
     C.assign(m.ntotal, 0.0);
     if (m.ray.empty()) return;
-    std::vector<double> diag;
-    lumped_element_diag(m, diag);
+    const std::vector<double>& diag = lumped_element_ref(m);
     for (int e = 0; e < m.nelem; ++e) {
         const double am = m.ray[2 * (size_t)e];
         if (am == 0.0) continue;
@@ -371,22 +373,37 @@ int build_load_tables(const HostModel& m, const svl_load_desc* L, LoadTables& o)
 
 void build_total_to_free(const HostModel& m, std::vector<int32_t>& ptr,
                          std::vector<int32_t>& col, std::vector<double>& val) {
-    std::vector<std::vector<std::pair<int32_t, double>>> rows(m.ntotal);
+    // rows of T as CSR: the identity entry of a free dof, then the masters of
+    // a constrained one in constraint order; each row sorted by column (a
+    // stable sort) with repeated columns summed
+    const int nt = m.ntotal;
+    std::vector<int64_t> start(nt + 1, 0);
+    for (int n = 0; n < m.nnode; ++n)
+        for (int j = 0; j < m.nndof[n]; ++j)
+            if (m.fdof_all[(size_t)n * m.dstride + j] > -1) ++start[m.tdof_all[(size_t)n * m.dstride + j] + 1];
+    for (int c = 0; c < m.nconstraint; ++c) start[m.cslave[c] + 1] += m.cptr[c + 1] - m.cptr[c];
+    for (int t = 0; t < nt; ++t) start[t + 1] += start[t];
+    std::vector<std::pair<int32_t, double>> ent((size_t)start[nt]);
+    std::vector<int64_t> fill(start.begin(), start.end() - 1);
     for (int n = 0; n < m.nnode; ++n)
         for (int j = 0; j < m.nndof[n]; ++j) {
             const int32_t f = m.fdof_all[(size_t)n * m.dstride + j];
-            if (f > -1) rows[m.tdof_all[(size_t)n * m.dstride + j]].push_back({f, 1.0});
+            if (f > -1) ent[(size_t)fill[m.tdof_all[(size_t)n * m.dstride + j]]++] = {f, 1.0};
         }
     for (int c = 0; c < m.nconstraint; ++c)
-        for (int i = m.cptr[c]; i < m.cptr[c + 1]; ++i) rows[m.cslave[c]].push_back({m.cmaster[i], m.cfactor[i]});
-    ptr.assign(m.ntotal + 1, 0);
+        for (int i = m.cptr[c]; i < m.cptr[c + 1]; ++i) ent[(size_t)fill[m.cslave[c]]++] = {m.cmaster[i], m.cfactor[i]};
+    ptr.assign(nt + 1, 0);
     col.clear(); val.clear();
-    for (int t = 0; t < m.ntotal; ++t) {
-        std::sort(rows[t].begin(), rows[t].end(),
-                  [](const std::pair<int32_t, double>& a, const std::pair<int32_t, double>& b) { return a.first < b.first; });
-        for (size_t i = 0; i < rows[t].size(); ++i) {
-            if (!col.empty() && (int)col.size() > ptr[t] && col.back() == rows[t][i].first) val.back() += rows[t][i].second;
-            else { col.push_back(rows[t][i].first); val.push_back(rows[t][i].second); }
+    col.reserve(ent.size()); val.reserve(ent.size());
+    for (int t = 0; t < nt; ++t) {
+        auto b = ent.begin() + start[t], e = ent.begin() + start[t + 1];
+        if (e - b > 1)
+            std::stable_sort(b, e, [](const std::pair<int32_t, double>& x, const std::pair<int32_t, double>& y) {
+                return x.first < y.first;
+            });
+        for (auto it = b; it != e; ++it) {
+            if ((int)col.size() > ptr[t] && col.back() == it->first) val.back() += it->second;
+            else { col.push_back(it->first); val.push_back(it->second); }
         }
         ptr[t + 1] = (int32_t)col.size();
     }
@@ -437,8 +454,7 @@ int explicit_pml_tables(const HostModel& m, double dt, double mtol, const LoadTa
     std::vector<int> sidx_of(m.nelem, -1), pidx_of(m.nelem, -1);
     for (size_t i = 0; i < sol.size(); ++i) sidx_of[sol[i]] = (int)i;
     for (size_t i = 0; i < pml.size(); ++i) pidx_of[pml[i]] = (int)i;
-    std::vector<double> ml;
-    element_lumped_masses(m, ml);                 // [(e nen + a) nd + j]
+    const std::vector<double>& ml = lumped_element_ref(m);   // [(e nen + a) nd + j]
     // per PML element, matrix w and node j the Gauss sum g = sum_q s_w N_j w|J|
     // (every entry of the node's lumped blocks is g times a material constant),
     // in parallel; assembled below in element order

@@ -58,6 +58,9 @@ struct HostModel {
     std::vector<int32_t> cslave, cptr, cmaster;
     std::vector<double> cfactor;
     int lumped = 1;
+    // row-sum lumped element masses [(e nen + a) nd + j], filled by the first
+    // caller that needs them (the model does not change afterwards)
+    mutable std::vector<double> elem_lumped;
 
     bool has_j2() const;
     bool has_pml() const { return !epml.empty(); }
