@@ -199,6 +199,8 @@ struct CdxView {
                                          // -1 on the displacement dofs of PML nodes
     float* fsol;                         // PML nodes: the solid elements' force sum (same layout), or null
     const float* __restrict__ bop;       // [B_ROWS x 24] hi then lo operand image
+    float kscale;                        // the B image holds K / kscale (1: hi/lo split of K)
+    int b_exact;                         // 1: the B image is exact in TF32 (its lo half zero)
     // external loads grouped by tile, then by dof
     const int* __restrict__ tl_ptr;      // [full tiles + 1] into the unique-dof arrays
     const long long* __restrict__ ld_dof;// padded index of the dof
@@ -394,9 +396,10 @@ k_cdx_step(const __grid_constant__ CUtensorMap tmap_u, const __grid_constant__ C
 #pragma unroll
                 for (int ks = 0; ks < KDIM / 8; ++ks) {       // three K=8 steps (2 core matrices each)
                     const uint32_t koff = ks * 2 * LBO;
-                    // the two small correction products first, then the main one
+                    // the small correction products first, then the main one;
+                    // an exact B image has no lo half
                     mma_tf32(d, make_desc(a_lo + koff), make_desc(bB + koff), kIdescN48, ks > 0);
-                    mma_tf32(d, make_desc(a_hi + koff), make_desc(bB + B_LO_OFF + koff), kIdescN48, 1);
+                    if (!v.b_exact) mma_tf32(d, make_desc(a_hi + koff), make_desc(bB + B_LO_OFF + koff), kIdescN48, 1);
                     mma_tf32(d, make_desc(a_hi + koff), make_desc(bB + koff), kIdescN48, 1);
                 }
                 mma_commit(B_DFULL(db));
@@ -438,7 +441,7 @@ k_cdx_step(const __grid_constant__ CUtensorMap tmap_u, const __grid_constant__ C
                     const uint32_t row = tmem + (uint32_t)b * ACC_COLS + ((uint32_t)(q * 32) << 16);
                     const int le = t * 128 + q * 32 + lane;
                     const int lx = le % EX, lr = min(le, NEL - 1) / EX;          // lr = lz*EY + ly
-                    const float l = tlam[lr * LMX + LM_SHIFT + lx], mu = tmu[lr * LMX + LM_SHIFT + lx];
+                    const float l = tlam[lr * LMX + LM_SHIFT + lx] * v.kscale, mu = tmu[lr * LMX + LM_SHIFT + lx] * v.kscale;
                     // cols 0-23 K_lambda u, 24-47 K_mu u
                     float dv[48];
 #pragma unroll
@@ -992,6 +995,8 @@ struct svl_cdx {
     int ntx = 0, nty = 0, ntz = 0, ntiles = 0, grid = 0;
     double dt = 0;
     double hgrid = 0;                    // element side (uniform cubes)
+    bool b_exact = false;                // the B image is exact in TF32 (see the image's construction)
+    float kscale = 1.0f;
     cudaStream_t stream = nullptr;
     std::vector<void*> allocs;
     float* uh[2] = {nullptr, nullptr};   // compensated displacement pairs (hi, lo), padded rows
@@ -1500,8 +1505,23 @@ static int cdx_create_impl(const svl_grid_spec* g, int32_t ninst, const svl_mode
         }
     }
     // B operand image, canonical K-major layout, 96 rows:
-    // [K_lambda hi; K_mu hi; K_lambda lo; K_mu lo] (24 rows each)
+    // [K_lambda hi; K_mu hi; K_lambda lo; K_mu lo] (24 rows each).  For a cube
+    // of side h every entry of K_lambda and K_mu is an integer times h/72 (up
+    // to the rounding of the Gauss abscissa, ~1e-15): the image then holds the
+    // integers, exact in TF32, its lo half is zero, the element force takes
+    // two products instead of three and lambda, mu are scaled by h/72.
     std::vector<float> bop(B_BYTES / 4, 0.f);
+    {
+        const double c = 72.0 / h->hgrid;
+        bool exact = g->h[1] == g->h[0] && g->h[2] == g->h[0];
+        for (int i2 = 0; i2 < 24 * 24 && exact; ++i2)
+            for (double kv : {Klam[i2] * c, Kmu[i2] * c})
+                exact = exact && std::fabs(kv - std::nearbyint(kv)) <= 1e-9 && std::fabs(kv) <= 1024.0;
+        h->b_exact = exact;
+        h->kscale = exact ? (float)(h->hgrid / 72.0) : 1.0f;
+        if (exact)
+            for (int i2 = 0; i2 < 24 * 24; ++i2) { Klam[i2] = std::nearbyint(Klam[i2] * c); Kmu[i2] = std::nearbyint(Kmu[i2] * c); }
+    }
     for (int n = 0; n < 48; ++n)
         for (int k = 0; k < 24; ++k) {
             const double val = n < 24 ? Klam[n * 24 + k] : Kmu[(n - 24) * 24 + k];
@@ -1858,6 +1878,8 @@ static int cdx_step(svl_cdx* h, int k, bool want_va) {
     v.tl_ptr = h->tl_ptr; v.ld_dof = h->ld_dof; v.ld_ptr = h->ld_ptr; v.ld_ser = h->ld_ser; v.ld_coef = h->ld_coef;
     v.s_ptr = h->s_ptr; v.s_val = h->s_val;
     v.k = k;
+    v.kscale = h->kscale;
+    v.b_exact = h->b_exact ? 1 : 0;
     v.status = h->status;
     v.fsol = h->fsol;
     const size_t ns = (size_t)h->nstate;
