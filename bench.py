@@ -603,7 +603,7 @@ def main():
     cd.run(1, warm)                                   # warm-up
     # schedule autotuner of the fused step (svl_cdx_tune): CTA count, tile
     # order, band block size and stream priority; the state is reset below
-    sched = cd.tune(1 + warm, 8) if hasattr(cd, "tune") else None
+    sched = cd.tune(1 + warm, 12) if hasattr(cd, "tune") else None
     prof = cd.profile(1 + warm + 200, 20) if hasattr(cd, "profile") else None
     prof_full = None
     if sched is not None:
