@@ -344,8 +344,8 @@ int  svl_cdx_get_ctas(svl_cdx* cdx, int32_t* ctas);
 int  svl_cdx_set_schedule(svl_cdx* cdx, const int32_t* choice);
 int  svl_cdx_get_schedule(svl_cdx* cdx, int32_t* choice);
 /* Autotuner: times nsteps steps (from k_first on, after two warm-up steps) of
- * every schedule in a small grid (six CTA counts from one per SM down to
- * 5/8 of the SMs, the four tile orders and, with a PML band, both block
+ * every schedule in a small grid (eight CTA counts from one per SM down to
+ * half of the SMs, the four tile orders and, with a PML band, both block
  * sizes and priorities), times the four fastest again over 4 * nsteps steps,
  * keeps the fastest of those and returns it in choice[4] (*ms_best: its time
  * per step in the second timing).  The steps advance the state: set the

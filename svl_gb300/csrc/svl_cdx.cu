@@ -2198,10 +2198,11 @@ int svl_cdx_tune(svl_cdx* h, int32_t k_first, int32_t nsteps, int32_t* choice, f
     int dev = 0, sms = 0;
     CUDA_TRY(cudaGetDevice(&dev));
     CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    // CTA counts from one per SM down to 5/8 of the SMs: fewer step CTAs
+    // CTA counts from one per SM down to half of the SMs: fewer step CTAs
     // leave whole SMs to the band kernels, which then overlap the step
     std::vector<int> ctas;
-    for (int c : {sms, sms - sms / 16, sms - sms / 8, sms - sms / 4, sms - 5 * sms / 16, sms - 3 * sms / 8}) {
+    for (int c : {sms, sms - sms / 16, sms - sms / 8, sms - sms / 4, sms - 5 * sms / 16, sms - 3 * sms / 8,
+                  sms - 7 * sms / 16, sms / 2}) {
         c = std::max(1, std::min(c, h->ntiles));                  // as svl_cdx_set_ctas clamps it
         if (std::find(ctas.begin(), ctas.end(), c) == ctas.end()) ctas.push_back(c);
     }
