@@ -283,8 +283,9 @@ void svl_cd_destroy(svl_cd* cd);
  * advanced together by one fused kernel per step.  The element force is the
  * tensor-core contraction F_e = lambda_e (K_lambda u_e) + mu_e (K_mu u_e):
  * the 48 x 24 stacked reference matrix times the 24 x elements displacement
- * block, TF32 hi/lo split operands (three products) with FP32 accumulation
- * in TMEM.  The displacement state is a compensated pair of FP32 numbers per
+ * block, the displacements split into TF32 hi + lo parts and the reference
+ * matrix exact in TF32 for cubes (integers times h/72; other shapes: also
+ * split, three products) with FP32 accumulation in TMEM.  The displacement state is a compensated pair of FP32 numbers per
  * dof (hi + lo, about 48 significant bits, updated with error-free TwoSum
  * transformations), not FP64; results state their error against the FP64
  * path (<= 1e-5 relative L2 over the history in the tests).  Reference summation order
