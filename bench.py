@@ -709,19 +709,20 @@ def main():
         ne2e = E2E_STEPS[args.workload]
         chunk = 20 if args.precision == "mixed" else (ne2e if args.workload == "config1" else 200)
         hbuf = pinned_empty((chunk, nb, m.ntotal) if args.precision == "mixed" else (chunk, m.ntotal))
-        t0 = time.perf_counter()
-        cd2 = make_handle()                             # host arrays -> device
-        t1 = time.perf_counter()
-        call_ms = []
-        for s0 in range(0, ne2e, chunk):
-            n = min(chunk, ne2e - s0)
-            tc = time.perf_counter()
-            if args.precision == "mixed" or not pml:
-                cd2.run(1 + s0, n, out=hbuf[:n])
-            else:                                       # the FP64 PML handle copies its history itself
-                hbuf[:n] = cd2.run(1 + s0, n, history=True)
-            call_ms.append((time.perf_counter() - tc) * 1e3 / n)
-        t2 = time.perf_counter()
+        with ClockSampler(local) as clk2:
+            t0 = time.perf_counter()
+            cd2 = make_handle()                             # host arrays -> device
+            t1 = time.perf_counter()
+            call_ms = []
+            for s0 in range(0, ne2e, chunk):
+                n = min(chunk, ne2e - s0)
+                tc = time.perf_counter()
+                if args.precision == "mixed" or not pml:
+                    cd2.run(1 + s0, n, out=hbuf[:n])
+                else:                                       # the FP64 PML handle copies its history itself
+                    hbuf[:n] = cd2.run(1 + s0, n, history=True)
+                call_ms.append((time.perf_counter() - tc) * 1e3 / n)
+            t2 = time.perf_counter()
         cd2.close()
         md_bytes = nb * (m.coords.nbytes + m.totaldof.nbytes + m.freedof.nbytes + m.conn.nbytes +
                          m.elem_mat.nbytes + m.mat_param.nbytes + m.mat_type.nbytes +
@@ -733,7 +734,10 @@ def main():
                "run_only_value": ws * nfree_total * ne2e / (t2 - t1),
                "chunk_steps": chunk,
                "call_ms_per_step_p10_p50_p90": [float(x) for x in np.percentile(call_ms, [10, 50, 90])],
+               "calls_slower_than_1.5x_median": int(np.sum(np.array(call_ms[1:]) > 1.5 * np.median(call_ms))),
+               "calls": len(call_ms),
                "first_call_ms_per_step": float(call_ms[0]),
+               "clocks": clk2.summary(),
                "includes": "handle creation from host arrays (model, loads) + the whole run with every instance's "
                            "full total-dof vector (displacements and PML stress dofs) copied to page-locked host "
                            "memory every step"}

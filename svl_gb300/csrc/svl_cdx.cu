@@ -1284,7 +1284,6 @@ static int cdx_create_impl(const svl_grid_spec* g, int32_t ninst, const svl_mode
     for (int b = 0; b < ninst; ++b) {
         if (pst[b]) return fail(pst[b]);
         HostModel& m = hms[b];
-        int st = SVL_OK;
         if (b == 0) {
             // numbering maps and the PML band layout, shared by every instance
             h->ntotal = m.ntotal;
