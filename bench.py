@@ -9,7 +9,7 @@ rho = 2100, double-couple body force (Ricker 3 Hz), dt = 0.5 h / max Vp, with
 their nodes) advanced by the library's explicit PML scheme -- as a batch of 4
 seeded realisations on the mixed-precision path: the elastic interior by the
 tcgen05 tensor-core step (TF32 hi/lo element forces, FP32 accumulation), the
-PML band by FP32 kernels, the state as compensated FP32 pairs ("tf32x3+f32x2").
+PML band by FP32 kernels, the state as compensated FP32 pairs ("tf32x2+f32x2": two TF32 products, hi and lo displacements times the exact stiffness patterns).
 The FP64 plain path (the same scheme in FP64 on the general handle) is timed
 on one realisation beside it, with the mixed result's error against it.
 
@@ -766,11 +766,12 @@ def main():
         line = {
             "metric": "DOF-steps/s", "value": value, "unit": "DOF-steps/s", "n_gpus": ws, "steps": args.steps,
             "warmup": warm, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "tf32x3+f32x2" if args.precision == "mixed" else "f64",
+            "vs_baseline": None, "dtype": "tf32x2+f32x2" if args.precision == "mixed" else "f64",
             "data": "synthetic (seeded)",
             "config": workload_config(desc, insts, dt, E2E_STEPS[args.workload]),
-            "precision": ("mixed: TF32 hi/lo tensor-core element forces with FP32 accumulation in the elastic "
-                          "interior, FP32 PML-band kernels, state as compensated FP32 pairs (~48 bits)"
+            "precision": ("mixed: tensor-core element forces in the elastic interior (displacements split into "
+                          "TF32 hi + lo, the element stiffness patterns exact in TF32, FP32 accumulation), FP32 "
+                          "PML-band kernels, state as compensated FP32 pairs (~48 bits)"
                           if args.precision == "mixed" else "fp64 plain"),
             "parallelism": "replicas" if ws > 1 else "single GPU",
             "l2": "no flush; working set ~%d MB > 129 MB L2" % ws_mb,
