@@ -338,35 +338,42 @@ k_cdx_step(const __grid_constant__ CUtensorMap tmap_u, const __grid_constant__ C
         // ===== builders: A operand rows (element x 24 dofs), TF32 hi / lo =====
         uint32_t ph_tma = 0u, ph_aempty = 3u;
         const int h = tid >> 7, m = tid & 127;
+        // half an element row of M-tile t from the halo: TF32 hi and lo parts
+        auto build_row = [&](const float* raw, int t, float (&hv)[12], float (&lv)[12]) {
+            const int le = t * 128 + m;
+            if (le < NEL) {
+                const int lx = le % EX, ly = (le / EX) % EY, lz = le / (EX * EY);
+                // nodes n1..n4 (h = 0) or n5..n8 (h = 1) of the element, in the raw halo rows
+                const int r0 = (lz + h) * HY + ly;
+                const float* p0 = raw + r0 * RAWX + (RAW_SHIFT + lx) * 3;
+                const float* p1 = p0 + RAWX;
+                const float u[12] = {p0[0], p0[1], p0[2], p0[3], p0[4], p0[5],
+                                     p1[3], p1[4], p1[5], p1[0], p1[1], p1[2]};
+#pragma unroll
+                for (int i = 0; i < 12; ++i) {
+                    hv[i] = to_tf32(u[i]);
+                    lv[i] = to_tf32(__fsub_rn(u[i], hv[i]));
+                }
+            } else {
+#pragma unroll
+                for (int i = 0; i < 12; ++i) { hv[i] = 0.f; lv[i] = 0.f; }
+            }
+        };
         for (int it = 0, mt = 0; it < ntile_cta && ok; ++it) {
             const int buf = it & 1;
             ok = mbar_wait(B_TMA(buf), PH(ph_tma, buf));
             FLIP(ph_tma, buf);
             const float* raw = reinterpret_cast<const float*>(smem + OFF_TT + buf * TT_STRIDE);
+            // the row of the next M-tile is read and converted while the
+            // current one's MMA runs (the halo buffer stays until this tile's
+            // update, which needs every M-tile's product first)
+            float hv[12], lv[12];
+            build_row(raw, 0, hv, lv);
             for (int t = 0; t < NMT && ok; ++t, ++mt) {
                 const int b = mt & 1;
                 ok = mbar_wait(B_AEMPTY(b), PH(ph_aempty, b));
                 FLIP(ph_aempty, b);
                 if (!ok) break;
-                const int le = t * 128 + m;
-                float hv[12], lv[12];
-                if (le < NEL) {
-                    const int lx = le % EX, ly = (le / EX) % EY, lz = le / (EX * EY);
-                    // nodes n1..n4 (h = 0) or n5..n8 (h = 1) of the element, in the raw halo rows
-                    const int r0 = (lz + h) * HY + ly;
-                    const float* p0 = raw + r0 * RAWX + (RAW_SHIFT + lx) * 3;
-                    const float* p1 = p0 + RAWX;
-                    const float u[12] = {p0[0], p0[1], p0[2], p0[3], p0[4], p0[5],
-                                         p1[3], p1[4], p1[5], p1[0], p1[1], p1[2]};
-#pragma unroll
-                    for (int i = 0; i < 12; ++i) {
-                        hv[i] = to_tf32(u[i]);
-                        lv[i] = to_tf32(__fsub_rn(u[i], hv[i]));
-                    }
-                } else {
-#pragma unroll
-                    for (int i = 0; i < 12; ++i) { hv[i] = 0.f; lv[i] = 0.f; }
-                }
                 unsigned char* Ab = smem + OFF_A + b * A_STRIDE;
                 const int off = (m >> 3) * SBO + (3 * h) * LBO + (m & 7) * 16;
 #pragma unroll
@@ -376,10 +383,11 @@ k_cdx_step(const __grid_constant__ CUtensorMap tmap_u, const __grid_constant__ C
                 }
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                 mbar_arrive(B_AFULL(b));
+                if (t + 1 < NMT) build_row(raw, t + 1, hv, lv);
             }
         }
     } else if (warp == ISSUE_WARP) {
-        // ===== MMA issuer: D = A_lo K_hi + A_hi K_lo + A_hi K_hi in one accumulator =====
+        // ===== MMA issuer: D = A_lo K_hi (+ A_hi K_lo when K is split) + A_hi K_hi in one accumulator =====
         if (lane == 0) {
             uint32_t ph_afull = 0u, ph_dempty = (1u << NDB) - 1u;
             const uint32_t bB = smem_u32(smem + OFF_B);
