@@ -556,7 +556,7 @@ void svl_xnm_destroy(svl_xnm* x);
  * D = diag(K_eff), rho = (4/dt^2 m) / D; four 3x3x3 convolutions
  * 6 -> 16 -> 16 -> 16 -> 3 with ReLU between them, FP32.  The solve is then a
  * flexible conjugate gradient (each direction K_eff-orthogonalised against
- * the previous one).  Jacobi-PCG is both the fallback and the judge: a solve
+ * the previous one).  Jacobi-PCG is both the fallback and the yardstick: a solve
  * that has used as many iterations as the last plain Jacobi-PCG solve without
  * reaching pcg_tol continues with Jacobi-PCG from where it stands, and every
  * solve ends on the true FP64 residual.  The network is trained on the GPU
