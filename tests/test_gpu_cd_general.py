@@ -148,3 +148,20 @@ def test_nondiagonal_central_difference_j2_constraints_support_motion_dashpots(c
     ho, *_ = O.cd_run(m, L, dt, n)
     assert np.abs(ho).max() > 0
     assert rel_l2(hg, ho) <= 1e-8
+
+
+def test_nondiagonal_central_difference_periodic_column_support_motion(gpu):
+    """Elastic periodic soil column shaken at the base, consistent mass and
+    Rayleigh (am, ak): T^T K T solve with T^T K SM(k) on the GPU against the
+    oracle (itself pinned to a dense restatement with T and SM)."""
+    from tests.test_cd_general_oracle import _column
+    m, L, dt = _column()
+    n = 150
+    cd = CentralDifference(m, L, dt)
+    assert isinstance(cd, CentralDifferenceSolve)
+    cd.Initialize()
+    hg = cd.run(1, n, history=True)
+    cd.close()
+    ho, *_ = O.cd_run(m, L, dt, n)
+    assert np.abs(ho).max() > 0
+    assert rel_l2(hg, ho) <= 1e-9
