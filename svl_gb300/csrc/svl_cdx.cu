@@ -1053,6 +1053,7 @@ struct svl_cdx {
     // longer one, so its stream has the higher priority.
     cudaStream_t bstream = nullptr;
     cudaEvent_t ev_c = nullptr, ev_uu = nullptr, ev_band = nullptr;
+    cudaEvent_t ev_hist[2] = {nullptr, nullptr};   // history row of the last even / odd step (band stream)
     // schedule (svl_cdx_set_schedule / svl_cdx_tune): tile order of the fused
     // kernel, block size of the band's element kernels, band stream priority
     std::vector<int32_t> tiles_base;     // the scheduled tiles in natural order (full ids)
@@ -1092,7 +1093,7 @@ struct svl_cdx {
         if (copy_stream) cudaStreamDestroy(copy_stream);
         if (bstream) cudaStreamSynchronize(bstream);
         if (bstream) cudaStreamDestroy(bstream);
-        for (cudaEvent_t e : {ev_c, ev_uu, ev_band})
+        for (cudaEvent_t e : {ev_c, ev_uu, ev_band, ev_hist[0], ev_hist[1]})
             if (e) cudaEventDestroy(e);
         if (stream) cudaStreamDestroy(stream);
     }
@@ -1244,7 +1245,9 @@ static int cdx_create_impl(const svl_grid_spec* g, int32_t ninst, const svl_mode
             cudaStreamCreateWithPriority(&h->bstream, cudaStreamNonBlocking, hi_pri) != cudaSuccess ||
             cudaEventCreateWithFlags(&h->ev_c, cudaEventDisableTiming) != cudaSuccess ||
             cudaEventCreateWithFlags(&h->ev_uu, cudaEventDisableTiming) != cudaSuccess ||
-            cudaEventCreateWithFlags(&h->ev_band, cudaEventDisableTiming) != cudaSuccess) {
+            cudaEventCreateWithFlags(&h->ev_band, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&h->ev_hist[0], cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&h->ev_hist[1], cudaEventDisableTiming) != cudaSuccess) {
             set_error("cudaStreamCreate failed"); return fail(SVL_ERR_CUDA);
         }
     }
@@ -1952,20 +1955,29 @@ static int cdx_status(svl_cdx* h) {
 
 // Enqueues steps [s0, s0 + n) of a run on the compute stream, writing each
 // step's FP64 fields into history chunk `slot`.
+// With a PML band the history row of a step is written on the band stream,
+// right after the step's stress update (k_cdp_su): the next step's kernels do
+// not wait for the band to finish.  The row reads u_{n+1} and S^{n+3/2}, which
+// step n + 2 overwrites (its tensor-core step on the compute stream, its band
+// kernels after the row in band-stream order): step n + 2 waits for the row's
+// event.
 static int cdx_fill_chunk(svl_cdx* h, int k_first, int s0, int n, int nsteps, int slot) {
     const long long per_step = h->hist_n;
-    CUDA_TRY(cudaStreamWaitEvent(h->stream, h->drained[slot], 0));       // the chunk's previous copy is done
+    const bool band = h->np > 0;
+    cudaStream_t hs = band ? h->bstream : h->stream;                      // the stream of the history rows
+    CUDA_TRY(cudaStreamWaitEvent(hs, h->drained[slot], 0));              // the chunk's previous copy is done
     for (int i = 0; i < n; ++i) {
         const int s = s0 + i;
+        if (band) CUDA_TRY(cudaStreamWaitEvent(h->stream, h->ev_hist[s & 1], 0));   // row of step s - 2
         TRY(cdx_step(h, k_first + s, s == nsteps - 1));
-        TRY(cdx_join(h));                                                  // S of this step
-        k_cdx_hist<<<(unsigned)((per_step + 255) / 256), 256, 0, h->stream>>>(
+        k_cdx_hist<<<(unsigned)((per_step + 255) / 256), 256, 0, hs>>>(
             h->uh[h->cur], h->ul[h->cur], h->sh[h->cur], h->sl[h->cur], h->d_hmap, h->hist[slot] + (size_t)i * per_step,
             per_step);
         ++h->launches;
+        if (band) CUDA_TRY(cudaEventRecord(h->ev_hist[s & 1], h->bstream));
     }
     CUDA_TRY(cudaGetLastError());
-    CUDA_TRY(cudaEventRecord(h->filled[slot], h->stream));
+    CUDA_TRY(cudaEventRecord(h->filled[slot], hs));
     return SVL_OK;
 }
 
@@ -2016,6 +2028,7 @@ int svl_cdx_run(svl_cdx* h, int32_t k_first, int32_t nsteps, double* U_hist) {
                                      cudaMemcpyDeviceToHost, h->copy_stream));
             CUDA_TRY(cudaEventRecord(h->drained[slot], h->copy_stream));
         }
+        TRY(cdx_join(h));                    // later work on the compute stream follows the band's
         CUDA_TRY(cudaStreamSynchronize(h->copy_stream));
     }
     h->va_valid = nsteps > 0;
