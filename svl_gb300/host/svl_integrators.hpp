@@ -27,6 +27,41 @@ inline void check(int st) {
     if (st != SVL_OK) throw Error(st, svl_last_error());
 }
 
+// The force entries of a load descriptor (point, body-point and element body
+// loads resolved to dofs), kept by the integrators for ComputeProgressiveForce.
+class ExternalForce {
+public:
+    ExternalForce() = default;
+    explicit ExternalForce(const svl_load_desc& L) {
+        if (L.ndrm > 0) drm_ = true;
+        if (L.nseries > 0 && L.series_ptr && L.series_val) {
+            ptr_.assign(L.series_ptr, L.series_ptr + L.nseries + 1);
+            val_.assign(L.series_val, L.series_val + ptr_.back());
+        }
+        if (L.nforce > 0) {
+            dof_.assign(L.force_dof, L.force_dof + L.nforce);
+            ser_.assign(L.force_series, L.force_series + L.nforce);
+            coef_.assign(L.force_coef, L.force_coef + L.nforce);
+        }
+    }
+    // Fext(k) on ntotal dofs: sum of coef * series[k], a series read past its
+    // end giving 0 (Assembler::ComputeExternalForceVector, Assembler.cpp:291-489).
+    std::vector<double> at(unsigned k, int ntotal) const {
+        if (drm_) throw Error(SVL_ERR_UNSUPPORTED, "domain-reduction forces are computed on the device only");
+        std::vector<double> f((size_t)ntotal, 0.0);
+        for (size_t i = 0; i < dof_.size(); ++i) {
+            const int s = ser_[i], b = ptr_[s], n = ptr_[s + 1] - b;
+            if ((int)k < n) f[dof_[i]] += coef_[i] * val_[b + k];
+        }
+        return f;
+    }
+
+private:
+    std::vector<int32_t> ptr_, dof_, ser_;
+    std::vector<double> val_, coef_;
+    bool drm_ = false;
+};
+
 class CentralDifference {
 public:
     // CentralDifference(mesh, dt, mtol, ktol, ftol) (CentralDifference.cpp:6-27)
@@ -36,7 +71,7 @@ public:
     // never applies G, CentralDifference.cpp:114-120).
     CentralDifference(const svl_model_desc& model, const svl_load_desc& loads, double dt,
                       double mtol = 1e-12, double ftol = 1e-12)
-        : ntotal_(model.ntotal) {
+        : ntotal_(model.ntotal), fext_(loads) {
         bool pml = false;
         for (int e = 0; model.elem_pml && e < model.nelem; ++e) pml = pml || model.elem_pml[e] != 0;
         if (pml) {
@@ -92,6 +127,9 @@ public:
     std::vector<double> GetDisplacements() const { return get(0); }
     std::vector<double> GetVelocities() const { return get(1); }
     std::vector<double> GetAccelerations() const { return get(2); }
+    // ComputeProgressiveForce(mesh, k) (CentralDifference.cpp:174-186 and the
+    // Newmark integrators): Fext(k) + Fbar, Fbar = 0 in a single-stage run
+    std::vector<double> ComputeProgressiveForce(unsigned int k) const { return fext_.at(k, ntotal_); }
     // ComputeReactionForce(mesh, k) after step k (CentralDifference.cpp:156-171),
     // as DynamicAnalysis::UpdateDomain stores it at the fixed nodes
     std::vector<double> ComputeReactionForce(unsigned int k) const {
@@ -111,6 +149,7 @@ private:
     svl_xnm* x_ = nullptr;                 // set instead of h_ for models with PML layers
     svl_nm* n_ = nullptr;                  // set instead of h_ when K is not diagonal
     int ntotal_ = 0;
+    ExternalForce fext_;
 };
 
 // NewtonRaphson(solver, mesh, cnvgtol, nstep, cnvgtest) as the Driver builds it
@@ -130,7 +169,7 @@ class NewmarkBeta {
 public:
     NewmarkBeta(const svl_model_desc& model, const svl_load_desc& loads, double dt, double tol = 1e-8,
                 double mtol = 1e-12, double ftol = 1e-12, int maxit = 20000, const NewtonRaphson* newton = nullptr)
-        : ntotal_(model.ntotal) {
+        : ntotal_(model.ntotal), fext_(loads) {
         bool pml = false;
         for (int e = 0; model.elem_pml && e < model.nelem; ++e) pml = pml || model.elem_pml[e] != 0;
         if (pml) {
@@ -194,6 +233,9 @@ public:
     std::vector<double> GetDisplacements() const { return get(0); }
     std::vector<double> GetVelocities() const { return get(1); }
     std::vector<double> GetAccelerations() const { return get(2); }
+    // ComputeProgressiveForce(mesh, k) (CentralDifference.cpp:174-186 and the
+    // Newmark integrators): Fext(k) + Fbar, Fbar = 0 in a single-stage run
+    std::vector<double> ComputeProgressiveForce(unsigned int k) const { return fext_.at(k, ntotal_); }
     // NewmarkBeta::ComputeReactionForce after step k
     std::vector<double> ComputeReactionForce(unsigned int k) const {
         std::vector<double> r(ntotal_);
@@ -210,6 +252,7 @@ private:
     svl_nm* h_ = nullptr;
     svl_xnm* x_ = nullptr;                 // set instead of h_ for models with PML layers
     int ntotal_ = 0;
+    ExternalForce fext_;
 };
 
 // ExtendedNewmarkBeta(mesh, dt, mtol, ktol, ftol) with the Linear algorithm or
@@ -222,7 +265,7 @@ public:
     ExtendedNewmarkBeta(const svl_model_desc& model, const svl_load_desc& loads, double dt, double tol = 1e-10,
                         double mtol = 1e-12, double ftol = 1e-12, int maxit = 100000,
                         const NewtonRaphson* newton = nullptr)
-        : ntotal_(model.ntotal) {
+        : ntotal_(model.ntotal), fext_(loads) {
         svl_xnm_opts o{};
         o.dt = dt;
         o.ftol = ftol;
@@ -257,6 +300,9 @@ public:
     std::vector<double> GetDisplacements() const { return get(0); }
     std::vector<double> GetVelocities() const { return get(1); }
     std::vector<double> GetAccelerations() const { return get(2); }
+    // ComputeProgressiveForce(mesh, k) (CentralDifference.cpp:174-186 and the
+    // Newmark integrators): Fext(k) + Fbar, Fbar = 0 in a single-stage run
+    std::vector<double> ComputeProgressiveForce(unsigned int k) const { return fext_.at(k, ntotal_); }
     std::vector<double> GetPMLHistoryVector() const { return get(3); }
     // ComputeReactionForce(mesh, k) after step k (:158-172), as
     // DynamicAnalysis::UpdateDomain stores it at the fixed nodes
@@ -274,6 +320,7 @@ private:
     }
     svl_xnm* h_ = nullptr;
     int ntotal_ = 0;
+    ExternalForce fext_;
 };
 
 }  // namespace gpu

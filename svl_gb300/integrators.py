@@ -38,7 +38,8 @@ class CentralDifference:
         self.model = model
         self.dt = float(dt)
         self._md = model.desc()
-        self._ld = (loads or Loads()).desc()
+        self.loads = loads or Loads()
+        self._ld = self.loads.desc()
         opts = capi.CdOpts(dt=self.dt, ftol=ftol, mtol=mtol, precision=capi.SVL_PREC_FP64,
                            check_every=check_every)
         h = C.c_void_p()
@@ -63,6 +64,12 @@ class CentralDifference:
 
     def GetAccelerations(self) -> np.ndarray:
         return self._get(2)
+
+    def ComputeProgressiveForce(self, k: int) -> np.ndarray:
+        """Fext(k) + Fbar (ComputeProgressiveForce of the reference's
+        integrators, e.g. CentralDifference.cpp:174-186): the stage force Fbar
+        of earlier stages is zero in a single-stage run."""
+        return self.loads.external_force(self.ntotal, int(k))
 
     def ComputeReactionForce(self, k: int) -> np.ndarray:
         """Reaction forces after step k (CentralDifference.cpp:156-171): total-dof
@@ -265,7 +272,8 @@ class ExtendedNewmarkBeta:
         self.model = model
         self.dt = float(dt)
         self._md = model.desc()
-        self._ld = (loads or Loads()).desc()
+        self.loads = loads or Loads()
+        self._ld = self.loads.desc()
         algo = {"linear": capi.SVL_ALGO_LINEAR, "newton": capi.SVL_ALGO_NEWTON}[algorithm.lower()]
         integ = {"extendednewmark": capi.SVL_XNM_EXTENDED_NEWMARK, "newmark": capi.SVL_XNM_NEWMARK,
                  "centraldifference": capi.SVL_XNM_CENTRAL_DIFFERENCE}[integrator.lower()]
@@ -298,6 +306,12 @@ class ExtendedNewmarkBeta:
 
     def GetAccelerations(self) -> np.ndarray:
         return self._get(2)
+
+    def ComputeProgressiveForce(self, k: int) -> np.ndarray:
+        """Fext(k) + Fbar (ComputeProgressiveForce of the reference's
+        integrators, e.g. CentralDifference.cpp:174-186): the stage force Fbar
+        of earlier stages is zero in a single-stage run."""
+        return self.loads.external_force(self.ntotal, int(k))
 
     def GetPMLHistoryVector(self) -> np.ndarray:
         return self._get(3)
@@ -374,7 +388,8 @@ class NewmarkBeta:
         self.model = model
         self.dt = float(dt)
         self._md = model.desc()
-        self._ld = (loads or Loads()).desc()
+        self.loads = loads or Loads()
+        self._ld = self.loads.desc()
         algo = {"linear": capi.SVL_ALGO_LINEAR, "newton": capi.SVL_ALGO_NEWTON}[algorithm.lower()]
         opts = capi.NmOpts(dt=self.dt, ftol=ftol, mtol=mtol, pcg_tol=float(pcg_tol), pcg_maxit=int(pcg_maxit),
                            precond=int(precond), algorithm=algo, maxit=int(maxit), cnvgtol=float(cnvgtol),
@@ -401,6 +416,12 @@ class NewmarkBeta:
 
     def GetAccelerations(self) -> np.ndarray:
         return self._get(2)
+
+    def ComputeProgressiveForce(self, k: int) -> np.ndarray:
+        """Fext(k) + Fbar (ComputeProgressiveForce of the reference's
+        integrators, e.g. CentralDifference.cpp:174-186): the stage force Fbar
+        of earlier stages is zero in a single-stage run."""
+        return self.loads.external_force(self.ntotal, int(k))
 
     def element_response(self, response: str, elems) -> np.ndarray:
         """ELEMENT recorder values after the last step (as CentralDifference)."""

@@ -297,6 +297,21 @@ class Loads:
         self.sm_series.append(series)
         self.sm_factor.append(float(factor))
 
+    def external_force(self, ntotal: int, k: int) -> np.ndarray:
+        """Fext(k) on total dofs from the force entries (point, body-point and
+        element body loads already resolved to dofs): sum of coef * series[k],
+        a series read past its end giving 0 (Assembler::ComputeExternalForceVector,
+        Assembler.cpp:291-489).  Domain-reduction forces are computed on the
+        device inside the step and are not covered here."""
+        if self.drm_elem:
+            raise ValueError("external_force: domain-reduction loads are not covered on the host")
+        f = np.zeros(int(ntotal))
+        for dof, s_, c in zip(self.force_dof, self.force_series, self.force_coef):
+            ser = self.series[s_]
+            if 0 <= k < ser.size:
+                f[dof] += c * ser[k]
+        return f
+
     @staticmethod
     def concat(parts: List["Loads"], models: List[Model]) -> "Loads":
         out = Loads()

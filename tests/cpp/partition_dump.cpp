@@ -1,7 +1,8 @@
 // Reads a partition file with the C++ reader (svl_gb300/host/svl_partition.hpp)
 // and either prints the model and load descriptors as JSON (`dump`, no GPU
-// needed) or runs the simulation block through the C++ Integrator mirror and
-// prints the final displacement vector (`run`).
+// needed), prints Fext(k) of its loads for every step (`fext`, no GPU), or
+// runs the simulation block through the C++ Integrator mirror and prints the
+// final displacement vector (`run`).
 #include <cstdio>
 #include <string>
 #include <vector>
@@ -70,14 +71,28 @@ static int run(const svl::gpu::Partition& P) {
     return 0;
 }
 
+// Fext(k) of the partition's loads on the host (the integrators'
+// ComputeProgressiveForce without a stage force), for every k in 0..nt.
+static int fext(const svl::gpu::Partition& P) {
+    const svl::gpu::ExternalForce F(P.loads());
+    for (int k = 0; k <= P.nt; ++k) {
+        const std::vector<double> f = F.at((unsigned)k, P.ntotal);
+        std::printf("%d", k);
+        for (double v : f) std::printf(" %.17g", v);
+        std::printf("\n");
+    }
+    return 0;
+}
+
 int main(int argc, char** argv) {
     if (argc < 3) {
-        std::fprintf(stderr, "usage: %s dump|run <partition file>\n", argv[0]);
+        std::fprintf(stderr, "usage: %s dump|run|fext <partition file>\n", argv[0]);
         return 1;
     }
     try {
         const svl::gpu::Partition P = svl::gpu::load_partition(argv[2]);
-        return std::string(argv[1]) == "run" ? run(P) : dump(P);
+        const std::string mode = argv[1];
+        return mode == "run" ? run(P) : (mode == "fext" ? fext(P) : dump(P));
     } catch (const svl::gpu::Error& e) {
         std::printf("error %d %s\n", e.code, e.what());
         return 4;

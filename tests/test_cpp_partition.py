@@ -91,6 +91,23 @@ def test_cpp_reader_gives_the_python_descriptors(exe, fx):
         _eq(c["drm_motion"], np.concatenate([L.drm_motion[n][0] for n in nodes]), "drm_motion")
 
 
+@pytest.mark.parametrize("fx", [f for f in FIXTURES if "drm" not in f.name], ids=lambda p: p.name)
+def test_progressive_force_of_both_mirrors(exe, fx):
+    """ComputeProgressiveForce(k) = Fext(k) (+ a zero stage force): the C++
+    mirror's host sum over the load entries equals the Python one's on every
+    step of the pre-processor fixtures."""
+    r = subprocess.run([str(exe), "fext", str(_file(fx))], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr
+    p = load_partition(_file(fx))
+    rows = [ln.split() for ln in r.stdout.splitlines()]
+    assert len(rows) == p.nt + 1
+    for row in rows:
+        k = int(row[0])
+        fc = np.array([float(v) for v in row[1:]])
+        fp = p.loads.external_force(p.model.ntotal, k)
+        assert np.array_equal(fc, fp), k
+
+
 def test_cpp_reader_reports_what_it_does_not_cover(exe, tmp_path):
     d = json.loads(_file(ROOT / "tests/golden/partition_q4_cd").read_text())
     tag = sorted(d["Materials"], key=int)[0]

@@ -163,3 +163,25 @@ def test_nm_options_layout_and_central_difference_dispatch():
     m.rayleigh = None
     m.lumped = False
     assert _cd_nondiagonal(m)
+
+
+def test_external_force_sums_the_load_entries():
+    """Loads.external_force(k) (ComputeProgressiveForce without a stage
+    force): coef * series[k] summed per dof, 0 past a series' end; DRM loads
+    are refused on the host."""
+    from tests.helpers import drm_box, q4_box
+    m, L, dt = q4_box(6, 4, nt=30)
+    s2 = L.add_series(np.linspace(1.0, 2.0, 10))
+    L.add_point_load(m, 5, (0.5, -1.0), s2, factor=2.0)
+    for k in (0, 3, 9, 10, 40):
+        f = L.external_force(m.ntotal, k)
+        ref = np.zeros(m.ntotal)
+        for d, s_, c in zip(L.force_dof, L.force_series, L.force_coef):
+            if k < L.series[s_].size:
+                ref[d] += c * L.series[s_][k]
+        assert np.array_equal(f, ref)
+    assert np.abs(L.external_force(m.ntotal, 3)).max() > 0
+    assert not L.external_force(m.ntotal, 40).any()
+    md, Ld, dt2, _, _ = drm_box(nt=10)
+    with pytest.raises(ValueError):
+        Ld.external_force(md.ntotal, 1)
