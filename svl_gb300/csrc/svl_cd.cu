@@ -1797,15 +1797,33 @@ __global__ void k_nmg_wdamp(DevView d, const double* __restrict__ dUt, double c_
     if (t < d.ntotal) w[t] = d.V[t] - c_u * dUt[t];
 }
 
-// ft += C w: the element damping vectors in d.fe plus the mass-proportional diagonal
+// w = 4/dt V + A - 4/dt^2 dU_t: the vector the mass acts on in the effective
+// force (NewmarkBeta.cpp:215), for a consistent mass on the general path
+__global__ void k_nmg_wmass(DevView d, const double* __restrict__ dUt, double c_v, double c_m, double* __restrict__ w) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < d.ntotal) w[t] = (c_v * d.V[t] + d.A[t]) - c_m * dUt[t];
+}
+
+// ft += sum_e blk_e per total dof (element order)
 template <int ND>
-__global__ void __launch_bounds__(256) k_nmg_damp(DevView d, const double* __restrict__ w, double* __restrict__ ft) {
+__global__ void __launch_bounds__(256) k_nmg_addblk(DevView d, const double* __restrict__ blk, double* __restrict__ ft) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= d.nnode) return;
+#pragma unroll
+    for (int c = 0; c < ND; ++c) ft[d.ntdof[n * ND + c]] += gather_block<ND>(d, blk, n, c);
+}
+
+// ft += C w: the element damping vectors in d.fe (gather_fe) plus the
+// mass-proportional diagonal
+template <int ND>
+__global__ void __launch_bounds__(256) k_nmg_damp(DevView d, const double* __restrict__ w, double* __restrict__ ft,
+                                                  int gather_fe) {
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= d.nnode) return;
 #pragma unroll
     for (int c = 0; c < ND; ++c) {
         const int t = d.ntdof[n * ND + c];
-        double v = d.dk0 ? gather_fint<ND>(d, n, c) : 0.0;
+        double v = gather_fe ? gather_fint<ND>(d, n, c) : 0.0;
         if (d.Cd) v += d.Cd[t] * w[t];
         if (d.dp_ptr) v += dashpot_sum(d, t, w);
         ft[t] += v;
@@ -2403,6 +2421,14 @@ static int nm_op_total(svl_nm* nm, const double* pt, double* out) {
         else k_element<3, 8><<<eg, 128, 0, cd->stream>>>(d, pt, m.ngp, 0);
     }
     const double c_m = 4.0 / nm->opts.dt / nm->opts.dt;
+    if (nm->consistent) {
+        // + sum_e (4/dt^2 + 2/dt am_e) M_e p_e; the diagonal keeps the nodal
+        // masses only and no lumped mass-proportional part
+        if (m.ndim == 2) k_mass_elem<2, 4><<<eg, 128, 0, cd->stream>>>(d, pt, nm->fe_op, c_m, 1, nm->eam, c_c);
+        else k_mass_elem<3, 8><<<eg, 128, 0, cd->stream>>>(d, pt, nm->fe_op, c_m, 1, nm->eam, c_c);
+        d.Cd = nullptr;
+        cd->launches += 1;
+    }
     if (m.ndim == 2) k_nmg_total<2><<<ng, tb, 0, cd->stream>>>(d, pt, out, c_m, c_c);
     else k_nmg_total<3><<<ng, tb, 0, cd->stream>>>(d, pt, out, c_m, c_c);
     cd->launches += 2;
@@ -2890,10 +2916,6 @@ int svl_nm_create(const svl_model_desc* model, const svl_load_desc* loads, const
     lumped_mass_diag(m, opts->mtol, M);
     nm->consistent = !m.lumped;
     if (nm->consistent) {
-        if (nm->general) {
-            set_error("a consistent mass is covered without constraints, support motion or damping");
-            return fail(SVL_ERR_UNSUPPORTED);
-        }
         // diagonal of the consistent mass: rho sum_q w t |J| N_a^2, plus the nodal masses
         std::fill(M.begin(), M.end(), 0.0);
         for (int e = 0; e < m.nelem; ++e) {
@@ -2907,7 +2929,19 @@ int svl_nm_create(const svl_model_desc* model, const svl_load_desc* loads, const
     }
     if (nm->damped) {                       // + 2/dt (sum_e am_e M_e + dashpot diagonal)
         std::vector<double> Cm;
-        rayleigh_mass_diag(m, Cm);
+        if (nm->consistent) {               // am_e times the consistent element mass's diagonal
+            Cm.assign(m.ntotal, 0.0);
+            for (int e = 0; e < m.nelem && !m.ray.empty(); ++e) {
+                const double am = m.ray[2 * (size_t)e];
+                if (am == 0.0) continue;
+                double md[8];
+                elem_cmass_diag(m, e, md);
+                for (int a = 0; a < m.nen; ++a)
+                    for (int c = 0; c < m.ndof; ++c) Cm[m.tdof[(size_t)m.conn[(size_t)e * m.nen + a] * m.ndof + c]] += am * md[a];
+            }
+        } else {
+            rayleigh_mass_diag(m, Cm);
+        }
         for (int t = 0; t < m.ntotal; ++t) Kd[t] += c_c * Cm[t];
         for (size_t i = 0; i < m.dp_eta.size(); ++i) {
             Kd[m.dp_dof[2 * i]] += c_c * m.dp_eta[i];
@@ -2944,6 +2978,15 @@ int svl_nm_create(const svl_model_desc* model, const svl_load_desc* loads, const
         double* fm = nullptr;
         if ((st = cd->zeros((size_t)nc * m.nelem, &fm)) || (st = cd->zeros((size_t)m.ntotal, &nm->wvec))) return fail(st);
         cd->d.fem = fm;
+        bool any_am = false;
+        for (size_t e = 0; e < m.ray.size() / 2; ++e) any_am = any_am || m.ray[2 * e] != 0.0;
+        if (any_am) {                       // am_e of the consistent element masses in C
+            std::vector<double> eam(m.nelem);
+            for (int e = 0; e < m.nelem; ++e) eam[e] = m.ray[2 * (size_t)e];
+            const double* ea = nullptr;
+            if ((st = cd->upload(eam, &ea))) return fail(st);
+            nm->eam = const_cast<double*>(ea);
+        }
     }
     if (nm->general) {
         double** tv[] = {&nm->ft, &nm->dUt, &nm->smv, &nm->lg, &nm->pt2};
@@ -3130,19 +3173,41 @@ static int nmg_rhs(svl_nm* nm) {
     if (m.ndim == 2) k_nmg_rhs<2><<<ng, tb, 0, cd->stream>>>(cd->d, nm->ft, nm->dUt, 4.0 / dt, 4.0 / dt / dt);
     else k_nmg_rhs<3><<<ng, tb, 0, cd->stream>>>(cd->d, nm->ft, nm->dUt, 4.0 / dt, 4.0 / dt / dt);
     cd->launches += 1;
+    const int eg = (m.nelem + 127) / 128;
+    if (nm->consistent) {
+        // + sum_e M_e (4/dt V + A - 4/dt^2 dU)_e (the diagonal above holds the nodal masses)
+        DevView d = cd->d;
+        double* blk = const_cast<double*>(cd->d.fem);
+        k_nmg_wmass<<<(m.ntotal + tb - 1) / tb, tb, 0, cd->stream>>>(d, nm->dUt, 4.0 / dt, 4.0 / dt / dt, nm->wvec);
+        if (m.ndim == 2) k_mass_elem<2, 4><<<eg, 128, 0, cd->stream>>>(d, nm->wvec, blk, 1.0, 0);
+        else k_mass_elem<3, 8><<<eg, 128, 0, cd->stream>>>(d, nm->wvec, blk, 1.0, 0);
+        if (m.ndim == 2) k_nmg_addblk<2><<<ng, tb, 0, cd->stream>>>(d, blk, nm->ft);
+        else k_nmg_addblk<3><<<ng, tb, 0, cd->stream>>>(d, blk, nm->ft);
+        cd->launches += 3;
+    }
     if (nm->damped) {
         // + C (V - 2/dt dU) (NewmarkBeta.cpp:215)
         DevView d = cd->d;
         d.fe = nm->fe_op;
-        const int eg = (m.nelem + 127) / 128;
         k_nmg_wdamp<<<(m.ntotal + tb - 1) / tb, tb, 0, cd->stream>>>(d, nm->dUt, 2.0 / dt, nm->pt2);
+        bool elem = false;
         if (d.dk0) {
             if (m.ndim == 2) k_element_tan<2, 4><<<eg, 128, 0, cd->stream>>>(d, nm->pt2, m.ngp, 0, 1.0);
             else k_element_tan<3, 8><<<eg, 128, 0, cd->stream>>>(d, nm->pt2, m.ngp, 0, 1.0);
+            elem = true;
             cd->launches += 1;
         }
-        if (m.ndim == 2) k_nmg_damp<2><<<ng, tb, 0, cd->stream>>>(d, nm->pt2, nm->ft);
-        else k_nmg_damp<3><<<ng, tb, 0, cd->stream>>>(d, nm->pt2, nm->ft);
+        if (nm->consistent) {               // am_e M_e with the consistent element mass, not the lumped diagonal
+            if (nm->eam) {
+                if (m.ndim == 2) k_mass_elem<2, 4><<<eg, 128, 0, cd->stream>>>(d, nm->pt2, nm->fe_op, 0.0, elem ? 1 : 0, nm->eam, 1.0);
+                else k_mass_elem<3, 8><<<eg, 128, 0, cd->stream>>>(d, nm->pt2, nm->fe_op, 0.0, elem ? 1 : 0, nm->eam, 1.0);
+                elem = true;
+                cd->launches += 1;
+            }
+            d.Cd = nullptr;
+        }
+        if (m.ndim == 2) k_nmg_damp<2><<<ng, tb, 0, cd->stream>>>(d, nm->pt2, nm->ft, elem ? 1 : 0);
+        else k_nmg_damp<3><<<ng, tb, 0, cd->stream>>>(d, nm->pt2, nm->ft, elem ? 1 : 0);
         cd->launches += 2;
     }
     const double* lg = nullptr;

@@ -101,10 +101,6 @@ def test_nm_rejects_models_it_does_not_cover(gpu):
     with pytest.raises(SvlError) as ei:        # learned preconditioner off the node lattice
         NewmarkBeta(m, L, dt, precond=capi.SVL_PRECOND_LEARNED)
     assert ei.value.code == capi.SVL_ERR_UNSUPPORTED
-    m.lumped = False
-    with pytest.raises(SvlError) as ei:        # consistent mass with constraints / support motion
-        NewmarkBeta(m, L, dt)
-    assert ei.value.code == capi.SVL_ERR_UNSUPPORTED
 
 
 @pytest.mark.parametrize("shape", [(16, 8), (6, 5, 4)], ids=["quad", "hexa"])
@@ -130,4 +126,35 @@ def test_nm_consistent_mass_matches_oracle(gpu, shape):
     hl, _ = O.newmark_run(m, L, dt, nt, solver=0)
     assert np.abs(ho).max() > 0 and res <= TOL_SOLVE
     assert rel_l2(ho, hl) > 1e-4               # the mass form matters
+    assert rel_l2(hist, ho) <= TOL_HIST
+
+
+@pytest.mark.parametrize("case", ["column_rayleigh", "j2_columns_newton"])
+def test_nm_consistent_mass_constraints_support_motion_damping(gpu, case):
+    """massform Consistent on the general path: EQUAL constraints (periodic
+    columns), base support motion and Rayleigh (am with the consistent
+    element mass, ak with K0): T^T (K + 4/dt^2 M + 2/dt C) T solved by PCG,
+    the effective force's mass and damping terms through the element mass
+    action, against the oracle's assembled matrices and dense LDL^T."""
+    from tests.test_cd_general_oracle import _column
+    if case == "column_rayleigh":
+        m, L, dt = _column(nt=120)
+        dt *= 4.0
+        kw = {}
+    else:
+        m, L, dt = q4_j2_columns(ncol=2, heights=(6, 9), nt=80)
+        m.lumped = False
+        m.rayleigh = np.tile([1.0, 1.0e-4], (m.nelem, 1))
+        dt *= 2.0
+        kw = dict(algorithm="newton", maxit=3, cnvgtol=0.0)
+    nt = 40
+    nm = NewmarkBeta(m, L, dt, pcg_tol=TOL_SOLVE, **kw)
+    nm.Initialize()
+    hist = nm.run(1, nt, history=True)
+    nm.close()
+    if kw:
+        ho, _ = O.newmark_run(m, L, dt, nt, algo=1, maxit=3, cnvgtol=0.0, solver=0)
+    else:
+        ho, _ = O.newmark_run(m, L, dt, nt, solver=0)
+    assert np.abs(ho).max() > 0
     assert rel_l2(hist, ho) <= TOL_HIST
