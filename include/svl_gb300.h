@@ -377,8 +377,12 @@ void svl_cdx_destroy(svl_cdx* cdx);
  * as Material::GetTangentStiffness returns it), the states updated from
  * U + dU, until the chosen convergence test passes or `maxit` iterations.
  * Covered: elastic materials (both algorithms), J2 materials (Newton),
- * lumped mass, no constraints, no support motion; other models return
- * SVL_ERR_UNSUPPORTED. */
+ * lumped or consistent mass (massform CONSISTENT: the element mass action in
+ * the operator and the effective force), Rayleigh damping (am with the
+ * element's mass, ak with its initial stiffness), ZeroLength1D dashpots,
+ * EQUAL constraints (T^T Keff T) and support motion (T^T Keff SM of step
+ * k - 1, NewmarkBeta.cpp:180-194), domain-reduction loads with a lumped
+ * elastic layer; other models return SVL_ERR_UNSUPPORTED. */
 #define SVL_ALGO_LINEAR     0   /* Linear.cpp:22-56: one solve per step           */
 #define SVL_ALGO_NEWTON     1   /* NewtonRaphson.cpp:24-75: tangent iterations    */
 #define SVL_PRECOND_JACOBI  0
