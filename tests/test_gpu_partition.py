@@ -138,6 +138,26 @@ def test_consistent_mass_partition_cd_matches_oracle(gpu, tmp_path):
     assert np.allclose(rows, U[:, cols], rtol=10.0 ** -r.precision, atol=0)
 
 
+def test_consistent_mass_damped_partition_newmark_matches_oracle(gpu, tmp_path):
+    """The Rayleigh (am and ak) NEWMARK fixture with its massform switched to
+    CONSISTENT: the general path with the consistent element mass in the
+    operator, the effective force and the damping."""
+    import json
+    import shutil
+    src = GOLD / "partition_q4_newmark_rayleigh"
+    shutil.copytree(src, tmp_path / "case")
+    f = tmp_path / "case" / "Partition" / "Fixture.1.0.json"
+    d = json.loads(f.read_text())
+    d["Global"]["massform"] = "CONSISTENT"
+    f.write_text(json.dumps(d))
+    p = load_partition(f)
+    assert not p.model.lumped and p.model.rayleigh is not None
+    U = p.run(write_recorders=False)
+    ho, _ = O.newmark_run(p.model, p.loads, p.dt, p.nt - 1, solver=0)
+    assert np.abs(ho).max() > 0
+    assert rel_l2(U, ho) <= 1e-9
+
+
 def test_body_point_load_partition_cd_matches_oracle(gpu, tmp_path):
     """POINTLOAD BODY (nodal acceleration times the node's mass) beside a
     concentrated load, central difference, written by the pre-processor."""
