@@ -698,7 +698,8 @@ def main():
         # ncu capture (dram__bytes_read.sum + dram__bytes_write.sum), scaled by
         # the instance count
         traffic = CDX_STEP_DRAM_BYTES_4INST * nb / 4.0
-        traffic_src = "ncu, 4-instance capture: 298 MB read + 59 MB write per launch"
+        traffic_src = ("ncu, 4-instance capture of the step kernel over all tiles in one launch (before the step "
+                       "was split into far and near launches): 298 MB read + 59 MB write per step")
 
     e2e = None
     if not args.no_e2e:
@@ -777,7 +778,7 @@ def main():
             "l2": "no flush; working set ~%d MB > 129 MB L2" % ws_mb,
             "roofline": {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_source": peak_kind + " (HBM copy)",
-                         "traffic": traffic, "traffic_unit": "bytes per launch" if traffic else None,
+                         "traffic": traffic, "traffic_unit": "bytes per step" if traffic else None,
                          "traffic_source": traffic_src,
                          "algorithmic_bytes_per_step": algo_bytes, "kernel_ms_per_step": k_ms,
                          "kernel_share": shares, "per_kernel": per_kernel, "kernel_one_cta_per_sm": full_grid},
